@@ -1,0 +1,236 @@
+/*
+ * jbgpu.h -- C ABI of the GB300 rigid-body step (JBullet's DiscreteDynamicsWorld
+ * per-step pipeline: broadphase pairs, narrowphase + persistent manifolds,
+ * sequential-impulse contact solver, transform integration).
+ *
+ * Every entry point returns an int status (JBGPU_OK == 0).  Plain pointers and
+ * sizes only; host buffers are owned by the caller, device memory by the library.
+ * One world per host thread; each world owns one CUDA stream.
+ *
+ * Reference interfaces replaced (paths relative to src/com/bulletphysics/):
+ *   jbgpu_world_create            DiscreteDynamicsWorld(dispatcher, broadphase, solver, config)
+ *                                 dynamics/DiscreteDynamicsWorld.java:86-102 with the defaults of
+ *                                 ContactSolverInfo (dynamics/constraintsolver/ContactSolverInfo.java:33-48)
+ *                                 and BulletGlobals (BulletGlobals.java:59-66)
+ *   jbgpu_world_add_shape         BoxShape/SphereShape/CapsuleShape/ConvexHullShape/StaticPlaneShape constructors
+ *                                 (collision/shapes/BoxShape.java:46-50, SphereShape.java:38-41,
+ *                                 CapsuleShape.java:55-58, ConvexHullShape.java:44-50, StaticPlaneShape.java:45-48)
+ *   jbgpu_shape_local_inertia     CollisionShape.calculateLocalInertia (BoxShape.java:153-167,
+ *                                 SphereShape.java:72-76, CapsuleShape.java:125-153, PolyhedralConvexShape.java:133-159)
+ *   jbgpu_world_add_bodies        new RigidBody(RigidBodyConstructionInfo) + DiscreteDynamicsWorld.addRigidBody
+ *                                 (dynamics/RigidBody.java:121-164, dynamics/DiscreteDynamicsWorld.java:426-440,
+ *                                 collision/dispatch/CollisionWorld.java:103-121; uid = ++gid at
+ *                                 collision/broadphase/DbvtBroadphase.java:179)
+ *   jbgpu_world_step_simulation   DynamicsWorld.stepSimulation(timeStep, maxSubSteps, fixedTimeStep)
+ *                                 (dynamics/DiscreteDynamicsWorld.java:290-354)
+ *   jbgpu_world_step              stepSimulation with maxSubSteps == substeps and an exact substep count
+ *   jbgpu_world_stage             the protected phase methods of DiscreteDynamicsWorld that a subclass
+ *                                 overrides (dynamics/DiscreteDynamicsWorld.java:356-400, 620-767)
+ *   jbgpu_world_get_pairs         OverlappingPairCache.getOverlappingPairArray
+ *                                 (collision/broadphase/OverlappingPairCache.java:34-54)
+ *   jbgpu_world_get_manifolds     Dispatcher.getNumManifolds/getManifoldByIndexInternal
+ *                                 (collision/broadphase/Dispatcher.java:38-67)
+ *   jbgpu_world_get/set_state     RigidBody getters/setters (dynamics/RigidBody.java:480-520) and
+ *                                 CollisionObject activation state (collision/dispatch/CollisionObject.java:145-180)
+ *   jbgpu_world_counters          BulletStats counters (BulletStats.java:34-56)
+ */
+#ifndef JBGPU_H
+#define JBGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define JBGPU_OK                   0
+#define JBGPU_ERR_INVALID_ARGUMENT 1  /* bad pointer, size, shape id or config value */
+#define JBGPU_ERR_CAPACITY         2  /* a device buffer could not be grown */
+#define JBGPU_ERR_CUDA             3  /* a CUDA runtime call failed (see jbgpu_last_error) */
+#define JBGPU_ERR_NAN              4  /* a non-finite body state was detected after a step */
+#define JBGPU_ERR_TIMEOUT          5  /* a bounded device-side wait gave up */
+#define JBGPU_ERR_UNSUPPORTED      6  /* feature of the reference not on this path */
+#define JBGPU_ERR_EPA_OVERFLOW     7  /* an EPA polytope outgrew its fixed face pool */
+#define JBGPU_ERR_NO_DEVICE        8  /* no CUDA device could be used */
+
+/* ---- shape types: BroadphaseNativeType ordinals (collision/broadphase/BroadphaseNativeType.java:34-112) */
+#define JBGPU_SHAPE_BOX          0
+#define JBGPU_SHAPE_CONVEX_HULL  4
+#define JBGPU_SHAPE_SPHERE       6
+#define JBGPU_SHAPE_CAPSULE      8
+#define JBGPU_SHAPE_STATIC_PLANE 23
+
+/* ---- activation states (collision/dispatch/CollisionObject.java:43-47) ------------ */
+#define JBGPU_ACTIVE_TAG           1
+#define JBGPU_ISLAND_SLEEPING      2
+#define JBGPU_WANTS_DEACTIVATION   3
+#define JBGPU_DISABLE_DEACTIVATION 4
+#define JBGPU_DISABLE_SIMULATION   5
+
+/* ---- SolverMode bits (dynamics/constraintsolver/SolverMode.java:33-36) ------------ */
+#define JBGPU_SOLVER_RANDMIZE_ORDER    1  /* rejected: the GPU order is the colour order */
+#define JBGPU_SOLVER_FRICTION_SEPARATE 2
+#define JBGPU_SOLVER_USE_WARMSTARTING  4
+#define JBGPU_SOLVER_CACHE_FRIENDLY    8
+
+/* ---- phases of internalSingleStepSimulation, for jbgpu_world_stage --------------- */
+#define JBGPU_STAGE_APPLY_GRAVITY 0 /* DiscreteDynamicsWorld.applyGravity               */
+#define JBGPU_STAGE_PREDICT       1 /* predictUnconstraintMotion                        */
+#define JBGPU_STAGE_AABB          2 /* CollisionWorld.updateAabbs                       */
+#define JBGPU_STAGE_PAIRS         3 /* BroadphaseInterface.calculateOverlappingPairs    */
+#define JBGPU_STAGE_NARROWPHASE   4 /* Dispatcher.dispatchAllCollisionPairs             */
+#define JBGPU_STAGE_ISLANDS       5 /* calculateSimulationIslands + buildIslands        */
+#define JBGPU_STAGE_SOLVE         6 /* solveConstraints (colour, setup, PGS, write-back) */
+#define JBGPU_STAGE_INTEGRATE     7 /* integrateTransforms                              */
+#define JBGPU_STAGE_ACTIVATION    8 /* updateActivationState                            */
+#define JBGPU_STAGE_CLEAR_FORCES  9 /* clearForces                                      */
+
+/* Floats per manifold point in jbgpu_manifolds.points (ManifoldPoint,
+ * collision/narrowphase/ManifoldPoint.java:36-62):
+ *  0-2 localPointA   3-5 localPointB   6-8 positionWorldOnA   9-11 positionWorldOnB
+ *  12-14 normalWorldOnB  15 distance1  16 combinedFriction  17 combinedRestitution
+ *  18 appliedImpulse  19 appliedImpulseLateral1  20 appliedImpulseLateral2
+ *  21 lateralFrictionInitialized (0/1)  22 lifeTime (integer value)
+ *  23-25 lateralFrictionDir1  26-28 lateralFrictionDir2  29-31 unused (0)          */
+#define JBGPU_POINT_FLOATS 32
+#define JBGPU_MANIFOLD_POINTS 4
+
+/* Pair keys.  A pair of bodies (a, b) (body index = uid - 1) is stored under the
+ * canonical key (owner << 32) | partner, where the owner is the non-plane body
+ * when exactly one body is a static plane, else min(a, b).  Keys are unique and
+ * pair arrays are always sorted by key.  The reference keeps the same set
+ * (collision/broadphase/HashedOverlappingPairCache.java:291-347) in hash order. */
+
+typedef struct jbgpu_config {
+    float   gravity[3];                 /* default (0,-10,0)  DiscreteDynamicsWorld.java:71 */
+    float   contact_breaking_threshold; /* default 0.02       BulletGlobals.java:61 */
+    float   deactivation_time;          /* default 2.0        BulletGlobals.java:63 */
+    int32_t disable_deactivation;       /* default 0          BulletGlobals.java:64 */
+    int32_t num_iterations;             /* default 10         ContactSolverInfo.java:38 */
+    float   erp;                        /* default 0.2        ContactSolverInfo.java:41 */
+    float   warmstarting_factor;        /* default 0.85       ContactSolverInfo.java:46 */
+    float   linear_slop;                /* default 0          ContactSolverInfo.java:45 */
+    int32_t solver_mode;                /* default CACHE_FRIENDLY|USE_WARMSTARTING */
+    int32_t device;                     /* CUDA device ordinal, default 0 */
+    int32_t initial_body_capacity;      /* device arrays grow on demand; default 1024 */
+    int32_t pairs_per_body;             /* initial pair capacity per body, default 16 */
+    int32_t reserved[8];
+} jbgpu_config;
+
+typedef struct jbgpu_shape_desc {
+    int32_t      type;       /* JBGPU_SHAPE_* */
+    float        params[4];  /* BOX: half extents xyz (BoxShape(Vector3)); SPHERE: radius;
+                                CAPSULE: radius, height (CapsuleShape(radius, height), up axis y);
+                                STATIC_PLANE: normal xyz, plane constant; CONVEX_HULL: unused */
+    const float* points;     /* CONVEX_HULL: num_points * 3 floats (ConvexHullShape(points)) */
+    int32_t      num_points;
+} jbgpu_shape_desc;
+
+/* RigidBodyConstructionInfo (dynamics/RigidBodyConstructionInfo.java:46-79) plus the
+ * velocities a caller sets with setLinearVelocity/setAngularVelocity before stepping. */
+typedef struct jbgpu_body_desc {
+    float   mass;                       /* 0 => static object */
+    int32_t shape;                      /* id from jbgpu_world_add_shape */
+    float   transform[12];              /* basis row-major (9), origin (3) */
+    float   local_inertia[3];           /* usually from jbgpu_shape_local_inertia */
+    float   linear_damping;             /* 0 */
+    float   angular_damping;            /* 0 */
+    float   friction;                   /* 0.5 */
+    float   restitution;                /* 0 */
+    float   linear_sleeping_threshold;  /* 0.8 */
+    float   angular_sleeping_threshold; /* 1.0 */
+    float   linear_velocity[3];
+    float   angular_velocity[3];
+    int32_t collision_group;            /* -1: DEFAULT (dynamic) / STATIC (static) */
+    int32_t collision_mask;             /* -1: ALL / ALL^STATIC  (DiscreteDynamicsWorld.java:426-440) */
+    int32_t world;                      /* batch world index: bodies of different worlds never collide
+                                           (0 for an ordinary single world) */
+} jbgpu_body_desc;
+
+/* Body state, structure of arrays.  Any pointer may be NULL (field skipped). */
+typedef struct jbgpu_state {
+    int32_t  n_bodies;            /* get: written; set: must equal the world's body count */
+    float*   transform;           /* 12 per body */
+    float*   linear_velocity;     /* 3 */
+    float*   angular_velocity;    /* 3 */
+    float*   inv_inertia_world;   /* 9 (row-major) */
+    float*   total_force;         /* 3 */
+    float*   total_torque;        /* 3 */
+    float*   aabb;                /* 6: broadphase proxy aabb min xyz, max xyz */
+    int32_t* activation_state;    /* JBGPU_ACTIVE_TAG ... */
+    float*   deactivation_time;
+    int32_t* island_tag;          /* get only: island root body index, -1 for static/kinematic */
+} jbgpu_state;
+
+/* Overlapping pairs with their persistent manifolds (one per pair). */
+typedef struct jbgpu_manifolds {
+    int32_t   n_pairs;     /* get: written; set: number of entries provided */
+    int32_t   capacity;    /* get: entries the caller's arrays can hold */
+    uint64_t* keys;        /* canonical keys, sorted ascending */
+    int32_t*  flags;       /* bit0: the pair owns a collision algorithm and manifold */
+    int32_t*  num_points;  /* 0..4 */
+    float*    points;      /* capacity * 4 * JBGPU_POINT_FLOATS */
+} jbgpu_manifolds;
+
+typedef struct jbgpu_counters {
+    int64_t steps;            /* internal single steps taken */
+    int32_t bodies;
+    int32_t pairs;            /* overlapping pairs after the last broadphase */
+    int32_t manifolds;        /* pairs owning a manifold */
+    int32_t contacts;         /* manifold points over all manifolds */
+    int32_t solver_manifolds; /* manifolds with >= 1 solver row in the last solve */
+    int32_t solver_rows;      /* normal rows (each adds 2 friction rows) */
+    int32_t colours;          /* colours of the last solve */
+    int32_t islands;          /* islands with >= 1 dynamic body */
+    int32_t gjk_calls;        /* BulletStats.gNumGjkChecks for the last step */
+    int32_t epa_calls;        /* BulletStats.gNumDeepPenetrationChecks for the last step */
+    int32_t status_flags;     /* bit0 capacity, bit1 EPA pool, bit2 timeout, bit3 non-finite */
+    int32_t reserved[6];
+} jbgpu_counters;
+
+/* ---- library -------------------------------------------------------------------- */
+const char* jbgpu_version(void);
+const char* jbgpu_last_error(void);          /* thread-local message for the last failure */
+void        jbgpu_config_default(jbgpu_config* cfg);
+
+/* CollisionShape.calculateLocalInertia for a shape description (host arithmetic). */
+int jbgpu_shape_local_inertia(const jbgpu_shape_desc* shape, float mass, float inertia_out[3]);
+
+/* ---- world ---------------------------------------------------------------------- */
+typedef struct jbgpu_world jbgpu_world;
+
+int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out);
+int jbgpu_world_destroy(jbgpu_world* world);
+int jbgpu_world_add_shape(jbgpu_world* world, const jbgpu_shape_desc* shape, int32_t* shape_id);
+/* n shapes at once; ids_out (may be NULL) receives consecutive ids. */
+int jbgpu_world_add_shapes(jbgpu_world* world, const jbgpu_shape_desc* shapes, int32_t n, int32_t* ids_out);
+int jbgpu_world_add_bodies(jbgpu_world* world, const jbgpu_body_desc* bodies, int32_t n, int32_t* uids_out);
+int jbgpu_world_num_bodies(const jbgpu_world* world, int32_t* n);
+
+/* stepSimulation: the reference's fixed-timestep accumulator, applyGravity once per call,
+ * then min(numSubSteps, maxSubSteps) internal single steps, then clearForces. */
+int jbgpu_world_step_simulation(jbgpu_world* world, float time_step, int32_t max_sub_steps,
+                                float fixed_time_step, int32_t* num_sub_steps);
+/* applyGravity, `substeps` internal single steps of `fixed_time_step`, clearForces. */
+int jbgpu_world_step(jbgpu_world* world, float fixed_time_step, int32_t substeps);
+/* One phase of internalSingleStepSimulation (JBGPU_STAGE_*), for open-loop checks. */
+int jbgpu_world_stage(jbgpu_world* world, int32_t stage, float time_step);
+/* Wait for the world's stream. */
+int jbgpu_world_synchronize(jbgpu_world* world);
+
+int jbgpu_world_get_state(jbgpu_world* world, jbgpu_state* state);
+int jbgpu_world_set_state(jbgpu_world* world, const jbgpu_state* state);
+int jbgpu_world_get_pairs(jbgpu_world* world, uint64_t* keys, int32_t capacity, int32_t* n_pairs);
+int jbgpu_world_get_manifolds(jbgpu_world* world, jbgpu_manifolds* m);
+int jbgpu_world_set_manifolds(jbgpu_world* world, const jbgpu_manifolds* m);
+/* Pair indices of the manifolds of the last solve, in the sequential order the colour
+ * phases are equivalent to (the order fed to the reference solver for parity). */
+int jbgpu_world_get_solver_order(jbgpu_world* world, int32_t* pair_index, int32_t capacity, int32_t* n);
+int jbgpu_world_counters(jbgpu_world* world, jbgpu_counters* counters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* JBGPU_H */

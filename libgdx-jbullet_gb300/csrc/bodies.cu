@@ -1,0 +1,149 @@
+// Per-body phases of the step: applyGravity, predictUnconstraintMotion, updateAabbs,
+// integrateTransforms, updateActivationState, clearForces.  One thread per body; every
+// kernel streams structure-of-arrays body records (HBM bound).
+// Citations relative to src/com/bulletphysics/ of the reference.
+#include "shapes.cuh"
+
+namespace jbg {
+using namespace jbd;
+
+static inline int grid_for(int n, int block) { return (n + block - 1) / block; }
+
+// DiscreteDynamicsWorld.applyGravity (dynamics/DiscreteDynamicsWorld.java:239-249)
+__global__ void k_apply_gravity(DevWorld w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    if (!is_active_state(w.act[i]) || is_static_or_kin(w.flags[i])) return;
+    float4 f = w.force[i], g = w.gravity[i];
+    w.force[i] = make_float4(__fadd_rn(f.x, g.x), __fadd_rn(f.y, g.y), __fadd_rn(f.z, g.z), 0.0f);
+}
+
+// predictUnconstraintMotion (DiscreteDynamicsWorld.java:741-767):
+// RigidBody.integrateVelocities + applyDamping (dynamics/RigidBody.java:246-299,323-342)
+__global__ void k_predict(DevWorld w, float dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    if (is_static_or_kin(w.flags[i]) || !is_active_state(w.act[i])) return;
+    const float MAX_ANGVEL = __fmul_rn(SIMD_2_PI, 0.25f);
+    float im = w.iloc[i].w;
+    float4 F = w.force[i];
+    V lv = mk4(w.linvel[i]);
+    float imdt = __fmul_rn(im, dt);
+    lv.x = __fadd_rn(lv.x, __fmul_rn(imdt, F.x));
+    lv.y = __fadd_rn(lv.y, __fmul_rn(imdt, F.y));
+    lv.z = __fadd_rn(lv.z, __fmul_rn(imdt, F.z));
+    V av = mk4(w.angvel[i]);
+    V tmp = scl(mulMv(mk4(w.torque[i]), load_iw(w, i)), dt);
+    av = add(av, tmp);
+    float a = len(av);
+    if (__fmul_rn(a, dt) > MAX_ANGVEL) av = scl(av, jdiv(jdiv(MAX_ANGVEL, dt), a));
+    float ld = w.linDamp[i], ad = w.angDamp[i];
+    lv = scl(lv, jpow(__fsub_rn(1.0f, ld), dt));
+    av = scl(av, jpow(__fsub_rn(1.0f, ad), dt));
+    w.linvel[i] = f4(lv, 0.0f);
+    w.angvel[i] = f4(av, 0.0f);
+}
+
+// CollisionWorld.updateSingleAabb (collision/dispatch/CollisionWorld.java:195-229)
+__global__ void k_aabb(DevWorld w) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    int act = w.act[i];
+    if (!is_active_state(act)) return;
+    Xf t = load_xf(w, i);
+    V mn, mx;
+    shape_aabb(w.sh, w.shape[i], t, mn, mx);
+    float c = w.cbt;
+    mn = sub(mn, mk(c, c, c));
+    mx = add(mx, mk(c, c, c));
+    V d = sub(mx, mn);
+    if ((w.flags[i] & CF_STATIC) || (len2(d) < 1e12f)) {
+        w.amin[i] = f4(mn, 0.0f);
+        w.amax[i] = f4(mx, 0.0f);
+    } else {
+        w.act[i] = set_activation(act, DISABLE_SIMULATION);
+    }
+}
+
+// integrateTransforms (DiscreteDynamicsWorld.java:679-739), CCD off; then
+// RigidBody.setCenterOfMassTransform -> updateInertiaTensor (dynamics/RigidBody.java:344-354,449-459)
+__global__ void k_integrate(DevWorld w, float dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    if (!is_active_state(w.act[i]) || is_static_or_kin(w.flags[i])) return;
+    Xf t = load_xf(w, i);
+    Xf p = integrate_transform(t, mk4(w.linvel[i]), mk4(w.angvel[i]), dt);
+    store_xf(w, i, p);
+    M m1 = scaleM(p.b, mk4(w.iloc[i]));
+    M iw = mulMM(m1, transpose(p.b));
+    w.iw0[i] = f4(iw.r[0], 0.0f);
+    w.iw1[i] = f4(iw.r[1], 0.0f);
+    w.iw2[i] = f4(iw.r[2], 0.0f);
+}
+
+// updateActivationState (DiscreteDynamicsWorld.java:475-512) with RigidBody.updateDeactivation /
+// wantsSleeping (dynamics/RigidBody.java:543-576)
+__global__ void k_activation(DevWorld w, float dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    int act = w.act[i];
+    float dtime = w.deact[i];
+    V lv = mk4(w.linvel[i]), av = mk4(w.angvel[i]);
+    if (!(act == ISLAND_SLEEPING || act == DISABLE_DEACTIVATION)) {
+        float ls = w.linSleep[i], as = w.angSleep[i];
+        if (len2(lv) < __fmul_rn(ls, ls) && len2(av) < __fmul_rn(as, as)) {
+            dtime = __fadd_rn(dtime, dt);
+        } else {
+            dtime = 0.0f;
+            act = set_activation(act, 0);
+        }
+    }
+    bool wants;
+    if (act == DISABLE_DEACTIVATION) wants = false;
+    else if (w.disableDeact || w.deactTime == 0.0f) wants = false;
+    else if (act == ISLAND_SLEEPING || act == WANTS_DEACTIVATION) wants = true;
+    else wants = dtime > w.deactTime;
+    if (wants) {
+        if (is_static_or_kin(w.flags[i])) {
+            act = set_activation(act, ISLAND_SLEEPING);
+        } else {
+            if (act == ACTIVE_TAG) act = set_activation(act, WANTS_DEACTIVATION);
+            if (act == ISLAND_SLEEPING) {
+                w.linvel[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                w.angvel[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+        }
+    } else {
+        if (act != DISABLE_DEACTIVATION) act = set_activation(act, ACTIVE_TAG);
+    }
+    w.act[i] = act;
+    w.deact[i] = dtime;
+}
+
+__global__ void k_clear_forces(DevWorld w) {   // DiscreteDynamicsWorld.clearForces (java:226-236)
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    w.force[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    w.torque[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+void launch_apply_gravity(const DevWorld& w, cudaStream_t s) {
+    if (w.nBodies) k_apply_gravity<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w);
+}
+void launch_predict(const DevWorld& w, float dt, cudaStream_t s) {
+    if (w.nBodies) k_predict<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, dt);
+}
+void launch_aabb(const DevWorld& w, cudaStream_t s) {
+    if (w.nBodies) k_aabb<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w);
+}
+void launch_integrate(const DevWorld& w, float dt, cudaStream_t s) {
+    if (w.nBodies) k_integrate<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, dt);
+}
+void launch_activation(const DevWorld& w, float dt, cudaStream_t s) {
+    if (w.nBodies) k_activation<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, dt);
+}
+void launch_clear_forces(const DevWorld& w, cudaStream_t s) {
+    if (w.nBodies) k_clear_forces<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w);
+}
+
+}  // namespace jbg

@@ -1,0 +1,335 @@
+// Broadphase: the overlapping-pair set of the reference's DbvtBroadphase, rebuilt each step.
+//
+// The reference keeps an incremental dynamic AABB tree and, after collide(), its pair cache
+// holds exactly the filter-passing pairs whose proxy aabbs intersect inclusively
+// (collision/broadphase/DbvtBroadphase.java:89-150, DbvtTreeCollider.java:36-51,
+// DbvtAabbMm.java:209-212, HashedOverlappingPairCache.java:179-188).  Here:
+//   1. 30-bit Morton codes of finite proxy aabb centres, world index in the high key bits;
+//   2. stable radix sort; 3. Karras radix tree over the sorted leaves (one root per world);
+//   4. bottom-up refit; 5. a counting traversal (pair owner = the lower body index, or the
+//   finite body of a pair with a static plane), exclusive scan -> per-owner CSR;
+//   6. a filling traversal, per-owner partner sort -> keys sorted ascending;
+//   7. persistence: each new key is looked up among last step's sorted keys and its
+//   manifold (the reference's algorithm lifetime, HashedOverlappingPairCache.java:222-228) is
+//   carried over.
+// Static planes (infinite aabb, StaticPlaneShape.java:124-128) stay out of the tree; each
+// finite body tests the planes of its world directly.
+#include "broadphase.cuh"
+#include "prims.cuh"
+
+namespace jbg {
+using namespace jbd;
+
+__device__ __forceinline__ unsigned f2ord(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(unsigned u) {
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Scene bounds of finite aabb centres (ordered-int atomics).
+__global__ void k_bounds(DevWorld w, unsigned* bnd) {
+    __shared__ unsigned s[6];
+    if (threadIdx.x < 6) s[threadIdx.x] = (threadIdx.x < 3) ? 0xffffffffu : 0u;
+    __syncthreads();
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < w.nBodies && !(w.flags[i] & CF_PLANE)) {
+        float4 a = w.amin[i], b = w.amax[i];
+        float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+        for (int k = 0; k < 3; k++) {
+            atomicMin(&s[k], f2ord(c[k]));
+            atomicMax(&s[3 + k], f2ord(c[k]));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) atomicMin(&bnd[threadIdx.x], s[threadIdx.x]);
+    else if (threadIdx.x < 6) atomicMax(&bnd[threadIdx.x], s[threadIdx.x]);
+}
+
+__device__ __forceinline__ unsigned expand_bits(unsigned v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+// key = world << 32 | morton30 for finite bodies; planes get the all-ones key (sorted last).
+__global__ void k_morton(DevWorld w, const unsigned* bnd, uint64_t* keys, int* vals) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    vals[i] = i;
+    if (w.flags[i] & CF_PLANE) { keys[i] = ~0ull; return; }
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; k++) { lo[k] = ord2f(bnd[k]); hi[k] = ord2f(bnd[3 + k]); }
+    float4 a = w.amin[i], b = w.amax[i];
+    float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+    unsigned q[3];
+    for (int k = 0; k < 3; k++) {
+        float ext = hi[k] - lo[k];
+        float t = ext > 0.0f ? (c[k] - lo[k]) / ext : 0.5f;
+        t = fminf(fmaxf(t, 0.0f), 1.0f);
+        q[k] = min((unsigned)(t * 1024.0f), 1023u);
+    }
+    unsigned m = (expand_bits(q[0]) << 2) | (expand_bits(q[1]) << 1) | expand_bits(q[2]);
+    keys[i] = ((uint64_t)(unsigned)w.world[i] << 32) | m;
+}
+
+__device__ __forceinline__ int delta(const uint64_t* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = k[i], b = k[j];
+    if (a == b) return 64 + __clz(i ^ j);
+    return __clzll(a ^ b);
+}
+
+// World leaf ranges in the sorted leaf order; single-leaf worlds get the leaf as root.
+__global__ void k_world_ranges(const uint64_t* keys, int nf, int* wstart, int* wend, int* wroot) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    int wi = (int)(keys[i] >> 32);
+    if (i == 0 || (int)(keys[i - 1] >> 32) != wi) wstart[wi] = i;
+    if (i == nf - 1 || (int)(keys[i + 1] >> 32) != wi) {
+        wend[wi] = i + 1;
+        int s = (i == 0 || (int)(keys[i - 1] >> 32) != wi) ? i : -1;
+        if (s == i) wroot[wi] = LEAF_FLAG | i;
+    }
+}
+
+// Karras 2012 radix-tree construction over nf sorted leaves.
+__global__ void k_karras(const uint64_t* keys, int nf, Bvh t, const int* wstart, const int* wend, int* wroot) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf - 1) return;
+    int d = (delta(keys, nf, i, i + 1) - delta(keys, nf, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(keys, nf, i, i - d);
+    int lmax = 2;
+    while (delta(keys, nf, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int s = lmax >> 1; s >= 1; s >>= 1)
+        if (delta(keys, nf, i, i + (l + s) * d) > dmin) l += s;
+    int j = i + l * d;
+    int dnode = delta(keys, nf, i, j);
+    int s = 0, tt = l;
+    do {
+        tt = (tt + 1) >> 1;
+        if (delta(keys, nf, i, i + (s + tt) * d) > dnode) s += tt;
+    } while (tt > 1);
+    int gamma = i + s * d + min(d, 0);
+    int lo = min(i, j), hi = max(i, j);
+    int left = (lo == gamma) ? (LEAF_FLAG | gamma) : gamma;
+    int right = (hi == gamma + 1) ? (LEAF_FLAG | (gamma + 1)) : (gamma + 1);
+    t.left[i] = left;
+    t.right[i] = right;
+    t.lo[i] = lo;
+    t.hi[i] = hi;
+    if (left & LEAF_FLAG) t.leafParent[gamma] = i; else t.parent[gamma] = i;
+    if (right & LEAF_FLAG) t.leafParent[gamma + 1] = i; else t.parent[gamma + 1] = i;
+    int wi = (int)(keys[lo] >> 32);
+    if (wstart[wi] == lo && wend[wi] == hi + 1) wroot[wi] = i;
+}
+
+// Bottom-up refit: the second child to arrive merges the boxes (node 0's parent is -1).
+__global__ void k_refit(DevWorld w, const int* sortedBody, int nf, Bvh t) {
+    int leaf = blockIdx.x * blockDim.x + threadIdx.x;
+    if (leaf >= nf) return;
+    int node = t.leafParent[leaf];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&t.visit[node], 1) == 0) return;
+        __threadfence();
+        float4 mn[2], mx[2];
+        int ch[2] = {t.left[node], t.right[node]};
+        for (int c = 0; c < 2; c++) {
+            if (ch[c] & LEAF_FLAG) {
+                int b = sortedBody[ch[c] & ~LEAF_FLAG];
+                mn[c] = w.amin[b];
+                mx[c] = w.amax[b];
+            } else {
+                mn[c] = __ldcg(&t.bmin[ch[c]]);
+                mx[c] = __ldcg(&t.bmax[ch[c]]);
+            }
+        }
+        __stcg(&t.bmin[node], make_float4(fminf(mn[0].x, mn[1].x), fminf(mn[0].y, mn[1].y), fminf(mn[0].z, mn[1].z), 0.0f));
+        __stcg(&t.bmax[node], make_float4(fmaxf(mx[0].x, mx[1].x), fmaxf(mx[0].y, mx[1].y), fmaxf(mx[0].z, mx[1].z), 0.0f));
+        node = t.parent[node];
+    }
+}
+
+__device__ __forceinline__ bool ovl(float4 a0, float4 a1, float4 b0, float4 b1) {
+    return (a0.x <= b1.x) && (a1.x >= b0.x) && (a0.y <= b1.y) && (a1.y >= b0.y) && (a0.z <= b1.z) && (a1.z >= b0.z);
+}
+__device__ __forceinline__ bool filt(const DevWorld& w, int a, int b) {
+    return (w.group[a] & w.mask[b]) != 0 && (w.group[b] & w.mask[a]) != 0;
+}
+
+constexpr int STACK = 96;
+
+// One leaf's traversal: pairs (s, t) with t > s in sorted order.  FILL == false counts
+// pairs per owner; FILL == true writes partners into the owner's CSR segment.
+template <bool FILL>
+__global__ void k_traverse(DevWorld w, const int* sortedBody, int nf, Bvh t, const int* wroot, int* cnt, const int* off,
+                           int* cursor, int* partners, int capacity) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nf) return;
+    int bi = sortedBody[s];
+    float4 a0 = w.amin[bi], a1 = w.amax[bi];
+    int root = wroot[w.world[bi]];
+    if (root & LEAF_FLAG) return;   // single-leaf world
+    int stack[STACK];
+    int sp = 0;
+    stack[sp++] = root;
+    while (sp > 0) {
+        int node = stack[--sp];
+        int ch[2] = {t.left[node], t.right[node]};
+        for (int c = 0; c < 2; c++) {
+            int x = ch[c];
+            if (x & LEAF_FLAG) {
+                int tl = x & ~LEAF_FLAG;
+                if (tl <= s) continue;
+                int bj = sortedBody[tl];
+                if (!ovl(a0, a1, w.amin[bj], w.amax[bj]) || !filt(w, bi, bj)) continue;
+                int owner = bi < bj ? bi : bj, partner = bi < bj ? bj : bi;
+                if (!FILL) {
+                    atomicAdd(&cnt[owner], 1);
+                } else {
+                    int pos = off[owner] + atomicAdd(&cursor[owner], 1);
+                    if (pos < capacity) partners[pos] = partner;
+                }
+            } else {
+                if (t.hi[x] <= s) continue;
+                if (!ovl(a0, a1, t.bmin[x], t.bmax[x])) continue;
+                if (sp < STACK) stack[sp++] = x;
+                else atomicOr(&w.ctr[C_STATUS], ST_CAPACITY);
+            }
+        }
+    }
+}
+
+// Pairs of each finite body with the static planes of its world.
+template <bool FILL>
+__global__ void k_plane_pairs(DevWorld w, const int* planeList, const int* planeStart, int* cnt, const int* off,
+                              int* cursor, int* partners, int capacity) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies || (w.flags[i] & CF_PLANE)) return;
+    int wi = w.world[i];
+    float4 a0 = w.amin[i], a1 = w.amax[i];
+    for (int k = planeStart[wi]; k < planeStart[wi + 1]; k++) {
+        int p = planeList[k];
+        if (!ovl(a0, a1, w.amin[p], w.amax[p]) || !filt(w, i, p)) continue;
+        if (!FILL) atomicAdd(&cnt[i], 1);
+        else {
+            int pos = off[i] + atomicAdd(&cursor[i], 1);
+            if (pos < capacity) partners[pos] = p;
+        }
+    }
+}
+
+// Sort each owner's partners ascending and emit the canonical keys.
+__global__ void k_segment_sort(int n, const int* off, const int* cnt, int* partners, uint64_t* keys, int capacity) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int o = off[i], c = cnt[i];
+    if (o + c > capacity) return;
+    int* p = partners + o;
+    if (c <= 32) {
+        int v[32];
+        for (int k = 0; k < c; k++) v[k] = p[k];
+        for (int k = 1; k < c; k++) {
+            int x = v[k], j = k - 1;
+            while (j >= 0 && v[j] > x) { v[j + 1] = v[j]; j--; }
+            v[j + 1] = x;
+        }
+        for (int k = 0; k < c; k++) keys[o + k] = ((uint64_t)(unsigned)i << 32) | (unsigned)v[k];
+    } else {
+        for (int gap = c / 2; gap > 0; gap /= 2)          // Shell sort for rare crowded owners
+            for (int k = gap; k < c; k++) {
+                int x = p[k], j = k;
+                while (j >= gap && p[j - gap] > x) { p[j] = p[j - gap]; j -= gap; }
+                p[j] = x;
+            }
+        for (int k = 0; k < c; k++) keys[o + k] = ((uint64_t)(unsigned)i << 32) | (unsigned)p[k];
+    }
+}
+
+// Carry manifolds of persisting pairs (binary search in last step's sorted keys).
+__global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int nOld) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nNew) return;
+    uint64_t key = nw.keys[p];
+    int lo = 0, hi = nOld - 1, found = -1;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        uint64_t k = old.keys[mid];
+        if (k == key) { found = mid; break; }
+        if (k < key) lo = mid + 1; else hi = mid - 1;
+    }
+    int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+    if (found >= 0 && old.has[found]) {
+        int n = old.n[found];
+        nw.has[p] = 1;
+        nw.n[p] = n;
+        nw.b0[p] = old.b0[found];
+        nw.b1[p] = old.b1[found];
+        for (int j = 0; j < n; j++) {
+            int s = found * 4 + j, d = p * 4 + j;
+            nw.pA[d] = old.pA[s]; nw.pB[d] = old.pB[s]; nw.wA[d] = old.wA[s]; nw.wB[d] = old.wB[s];
+            nw.nrm[d] = old.nrm[s]; nw.imp[d] = old.imp[s]; nw.d1[d] = old.d1[s]; nw.d2[d] = old.d2[s];
+        }
+    } else {
+        nw.has[p] = 0;
+        nw.n[p] = 0;
+        bool bPlane = (w.flags[b] & CF_PLANE) != 0;
+        nw.b0[p] = bPlane ? a : min(a, b);   // manifold (convex, plane) or (lower uid, higher uid)
+        nw.b1[p] = bPlane ? b : max(a, b);
+    }
+}
+
+static inline int gridn(int n, int b) { return (n + b - 1) / b; }
+
+void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s) {
+    int n = w.nBodies;
+    cudaMemsetAsync(bb.bounds, 0, sizeof(unsigned) * 6, s);
+    cudaMemsetAsync(bb.bounds, 0xff, sizeof(unsigned) * 3, s);
+    k_bounds<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds);
+    k_morton<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds, bb.mkeys, bb.sortedBody);
+    radix_sort_pairs(bb.mkeys, bb.sortedBody, bb.mkeys_alt, bb.vals_alt, n, 32 + bb.worldBits, bb.sortScratch, s);
+    int nf = bb.nFinite;
+    cudaMemsetAsync(bb.cnt, 0, sizeof(int) * (n + 1), s);
+    if (nf > 0) {
+        cudaMemsetAsync(bb.wstart, 0xff, sizeof(int) * bb.nWorlds, s);
+        cudaMemsetAsync(bb.wend, 0xff, sizeof(int) * bb.nWorlds, s);
+        cudaMemsetAsync(bb.wroot, 0xff, sizeof(int) * bb.nWorlds, s);
+        k_world_ranges<<<gridn(nf, 256), 256, 0, s>>>(bb.mkeys, nf, bb.wstart, bb.wend, bb.wroot);
+        if (nf > 1) {
+            cudaMemsetAsync(bb.bvh.visit, 0, sizeof(int) * (nf - 1), s);
+            cudaMemsetAsync(bb.bvh.parent, 0xff, sizeof(int) * (nf - 1), s);
+            k_karras<<<gridn(nf - 1, 256), 256, 0, s>>>(bb.mkeys, nf, bb.bvh, bb.wstart, bb.wend, bb.wroot);
+            k_refit<<<gridn(nf, 256), 256, 0, s>>>(w, bb.sortedBody, nf, bb.bvh);
+            k_traverse<false><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, bb.cnt, nullptr,
+                                                              nullptr, nullptr, 0);
+        }
+    }
+    if (bb.nPlanes > 0)
+        k_plane_pairs<false><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, bb.cnt, nullptr, nullptr,
+                                                            nullptr, 0);
+    exclusive_scan(bb.cnt, bb.off, bb.total, n + 1, bb.scanScratch, s);
+}
+
+void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, int capacity, cudaStream_t s) {
+    int n = w.nBodies, nf = bb.nFinite;
+    cudaMemsetAsync(bb.cursor, 0, sizeof(int) * (n + 1), s);
+    // counts are recovered from the offsets: cnt[i] = off[i+1] - off[i]
+    if (nf > 1)
+        k_traverse<true><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, nullptr, bb.off,
+                                                         bb.cursor, bb.partners, capacity);
+    if (bb.nPlanes > 0)
+        k_plane_pairs<true><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, nullptr, bb.off, bb.cursor,
+                                                           bb.partners, capacity);
+    k_segment_sort<<<gridn(n, 128), 128, 0, s>>>(n, bb.off, bb.cursor, bb.partners, nw.keys, capacity);
+}
+
+void broadphase_persist(const DevWorld& w, DevPairs& nw, const DevPairs& old, int nNew, int nOld, cudaStream_t s) {
+    if (nNew > 0) k_persist<<<gridn(nNew, 256), 256, 0, s>>>(w, nw, old, nNew, nOld);
+}
+
+}  // namespace jbg

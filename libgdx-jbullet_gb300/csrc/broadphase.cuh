@@ -1,0 +1,46 @@
+#pragma once
+#include "jbgpu_internal.cuh"
+
+namespace jbg {
+
+constexpr int LEAF_FLAG = 0x40000000;
+
+struct Bvh {           // Karras radix tree over nf sorted leaves; internal nodes 0..nf-2
+    int* left;
+    int* right;        // child index, LEAF_FLAG set for leaves
+    int* lo;
+    int* hi;           // sorted-leaf range covered by the node
+    int* parent;       // internal node parents (-1 at roots)
+    int* leafParent;
+    int* visit;        // refit arrival counters
+    float4* bmin;
+    float4* bmax;
+};
+
+struct BroadphaseBuffers {
+    int nFinite = 0, nPlanes = 0, nWorlds = 1, worldBits = 0;
+    unsigned* bounds = nullptr;          // 6 ordered-int scene bounds
+    uint64_t* mkeys = nullptr;           // morton keys (sorted in place)
+    uint64_t* mkeys_alt = nullptr;
+    int* sortedBody = nullptr;           // body of each sorted leaf
+    int* vals_alt = nullptr;
+    void* sortScratch = nullptr;
+    void* scanScratch = nullptr;
+    Bvh bvh{};
+    int* wstart = nullptr;               // per world sorted-leaf range and root
+    int* wend = nullptr;
+    int* wroot = nullptr;
+    int* planeList = nullptr;            // plane bodies grouped by world
+    int* planeStart = nullptr;           // nWorlds + 1 offsets into planeList
+    int* cnt = nullptr;                  // pairs per owner (n + 1)
+    int* off = nullptr;                  // exclusive scan of cnt (n + 1); off[n] = total
+    int* cursor = nullptr;               // fill cursors (n + 1)
+    int* total = nullptr;                // device total pair count
+    int* partners = nullptr;             // CSR partner lists (pair capacity)
+};
+
+void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s);
+void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, int capacity, cudaStream_t s);
+void broadphase_persist(const DevWorld& w, DevPairs& nw, const DevPairs& old, int nNew, int nOld, cudaStream_t s);
+
+}  // namespace jbg

@@ -1,0 +1,139 @@
+// Device-side layout of a world: structure-of-arrays in HBM, one entry per body / shape /
+// pair / manifold point.  Kernels receive a DevWorld by value (plain device pointers).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "jbm.cuh"
+
+namespace jbg {
+
+enum { SHAPE_BOX = 0, SHAPE_HULL = 4, SHAPE_SPHERE = 6, SHAPE_CAPSULE = 8, SHAPE_PLANE = 23 };
+enum { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEACTIVATION = 4, DISABLE_SIMULATION = 5 };
+enum { CF_STATIC = 1, CF_KINEMATIC = 2, CF_NO_CONTACT_RESPONSE = 4, CF_PLANE = 64 };
+enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8 };
+
+// Counters kept on the device (indices into DevWorld::ctr).
+enum {
+    C_PAIRS = 0, C_FILL_OVERFLOW, C_EPA_QUEUE, C_GJK, C_EPA, C_SOLVE_N, C_COLOURS, C_ISLANDS,
+    C_MANIFOLDS, C_CONTACTS, C_ROWS, C_STATUS, C_BAR_COUNT, C_BAR_GEN, C_REMAIN0, C_REMAIN1, C_NCTR = 32
+};
+
+struct DevShapes {
+    int* type;
+    float* margin;        // getMargin() (sphere: radius)
+    float4* dims;         // implicitShapeDimensions xyz; w: capsule up axis
+    float4* laabb_min;    // hull local aabb (PolyhedralConvexShape.recalcLocalAabb)
+    float4* laabb_max;
+    float4* plane;        // static plane normal xyz, constant w
+    int* hull_off;
+    int* hull_cnt;
+    float4* hull_pts;
+};
+
+// Manifold point, one record spread over eight float4 arrays indexed [pair * 4 + point]:
+//  pA  = localPointA.xyz, distance1        pB  = localPointB.xyz, lifeTime (int bits)
+//  wA  = positionWorldOnA.xyz, friction    wB  = positionWorldOnB.xyz, restitution
+//  nrm = normalWorldOnB.xyz, appliedImpulse
+//  imp = appliedImpulseLateral1, appliedImpulseLateral2, lateralFrictionInitialized, 0
+//  d1  = lateralFrictionDir1.xyz           d2  = lateralFrictionDir2.xyz
+struct DevPairs {
+    uint64_t* keys;       // sorted canonical keys (owner << 32 | partner)
+    int* has;             // pair owns an algorithm + manifold
+    int* n;               // manifold points
+    int* b0;              // manifold body0 / body1
+    int* b1;
+    float4 *pA, *pB, *wA, *wB, *nrm, *imp, *d1, *d2;
+};
+
+// Solver rows, indexed by solve slot * 4 + point (normal) and (solve slot * 4 + point) * 2 + k
+// (friction).  Slots are grouped by colour.
+struct DevRows {
+    float4* n_nrm;    // contactNormal, jacDiagABInv
+    float4* n_rp1;    // relpos1CrossNormal, penetration
+    float4* n_rp2;    // relpos2CrossNormal, restitution
+    float4* n_angA;   // angularComponentA, friction
+    float4* n_angB;   // angularComponentB, appliedImpulse
+    float4* f_nrm;    // friction rows: direction, jacDiagABInv
+    float4* f_rp1;    // relpos1CrossNormal, appliedImpulse
+    float4* f_rp2;
+    float4* f_angA;
+    float4* f_angB;
+    int* slot_pair;   // pair index of the manifold in each solve slot
+    int* slot_mask;   // bit j: point j has rows
+    int* colour_start;// colour c occupies slots [colour_start[c], colour_start[c+1])
+};
+
+struct DevWorld {
+    int nBodies;
+    int nPairs;           // pairs of the current pair arrays (device copy in ctr[C_PAIRS])
+    // body state
+    float4 *xr0, *xr1, *xr2;        // basis rows; origin in .w
+    float4 *linvel, *angvel;
+    float4 *iw0, *iw1, *iw2;        // inverse inertia tensor (world) rows
+    float4 *iloc;                   // inverse inertia (local) xyz, inverse mass w
+    float4 *force, *torque, *gravity;
+    float4 *amin, *amax;            // broadphase proxy aabb
+    int* act;
+    float* deact;
+    int* flags;
+    int* shape;
+    int* group;
+    int* mask;
+    int* world;                     // batch world index (0 for single worlds)
+    float* friction;
+    float* restitution;
+    float* linSleep;
+    float* angSleep;
+    float* linDamp;
+    float* angDamp;
+    int* island;                    // island root body (min index), -1 static/kinematic
+    DevShapes sh;
+    int* ctr;                       // device counters
+    // config
+    float gravityAcc[3];
+    float cbt;
+    float deactTime;
+    int disableDeact;
+    int numIter;
+    float erp, warm, slop;
+    int solverMode;
+};
+
+JBD jbd::Xf load_xf(const DevWorld& w, int i) {
+    float4 a = w.xr0[i], b = w.xr1[i], c = w.xr2[i];
+    jbd::Xf t;
+    t.b.r[0] = jbd::mk(a.x, a.y, a.z);
+    t.b.r[1] = jbd::mk(b.x, b.y, b.z);
+    t.b.r[2] = jbd::mk(c.x, c.y, c.z);
+    t.o = jbd::mk(a.w, b.w, c.w);
+    return t;
+}
+JBD void store_xf(const DevWorld& w, int i, const jbd::Xf& t) {
+    w.xr0[i] = make_float4(t.b.r[0].x, t.b.r[0].y, t.b.r[0].z, t.o.x);
+    w.xr1[i] = make_float4(t.b.r[1].x, t.b.r[1].y, t.b.r[1].z, t.o.y);
+    w.xr2[i] = make_float4(t.b.r[2].x, t.b.r[2].y, t.b.r[2].z, t.o.z);
+}
+JBD jbd::M load_iw(const DevWorld& w, int i) {
+    jbd::M m;
+    m.r[0] = jbd::mk4(w.iw0[i]);
+    m.r[1] = jbd::mk4(w.iw1[i]);
+    m.r[2] = jbd::mk4(w.iw2[i]);
+    return m;
+}
+JBD bool is_active_state(int a) { return a != ISLAND_SLEEPING && a != DISABLE_SIMULATION; }
+JBD bool is_static_or_kin(int f) { return (f & (CF_STATIC | CF_KINEMATIC)) != 0; }
+JBD bool merges_islands(int f) { return (f & (CF_STATIC | CF_KINEMATIC | CF_NO_CONTACT_RESPONSE)) == 0; }
+JBD int set_activation(int cur, int s) { return (cur != DISABLE_DEACTIVATION && cur != DISABLE_SIMULATION) ? s : cur; }
+
+// ---- launchers (one per translation unit) ------------------------------------------------
+struct BroadphaseScratch;   // world.cu owns the buffers; broadphase.cu reads them
+void launch_apply_gravity(const DevWorld& w, cudaStream_t s);
+void launch_predict(const DevWorld& w, float dt, cudaStream_t s);
+void launch_aabb(const DevWorld& w, cudaStream_t s);
+void launch_integrate(const DevWorld& w, float dt, cudaStream_t s);
+void launch_activation(const DevWorld& w, float dt, cudaStream_t s);
+void launch_clear_forces(const DevWorld& w, cudaStream_t s);
+
+int num_sms();
+
+}  // namespace jbg

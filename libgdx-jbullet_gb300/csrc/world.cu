@@ -1,0 +1,1020 @@
+// Host side of the C ABI (include/jbgpu.h): world creation, body/shape upload, device
+// buffer management and the per-step launch sequence of internalSingleStepSimulation
+// (dynamics/DiscreteDynamicsWorld.java:356-400 of the reference):
+//   predict -> aabbs -> pairs (count | host capacity check | fill, sort, persist)
+//   -> narrowphase (GJK pass, EPA pass) -> islands -> colour + setup + PGS -> integrate
+//   -> activation.
+// All kernels of a world run on the world's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/jbgpu.h"
+#include "broadphase.cuh"
+#include "jbgpu_internal.cuh"
+#include "narrowphase.cuh"
+#include "prims.cuh"
+#include "solver.cuh"
+
+using namespace jbg;
+
+static thread_local std::string g_err;
+static int fail(int code, const std::string& msg) { g_err = msg; return code; }
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return fail(JBGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+namespace {
+
+struct HostShape {
+    int type;
+    float margin;
+    float dims[4];
+    float lmin[4], lmax[4];
+    float plane[4];
+    int hull_off, hull_cnt;
+};
+
+template <class T> static cudaError_t dalloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    return cudaMalloc((void**)p, sizeof(T) * n);
+}
+template <class T> static void dfree(T*& p) { if (p) cudaFree((void*)p); p = nullptr; }
+
+// Grow a device array to n elements keeping the first keep elements.
+template <class T> static cudaError_t dgrow(T** p, size_t oldn, size_t n, size_t keep, cudaStream_t s) {
+    T* q = nullptr;
+    cudaError_t e = dalloc(&q, n);
+    if (e != cudaSuccess) return e;
+    if (*p && keep) e = cudaMemcpyAsync(q, *p, sizeof(T) * std::min(keep, oldn), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    cudaStreamSynchronize(s);
+    if (*p) cudaFree(*p);
+    *p = q;
+    return cudaSuccess;
+}
+
+}  // namespace
+
+struct jbgpu_world {
+    jbgpu_config cfg;
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    float localTime = 1.0f / 60.0f;
+    long long steps = 0;
+    // shapes
+    std::vector<HostShape> shapes;
+    std::vector<float4> hullPts;
+    bool shapesDirty = true;
+    int capShapes = 0, capHull = 0;
+    // bodies
+    int nBodies = 0, capBodies = 0;
+    std::vector<int> hShape, hWorld, hFlags;
+    int nWorlds = 1;
+    bool planesDirty = true;
+    DevWorld dw{};
+    // pairs: two buffers, cur holds the pairs of the last broadphase
+    DevPairs pairs[2]{};
+    int capPairs[2] = {0, 0};
+    int cur = 0;
+    int nPairs = 0;
+    int capRows = 0;          // pair-capacity of the pair-sized work buffers
+    DevRows rows{};
+    BroadphaseBuffers bb;
+    NarrowBuffers nb;
+    SolverBuffers sb;
+    int* hostPinned = nullptr;
+};
+
+namespace {
+
+int num_sms_of(int dev) {
+    int s = 0;
+    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+    return s > 0 ? s : 1;
+}
+
+int alloc_pairs(DevPairs& P, int cap) {
+    CK(dalloc(&P.keys, cap)); CK(dalloc(&P.has, cap)); CK(dalloc(&P.n, cap));
+    CK(dalloc(&P.b0, cap)); CK(dalloc(&P.b1, cap));
+    size_t c4 = (size_t)cap * 4;
+    CK(dalloc(&P.pA, c4)); CK(dalloc(&P.pB, c4)); CK(dalloc(&P.wA, c4)); CK(dalloc(&P.wB, c4));
+    CK(dalloc(&P.nrm, c4)); CK(dalloc(&P.imp, c4)); CK(dalloc(&P.d1, c4)); CK(dalloc(&P.d2, c4));
+    return JBGPU_OK;
+}
+void free_pairs(DevPairs& P) {
+    dfree(P.keys); dfree(P.has); dfree(P.n); dfree(P.b0); dfree(P.b1);
+    dfree(P.pA); dfree(P.pB); dfree(P.wA); dfree(P.wB); dfree(P.nrm); dfree(P.imp); dfree(P.d1); dfree(P.d2);
+}
+
+// Work buffers whose size follows the pair capacity.
+int alloc_pair_work(jbgpu_world* w, int cap) {
+    DevRows& R = w->rows;
+    dfree(R.n_nrm); dfree(R.n_rp1); dfree(R.n_rp2); dfree(R.n_angA); dfree(R.n_angB);
+    dfree(R.f_nrm); dfree(R.f_rp1); dfree(R.f_rp2); dfree(R.f_angA); dfree(R.f_angB);
+    dfree(R.slot_pair); dfree(R.slot_mask);
+    size_t c4 = (size_t)cap * 4, c8 = (size_t)cap * 8;
+    CK(dalloc(&R.n_nrm, c4)); CK(dalloc(&R.n_rp1, c4)); CK(dalloc(&R.n_rp2, c4)); CK(dalloc(&R.n_angA, c4)); CK(dalloc(&R.n_angB, c4));
+    CK(dalloc(&R.f_nrm, c8)); CK(dalloc(&R.f_rp1, c8)); CK(dalloc(&R.f_rp2, c8)); CK(dalloc(&R.f_angA, c8)); CK(dalloc(&R.f_angB, c8));
+    CK(dalloc(&R.slot_pair, cap)); CK(dalloc(&R.slot_mask, cap));
+    SolverBuffers& S = w->sb;
+    dfree(S.flag); dfree(S.candIdx); dfree(S.cand); dfree(S.colourOf); dfree(S.remA); dfree(S.remB);
+    CK(dalloc(&S.flag, cap)); CK(dalloc(&S.candIdx, cap)); CK(dalloc(&S.cand, cap)); CK(dalloc(&S.colourOf, cap));
+    CK(dalloc(&S.remA, cap)); CK(dalloc(&S.remB, cap));
+    if (S.scanScratch) cudaFree(S.scanScratch);
+    CK(cudaMalloc(&S.scanScratch, scan_scratch_bytes(cap)));
+    if (w->nb.queue) cudaFree(w->nb.queue);
+    CK(cudaMalloc(&w->nb.queue, epa_queue_record_bytes() * (size_t)std::max(cap, 1)));
+    dfree(w->bb.partners);
+    CK(dalloc(&w->bb.partners, cap));
+    w->capRows = cap;
+    return JBGPU_OK;
+}
+
+int grow_bodies(jbgpu_world* w, int need) {
+    if (need <= w->capBodies) return JBGPU_OK;
+    int oldc = w->capBodies;
+    int nc = std::max(need, std::max(2 * oldc, w->cfg.initial_body_capacity > 0 ? w->cfg.initial_body_capacity : 1024));
+    cudaStream_t s = w->stream;
+    DevWorld& d = w->dw;
+    size_t keep = (size_t)w->nBodies;
+#define G(ptr) CK(dgrow(&d.ptr, oldc, nc, keep, s))
+    G(xr0); G(xr1); G(xr2); G(linvel); G(angvel); G(iw0); G(iw1); G(iw2); G(iloc); G(force); G(torque); G(gravity);
+    G(amin); G(amax); G(act); G(deact); G(flags); G(shape); G(group); G(mask); G(world); G(friction); G(restitution);
+    G(linSleep); G(angSleep); G(linDamp); G(angDamp); G(island);
+#undef G
+    // per-body work buffers (contents not kept)
+    BroadphaseBuffers& B = w->bb;
+    dfree(B.mkeys); dfree(B.mkeys_alt); dfree(B.sortedBody); dfree(B.vals_alt);
+    dfree(B.bvh.left); dfree(B.bvh.right); dfree(B.bvh.lo); dfree(B.bvh.hi); dfree(B.bvh.parent); dfree(B.bvh.leafParent);
+    dfree(B.bvh.visit); dfree(B.bvh.bmin); dfree(B.bvh.bmax); dfree(B.cnt); dfree(B.off); dfree(B.cursor);
+    CK(dalloc(&B.mkeys, nc)); CK(dalloc(&B.mkeys_alt, nc)); CK(dalloc(&B.sortedBody, nc)); CK(dalloc(&B.vals_alt, nc));
+    CK(dalloc(&B.bvh.left, nc)); CK(dalloc(&B.bvh.right, nc)); CK(dalloc(&B.bvh.lo, nc)); CK(dalloc(&B.bvh.hi, nc));
+    CK(dalloc(&B.bvh.parent, nc)); CK(dalloc(&B.bvh.leafParent, nc)); CK(dalloc(&B.bvh.visit, nc));
+    CK(dalloc(&B.bvh.bmin, nc)); CK(dalloc(&B.bvh.bmax, nc));
+    CK(dalloc(&B.cnt, nc + 1)); CK(dalloc(&B.off, nc + 1)); CK(dalloc(&B.cursor, nc + 1));
+    if (B.sortScratch) cudaFree(B.sortScratch);
+    CK(cudaMalloc(&B.sortScratch, sort_scratch_bytes(nc)));
+    if (B.scanScratch) cudaFree(B.scanScratch);
+    CK(cudaMalloc(&B.scanScratch, scan_scratch_bytes(nc + 1)));
+    SolverBuffers& S = w->sb;
+    dfree(S.parent); dfree(S.keepAwake); dfree(S.inactive); dfree(S.claim);
+    CK(dalloc(&S.parent, nc)); CK(dalloc(&S.keepAwake, nc)); CK(dalloc(&S.inactive, nc)); CK(dalloc(&S.claim, nc));
+    w->capBodies = nc;
+    return JBGPU_OK;
+}
+
+int ensure_pair_capacity(jbgpu_world* w, int buf, int need) {
+    if (need <= w->capPairs[buf] && need <= w->capRows) return JBGPU_OK;
+    int nc = std::max(need + need / 2 + 64, 2 * w->capPairs[buf]);
+    if (need > w->capPairs[buf]) {
+        free_pairs(w->pairs[buf]);
+        int rc = alloc_pairs(w->pairs[buf], nc);
+        if (rc) return rc;
+        w->capPairs[buf] = nc;
+    }
+    if (need > w->capRows) {
+        int rc = alloc_pair_work(w, std::max(nc, w->capRows));
+        if (rc) return rc;
+    }
+    return JBGPU_OK;
+}
+
+int sync_shapes(jbgpu_world* w) {
+    if (!w->shapesDirty) return JBGPU_OK;
+    int ns = (int)w->shapes.size();
+    DevShapes& S = w->dw.sh;
+    if (ns > w->capShapes) {
+        dfree(S.type); dfree(S.margin); dfree(S.dims); dfree(S.laabb_min); dfree(S.laabb_max); dfree(S.plane);
+        dfree(S.hull_off); dfree(S.hull_cnt);
+        int c = std::max(ns, 2 * w->capShapes);
+        CK(dalloc(&S.type, c)); CK(dalloc(&S.margin, c)); CK(dalloc(&S.dims, c)); CK(dalloc(&S.laabb_min, c));
+        CK(dalloc(&S.laabb_max, c)); CK(dalloc(&S.plane, c)); CK(dalloc(&S.hull_off, c)); CK(dalloc(&S.hull_cnt, c));
+        w->capShapes = c;
+    }
+    int nh = (int)w->hullPts.size();
+    if (nh > w->capHull || !S.hull_pts) {
+        dfree(S.hull_pts);
+        int c = std::max(nh, std::max(1, 2 * w->capHull));
+        CK(dalloc(&S.hull_pts, c));
+        w->capHull = c;
+    }
+    std::vector<int> type(ns), off(ns), cnt(ns);
+    std::vector<float> margin(ns);
+    std::vector<float4> dims(ns), lmin(ns), lmax(ns), plane(ns);
+    for (int i = 0; i < ns; i++) {
+        const HostShape& h = w->shapes[i];
+        type[i] = h.type; off[i] = h.hull_off; cnt[i] = h.hull_cnt; margin[i] = h.margin;
+        dims[i] = make_float4(h.dims[0], h.dims[1], h.dims[2], h.dims[3]);
+        lmin[i] = make_float4(h.lmin[0], h.lmin[1], h.lmin[2], 0);
+        lmax[i] = make_float4(h.lmax[0], h.lmax[1], h.lmax[2], 0);
+        plane[i] = make_float4(h.plane[0], h.plane[1], h.plane[2], h.plane[3]);
+    }
+    cudaStream_t s = w->stream;
+    if (ns) {
+        CK(cudaMemcpyAsync(S.type, type.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.hull_off, off.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.hull_cnt, cnt.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.margin, margin.data(), sizeof(float) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.dims, dims.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.laabb_min, lmin.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.laabb_max, lmax.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.plane, plane.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, s));
+    }
+    if (nh) CK(cudaMemcpyAsync(S.hull_pts, w->hullPts.data(), sizeof(float4) * nh, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    w->shapesDirty = false;
+    return JBGPU_OK;
+}
+
+int sync_planes(jbgpu_world* w) {
+    if (!w->planesDirty) return JBGPU_OK;
+    BroadphaseBuffers& B = w->bb;
+    int nw = 1;
+    for (int i = 0; i < w->nBodies; i++) nw = std::max(nw, w->hWorld[i] + 1);
+    std::vector<std::vector<int>> per(nw);
+    int nf = 0, np = 0;
+    for (int i = 0; i < w->nBodies; i++) {
+        if (w->hFlags[i] & CF_PLANE) { per[w->hWorld[i]].push_back(i); np++; }
+        else nf++;
+    }
+    std::vector<int> list, start(nw + 1, 0);
+    for (int k = 0; k < nw; k++) { start[k] = (int)list.size(); list.insert(list.end(), per[k].begin(), per[k].end()); }
+    start[nw] = (int)list.size();
+    dfree(B.planeList); dfree(B.planeStart); dfree(B.wstart); dfree(B.wend); dfree(B.wroot); dfree(B.bounds); dfree(B.total);
+    CK(dalloc(&B.planeList, std::max<size_t>(1, list.size()))); CK(dalloc(&B.planeStart, nw + 1));
+    CK(dalloc(&B.wstart, nw)); CK(dalloc(&B.wend, nw)); CK(dalloc(&B.wroot, nw)); CK(dalloc(&B.bounds, 6)); CK(dalloc(&B.total, 1));
+    if (!list.empty()) CK(cudaMemcpy(B.planeList, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(B.planeStart, start.data(), sizeof(int) * (nw + 1), cudaMemcpyHostToDevice));
+    B.nFinite = nf;
+    B.nPlanes = np;
+    B.nWorlds = nw;
+    int bits = 0;
+    while ((1 << bits) < nw) bits++;
+    B.worldBits = nw > 1 ? bits : 0;
+    w->nWorlds = nw;
+    w->planesDirty = false;
+    return JBGPU_OK;
+}
+
+DevWorld dev_view(jbgpu_world* w) {
+    DevWorld d = w->dw;
+    d.nBodies = w->nBodies;
+    d.nPairs = w->nPairs;
+    return d;
+}
+
+int check_status(jbgpu_world* w) {
+    int st = 0;
+    CK(cudaMemcpyAsync(w->hostPinned, w->dw.ctr + C_STATUS, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    st = *w->hostPinned;
+    if (st & ST_TIMEOUT) return fail(JBGPU_ERR_TIMEOUT, "a bounded device wait gave up");
+    if (st & ST_EPA_POOL) return fail(JBGPU_ERR_EPA_OVERFLOW, "EPA face pool overflow");
+    if (st & ST_CAPACITY) return fail(JBGPU_ERR_CAPACITY, "device capacity exceeded (traversal stack or colours)");
+    return JBGPU_OK;
+}
+
+// ---- stages --------------------------------------------------------------------------------
+int stage_pairs(jbgpu_world* w) {
+    DevWorld d = dev_view(w);
+    cudaStream_t s = w->stream;
+    broadphase_run_count(d, w->bb, s);
+    CK(cudaMemcpyAsync(w->hostPinned, w->bb.total, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    int total = *w->hostPinned;
+    int nxt = w->cur ^ 1;
+    int rc = ensure_pair_capacity(w, nxt, total);
+    if (rc) return rc;
+    broadphase_run_fill(d, w->bb, w->pairs[nxt], w->capRows, s);
+    broadphase_persist(d, w->pairs[nxt], w->pairs[w->cur], total, w->nPairs, s);
+    w->cur = nxt;
+    w->nPairs = total;
+    CK(cudaMemcpyAsync(w->dw.ctr + C_PAIRS, w->bb.total, sizeof(int), cudaMemcpyDeviceToDevice, s));
+    return JBGPU_OK;
+}
+
+int run_stage(jbgpu_world* w, int stage, float dt) {
+    cudaStream_t s = w->stream;
+    DevWorld d = dev_view(w);
+    switch (stage) {
+    case JBGPU_STAGE_APPLY_GRAVITY: launch_apply_gravity(d, s); break;
+    case JBGPU_STAGE_PREDICT: launch_predict(d, dt, s); break;
+    case JBGPU_STAGE_AABB: launch_aabb(d, s); break;
+    case JBGPU_STAGE_PAIRS: { int rc = stage_pairs(w); if (rc) return rc; break; }
+    case JBGPU_STAGE_NARROWPHASE:
+        CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
+        narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s);
+        break;
+    case JBGPU_STAGE_ISLANDS:
+        CK(cudaMemsetAsync(w->dw.ctr + C_ISLANDS, 0, sizeof(int) * 4, s));
+        islands_launch(d, w->pairs[w->cur], w->nPairs, w->sb, s);
+        break;
+    case JBGPU_STAGE_SOLVE:
+        CK(cudaMemsetAsync(w->dw.ctr + C_ROWS, 0, sizeof(int), s));
+        solve_launch(d, w->pairs[w->cur], w->nPairs, w->rows, w->sb, dt, s);
+        break;
+    case JBGPU_STAGE_INTEGRATE: launch_integrate(d, dt, s); break;
+    case JBGPU_STAGE_ACTIVATION: launch_activation(d, dt, s); break;
+    case JBGPU_STAGE_CLEAR_FORCES: launch_clear_forces(d, s); break;
+    default: return fail(JBGPU_ERR_INVALID_ARGUMENT, "unknown stage");
+    }
+    CK(cudaGetLastError());
+    return JBGPU_OK;
+}
+
+int prepare(jbgpu_world* w) {
+    CK(cudaSetDevice(w->device));
+    int rc = sync_shapes(w);
+    if (rc) return rc;
+    return sync_planes(w);
+}
+
+int single_step(jbgpu_world* w, float dt) {
+    static const int order[] = {JBGPU_STAGE_PREDICT, JBGPU_STAGE_AABB, JBGPU_STAGE_PAIRS, JBGPU_STAGE_NARROWPHASE,
+                                JBGPU_STAGE_ISLANDS, JBGPU_STAGE_SOLVE, JBGPU_STAGE_INTEGRATE, JBGPU_STAGE_ACTIVATION};
+    for (int st : order) {
+        int rc = run_stage(w, st, dt);
+        if (rc) return rc;
+    }
+    w->steps++;
+    return JBGPU_OK;
+}
+
+// RigidBody setup arithmetic on the host (dynamics/RigidBody.java:121-164,207-217,301-312):
+// binary32 operations, no contraction (this file's host code is built with -ffp-contract=off).
+struct BodyInit {
+    float invMass, il[3], grav[3], linDamp, angDamp;
+    int flags, group, mask;
+};
+
+}  // namespace
+
+// Kernel: invInertiaTensorWorld and the creation-time proxy aabb (shape aabb without the
+// contact threshold, CollisionWorld.addCollisionObject) for a range of new bodies.
+__global__ void k_init_bodies(DevWorld w, int first, int count);
+
+extern "C" {
+
+const char* jbgpu_version(void) { return "jbgpu 0.1 (sm_103a)"; }
+const char* jbgpu_last_error(void) { return g_err.c_str(); }
+
+void jbgpu_config_default(jbgpu_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->gravity[0] = 0.0f; c->gravity[1] = -10.0f; c->gravity[2] = 0.0f;
+    c->contact_breaking_threshold = 0.02f;
+    c->deactivation_time = 2.0f;
+    c->disable_deactivation = 0;
+    c->num_iterations = 10;
+    c->erp = 0.2f;
+    c->warmstarting_factor = 0.85f;
+    c->linear_slop = 0.0f;
+    c->solver_mode = JBGPU_SOLVER_CACHE_FRIENDLY | JBGPU_SOLVER_USE_WARMSTARTING;
+    c->device = 0;
+    c->initial_body_capacity = 1024;
+    c->pairs_per_body = 16;
+}
+
+int jbgpu_shape_local_inertia(const jbgpu_shape_desc* d, float mass, float out[3]) {
+    if (!d || !out) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null argument");
+    const float margin = 0.04f;
+    switch (d->type) {
+    case JBGPU_SHAPE_BOX: {       // BoxShape: dims = he - margin; calculateLocalInertia uses dims + margin
+        float he[3];
+        for (int k = 0; k < 3; k++) { volatile float dim = d->params[k] * 1.0f - margin; he[k] = dim + margin; }
+        float lx = 2.0f * he[0], ly = 2.0f * he[1], lz = 2.0f * he[2];
+        out[0] = mass / 12.0f * (ly * ly + lz * lz);
+        out[1] = mass / 12.0f * (lx * lx + lz * lz);
+        out[2] = mass / 12.0f * (lx * lx + ly * ly);
+        return JBGPU_OK;
+    }
+    case JBGPU_SHAPE_SPHERE: {
+        float r = d->params[0];
+        float e = 0.4f * mass * r * r;
+        out[0] = out[1] = out[2] = e;
+        return JBGPU_OK;
+    }
+    case JBGPU_SHAPE_CAPSULE: {
+        float r = d->params[0], hh = 0.5f * d->params[1];
+        float he[3] = {r, r + hh, r};
+        float lx = 2.0f * (he[0] + margin), ly = 2.0f * (he[1] + margin), lz = 2.0f * (he[2] + margin);
+        float x2 = lx * lx, y2 = ly * ly, z2 = lz * lz, sm = mass * 0.08333333f;
+        out[0] = sm * (y2 + z2); out[1] = sm * (x2 + z2); out[2] = sm * (x2 + y2);
+        return JBGPU_OK;
+    }
+    case JBGPU_SHAPE_CONVEX_HULL: {
+        if (!d->points || d->num_points <= 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "hull without points");
+        float mx[3], mn[3];
+        for (int i = 0; i < 3; i++) {
+            float bp = -1e30f, bm = -1e30f, vp = 0, vm = 0;
+            for (int k = 0; k < d->num_points; k++) {
+                float x = d->points[3 * k + i];
+                if (x > bp) { bp = x; vp = x; }
+                if (-x > bm) { bm = -x; vm = x; }
+            }
+            mx[i] = vp + margin;
+            mn[i] = vm - margin;
+        }
+        float lhe[3], lc[3], amin[3], amax[3], he[3];
+        for (int i = 0; i < 3; i++) {
+            lhe[i] = (mx[i] - mn[i]) * 0.5f + margin;
+            lc[i] = (mx[i] + mn[i]) * 0.5f;
+            amin[i] = lc[i] - lhe[i];
+            amax[i] = lc[i] + lhe[i];
+            he[i] = (amax[i] - amin[i]) * 0.5f;
+        }
+        float lx = 2.0f * (he[0] + margin), ly = 2.0f * (he[1] + margin), lz = 2.0f * (he[2] + margin);
+        float x2 = lx * lx, y2 = ly * ly, z2 = lz * lz, sm = mass * 0.08333333f;
+        out[0] = (y2 + z2) * sm; out[1] = (x2 + z2) * sm; out[2] = (x2 + y2) * sm;
+        return JBGPU_OK;
+    }
+    case JBGPU_SHAPE_STATIC_PLANE:
+        out[0] = out[1] = out[2] = 0.0f;
+        return JBGPU_OK;
+    }
+    return fail(JBGPU_ERR_INVALID_ARGUMENT, "unknown shape type");
+}
+
+int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
+    if (!out) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null out");
+    *out = nullptr;
+    jbgpu_config c;
+    if (cfg) c = *cfg; else jbgpu_config_default(&c);
+    if (c.solver_mode & JBGPU_SOLVER_RANDMIZE_ORDER)
+        return fail(JBGPU_ERR_UNSUPPORTED, "SOLVER_RANDMIZE_ORDER: the solver order is the colour order");
+    if (!(c.solver_mode & JBGPU_SOLVER_CACHE_FRIENDLY))
+        return fail(JBGPU_ERR_UNSUPPORTED, "only the cache-friendly solver path is implemented");
+    if (c.num_iterations < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "num_iterations < 0");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(JBGPU_ERR_NO_DEVICE, "no CUDA device");
+    if (c.device < 0 || c.device >= ndev) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad device ordinal");
+    jbgpu_world* w = new jbgpu_world();
+    w->cfg = c;
+    w->device = c.device;
+    if (cudaSetDevice(w->device) != cudaSuccess) { delete w; return fail(JBGPU_ERR_CUDA, "cudaSetDevice"); }
+    w->sms = num_sms_of(w->device);
+    if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) { delete w; return fail(JBGPU_ERR_CUDA, "stream"); }
+    DevWorld& d = w->dw;
+    for (int k = 0; k < 3; k++) d.gravityAcc[k] = c.gravity[k];
+    d.cbt = c.contact_breaking_threshold;
+    d.deactTime = c.deactivation_time;
+    d.disableDeact = c.disable_deactivation;
+    d.numIter = c.num_iterations;
+    d.erp = c.erp;
+    d.warm = c.warmstarting_factor;
+    d.slop = c.linear_slop;
+    d.solverMode = c.solver_mode;
+    int rc;
+    if (cudaMalloc(&d.ctr, sizeof(int) * C_NCTR) != cudaSuccess || cudaMemset(d.ctr, 0, sizeof(int) * C_NCTR) != cudaSuccess ||
+        cudaMallocHost(&w->hostPinned, sizeof(int) * 64) != cudaSuccess) {
+        delete w;
+        return fail(JBGPU_ERR_CUDA, "counter allocation");
+    }
+    SolverBuffers& S = w->sb;
+    if ((rc = [&]() -> int {
+             CK(dalloc(&S.colourCount, MAX_COLOURS + 1)); CK(dalloc(&S.colourFill, MAX_COLOURS + 1));
+             CK(dalloc(&S.colourStart, MAX_COLOURS + 1)); CK(dalloc(&S.nCand, 1)); CK(dalloc(&S.nColours, 1));
+             CK(cudaMemset(S.nCand, 0, sizeof(int))); CK(cudaMemset(S.nColours, 0, sizeof(int)));
+             w->rows.colour_start = S.colourStart;
+             S.coopBlocksColour = solver_coop_blocks(false);
+             S.coopBlocksPgs = solver_coop_blocks(true);
+             NarrowBuffers& N = w->nb;
+             N.slots = w->sms * 96;
+             size_t fs = (size_t)N.slots * 1024, ms = (size_t)N.slots * 288, ss = (size_t)N.slots * 136, st = (size_t)N.slots * 2048;
+             CK(dalloc(&N.fN, fs)); CK(dalloc(&N.fV, fs)); CK(dalloc(&N.fF, fs)); CK(dalloc(&N.fE, fs));
+             CK(dalloc(&N.mW, ms)); CK(dalloc(&N.mR, ms)); CK(dalloc(&N.seen, ss)); CK(dalloc(&N.stack, st));
+             CK(dalloc(&N.queueCount, 1));
+             return grow_bodies(w, std::max(1, c.initial_body_capacity));
+         }()) != JBGPU_OK) {
+        jbgpu_world_destroy(w);
+        return rc;
+    }
+    *out = w;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_destroy(jbgpu_world* w) {
+    if (!w) return JBGPU_OK;
+    cudaSetDevice(w->device);
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    DevWorld& d = w->dw;
+    dfree(d.xr0); dfree(d.xr1); dfree(d.xr2); dfree(d.linvel); dfree(d.angvel); dfree(d.iw0); dfree(d.iw1); dfree(d.iw2);
+    dfree(d.iloc); dfree(d.force); dfree(d.torque); dfree(d.gravity); dfree(d.amin); dfree(d.amax); dfree(d.act);
+    dfree(d.deact); dfree(d.flags); dfree(d.shape); dfree(d.group); dfree(d.mask); dfree(d.world); dfree(d.friction);
+    dfree(d.restitution); dfree(d.linSleep); dfree(d.angSleep); dfree(d.linDamp); dfree(d.angDamp); dfree(d.island);
+    dfree(d.ctr);
+    DevShapes& S = d.sh;
+    dfree(S.type); dfree(S.margin); dfree(S.dims); dfree(S.laabb_min); dfree(S.laabb_max); dfree(S.plane);
+    dfree(S.hull_off); dfree(S.hull_cnt); dfree(S.hull_pts);
+    free_pairs(w->pairs[0]);
+    free_pairs(w->pairs[1]);
+    DevRows& R = w->rows;
+    dfree(R.n_nrm); dfree(R.n_rp1); dfree(R.n_rp2); dfree(R.n_angA); dfree(R.n_angB);
+    dfree(R.f_nrm); dfree(R.f_rp1); dfree(R.f_rp2); dfree(R.f_angA); dfree(R.f_angB);
+    dfree(R.slot_pair); dfree(R.slot_mask);
+    BroadphaseBuffers& B = w->bb;
+    dfree(B.bounds); dfree(B.mkeys); dfree(B.mkeys_alt); dfree(B.sortedBody); dfree(B.vals_alt);
+    if (B.sortScratch) cudaFree(B.sortScratch);
+    if (B.scanScratch) cudaFree(B.scanScratch);
+    dfree(B.bvh.left); dfree(B.bvh.right); dfree(B.bvh.lo); dfree(B.bvh.hi); dfree(B.bvh.parent); dfree(B.bvh.leafParent);
+    dfree(B.bvh.visit); dfree(B.bvh.bmin); dfree(B.bvh.bmax); dfree(B.wstart); dfree(B.wend); dfree(B.wroot);
+    dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.cursor); dfree(B.total); dfree(B.partners);
+    NarrowBuffers& N = w->nb;
+    if (N.queue) cudaFree(N.queue);
+    dfree(N.queueCount); dfree(N.fN); dfree(N.fV); dfree(N.fF); dfree(N.fE); dfree(N.mW); dfree(N.mR); dfree(N.seen); dfree(N.stack);
+    SolverBuffers& V = w->sb;
+    dfree(V.parent); dfree(V.keepAwake); dfree(V.inactive); dfree(V.flag); dfree(V.candIdx); dfree(V.cand); dfree(V.colourOf);
+    dfree(V.remA); dfree(V.remB); dfree(V.claim); dfree(V.colourCount); dfree(V.colourFill); dfree(V.colourStart);
+    dfree(V.nCand); dfree(V.nColours);
+    if (V.scanScratch) cudaFree(V.scanScratch);
+    if (w->hostPinned) cudaFreeHost(w->hostPinned);
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_add_shapes(jbgpu_world* w, const jbgpu_shape_desc* shapes, int32_t n, int32_t* ids) {
+    if (!w || (!shapes && n > 0) || n < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
+    for (int i = 0; i < n; i++) {
+        const jbgpu_shape_desc& d = shapes[i];
+        HostShape h;
+        std::memset(&h, 0, sizeof(h));
+        h.type = d.type;
+        h.margin = 0.04f;
+        h.hull_off = 0;
+        h.hull_cnt = 0;
+        switch (d.type) {
+        case JBGPU_SHAPE_BOX:       // BoxShape: implicit dims = halfExtents * scaling - margin
+            for (int k = 0; k < 3; k++) { volatile float v = d.params[k] * 1.0f; h.dims[k] = v - 0.04f; }
+            break;
+        case JBGPU_SHAPE_SPHERE:    // SphereShape: radius in dims.x, margin == radius
+            h.dims[0] = d.params[0];
+            h.margin = d.params[0];
+            break;
+        case JBGPU_SHAPE_CAPSULE:   // CapsuleShape(radius, height), up axis y
+            h.dims[0] = d.params[0]; h.dims[1] = 0.5f * d.params[1]; h.dims[2] = d.params[0]; h.dims[3] = 1.0f;
+            break;
+        case JBGPU_SHAPE_CONVEX_HULL: {
+            if (!d.points || d.num_points <= 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "hull without points");
+            h.hull_off = (int)w->hullPts.size();
+            h.hull_cnt = d.num_points;
+            for (int k = 0; k < d.num_points; k++)
+                w->hullPts.push_back(make_float4(d.points[3 * k], d.points[3 * k + 1], d.points[3 * k + 2], 0.0f));
+            for (int a = 0; a < 3; a++) {   // PolyhedralConvexShape.recalcLocalAabb: strict > argmax
+                float bp = -1e30f, bm = -1e30f, vp = 0.0f, vm = 0.0f;
+                for (int k = 0; k < d.num_points; k++) {
+                    float x = d.points[3 * k + a];
+                    if (x > bp) { bp = x; vp = x; }
+                    if (-x > bm) { bm = -x; vm = x; }
+                }
+                h.lmax[a] = vp + 0.04f;
+                h.lmin[a] = vm - 0.04f;
+            }
+            break;
+        }
+        case JBGPU_SHAPE_STATIC_PLANE: {   // normal.nor() (libGDX: skipped when len2 is 0 or 1)
+            float x = d.params[0], y = d.params[1], z = d.params[2];
+            float l2 = x * x + y * y + z * z;
+            if (!(l2 == 0.0f || l2 == 1.0f)) {
+                float s = 1.0f / std::sqrt(l2);
+                x = x * s; y = y * s; z = z * s;
+            }
+            h.plane[0] = x; h.plane[1] = y; h.plane[2] = z; h.plane[3] = d.params[3];
+            break;
+        }
+        default:
+            return fail(JBGPU_ERR_UNSUPPORTED, "shape type not on this path");
+        }
+        if (ids) ids[i] = (int)w->shapes.size();
+        w->shapes.push_back(h);
+    }
+    w->shapesDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_add_shape(jbgpu_world* w, const jbgpu_shape_desc* s, int32_t* id) { return jbgpu_world_add_shapes(w, s, 1, id); }
+
+int jbgpu_world_num_bodies(const jbgpu_world* w, int32_t* n) {
+    if (!w || !n) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    *n = w->nBodies;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, int32_t* uids) {
+    if (!w || (!b && n > 0) || n < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (n == 0) return JBGPU_OK;
+    CK(cudaSetDevice(w->device));
+    for (int i = 0; i < n; i++) {
+        if (b[i].shape < 0 || b[i].shape >= (int)w->shapes.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad shape id");
+        if (w->shapes[b[i].shape].type == JBGPU_SHAPE_STATIC_PLANE && b[i].mass != 0.0f)
+            return fail(JBGPU_ERR_INVALID_ARGUMENT, "a static plane must have mass 0");
+        if (b[i].world < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "negative world index");
+    }
+    int rc = grow_bodies(w, w->nBodies + n);
+    if (rc) return rc;
+    rc = sync_shapes(w);
+    if (rc) return rc;
+    std::vector<float4> xr0(n), xr1(n), xr2(n), lv(n), av(n), iloc(n), grav(n), zero(n, make_float4(0, 0, 0, 0));
+    std::vector<int> act(n, JBGPU_ACTIVE_TAG), flags(n), shape(n), group(n), mask(n), world(n);
+    std::vector<float> deact(n, 0.0f), fr(n), re(n), ls(n), as(n), ld(n), ad(n);
+    for (int i = 0; i < n; i++) {
+        const jbgpu_body_desc& d = b[i];
+        const float* t = d.transform;
+        xr0[i] = make_float4(t[0], t[1], t[2], t[9]);
+        xr1[i] = make_float4(t[3], t[4], t[5], t[10]);
+        xr2[i] = make_float4(t[6], t[7], t[8], t[11]);
+        lv[i] = make_float4(d.linear_velocity[0], d.linear_velocity[1], d.linear_velocity[2], 0);
+        av[i] = make_float4(d.angular_velocity[0], d.angular_velocity[1], d.angular_velocity[2], 0);
+        int f = 0;
+        float im;
+        if (d.mass == 0.0f) { f |= CF_STATIC; im = 0.0f; } else im = 1.0f / d.mass;
+        if (w->shapes[d.shape].type == JBGPU_SHAPE_STATIC_PLANE) f |= CF_PLANE;
+        float il[3];
+        for (int k = 0; k < 3; k++) il[k] = d.local_inertia[k] != 0.0f ? 1.0f / d.local_inertia[k] : 0.0f;
+        iloc[i] = make_float4(il[0], il[1], il[2], im);
+        float g[3] = {0, 0, 0};
+        if (!(f & (CF_STATIC | CF_KINEMATIC)) && im != 0.0f) {
+            float inv = 1.0f / im;
+            for (int k = 0; k < 3; k++) g[k] = w->cfg.gravity[k] * inv;
+        }
+        grav[i] = make_float4(g[0], g[1], g[2], 0);
+        bool dynamic = !(f & (CF_STATIC | CF_KINEMATIC));
+        group[i] = d.collision_group != -1 ? (int)(short)d.collision_group : (dynamic ? 1 : 2);
+        mask[i] = d.collision_mask != -1 ? (int)(short)d.collision_mask : (dynamic ? -1 : (int)(short)(-1 ^ 2));
+        flags[i] = f;
+        shape[i] = d.shape;
+        world[i] = d.world;
+        fr[i] = d.friction; re[i] = d.restitution; ls[i] = d.linear_sleeping_threshold; as[i] = d.angular_sleeping_threshold;
+        auto clamp01 = [](float x) { return x < 0.0f ? 0.0f : (1.0f < x ? 1.0f : x); };
+        ld[i] = clamp01(d.linear_damping);
+        ad[i] = clamp01(d.angular_damping);
+        w->hShape.push_back(d.shape);
+        w->hWorld.push_back(d.world);
+        w->hFlags.push_back(f);
+        if (uids) uids[i] = w->nBodies + i + 1;
+    }
+    int o = w->nBodies;
+    cudaStream_t s = w->stream;
+    DevWorld& D = w->dw;
+#define UP(dst, src, T) CK(cudaMemcpyAsync(D.dst + o, src.data(), sizeof(T) * n, cudaMemcpyHostToDevice, s))
+    UP(xr0, xr0, float4); UP(xr1, xr1, float4); UP(xr2, xr2, float4); UP(linvel, lv, float4); UP(angvel, av, float4);
+    UP(iloc, iloc, float4); UP(gravity, grav, float4); UP(force, zero, float4); UP(torque, zero, float4);
+    UP(act, act, int); UP(deact, deact, float); UP(flags, flags, int); UP(shape, shape, int); UP(group, group, int);
+    UP(mask, mask, int); UP(world, world, int); UP(friction, fr, float); UP(restitution, re, float);
+    UP(linSleep, ls, float); UP(angSleep, as, float); UP(linDamp, ld, float); UP(angDamp, ad, float);
+#undef UP
+    w->nBodies += n;
+    DevWorld dv = dev_view(w);
+    k_init_bodies<<<(n + 255) / 256, 256, 0, s>>>(dv, o, n);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    w->planesDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_step(jbgpu_world* w, float dt, int32_t substeps) {
+    if (!w || substeps < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
+    int rc = prepare(w);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), w->stream));
+    if ((rc = run_stage(w, JBGPU_STAGE_APPLY_GRAVITY, dt))) return rc;
+    for (int i = 0; i < substeps; i++)
+        if ((rc = single_step(w, dt))) return rc;
+    if ((rc = run_stage(w, JBGPU_STAGE_CLEAR_FORCES, dt))) return rc;
+    return check_status(w);
+}
+
+int jbgpu_world_step_simulation(jbgpu_world* w, float timeStep, int32_t maxSubSteps, float fixedTimeStep, int32_t* numOut) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    int num = 0;
+    if (maxSubSteps != 0) {
+        w->localTime += timeStep;
+        if (w->localTime >= fixedTimeStep) {
+            num = (int)(w->localTime / fixedTimeStep);
+            w->localTime -= num * fixedTimeStep;
+        }
+    } else {
+        fixedTimeStep = timeStep;
+        w->localTime = timeStep;
+        if (std::fabs(timeStep) < 1.19209290e-07f) { num = 0; maxSubSteps = 0; }
+        else { num = 1; maxSubSteps = 1; }
+    }
+    if (numOut) *numOut = num;
+    int rc = prepare(w);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), w->stream));
+    if (num != 0) {
+        if ((rc = run_stage(w, JBGPU_STAGE_APPLY_GRAVITY, fixedTimeStep))) return rc;
+        int clamped = num > maxSubSteps ? maxSubSteps : num;
+        for (int i = 0; i < clamped; i++)
+            if ((rc = single_step(w, fixedTimeStep))) return rc;
+    }
+    if ((rc = run_stage(w, JBGPU_STAGE_CLEAR_FORCES, fixedTimeStep))) return rc;
+    return check_status(w);
+}
+
+int jbgpu_world_stage(jbgpu_world* w, int32_t stage, float dt) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    int rc = prepare(w);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), w->stream));
+    if ((rc = run_stage(w, stage, dt))) return rc;
+    return check_status(w);
+}
+
+int jbgpu_world_synchronize(jbgpu_world* w) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    CK(cudaStreamSynchronize(w->stream));
+    return JBGPU_OK;
+}
+
+int jbgpu_world_get_state(jbgpu_world* w, jbgpu_state* st) {
+    if (!w || !st) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    CK(cudaSetDevice(w->device));
+    int n = w->nBodies;
+    st->n_bodies = n;
+    if (n == 0) return JBGPU_OK;
+    cudaStream_t s = w->stream;
+    DevWorld& D = w->dw;
+    std::vector<float4> a(n), b(n), c(n);
+    auto get4 = [&](float4* src, std::vector<float4>& dst) -> int { CK(cudaMemcpyAsync(dst.data(), src, sizeof(float4) * n, cudaMemcpyDeviceToHost, s)); return 0; };
+    int rc;
+    if (st->transform) {
+        if ((rc = get4(D.xr0, a)) || (rc = get4(D.xr1, b)) || (rc = get4(D.xr2, c))) return rc;
+        CK(cudaStreamSynchronize(s));
+        for (int i = 0; i < n; i++) {
+            float* t = st->transform + 12 * i;
+            t[0] = a[i].x; t[1] = a[i].y; t[2] = a[i].z; t[3] = b[i].x; t[4] = b[i].y; t[5] = b[i].z;
+            t[6] = c[i].x; t[7] = c[i].y; t[8] = c[i].z; t[9] = a[i].w; t[10] = b[i].w; t[11] = c[i].w;
+        }
+    }
+    if (st->inv_inertia_world) {
+        if ((rc = get4(D.iw0, a)) || (rc = get4(D.iw1, b)) || (rc = get4(D.iw2, c))) return rc;
+        CK(cudaStreamSynchronize(s));
+        for (int i = 0; i < n; i++) {
+            float* t = st->inv_inertia_world + 9 * i;
+            t[0] = a[i].x; t[1] = a[i].y; t[2] = a[i].z; t[3] = b[i].x; t[4] = b[i].y; t[5] = b[i].z;
+            t[6] = c[i].x; t[7] = c[i].y; t[8] = c[i].z;
+        }
+    }
+    auto get3 = [&](float4* src, float* dst) -> int {
+        if (!dst) return 0;
+        CK(cudaMemcpyAsync(a.data(), src, sizeof(float4) * n, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        for (int i = 0; i < n; i++) { dst[3 * i] = a[i].x; dst[3 * i + 1] = a[i].y; dst[3 * i + 2] = a[i].z; }
+        return 0;
+    };
+    if ((rc = get3(D.linvel, st->linear_velocity)) || (rc = get3(D.angvel, st->angular_velocity)) ||
+        (rc = get3(D.force, st->total_force)) || (rc = get3(D.torque, st->total_torque)))
+        return rc;
+    if (st->aabb) {
+        if ((rc = get4(D.amin, a)) || (rc = get4(D.amax, b))) return rc;
+        CK(cudaStreamSynchronize(s));
+        for (int i = 0; i < n; i++) {
+            float* t = st->aabb + 6 * i;
+            t[0] = a[i].x; t[1] = a[i].y; t[2] = a[i].z; t[3] = b[i].x; t[4] = b[i].y; t[5] = b[i].z;
+        }
+    }
+    if (st->activation_state) CK(cudaMemcpyAsync(st->activation_state, D.act, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+    if (st->deactivation_time) CK(cudaMemcpyAsync(st->deactivation_time, D.deact, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
+    if (st->island_tag) CK(cudaMemcpyAsync(st->island_tag, D.island, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_state(jbgpu_world* w, const jbgpu_state* st) {
+    if (!w || !st) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    if (st->n_bodies != w->nBodies) return fail(JBGPU_ERR_INVALID_ARGUMENT, "body count mismatch");
+    CK(cudaSetDevice(w->device));
+    int n = w->nBodies;
+    if (n == 0) return JBGPU_OK;
+    cudaStream_t s = w->stream;
+    DevWorld& D = w->dw;
+    std::vector<float4> a(n), b(n), c(n);
+    if (st->transform) {
+        for (int i = 0; i < n; i++) {
+            const float* t = st->transform + 12 * i;
+            a[i] = make_float4(t[0], t[1], t[2], t[9]); b[i] = make_float4(t[3], t[4], t[5], t[10]); c[i] = make_float4(t[6], t[7], t[8], t[11]);
+        }
+        CK(cudaMemcpyAsync(D.xr0, a.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.xr1, b.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.xr2, c.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    if (st->inv_inertia_world) {
+        for (int i = 0; i < n; i++) {
+            const float* t = st->inv_inertia_world + 9 * i;
+            a[i] = make_float4(t[0], t[1], t[2], 0); b[i] = make_float4(t[3], t[4], t[5], 0); c[i] = make_float4(t[6], t[7], t[8], 0);
+        }
+        CK(cudaMemcpyAsync(D.iw0, a.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.iw1, b.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.iw2, c.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    auto put3 = [&](float4* dst, const float* src) -> int {
+        if (!src) return 0;
+        for (int i = 0; i < n; i++) a[i] = make_float4(src[3 * i], src[3 * i + 1], src[3 * i + 2], 0);
+        CK(cudaMemcpyAsync(dst, a.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaStreamSynchronize(s));
+        return 0;
+    };
+    int rc;
+    if ((rc = put3(D.linvel, st->linear_velocity)) || (rc = put3(D.angvel, st->angular_velocity)) ||
+        (rc = put3(D.force, st->total_force)) || (rc = put3(D.torque, st->total_torque)))
+        return rc;
+    if (st->aabb) {
+        for (int i = 0; i < n; i++) {
+            const float* t = st->aabb + 6 * i;
+            a[i] = make_float4(t[0], t[1], t[2], 0); b[i] = make_float4(t[3], t[4], t[5], 0);
+        }
+        CK(cudaMemcpyAsync(D.amin, a.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(D.amax, b.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    }
+    if (st->activation_state) CK(cudaMemcpyAsync(D.act, st->activation_state, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    if (st->deactivation_time) CK(cudaMemcpyAsync(D.deact, st->deactivation_time, sizeof(float) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    return JBGPU_OK;
+}
+
+int jbgpu_world_get_pairs(jbgpu_world* w, uint64_t* keys, int32_t cap, int32_t* n) {
+    if (!w || !n) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    *n = w->nPairs;
+    if (w->nPairs > cap) return fail(JBGPU_ERR_CAPACITY, "caller buffer too small");
+    if (w->nPairs && keys) {
+        CK(cudaMemcpyAsync(keys, w->pairs[w->cur].keys, sizeof(uint64_t) * w->nPairs, cudaMemcpyDeviceToHost, w->stream));
+        CK(cudaStreamSynchronize(w->stream));
+    }
+    return JBGPU_OK;
+}
+
+int jbgpu_world_get_manifolds(jbgpu_world* w, jbgpu_manifolds* m) {
+    if (!w || !m) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    int np = w->nPairs;
+    m->n_pairs = np;
+    if (np > m->capacity) return fail(JBGPU_ERR_CAPACITY, "caller buffer too small");
+    if (np == 0) return JBGPU_OK;
+    cudaStream_t s = w->stream;
+    DevPairs& P = w->pairs[w->cur];
+    std::vector<int> has(np), cnt(np);
+    std::vector<float4> f[8];
+    float4* src[8] = {P.pA, P.pB, P.wA, P.wB, P.nrm, P.imp, P.d1, P.d2};
+    if (m->keys) CK(cudaMemcpyAsync(m->keys, P.keys, sizeof(uint64_t) * np, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(has.data(), P.has, sizeof(int) * np, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(cnt.data(), P.n, sizeof(int) * np, cudaMemcpyDeviceToHost, s));
+    if (m->points)
+        for (int k = 0; k < 8; k++) {
+            f[k].resize((size_t)np * 4);
+            CK(cudaMemcpyAsync(f[k].data(), src[k], sizeof(float4) * np * 4, cudaMemcpyDeviceToHost, s));
+        }
+    CK(cudaStreamSynchronize(s));
+    for (int i = 0; i < np; i++) {
+        int nn = has[i] ? cnt[i] : 0;
+        if (m->flags) m->flags[i] = has[i] ? 1 : 0;
+        if (m->num_points) m->num_points[i] = nn;
+        if (!m->points) continue;
+        for (int j = 0; j < 4; j++) {
+            float* o = m->points + ((size_t)i * 4 + j) * JBGPU_POINT_FLOATS;
+            std::memset(o, 0, sizeof(float) * JBGPU_POINT_FLOATS);
+            if (j >= nn) continue;
+            size_t k = (size_t)i * 4 + j;
+            float4 pA = f[0][k], pB = f[1][k], wA = f[2][k], wB = f[3][k], nr = f[4][k], im = f[5][k], d1 = f[6][k], d2 = f[7][k];
+            o[0] = pA.x; o[1] = pA.y; o[2] = pA.z; o[3] = pB.x; o[4] = pB.y; o[5] = pB.z;
+            o[6] = wA.x; o[7] = wA.y; o[8] = wA.z; o[9] = wB.x; o[10] = wB.y; o[11] = wB.z;
+            o[12] = nr.x; o[13] = nr.y; o[14] = nr.z; o[15] = pA.w; o[16] = wA.w; o[17] = wB.w;
+            o[18] = nr.w; o[19] = im.x; o[20] = im.y; o[21] = im.z;
+            int life;
+            std::memcpy(&life, &pB.w, 4);
+            o[22] = (float)life;
+            o[23] = d1.x; o[24] = d1.y; o[25] = d1.z; o[26] = d2.x; o[27] = d2.y; o[28] = d2.z;
+        }
+    }
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_manifolds(jbgpu_world* w, const jbgpu_manifolds* m) {
+    if (!w || !m || m->n_pairs < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    CK(cudaSetDevice(w->device));
+    int rc = prepare(w);
+    if (rc) return rc;
+    int np = m->n_pairs;
+    if ((rc = ensure_pair_capacity(w, w->cur, std::max(np, 1)))) return rc;
+    cudaStream_t s = w->stream;
+    DevPairs& P = w->pairs[w->cur];
+    std::vector<int> has(np), cnt(np), b0(np), b1(np);
+    std::vector<float4> f[8];
+    for (int k = 0; k < 8; k++) f[k].assign((size_t)np * 4, make_float4(0, 0, 0, 0));
+    for (int i = 0; i < np; i++) {
+        uint64_t key = m->keys[i];
+        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+        if (a < 0 || b < 0 || a >= w->nBodies || b >= w->nBodies || a == b) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad pair key");
+        if (i > 0 && m->keys[i - 1] >= key) return fail(JBGPU_ERR_INVALID_ARGUMENT, "keys not strictly ascending");
+        bool bPlane = (w->hFlags[b] & CF_PLANE) != 0;
+        b0[i] = bPlane ? a : std::min(a, b);
+        b1[i] = bPlane ? b : std::max(a, b);
+        has[i] = (m->flags[i] & 1) ? 1 : 0;
+        cnt[i] = has[i] ? m->num_points[i] : 0;
+        if (cnt[i] < 0 || cnt[i] > 4) return fail(JBGPU_ERR_INVALID_ARGUMENT, "num_points out of range");
+        for (int j = 0; j < cnt[i]; j++) {
+            const float* o = m->points + ((size_t)i * 4 + j) * JBGPU_POINT_FLOATS;
+            size_t k = (size_t)i * 4 + j;
+            int life = (int)o[22];
+            float lifef;
+            std::memcpy(&lifef, &life, 4);
+            f[0][k] = make_float4(o[0], o[1], o[2], o[15]);
+            f[1][k] = make_float4(o[3], o[4], o[5], lifef);
+            f[2][k] = make_float4(o[6], o[7], o[8], o[16]);
+            f[3][k] = make_float4(o[9], o[10], o[11], o[17]);
+            f[4][k] = make_float4(o[12], o[13], o[14], o[18]);
+            f[5][k] = make_float4(o[19], o[20], o[21], 0.0f);
+            f[6][k] = make_float4(o[23], o[24], o[25], 0.0f);
+            f[7][k] = make_float4(o[26], o[27], o[28], 0.0f);
+        }
+    }
+    if (np) {
+        float4* dst[8] = {P.pA, P.pB, P.wA, P.wB, P.nrm, P.imp, P.d1, P.d2};
+        CK(cudaMemcpyAsync(P.keys, m->keys, sizeof(uint64_t) * np, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(P.has, has.data(), sizeof(int) * np, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(P.n, cnt.data(), sizeof(int) * np, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(P.b0, b0.data(), sizeof(int) * np, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(P.b1, b1.data(), sizeof(int) * np, cudaMemcpyHostToDevice, s));
+        for (int k = 0; k < 8; k++) CK(cudaMemcpyAsync(dst[k], f[k].data(), sizeof(float4) * np * 4, cudaMemcpyHostToDevice, s));
+    }
+    CK(cudaStreamSynchronize(s));
+    w->nPairs = np;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_get_solver_order(jbgpu_world* w, int32_t* out, int32_t cap, int32_t* n) {
+    if (!w || !n) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    cudaStream_t s = w->stream;
+    int nc = 0, ncol = 0;
+    CK(cudaMemcpyAsync(&nc, w->sb.nCand, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&ncol, w->sb.nColours, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *n = nc;
+    if (nc > cap) return fail(JBGPU_ERR_CAPACITY, "caller buffer too small");
+    if (nc == 0 || !out) return JBGPU_OK;
+    std::vector<int> cand(nc), col(nc);
+    CK(cudaMemcpyAsync(cand.data(), w->sb.cand, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(col.data(), w->sb.colourOf, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<std::pair<int, int>> v(nc);
+    for (int k = 0; k < nc; k++) v[k] = std::make_pair(col[k], cand[k]);
+    std::sort(v.begin(), v.end());
+    for (int k = 0; k < nc; k++) out[k] = v[k].second;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_counters(jbgpu_world* w, jbgpu_counters* c) {
+    if (!w || !c) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    int h[C_NCTR];
+    int nc = 0;
+    CK(cudaMemcpyAsync(h, w->dw.ctr, sizeof(int) * C_NCTR, cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaMemcpyAsync(&nc, w->sb.nCand, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    std::memset(c, 0, sizeof(*c));
+    c->steps = w->steps;
+    c->bodies = w->nBodies;
+    c->pairs = w->nPairs;
+    c->manifolds = h[C_MANIFOLDS];
+    c->contacts = h[C_CONTACTS];
+    c->solver_manifolds = nc;
+    c->solver_rows = h[C_ROWS];
+    c->colours = h[C_COLOURS];
+    c->islands = h[C_ISLANDS];
+    c->gjk_calls = h[C_GJK];
+    c->epa_calls = h[C_EPA];
+    c->status_flags = h[C_STATUS];
+    return JBGPU_OK;
+}
+
+}  // extern "C"
+
+// updateInertiaTensor and the creation-time proxy aabb for new bodies.
+#include "shapes.cuh"
+__global__ void k_init_bodies(DevWorld w, int first, int count) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    int i = first + k;
+    using namespace jbd;
+    Xf t = load_xf(w, i);
+    M m1 = scaleM(t.b, mk4(w.iloc[i]));
+    M iw = mulMM(m1, transpose(t.b));
+    w.iw0[i] = f4(iw.r[0], 0.0f);
+    w.iw1[i] = f4(iw.r[1], 0.0f);
+    w.iw2[i] = f4(iw.r[2], 0.0f);
+    V mn, mx;
+    shape_aabb(w.sh, w.shape[i], t, mn, mx);
+    w.amin[i] = f4(mn, 0.0f);
+    w.amax[i] = f4(mx, 0.0f);
+    w.island[i] = -1;
+}

@@ -1,0 +1,173 @@
+"""ctypes binding of libjbgpu.so (include/jbgpu.h).
+
+`GpuWorld` is a thin handle over one `jbgpu_world`: scene upload, stepping, stage-by-stage
+execution for open-loop checks, and state/manifold snapshots in the host layout of
+_abi.StateBuffers / _abi.ManifoldBuffers.  The library is built in-tree (see _build.py);
+loading fails loudly when it is missing: there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi
+from ._build import LIB
+
+_lib = None
+
+
+class JbgpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("jbgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError("libjbgpu.so is not built (run __graft_entry__.build() or jbgpu._build.build())")
+        L = C.CDLL(LIB)
+        P = C.POINTER
+        sigs = {
+            "jbgpu_version": ([], C.c_char_p),
+            "jbgpu_last_error": ([], C.c_char_p),
+            "jbgpu_config_default": ([P(_abi.Config)], None),
+            "jbgpu_shape_local_inertia": ([P(_abi.ShapeDesc), C.c_float, _abi.f32p], C.c_int),
+            "jbgpu_world_create": ([P(_abi.Config), P(C.c_void_p)], C.c_int),
+            "jbgpu_world_destroy": ([C.c_void_p], C.c_int),
+            "jbgpu_world_add_shape": ([C.c_void_p, P(_abi.ShapeDesc), _abi.i32p], C.c_int),
+            "jbgpu_world_add_shapes": ([C.c_void_p, P(_abi.ShapeDesc), C.c_int32, _abi.i32p], C.c_int),
+            "jbgpu_world_add_bodies": ([C.c_void_p, P(_abi.BodyDesc), C.c_int32, _abi.i32p], C.c_int),
+            "jbgpu_world_num_bodies": ([C.c_void_p, _abi.i32p], C.c_int),
+            "jbgpu_world_step_simulation": ([C.c_void_p, C.c_float, C.c_int32, C.c_float, _abi.i32p], C.c_int),
+            "jbgpu_world_step": ([C.c_void_p, C.c_float, C.c_int32], C.c_int),
+            "jbgpu_world_stage": ([C.c_void_p, C.c_int32, C.c_float], C.c_int),
+            "jbgpu_world_synchronize": ([C.c_void_p], C.c_int),
+            "jbgpu_world_get_state": ([C.c_void_p, P(_abi.State)], C.c_int),
+            "jbgpu_world_set_state": ([C.c_void_p, P(_abi.State)], C.c_int),
+            "jbgpu_world_get_pairs": ([C.c_void_p, _abi.u64p, C.c_int32, _abi.i32p], C.c_int),
+            "jbgpu_world_get_manifolds": ([C.c_void_p, P(_abi.Manifolds)], C.c_int),
+            "jbgpu_world_set_manifolds": ([C.c_void_p, P(_abi.Manifolds)], C.c_int),
+            "jbgpu_world_get_solver_order": ([C.c_void_p, _abi.i32p, C.c_int32, _abi.i32p], C.c_int),
+            "jbgpu_world_counters": ([C.c_void_p, P(_abi.Counters)], C.c_int),
+        }
+        for name, (args, res) in sigs.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+EXPORTED = [
+    "jbgpu_version", "jbgpu_last_error", "jbgpu_config_default", "jbgpu_shape_local_inertia", "jbgpu_world_create",
+    "jbgpu_world_destroy", "jbgpu_world_add_shape", "jbgpu_world_add_shapes", "jbgpu_world_add_bodies",
+    "jbgpu_world_num_bodies", "jbgpu_world_step_simulation", "jbgpu_world_step", "jbgpu_world_stage",
+    "jbgpu_world_synchronize", "jbgpu_world_get_state", "jbgpu_world_set_state", "jbgpu_world_get_pairs",
+    "jbgpu_world_get_manifolds", "jbgpu_world_set_manifolds", "jbgpu_world_get_solver_order", "jbgpu_world_counters",
+]
+
+
+def check(rc):
+    if rc != 0:
+        msg = lib().jbgpu_last_error()
+        raise JbgpuError(rc, msg.decode() if msg else "")
+    return rc
+
+
+class GpuWorld:
+    def __init__(self, scene=None, config=None):
+        cfg = config if config is not None else _abi.default_config(**(scene.config if scene else {}))
+        self._cfg = cfg
+        h = C.c_void_p()
+        check(lib().jbgpu_world_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        if scene is not None:
+            self.add_scene(scene)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().jbgpu_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_scene(self, scene):
+        descs = scene.shape_descs()
+        check(lib().jbgpu_world_add_shapes(self.h, descs, len(descs), None))
+        b, ptr = scene.body_descs_ptr()
+        check(lib().jbgpu_world_add_bodies(self.h, ptr, len(b), None))
+
+    @property
+    def n_bodies(self):
+        n = C.c_int32()
+        check(lib().jbgpu_world_num_bodies(self.h, C.byref(n)))
+        return n.value
+
+    def step(self, dt, substeps=1):
+        check(lib().jbgpu_world_step(self.h, dt, substeps))
+
+    def step_simulation(self, time_step, max_sub_steps=1, fixed_time_step=1.0 / 60.0):
+        n = C.c_int32()
+        check(lib().jbgpu_world_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step, C.byref(n)))
+        return n.value
+
+    def stage(self, stage, dt=1.0 / 60.0):
+        check(lib().jbgpu_world_stage(self.h, stage, dt))
+
+    def synchronize(self):
+        check(lib().jbgpu_world_synchronize(self.h))
+
+    def get_state(self):
+        sb = _abi.StateBuffers(self.n_bodies)
+        check(lib().jbgpu_world_get_state(self.h, C.byref(sb.struct)))
+        return sb.copy_arrays()
+
+    def set_state(self, arrays):
+        arrays = {k: v for k, v in arrays.items() if k != "island_tag"}
+        sb = _abi.StateBuffers.from_arrays(arrays)
+        check(lib().jbgpu_world_set_state(self.h, C.byref(sb.struct)))
+
+    def get_pairs(self):
+        n = C.c_int32()
+        lib().jbgpu_world_get_pairs(self.h, None, 0, C.byref(n))
+        keys = np.zeros(max(1, n.value), np.uint64)
+        check(lib().jbgpu_world_get_pairs(self.h, keys.ctypes.data_as(_abi.u64p), len(keys), C.byref(n)))
+        return keys[:n.value]
+
+    def get_manifolds(self):
+        n = C.c_int32()
+        lib().jbgpu_world_get_pairs(self.h, None, 0, C.byref(n))
+        mb = _abi.ManifoldBuffers(max(1, n.value))
+        check(lib().jbgpu_world_get_manifolds(self.h, C.byref(mb.struct)))
+        return mb.view()
+
+    def set_manifolds(self, m):
+        mb = _abi.ManifoldBuffers.from_arrays(m["keys"], m["flags"], m["num_points"], m["points"])
+        check(lib().jbgpu_world_set_manifolds(self.h, C.byref(mb.struct)))
+
+    def solver_order(self):
+        n = C.c_int32()
+        lib().jbgpu_world_get_solver_order(self.h, None, 0, C.byref(n))
+        out = np.zeros(max(1, n.value), np.int32)
+        check(lib().jbgpu_world_get_solver_order(self.h, out.ctypes.data_as(_abi.i32p), len(out), C.byref(n)))
+        return out[:n.value]
+
+    def counters(self):
+        c = _abi.Counters()
+        check(lib().jbgpu_world_counters(self.h, C.byref(c)))
+        return c.as_dict()
+
+
+def shape_local_inertia(shape_dict, mass):
+    from .scenes import Scene
+    sc = Scene("one", 0, 0, {}, [shape_dict], np.zeros(0))
+    d = sc.shape_descs()
+    out = np.zeros(3, np.float32)
+    check(lib().jbgpu_shape_local_inertia(C.byref(d[0]), mass, out.ctypes.data_as(_abi.f32p)))
+    return out

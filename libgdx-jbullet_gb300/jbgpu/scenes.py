@@ -1,0 +1,356 @@
+"""Seeded synthetic scenes for the rigid-body step.
+
+The reference ships no benchmark scene or dataset; these generators build the five
+workloads the step is measured on (boxes on a plane; 100k mixed spheres/boxes/capsules;
+20k convex hulls; 4,096 batched worlds; pyramids for the warm-start study) from a PCG64
+stream, so the same seed yields the same bodies on every machine.
+
+Mass properties follow the reference's CollisionShape.calculateLocalInertia, evaluated in
+binary32 with the reference's operation order (collision/shapes/BoxShape.java:153-167,
+SphereShape.java:72-76, CapsuleShape.java:125-153, PolyhedralConvexShape.java:133-159),
+so that the oracle and the GPU library receive identical inputs.
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi
+
+F = np.float32
+
+BODY_DTYPE = np.dtype([
+    ("mass", "<f4"), ("shape", "<i4"), ("transform", "<f4", (12,)), ("local_inertia", "<f4", (3,)),
+    ("linear_damping", "<f4"), ("angular_damping", "<f4"), ("friction", "<f4"), ("restitution", "<f4"),
+    ("linear_sleeping_threshold", "<f4"), ("angular_sleeping_threshold", "<f4"),
+    ("linear_velocity", "<f4", (3,)), ("angular_velocity", "<f4", (3,)),
+    ("collision_group", "<i4"), ("collision_mask", "<i4"), ("world", "<i4"),
+])
+assert BODY_DTYPE.itemsize == 128
+
+
+@dataclass
+class Scene:
+    name: str
+    dt: float
+    steps: int
+    config: dict
+    shapes: list                      # dicts: type, params (4 floats), points (n,3) float32 or None
+    bodies: np.ndarray                # BODY_DTYPE records, insertion order (uid = index + 1)
+    world_of_body: np.ndarray = None  # batched scenes: world index per body
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def n_bodies(self):
+        return len(self.bodies)
+
+    def shape_descs(self):
+        """ctypes array of ShapeDesc (keeps point buffers alive on the returned object)."""
+        arr = (_abi.ShapeDesc * len(self.shapes))()
+        keep = []
+        for i, s in enumerate(self.shapes):
+            arr[i].type = s["type"]
+            arr[i].params[:] = tuple(float(x) for x in s["params"])
+            if s.get("points") is not None:
+                p = np.ascontiguousarray(s["points"], dtype=np.float32)
+                keep.append(p)
+                arr[i].points = p.ctypes.data_as(_abi.f32p)
+                arr[i].num_points = len(p)
+            else:
+                arr[i].points = None
+                arr[i].num_points = 0
+        arr._keep = keep
+        return arr
+
+    def body_descs_ptr(self):
+        b = np.ascontiguousarray(self.bodies)
+        return b, b.ctypes.data_as(_abi.C.POINTER(_abi.BodyDesc))
+
+
+# ---- binary32 mass properties (reference operation order) --------------------------------
+def box_inertia(mass, half_extents, margin=F(0.04)):
+    he = np.asarray(half_extents, F)
+    dims = he * F(1) - margin                      # BoxShape ctor: implicit dims
+    hm = dims + margin                             # getHalfExtentsWithMargin
+    lx, ly, lz = F(2) * hm[0], F(2) * hm[1], F(2) * hm[2]
+    m12 = F(mass) / F(12)
+    return np.array([m12 * (ly * ly + lz * lz), m12 * (lx * lx + lz * lz), m12 * (lx * lx + ly * ly)], F)
+
+
+def sphere_inertia(mass, r):
+    e = F(0.4) * F(mass) * F(r) * F(r)
+    return np.array([e, e, e], F)
+
+
+def capsule_inertia(mass, r, height):
+    r = F(r)
+    hh = F(0.5) * F(height)
+    he = np.array([r, r + hh, r], F)
+    margin = F(0.04)
+    lx, ly, lz = F(2) * (he[0] + margin), F(2) * (he[1] + margin), F(2) * (he[2] + margin)
+    x2, y2, z2 = lx * lx, ly * ly, lz * lz
+    sm = F(mass) * F(0.08333333)
+    return np.array([sm * (y2 + z2), sm * (x2 + z2), sm * (x2 + y2)], F)
+
+
+def hull_local_aabb(points, margin=F(0.04)):
+    """PolyhedralConvexShape.recalcLocalAabb (strict > argmax in point order)."""
+    p = np.asarray(points, F)
+    mx = np.empty(3, F)
+    mn = np.empty(3, F)
+    for i in range(3):
+        # dot with a unit axis: x*1 + y*0 + z*0 has the value of the coordinate
+        mx[i] = p[int(np.argmax(p[:, i])), i] + margin
+        mn[i] = p[int(np.argmax(-p[:, i])), i] - margin
+    return mn, mx
+
+
+def hull_inertia(mass, points, margin=F(0.04)):
+    mn, mx = hull_local_aabb(points, margin)
+    lhe = (mx - mn) * F(0.5) + margin              # transformAabb with the identity transform
+    lc = (mx + mn) * F(0.5)
+    amin, amax = lc - lhe, lc + lhe
+    he = (amax - amin) * F(0.5)
+    lx, ly, lz = F(2) * (he[0] + margin), F(2) * (he[1] + margin), F(2) * (he[2] + margin)
+    x2, y2, z2 = lx * lx, ly * ly, lz * lz
+    sm = F(mass) * F(0.08333333)
+    return np.array([y2 + z2, x2 + z2, x2 + y2], F) * sm
+
+
+# ---- helpers ------------------------------------------------------------------------------
+def random_rotations(rng, n):
+    """Uniform rotations from normalised 4-D Gaussians, as row-major 3x3 bases (float32)."""
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    x, y, z, w = q[:, 0], q[:, 1], q[:, 2], q[:, 3]
+    R = np.empty((n, 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z); R[:, 0, 1] = 2 * (x * y - w * z); R[:, 0, 2] = 2 * (x * z + w * y)
+    R[:, 1, 0] = 2 * (x * y + w * z); R[:, 1, 1] = 1 - 2 * (x * x + z * z); R[:, 1, 2] = 2 * (y * z - w * x)
+    R[:, 2, 0] = 2 * (x * z - w * y); R[:, 2, 1] = 2 * (y * z + w * x); R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R.astype(F)
+
+
+def _bodies(n):
+    b = np.zeros(n, BODY_DTYPE)
+    b["friction"] = 0.5
+    b["linear_sleeping_threshold"] = 0.8
+    b["angular_sleeping_threshold"] = 1.0
+    b["collision_group"] = -1
+    b["collision_mask"] = -1
+    b["transform"][:, 0] = 1
+    b["transform"][:, 4] = 1
+    b["transform"][:, 8] = 1
+    return b
+
+
+def _plane_body(shape_id):
+    b = _bodies(1)
+    b["shape"] = shape_id
+    return b
+
+
+PLANE = {"type": _abi.SHAPE_STATIC_PLANE, "params": (0.0, 1.0, 0.0, 0.0), "points": None}
+
+
+def _set_transforms(b, R, pos):
+    b["transform"][:, :9] = R.reshape(-1, 9)
+    b["transform"][:, 9:] = pos.astype(F)
+
+
+# ---- the five workloads -------------------------------------------------------------------
+def boxes_on_plane(n=1000, seed=0, region=(20.0, 50.0, 20.0), y0=1.0, steps=300):
+    """1,000 unit boxes (half-extent 0.5, mass 1, friction 0.5, restitution 0), uniform in a
+    20x50x20 m region above a static plane y=0, uniform random orientations, at rest;
+    gravity -9.81, 10 PGS iterations, warm start 0.85, dt 1/60."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE), {"type": _abi.SHAPE_BOX, "params": (0.5, 0.5, 0.5, 0.0), "points": None}]
+    b = _bodies(n)
+    b["shape"] = 1
+    b["mass"] = 1.0
+    b["local_inertia"] = box_inertia(1.0, (0.5, 0.5, 0.5))
+    pos = np.stack([rng.uniform(-region[0] / 2, region[0] / 2, n), rng.uniform(y0, y0 + region[1], n),
+                    rng.uniform(-region[2] / 2, region[2] / 2, n)], 1)
+    _set_transforms(b, random_rotations(rng, n), pos)
+    bodies = np.concatenate([_plane_body(0), b])
+    return Scene("boxes_on_plane_%d" % n, 1.0 / 60.0, steps, {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10},
+                 shapes, bodies, meta={"seed": seed})
+
+
+def mixed_100k(n=100_000, seed=0, region=(200.0, 100.0, 200.0), y0=1.0, steps=600):
+    """100,000 bodies: 40% spheres r~U[0.2,0.6], 40% boxes half-extents~U[0.2,0.6]^3,
+    20% capsules r=0.25 half-height~U[0.2,0.8] (CapsuleShape(r, 2*hh)); density 1000;
+    200x100x200 m region, random orientations, v~N(0,1) per axis; 10 iterations, dt 1/120."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    kind = rng.permutation(np.repeat(np.arange(3), [int(0.4 * n), int(0.4 * n), n - 2 * int(0.4 * n)]))
+    shapes = [dict(PLANE)]
+    b = _bodies(n)
+    rs = rng.uniform(0.2, 0.6, n)
+    he = rng.uniform(0.2, 0.6, (n, 3))
+    hh = rng.uniform(0.2, 0.8, n)
+    rho = 1000.0
+    for i in range(n):
+        k = kind[i]
+        if k == 0:
+            r = F(rs[i])
+            shapes.append({"type": _abi.SHAPE_SPHERE, "params": (float(r), 0.0, 0.0, 0.0), "points": None})
+            m = F(rho * 4.0 / 3.0 * np.pi * float(r) ** 3)
+            b["local_inertia"][i] = sphere_inertia(m, r)
+        elif k == 1:
+            h = he[i].astype(F)
+            shapes.append({"type": _abi.SHAPE_BOX, "params": (float(h[0]), float(h[1]), float(h[2]), 0.0), "points": None})
+            m = F(rho * 8.0 * float(h[0]) * float(h[1]) * float(h[2]))
+            b["local_inertia"][i] = box_inertia(m, h)
+        else:
+            r, height = F(0.25), F(2.0 * hh[i])
+            shapes.append({"type": _abi.SHAPE_CAPSULE, "params": (float(r), float(height), 0.0, 0.0), "points": None})
+            m = F(rho * (np.pi * 0.25 ** 2 * float(height) + 4.0 / 3.0 * np.pi * 0.25 ** 3))
+            b["local_inertia"][i] = capsule_inertia(m, r, height)
+        b["mass"][i] = m
+        b["shape"][i] = i + 1
+    pos = np.stack([rng.uniform(-region[0] / 2, region[0] / 2, n), rng.uniform(y0, y0 + region[1], n),
+                    rng.uniform(-region[2] / 2, region[2] / 2, n)], 1)
+    _set_transforms(b, random_rotations(rng, n), pos)
+    b["linear_velocity"] = rng.standard_normal((n, 3)).astype(F)
+    bodies = np.concatenate([_plane_body(0), b])
+    return Scene("mixed_%d" % n, 1.0 / 120.0, steps, {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10},
+                 shapes, bodies, meta={"seed": seed, "kinds": np.concatenate([[-1], kind])})
+
+
+def hulls(n=20_000, seed=0, box=60.0, y0=1.0, npts=32, steps=400):
+    """n convex hulls, each the hull of 32 points uniform on an ellipsoid with semi-axes
+    U[0.3,1.0]; placed by random sequential addition of non-overlapping bounding spheres in a
+    60^3 m box with random orientations; density 1000 (box-inertia of the hull, as the
+    reference computes it); 15 iterations, dt 1/60."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE)]
+    b = _bodies(n)
+    axes = rng.uniform(0.3, 1.0, (n, 3))
+    radius = axes.max(axis=1)
+    cell = 2.0
+    grid = {}
+    pos = np.zeros((n, 3))
+    lo = np.array([-box / 2, y0, -box / 2])
+    for i in range(n):
+        for _ in range(10000):
+            p = lo + rng.uniform(0, 1, 3) * box
+            c = tuple((p // cell).astype(int))
+            ok = True
+            for dx in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    for dz in (-1, 0, 1):
+                        for j in grid.get((c[0] + dx, c[1] + dy, c[2] + dz), ()):
+                            if np.sum((pos[j] - p) ** 2) < (radius[i] + radius[j]) ** 2:
+                                ok = False
+                                break
+                        if not ok:
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                break
+        pos[i] = p
+        grid.setdefault(c, []).append(i)
+    for i in range(n):
+        d = rng.standard_normal((npts, 3))
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+        pts = (d * axes[i]).astype(F)
+        shapes.append({"type": _abi.SHAPE_CONVEX_HULL, "params": (0.0, 0.0, 0.0, 0.0), "points": pts})
+        m = F(1000.0 * 4.0 / 3.0 * np.pi * axes[i].prod())
+        b["mass"][i] = m
+        b["local_inertia"][i] = hull_inertia(m, pts)
+        b["shape"][i] = i + 1
+    _set_transforms(b, random_rotations(rng, n), pos)
+    bodies = np.concatenate([_plane_body(0), b])
+    return Scene("hulls_%d" % n, 1.0 / 60.0, steps, {"gravity": (0.0, -9.81, 0.0), "num_iterations": 15},
+                 shapes, bodies, meta={"seed": seed})
+
+
+def batched_worlds(n_worlds=4096, seed=0, nmin=16, nmax=2048, sphere_frac=0.1, steps=300):
+    """n_worlds independent worlds with log-uniform[16, 2048] bodies each: 90% unit boxes
+    (half-extent 0.5, mass 1) and 10% spheres of radius 0.5, each world with its own plane
+    and layout in a 20x50x20 m region; 10 iterations, dt 1/60.  Worlds are laid out one
+    after the other (plane first in each), bodies only collide within their world."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    counts = np.exp(rng.uniform(np.log(nmin), np.log(nmax), n_worlds)).astype(int)
+    shapes = [dict(PLANE), {"type": _abi.SHAPE_BOX, "params": (0.5, 0.5, 0.5, 0.0), "points": None},
+              {"type": _abi.SHAPE_SPHERE, "params": (0.5, 0.0, 0.0, 0.0), "points": None}]
+    parts, wid = [], []
+    for w in range(n_worlds):
+        nw = int(counts[w])
+        b = _bodies(nw)
+        sph = rng.uniform(0, 1, nw) < sphere_frac
+        b["shape"] = np.where(sph, 2, 1)
+        b["mass"] = 1.0
+        b["local_inertia"] = np.where(sph[:, None], sphere_inertia(1.0, 0.5), box_inertia(1.0, (0.5, 0.5, 0.5)))
+        pos = np.stack([rng.uniform(-10, 10, nw), rng.uniform(1.0, 51.0, nw), rng.uniform(-10, 10, nw)], 1)
+        _set_transforms(b, random_rotations(rng, nw), pos)
+        parts += [_plane_body(0), b]
+        wid.append(np.full(nw + 1, w, np.int32))
+    bodies = np.concatenate(parts)
+    bodies["world"] = np.concatenate(wid)
+    return Scene("batched_%d_worlds" % n_worlds, 1.0 / 60.0, steps, {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10},
+                 shapes, bodies, world_of_body=np.concatenate(wid), meta={"seed": seed, "counts": counts})
+
+
+def box_stack(levels=4, seed=0, steps=120):
+    """A small pyramid of unit boxes resting on the plane (a solver-hard, deterministic case)."""
+    shapes = [dict(PLANE), {"type": _abi.SHAPE_BOX, "params": (0.5, 0.5, 0.5, 0.0), "points": None}]
+    recs = []
+    for lv in range(levels):
+        for k in range(levels - lv):
+            x = (k - (levels - lv - 1) / 2.0) * 1.0
+            recs.append((x, 0.5 + lv * 1.0, 0.0))
+    b = _bodies(len(recs))
+    b["shape"] = 1
+    b["mass"] = 1.0
+    b["local_inertia"] = box_inertia(1.0, (0.5, 0.5, 0.5))
+    b["transform"][:, 9:] = np.array(recs, F)
+    bodies = np.concatenate([_plane_body(0), b])
+    return Scene("box_stack_%d" % levels, 1.0 / 60.0, steps, {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10},
+                 shapes, bodies, meta={"seed": seed})
+
+
+def small_mixed(n=60, seed=0, region=(6.0, 8.0, 6.0), steps=200, with_hulls=True):
+    """A small dense mix of every shape type for stage-by-stage parity checks."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE)]
+    b = _bodies(n)
+    for i in range(n):
+        k = i % (4 if with_hulls else 3)
+        if k == 0:
+            r = F(rng.uniform(0.2, 0.6))
+            shapes.append({"type": _abi.SHAPE_SPHERE, "params": (float(r), 0, 0, 0), "points": None})
+            m = F(1.0); b["local_inertia"][i] = sphere_inertia(m, r)
+        elif k == 1:
+            h = rng.uniform(0.2, 0.6, 3).astype(F)
+            shapes.append({"type": _abi.SHAPE_BOX, "params": (float(h[0]), float(h[1]), float(h[2]), 0), "points": None})
+            m = F(1.0); b["local_inertia"][i] = box_inertia(m, h)
+        elif k == 2:
+            height = F(2.0 * rng.uniform(0.2, 0.8))
+            shapes.append({"type": _abi.SHAPE_CAPSULE, "params": (0.25, float(height), 0, 0), "points": None})
+            m = F(1.0); b["local_inertia"][i] = capsule_inertia(m, F(0.25), height)
+        else:
+            d = rng.standard_normal((32, 3)); d /= np.linalg.norm(d, axis=1, keepdims=True)
+            pts = (d * rng.uniform(0.3, 1.0, 3)).astype(F)
+            shapes.append({"type": _abi.SHAPE_CONVEX_HULL, "params": (0, 0, 0, 0), "points": pts})
+            m = F(1.0); b["local_inertia"][i] = hull_inertia(m, pts)
+        b["mass"][i] = m
+        b["shape"][i] = i + 1
+    pos = np.stack([rng.uniform(-region[0] / 2, region[0] / 2, n), rng.uniform(0.5, 0.5 + region[1], n),
+                    rng.uniform(-region[2] / 2, region[2] / 2, n)], 1)
+    _set_transforms(b, random_rotations(rng, n), pos)
+    b["linear_velocity"] = rng.standard_normal((n, 3)).astype(F)
+    bodies = np.concatenate([_plane_body(0), b])
+    return Scene("small_mixed_%d" % n, 1.0 / 60.0, steps, {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10},
+                 shapes, bodies, meta={"seed": seed})
+
+
+SCENES = {
+    "boxes_1k": boxes_on_plane,
+    "mixed_100k": mixed_100k,
+    "hulls_20k": hulls,
+    "batched_4096": batched_worlds,
+    "box_stack": box_stack,
+    "small_mixed": small_mixed,
+}

@@ -1,0 +1,245 @@
+// ORACLE (test infrastructure only): C entry points over the CPU restatement, loaded by the
+// tests and by bench.py's CPU-baseline leg through ctypes.  Uses the POD layouts of
+// include/jbgpu.h so that oracle and GPU library exchange identical state buffers.
+#include <cstring>
+#include <vector>
+#include "../include/jbgpu.h"
+#include "jb_world.h"
+
+using namespace jb;
+
+static Xf xf_from12(const float* t) {
+    Xf x;
+    for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) x.b.m[r][c] = t[r * 3 + c];
+    x.o = v3(t[9], t[10], t[11]);
+    return x;
+}
+static void xf_to12(const Xf& x, float* t) {
+    for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) t[r * 3 + c] = x.b.m[r][c];
+    t[9] = x.o.x; t[10] = x.o.y; t[11] = x.o.z;
+}
+static Shape shape_from_desc(const jbgpu_shape_desc* d) {
+    switch (d->type) {
+    case JBGPU_SHAPE_BOX: return make_box(v3(d->params[0], d->params[1], d->params[2]));
+    case JBGPU_SHAPE_SPHERE: return make_sphere(d->params[0]);
+    case JBGPU_SHAPE_CAPSULE: return make_capsule(d->params[0], d->params[1]);
+    case JBGPU_SHAPE_CONVEX_HULL: return make_hull(d->points, d->num_points);
+    default: return make_plane(v3(d->params[0], d->params[1], d->params[2]), d->params[3]);
+    }
+}
+
+extern "C" {
+
+void* orc_create(const jbgpu_config* c) {
+    World* w = new World();
+    if (c) {
+        w->cfg.gravity = v3(c->gravity[0], c->gravity[1], c->gravity[2]);
+        w->cfg.contactBreakingThreshold = c->contact_breaking_threshold;
+        w->cfg.deactivationTime = c->deactivation_time;
+        w->cfg.disableDeactivation = c->disable_deactivation != 0;
+        w->cfg.numIterations = c->num_iterations;
+        w->cfg.erp = c->erp;
+        w->cfg.warmstartingFactor = c->warmstarting_factor;
+        w->cfg.linearSlop = c->linear_slop;
+        w->cfg.solverMode = c->solver_mode;
+    }
+    return w;
+}
+void orc_destroy(void* h) { delete (World*)h; }
+
+int orc_add_shape(void* h, const jbgpu_shape_desc* d) {
+    World* w = (World*)h;
+    w->shapes.push_back(shape_from_desc(d));
+    return (int)w->shapes.size() - 1;
+}
+
+int orc_shape_local_inertia(const jbgpu_shape_desc* d, float mass, float* out) {
+    Shape s = shape_from_desc(d);
+    V3 i = shape_local_inertia(s, mass);
+    out[0] = i.x; out[1] = i.y; out[2] = i.z;
+    return 0;
+}
+
+int orc_add_bodies(void* h, const jbgpu_body_desc* b, int n) {
+    World* w = (World*)h;
+    for (int i = 0; i < n; i++) {
+        const jbgpu_body_desc& d = b[i];
+        add_body(*w, d.mass, d.shape, xf_from12(d.transform), v3(d.local_inertia[0], d.local_inertia[1], d.local_inertia[2]),
+                 d.linear_damping, d.angular_damping, d.friction, d.restitution, d.linear_sleeping_threshold,
+                 d.angular_sleeping_threshold, v3(d.linear_velocity[0], d.linear_velocity[1], d.linear_velocity[2]),
+                 v3(d.angular_velocity[0], d.angular_velocity[1], d.angular_velocity[2]), d.collision_group, d.collision_mask,
+                 d.world);
+    }
+    return (int)w->bodies.size();
+}
+
+int orc_step_simulation(void* h, float ts, int maxSub, float fixed) { return step_simulation(*(World*)h, ts, maxSub, fixed); }
+void orc_step(void* h, float dt, int substeps) { step_fixed(*(World*)h, dt, substeps); }
+
+void orc_stage(void* h, int stage, float dt) {
+    World& w = *(World*)h;
+    switch (stage) {
+    case JBGPU_STAGE_APPLY_GRAVITY: stage_apply_gravity(w); break;
+    case JBGPU_STAGE_PREDICT: stage_predict(w, dt); break;
+    case JBGPU_STAGE_AABB: stage_aabbs(w); break;
+    case JBGPU_STAGE_PAIRS: stage_pairs(w); break;
+    case JBGPU_STAGE_NARROWPHASE: stage_narrowphase(w); break;
+    case JBGPU_STAGE_ISLANDS: stage_islands(w); break;
+    case JBGPU_STAGE_SOLVE: stage_solve(w, dt); break;
+    case JBGPU_STAGE_INTEGRATE: stage_integrate(w, dt); break;
+    case JBGPU_STAGE_ACTIVATION: stage_activation(w, dt); break;
+    case JBGPU_STAGE_CLEAR_FORCES: stage_clear_forces(w); break;
+    }
+}
+
+void orc_set_order_mode(void* h, int mode) { ((World*)h)->orderMode = mode; }
+void orc_set_explicit_order(void* h, const int* order, int n) { ((World*)h)->explicitOrder.assign(order, order + n); }
+void orc_set_brute_force(void* h, int on) { ((World*)h)->bruteForcePairs = on != 0; }
+int orc_num_bodies(void* h) { return (int)((World*)h)->bodies.size(); }
+
+int orc_get_state(void* h, jbgpu_state* s) {
+    World& w = *(World*)h;
+    int n = (int)w.bodies.size();
+    s->n_bodies = n;
+    for (int i = 0; i < n; i++) {
+        const Body& b = w.bodies[i];
+        if (s->transform) xf_to12(b.xf, s->transform + 12 * i);
+        if (s->linear_velocity) { float* p = s->linear_velocity + 3 * i; p[0] = b.linvel.x; p[1] = b.linvel.y; p[2] = b.linvel.z; }
+        if (s->angular_velocity) { float* p = s->angular_velocity + 3 * i; p[0] = b.angvel.x; p[1] = b.angvel.y; p[2] = b.angvel.z; }
+        if (s->inv_inertia_world) for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) s->inv_inertia_world[9 * i + 3 * r + c] = b.invInertiaWorld.m[r][c];
+        if (s->total_force) { float* p = s->total_force + 3 * i; p[0] = b.totalForce.x; p[1] = b.totalForce.y; p[2] = b.totalForce.z; }
+        if (s->total_torque) { float* p = s->total_torque + 3 * i; p[0] = b.totalTorque.x; p[1] = b.totalTorque.y; p[2] = b.totalTorque.z; }
+        if (s->aabb) { float* p = s->aabb + 6 * i; p[0] = b.aabbMin.x; p[1] = b.aabbMin.y; p[2] = b.aabbMin.z; p[3] = b.aabbMax.x; p[4] = b.aabbMax.y; p[5] = b.aabbMax.z; }
+        if (s->activation_state) s->activation_state[i] = b.activation;
+        if (s->deactivation_time) s->deactivation_time[i] = b.deactivationTime;
+        if (s->island_tag) s->island_tag[i] = b.islandTag;
+    }
+    return 0;
+}
+
+int orc_set_state(void* h, const jbgpu_state* s) {
+    World& w = *(World*)h;
+    int n = (int)w.bodies.size();
+    if (s->n_bodies != n) return JBGPU_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < n; i++) {
+        Body& b = w.bodies[i];
+        if (s->transform) b.xf = xf_from12(s->transform + 12 * i);
+        if (s->linear_velocity) { const float* p = s->linear_velocity + 3 * i; b.linvel = v3(p[0], p[1], p[2]); }
+        if (s->angular_velocity) { const float* p = s->angular_velocity + 3 * i; b.angvel = v3(p[0], p[1], p[2]); }
+        if (s->inv_inertia_world) for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) b.invInertiaWorld.m[r][c] = s->inv_inertia_world[9 * i + 3 * r + c];
+        if (s->total_force) { const float* p = s->total_force + 3 * i; b.totalForce = v3(p[0], p[1], p[2]); }
+        if (s->total_torque) { const float* p = s->total_torque + 3 * i; b.totalTorque = v3(p[0], p[1], p[2]); }
+        if (s->aabb) { const float* p = s->aabb + 6 * i; b.aabbMin = v3(p[0], p[1], p[2]); b.aabbMax = v3(p[3], p[4], p[5]); }
+        if (s->activation_state) b.activation = s->activation_state[i];
+        if (s->deactivation_time) b.deactivationTime = s->deactivation_time[i];
+    }
+    return 0;
+}
+
+static void point_to(const ManifoldPoint& p, float* f) {
+    std::memset(f, 0, sizeof(float) * JBGPU_POINT_FLOATS);
+    V3 vs[5] = {p.localA, p.localB, p.worldA, p.worldB, p.normal};
+    for (int k = 0; k < 5; k++) { f[3 * k] = vs[k].x; f[3 * k + 1] = vs[k].y; f[3 * k + 2] = vs[k].z; }
+    f[15] = p.distance; f[16] = p.friction; f[17] = p.restitution;
+    f[18] = p.appliedImpulse; f[19] = p.lat1; f[20] = p.lat2;
+    f[21] = p.latInit ? 1.0f : 0.0f; f[22] = (float)p.lifeTime;
+    f[23] = p.latDir1.x; f[24] = p.latDir1.y; f[25] = p.latDir1.z;
+    f[26] = p.latDir2.x; f[27] = p.latDir2.y; f[28] = p.latDir2.z;
+}
+static void point_from(ManifoldPoint& p, const float* f) {
+    V3* vs[5] = {&p.localA, &p.localB, &p.worldA, &p.worldB, &p.normal};
+    for (int k = 0; k < 5; k++) *vs[k] = v3(f[3 * k], f[3 * k + 1], f[3 * k + 2]);
+    p.distance = f[15]; p.friction = f[16]; p.restitution = f[17];
+    p.appliedImpulse = f[18]; p.lat1 = f[19]; p.lat2 = f[20];
+    p.latInit = f[21] != 0.0f; p.lifeTime = (int)f[22];
+    p.latDir1 = v3(f[23], f[24], f[25]);
+    p.latDir2 = v3(f[26], f[27], f[28]);
+}
+
+int orc_get_manifolds(void* h, jbgpu_manifolds* m) {
+    World& w = *(World*)h;
+    int n = (int)w.pairKeys.size();
+    m->n_pairs = n;
+    if (n > m->capacity) return JBGPU_ERR_CAPACITY;
+    for (int i = 0; i < n; i++) {
+        if (m->keys) m->keys[i] = w.pairKeys[i];
+        if (m->flags) m->flags[i] = w.pairHasAlgo[i] ? 1 : 0;
+        if (m->num_points) m->num_points[i] = w.pairHasAlgo[i] ? w.pairMf[i].n : 0;
+        if (m->points)
+            for (int j = 0; j < 4; j++) {
+                float* f = m->points + ((size_t)i * 4 + j) * JBGPU_POINT_FLOATS;
+                if (w.pairHasAlgo[i] && j < w.pairMf[i].n) point_to(w.pairMf[i].pts[j], f);
+                else std::memset(f, 0, sizeof(float) * JBGPU_POINT_FLOATS);
+            }
+    }
+    return 0;
+}
+
+// Manifold body order is implied by the key: (convex, plane) for plane pairs, (lo, hi) otherwise.
+int orc_set_manifolds(void* h, const jbgpu_manifolds* m) {
+    World& w = *(World*)h;
+    int n = m->n_pairs;
+    w.pairKeys.assign(m->keys, m->keys + n);
+    w.pairHasAlgo.assign(n, 0);
+    w.pairMf.assign(n, Manifold());
+    for (int i = 0; i < n; i++) {
+        int a = (int)(m->keys[i] >> 32), b = (int)(m->keys[i] & 0xffffffffu);
+        bool pb = w.shapes[w.bodies[b].shape].type == STATIC_PLANE;
+        Manifold& mf = w.pairMf[i];
+        if (pb) { mf.body0 = a; mf.body1 = b; }
+        else { mf.body0 = a < b ? a : b; mf.body1 = a < b ? b : a; }
+        w.pairHasAlgo[i] = (m->flags[i] & 1) ? 1 : 0;
+        mf.n = w.pairHasAlgo[i] ? m->num_points[i] : 0;
+        for (int j = 0; j < mf.n; j++) point_from(mf.pts[j], m->points + ((size_t)i * 4 + j) * JBGPU_POINT_FLOATS);
+    }
+    return 0;
+}
+
+int orc_get_solver_order(void* h, int* out, int cap) {
+    World& w = *(World*)h;
+    int n = (int)w.lastOrder.size();
+    for (int i = 0; i < n && i < cap; i++) out[i] = w.lastOrder[i];
+    return n;
+}
+
+void orc_counters(void* h, jbgpu_counters* c) {
+    World& w = *(World*)h;
+    std::memset(c, 0, sizeof(*c));
+    c->steps = w.counters.steps;
+    c->bodies = (int)w.bodies.size();
+    c->pairs = w.counters.pairs;
+    c->manifolds = w.counters.manifolds;
+    c->contacts = w.counters.contacts;
+    c->solver_manifolds = w.counters.solverManifolds;
+    c->solver_rows = w.counters.solverRows;
+    c->colours = w.counters.colours;
+    c->islands = w.counters.islands;
+    c->gjk_calls = w.counters.gjk;
+    c->epa_calls = w.counters.epa;
+}
+
+void orc_phase_seconds(void* h, double* out) {
+    World& w = *(World*)h;
+    for (int i = 0; i < 10; i++) out[i] = w.phaseSeconds[i];
+}
+
+// GjkPairDetector.getClosestPoints between two shapes at given transforms (12 floats each).
+// out: normal(3), pointOnB(3), distance, valid, usedEpa
+int orc_gjk(const jbgpu_shape_desc* da, const float* ta, const jbgpu_shape_desc* db, const float* tb, float maxDist2, float* out) {
+    Shape sa = shape_from_desc(da), sb = shape_from_desc(db);
+    GjkOut g = gjk_closest_points(sa, xf_from12(ta), sb, xf_from12(tb), maxDist2);
+    out[0] = g.valid ? g.normal.x : 0; out[1] = g.valid ? g.normal.y : 0; out[2] = g.valid ? g.normal.z : 0;
+    out[3] = g.valid ? g.pointOnB.x : 0; out[4] = g.valid ? g.pointOnB.y : 0; out[5] = g.valid ? g.pointOnB.z : 0;
+    out[6] = g.valid ? g.distance : 0;
+    out[7] = g.valid ? 1.0f : 0.0f;
+    out[8] = (float)g.usedEpa;
+    return g.valid ? 1 : 0;
+}
+
+// TransformUtil.integrateTransform on one transform, for unit checks of the libGDX boundary.
+void orc_integrate_transform(const float* t12, const float* lin, const float* ang, float dt, float* out12) {
+    Xf x = integrate_transform(xf_from12(t12), v3(lin[0], lin[1], lin[2]), v3(ang[0], ang[1], ang[2]), dt);
+    xf_to12(x, out12);
+}
+
+}  // extern "C"

@@ -1,0 +1,712 @@
+// ORACLE (test infrastructure only): world step of the reference, restated.
+// Citations relative to src/com/bulletphysics/.
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include "jb_world.h"
+
+namespace jb {
+
+static double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+struct PhaseTimer {
+    World& w; int i; double t0;
+    PhaseTimer(World& ww, int ii) : w(ww), i(ii), t0(now_s()) {}
+    ~PhaseTimer() { w.phaseSeconds[i] += now_s() - t0; }
+};
+
+// RigidBody.updateInertiaTensor (dynamics/RigidBody.java:449-459)
+static void update_inertia_tensor(Body& b) {
+    M3 mat1 = scaleM(b.xf.b, b.invInertiaLocal);
+    M3 mat2 = transpose(b.xf.b);
+    b.invInertiaWorld = mulMM(mat1, mat2);
+}
+
+static float gen_clamped(float a, float lb, float ub) { return a < lb ? lb : (ub < a ? ub : a); }   // MiscUtil.GEN_clamped
+
+// RigidBody.setupRigidBody + DiscreteDynamicsWorld.addRigidBody + CollisionWorld.addCollisionObject
+// (dynamics/RigidBody.java:121-164,301-312; dynamics/DiscreteDynamicsWorld.java:426-440;
+//  collision/dispatch/CollisionWorld.java:103-121)
+int add_body(World& w, float mass, int shape, const Xf& xf, V3 inertia, float linDamp, float angDamp, float friction,
+             float restitution, float linSleep, float angSleep, V3 linvel, V3 angvel, int group, int mask, int world) {
+    Body b;
+    b.world = world;
+    b.xf = xf;
+    b.shape = shape;
+    b.friction = friction;
+    b.restitution = restitution;
+    b.linSleep = linSleep;
+    b.angSleep = angSleep;
+    if (mass == 0.0f) { b.flags |= CF_STATIC_OBJECT; b.invMass = 0.0f; }
+    else { b.flags &= ~CF_STATIC_OBJECT; b.invMass = 1.0f / mass; }
+    b.invInertiaLocal = v3(inertia.x != 0.0f ? 1.0f / inertia.x : 0.0f, inertia.y != 0.0f ? 1.0f / inertia.y : 0.0f,
+                           inertia.z != 0.0f ? 1.0f / inertia.z : 0.0f);
+    b.linearDamping = gen_clamped(linDamp, 0.0f, 1.0f);
+    b.angularDamping = gen_clamped(angDamp, 0.0f, 1.0f);
+    update_inertia_tensor(b);
+    if (!b.isStaticOrKinematic()) {
+        if (b.invMass != 0.0f) b.gravity = scl(w.cfg.gravity, 1.0f / b.invMass);   // RigidBody.setGravity
+    }
+    bool isDynamic = !(b.isStatic() || b.isKinematic());
+    b.group = group != -1 ? group : (isDynamic ? 1 : 2);
+    b.mask = mask != -1 ? mask : (isDynamic ? -1 : (short)(-1 ^ 2));
+    b.linvel = linvel;
+    b.angvel = angvel;
+    shape_aabb(w.shapes[shape], b.xf, b.aabbMin, b.aabbMax);   // createProxy with the shape aabb
+    w.bodies.push_back(b);
+    return (int)w.bodies.size() - 1;
+}
+
+static bool is_plane(const World& w, int i) { return w.shapes[w.bodies[i].shape].type == STATIC_PLANE; }
+
+uint64_t pair_key(const World& w, int a, int b) {
+    bool pa = is_plane(w, a), pb = is_plane(w, b);
+    int owner, partner;
+    if (pa && !pb) { owner = b; partner = a; }
+    else if (pb && !pa) { owner = a; partner = b; }
+    else { owner = a < b ? a : b; partner = a < b ? b : a; }
+    return ((uint64_t)(uint32_t)owner << 32) | (uint32_t)partner;
+}
+
+// ---------------------------------------------------------------------------------------
+// DiscreteDynamicsWorld.applyGravity (dynamics/DiscreteDynamicsWorld.java:239-249)
+void stage_apply_gravity(World& w) {
+    for (Body& b : w.bodies) {
+        if (b.isActive() && !b.isStaticOrKinematic()) {   // RigidBody.applyGravity -> applyCentralForce
+            b.totalForce.x += b.gravity.x * b.linearFactor.x;
+            b.totalForce.y += b.gravity.y * b.linearFactor.y;
+            b.totalForce.z += b.gravity.z * b.linearFactor.z;
+        }
+    }
+}
+
+// predictUnconstraintMotion (DiscreteDynamicsWorld.java:741-767): integrateVelocities + applyDamping.
+// The predicted transform it computes goes into a temporary and is discarded (CollisionObject.java:230-233).
+void stage_predict(World& w, float dt) {
+    PhaseTimer pt(w, 1);
+    const float MAX_ANGVEL = SIMD_HALF_PI;
+    for (Body& b : w.bodies) {
+        if (b.isStaticOrKinematic() || !b.isActive()) continue;
+        // RigidBody.integrateVelocities (dynamics/RigidBody.java:323-342)
+        b.linvel.x += b.invMass * dt * b.totalForce.x;
+        b.linvel.y += b.invMass * dt * b.totalForce.y;
+        b.linvel.z += b.invMass * dt * b.totalForce.z;
+        V3 tmp = scl(mulMv(b.totalTorque, b.invInertiaWorld), dt);
+        b.angvel = add(b.angvel, tmp);
+        float angvel = len(b.angvel);
+        if (angvel * dt > MAX_ANGVEL) b.angvel = scl(b.angvel, (MAX_ANGVEL / dt) / angvel);
+        // RigidBody.applyDamping (dynamics/RigidBody.java:246-299), additionalDamping off
+        b.linvel = scl(b.linvel, jpow(1.0f - b.linearDamping, dt));
+        b.angvel = scl(b.angvel, jpow(1.0f - b.angularDamping, dt));
+    }
+}
+
+// CollisionWorld.updateAabbs / updateSingleAabb (collision/dispatch/CollisionWorld.java:195-245)
+void stage_aabbs(World& w) {
+    PhaseTimer pt(w, 2);
+    const float t = w.cfg.contactBreakingThreshold;
+    for (Body& b : w.bodies) {
+        if (!b.isActive()) continue;
+        V3 mn, mx;
+        shape_aabb(w.shapes[b.shape], b.xf, mn, mx);
+        mn = sub(mn, v3(t, t, t));
+        mx = add(mx, v3(t, t, t));
+        V3 d = sub(mx, mn);
+        if (b.isStatic() || (len2(d) < 1e12f)) { b.aabbMin = mn; b.aabbMax = mx; }
+        else b.setActivationState(DISABLE_SIMULATION);
+    }
+}
+
+// DbvtAabbMm.Intersect (collision/broadphase/DbvtAabbMm.java:209-212), inclusive
+static inline bool aabb_overlap(const Body& a, const Body& b) {
+    return (a.aabbMin.x <= b.aabbMax.x) && (a.aabbMax.x >= b.aabbMin.x) && (a.aabbMin.y <= b.aabbMax.y) &&
+           (a.aabbMax.y >= b.aabbMin.y) && (a.aabbMin.z <= b.aabbMax.z) && (a.aabbMax.z >= b.aabbMin.z);
+}
+// HashedOverlappingPairCache.needsBroadphaseCollision (java:179-188)
+static inline bool filter_pass(const Body& a, const Body& b) {
+    return a.world == b.world && ((short)a.group & (short)b.mask) != 0 && ((short)b.group & (short)a.mask) != 0;
+}
+
+// The pair set the DBVT broadphase holds after collide() (collision/broadphase/DbvtBroadphase.java:89-150):
+// every filter-passing pair whose proxy aabbs intersect inclusively.  Found here with a
+// median-split box tree over the finite proxies; static planes are tested against all.
+namespace {
+struct BNode { V3 mn, mx; int left, right, first, count; };
+struct BTree {
+    std::vector<BNode> nodes;
+    std::vector<int> idx;
+    const World* w;
+    int build(int first, int count) {
+        BNode n;
+        n.mn = v3(3e38f, 3e38f, 3e38f); n.mx = v3(-3e38f, -3e38f, -3e38f);
+        for (int i = first; i < first + count; i++) {
+            const Body& b = w->bodies[idx[i]];
+            n.mn = v3(std::min(n.mn.x, b.aabbMin.x), std::min(n.mn.y, b.aabbMin.y), std::min(n.mn.z, b.aabbMin.z));
+            n.mx = v3(std::max(n.mx.x, b.aabbMax.x), std::max(n.mx.y, b.aabbMax.y), std::max(n.mx.z, b.aabbMax.z));
+        }
+        n.left = n.right = -1; n.first = first; n.count = count;
+        int id = (int)nodes.size();
+        nodes.push_back(n);
+        if (count > 4) {
+            V3 e = sub(n.mx, n.mn);
+            int axis = (e.x >= e.y && e.x >= e.z) ? 0 : (e.y >= e.z ? 1 : 2);
+            int mid = first + count / 2;
+            std::nth_element(idx.begin() + first, idx.begin() + mid, idx.begin() + first + count, [&](int a, int b) {
+                const Body& A = w->bodies[a]; const Body& B = w->bodies[b];
+                float ca = coord(A.aabbMin, axis) + coord(A.aabbMax, axis), cb = coord(B.aabbMin, axis) + coord(B.aabbMax, axis);
+                return ca < cb || (ca == cb && a < b);
+            });
+            int l = build(first, mid - first);
+            int r = build(mid, first + count - mid);
+            nodes[id].left = l; nodes[id].right = r;
+        }
+        return id;
+    }
+};
+}  // namespace
+
+void stage_pairs(World& w) {
+    PhaseTimer pt(w, 3);
+    const int n = (int)w.bodies.size();
+    std::vector<uint64_t> keys;
+    std::vector<int> planes, finite;
+    for (int i = 0; i < n; i++) (is_plane(w, i) ? planes : finite).push_back(i);
+    if (w.bruteForcePairs) {   // SimpleBroadphase.calculateOverlappingPairs-style O(n^2) (SimpleBroadphase.java:87-110)
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++)
+                if (!(is_plane(w, i) && is_plane(w, j)) && aabb_overlap(w.bodies[i], w.bodies[j]) && filter_pass(w.bodies[i], w.bodies[j]))
+                    keys.push_back(pair_key(w, i, j));
+    } else {
+        for (int p : planes)
+            for (int j = 0; j < n; j++)
+                if (j != p && !is_plane(w, j) && aabb_overlap(w.bodies[p], w.bodies[j]) && filter_pass(w.bodies[p], w.bodies[j]))
+                    keys.push_back(pair_key(w, p, j));
+        if (!finite.empty()) {
+            BTree t;
+            t.w = &w;
+            t.idx = finite;
+            t.nodes.reserve(2 * finite.size() / 4 + 8);
+            t.build(0, (int)finite.size());
+            std::vector<int> stack;
+            for (int i : finite) {
+                const Body& bi = w.bodies[i];
+                stack.clear();
+                stack.push_back(0);
+                while (!stack.empty()) {
+                    const BNode& nd = t.nodes[stack.back()];
+                    stack.pop_back();
+                    if (!(bi.aabbMin.x <= nd.mx.x && bi.aabbMax.x >= nd.mn.x && bi.aabbMin.y <= nd.mx.y &&
+                          bi.aabbMax.y >= nd.mn.y && bi.aabbMin.z <= nd.mx.z && bi.aabbMax.z >= nd.mn.z)) continue;
+                    if (nd.left < 0) {
+                        for (int k = nd.first; k < nd.first + nd.count; k++) {
+                            int j = t.idx[k];
+                            if (j > i && aabb_overlap(bi, w.bodies[j]) && filter_pass(bi, w.bodies[j])) keys.push_back(pair_key(w, i, j));
+                        }
+                    } else {
+                        stack.push_back(nd.left);
+                        stack.push_back(nd.right);
+                    }
+                }
+            }
+        }
+    }
+    std::sort(keys.begin(), keys.end());
+    // carry algorithms/manifolds of pairs that persist; others are released
+    // (HashedOverlappingPairCache.removeOverlappingPair -> cleanOverlappingPair, java:77-177,222-228)
+    std::vector<uint8_t> has(keys.size(), 0);
+    std::vector<Manifold> mf(keys.size());
+    size_t o = 0;
+    for (size_t k = 0; k < keys.size(); k++) {
+        while (o < w.pairKeys.size() && w.pairKeys[o] < keys[k]) o++;
+        if (o < w.pairKeys.size() && w.pairKeys[o] == keys[k]) { has[k] = w.pairHasAlgo[o]; mf[k] = w.pairMf[o]; }
+    }
+    w.pairKeys.swap(keys);
+    w.pairHasAlgo.swap(has);
+    w.pairMf.swap(mf);
+    w.counters.pairs = (int)w.pairKeys.size();
+}
+
+// CollisionDispatcher.dispatchAllCollisionPairs (collision/dispatch/CollisionDispatcher.java:252-257)
+void stage_narrowphase(World& w) {
+    PhaseTimer pt(w, 4);
+    w.counters.gjk = 0;
+    w.counters.epa = 0;
+    for (size_t i = 0; i < w.pairKeys.size(); i++) process_pair(w, (int)i);
+    int nm = 0, nc = 0;
+    for (size_t i = 0; i < w.pairKeys.size(); i++) if (w.pairHasAlgo[i]) { nm++; nc += w.pairMf[i].n; }
+    w.counters.manifolds = nm;
+    w.counters.contacts = nc;
+}
+
+// ---------------------------------------------------------------------------------------
+// UnionFind (collision/dispatch/UnionFind.java:55-143), path-compressing find
+namespace {
+struct UF {
+    std::vector<int> id, sz;
+    void reset(int n) { id.resize(n); sz.assign(n, 1); for (int i = 0; i < n; i++) id[i] = i; }
+    int find(int x) { while (x != id[x]) { id[x] = id[id[x]]; x = id[x]; } return x; }
+    void unite(int p, int q) { int i = find(p), j = find(q); if (i == j) return; id[i] = j; sz[j] += sz[i]; }
+};
+// MiscUtil.quickSortInternal (linearmath/MiscUtil.java:187-209)
+template <class T, class C> static void quick_sort(std::vector<T>& a, int lo, int hi, C cmp) {
+    int i = lo, j = hi;
+    T x = a[(lo + hi) / 2];
+    do {
+        while (cmp(a[i], x) < 0) i++;
+        while (cmp(x, a[j]) < 0) j--;
+        if (i <= j) { std::swap(a[i], a[j]); i++; j--; }
+    } while (i <= j);
+    if (lo < j) quick_sort(a, lo, j, cmp);
+    if (i < hi) quick_sort(a, i, hi, cmp);
+}
+}  // namespace
+
+static std::vector<int> g_islandManifolds;    // islandmanifold of the last ISLANDS stage (pair indices)
+
+// calculateSimulationIslands + SimulationIslandManager.buildIslands
+// (dynamics/DiscreteDynamicsWorld.java:649-677; collision/dispatch/SimulationIslandManager.java:57-240)
+void stage_islands(World& w) {
+    PhaseTimer pt(w, 5);
+    const int n = (int)w.bodies.size();
+    UF uf;
+    uf.reset(n);
+    for (int i = 0; i < n; i++) { w.bodies[i].islandTag = i; w.bodies[i].companionId = -1; }
+    for (size_t k = 0; k < w.pairKeys.size(); k++) {   // findUnions over the pair array
+        int a = (int)(w.pairKeys[k] >> 32), b = (int)(w.pairKeys[k] & 0xffffffffu);
+        int lo = a < b ? a : b, hi = a < b ? b : a;
+        if (w.bodies[lo].mergesIslands() && w.bodies[hi].mergesIslands()) uf.unite(w.bodies[lo].islandTag, w.bodies[hi].islandTag);
+    }
+    for (int i = 0; i < n; i++) {   // storeIslandActivationState
+        Body& b = w.bodies[i];
+        if (!b.isStaticOrKinematic()) { b.islandTag = uf.find(i); b.companionId = -1; }
+        else { b.islandTag = -1; b.companionId = -2; }
+    }
+    // per island: sleep if no member is ACTIVE_TAG or DISABLE_DEACTIVATION, else wake sleepers
+    std::vector<uint8_t> keepAwake(n, 0), hasMember(n, 0);
+    for (int i = 0; i < n; i++) {
+        const Body& b = w.bodies[i];
+        if (b.islandTag < 0) continue;
+        hasMember[b.islandTag] = 1;
+        if (b.activation == ACTIVE_TAG || b.activation == DISABLE_DEACTIVATION) keepAwake[b.islandTag] = 1;
+    }
+    int islands = 0;
+    for (int i = 0; i < n; i++) islands += hasMember[i];
+    w.counters.islands = islands;
+    for (int i = 0; i < n; i++) {
+        Body& b = w.bodies[i];
+        if (b.islandTag < 0) continue;
+        if (!keepAwake[b.islandTag]) b.setActivationState(ISLAND_SLEEPING);
+        else if (b.activation == ISLAND_SLEEPING) b.setActivationState(WANTS_DEACTIVATION);
+    }
+    // islandmanifold: manifolds with a non-sleeping body that need a response
+    g_islandManifolds.clear();
+    for (size_t k = 0; k < w.pairKeys.size(); k++) {
+        if (!w.pairHasAlgo[k]) continue;
+        const Manifold& m = w.pairMf[k];
+        const Body& b0 = w.bodies[m.body0];
+        const Body& b1 = w.bodies[m.body1];
+        if (b0.activation != ISLAND_SLEEPING || b1.activation != ISLAND_SLEEPING) {
+            bool resp = b0.hasContactResponse() && b1.hasContactResponse() && (!b0.isStaticOrKinematic() || !b1.isStaticOrKinematic());
+            if (resp) g_islandManifolds.push_back((int)k);
+        }
+    }
+    // islands whose members are all active are processed (SimulationIslandManager.java:283-296)
+    std::vector<uint8_t> inactive(n, 0);
+    for (int i = 0; i < n; i++) if (w.bodies[i].islandTag >= 0 && !w.bodies[i].isActive()) inactive[w.bodies[i].islandTag] = 1;
+    w.solveList.clear();
+    for (int k : g_islandManifolds) {
+        const Manifold& m = w.pairMf[k];
+        int isl = w.bodies[m.body0].islandTag >= 0 ? w.bodies[m.body0].islandTag : w.bodies[m.body1].islandTag;
+        if (!inactive[isl]) w.solveList.push_back(k);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// SequentialImpulseConstraintSolver (dynamics/constraintsolver/SequentialImpulseConstraintSolver.java)
+namespace {
+struct SolverBody {   // dynamics/constraintsolver/SolverBody.java:36-119
+    V3 angvel, linvel, angularFactor, linearFactor;
+    float invMass;
+    int original;
+    void apply(V3 lin, V3 ang, float imp) {   // internalApplyImpulse
+        if (invMass != 0.0f) {
+            linvel.x += imp * linearFactor.x * lin.x;
+            linvel.y += imp * linearFactor.y * lin.y;
+            linvel.z += imp * linearFactor.z * lin.z;
+            angvel.x += imp * angularFactor.x * ang.x;
+            angvel.y += imp * angularFactor.y * ang.y;
+            angvel.z += imp * angularFactor.z * ang.z;
+        }
+    }
+};
+struct Row {          // dynamics/constraintsolver/SolverConstraint.java:34-58
+    V3 rp1xn, normal, rp2xn, angA, angB;
+    float pushImpulse = 0, impulse = 0, friction = 0, restitution = 0, jacDiagABInv = 0, penetration = 0;
+    int bodyA = -1, bodyB = -1, frictionIndex = -1;
+    int mfPair = -1, mfPoint = -1;
+};
+}  // namespace
+
+static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
+    const Config& cfg = w.cfg;
+    std::vector<SolverBody> sb;
+    std::vector<Row> rows, frows;
+    sb.reserve(manifolds.size() * 2);
+    auto init_sb = [&](int bi) {   // initSolverBody (java:151-177)
+        const Body& b = w.bodies[bi];
+        SolverBody s;
+        s.angvel = b.angvel;
+        s.invMass = b.invMass;
+        s.linvel = b.linvel;
+        s.original = bi;
+        s.angularFactor = b.angularFactor;
+        s.linearFactor = b.linearFactor;
+        sb.push_back(s);
+        return (int)sb.size() - 1;
+    };
+    auto get_sb = [&](int bi) {
+        Body& b = w.bodies[bi];
+        if (b.islandTag >= 0) {
+            if (b.companionId >= 0) return b.companionId;
+            int id = init_sb(bi);
+            b.companionId = id;
+            return id;
+        }
+        return init_sb(bi);   // static body: a private solver body per manifold
+    };
+    // addFrictionConstraint (java:349-416)
+    auto add_friction = [&](V3 normalAxis, int sbA, int sbB, int frictionIndex, const ManifoldPoint& cp, V3 rp1, V3 rp2,
+                            const Body& b0, const Body& b1) {
+        Row r;
+        r.normal = normalAxis;
+        r.bodyA = sbA; r.bodyB = sbB;
+        r.frictionIndex = frictionIndex;
+        r.friction = cp.friction;
+        r.impulse = 0; r.pushImpulse = 0; r.penetration = 0;
+        V3 ft = crs(rp1, r.normal);
+        r.rp1xn = ft;
+        r.angA = mulMv(ft, b0.invInertiaWorld);
+        ft = crs(rp2, r.normal);
+        r.rp2xn = ft;
+        r.angB = mulMv(ft, b1.invInertiaWorld);
+        float denom0 = b0.invMass + dot(normalAxis, crs(r.angA, rp1));
+        float denom1 = b1.invMass + dot(normalAxis, crs(r.angB, rp2));
+        r.jacDiagABInv = 1.0f / (denom0 + denom1);
+        frows.push_back(r);
+    };
+    const bool warm = (cfg.solverMode & SOLVER_USE_WARMSTARTING) != 0;
+    // solveGroupCacheFriendlySetup (java:418-786)
+    for (int pi : manifolds) {
+        Manifold& m = w.pairMf[pi];
+        const Body& b0 = w.bodies[m.body0];
+        const Body& b1 = w.bodies[m.body1];
+        int sbA = -1, sbB = -1;
+        if (m.n != 0) { sbA = get_sb(m.body0); sbB = get_sb(m.body1); }
+        for (int j = 0; j < m.n; j++) {
+            ManifoldPoint& cp = m.pts[j];
+            if (!(cp.distance <= 0.0f)) continue;
+            V3 pos1 = cp.worldA, pos2 = cp.worldB;
+            V3 rp1 = sub(pos1, b0.xf.o), rp2 = sub(pos2, b1.xf.o);
+            float relaxation = 1.0f;
+            int frictionIndex = (int)rows.size();
+            Row r;
+            r.bodyA = sbA; r.bodyB = sbB;
+            r.mfPair = pi; r.mfPoint = j;
+            V3 ta0 = crs(rp1, cp.normal);
+            r.angA = mulMv(ta0, b0.invInertiaWorld);
+            V3 ta1 = crs(rp2, cp.normal);
+            r.angB = mulMv(ta1, b1.invInertiaWorld);
+            {
+                float denom0 = b0.invMass + dot(cp.normal, crs(r.angA, rp1));
+                float denom1 = b1.invMass + dot(cp.normal, crs(r.angB, rp2));
+                r.jacDiagABInv = relaxation / (denom0 + denom1);
+            }
+            r.normal = cp.normal;
+            r.rp1xn = crs(rp1, cp.normal);
+            r.rp2xn = crs(rp2, cp.normal);
+            V3 vel1 = add(crs(b0.angvel, rp1), b0.linvel);   // RigidBody.getVelocityInLocalPoint
+            V3 vel2 = add(crs(b1.angvel, rp2), b1.linvel);
+            V3 vel = sub(vel1, vel2);
+            float rel_vel = dot(cp.normal, vel);
+            r.penetration = jmin(cp.distance + cfg.linearSlop, 0.0f);
+            r.friction = cp.friction;
+            r.restitution = cp.restitution * -rel_vel;   // restitutionCurve
+            if (r.restitution <= 0.0f) r.restitution = 0.0f;
+            float penVel = -r.penetration / dt;
+            if (r.restitution > penVel) r.penetration = 0.0f;
+            if (warm) {
+                r.impulse = cp.appliedImpulse * cfg.warmstartingFactor;
+                sb[r.bodyA].apply(scl(r.normal, b0.invMass), r.angA, r.impulse);
+                sb[r.bodyB].apply(scl(r.normal, b1.invMass), r.angB, -r.impulse);
+            } else {
+                r.impulse = 0.0f;
+            }
+            r.pushImpulse = 0.0f;
+            r.frictionIndex = (int)frows.size();
+            rows.push_back(r);
+            if (!cp.latInit) {
+                cp.latDir1 = sub(vel, scl(cp.normal, rel_vel));
+                float lat_rel_vel = len2(cp.latDir1);
+                if (lat_rel_vel > FLT_EPS) {
+                    cp.latDir1 = scl(cp.latDir1, 1.0f / jsqrt(lat_rel_vel));
+                    add_friction(cp.latDir1, sbA, sbB, frictionIndex, cp, rp1, rp2, b0, b1);
+                    cp.latDir2 = nor(crs(cp.latDir1, cp.normal));
+                    add_friction(cp.latDir2, sbA, sbB, frictionIndex, cp, rp1, rp2, b0, b1);
+                } else {
+                    plane_space1(cp.normal, cp.latDir1, cp.latDir2);
+                    add_friction(cp.latDir1, sbA, sbB, frictionIndex, cp, rp1, rp2, b0, b1);
+                    add_friction(cp.latDir2, sbA, sbB, frictionIndex, cp, rp1, rp2, b0, b1);
+                }
+                cp.latInit = true;
+            } else {
+                add_friction(cp.latDir1, sbA, sbB, frictionIndex, cp, rp1, rp2, b0, b1);
+                add_friction(cp.latDir2, sbA, sbB, frictionIndex, cp, rp1, rp2, b0, b1);
+            }
+            Row& nr = rows.back();
+            for (int f = 0; f < 2; f++) {
+                Row& fr = frows[nr.frictionIndex + f];
+                if (warm) {
+                    fr.impulse = (f == 0 ? cp.lat1 : cp.lat2) * cfg.warmstartingFactor;
+                    sb[nr.bodyA].apply(scl(fr.normal, b0.invMass), fr.angA, fr.impulse);
+                    sb[nr.bodyB].apply(scl(fr.normal, b1.invMass), fr.angB, -fr.impulse);
+                } else {
+                    fr.impulse = 0.0f;
+                }
+            }
+        }
+    }
+    w.counters.solverRows += (int)rows.size();
+    // solveGroupCacheFriendlyIterations (java:788-890), split impulse off
+    for (int it = 0; it < cfg.numIterations; it++) {
+        for (Row& c : rows) {   // resolveSingleCollisionCombinedCacheFriendly (java:234-284)
+            SolverBody& A = sb[c.bodyA];
+            SolverBody& B = sb[c.bodyB];
+            float vel1Dotn = dot(c.normal, A.linvel) + dot(c.rp1xn, A.angvel);
+            float vel2Dotn = dot(c.normal, B.linvel) + dot(c.rp2xn, B.angvel);
+            float rel_vel = vel1Dotn - vel2Dotn;
+            float positionalError = -c.penetration * cfg.erp / dt;
+            float velocityError = c.restitution - rel_vel;
+            float penetrationImpulse = positionalError * c.jacDiagABInv;
+            float velocityImpulse = velocityError * c.jacDiagABInv;
+            float normalImpulse = penetrationImpulse + velocityImpulse;
+            float oldImpulse = c.impulse;
+            float sum = oldImpulse + normalImpulse;
+            c.impulse = 0.0f > sum ? 0.0f : sum;
+            normalImpulse = c.impulse - oldImpulse;
+            A.apply(scl(c.normal, A.invMass), c.angA, normalImpulse);
+            B.apply(scl(c.normal, B.invMass), c.angB, -normalImpulse);
+        }
+        for (Row& c : frows) {  // resolveSingleFrictionCacheFriendly (java:286-346)
+            float total = rows[c.frictionIndex].impulse + rows[c.frictionIndex].pushImpulse;
+            float limit = total * c.friction;
+            if (total > 0.0f) {
+                SolverBody& A = sb[c.bodyA];
+                SolverBody& B = sb[c.bodyB];
+                float vel1Dotn = dot(c.normal, A.linvel) + dot(c.rp1xn, A.angvel);
+                float vel2Dotn = dot(c.normal, B.linvel) + dot(c.rp2xn, B.angvel);
+                float rel_vel = vel1Dotn - vel2Dotn;
+                float j1 = -rel_vel * c.jacDiagABInv;
+                float old = c.impulse;
+                c.impulse = old + j1;
+                if (limit < c.impulse) c.impulse = limit;
+                else if (c.impulse < -limit) c.impulse = -limit;
+                j1 = c.impulse - old;
+                A.apply(scl(c.normal, A.invMass), c.angA, j1);
+                B.apply(scl(c.normal, B.invMass), c.angB, -j1);
+            }
+        }
+    }
+    // write-back (java:901-924): appliedImpulseLateral1 is assigned twice, lateral2 never
+    for (const Row& c : rows) {
+        ManifoldPoint& pt = w.pairMf[c.mfPair].pts[c.mfPoint];
+        pt.appliedImpulse = c.impulse;
+        pt.lat1 = frows[c.frictionIndex].impulse;
+        pt.lat1 = frows[c.frictionIndex + 1].impulse;
+    }
+    for (const SolverBody& s : sb) {
+        if (s.invMass != 0.0f) { w.bodies[s.original].linvel = s.linvel; w.bodies[s.original].angvel = s.angvel; }
+    }
+}
+
+static int island_of(const World& w, int pi) {   // SimulationIslandManager.getIslandId (java:111-117)
+    const Manifold& m = w.pairMf[pi];
+    return w.bodies[m.body0].islandTag >= 0 ? w.bodies[m.body0].islandTag : w.bodies[m.body1].islandTag;
+}
+
+static bool has_rows(const World& w, int pi) {
+    const Manifold& m = w.pairMf[pi];
+    for (int j = 0; j < m.n; j++) if (m.pts[j].distance <= 0.0f) return true;
+    return false;
+}
+
+// Deterministic colouring (the GPU's): rounds of "each dynamic body is claimed by the lowest
+// pair index among uncoloured manifolds touching it; manifolds holding all their claims take
+// the round's colour".  Returns the manifolds ordered by (colour, pair index).
+static std::vector<int> colour_order(World& w, const std::vector<int>& cand, std::vector<int>& colourOut) {
+    std::vector<int> rem(cand), next;
+    std::vector<int> claim(w.bodies.size(), INT_MAX);
+    std::vector<std::pair<int, int>> cm;
+    int round = 0;
+    while (!rem.empty()) {
+        for (int pi : rem) {
+            const Manifold& m = w.pairMf[pi];
+            int bs[2] = {m.body0, m.body1};
+            for (int b : bs) if (w.bodies[b].islandTag >= 0) claim[b] = std::min(claim[b], pi);
+        }
+        next.clear();
+        for (int pi : rem) {
+            const Manifold& m = w.pairMf[pi];
+            bool win = true;
+            int bs[2] = {m.body0, m.body1};
+            for (int b : bs) if (w.bodies[b].islandTag >= 0 && claim[b] != pi) win = false;
+            if (win) cm.push_back(std::make_pair(round, pi));
+            else next.push_back(pi);
+        }
+        for (int pi : rem) {
+            const Manifold& m = w.pairMf[pi];
+            claim[m.body0] = INT_MAX;
+            claim[m.body1] = INT_MAX;
+        }
+        rem.swap(next);
+        round++;
+    }
+    std::sort(cm.begin(), cm.end());
+    std::vector<int> order;
+    colourOut.clear();
+    for (auto& p : cm) { order.push_back(p.second); colourOut.push_back(p.first); }
+    w.counters.colours = round;
+    return order;
+}
+
+// solveConstraints -> buildAndProcessIslands (DiscreteDynamicsWorld.java:620-647; SimulationIslandManager.java:242-333)
+void stage_solve(World& w, float dt) {
+    PhaseTimer pt(w, 6);
+    w.counters.solverRows = 0;
+    w.lastOrder.clear();
+    w.lastColour.clear();
+    if (w.orderMode == ORDER_REFERENCE) {
+        std::vector<int> im = g_islandManifolds;
+        if (im.size() > 1)
+            quick_sort(im, 0, (int)im.size() - 1, [&](int a, int b) { return island_of(w, a) < island_of(w, b) ? -1 : +1; });
+        std::vector<uint8_t> inactive(w.bodies.size(), 0);
+        for (const Body& b : w.bodies) if (b.islandTag >= 0 && !b.isActive()) inactive[b.islandTag] = 1;
+        size_t s = 0;
+        while (s < im.size()) {
+            int isl = island_of(w, im[s]);
+            size_t e = s + 1;
+            while (e < im.size() && island_of(w, im[e]) == isl) e++;
+            if (!inactive[isl]) {
+                std::vector<int> grp(im.begin() + s, im.begin() + e);
+                solve_group(w, grp, dt);
+                for (int k : grp) if (has_rows(w, k)) w.lastOrder.push_back(k);
+            }
+            s = e;
+        }
+        w.counters.colours = 0;
+    } else {
+        std::vector<int> order;
+        if (w.orderMode == ORDER_EXPLICIT) {
+            order = w.explicitOrder;
+        } else {
+            std::vector<int> cand;
+            for (int k : w.solveList) if (has_rows(w, k)) cand.push_back(k);
+            order = colour_order(w, cand, w.lastColour);
+        }
+        solve_group(w, order, dt);
+        w.lastOrder = order;
+    }
+    w.counters.solverManifolds = (int)w.lastOrder.size();
+}
+
+// integrateTransforms (dynamics/DiscreteDynamicsWorld.java:679-739), CCD off
+void stage_integrate(World& w, float dt) {
+    PhaseTimer pt(w, 7);
+    for (Body& b : w.bodies) {
+        if (b.isActive() && !b.isStaticOrKinematic()) {
+            Xf p = integrate_transform(b.xf, b.linvel, b.angvel, dt);
+            b.xf = p;                  // RigidBody.setCenterOfMassTransform
+            update_inertia_tensor(b);
+        }
+    }
+}
+
+// updateActivationState (dynamics/DiscreteDynamicsWorld.java:475-512) with
+// RigidBody.updateDeactivation / wantsSleeping (dynamics/RigidBody.java:543-576)
+void stage_activation(World& w, float dt) {
+    PhaseTimer pt(w, 8);
+    for (Body& b : w.bodies) {
+        if (!(b.activation == ISLAND_SLEEPING || b.activation == DISABLE_DEACTIVATION)) {
+            if (len2(b.linvel) < b.linSleep * b.linSleep && len2(b.angvel) < b.angSleep * b.angSleep) {
+                b.deactivationTime += dt;
+            } else {
+                b.deactivationTime = 0.0f;
+                b.setActivationState(0);
+            }
+        }
+        bool wants;
+        if (b.activation == DISABLE_DEACTIVATION) wants = false;
+        else if (w.cfg.disableDeactivation || w.cfg.deactivationTime == 0.0f) wants = false;
+        else if (b.activation == ISLAND_SLEEPING || b.activation == WANTS_DEACTIVATION) wants = true;
+        else wants = b.deactivationTime > w.cfg.deactivationTime;
+        if (wants) {
+            if (b.isStaticOrKinematic()) {
+                b.setActivationState(ISLAND_SLEEPING);
+            } else {
+                if (b.activation == ACTIVE_TAG) b.setActivationState(WANTS_DEACTIVATION);
+                if (b.activation == ISLAND_SLEEPING) { b.angvel = v3(0, 0, 0); b.linvel = v3(0, 0, 0); }
+            }
+        } else {
+            if (b.activation != DISABLE_DEACTIVATION) b.setActivationState(ACTIVE_TAG);
+        }
+    }
+}
+
+void stage_clear_forces(World& w) {   // DiscreteDynamicsWorld.clearForces (java:226-236)
+    for (Body& b : w.bodies) { b.totalForce = v3(0, 0, 0); b.totalTorque = v3(0, 0, 0); }
+}
+
+// internalSingleStepSimulation (dynamics/DiscreteDynamicsWorld.java:356-400)
+void internal_single_step(World& w, float dt) {
+    stage_predict(w, dt);
+    stage_aabbs(w);
+    stage_pairs(w);
+    stage_narrowphase(w);
+    stage_islands(w);
+    stage_solve(w, dt);
+    stage_integrate(w, dt);
+    stage_activation(w, dt);
+    w.counters.steps++;
+}
+
+// stepSimulation (dynamics/DiscreteDynamicsWorld.java:290-354)
+int step_simulation(World& w, float timeStep, int maxSubSteps, float fixedTimeStep) {
+    int num = 0;
+    if (maxSubSteps != 0) {
+        w.localTime += timeStep;
+        if (w.localTime >= fixedTimeStep) {
+            num = (int)(w.localTime / fixedTimeStep);
+            w.localTime -= num * fixedTimeStep;
+        }
+    } else {
+        fixedTimeStep = timeStep;
+        w.localTime = timeStep;
+        if (std::fabs(timeStep) < FLT_EPS) { num = 0; maxSubSteps = 0; }
+        else { num = 1; maxSubSteps = 1; }
+    }
+    if (num != 0) {
+        stage_apply_gravity(w);
+        int clamped = num > maxSubSteps ? maxSubSteps : num;
+        for (int i = 0; i < clamped; i++) internal_single_step(w, fixedTimeStep);
+    }
+    stage_clear_forces(w);
+    return num;
+}
+
+void step_fixed(World& w, float dt, int substeps) {
+    stage_apply_gravity(w);
+    for (int i = 0; i < substeps; i++) internal_single_step(w, dt);
+    stage_clear_forces(w);
+}
+
+}  // namespace jb

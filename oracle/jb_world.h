@@ -1,0 +1,155 @@
+// ORACLE (test infrastructure only): single-threaded CPU restatement of JBullet's per-step
+// rigid-body pipeline (vbousquet/libgdx-jbullet).  It is the parity checker for the GPU
+// library and the timed CPU baseline; the product never links it.
+// Citations are relative to src/com/bulletphysics/ of the reference.
+#pragma once
+#include <cstdint>
+#include <vector>
+#include "jb_math.h"
+
+namespace jb {
+
+enum ShapeType { BOX = 0, CONVEX_HULL = 4, SPHERE = 6, CAPSULE = 8, STATIC_PLANE = 23 };
+enum ActState { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEACTIVATION = 4, DISABLE_SIMULATION = 5 };
+enum { CF_STATIC_OBJECT = 1, CF_KINEMATIC_OBJECT = 2, CF_NO_CONTACT_RESPONSE = 4 };
+enum { SOLVER_RANDMIZE_ORDER = 1, SOLVER_USE_WARMSTARTING = 4, SOLVER_CACHE_FRIENDLY = 8 };
+
+// collision/shapes/*.java: one record for the five shape classes on the path.
+struct Shape {
+    int type = BOX;
+    float collisionMargin = 0.04f;          // ConvexInternalShape.collisionMargin (BulletGlobals.CONVEX_DISTANCE_MARGIN)
+    V3 implicitDims = {0, 0, 0};            // ConvexInternalShape.implicitShapeDimensions
+    V3 localScaling = {1, 1, 1};
+    int upAxis = 1;                         // CapsuleShape.upAxis
+    std::vector<V3> points;                 // ConvexHullShape.points
+    V3 localAabbMin = {1, 1, 1}, localAabbMax = {-1, -1, -1};  // PolyhedralConvexShape local aabb
+    V3 planeNormal = {0, 1, 0};             // StaticPlaneShape
+    float planeConstant = 0;
+    bool isConvex() const { return type != STATIC_PLANE; }
+    float getMargin() const;                // SphereShape.getMargin returns the radius
+    float capsuleRadius() const { return coord(implicitDims, (upAxis + 2) % 3); }
+    float capsuleHalfHeight() const { return coord(implicitDims, upAxis); }
+};
+
+Shape make_box(V3 halfExtents);
+Shape make_sphere(float radius);
+Shape make_capsule(float radius, float height);
+Shape make_hull(const float* pts, int n);
+Shape make_plane(V3 normal, float constant);
+V3 shape_local_inertia(const Shape& s, float mass);
+void shape_aabb(const Shape& s, const Xf& t, V3& mn, V3& mx);
+V3 support_without_margin(const Shape& s, V3 vec);
+V3 support_with_margin(const Shape& s, V3 vec);
+
+struct ManifoldPoint {   // collision/narrowphase/ManifoldPoint.java:36-62
+    V3 localA{0, 0, 0}, localB{0, 0, 0}, worldA{0, 0, 0}, worldB{0, 0, 0}, normal{0, 0, 0};
+    float distance = 0, friction = 0, restitution = 0;
+    float appliedImpulse = 0, lat1 = 0, lat2 = 0;
+    bool latInit = false;
+    int lifeTime = 0;
+    V3 latDir1{0, 0, 0}, latDir2{0, 0, 0};
+};
+
+struct Manifold {        // collision/narrowphase/PersistentManifold.java
+    int body0 = -1, body1 = -1;
+    int n = 0;
+    ManifoldPoint pts[4];
+};
+
+struct Body {            // dynamics/RigidBody.java + collision/dispatch/CollisionObject.java
+    Xf xf;
+    V3 linvel{0, 0, 0}, angvel{0, 0, 0};
+    float invMass = 0;
+    V3 invInertiaLocal{0, 0, 0};
+    M3 invInertiaWorld;
+    V3 gravity{0, 0, 0}, totalForce{0, 0, 0}, totalTorque{0, 0, 0};
+    V3 linearFactor{1, 1, 1}, angularFactor{1, 1, 1};
+    float linearDamping = 0, angularDamping = 0;
+    float linSleep = 0.8f, angSleep = 1.0f;
+    float friction = 0.5f, restitution = 0;
+    int flags = 0;
+    int activation = ACTIVE_TAG;
+    float deactivationTime = 0;
+    int islandTag = -1, companionId = -1;
+    int shape = -1;
+    int group = 1, mask = -1;
+    int world = 0;                          // batch world index: bodies of different worlds never pair
+    V3 aabbMin{0, 0, 0}, aabbMax{0, 0, 0};  // broadphase proxy aabb
+    bool isStaticOrKinematic() const { return (flags & (CF_STATIC_OBJECT | CF_KINEMATIC_OBJECT)) != 0; }
+    bool isStatic() const { return (flags & CF_STATIC_OBJECT) != 0; }
+    bool isKinematic() const { return (flags & CF_KINEMATIC_OBJECT) != 0; }
+    bool isActive() const { return activation != ISLAND_SLEEPING && activation != DISABLE_SIMULATION; }
+    bool mergesIslands() const { return (flags & (CF_STATIC_OBJECT | CF_KINEMATIC_OBJECT | CF_NO_CONTACT_RESPONSE)) == 0; }
+    bool hasContactResponse() const { return (flags & CF_NO_CONTACT_RESPONSE) == 0; }
+    void setActivationState(int s) { if (activation != DISABLE_DEACTIVATION && activation != DISABLE_SIMULATION) activation = s; }
+};
+
+struct Config {
+    V3 gravity{0, -10, 0};
+    float contactBreakingThreshold = 0.02f;
+    float deactivationTime = 2.0f;
+    bool disableDeactivation = false;
+    int numIterations = 10;
+    float erp = 0.2f, warmstartingFactor = 0.85f, linearSlop = 0.0f;
+    int solverMode = SOLVER_CACHE_FRIENDLY | SOLVER_USE_WARMSTARTING;
+};
+
+struct Counters {
+    long long steps = 0;
+    int pairs = 0, manifolds = 0, contacts = 0, solverManifolds = 0, solverRows = 0, colours = 0, islands = 0;
+    int gjk = 0, epa = 0;
+};
+
+// Solver order policy (the reference's F8 hook, SequentialImpulseConstraintSolver.java:769-779):
+//  ORDER_REFERENCE: manifolds quick-sorted by island exactly as SimulationIslandManager does,
+//                   islands solved one after the other (dispatcher order stands in for the
+//                   reference's hash-dependent manifold creation order: ascending pair key);
+//  ORDER_COLOUR:    the GPU's deterministic colour order (colour-major, pair index minor),
+//                   all islands in one group (equivalent because islands share no body);
+//  ORDER_EXPLICIT:  a caller-provided list of pair indices.
+enum { ORDER_REFERENCE = 0, ORDER_COLOUR = 1, ORDER_EXPLICIT = 2 };
+
+struct World {
+    Config cfg;
+    std::vector<Shape> shapes;
+    std::vector<Body> bodies;
+    // overlapping pairs sorted by canonical key, each owning its algorithm/manifold state
+    std::vector<uint64_t> pairKeys;
+    std::vector<uint8_t> pairHasAlgo;
+    std::vector<Manifold> pairMf;
+    float localTime = 1.0f / 60.0f;       // DiscreteDynamicsWorld.localTime
+    int orderMode = ORDER_COLOUR;
+    std::vector<int> explicitOrder;
+    std::vector<int> solveList;           // pair indices of islandmanifold (after ISLANDS stage)
+    std::vector<int> lastOrder;           // pair indices in the order the last solve used
+    std::vector<int> lastColour;          // colour per entry of lastOrder (ORDER_COLOUR)
+    bool bruteForcePairs = false;         // SimpleBroadphase-style O(n^2) pair search
+    Counters counters;
+    double phaseSeconds[10] = {0};        // CProfile-like per-phase timers
+};
+
+uint64_t pair_key(const World& w, int a, int b);
+void stage_apply_gravity(World& w);
+void stage_predict(World& w, float dt);
+void stage_aabbs(World& w);
+void stage_pairs(World& w);
+void stage_narrowphase(World& w);
+void stage_islands(World& w);
+void stage_solve(World& w, float dt);
+void stage_integrate(World& w, float dt);
+void stage_activation(World& w, float dt);
+void stage_clear_forces(World& w);
+void internal_single_step(World& w, float dt);
+int step_simulation(World& w, float timeStep, int maxSubSteps, float fixedTimeStep);
+void step_fixed(World& w, float dt, int substeps);
+int add_body(World& w, float mass, int shape, const Xf& xf, V3 localInertia, float linDamp, float angDamp,
+             float friction, float restitution, float linSleep, float angSleep, V3 linvel, V3 angvel, int group, int mask,
+             int world = 0);
+
+// narrowphase entry (collision/dispatch/DefaultNearCallback.java:39-66 for one pair)
+void process_pair(World& w, int pairIndex);
+// GJK/EPA closest points between two convex bodies (GjkPairDetector.getClosestPoints), exposed for tests.
+struct GjkOut { bool valid; V3 normal; V3 pointOnB; float distance; int usedEpa; };
+GjkOut gjk_closest_points(const Shape& sa, const Xf& ta, const Shape& sb, const Xf& tb, float maxDist2);
+
+}  // namespace jb

@@ -1,0 +1,176 @@
+"""ORACLE (test infrastructure only): ctypes wrapper over oracle/_build/liboracle.so, the
+single-threaded CPU restatement of the reference's step.  Imported by tests/, by
+__graft_entry__.smoke() and by bench.py's CPU-baseline leg; never by the product."""
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_REPO = os.path.dirname(_HERE)
+sys.path.insert(0, os.path.join(_REPO, "libgdx-jbullet_gb300"))
+from jbgpu import _abi  # noqa: E402
+
+LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+ORDER_REFERENCE, ORDER_COLOUR, ORDER_EXPLICIT = 0, 1, 2
+_lib = None
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-j8"], cwd=_HERE)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [C.POINTER(_abi.Config)]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_add_shape.argtypes = [C.c_void_p, C.POINTER(_abi.ShapeDesc)]
+        L.orc_add_bodies.argtypes = [C.c_void_p, C.POINTER(_abi.BodyDesc), C.c_int]
+        L.orc_step_simulation.argtypes = [C.c_void_p, C.c_float, C.c_int, C.c_float]
+        L.orc_step.argtypes = [C.c_void_p, C.c_float, C.c_int]
+        L.orc_stage.argtypes = [C.c_void_p, C.c_int, C.c_float]
+        L.orc_set_order_mode.argtypes = [C.c_void_p, C.c_int]
+        L.orc_set_explicit_order.argtypes = [C.c_void_p, _abi.i32p, C.c_int]
+        L.orc_set_brute_force.argtypes = [C.c_void_p, C.c_int]
+        L.orc_num_bodies.argtypes = [C.c_void_p]
+        L.orc_get_state.argtypes = [C.c_void_p, C.POINTER(_abi.State)]
+        L.orc_set_state.argtypes = [C.c_void_p, C.POINTER(_abi.State)]
+        L.orc_get_manifolds.argtypes = [C.c_void_p, C.POINTER(_abi.Manifolds)]
+        L.orc_set_manifolds.argtypes = [C.c_void_p, C.POINTER(_abi.Manifolds)]
+        L.orc_get_solver_order.argtypes = [C.c_void_p, _abi.i32p, C.c_int]
+        L.orc_counters.argtypes = [C.c_void_p, C.POINTER(_abi.Counters)]
+        L.orc_phase_seconds.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+        L.orc_shape_local_inertia.argtypes = [C.POINTER(_abi.ShapeDesc), C.c_float, _abi.f32p]
+        L.orc_gjk.argtypes = [C.POINTER(_abi.ShapeDesc), _abi.f32p, C.POINTER(_abi.ShapeDesc), _abi.f32p, C.c_float, _abi.f32p]
+        L.orc_integrate_transform.argtypes = [_abi.f32p, _abi.f32p, _abi.f32p, C.c_float, _abi.f32p]
+        _lib = L
+    return _lib
+
+
+def _fp(a):
+    return a.ctypes.data_as(_abi.f32p)
+
+
+class OracleWorld:
+    def __init__(self, scene=None, config=None, order_mode=ORDER_COLOUR):
+        cfg = config if config is not None else _abi.default_config(**(scene.config if scene else {}))
+        self._cfg = cfg
+        self.h = lib().orc_create(C.byref(cfg))
+        self.set_order_mode(order_mode)
+        if scene is not None:
+            self.add_scene(scene)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def add_scene(self, scene):
+        descs = scene.shape_descs()
+        for i in range(len(descs)):
+            lib().orc_add_shape(self.h, C.byref(descs[i]))
+        b, ptr = scene.body_descs_ptr()
+        lib().orc_add_bodies(self.h, ptr, len(b))
+
+    @property
+    def n_bodies(self):
+        return lib().orc_num_bodies(self.h)
+
+    def set_order_mode(self, mode):
+        lib().orc_set_order_mode(self.h, mode)
+
+    def set_explicit_order(self, order):
+        o = np.ascontiguousarray(order, np.int32)
+        lib().orc_set_explicit_order(self.h, o.ctypes.data_as(_abi.i32p), len(o))
+        self.set_order_mode(ORDER_EXPLICIT)
+
+    def set_brute_force_pairs(self, on=True):
+        lib().orc_set_brute_force(self.h, 1 if on else 0)
+
+    def step(self, dt, substeps=1):
+        lib().orc_step(self.h, dt, substeps)
+
+    def step_simulation(self, time_step, max_sub_steps=1, fixed_time_step=1.0 / 60.0):
+        return lib().orc_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step)
+
+    def stage(self, stage, dt=1.0 / 60.0):
+        lib().orc_stage(self.h, stage, dt)
+
+    def get_state(self):
+        sb = _abi.StateBuffers(self.n_bodies)
+        lib().orc_get_state(self.h, C.byref(sb.struct))
+        return sb.copy_arrays()
+
+    def set_state(self, arrays):
+        arrays = {k: v for k, v in arrays.items() if k != "island_tag"}
+        sb = _abi.StateBuffers.from_arrays(arrays)
+        rc = lib().orc_set_state(self.h, C.byref(sb.struct))
+        assert rc == 0, rc
+
+    def get_manifolds(self):
+        cap = 1024
+        while True:
+            mb = _abi.ManifoldBuffers(cap)
+            rc = lib().orc_get_manifolds(self.h, C.byref(mb.struct))
+            if rc == 0:
+                return mb.view()
+            cap = mb.struct.n_pairs + 16
+
+    def set_manifolds(self, m):
+        mb = _abi.ManifoldBuffers.from_arrays(m["keys"], m["flags"], m["num_points"], m["points"])
+        lib().orc_set_manifolds(self.h, C.byref(mb.struct))
+
+    def get_pairs(self):
+        return self.get_manifolds()["keys"]
+
+    def solver_order(self):
+        cap = max(16, self.counters()["pairs"] + 16)
+        out = np.zeros(cap, np.int32)
+        n = lib().orc_get_solver_order(self.h, out.ctypes.data_as(_abi.i32p), cap)
+        return out[:n].copy()
+
+    def counters(self):
+        c = _abi.Counters()
+        lib().orc_counters(self.h, C.byref(c))
+        return c.as_dict()
+
+    def phase_seconds(self):
+        out = (C.c_double * 10)()
+        lib().orc_phase_seconds(self.h, out)
+        return list(out)
+
+
+def shape_local_inertia(shape_dict, mass):
+    from jbgpu.scenes import Scene
+    sc = Scene("one", 0, 0, {}, [shape_dict], np.zeros(0))
+    d = sc.shape_descs()
+    out = np.zeros(3, np.float32)
+    lib().orc_shape_local_inertia(C.byref(d[0]), mass, _fp(out))
+    return out
+
+
+def gjk(shape_a, xf_a, shape_b, xf_b, max_dist2):
+    from jbgpu.scenes import Scene
+    sc = Scene("two", 0, 0, {}, [shape_a, shape_b], np.zeros(0))
+    d = sc.shape_descs()
+    ta = np.ascontiguousarray(xf_a, np.float32)
+    tb = np.ascontiguousarray(xf_b, np.float32)
+    out = np.zeros(9, np.float32)
+    lib().orc_gjk(C.byref(d[0]), _fp(ta), C.byref(d[1]), _fp(tb), max_dist2, _fp(out))
+    return out
+
+
+def integrate_transform(t12, lin, ang, dt):
+    t = np.ascontiguousarray(t12, np.float32)
+    l = np.ascontiguousarray(lin, np.float32)
+    a = np.ascontiguousarray(ang, np.float32)
+    out = np.zeros(12, np.float32)
+    lib().orc_integrate_transform(_fp(t), _fp(l), _fp(a), dt, _fp(out))
+    return out
