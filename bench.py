@@ -1,0 +1,364 @@
+#!/usr/bin/env python
+"""Benchmark of the GPU rigid-body step (JBullet's stepSimulation pipeline) on one GB300.
+
+Workload (default): 100,000 bodies (40% spheres, 40% boxes, 20% capsules) dropped on a static
+plane, dt = 1/120, 10 PGS iterations; a "step" is one internal single step of the whole
+pipeline (gravity, predict, aabbs, pairs, narrowphase, islands, solver, integrate,
+activation) over all bodies.  Metric: body-steps/s.
+
+  value  device-timed throughput: W warm-up steps, then K steps through jbgpu_world_step with
+         the world resident in HBM (per-step working set of bodies, pairs, manifolds and solver
+         rows exceeds the 129 MB L2; no separate flush).
+  e2e    the same K steps from a fresh world through the reference-facing call
+         jbgpu_world_step_simulation, each step with a host->device upload of per-body forces
+         (RigidBody.applyCentralForce) and a device->host read of all body transforms
+         (MotionState synchronisation), both from pinned host memory.
+  roofline  the phase with the largest device time (CUDA events on the world's stream),
+         algorithmic bytes from the per-step counters / measured phase time vs the measured
+         HBM copy bandwidth.
+  cpu_baseline  the CPU restatement of the reference (oracle, one core, the reference's island
+         solver order) timed on windows of the same trajectory: GPU snapshots at steps
+         0, K/2 and K-window, each continued for --cpu-window steps.
+
+--impl reference times that CPU restatement alone over the same W + K steps from the start.
+Multi-GPU: one process per GPU (torchrun); each rank steps an independent world (weak scaling,
+no collective on the data path); rank 0 prints the line.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "libgdx-jbullet_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "body-steps/s @100k bodies"
+UNIT = "body-steps/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=600)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="mixed_100k")
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--cpu-window", type=int, default=10)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self):
+        self.rank, self.size, self.local = dist_env()
+        self.pg = None
+        if self.size > 1:
+            import torch.distributed as td
+            td.init_process_group(backend="gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.size > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.size == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if self.size == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.size > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join("/tmp", "jbgpu_clocks_%d_%d.csv" % (os.getpid(), device))
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        sm = np.array([r[0] for r in rows])
+        pw = np.array([r[2] for r in rows])
+        load = sm[pw >= np.median(pw)] if len(rows) > 2 else sm
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median(load)), "sm_max_mhz": float(max(r[1] for r in rows)), "reasons": reasons,
+                "samples": len(rows), "power_w_max": float(pw.max())}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+# Algorithmic bytes per step of each phase: the per-unit figures of the step's data movement
+# (per body: predict 112, aabb 80, morton 40 + radix 64 + tree build/refit 150 + traversal 32,
+# integrate 150; per pair: key write 8 + persistence 32; per executed pair: two body states
+# 96 + manifold read/write 512; per contact: setup 400, write-back 12; per solver row and
+# iteration: 64 B row + 8 B impulse + 2 x 48 B body velocities = 168, three rows per contact).
+def phase_bytes(phase, c, bodies, iters):
+    rows = c["solver_rows"]
+    return {
+        "predict": 112 * bodies,
+        "aabb": 80 * bodies,
+        "pair_count": (40 + 64 + 150 + 32) * bodies,
+        "pair_fill": 40 * c["pairs"] + 32 * bodies,
+        "narrow_gjk": (96 + 512) * c["pairs"],
+        "narrow_epa": (96 + 512) * c["epa_calls"],
+        "setup": 400 * rows,
+        "pgs": (iters + 1) * 3 * rows * 168 + 12 * rows,
+        "integrate": 150 * bodies,
+        "activation": 48 * bodies,
+    }.get(phase)
+
+
+def make_scene(name, seed):
+    from jbgpu import scenes
+    return scenes.SCENES[name](seed=seed)
+
+
+def pinned(shape):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()
+    except Exception:
+        pass
+    return np.zeros(shape, np.float32)
+
+
+def run_cpu_baseline(scene, world_cls, snap_steps, window):
+    """Oracle (reference island order, 1 core) continued for `window` steps from GPU snapshots."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    from jbgpu import _abi
+    g = world_cls(scene)
+    o = pyoracle.OracleWorld(scene, order_mode=pyoracle.ORDER_REFERENCE)
+    done, total_t, total_steps = 0, 0.0, 0
+    for s in sorted(set(snap_steps)):
+        while done < s:
+            g.step(scene.dt)
+            done += 1
+        st = g.get_state()
+        o.set_state({k: st[k] for k in ("transform", "linear_velocity", "angular_velocity", "inv_inertia_world",
+                                         "total_force", "total_torque", "aabb", "activation_state", "deactivation_time")})
+        o.set_manifolds(g.get_manifolds())
+        t0 = time.perf_counter()
+        for _ in range(window):
+            o.step(scene.dt)
+        total_t += time.perf_counter() - t0
+        total_steps += window
+    g.close()
+    value = scene.n_bodies * total_steps / total_t
+    return {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "CPU restatement of the reference (oracle, 1 thread, reference island solver order): %d-step windows "
+                      "from GPU snapshots at steps %s of the %s trajectory, %.1f s of CPU work" % (
+                          window, sorted(set(snap_steps)), scene.name, total_t)}
+
+
+def run_ours(args, dist):
+    from jbgpu import _abi, _build, lib
+    from jbgpu.lib import GpuWorld
+    _build.build()
+    sc = make_scene(args.workload, args.seed + dist.rank)
+    cfg = _abi.default_config(**sc.config)
+    cfg.device = dist.local
+    iters = cfg.num_iterations
+    n = sc.n_bodies
+    K, W = args.steps, args.warmup
+    # ---- device-timed run -----------------------------------------------------------------
+    w = GpuWorld(sc, config=cfg)
+    for _ in range(W):
+        w.step(sc.dt)
+    w.set_profiling(K)
+    clk = ClockSampler(dist.local)
+    clk.start()
+    dist.barrier()
+    w.synchronize()
+    l0 = lib.launch_count()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        w.step(sc.dt)
+    w.synchronize()
+    t1 = time.perf_counter()
+    launches = lib.launch_count() - l0
+    dist.barrier()
+    clocks = clk.stop()
+    phases, nsteps, window_ms = w.phase_times()
+    ctrs = w.profile_counters()
+    final = w.counters()
+    w.close()
+    wall = t1 - t0
+    elapsed = dist.max(wall)
+    total_body_steps = dist.sum(n * K)
+    value = total_body_steps / elapsed
+    # ---- roofline of the dominant phase ----------------------------------------------------
+    dom = max(phases, key=lambda k: phases[k])
+    pk = peaks()
+    roof = None
+    side = {}
+    for ph, ms in phases.items():
+        by = [phase_bytes(ph, c, n, iters) for c in ctrs]
+        if by and by[0] is not None and ms > 0:
+            side[ph] = {"ms_per_step": ms / nsteps, "GB_per_s": sum(by) / (ms * 1e-3) / 1e9}
+        else:
+            side[ph] = {"ms_per_step": ms / nsteps}
+    by = [phase_bytes(dom, c, n, iters) for c in ctrs]
+    if by and by[0] is not None:
+        achieved = sum(by) / (phases[dom] * 1e-3) / 1e9
+        peak = pk["hbm_gbs"] if pk else 6800.0
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "traffic.json")
+        if os.path.exists(tp):
+            traffic = json.load(open(tp)).get(dom)
+        roof = {"bound": "hbm", "kernel_phase": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": sum(by) / len(by)}
+    # ---- end to end through the reference-facing call with host buffers --------------------
+    e2e = None
+    if not args.no_e2e:
+        w = GpuWorld(sc, config=cfg)
+        force = pinned((n, 3))
+        xout = pinned((n, 12))
+        for _ in range(W):
+            w.step(sc.dt)
+        dist.barrier()
+        w.synchronize()
+        ts = time.perf_counter()
+        sub = 0
+        for _ in range(K):
+            w.apply_forces(force, None)
+            sub += w.step_simulation(sc.dt, 1, sc.dt)
+            w.get_transforms(xout)
+        te = time.perf_counter()
+        dist.barrier()
+        w.close()
+        e_el = dist.max(te - ts)
+        e2e = {"value": dist.sum(n * sub) / e_el, "unit": UNIT, "h2d_bytes_per_step": int(force.nbytes),
+               "d2h_bytes_per_step": int(xout.nbytes), "substeps": sub}
+    # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------------------------
+    cpu = None
+    if dist.rank == 0 and dist.size == 1 and not args.no_cpu:
+        total = W + K
+        snaps = [0, total // 2, max(0, total - args.cpu_window)]
+        cpu = run_cpu_baseline(sc, GpuWorld, snaps, args.cpu_window)
+    last = ctrs[-1] if ctrs else final
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.size, "steps": K, "warmup": W,
+        "ms_per_step": elapsed * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: seeded PCG64 scene generator (no dataset exists for this workload)",
+        "config": {"workload": sc.name, "bodies": n, "dt": sc.dt, "iterations": iters, "warmup_steps_from_rest": W,
+                   "timed_steps": "%d..%d of the drop" % (W, W + K - 1), "parallelism": "independent world per GPU",
+                   "l2": "no flush: per-step working set (bodies, two pair/manifold buffers, solver rows) exceeds L2",
+                   "last_step_counters": {k: last[k] for k in ("pairs", "contacts", "solver_manifolds", "solver_rows",
+                                                               "colours", "islands", "gjk_calls", "epa_calls")}},
+        "device_window_ms": window_ms,
+        "gpu_launches": int(launches),
+        "phases": side,
+        "roofline": roof,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "status_flags": final["status_flags"],
+    }
+    return out
+
+
+def run_reference(args, dist):
+    """The reference's CPU path (restated, 1 thread) on the same workload and steps."""
+    if dist.rank != 0:
+        return None
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    pyoracle.build()
+    sc = make_scene(args.workload, args.seed)
+    o = pyoracle.OracleWorld(sc, order_mode=pyoracle.ORDER_REFERENCE)
+    for _ in range(args.warmup):
+        o.step(sc.dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(sc.dt)
+    el = time.perf_counter() - t0
+    value = sc.n_bodies * args.steps / el
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.size, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded PCG64 scene generator",
+            "config": {"workload": sc.name, "bodies": sc.n_bodies, "dt": sc.dt},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": "CPU restatement of the reference (no JVM on this machine), 1 thread, full "
+                                       "workload, steps %d..%d from rest" % (args.warmup, args.warmup + args.steps - 1)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    out = run_reference(args, dist) if args.impl == "reference" else run_ours(args, dist)
+    if dist.rank == 0 and out is not None:
+        print(json.dumps(out))
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

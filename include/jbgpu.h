@@ -192,6 +192,7 @@ typedef struct jbgpu_counters {
 
 /* ---- library -------------------------------------------------------------------- */
 const char* jbgpu_version(void);
+int64_t     jbgpu_launch_count(void);        /* kernels this library has launched in the process */
 const char* jbgpu_last_error(void);          /* thread-local message for the last failure */
 void        jbgpu_config_default(jbgpu_config* cfg);
 
@@ -229,6 +230,28 @@ int jbgpu_world_set_manifolds(jbgpu_world* world, const jbgpu_manifolds* m);
  * phases are equivalent to (the order fed to the reference solver for parity). */
 int jbgpu_world_get_solver_order(jbgpu_world* world, int32_t* pair_index, int32_t capacity, int32_t* n);
 int jbgpu_world_counters(jbgpu_world* world, jbgpu_counters* counters);
+
+/* RigidBody.applyCentralForce / applyTorque for every body (dynamics/RigidBody.java:362-376):
+ * adds n_bodies * 3 floats of force and torque (either may be NULL) read from host memory
+ * (pinned memory makes the copy asynchronous) to the accumulators cleared by clearForces. */
+int jbgpu_world_apply_forces(jbgpu_world* world, const float* force, const float* torque);
+/* Copies the n_bodies * 12 floats of body transforms (basis row-major, origin) to host memory;
+ * the transform part of jbgpu_world_get_state, for MotionState synchronisation. */
+int jbgpu_world_get_transforms(jbgpu_world* world, float* transforms);
+
+/* Per-phase device timing with CUDA events on the world's stream (profiling builds the
+ * reference's CProfileManager table, linearmath/CProfileManager.java:41-100).  Phases:
+ * 0 predict, 1 aabb, 2 pair count (bounds, morton, sort, tree, count, scan), 3 pair fill
+ * (fill, sort, persist), 4 narrowphase GJK pass, 5 EPA pass, 6 islands, 7 colouring,
+ * 8 solver setup, 9 PGS, 10 integrate, 11 activation, 12 gravity + clear forces. */
+#define JBGPU_NUM_PHASES 13
+int jbgpu_world_set_profiling(jbgpu_world* world, int32_t max_steps);   /* 0 turns it off */
+/* Sum of each phase's device milliseconds over the profiled steps so far (waits for them).
+ * With n_phases > JBGPU_NUM_PHASES, ms[JBGPU_NUM_PHASES] receives the device time of the whole
+ * profiled window (first phase mark of the first step to the last mark of the last step). */
+int jbgpu_world_phase_times(jbgpu_world* world, double* ms, int32_t n_phases, int32_t* steps);
+/* The step counters of each profiled step (pairs, contacts, solver rows, ...). */
+int jbgpu_world_profile_counters(jbgpu_world* world, jbgpu_counters* per_step, int32_t capacity, int32_t* steps);
 
 #ifdef __cplusplus
 }

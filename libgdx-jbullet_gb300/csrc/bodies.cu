@@ -128,22 +128,22 @@ __global__ void k_clear_forces(DevWorld w) {   // DiscreteDynamicsWorld.clearFor
 }
 
 void launch_apply_gravity(const DevWorld& w, cudaStream_t s) {
-    if (w.nBodies) k_apply_gravity<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w);
+    if (w.nBodies) { k_apply_gravity<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w); note_launch(); }
 }
 void launch_predict(const DevWorld& w, float dt, cudaStream_t s) {
-    if (w.nBodies) k_predict<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, dt);
+    if (w.nBodies) { k_predict<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, dt); note_launch(); }
 }
 void launch_aabb(const DevWorld& w, cudaStream_t s) {
-    if (w.nBodies) k_aabb<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w);
+    if (w.nBodies) { k_aabb<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w); note_launch(); }
 }
 void launch_integrate(const DevWorld& w, float dt, cudaStream_t s) {
-    if (w.nBodies) k_integrate<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, dt);
+    if (w.nBodies) { k_integrate<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, dt); note_launch(); }
 }
 void launch_activation(const DevWorld& w, float dt, cudaStream_t s) {
-    if (w.nBodies) k_activation<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, dt);
+    if (w.nBodies) { k_activation<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, dt); note_launch(); }
 }
 void launch_clear_forces(const DevWorld& w, cudaStream_t s) {
-    if (w.nBodies) k_clear_forces<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w);
+    if (w.nBodies) { k_clear_forces<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w); note_launch(); }
 }
 
 }  // namespace jbg

@@ -290,8 +290,8 @@ void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t
     int n = w.nBodies;
     cudaMemsetAsync(bb.bounds, 0, sizeof(unsigned) * 6, s);
     cudaMemsetAsync(bb.bounds, 0xff, sizeof(unsigned) * 3, s);
-    k_bounds<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds);
-    k_morton<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds, bb.mkeys, bb.sortedBody);
+    k_bounds<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds); note_launch();
+    k_morton<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds, bb.mkeys, bb.sortedBody); note_launch();
     radix_sort_pairs(bb.mkeys, bb.sortedBody, bb.mkeys_alt, bb.vals_alt, n, 32 + bb.worldBits, bb.sortScratch, s);
     int nf = bb.nFinite;
     cudaMemsetAsync(bb.cnt, 0, sizeof(int) * (n + 1), s);
@@ -299,19 +299,19 @@ void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t
         cudaMemsetAsync(bb.wstart, 0xff, sizeof(int) * bb.nWorlds, s);
         cudaMemsetAsync(bb.wend, 0xff, sizeof(int) * bb.nWorlds, s);
         cudaMemsetAsync(bb.wroot, 0xff, sizeof(int) * bb.nWorlds, s);
-        k_world_ranges<<<gridn(nf, 256), 256, 0, s>>>(bb.mkeys, nf, bb.wstart, bb.wend, bb.wroot);
+        k_world_ranges<<<gridn(nf, 256), 256, 0, s>>>(bb.mkeys, nf, bb.wstart, bb.wend, bb.wroot); note_launch();
         if (nf > 1) {
             cudaMemsetAsync(bb.bvh.visit, 0, sizeof(int) * (nf - 1), s);
             cudaMemsetAsync(bb.bvh.parent, 0xff, sizeof(int) * (nf - 1), s);
-            k_karras<<<gridn(nf - 1, 256), 256, 0, s>>>(bb.mkeys, nf, bb.bvh, bb.wstart, bb.wend, bb.wroot);
-            k_refit<<<gridn(nf, 256), 256, 0, s>>>(w, bb.sortedBody, nf, bb.bvh);
+            k_karras<<<gridn(nf - 1, 256), 256, 0, s>>>(bb.mkeys, nf, bb.bvh, bb.wstart, bb.wend, bb.wroot); note_launch();
+            k_refit<<<gridn(nf, 256), 256, 0, s>>>(w, bb.sortedBody, nf, bb.bvh); note_launch();
             k_traverse<false><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, bb.cnt, nullptr,
-                                                              nullptr, nullptr, 0);
+                                                              nullptr, nullptr, 0); note_launch();
         }
     }
     if (bb.nPlanes > 0)
         k_plane_pairs<false><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, bb.cnt, nullptr, nullptr,
-                                                            nullptr, 0);
+                                                            nullptr, 0); note_launch();
     exclusive_scan(bb.cnt, bb.off, bb.total, n + 1, bb.scanScratch, s);
 }
 
@@ -321,15 +321,15 @@ void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw,
     // counts are recovered from the offsets: cnt[i] = off[i+1] - off[i]
     if (nf > 1)
         k_traverse<true><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, nullptr, bb.off,
-                                                         bb.cursor, bb.partners, capacity);
+                                                         bb.cursor, bb.partners, capacity); note_launch();
     if (bb.nPlanes > 0)
         k_plane_pairs<true><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, nullptr, bb.off, bb.cursor,
-                                                           bb.partners, capacity);
-    k_segment_sort<<<gridn(n, 128), 128, 0, s>>>(n, bb.off, bb.cursor, bb.partners, nw.keys, capacity);
+                                                           bb.partners, capacity); note_launch();
+    k_segment_sort<<<gridn(n, 128), 128, 0, s>>>(n, bb.off, bb.cursor, bb.partners, nw.keys, capacity); note_launch();
 }
 
 void broadphase_persist(const DevWorld& w, DevPairs& nw, const DevPairs& old, int nNew, int nOld, cudaStream_t s) {
-    if (nNew > 0) k_persist<<<gridn(nNew, 256), 256, 0, s>>>(w, nw, old, nNew, nOld);
+    if (nNew > 0) { k_persist<<<gridn(nNew, 256), 256, 0, s>>>(w, nw, old, nNew, nOld); note_launch(); }
 }
 
 }  // namespace jbg

@@ -125,6 +125,23 @@ JBD bool is_static_or_kin(int f) { return (f & (CF_STATIC | CF_KINEMATIC)) != 0;
 JBD bool merges_islands(int f) { return (f & (CF_STATIC | CF_KINEMATIC | CF_NO_CONTACT_RESPONSE)) == 0; }
 JBD int set_activation(int cur, int s) { return (cur != DISABLE_DEACTIVATION && cur != DISABLE_SIMULATION) ? s : cur; }
 
+// ---- per-phase event timing ---------------------------------------------------------------
+enum { PH_PREDICT = 0, PH_AABB, PH_PAIR_COUNT, PH_PAIR_FILL, PH_NARROW, PH_EPA, PH_ISLANDS, PH_COLOUR, PH_SETUP, PH_PGS,
+       PH_INTEGRATE, PH_ACTIVATION, PH_OTHER, NUM_PHASES };
+
+struct Prof {
+    int maxSteps = 0;
+    int step = 0;                 // profiled steps recorded so far
+    cudaEvent_t* ev = nullptr;    // [maxSteps][NUM_PHASES][2]
+    bool active() const { return step < maxSteps && ev != nullptr; }
+    void mark(int phase, int which, cudaStream_t s) const {
+        if (active()) cudaEventRecord(ev[((size_t)step * NUM_PHASES + phase) * 2 + which], s);
+    }
+};
+
+// Counts a kernel launch of this library (process-wide, reported by jbgpu_launch_count).
+void note_launch();
+
 // ---- launchers (one per translation unit) ------------------------------------------------
 struct BroadphaseScratch;   // world.cu owns the buffers; broadphase.cu reads them
 void launch_apply_gravity(const DevWorld& w, cudaStream_t s);

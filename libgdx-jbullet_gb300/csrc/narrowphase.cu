@@ -154,14 +154,18 @@ __global__ void k_narrow_epa(DevWorld w, DevPairs P, const EpaRec* queue, const 
     }
 }
 
-void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s) {
+void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
+                        const Prof* prof) {
+    if (prof) prof->mark(PH_NARROW, 0, s);
     cudaMemsetAsync(nb.queueCount, 0, sizeof(int), s);
-    if (nPairs > 0) k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, (EpaRec*)nb.queue, nb.queueCount);
+    if (nPairs > 0) { k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, (EpaRec*)nb.queue, nb.queueCount); note_launch(); }
+    if (prof) { prof->mark(PH_NARROW, 1, s); prof->mark(PH_EPA, 0, s); }
     EpaArena ar;
     ar.fN = nb.fN; ar.fV = nb.fV; ar.fF = nb.fF; ar.fE = nb.fE;
     ar.mW = nb.mW; ar.mR = nb.mR; ar.seen = nb.seen; ar.stack = nb.stack;
     ar.slots = nb.slots;
-    if (nPairs > 0) k_narrow_epa<<<(nb.slots + 63) / 64, 64, 0, s>>>(w, P, (const EpaRec*)nb.queue, nb.queueCount, ar);
+    if (nPairs > 0) { k_narrow_epa<<<(nb.slots + 63) / 64, 64, 0, s>>>(w, P, (const EpaRec*)nb.queue, nb.queueCount, ar); note_launch(); }
+    if (prof) prof->mark(PH_EPA, 1, s);
 }
 
 size_t epa_queue_record_bytes() { return sizeof(EpaRec); }

@@ -14,6 +14,7 @@ struct NarrowBuffers {
 };
 
 size_t epa_queue_record_bytes();
-void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s);
+void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
+                        const Prof* prof = nullptr);
 
 }  // namespace jbg

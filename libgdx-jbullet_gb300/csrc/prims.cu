@@ -90,9 +90,9 @@ void exclusive_scan(const int* in, int* out, int* total, int n, void* scratch, c
     }
     int tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     int* sums = (int*)scratch;
-    k_scan_tiles<<<tiles, SCAN_BLOCK, 0, s>>>(in, out, sums, n);
-    k_scan_single<<<1, SCAN_BLOCK, 0, s>>>(sums, tiles, total);
-    if (tiles > 1) k_scan_add<<<tiles, 256, 0, s>>>(out, sums, n);
+    k_scan_tiles<<<tiles, SCAN_BLOCK, 0, s>>>(in, out, sums, n); note_launch();
+    k_scan_single<<<1, SCAN_BLOCK, 0, s>>>(sums, tiles, total); note_launch();
+    if (tiles > 1) { k_scan_add<<<tiles, 256, 0, s>>>(out, sums, n); note_launch(); }
 }
 
 // ---- radix sort ---------------------------------------------------------------------------
@@ -160,9 +160,9 @@ void radix_sort_pairs(uint64_t* keys, int* vals, uint64_t* keys_alt, int* vals_a
     int *va = vals, *vb = vals_alt;
     for (int p = 0; p < passes; p++) {
         int shift = 8 * p;
-        k_rs_hist<<<tiles, RS_THREADS, 0, s>>>(ka, n, shift, hist, tiles);
+        k_rs_hist<<<tiles, RS_THREADS, 0, s>>>(ka, n, shift, hist, tiles); note_launch();
         exclusive_scan(hist, hist, nullptr, tiles * RS_BINS, scanScratch, s);
-        k_rs_scatter<<<tiles, RS_THREADS, 0, s>>>(ka, va, kb, vb, n, shift, hist, tiles);
+        k_rs_scatter<<<tiles, RS_THREADS, 0, s>>>(ka, va, kb, vb, n, shift, hist, tiles); note_launch();
         uint64_t* tk = ka; ka = kb; kb = tk;
         int* tv = va; va = vb; vb = tv;
     }

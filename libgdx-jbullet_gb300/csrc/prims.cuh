@@ -7,6 +7,9 @@
 
 namespace jbg {
 
+// Counts a kernel launch of this library (process-wide, reported by jbgpu_launch_count).
+void note_launch();
+
 // Scratch sizes (bytes) for n elements.
 size_t scan_scratch_bytes(int n);
 size_t sort_scratch_bytes(int n);

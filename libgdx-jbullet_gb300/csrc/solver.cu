@@ -130,16 +130,16 @@ __global__ void k_count_manifolds(DevPairs P, int nPairs, int* ctr) {
 
 void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s) {
     int n = w.nBodies;
-    k_uf_init<<<gridn(n, 256), 256, 0, s>>>(n, sb.parent);
-    if (nPairs > 0) k_uf_union<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.parent);
-    k_islands<<<gridn(n, 256), 256, 0, s>>>(w, sb.parent, sb.keepAwake, sb.inactive);
-    k_island_awake<<<gridn(n, 256), 256, 0, s>>>(w, sb.keepAwake);
-    k_island_sleep<<<gridn(n, 256), 256, 0, s>>>(w, sb.keepAwake, sb.inactive);
+    k_uf_init<<<gridn(n, 256), 256, 0, s>>>(n, sb.parent); note_launch();
+    if (nPairs > 0) { k_uf_union<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.parent); note_launch(); }
+    k_islands<<<gridn(n, 256), 256, 0, s>>>(w, sb.parent, sb.keepAwake, sb.inactive); note_launch();
+    k_island_awake<<<gridn(n, 256), 256, 0, s>>>(w, sb.keepAwake); note_launch();
+    k_island_sleep<<<gridn(n, 256), 256, 0, s>>>(w, sb.keepAwake, sb.inactive); note_launch();
     if (nPairs > 0) {
-        k_select<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.inactive, sb.flag);
+        k_select<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.inactive, sb.flag); note_launch();
         exclusive_scan(sb.flag, sb.candIdx, sb.nCand, nPairs, sb.scanScratch, s);
-        k_compact<<<gridn(nPairs, 256), 256, 0, s>>>(nPairs, sb.flag, sb.candIdx, sb.cand);
-        k_count_manifolds<<<gridn(nPairs, 256), 256, 0, s>>>(P, nPairs, w.ctr);
+        k_compact<<<gridn(nPairs, 256), 256, 0, s>>>(nPairs, sb.flag, sb.candIdx, sb.cand); note_launch();
+        k_count_manifolds<<<gridn(nPairs, 256), 256, 0, s>>>(P, nPairs, w.ctr); note_launch();
     } else {
         cudaMemsetAsync(sb.nCand, 0, sizeof(int), s);
     }
@@ -498,22 +498,33 @@ int solver_coop_blocks(bool pgs) {
     return sms * (per < 2 ? per : 2);
 }
 
-void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, SolverBuffers& sb, float dt, cudaStream_t s) {
+void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, SolverBuffers& sb, float dt, cudaStream_t s,
+                  const Prof* prof) {
+    if (prof) prof->mark(PH_COLOUR, 0, s);
     if (nPairs <= 0) {
         cudaMemsetAsync(sb.nColours, 0, sizeof(int), s);
+        if (prof) {
+            prof->mark(PH_COLOUR, 1, s);
+            prof->mark(PH_SETUP, 0, s); prof->mark(PH_SETUP, 1, s);
+            prof->mark(PH_PGS, 0, s); prof->mark(PH_PGS, 1, s);
+        }
         return;
     }
     cudaMemsetAsync(sb.claim, 0xff, sizeof(unsigned long long) * w.nBodies, s);
+    cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
     {
         DevWorld wc = w;
         DevPairs pc = P;
         SolverBuffers sc = sb;
         void* args[] = {&wc, &pc, &sc};
-        cudaLaunchCooperativeKernel((void*)k_colour, sb.coopBlocksColour, 256, args, 0, s);
+        cudaLaunchCooperativeKernel((void*)k_colour, sb.coopBlocksColour, 256, args, 0, s); note_launch();
     }
     cudaMemsetAsync(sb.colourFill, 0, sizeof(int) * (MAX_COLOURS + 1), s);
-    k_slots<<<gridn(nPairs, 256), 256, 0, s>>>(sb, R);
-    k_setup<<<gridn(nPairs, 128), 128, 0, s>>>(w, P, R, sb.nCand, dt);
+    k_slots<<<gridn(nPairs, 256), 256, 0, s>>>(sb, R); note_launch();
+    if (prof) { prof->mark(PH_COLOUR, 1, s); prof->mark(PH_SETUP, 0, s); }
+    k_setup<<<gridn(nPairs, 128), 128, 0, s>>>(w, P, R, sb.nCand, dt); note_launch();
+    if (prof) { prof->mark(PH_SETUP, 1, s); prof->mark(PH_PGS, 0, s); }
+    cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
     {
         DevWorld wc = w;
         DevPairs pc = P;
@@ -522,8 +533,9 @@ void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, Solver
         const int* ncand = sb.nCand;
         float dtc = dt;
         void* args[] = {&wc, &pc, &rc, &ncol, &ncand, &dtc};
-        cudaLaunchCooperativeKernel((void*)k_pgs, sb.coopBlocksPgs, 256, args, 0, s);
+        cudaLaunchCooperativeKernel((void*)k_pgs, sb.coopBlocksPgs, 256, args, 0, s); note_launch();
     }
+    if (prof) prof->mark(PH_PGS, 1, s);
 }
 
 }  // namespace jbg

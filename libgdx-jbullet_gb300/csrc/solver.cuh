@@ -27,7 +27,8 @@ struct SolverBuffers {
 constexpr int MAX_COLOURS = 1024;
 
 void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
-void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& rows, SolverBuffers& sb, float dt, cudaStream_t s);
+void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& rows, SolverBuffers& sb, float dt, cudaStream_t s,
+                  const Prof* prof = nullptr);
 int solver_coop_blocks(bool pgs);
 
 }  // namespace jbg

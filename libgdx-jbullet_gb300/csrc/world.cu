@@ -24,6 +24,10 @@ using namespace jbg;
 static thread_local std::string g_err;
 static int fail(int code, const std::string& msg) { g_err = msg; return code; }
 
+#include <atomic>
+static std::atomic<long long> g_launches{0};
+void jbg::note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 #define CK(call)                                                                                     \
     do {                                                                                             \
         cudaError_t e_ = (call);                                                                     \
@@ -92,6 +96,10 @@ struct jbgpu_world {
     NarrowBuffers nb;
     SolverBuffers sb;
     int* hostPinned = nullptr;
+    Prof prof;
+    int* profHist = nullptr;      // per profiled step: device counters + solver manifolds
+    float* ioStage = nullptr;     // device staging for apply_forces / get_transforms (12 floats per body)
+    int capIo = 0;
 };
 
 namespace {
@@ -287,15 +295,19 @@ int check_status(jbgpu_world* w) {
 int stage_pairs(jbgpu_world* w) {
     DevWorld d = dev_view(w);
     cudaStream_t s = w->stream;
+    w->prof.mark(PH_PAIR_COUNT, 0, s);
     broadphase_run_count(d, w->bb, s);
+    w->prof.mark(PH_PAIR_COUNT, 1, s);
     CK(cudaMemcpyAsync(w->hostPinned, w->bb.total, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     int total = *w->hostPinned;
     int nxt = w->cur ^ 1;
     int rc = ensure_pair_capacity(w, nxt, total);
     if (rc) return rc;
+    w->prof.mark(PH_PAIR_FILL, 0, s);
     broadphase_run_fill(d, w->bb, w->pairs[nxt], w->capRows, s);
     broadphase_persist(d, w->pairs[nxt], w->pairs[w->cur], total, w->nPairs, s);
+    w->prof.mark(PH_PAIR_FILL, 1, s);
     w->cur = nxt;
     w->nPairs = total;
     CK(cudaMemcpyAsync(w->dw.ctr + C_PAIRS, w->bb.total, sizeof(int), cudaMemcpyDeviceToDevice, s));
@@ -305,25 +317,28 @@ int stage_pairs(jbgpu_world* w) {
 int run_stage(jbgpu_world* w, int stage, float dt) {
     cudaStream_t s = w->stream;
     DevWorld d = dev_view(w);
+    const Prof& P = w->prof;
     switch (stage) {
-    case JBGPU_STAGE_APPLY_GRAVITY: launch_apply_gravity(d, s); break;
-    case JBGPU_STAGE_PREDICT: launch_predict(d, dt, s); break;
-    case JBGPU_STAGE_AABB: launch_aabb(d, s); break;
+    case JBGPU_STAGE_APPLY_GRAVITY: P.mark(PH_OTHER, 0, s); launch_apply_gravity(d, s); P.mark(PH_OTHER, 1, s); break;
+    case JBGPU_STAGE_PREDICT: P.mark(PH_PREDICT, 0, s); launch_predict(d, dt, s); P.mark(PH_PREDICT, 1, s); break;
+    case JBGPU_STAGE_AABB: P.mark(PH_AABB, 0, s); launch_aabb(d, s); P.mark(PH_AABB, 1, s); break;
     case JBGPU_STAGE_PAIRS: { int rc = stage_pairs(w); if (rc) return rc; break; }
     case JBGPU_STAGE_NARROWPHASE:
         CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
-        narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s);
+        narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s, &P);
         break;
     case JBGPU_STAGE_ISLANDS:
+        P.mark(PH_ISLANDS, 0, s);
         CK(cudaMemsetAsync(w->dw.ctr + C_ISLANDS, 0, sizeof(int) * 4, s));
         islands_launch(d, w->pairs[w->cur], w->nPairs, w->sb, s);
+        P.mark(PH_ISLANDS, 1, s);
         break;
     case JBGPU_STAGE_SOLVE:
         CK(cudaMemsetAsync(w->dw.ctr + C_ROWS, 0, sizeof(int), s));
-        solve_launch(d, w->pairs[w->cur], w->nPairs, w->rows, w->sb, dt, s);
+        solve_launch(d, w->pairs[w->cur], w->nPairs, w->rows, w->sb, dt, s, &P);
         break;
-    case JBGPU_STAGE_INTEGRATE: launch_integrate(d, dt, s); break;
-    case JBGPU_STAGE_ACTIVATION: launch_activation(d, dt, s); break;
+    case JBGPU_STAGE_INTEGRATE: P.mark(PH_INTEGRATE, 0, s); launch_integrate(d, dt, s); P.mark(PH_INTEGRATE, 1, s); break;
+    case JBGPU_STAGE_ACTIVATION: P.mark(PH_ACTIVATION, 0, s); launch_activation(d, dt, s); P.mark(PH_ACTIVATION, 1, s); break;
     case JBGPU_STAGE_CLEAR_FORCES: launch_clear_forces(d, s); break;
     default: return fail(JBGPU_ERR_INVALID_ARGUMENT, "unknown stage");
     }
@@ -346,7 +361,23 @@ int single_step(jbgpu_world* w, float dt) {
         if (rc) return rc;
     }
     w->steps++;
+    if (w->prof.active()) {
+        int* h = w->profHist + (size_t)w->prof.step * (C_NCTR + 1);
+        CK(cudaMemcpyAsync(h, w->dw.ctr, sizeof(int) * C_NCTR, cudaMemcpyDeviceToDevice, w->stream));
+        CK(cudaMemcpyAsync(h + C_NCTR, w->sb.nCand, sizeof(int), cudaMemcpyDeviceToDevice, w->stream));
+        w->prof.step++;
+    }
     return JBGPU_OK;
+}
+
+void free_prof(Prof& p) {
+    if (p.ev) {
+        for (size_t i = 0; i < (size_t)p.maxSteps * NUM_PHASES * 2; i++) cudaEventDestroy(p.ev[i]);
+        delete[] p.ev;
+    }
+    p.ev = nullptr;
+    p.maxSteps = 0;
+    p.step = 0;
 }
 
 // RigidBody setup arithmetic on the host (dynamics/RigidBody.java:121-164,207-217,301-312):
@@ -361,10 +392,25 @@ struct BodyInit {
 // Kernel: invInertiaTensorWorld and the creation-time proxy aabb (shape aabb without the
 // contact threshold, CollisionWorld.addCollisionObject) for a range of new bodies.
 __global__ void k_init_bodies(DevWorld w, int first, int count);
+__global__ void k_add_forces(DevWorld w, const float* f, const float* t);
+__global__ void k_pack_transforms(DevWorld w, float* out);
+
+namespace {
+int ensure_io(jbgpu_world* w) {
+    if (w->capIo >= w->nBodies && w->ioStage) return JBGPU_OK;
+    if (w->ioStage) cudaFree(w->ioStage);
+    w->ioStage = nullptr;
+    int c = std::max(w->nBodies, w->capBodies);
+    CK(cudaMalloc(&w->ioStage, sizeof(float) * 12 * (size_t)std::max(c, 1)));
+    w->capIo = c;
+    return JBGPU_OK;
+}
+}  // namespace
 
 extern "C" {
 
 const char* jbgpu_version(void) { return "jbgpu 0.1 (sm_103a)"; }
+int64_t jbgpu_launch_count(void) { return g_launches.load(); }
 const char* jbgpu_last_error(void) { return g_err.c_str(); }
 
 void jbgpu_config_default(jbgpu_config* c) {
@@ -537,6 +583,9 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(V.nCand); dfree(V.nColours);
     if (V.scanScratch) cudaFree(V.scanScratch);
     if (w->hostPinned) cudaFreeHost(w->hostPinned);
+    free_prof(w->prof);
+    if (w->profHist) cudaFree(w->profHist);
+    if (w->ioStage) cudaFree(w->ioStage);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
     return JBGPU_OK;
@@ -674,7 +723,7 @@ int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, 
 #undef UP
     w->nBodies += n;
     DevWorld dv = dev_view(w);
-    k_init_bodies<<<(n + 255) / 256, 256, 0, s>>>(dv, o, n);
+    k_init_bodies<<<(n + 255) / 256, 256, 0, s>>>(dv, o, n); note_launch();
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
     w->planesDirty = true;
@@ -997,7 +1046,127 @@ int jbgpu_world_counters(jbgpu_world* w, jbgpu_counters* c) {
     return JBGPU_OK;
 }
 
+int jbgpu_world_apply_forces(jbgpu_world* w, const float* force, const float* torque) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (w->nBodies == 0 || (!force && !torque)) return JBGPU_OK;
+    CK(cudaSetDevice(w->device));
+    int rc = ensure_io(w);
+    if (rc) return rc;
+    size_t n3 = (size_t)w->nBodies * 3;
+    cudaStream_t s = w->stream;
+    if (force) CK(cudaMemcpyAsync(w->ioStage, force, sizeof(float) * n3, cudaMemcpyHostToDevice, s));
+    if (torque) CK(cudaMemcpyAsync(w->ioStage + n3, torque, sizeof(float) * n3, cudaMemcpyHostToDevice, s));
+    DevWorld d = dev_view(w);
+    k_add_forces<<<(w->nBodies + 255) / 256, 256, 0, s>>>(d, force ? w->ioStage : nullptr, torque ? w->ioStage + n3 : nullptr); note_launch();
+    CK(cudaGetLastError());
+    return JBGPU_OK;
+}
+
+int jbgpu_world_get_transforms(jbgpu_world* w, float* out) {
+    if (!w || !out) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    if (w->nBodies == 0) return JBGPU_OK;
+    CK(cudaSetDevice(w->device));
+    int rc = ensure_io(w);
+    if (rc) return rc;
+    cudaStream_t s = w->stream;
+    DevWorld d = dev_view(w);
+    k_pack_transforms<<<(w->nBodies + 255) / 256, 256, 0, s>>>(d, w->ioStage); note_launch();
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, w->ioStage, sizeof(float) * 12 * (size_t)w->nBodies, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_profiling(jbgpu_world* w, int32_t max_steps) {
+    if (!w || max_steps < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
+    CK(cudaSetDevice(w->device));
+    CK(cudaStreamSynchronize(w->stream));
+    free_prof(w->prof);
+    if (w->profHist) cudaFree(w->profHist);
+    w->profHist = nullptr;
+    if (max_steps == 0) return JBGPU_OK;
+    CK(cudaMalloc(&w->profHist, sizeof(int) * (C_NCTR + 1) * (size_t)max_steps));
+    size_t ne = (size_t)max_steps * NUM_PHASES * 2;
+    w->prof.ev = new cudaEvent_t[ne];
+    for (size_t i = 0; i < ne; i++) CK(cudaEventCreate(&w->prof.ev[i]));
+    w->prof.maxSteps = max_steps;
+    w->prof.step = 0;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_phase_times(jbgpu_world* w, double* ms, int32_t nph, int32_t* steps) {
+    if (!w || !ms) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    CK(cudaStreamSynchronize(w->stream));
+    for (int p = 0; p < nph; p++) ms[p] = 0.0;
+    const Prof& P = w->prof;
+    for (int st = 0; st < P.step; st++)
+        for (int p = 0; p < NUM_PHASES && p < nph; p++) {
+            float t = 0.0f;
+            size_t k = ((size_t)st * NUM_PHASES + p) * 2;
+            if (cudaEventElapsedTime(&t, P.ev[k], P.ev[k + 1]) == cudaSuccess) ms[p] += t;
+            else cudaGetLastError();
+        }
+    if (steps) *steps = P.step;
+    if (nph > NUM_PHASES && P.step > 0) {   // whole profiled window: first gravity mark to last activation mark
+        float t = 0.0f;
+        size_t a = (size_t)PH_OTHER * 2, b = (((size_t)(P.step - 1)) * NUM_PHASES + PH_ACTIVATION) * 2 + 1;
+        if (cudaEventElapsedTime(&t, P.ev[a], P.ev[b]) == cudaSuccess) ms[NUM_PHASES] = t;
+        else cudaGetLastError();
+    }
+    return JBGPU_OK;
+}
+
+int jbgpu_world_profile_counters(jbgpu_world* w, jbgpu_counters* out, int32_t cap, int32_t* n) {
+    if (!w || !n) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    int steps = w->prof.step;
+    *n = steps;
+    if (!out || steps == 0) return JBGPU_OK;
+    if (steps > cap) return fail(JBGPU_ERR_CAPACITY, "caller buffer too small");
+    std::vector<int> h((size_t)steps * (C_NCTR + 1));
+    CK(cudaMemcpyAsync(h.data(), w->profHist, sizeof(int) * h.size(), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    for (int s = 0; s < steps; s++) {
+        const int* c = h.data() + (size_t)s * (C_NCTR + 1);
+        jbgpu_counters& o = out[s];
+        std::memset(&o, 0, sizeof(o));
+        o.bodies = w->nBodies;
+        o.pairs = c[C_PAIRS];
+        o.manifolds = c[C_MANIFOLDS];
+        o.contacts = c[C_CONTACTS];
+        o.solver_manifolds = c[C_NCTR];
+        o.solver_rows = c[C_ROWS];
+        o.colours = c[C_COLOURS];
+        o.islands = c[C_ISLANDS];
+        o.gjk_calls = c[C_GJK];
+        o.epa_calls = c[C_EPA];
+        o.status_flags = c[C_STATUS];
+    }
+    return JBGPU_OK;
+}
+
 }  // extern "C"
+
+__global__ void k_add_forces(DevWorld w, const float* f, const float* t) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    if (f) {   // applyCentralForce: totalForce += force * linearFactor (linearFactor is (1,1,1))
+        float4 a = w.force[i];
+        w.force[i] = make_float4(__fadd_rn(a.x, f[3 * i]), __fadd_rn(a.y, f[3 * i + 1]), __fadd_rn(a.z, f[3 * i + 2]), 0.0f);
+    }
+    if (t) {   // applyTorque: totalTorque += torque
+        float4 a = w.torque[i];
+        w.torque[i] = make_float4(__fadd_rn(a.x, t[3 * i]), __fadd_rn(a.y, t[3 * i + 1]), __fadd_rn(a.z, t[3 * i + 2]), 0.0f);
+    }
+}
+
+__global__ void k_pack_transforms(DevWorld w, float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    float4 a = w.xr0[i], b = w.xr1[i], c = w.xr2[i];
+    float* o = out + 12 * (size_t)i;
+    o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = b.x; o[4] = b.y; o[5] = b.z;
+    o[6] = c.x; o[7] = c.y; o[8] = c.z; o[9] = a.w; o[10] = b.w; o[11] = c.w;
+}
 
 // updateInertiaTensor and the creation-time proxy aabb for new bodies.
 #include "shapes.cuh"

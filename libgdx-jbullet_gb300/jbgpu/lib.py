@@ -31,6 +31,7 @@ def lib():
         P = C.POINTER
         sigs = {
             "jbgpu_version": ([], C.c_char_p),
+            "jbgpu_launch_count": ([], C.c_int64),
             "jbgpu_last_error": ([], C.c_char_p),
             "jbgpu_config_default": ([P(_abi.Config)], None),
             "jbgpu_shape_local_inertia": ([P(_abi.ShapeDesc), C.c_float, _abi.f32p], C.c_int),
@@ -51,6 +52,11 @@ def lib():
             "jbgpu_world_set_manifolds": ([C.c_void_p, P(_abi.Manifolds)], C.c_int),
             "jbgpu_world_get_solver_order": ([C.c_void_p, _abi.i32p, C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_counters": ([C.c_void_p, P(_abi.Counters)], C.c_int),
+            "jbgpu_world_apply_forces": ([C.c_void_p, _abi.f32p, _abi.f32p], C.c_int),
+            "jbgpu_world_get_transforms": ([C.c_void_p, _abi.f32p], C.c_int),
+            "jbgpu_world_set_profiling": ([C.c_void_p, C.c_int32], C.c_int),
+            "jbgpu_world_phase_times": ([C.c_void_p, P(C.c_double), C.c_int32, _abi.i32p], C.c_int),
+            "jbgpu_world_profile_counters": ([C.c_void_p, P(_abi.Counters), C.c_int32, _abi.i32p], C.c_int),
         }
         for name, (args, res) in sigs.items():
             f = getattr(L, name)
@@ -61,12 +67,21 @@ def lib():
 
 
 EXPORTED = [
-    "jbgpu_version", "jbgpu_last_error", "jbgpu_config_default", "jbgpu_shape_local_inertia", "jbgpu_world_create",
+    "jbgpu_version", "jbgpu_launch_count", "jbgpu_last_error", "jbgpu_config_default", "jbgpu_shape_local_inertia", "jbgpu_world_create",
     "jbgpu_world_destroy", "jbgpu_world_add_shape", "jbgpu_world_add_shapes", "jbgpu_world_add_bodies",
     "jbgpu_world_num_bodies", "jbgpu_world_step_simulation", "jbgpu_world_step", "jbgpu_world_stage",
     "jbgpu_world_synchronize", "jbgpu_world_get_state", "jbgpu_world_set_state", "jbgpu_world_get_pairs",
     "jbgpu_world_get_manifolds", "jbgpu_world_set_manifolds", "jbgpu_world_get_solver_order", "jbgpu_world_counters",
+    "jbgpu_world_apply_forces", "jbgpu_world_get_transforms", "jbgpu_world_set_profiling", "jbgpu_world_phase_times",
+    "jbgpu_world_profile_counters",
 ]
+
+
+def launch_count():
+    return lib().jbgpu_launch_count()
+
+PHASES = ["predict", "aabb", "pair_count", "pair_fill", "narrow_gjk", "narrow_epa", "islands", "colour", "setup", "pgs",
+          "integrate", "activation", "gravity"]
 
 
 def check(rc):
@@ -162,6 +177,35 @@ class GpuWorld:
         c = _abi.Counters()
         check(lib().jbgpu_world_counters(self.h, C.byref(c)))
         return c.as_dict()
+
+    def apply_forces(self, force=None, torque=None):
+        f = None if force is None else np.ascontiguousarray(force, np.float32)
+        t = None if torque is None else np.ascontiguousarray(torque, np.float32)
+        check(lib().jbgpu_world_apply_forces(self.h, None if f is None else f.ctypes.data_as(_abi.f32p),
+                                             None if t is None else t.ctypes.data_as(_abi.f32p)))
+
+    def get_transforms(self, out=None):
+        if out is None:
+            out = np.zeros((self.n_bodies, 12), np.float32)
+        check(lib().jbgpu_world_get_transforms(self.h, out.ctypes.data_as(_abi.f32p)))
+        return out
+
+    def set_profiling(self, max_steps):
+        check(lib().jbgpu_world_set_profiling(self.h, max_steps))
+
+    def phase_times(self):
+        """({phase: total device ms}, profiled steps, whole-window device ms)."""
+        ms = (C.c_double * (len(PHASES) + 1))()
+        n = C.c_int32()
+        check(lib().jbgpu_world_phase_times(self.h, ms, len(PHASES) + 1, C.byref(n)))
+        return dict(zip(PHASES, list(ms)[:len(PHASES)])), n.value, ms[len(PHASES)]
+
+    def profile_counters(self):
+        n = C.c_int32()
+        check(lib().jbgpu_world_profile_counters(self.h, None, 0, C.byref(n)))
+        arr = (_abi.Counters * max(1, n.value))()
+        check(lib().jbgpu_world_profile_counters(self.h, arr, len(arr), C.byref(n)))
+        return [arr[i].as_dict() for i in range(n.value)]
 
 
 def shape_local_inertia(shape_dict, mass):
