@@ -1,0 +1,330 @@
+"""Host-side mirror of the reference's world / body / shape API over the C ABI.
+
+Names, argument meaning and defaults follow JBullet (src/com/bulletphysics/ of the reference):
+DiscreteDynamicsWorld (dynamics/DiscreteDynamicsWorld.java), RigidBody and
+RigidBodyConstructionInfo (dynamics/RigidBody.java, RigidBodyConstructionInfo.java), the
+shapes of collision/shapes/, ContactSolverInfo (dynamics/constraintsolver/ContactSolverInfo.java).
+The dispatcher, broadphase and constraint solver arguments of the world constructor are
+accepted and ignored: the GPU step replaces all three behind the same stepSimulation call.
+
+Bodies are staged on the host and uploaded in bulk the first time the world steps (or when
+queried); after that their state lives on the device and RigidBody getters read it back.
+"""
+import numpy as np
+
+from . import _abi
+from .lib import GpuWorld
+
+ACTIVE_TAG, ISLAND_SLEEPING, WANTS_DEACTIVATION, DISABLE_DEACTIVATION, DISABLE_SIMULATION = 1, 2, 3, 4, 5
+
+
+class Transform:
+    """linearmath/Transform.java: basis (3x3, row-major) and origin."""
+
+    def __init__(self, basis=None, origin=(0.0, 0.0, 0.0)):
+        self.basis = np.eye(3, dtype=np.float32) if basis is None else np.asarray(basis, np.float32).reshape(3, 3)
+        self.origin = np.asarray(origin, np.float32).reshape(3)
+
+    def setIdentity(self):
+        self.basis = np.eye(3, dtype=np.float32)
+        self.origin = np.zeros(3, np.float32)
+
+    def as12(self):
+        return np.concatenate([self.basis.reshape(9), self.origin]).astype(np.float32)
+
+    @classmethod
+    def from12(cls, t):
+        return cls(np.asarray(t[:9]).reshape(3, 3), t[9:12])
+
+
+class _Shape:
+    shape_type = None
+
+    def __init__(self):
+        self._id = None
+
+    def desc(self):
+        raise NotImplementedError
+
+    def calculateLocalInertia(self, mass):
+        """CollisionShape.calculateLocalInertia (binary32, the reference's operation order)."""
+        from . import lib
+        return lib.shape_local_inertia(self.desc(), mass)
+
+
+class BoxShape(_Shape):
+    def __init__(self, boxHalfExtents):
+        super().__init__()
+        self.halfExtents = tuple(float(x) for x in boxHalfExtents)
+
+    def desc(self):
+        return {"type": _abi.SHAPE_BOX, "params": self.halfExtents + (0.0,), "points": None}
+
+
+class SphereShape(_Shape):
+    def __init__(self, radius):
+        super().__init__()
+        self.radius = float(radius)
+
+    def desc(self):
+        return {"type": _abi.SHAPE_SPHERE, "params": (self.radius, 0.0, 0.0, 0.0), "points": None}
+
+
+class CapsuleShape(_Shape):
+    def __init__(self, radius, height):
+        super().__init__()
+        self.radius, self.height = float(radius), float(height)
+
+    def desc(self):
+        return {"type": _abi.SHAPE_CAPSULE, "params": (self.radius, self.height, 0.0, 0.0), "points": None}
+
+
+class ConvexHullShape(_Shape):
+    def __init__(self, points):
+        super().__init__()
+        self.points = np.asarray(points, np.float32).reshape(-1, 3)
+
+    def desc(self):
+        return {"type": _abi.SHAPE_CONVEX_HULL, "params": (0.0, 0.0, 0.0, 0.0), "points": self.points}
+
+
+class StaticPlaneShape(_Shape):
+    def __init__(self, planeNormal, planeConstant):
+        super().__init__()
+        self.normal, self.constant = tuple(float(x) for x in planeNormal), float(planeConstant)
+
+    def desc(self):
+        return {"type": _abi.SHAPE_STATIC_PLANE, "params": self.normal + (self.constant,), "points": None}
+
+
+class RigidBodyConstructionInfo:
+    def __init__(self, mass, motionState, collisionShape, localInertia=(0.0, 0.0, 0.0)):
+        self.mass = float(mass)
+        self.motionState = motionState
+        self.collisionShape = collisionShape
+        self.localInertia = tuple(float(x) for x in localInertia)
+        self.startWorldTransform = Transform()
+        self.linearDamping = 0.0
+        self.angularDamping = 0.0
+        self.friction = 0.5
+        self.restitution = 0.0
+        self.linearSleepingThreshold = 0.8
+        self.angularSleepingThreshold = 1.0
+
+
+class RigidBody:
+    def __init__(self, info):
+        self.info = info
+        self._world = None
+        self._index = None
+        self._linvel = (0.0, 0.0, 0.0)
+        self._angvel = (0.0, 0.0, 0.0)
+        self._group = -1
+        self._mask = -1
+
+    # velocities set before the body enters the world are uploaded with it
+    def setLinearVelocity(self, v):
+        if self._world is not None and self._world._g is not None:
+            self._world._set_field("linear_velocity", self._index, v)
+        else:
+            self._linvel = tuple(float(x) for x in v)
+
+    def setAngularVelocity(self, v):
+        if self._world is not None and self._world._g is not None:
+            self._world._set_field("angular_velocity", self._index, v)
+        else:
+            self._angvel = tuple(float(x) for x in v)
+
+    def _state(self, field):
+        return self._world._get_field(field, self._index)
+
+    def getCenterOfMassTransform(self):
+        return Transform.from12(self._state("transform"))
+
+    getWorldTransform = getCenterOfMassTransform
+
+    def getLinearVelocity(self):
+        return self._state("linear_velocity")
+
+    def getAngularVelocity(self):
+        return self._state("angular_velocity")
+
+    def getActivationState(self):
+        return int(self._state("activation_state"))
+
+    def isActive(self):
+        return self.getActivationState() not in (ISLAND_SLEEPING, DISABLE_SIMULATION)
+
+    def getInvMass(self):
+        return 0.0 if self.info.mass == 0.0 else 1.0 / np.float32(self.info.mass)
+
+    def applyCentralForce(self, f):
+        self._world._pending_force(self._index, f)
+
+    def getUid(self):
+        return self._index + 1
+
+
+class ContactSolverInfo:
+    def __init__(self):
+        self.numIterations = 10
+        self.erp = 0.2
+        self.warmstartingFactor = 0.85
+        self.linearSlop = 0.0
+        self.solverMode = _abi.SOLVER_CACHE_FRIENDLY | _abi.SOLVER_USE_WARMSTARTING
+
+
+class DiscreteDynamicsWorld:
+    def __init__(self, dispatcher=None, pairCache=None, constraintSolver=None, collisionConfiguration=None, device=0):
+        self._gravity = (0.0, -10.0, 0.0)
+        self._solver = ContactSolverInfo()
+        self._device = device
+        self._bodies = []
+        self._shapes = []
+        self._g = None
+        self._forces = None
+        self._uploaded = 0
+
+    # -- configuration (before the first step) --
+    def setGravity(self, g):
+        if self._g is not None:
+            raise RuntimeError("setGravity after the first step is not supported by the GPU world")
+        self._gravity = tuple(float(x) for x in g)
+
+    def getGravity(self):
+        return self._gravity
+
+    def getSolverInfo(self):
+        return self._solver
+
+    def addRigidBody(self, body, group=None, mask=None):
+        if self._g is not None and self._uploaded != len(self._bodies):
+            raise RuntimeError("internal: bodies not uploaded")
+        body._world = self
+        body._index = len(self._bodies)
+        if group is not None:
+            body._group, body._mask = int(group), int(mask)
+        self._bodies.append(body)
+        if self._g is not None:
+            self._upload()
+
+    def getNumCollisionObjects(self):
+        return len(self._bodies)
+
+    # -- stepping --
+    def _ensure(self):
+        if self._g is None:
+            s = self._solver
+            cfg = _abi.default_config(gravity=self._gravity)
+            cfg.num_iterations = s.numIterations
+            cfg.erp = s.erp
+            cfg.warmstarting_factor = s.warmstartingFactor
+            cfg.linear_slop = s.linearSlop
+            cfg.solver_mode = s.solverMode
+            cfg.device = self._device
+            self._g = GpuWorld(config=cfg)
+        if self._uploaded != len(self._bodies):
+            self._upload()
+        return self._g
+
+    def _upload(self):
+        from .scenes import BODY_DTYPE, Scene
+        new = self._bodies[self._uploaded:]
+        shapes, ids = [], {}
+        for b in new:
+            sh = b.info.collisionShape
+            if sh._id is None:
+                ids[id(sh)] = len(self._shapes) + len(shapes)
+                shapes.append(sh)
+        recs = np.zeros(len(new), BODY_DTYPE)
+        for k, b in enumerate(new):
+            i = b.info
+            sh = i.collisionShape
+            recs[k]["mass"] = i.mass
+            recs[k]["shape"] = sh._id if sh._id is not None else ids[id(sh)]
+            t = i.startWorldTransform
+            if i.motionState is not None and hasattr(i.motionState, "getWorldTransform"):
+                t = i.motionState.getWorldTransform()
+            recs[k]["transform"] = t.as12()
+            recs[k]["local_inertia"] = i.localInertia
+            recs[k]["linear_damping"] = i.linearDamping
+            recs[k]["angular_damping"] = i.angularDamping
+            recs[k]["friction"] = i.friction
+            recs[k]["restitution"] = i.restitution
+            recs[k]["linear_sleeping_threshold"] = i.linearSleepingThreshold
+            recs[k]["angular_sleeping_threshold"] = i.angularSleepingThreshold
+            recs[k]["linear_velocity"] = b._linvel
+            recs[k]["angular_velocity"] = b._angvel
+            recs[k]["collision_group"] = b._group
+            recs[k]["collision_mask"] = b._mask
+        sc = Scene("staged", 0, 0, {}, [s.desc() for s in shapes], recs)
+        g = self._g
+        if shapes:
+            from . import lib
+            descs = sc.shape_descs()
+            lib.check(lib.lib().jbgpu_world_add_shapes(g.h, descs, len(descs), None))
+            for s in shapes:
+                s._id = ids[id(s)]
+        self._shapes += shapes
+        b, ptr = sc.body_descs_ptr()
+        from . import lib
+        lib.check(lib.lib().jbgpu_world_add_bodies(g.h, ptr, len(b), None))
+        self._uploaded = len(self._bodies)
+        self._forces = None
+
+    def _pending_force(self, index, f):
+        if self._forces is None:
+            self._forces = np.zeros((len(self._bodies), 3), np.float32)
+        self._forces[index] += np.asarray(f, np.float32)
+
+    def stepSimulation(self, timeStep, maxSubSteps=1, fixedTimeStep=1.0 / 60.0):
+        g = self._ensure()
+        if self._forces is not None:
+            g.apply_forces(self._forces)
+            self._forces = None
+        n = g.step_simulation(timeStep, maxSubSteps, fixedTimeStep)
+        self._cache = None
+        return n
+
+    # -- state access --
+    _cache = None
+
+    def _state(self):
+        if self._cache is None:
+            self._cache = self._ensure().get_state()
+        return self._cache
+
+    def _get_field(self, field, index):
+        return self._state()[field][index].copy()
+
+    def _set_field(self, field, index, value):
+        st = self._state()
+        st[field][index] = value
+        self._g.set_state({field: st[field]})
+        self._cache = None
+
+    def getDispatcher(self):
+        return _Dispatcher(self)
+
+    def getPairCache(self):
+        return self._ensure().get_pairs()
+
+    def close(self):
+        if self._g is not None:
+            self._g.close()
+            self._g = None
+
+
+class _Dispatcher:
+    """CollisionDispatcher read access: getNumManifolds / getManifoldByIndexInternal."""
+
+    def __init__(self, world):
+        self._m = world._ensure().get_manifolds()
+
+    def getNumManifolds(self):
+        return int(np.sum(self._m["flags"] & 1))
+
+    def getManifoldByIndexInternal(self, i):
+        idx = np.nonzero(self._m["flags"] & 1)[0][i]
+        return {"key": int(self._m["keys"][idx]), "numContacts": int(self._m["num_points"][idx]),
+                "points": self._m["points"][idx, :self._m["num_points"][idx]]}

@@ -164,8 +164,11 @@ def test_full_size_100k_pairs_and_properties(gpu_lib, oracle_lib):
     pts = m["points"][mask]
     assert np.all(pts[:, 15] <= 0.02 + 1e-7)                 # refreshContactPoints drops points beyond the threshold
     assert np.all(pts[:, 18] >= 0)                          # accumulated normal impulse clamp
-    fr = pts[:, 16] * pts[:, 18]
-    assert np.all(np.abs(pts[:, 19]) <= fr * (1 + 1e-5) + 1e-6)   # friction impulse inside the cone
+    # friction inside the cone where the normal impulse is positive (the reference skips the
+    # friction rows of a point whose normal impulse is zero, leaving its warm-started value)
+    on = pts[:, 18] > 0
+    fr = pts[on, 16] * pts[on, 18]
+    assert np.all(np.abs(pts[on, 19]) <= fr * (1 + 1e-5) + 1e-6)
     st = g.get_state()
     for k in ("transform", "linear_velocity", "angular_velocity"):
         assert np.all(np.isfinite(st[k]))
