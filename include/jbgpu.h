@@ -116,7 +116,11 @@ typedef struct jbgpu_config {
     int32_t device;                     /* CUDA device ordinal, default 0 */
     int32_t initial_body_capacity;      /* device arrays grow on demand; default 1024 */
     int32_t pairs_per_body;             /* initial pair capacity per body, default 16 */
-    int32_t reserved[8];
+    int32_t solver_parts;               /* 0 (default): one solver part per batch world when every
+                                           world has at most 2048 finite bodies, else ranges of
+                                           the Morton order; > 0: that many range parts (at least
+                                           finite bodies / 2048).  No counterpart in the reference. */
+    int32_t reserved[7];
 } jbgpu_config;
 
 typedef struct jbgpu_shape_desc {

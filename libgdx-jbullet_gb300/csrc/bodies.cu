@@ -37,9 +37,10 @@ __global__ void k_predict(DevWorld w, float dt) {
     av = add(av, tmp);
     float a = len(av);
     if (__fmul_rn(a, dt) > MAX_ANGVEL) av = scl(av, jdiv(jdiv(MAX_ANGVEL, dt), a));
-    float ld = w.linDamp[i], ad = w.angDamp[i];
-    lv = scl(lv, jpow(__fsub_rn(1.0f, ld), dt));
-    av = scl(av, jpow(__fsub_rn(1.0f, ad), dt));
+    // (float)Math.pow(1 - damping, dt); pow(1, y) == 1 exactly, so zero damping skips the FP64 call
+    float ld = __fsub_rn(1.0f, w.linDamp[i]), ad = __fsub_rn(1.0f, w.angDamp[i]);
+    lv = scl(lv, ld == 1.0f ? 1.0f : jpow(ld, dt));
+    av = scl(av, ad == 1.0f ? 1.0f : jpow(ad, dt));
     w.linvel[i] = f4(lv, 0.0f);
     w.angvel[i] = f4(av, 0.0f);
 }

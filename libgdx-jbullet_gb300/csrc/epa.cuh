@@ -13,11 +13,17 @@ constexpr int EPA_MKV_CAP = 288;
 constexpr int EPA_SEEN_CAP = 136;
 constexpr int EPA_STACK_CAP = 2 * EPA_FACE_CAP;
 
+// The reference keeps the polytope's faces in a doubly linked list, newest first, and FindBest
+// walks it for the first face of strictly smallest distance.  Faces enter the list only when
+// created (prepended) and leave only through Detach, so the list is always the live faces in
+// decreasing creation order: here a face is live when fE.w == 1, fD holds its distance (+inf
+// once detached), and FindBest scans fD from the newest face down, which selects the same face.
 struct EpaSlot {          // one thread's polytope
     float4* fN;           // face normal xyz, distance w
     int4* fV;             // vertex ids, mark
-    int4* fF;             // adjacent faces, prev
-    int4* fE;             // adjacent edges, next
+    int4* fF;             // adjacent faces
+    int4* fE;             // adjacent edges, live flag (w)
+    float* fD;            // distance of live faces, +inf for faces outside the list
     float4* mW;           // Minkowski vertex w
     float4* mR;           // support direction r
     float4* seen;         // rays fetched by SearchOrigin (the reference's 64-bucket hash, as a set)
@@ -27,12 +33,14 @@ struct EpaSlot {          // one thread's polytope
 struct EpaArena {
     float4 *fN, *mW, *mR, *seen;
     int4 *fV, *fF, *fE;
+    float* fD;
     int2* stack;
     int slots;
 };
 
 JBD EpaSlot epa_slot(const EpaArena& a, int s) {
     EpaSlot e;
+    e.fD = a.fD + (size_t)s * EPA_FACE_CAP;
     e.fN = a.fN + (size_t)s * EPA_FACE_CAP;
     e.fV = a.fV + (size_t)s * EPA_FACE_CAP;
     e.fF = a.fF + (size_t)s * EPA_FACE_CAP;
@@ -226,36 +234,21 @@ JBD int epa_new_face(EpaCtx& c, int a, int b, int cc) {     // EPA.NewFace + EPA
     float d = jmax(0.0f, -dot(n, aw));
     c.sl.fN[id] = f4(n, d);
     c.sl.fV[id] = make_int4(a, b, cc, 0);
-    int prev = -1, next = -1;
-    if (valid) {
-        if (c.root >= 0) { int4 rf = c.sl.fF[c.root]; rf.w = id; c.sl.fF[c.root] = rf; }
-        prev = -1;
-        next = c.root;
-        c.root = id;
-        ++c.nfaces;
-    }
-    c.sl.fF[id] = make_int4(-1, -1, -1, prev);
-    c.sl.fE[id] = make_int4(0, 0, 0, next);
+    c.sl.fF[id] = make_int4(-1, -1, -1, 0);
+    c.sl.fE[id] = make_int4(0, 0, 0, valid ? 1 : 0);   // prepended to the list when valid
+    c.sl.fD[id] = valid ? d : __int_as_float(0x7f800000);
+    if (valid) ++c.nfaces;
     return id;
 }
+// EPA.Detach: a listed face leaves the list unless it is the list's only face (then it has
+// neither prev nor next and the reference's condition skips it).
 JBD void epa_detach(EpaCtx& c, int f) {
-    int4 F = c.sl.fF[f], E = c.sl.fE[f];
-    int prev = F.w, next = E.w;
-    if (prev >= 0 || next >= 0) {
+    int4 E = c.sl.fE[f];
+    if (E.w && c.nfaces > 1) {
         --c.nfaces;
-        if (f == c.root) {
-            c.root = next;
-            if (c.root >= 0) { int4 r = c.sl.fF[c.root]; r.w = -1; c.sl.fF[c.root] = r; }
-        } else {
-            if (next < 0) { int4 p = c.sl.fE[prev]; p.w = -1; c.sl.fE[prev] = p; }
-            else {
-                int4 p = c.sl.fE[prev]; p.w = next; c.sl.fE[prev] = p;
-                int4 q = c.sl.fF[next]; q.w = prev; c.sl.fF[next] = q;
-            }
-        }
-        F.w = -1; E.w = -1;
-        c.sl.fF[f] = F;
+        E.w = 0;
         c.sl.fE[f] = E;
+        c.sl.fD[f] = __int_as_float(0x7f800000);
     }
 }
 JBD void epa_link(EpaCtx& c, int f0, int e0, int f1, int e1) {
@@ -328,15 +321,13 @@ JBD bool epa_pen_depth(const ShapeRef& s0, const Xf& t0, const ShapeRef& s1, con
     }
     if (c.nfaces == 0) { overflow = c.overflow; return false; }   // depth = -inf, not > 0
     for (int it = 0; it < 256 && !c.overflow; ++it) {
-        int best = -1;                                               // FindBest
-        if (c.root >= 0) {
-            int cf = c.root, guard = 0;
+        int best = -1;                                               // FindBest, newest face first
+        {
             float bd = SIMD_INFINITY;
-            do {
-                float d = c.sl.fN[cf].w;
-                if (d < bd) { bd = d; best = cf; }
-                if (++guard > c.nface) { c.overflow = true; break; }   // a well-formed list has <= nface entries
-            } while ((cf = c.sl.fE[cf].w) >= 0);
+            for (int f = c.nface - 1; f >= 0; f--) {
+                float d = c.sl.fD[f];
+                if (d < bd) { bd = d; best = f; }
+            }
         }
         if (best < 0) break;
         float4 bn = c.sl.fN[best];

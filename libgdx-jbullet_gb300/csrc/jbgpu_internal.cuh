@@ -15,7 +15,7 @@ enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8 };
 // Counters kept on the device (indices into DevWorld::ctr).
 enum {
     C_PAIRS = 0, C_FILL_OVERFLOW, C_EPA_QUEUE, C_GJK, C_EPA, C_SOLVE_N, C_COLOURS, C_ISLANDS,
-    C_MANIFOLDS, C_CONTACTS, C_ROWS, C_STATUS, C_BAR_COUNT, C_BAR_GEN, C_REMAIN0, C_REMAIN1, C_NCTR = 32
+    C_MANIFOLDS, C_CONTACTS, C_ROWS, C_STATUS, C_BAR_COUNT, C_BAR_GEN, C_CUT_DONE, C_WIN0, C_WIN1, C_WIN2, C_NCTR = 32
 };
 
 struct DevShapes {
@@ -46,7 +46,7 @@ struct DevPairs {
 };
 
 // Solver rows, indexed by solve slot * 4 + point (normal) and (solve slot * 4 + point) * 2 + k
-// (friction).  Slots are grouped by colour.
+// (friction).  Slots are grouped by part and local colour, then by cut colour.
 struct DevRows {
     float4* n_nrm;    // contactNormal, jacDiagABInv
     float4* n_rp1;    // relpos1CrossNormal, penetration
@@ -59,8 +59,8 @@ struct DevRows {
     float4* f_angA;
     float4* f_angB;
     int* slot_pair;   // pair index of the manifold in each solve slot
-    int* slot_mask;   // bit j: point j has rows
-    int* colour_start;// colour c occupies slots [colour_start[c], colour_start[c+1])
+    int4* slot_desc;  // body0, body1, point mask (bit j: point j has rows), local body indices
+    float2* slot_im;  // inverse masses of body0, body1
 };
 
 struct DevWorld {

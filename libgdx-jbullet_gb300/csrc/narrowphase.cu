@@ -161,7 +161,7 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
     if (nPairs > 0) { k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, (EpaRec*)nb.queue, nb.queueCount); note_launch(); }
     if (prof) { prof->mark(PH_NARROW, 1, s); prof->mark(PH_EPA, 0, s); }
     EpaArena ar;
-    ar.fN = nb.fN; ar.fV = nb.fV; ar.fF = nb.fF; ar.fE = nb.fE;
+    ar.fN = nb.fN; ar.fV = nb.fV; ar.fF = nb.fF; ar.fE = nb.fE; ar.fD = nb.fD;
     ar.mW = nb.mW; ar.mR = nb.mR; ar.seen = nb.seen; ar.stack = nb.stack;
     ar.slots = nb.slots;
     if (nPairs > 0) { k_narrow_epa<<<(nb.slots + 63) / 64, 64, 0, s>>>(w, P, (const EpaRec*)nb.queue, nb.queueCount, ar); note_launch(); }

@@ -10,6 +10,7 @@ struct NarrowBuffers {
     int slots = 0;                // concurrent EPA threads, each owning one slot
     float4 *fN = nullptr, *mW = nullptr, *mR = nullptr, *seen = nullptr;
     int4 *fV = nullptr, *fF = nullptr, *fE = nullptr;
+    float* fD = nullptr;
     int2* stack = nullptr;
 };
 

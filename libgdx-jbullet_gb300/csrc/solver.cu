@@ -8,16 +8,19 @@
 // (SimulationIslandManager.java:283-296).
 //
 // Solver: SequentialImpulseConstraintSolver.solveGroupCacheFriendly
-// (dynamics/constraintsolver/SequentialImpulseConstraintSolver.java:418-924), made parallel by
-// colouring manifolds so that no two manifolds of a colour share a dynamic body.  Gauss-Seidel
-// within a colour is then order-independent and the colour phases equal the reference solver
-// run on the manifolds sorted by (colour, pair index), the order hook of F8
-// (SequentialImpulseConstraintSolver.java:769-779).  Colouring: each round, every dynamic body
-// is claimed by the lowest candidate index touching it; candidates holding all their claims
-// take the round's colour.  One cooperative persistent kernel colours, another runs warm
-// start, numIterations x (normal colours, friction colours) and write-back, separated by a
-// bounded grid barrier.
-#include <cooperative_groups.h>
+// (dynamics/constraintsolver/SequentialImpulseConstraintSolver.java:418-924) made parallel
+// without changing its arithmetic.  Gauss-Seidel over manifolds gives the same floats for any
+// two manifold orders in which every pair of manifolds sharing a dynamic body keeps its relative
+// order.  Dynamic bodies are split into parts (a batch world each, or ranges of the Morton leaf
+// order); a manifold whose dynamic bodies lie in one part is internal to it, else cut.  Internal
+// manifolds are coloured per part, cut manifolds grid-wide, so that no two manifolds of a colour
+// share a dynamic body.  Every phase (warm start, then numIterations x normal rows, friction
+// rows) runs the parts' local colours with their velocities in shared memory, then the cut
+// colours: the reference solver run on the manifolds sorted by (part, colour) with cut
+// manifolds last, the order hook of SequentialImpulseConstraintSolver.java:769-779.
+#include <algorithm>
+#include <cstdlib>
+#include "../../include/jbgpu.h"
 #include "manifold.cuh"
 #include "prims.cuh"
 #include "solver.cuh"
@@ -146,98 +149,244 @@ void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuff
 }
 
 // ---- grid barrier (bounded wait) -----------------------------------------------------------
+// Arrival by an acquire-release atomic, release of the generation by the last block, acquire
+// polling.  A wait gives up after a bounded number of polls and sets ST_TIMEOUT (the host
+// reports JBGPU_ERR_TIMEOUT); once the flag is set every later barrier returns at once.
 constexpr long long BARRIER_SPIN_LIMIT = 20000000;
+
+__device__ __forceinline__ unsigned ld_acquire(const int* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel(int* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void st_release(int* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 __device__ __forceinline__ void grid_barrier(int* ctr, int nblocks) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile int* vgen = &ctr[C_BAR_GEN];
-        volatile int* vst = &ctr[C_STATUS];
-        int g = *vgen;
-        __threadfence();
-        int arrived = atomicAdd(&ctr[C_BAR_COUNT], 1);
-        if (arrived == nblocks - 1) {
+        unsigned g = ld_acquire(&ctr[C_BAR_GEN]);
+        unsigned arrived = atom_add_acq_rel(&ctr[C_BAR_COUNT], 1u);
+        if (arrived == (unsigned)nblocks - 1u) {
             atomicExch(&ctr[C_BAR_COUNT], 0);
-            __threadfence();
-            atomicAdd(&ctr[C_BAR_GEN], 1);
+            st_release(&ctr[C_BAR_GEN], g + 1u);
         } else {
             long long spins = 0;
-            while (*vgen == g) {
-                __nanosleep(32);
-                if (++spins > BARRIER_SPIN_LIMIT || (*vst & ST_TIMEOUT)) { atomicOr(&ctr[C_STATUS], ST_TIMEOUT); break; }
+            while (ld_acquire(&ctr[C_BAR_GEN]) == g) {
+                if (++spins > BARRIER_SPIN_LIMIT || (ld_acquire(&ctr[C_STATUS]) & ST_TIMEOUT)) {
+                    atomicOr(&ctr[C_STATUS], ST_TIMEOUT);
+                    break;
+                }
             }
         }
-        __threadfence();
     }
     __syncthreads();
 }
 
-// ---- colouring (cooperative) --------------------------------------------------------------
+// ---- parts and buckets ---------------------------------------------------------------------
 __device__ __forceinline__ bool dyn(const DevWorld& w, int b) { return w.island[b] >= 0; }
 
-__global__ void k_colour(DevWorld w, DevPairs P, SolverBuffers sb) {
+// Claim tag of candidate k in claim pass t.  Later passes carry smaller tags, so a claim left
+// from an earlier pass never beats a claim of the current one.
+__device__ __forceinline__ unsigned long long ctag(int t, int k) {
+    return ((unsigned long long)(0x7fffffff - t) << 32) | (unsigned)k;
+}
+
+// Part of dynamic body b, or -1 when b has no position in the body order.
+__device__ __forceinline__ int part_of(const DevWorld& w, const SolverBuffers& sb, int b) {
+    int pos = sb.posOf[b];
+    if (pos < 0) return -1;
+    return sb.worldParts ? w.world[b] : (int)(((long long)pos * sb.nParts) / sb.nFinite);
+}
+
+__global__ void k_posof(SolverBuffers sb) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < sb.nFinite) sb.posOf[sb.order[s]] = s;
+}
+
+// Bucket of candidate k: the part holding all its dynamic bodies, else nParts (cut).
+__global__ void k_classify(DevWorld w, DevPairs P, SolverBuffers sb) {
+    int nCand = *sb.nCand;
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nCand) return;
+    int p = sb.cand[k];
+    int b0 = P.b0[p], b1 = P.b1[p];
+    bool d0 = dyn(w, b0), d1 = dyn(w, b1);
+    int q0 = d0 ? part_of(w, sb, b0) : -2, q1 = d1 ? part_of(w, sb, b1) : -2;
+    int q = d0 ? q0 : q1;
+    if (q == -1 || (d0 && d1 && q0 != q1)) q = sb.nParts;
+    sb.bucket[k] = q;
+    atomicAdd(&sb.bucketCount[q], 1);
+}
+
+__global__ void k_bucket_scatter(SolverBuffers sb) {
+    int nCand = *sb.nCand;
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nCand) return;
+    int b = sb.bucket[k];
+    sb.bucketList[sb.bucketStart[b] + atomicAdd(&sb.bucketFill[b], 1)] = k;
+}
+
+// ---- colouring (cooperative) ---------------------------------------------------------------
+// Each colour is grown to a maximal set by claim passes: every dynamic body is claimed by the
+// lowest candidate index touching it among the eligible candidates (uncoloured, no dynamic body
+// taken by the colour yet); candidates holding all their claims join the colour and take their
+// bodies; passes repeat until one adds nothing (at most MAX_SUB).  Manifolds internal to a part
+// are coloured by the block owning the part with block barriers; cut manifolds are coloured
+// grid-wide afterwards with grid barriers.
+__device__ __forceinline__ bool eligible(const DevWorld& w, const DevPairs& P, const SolverBuffers& sb, int k, int mark,
+                                         int& b0, int& b1) {
+    if (__ldcg(&sb.colourOf[k]) >= 0) return false;
+    int p = sb.cand[k];
+    b0 = P.b0[p];
+    b1 = P.b1[p];
+    if (dyn(w, b0) && __ldcg(&sb.taken[b0]) == mark) return false;
+    if (dyn(w, b1) && __ldcg(&sb.taken[b1]) == mark) return false;
+    return true;
+}
+
+__device__ __forceinline__ bool holds_claims(const DevWorld& w, const SolverBuffers& sb, int b0, int b1,
+                                             unsigned long long me) {
+    return (!dyn(w, b0) || __ldcg(&sb.claim[b0]) == me) && (!dyn(w, b1) || __ldcg(&sb.claim[b1]) == me);
+}
+
+__global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs P, SolverBuffers sb) {
     const int nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int nCand = *sb.nCand;
-    int* rem[2] = {sb.remA, sb.remB};
-    for (int k = tid; k < nCand; k += nth) rem[0][k] = k;
+    __shared__ int shWin, shDone;
+    for (int k = tid; k < nCand; k += nth) sb.colourOf[k] = -1;
+    for (int c = tid; c < sb.nParts * (MAX_LOCAL + 1); c += nth) sb.lcCount[c] = 0;
     for (int c = tid; c <= MAX_COLOURS; c += nth) sb.colourCount[c] = 0;
-    if (tid == 0) { w.ctr[C_REMAIN0] = nCand; w.ctr[C_REMAIN1] = 0; }
+    if (tid == 0) { w.ctr[C_CUT_DONE] = 0; w.ctr[C_WIN0] = w.ctr[C_WIN1] = w.ctr[C_WIN2] = 0; }
     grid_barrier(w.ctr, nb);
-    int round = 0;
-    for (; round < MAX_COLOURS; round++) {
-        int cur = round & 1;
-        int nrem = __ldcg(&w.ctr[C_REMAIN0 + cur]);
-        if (nrem == 0) break;
-        if (tid == 0) w.ctr[C_REMAIN0 + (cur ^ 1)] = 0;
-        unsigned long long tag = (unsigned long long)(MAX_COLOURS - round) << 32;
-        for (int i = tid; i < nrem; i += nth) {
-            int k = __ldcg(&rem[cur][i]);
-            int p = sb.cand[k];
-            int b0 = P.b0[p], b1 = P.b1[p];
-            if (dyn(w, b0)) atomicMin(&sb.claim[b0], tag | (unsigned)k);
-            if (dyn(w, b1)) atomicMin(&sb.claim[b1], tag | (unsigned)k);
-        }
-        grid_barrier(w.ctr, nb);
-        for (int i = tid; i < nrem; i += nth) {
-            int k = __ldcg(&rem[cur][i]);
-            int p = sb.cand[k];
-            int b0 = P.b0[p], b1 = P.b1[p];
-            unsigned long long me = tag | (unsigned)k;
-            bool win = (!dyn(w, b0) || __ldcg(&sb.claim[b0]) == me) && (!dyn(w, b1) || __ldcg(&sb.claim[b1]) == me);
-            if (win) {
-                sb.colourOf[k] = round;
-                atomicAdd(&sb.colourCount[round], 1);
-            } else {
-                int q = atomicAdd(&w.ctr[C_REMAIN0 + (cur ^ 1)], 1);
-                rem[cur ^ 1][q] = k;
+    // manifolds internal to the parts of this block
+    for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
+        const int s0 = sb.bucketStart[part], s1 = sb.bucketStart[part + 1];
+        int* lc = sb.lcCount + part * (MAX_LOCAL + 1);
+        if (threadIdx.x == 0) shDone = 0;
+        __syncthreads();
+        int r = 0;
+        for (; r < MAX_LOCAL && shDone < s1 - s0; r++) {
+            for (int sub = 0; sub < MAX_SUB; sub++) {
+                const int t = r * MAX_SUB + sub;
+                for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+                    int k = sb.bucketList[i], b0, b1;
+                    if (!eligible(w, P, sb, k, r, b0, b1)) continue;
+                    if (dyn(w, b0)) atomicMin(&sb.claim[b0], ctag(t, k));
+                    if (dyn(w, b1)) atomicMin(&sb.claim[b1], ctag(t, k));
+                }
+                if (threadIdx.x == 0) shWin = 0;
+                __syncthreads();
+                for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+                    int k = sb.bucketList[i], b0, b1;
+                    if (!eligible(w, P, sb, k, r, b0, b1)) continue;
+                    if (holds_claims(w, sb, b0, b1, ctag(t, k))) {
+                        sb.colourOf[k] = r;
+                        if (dyn(w, b0)) sb.taken[b0] = r;
+                        if (dyn(w, b1)) sb.taken[b1] = r;
+                        atomicAdd(&shWin, 1);
+                        atomicAdd(&lc[r], 1);
+                    }
+                }
+                __syncthreads();
+                const int won = shWin;
+                if (threadIdx.x == 0) shDone += won;
+                __syncthreads();
+                if (won == 0) break;
             }
         }
-        grid_barrier(w.ctr, nb);
+        if (threadIdx.x == 0) {
+            if (shDone < s1 - s0) atomicOr(&w.ctr[C_STATUS], ST_CAPACITY);
+            sb.nLocal[part] = r;
+            int* st = sb.lcStart + part * (MAX_LOCAL + 1);
+            int run = s0;
+            for (int c = 0; c < r; c++) { st[c] = run; run += __ldcg(&lc[c]); }
+            st[r] = run;
+        }
+        __syncthreads();
     }
-    if (round >= MAX_COLOURS && __ldcg(&w.ctr[C_REMAIN0 + (round & 1)]) != 0) {
-        if (tid == 0) atomicOr(&w.ctr[C_STATUS], ST_CAPACITY);
-        round = MAX_COLOURS;
+    // cut manifolds, grid-wide
+    grid_barrier(w.ctr, nb);
+    const int c0 = sb.bucketStart[sb.nParts], c1 = sb.bucketStart[sb.nParts + 1];
+    const int nCut = c1 - c0;
+    int g = 0, round = 0;
+    for (; round < MAX_COLOURS; round++) {
+        if (__ldcg(&w.ctr[C_CUT_DONE]) >= nCut) break;
+        const int mark = (1 << 20) | round;
+        for (int sub = 0; sub < MAX_SUB; sub++, g++) {
+            const int t = (MAX_LOCAL + 1 + round) * MAX_SUB + sub;
+            if (tid == 0) w.ctr[C_WIN0 + (g + 1) % 3] = 0;
+            for (int i = c0 + tid; i < c1; i += nth) {
+                int k = sb.bucketList[i], b0, b1;
+                if (!eligible(w, P, sb, k, mark, b0, b1)) continue;
+                if (dyn(w, b0)) atomicMin(&sb.claim[b0], ctag(t, k));
+                if (dyn(w, b1)) atomicMin(&sb.claim[b1], ctag(t, k));
+            }
+            grid_barrier(w.ctr, nb);
+            int won = 0;
+            for (int i = c0 + tid; i < c1; i += nth) {
+                int k = sb.bucketList[i], b0, b1;
+                if (!eligible(w, P, sb, k, mark, b0, b1)) continue;
+                if (holds_claims(w, sb, b0, b1, ctag(t, k))) {
+                    sb.colourOf[k] = round;
+                    if (dyn(w, b0)) sb.taken[b0] = mark;
+                    if (dyn(w, b1)) sb.taken[b1] = mark;
+                    atomicAdd(&sb.colourCount[round], 1);
+                    won++;
+                }
+            }
+            if (won) { atomicAdd(&w.ctr[C_WIN0 + g % 3], won); atomicAdd(&w.ctr[C_CUT_DONE], won); }
+            grid_barrier(w.ctr, nb);
+            if (__ldcg(&w.ctr[C_WIN0 + g % 3]) == 0) { g++; break; }
+        }
     }
     if (tid == 0) {
-        int run = 0;
+        if (__ldcg(&w.ctr[C_CUT_DONE]) < nCut) atomicOr(&w.ctr[C_STATUS], ST_CAPACITY);
+        int run = c0;
         for (int c = 0; c < round; c++) { sb.colourStart[c] = run; run += __ldcg(&sb.colourCount[c]); }
         sb.colourStart[round] = run;
         *sb.nColours = round;
-        w.ctr[C_COLOURS] = round;
+        int maxLocal = 0;
+        for (int p = 0; p < sb.nParts; p++) maxLocal = max(maxLocal, __ldcg(&sb.nLocal[p]));
+        w.ctr[C_COLOURS] = round + maxLocal;
     }
 }
 
-// Slot assignment (kept out of the cooperative kernel for clarity): slot -> pair.
-__global__ void k_slots(SolverBuffers sb, DevRows rows) {
+// Slot of each candidate: internal ones by (part, local colour), cut ones by colour.  Candidates
+// left uncoloured (capacity exceeded, reported as an error) fill the rest of their bucket so
+// that every slot below nCand names a valid pair; they are set up but never solved.
+__global__ void k_slots(DevWorld w, DevPairs P, SolverBuffers sb, DevRows R) {
     int nCand = *sb.nCand;
-    int nCol = *sb.nColours;
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nCand) return;
-    int c = sb.colourOf[k];
-    if (c >= nCol) return;
-    int slot = sb.colourStart[c] + atomicAdd(&sb.colourFill[c], 1);
-    rows.slot_pair[slot] = sb.cand[k];
+    int b = sb.bucket[k], c = sb.colourOf[k];
+    int slot;
+    if (b < sb.nParts) {
+        int* fill = sb.lcFill + b * (MAX_LOCAL + 1);
+        const int* st = sb.lcStart + b * (MAX_LOCAL + 1);
+        if (c < 0) c = sb.nLocal[b];
+        slot = st[c] + atomicAdd(&fill[c], 1);
+    } else {
+        if (c < 0) c = *sb.nColours;
+        slot = sb.colourStart[c] + atomicAdd(&sb.colourFill[c], 1);
+    }
+    int p = sb.cand[k];
+    R.slot_pair[slot] = p;
+    int b0 = P.b0[p], b1 = P.b1[p];
+    int lb0 = 0xffff, lb1 = 0xffff;
+    if (b < sb.nParts && sb.partSmem) {
+        int ps = sb.partStart[b];
+        if (dyn(w, b0)) lb0 = sb.posOf[b0] - ps;
+        if (dyn(w, b1)) lb1 = sb.posOf[b1] - ps;
+    }
+    R.slot_desc[slot] = make_int4(b0, b1, 0, lb0 | (lb1 << 16));
 }
 
 // ---- row setup (solveGroupCacheFriendlySetup, java:418-786) -------------------------------
@@ -271,8 +420,8 @@ __global__ void k_setup(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, 
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nSlots) return;
     int p = R.slot_pair[s];
-    int b0 = P.b0[p], b1 = P.b1[p];
-    BodyV A = load_body(w, b0), B = load_body(w, b1);
+    int4 desc = R.slot_desc[s];
+    BodyV A = load_body(w, desc.x), B = load_body(w, desc.y);
     const bool warm = (w.solverMode & 4) != 0;
     int n = P.n[p];
     int mask = 0;
@@ -327,11 +476,13 @@ __global__ void k_setup(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, 
         friction_row(R, ni * 2 + 0, dir1, rp1, rp2, A, B, warm ? __fmul_rn(im.x, w.warm) : 0.0f);
         friction_row(R, ni * 2 + 1, dir2, rp1, rp2, A, B, warm ? __fmul_rn(im.y, w.warm) : 0.0f);
     }
-    R.slot_mask[s] = mask;
+    desc.z = mask;
+    R.slot_desc[s] = desc;
+    R.slot_im[s] = make_float2(A.im, B.im);
     atomicAdd(&w.ctr[C_ROWS], __popc(mask));
 }
 
-// ---- PGS (cooperative) --------------------------------------------------------------------
+// ---- PGS (cooperative) ---------------------------------------------------------------------
 JBD void apply_imp(V& lin, V& ang, V n, float im, V angc, float imp) {   // SolverBody.internalApplyImpulse
     if (im != 0.0f) {
         V lc = scl(n, im);
@@ -344,165 +495,289 @@ JBD void apply_imp(V& lin, V& ang, V n, float im, V angc, float imp) {   // Solv
     }
 }
 
-struct Vel { V l0, a0, l1, a1; float im0, im1; };
+enum { PH_WARM = 0, PH_NORMAL = 1, PH_FRICTION = 2 };
 
-JBD void load_vel(const DevWorld& w, int b0, int b1, Vel& v) {
-    float4 t;
-    t = __ldcg(&w.linvel[b0]); v.l0 = mk(t.x, t.y, t.z);
-    t = __ldcg(&w.angvel[b0]); v.a0 = mk(t.x, t.y, t.z);
-    t = __ldcg(&w.linvel[b1]); v.l1 = mk(t.x, t.y, t.z);
-    t = __ldcg(&w.angvel[b1]); v.a1 = mk(t.x, t.y, t.z);
-    v.im0 = w.iloc[b0].w;
-    v.im1 = w.iloc[b1].w;
-}
-JBD void store_vel(const DevWorld& w, int b0, int b1, const Vel& v) {
-    if (v.im0 != 0.0f) { __stcg(&w.linvel[b0], f4(v.l0, 0.0f)); __stcg(&w.angvel[b0], f4(v.a0, 0.0f)); }
-    if (v.im1 != 0.0f) { __stcg(&w.linvel[b1], f4(v.l1, 0.0f)); __stcg(&w.angvel[b1], f4(v.a1, 0.0f)); }
+// The rows of one manifold for one phase, on velocities held in registers.  Warm start applies
+// per point the normal, then both friction impulses (setup order, java:680-760).
+JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int mask, int kind, V& l0, V& a0, V& l1, V& a1,
+                        float im0, float im1, float dt) {
+    for (int j = 0; j < 4; j++) {
+        if (!(mask & (1 << j))) continue;
+        const int ni = s * 4 + j;
+        if (kind == PH_WARM) {
+            float4 nn = R.n_nrm[ni];
+            V n = mk(nn.x, nn.y, nn.z);
+            float imp = R.n_angB[ni].w;
+            apply_imp(l0, a0, n, im0, mk4(R.n_angA[ni]), imp);
+            apply_imp(l1, a1, n, im1, mk4(R.n_angB[ni]), -imp);
+            for (int f = 0; f < 2; f++) {
+                int fi = ni * 2 + f;
+                V d = mk4(R.f_nrm[fi]);
+                float fimp = R.f_rp1[fi].w;
+                apply_imp(l0, a0, d, im0, mk4(R.f_angA[fi]), fimp);
+                apply_imp(l1, a1, d, im1, mk4(R.f_angB[fi]), -fimp);
+            }
+        } else if (kind == PH_NORMAL) {   // resolveSingleCollisionCombinedCacheFriendly (java:234-284)
+            float4 nn = R.n_nrm[ni], r1 = R.n_rp1[ni], r2 = R.n_rp2[ni], aA = R.n_angA[ni];
+            float4 aB = __ldcg(&R.n_angB[ni]);
+            V n = mk(nn.x, nn.y, nn.z);
+            float vel1 = __fadd_rn(dot(n, l0), dot(mk(r1.x, r1.y, r1.z), a0));
+            float vel2 = __fadd_rn(dot(n, l1), dot(mk(r2.x, r2.y, r2.z), a1));
+            float rel = __fsub_rn(vel1, vel2);
+            float posErr = jdiv(__fmul_rn(-r1.w, w.erp), dt);
+            float velErr = __fsub_rn(r2.w, rel);
+            float ni1 = __fadd_rn(__fmul_rn(posErr, nn.w), __fmul_rn(velErr, nn.w));
+            float old = aB.w;
+            float sum = __fadd_rn(old, ni1);
+            float acc = 0.0f > sum ? 0.0f : sum;
+            float d = __fsub_rn(acc, old);
+            apply_imp(l0, a0, n, im0, mk(aA.x, aA.y, aA.z), d);
+            apply_imp(l1, a1, n, im1, mk(aB.x, aB.y, aB.z), -d);
+            aB.w = acc;
+            __stcg(&R.n_angB[ni], aB);
+        } else {                          // resolveSingleFrictionCacheFriendly (java:286-346)
+            float total = __fadd_rn(__ldcg(&R.n_angB[ni]).w, 0.0f);   // appliedImpulse + appliedPushImpulse
+            float fric = R.n_angA[ni].w;
+            float limit = __fmul_rn(total, fric);
+            if (!(total > 0.0f)) continue;
+            for (int f = 0; f < 2; f++) {
+                int fi = ni * 2 + f;
+                float4 fn = R.f_nrm[fi];
+                float4 r1 = __ldcg(&R.f_rp1[fi]);
+                float4 r2 = R.f_rp2[fi];
+                V n = mk(fn.x, fn.y, fn.z);
+                float vel1 = __fadd_rn(dot(n, l0), dot(mk(r1.x, r1.y, r1.z), a0));
+                float vel2 = __fadd_rn(dot(n, l1), dot(mk(r2.x, r2.y, r2.z), a1));
+                float rel = __fsub_rn(vel1, vel2);
+                float j1 = __fmul_rn(-rel, fn.w);
+                float old = r1.w;
+                float acc = __fadd_rn(old, j1);
+                if (limit < acc) acc = limit;
+                else if (acc < -limit) acc = -limit;
+                j1 = __fsub_rn(acc, old);
+                apply_imp(l0, a0, n, im0, mk4(R.f_angA[fi]), j1);
+                apply_imp(l1, a1, n, im1, mk4(R.f_angB[fi]), -j1);
+                r1.w = acc;
+                __stcg(&R.f_rp1[fi], r1);
+            }
+        }
+    }
 }
 
-__global__ void k_pgs(DevWorld w, DevPairs P, DevRows R, const int* nColoursPtr, const int* nCandPtr, float dt) {
+JBD void gload(const DevWorld& w, int b, V& l, V& a) {
+    float4 t = __ldcg(&w.linvel[b]);
+    l = mk(t.x, t.y, t.z);
+    t = __ldcg(&w.angvel[b]);
+    a = mk(t.x, t.y, t.z);
+}
+JBD void gstore(const DevWorld& w, int b, V l, V a) {
+    __stcg(&w.linvel[b], f4(l, 0.0f));
+    __stcg(&w.angvel[b], f4(a, 0.0f));
+}
+
+// write-back (java:901-912): appliedImpulse; appliedImpulseLateral1 ends as friction row 2's
+JBD void writeback_slot(const DevPairs& P, const DevRows& R, int s) {
+    int p = R.slot_pair[s];
+    int mask = R.slot_desc[s].z;
+    for (int j = 0; j < 4; j++) {
+        if (!(mask & (1 << j))) continue;
+        int ni = s * 4 + j, k = p * 4 + j;
+        float4 nr = P.nrm[k];
+        nr.w = __ldcg(&R.n_angB[ni]).w;
+        P.nrm[k] = nr;
+        float4 im = P.imp[k];
+        im.x = __ldcg(&R.f_rp1[ni * 2 + 1]).w;
+        P.imp[k] = im;
+    }
+}
+
+struct PartView {
+    int ps, np, nLoc;
+    const int* lcs;
+};
+
+JBD PartView part_view(const SolverBuffers& sb, int part) {
+    PartView v;
+    v.ps = sb.partStart[part];
+    v.np = sb.partStart[part + 1] - v.ps;
+    v.nLoc = sb.nLocal[part];
+    v.lcs = sb.lcStart + part * (MAX_LOCAL + 1);
+    return v;
+}
+
+// Velocities of the part's bodies to shared memory and back (static and kinematic bodies are
+// never written).
+JBD void stage_in(const DevWorld& w, const SolverBuffers& sb, const PartView& v, float4* sl, float4* sa) {
+    for (int i = threadIdx.x; i < v.np; i += blockDim.x) {
+        int b = sb.order[v.ps + i];
+        sl[i] = __ldcg(&w.linvel[b]);
+        sa[i] = __ldcg(&w.angvel[b]);
+    }
+}
+JBD void stage_out(const DevWorld& w, const SolverBuffers& sb, const PartView& v, const float4* sl, const float4* sa) {
+    for (int i = threadIdx.x; i < v.np; i += blockDim.x) {
+        int b = sb.order[v.ps + i];
+        if (w.iloc[b].w != 0.0f) { __stcg(&w.linvel[b], sl[i]); __stcg(&w.angvel[b], sa[i]); }
+    }
+}
+
+// One local colour of a part: its manifolds share no dynamic body; the part's bodies are in
+// shared memory (global memory when the part does not fit).
+JBD void local_colour(const DevWorld& w, const DevRows& R, int s0, int s1, int kind, bool smem, float4* sl, float4* sa,
+                      float dt) {
+    for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+        const int4 d = R.slot_desc[s];
+        const float2 im = R.slot_im[s];
+        const int lb0 = d.w & 0xffff, lb1 = (d.w >> 16) & 0xffff;
+        const bool m0 = smem && lb0 != 0xffff, m1 = smem && lb1 != 0xffff;
+        V l0, a0, l1, a1;
+        if (m0) { l0 = mk4(sl[lb0]); a0 = mk4(sa[lb0]); } else gload(w, d.x, l0, a0);
+        if (m1) { l1 = mk4(sl[lb1]); a1 = mk4(sa[lb1]); } else gload(w, d.y, l1, a1);
+        solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, dt);
+        if (im.x != 0.0f) { if (m0) { sl[lb0] = f4(l0, 0.0f); sa[lb0] = f4(a0, 0.0f); } else gstore(w, d.x, l0, a0); }
+        if (im.y != 0.0f) { if (m1) { sl[lb1] = f4(l1, 0.0f); sa[lb1] = f4(a1, 0.0f); } else gstore(w, d.y, l1, a1); }
+    }
+}
+
+JBD int phase_kind(int ph) { return ph == 0 ? PH_WARM : ((ph - 1) % 2 == 0 ? PH_NORMAL : PH_FRICTION); }
+
+// Phases: warm start, then numIterations x (normal rows, friction rows).  Within a phase the
+// parts' internal manifolds run first (parts share no dynamic body), then the cut colours.
+// Without cut manifolds every part runs all phases on its own, with no grid barrier.
+__global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs P, DevRows R, SolverBuffers sb, float dt) {
+    extern __shared__ float4 smv[];
     const int nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
-    const int nCol = *nColoursPtr;
-    const int nSlots = *nCandPtr;
-    // warm start, in setup order within each manifold: normal, friction 1, friction 2 per point
-    for (int c = 0; c < nCol; c++) {
-        int s0 = R.colour_start[c], s1 = R.colour_start[c + 1];
-        for (int s = s0 + tid; s < s1; s += nth) {
-            int p = R.slot_pair[s];
-            int b0 = P.b0[p], b1 = P.b1[p];
-            Vel v;
-            load_vel(w, b0, b1, v);
-            int mask = R.slot_mask[s];
-            for (int j = 0; j < 4; j++) {
-                if (!(mask & (1 << j))) continue;
-                int ni = s * 4 + j;
-                float4 nn = R.n_nrm[ni];
-                V n = mk(nn.x, nn.y, nn.z);
-                float imp = R.n_angB[ni].w;
-                apply_imp(v.l0, v.a0, n, v.im0, mk4(R.n_angA[ni]), imp);
-                apply_imp(v.l1, v.a1, n, v.im1, mk4(R.n_angB[ni]), -imp);
-                for (int f = 0; f < 2; f++) {
-                    int fi = ni * 2 + f;
-                    V d = mk4(R.f_nrm[fi]);
-                    float fimp = R.f_rp1[fi].w;
-                    apply_imp(v.l0, v.a0, d, v.im0, mk4(R.f_angA[fi]), fimp);
-                    apply_imp(v.l1, v.a1, d, v.im1, mk4(R.f_angB[fi]), -fimp);
+    const int nCut = *sb.nColours;
+    const int nSlots = *sb.nCand;
+    const bool smem = sb.partSmem != 0;
+    float4* sl = smv;
+    float4* sa = smv + sb.partMax;
+    const int nPhases = 1 + 2 * w.numIter;
+    if (nCut == 0) {
+        for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
+            const PartView v = part_view(sb, part);
+            if (smem) stage_in(w, sb, v, sl, sa);
+            __syncthreads();
+            for (int ph = 0; ph < nPhases; ph++) {
+                const int kind = phase_kind(ph);
+                for (int c = 0; c < v.nLoc; c++) {
+                    local_colour(w, R, v.lcs[c], v.lcs[c + 1], kind, smem, sl, sa, dt);
+                    __syncthreads();
                 }
             }
-            store_vel(w, b0, b1, v);
+            if (smem) stage_out(w, sb, v, sl, sa);
+            for (int s = sb.bucketStart[part] + threadIdx.x; s < sb.bucketStart[part + 1]; s += blockDim.x)
+                writeback_slot(P, R, s);
+            __syncthreads();
+        }
+        return;
+    }
+    for (int ph = 0; ph < nPhases; ph++) {
+        const int kind = phase_kind(ph);
+        for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
+            const PartView v = part_view(sb, part);
+            if (smem) stage_in(w, sb, v, sl, sa);
+            __syncthreads();
+            for (int c = 0; c < v.nLoc; c++) {
+                local_colour(w, R, v.lcs[c], v.lcs[c + 1], kind, smem, sl, sa, dt);
+                __syncthreads();
+            }
+            if (smem) stage_out(w, sb, v, sl, sa);
+            __syncthreads();
         }
         grid_barrier(w.ctr, nb);
-    }
-    for (int it = 0; it < w.numIter; it++) {
-        for (int c = 0; c < nCol; c++) {      // resolveSingleCollisionCombinedCacheFriendly (java:234-284)
-            int s0 = R.colour_start[c], s1 = R.colour_start[c + 1];
+        for (int c = 0; c < nCut; c++) {
+            const int s0 = sb.colourStart[c], s1 = sb.colourStart[c + 1];
             for (int s = s0 + tid; s < s1; s += nth) {
-                int p = R.slot_pair[s];
-                int b0 = P.b0[p], b1 = P.b1[p];
-                Vel v;
-                load_vel(w, b0, b1, v);
-                int mask = R.slot_mask[s];
-                for (int j = 0; j < 4; j++) {
-                    if (!(mask & (1 << j))) continue;
-                    int ni = s * 4 + j;
-                    float4 nn = R.n_nrm[ni], r1 = R.n_rp1[ni], r2 = R.n_rp2[ni], aA = R.n_angA[ni];
-                    float4 aB = __ldcg(&R.n_angB[ni]);
-                    V n = mk(nn.x, nn.y, nn.z);
-                    float vel1 = __fadd_rn(dot(n, v.l0), dot(mk(r1.x, r1.y, r1.z), v.a0));
-                    float vel2 = __fadd_rn(dot(n, v.l1), dot(mk(r2.x, r2.y, r2.z), v.a1));
-                    float rel = __fsub_rn(vel1, vel2);
-                    float posErr = jdiv(__fmul_rn(-r1.w, w.erp), dt);
-                    float velErr = __fsub_rn(r2.w, rel);
-                    float ni1 = __fadd_rn(__fmul_rn(posErr, nn.w), __fmul_rn(velErr, nn.w));
-                    float old = aB.w;
-                    float sum = __fadd_rn(old, ni1);
-                    float acc = 0.0f > sum ? 0.0f : sum;
-                    float d = __fsub_rn(acc, old);
-                    apply_imp(v.l0, v.a0, n, v.im0, mk(aA.x, aA.y, aA.z), d);
-                    apply_imp(v.l1, v.a1, n, v.im1, mk(aB.x, aB.y, aB.z), -d);
-                    aB.w = acc;
-                    __stcg(&R.n_angB[ni], aB);
-                }
-                store_vel(w, b0, b1, v);
-            }
-            grid_barrier(w.ctr, nb);
-        }
-        for (int c = 0; c < nCol; c++) {      // resolveSingleFrictionCacheFriendly (java:286-346)
-            int s0 = R.colour_start[c], s1 = R.colour_start[c + 1];
-            for (int s = s0 + tid; s < s1; s += nth) {
-                int p = R.slot_pair[s];
-                int b0 = P.b0[p], b1 = P.b1[p];
-                Vel v;
-                load_vel(w, b0, b1, v);
-                int mask = R.slot_mask[s];
-                for (int j = 0; j < 4; j++) {
-                    if (!(mask & (1 << j))) continue;
-                    int ni = s * 4 + j;
-                    float total = __fadd_rn(__ldcg(&R.n_angB[ni]).w, 0.0f);   // appliedImpulse + appliedPushImpulse
-                    float fric = R.n_angA[ni].w;
-                    float limit = __fmul_rn(total, fric);
-                    if (!(total > 0.0f)) continue;
-                    for (int f = 0; f < 2; f++) {
-                        int fi = ni * 2 + f;
-                        float4 fn = R.f_nrm[fi];
-                        float4 r1 = __ldcg(&R.f_rp1[fi]);
-                        float4 r2 = R.f_rp2[fi];
-                        V n = mk(fn.x, fn.y, fn.z);
-                        float vel1 = __fadd_rn(dot(n, v.l0), dot(mk(r1.x, r1.y, r1.z), v.a0));
-                        float vel2 = __fadd_rn(dot(n, v.l1), dot(mk(r2.x, r2.y, r2.z), v.a1));
-                        float rel = __fsub_rn(vel1, vel2);
-                        float j1 = __fmul_rn(-rel, fn.w);
-                        float old = r1.w;
-                        float acc = __fadd_rn(old, j1);
-                        if (limit < acc) acc = limit;
-                        else if (acc < -limit) acc = -limit;
-                        j1 = __fsub_rn(acc, old);
-                        apply_imp(v.l0, v.a0, n, v.im0, mk4(R.f_angA[fi]), j1);
-                        apply_imp(v.l1, v.a1, n, v.im1, mk4(R.f_angB[fi]), -j1);
-                        r1.w = acc;
-                        __stcg(&R.f_rp1[fi], r1);
-                    }
-                }
-                store_vel(w, b0, b1, v);
+                const int4 d = R.slot_desc[s];
+                const float2 im = R.slot_im[s];
+                V l0, a0, l1, a1;
+                gload(w, d.x, l0, a0);
+                gload(w, d.y, l1, a1);
+                solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, dt);
+                if (im.x != 0.0f) gstore(w, d.x, l0, a0);
+                if (im.y != 0.0f) gstore(w, d.y, l1, a1);
             }
             grid_barrier(w.ctr, nb);
         }
     }
-    // write-back (java:901-912): appliedImpulse; appliedImpulseLateral1 ends as friction row 2's
-    for (int s = tid; s < nSlots; s += nth) {
-        int p = R.slot_pair[s];
-        int mask = R.slot_mask[s];
-        for (int j = 0; j < 4; j++) {
-            if (!(mask & (1 << j))) continue;
-            int ni = s * 4 + j, k = p * 4 + j;
-            float4 nr = P.nrm[k];
-            nr.w = __ldcg(&R.n_angB[ni]).w;
-            P.nrm[k] = nr;
-            float4 im = P.imp[k];
-            im.x = __ldcg(&R.f_rp1[ni * 2 + 1]).w;
-            P.imp[k] = im;
-        }
-    }
+    for (int s = tid; s < nSlots; s += nth) writeback_slot(P, R, s);
 }
 
-int solver_coop_blocks(bool pgs) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int per = 0;
-    if (pgs) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pgs, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_colour, 256, 0);
-    if (per < 1) per = 1;
-    return sms * (per < 2 ? per : 2);
+// ---- host side ------------------------------------------------------------------------------
+template <class T> static cudaError_t salloc(T** p, size_t n) {
+    return cudaMalloc((void**)p, sizeof(T) * (n ? n : 1));
+}
+template <class T> static void sfree(T*& p) { if (p) cudaFree((void*)p); p = nullptr; }
+
+static size_t pgs_smem(const SolverBuffers& sb) { return sb.partSmem ? (size_t)sb.partMax * 32 : 0; }
+
+int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts) {
+    int maxWorld = 0;
+    for (int c : worldCounts) maxWorld = std::max(maxWorld, c);
+    std::vector<int> start;
+    int parts;
+    if (rangeParts <= 0 && !worldCounts.empty() && maxWorld <= PART_MAX_BODIES) {
+        sb.worldParts = 1;
+        parts = (int)worldCounts.size();
+        start.resize(parts + 1);
+        start[0] = 0;
+        for (int p = 0; p < parts; p++) start[p + 1] = start[p] + worldCounts[p];
+    } else {
+        sb.worldParts = 0;
+        const int minParts = (nFinite + PART_MAX_BODIES - 1) / PART_MAX_BODIES;
+        parts = std::max(rangeParts > 0 ? rangeParts : 2 * sms, minParts);
+        parts = std::max(1, std::min(parts, std::max(nFinite, 1)));
+        start.resize(parts + 1);
+        for (int p = 0; p <= parts; p++) start[p] = (int)(((long long)p * nFinite + parts - 1) / parts);
+    }
+    int partMax = 1;
+    for (int p = 0; p < parts; p++) partMax = std::max(partMax, start[p + 1] - start[p]);
+    if (parts > sb.partsCap) {
+        sfree(sb.bucketCount); sfree(sb.bucketFill); sfree(sb.bucketStart);
+        sfree(sb.lcCount); sfree(sb.lcFill); sfree(sb.lcStart); sfree(sb.nLocal); sfree(sb.partStart);
+        size_t lc = (size_t)parts * (MAX_LOCAL + 1);
+        if (salloc(&sb.bucketCount, parts + 2) || salloc(&sb.bucketFill, parts + 2) || salloc(&sb.bucketStart, parts + 2) ||
+            salloc(&sb.lcCount, lc) || salloc(&sb.lcFill, lc) || salloc(&sb.lcStart, lc) || salloc(&sb.nLocal, parts) ||
+            salloc(&sb.partStart, parts + 1)) {
+            sb.partsCap = 0;
+            return JBGPU_ERR_CUDA;
+        }
+        sb.partsCap = parts;
+    }
+    if (cudaMemcpy(sb.partStart, start.data(), sizeof(int) * (parts + 1), cudaMemcpyHostToDevice) != cudaSuccess)
+        return JBGPU_ERR_CUDA;
+    sb.nFinite = nFinite;
+    sb.nParts = parts;
+    sb.partMax = partMax;
+    sb.partSmem = (partMax < 0xffff && (size_t)partMax * 32 <= 96 * 1024) ? 1 : 0;
+    size_t smem = pgs_smem(sb);
+    if (cudaFuncSetAttribute(k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) != cudaSuccess)
+        return JBGPU_ERR_CUDA;
+    int perPgs = 0, perColour = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perPgs, k_pgs, SOLVER_THREADS, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perColour, k_colour, SOLVER_THREADS, 0) != cudaSuccess ||
+        perPgs < 1 || perColour < 1)
+        return JBGPU_ERR_CUDA;
+    sb.gridPgs = std::min(parts, perPgs * sms);
+    sb.gridColour = std::min(parts, perColour * sms);
+    return JBGPU_OK;
+}
+
+void solver_free(SolverBuffers& sb) {
+    sfree(sb.bucketCount); sfree(sb.bucketFill); sfree(sb.bucketStart);
+    sfree(sb.lcCount); sfree(sb.lcFill); sfree(sb.lcStart); sfree(sb.nLocal); sfree(sb.partStart);
+    sfree(sb.orderFallback);
+    sb.partsCap = 0;
 }
 
 void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, SolverBuffers& sb, float dt, cudaStream_t s,
                   const Prof* prof) {
     if (prof) prof->mark(PH_COLOUR, 0, s);
-    if (nPairs <= 0) {
+    if (nPairs <= 0 || sb.nFinite <= 0 || sb.nParts <= 0) {
         cudaMemsetAsync(sb.nColours, 0, sizeof(int), s);
+        cudaMemsetAsync(sb.nCand, 0, sizeof(int), s);
         if (prof) {
             prof->mark(PH_COLOUR, 1, s);
             prof->mark(PH_SETUP, 0, s); prof->mark(PH_SETUP, 1, s);
@@ -510,17 +785,27 @@ void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, Solver
         }
         return;
     }
+    const int parts = sb.nParts;
     cudaMemsetAsync(sb.claim, 0xff, sizeof(unsigned long long) * w.nBodies, s);
+    cudaMemsetAsync(sb.taken, 0xff, sizeof(int) * w.nBodies, s);
+    cudaMemsetAsync(sb.posOf, 0xff, sizeof(int) * w.nBodies, s);
+    cudaMemsetAsync(sb.bucketCount, 0, sizeof(int) * (parts + 2), s);
+    cudaMemsetAsync(sb.bucketFill, 0, sizeof(int) * (parts + 2), s);
+    cudaMemsetAsync(sb.lcFill, 0, sizeof(int) * parts * (MAX_LOCAL + 1), s);
+    cudaMemsetAsync(sb.colourFill, 0, sizeof(int) * (MAX_COLOURS + 1), s);
     cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
+    k_posof<<<gridn(sb.nFinite, 256), 256, 0, s>>>(sb); note_launch();
+    k_classify<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, sb); note_launch();
+    exclusive_scan(sb.bucketCount, sb.bucketStart, nullptr, parts + 2, sb.scanScratch, s);
+    k_bucket_scatter<<<gridn(nPairs, 256), 256, 0, s>>>(sb); note_launch();
     {
         DevWorld wc = w;
         DevPairs pc = P;
         SolverBuffers sc = sb;
         void* args[] = {&wc, &pc, &sc};
-        cudaLaunchCooperativeKernel((void*)k_colour, sb.coopBlocksColour, 256, args, 0, s); note_launch();
+        cudaLaunchCooperativeKernel((void*)k_colour, sb.gridColour, SOLVER_THREADS, args, 0, s); note_launch();
     }
-    cudaMemsetAsync(sb.colourFill, 0, sizeof(int) * (MAX_COLOURS + 1), s);
-    k_slots<<<gridn(nPairs, 256), 256, 0, s>>>(sb, R); note_launch();
+    k_slots<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, sb, R); note_launch();
     if (prof) { prof->mark(PH_COLOUR, 1, s); prof->mark(PH_SETUP, 0, s); }
     k_setup<<<gridn(nPairs, 128), 128, 0, s>>>(w, P, R, sb.nCand, dt); note_launch();
     if (prof) { prof->mark(PH_SETUP, 1, s); prof->mark(PH_PGS, 0, s); }
@@ -529,11 +814,10 @@ void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, Solver
         DevWorld wc = w;
         DevPairs pc = P;
         DevRows rc = R;
-        const int* ncol = sb.nColours;
-        const int* ncand = sb.nCand;
+        SolverBuffers sc = sb;
         float dtc = dt;
-        void* args[] = {&wc, &pc, &rc, &ncol, &ncand, &dtc};
-        cudaLaunchCooperativeKernel((void*)k_pgs, sb.coopBlocksPgs, 256, args, 0, s); note_launch();
+        void* args[] = {&wc, &pc, &rc, &sc, &dtc};
+        cudaLaunchCooperativeKernel((void*)k_pgs, sb.gridPgs, SOLVER_THREADS, args, pgs_smem(sb), s); note_launch();
     }
     if (prof) prof->mark(PH_PGS, 1, s);
 }

@@ -1,8 +1,19 @@
 #pragma once
+#include <vector>
 #include "jbgpu_internal.cuh"
 
 namespace jbg {
 
+constexpr int MAX_COLOURS = 1024;     // grid-wide colours of cut manifolds
+constexpr int MAX_LOCAL = 128;        // colours of the manifolds internal to one part
+constexpr int MAX_SUB = 16;           // claim passes that grow one colour towards a maximal set
+constexpr int SOLVER_THREADS = 256;
+constexpr int PART_MAX_BODIES = 2048; // bodies of one part (velocities staged in 64 KB of shared memory)
+
+// Solver parts.  Dynamic bodies are split into parts of consecutive positions in a body order
+// (the broadphase's sorted leaf order: Morton code with the batch world in the high bits).
+// World parts: every world holds at most PART_MAX_BODIES finite bodies, and each world is one
+// part.  Range parts otherwise: nParts equal ranges of the order.
 struct SolverBuffers {
     int* parent = nullptr;        // union-find (bodies)
     int* keepAwake = nullptr;     // per island root
@@ -10,25 +21,45 @@ struct SolverBuffers {
     int* flag = nullptr;          // per pair: manifold is solved this step
     int* candIdx = nullptr;       // exclusive scan of flag
     int* cand = nullptr;          // pair index of candidate k (ascending)
-    int* colourOf = nullptr;      // colour of candidate k
-    int* remA = nullptr;          // colouring work lists
-    int* remB = nullptr;
+    int* colourOf = nullptr;      // colour of candidate k (local colour for internal ones)
+    int* bucket = nullptr;        // part of candidate k, nParts when cut
+    int* bucketList = nullptr;    // candidates grouped by bucket
     unsigned long long* claim = nullptr;  // per body
-    int* colourCount = nullptr;   // per colour (MAX_COLOURS + 1)
+    int* taken = nullptr;         // per body: colouring round that took it
+    int* posOf = nullptr;         // per body: position in the body order (-1 none)
+    int* colourCount = nullptr;   // per cut colour (MAX_COLOURS + 1)
     int* colourFill = nullptr;
     int* colourStart = nullptr;
     int* nCand = nullptr;         // device scalars
-    int* nColours = nullptr;
+    int* nColours = nullptr;      // cut colours
     void* scanScratch = nullptr;
-    int coopBlocksColour = 0;
-    int coopBlocksPgs = 0;
+    // part tables (capacity partsCap)
+    int* bucketCount = nullptr;   // nParts + 2
+    int* bucketFill = nullptr;
+    int* bucketStart = nullptr;
+    int* lcCount = nullptr;       // nParts * (MAX_LOCAL + 1)
+    int* lcFill = nullptr;
+    int* lcStart = nullptr;
+    int* nLocal = nullptr;        // nParts
+    int* partStart = nullptr;     // nParts + 1 positions of the body order
+    int* orderFallback = nullptr; // body order built on the host when the broadphase order is stale
+    const int* order = nullptr;   // body order in use
+    int nFinite = 0;
+    int nParts = 0;
+    int partsCap = 0;
+    int partMax = 0;              // largest part, bodies
+    int partSmem = 0;             // velocities of internal manifolds staged in shared memory
+    int worldParts = 0;
+    int gridColour = 0;           // co-resident blocks of the cooperative kernels
+    int gridPgs = 0;
 };
 
-constexpr int MAX_COLOURS = 1024;
-
+// (Re)plans the parts for nFinite ordered bodies.  worldCounts: finite bodies per batch world;
+// rangeParts > 0 asks for that many range parts.
+int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts);
 void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
 void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& rows, SolverBuffers& sb, float dt, cudaStream_t s,
                   const Prof* prof = nullptr);
-int solver_coop_blocks(bool pgs);
+void solver_free(SolverBuffers& sb);
 
 }  // namespace jbg

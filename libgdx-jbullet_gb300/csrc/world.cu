@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/jbgpu.h"
@@ -84,6 +85,10 @@ struct jbgpu_world {
     std::vector<int> hShape, hWorld, hFlags;
     int nWorlds = 1;
     bool planesDirty = true;
+    std::vector<int> worldFinite;   // finite (non-plane) bodies per batch world
+    bool orderValid = false;        // the broadphase leaf order covers every body added
+    bool solverDirty = true;        // solver parts must be planned again
+    int solverOrderFinite = -1;     // nFinite the parts were planned for
     DevWorld dw{};
     // pairs: two buffers, cur holds the pairs of the last broadphase
     DevPairs pairs[2]{};
@@ -128,15 +133,15 @@ int alloc_pair_work(jbgpu_world* w, int cap) {
     DevRows& R = w->rows;
     dfree(R.n_nrm); dfree(R.n_rp1); dfree(R.n_rp2); dfree(R.n_angA); dfree(R.n_angB);
     dfree(R.f_nrm); dfree(R.f_rp1); dfree(R.f_rp2); dfree(R.f_angA); dfree(R.f_angB);
-    dfree(R.slot_pair); dfree(R.slot_mask);
+    dfree(R.slot_pair); dfree(R.slot_desc); dfree(R.slot_im);
     size_t c4 = (size_t)cap * 4, c8 = (size_t)cap * 8;
     CK(dalloc(&R.n_nrm, c4)); CK(dalloc(&R.n_rp1, c4)); CK(dalloc(&R.n_rp2, c4)); CK(dalloc(&R.n_angA, c4)); CK(dalloc(&R.n_angB, c4));
     CK(dalloc(&R.f_nrm, c8)); CK(dalloc(&R.f_rp1, c8)); CK(dalloc(&R.f_rp2, c8)); CK(dalloc(&R.f_angA, c8)); CK(dalloc(&R.f_angB, c8));
-    CK(dalloc(&R.slot_pair, cap)); CK(dalloc(&R.slot_mask, cap));
+    CK(dalloc(&R.slot_pair, cap)); CK(dalloc(&R.slot_desc, cap)); CK(dalloc(&R.slot_im, cap));
     SolverBuffers& S = w->sb;
-    dfree(S.flag); dfree(S.candIdx); dfree(S.cand); dfree(S.colourOf); dfree(S.remA); dfree(S.remB);
+    dfree(S.flag); dfree(S.candIdx); dfree(S.cand); dfree(S.colourOf); dfree(S.bucket); dfree(S.bucketList);
     CK(dalloc(&S.flag, cap)); CK(dalloc(&S.candIdx, cap)); CK(dalloc(&S.cand, cap)); CK(dalloc(&S.colourOf, cap));
-    CK(dalloc(&S.remA, cap)); CK(dalloc(&S.remB, cap));
+    CK(dalloc(&S.bucket, cap)); CK(dalloc(&S.bucketList, cap));
     if (S.scanScratch) cudaFree(S.scanScratch);
     CK(cudaMalloc(&S.scanScratch, scan_scratch_bytes(cap)));
     if (w->nb.queue) cudaFree(w->nb.queue);
@@ -174,8 +179,9 @@ int grow_bodies(jbgpu_world* w, int need) {
     if (B.scanScratch) cudaFree(B.scanScratch);
     CK(cudaMalloc(&B.scanScratch, scan_scratch_bytes(nc + 1)));
     SolverBuffers& S = w->sb;
-    dfree(S.parent); dfree(S.keepAwake); dfree(S.inactive); dfree(S.claim);
+    dfree(S.parent); dfree(S.keepAwake); dfree(S.inactive); dfree(S.claim); dfree(S.taken); dfree(S.posOf);
     CK(dalloc(&S.parent, nc)); CK(dalloc(&S.keepAwake, nc)); CK(dalloc(&S.inactive, nc)); CK(dalloc(&S.claim, nc));
+    CK(dalloc(&S.taken, nc)); CK(dalloc(&S.posOf, nc));
     w->capBodies = nc;
     return JBGPU_OK;
 }
@@ -250,9 +256,10 @@ int sync_planes(jbgpu_world* w) {
     for (int i = 0; i < w->nBodies; i++) nw = std::max(nw, w->hWorld[i] + 1);
     std::vector<std::vector<int>> per(nw);
     int nf = 0, np = 0;
+    std::vector<int> finite(nw, 0);
     for (int i = 0; i < w->nBodies; i++) {
         if (w->hFlags[i] & CF_PLANE) { per[w->hWorld[i]].push_back(i); np++; }
-        else nf++;
+        else { nf++; finite[w->hWorld[i]]++; }
     }
     std::vector<int> list, start(nw + 1, 0);
     for (int k = 0; k < nw; k++) { start[k] = (int)list.size(); list.insert(list.end(), per[k].begin(), per[k].end()); }
@@ -269,6 +276,9 @@ int sync_planes(jbgpu_world* w) {
     while ((1 << bits) < nw) bits++;
     B.worldBits = nw > 1 ? bits : 0;
     w->nWorlds = nw;
+    w->worldFinite = finite;
+    w->solverDirty = true;
+    w->orderValid = false;
     w->planesDirty = false;
     return JBGPU_OK;
 }
@@ -297,6 +307,7 @@ int stage_pairs(jbgpu_world* w) {
     cudaStream_t s = w->stream;
     w->prof.mark(PH_PAIR_COUNT, 0, s);
     broadphase_run_count(d, w->bb, s);
+    w->orderValid = true;
     w->prof.mark(PH_PAIR_COUNT, 1, s);
     CK(cudaMemcpyAsync(w->hostPinned, w->bb.total, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -311,6 +322,32 @@ int stage_pairs(jbgpu_world* w) {
     w->cur = nxt;
     w->nPairs = total;
     CK(cudaMemcpyAsync(w->dw.ctr + C_PAIRS, w->bb.total, sizeof(int), cudaMemcpyDeviceToDevice, s));
+    return JBGPU_OK;
+}
+
+// Solver parts and the body order they index: the broadphase leaf order when it covers every
+// body, else finite bodies grouped by world in index order, built here.
+int prepare_solver(jbgpu_world* w) {
+    SolverBuffers& S = w->sb;
+    const int nf = w->bb.nFinite;
+    if (w->solverDirty) {
+        int rc = solver_configure(S, nf, w->worldFinite, w->sms, w->cfg.solver_parts);
+        if (rc) return fail(rc, "solver part tables");
+        w->solverDirty = false;
+    }
+    if (w->orderValid) {
+        S.order = w->bb.sortedBody;
+        return JBGPU_OK;
+    }
+    std::vector<int> at(w->nWorlds + 1, 0), ord(std::max(nf, 1));
+    for (int q = 0; q < w->nWorlds; q++) at[q + 1] = at[q] + w->worldFinite[q];
+    for (int i = 0; i < w->nBodies; i++)
+        if (!(w->hFlags[i] & CF_PLANE)) ord[at[w->hWorld[i]]++] = i;
+    dfree(S.orderFallback);
+    CK(dalloc(&S.orderFallback, ord.size()));
+    CK(cudaMemcpyAsync(S.orderFallback, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    S.order = S.orderFallback;
     return JBGPU_OK;
 }
 
@@ -333,10 +370,13 @@ int run_stage(jbgpu_world* w, int stage, float dt) {
         islands_launch(d, w->pairs[w->cur], w->nPairs, w->sb, s);
         P.mark(PH_ISLANDS, 1, s);
         break;
-    case JBGPU_STAGE_SOLVE:
+    case JBGPU_STAGE_SOLVE: {
+        int rc = prepare_solver(w);
+        if (rc) return rc;
         CK(cudaMemsetAsync(w->dw.ctr + C_ROWS, 0, sizeof(int), s));
         solve_launch(d, w->pairs[w->cur], w->nPairs, w->rows, w->sb, dt, s, &P);
         break;
+    }
     case JBGPU_STAGE_INTEGRATE: P.mark(PH_INTEGRATE, 0, s); launch_integrate(d, dt, s); P.mark(PH_INTEGRATE, 1, s); break;
     case JBGPU_STAGE_ACTIVATION: P.mark(PH_ACTIVATION, 0, s); launch_activation(d, dt, s); P.mark(PH_ACTIVATION, 1, s); break;
     case JBGPU_STAGE_CLEAR_FORCES: launch_clear_forces(d, s); break;
@@ -500,6 +540,7 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
     if (!(c.solver_mode & JBGPU_SOLVER_CACHE_FRIENDLY))
         return fail(JBGPU_ERR_UNSUPPORTED, "only the cache-friendly solver path is implemented");
     if (c.num_iterations < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "num_iterations < 0");
+    if (c.solver_parts < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "solver_parts < 0");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(JBGPU_ERR_NO_DEVICE, "no CUDA device");
     if (c.device < 0 || c.device >= ndev) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad device ordinal");
@@ -530,13 +571,10 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
              CK(dalloc(&S.colourCount, MAX_COLOURS + 1)); CK(dalloc(&S.colourFill, MAX_COLOURS + 1));
              CK(dalloc(&S.colourStart, MAX_COLOURS + 1)); CK(dalloc(&S.nCand, 1)); CK(dalloc(&S.nColours, 1));
              CK(cudaMemset(S.nCand, 0, sizeof(int))); CK(cudaMemset(S.nColours, 0, sizeof(int)));
-             w->rows.colour_start = S.colourStart;
-             S.coopBlocksColour = solver_coop_blocks(false);
-             S.coopBlocksPgs = solver_coop_blocks(true);
              NarrowBuffers& N = w->nb;
              N.slots = w->sms * 96;
              size_t fs = (size_t)N.slots * 1024, ms = (size_t)N.slots * 288, ss = (size_t)N.slots * 136, st = (size_t)N.slots * 2048;
-             CK(dalloc(&N.fN, fs)); CK(dalloc(&N.fV, fs)); CK(dalloc(&N.fF, fs)); CK(dalloc(&N.fE, fs));
+             CK(dalloc(&N.fN, fs)); CK(dalloc(&N.fV, fs)); CK(dalloc(&N.fF, fs)); CK(dalloc(&N.fE, fs)); CK(dalloc(&N.fD, fs));
              CK(dalloc(&N.mW, ms)); CK(dalloc(&N.mR, ms)); CK(dalloc(&N.seen, ss)); CK(dalloc(&N.stack, st));
              CK(dalloc(&N.queueCount, 1));
              return grow_bodies(w, std::max(1, c.initial_body_capacity));
@@ -566,7 +604,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     DevRows& R = w->rows;
     dfree(R.n_nrm); dfree(R.n_rp1); dfree(R.n_rp2); dfree(R.n_angA); dfree(R.n_angB);
     dfree(R.f_nrm); dfree(R.f_rp1); dfree(R.f_rp2); dfree(R.f_angA); dfree(R.f_angB);
-    dfree(R.slot_pair); dfree(R.slot_mask);
+    dfree(R.slot_pair); dfree(R.slot_desc); dfree(R.slot_im);
     BroadphaseBuffers& B = w->bb;
     dfree(B.bounds); dfree(B.mkeys); dfree(B.mkeys_alt); dfree(B.sortedBody); dfree(B.vals_alt);
     if (B.sortScratch) cudaFree(B.sortScratch);
@@ -576,10 +614,12 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.cursor); dfree(B.total); dfree(B.partners);
     NarrowBuffers& N = w->nb;
     if (N.queue) cudaFree(N.queue);
-    dfree(N.queueCount); dfree(N.fN); dfree(N.fV); dfree(N.fF); dfree(N.fE); dfree(N.mW); dfree(N.mR); dfree(N.seen); dfree(N.stack);
+    dfree(N.queueCount); dfree(N.fN); dfree(N.fV); dfree(N.fF); dfree(N.fE); dfree(N.fD); dfree(N.mW); dfree(N.mR); dfree(N.seen); dfree(N.stack);
     SolverBuffers& V = w->sb;
     dfree(V.parent); dfree(V.keepAwake); dfree(V.inactive); dfree(V.flag); dfree(V.candIdx); dfree(V.cand); dfree(V.colourOf);
-    dfree(V.remA); dfree(V.remB); dfree(V.claim); dfree(V.colourCount); dfree(V.colourFill); dfree(V.colourStart);
+    dfree(V.bucket); dfree(V.bucketList); dfree(V.claim); dfree(V.taken); dfree(V.posOf);
+    dfree(V.colourCount); dfree(V.colourFill); dfree(V.colourStart);
+    solver_free(V);
     dfree(V.nCand); dfree(V.nColours);
     if (V.scanScratch) cudaFree(V.scanScratch);
     if (w->hostPinned) cudaFreeHost(w->hostPinned);
@@ -1012,14 +1052,16 @@ int jbgpu_world_get_solver_order(jbgpu_world* w, int32_t* out, int32_t cap, int3
     *n = nc;
     if (nc > cap) return fail(JBGPU_ERR_CAPACITY, "caller buffer too small");
     if (nc == 0 || !out) return JBGPU_OK;
-    std::vector<int> cand(nc), col(nc);
+    std::vector<int> cand(nc), col(nc), bucket(nc);
     CK(cudaMemcpyAsync(cand.data(), w->sb.cand, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(col.data(), w->sb.colourOf, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(bucket.data(), w->sb.bucket, sizeof(int) * nc, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    std::vector<std::pair<int, int>> v(nc);
-    for (int k = 0; k < nc; k++) v[k] = std::make_pair(col[k], cand[k]);
+    // an order equivalent to the solve: by part (cut manifolds last), colour, pair index
+    std::vector<std::tuple<int, int, int>> v(nc);
+    for (int k = 0; k < nc; k++) v[k] = std::make_tuple(bucket[k], col[k], cand[k]);
     std::sort(v.begin(), v.end());
-    for (int k = 0; k < nc; k++) out[k] = v[k].second;
+    for (int k = 0; k < nc; k++) out[k] = std::get<2>(v[k]);
     return JBGPU_OK;
 }
 

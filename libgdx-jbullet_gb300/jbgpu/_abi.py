@@ -67,7 +67,8 @@ class Config(C.Structure):
         ("device", C.c_int32),
         ("initial_body_capacity", C.c_int32),
         ("pairs_per_body", C.c_int32),
-        ("reserved", C.c_int32 * 8),
+        ("solver_parts", C.c_int32),
+        ("reserved", C.c_int32 * 7),
     ]
 
 

@@ -6,6 +6,10 @@
 #include "../include/jbgpu.h"
 #include "jb_world.h"
 
+// status_flags bit of orc_counters: an explicit solver order was not a permutation of the
+// manifolds the oracle itself would solve.
+static const int ORC_ORDER_MISMATCH = 1 << 16;
+
 using namespace jb;
 
 static Xf xf_from12(const float* t) {
@@ -216,6 +220,7 @@ void orc_counters(void* h, jbgpu_counters* c) {
     c->islands = w.counters.islands;
     c->gjk_calls = w.counters.gjk;
     c->epa_calls = w.counters.epa;
+    c->status_flags = w.counters.orderMismatch ? ORC_ORDER_MISMATCH : 0;
 }
 
 void orc_phase_seconds(void* h, double* out) {

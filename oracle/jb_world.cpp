@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <chrono>
 #include <climits>
+#include <tuple>
 #include "jb_world.h"
 
 namespace jb {
@@ -540,41 +541,60 @@ static bool has_rows(const World& w, int pi) {
     return false;
 }
 
-// Deterministic colouring (the GPU's): rounds of "each dynamic body is claimed by the lowest
-// pair index among uncoloured manifolds touching it; manifolds holding all their claims take
-// the round's colour".  Returns the manifolds ordered by (colour, pair index).
+// Deterministic colouring (the GPU's, when every batch world forms one solver part).  Colours
+// are grown round by round into maximal sets by claim passes: each dynamic body is claimed by the
+// lowest pair index among the eligible manifolds touching it (uncoloured, no dynamic body taken
+// by the round); manifolds holding all their claims join the round's colour and take their
+// bodies; a round ends after a pass that adds nothing, or after 16 passes.  Returns the
+// manifolds ordered by (world, colour, pair index).
 static std::vector<int> colour_order(World& w, const std::vector<int>& cand, std::vector<int>& colourOut) {
-    std::vector<int> rem(cand), next;
-    std::vector<int> claim(w.bodies.size(), INT_MAX);
-    std::vector<std::pair<int, int>> cm;
+    const int kMaxPasses = 16;
+    const size_t n = cand.size();
+    std::vector<int> colour(n, -1), taken(w.bodies.size(), -1), claim(w.bodies.size(), INT_MAX);
+    auto dyn = [&](int b) { return w.bodies[b].islandTag >= 0; };
+    size_t done = 0;
     int round = 0;
-    while (!rem.empty()) {
-        for (int pi : rem) {
-            const Manifold& m = w.pairMf[pi];
-            int bs[2] = {m.body0, m.body1};
-            for (int b : bs) if (w.bodies[b].islandTag >= 0) claim[b] = std::min(claim[b], pi);
+    std::vector<size_t> elig;
+    while (done < n) {
+        for (int pass = 0; pass < kMaxPasses; pass++) {
+            elig.clear();
+            for (size_t i = 0; i < n; i++) {
+                if (colour[i] >= 0) continue;
+                const Manifold& m = w.pairMf[cand[i]];
+                if ((dyn(m.body0) && taken[m.body0] == round) || (dyn(m.body1) && taken[m.body1] == round)) continue;
+                elig.push_back(i);
+            }
+            for (size_t i : elig) {
+                const Manifold& m = w.pairMf[cand[i]];
+                if (dyn(m.body0)) claim[m.body0] = std::min(claim[m.body0], cand[i]);
+                if (dyn(m.body1)) claim[m.body1] = std::min(claim[m.body1], cand[i]);
+            }
+            size_t won = 0;
+            for (size_t i : elig) {
+                const Manifold& m = w.pairMf[cand[i]];
+                bool win = (!dyn(m.body0) || claim[m.body0] == cand[i]) && (!dyn(m.body1) || claim[m.body1] == cand[i]);
+                if (!win) continue;
+                colour[i] = round;
+                if (dyn(m.body0)) taken[m.body0] = round;
+                if (dyn(m.body1)) taken[m.body1] = round;
+                won++;
+            }
+            for (size_t i : elig) {
+                const Manifold& m = w.pairMf[cand[i]];
+                claim[m.body0] = INT_MAX;
+                claim[m.body1] = INT_MAX;
+            }
+            done += won;
+            if (won == 0) break;
         }
-        next.clear();
-        for (int pi : rem) {
-            const Manifold& m = w.pairMf[pi];
-            bool win = true;
-            int bs[2] = {m.body0, m.body1};
-            for (int b : bs) if (w.bodies[b].islandTag >= 0 && claim[b] != pi) win = false;
-            if (win) cm.push_back(std::make_pair(round, pi));
-            else next.push_back(pi);
-        }
-        for (int pi : rem) {
-            const Manifold& m = w.pairMf[pi];
-            claim[m.body0] = INT_MAX;
-            claim[m.body1] = INT_MAX;
-        }
-        rem.swap(next);
         round++;
     }
+    std::vector<std::tuple<int, int, int>> cm(n);
+    for (size_t i = 0; i < n; i++) cm[i] = std::make_tuple(w.bodies[w.pairMf[cand[i]].body0].world, colour[i], cand[i]);
     std::sort(cm.begin(), cm.end());
     std::vector<int> order;
     colourOut.clear();
-    for (auto& p : cm) { order.push_back(p.second); colourOut.push_back(p.first); }
+    for (auto& t : cm) { order.push_back(std::get<2>(t)); colourOut.push_back(std::get<1>(t)); }
     w.counters.colours = round;
     return order;
 }
@@ -606,11 +626,15 @@ void stage_solve(World& w, float dt) {
         w.counters.colours = 0;
     } else {
         std::vector<int> order;
+        std::vector<int> cand;
+        for (int k : w.solveList) if (has_rows(w, k)) cand.push_back(k);
         if (w.orderMode == ORDER_EXPLICIT) {
             order = w.explicitOrder;
+            std::vector<int> a(order), b(cand);
+            std::sort(a.begin(), a.end());
+            std::sort(b.begin(), b.end());
+            if (a != b) w.counters.orderMismatch++;
         } else {
-            std::vector<int> cand;
-            for (int k : w.solveList) if (has_rows(w, k)) cand.push_back(k);
             order = colour_order(w, cand, w.lastColour);
         }
         solve_group(w, order, dt);

@@ -98,14 +98,16 @@ struct Counters {
     long long steps = 0;
     int pairs = 0, manifolds = 0, contacts = 0, solverManifolds = 0, solverRows = 0, colours = 0, islands = 0;
     int gjk = 0, epa = 0;
+    int orderMismatch = 0;   // solves whose explicit order was not a permutation of the candidates
 };
 
 // Solver order policy (the reference's F8 hook, SequentialImpulseConstraintSolver.java:769-779):
 //  ORDER_REFERENCE: manifolds quick-sorted by island exactly as SimulationIslandManager does,
 //                   islands solved one after the other (dispatcher order stands in for the
 //                   reference's hash-dependent manifold creation order: ascending pair key);
-//  ORDER_COLOUR:    the GPU's deterministic colour order (colour-major, pair index minor),
-//                   all islands in one group (equivalent because islands share no body);
+//  ORDER_COLOUR:    the GPU's deterministic colour order when every batch world is one solver
+//                   part (world, then colour, then pair index), all islands in one group
+//                   (equivalent because islands share no body);
 //  ORDER_EXPLICIT:  a caller-provided list of pair indices.
 enum { ORDER_REFERENCE = 0, ORDER_COLOUR = 1, ORDER_EXPLICIT = 2 };
 

@@ -89,6 +89,29 @@ def test_closed_loop_bit_exact(gpu_lib, oracle_lib, name):
     g.close()
 
 
+@pytest.mark.parametrize("name", ["mixed120", "boxes300", "hulls60"])
+@pytest.mark.parametrize("parts", [3, 16])
+def test_range_parts_lockstep_bit_exact(gpu_lib, oracle_lib, name, parts):
+    """Solver parts as ranges of the Morton leaf order, so that many manifolds are cut between
+    parts and coloured grid-wide: each GPU step exports its solver order, the oracle steps in
+    that order, and the two worlds stay bit-identical."""
+    sc = SCENES[name]()
+    o = pyoracle.OracleWorld(sc)
+    g = GpuWorld(sc, config=_abi.default_config(**dict(sc.config, solver_parts=parts)))
+    for s in range(120):
+        g.step(sc.dt)
+        order = g.solver_order()
+        o.set_explicit_order(order)
+        o.step(sc.dt)
+        assert o.counters()["status_flags"] == 0, s   # the order covers exactly the oracle's manifolds
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+            assert not bs and not bm, (s, bs, bm)
+    assert g.counters()["status_flags"] == 0
+    g.close()
+
+
 def test_boxes_1k_300_steps_within_contract_tolerance(gpu_lib, oracle_lib):
     """The 1,000-box workload for its full 300 steps: per-step pair sets identical and
     body state within 1e-4 relative (the solver contract) of the oracle in colour order."""
@@ -120,7 +143,8 @@ def test_step_simulation_accumulator(gpu_lib, oracle_lib):
 
 def test_batched_worlds_equal_solo_runs(gpu_lib):
     """Bodies of different batch worlds never interact: stepping the batch equals stepping each
-    world alone, bit for bit."""
+    world alone, bit for bit (every world has at most 2048 bodies, so each is one solver part
+    and its manifolds are coloured the same way in the batch and alone)."""
     sc = scenes.batched_worlds(n_worlds=5, seed=3, nmin=16, nmax=120)
     big = GpuWorld(sc)
     counts = sc.meta["counts"]
@@ -141,6 +165,29 @@ def test_batched_worlds_equal_solo_runs(gpu_lib):
             assert np.array_equal(sb[k][starts[wi]:starts[wi + 1]], ss[k]), (wi, k)
         s.close()
     big.close()
+
+
+def test_full_size_100k_solver_lockstep(gpu_lib, oracle_lib):
+    """At the full 100k-body size (range solver parts, cut manifolds coloured grid-wide): from
+    the GPU's settled state, three whole steps with the oracle fed the GPU's solver order stay
+    bit-identical."""
+    sc = scenes.mixed_100k(100_000, seed=0)
+    g = GpuWorld(sc)
+    for _ in range(400):
+        g.step(sc.dt)
+    o = pyoracle.OracleWorld(sc)
+    H.copy_world(g, o, manifolds=True)
+    for s in range(3):
+        g.step(sc.dt)
+        o.set_explicit_order(g.solver_order())
+        o.step(sc.dt)
+        assert o.counters()["status_flags"] == 0, s
+        bs = H.compare_state(o.get_state(), g.get_state())
+        bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+        assert not bs and not bm, (s, bs, bm)
+    c = g.counters()
+    assert c["status_flags"] == 0 and c["solver_manifolds"] > 20_000
+    g.close()
 
 
 def test_full_size_100k_pairs_and_properties(gpu_lib, oracle_lib):
