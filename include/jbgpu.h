@@ -222,6 +222,20 @@ int jbgpu_world_step_simulation(jbgpu_world* world, float time_step, int32_t max
 int jbgpu_world_step(jbgpu_world* world, float fixed_time_step, int32_t substeps);
 /* One phase of internalSingleStepSimulation (JBGPU_STAGE_*), for open-loop checks. */
 int jbgpu_world_stage(jbgpu_world* world, int32_t stage, float time_step);
+/* The narrowphase stage, as jbgpu_world_stage(world, JBGPU_STAGE_NARROWPHASE, dt) computes it,
+ * for callers that may not allocate device memory on this path: its EPA pass takes scratch
+ * from a fixed array compiled into the library (JBGPU_STATIC_EPA_SLOTS_MAX slots of 95.1 KiB,
+ * 2.97 MiB per device) instead of the world's EPA arena, and the call allocates nothing.
+ * epa_slots (1..JBGPU_STATIC_EPA_SLOTS_MAX) EPA threads share the queued pairs; a larger value
+ * is rejected with JBGPU_ERR_CAPACITY.  The first call on a device looks the array up once
+ * (cudaGetSymbolAddress with the world's device current); make that first call before any
+ * stream capture begins.  The array is shared by every world of a device: calls that overlap in
+ * time on one device race on it and must be serialised by the caller.  Shapes or bodies added
+ * since the last step or stage are refused (uploading them allocates).  No counterpart in the
+ * reference. */
+#define JBGPU_STATIC_EPA_SLOTS_MAX 32
+int jbgpu_world_narrowphase_static(jbgpu_world* world, int32_t epa_slots);
+
 /* Wait for the world's stream. */
 int jbgpu_world_synchronize(jbgpu_world* world);
 

@@ -10,6 +10,8 @@
 // Pass 2 (one thread per queued pair, grid-stride over a fixed set of scratch slots):
 // GJK-EPA penetration depth, the deeper-result choice of GjkPairDetector.java:260-303,
 // then the same manifold update.
+#include <mutex>
+
 #include "epa.cuh"
 #include "manifold.cuh"
 #include "narrowphase.cuh"
@@ -169,5 +171,73 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
 }
 
 size_t epa_queue_record_bytes() { return sizeof(EpaRec); }
+
+// ---- EPA pass on scratch compiled into the library ----------------------------------------
+// Some hosts cannot allocate device memory on the per-frame path: an engine that reserves its
+// whole device budget at start-up and treats any later cudaMalloc as a failure, or a frame
+// loop that cannot afford the device-wide synchronisation that cudaFree implies.  For them the
+// EPA pass can take its per-slot polytope scratch from this file-scope array instead of the
+// world's arena.  Size: STATIC_EPA_SLOTS (32) slots of 95.1 KiB each, 2.97 MiB in all.
+// Nothing in it needs to start at zero: an EPA run writes every face, vertex, seen-ray and
+// stack entry before it reads it.  One array per device, shared by every world on it, so two
+// calls that overlap in time on one device (other streams or host threads) race on it.
+namespace {
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr size_t EPA_FACE_BYTES = (size_t)STATIC_EPA_SLOTS * EPA_FACE_CAP * sizeof(float4);
+constexpr size_t EPA_FACED_BYTES = (size_t)STATIC_EPA_SLOTS * EPA_FACE_CAP * sizeof(float);
+constexpr size_t EPA_MKV_BYTES = (size_t)STATIC_EPA_SLOTS * EPA_MKV_CAP * sizeof(float4);
+constexpr size_t EPA_SEEN_BYTES = (size_t)STATIC_EPA_SLOTS * EPA_SEEN_CAP * sizeof(float4);
+constexpr size_t EPA_STACK_BYTES = (size_t)STATIC_EPA_SLOTS * EPA_STACK_CAP * sizeof(int2);
+// fN, fV, fF, fE | fD | mW, mR | seen | stack, each region 256-byte aligned
+constexpr size_t OFF_FN = 0;
+constexpr size_t OFF_FV = OFF_FN + align256(EPA_FACE_BYTES);
+constexpr size_t OFF_FF = OFF_FV + align256(EPA_FACE_BYTES);
+constexpr size_t OFF_FE = OFF_FF + align256(EPA_FACE_BYTES);
+constexpr size_t OFF_FD = OFF_FE + align256(EPA_FACE_BYTES);
+constexpr size_t OFF_MW = OFF_FD + align256(EPA_FACED_BYTES);
+constexpr size_t OFF_MR = OFF_MW + align256(EPA_MKV_BYTES);
+constexpr size_t OFF_SEEN = OFF_MR + align256(EPA_MKV_BYTES);
+constexpr size_t OFF_STACK = OFF_SEEN + align256(EPA_SEEN_BYTES);
+constexpr size_t STATIC_EPA_BYTES = OFF_STACK + align256(EPA_STACK_BYTES);
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_epaScratch[STATIC_EPA_BYTES];
+
+size_t epa_static_scratch_bytes() { return STATIC_EPA_BYTES; }
+
+int epa_static_scratch(int device, void** base) {
+    static std::mutex mu;
+    static void* perDevice[MAX_STATIC_DEVICES] = {};
+    if (device < 0 || device >= MAX_STATIC_DEVICES) return 1;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!perDevice[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_epaScratch);   // the caller made `device` current
+        if (e != cudaSuccess || !p) return 1;
+        perDevice[device] = p;
+    }
+    *base = perDevice[device];
+    return 0;
+}
+
+void narrowphase_launch_static(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, void* base, int slots,
+                               cudaStream_t s) {
+    cudaMemsetAsync(nb.queueCount, 0, sizeof(int), s);
+    if (nPairs <= 0) return;
+    k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, (EpaRec*)nb.queue, nb.queueCount); note_launch();
+    unsigned char* b = (unsigned char*)base;
+    EpaArena ar;
+    ar.fN = (float4*)(b + OFF_FN);
+    ar.fV = (int4*)(b + OFF_FV);
+    ar.fF = (int4*)(b + OFF_FF);
+    ar.fE = (int4*)(b + OFF_FE);
+    ar.fD = (float*)(b + OFF_FD);
+    ar.mW = (float4*)(b + OFF_MW);
+    ar.mR = (float4*)(b + OFF_MR);
+    ar.seen = (float4*)(b + OFF_SEEN);
+    ar.stack = (int2*)(b + OFF_STACK);
+    ar.slots = slots;
+    k_narrow_epa<<<(slots + 63) / 64, 64, 0, s>>>(w, P, (const EpaRec*)nb.queue, nb.queueCount, ar); note_launch();
+}
 
 }  // namespace jbg

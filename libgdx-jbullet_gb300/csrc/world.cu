@@ -820,6 +820,29 @@ int jbgpu_world_stage(jbgpu_world* w, int32_t stage, float dt) {
     return check_status(w);
 }
 
+// The narrowphase stage with the EPA scratch compiled into the library: no device or host
+// allocation on this path (the lookup of the scratch address, once per device, allocates
+// nothing either).  Shapes or bodies added since the last step or stage would be uploaded by
+// an allocating path, so they are refused here instead.
+int jbgpu_world_narrowphase_static(jbgpu_world* w, int32_t epa_slots) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (epa_slots <= 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "epa_slots must be positive");
+    if (epa_slots > JBGPU_STATIC_EPA_SLOTS_MAX)
+        return fail(JBGPU_ERR_CAPACITY, "epa_slots exceeds the static EPA scratch (JBGPU_STATIC_EPA_SLOTS_MAX = 32)");
+    if (w->shapesDirty || w->planesDirty)
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "shapes or bodies added since the last step or stage: run one first");
+    if (w->device >= MAX_STATIC_DEVICES) return fail(JBGPU_ERR_UNSUPPORTED, "device ordinal beyond the static scratch table");
+    CK(cudaSetDevice(w->device));
+    void* base = nullptr;
+    if (epa_static_scratch(w->device, &base)) return fail(JBGPU_ERR_CUDA, "cudaGetSymbolAddress of the static EPA scratch");
+    cudaStream_t s = w->stream;
+    CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), s));
+    CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
+    narrowphase_launch_static(dev_view(w), w->pairs[w->cur], w->nPairs, w->nb, base, epa_slots, s);
+    CK(cudaGetLastError());
+    return check_status(w);
+}
+
 int jbgpu_world_synchronize(jbgpu_world* w) {
     if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
     CK(cudaStreamSynchronize(w->stream));
