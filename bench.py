@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--cpu-window", type=int, default=10)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--solver-parts", type=int, default=0, help="jbgpu_config.solver_parts (0: automatic)")
+    p.add_argument("--solver-threads", type=int, default=0, help="jbgpu_config.solver_threads (0: 256)")
     return p.parse_args()
 
 
@@ -223,6 +225,8 @@ def run_ours(args, dist):
     sc = make_scene(args.workload, args.seed + dist.rank)
     cfg = _abi.default_config(**sc.config)
     cfg.device = dist.local
+    cfg.solver_parts = args.solver_parts
+    cfg.solver_threads = args.solver_threads
     iters = cfg.num_iterations
     n = sc.n_bodies
     K, W = args.steps, args.warmup

@@ -120,7 +120,16 @@ typedef struct jbgpu_config {
                                            world has at most 2048 finite bodies, else ranges of
                                            the Morton order; > 0: that many range parts (at least
                                            finite bodies / 2048).  No counterpart in the reference. */
-    int32_t reserved[7];
+    int32_t solver_threads;             /* threads per solver block: 0 (default 256), 64, 128 or 256.
+                                           No counterpart in the reference. */
+    float   solver_residual;            /* 0 (default): num_iterations PGS iterations, as the reference.
+                                           > 0: iterate until the residual
+                                           max|lambda_k - lambda_k-1| / max(max|lambda_k|, 1e-6) over
+                                           all rows of a world is <= this value (batched worlds: per
+                                           world when each world is one solver part, else over the
+                                           batch), at most solver_max_iterations. */
+    int32_t solver_max_iterations;      /* cap for solver_residual > 0; 0 means 200 */
+    int32_t reserved[4];
 } jbgpu_config;
 
 typedef struct jbgpu_shape_desc {
@@ -191,7 +200,10 @@ typedef struct jbgpu_counters {
     int32_t gjk_calls;        /* BulletStats.gNumGjkChecks for the last step */
     int32_t epa_calls;        /* BulletStats.gNumDeepPenetrationChecks for the last step */
     int32_t status_flags;     /* bit0 capacity, bit1 EPA pool, bit2 timeout, bit3 non-finite */
-    int32_t reserved[6];
+    int32_t solver_iterations;/* PGS iterations of the last solve (the largest over worlds) */
+    int32_t cut_colours;      /* colours of manifolds cut between solver parts (GPU only) */
+    int32_t cut_manifolds;    /* manifolds cut between solver parts (GPU only) */
+    int32_t reserved[3];
 } jbgpu_counters;
 
 /* ---- library -------------------------------------------------------------------- */
@@ -226,7 +238,7 @@ int jbgpu_world_stage(jbgpu_world* world, int32_t stage, float time_step);
  * for callers that may not allocate device memory on this path: its EPA pass takes scratch
  * from a fixed array compiled into the library (JBGPU_STATIC_EPA_SLOTS_MAX slots of 95.1 KiB,
  * 2.97 MiB per device) instead of the world's EPA arena, and the call allocates nothing.
- * epa_slots (1..JBGPU_STATIC_EPA_SLOTS_MAX) EPA threads share the queued pairs; a larger value
+ * epa_slots (1..JBGPU_STATIC_EPA_SLOTS_MAX) EPA warps share the queued pairs; a larger value
  * is rejected with JBGPU_ERR_CAPACITY.  The first call on a device looks the array up once
  * (cudaGetSymbolAddress with the world's device current); make that first call before any
  * stream capture begins.  The array is shared by every world of a device: calls that overlap in

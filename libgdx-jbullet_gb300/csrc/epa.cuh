@@ -1,7 +1,12 @@
 // Penetration depth by GJK + EPA (collision/narrowphase/GjkEpaSolver.java and
 // GjkEpaPenetrationDepthSolver.java of the reference) on the device.  The polytope (faces,
-// Minkowski vertices), the visited-ray set and the horizon stack live in a per-thread slot
-// of a global scratch arena; the recursion of BuildHorizon runs on an explicit stack.
+// Minkowski vertices), the visited-ray set and the horizon stack live in a slot of a global
+// scratch arena; the recursion of BuildHorizon runs on an explicit stack.
+//
+// One warp runs one query.  Every lane executes the whole (sequential) algorithm on identical
+// values, so every lane reads back its own stores; the three scans — the best-face search, the
+// visited-ray test and the hull support map — are split across the lanes and combined with warp
+// shuffles under the reference's own selection rules, which gives the same result in every lane.
 #pragma once
 #include "gjk.cuh"
 
@@ -18,7 +23,7 @@ constexpr int EPA_STACK_CAP = 2 * EPA_FACE_CAP;
 // created (prepended) and leave only through Detach, so the list is always the live faces in
 // decreasing creation order: here a face is live when fE.w == 1, fD holds its distance (+inf
 // once detached), and FindBest scans fD from the newest face down, which selects the same face.
-struct EpaSlot {          // one thread's polytope
+struct EpaSlot {          // one query's polytope
     float4* fN;           // face normal xyz, distance w
     int4* fV;             // vertex ids, mark
     int4* fF;             // adjacent faces
@@ -63,11 +68,44 @@ struct EpaCtx {
     bool failed, overflow;
     EpaSlot sl;
     int nmkv, nface, root, nfaces;
+    int lane, nl;         // lane in the warp and lanes sharing the query (1 or 32)
 };
+
+constexpr unsigned FULL_MASK = 0xffffffffu;
+
+// support_with_margin with the hull's vertex scan split across nl lanes: each lane keeps the
+// first strictly larger dot of its vertices, the warp then keeps the larger dot and, on equal
+// dots, the lower vertex index — the vertex the sequential first-strict-maximum scan selects.
+JBD V support_with_margin_lanes(const ShapeRef& s, V vec, int lane, int nl) {
+    if (nl == 1 || s.type != SHAPE_HULL) return support_with_margin(s, vec);
+    V v = normalize_dir(vec);
+    float maxDot = -1e30f;
+    int idx = 0x7fffffff;
+    for (int i = lane; i < s.npts; i += 32) {
+        float4 p = s.pts[i];
+        float nd = dot(v, mk(p.x, p.y, p.z));
+        if (nd > maxDot) { maxDot = nd; idx = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        float od = __shfl_xor_sync(FULL_MASK, maxDot, o);
+        int oi = __shfl_xor_sync(FULL_MASK, idx, o);
+        if (od > maxDot || (od == maxDot && oi < idx)) { maxDot = od; idx = oi; }
+    }
+    V sup = mk(0.0f, 0.0f, 0.0f);
+    if (idx != 0x7fffffff) { float4 p = s.pts[idx]; sup = mk(p.x, p.y, p.z); }
+    if (s.margin != 0.0f) {          // ConvexInternalShape.localGetSupportingVertex
+        V vn = vec;
+        if (len2(vn) < __fmul_rn(FLT_EPS, FLT_EPS)) vn = mk(-1.0f, -1.0f, -1.0f);
+        vn = nor(vn);
+        vn = scl(vn, s.margin);
+        sup = add(sup, vn);
+    }
+    return sup;
+}
 
 JBD V epa_local_support(const EpaCtx& c, V d, int i) {     // GjkEpaSolver.GJK.LocalSupport
     V t = mulMTv(d, c.rot[i]);
-    V o = support_with_margin(c.sh[i], t);
+    V o = support_with_margin_lanes(c.sh[i], t, c.lane, c.nl);
     o = mulMv(o, c.rot[i]);
     return add(o, c.pos[i]);
 }
@@ -81,10 +119,13 @@ JBD void epa_support(const EpaCtx& c, V d, V& w, V& r) {    // GjkEpaSolver.GJK.
     w.z = __fadd_rn(w.z, __fmul_rn(c.margin, d.z));
 }
 JBD bool epa_fetch(EpaCtx& c) {                             // FetchSupport
-    for (int k = 0; k < c.nseen; k++) {
+    bool hit = false;
+    for (int k = c.lane; k < c.nseen; k += c.nl) {
         float4 s = c.sl.seen[k];
-        if (vequals(mk(s.x, s.y, s.z), c.ray)) { --c.order; return false; }
+        if (vequals(mk(s.x, s.y, s.z), c.ray)) hit = true;
     }
+    if (c.nl > 1) hit = __any_sync(FULL_MASK, hit);
+    if (hit) { --c.order; return false; }
     if (c.nseen < EPA_SEEN_CAP) c.sl.seen[c.nseen++] = f4(c.ray, 0.0f);
     else c.overflow = true;
     ++c.order;
@@ -293,8 +334,10 @@ JBD int epa_horizon(EpaCtx& c, int markid, int w, int f0, int e0, int& cf, int& 
 
 // GjkEpaSolver.collide -> EPA.EvaluatePD; returns true with witnesses on penetration.
 JBD bool epa_pen_depth(const ShapeRef& s0, const Xf& t0, const ShapeRef& s1, const Xf& t1, EpaSlot slot, V& wA, V& wB,
-                       bool& overflow) {
+                       bool& overflow, int lane, int nl) {
     EpaCtx c;
+    c.lane = lane;
+    c.nl = nl;
     c.sh[0] = s0; c.rot[0] = t0.b; c.pos[0] = t0.o;
     c.sh[1] = s1; c.rot[1] = t1.b; c.pos[1] = t1.o;
     c.margin = __fadd_rn(0.0f, 0.001f);
@@ -324,9 +367,16 @@ JBD bool epa_pen_depth(const ShapeRef& s0, const Xf& t0, const ShapeRef& s1, con
         int best = -1;                                               // FindBest, newest face first
         {
             float bd = SIMD_INFINITY;
-            for (int f = c.nface - 1; f >= 0; f--) {
+            for (int f = c.nface - 1 - c.lane; f >= 0; f -= c.nl) {
                 float d = c.sl.fD[f];
                 if (d < bd) { bd = d; best = f; }
+            }
+            if (c.nl > 1) {          // smallest distance; on equal distances the newer face
+                for (int o = 16; o > 0; o >>= 1) {
+                    float od = __shfl_xor_sync(FULL_MASK, bd, o);
+                    int ob = __shfl_xor_sync(FULL_MASK, best, o);
+                    if (od < bd || (od == bd && ob > best)) { bd = od; best = ob; }
+                }
             }
         }
         if (best < 0) break;

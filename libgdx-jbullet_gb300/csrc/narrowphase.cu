@@ -7,9 +7,9 @@
 // (ConvexConvexAlgorithm.java:90-139), adding at most one point and refreshing the
 // manifold.  Convex pairs whose GJK ends in the penetration case are queued with their
 // partial GJK result.
-// Pass 2 (one thread per queued pair, grid-stride over a fixed set of scratch slots):
-// GJK-EPA penetration depth, the deeper-result choice of GjkPairDetector.java:260-303,
-// then the same manifold update.
+// Pass 2 (one warp per queued pair, warp-stride over a fixed set of scratch slots, one slot per
+// warp): GJK-EPA penetration depth, the deeper-result choice of GjkPairDetector.java:260-303,
+// then the same manifold update (lane 0).
 #include <mutex>
 
 #include "epa.cuh"
@@ -107,44 +107,41 @@ __global__ void k_narrow(DevWorld w, DevPairs P, int nPairs, EpaRec* queue, int*
     store_mf(P, p, m);
 }
 
-__global__ void k_narrow_epa(DevWorld w, DevPairs P, const EpaRec* queue, const int* queueCount, EpaArena arena) {
-    int n = *queueCount;
-    int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= arena.slots) return;
-    EpaSlot sl = epa_slot(arena, slot);
-    for (int qi = slot; qi < n; qi += arena.slots) {
-        EpaRec r = queue[qi];
-        int p = r.pair;
-        uint64_t key = P.keys[p];
-        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
-        int col0 = min(a, b), col1 = max(a, b);
-        int mb0 = P.b0[p], mb1 = P.b1[p];
-        Xf x0 = load_xf(w, col0), x1 = load_xf(w, col1);
-        ShapeRef sa = shape_ref(w.sh, w.shape[col0]), sb = shape_ref(w.sh, w.shape[col1]);
-        V offset = scl(add(x0.o, x1.o), 0.5f);
-        Xf lA = x0, lB = x1;
-        lA.o = sub(lA.o, offset);
-        lB.o = sub(lB.o, offset);
-        bool isValid = r.valid != 0;
-        float distance = r.distance;
-        V pointOnB = mk4(r.pB), normalInB = mk4(r.nB);
-        atomicAdd(&w.ctr[C_EPA], 1);
-        V wA, wB;
-        bool ovf = false;
-        if (epa_pen_depth(sa, lA, sb, lB, sl, wA, wB, ovf)) {
-            V tn = sub(wB, wA);
-            float lenSqr = len2(tn);
-            if (lenSqr > __fmul_rn(FLT_EPS, FLT_EPS)) {
-                tn = scl(tn, jdiv(1.0f, jsqrt(lenSqr)));
-                float distance2 = -len(sub(wA, wB));
-                if (!isValid || (distance2 < distance)) {
-                    distance = distance2;
-                    pointOnB = wB;
-                    normalInB = tn;
-                    isValid = true;
-                }
+// One queued pair, by the 32 lanes of a warp (see epa.cuh); lane 0 updates the manifold.
+__device__ void epa_query(const DevWorld& w, DevPairs& P, const EpaRec* queue, int qi, const EpaSlot& sl, int lane) {
+    EpaRec r = queue[qi];
+    int p = r.pair;
+    uint64_t key = P.keys[p];
+    int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+    int col0 = min(a, b), col1 = max(a, b);
+    int mb0 = P.b0[p], mb1 = P.b1[p];
+    Xf x0 = load_xf(w, col0), x1 = load_xf(w, col1);
+    ShapeRef sa = shape_ref(w.sh, w.shape[col0]), sb = shape_ref(w.sh, w.shape[col1]);
+    V offset = scl(add(x0.o, x1.o), 0.5f);
+    Xf lA = x0, lB = x1;
+    lA.o = sub(lA.o, offset);
+    lB.o = sub(lB.o, offset);
+    bool isValid = r.valid != 0;
+    float distance = r.distance;
+    V pointOnB = mk4(r.pB), normalInB = mk4(r.nB);
+    V wA, wB;
+    bool ovf = false;
+    if (epa_pen_depth(sa, lA, sb, lB, sl, wA, wB, ovf, lane, 32)) {
+        V tn = sub(wB, wA);
+        float lenSqr = len2(tn);
+        if (lenSqr > __fmul_rn(FLT_EPS, FLT_EPS)) {
+            tn = scl(tn, jdiv(1.0f, jsqrt(lenSqr)));
+            float distance2 = -len(sub(wA, wB));
+            if (!isValid || (distance2 < distance)) {
+                distance = distance2;
+                pointOnB = wB;
+                normalInB = tn;
+                isValid = true;
             }
         }
+    }
+    if (lane == 0) {
+        atomicAdd(&w.ctr[C_EPA], 1);
         if (ovf) atomicOr(&w.ctr[C_STATUS], ST_EPA_POOL);
         Mf m;
         load_mf(P, p, m);
@@ -154,6 +151,39 @@ __global__ void k_narrow_epa(DevWorld w, DevPairs P, const EpaRec* queue, const 
         manifold_refresh(m, w, mb0, mb1);
         store_mf(P, p, m);
     }
+    __syncwarp();
+}
+
+// EPA pass with each warp's polytope in a slot of a global arena.
+__global__ void k_narrow_epa(DevWorld w, DevPairs P, const EpaRec* queue, const int* queueCount, EpaArena arena) {
+    int n = *queueCount;
+    int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (slot >= arena.slots) return;
+    EpaSlot sl = epa_slot(arena, slot);
+    for (int qi = slot; qi < n; qi += arena.slots) epa_query(w, P, queue, qi, sl, lane);
+}
+
+// EPA pass with the polytope in shared memory: one warp per block, 97,408 bytes of dynamic
+// shared memory (two blocks per SM), blocks stride over the queue.
+constexpr size_t EPA_SMEM_BYTES = (size_t)EPA_FACE_CAP * (4 * sizeof(float4) + sizeof(float)) +
+                                  (size_t)EPA_MKV_CAP * 2 * sizeof(float4) + (size_t)EPA_SEEN_CAP * sizeof(float4) +
+                                  (size_t)EPA_STACK_CAP * sizeof(int2);
+
+__global__ void __launch_bounds__(32) k_narrow_epa_smem(DevWorld w, DevPairs P, const EpaRec* queue, const int* queueCount) {
+    extern __shared__ float4 epaSmem[];
+    int n = *queueCount;
+    EpaSlot sl;
+    sl.fN = epaSmem;
+    sl.fV = (int4*)(sl.fN + EPA_FACE_CAP);
+    sl.fF = sl.fV + EPA_FACE_CAP;
+    sl.fE = sl.fF + EPA_FACE_CAP;
+    sl.mW = (float4*)(sl.fE + EPA_FACE_CAP);
+    sl.mR = sl.mW + EPA_MKV_CAP;
+    sl.seen = sl.mR + EPA_MKV_CAP;
+    sl.stack = (int2*)(sl.seen + EPA_SEEN_CAP);
+    sl.fD = (float*)(sl.stack + EPA_STACK_CAP);
+    for (int qi = blockIdx.x; qi < n; qi += gridDim.x) epa_query(w, P, queue, qi, sl, threadIdx.x);
 }
 
 void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
@@ -162,15 +192,19 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
     cudaMemsetAsync(nb.queueCount, 0, sizeof(int), s);
     if (nPairs > 0) { k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, (EpaRec*)nb.queue, nb.queueCount); note_launch(); }
     if (prof) { prof->mark(PH_NARROW, 1, s); prof->mark(PH_EPA, 0, s); }
-    EpaArena ar;
-    ar.fN = nb.fN; ar.fV = nb.fV; ar.fF = nb.fF; ar.fE = nb.fE; ar.fD = nb.fD;
-    ar.mW = nb.mW; ar.mR = nb.mR; ar.seen = nb.seen; ar.stack = nb.stack;
-    ar.slots = nb.slots;
-    if (nPairs > 0) { k_narrow_epa<<<(nb.slots + 63) / 64, 64, 0, s>>>(w, P, (const EpaRec*)nb.queue, nb.queueCount, ar); note_launch(); }
+    if (nPairs > 0) {
+        k_narrow_epa_smem<<<nb.slots, 32, EPA_SMEM_BYTES, s>>>(w, P, (const EpaRec*)nb.queue, nb.queueCount);
+        note_launch();
+    }
     if (prof) prof->mark(PH_EPA, 1, s);
 }
 
 size_t epa_queue_record_bytes() { return sizeof(EpaRec); }
+
+int narrowphase_configure() {
+    return cudaFuncSetAttribute(k_narrow_epa_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EPA_SMEM_BYTES) ==
+                   cudaSuccess ? 0 : 1;
+}
 
 // ---- EPA pass on scratch compiled into the library ----------------------------------------
 // Some hosts cannot allocate device memory on the per-frame path: an engine that reserves its
@@ -237,7 +271,7 @@ void narrowphase_launch_static(const DevWorld& w, DevPairs& P, int nPairs, Narro
     ar.seen = (float4*)(b + OFF_SEEN);
     ar.stack = (int2*)(b + OFF_STACK);
     ar.slots = slots;
-    k_narrow_epa<<<(slots + 63) / 64, 64, 0, s>>>(w, P, (const EpaRec*)nb.queue, nb.queueCount, ar); note_launch();
+    k_narrow_epa<<<(slots * 32 + 127) / 128, 128, 0, s>>>(w, P, (const EpaRec*)nb.queue, nb.queueCount, ar); note_launch();
 }
 
 }  // namespace jbg

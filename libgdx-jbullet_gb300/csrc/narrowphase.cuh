@@ -4,23 +4,20 @@
 
 namespace jbg {
 
-// EPA queue + scratch arena (per-slot polytopes; see epa.cuh for the slot layout).
+// EPA queue (the polytopes live in shared memory, one warp and one polytope per block).
 struct NarrowBuffers {
     void* queue = nullptr;        // EpaRec per queued pair (pair capacity)
     int* queueCount = nullptr;
-    int slots = 0;                // concurrent EPA threads, each owning one slot
-    float4 *fN = nullptr, *mW = nullptr, *mR = nullptr, *seen = nullptr;
-    int4 *fV = nullptr, *fF = nullptr, *fE = nullptr;
-    float* fD = nullptr;
-    int2* stack = nullptr;
+    int slots = 0;                // EPA blocks, striding over the queue
 };
 
 size_t epa_queue_record_bytes();
+int narrowphase_configure();      // once per world: the EPA kernel's shared-memory size
 void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
                         const Prof* prof = nullptr);
 
 // Narrowphase whose EPA pass uses scratch compiled into the library (no allocation).
-constexpr int STATIC_EPA_SLOTS = JBGPU_STATIC_EPA_SLOTS_MAX;   // EPA threads that can run at once on it
+constexpr int STATIC_EPA_SLOTS = JBGPU_STATIC_EPA_SLOTS_MAX;   // EPA warps that can run at once on it
 constexpr int MAX_STATIC_DEVICES = 64;
 size_t epa_static_scratch_bytes();
 // Device address of the static scratch on `device`, which must be current; looked up once per

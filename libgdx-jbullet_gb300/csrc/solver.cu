@@ -131,12 +131,20 @@ __global__ void k_count_manifolds(DevPairs P, int nPairs, int* ctr) {
     if ((threadIdx.x & 31) == 0 && (m || c)) { atomicAdd(&ctr[C_MANIFOLDS], m); atomicAdd(&ctr[C_CONTACTS], c); }
 }
 
-void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s) {
+// Unions and the awake test read only pairs, flags and activation states, none of which the
+// narrowphase writes, so a step runs them beside the narrowphase on a second stream.
+void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s) {
     int n = w.nBodies;
     k_uf_init<<<gridn(n, 256), 256, 0, s>>>(n, sb.parent); note_launch();
     if (nPairs > 0) { k_uf_union<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.parent); note_launch(); }
     k_islands<<<gridn(n, 256), 256, 0, s>>>(w, sb.parent, sb.keepAwake, sb.inactive); note_launch();
     k_island_awake<<<gridn(n, 256), 256, 0, s>>>(w, sb.keepAwake); note_launch();
+}
+
+// Sleep decisions (they change activation states, which the narrowphase reads) and the
+// manifold selection (it reads the narrowphase's points): after the narrowphase.
+void islands_launch_select(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s) {
+    int n = w.nBodies;
     k_island_sleep<<<gridn(n, 256), 256, 0, s>>>(w, sb.keepAwake, sb.inactive); note_launch();
     if (nPairs > 0) {
         k_select<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.inactive, sb.flag); note_launch();
@@ -146,6 +154,11 @@ void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuff
     } else {
         cudaMemsetAsync(sb.nCand, 0, sizeof(int), s);
     }
+}
+
+void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s) {
+    islands_launch_unions(w, P, nPairs, sb, s);
+    islands_launch_select(w, P, nPairs, sb, s);
 }
 
 // ---- grid barrier (bounded wait) -----------------------------------------------------------
@@ -356,6 +369,8 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
         int maxLocal = 0;
         for (int p = 0; p < sb.nParts; p++) maxLocal = max(maxLocal, __ldcg(&sb.nLocal[p]));
         w.ctr[C_COLOURS] = round + maxLocal;
+        w.ctr[C_CUT_COLOURS] = round;
+        w.ctr[C_CUT_MANIFOLDS] = nCut;
     }
 }
 
@@ -452,7 +467,7 @@ __global__ void k_setup(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, 
         float imp = warm ? __fmul_rn(nr.w, w.warm) : 0.0f;
         int ni = s * 4 + j;
         R.n_nrm[ni] = f4(nrm, jac);
-        R.n_rp1[ni] = f4(rp1xn, pen);
+        R.n_rp1[ni] = f4(rp1xn, jdiv(__fmul_rn(-pen, w.erp), dt));   // positionalError (java:248)
         R.n_rp2[ni] = f4(rp2xn, rest);
         R.n_angA[ni] = f4(angA, wa.w);   // friction coefficient
         R.n_angB[ni] = f4(angB, imp);
@@ -497,10 +512,22 @@ JBD void apply_imp(V& lin, V& ang, V n, float im, V angc, float imp) {   // Solv
 
 enum { PH_WARM = 0, PH_NORMAL = 1, PH_FRICTION = 2 };
 
+// Largest |delta lambda| and |lambda| a thread has seen in the current iteration (the
+// residual of the residual-terminated mode).  `x > m` keeps NaN out, as the oracle does.
+struct Resid {
+    float d = 0.0f, l = 0.0f;
+    JBD void add(float dl, float lam) {
+        dl = fabsf(dl);
+        lam = fabsf(lam);
+        if (dl > d) d = dl;
+        if (lam > l) l = lam;
+    }
+};
+
 // The rows of one manifold for one phase, on velocities held in registers.  Warm start applies
 // per point the normal, then both friction impulses (setup order, java:680-760).
 JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int mask, int kind, V& l0, V& a0, V& l1, V& a1,
-                        float im0, float im1, float dt) {
+                        float im0, float im1, Resid& res) {
     for (int j = 0; j < 4; j++) {
         if (!(mask & (1 << j))) continue;
         const int ni = s * 4 + j;
@@ -524,7 +551,7 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int mask, in
             float vel1 = __fadd_rn(dot(n, l0), dot(mk(r1.x, r1.y, r1.z), a0));
             float vel2 = __fadd_rn(dot(n, l1), dot(mk(r2.x, r2.y, r2.z), a1));
             float rel = __fsub_rn(vel1, vel2);
-            float posErr = jdiv(__fmul_rn(-r1.w, w.erp), dt);
+            float posErr = r1.w;          // -penetration * erp / timeStep, formed once by the setup
             float velErr = __fsub_rn(r2.w, rel);
             float ni1 = __fadd_rn(__fmul_rn(posErr, nn.w), __fmul_rn(velErr, nn.w));
             float old = aB.w;
@@ -535,11 +562,16 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int mask, in
             apply_imp(l1, a1, n, im1, mk(aB.x, aB.y, aB.z), -d);
             aB.w = acc;
             __stcg(&R.n_angB[ni], aB);
+            res.add(d, acc);
         } else {                          // resolveSingleFrictionCacheFriendly (java:286-346)
             float total = __fadd_rn(__ldcg(&R.n_angB[ni]).w, 0.0f);   // appliedImpulse + appliedPushImpulse
             float fric = R.n_angA[ni].w;
             float limit = __fmul_rn(total, fric);
-            if (!(total > 0.0f)) continue;
+            if (!(total > 0.0f)) {
+                res.add(0.0f, __ldcg(&R.f_rp1[ni * 2]).w);
+                res.add(0.0f, __ldcg(&R.f_rp1[ni * 2 + 1]).w);
+                continue;
+            }
             for (int f = 0; f < 2; f++) {
                 int fi = ni * 2 + f;
                 float4 fn = R.f_nrm[fi];
@@ -559,6 +591,7 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int mask, in
                 apply_imp(l1, a1, n, im1, mk4(R.f_angB[fi]), -j1);
                 r1.w = acc;
                 __stcg(&R.f_rp1[fi], r1);
+                res.add(j1, acc);
             }
         }
     }
@@ -624,7 +657,7 @@ JBD void stage_out(const DevWorld& w, const SolverBuffers& sb, const PartView& v
 // One local colour of a part: its manifolds share no dynamic body; the part's bodies are in
 // shared memory (global memory when the part does not fit).
 JBD void local_colour(const DevWorld& w, const DevRows& R, int s0, int s1, int kind, bool smem, float4* sl, float4* sa,
-                      float dt) {
+                      Resid& res) {
     for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
         const int4 d = R.slot_desc[s];
         const float2 im = R.slot_im[s];
@@ -633,19 +666,34 @@ JBD void local_colour(const DevWorld& w, const DevRows& R, int s0, int s1, int k
         V l0, a0, l1, a1;
         if (m0) { l0 = mk4(sl[lb0]); a0 = mk4(sa[lb0]); } else gload(w, d.x, l0, a0);
         if (m1) { l1 = mk4(sl[lb1]); a1 = mk4(sa[lb1]); } else gload(w, d.y, l1, a1);
-        solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, dt);
+        solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
         if (im.x != 0.0f) { if (m0) { sl[lb0] = f4(l0, 0.0f); sa[lb0] = f4(a0, 0.0f); } else gstore(w, d.x, l0, a0); }
         if (im.y != 0.0f) { if (m1) { sl[lb1] = f4(l1, 0.0f); sa[lb1] = f4(a1, 0.0f); } else gstore(w, d.y, l1, a1); }
     }
 }
 
-JBD int phase_kind(int ph) { return ph == 0 ? PH_WARM : ((ph - 1) % 2 == 0 ? PH_NORMAL : PH_FRICTION); }
+// Block-wide maxima of the threads' residual terms (non-negative floats order as their bits).
+JBD void block_resid(const Resid& r, unsigned* sh, float& dmax, float& lmax) {
+    if (threadIdx.x == 0) { sh[0] = 0u; sh[1] = 0u; }
+    __syncthreads();
+    atomicMax(&sh[0], __float_as_uint(r.d));
+    atomicMax(&sh[1], __float_as_uint(r.l));
+    __syncthreads();
+    dmax = __uint_as_float(sh[0]);
+    lmax = __uint_as_float(sh[1]);
+    __syncthreads();
+}
 
-// Phases: warm start, then numIterations x (normal rows, friction rows).  Within a phase the
-// parts' internal manifolds run first (parts share no dynamic body), then the cut colours.
-// Without cut manifolds every part runs all phases on its own, with no grid barrier.
+JBD bool resid_done(float dmax, float lmax, float tol) { return jdiv(dmax, lmax > 1e-6f ? lmax : 1e-6f) <= tol; }
+
+// Phases: warm start, then iterations of (normal rows, friction rows): numIterations of them,
+// or, with a residual tolerance, until the residual of the rows' world is within it (at most
+// maxIter).  Within a phase the parts' internal manifolds run first (parts share no dynamic
+// body), then the cut colours.  Without cut manifolds — and, for the residual, with one world
+// per part — every part runs all phases on its own, with no grid barrier.
 __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs P, DevRows R, SolverBuffers sb, float dt) {
     extern __shared__ float4 smv[];
+    __shared__ unsigned shRes[2];
     const int nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int nCut = *sb.nColours;
@@ -653,55 +701,101 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
     const bool smem = sb.partSmem != 0;
     float4* sl = smv;
     float4* sa = smv + sb.partMax;
-    const int nPhases = 1 + 2 * w.numIter;
-    if (nCut == 0) {
+    const bool byRes = w.resTol > 0.0f;
+    const int maxIt = byRes ? w.maxIter : w.numIter;
+    if (nCut == 0 && (!byRes || sb.worldParts)) {
+        int itMax = 0;
         for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
             const PartView v = part_view(sb, part);
             if (smem) stage_in(w, sb, v, sl, sa);
             __syncthreads();
-            for (int ph = 0; ph < nPhases; ph++) {
-                const int kind = phase_kind(ph);
+            Resid res;
+            for (int c = 0; c < v.nLoc; c++) {
+                local_colour(w, R, v.lcs[c], v.lcs[c + 1], PH_WARM, smem, sl, sa, res);
+                __syncthreads();
+            }
+            int it = 0;
+            while (it < maxIt && v.nLoc > 0) {
+                Resid r;
                 for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, v.lcs[c], v.lcs[c + 1], kind, smem, sl, sa, dt);
+                    local_colour(w, R, v.lcs[c], v.lcs[c + 1], PH_NORMAL, smem, sl, sa, r);
                     __syncthreads();
                 }
+                for (int c = 0; c < v.nLoc; c++) {
+                    local_colour(w, R, v.lcs[c], v.lcs[c + 1], PH_FRICTION, smem, sl, sa, r);
+                    __syncthreads();
+                }
+                ++it;
+                if (byRes) {
+                    float dm, lm;
+                    block_resid(r, shRes, dm, lm);
+                    if (resid_done(dm, lm, w.resTol)) break;
+                }
             }
+            if (it > itMax) itMax = it;
             if (smem) stage_out(w, sb, v, sl, sa);
             for (int s = sb.bucketStart[part] + threadIdx.x; s < sb.bucketStart[part + 1]; s += blockDim.x)
                 writeback_slot(P, R, s);
             __syncthreads();
         }
+        if (threadIdx.x == 0 && itMax > 0) atomicMax(&w.ctr[C_PGS_ITERS], itMax);
         return;
     }
-    for (int ph = 0; ph < nPhases; ph++) {
-        const int kind = phase_kind(ph);
-        for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
-            const PartView v = part_view(sb, part);
-            if (smem) stage_in(w, sb, v, sl, sa);
-            __syncthreads();
-            for (int c = 0; c < v.nLoc; c++) {
-                local_colour(w, R, v.lcs[c], v.lcs[c + 1], kind, smem, sl, sa, dt);
+    if (nSlots == 0) return;
+    if (tid == 0) for (int k = 0; k < 6; k++) w.ctr[C_RES0 + k] = 0;
+    Resid res;
+    int it = -1;          // -1: the warm-start phase
+    for (;;) {
+        for (int sub = 0; sub < (it < 0 ? 1 : 2); sub++) {
+            const int kind = it < 0 ? PH_WARM : (sub == 0 ? PH_NORMAL : PH_FRICTION);
+            for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
+                const PartView v = part_view(sb, part);
+                if (smem) stage_in(w, sb, v, sl, sa);
+                __syncthreads();
+                for (int c = 0; c < v.nLoc; c++) {
+                    local_colour(w, R, v.lcs[c], v.lcs[c + 1], kind, smem, sl, sa, res);
+                    __syncthreads();
+                }
+                if (smem) stage_out(w, sb, v, sl, sa);
                 __syncthreads();
             }
-            if (smem) stage_out(w, sb, v, sl, sa);
-            __syncthreads();
+            grid_barrier(w.ctr, nb);
+            for (int c = 0; c < nCut; c++) {
+                const int s0 = sb.colourStart[c], s1 = sb.colourStart[c + 1];
+                for (int s = s0 + tid; s < s1; s += nth) {
+                    const int4 d = R.slot_desc[s];
+                    const float2 im = R.slot_im[s];
+                    V l0, a0, l1, a1;
+                    gload(w, d.x, l0, a0);
+                    gload(w, d.y, l1, a1);
+                    solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
+                    if (im.x != 0.0f) gstore(w, d.x, l0, a0);
+                    if (im.y != 0.0f) gstore(w, d.y, l1, a1);
+                }
+                grid_barrier(w.ctr, nb);
+            }
         }
-        grid_barrier(w.ctr, nb);
-        for (int c = 0; c < nCut; c++) {
-            const int s0 = sb.colourStart[c], s1 = sb.colourStart[c + 1];
-            for (int s = s0 + tid; s < s1; s += nth) {
-                const int4 d = R.slot_desc[s];
-                const float2 im = R.slot_im[s];
-                V l0, a0, l1, a1;
-                gload(w, d.x, l0, a0);
-                gload(w, d.y, l1, a1);
-                solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, dt);
-                if (im.x != 0.0f) gstore(w, d.x, l0, a0);
-                if (im.y != 0.0f) gstore(w, d.y, l1, a1);
+        ++it;
+        if (it >= maxIt) break;
+        if (byRes && it > 0) {
+            // slot it % 3 collects this iteration; slot (it + 1) % 3 was last read two iterations
+            // ago, behind at least two grid barriers, and is cleared for the next one
+            const int slot = C_RES0 + 2 * (it % 3);
+            if (tid == 0) { w.ctr[C_RES0 + 2 * ((it + 1) % 3)] = 0; w.ctr[C_RES0 + 2 * ((it + 1) % 3) + 1] = 0; }
+            float dm, lm;
+            block_resid(res, shRes, dm, lm);
+            if (threadIdx.x == 0) {
+                atomicMax((unsigned*)&w.ctr[slot], __float_as_uint(dm));
+                atomicMax((unsigned*)&w.ctr[slot + 1], __float_as_uint(lm));
             }
             grid_barrier(w.ctr, nb);
+            dm = __uint_as_float((unsigned)__ldcg(&w.ctr[slot]));
+            lm = __uint_as_float((unsigned)__ldcg(&w.ctr[slot + 1]));
+            if (resid_done(dm, lm, w.resTol)) break;
         }
+        res = Resid();
     }
+    if (tid == 0 && it > 0) atomicMax(&w.ctr[C_PGS_ITERS], it);
     for (int s = tid; s < nSlots; s += nth) writeback_slot(P, R, s);
 }
 
@@ -713,7 +807,9 @@ template <class T> static void sfree(T*& p) { if (p) cudaFree((void*)p); p = nul
 
 static size_t pgs_smem(const SolverBuffers& sb) { return sb.partSmem ? (size_t)sb.partMax * 32 : 0; }
 
-int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts) {
+int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts,
+                     int threads) {
+    sb.threads = threads;
     int maxWorld = 0;
     for (int c : worldCounts) maxWorld = std::max(maxWorld, c);
     std::vector<int> start;
@@ -756,8 +852,8 @@ int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& wor
     if (cudaFuncSetAttribute(k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) != cudaSuccess)
         return JBGPU_ERR_CUDA;
     int perPgs = 0, perColour = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perPgs, k_pgs, SOLVER_THREADS, smem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perColour, k_colour, SOLVER_THREADS, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perPgs, k_pgs, threads, smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perColour, k_colour, threads, 0) != cudaSuccess ||
         perPgs < 1 || perColour < 1)
         return JBGPU_ERR_CUDA;
     sb.gridPgs = std::min(parts, perPgs * sms);
@@ -794,6 +890,7 @@ void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, Solver
     cudaMemsetAsync(sb.lcFill, 0, sizeof(int) * parts * (MAX_LOCAL + 1), s);
     cudaMemsetAsync(sb.colourFill, 0, sizeof(int) * (MAX_COLOURS + 1), s);
     cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
+    cudaMemsetAsync(w.ctr + C_PGS_ITERS, 0, sizeof(int), s);
     k_posof<<<gridn(sb.nFinite, 256), 256, 0, s>>>(sb); note_launch();
     k_classify<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, sb); note_launch();
     exclusive_scan(sb.bucketCount, sb.bucketStart, nullptr, parts + 2, sb.scanScratch, s);
@@ -803,7 +900,7 @@ void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, Solver
         DevPairs pc = P;
         SolverBuffers sc = sb;
         void* args[] = {&wc, &pc, &sc};
-        cudaLaunchCooperativeKernel((void*)k_colour, sb.gridColour, SOLVER_THREADS, args, 0, s); note_launch();
+        cudaLaunchCooperativeKernel((void*)k_colour, sb.gridColour, sb.threads, args, 0, s); note_launch();
     }
     k_slots<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, sb, R); note_launch();
     if (prof) { prof->mark(PH_COLOUR, 1, s); prof->mark(PH_SETUP, 0, s); }
@@ -817,7 +914,7 @@ void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, Solver
         SolverBuffers sc = sb;
         float dtc = dt;
         void* args[] = {&wc, &pc, &rc, &sc, &dtc};
-        cudaLaunchCooperativeKernel((void*)k_pgs, sb.gridPgs, SOLVER_THREADS, args, pgs_smem(sb), s); note_launch();
+        cudaLaunchCooperativeKernel((void*)k_pgs, sb.gridPgs, sb.threads, args, pgs_smem(sb), s); note_launch();
     }
     if (prof) prof->mark(PH_PGS, 1, s);
 }

@@ -52,12 +52,16 @@ struct SolverBuffers {
     int worldParts = 0;
     int gridColour = 0;           // co-resident blocks of the cooperative kernels
     int gridPgs = 0;
+    int threads = SOLVER_THREADS;
 };
 
 // (Re)plans the parts for nFinite ordered bodies.  worldCounts: finite bodies per batch world;
-// rangeParts > 0 asks for that many range parts.
-int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts);
+// rangeParts > 0 asks for that many range parts; threads per block of the colouring and PGS.
+int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts,
+                     int threads);
 void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
+void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
+void islands_launch_select(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
 void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& rows, SolverBuffers& sb, float dt, cudaStream_t s,
                   const Prof* prof = nullptr);
 void solver_free(SolverBuffers& sb);

@@ -73,6 +73,8 @@ struct jbgpu_world {
     int device = 0;
     int sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux = nullptr;       // second stream: island unions beside the narrowphase
+    cudaEvent_t evFork = nullptr, evJoin = nullptr;
     float localTime = 1.0f / 60.0f;
     long long steps = 0;
     // shapes
@@ -331,7 +333,8 @@ int prepare_solver(jbgpu_world* w) {
     SolverBuffers& S = w->sb;
     const int nf = w->bb.nFinite;
     if (w->solverDirty) {
-        int rc = solver_configure(S, nf, w->worldFinite, w->sms, w->cfg.solver_parts);
+        int rc = solver_configure(S, nf, w->worldFinite, w->sms, w->cfg.solver_parts,
+                                  w->cfg.solver_threads ? w->cfg.solver_threads : SOLVER_THREADS);
         if (rc) return fail(rc, "solver part tables");
         w->solverDirty = false;
     }
@@ -393,11 +396,31 @@ int prepare(jbgpu_world* w) {
     return sync_planes(w);
 }
 
+// Narrowphase and islands of one step: the island unions run on the second stream while the
+// narrowphase runs on the world's stream; sleep decisions and manifold selection follow both.
+int narrow_and_islands(jbgpu_world* w) {
+    cudaStream_t s = w->stream, a = w->aux;
+    DevWorld d = dev_view(w);
+    CK(cudaEventRecord(w->evFork, s));
+    CK(cudaStreamWaitEvent(a, w->evFork, 0));
+    CK(cudaMemsetAsync(w->dw.ctr + C_ISLANDS, 0, sizeof(int) * 4, a));
+    islands_launch_unions(d, w->pairs[w->cur], w->nPairs, w->sb, a);
+    CK(cudaEventRecord(w->evJoin, a));
+    CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
+    narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s, &w->prof);
+    CK(cudaStreamWaitEvent(s, w->evJoin, 0));
+    w->prof.mark(PH_ISLANDS, 0, s);
+    islands_launch_select(d, w->pairs[w->cur], w->nPairs, w->sb, s);
+    w->prof.mark(PH_ISLANDS, 1, s);
+    CK(cudaGetLastError());
+    return JBGPU_OK;
+}
+
 int single_step(jbgpu_world* w, float dt) {
     static const int order[] = {JBGPU_STAGE_PREDICT, JBGPU_STAGE_AABB, JBGPU_STAGE_PAIRS, JBGPU_STAGE_NARROWPHASE,
-                                JBGPU_STAGE_ISLANDS, JBGPU_STAGE_SOLVE, JBGPU_STAGE_INTEGRATE, JBGPU_STAGE_ACTIVATION};
+                                JBGPU_STAGE_SOLVE, JBGPU_STAGE_INTEGRATE, JBGPU_STAGE_ACTIVATION};
     for (int st : order) {
-        int rc = run_stage(w, st, dt);
+        int rc = st == JBGPU_STAGE_NARROWPHASE ? narrow_and_islands(w) : run_stage(w, st, dt);
         if (rc) return rc;
     }
     w->steps++;
@@ -541,6 +564,8 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
         return fail(JBGPU_ERR_UNSUPPORTED, "only the cache-friendly solver path is implemented");
     if (c.num_iterations < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "num_iterations < 0");
     if (c.solver_parts < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "solver_parts < 0");
+    if (c.solver_threads != 0 && c.solver_threads != 64 && c.solver_threads != 128 && c.solver_threads != 256)
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "solver_threads must be 0, 64, 128 or 256");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return fail(JBGPU_ERR_NO_DEVICE, "no CUDA device");
     if (c.device < 0 || c.device >= ndev) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad device ordinal");
@@ -549,13 +574,21 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
     w->device = c.device;
     if (cudaSetDevice(w->device) != cudaSuccess) { delete w; return fail(JBGPU_ERR_CUDA, "cudaSetDevice"); }
     w->sms = num_sms_of(w->device);
-    if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) { delete w; return fail(JBGPU_ERR_CUDA, "stream"); }
+    if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&w->aux, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w->evFork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&w->evJoin, cudaEventDisableTiming) != cudaSuccess) {
+        jbgpu_world_destroy(w);
+        return fail(JBGPU_ERR_CUDA, "stream");
+    }
     DevWorld& d = w->dw;
     for (int k = 0; k < 3; k++) d.gravityAcc[k] = c.gravity[k];
     d.cbt = c.contact_breaking_threshold;
     d.deactTime = c.deactivation_time;
     d.disableDeact = c.disable_deactivation;
     d.numIter = c.num_iterations;
+    d.resTol = c.solver_residual > 0.0f ? c.solver_residual : 0.0f;
+    d.maxIter = c.solver_max_iterations > 0 ? c.solver_max_iterations : 200;
     d.erp = c.erp;
     d.warm = c.warmstarting_factor;
     d.slop = c.linear_slop;
@@ -572,10 +605,8 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
              CK(dalloc(&S.colourStart, MAX_COLOURS + 1)); CK(dalloc(&S.nCand, 1)); CK(dalloc(&S.nColours, 1));
              CK(cudaMemset(S.nCand, 0, sizeof(int))); CK(cudaMemset(S.nColours, 0, sizeof(int)));
              NarrowBuffers& N = w->nb;
-             N.slots = w->sms * 96;
-             size_t fs = (size_t)N.slots * 1024, ms = (size_t)N.slots * 288, ss = (size_t)N.slots * 136, st = (size_t)N.slots * 2048;
-             CK(dalloc(&N.fN, fs)); CK(dalloc(&N.fV, fs)); CK(dalloc(&N.fF, fs)); CK(dalloc(&N.fE, fs)); CK(dalloc(&N.fD, fs));
-             CK(dalloc(&N.mW, ms)); CK(dalloc(&N.mR, ms)); CK(dalloc(&N.seen, ss)); CK(dalloc(&N.stack, st));
+             N.slots = w->sms * 2;
+             if (narrowphase_configure()) return fail(JBGPU_ERR_CUDA, "EPA shared-memory size");
              CK(dalloc(&N.queueCount, 1));
              return grow_bodies(w, std::max(1, c.initial_body_capacity));
          }()) != JBGPU_OK) {
@@ -590,6 +621,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     if (!w) return JBGPU_OK;
     cudaSetDevice(w->device);
     if (w->stream) cudaStreamSynchronize(w->stream);
+    if (w->aux) cudaStreamSynchronize(w->aux);
     DevWorld& d = w->dw;
     dfree(d.xr0); dfree(d.xr1); dfree(d.xr2); dfree(d.linvel); dfree(d.angvel); dfree(d.iw0); dfree(d.iw1); dfree(d.iw2);
     dfree(d.iloc); dfree(d.force); dfree(d.torque); dfree(d.gravity); dfree(d.amin); dfree(d.amax); dfree(d.act);
@@ -614,7 +646,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.cursor); dfree(B.total); dfree(B.partners);
     NarrowBuffers& N = w->nb;
     if (N.queue) cudaFree(N.queue);
-    dfree(N.queueCount); dfree(N.fN); dfree(N.fV); dfree(N.fF); dfree(N.fE); dfree(N.fD); dfree(N.mW); dfree(N.mR); dfree(N.seen); dfree(N.stack);
+    dfree(N.queueCount);
     SolverBuffers& V = w->sb;
     dfree(V.parent); dfree(V.keepAwake); dfree(V.inactive); dfree(V.flag); dfree(V.candIdx); dfree(V.cand); dfree(V.colourOf);
     dfree(V.bucket); dfree(V.bucketList); dfree(V.claim); dfree(V.taken); dfree(V.posOf);
@@ -626,6 +658,9 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     free_prof(w->prof);
     if (w->profHist) cudaFree(w->profHist);
     if (w->ioStage) cudaFree(w->ioStage);
+    if (w->evFork) cudaEventDestroy(w->evFork);
+    if (w->evJoin) cudaEventDestroy(w->evJoin);
+    if (w->aux) cudaStreamDestroy(w->aux);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
     return JBGPU_OK;
@@ -1108,6 +1143,9 @@ int jbgpu_world_counters(jbgpu_world* w, jbgpu_counters* c) {
     c->gjk_calls = h[C_GJK];
     c->epa_calls = h[C_EPA];
     c->status_flags = h[C_STATUS];
+    c->solver_iterations = h[C_PGS_ITERS];
+    c->cut_colours = h[C_CUT_COLOURS];
+    c->cut_manifolds = h[C_CUT_MANIFOLDS];
     return JBGPU_OK;
 }
 
@@ -1205,6 +1243,9 @@ int jbgpu_world_profile_counters(jbgpu_world* w, jbgpu_counters* out, int32_t ca
         o.gjk_calls = c[C_GJK];
         o.epa_calls = c[C_EPA];
         o.status_flags = c[C_STATUS];
+        o.solver_iterations = c[C_PGS_ITERS];
+        o.cut_colours = c[C_CUT_COLOURS];
+        o.cut_manifolds = c[C_CUT_MANIFOLDS];
     }
     return JBGPU_OK;
 }

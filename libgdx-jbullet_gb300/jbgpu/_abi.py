@@ -68,7 +68,10 @@ class Config(C.Structure):
         ("initial_body_capacity", C.c_int32),
         ("pairs_per_body", C.c_int32),
         ("solver_parts", C.c_int32),
-        ("reserved", C.c_int32 * 7),
+        ("solver_threads", C.c_int32),
+        ("solver_residual", C.c_float),
+        ("solver_max_iterations", C.c_int32),
+        ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -165,7 +168,10 @@ class Counters(C.Structure):
         ("gjk_calls", C.c_int32),
         ("epa_calls", C.c_int32),
         ("status_flags", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("solver_iterations", C.c_int32),
+        ("cut_colours", C.c_int32),
+        ("cut_manifolds", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
     def as_dict(self):

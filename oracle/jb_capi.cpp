@@ -46,6 +46,8 @@ void* orc_create(const jbgpu_config* c) {
         w->cfg.warmstartingFactor = c->warmstarting_factor;
         w->cfg.linearSlop = c->linear_slop;
         w->cfg.solverMode = c->solver_mode;
+        w->cfg.residualTol = c->solver_residual;
+        w->cfg.maxIterations = c->solver_max_iterations > 0 ? c->solver_max_iterations : 200;
     }
     return w;
 }
@@ -221,6 +223,7 @@ void orc_counters(void* h, jbgpu_counters* c) {
     c->gjk_calls = w.counters.gjk;
     c->epa_calls = w.counters.epa;
     c->status_flags = w.counters.orderMismatch ? ORC_ORDER_MISMATCH : 0;
+    c->solver_iterations = w.counters.solverIterations;
 }
 
 void orc_phase_seconds(void* h, double* out) {

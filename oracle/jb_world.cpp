@@ -478,9 +478,32 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
         }
     }
     w.counters.solverRows += (int)rows.size();
-    // solveGroupCacheFriendlyIterations (java:788-890), split impulse off
-    for (int it = 0; it < cfg.numIterations; it++) {
+    // solveGroupCacheFriendlyIterations (java:788-890), split impulse off.  With a residual
+    // tolerance the iterations of a world stop once max|delta lambda| / max(max|lambda|, 1e-6)
+    // over its rows is within it (the GPU's residual-terminated mode); rows of converged worlds
+    // are skipped.
+    const bool byResidual = cfg.residualTol > 0.0f;
+    const int maxIt = byResidual ? cfg.maxIterations : cfg.numIterations;
+    int nWorlds = 1;
+    for (const Row& c : rows) nWorlds = std::max(nWorlds, w.bodies[w.pairMf[c.mfPair].body0].world + 1);
+    auto world_of = [&](const Row& c) { return w.bodies[w.pairMf[c.mfPair].body0].world; };
+    std::vector<uint8_t> converged(nWorlds, 1);      // worlds without rows take no iteration
+    for (const Row& c : rows) converged[world_of(c)] = 0;
+    std::vector<float> dmax(nWorlds), lmax(nWorlds);
+    auto track = [&](int wi, float d, float l) {
+        d = d < 0.0f ? -d : d;
+        l = l < 0.0f ? -l : l;
+        if (d > dmax[wi]) dmax[wi] = d;
+        if (l > lmax[wi]) lmax[wi] = l;
+    };
+    int itersUsed = 0;
+    for (int it = 0; it < maxIt; it++) {
+        bool any = false;
+        for (int k = 0; k < nWorlds; k++) { dmax[k] = 0.0f; lmax[k] = 0.0f; any = any || !converged[k]; }
+        if (!any) break;
+        itersUsed = it + 1;
         for (Row& c : rows) {   // resolveSingleCollisionCombinedCacheFriendly (java:234-284)
+            if (converged[world_of(c)]) continue;
             SolverBody& A = sb[c.bodyA];
             SolverBody& B = sb[c.bodyB];
             float vel1Dotn = dot(c.normal, A.linvel) + dot(c.rp1xn, A.angvel);
@@ -497,10 +520,14 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
             normalImpulse = c.impulse - oldImpulse;
             A.apply(scl(c.normal, A.invMass), c.angA, normalImpulse);
             B.apply(scl(c.normal, B.invMass), c.angB, -normalImpulse);
+            track(world_of(c), normalImpulse, c.impulse);
         }
         for (Row& c : frows) {  // resolveSingleFrictionCacheFriendly (java:286-346)
+            const int wi = world_of(rows[c.frictionIndex]);
+            if (converged[wi]) continue;
             float total = rows[c.frictionIndex].impulse + rows[c.frictionIndex].pushImpulse;
             float limit = total * c.friction;
+            if (!(total > 0.0f)) track(wi, 0.0f, c.impulse);
             if (total > 0.0f) {
                 SolverBody& A = sb[c.bodyA];
                 SolverBody& B = sb[c.bodyB];
@@ -515,9 +542,14 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
                 j1 = c.impulse - old;
                 A.apply(scl(c.normal, A.invMass), c.angA, j1);
                 B.apply(scl(c.normal, B.invMass), c.angB, -j1);
+                track(wi, j1, c.impulse);
             }
         }
+        if (byResidual)
+            for (int k = 0; k < nWorlds; k++)
+                if (!converged[k] && dmax[k] / (lmax[k] > 1e-6f ? lmax[k] : 1e-6f) <= cfg.residualTol) converged[k] = 1;
     }
+    if (itersUsed > w.counters.solverIterations) w.counters.solverIterations = itersUsed;
     // write-back (java:901-924): appliedImpulseLateral1 is assigned twice, lateral2 never
     for (const Row& c : rows) {
         ManifoldPoint& pt = w.pairMf[c.mfPair].pts[c.mfPoint];
@@ -603,6 +635,7 @@ static std::vector<int> colour_order(World& w, const std::vector<int>& cand, std
 void stage_solve(World& w, float dt) {
     PhaseTimer pt(w, 6);
     w.counters.solverRows = 0;
+    w.counters.solverIterations = 0;
     w.lastOrder.clear();
     w.lastColour.clear();
     if (w.orderMode == ORDER_REFERENCE) {

@@ -92,6 +92,8 @@ struct Config {
     int numIterations = 10;
     float erp = 0.2f, warmstartingFactor = 0.85f, linearSlop = 0.0f;
     int solverMode = SOLVER_CACHE_FRIENDLY | SOLVER_USE_WARMSTARTING;
+    float residualTol = 0.0f;         // > 0: iterate to this residual per world (jbgpu_config.solver_residual)
+    int maxIterations = 200;
 };
 
 struct Counters {
@@ -99,6 +101,7 @@ struct Counters {
     int pairs = 0, manifolds = 0, contacts = 0, solverManifolds = 0, solverRows = 0, colours = 0, islands = 0;
     int gjk = 0, epa = 0;
     int orderMismatch = 0;   // solves whose explicit order was not a permutation of the candidates
+    int solverIterations = 0;
 };
 
 // Solver order policy (the reference's F8 hook, SequentialImpulseConstraintSolver.java:769-779):

@@ -112,6 +112,34 @@ def test_range_parts_lockstep_bit_exact(gpu_lib, oracle_lib, name, parts):
     g.close()
 
 
+@pytest.mark.parametrize("name", ["stack", "mixed120", "boxes300"])
+@pytest.mark.parametrize("parts", [0, 3])
+def test_residual_mode_bit_exact(gpu_lib, oracle_lib, name, parts):
+    """Residual-terminated PGS (tolerance 1e-4, at most 60 iterations): the GPU stops after the
+    same iteration as the oracle fed its order, and state and manifolds stay bit-identical.
+    parts 0: one solver part per world (block-local residual); 3: range parts, cut manifolds
+    and a grid-wide residual."""
+    sc = SCENES[name]()
+    cfg = dict(sc.config, solver_residual=1e-4, solver_max_iterations=60)
+    o = pyoracle.OracleWorld(sc, config=_abi.default_config(**cfg))
+    g = GpuWorld(sc, config=_abi.default_config(**dict(cfg, solver_parts=parts)))
+    iters = []
+    for s in range(80):
+        g.step(sc.dt)
+        o.set_explicit_order(g.solver_order())
+        o.step(sc.dt)
+        co, cg = o.counters(), g.counters()
+        assert co["status_flags"] == 0 and cg["status_flags"] == 0, s
+        assert co["solver_iterations"] == cg["solver_iterations"], (s, co["solver_iterations"], cg["solver_iterations"])
+        iters.append(cg["solver_iterations"])
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+            assert not bs and not bm, (s, bs, bm)
+    assert max(iters) > 10          # the tolerance, not the default 10 iterations, decided
+    g.close()
+
+
 def test_boxes_1k_300_steps_within_contract_tolerance(gpu_lib, oracle_lib):
     """The 1,000-box workload for its full 300 steps: per-step pair sets identical and
     body state within 1e-4 relative (the solver contract) of the oracle in colour order."""

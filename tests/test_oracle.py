@@ -143,3 +143,28 @@ def test_batched_worlds_equal_solo_worlds(oracle_lib):
         ss = s.get_state()
         for k in ("transform", "linear_velocity", "angular_velocity"):
             assert np.array_equal(sb[k][starts[wi]:starts[wi + 1]], ss[k]), (wi, k)
+
+
+def test_residual_mode_iterates_to_the_tolerance(oracle_lib):
+    """Residual-terminated PGS: a loose tolerance stops after one iteration, tighter ones take
+    more iterations (capped), and a fixed iteration count is unaffected by the cap."""
+    sc = scenes.box_stack(4)
+    warm = pyoracle.OracleWorld(sc)
+    for _ in range(30):
+        warm.step(sc.dt)
+    its = {}
+    for tol in (10.0, 1e-2, 1e-4, 1e-6):
+        o = pyoracle.OracleWorld(sc, config=_abi.default_config(**dict(sc.config, solver_residual=tol,
+                                                                          solver_max_iterations=150)))
+        o.set_state(warm.get_state())
+        o.set_manifolds(warm.get_manifolds())
+        o.step(sc.dt)
+        its[tol] = o.counters()["solver_iterations"]
+    assert its[10.0] == 1
+    assert its[10.0] <= its[1e-2] <= its[1e-4] <= its[1e-6] <= 150
+    assert its[1e-4] > 10
+    f = pyoracle.OracleWorld(sc)
+    f.set_state(warm.get_state())
+    f.set_manifolds(warm.get_manifolds())
+    f.step(sc.dt)
+    assert f.counters()["solver_iterations"] == sc.config["num_iterations"]
