@@ -123,11 +123,10 @@ typedef struct jbgpu_config {
     int32_t solver_threads;             /* threads per solver block: 0 (default 256), 64, 128 or 256.
                                            No counterpart in the reference. */
     float   solver_residual;            /* 0 (default): num_iterations PGS iterations, as the reference.
-                                           > 0: iterate until the residual
-                                           max|lambda_k - lambda_k-1| / max(max|lambda_k|, 1e-6) over
-                                           all rows of a world is <= this value (batched worlds: per
-                                           world when each world is one solver part, else over the
-                                           batch), at most solver_max_iterations. */
+                                           > 0: the rows of an island (the group one reference
+                                           solveGroup call receives) iterate until its residual
+                                           max|lambda_k - lambda_k-1| / max(max|lambda_k|, 1e-6) is
+                                           <= this value, at most solver_max_iterations. */
     int32_t solver_max_iterations;      /* cap for solver_residual > 0; 0 means 200 */
     int32_t reserved[4];
 } jbgpu_config;
@@ -203,7 +202,9 @@ typedef struct jbgpu_counters {
     int32_t solver_iterations;/* PGS iterations of the last solve (the largest over worlds) */
     int32_t cut_colours;      /* colours of manifolds cut between solver parts (GPU only) */
     int32_t cut_manifolds;    /* manifolds cut between solver parts (GPU only) */
-    int32_t reserved[3];
+    int32_t solver_islands;   /* residual mode: islands with solver rows in the last solve */
+    int32_t solver_islands_converged;  /* ... of which reached the residual */
+    int32_t solver_island_iterations;  /* ... sum over them of the iterations they took */
 } jbgpu_counters;
 
 /* ---- library -------------------------------------------------------------------- */
@@ -250,6 +251,55 @@ int jbgpu_world_narrowphase_static(jbgpu_world* world, int32_t epa_slots);
 
 /* Wait for the world's stream. */
 int jbgpu_world_synchronize(jbgpu_world* world);
+
+/* The iteration fields of the world's ContactSolverInfo, changed between steps as a caller of
+ * the reference changes getSolverInfo().numIterations (dynamics/constraintsolver/
+ * ContactSolverInfo.java:38): num_iterations (> 0), and solver_residual / solver_max_iterations
+ * with the meaning of jbgpu_config. */
+int jbgpu_world_set_solver_iterations(jbgpu_world* world, int32_t num_iterations, float residual,
+                                      int32_t max_iterations);
+
+/* ---- learned warm start (no counterpart in the reference) ---------------------------
+ * A per-contact MLP 24 -> 64 -> 64 -> 3 (GELU, BF16 weights and activations on the tensor
+ * cores, FP32 accumulation) predicts each contact point's converged normal and two friction
+ * impulses from its features; the PGS then starts from the prediction instead of
+ * warmstarting_factor x last step's impulses, and runs to jbgpu_config.solver_residual.
+ * Features of a point (JBGPU_MLP_INPUTS floats): normal (3), distance (1), relative velocity
+ * at the contact (3), relative angular velocity (3), inverse masses (2), inverse-inertia-
+ * projected normals of both bodies (6), last applied / lateral impulses (3), friction,
+ * restitution (2), lifetime (1).  Targets (JBGPU_MLP_OUTPUTS floats): the converged impulses of
+ * the normal row and both friction rows. */
+#define JBGPU_MLP_INPUTS  24
+#define JBGPU_MLP_OUTPUTS 3
+#define JBGPU_MLP_PARAMS  5955  /* W1[64][24] b1[64] W2[64][64] b2[64] W3[3][64] b3[3] */
+#define JBGPU_MLP_NORM    55    /* in_mean[24] in_scale[24] out_mean[3] out_scale[3] unit:
+                                   x' = asinh((x - in_mean) * in_scale);  y = y' * out_scale + out_mean;
+                                   unit: impulse scale of the warm-start transform below */
+typedef struct jbgpu_mlp jbgpu_mlp;
+int jbgpu_mlp_create(int32_t device, uint64_t seed, jbgpu_mlp** out);   /* Xavier weights, identity normalisation */
+int jbgpu_mlp_destroy(jbgpu_mlp* mlp);
+int jbgpu_mlp_get_params(jbgpu_mlp* mlp, float* params, float* normalization);       /* either may be NULL */
+int jbgpu_mlp_set_params(jbgpu_mlp* mlp, const float* params, const float* normalization);
+/* y[n][3] = MLP(x[n][24]) in raw units (host buffers). */
+int jbgpu_mlp_forward(jbgpu_mlp* mlp, const float* x, int32_t n, float* y);
+/* Gradient (JBGPU_MLP_PARAMS floats) and value of the mean squared error of the normalised
+ * outputs over the n samples (host buffers). */
+int jbgpu_mlp_gradients(jbgpu_mlp* mlp, const float* x, const float* t, int32_t n, float* grad, float* loss);
+/* Training set to the device, then Adam (0.9, 0.999, 1e-8) over shuffled mini-batches. */
+int jbgpu_mlp_load_samples(jbgpu_mlp* mlp, const float* x, const float* t, int32_t n);
+int jbgpu_mlp_train(jbgpu_mlp* mlp, int32_t epochs, int32_t batch, float learning_rate, uint64_t seed,
+                    float* loss_per_epoch);
+/* Warm-start impulses from `mlp` (NULL: the reference warm start).  With b the point's last
+ * normal impulse, mu its friction, u = unit / (invMass0 + invMass1) and y = 0.01 sinh(output),
+ * the outputs map to normal = max(0, b + y0 (b + u)) and friction k = y(1+k) mu (b + u), clamped
+ * to the cone.  The MLP must live on the world's device and outlive its use by the world. */
+int jbgpu_world_set_warmstart_mlp(jbgpu_world* world, jbgpu_mlp* mlp);
+/* Record features before and converged impulses after every solve (training data). */
+int jbgpu_world_set_sample_logging(jbgpu_world* world, int32_t on);
+/* The last solve's samples: x[n][24], t[n][3] (host buffers); with x or t NULL only *n is set;
+ * n > capacity is JBGPU_ERR_CAPACITY with *n set.  With solver_residual > 0 only points of
+ * islands that reached the residual are samples. */
+int jbgpu_world_get_samples(jbgpu_world* world, float* x, float* t, int32_t capacity, int32_t* n);
 
 int jbgpu_world_get_state(jbgpu_world* world, jbgpu_state* state);
 int jbgpu_world_set_state(jbgpu_world* world, const jbgpu_state* state);

@@ -22,6 +22,7 @@
 #include <cstdlib>
 #include "../../include/jbgpu.h"
 #include "manifold.cuh"
+#include "mlp.cuh"
 #include "prims.cuh"
 #include "solver.cuh"
 
@@ -654,11 +655,33 @@ JBD void stage_out(const DevWorld& w, const SolverBuffers& sb, const PartView& v
     }
 }
 
+// Residual bookkeeping of one manifold (residual mode): skipped once its island converged,
+// else its largest |delta lambda| and |lambda| of this iteration kept per slot.
+struct ResCtl {
+    bool on = false;        // residual-terminated mode
+    bool skipConv = false;  // an island convergence test has run (iteration >= 2)
+};
+JBD bool res_skip(const SolverBuffers& sb, const ResCtl& rc, int s) {
+    return rc.on && rc.skipConv && __ldcg(&sb.islConv[sb.slotIsl[s]]) != 0;
+}
+JBD void res_keep(const SolverBuffers& sb, const ResCtl& rc, int kind, int s, const Resid& r) {
+    if (!rc.on || kind == PH_WARM) return;
+    if (kind == PH_NORMAL) {
+        __stcg(&sb.md[s], r.d);
+        __stcg(&sb.ml[s], r.l);
+    } else {
+        float d = __ldcg(&sb.md[s]), l = __ldcg(&sb.ml[s]);
+        if (r.d > d) __stcg(&sb.md[s], r.d);
+        if (r.l > l) __stcg(&sb.ml[s], r.l);
+    }
+}
+
 // One local colour of a part: its manifolds share no dynamic body; the part's bodies are in
 // shared memory (global memory when the part does not fit).
-JBD void local_colour(const DevWorld& w, const DevRows& R, int s0, int s1, int kind, bool smem, float4* sl, float4* sa,
-                      Resid& res) {
+JBD void local_colour(const DevWorld& w, const DevRows& R, const SolverBuffers& sb, int s0, int s1, int kind, bool smem,
+                      float4* sl, float4* sa, const ResCtl& rc) {
     for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+        if (res_skip(sb, rc, s)) continue;
         const int4 d = R.slot_desc[s];
         const float2 im = R.slot_im[s];
         const int lb0 = d.w & 0xffff, lb1 = (d.w >> 16) & 0xffff;
@@ -666,34 +689,69 @@ JBD void local_colour(const DevWorld& w, const DevRows& R, int s0, int s1, int k
         V l0, a0, l1, a1;
         if (m0) { l0 = mk4(sl[lb0]); a0 = mk4(sa[lb0]); } else gload(w, d.x, l0, a0);
         if (m1) { l1 = mk4(sl[lb1]); a1 = mk4(sa[lb1]); } else gload(w, d.y, l1, a1);
+        Resid res;
         solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
+        res_keep(sb, rc, kind, s, res);
         if (im.x != 0.0f) { if (m0) { sl[lb0] = f4(l0, 0.0f); sa[lb0] = f4(a0, 0.0f); } else gstore(w, d.x, l0, a0); }
         if (im.y != 0.0f) { if (m1) { sl[lb1] = f4(l1, 0.0f); sa[lb1] = f4(a1, 0.0f); } else gstore(w, d.y, l1, a1); }
     }
 }
 
-// Block-wide maxima of the threads' residual terms (non-negative floats order as their bits).
-JBD void block_resid(const Resid& r, unsigned* sh, float& dmax, float& lmax) {
-    if (threadIdx.x == 0) { sh[0] = 0u; sh[1] = 0u; }
-    __syncthreads();
-    atomicMax(&sh[0], __float_as_uint(r.d));
-    atomicMax(&sh[1], __float_as_uint(r.l));
-    __syncthreads();
-    dmax = __uint_as_float(sh[0]);
-    lmax = __uint_as_float(sh[1]);
-    __syncthreads();
-}
-
 JBD bool resid_done(float dmax, float lmax, float tol) { return jdiv(dmax, lmax > 1e-6f ? lmax : 1e-6f) <= tol; }
 
+// Island residuals after an iteration: one warp per chunk of up to ISL_CHUNK slots of an
+// island.  An island of one chunk is decided by its warp; a larger one combines its chunks'
+// maxima with atomics, and the warp that finishes its last chunk decides (and clears the
+// accumulators for the next iteration).  Unconverged islands are counted in ctr[flag].
+constexpr int ISL_CHUNK = 1024;
+
+JBD void island_residuals(const DevWorld& w, const SolverBuffers& sb, int flag, int it) {
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    const int nChunks = *sb.nIslChunks;
+    for (int ch = gw; ch < nChunks; ch += nw) {
+        const int2 cd = sb.islChunk[ch];
+        const int isl = cd.x;
+        if (__ldcg(&sb.islConv[isl])) continue;
+        const int i0 = sb.islStart[isl], i1 = sb.islStart[isl + 1];
+        const int e0 = i0 + cd.y * ISL_CHUNK, e1 = min(e0 + ISL_CHUNK, i1);
+        Resid r;
+        for (int e = e0 + lane; e < e1; e += 32) {
+            const int s = sb.islList[e];
+            r.add(__ldcg(&sb.md[s]), __ldcg(&sb.ml[s]));
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            float od = __shfl_xor_sync(0xffffffffu, r.d, o), ol = __shfl_xor_sync(0xffffffffu, r.l, o);
+            if (od > r.d) r.d = od;
+            if (ol > r.l) r.l = ol;
+        }
+        if (lane != 0) continue;
+        float dm = r.d, lm = r.l;
+        const int nch = (i1 - i0 + ISL_CHUNK - 1) / ISL_CHUNK;
+        if (nch > 1) {
+            atomicMax((unsigned*)&sb.islAcc[2 * isl], __float_as_uint(dm));
+            atomicMax((unsigned*)&sb.islAcc[2 * isl + 1], __float_as_uint(lm));
+            __threadfence();
+            if (atomicAdd(&sb.islDone[isl], 1) != nch - 1) continue;
+            __threadfence();
+            dm = __uint_as_float((unsigned)__ldcg(&sb.islAcc[2 * isl]));
+            lm = __uint_as_float((unsigned)__ldcg(&sb.islAcc[2 * isl + 1]));
+            sb.islAcc[2 * isl] = 0;
+            sb.islAcc[2 * isl + 1] = 0;
+            sb.islDone[isl] = 0;
+        }
+        if (resid_done(dm, lm, w.resTol)) sb.islConv[isl] = it;
+        else atomicAdd(&w.ctr[flag], 1);
+    }
+}
+
 // Phases: warm start, then iterations of (normal rows, friction rows): numIterations of them,
-// or, with a residual tolerance, until the residual of the rows' world is within it (at most
-// maxIter).  Within a phase the parts' internal manifolds run first (parts share no dynamic
-// body), then the cut colours.  Without cut manifolds — and, for the residual, with one world
-// per part — every part runs all phases on its own, with no grid barrier.
+// or, with a residual tolerance, until every island's residual is within it (at most maxIter;
+// the rows of an island stop once it converges).  Within a phase the parts' internal
+// manifolds run first (parts share no dynamic body), then the cut colours.  With fixed
+// iterations and no cut manifold every part runs all phases on its own, with no grid barrier.
 __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs P, DevRows R, SolverBuffers sb, float dt) {
     extern __shared__ float4 smv[];
-    __shared__ unsigned shRes[2];
     const int nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int nCut = *sb.nColours;
@@ -703,33 +761,27 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
     float4* sa = smv + sb.partMax;
     const bool byRes = w.resTol > 0.0f;
     const int maxIt = byRes ? w.maxIter : w.numIter;
-    if (nCut == 0 && (!byRes || sb.worldParts)) {
+    ResCtl rc;
+    rc.on = byRes;
+    if (nCut == 0 && !byRes) {
         int itMax = 0;
         for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
             const PartView v = part_view(sb, part);
             if (smem) stage_in(w, sb, v, sl, sa);
             __syncthreads();
-            Resid res;
             for (int c = 0; c < v.nLoc; c++) {
-                local_colour(w, R, v.lcs[c], v.lcs[c + 1], PH_WARM, smem, sl, sa, res);
+                local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_WARM, smem, sl, sa, rc);
                 __syncthreads();
             }
             int it = 0;
-            while (it < maxIt && v.nLoc > 0) {
-                Resid r;
+            for (; it < maxIt && v.nLoc > 0; it++) {
                 for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, v.lcs[c], v.lcs[c + 1], PH_NORMAL, smem, sl, sa, r);
+                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_NORMAL, smem, sl, sa, rc);
                     __syncthreads();
                 }
                 for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, v.lcs[c], v.lcs[c + 1], PH_FRICTION, smem, sl, sa, r);
+                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_FRICTION, smem, sl, sa, rc);
                     __syncthreads();
-                }
-                ++it;
-                if (byRes) {
-                    float dm, lm;
-                    block_resid(r, shRes, dm, lm);
-                    if (resid_done(dm, lm, w.resTol)) break;
                 }
             }
             if (it > itMax) itMax = it;
@@ -742,8 +794,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
         return;
     }
     if (nSlots == 0) return;
-    if (tid == 0) for (int k = 0; k < 6; k++) w.ctr[C_RES0 + k] = 0;
-    Resid res;
+    if (tid == 0) for (int k = 0; k < 3; k++) w.ctr[C_RES0 + k] = 0;
     int it = -1;          // -1: the warm-start phase
     for (;;) {
         for (int sub = 0; sub < (it < 0 ? 1 : 2); sub++) {
@@ -753,7 +804,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                 if (smem) stage_in(w, sb, v, sl, sa);
                 __syncthreads();
                 for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, v.lcs[c], v.lcs[c + 1], kind, smem, sl, sa, res);
+                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, smem, sl, sa, rc);
                     __syncthreads();
                 }
                 if (smem) stage_out(w, sb, v, sl, sa);
@@ -763,12 +814,15 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             for (int c = 0; c < nCut; c++) {
                 const int s0 = sb.colourStart[c], s1 = sb.colourStart[c + 1];
                 for (int s = s0 + tid; s < s1; s += nth) {
+                    if (res_skip(sb, rc, s)) continue;
                     const int4 d = R.slot_desc[s];
                     const float2 im = R.slot_im[s];
                     V l0, a0, l1, a1;
                     gload(w, d.x, l0, a0);
                     gload(w, d.y, l1, a1);
+                    Resid res;
                     solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
+                    res_keep(sb, rc, kind, s, res);
                     if (im.x != 0.0f) gstore(w, d.x, l0, a0);
                     if (im.y != 0.0f) gstore(w, d.y, l1, a1);
                 }
@@ -778,25 +832,164 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
         ++it;
         if (it >= maxIt) break;
         if (byRes && it > 0) {
-            // slot it % 3 collects this iteration; slot (it + 1) % 3 was last read two iterations
-            // ago, behind at least two grid barriers, and is cleared for the next one
-            const int slot = C_RES0 + 2 * (it % 3);
-            if (tid == 0) { w.ctr[C_RES0 + 2 * ((it + 1) % 3)] = 0; w.ctr[C_RES0 + 2 * ((it + 1) % 3) + 1] = 0; }
-            float dm, lm;
-            block_resid(res, shRes, dm, lm);
-            if (threadIdx.x == 0) {
-                atomicMax((unsigned*)&w.ctr[slot], __float_as_uint(dm));
-                atomicMax((unsigned*)&w.ctr[slot + 1], __float_as_uint(lm));
-            }
+            // island residuals of this iteration; ctr[C_RES0 + it % 3] counts islands still
+            // above the tolerance, the next slot is cleared (last read two iterations ago)
+            const int flag = C_RES0 + it % 3;
+            if (tid == 0) w.ctr[C_RES0 + (it + 1) % 3] = 0;
+            island_residuals(w, sb, flag, it);
             grid_barrier(w.ctr, nb);
-            dm = __uint_as_float((unsigned)__ldcg(&w.ctr[slot]));
-            lm = __uint_as_float((unsigned)__ldcg(&w.ctr[slot + 1]));
-            if (resid_done(dm, lm, w.resTol)) break;
+            if (__ldcg(&w.ctr[flag]) == 0) break;
+            rc.skipConv = true;
         }
-        res = Resid();
     }
     if (tid == 0 && it > 0) atomicMax(&w.ctr[C_PGS_ITERS], it);
+    if (byRes) {          // per-island statistics: islConv holds the iteration an island converged at
+        const int nChunks = *sb.nIslChunks;
+        for (int ch = tid; ch < nChunks; ch += nth) {
+            const int2 cd = sb.islChunk[ch];
+            if (cd.y != 0) continue;
+            const int c = __ldcg(&sb.islConv[cd.x]);
+            atomicAdd(&w.ctr[C_ISL_N], 1);
+            if (c > 0) atomicAdd(&w.ctr[C_ISL_CONV], 1);
+            atomicAdd(&w.ctr[C_ISL_ITERS], c > 0 ? c : it);
+        }
+    }
     for (int s = tid; s < nSlots; s += nth) writeback_slot(P, R, s);
+}
+
+// Island index of every solve slot and the slots grouped by island (residual mode).
+__global__ void k_isl_count(DevWorld w, DevRows R, SolverBuffers sb) {
+    int nSlots = *sb.nCand;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nSlots) return;
+    int4 d = R.slot_desc[s];
+    int isl = w.island[d.x] >= 0 ? w.island[d.x] : w.island[d.y];
+    sb.slotIsl[s] = isl;
+    atomicAdd(&sb.islCount[isl], 1);
+}
+__global__ void k_isl_scatter(SolverBuffers sb, int nBodies) {
+    int nSlots = *sb.nCand;
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nSlots) {
+        int isl = sb.slotIsl[s];
+        sb.islList[sb.islStart[isl] + atomicAdd(&sb.islFill[isl], 1)] = s;
+    }
+    if (s < nBodies) sb.segFlag[s] = (sb.islCount[s] + ISL_CHUNK - 1) / ISL_CHUNK;   // chunks of island s
+}
+__global__ void k_isl_segments(SolverBuffers sb, int nBodies) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nBodies) return;
+    int nch = (sb.islCount[i] + ISL_CHUNK - 1) / ISL_CHUNK;
+    for (int c = 0; c < nch; c++) sb.islChunk[sb.segIdx[i] + c] = make_int2(i, c);
+}
+
+// ---- learned warm start and contact samples ------------------------------------------------
+// Features of contact point q = slot * 4 + j (24 floats), from the rows just set up and the body
+// state before the solve: normal (3), distance (1), relative velocity at the contact (3),
+// relative angular velocity (3), inverse masses (2), inverse-inertia-projected normals of
+// both bodies (6), the point's previous applied impulse and lateral impulses (3), friction,
+// restitution (2), lifetime (1).
+JBD void contact_features(const DevWorld& w, const DevPairs& P, const DevRows& R, int s, int j, float* f) {
+    const int p = R.slot_pair[s], k = p * 4 + j, ni = s * 4 + j;
+    const int4 d = R.slot_desc[s];
+    const float2 im = R.slot_im[s];
+    float4 nn = R.n_nrm[ni], aA = R.n_angA[ni], aB = R.n_angB[ni];
+    float4 wa = P.wA[k], wb = P.wB[k], pa = P.pA[k], pb = P.pB[k], nr = P.nrm[k], ii = P.imp[k];
+    V com0 = mk(w.xr0[d.x].w, w.xr1[d.x].w, w.xr2[d.x].w), com1 = mk(w.xr0[d.y].w, w.xr1[d.y].w, w.xr2[d.y].w);
+    V l0 = mk4(w.linvel[d.x]), a0 = mk4(w.angvel[d.x]), l1 = mk4(w.linvel[d.y]), a1 = mk4(w.angvel[d.y]);
+    V rp1 = sub(mk(wa.x, wa.y, wa.z), com0), rp2 = sub(mk(wb.x, wb.y, wb.z), com1);
+    V vel = sub(add(crs(a0, rp1), l0), add(crs(a1, rp2), l1));
+    V dw = sub(a0, a1);
+    f[0] = nn.x; f[1] = nn.y; f[2] = nn.z;
+    f[3] = pa.w;
+    f[4] = vel.x; f[5] = vel.y; f[6] = vel.z;
+    f[7] = dw.x; f[8] = dw.y; f[9] = dw.z;
+    f[10] = im.x; f[11] = im.y;
+    f[12] = aA.x; f[13] = aA.y; f[14] = aA.z;
+    f[15] = aB.x; f[16] = aB.y; f[17] = aB.z;
+    f[18] = nr.w; f[19] = ii.x; f[20] = ii.y;
+    f[21] = aA.w; f[22] = wb.w;
+    f[23] = (float)__float_as_int(pb.w);
+}
+
+__global__ void k_contact_features(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, float* X) {
+    const int nq = *nCandPtr * 4;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const int s = q >> 2, j = q & 3;
+        if (!(R.slot_desc[s].z & (1 << j))) continue;
+        float f[MLP_IN];
+        contact_features(w, P, R, s, j, f);
+        for (int e = 0; e < MLP_IN; e++) X[(size_t)q * MLP_IN + e] = f[e];
+    }
+}
+
+// Targets of points whose island did not reach the residual (residual mode) are NaN: they are
+// not converged impulses, and the sample export leaves them out.
+__global__ void k_contact_targets(DevWorld w, DevRows R, SolverBuffers sb, float* T) {
+    const int nq = *sb.nCand * 4;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        if (!(R.slot_desc[q >> 2].z & (1 << (q & 3)))) continue;
+        if (w.resTol > 0.0f && __ldcg(&sb.islConv[sb.slotIsl[q >> 2]]) == 0) {
+            T[(size_t)q * 3 + 0] = T[(size_t)q * 3 + 1] = T[(size_t)q * 3 + 2] = __int_as_float(0x7fc00000);
+            continue;
+        }
+        T[(size_t)q * 3 + 0] = R.n_angB[q].w;
+        T[(size_t)q * 3 + 1] = R.f_rp1[q * 2].w;
+        T[(size_t)q * 3 + 2] = R.f_rp1[q * 2 + 1].w;
+    }
+}
+
+// Warm-start impulses predicted by the MLP for 64 contact points per tile.  The network's three
+// outputs o give y = MLP_REL sinh(o), relative to the point's last normal impulse b (feature 18)
+// and an impulse scale u = unit / (invMass0 + invMass1): normal = max(0, b + y0 (b + u)),
+// friction k = y(1+k) mu (b + u) clamped to the cone of that normal impulse.  They replace warmstartingFactor x last step's
+// impulses before the PGS warm-start phase.
+__global__ void __launch_bounds__(MLP_THREADS) k_mlp_warmstart(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr,
+                                                                MlpDev M) {
+    extern __shared__ __align__(16) unsigned char mlpSmem[];
+    MlpSmem& S = *reinterpret_cast<MlpSmem*>(mlpSmem);
+    const int nq = *nCandPtr * 4;
+    mlp_load_weights(S, M);
+    for (int first = blockIdx.x * MLP_TILE; first < nq; first += gridDim.x * MLP_TILE) {
+        if (threadIdx.x < MLP_TILE) {
+            const int q = first + threadIdx.x;
+            float f[MLP_IN];
+            bool on = q < nq && (R.slot_desc[q >> 2].z & (1 << (q & 3)));
+            if (on) contact_features(w, P, R, q >> 2, q & 3, f);
+            for (int e = 0; e < MLP_INP; e++) {
+                float v = (on && e < MLP_IN) ? mlp_norm_in(M.norm, e, f[e]) : 0.0f;
+                S.x[threadIdx.x][e] = __float2bfloat16_rn(v);
+            }
+        }
+        __syncthreads();
+        mlp_forward(S, M);
+        if (threadIdx.x < MLP_TILE) {
+            const int q = first + threadIdx.x;
+            if (q < nq && (R.slot_desc[q >> 2].z & (1 << (q & 3)))) {
+                float y[MLP_OUT];
+                for (int o = 0; o < MLP_OUT; o++)
+                    y[o] = MLP_REL * sinhf(S.y[threadIdx.x][o] * M.norm[2 * MLP_IN + MLP_OUT + o] + M.norm[2 * MLP_IN + o]);
+                const float2 im = R.slot_im[q >> 2];
+                const float base = fmaxf(P.nrm[R.slot_pair[q >> 2] * 4 + (q & 3)].w, 0.0f);
+                const float unit = M.norm[MLP_NORM_UNIT] / fmaxf(im.x + im.y, 1e-6f);
+                const float mu = R.n_angA[q].w;
+                float ln = base + y[0] * (base + unit);
+                ln = ln > 0.0f ? ln : 0.0f;
+                float lim = ln * mu;
+                float4 b = R.n_angB[q];
+                b.w = ln;
+                R.n_angB[q] = b;
+                for (int f2 = 0; f2 < 2; f2++) {
+                    float v = y[1 + f2] * mu * (base + unit);
+                    v = v > lim ? lim : (v < -lim ? -lim : v);
+                    float4 r = R.f_rp1[q * 2 + f2];
+                    r.w = v;
+                    R.f_rp1[q * 2 + f2] = r;
+                }
+            }
+        }
+        __syncthreads();
+    }
 }
 
 // ---- host side ------------------------------------------------------------------------------
@@ -868,8 +1061,20 @@ void solver_free(SolverBuffers& sb) {
     sb.partsCap = 0;
 }
 
+size_t mlp_smem_bytes();   // mlp.cu
+
+int solver_learn_configure() {
+    return cudaFuncSetAttribute(k_mlp_warmstart, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mlp_smem_bytes()) ==
+                   cudaSuccess ? 0 : 1;
+}
+
 void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, SolverBuffers& sb, float dt, cudaStream_t s,
                   const Prof* prof) {
+    solve_launch_learn(w, P, nPairs, R, sb, dt, s, prof, SolverLearn());
+}
+
+void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, SolverBuffers& sb, float dt,
+                        cudaStream_t s, const Prof* prof, const SolverLearn& learn) {
     if (prof) prof->mark(PH_COLOUR, 0, s);
     if (nPairs <= 0 || sb.nFinite <= 0 || sb.nParts <= 0) {
         cudaMemsetAsync(sb.nColours, 0, sizeof(int), s);
@@ -891,6 +1096,7 @@ void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, Solver
     cudaMemsetAsync(sb.colourFill, 0, sizeof(int) * (MAX_COLOURS + 1), s);
     cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
     cudaMemsetAsync(w.ctr + C_PGS_ITERS, 0, sizeof(int), s);
+    cudaMemsetAsync(w.ctr + C_ISL_N, 0, sizeof(int) * 3, s);
     k_posof<<<gridn(sb.nFinite, 256), 256, 0, s>>>(sb); note_launch();
     k_classify<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, sb); note_launch();
     exclusive_scan(sb.bucketCount, sb.bucketStart, nullptr, parts + 2, sb.scanScratch, s);
@@ -903,8 +1109,30 @@ void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, Solver
         cudaLaunchCooperativeKernel((void*)k_colour, sb.gridColour, sb.threads, args, 0, s); note_launch();
     }
     k_slots<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, sb, R); note_launch();
+    if (w.resTol > 0.0f) {        // residual mode: slots grouped by island
+        const int n = w.nBodies;
+        cudaMemsetAsync(sb.islCount, 0, sizeof(int) * (n + 1), s);
+        cudaMemsetAsync(sb.islFill, 0, sizeof(int) * (n + 1), s);
+        cudaMemsetAsync(sb.islConv, 0, sizeof(int) * n, s);
+        cudaMemsetAsync(sb.islAcc, 0, sizeof(int) * 2 * n, s);
+        cudaMemsetAsync(sb.islDone, 0, sizeof(int) * n, s);
+        k_isl_count<<<gridn(nPairs, 256), 256, 0, s>>>(w, R, sb); note_launch();
+        exclusive_scan(sb.islCount, sb.islStart, nullptr, n + 1, sb.islScratch, s);
+        k_isl_scatter<<<gridn(std::max(nPairs, n), 256), 256, 0, s>>>(sb, n); note_launch();
+        exclusive_scan(sb.segFlag, sb.segIdx, sb.nIslChunks, n, sb.islScratch, s);
+        k_isl_segments<<<gridn(n, 256), 256, 0, s>>>(sb, n); note_launch();
+    }
     if (prof) { prof->mark(PH_COLOUR, 1, s); prof->mark(PH_SETUP, 0, s); }
     k_setup<<<gridn(nPairs, 128), 128, 0, s>>>(w, P, R, sb.nCand, dt); note_launch();
+    if (learn.sampleX) {
+        k_contact_features<<<std::min(gridn(nPairs * 4, 256), 4096), 256, 0, s>>>(w, P, R, sb.nCand, learn.sampleX);
+        note_launch();
+    }
+    if (learn.mlp) {
+        int tiles = std::min(gridn(nPairs * 4, MLP_TILE), 2048);
+        k_mlp_warmstart<<<tiles, MLP_THREADS, mlp_smem_bytes(), s>>>(w, P, R, sb.nCand, *learn.mlp);
+        note_launch();
+    }
     if (prof) { prof->mark(PH_SETUP, 1, s); prof->mark(PH_PGS, 0, s); }
     cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
     {
@@ -917,6 +1145,10 @@ void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, Solver
         cudaLaunchCooperativeKernel((void*)k_pgs, sb.gridPgs, sb.threads, args, pgs_smem(sb), s); note_launch();
     }
     if (prof) prof->mark(PH_PGS, 1, s);
+    if (learn.sampleT) {
+        k_contact_targets<<<std::min(gridn(nPairs * 4, 256), 4096), 256, 0, s>>>(w, R, sb, learn.sampleT);
+        note_launch();
+    }
 }
 
 }  // namespace jbg

@@ -43,6 +43,22 @@ struct SolverBuffers {
     int* nLocal = nullptr;        // nParts
     int* partStart = nullptr;     // nParts + 1 positions of the body order
     int* orderFallback = nullptr; // body order built on the host when the broadphase order is stale
+    // residual mode: per slot maxima and island grouping (slots by island root)
+    float* md = nullptr;          // per slot: largest |delta lambda| of the iteration
+    float* ml = nullptr;          // per slot: largest |lambda|
+    int* slotIsl = nullptr;       // per slot: island root
+    int* islList = nullptr;       // slots grouped by island (pair capacity)
+    int* islCount = nullptr;      // per body index (island root): slots, nBodies + 1
+    int* islFill = nullptr;
+    int* islStart = nullptr;
+    int* segFlag = nullptr;       // per body index: chunks of the island's slots
+    int* segIdx = nullptr;        // first chunk of the island
+    int2* islChunk = nullptr;     // (island root, chunk) for every chunk; capacity pairs + bodies
+    int* islConv = nullptr;       // per island root: converged this solve
+    int* islAcc = nullptr;        // per island root: chunk maxima (float bits), 2 per island
+    int* islDone = nullptr;       // per island root: chunks reduced this iteration
+    int* nIslChunks = nullptr;    // device scalar
+    void* islScratch = nullptr;   // scan scratch for nBodies + 1
     const int* order = nullptr;   // body order in use
     int nFinite = 0;
     int nParts = 0;
@@ -65,5 +81,17 @@ void islands_launch_select(const DevWorld& w, const DevPairs& P, int nPairs, Sol
 void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& rows, SolverBuffers& sb, float dt, cudaStream_t s,
                   const Prof* prof = nullptr);
 void solver_free(SolverBuffers& sb);
+
+// Learned warm start and contact samples (solver.cu): per contact point q = slot * 4 + point,
+// 24 features (X) before the solve and the 3 converged impulses (T) after it.
+struct MlpDev;
+struct SolverLearn {
+    const MlpDev* mlp = nullptr;    // non-null: warm-start impulses predicted by the MLP
+    float* sampleX = nullptr;       // non-null: features written (capacity rows * 4 * 24)
+    float* sampleT = nullptr;       // non-null: converged impulses written (rows * 4 * 3)
+};
+int solver_learn_configure();     // once per world: shared-memory size of the warm-start kernel
+void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& rows, SolverBuffers& sb, float dt,
+                        cudaStream_t s, const Prof* prof, const SolverLearn& learn);
 
 }  // namespace jbg

@@ -16,6 +16,7 @@
 #include "../../include/jbgpu.h"
 #include "broadphase.cuh"
 #include "jbgpu_internal.cuh"
+#include "mlp.cuh"
 #include "narrowphase.cuh"
 #include "prims.cuh"
 #include "solver.cuh"
@@ -24,6 +25,9 @@ using namespace jbg;
 
 static thread_local std::string g_err;
 static int fail(int code, const std::string& msg) { g_err = msg; return code; }
+namespace jbg {
+int set_last_error(int code, const char* msg) { return fail(code, msg); }
+}
 
 #include <atomic>
 static std::atomic<long long> g_launches{0};
@@ -107,6 +111,13 @@ struct jbgpu_world {
     int* profHist = nullptr;      // per profiled step: device counters + solver manifolds
     float* ioStage = nullptr;     // device staging for apply_forces / get_transforms (12 floats per body)
     int capIo = 0;
+    // learned warm start and training samples
+    jbgpu_mlp* mlp = nullptr;     // not owned
+    bool learnReady = false;      // warm-start kernel configured
+    bool logSamples = false;
+    float* sampleX = nullptr;     // capRows * 4 * 24
+    float* sampleT = nullptr;     // capRows * 4 * 3
+    int sampleCap = 0;            // rows the sample buffers hold
 };
 
 namespace {
@@ -142,8 +153,11 @@ int alloc_pair_work(jbgpu_world* w, int cap) {
     CK(dalloc(&R.slot_pair, cap)); CK(dalloc(&R.slot_desc, cap)); CK(dalloc(&R.slot_im, cap));
     SolverBuffers& S = w->sb;
     dfree(S.flag); dfree(S.candIdx); dfree(S.cand); dfree(S.colourOf); dfree(S.bucket); dfree(S.bucketList);
+    dfree(S.md); dfree(S.ml); dfree(S.slotIsl); dfree(S.islList); dfree(S.islChunk);
     CK(dalloc(&S.flag, cap)); CK(dalloc(&S.candIdx, cap)); CK(dalloc(&S.cand, cap)); CK(dalloc(&S.colourOf, cap));
     CK(dalloc(&S.bucket, cap)); CK(dalloc(&S.bucketList, cap));
+    CK(dalloc(&S.md, cap)); CK(dalloc(&S.ml, cap)); CK(dalloc(&S.slotIsl, cap)); CK(dalloc(&S.islList, cap));
+    CK(dalloc(&S.islChunk, (size_t)cap + std::max(w->capBodies, 1)));
     if (S.scanScratch) cudaFree(S.scanScratch);
     CK(cudaMalloc(&S.scanScratch, scan_scratch_bytes(cap)));
     if (w->nb.queue) cudaFree(w->nb.queue);
@@ -182,8 +196,15 @@ int grow_bodies(jbgpu_world* w, int need) {
     CK(cudaMalloc(&B.scanScratch, scan_scratch_bytes(nc + 1)));
     SolverBuffers& S = w->sb;
     dfree(S.parent); dfree(S.keepAwake); dfree(S.inactive); dfree(S.claim); dfree(S.taken); dfree(S.posOf);
+    dfree(S.islCount); dfree(S.islFill); dfree(S.islStart); dfree(S.segFlag); dfree(S.segIdx);
+    dfree(S.islConv); dfree(S.islAcc); dfree(S.islDone);
     CK(dalloc(&S.parent, nc)); CK(dalloc(&S.keepAwake, nc)); CK(dalloc(&S.inactive, nc)); CK(dalloc(&S.claim, nc));
     CK(dalloc(&S.taken, nc)); CK(dalloc(&S.posOf, nc));
+    CK(dalloc(&S.islCount, nc + 1)); CK(dalloc(&S.islFill, nc + 1)); CK(dalloc(&S.islStart, nc + 1));
+    CK(dalloc(&S.segFlag, nc + 1)); CK(dalloc(&S.segIdx, nc + 1)); CK(dalloc(&S.islConv, nc));
+    CK(dalloc(&S.islAcc, 2 * (size_t)nc)); CK(dalloc(&S.islDone, nc));
+    if (S.islScratch) cudaFree(S.islScratch);
+    CK(cudaMalloc(&S.islScratch, scan_scratch_bytes(nc + 1)));
     w->capBodies = nc;
     return JBGPU_OK;
 }
@@ -377,7 +398,25 @@ int run_stage(jbgpu_world* w, int stage, float dt) {
         int rc = prepare_solver(w);
         if (rc) return rc;
         CK(cudaMemsetAsync(w->dw.ctr + C_ROWS, 0, sizeof(int), s));
-        solve_launch(d, w->pairs[w->cur], w->nPairs, w->rows, w->sb, dt, s, &P);
+        SolverLearn learn;
+        MlpDev md;
+        if (w->mlp) {
+            md = mlp_view(w->mlp);
+            learn.mlp = &md;
+        }
+        if (w->logSamples) {
+            if (w->sampleCap < w->capRows) {
+                dfree(w->sampleX);
+                dfree(w->sampleT);
+                w->sampleCap = 0;
+                CK(dalloc(&w->sampleX, (size_t)w->capRows * 4 * JBGPU_MLP_INPUTS));
+                CK(dalloc(&w->sampleT, (size_t)w->capRows * 4 * JBGPU_MLP_OUTPUTS));
+                w->sampleCap = w->capRows;
+            }
+            learn.sampleX = w->sampleX;
+            learn.sampleT = w->sampleT;
+        }
+        solve_launch_learn(d, w->pairs[w->cur], w->nPairs, w->rows, w->sb, dt, s, &P, learn);
         break;
     }
     case JBGPU_STAGE_INTEGRATE: P.mark(PH_INTEGRATE, 0, s); launch_integrate(d, dt, s); P.mark(PH_INTEGRATE, 1, s); break;
@@ -603,6 +642,7 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
     if ((rc = [&]() -> int {
              CK(dalloc(&S.colourCount, MAX_COLOURS + 1)); CK(dalloc(&S.colourFill, MAX_COLOURS + 1));
              CK(dalloc(&S.colourStart, MAX_COLOURS + 1)); CK(dalloc(&S.nCand, 1)); CK(dalloc(&S.nColours, 1));
+             CK(dalloc(&S.nIslChunks, 1));
              CK(cudaMemset(S.nCand, 0, sizeof(int))); CK(cudaMemset(S.nColours, 0, sizeof(int)));
              NarrowBuffers& N = w->nb;
              N.slots = w->sms * 2;
@@ -650,6 +690,10 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     SolverBuffers& V = w->sb;
     dfree(V.parent); dfree(V.keepAwake); dfree(V.inactive); dfree(V.flag); dfree(V.candIdx); dfree(V.cand); dfree(V.colourOf);
     dfree(V.bucket); dfree(V.bucketList); dfree(V.claim); dfree(V.taken); dfree(V.posOf);
+    dfree(V.md); dfree(V.ml); dfree(V.slotIsl); dfree(V.islList); dfree(V.islCount); dfree(V.islFill); dfree(V.islStart);
+    dfree(V.segFlag); dfree(V.segIdx); dfree(V.islChunk); dfree(V.islConv); dfree(V.islAcc); dfree(V.islDone);
+    dfree(V.nIslChunks);
+    if (V.islScratch) cudaFree(V.islScratch);
     dfree(V.colourCount); dfree(V.colourFill); dfree(V.colourStart);
     solver_free(V);
     dfree(V.nCand); dfree(V.nColours);
@@ -658,6 +702,8 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     free_prof(w->prof);
     if (w->profHist) cudaFree(w->profHist);
     if (w->ioStage) cudaFree(w->ioStage);
+    dfree(w->sampleX);
+    dfree(w->sampleT);
     if (w->evFork) cudaEventDestroy(w->evFork);
     if (w->evJoin) cudaEventDestroy(w->evJoin);
     if (w->aux) cudaStreamDestroy(w->aux);
@@ -876,6 +922,70 @@ int jbgpu_world_narrowphase_static(jbgpu_world* w, int32_t epa_slots) {
     narrowphase_launch_static(dev_view(w), w->pairs[w->cur], w->nPairs, w->nb, base, epa_slots, s);
     CK(cudaGetLastError());
     return check_status(w);
+}
+
+int jbgpu_world_set_solver_iterations(jbgpu_world* w, int32_t num_iterations, float residual, int32_t max_iterations) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (num_iterations < 0 || max_iterations < 0 || !(residual >= 0.0f))
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "negative iteration count or residual");
+    CK(cudaSetDevice(w->device));
+    CK(cudaStreamSynchronize(w->stream));
+    w->cfg.num_iterations = num_iterations;
+    w->cfg.solver_residual = residual;
+    w->cfg.solver_max_iterations = max_iterations;
+    w->dw.numIter = num_iterations;
+    w->dw.resTol = residual;
+    w->dw.maxIter = max_iterations > 0 ? max_iterations : 200;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_warmstart_mlp(jbgpu_world* w, jbgpu_mlp* mlp) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    CK(cudaSetDevice(w->device));
+    if (mlp && !w->learnReady) {
+        if (solver_learn_configure()) return fail(JBGPU_ERR_CUDA, "warm-start kernel shared-memory size");
+        w->learnReady = true;
+    }
+    CK(cudaStreamSynchronize(w->stream));
+    w->mlp = mlp;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_sample_logging(jbgpu_world* w, int32_t on) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    w->logSamples = on != 0;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_get_samples(jbgpu_world* w, float* x, float* t, int32_t capacity, int32_t* n) {
+    if (!w || !n) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    *n = 0;
+    if (!w->logSamples || !w->sampleX) return JBGPU_OK;
+    CK(cudaSetDevice(w->device));
+    cudaStream_t s = w->stream;
+    int nc = 0;
+    CK(cudaMemcpyAsync(&nc, w->sb.nCand, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (nc <= 0) return JBGPU_OK;
+    std::vector<int4> desc(nc);
+    std::vector<float> X((size_t)nc * 4 * JBGPU_MLP_INPUTS), T((size_t)nc * 4 * JBGPU_MLP_OUTPUTS);
+    CK(cudaMemcpyAsync(desc.data(), w->rows.slot_desc, sizeof(int4) * nc, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(X.data(), w->sampleX, sizeof(float) * X.size(), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(T.data(), w->sampleT, sizeof(float) * T.size(), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    int cnt = 0;
+    for (int q = 0; q < nc * 4; q++) {
+        if (!(desc[q >> 2].z & (1 << (q & 3)))) continue;
+        if (std::isnan(T[(size_t)q * JBGPU_MLP_OUTPUTS])) continue;   // island not converged
+        if (cnt < capacity && x && t) {
+            std::memcpy(x + (size_t)cnt * JBGPU_MLP_INPUTS, &X[(size_t)q * JBGPU_MLP_INPUTS], sizeof(float) * JBGPU_MLP_INPUTS);
+            std::memcpy(t + (size_t)cnt * JBGPU_MLP_OUTPUTS, &T[(size_t)q * JBGPU_MLP_OUTPUTS], sizeof(float) * JBGPU_MLP_OUTPUTS);
+        }
+        cnt++;
+    }
+    *n = cnt;
+    if (cnt > capacity && x && t) return fail(JBGPU_ERR_CAPACITY, "sample buffer too small");
+    return JBGPU_OK;
 }
 
 int jbgpu_world_synchronize(jbgpu_world* w) {
@@ -1146,6 +1256,9 @@ int jbgpu_world_counters(jbgpu_world* w, jbgpu_counters* c) {
     c->solver_iterations = h[C_PGS_ITERS];
     c->cut_colours = h[C_CUT_COLOURS];
     c->cut_manifolds = h[C_CUT_MANIFOLDS];
+    c->solver_islands = h[C_ISL_N];
+    c->solver_islands_converged = h[C_ISL_CONV];
+    c->solver_island_iterations = h[C_ISL_ITERS];
     return JBGPU_OK;
 }
 
@@ -1246,6 +1359,9 @@ int jbgpu_world_profile_counters(jbgpu_world* w, jbgpu_counters* out, int32_t ca
         o.solver_iterations = c[C_PGS_ITERS];
         o.cut_colours = c[C_CUT_COLOURS];
         o.cut_manifolds = c[C_CUT_MANIFOLDS];
+        o.solver_islands = c[C_ISL_N];
+        o.solver_islands_converged = c[C_ISL_CONV];
+        o.solver_island_iterations = c[C_ISL_ITERS];
     }
     return JBGPU_OK;
 }

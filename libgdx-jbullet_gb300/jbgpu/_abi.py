@@ -171,7 +171,9 @@ class Counters(C.Structure):
         ("solver_iterations", C.c_int32),
         ("cut_colours", C.c_int32),
         ("cut_manifolds", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("solver_islands", C.c_int32),
+        ("solver_islands_converged", C.c_int32),
+        ("solver_island_iterations", C.c_int32),
     ]
 
     def as_dict(self):

@@ -57,6 +57,19 @@ def lib():
             "jbgpu_world_set_profiling": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_phase_times": ([C.c_void_p, P(C.c_double), C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_profile_counters": ([C.c_void_p, P(_abi.Counters), C.c_int32, _abi.i32p], C.c_int),
+            "jbgpu_world_narrowphase_static": ([C.c_void_p, C.c_int32], C.c_int),
+            "jbgpu_mlp_create": ([C.c_int32, C.c_uint64, P(C.c_void_p)], C.c_int),
+            "jbgpu_mlp_destroy": ([C.c_void_p], C.c_int),
+            "jbgpu_mlp_get_params": ([C.c_void_p, _abi.f32p, _abi.f32p], C.c_int),
+            "jbgpu_mlp_set_params": ([C.c_void_p, _abi.f32p, _abi.f32p], C.c_int),
+            "jbgpu_mlp_forward": ([C.c_void_p, _abi.f32p, C.c_int32, _abi.f32p], C.c_int),
+            "jbgpu_mlp_gradients": ([C.c_void_p, _abi.f32p, _abi.f32p, C.c_int32, _abi.f32p, _abi.f32p], C.c_int),
+            "jbgpu_mlp_load_samples": ([C.c_void_p, _abi.f32p, _abi.f32p, C.c_int32], C.c_int),
+            "jbgpu_mlp_train": ([C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_uint64, _abi.f32p], C.c_int),
+            "jbgpu_world_set_warmstart_mlp": ([C.c_void_p, C.c_void_p], C.c_int),
+            "jbgpu_world_set_solver_iterations": ([C.c_void_p, C.c_int32, C.c_float, C.c_int32], C.c_int),
+            "jbgpu_world_set_sample_logging": ([C.c_void_p, C.c_int32], C.c_int),
+            "jbgpu_world_get_samples": ([C.c_void_p, _abi.f32p, _abi.f32p, C.c_int32, _abi.i32p], C.c_int),
         }
         for name, (args, res) in sigs.items():
             f = getattr(L, name)
@@ -79,6 +92,68 @@ EXPORTED = [
 
 def launch_count():
     return lib().jbgpu_launch_count()
+
+
+MLP_INPUTS, MLP_OUTPUTS, MLP_PARAMS, MLP_NORM = 24, 3, 5955, 55
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, np.float32)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class Mlp:
+    """The warm-start MLP (jbgpu_mlp_*): 24 -> 64 -> 64 -> 3 on the device's tensor cores."""
+
+    def __init__(self, device=0, seed=0):
+        h = C.c_void_p()
+        check(lib().jbgpu_mlp_create(device, seed, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().jbgpu_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        p = np.zeros(MLP_PARAMS, np.float32)
+        nrm = np.zeros(MLP_NORM, np.float32)
+        check(lib().jbgpu_mlp_get_params(self.h, _abi._ptr(p, _abi.f32p), _abi._ptr(nrm, _abi.f32p)))
+        return p, nrm
+
+    def set_params(self, params=None, norm=None):
+        p = None if params is None else _f32(params, (MLP_PARAMS,))
+        n = None if norm is None else _f32(norm, (MLP_NORM,))
+        check(lib().jbgpu_mlp_set_params(self.h, _abi._ptr(p, _abi.f32p), _abi._ptr(n, _abi.f32p)))
+
+    def forward(self, x):
+        x = _f32(x)
+        y = np.zeros((len(x), MLP_OUTPUTS), np.float32)
+        check(lib().jbgpu_mlp_forward(self.h, _abi._ptr(x, _abi.f32p), len(x), _abi._ptr(y, _abi.f32p)))
+        return y
+
+    def gradients(self, x, t):
+        x, t = _f32(x), _f32(t)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        check(lib().jbgpu_mlp_gradients(self.h, _abi._ptr(x, _abi.f32p), _abi._ptr(t, _abi.f32p), len(x),
+                                        _abi._ptr(g, _abi.f32p), _abi._ptr(loss, _abi.f32p)))
+        return g, float(loss[0])
+
+    def train(self, x, t, epochs, batch=1024, lr=1e-3, seed=0):
+        x, t = _f32(x), _f32(t)
+        check(lib().jbgpu_mlp_load_samples(self.h, _abi._ptr(x, _abi.f32p), _abi._ptr(t, _abi.f32p), len(x)))
+        losses = np.zeros(epochs, np.float32)
+        check(lib().jbgpu_mlp_train(self.h, epochs, batch, lr, seed, _abi._ptr(losses, _abi.f32p)))
+        return losses
 
 PHASES = ["predict", "aabb", "pair_count", "pair_fill", "narrow_gjk", "narrow_epa", "islands", "colour", "setup", "pgs",
           "integrate", "activation", "gravity"]
@@ -172,6 +247,25 @@ class GpuWorld:
         out = np.zeros(max(1, n.value), np.int32)
         check(lib().jbgpu_world_get_solver_order(self.h, out.ctypes.data_as(_abi.i32p), len(out), C.byref(n)))
         return out[:n.value]
+
+    def set_solver_iterations(self, num_iterations, residual=0.0, max_iterations=0):
+        check(lib().jbgpu_world_set_solver_iterations(self.h, num_iterations, residual, max_iterations))
+
+    def set_warmstart_mlp(self, mlp):
+        self._mlp = mlp
+        check(lib().jbgpu_world_set_warmstart_mlp(self.h, mlp.h if mlp is not None else None))
+
+    def set_sample_logging(self, on=True):
+        check(lib().jbgpu_world_set_sample_logging(self.h, 1 if on else 0))
+
+    def get_samples(self):
+        n = C.c_int32()
+        check(lib().jbgpu_world_get_samples(self.h, None, None, 0, C.byref(n)))
+        x = np.zeros((max(1, n.value), MLP_INPUTS), np.float32)
+        t = np.zeros((max(1, n.value), MLP_OUTPUTS), np.float32)
+        check(lib().jbgpu_world_get_samples(self.h, _abi._ptr(x, _abi.f32p), _abi._ptr(t, _abi.f32p), len(x),
+                                            C.byref(n)))
+        return x[:n.value], t[:n.value]
 
     def counters(self):
         c = _abi.Counters()

@@ -346,6 +346,43 @@ def small_mixed(n=60, seed=0, region=(6.0, 8.0, 6.0), steps=200, with_hulls=True
                  shapes, bodies, meta={"seed": seed})
 
 
+def learned_warmstart(n=100_000, seed=0, pyramids=50, levels=15, region=(200.0, 100.0, 200.0), steps=600):
+    """The learned-warm-start workload: the 100k mixed bodies plus `pyramids` 2-D pyramids of
+    `levels` levels of unit boxes (half-extent 0.5, mass 1, 120 boxes for 15 levels) standing on
+    the plane at seeded, non-overlapping places inside the region (a solver-hard case)."""
+    base = mixed_100k(n, seed=seed, region=region, steps=steps) if n > 0 else None
+    rng = np.random.Generator(np.random.PCG64(seed + 7919))
+    per = levels * (levels + 1) // 2
+    shapes = list(base.shapes) if base is not None else [dict(PLANE)]
+    box_id = len(shapes)
+    shapes.append({"type": _abi.SHAPE_BOX, "params": (0.5, 0.5, 0.5, 0.0), "points": None})
+    b = _bodies(pyramids * per)
+    b["shape"] = box_id
+    b["mass"] = 1.0
+    b["local_inertia"] = box_inertia(F(1.0), (0.5, 0.5, 0.5))
+    centres = []
+    span = float(levels) + 2.0
+    while len(centres) < pyramids:
+        c = rng.uniform(-region[0] / 2 + span, region[0] / 2 - span, 2)
+        if all(abs(c[0] - d[0]) > span or abs(c[1] - d[1]) > 3.0 for d in centres):
+            centres.append(c)
+    pos = []
+    for c in centres:
+        for lv in range(levels):
+            for k in range(levels - lv):
+                pos.append((c[0] + (k - (levels - lv - 1) / 2.0), 0.5 + lv, c[1]))
+    b["transform"][:, 9:] = np.array(pos, F)
+    if base is None:
+        bodies = np.concatenate([_plane_body(0), b])
+        cfg = {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10}
+        dt = 1.0 / 120.0
+    else:
+        bodies = np.concatenate([base.bodies, b])
+        cfg, dt = base.config, base.dt
+    return Scene("learned_warmstart_%d_%dx%d" % (n, pyramids, levels), dt, steps, cfg, shapes, bodies,
+                 meta={"seed": seed, "pyramid_bodies": pyramids * per})
+
+
 SCENES = {
     "boxes_1k": boxes_on_plane,
     "mixed_100k": mixed_100k,
@@ -353,4 +390,5 @@ SCENES = {
     "batched_4096": batched_worlds,
     "box_stack": box_stack,
     "small_mixed": small_mixed,
+    "learned_warmstart": learned_warmstart,
 }

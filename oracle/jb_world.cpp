@@ -479,14 +479,17 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
     }
     w.counters.solverRows += (int)rows.size();
     // solveGroupCacheFriendlyIterations (java:788-890), split impulse off.  With a residual
-    // tolerance the iterations of a world stop once max|delta lambda| / max(max|lambda|, 1e-6)
-    // over its rows is within it (the GPU's residual-terminated mode); rows of converged worlds
-    // are skipped.
+    // tolerance the iterations of an island (the group a reference solveGroup call receives)
+    // stop once max|delta lambda| / max(max|lambda|, 1e-6) over its rows is within it (the
+    // GPU's residual-terminated mode); rows of converged islands are skipped.
     const bool byResidual = cfg.residualTol > 0.0f;
     const int maxIt = byResidual ? cfg.maxIterations : cfg.numIterations;
+    auto world_of = [&](const Row& c) {   // island of the row (the dynamic body's island)
+        const Manifold& m = w.pairMf[c.mfPair];
+        return w.bodies[m.body0].islandTag >= 0 ? w.bodies[m.body0].islandTag : w.bodies[m.body1].islandTag;
+    };
     int nWorlds = 1;
-    for (const Row& c : rows) nWorlds = std::max(nWorlds, w.bodies[w.pairMf[c.mfPair].body0].world + 1);
-    auto world_of = [&](const Row& c) { return w.bodies[w.pairMf[c.mfPair].body0].world; };
+    for (const Row& c : rows) nWorlds = std::max(nWorlds, world_of(c) + 1);
     std::vector<uint8_t> converged(nWorlds, 1);      // worlds without rows take no iteration
     for (const Row& c : rows) converged[world_of(c)] = 0;
     std::vector<float> dmax(nWorlds), lmax(nWorlds);
