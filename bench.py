@@ -53,6 +53,9 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--solver-parts", type=int, default=0, help="jbgpu_config.solver_parts (0: automatic)")
     p.add_argument("--solver-threads", type=int, default=0, help="jbgpu_config.solver_threads (0: 256)")
+    p.add_argument("--solver-smem-bodies", type=int, default=0, help="jbgpu_config.solver_smem_bodies (0: 2048)")
+    p.add_argument("--autotune", action="store_true", help="choose the solver knobs with jbgpu.autotune first")
+    p.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start comparison")
     return p.parse_args()
 
 
@@ -227,6 +230,13 @@ def run_ours(args, dist):
     cfg.device = dist.local
     cfg.solver_parts = args.solver_parts
     cfg.solver_threads = args.solver_threads
+    cfg.solver_smem_bodies = args.solver_smem_bodies
+    tuned = None
+    if args.autotune:
+        from jbgpu import autotune
+        tuned = autotune.tune(sc, device=dist.local)
+        for k, v in tuned["best"].items():
+            setattr(cfg, k, v)
     iters = cfg.num_iterations
     n = sc.n_bodies
     K, W = args.steps, args.warmup
@@ -307,6 +317,15 @@ def run_ours(args, dist):
         total = W + K
         snaps = [0, total // 2, max(0, total - args.cpu_window)]
         cpu = run_cpu_baseline(sc, GpuWorld, snaps, args.cpu_window)
+    # ---- learned warm start vs the reference warm start at residual 1e-4 (rank 0) -----------
+    learned = None
+    if dist.rank == 0 and not args.no_learned:
+        from jbgpu import warmstart
+        if os.path.exists(warmstart.WEIGHTS):
+            m = warmstart.load(device=dist.local)
+            learned = warmstart.evaluate(m, seed=args.seed + 10, settle=900, steps=10)
+            learned["weights"] = "jbgpu/warmstart_weights.npz (trained by python -m jbgpu.warmstart train)"
+            m.close()
     last = ctrs[-1] if ctrs else final
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.size, "steps": K, "warmup": W,
@@ -323,8 +342,10 @@ def run_ours(args, dist):
         "roofline": roof,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "learned_warmstart": learned,
         "clocks": clocks,
         "status_flags": final["status_flags"],
+        "autotune": tuned,
     }
     return out
 

@@ -128,7 +128,10 @@ typedef struct jbgpu_config {
                                            max|lambda_k - lambda_k-1| / max(max|lambda_k|, 1e-6) is
                                            <= this value, at most solver_max_iterations. */
     int32_t solver_max_iterations;      /* cap for solver_residual > 0; 0 means 200 */
-    int32_t reserved[4];
+    int32_t solver_smem_bodies;         /* solver parts of at most this many bodies keep their
+                                           velocities in shared memory (0: 2048).  No counterpart
+                                           in the reference; a tuning knob. */
+    int32_t reserved[3];
 } jbgpu_config;
 
 typedef struct jbgpu_shape_desc {

@@ -17,7 +17,7 @@ enum {
     C_PAIRS = 0, C_FILL_OVERFLOW, C_EPA_QUEUE, C_GJK, C_EPA, C_SOLVE_N, C_COLOURS, C_ISLANDS,
     C_MANIFOLDS, C_CONTACTS, C_ROWS, C_STATUS, C_BAR_COUNT, C_BAR_GEN, C_CUT_DONE, C_WIN0, C_WIN1, C_WIN2,
     C_PGS_ITERS, C_CUT_COLOURS, C_CUT_MANIFOLDS, C_RES0, C_RES1, C_RES2, C_ISL_N, C_ISL_CONV, C_ISL_ITERS,
-    C_NCTR = 32
+    C_PART_NEXT0, C_PART_NEXT1, C_NCTR = 32
 };
 
 struct DevShapes {

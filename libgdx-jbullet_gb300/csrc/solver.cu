@@ -247,6 +247,16 @@ __global__ void k_bucket_scatter(SolverBuffers sb) {
     sb.bucketList[sb.bucketStart[b] + atomicAdd(&sb.bucketFill[b], 1)] = k;
 }
 
+// Blocks take parts largest first from a shared counter (ctr[counter], cleared before the
+// launch), so that one large part does not leave the other blocks idle at the end.
+JBD int next_part(const DevWorld& w, const SolverBuffers& sb, int counter, int* sh) {
+    __syncthreads();
+    if (threadIdx.x == 0) *sh = atomicAdd(&w.ctr[counter], 1);
+    __syncthreads();
+    const int k = *sh;
+    return k < sb.nParts ? sb.partOrder[k] : -1;
+}
+
 // ---- colouring (cooperative) ---------------------------------------------------------------
 // Each colour is grown to a maximal set by claim passes: every dynamic body is claimed by the
 // lowest candidate index touching it among the eligible candidates (uncoloured, no dynamic body
@@ -274,14 +284,14 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
     const int nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int nCand = *sb.nCand;
-    __shared__ int shWin, shDone;
+    __shared__ int shWin, shDone, shPart;
     for (int k = tid; k < nCand; k += nth) sb.colourOf[k] = -1;
     for (int c = tid; c < sb.nParts * (MAX_LOCAL + 1); c += nth) sb.lcCount[c] = 0;
     for (int c = tid; c <= MAX_COLOURS; c += nth) sb.colourCount[c] = 0;
     if (tid == 0) { w.ctr[C_CUT_DONE] = 0; w.ctr[C_WIN0] = w.ctr[C_WIN1] = w.ctr[C_WIN2] = 0; }
     grid_barrier(w.ctr, nb);
-    // manifolds internal to the parts of this block
-    for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
+    // manifolds internal to the parts this block takes
+    for (int part = next_part(w, sb, C_PART_NEXT0, &shPart); part >= 0; part = next_part(w, sb, C_PART_NEXT0, &shPart)) {
         const int s0 = sb.bucketStart[part], s1 = sb.bucketStart[part + 1];
         int* lc = sb.lcCount + part * (MAX_LOCAL + 1);
         if (threadIdx.x == 0) shDone = 0;
@@ -397,7 +407,7 @@ __global__ void k_slots(DevWorld w, DevPairs P, SolverBuffers sb, DevRows R) {
     R.slot_pair[slot] = p;
     int b0 = P.b0[p], b1 = P.b1[p];
     int lb0 = 0xffff, lb1 = 0xffff;
-    if (b < sb.nParts && sb.partSmem) {
+    if (b < sb.nParts && sb.partSmem && sb.partStart[b + 1] - sb.partStart[b] <= sb.smemCap) {
         int ps = sb.partStart[b];
         if (dyn(w, b0)) lb0 = sb.posOf[b0] - ps;
         if (dyn(w, b1)) lb1 = sb.posOf[b1] - ps;
@@ -527,6 +537,7 @@ struct Resid {
 
 // The rows of one manifold for one phase, on velocities held in registers.  Warm start applies
 // per point the normal, then both friction impulses (setup order, java:680-760).
+template <bool TRACK>
 JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int mask, int kind, V& l0, V& a0, V& l1, V& a1,
                         float im0, float im1, Resid& res) {
     for (int j = 0; j < 4; j++) {
@@ -563,14 +574,16 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int mask, in
             apply_imp(l1, a1, n, im1, mk(aB.x, aB.y, aB.z), -d);
             aB.w = acc;
             __stcg(&R.n_angB[ni], aB);
-            res.add(d, acc);
+            if (TRACK) res.add(d, acc);
         } else {                          // resolveSingleFrictionCacheFriendly (java:286-346)
             float total = __fadd_rn(__ldcg(&R.n_angB[ni]).w, 0.0f);   // appliedImpulse + appliedPushImpulse
             float fric = R.n_angA[ni].w;
             float limit = __fmul_rn(total, fric);
             if (!(total > 0.0f)) {
-                res.add(0.0f, __ldcg(&R.f_rp1[ni * 2]).w);
-                res.add(0.0f, __ldcg(&R.f_rp1[ni * 2 + 1]).w);
+                if (TRACK) {
+                    res.add(0.0f, __ldcg(&R.f_rp1[ni * 2]).w);
+                    res.add(0.0f, __ldcg(&R.f_rp1[ni * 2 + 1]).w);
+                }
                 continue;
             }
             for (int f = 0; f < 2; f++) {
@@ -592,7 +605,7 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int mask, in
                 apply_imp(l1, a1, n, im1, mk4(R.f_angB[fi]), -j1);
                 r1.w = acc;
                 __stcg(&R.f_rp1[fi], r1);
-                res.add(j1, acc);
+                if (TRACK) res.add(j1, acc);
             }
         }
     }
@@ -690,7 +703,8 @@ JBD void local_colour(const DevWorld& w, const DevRows& R, const SolverBuffers& 
         if (m0) { l0 = mk4(sl[lb0]); a0 = mk4(sa[lb0]); } else gload(w, d.x, l0, a0);
         if (m1) { l1 = mk4(sl[lb1]); a1 = mk4(sa[lb1]); } else gload(w, d.y, l1, a1);
         Resid res;
-        solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
+        if (rc.on) solve_manifold<true>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
+        else solve_manifold<false>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
         res_keep(sb, rc, kind, s, res);
         if (im.x != 0.0f) { if (m0) { sl[lb0] = f4(l0, 0.0f); sa[lb0] = f4(a0, 0.0f); } else gstore(w, d.x, l0, a0); }
         if (im.y != 0.0f) { if (m1) { sl[lb1] = f4(l1, 0.0f); sa[lb1] = f4(a1, 0.0f); } else gstore(w, d.y, l1, a1); }
@@ -758,34 +772,36 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
     const int nSlots = *sb.nCand;
     const bool smem = sb.partSmem != 0;
     float4* sl = smv;
-    float4* sa = smv + sb.partMax;
+    float4* sa = smv + sb.smemCap;
     const bool byRes = w.resTol > 0.0f;
     const int maxIt = byRes ? w.maxIter : w.numIter;
     ResCtl rc;
     rc.on = byRes;
     if (nCut == 0 && !byRes) {
+        __shared__ int shPart;
         int itMax = 0;
-        for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
+        for (int part = next_part(w, sb, C_PART_NEXT1, &shPart); part >= 0; part = next_part(w, sb, C_PART_NEXT1, &shPart)) {
             const PartView v = part_view(sb, part);
-            if (smem) stage_in(w, sb, v, sl, sa);
+            const bool psm = smem && v.np <= sb.smemCap;
+            if (psm) stage_in(w, sb, v, sl, sa);
             __syncthreads();
             for (int c = 0; c < v.nLoc; c++) {
-                local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_WARM, smem, sl, sa, rc);
+                local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_WARM, psm, sl, sa, rc);
                 __syncthreads();
             }
             int it = 0;
             for (; it < maxIt && v.nLoc > 0; it++) {
                 for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_NORMAL, smem, sl, sa, rc);
+                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_NORMAL, psm, sl, sa, rc);
                     __syncthreads();
                 }
                 for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_FRICTION, smem, sl, sa, rc);
+                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_FRICTION, psm, sl, sa, rc);
                     __syncthreads();
                 }
             }
             if (it > itMax) itMax = it;
-            if (smem) stage_out(w, sb, v, sl, sa);
+            if (psm) stage_out(w, sb, v, sl, sa);
             for (int s = sb.bucketStart[part] + threadIdx.x; s < sb.bucketStart[part + 1]; s += blockDim.x)
                 writeback_slot(P, R, s);
             __syncthreads();
@@ -801,13 +817,14 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             const int kind = it < 0 ? PH_WARM : (sub == 0 ? PH_NORMAL : PH_FRICTION);
             for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
                 const PartView v = part_view(sb, part);
-                if (smem) stage_in(w, sb, v, sl, sa);
+                const bool psm = smem && v.np <= sb.smemCap;
+                if (psm) stage_in(w, sb, v, sl, sa);
                 __syncthreads();
                 for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, smem, sl, sa, rc);
+                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc);
                     __syncthreads();
                 }
-                if (smem) stage_out(w, sb, v, sl, sa);
+                if (psm) stage_out(w, sb, v, sl, sa);
                 __syncthreads();
             }
             grid_barrier(w.ctr, nb);
@@ -821,7 +838,8 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                     gload(w, d.x, l0, a0);
                     gload(w, d.y, l1, a1);
                     Resid res;
-                    solve_manifold(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
+                    if (rc.on) solve_manifold<true>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
+                    else solve_manifold<false>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
                     res_keep(sb, rc, kind, s, res);
                     if (im.x != 0.0f) gstore(w, d.x, l0, a0);
                     if (im.y != 0.0f) gstore(w, d.y, l1, a1);
@@ -998,10 +1016,10 @@ template <class T> static cudaError_t salloc(T** p, size_t n) {
 }
 template <class T> static void sfree(T*& p) { if (p) cudaFree((void*)p); p = nullptr; }
 
-static size_t pgs_smem(const SolverBuffers& sb) { return sb.partSmem ? (size_t)sb.partMax * 32 : 0; }
+static size_t pgs_smem(const SolverBuffers& sb) { return sb.partSmem ? (size_t)sb.smemCap * 32 : 0; }
 
 int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts,
-                     int threads) {
+                     int threads, int smemBodies) {
     sb.threads = threads;
     int maxWorld = 0;
     for (int c : worldCounts) maxWorld = std::max(maxWorld, c);
@@ -1025,22 +1043,28 @@ int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& wor
     for (int p = 0; p < parts; p++) partMax = std::max(partMax, start[p + 1] - start[p]);
     if (parts > sb.partsCap) {
         sfree(sb.bucketCount); sfree(sb.bucketFill); sfree(sb.bucketStart);
-        sfree(sb.lcCount); sfree(sb.lcFill); sfree(sb.lcStart); sfree(sb.nLocal); sfree(sb.partStart);
+        sfree(sb.lcCount); sfree(sb.lcFill); sfree(sb.lcStart); sfree(sb.nLocal); sfree(sb.partStart); sfree(sb.partOrder);
         size_t lc = (size_t)parts * (MAX_LOCAL + 1);
         if (salloc(&sb.bucketCount, parts + 2) || salloc(&sb.bucketFill, parts + 2) || salloc(&sb.bucketStart, parts + 2) ||
             salloc(&sb.lcCount, lc) || salloc(&sb.lcFill, lc) || salloc(&sb.lcStart, lc) || salloc(&sb.nLocal, parts) ||
-            salloc(&sb.partStart, parts + 1)) {
+            salloc(&sb.partStart, parts + 1) || salloc(&sb.partOrder, parts)) {
             sb.partsCap = 0;
             return JBGPU_ERR_CUDA;
         }
         sb.partsCap = parts;
     }
-    if (cudaMemcpy(sb.partStart, start.data(), sizeof(int) * (parts + 1), cudaMemcpyHostToDevice) != cudaSuccess)
+    std::vector<int> order(parts);
+    for (int p = 0; p < parts; p++) order[p] = p;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return start[a + 1] - start[a] > start[b + 1] - start[b]; });
+    if (cudaMemcpy(sb.partStart, start.data(), sizeof(int) * (parts + 1), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(sb.partOrder, order.data(), sizeof(int) * parts, cudaMemcpyHostToDevice) != cudaSuccess)
         return JBGPU_ERR_CUDA;
     sb.nFinite = nFinite;
     sb.nParts = parts;
     sb.partMax = partMax;
-    sb.partSmem = (partMax < 0xffff && (size_t)partMax * 32 <= 96 * 1024) ? 1 : 0;
+    sb.smemCap = std::min(partMax, smemBodies > 0 ? smemBodies : PART_MAX_BODIES);
+    sb.partSmem = (sb.smemCap < 0xffff && (size_t)sb.smemCap * 32 <= 96 * 1024) ? 1 : 0;
     size_t smem = pgs_smem(sb);
     if (cudaFuncSetAttribute(k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) != cudaSuccess)
         return JBGPU_ERR_CUDA;
@@ -1056,7 +1080,7 @@ int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& wor
 
 void solver_free(SolverBuffers& sb) {
     sfree(sb.bucketCount); sfree(sb.bucketFill); sfree(sb.bucketStart);
-    sfree(sb.lcCount); sfree(sb.lcFill); sfree(sb.lcStart); sfree(sb.nLocal); sfree(sb.partStart);
+    sfree(sb.lcCount); sfree(sb.lcFill); sfree(sb.lcStart); sfree(sb.nLocal); sfree(sb.partStart); sfree(sb.partOrder);
     sfree(sb.orderFallback);
     sb.partsCap = 0;
 }
@@ -1096,7 +1120,7 @@ void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, 
     cudaMemsetAsync(sb.colourFill, 0, sizeof(int) * (MAX_COLOURS + 1), s);
     cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
     cudaMemsetAsync(w.ctr + C_PGS_ITERS, 0, sizeof(int), s);
-    cudaMemsetAsync(w.ctr + C_ISL_N, 0, sizeof(int) * 3, s);
+    cudaMemsetAsync(w.ctr + C_ISL_N, 0, sizeof(int) * 5, s);   // island statistics, part counters
     k_posof<<<gridn(sb.nFinite, 256), 256, 0, s>>>(sb); note_launch();
     k_classify<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, sb); note_launch();
     exclusive_scan(sb.bucketCount, sb.bucketStart, nullptr, parts + 2, sb.scanScratch, s);

@@ -42,6 +42,7 @@ struct SolverBuffers {
     int* lcStart = nullptr;
     int* nLocal = nullptr;        // nParts
     int* partStart = nullptr;     // nParts + 1 positions of the body order
+    int* partOrder = nullptr;     // parts by decreasing size (the order blocks take them in)
     int* orderFallback = nullptr; // body order built on the host when the broadphase order is stale
     // residual mode: per slot maxima and island grouping (slots by island root)
     float* md = nullptr;          // per slot: largest |delta lambda| of the iteration
@@ -65,6 +66,7 @@ struct SolverBuffers {
     int partsCap = 0;
     int partMax = 0;              // largest part, bodies
     int partSmem = 0;             // velocities of internal manifolds staged in shared memory
+    int smemCap = 0;              // parts of at most this many bodies are staged
     int worldParts = 0;
     int gridColour = 0;           // co-resident blocks of the cooperative kernels
     int gridPgs = 0;
@@ -72,9 +74,10 @@ struct SolverBuffers {
 };
 
 // (Re)plans the parts for nFinite ordered bodies.  worldCounts: finite bodies per batch world;
-// rangeParts > 0 asks for that many range parts; threads per block of the colouring and PGS.
+// rangeParts > 0 asks for that many range parts; threads per block of the colouring and PGS;
+// smemBodies > 0 caps the parts whose velocities are staged in shared memory.
 int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts,
-                     int threads);
+                     int threads, int smemBodies);
 void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
 void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
 void islands_launch_select(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);

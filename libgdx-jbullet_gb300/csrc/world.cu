@@ -355,7 +355,7 @@ int prepare_solver(jbgpu_world* w) {
     const int nf = w->bb.nFinite;
     if (w->solverDirty) {
         int rc = solver_configure(S, nf, w->worldFinite, w->sms, w->cfg.solver_parts,
-                                  w->cfg.solver_threads ? w->cfg.solver_threads : SOLVER_THREADS);
+                                  w->cfg.solver_threads ? w->cfg.solver_threads : SOLVER_THREADS, w->cfg.solver_smem_bodies);
         if (rc) return fail(rc, "solver part tables");
         w->solverDirty = false;
     }
@@ -603,6 +603,7 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
         return fail(JBGPU_ERR_UNSUPPORTED, "only the cache-friendly solver path is implemented");
     if (c.num_iterations < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "num_iterations < 0");
     if (c.solver_parts < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "solver_parts < 0");
+    if (c.solver_smem_bodies < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "solver_smem_bodies < 0");
     if (c.solver_threads != 0 && c.solver_threads != 64 && c.solver_threads != 128 && c.solver_threads != 256)
         return fail(JBGPU_ERR_INVALID_ARGUMENT, "solver_threads must be 0, 64, 128 or 256");
     int ndev = 0;

@@ -71,7 +71,8 @@ class Config(C.Structure):
         ("solver_threads", C.c_int32),
         ("solver_residual", C.c_float),
         ("solver_max_iterations", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("solver_smem_bodies", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 
