@@ -33,6 +33,7 @@ struct EpaSlot {          // one query's polytope
     float4* mR;           // support direction r
     float4* seen;         // rays fetched by SearchOrigin (the reference's 64-bucket hash, as a set)
     int2* stack;          // BuildHorizon work list
+    int faceCap, mkvCap, seenCap, stackCap;   // capacities (exceeding one sets the overflow flag)
 };
 
 struct EpaArena {
@@ -54,6 +55,10 @@ JBD EpaSlot epa_slot(const EpaArena& a, int s) {
     e.mR = a.mR + (size_t)s * EPA_MKV_CAP;
     e.seen = a.seen + (size_t)s * EPA_SEEN_CAP;
     e.stack = a.stack + (size_t)s * EPA_STACK_CAP;
+    e.faceCap = EPA_FACE_CAP;
+    e.mkvCap = EPA_MKV_CAP;
+    e.seenCap = EPA_SEEN_CAP;
+    e.stackCap = EPA_STACK_CAP;
     return e;
 }
 
@@ -126,7 +131,7 @@ JBD bool epa_fetch(EpaCtx& c) {                             // FetchSupport
     }
     if (c.nl > 1) hit = __any_sync(FULL_MASK, hit);
     if (hit) { --c.order; return false; }
-    if (c.nseen < EPA_SEEN_CAP) c.sl.seen[c.nseen++] = f4(c.ray, 0.0f);
+    if (c.nseen < c.sl.seenCap) c.sl.seen[c.nseen++] = f4(c.ray, 0.0f);
     else c.overflow = true;
     ++c.order;
     epa_support(c, c.ray, c.sw[c.order], c.sr[c.order]);
@@ -257,13 +262,13 @@ JBD void fset(int4& v, int i, int x) { if (i == 0) v.x = x; else if (i == 1) v.y
 JBD V mw(const EpaCtx& c, int i) { float4 a = c.sl.mW[i]; return mk(a.x, a.y, a.z); }
 
 JBD int epa_new_mkv(EpaCtx& c, V w, V r) {
-    if (c.nmkv >= EPA_MKV_CAP) { c.overflow = true; return c.nmkv - 1; }
+    if (c.nmkv >= c.sl.mkvCap) { c.overflow = true; return c.nmkv - 1; }
     c.sl.mW[c.nmkv] = f4(w, 0.0f);
     c.sl.mR[c.nmkv] = f4(r, 0.0f);
     return c.nmkv++;
 }
 JBD int epa_new_face(EpaCtx& c, int a, int b, int cc) {     // EPA.NewFace + EPA.Set
-    if (c.nface >= EPA_FACE_CAP) { c.overflow = true; return c.nface - 1; }
+    if (c.nface >= c.sl.faceCap) { c.overflow = true; return c.nface - 1; }
     int id = c.nface++;
     V aw = mw(c, a), bw = mw(c, b), cw = mw(c, cc);
     V nrm = crs(sub(bw, aw), sub(cw, aw));
@@ -324,7 +329,7 @@ JBD int epa_horizon(EpaCtx& c, int markid, int w, int f0, int e0, int& cf, int& 
             fv.w = markid;
             c.sl.fV[f] = fv;
             int4 F = c.sl.fF[f], E = c.sl.fE[f];
-            if (sp + 2 > EPA_STACK_CAP) { c.overflow = true; return ne; }
+            if (sp + 2 > c.sl.stackCap) { c.overflow = true; return ne; }
             c.sl.stack[sp++] = make_int2(fget(F, e2), fget(E, e2));
             c.sl.stack[sp++] = make_int2(fget(F, e1), fget(E, e1));
         }

@@ -107,8 +107,12 @@ __global__ void k_narrow(DevWorld w, DevPairs P, int nPairs, EpaRec* queue, int*
     store_mf(P, p, m);
 }
 
-// One queued pair, by the 32 lanes of a warp (see epa.cuh); lane 0 updates the manifold.
-__device__ void epa_query(const DevWorld& w, DevPairs& P, const EpaRec* queue, int qi, const EpaSlot& sl, int lane) {
+// One queued pair, by the 32 lanes of a warp (see epa.cuh); lane 0 updates the manifold.  With
+// ovfQueue (the small-slot tier) a query that outgrows its slot leaves no result and is queued
+// for the tier with the full capacities: EPA is deterministic, so its result does not depend on
+// which tier finishes it.
+__device__ void epa_query(const DevWorld& w, DevPairs& P, const EpaRec* queue, int qi, const EpaSlot& sl, int lane,
+                          int* ovfQueue = nullptr, int* ovfCount = nullptr) {
     EpaRec r = queue[qi];
     int p = r.pair;
     uint64_t key = P.keys[p];
@@ -140,6 +144,11 @@ __device__ void epa_query(const DevWorld& w, DevPairs& P, const EpaRec* queue, i
             }
         }
     }
+    if (ovf && ovfQueue) {
+        if (lane == 0) ovfQueue[atomicAdd(ovfCount, 1)] = qi;
+        __syncwarp();
+        return;
+    }
     if (lane == 0) {
         atomicAdd(&w.ctr[C_EPA], 1);
         if (ovf) atomicOr(&w.ctr[C_STATUS], ST_EPA_POOL);
@@ -170,9 +179,44 @@ constexpr size_t EPA_SMEM_BYTES = (size_t)EPA_FACE_CAP * (4 * sizeof(float4) + s
                                   (size_t)EPA_MKV_CAP * 2 * sizeof(float4) + (size_t)EPA_SEEN_CAP * sizeof(float4) +
                                   (size_t)EPA_STACK_CAP * sizeof(int2);
 
-__global__ void __launch_bounds__(32) k_narrow_epa_smem(DevWorld w, DevPairs P, const EpaRec* queue, const int* queueCount) {
+// Small-slot tier: EPA_SMALL_WARPS warps per block, each with a polytope of reduced
+// capacities in shared memory; queries that outgrow them go to the overflow queue.
+constexpr int EPA_SMALL_WARPS = 4;
+constexpr int EPA_S_FACES = 192, EPA_S_MKV = 96, EPA_S_SEEN = 64, EPA_S_STACK = 384;
+constexpr size_t EPA_SMALL_SLOT_BYTES = (size_t)EPA_S_FACES * (4 * sizeof(float4) + sizeof(float)) +
+                                        (size_t)EPA_S_MKV * 2 * sizeof(float4) + (size_t)EPA_S_SEEN * sizeof(float4) +
+                                        (size_t)EPA_S_STACK * sizeof(int2);
+constexpr size_t EPA_SMALL_SMEM_BYTES = EPA_SMALL_WARPS * EPA_SMALL_SLOT_BYTES;
+
+__global__ void __launch_bounds__(32 * EPA_SMALL_WARPS) k_narrow_epa_small(DevWorld w, DevPairs P, const EpaRec* queue,
+                                                                            const int* queueCount, int* ovfQueue,
+                                                                            int* ovfCount) {
     extern __shared__ float4 epaSmem[];
-    int n = *queueCount;
+    const int n = *queueCount;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    EpaSlot sl;
+    sl.fN = (float4*)((unsigned char*)epaSmem + warp * EPA_SMALL_SLOT_BYTES);
+    sl.fV = (int4*)(sl.fN + EPA_S_FACES);
+    sl.fF = sl.fV + EPA_S_FACES;
+    sl.fE = sl.fF + EPA_S_FACES;
+    sl.mW = (float4*)(sl.fE + EPA_S_FACES);
+    sl.mR = sl.mW + EPA_S_MKV;
+    sl.seen = sl.mR + EPA_S_MKV;
+    sl.stack = (int2*)(sl.seen + EPA_S_SEEN);
+    sl.fD = (float*)(sl.stack + EPA_S_STACK);
+    sl.faceCap = EPA_S_FACES;
+    sl.mkvCap = EPA_S_MKV;
+    sl.seenCap = EPA_S_SEEN;
+    sl.stackCap = EPA_S_STACK;
+    const int gw = blockIdx.x * EPA_SMALL_WARPS + warp, nw = gridDim.x * EPA_SMALL_WARPS;
+    for (int qi = gw; qi < n; qi += nw) epa_query(w, P, queue, qi, sl, lane, ovfQueue, ovfCount);
+}
+
+// Full-capacity tier over the queries the small tier could not finish.
+__global__ void __launch_bounds__(32) k_narrow_epa_smem(DevWorld w, DevPairs P, const EpaRec* queue, const int* list,
+                                                       const int* listCount) {
+    extern __shared__ float4 epaSmem[];
+    int n = *listCount;
     EpaSlot sl;
     sl.fN = epaSmem;
     sl.fV = (int4*)(sl.fN + EPA_FACE_CAP);
@@ -183,7 +227,11 @@ __global__ void __launch_bounds__(32) k_narrow_epa_smem(DevWorld w, DevPairs P, 
     sl.seen = sl.mR + EPA_MKV_CAP;
     sl.stack = (int2*)(sl.seen + EPA_SEEN_CAP);
     sl.fD = (float*)(sl.stack + EPA_STACK_CAP);
-    for (int qi = blockIdx.x; qi < n; qi += gridDim.x) epa_query(w, P, queue, qi, sl, threadIdx.x);
+    sl.faceCap = EPA_FACE_CAP;
+    sl.mkvCap = EPA_MKV_CAP;
+    sl.seenCap = EPA_SEEN_CAP;
+    sl.stackCap = EPA_STACK_CAP;
+    for (int j = blockIdx.x; j < n; j += gridDim.x) epa_query(w, P, queue, list[j], sl, threadIdx.x);
 }
 
 void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
@@ -193,7 +241,11 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
     if (nPairs > 0) { k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, (EpaRec*)nb.queue, nb.queueCount); note_launch(); }
     if (prof) { prof->mark(PH_NARROW, 1, s); prof->mark(PH_EPA, 0, s); }
     if (nPairs > 0) {
-        k_narrow_epa_smem<<<nb.slots, 32, EPA_SMEM_BYTES, s>>>(w, P, (const EpaRec*)nb.queue, nb.queueCount);
+        cudaMemsetAsync(nb.ovfCount, 0, sizeof(int), s);
+        k_narrow_epa_small<<<nb.slots, 32 * EPA_SMALL_WARPS, EPA_SMALL_SMEM_BYTES, s>>>(
+            w, P, (const EpaRec*)nb.queue, nb.queueCount, nb.ovfQueue, nb.ovfCount);
+        note_launch();
+        k_narrow_epa_smem<<<nb.slots, 32, EPA_SMEM_BYTES, s>>>(w, P, (const EpaRec*)nb.queue, nb.ovfQueue, nb.ovfCount);
         note_launch();
     }
     if (prof) prof->mark(PH_EPA, 1, s);
@@ -202,8 +254,10 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
 size_t epa_queue_record_bytes() { return sizeof(EpaRec); }
 
 int narrowphase_configure() {
-    return cudaFuncSetAttribute(k_narrow_epa_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EPA_SMEM_BYTES) ==
-                   cudaSuccess ? 0 : 1;
+    return (cudaFuncSetAttribute(k_narrow_epa_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EPA_SMEM_BYTES) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(k_narrow_epa_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)EPA_SMALL_SMEM_BYTES) == cudaSuccess) ? 0 : 1;
 }
 
 // ---- EPA pass on scratch compiled into the library ----------------------------------------

@@ -9,6 +9,8 @@ struct NarrowBuffers {
     void* queue = nullptr;        // EpaRec per queued pair (pair capacity)
     int* queueCount = nullptr;
     int slots = 0;                // EPA blocks, striding over the queue
+    int* ovfQueue = nullptr;      // queries the small-slot tier left to the full-capacity tier
+    int* ovfCount = nullptr;
 };
 
 size_t epa_queue_record_bytes();

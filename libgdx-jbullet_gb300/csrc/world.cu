@@ -162,6 +162,8 @@ int alloc_pair_work(jbgpu_world* w, int cap) {
     CK(cudaMalloc(&S.scanScratch, scan_scratch_bytes(cap)));
     if (w->nb.queue) cudaFree(w->nb.queue);
     CK(cudaMalloc(&w->nb.queue, epa_queue_record_bytes() * (size_t)std::max(cap, 1)));
+    dfree(w->nb.ovfQueue);
+    CK(dalloc(&w->nb.ovfQueue, cap));
     dfree(w->bb.partners);
     CK(dalloc(&w->bb.partners, cap));
     w->capRows = cap;
@@ -649,6 +651,7 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
              N.slots = w->sms * 2;
              if (narrowphase_configure()) return fail(JBGPU_ERR_CUDA, "EPA shared-memory size");
              CK(dalloc(&N.queueCount, 1));
+             CK(dalloc(&N.ovfCount, 1));
              return grow_bodies(w, std::max(1, c.initial_body_capacity));
          }()) != JBGPU_OK) {
         jbgpu_world_destroy(w);
@@ -687,7 +690,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.cursor); dfree(B.total); dfree(B.partners);
     NarrowBuffers& N = w->nb;
     if (N.queue) cudaFree(N.queue);
-    dfree(N.queueCount);
+    dfree(N.queueCount); dfree(N.ovfQueue); dfree(N.ovfCount);
     SolverBuffers& V = w->sb;
     dfree(V.parent); dfree(V.keepAwake); dfree(V.inactive); dfree(V.flag); dfree(V.candIdx); dfree(V.cand); dfree(V.colourOf);
     dfree(V.bucket); dfree(V.bucketList); dfree(V.claim); dfree(V.taken); dfree(V.posOf);
