@@ -55,6 +55,7 @@ def parse():
     p.add_argument("--solver-threads", type=int, default=0, help="jbgpu_config.solver_threads (0: 256)")
     p.add_argument("--solver-smem-bodies", type=int, default=0, help="jbgpu_config.solver_smem_bodies (0: 2048)")
     p.add_argument("--autotune", action="store_true", help="choose the solver knobs with jbgpu.autotune first")
+    p.add_argument("--rebuild-interval", type=int, default=None, help="jbgpu_config.broadphase_rebuild_interval")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start comparison")
     return p.parse_args()
 
@@ -231,6 +232,8 @@ def run_ours(args, dist):
     cfg.solver_parts = args.solver_parts
     cfg.solver_threads = args.solver_threads
     cfg.solver_smem_bodies = args.solver_smem_bodies
+    if args.rebuild_interval is not None:
+        cfg.broadphase_rebuild_interval = args.rebuild_interval
     tuned = None
     if args.autotune:
         from jbgpu import autotune

@@ -131,7 +131,10 @@ typedef struct jbgpu_config {
     int32_t solver_smem_bodies;         /* solver parts of at most this many bodies keep their
                                            velocities in shared memory (0: 2048).  No counterpart
                                            in the reference; a tuning knob. */
-    int32_t reserved[3];
+    int32_t broadphase_rebuild_interval;/* rebuild the broadphase tree every this many steps and
+                                           refit it in between (0 or 1: every step; default 4).  The
+                                           pair set is the same either way.  A tuning knob. */
+    int32_t reserved[2];
 } jbgpu_config;
 
 typedef struct jbgpu_shape_desc {

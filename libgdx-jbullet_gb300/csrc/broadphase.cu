@@ -286,8 +286,29 @@ __global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int n
 
 static inline int gridn(int n, int b) { return (n + b - 1) / b; }
 
+// The tree over the Morton order is rebuilt every rebuildInterval steps and only refitted to the
+// new AABBs in between: a refitted tree bounds every body exactly, so the traversal finds the
+// same pair set whatever the tree's shape; only its cost depends on how stale the order is.
 void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s) {
     int n = w.nBodies;
+    if (bb.built && bb.sinceBuild + 1 < bb.rebuildInterval) {
+        bb.sinceBuild++;
+        int nf = bb.nFinite;
+        cudaMemsetAsync(bb.cnt, 0, sizeof(int) * (n + 1), s);
+        if (nf > 1) {
+            cudaMemsetAsync(bb.bvh.visit, 0, sizeof(int) * (nf - 1), s);
+            k_refit<<<gridn(nf, 256), 256, 0, s>>>(w, bb.sortedBody, nf, bb.bvh); note_launch();
+            k_traverse<false><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, bb.cnt, nullptr,
+                                                              nullptr, nullptr, 0); note_launch();
+        }
+        if (bb.nPlanes > 0)
+            k_plane_pairs<false><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, bb.cnt, nullptr, nullptr,
+                                                                nullptr, 0); note_launch();
+        exclusive_scan(bb.cnt, bb.off, bb.total, n + 1, bb.scanScratch, s);
+        return;
+    }
+    bb.built = true;
+    bb.sinceBuild = 0;
     cudaMemsetAsync(bb.bounds, 0, sizeof(unsigned) * 6, s);
     cudaMemsetAsync(bb.bounds, 0xff, sizeof(unsigned) * 3, s);
     k_bounds<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds); note_launch();

@@ -19,6 +19,9 @@ struct Bvh {           // Karras radix tree over nf sorted leaves; internal node
 
 struct BroadphaseBuffers {
     int nFinite = 0, nPlanes = 0, nWorlds = 1, worldBits = 0;
+    int rebuildInterval = 1;             // rebuild the tree every this many steps, refit in between
+    int sinceBuild = 0;                  // steps since the last build
+    bool built = false;                  // the tree matches the current body set
     unsigned* bounds = nullptr;          // 6 ordered-int scene bounds
     uint64_t* mkeys = nullptr;           // morton keys (sorted in place)
     uint64_t* mkeys_alt = nullptr;

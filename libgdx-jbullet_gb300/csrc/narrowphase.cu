@@ -13,6 +13,7 @@
 #include <mutex>
 
 #include "epa.cuh"
+#include "prims.cuh"
 #include "manifold.cuh"
 #include "narrowphase.cuh"
 
@@ -32,9 +33,86 @@ JBD void manifold_refresh(Mf& m, const DevWorld& w, int mb0, int mb1) {
     refresh_points(m, load_xf(w, mb0), load_xf(w, mb1), w.cbt);
 }
 
-__global__ void k_narrow(DevWorld w, DevPairs P, int nPairs, EpaRec* queue, int* queueCount) {
+// Pairs grouped by algorithm before the pass, so that the threads of a warp run the same code:
+// bucket 0 = nothing to do (both bodies inactive, or two planes), 1 convex-plane, 2 sphere-
+// sphere, then GJK pairs by shape kinds: 3 box-box, 4 with a sphere, 5 with a capsule, 6 with a
+// hull.  perm lists buckets 1..6 in order; the pass covers nPairs - count[0] entries.
+constexpr int NB_BUCKETS = 7;
+
+JBD int narrow_bucket(const DevWorld& w, const DevPairs& P, int p) {
+    uint64_t key = P.keys[p];
+    int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+    int col0 = min(a, b), col1 = max(a, b);
+    if (!is_active_state(w.act[col0]) && !is_active_state(w.act[col1])) return 0;
+    int t0 = w.sh.type[w.shape[col0]], t1 = w.sh.type[w.shape[col1]];
+    if (t0 == SHAPE_PLANE && t1 == SHAPE_PLANE) return 0;
+    if (t0 == SHAPE_PLANE || t1 == SHAPE_PLANE) return 1;
+    if (t0 == SHAPE_SPHERE && t1 == SHAPE_SPHERE) return 2;
+    if (t0 == SHAPE_HULL || t1 == SHAPE_HULL) return 6;
+    if (t0 == SHAPE_CAPSULE || t1 == SHAPE_CAPSULE) return 5;
+    if (t0 == SHAPE_SPHERE || t1 == SHAPE_SPHERE) return 4;
+    return 3;
+}
+
+// Stable grouping: per block and bucket counts, laid out bucket-major with bucket 0 last, then
+// one exclusive scan gives every block its place in every bucket; within a block the pairs
+// keep their order (the owner-sorted order of the pair keys, which keeps shape data of an
+// owner body in cache).
+constexpr int NB_THREADS = 256;
+JBD int bucket_row(int v) { return v == 0 ? NB_BUCKETS - 1 : v - 1; }
+
+// Per-warp bucket counts of the block in shared memory (one ballot per bucket, one barrier);
+// then a thread's rank among the block's threads of its bucket and each bucket's block count.
+JBD void block_bucket_counts(int v, int (*shc)[NB_THREADS / 32]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int u = 0; u < NB_BUCKETS; u++) {
+        unsigned m = __ballot_sync(0xffffffffu, v == u);
+        if (lane == 0) shc[u][warp] = __popc(m);
+    }
+    __syncthreads();
+}
+__global__ void k_narrow_count(DevWorld w, DevPairs P, int nPairs, unsigned char* bucket, int* blockCnt) {
+    __shared__ int shc[NB_BUCKETS][NB_THREADS / 32];
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nPairs) return;
+    int v = -1;
+    if (p < nPairs) {
+        v = narrow_bucket(w, P, p);
+        bucket[p] = (unsigned char)v;
+    }
+    block_bucket_counts(v, shc);
+    if (threadIdx.x < NB_BUCKETS) {
+        int total = 0;
+        for (int k = 0; k < NB_THREADS / 32; k++) total += shc[threadIdx.x][k];
+        blockCnt[bucket_row(threadIdx.x) * gridDim.x + blockIdx.x] = total;
+    }
+}
+
+__global__ void k_narrow_scatter(int nPairs, const unsigned char* bucket, const int* blockOff, int* perm) {
+    __shared__ int shc[NB_BUCKETS][NB_THREADS / 32];
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    int v = p < nPairs ? bucket[p] : -1;
+    block_bucket_counts(v, shc);
+    if (v < 0) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int before = 0;
+    for (int k = 0; k < warp; k++) before += shc[v][k];
+    unsigned mv = 0;
+    for (int u = 0; u < NB_BUCKETS; u++) {
+        unsigned m = __ballot_sync(__activemask(), v == u);
+        if (v == u) mv = m;
+    }
+    perm[blockOff[bucket_row(v) * gridDim.x + blockIdx.x] + before + __popc(mv & ((1u << lane) - 1u))] = p;
+}
+
+// Entries of the pass: the pairs of buckets 1..6 = the start of bucket 0's row.
+JBD int narrow_active(const int* blockOff, int nBlocks) { return blockOff[(NB_BUCKETS - 1) * nBlocks]; }
+
+// With perm: n = the grouping's pair blocks and entry i is pair perm[i]; without: n = pairs.
+__global__ void k_narrow(DevWorld w, DevPairs P, int n, const int* perm, const int* blockOff, EpaRec* queue,
+                         int* queueCount) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (perm ? narrow_active(blockOff, n) : n)) return;
+    int p = perm ? perm[i] : i;
     uint64_t key = P.keys[p];
     int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
     int col0 = min(a, b), col1 = max(a, b);
@@ -234,11 +312,30 @@ __global__ void __launch_bounds__(32) k_narrow_epa_smem(DevWorld w, DevPairs P, 
     for (int j = blockIdx.x; j < n; j += gridDim.x) epa_query(w, P, queue, list[j], sl, threadIdx.x);
 }
 
+static int gridn_nb(int nPairs) { return (nPairs + NB_THREADS - 1) / NB_THREADS; }
+
+// Groups the pairs by bucket into nb.perm (blockOff: scanned per-block bucket counts).
+static void narrow_group(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s) {
+    const int blocks = gridn_nb(nPairs);
+    k_narrow_count<<<blocks, NB_THREADS, 0, s>>>(w, P, nPairs, nb.pairBucket, nb.blockOff); note_launch();
+    exclusive_scan(nb.blockOff, nb.blockOff, nullptr, NB_BUCKETS * blocks, nb.scanScratch, s);
+    k_narrow_scatter<<<blocks, NB_THREADS, 0, s>>>(nPairs, nb.pairBucket, nb.blockOff, nb.perm); note_launch();
+}
+
 void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
                         const Prof* prof) {
     if (prof) prof->mark(PH_NARROW, 0, s);
     cudaMemsetAsync(nb.queueCount, 0, sizeof(int), s);
-    if (nPairs > 0) { k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, (EpaRec*)nb.queue, nb.queueCount); note_launch(); }
+    if (nPairs > 0) {
+        if (nb.group) {
+            narrow_group(w, P, nPairs, nb, s);
+            k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, gridn_nb(nPairs), nb.perm, nb.blockOff,
+                                                           (EpaRec*)nb.queue, nb.queueCount); note_launch();
+        } else {
+            k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, nullptr, nullptr, (EpaRec*)nb.queue,
+                                                           nb.queueCount); note_launch();
+        }
+    }
     if (prof) { prof->mark(PH_NARROW, 1, s); prof->mark(PH_EPA, 0, s); }
     if (nPairs > 0) {
         cudaMemsetAsync(nb.ovfCount, 0, sizeof(int), s);
@@ -312,7 +409,9 @@ void narrowphase_launch_static(const DevWorld& w, DevPairs& P, int nPairs, Narro
                                cudaStream_t s) {
     cudaMemsetAsync(nb.queueCount, 0, sizeof(int), s);
     if (nPairs <= 0) return;
-    k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, (EpaRec*)nb.queue, nb.queueCount); note_launch();
+    narrow_group(w, P, nPairs, nb, s);
+    k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, gridn_nb(nPairs), nb.perm, nb.blockOff, (EpaRec*)nb.queue,
+                                                   nb.queueCount); note_launch();
     unsigned char* b = (unsigned char*)base;
     EpaArena ar;
     ar.fN = (float4*)(b + OFF_FN);

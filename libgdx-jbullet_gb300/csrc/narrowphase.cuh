@@ -11,6 +11,11 @@ struct NarrowBuffers {
     int slots = 0;                // EPA blocks, striding over the queue
     int* ovfQueue = nullptr;      // queries the small-slot tier left to the full-capacity tier
     int* ovfCount = nullptr;
+    unsigned char* pairBucket = nullptr;   // algorithm bucket per pair (pair capacity)
+    int* perm = nullptr;          // pairs grouped by bucket (pair capacity)
+    int* blockOff = nullptr;      // per block and bucket counts, scanned in place (7 x pair blocks)
+    bool group = true;            // group pairs by algorithm (worth it with two or more shape kinds)
+    void* scanScratch = nullptr;  // scan scratch for blockOff
 };
 
 size_t epa_queue_record_bytes();

@@ -162,8 +162,14 @@ int alloc_pair_work(jbgpu_world* w, int cap) {
     CK(cudaMalloc(&S.scanScratch, scan_scratch_bytes(cap)));
     if (w->nb.queue) cudaFree(w->nb.queue);
     CK(cudaMalloc(&w->nb.queue, epa_queue_record_bytes() * (size_t)std::max(cap, 1)));
-    dfree(w->nb.ovfQueue);
-    CK(dalloc(&w->nb.ovfQueue, cap));
+    dfree(w->nb.ovfQueue); dfree(w->nb.pairBucket); dfree(w->nb.perm); dfree(w->nb.blockOff);
+    CK(dalloc(&w->nb.ovfQueue, cap)); CK(dalloc(&w->nb.pairBucket, cap)); CK(dalloc(&w->nb.perm, cap));
+    {
+        int nbk = 7 * ((cap + 255) / 256) + 1;
+        CK(dalloc(&w->nb.blockOff, nbk));
+        if (w->nb.scanScratch) cudaFree(w->nb.scanScratch);
+        CK(cudaMalloc(&w->nb.scanScratch, scan_scratch_bytes(nbk)));
+    }
     dfree(w->bb.partners);
     CK(dalloc(&w->bb.partners, cap));
     w->capRows = cap;
@@ -282,10 +288,16 @@ int sync_planes(jbgpu_world* w) {
     std::vector<std::vector<int>> per(nw);
     int nf = 0, np = 0;
     std::vector<int> finite(nw, 0);
+    unsigned kinds = 0;                 // convex shape kinds present
     for (int i = 0; i < w->nBodies; i++) {
         if (w->hFlags[i] & CF_PLANE) { per[w->hWorld[i]].push_back(i); np++; }
-        else { nf++; finite[w->hWorld[i]]++; }
+        else {
+            nf++;
+            finite[w->hWorld[i]]++;
+            kinds |= 1u << (w->shapes[w->hShape[i]].type & 31);
+        }
     }
+    w->nb.group = __builtin_popcount(kinds) >= 2;
     std::vector<int> list, start(nw + 1, 0);
     for (int k = 0; k < nw; k++) { start[k] = (int)list.size(); list.insert(list.end(), per[k].begin(), per[k].end()); }
     start[nw] = (int)list.size();
@@ -302,6 +314,7 @@ int sync_planes(jbgpu_world* w) {
     B.worldBits = nw > 1 ? bits : 0;
     w->nWorlds = nw;
     w->worldFinite = finite;
+    w->bb.built = false;
     w->solverDirty = true;
     w->orderValid = false;
     w->planesDirty = false;
@@ -532,6 +545,7 @@ void jbgpu_config_default(jbgpu_config* c) {
     c->device = 0;
     c->initial_body_capacity = 1024;
     c->pairs_per_body = 16;
+    c->broadphase_rebuild_interval = 4;
 }
 
 int jbgpu_shape_local_inertia(const jbgpu_shape_desc* d, float mass, float out[3]) {
@@ -606,6 +620,7 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
     if (c.num_iterations < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "num_iterations < 0");
     if (c.solver_parts < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "solver_parts < 0");
     if (c.solver_smem_bodies < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "solver_smem_bodies < 0");
+    if (c.broadphase_rebuild_interval < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "broadphase_rebuild_interval < 0");
     if (c.solver_threads != 0 && c.solver_threads != 64 && c.solver_threads != 128 && c.solver_threads != 256)
         return fail(JBGPU_ERR_INVALID_ARGUMENT, "solver_threads must be 0, 64, 128 or 256");
     int ndev = 0;
@@ -629,6 +644,7 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
     d.deactTime = c.deactivation_time;
     d.disableDeact = c.disable_deactivation;
     d.numIter = c.num_iterations;
+    w->bb.rebuildInterval = std::max(1, c.broadphase_rebuild_interval);
     d.resTol = c.solver_residual > 0.0f ? c.solver_residual : 0.0f;
     d.maxIter = c.solver_max_iterations > 0 ? c.solver_max_iterations : 200;
     d.erp = c.erp;
@@ -652,6 +668,7 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
              if (narrowphase_configure()) return fail(JBGPU_ERR_CUDA, "EPA shared-memory size");
              CK(dalloc(&N.queueCount, 1));
              CK(dalloc(&N.ovfCount, 1));
+
              return grow_bodies(w, std::max(1, c.initial_body_capacity));
          }()) != JBGPU_OK) {
         jbgpu_world_destroy(w);
@@ -690,7 +707,8 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.cursor); dfree(B.total); dfree(B.partners);
     NarrowBuffers& N = w->nb;
     if (N.queue) cudaFree(N.queue);
-    dfree(N.queueCount); dfree(N.ovfQueue); dfree(N.ovfCount);
+    dfree(N.queueCount); dfree(N.ovfQueue); dfree(N.ovfCount); dfree(N.pairBucket); dfree(N.perm); dfree(N.blockOff);
+    if (N.scanScratch) cudaFree(N.scanScratch);
     SolverBuffers& V = w->sb;
     dfree(V.parent); dfree(V.keepAwake); dfree(V.inactive); dfree(V.flag); dfree(V.candIdx); dfree(V.cand); dfree(V.colourOf);
     dfree(V.bucket); dfree(V.bucketList); dfree(V.claim); dfree(V.taken); dfree(V.posOf);

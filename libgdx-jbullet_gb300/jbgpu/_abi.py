@@ -72,7 +72,8 @@ class Config(C.Structure):
         ("solver_residual", C.c_float),
         ("solver_max_iterations", C.c_int32),
         ("solver_smem_bodies", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("broadphase_rebuild_interval", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -91,6 +92,7 @@ def default_config(**overrides):
     c.device = 0
     c.initial_body_capacity = 1024
     c.pairs_per_body = 16
+    c.broadphase_rebuild_interval = 4
     for k, v in overrides.items():
         if k == "gravity":
             c.gravity[:] = tuple(v)
