@@ -47,8 +47,10 @@ struct DevPairs {
     float4 *pA, *pB, *wA, *wB, *nrm, *imp, *d1, *d2;
 };
 
-// Solver rows, indexed by solve slot * 4 + point (normal) and (solve slot * 4 + point) * 2 + k
-// (friction).  Slots are grouped by part and local colour, then by cut colour.
+// Solver rows, one normal row per contact point with distance <= 0, stored compactly: the
+// points of solve slot s are rows [pt0, pt0 + popcount(mask)) with slot_desc[s].z = pt0 << 4 |
+// mask; friction rows at 2 * row + k.  Slots are grouped by part and local colour, then by cut
+// colour.
 struct DevRows {
     float4* n_nrm;    // contactNormal, jacDiagABInv
     float4* n_rp1;    // relpos1CrossNormal, penetration
@@ -61,8 +63,11 @@ struct DevRows {
     float4* f_angA;
     float4* f_angB;
     int* slot_pair;   // pair index of the manifold in each solve slot
-    int4* slot_desc;  // body0, body1, point mask (bit j: point j has rows), local body indices
+    int4* slot_desc;  // body0, body1, first row << 4 | point mask, local body indices
     float2* slot_im;  // inverse masses of body0, body1
+    int* slot_pt0;    // per slot: point count, then (scanned) first row
+    int* pt_key;      // per row: slot << 2 | point
+    int* nPts;        // device scalar: rows
 };
 
 struct DevWorld {

@@ -441,6 +441,34 @@ JBD void friction_row(const DevRows& R, int fi, V dir, V rp1, V rp2, const BodyV
     R.f_angB[fi] = f4(angB, 0.0f);
 }
 
+// Points with rows (distance <= 0) of every slot: the mask into slot_desc.z and the count into
+// slot_pt0 (scanned afterwards into the slot's first point row); 0 beyond the candidates.
+__global__ void k_point_masks(DevPairs P, DevRows R, const int* nCandPtr, int nPairs) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nPairs) return;
+    int cnt = 0;
+    if (s < *nCandPtr) {
+        int p = R.slot_pair[s];
+        int n = P.n[p], mask = 0;
+        for (int j = 0; j < n; j++)
+            if (P.pA[p * 4 + j].w <= 0.0f) mask |= 1 << j;
+        R.slot_desc[s].z = mask;
+        cnt = __popc(mask);
+    }
+    R.slot_pt0[s] = cnt;
+}
+
+// slot_desc.z = first point row << 4 | point mask (after the scan of the counts).
+__global__ void k_point_rows(DevRows R, const int* nCandPtr) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= *nCandPtr) return;
+    int4 d = R.slot_desc[s];
+    d.z = (R.slot_pt0[s] << 4) | (d.z & 15);
+    R.slot_desc[s] = d;
+}
+
+// Rows are stored per point, compactly: the rows of slot s are [pt0, pt0 + popcount(mask)),
+// one normal row per point and its two friction rows at 2 * row and 2 * row + 1.
 __global__ void k_setup(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, float dt) {
     int nSlots = *nCandPtr;
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -449,14 +477,13 @@ __global__ void k_setup(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, 
     int4 desc = R.slot_desc[s];
     BodyV A = load_body(w, desc.x), B = load_body(w, desc.y);
     const bool warm = (w.solverMode & 4) != 0;
-    int n = P.n[p];
-    int mask = 0;
-    for (int j = 0; j < n; j++) {
+    const int mask = desc.z & 15;
+    int ni = desc.z >> 4;
+    for (int j = 0; j < 4; j++) {
+        if (!(mask & (1 << j))) continue;
         int k = p * 4 + j;
         float4 pa = P.pA[k];
         float dist = pa.w;
-        if (!(dist <= 0.0f)) continue;
-        mask |= 1 << j;
         float4 wa = P.wA[k], wb = P.wB[k], nr = P.nrm[k], im = P.imp[k];
         V nrm = mk(nr.x, nr.y, nr.z);
         V rp1 = sub(mk(wa.x, wa.y, wa.z), A.com), rp2 = sub(mk(wb.x, wb.y, wb.z), B.com);
@@ -476,7 +503,7 @@ __global__ void k_setup(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, 
         float penVel = jdiv(-pen, dt);
         if (rest > penVel) pen = 0.0f;
         float imp = warm ? __fmul_rn(nr.w, w.warm) : 0.0f;
-        int ni = s * 4 + j;
+        R.pt_key[ni] = (s << 2) | j;
         R.n_nrm[ni] = f4(nrm, jac);
         R.n_rp1[ni] = f4(rp1xn, jdiv(__fmul_rn(-pen, w.erp), dt));   // positionalError (java:248)
         R.n_rp2[ni] = f4(rp2xn, rest);
@@ -501,9 +528,8 @@ __global__ void k_setup(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, 
         }
         friction_row(R, ni * 2 + 0, dir1, rp1, rp2, A, B, warm ? __fmul_rn(im.x, w.warm) : 0.0f);
         friction_row(R, ni * 2 + 1, dir2, rp1, rp2, A, B, warm ? __fmul_rn(im.y, w.warm) : 0.0f);
+        ++ni;
     }
-    desc.z = mask;
-    R.slot_desc[s] = desc;
     R.slot_im[s] = make_float2(A.im, B.im);
     atomicAdd(&w.ctr[C_ROWS], __popc(mask));
 }
@@ -538,11 +564,10 @@ struct Resid {
 // The rows of one manifold for one phase, on velocities held in registers.  Warm start applies
 // per point the normal, then both friction impulses (setup order, java:680-760).
 template <bool TRACK>
-JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int mask, int kind, V& l0, V& a0, V& l1, V& a1,
+JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int z, int kind, V& l0, V& a0, V& l1, V& a1,
                         float im0, float im1, Resid& res) {
-    for (int j = 0; j < 4; j++) {
-        if (!(mask & (1 << j))) continue;
-        const int ni = s * 4 + j;
+    const int npt = __popc(z & 15), pt0 = z >> 4;
+    for (int ni = pt0; ni < pt0 + npt; ni++) {
         if (kind == PH_WARM) {
             float4 nn = R.n_nrm[ni];
             V n = mk(nn.x, nn.y, nn.z);
@@ -625,16 +650,18 @@ JBD void gstore(const DevWorld& w, int b, V l, V a) {
 // write-back (java:901-912): appliedImpulse; appliedImpulseLateral1 ends as friction row 2's
 JBD void writeback_slot(const DevPairs& P, const DevRows& R, int s) {
     int p = R.slot_pair[s];
-    int mask = R.slot_desc[s].z;
+    int z = R.slot_desc[s].z, mask = z & 15;
+    int ni = z >> 4;
     for (int j = 0; j < 4; j++) {
         if (!(mask & (1 << j))) continue;
-        int ni = s * 4 + j, k = p * 4 + j;
+        int k = p * 4 + j;
         float4 nr = P.nrm[k];
         nr.w = __ldcg(&R.n_angB[ni]).w;
         P.nrm[k] = nr;
         float4 im = P.imp[k];
         im.x = __ldcg(&R.f_rp1[ni * 2 + 1]).w;
         P.imp[k] = im;
+        ++ni;
     }
 }
 
@@ -907,8 +934,9 @@ __global__ void k_isl_segments(SolverBuffers sb, int nBodies) {
 // relative angular velocity (3), inverse masses (2), inverse-inertia-projected normals of
 // both bodies (6), the point's previous applied impulse and lateral impulses (3), friction,
 // restitution (2), lifetime (1).
-JBD void contact_features(const DevWorld& w, const DevPairs& P, const DevRows& R, int s, int j, float* f) {
-    const int p = R.slot_pair[s], k = p * 4 + j, ni = s * 4 + j;
+JBD void contact_features(const DevWorld& w, const DevPairs& P, const DevRows& R, int ni, float* f) {
+    const int s = R.pt_key[ni] >> 2, j = R.pt_key[ni] & 3;
+    const int p = R.slot_pair[s], k = p * 4 + j;
     const int4 d = R.slot_desc[s];
     const float2 im = R.slot_im[s];
     float4 nn = R.n_nrm[ni], aA = R.n_angA[ni], aB = R.n_angB[ni];
@@ -930,13 +958,11 @@ JBD void contact_features(const DevWorld& w, const DevPairs& P, const DevRows& R
     f[23] = (float)__float_as_int(pb.w);
 }
 
-__global__ void k_contact_features(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, float* X) {
-    const int nq = *nCandPtr * 4;
+__global__ void k_contact_features(DevWorld w, DevPairs P, DevRows R, const int* nPtsPtr, float* X) {
+    const int nq = *nPtsPtr;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
-        const int s = q >> 2, j = q & 3;
-        if (!(R.slot_desc[s].z & (1 << j))) continue;
         float f[MLP_IN];
-        contact_features(w, P, R, s, j, f);
+        contact_features(w, P, R, q, f);
         for (int e = 0; e < MLP_IN; e++) X[(size_t)q * MLP_IN + e] = f[e];
     }
 }
@@ -944,10 +970,9 @@ __global__ void k_contact_features(DevWorld w, DevPairs P, DevRows R, const int*
 // Targets of points whose island did not reach the residual (residual mode) are NaN: they are
 // not converged impulses, and the sample export leaves them out.
 __global__ void k_contact_targets(DevWorld w, DevRows R, SolverBuffers sb, float* T) {
-    const int nq = *sb.nCand * 4;
+    const int nq = *R.nPts;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
-        if (!(R.slot_desc[q >> 2].z & (1 << (q & 3)))) continue;
-        if (w.resTol > 0.0f && __ldcg(&sb.islConv[sb.slotIsl[q >> 2]]) == 0) {
+        if (w.resTol > 0.0f && __ldcg(&sb.islConv[sb.slotIsl[R.pt_key[q] >> 2]]) == 0) {
             T[(size_t)q * 3 + 0] = T[(size_t)q * 3 + 1] = T[(size_t)q * 3 + 2] = __int_as_float(0x7fc00000);
             continue;
         }
@@ -962,18 +987,17 @@ __global__ void k_contact_targets(DevWorld w, DevRows R, SolverBuffers sb, float
 // and an impulse scale u = unit / (invMass0 + invMass1): normal = max(0, b + y0 (b + u)),
 // friction k = y(1+k) mu (b + u) clamped to the cone of that normal impulse.  They replace warmstartingFactor x last step's
 // impulses before the PGS warm-start phase.
-__global__ void __launch_bounds__(MLP_THREADS) k_mlp_warmstart(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr,
-                                                                MlpDev M) {
+__global__ void __launch_bounds__(MLP_THREADS) k_mlp_warmstart(DevWorld w, DevPairs P, DevRows R, MlpDev M) {
     extern __shared__ __align__(16) unsigned char mlpSmem[];
     MlpSmem& S = *reinterpret_cast<MlpSmem*>(mlpSmem);
-    const int nq = *nCandPtr * 4;
+    const int nq = *R.nPts;
     mlp_load_weights(S, M);
     for (int first = blockIdx.x * MLP_TILE; first < nq; first += gridDim.x * MLP_TILE) {
         if (threadIdx.x < MLP_TILE) {
             const int q = first + threadIdx.x;
             float f[MLP_IN];
-            bool on = q < nq && (R.slot_desc[q >> 2].z & (1 << (q & 3)));
-            if (on) contact_features(w, P, R, q >> 2, q & 3, f);
+            bool on = q < nq;
+            if (on) contact_features(w, P, R, q, f);
             for (int e = 0; e < MLP_INP; e++) {
                 float v = (on && e < MLP_IN) ? mlp_norm_in(M.norm, e, f[e]) : 0.0f;
                 S.x[threadIdx.x][e] = __float2bfloat16_rn(v);
@@ -983,12 +1007,13 @@ __global__ void __launch_bounds__(MLP_THREADS) k_mlp_warmstart(DevWorld w, DevPa
         mlp_forward(S, M);
         if (threadIdx.x < MLP_TILE) {
             const int q = first + threadIdx.x;
-            if (q < nq && (R.slot_desc[q >> 2].z & (1 << (q & 3)))) {
+            if (q < nq) {
+                const int key = R.pt_key[q];
                 float y[MLP_OUT];
                 for (int o = 0; o < MLP_OUT; o++)
                     y[o] = MLP_REL * sinhf(S.y[threadIdx.x][o] * M.norm[2 * MLP_IN + MLP_OUT + o] + M.norm[2 * MLP_IN + o]);
-                const float2 im = R.slot_im[q >> 2];
-                const float base = fmaxf(P.nrm[R.slot_pair[q >> 2] * 4 + (q & 3)].w, 0.0f);
+                const float2 im = R.slot_im[key >> 2];
+                const float base = fmaxf(P.nrm[R.slot_pair[key >> 2] * 4 + (key & 3)].w, 0.0f);
                 const float unit = M.norm[MLP_NORM_UNIT] / fmaxf(im.x + im.y, 1e-6f);
                 const float mu = R.n_angA[q].w;
                 float ln = base + y[0] * (base + unit);
@@ -1147,14 +1172,17 @@ void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, 
         k_isl_segments<<<gridn(n, 256), 256, 0, s>>>(sb, n); note_launch();
     }
     if (prof) { prof->mark(PH_COLOUR, 1, s); prof->mark(PH_SETUP, 0, s); }
+    k_point_masks<<<gridn(nPairs, 256), 256, 0, s>>>(P, R, sb.nCand, nPairs); note_launch();
+    exclusive_scan(R.slot_pt0, R.slot_pt0, R.nPts, nPairs, sb.scanScratch, s);
+    k_point_rows<<<gridn(nPairs, 256), 256, 0, s>>>(R, sb.nCand); note_launch();
     k_setup<<<gridn(nPairs, 128), 128, 0, s>>>(w, P, R, sb.nCand, dt); note_launch();
     if (learn.sampleX) {
-        k_contact_features<<<std::min(gridn(nPairs * 4, 256), 4096), 256, 0, s>>>(w, P, R, sb.nCand, learn.sampleX);
+        k_contact_features<<<std::min(gridn(nPairs * 4, 256), 4096), 256, 0, s>>>(w, P, R, R.nPts, learn.sampleX);
         note_launch();
     }
     if (learn.mlp) {
         int tiles = std::min(gridn(nPairs * 4, MLP_TILE), 2048);
-        k_mlp_warmstart<<<tiles, MLP_THREADS, mlp_smem_bytes(), s>>>(w, P, R, sb.nCand, *learn.mlp);
+        k_mlp_warmstart<<<tiles, MLP_THREADS, mlp_smem_bytes(), s>>>(w, P, R, *learn.mlp);
         note_launch();
     }
     if (prof) { prof->mark(PH_SETUP, 1, s); prof->mark(PH_PGS, 0, s); }

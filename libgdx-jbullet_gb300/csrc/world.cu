@@ -146,11 +146,12 @@ int alloc_pair_work(jbgpu_world* w, int cap) {
     DevRows& R = w->rows;
     dfree(R.n_nrm); dfree(R.n_rp1); dfree(R.n_rp2); dfree(R.n_angA); dfree(R.n_angB);
     dfree(R.f_nrm); dfree(R.f_rp1); dfree(R.f_rp2); dfree(R.f_angA); dfree(R.f_angB);
-    dfree(R.slot_pair); dfree(R.slot_desc); dfree(R.slot_im);
+    dfree(R.slot_pair); dfree(R.slot_desc); dfree(R.slot_im); dfree(R.slot_pt0); dfree(R.pt_key);
     size_t c4 = (size_t)cap * 4, c8 = (size_t)cap * 8;
     CK(dalloc(&R.n_nrm, c4)); CK(dalloc(&R.n_rp1, c4)); CK(dalloc(&R.n_rp2, c4)); CK(dalloc(&R.n_angA, c4)); CK(dalloc(&R.n_angB, c4));
     CK(dalloc(&R.f_nrm, c8)); CK(dalloc(&R.f_rp1, c8)); CK(dalloc(&R.f_rp2, c8)); CK(dalloc(&R.f_angA, c8)); CK(dalloc(&R.f_angB, c8));
     CK(dalloc(&R.slot_pair, cap)); CK(dalloc(&R.slot_desc, cap)); CK(dalloc(&R.slot_im, cap));
+    CK(dalloc(&R.slot_pt0, cap)); CK(dalloc(&R.pt_key, c4));
     SolverBuffers& S = w->sb;
     dfree(S.flag); dfree(S.candIdx); dfree(S.cand); dfree(S.colourOf); dfree(S.bucket); dfree(S.bucketList);
     dfree(S.md); dfree(S.ml); dfree(S.slotIsl); dfree(S.islList); dfree(S.islChunk);
@@ -662,6 +663,8 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
              CK(dalloc(&S.colourCount, MAX_COLOURS + 1)); CK(dalloc(&S.colourFill, MAX_COLOURS + 1));
              CK(dalloc(&S.colourStart, MAX_COLOURS + 1)); CK(dalloc(&S.nCand, 1)); CK(dalloc(&S.nColours, 1));
              CK(dalloc(&S.nIslChunks, 1));
+             CK(dalloc(&w->rows.nPts, 1));
+             CK(cudaMemset(w->rows.nPts, 0, sizeof(int)));
              CK(cudaMemset(S.nCand, 0, sizeof(int))); CK(cudaMemset(S.nColours, 0, sizeof(int)));
              NarrowBuffers& N = w->nb;
              N.slots = w->sms * 2;
@@ -697,7 +700,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     DevRows& R = w->rows;
     dfree(R.n_nrm); dfree(R.n_rp1); dfree(R.n_rp2); dfree(R.n_angA); dfree(R.n_angB);
     dfree(R.f_nrm); dfree(R.f_rp1); dfree(R.f_rp2); dfree(R.f_angA); dfree(R.f_angB);
-    dfree(R.slot_pair); dfree(R.slot_desc); dfree(R.slot_im);
+    dfree(R.slot_pair); dfree(R.slot_desc); dfree(R.slot_im); dfree(R.slot_pt0); dfree(R.pt_key); dfree(R.nPts);
     BroadphaseBuffers& B = w->bb;
     dfree(B.bounds); dfree(B.mkeys); dfree(B.mkeys_alt); dfree(B.sortedBody); dfree(B.vals_alt);
     if (B.sortScratch) cudaFree(B.sortScratch);
@@ -985,19 +988,17 @@ int jbgpu_world_get_samples(jbgpu_world* w, float* x, float* t, int32_t capacity
     if (!w->logSamples || !w->sampleX) return JBGPU_OK;
     CK(cudaSetDevice(w->device));
     cudaStream_t s = w->stream;
-    int nc = 0;
+    int nc = 0, np = 0;
     CK(cudaMemcpyAsync(&nc, w->sb.nCand, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(&np, w->rows.nPts, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    if (nc <= 0) return JBGPU_OK;
-    std::vector<int4> desc(nc);
-    std::vector<float> X((size_t)nc * 4 * JBGPU_MLP_INPUTS), T((size_t)nc * 4 * JBGPU_MLP_OUTPUTS);
-    CK(cudaMemcpyAsync(desc.data(), w->rows.slot_desc, sizeof(int4) * nc, cudaMemcpyDeviceToHost, s));
+    if (nc <= 0 || np <= 0) return JBGPU_OK;
+    std::vector<float> X((size_t)np * JBGPU_MLP_INPUTS), T((size_t)np * JBGPU_MLP_OUTPUTS);
     CK(cudaMemcpyAsync(X.data(), w->sampleX, sizeof(float) * X.size(), cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(T.data(), w->sampleT, sizeof(float) * T.size(), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     int cnt = 0;
-    for (int q = 0; q < nc * 4; q++) {
-        if (!(desc[q >> 2].z & (1 << (q & 3)))) continue;
+    for (int q = 0; q < np; q++) {
         if (std::isnan(T[(size_t)q * JBGPU_MLP_OUTPUTS])) continue;   // island not converged
         if (cnt < capacity && x && t) {
             std::memcpy(x + (size_t)cnt * JBGPU_MLP_INPUTS, &X[(size_t)q * JBGPU_MLP_INPUTS], sizeof(float) * JBGPU_MLP_INPUTS);

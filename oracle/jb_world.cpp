@@ -4,6 +4,7 @@
 #include <chrono>
 #include <climits>
 #include <tuple>
+#include <unordered_map>
 #include "jb_world.h"
 
 namespace jb {
@@ -484,15 +485,21 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
     // GPU's residual-terminated mode); rows of converged islands are skipped.
     const bool byResidual = cfg.residualTol > 0.0f;
     const int maxIt = byResidual ? cfg.maxIterations : cfg.numIterations;
-    auto world_of = [&](const Row& c) {   // island of the row (the dynamic body's island)
-        const Manifold& m = w.pairMf[c.mfPair];
-        return w.bodies[m.body0].islandTag >= 0 ? w.bodies[m.body0].islandTag : w.bodies[m.body1].islandTag;
-    };
-    int nWorlds = 1;
-    for (const Row& c : rows) nWorlds = std::max(nWorlds, world_of(c) + 1);
-    std::vector<uint8_t> converged(nWorlds, 1);      // worlds without rows take no iteration
-    for (const Row& c : rows) converged[world_of(c)] = 0;
-    std::vector<float> dmax(nWorlds), lmax(nWorlds);
+    std::vector<int> rowIsl;            // residual mode: compact island index of each normal row
+    int nIsl = 0;
+    if (byResidual) {
+        std::unordered_map<int, int> index;
+        rowIsl.resize(rows.size());
+        for (size_t r = 0; r < rows.size(); r++) {
+            const Manifold& m = w.pairMf[rows[r].mfPair];
+            int tag = w.bodies[m.body0].islandTag >= 0 ? w.bodies[m.body0].islandTag : w.bodies[m.body1].islandTag;
+            auto it = index.find(tag);
+            if (it == index.end()) it = index.emplace(tag, nIsl++).first;
+            rowIsl[r] = it->second;
+        }
+    }
+    std::vector<uint8_t> converged(nIsl, 0);
+    std::vector<float> dmax(nIsl), lmax(nIsl);
     auto track = [&](int wi, float d, float l) {
         d = d < 0.0f ? -d : d;
         l = l < 0.0f ? -l : l;
@@ -500,13 +507,16 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
         if (l > lmax[wi]) lmax[wi] = l;
     };
     int itersUsed = 0;
-    for (int it = 0; it < maxIt; it++) {
-        bool any = false;
-        for (int k = 0; k < nWorlds; k++) { dmax[k] = 0.0f; lmax[k] = 0.0f; any = any || !converged[k]; }
-        if (!any) break;
+    for (int it = 0; it < maxIt && !rows.empty(); it++) {
+        if (byResidual) {
+            bool any = false;
+            for (int k = 0; k < nIsl; k++) { dmax[k] = 0.0f; lmax[k] = 0.0f; any = any || !converged[k]; }
+            if (!any) break;
+        }
         itersUsed = it + 1;
-        for (Row& c : rows) {   // resolveSingleCollisionCombinedCacheFriendly (java:234-284)
-            if (converged[world_of(c)]) continue;
+        for (size_t r = 0; r < rows.size(); r++) {   // resolveSingleCollisionCombinedCacheFriendly (java:234-284)
+            Row& c = rows[r];
+            if (byResidual && converged[rowIsl[r]]) continue;
             SolverBody& A = sb[c.bodyA];
             SolverBody& B = sb[c.bodyB];
             float vel1Dotn = dot(c.normal, A.linvel) + dot(c.rp1xn, A.angvel);
@@ -523,14 +533,14 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
             normalImpulse = c.impulse - oldImpulse;
             A.apply(scl(c.normal, A.invMass), c.angA, normalImpulse);
             B.apply(scl(c.normal, B.invMass), c.angB, -normalImpulse);
-            track(world_of(c), normalImpulse, c.impulse);
+            if (byResidual) track(rowIsl[r], normalImpulse, c.impulse);
         }
         for (Row& c : frows) {  // resolveSingleFrictionCacheFriendly (java:286-346)
-            const int wi = world_of(rows[c.frictionIndex]);
-            if (converged[wi]) continue;
+            const int wi = byResidual ? rowIsl[c.frictionIndex] : 0;
+            if (byResidual && converged[wi]) continue;
             float total = rows[c.frictionIndex].impulse + rows[c.frictionIndex].pushImpulse;
             float limit = total * c.friction;
-            if (!(total > 0.0f)) track(wi, 0.0f, c.impulse);
+            if (byResidual && !(total > 0.0f)) track(wi, 0.0f, c.impulse);
             if (total > 0.0f) {
                 SolverBody& A = sb[c.bodyA];
                 SolverBody& B = sb[c.bodyB];
@@ -545,11 +555,11 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
                 j1 = c.impulse - old;
                 A.apply(scl(c.normal, A.invMass), c.angA, j1);
                 B.apply(scl(c.normal, B.invMass), c.angB, -j1);
-                track(wi, j1, c.impulse);
+                if (byResidual) track(wi, j1, c.impulse);
             }
         }
         if (byResidual)
-            for (int k = 0; k < nWorlds; k++)
+            for (int k = 0; k < nIsl; k++)
                 if (!converged[k] && dmax[k] / (lmax[k] > 1e-6f ? lmax[k] : 1e-6f) <= cfg.residualTol) converged[k] = 1;
     }
     if (itersUsed > w.counters.solverIterations) w.counters.solverIterations = itersUsed;
