@@ -236,6 +236,13 @@ __global__ void k_classify(DevWorld w, DevPairs P, SolverBuffers sb) {
     int q = d0 ? q0 : q1;
     if (q == -1 || (d0 && d1 && q0 != q1)) q = sb.nParts;
     sb.bucket[k] = q;
+    int lb0 = 0xffff, lb1 = 0xffff;   // dynamic bodies' indices within the part (internal candidates)
+    if (q < sb.nParts) {
+        int ps = sb.partStart[q];
+        if (d0) lb0 = sb.posOf[b0] - ps;
+        if (d1) lb1 = sb.posOf[b1] - ps;
+    }
+    sb.candLocal[k] = lb0 | (lb1 << 16);
     atomicAdd(&sb.bucketCount[q], 1);
 }
 
@@ -290,10 +297,17 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
     for (int c = tid; c <= MAX_COLOURS; c += nth) sb.colourCount[c] = 0;
     if (tid == 0) { w.ctr[C_CUT_DONE] = 0; w.ctr[C_WIN0] = w.ctr[C_WIN1] = w.ctr[C_WIN2] = 0; }
     grid_barrier(w.ctr, nb);
-    // manifolds internal to the parts this block takes
+    // manifolds internal to the parts this block takes; the part's claims and taken marks live
+    // in shared memory, indexed by the bodies' positions within the part
+    extern __shared__ unsigned long long colSmem[];
+    unsigned long long* shClaim = colSmem;
+    int* shTaken = (int*)(colSmem + sb.partMax);
+    constexpr int NONE = 0xffff;
     for (int part = next_part(w, sb, C_PART_NEXT0, &shPart); part >= 0; part = next_part(w, sb, C_PART_NEXT0, &shPart)) {
         const int s0 = sb.bucketStart[part], s1 = sb.bucketStart[part + 1];
+        const int np = sb.partStart[part + 1] - sb.partStart[part];
         int* lc = sb.lcCount + part * (MAX_LOCAL + 1);
+        for (int i = threadIdx.x; i < np; i += blockDim.x) { shClaim[i] = ~0ull; shTaken[i] = -1; }
         if (threadIdx.x == 0) shDone = 0;
         __syncthreads();
         int r = 0;
@@ -301,20 +315,23 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
             for (int sub = 0; sub < MAX_SUB; sub++) {
                 const int t = r * MAX_SUB + sub;
                 for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-                    int k = sb.bucketList[i], b0, b1;
-                    if (!eligible(w, P, sb, k, r, b0, b1)) continue;
-                    if (dyn(w, b0)) atomicMin(&sb.claim[b0], ctag(t, k));
-                    if (dyn(w, b1)) atomicMin(&sb.claim[b1], ctag(t, k));
+                    const int k = sb.bucketList[i], lb = sb.candLocal[k], l0 = lb & 0xffff, l1 = (lb >> 16) & 0xffff;
+                    if (__ldcg(&sb.colourOf[k]) >= 0 || (l0 != NONE && shTaken[l0] == r) || (l1 != NONE && shTaken[l1] == r))
+                        continue;
+                    if (l0 != NONE) atomicMin(&shClaim[l0], ctag(t, k));
+                    if (l1 != NONE) atomicMin(&shClaim[l1], ctag(t, k));
                 }
                 if (threadIdx.x == 0) shWin = 0;
                 __syncthreads();
                 for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
-                    int k = sb.bucketList[i], b0, b1;
-                    if (!eligible(w, P, sb, k, r, b0, b1)) continue;
-                    if (holds_claims(w, sb, b0, b1, ctag(t, k))) {
+                    const int k = sb.bucketList[i], lb = sb.candLocal[k], l0 = lb & 0xffff, l1 = (lb >> 16) & 0xffff;
+                    if (__ldcg(&sb.colourOf[k]) >= 0 || (l0 != NONE && shTaken[l0] == r) || (l1 != NONE && shTaken[l1] == r))
+                        continue;
+                    const unsigned long long me = ctag(t, k);
+                    if ((l0 == NONE || shClaim[l0] == me) && (l1 == NONE || shClaim[l1] == me)) {
                         sb.colourOf[k] = r;
-                        if (dyn(w, b0)) sb.taken[b0] = r;
-                        if (dyn(w, b1)) sb.taken[b1] = r;
+                        if (l0 != NONE) shTaken[l0] = r;
+                        if (l1 != NONE) shTaken[l1] = r;
                         atomicAdd(&shWin, 1);
                         atomicAdd(&lc[r], 1);
                     }
@@ -1042,6 +1059,7 @@ template <class T> static cudaError_t salloc(T** p, size_t n) {
 template <class T> static void sfree(T*& p) { if (p) cudaFree((void*)p); p = nullptr; }
 
 static size_t pgs_smem(const SolverBuffers& sb) { return sb.partSmem ? (size_t)sb.smemCap * 32 : 0; }
+static size_t colour_smem(const SolverBuffers& sb) { return (size_t)sb.partMax * (sizeof(unsigned long long) + sizeof(int)); }
 
 int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts,
                      int threads, int smemBodies) {
@@ -1095,7 +1113,7 @@ int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& wor
         return JBGPU_ERR_CUDA;
     int perPgs = 0, perColour = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perPgs, k_pgs, threads, smem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perColour, k_colour, threads, 0) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perColour, k_colour, threads, colour_smem(sb)) != cudaSuccess ||
         perPgs < 1 || perColour < 1)
         return JBGPU_ERR_CUDA;
     sb.gridPgs = std::min(parts, perPgs * sms);
@@ -1155,7 +1173,7 @@ void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, 
         DevPairs pc = P;
         SolverBuffers sc = sb;
         void* args[] = {&wc, &pc, &sc};
-        cudaLaunchCooperativeKernel((void*)k_colour, sb.gridColour, sb.threads, args, 0, s); note_launch();
+        cudaLaunchCooperativeKernel((void*)k_colour, sb.gridColour, sb.threads, args, colour_smem(sb), s); note_launch();
     }
     k_slots<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, sb, R); note_launch();
     if (w.resTol > 0.0f) {        // residual mode: slots grouped by island

@@ -24,6 +24,7 @@ struct SolverBuffers {
     int* colourOf = nullptr;      // colour of candidate k (local colour for internal ones)
     int* bucket = nullptr;        // part of candidate k, nParts when cut
     int* bucketList = nullptr;    // candidates grouped by bucket
+    int* candLocal = nullptr;     // per candidate: its dynamic bodies' indices within its part
     unsigned long long* claim = nullptr;  // per body
     int* taken = nullptr;         // per body: colouring round that took it
     int* posOf = nullptr;         // per body: position in the body order (-1 none)

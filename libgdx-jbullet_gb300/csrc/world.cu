@@ -154,10 +154,11 @@ int alloc_pair_work(jbgpu_world* w, int cap) {
     CK(dalloc(&R.slot_pt0, cap)); CK(dalloc(&R.pt_key, c4));
     SolverBuffers& S = w->sb;
     dfree(S.flag); dfree(S.candIdx); dfree(S.cand); dfree(S.colourOf); dfree(S.bucket); dfree(S.bucketList);
-    dfree(S.md); dfree(S.ml); dfree(S.slotIsl); dfree(S.islList); dfree(S.islChunk);
+    dfree(S.md); dfree(S.ml); dfree(S.slotIsl); dfree(S.islList); dfree(S.islChunk); dfree(S.candLocal);
     CK(dalloc(&S.flag, cap)); CK(dalloc(&S.candIdx, cap)); CK(dalloc(&S.cand, cap)); CK(dalloc(&S.colourOf, cap));
     CK(dalloc(&S.bucket, cap)); CK(dalloc(&S.bucketList, cap));
     CK(dalloc(&S.md, cap)); CK(dalloc(&S.ml, cap)); CK(dalloc(&S.slotIsl, cap)); CK(dalloc(&S.islList, cap));
+    CK(dalloc(&S.candLocal, cap));
     CK(dalloc(&S.islChunk, (size_t)cap + std::max(w->capBodies, 1)));
     if (S.scanScratch) cudaFree(S.scanScratch);
     CK(cudaMalloc(&S.scanScratch, scan_scratch_bytes(cap)));
@@ -714,7 +715,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     if (N.scanScratch) cudaFree(N.scanScratch);
     SolverBuffers& V = w->sb;
     dfree(V.parent); dfree(V.keepAwake); dfree(V.inactive); dfree(V.flag); dfree(V.candIdx); dfree(V.cand); dfree(V.colourOf);
-    dfree(V.bucket); dfree(V.bucketList); dfree(V.claim); dfree(V.taken); dfree(V.posOf);
+    dfree(V.bucket); dfree(V.bucketList); dfree(V.claim); dfree(V.taken); dfree(V.posOf); dfree(V.candLocal);
     dfree(V.md); dfree(V.ml); dfree(V.slotIsl); dfree(V.islList); dfree(V.islCount); dfree(V.islFill); dfree(V.islStart);
     dfree(V.segFlag); dfree(V.segIdx); dfree(V.islChunk); dfree(V.islConv); dfree(V.islAcc); dfree(V.islDone);
     dfree(V.nIslChunks);
