@@ -339,7 +339,8 @@ def run_ours(args, dist):
                    "timed_steps": "%d..%d of the drop" % (W, W + K - 1), "parallelism": "independent world per GPU",
                    "l2": "no flush: per-step working set (bodies, two pair/manifold buffers, solver rows) exceeds L2",
                    "last_step_counters": {k: last[k] for k in ("pairs", "contacts", "solver_manifolds", "solver_rows",
-                                                               "colours", "islands", "gjk_calls", "epa_calls")}},
+                                                               "colours", "cut_colours", "cut_manifolds", "islands",
+                                                               "gjk_calls", "epa_calls")}},
         "device_window_ms": window_ms,
         "gpu_launches": int(launches),
         "phases": side,

@@ -128,29 +128,29 @@ __global__ void k_karras(const uint64_t* keys, int nf, Bvh t, const int* wstart,
     if (wstart[wi] == lo && wend[wi] == hi + 1) wroot[wi] = i;
 }
 
-// Bottom-up refit: the second child to arrive merges the boxes (node 0's parent is -1).
+// Bottom-up refit into the parents' child records: a leaf writes its box into its parent's
+// record; the second child to arrive at a node merges the node's two child boxes and writes the
+// union into the node's slot in its own parent (roots have parent -1).
 __global__ void k_refit(DevWorld w, const int* sortedBody, int nf, Bvh t) {
     int leaf = blockIdx.x * blockDim.x + threadIdx.x;
     if (leaf >= nf) return;
+    const int b = sortedBody[leaf];
+    float4 mn = w.amin[b], mx = w.amax[b];
+    int child = LEAF_FLAG | leaf, last = leaf;
     int node = t.leafParent[leaf];
     while (node >= 0) {
+        const int side = t.left[node] == child ? 0 : 2;
+        __stcg(&t.node[4 * node + side], make_float4(mn.x, mn.y, mn.z, __int_as_float(child)));
+        __stcg(&t.node[4 * node + side + 1], make_float4(mx.x, mx.y, mx.z, __int_as_float(last)));
         __threadfence();
         if (atomicAdd(&t.visit[node], 1) == 0) return;
         __threadfence();
-        float4 mn[2], mx[2];
-        int ch[2] = {t.left[node], t.right[node]};
-        for (int c = 0; c < 2; c++) {
-            if (ch[c] & LEAF_FLAG) {
-                int b = sortedBody[ch[c] & ~LEAF_FLAG];
-                mn[c] = w.amin[b];
-                mx[c] = w.amax[b];
-            } else {
-                mn[c] = __ldcg(&t.bmin[ch[c]]);
-                mx[c] = __ldcg(&t.bmax[ch[c]]);
-            }
-        }
-        __stcg(&t.bmin[node], make_float4(fminf(mn[0].x, mn[1].x), fminf(mn[0].y, mn[1].y), fminf(mn[0].z, mn[1].z), 0.0f));
-        __stcg(&t.bmax[node], make_float4(fmaxf(mx[0].x, mx[1].x), fmaxf(mx[0].y, mx[1].y), fmaxf(mx[0].z, mx[1].z), 0.0f));
+        const float4 l0 = __ldcg(&t.node[4 * node]), l1 = __ldcg(&t.node[4 * node + 1]);
+        const float4 r0 = __ldcg(&t.node[4 * node + 2]), r1 = __ldcg(&t.node[4 * node + 3]);
+        mn = make_float4(fminf(l0.x, r0.x), fminf(l0.y, r0.y), fminf(l0.z, r0.z), 0.0f);
+        mx = make_float4(fmaxf(l1.x, r1.x), fmaxf(l1.y, r1.y), fmaxf(l1.z, r1.z), 0.0f);
+        child = node;
+        last = t.hi[node];
         node = t.parent[node];
     }
 }
@@ -165,44 +165,63 @@ __device__ __forceinline__ bool filt(const DevWorld& w, int a, int b) {
 constexpr int STACK = 96;
 
 // One leaf's traversal: pairs (s, t) with t > s in sorted order.  FILL == false counts
-// pairs per owner; FILL == true writes partners into the owner's CSR segment.
+// pairs per owner and keeps up to TRAV_CACHE of leaf s's partners; FILL == true writes partners
+// into the owner's CSR segment, from that cache when it holds all of them, else by traversing
+// again.
 template <bool FILL>
 __global__ void k_traverse(DevWorld w, const int* sortedBody, int nf, Bvh t, const int* wroot, int* cnt, const int* off,
-                           int* cursor, int* partners, int capacity) {
+                           int* cursor, int* partners, int capacity, int* tcount, int* tcache) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nf) return;
     int bi = sortedBody[s];
-    float4 a0 = w.amin[bi], a1 = w.amax[bi];
+    auto emit = [&](int bj) {
+        int owner = bi < bj ? bi : bj, partner = bi < bj ? bj : bi;
+        if (!FILL) {
+            atomicAdd(&cnt[owner], 1);
+        } else {
+            int pos = off[owner] + atomicAdd(&cursor[owner], 1);
+            if (pos < capacity) partners[pos] = partner;
+        }
+    };
+    if (FILL) {
+        const int found = tcount[s];
+        if (found <= TRAV_CACHE) {
+            for (int i = 0; i < found; i++) emit(sortedBody[tcache[(size_t)s * TRAV_CACHE + i]]);
+            return;
+        }
+    }
     int root = wroot[w.world[bi]];
-    if (root & LEAF_FLAG) return;   // single-leaf world
+    if (root & LEAF_FLAG) {   // single-leaf world
+        if (!FILL) tcount[s] = 0;
+        return;
+    }
+    float4 a0 = w.amin[bi], a1 = w.amax[bi];
+    int found = 0;
     int stack[STACK];
     int sp = 0;
     stack[sp++] = root;
     while (sp > 0) {
-        int node = stack[--sp];
-        int ch[2] = {t.left[node], t.right[node]};
+        const float4* nd = t.node + 4 * stack[--sp];
+        const float4 rec[4] = {nd[0], nd[1], nd[2], nd[3]};
         for (int c = 0; c < 2; c++) {
-            int x = ch[c];
+            const float4 mn = rec[2 * c], mx = rec[2 * c + 1];
+            if (__float_as_int(mx.w) <= s) continue;   // the child's leaves all precede s
+            if (!ovl(a0, a1, mn, mx)) continue;
+            const int x = __float_as_int(mn.w);
             if (x & LEAF_FLAG) {
-                int tl = x & ~LEAF_FLAG;
-                if (tl <= s) continue;
-                int bj = sortedBody[tl];
-                if (!ovl(a0, a1, w.amin[bj], w.amax[bj]) || !filt(w, bi, bj)) continue;
-                int owner = bi < bj ? bi : bj, partner = bi < bj ? bj : bi;
-                if (!FILL) {
-                    atomicAdd(&cnt[owner], 1);
-                } else {
-                    int pos = off[owner] + atomicAdd(&cursor[owner], 1);
-                    if (pos < capacity) partners[pos] = partner;
-                }
+                const int tl = x & ~LEAF_FLAG;
+                const int bj = sortedBody[tl];
+                if (!filt(w, bi, bj)) continue;
+                emit(bj);
+                if (!FILL && found < TRAV_CACHE) tcache[(size_t)s * TRAV_CACHE + found] = tl;
+                ++found;
             } else {
-                if (t.hi[x] <= s) continue;
-                if (!ovl(a0, a1, t.bmin[x], t.bmax[x])) continue;
                 if (sp < STACK) stack[sp++] = x;
                 else atomicOr(&w.ctr[C_STATUS], ST_CAPACITY);
             }
         }
     }
+    if (!FILL) tcount[s] = found;
 }
 
 // Pairs of each finite body with the static planes of its world.
@@ -299,7 +318,7 @@ void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t
             cudaMemsetAsync(bb.bvh.visit, 0, sizeof(int) * (nf - 1), s);
             k_refit<<<gridn(nf, 256), 256, 0, s>>>(w, bb.sortedBody, nf, bb.bvh); note_launch();
             k_traverse<false><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, bb.cnt, nullptr,
-                                                              nullptr, nullptr, 0); note_launch();
+                                                              nullptr, nullptr, 0, bb.tcount, bb.tcache); note_launch();
         }
         if (bb.nPlanes > 0)
             k_plane_pairs<false><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, bb.cnt, nullptr, nullptr,
@@ -324,10 +343,11 @@ void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t
         if (nf > 1) {
             cudaMemsetAsync(bb.bvh.visit, 0, sizeof(int) * (nf - 1), s);
             cudaMemsetAsync(bb.bvh.parent, 0xff, sizeof(int) * (nf - 1), s);
+            cudaMemsetAsync(bb.bvh.leafParent, 0xff, sizeof(int) * nf, s);   // single-leaf worlds keep -1
             k_karras<<<gridn(nf - 1, 256), 256, 0, s>>>(bb.mkeys, nf, bb.bvh, bb.wstart, bb.wend, bb.wroot); note_launch();
             k_refit<<<gridn(nf, 256), 256, 0, s>>>(w, bb.sortedBody, nf, bb.bvh); note_launch();
             k_traverse<false><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, bb.cnt, nullptr,
-                                                              nullptr, nullptr, 0); note_launch();
+                                                              nullptr, nullptr, 0, bb.tcount, bb.tcache); note_launch();
         }
     }
     if (bb.nPlanes > 0)
@@ -342,7 +362,7 @@ void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw,
     // counts are recovered from the offsets: cnt[i] = off[i+1] - off[i]
     if (nf > 1)
         k_traverse<true><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, nullptr, bb.off,
-                                                         bb.cursor, bb.partners, capacity); note_launch();
+                                                         bb.cursor, bb.partners, capacity, bb.tcount, bb.tcache); note_launch();
     if (bb.nPlanes > 0)
         k_plane_pairs<true><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, nullptr, bb.off, bb.cursor,
                                                            bb.partners, capacity); note_launch();

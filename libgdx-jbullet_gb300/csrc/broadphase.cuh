@@ -13,9 +13,13 @@ struct Bvh {           // Karras radix tree over nf sorted leaves; internal node
     int* parent;       // internal node parents (-1 at roots)
     int* leafParent;
     int* visit;        // refit arrival counters
-    float4* bmin;
-    float4* bmax;
+    // per internal node, 4 float4: left child's box min with the child index in .w, its box max
+    // with the child's last sorted leaf in .w, then the same for the right child (one 64-byte
+    // record read per visited node)
+    float4* node;
 };
+
+constexpr int TRAV_CACHE = 16;         // pairs a counting traversal keeps for the filling one
 
 struct BroadphaseBuffers {
     int nFinite = 0, nPlanes = 0, nWorlds = 1, worldBits = 0;
@@ -40,6 +44,8 @@ struct BroadphaseBuffers {
     int* cursor = nullptr;               // fill cursors (n + 1)
     int* total = nullptr;                // device total pair count
     int* partners = nullptr;             // CSR partner lists (pair capacity)
+    int* tcount = nullptr;               // per sorted leaf: pairs its counting traversal found
+    int* tcache = nullptr;               // per sorted leaf: the first TRAV_CACHE partners' sorted leaves
 };
 
 void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s);

@@ -194,11 +194,12 @@ int grow_bodies(jbgpu_world* w, int need) {
     BroadphaseBuffers& B = w->bb;
     dfree(B.mkeys); dfree(B.mkeys_alt); dfree(B.sortedBody); dfree(B.vals_alt);
     dfree(B.bvh.left); dfree(B.bvh.right); dfree(B.bvh.lo); dfree(B.bvh.hi); dfree(B.bvh.parent); dfree(B.bvh.leafParent);
-    dfree(B.bvh.visit); dfree(B.bvh.bmin); dfree(B.bvh.bmax); dfree(B.cnt); dfree(B.off); dfree(B.cursor);
+    dfree(B.bvh.visit); dfree(B.bvh.node); dfree(B.cnt); dfree(B.off); dfree(B.cursor);
+    dfree(B.tcount); dfree(B.tcache);
     CK(dalloc(&B.mkeys, nc)); CK(dalloc(&B.mkeys_alt, nc)); CK(dalloc(&B.sortedBody, nc)); CK(dalloc(&B.vals_alt, nc));
     CK(dalloc(&B.bvh.left, nc)); CK(dalloc(&B.bvh.right, nc)); CK(dalloc(&B.bvh.lo, nc)); CK(dalloc(&B.bvh.hi, nc));
     CK(dalloc(&B.bvh.parent, nc)); CK(dalloc(&B.bvh.leafParent, nc)); CK(dalloc(&B.bvh.visit, nc));
-    CK(dalloc(&B.bvh.bmin, nc)); CK(dalloc(&B.bvh.bmax, nc));
+    CK(dalloc(&B.bvh.node, 4 * (size_t)nc)); CK(dalloc(&B.tcount, nc)); CK(dalloc(&B.tcache, (size_t)TRAV_CACHE * nc));
     CK(dalloc(&B.cnt, nc + 1)); CK(dalloc(&B.off, nc + 1)); CK(dalloc(&B.cursor, nc + 1));
     if (B.sortScratch) cudaFree(B.sortScratch);
     CK(cudaMalloc(&B.sortScratch, sort_scratch_bytes(nc)));
@@ -707,7 +708,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     if (B.sortScratch) cudaFree(B.sortScratch);
     if (B.scanScratch) cudaFree(B.scanScratch);
     dfree(B.bvh.left); dfree(B.bvh.right); dfree(B.bvh.lo); dfree(B.bvh.hi); dfree(B.bvh.parent); dfree(B.bvh.leafParent);
-    dfree(B.bvh.visit); dfree(B.bvh.bmin); dfree(B.bvh.bmax); dfree(B.wstart); dfree(B.wend); dfree(B.wroot);
+    dfree(B.bvh.visit); dfree(B.bvh.node); dfree(B.tcount); dfree(B.tcache); dfree(B.wstart); dfree(B.wend); dfree(B.wroot);
     dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.cursor); dfree(B.total); dfree(B.partners);
     NarrowBuffers& N = w->nb;
     if (N.queue) cudaFree(N.queue);
