@@ -578,6 +578,31 @@ struct Resid {
     }
 };
 
+// Row loads.  Within k_pgs only the applied impulses (n_angB.w, f_rp1.w) change, and a row is
+// read and written by the same thread in every phase; the other fields are read through the
+// non-coherent path.  The loads are volatile so that all loads of a point issue together, ahead
+// of its stores, instead of one memory round trip per row.
+JBD float4 ld_ro(const float4* p) {
+    float4 v;
+    asm volatile("ld.global.nc.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    return v;
+}
+JBD float4 ld_rw(const float4* p) {
+    float4 v;
+    asm volatile("ld.global.cg.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    return v;
+}
+JBD float ld_rw_w(const float4* p) {
+    float v;
+    asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(v) : "l"((const float*)p + 3));
+    return v;
+}
+JBD float ld_ro_w(const float4* p) {
+    float v;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"((const float*)p + 3));
+    return v;
+}
+
 // The rows of one manifold for one phase, on velocities held in registers.  Warm start applies
 // per point the normal, then both friction impulses (setup order, java:680-760).
 template <bool TRACK>
@@ -599,8 +624,8 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int z, int k
                 apply_imp(l1, a1, d, im1, mk4(R.f_angB[fi]), -fimp);
             }
         } else if (kind == PH_NORMAL) {   // resolveSingleCollisionCombinedCacheFriendly (java:234-284)
-            float4 nn = R.n_nrm[ni], r1 = R.n_rp1[ni], r2 = R.n_rp2[ni], aA = R.n_angA[ni];
-            float4 aB = __ldcg(&R.n_angB[ni]);
+            const float4 nn = ld_ro(R.n_nrm + ni), r1 = ld_ro(R.n_rp1 + ni), r2 = ld_ro(R.n_rp2 + ni), aA = ld_ro(R.n_angA + ni);
+            float4 aB = ld_rw(R.n_angB + ni);
             V n = mk(nn.x, nn.y, nn.z);
             float vel1 = __fadd_rn(dot(n, l0), dot(mk(r1.x, r1.y, r1.z), a0));
             float vel2 = __fadd_rn(dot(n, l1), dot(mk(r2.x, r2.y, r2.z), a1));
@@ -618,21 +643,31 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int z, int k
             __stcg(&R.n_angB[ni], aB);
             if (TRACK) res.add(d, acc);
         } else {                          // resolveSingleFrictionCacheFriendly (java:286-346)
-            float total = __fadd_rn(__ldcg(&R.n_angB[ni]).w, 0.0f);   // appliedImpulse + appliedPushImpulse
-            float fric = R.n_angA[ni].w;
+            const float applied = ld_rw_w(R.n_angB + ni);
+            const float fric = ld_ro_w(R.n_angA + ni);
+            float4 fnv[2], r1v[2], r2v[2], fav[2], fbv[2];
+            for (int f = 0; f < 2; f++) {
+                const int fi = ni * 2 + f;
+                fnv[f] = ld_ro(R.f_nrm + fi);
+                r1v[f] = ld_rw(R.f_rp1 + fi);
+                r2v[f] = ld_ro(R.f_rp2 + fi);
+                fav[f] = ld_ro(R.f_angA + fi);
+                fbv[f] = ld_ro(R.f_angB + fi);
+            }
+            float total = __fadd_rn(applied, 0.0f);   // appliedImpulse + appliedPushImpulse
             float limit = __fmul_rn(total, fric);
             if (!(total > 0.0f)) {
                 if (TRACK) {
-                    res.add(0.0f, __ldcg(&R.f_rp1[ni * 2]).w);
-                    res.add(0.0f, __ldcg(&R.f_rp1[ni * 2 + 1]).w);
+                    res.add(0.0f, r1v[0].w);
+                    res.add(0.0f, r1v[1].w);
                 }
                 continue;
             }
             for (int f = 0; f < 2; f++) {
                 int fi = ni * 2 + f;
-                float4 fn = R.f_nrm[fi];
-                float4 r1 = __ldcg(&R.f_rp1[fi]);
-                float4 r2 = R.f_rp2[fi];
+                const float4 fn = fnv[f];
+                float4 r1 = r1v[f];
+                const float4 r2 = r2v[f];
                 V n = mk(fn.x, fn.y, fn.z);
                 float vel1 = __fadd_rn(dot(n, l0), dot(mk(r1.x, r1.y, r1.z), a0));
                 float vel2 = __fadd_rn(dot(n, l1), dot(mk(r2.x, r2.y, r2.z), a1));
@@ -643,8 +678,8 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int z, int k
                 if (limit < acc) acc = limit;
                 else if (acc < -limit) acc = -limit;
                 j1 = __fsub_rn(acc, old);
-                apply_imp(l0, a0, n, im0, mk4(R.f_angA[fi]), j1);
-                apply_imp(l1, a1, n, im1, mk4(R.f_angB[fi]), -j1);
+                apply_imp(l0, a0, n, im0, mk4(fav[f]), j1);
+                apply_imp(l1, a1, n, im1, mk4(fbv[f]), -j1);
                 r1.w = acc;
                 __stcg(&R.f_rp1[fi], r1);
                 if (TRACK) res.add(j1, acc);
