@@ -589,13 +589,44 @@ JBD float4 ld_ro(const float4* p) {
 }
 JBD float4 ld_rw(const float4* p) {
     float4 v;
-    asm volatile("ld.global.cg.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
+    asm volatile("ld.global.v4.f32 {%0,%1,%2,%3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p));
     return v;
 }
 JBD float ld_rw_w(const float4* p) {
     float v;
-    asm volatile("ld.global.cg.f32 %0, [%1];" : "=f"(v) : "l"((const float*)p + 3));
+    asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"((const float*)p + 3));
     return v;
+}
+
+// While a thread solves one colour it prefetches into L1 the rows of its slot in the next step
+// (the next colour, or the cut colours after the part's colours): the slot's first-row word is
+// loaded at the start of the colour, the rows' lines are prefetched at its end.
+JBD void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+JBD int next_z(const DevRows& R, int s, int s1) {
+    if (s >= s1) return -1;
+    int z;
+    asm volatile("ld.global.s32 %0, [%1];" : "=r"(z) : "l"((const int*)(R.slot_desc + s) + 2));
+    return z;
+}
+JBD void prefetch_rows(const DevRows& R, int kind, int z) {
+    if (z < 0) return;
+    const int npt = __popc(z & 15), p0 = z >> 4, p1 = p0 + npt - 1;
+    if (npt == 0) return;
+    if (kind != PH_FRICTION) {
+        prefetch_l1(R.n_nrm + p0); prefetch_l1(R.n_nrm + p1);
+        prefetch_l1(R.n_rp1 + p0); prefetch_l1(R.n_rp1 + p1);
+        prefetch_l1(R.n_rp2 + p0); prefetch_l1(R.n_rp2 + p1);
+    }
+    prefetch_l1(R.n_angA + p0); prefetch_l1(R.n_angA + p1);
+    prefetch_l1(R.n_angB + p0); prefetch_l1(R.n_angB + p1);
+    if (kind != PH_NORMAL) {
+        const int f0 = 2 * p0, f1 = 2 * p1 + 1;
+        prefetch_l1(R.f_nrm + f0); prefetch_l1(R.f_nrm + f1);
+        prefetch_l1(R.f_rp1 + f0); prefetch_l1(R.f_rp1 + f1);
+        prefetch_l1(R.f_rp2 + f0); prefetch_l1(R.f_rp2 + f1);
+        prefetch_l1(R.f_angA + f0); prefetch_l1(R.f_angA + f1);
+        prefetch_l1(R.f_angB + f0); prefetch_l1(R.f_angB + f1);
+    }
 }
 JBD float ld_ro_w(const float4* p) {
     float v;
@@ -770,8 +801,10 @@ JBD void res_keep(const SolverBuffers& sb, const ResCtl& rc, int kind, int s, co
 
 // One local colour of a part: its manifolds share no dynamic body; the part's bodies are in
 // shared memory (global memory when the part does not fit).
+// (s0n, s1n, kindn): the next step's slots, whose rows this thread prefetches.
 JBD void local_colour(const DevWorld& w, const DevRows& R, const SolverBuffers& sb, int s0, int s1, int kind, bool smem,
-                      float4* sl, float4* sa, const ResCtl& rc) {
+                      float4* sl, float4* sa, const ResCtl& rc, int sn, int s1n, int kindn) {
+    const int zn = next_z(R, sn, s1n);
     for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
         if (res_skip(sb, rc, s)) continue;
         const int4 d = R.slot_desc[s];
@@ -788,6 +821,7 @@ JBD void local_colour(const DevWorld& w, const DevRows& R, const SolverBuffers& 
         if (im.x != 0.0f) { if (m0) { sl[lb0] = f4(l0, 0.0f); sa[lb0] = f4(a0, 0.0f); } else gstore(w, d.x, l0, a0); }
         if (im.y != 0.0f) { if (m1) { sl[lb1] = f4(l1, 0.0f); sa[lb1] = f4(a1, 0.0f); } else gstore(w, d.y, l1, a1); }
     }
+    prefetch_rows(R, kindn, zn);
 }
 
 JBD bool resid_done(float dmax, float lmax, float tol) { return jdiv(dmax, lmax > 1e-6f ? lmax : 1e-6f) <= tol; }
@@ -864,20 +898,20 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             const bool psm = smem && v.np <= sb.smemCap;
             if (psm) stage_in(w, sb, v, sl, sa);
             __syncthreads();
-            for (int c = 0; c < v.nLoc; c++) {
-                local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_WARM, psm, sl, sa, rc);
+            // the step after (kind, c): the next colour, else colour 0 of the next phase
+            const int nl = v.nLoc;
+            auto run = [&](int kind, int c, int kindNext) {
+                const bool last = c + 1 == nl;
+                const int cn = last ? 0 : c + 1, kn = last ? kindNext : kind;
+                local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc,
+                             kn < 0 ? 0 : v.lcs[cn] + (int)threadIdx.x, kn < 0 ? 0 : v.lcs[cn + 1], kn);
                 __syncthreads();
-            }
+            };
+            for (int c = 0; c < nl; c++) run(PH_WARM, c, maxIt > 0 ? PH_NORMAL : -1);
             int it = 0;
-            for (; it < maxIt && v.nLoc > 0; it++) {
-                for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_NORMAL, psm, sl, sa, rc);
-                    __syncthreads();
-                }
-                for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], PH_FRICTION, psm, sl, sa, rc);
-                    __syncthreads();
-                }
+            for (; it < maxIt && nl > 0; it++) {
+                for (int c = 0; c < nl; c++) run(PH_NORMAL, c, PH_FRICTION);
+                for (int c = 0; c < nl; c++) run(PH_FRICTION, c, it + 1 < maxIt ? PH_NORMAL : -1);
             }
             if (it > itMax) itMax = it;
             if (psm) stage_out(w, sb, v, sl, sa);
@@ -900,7 +934,11 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                 if (psm) stage_in(w, sb, v, sl, sa);
                 __syncthreads();
                 for (int c = 0; c < v.nLoc; c++) {
-                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc);
+                    // after the last colour: this thread's slot in cut colour 0
+                    const bool last = c + 1 == v.nLoc;
+                    const int sn = last ? (nCut > 0 ? sb.colourStart[0] + tid : 0) : v.lcs[c + 1] + (int)threadIdx.x;
+                    const int s1n = last ? (nCut > 0 ? sb.colourStart[1] : 0) : v.lcs[c + 2];
+                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc, sn, s1n, kind);
                     __syncthreads();
                 }
                 if (psm) stage_out(w, sb, v, sl, sa);
@@ -909,6 +947,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             grid_barrier(w.ctr, nb);
             for (int c = 0; c < nCut; c++) {
                 const int s0 = sb.colourStart[c], s1 = sb.colourStart[c + 1];
+                const int zn = c + 1 < nCut ? next_z(R, sb.colourStart[c + 1] + tid, sb.colourStart[c + 2]) : -1;
                 for (int s = s0 + tid; s < s1; s += nth) {
                     if (res_skip(sb, rc, s)) continue;
                     const int4 d = R.slot_desc[s];
@@ -923,6 +962,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                     if (im.x != 0.0f) gstore(w, d.x, l0, a0);
                     if (im.y != 0.0f) gstore(w, d.y, l1, a1);
                 }
+                prefetch_rows(R, kind, zn);
                 grid_barrier(w.ctr, nb);
             }
         }
