@@ -48,12 +48,25 @@ __global__ void k_uf_init(int n, int* parent) {
     if (i < n) parent[i] = i;
 }
 
-__global__ void k_uf_union(DevWorld w, DevPairs P, int nPairs, int* parent) {
+// Unions in rounds over the pairs (sampling, as in the Afforest connected-components
+// algorithm): round 0 takes the first two pairs of every owner (keys are sorted by owner),
+// rounds 1 and 2 the third and the fourth, round 3 the rest; after each round every body is
+// pointed at its root.
+// A later round skips a pair whose bodies already point at the same root, so most pairs of a
+// large island cost two loads instead of finds and hooks along deep, contended paths.  The
+// partition is the same as one pass over all pairs.
+constexpr int UF_ROUNDS = 4;
+
+__global__ void k_uf_union(DevWorld w, DevPairs P, int nPairs, int* parent, int round) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nPairs) return;
     uint64_t key = P.keys[p];
     int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+    int rank = 0;               // pairs of the same owner before p, up to 4
+    while (rank < UF_ROUNDS && p - rank - 1 >= 0 && (int)(P.keys[p - rank - 1] >> 32) == a) rank++;
+    if ((rank < 2 ? 0 : rank - 1) != round) return;
     if (!merges_islands(w.flags[a]) || !merges_islands(w.flags[b])) return;
+    if (round > 0 && __ldcg(&parent[a]) == __ldcg(&parent[b])) return;
     for (int it = 0; it < 1 << 20; it++) {
         a = uf_find(parent, a);
         b = uf_find(parent, b);
@@ -62,6 +75,12 @@ __global__ void k_uf_union(DevWorld w, DevPairs P, int nPairs, int* parent) {
         if (atomicCAS(&parent[b], b, a) == b) return;
     }
     atomicOr(&w.ctr[C_STATUS], ST_TIMEOUT);
+}
+
+// Every body pointed at its root (between the union rounds).
+__global__ void k_uf_compress(int n, int* parent) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) parent[i] = uf_find(parent, i);
 }
 
 __global__ void k_islands(DevWorld w, int* parent, int* keepAwake, int* inactive) {
@@ -137,7 +156,12 @@ __global__ void k_count_manifolds(DevPairs P, int nPairs, int* ctr) {
 void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s) {
     int n = w.nBodies;
     k_uf_init<<<gridn(n, 256), 256, 0, s>>>(n, sb.parent); note_launch();
-    if (nPairs > 0) { k_uf_union<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.parent); note_launch(); }
+    if (nPairs > 0) {
+        for (int r = 0; r < UF_ROUNDS; r++) {
+            if (r > 0) { k_uf_compress<<<gridn(n, 256), 256, 0, s>>>(n, sb.parent); note_launch(); }
+            k_uf_union<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.parent, r); note_launch();
+        }
+    }
     k_islands<<<gridn(n, 256), 256, 0, s>>>(w, sb.parent, sb.keepAwake, sb.inactive); note_launch();
     k_island_awake<<<gridn(n, 256), 256, 0, s>>>(w, sb.keepAwake); note_launch();
 }
