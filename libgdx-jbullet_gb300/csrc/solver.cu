@@ -187,8 +187,8 @@ void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuff
 }
 
 // ---- grid barrier (bounded wait) -----------------------------------------------------------
-// Arrival by an acquire-release atomic, release of the generation by the last block, acquire
-// polling.  A wait gives up after a bounded number of polls and sets ST_TIMEOUT (the host
+// Arrival by an acquire-release atomic on a count that grows through the launch, acquire
+// polling of the count.  A wait gives up after a bounded number of polls and sets ST_TIMEOUT (the host
 // reports JBGPU_ERR_TIMEOUT); once the flag is set every later barrier returns at once.
 constexpr long long BARRIER_SPIN_LIMIT = 20000000;
 
@@ -209,18 +209,16 @@ __device__ __forceinline__ void st_release(int* p, unsigned v) {
 __device__ __forceinline__ void grid_barrier(int* ctr, int nblocks) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned g = ld_acquire(&ctr[C_BAR_GEN]);
-        unsigned arrived = atom_add_acq_rel(&ctr[C_BAR_COUNT], 1u);
-        if (arrived == (unsigned)nblocks - 1u) {
-            atomicExch(&ctr[C_BAR_COUNT], 0);
-            st_release(&ctr[C_BAR_GEN], g + 1u);
-        } else {
-            long long spins = 0;
-            while (ld_acquire(&ctr[C_BAR_GEN]) == g) {
-                if (++spins > BARRIER_SPIN_LIMIT || (ld_acquire(&ctr[C_STATUS]) & ST_TIMEOUT)) {
-                    atomicOr(&ctr[C_STATUS], ST_TIMEOUT);
-                    break;
-                }
+        // The arrival count only grows within a launch (it is cleared before each launch):
+        // barrier k is complete when it reaches k * nblocks, so the last arrival's atomic
+        // itself releases the waiting blocks.
+        const unsigned arrived = atom_add_acq_rel(&ctr[C_BAR_COUNT], 1u) + 1u;
+        const unsigned target = (arrived + (unsigned)nblocks - 1u) / (unsigned)nblocks * (unsigned)nblocks;
+        long long spins = 0;
+        while (ld_acquire(&ctr[C_BAR_COUNT]) < target) {
+            if ((++spins & 31) == 0 && (spins > BARRIER_SPIN_LIMIT || (ld_acquire(&ctr[C_STATUS]) & ST_TIMEOUT))) {
+                atomicOr(&ctr[C_STATUS], ST_TIMEOUT);
+                break;
             }
         }
     }
@@ -912,6 +910,9 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
     float4* sa = smv + sb.smemCap;
     const bool byRes = w.resTol > 0.0f;
     const int maxIt = byRes ? w.maxIter : w.numIter;
+    // cut slot i of a colour goes to block i % gridDim.x, so a colour's manifolds spread over
+    // every SM instead of filling the first blocks
+    const int spread = threadIdx.x * gridDim.x + blockIdx.x;
     ResCtl rc;
     rc.on = byRes;
     if (nCut == 0 && !byRes) {
@@ -960,7 +961,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                 for (int c = 0; c < v.nLoc; c++) {
                     // after the last colour: this thread's slot in cut colour 0
                     const bool last = c + 1 == v.nLoc;
-                    const int sn = last ? (nCut > 0 ? sb.colourStart[0] + tid : 0) : v.lcs[c + 1] + (int)threadIdx.x;
+                    const int sn = last ? (nCut > 0 ? sb.colourStart[0] + spread : 0) : v.lcs[c + 1] + (int)threadIdx.x;
                     const int s1n = last ? (nCut > 0 ? sb.colourStart[1] : 0) : v.lcs[c + 2];
                     local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc, sn, s1n, kind);
                     __syncthreads();
@@ -971,8 +972,8 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             grid_barrier(w.ctr, nb);
             for (int c = 0; c < nCut; c++) {
                 const int s0 = sb.colourStart[c], s1 = sb.colourStart[c + 1];
-                const int zn = c + 1 < nCut ? next_z(R, sb.colourStart[c + 1] + tid, sb.colourStart[c + 2]) : -1;
-                for (int s = s0 + tid; s < s1; s += nth) {
+                const int zn = c + 1 < nCut ? next_z(R, sb.colourStart[c + 1] + spread, sb.colourStart[c + 2]) : -1;
+                for (int s = s0 + spread; s < s1; s += nth) {
                     if (res_skip(sb, rc, s)) continue;
                     const int4 d = R.slot_desc[s];
                     const float2 im = R.slot_im[s];
