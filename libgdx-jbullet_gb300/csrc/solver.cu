@@ -206,16 +206,20 @@ __device__ __forceinline__ void st_release(int* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ void grid_barrier(int* ctr, int nblocks) {
+__device__ __forceinline__ void red_release_add(int* p, int v) {
+    asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// `passed` counts the arrivals of all blocks up to this barrier (thread 0 keeps it; every block
+// passes the same barriers).  The arrival is a fire-and-forget release add, so a block waits for
+// one round trip (its polls) rather than its atomic's return and then a poll.
+__device__ __forceinline__ void grid_barrier(int* ctr, int nblocks, unsigned& passed) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        // The arrival count only grows within a launch (it is cleared before each launch):
-        // barrier k is complete when it reaches k * nblocks, so the last arrival's atomic
-        // itself releases the waiting blocks.
-        const unsigned arrived = atom_add_acq_rel(&ctr[C_BAR_COUNT], 1u) + 1u;
-        const unsigned target = (arrived + (unsigned)nblocks - 1u) / (unsigned)nblocks * (unsigned)nblocks;
+        passed += (unsigned)nblocks;
+        red_release_add(&ctr[C_BAR_COUNT], 1);
         long long spins = 0;
-        while (ld_acquire(&ctr[C_BAR_COUNT]) < target) {
+        while (ld_acquire(&ctr[C_BAR_COUNT]) < passed) {
             if ((++spins & 31) == 0 && (spins > BARRIER_SPIN_LIMIT || (ld_acquire(&ctr[C_STATUS]) & ST_TIMEOUT))) {
                 atomicOr(&ctr[C_STATUS], ST_TIMEOUT);
                 break;
@@ -310,6 +314,7 @@ __device__ __forceinline__ bool holds_claims(const DevWorld& w, const SolverBuff
 }
 
 __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs P, SolverBuffers sb) {
+    unsigned barK = 0;
     const int nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
     const int nCand = *sb.nCand;
@@ -318,7 +323,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
     for (int c = tid; c < sb.nParts * (MAX_LOCAL + 1); c += nth) sb.lcCount[c] = 0;
     for (int c = tid; c <= MAX_COLOURS; c += nth) sb.colourCount[c] = 0;
     if (tid == 0) { w.ctr[C_CUT_DONE] = 0; w.ctr[C_WIN0] = w.ctr[C_WIN1] = w.ctr[C_WIN2] = 0; }
-    grid_barrier(w.ctr, nb);
+    grid_barrier(w.ctr, nb, barK);
     // manifolds internal to the parts this block takes; the part's claims and taken marks live
     // in shared memory, indexed by the bodies' positions within the part
     extern __shared__ unsigned long long colSmem[];
@@ -376,7 +381,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
         __syncthreads();
     }
     // cut manifolds, grid-wide
-    grid_barrier(w.ctr, nb);
+    grid_barrier(w.ctr, nb, barK);
     const int c0 = sb.bucketStart[sb.nParts], c1 = sb.bucketStart[sb.nParts + 1];
     const int nCut = c1 - c0;
     int g = 0, round = 0;
@@ -392,7 +397,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
                 if (dyn(w, b0)) atomicMin(&sb.claim[b0], ctag(t, k));
                 if (dyn(w, b1)) atomicMin(&sb.claim[b1], ctag(t, k));
             }
-            grid_barrier(w.ctr, nb);
+            grid_barrier(w.ctr, nb, barK);
             int won = 0;
             for (int i = c0 + tid; i < c1; i += nth) {
                 int k = sb.bucketList[i], b0, b1;
@@ -406,7 +411,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
                 }
             }
             if (won) { atomicAdd(&w.ctr[C_WIN0 + g % 3], won); atomicAdd(&w.ctr[C_CUT_DONE], won); }
-            grid_barrier(w.ctr, nb);
+            grid_barrier(w.ctr, nb, barK);
             if (__ldcg(&w.ctr[C_WIN0 + g % 3]) == 0) { g++; break; }
         }
     }
@@ -900,6 +905,7 @@ JBD void island_residuals(const DevWorld& w, const SolverBuffers& sb, int flag, 
 // manifolds run first (parts share no dynamic body), then the cut colours.  With fixed
 // iterations and no cut manifold every part runs all phases on its own, with no grid barrier.
 __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs P, DevRows R, SolverBuffers sb, float dt) {
+    unsigned barK = 0;
     extern __shared__ float4 smv[];
     const int nb = gridDim.x;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
@@ -969,7 +975,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                 if (psm) stage_out(w, sb, v, sl, sa);
                 __syncthreads();
             }
-            grid_barrier(w.ctr, nb);
+            grid_barrier(w.ctr, nb, barK);
             for (int c = 0; c < nCut; c++) {
                 const int s0 = sb.colourStart[c], s1 = sb.colourStart[c + 1];
                 const int zn = c + 1 < nCut ? next_z(R, sb.colourStart[c + 1] + spread, sb.colourStart[c + 2]) : -1;
@@ -988,7 +994,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                     if (im.y != 0.0f) gstore(w, d.y, l1, a1);
                 }
                 prefetch_rows(R, kind, zn);
-                grid_barrier(w.ctr, nb);
+                grid_barrier(w.ctr, nb, barK);
             }
         }
         ++it;
@@ -999,7 +1005,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             const int flag = C_RES0 + it % 3;
             if (tid == 0) w.ctr[C_RES0 + (it + 1) % 3] = 0;
             island_residuals(w, sb, flag, it);
-            grid_barrier(w.ctr, nb);
+            grid_barrier(w.ctr, nb, barK);
             if (__ldcg(&w.ctr[flag]) == 0) break;
             rc.skipConv = true;
         }
