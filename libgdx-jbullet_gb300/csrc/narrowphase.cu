@@ -163,7 +163,10 @@ __global__ void k_narrow(DevWorld w, DevPairs P, int n, const int* perm, const i
         ShapeRef sa = shape_ref(w.sh, s0), sb = shape_ref(w.sh, s1);
         float md = __fadd_rn(__fadd_rn(sa.margin, sb.margin), w.cbt);
         md = __fmul_rn(md, md);
-        atomicAdd(&w.ctr[C_GJK], 1);
+        {   // one counter atomic per group of converged lanes
+            const unsigned am = __activemask();
+            if ((threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(&w.ctr[C_GJK], __popc(am));
+        }
         GjkPart g = gjk_part(sa, x0, sb, x1, md);
         if (g.needEpa) {
             int q = atomicAdd(queueCount, 1);

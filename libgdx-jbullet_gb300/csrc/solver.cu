@@ -360,12 +360,14 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
                         if (l0 != NONE) shTaken[l0] = r;
                         if (l1 != NONE) shTaken[l1] = r;
                         atomicAdd(&shWin, 1);
-                        atomicAdd(&lc[r], 1);
                     }
                 }
                 __syncthreads();
                 const int won = shWin;
-                if (threadIdx.x == 0) shDone += won;
+                if (threadIdx.x == 0) {
+                    shDone += won;
+                    if (won) atomicAdd(&lc[r], won);
+                }
                 __syncthreads();
                 if (won == 0) break;
             }
@@ -406,11 +408,15 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
                     sb.colourOf[k] = round;
                     if (dyn(w, b0)) sb.taken[b0] = mark;
                     if (dyn(w, b1)) sb.taken[b1] = mark;
-                    atomicAdd(&sb.colourCount[round], 1);
                     won++;
                 }
             }
-            if (won) { atomicAdd(&w.ctr[C_WIN0 + g % 3], won); atomicAdd(&w.ctr[C_CUT_DONE], won); }
+            won = __reduce_add_sync(0xffffffffu, won);   // one set of counter atomics per warp
+            if ((threadIdx.x & 31) == 0 && won) {
+                atomicAdd(&sb.colourCount[round], won);
+                atomicAdd(&w.ctr[C_WIN0 + g % 3], won);
+                atomicAdd(&w.ctr[C_CUT_DONE], won);
+            }
             grid_barrier(w.ctr, nb, barK);
             if (__ldcg(&w.ctr[C_WIN0 + g % 3]) == 0) { g++; break; }
         }
@@ -575,7 +581,9 @@ __global__ void k_setup(DevWorld w, DevPairs P, DevRows R, const int* nCandPtr, 
         ++ni;
     }
     R.slot_im[s] = make_float2(A.im, B.im);
-    atomicAdd(&w.ctr[C_ROWS], __popc(mask));
+    const unsigned am = __activemask();
+    const int rows = __reduce_add_sync(am, __popc(mask));
+    if ((threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(&w.ctr[C_ROWS], rows);
 }
 
 // ---- PGS (cooperative) ---------------------------------------------------------------------
