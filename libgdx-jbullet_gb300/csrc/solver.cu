@@ -669,13 +669,72 @@ JBD float ld_ro_w(const float4* p) {
     return v;
 }
 
+// ---- point pool --------------------------------------------------------------------------
+// The points of a manifold are solved one after another, so a manifold with k points would
+// wait for k round trips to L2.  A thread that solves a manifold with more than one point
+// copies the rows of its second to last points into entries of a per-block pool in shared
+// memory with cp.async while it solves the first point from registers; they have arrived by
+// the time it needs them.  An entry holds one point's fields of the phase: normal phase
+// n_nrm, n_rp1, n_rp2, n_angA, n_angB; friction phase n_angA, n_angB and the two friction rows'
+// f_nrm, f_rp1, f_rp2, f_angA, f_angB.  Two pools alternate between consecutive colours; when
+// a pool is full the points are read from global memory.
+constexpr int POOL_F4 = 12;
+
+struct PointPool {
+    float4* e = nullptr;    // this colour's pool (POOL_F4 float4 per entry)
+    int* top = nullptr;     // its fill counter (shared memory)
+    int cap = 0;            // entries
+};
+struct PoolSlot {           // the entries one manifold took: its points 1.. are entries base..
+    const float4* e = nullptr;
+    bool waited = false;
+};
+
+JBD void cp_async16(void* dst, const void* src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+JBD void cp_async_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+JBD PoolSlot pool_take(const PointPool& pp, const DevRows& R, int kind, int z) {
+    PoolSlot ps;
+    const int npt = __popc(z & 15), pt0 = z >> 4;
+    if (pp.cap == 0 || npt < 2 || kind == PH_WARM) return ps;
+    const int base = atomicAdd(pp.top, npt - 1);
+    if (base + npt - 1 > pp.cap) return ps;
+    float4* e = pp.e + (size_t)base * POOL_F4;
+    for (int j = 1; j < npt; j++, e += POOL_F4) {
+        const int ni = pt0 + j;
+        if (kind == PH_NORMAL) {
+            cp_async16(e + 0, R.n_nrm + ni); cp_async16(e + 1, R.n_rp1 + ni); cp_async16(e + 2, R.n_rp2 + ni);
+            cp_async16(e + 3, R.n_angA + ni); cp_async16(e + 4, R.n_angB + ni);
+        } else {
+            cp_async16(e + 0, R.n_angA + ni); cp_async16(e + 1, R.n_angB + ni);
+            for (int f = 0; f < 2; f++) {
+                const int fi = ni * 2 + f;
+                cp_async16(e + 2 + 5 * f, R.f_nrm + fi); cp_async16(e + 3 + 5 * f, R.f_rp1 + fi);
+                cp_async16(e + 4 + 5 * f, R.f_rp2 + fi); cp_async16(e + 5 + 5 * f, R.f_angA + fi);
+                cp_async16(e + 6 + 5 * f, R.f_angB + fi);
+            }
+        }
+    }
+    ps.e = pp.e + (size_t)base * POOL_F4;
+    return ps;
+}
+
 // The rows of one manifold for one phase, on velocities held in registers.  Warm start applies
-// per point the normal, then both friction impulses (setup order, java:680-760).
+// per point the normal, then both friction impulses (setup order, java:680-760).  Points 1.. of
+// a manifold with pool entries are read from them.
 template <bool TRACK>
 JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int z, int kind, V& l0, V& a0, V& l1, V& a1,
-                        float im0, float im1, Resid& res) {
+                        float im0, float im1, Resid& res, PoolSlot ps = PoolSlot()) {
     const int npt = __popc(z & 15), pt0 = z >> 4;
     for (int ni = pt0; ni < pt0 + npt; ni++) {
+        const float4* pe = nullptr;     // this point's pool entry
+        if (ps.e && ni > pt0) {
+            if (!ps.waited) { cp_async_wait(); ps.waited = true; }
+            pe = ps.e + (size_t)(ni - pt0 - 1) * POOL_F4;
+        }
         if (kind == PH_WARM) {
             float4 nn = R.n_nrm[ni];
             V n = mk(nn.x, nn.y, nn.z);
@@ -690,8 +749,13 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int z, int k
                 apply_imp(l1, a1, d, im1, mk4(R.f_angB[fi]), -fimp);
             }
         } else if (kind == PH_NORMAL) {   // resolveSingleCollisionCombinedCacheFriendly (java:234-284)
-            const float4 nn = ld_ro(R.n_nrm + ni), r1 = ld_ro(R.n_rp1 + ni), r2 = ld_ro(R.n_rp2 + ni), aA = ld_ro(R.n_angA + ni);
-            float4 aB = ld_rw(R.n_angB + ni);
+            float4 nn, r1, r2, aA, aB;
+            if (pe) {
+                nn = pe[0]; r1 = pe[1]; r2 = pe[2]; aA = pe[3]; aB = pe[4];
+            } else {
+                nn = ld_ro(R.n_nrm + ni); r1 = ld_ro(R.n_rp1 + ni); r2 = ld_ro(R.n_rp2 + ni); aA = ld_ro(R.n_angA + ni);
+                aB = ld_rw(R.n_angB + ni);
+            }
             V n = mk(nn.x, nn.y, nn.z);
             float vel1 = __fadd_rn(dot(n, l0), dot(mk(r1.x, r1.y, r1.z), a0));
             float vel2 = __fadd_rn(dot(n, l1), dot(mk(r2.x, r2.y, r2.z), a1));
@@ -709,16 +773,26 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int z, int k
             __stcg(&R.n_angB[ni], aB);
             if (TRACK) res.add(d, acc);
         } else {                          // resolveSingleFrictionCacheFriendly (java:286-346)
-            const float applied = ld_rw_w(R.n_angB + ni);
-            const float fric = ld_ro_w(R.n_angA + ni);
+            float applied, fric;
             float4 fnv[2], r1v[2], r2v[2], fav[2], fbv[2];
-            for (int f = 0; f < 2; f++) {
-                const int fi = ni * 2 + f;
-                fnv[f] = ld_ro(R.f_nrm + fi);
-                r1v[f] = ld_rw(R.f_rp1 + fi);
-                r2v[f] = ld_ro(R.f_rp2 + fi);
-                fav[f] = ld_ro(R.f_angA + fi);
-                fbv[f] = ld_ro(R.f_angB + fi);
+            if (pe) {
+                fric = pe[0].w;
+                applied = pe[1].w;
+                for (int f = 0; f < 2; f++) {
+                    fnv[f] = pe[2 + 5 * f]; r1v[f] = pe[3 + 5 * f]; r2v[f] = pe[4 + 5 * f];
+                    fav[f] = pe[5 + 5 * f]; fbv[f] = pe[6 + 5 * f];
+                }
+            } else {
+                applied = ld_rw_w(R.n_angB + ni);
+                fric = ld_ro_w(R.n_angA + ni);
+                for (int f = 0; f < 2; f++) {
+                    const int fi = ni * 2 + f;
+                    fnv[f] = ld_ro(R.f_nrm + fi);
+                    r1v[f] = ld_rw(R.f_rp1 + fi);
+                    r2v[f] = ld_ro(R.f_rp2 + fi);
+                    fav[f] = ld_ro(R.f_angA + fi);
+                    fbv[f] = ld_ro(R.f_angB + fi);
+                }
             }
             float total = __fadd_rn(applied, 0.0f);   // appliedImpulse + appliedPushImpulse
             float limit = __fmul_rn(total, fric);
@@ -838,20 +912,21 @@ JBD void res_keep(const SolverBuffers& sb, const ResCtl& rc, int kind, int s, co
 // shared memory (global memory when the part does not fit).
 // (s0n, s1n, kindn): the next step's slots, whose rows this thread prefetches.
 JBD void local_colour(const DevWorld& w, const DevRows& R, const SolverBuffers& sb, int s0, int s1, int kind, bool smem,
-                      float4* sl, float4* sa, const ResCtl& rc, int sn, int s1n, int kindn) {
+                      float4* sl, float4* sa, const ResCtl& rc, int sn, int s1n, int kindn, const PointPool& pool) {
     const int zn = next_z(R, sn, s1n);
     for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
         if (res_skip(sb, rc, s)) continue;
         const int4 d = R.slot_desc[s];
         const float2 im = R.slot_im[s];
+        const PoolSlot ps = pool_take(pool, R, kind, d.z);
         const int lb0 = d.w & 0xffff, lb1 = (d.w >> 16) & 0xffff;
         const bool m0 = smem && lb0 != 0xffff, m1 = smem && lb1 != 0xffff;
         V l0, a0, l1, a1;
         if (m0) { l0 = mk4(sl[lb0]); a0 = mk4(sa[lb0]); } else gload(w, d.x, l0, a0);
         if (m1) { l1 = mk4(sl[lb1]); a1 = mk4(sa[lb1]); } else gload(w, d.y, l1, a1);
         Resid res;
-        if (rc.on) solve_manifold<true>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
-        else solve_manifold<false>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
+        if (rc.on) solve_manifold<true>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res, ps);
+        else solve_manifold<false>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res, ps);
         res_keep(sb, rc, kind, s, res);
         if (im.x != 0.0f) { if (m0) { sl[lb0] = f4(l0, 0.0f); sa[lb0] = f4(a0, 0.0f); } else gstore(w, d.x, l0, a0); }
         if (im.y != 0.0f) { if (m1) { sl[lb1] = f4(l1, 0.0f); sa[lb1] = f4(a1, 0.0f); } else gstore(w, d.y, l1, a1); }
@@ -922,6 +997,17 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
     const bool smem = sb.partSmem != 0;
     float4* sl = smv;
     float4* sa = smv + sb.smemCap;
+    __shared__ int shPoolTop[2];
+    float4* poolBase = smv + (smem ? 2 * sb.smemCap : 0);
+    // the pool of step c: entries pool(c).e, its counter cleared one step ahead
+    auto pool = [&](int c) {
+        PointPool pp;
+        pp.cap = sb.poolPts;
+        pp.e = poolBase + (size_t)(c & 1) * sb.poolPts * POOL_F4;
+        pp.top = &shPoolTop[c & 1];
+        return pp;
+    };
+    if (threadIdx.x < 2) shPoolTop[threadIdx.x] = 0;
     const bool byRes = w.resTol > 0.0f;
     const int maxIt = byRes ? w.maxIter : w.numIter;
     // cut slot i of a colour goes to block i % gridDim.x, so a colour's manifolds spread over
@@ -929,6 +1015,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
     const int spread = threadIdx.x * gridDim.x + blockIdx.x;
     ResCtl rc;
     rc.on = byRes;
+    int step = 0;           // colour steps this block has run (the pool alternates with it)
     if (nCut == 0 && !byRes) {
         __shared__ int shPart;
         int itMax = 0;
@@ -942,9 +1029,11 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             auto run = [&](int kind, int c, int kindNext) {
                 const bool last = c + 1 == nl;
                 const int cn = last ? 0 : c + 1, kn = last ? kindNext : kind;
+                if (threadIdx.x == 0) shPoolTop[(step + 1) & 1] = 0;
                 local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc,
-                             kn < 0 ? 0 : v.lcs[cn] + (int)threadIdx.x, kn < 0 ? 0 : v.lcs[cn + 1], kn);
+                             kn < 0 ? 0 : v.lcs[cn] + (int)threadIdx.x, kn < 0 ? 0 : v.lcs[cn + 1], kn, pool(step));
                 __syncthreads();
+                ++step;
             };
             for (int c = 0; c < nl; c++) run(PH_WARM, c, maxIt > 0 ? PH_NORMAL : -1);
             int it = 0;
@@ -977,8 +1066,10 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                     const bool last = c + 1 == v.nLoc;
                     const int sn = last ? (nCut > 0 ? sb.colourStart[0] + spread : 0) : v.lcs[c + 1] + (int)threadIdx.x;
                     const int s1n = last ? (nCut > 0 ? sb.colourStart[1] : 0) : v.lcs[c + 2];
-                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc, sn, s1n, kind);
+                    if (threadIdx.x == 0) shPoolTop[(step + 1) & 1] = 0;
+                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc, sn, s1n, kind, pool(step));
                     __syncthreads();
+                    ++step;
                 }
                 if (psm) stage_out(w, sb, v, sl, sa);
                 __syncthreads();
@@ -987,22 +1078,26 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             for (int c = 0; c < nCut; c++) {
                 const int s0 = sb.colourStart[c], s1 = sb.colourStart[c + 1];
                 const int zn = c + 1 < nCut ? next_z(R, sb.colourStart[c + 1] + spread, sb.colourStart[c + 2]) : -1;
+                if (threadIdx.x == 0) shPoolTop[(step + 1) & 1] = 0;
+                const PointPool pp = pool(step);
                 for (int s = s0 + spread; s < s1; s += nth) {
                     if (res_skip(sb, rc, s)) continue;
                     const int4 d = R.slot_desc[s];
                     const float2 im = R.slot_im[s];
+                    const PoolSlot ps = pool_take(pp, R, kind, d.z);
                     V l0, a0, l1, a1;
                     gload(w, d.x, l0, a0);
                     gload(w, d.y, l1, a1);
                     Resid res;
-                    if (rc.on) solve_manifold<true>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
-                    else solve_manifold<false>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res);
+                    if (rc.on) solve_manifold<true>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res, ps);
+                    else solve_manifold<false>(w, R, s, d.z, kind, l0, a0, l1, a1, im.x, im.y, res, ps);
                     res_keep(sb, rc, kind, s, res);
                     if (im.x != 0.0f) gstore(w, d.x, l0, a0);
                     if (im.y != 0.0f) gstore(w, d.y, l1, a1);
                 }
                 prefetch_rows(R, kind, zn);
                 grid_barrier(w.ctr, nb, barK);
+                ++step;
             }
         }
         ++it;
@@ -1172,7 +1267,9 @@ template <class T> static cudaError_t salloc(T** p, size_t n) {
 }
 template <class T> static void sfree(T*& p) { if (p) cudaFree((void*)p); p = nullptr; }
 
-static size_t pgs_smem(const SolverBuffers& sb) { return sb.partSmem ? (size_t)sb.smemCap * 32 : 0; }
+static size_t pgs_smem(const SolverBuffers& sb) {
+    return (sb.partSmem ? (size_t)sb.smemCap * 32 : 0) + (size_t)2 * sb.poolPts * POOL_F4 * 16;
+}
 static size_t colour_smem(const SolverBuffers& sb) { return (size_t)sb.partMax * (sizeof(unsigned long long) + sizeof(int)); }
 
 int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts,
@@ -1222,10 +1319,26 @@ int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& wor
     sb.partMax = partMax;
     sb.smemCap = std::min(partMax, smemBodies > 0 ? smemBodies : PART_MAX_BODIES);
     sb.partSmem = (sb.smemCap < 0xffff && (size_t)sb.smemCap * 32 <= 96 * 1024) ? 1 : 0;
-    size_t smem = pgs_smem(sb);
-    if (cudaFuncSetAttribute(k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) != cudaSuccess)
+    // one k_pgs attribute value for every world of the process (a smaller value set by another
+    // world would invalidate this world's occupancy)
+    int dev = 0, smemBlock = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&smemBlock, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncSetAttribute(k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBlock - 1024) != cudaSuccess)
         return JBGPU_ERR_CUDA;
-    int perPgs = 0, perColour = 0;
+    // point pools: half a block's threads in entries, fewer (or none) if they would cost occupancy
+    int perPgs = 0, perColour = 0, perBare = 0;
+    sb.poolPts = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perBare, k_pgs, threads, pgs_smem(sb)) != cudaSuccess)
+        return JBGPU_ERR_CUDA;
+    for (int pts = threads / 2; pts >= 16; pts /= 2) {
+        sb.poolPts = pts;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perPgs, k_pgs, threads, pgs_smem(sb)) != cudaSuccess)
+            return JBGPU_ERR_CUDA;
+        if (perPgs >= perBare) break;
+        sb.poolPts = 0;
+    }
+    size_t smem = pgs_smem(sb);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perPgs, k_pgs, threads, smem) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perColour, k_colour, threads, colour_smem(sb)) != cudaSuccess ||
         perPgs < 1 || perColour < 1)

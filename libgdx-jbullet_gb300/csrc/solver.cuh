@@ -68,6 +68,7 @@ struct SolverBuffers {
     int partMax = 0;              // largest part, bodies
     int partSmem = 0;             // velocities of internal manifolds staged in shared memory
     int smemCap = 0;              // parts of at most this many bodies are staged
+    int poolPts = 0;              // entries of each of k_pgs's two point pools (0: none)
     int worldParts = 0;
     int gridColour = 0;           // co-resident blocks of the cooperative kernels
     int gridPgs = 0;
