@@ -633,36 +633,6 @@ JBD float ld_rw_w(const float4* p) {
     return v;
 }
 
-// While a thread solves one colour it prefetches into L1 the rows of its slot in the next step
-// (the next colour, or the cut colours after the part's colours): the slot's first-row word is
-// loaded at the start of the colour, the rows' lines are prefetched at its end.
-JBD void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
-JBD int next_z(const DevRows& R, int s, int s1) {
-    if (s >= s1) return -1;
-    int z;
-    asm volatile("ld.global.s32 %0, [%1];" : "=r"(z) : "l"((const int*)(R.slot_desc + s) + 2));
-    return z;
-}
-JBD void prefetch_rows(const DevRows& R, int kind, int z) {
-    if (z < 0) return;
-    const int npt = __popc(z & 15), p0 = z >> 4, p1 = p0 + npt - 1;
-    if (npt == 0) return;
-    if (kind != PH_FRICTION) {
-        prefetch_l1(R.n_nrm + p0); prefetch_l1(R.n_nrm + p1);
-        prefetch_l1(R.n_rp1 + p0); prefetch_l1(R.n_rp1 + p1);
-        prefetch_l1(R.n_rp2 + p0); prefetch_l1(R.n_rp2 + p1);
-    }
-    prefetch_l1(R.n_angA + p0); prefetch_l1(R.n_angA + p1);
-    prefetch_l1(R.n_angB + p0); prefetch_l1(R.n_angB + p1);
-    if (kind != PH_NORMAL) {
-        const int f0 = 2 * p0, f1 = 2 * p1 + 1;
-        prefetch_l1(R.f_nrm + f0); prefetch_l1(R.f_nrm + f1);
-        prefetch_l1(R.f_rp1 + f0); prefetch_l1(R.f_rp1 + f1);
-        prefetch_l1(R.f_rp2 + f0); prefetch_l1(R.f_rp2 + f1);
-        prefetch_l1(R.f_angA + f0); prefetch_l1(R.f_angA + f1);
-        prefetch_l1(R.f_angB + f0); prefetch_l1(R.f_angB + f1);
-    }
-}
 JBD float ld_ro_w(const float4* p) {
     float v;
     asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"((const float*)p + 3));
@@ -685,9 +655,18 @@ struct PointPool {
     int* top = nullptr;     // its fill counter (shared memory)
     int cap = 0;            // entries
 };
-struct PoolSlot {           // the entries one manifold took: its points 1.. are entries base..
+struct PoolSlot {           // the entries one manifold took: its point j >= j0 is entry j - j0
     const float4* e = nullptr;
+    int j0 = 1;
     bool waited = false;
+};
+
+// A thread's slot of the next step, staged during the current one: its descriptor and inverse
+// masses, and (pool permitting) all its points' rows in entries of the next step's pool.
+struct Staged {
+    int4 d = make_int4(0, 0, -1, 0);    // d.z < 0: nothing staged
+    float2 im = make_float2(0.0f, 0.0f);
+    const float4* e = nullptr;
 };
 
 JBD void cp_async16(void* dst, const void* src) {
@@ -696,14 +675,15 @@ JBD void cp_async16(void* dst, const void* src) {
 }
 JBD void cp_async_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-JBD PoolSlot pool_take(const PointPool& pp, const DevRows& R, int kind, int z) {
-    PoolSlot ps;
+// Copies the fields of phase `kind` of points j0.. of the manifold with first-row word z into
+// entries of pool pp; null when the pool has no room.
+JBD float4* pool_copy(const PointPool& pp, const DevRows& R, int kind, int z, int j0) {
     const int npt = __popc(z & 15), pt0 = z >> 4;
-    if (pp.cap == 0 || npt < 2 || kind == PH_WARM) return ps;
-    const int base = atomicAdd(pp.top, npt - 1);
-    if (base + npt - 1 > pp.cap) return ps;
+    if (pp.cap == 0 || npt <= j0 || kind == PH_WARM) return nullptr;
+    const int base = atomicAdd(pp.top, npt - j0);
+    if (base + npt - j0 > pp.cap) return nullptr;
     float4* e = pp.e + (size_t)base * POOL_F4;
-    for (int j = 1; j < npt; j++, e += POOL_F4) {
+    for (int j = j0; j < npt; j++, e += POOL_F4) {
         const int ni = pt0 + j;
         if (kind == PH_NORMAL) {
             cp_async16(e + 0, R.n_nrm + ni); cp_async16(e + 1, R.n_rp1 + ni); cp_async16(e + 2, R.n_rp2 + ni);
@@ -718,7 +698,11 @@ JBD PoolSlot pool_take(const PointPool& pp, const DevRows& R, int kind, int z) {
             }
         }
     }
-    ps.e = pp.e + (size_t)base * POOL_F4;
+    return pp.e + (size_t)base * POOL_F4;
+}
+JBD PoolSlot pool_take(const PointPool& pp, const DevRows& R, int kind, int z) {
+    PoolSlot ps;
+    ps.e = pool_copy(pp, R, kind, z, 1);
     return ps;
 }
 
@@ -731,9 +715,9 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int z, int k
     const int npt = __popc(z & 15), pt0 = z >> 4;
     for (int ni = pt0; ni < pt0 + npt; ni++) {
         const float4* pe = nullptr;     // this point's pool entry
-        if (ps.e && ni > pt0) {
+        if (ps.e && ni - pt0 >= ps.j0) {
             if (!ps.waited) { cp_async_wait(); ps.waited = true; }
-            pe = ps.e + (size_t)(ni - pt0 - 1) * POOL_F4;
+            pe = ps.e + (size_t)(ni - pt0 - ps.j0) * POOL_F4;
         }
         if (kind == PH_WARM) {
             float4 nn = R.n_nrm[ni];
@@ -910,15 +894,25 @@ JBD void res_keep(const SolverBuffers& sb, const ResCtl& rc, int kind, int s, co
 
 // One local colour of a part: its manifolds share no dynamic body; the part's bodies are in
 // shared memory (global memory when the part does not fit).
-// (s0n, s1n, kindn): the next step's slots, whose rows this thread prefetches.
+// st: this thread's first slot of the colour, staged by the previous step (d.z < 0: not
+// staged); on return, its slot sn of the next step (sn >= s1n: none), staged into poolNext.
 JBD void local_colour(const DevWorld& w, const DevRows& R, const SolverBuffers& sb, int s0, int s1, int kind, bool smem,
-                      float4* sl, float4* sa, const ResCtl& rc, int sn, int s1n, int kindn, const PointPool& pool) {
-    const int zn = next_z(R, sn, s1n);
+                      float4* sl, float4* sa, const ResCtl& rc, int sn, int s1n, int kindn, const PointPool& pool,
+                      const PointPool& poolNext, Staged& st) {
+    int4 dn = make_int4(0, 0, -1, 0);
+    float2 imn = make_float2(0.0f, 0.0f);
+    if (sn < s1n) { dn = R.slot_desc[sn]; imn = R.slot_im[sn]; }
     for (int s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-        if (res_skip(sb, rc, s)) continue;
-        const int4 d = R.slot_desc[s];
-        const float2 im = R.slot_im[s];
-        const PoolSlot ps = pool_take(pool, R, kind, d.z);
+        const bool pre = s == s0 + (int)threadIdx.x && st.d.z >= 0;
+        if (res_skip(sb, rc, s)) {
+            if (pre && st.e) cp_async_wait();   // staged copies complete before the pool is reused
+            continue;
+        }
+        const int4 d = pre ? st.d : R.slot_desc[s];
+        const float2 im = pre ? st.im : R.slot_im[s];
+        PoolSlot ps;
+        if (pre && st.e) { ps.e = st.e; ps.j0 = 0; }
+        else ps = pool_take(pool, R, kind, d.z);
         const int lb0 = d.w & 0xffff, lb1 = (d.w >> 16) & 0xffff;
         const bool m0 = smem && lb0 != 0xffff, m1 = smem && lb1 != 0xffff;
         V l0, a0, l1, a1;
@@ -931,7 +925,9 @@ JBD void local_colour(const DevWorld& w, const DevRows& R, const SolverBuffers& 
         if (im.x != 0.0f) { if (m0) { sl[lb0] = f4(l0, 0.0f); sa[lb0] = f4(a0, 0.0f); } else gstore(w, d.x, l0, a0); }
         if (im.y != 0.0f) { if (m1) { sl[lb1] = f4(l1, 0.0f); sa[lb1] = f4(a1, 0.0f); } else gstore(w, d.y, l1, a1); }
     }
-    prefetch_rows(R, kindn, zn);
+    st.d = dn;
+    st.im = imn;
+    st.e = dn.z >= 0 ? pool_copy(poolNext, R, kindn, dn.z, 0) : nullptr;
 }
 
 JBD bool resid_done(float dmax, float lmax, float tol) { return jdiv(dmax, lmax > 1e-6f ? lmax : 1e-6f) <= tol; }
@@ -997,17 +993,20 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
     const bool smem = sb.partSmem != 0;
     float4* sl = smv;
     float4* sa = smv + sb.smemCap;
-    __shared__ int shPoolTop[2];
+    // Three pools rotate over the colour steps: step c takes entries of pool c % 3 for its
+    // manifolds' later points and stages its next slots into pool (c + 1) % 3; thread 0 clears
+    // the counter of pool (c + 2) % 3 at the start of step c (its last users finished step c - 1,
+    // its next users stage at the end of step c + 1, after step c's barrier).
+    __shared__ int shPoolTop[3];
     float4* poolBase = smv + (smem ? 2 * sb.smemCap : 0);
-    // the pool of step c: entries pool(c).e, its counter cleared one step ahead
     auto pool = [&](int c) {
         PointPool pp;
         pp.cap = sb.poolPts;
-        pp.e = poolBase + (size_t)(c & 1) * sb.poolPts * POOL_F4;
-        pp.top = &shPoolTop[c & 1];
+        pp.e = poolBase + (size_t)(c % 3) * sb.poolPts * POOL_F4;
+        pp.top = &shPoolTop[c % 3];
         return pp;
     };
-    if (threadIdx.x < 2) shPoolTop[threadIdx.x] = 0;
+    if (threadIdx.x < 3) shPoolTop[threadIdx.x] = 0;
     const bool byRes = w.resTol > 0.0f;
     const int maxIt = byRes ? w.maxIter : w.numIter;
     // cut slot i of a colour goes to block i % gridDim.x, so a colour's manifolds spread over
@@ -1024,22 +1023,22 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             const bool psm = smem && v.np <= sb.smemCap;
             if (psm) stage_in(w, sb, v, sl, sa);
             __syncthreads();
-            // the step after (kind, c): the next colour, else colour 0 of the next phase
+            // (small world parts: the next steps' slots are not staged, their pools are too small
+            // for a block's manifolds and staging measured slower there)
             const int nl = v.nLoc;
-            auto run = [&](int kind, int c, int kindNext) {
-                const bool last = c + 1 == nl;
-                const int cn = last ? 0 : c + 1, kn = last ? kindNext : kind;
-                if (threadIdx.x == 0) shPoolTop[(step + 1) & 1] = 0;
-                local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc,
-                             kn < 0 ? 0 : v.lcs[cn] + (int)threadIdx.x, kn < 0 ? 0 : v.lcs[cn + 1], kn, pool(step));
+            Staged st;
+            auto run = [&](int kind, int c) {
+                if (threadIdx.x == 0) shPoolTop[(step + 2) % 3] = 0;
+                local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc, 0, 0, kind, pool(step),
+                             pool(step + 1), st);
                 __syncthreads();
                 ++step;
             };
-            for (int c = 0; c < nl; c++) run(PH_WARM, c, maxIt > 0 ? PH_NORMAL : -1);
+            for (int c = 0; c < nl; c++) run(PH_WARM, c);
             int it = 0;
             for (; it < maxIt && nl > 0; it++) {
-                for (int c = 0; c < nl; c++) run(PH_NORMAL, c, PH_FRICTION);
-                for (int c = 0; c < nl; c++) run(PH_FRICTION, c, it + 1 < maxIt ? PH_NORMAL : -1);
+                for (int c = 0; c < nl; c++) run(PH_NORMAL, c);
+                for (int c = 0; c < nl; c++) run(PH_FRICTION, c);
             }
             if (it > itMax) itMax = it;
             if (psm) stage_out(w, sb, v, sl, sa);
@@ -1052,6 +1051,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
     }
     if (nSlots == 0) return;
     if (tid == 0) for (int k = 0; k < 3; k++) w.ctr[C_RES0 + k] = 0;
+    Staged st;
     int it = -1;          // -1: the warm-start phase
     for (;;) {
         for (int sub = 0; sub < (it < 0 ? 1 : 2); sub++) {
@@ -1061,13 +1061,17 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                 const bool psm = smem && v.np <= sb.smemCap;
                 if (psm) stage_in(w, sb, v, sl, sa);
                 __syncthreads();
+                st = Staged();
+                const bool lastPart = part + (int)gridDim.x >= sb.nParts;
                 for (int c = 0; c < v.nLoc; c++) {
-                    // after the last colour: this thread's slot in cut colour 0
+                    // after the last colour of the block's last part: its slot in cut colour 0
                     const bool last = c + 1 == v.nLoc;
-                    const int sn = last ? (nCut > 0 ? sb.colourStart[0] + spread : 0) : v.lcs[c + 1] + (int)threadIdx.x;
-                    const int s1n = last ? (nCut > 0 ? sb.colourStart[1] : 0) : v.lcs[c + 2];
-                    if (threadIdx.x == 0) shPoolTop[(step + 1) & 1] = 0;
-                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc, sn, s1n, kind, pool(step));
+                    const bool toCut = last && lastPart && nCut > 0;
+                    const int sn = last ? (toCut ? sb.colourStart[0] + spread : 0) : v.lcs[c + 1] + (int)threadIdx.x;
+                    const int s1n = last ? (toCut ? sb.colourStart[1] : 0) : v.lcs[c + 2];
+                    if (threadIdx.x == 0) shPoolTop[(step + 2) % 3] = 0;
+                    local_colour(w, R, sb, v.lcs[c], v.lcs[c + 1], kind, psm, sl, sa, rc, sn, s1n, kind, pool(step),
+                                 pool(step + 1), st);
                     __syncthreads();
                     ++step;
                 }
@@ -1077,14 +1081,26 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
             grid_barrier(w.ctr, nb, barK);
             for (int c = 0; c < nCut; c++) {
                 const int s0 = sb.colourStart[c], s1 = sb.colourStart[c + 1];
-                const int zn = c + 1 < nCut ? next_z(R, sb.colourStart[c + 1] + spread, sb.colourStart[c + 2]) : -1;
-                if (threadIdx.x == 0) shPoolTop[(step + 1) & 1] = 0;
+                // this thread's slot of the next cut colour, loaded now and staged at the end
+                int4 dn = make_int4(0, 0, -1, 0);
+                float2 imn = make_float2(0.0f, 0.0f);
+                if (c + 1 < nCut && sb.colourStart[c + 1] + spread < sb.colourStart[c + 2]) {
+                    dn = R.slot_desc[sb.colourStart[c + 1] + spread];
+                    imn = R.slot_im[sb.colourStart[c + 1] + spread];
+                }
+                if (threadIdx.x == 0) shPoolTop[(step + 2) % 3] = 0;
                 const PointPool pp = pool(step);
                 for (int s = s0 + spread; s < s1; s += nth) {
-                    if (res_skip(sb, rc, s)) continue;
-                    const int4 d = R.slot_desc[s];
-                    const float2 im = R.slot_im[s];
-                    const PoolSlot ps = pool_take(pp, R, kind, d.z);
+                    const bool pre = s == s0 + spread && st.d.z >= 0;
+                    if (res_skip(sb, rc, s)) {
+                        if (pre && st.e) cp_async_wait();   // staged copies complete before the pool is reused
+                        continue;
+                    }
+                    const int4 d = pre ? st.d : R.slot_desc[s];
+                    const float2 im = pre ? st.im : R.slot_im[s];
+                    PoolSlot ps;
+                    if (pre && st.e) { ps.e = st.e; ps.j0 = 0; }
+                    else ps = pool_take(pp, R, kind, d.z);
                     V l0, a0, l1, a1;
                     gload(w, d.x, l0, a0);
                     gload(w, d.y, l1, a1);
@@ -1095,7 +1111,9 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                     if (im.x != 0.0f) gstore(w, d.x, l0, a0);
                     if (im.y != 0.0f) gstore(w, d.y, l1, a1);
                 }
-                prefetch_rows(R, kind, zn);
+                st.d = dn;
+                st.im = imn;
+                st.e = dn.z >= 0 ? pool_copy(pool(step + 1), R, kind, dn.z, 0) : nullptr;
                 grid_barrier(w.ctr, nb, barK);
                 ++step;
             }
@@ -1268,7 +1286,7 @@ template <class T> static cudaError_t salloc(T** p, size_t n) {
 template <class T> static void sfree(T*& p) { if (p) cudaFree((void*)p); p = nullptr; }
 
 static size_t pgs_smem(const SolverBuffers& sb) {
-    return (sb.partSmem ? (size_t)sb.smemCap * 32 : 0) + (size_t)2 * sb.poolPts * POOL_F4 * 16;
+    return (sb.partSmem ? (size_t)sb.smemCap * 32 : 0) + (size_t)3 * sb.poolPts * POOL_F4 * 16;
 }
 static size_t colour_smem(const SolverBuffers& sb) { return (size_t)sb.partMax * (sizeof(unsigned long long) + sizeof(int)); }
 
@@ -1326,12 +1344,14 @@ int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& wor
         cudaDeviceGetAttribute(&smemBlock, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
         cudaFuncSetAttribute(k_pgs, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBlock - 1024) != cudaSuccess)
         return JBGPU_ERR_CUDA;
-    // point pools: half a block's threads in entries, fewer (or none) if they would cost occupancy
+    // point pools: half a block's threads in entries (a quarter with world parts, whose blocks
+    // stage nothing ahead and keep more of the SM as L1), fewer or none if they would cost
+    // occupancy
     int perPgs = 0, perColour = 0, perBare = 0;
     sb.poolPts = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perBare, k_pgs, threads, pgs_smem(sb)) != cudaSuccess)
         return JBGPU_ERR_CUDA;
-    for (int pts = threads / 2; pts >= 16; pts /= 2) {
+    for (int pts = sb.worldParts ? threads / 4 : threads / 2; pts >= 16; pts /= 2) {
         sb.poolPts = pts;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perPgs, k_pgs, threads, pgs_smem(sb)) != cudaSuccess)
             return JBGPU_ERR_CUDA;
