@@ -336,12 +336,32 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
         int* lc = sb.lcCount + part * (MAX_LOCAL + 1);
         for (int i = threadIdx.x; i < np; i += blockDim.x) { shClaim[i] = ~0ull; shTaken[i] = -1; }
         if (threadIdx.x == 0) shDone = 0;
+        // a thread's first COL_REG candidates (k, local bodies, coloured) stay in registers
+        // through all passes; a part with more candidates than COL_REG x blockDim takes the rest
+        // from global memory
+        int ck[COL_REG], cl[COL_REG];
+        unsigned done = 0;
+#pragma unroll
+        for (int j = 0; j < COL_REG; j++) {
+            const int i = s0 + threadIdx.x + j * (int)blockDim.x;
+            ck[j] = i < s1 ? sb.bucketList[i] : -1;
+            cl[j] = ck[j] >= 0 ? sb.candLocal[ck[j]] : 0;
+        }
+        const int sx = s0 + COL_REG * (int)blockDim.x;   // first candidate of the global path
         __syncthreads();
         int r = 0;
         for (; r < MAX_LOCAL && shDone < s1 - s0; r++) {
             for (int sub = 0; sub < MAX_SUB; sub++) {
                 const int t = r * MAX_SUB + sub;
-                for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+#pragma unroll
+                for (int j = 0; j < COL_REG; j++) {
+                    const int k = ck[j], l0 = cl[j] & 0xffff, l1 = (cl[j] >> 16) & 0xffff;
+                    if (k < 0 || (done >> j & 1u) || (l0 != NONE && shTaken[l0] == r) || (l1 != NONE && shTaken[l1] == r))
+                        continue;
+                    if (l0 != NONE) atomicMin(&shClaim[l0], ctag(t, k));
+                    if (l1 != NONE) atomicMin(&shClaim[l1], ctag(t, k));
+                }
+                for (int i = sx + threadIdx.x; i < s1; i += blockDim.x) {
                     const int k = sb.bucketList[i], lb = sb.candLocal[k], l0 = lb & 0xffff, l1 = (lb >> 16) & 0xffff;
                     if (__ldcg(&sb.colourOf[k]) >= 0 || (l0 != NONE && shTaken[l0] == r) || (l1 != NONE && shTaken[l1] == r))
                         continue;
@@ -350,7 +370,22 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
                 }
                 if (threadIdx.x == 0) shWin = 0;
                 __syncthreads();
-                for (int i = s0 + threadIdx.x; i < s1; i += blockDim.x) {
+                int myWin = 0;
+#pragma unroll
+                for (int j = 0; j < COL_REG; j++) {
+                    const int k = ck[j], l0 = cl[j] & 0xffff, l1 = (cl[j] >> 16) & 0xffff;
+                    if (k < 0 || (done >> j & 1u) || (l0 != NONE && shTaken[l0] == r) || (l1 != NONE && shTaken[l1] == r))
+                        continue;
+                    const unsigned long long me = ctag(t, k);
+                    if ((l0 == NONE || shClaim[l0] == me) && (l1 == NONE || shClaim[l1] == me)) {
+                        sb.colourOf[k] = r;
+                        done |= 1u << j;
+                        if (l0 != NONE) shTaken[l0] = r;
+                        if (l1 != NONE) shTaken[l1] = r;
+                        myWin++;
+                    }
+                }
+                for (int i = sx + threadIdx.x; i < s1; i += blockDim.x) {
                     const int k = sb.bucketList[i], lb = sb.candLocal[k], l0 = lb & 0xffff, l1 = (lb >> 16) & 0xffff;
                     if (__ldcg(&sb.colourOf[k]) >= 0 || (l0 != NONE && shTaken[l0] == r) || (l1 != NONE && shTaken[l1] == r))
                         continue;
@@ -359,9 +394,11 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
                         sb.colourOf[k] = r;
                         if (l0 != NONE) shTaken[l0] = r;
                         if (l1 != NONE) shTaken[l1] = r;
-                        atomicAdd(&shWin, 1);
+                        myWin++;
                     }
                 }
+                myWin = __reduce_add_sync(0xffffffffu, myWin);
+                if ((threadIdx.x & 31) == 0 && myWin) atomicAdd(&shWin, myWin);
                 __syncthreads();
                 const int won = shWin;
                 if (threadIdx.x == 0) {
@@ -386,6 +423,23 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
     grid_barrier(w.ctr, nb, barK);
     const int c0 = sb.bucketStart[sb.nParts], c1 = sb.bucketStart[sb.nParts + 1];
     const int nCut = c1 - c0;
+    // a thread's first COL_REG cut candidates (k and its dynamic bodies, -1 for a static one)
+    // stay in registers through all passes; the rest come from global memory
+    int gk[COL_REG], gb0[COL_REG], gb1[COL_REG];
+    unsigned gdone = 0;
+#pragma unroll
+    for (int j = 0; j < COL_REG; j++) {
+        const int i = c0 + tid + j * nth;
+        gk[j] = i < c1 ? sb.bucketList[i] : -1;
+        gb0[j] = gb1[j] = -1;
+        if (gk[j] >= 0) {
+            const int p = sb.cand[gk[j]];
+            const int b0 = P.b0[p], b1 = P.b1[p];
+            gb0[j] = dyn(w, b0) ? b0 : -1;
+            gb1[j] = dyn(w, b1) ? b1 : -1;
+        }
+    }
+    const int cx = c0 + COL_REG * nth;   // first candidate of the global path
     int g = 0, round = 0;
     for (; round < MAX_COLOURS; round++) {
         if (__ldcg(&w.ctr[C_CUT_DONE]) >= nCut) break;
@@ -393,7 +447,16 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
         for (int sub = 0; sub < MAX_SUB; sub++, g++) {
             const int t = (MAX_LOCAL + 1 + round) * MAX_SUB + sub;
             if (tid == 0) w.ctr[C_WIN0 + (g + 1) % 3] = 0;
-            for (int i = c0 + tid; i < c1; i += nth) {
+            bool elig[COL_REG];
+#pragma unroll
+            for (int j = 0; j < COL_REG; j++) {
+                elig[j] = gk[j] >= 0 && !(gdone >> j & 1u) && (gb0[j] < 0 || __ldcg(&sb.taken[gb0[j]]) != mark) &&
+                          (gb1[j] < 0 || __ldcg(&sb.taken[gb1[j]]) != mark);
+                if (!elig[j]) continue;
+                if (gb0[j] >= 0) atomicMin(&sb.claim[gb0[j]], ctag(t, gk[j]));
+                if (gb1[j] >= 0) atomicMin(&sb.claim[gb1[j]], ctag(t, gk[j]));
+            }
+            for (int i = cx + tid; i < c1; i += nth) {
                 int k = sb.bucketList[i], b0, b1;
                 if (!eligible(w, P, sb, k, mark, b0, b1)) continue;
                 if (dyn(w, b0)) atomicMin(&sb.claim[b0], ctag(t, k));
@@ -401,7 +464,19 @@ __global__ void __launch_bounds__(SOLVER_THREADS) k_colour(DevWorld w, DevPairs 
             }
             grid_barrier(w.ctr, nb, barK);
             int won = 0;
-            for (int i = c0 + tid; i < c1; i += nth) {
+#pragma unroll
+            for (int j = 0; j < COL_REG; j++) {
+                if (!elig[j]) continue;   // taken marks only change after this pass's check
+                const unsigned long long me = ctag(t, gk[j]);
+                if ((gb0[j] < 0 || __ldcg(&sb.claim[gb0[j]]) == me) && (gb1[j] < 0 || __ldcg(&sb.claim[gb1[j]]) == me)) {
+                    sb.colourOf[gk[j]] = round;
+                    gdone |= 1u << j;
+                    if (gb0[j] >= 0) sb.taken[gb0[j]] = mark;
+                    if (gb1[j] >= 0) sb.taken[gb1[j]] = mark;
+                    won++;
+                }
+            }
+            for (int i = cx + tid; i < c1; i += nth) {
                 int k = sb.bucketList[i], b0, b1;
                 if (!eligible(w, P, sb, k, mark, b0, b1)) continue;
                 if (holds_claims(w, sb, b0, b1, ctag(t, k))) {

@@ -6,7 +6,8 @@ namespace jbg {
 
 constexpr int MAX_COLOURS = 1024;     // grid-wide colours of cut manifolds
 constexpr int MAX_LOCAL = 128;        // colours of the manifolds internal to one part
-constexpr int MAX_SUB = 16;           // claim passes that grow one colour towards a maximal set
+constexpr int MAX_SUB = 16;
+constexpr int COL_REG = 4;            // internal-colouring candidates a thread keeps in registers           // claim passes that grow one colour towards a maximal set
 constexpr int SOLVER_THREADS = 256;
 constexpr int PART_MAX_BODIES = 2048; // bodies of one part (velocities staged in 64 KB of shared memory)
 
