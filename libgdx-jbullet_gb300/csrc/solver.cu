@@ -269,7 +269,19 @@ __global__ void k_classify(DevWorld w, DevPairs P, SolverBuffers sb) {
         if (d1) lb1 = sb.posOf[b1] - ps;
     }
     sb.candLocal[k] = lb0 | (lb1 << 16);
-    atomicAdd(&sb.bucketCount[q], 1);
+    const unsigned grp = __match_any_sync(__activemask(), q);   // one atomic per bucket and warp
+    if ((threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&sb.bucketCount[q], __popc(grp));
+}
+
+// Fill position of a lane among the lanes of its warp with the same key: the group's leader
+// takes the group's places from *ctr with one atomic.
+JBD int group_take(int* ctr, int key) {
+    const unsigned grp = __match_any_sync(__activemask(), key);
+    const int lane = threadIdx.x & 31, leader = __ffs(grp) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(ctr, __popc(grp));
+    base = __shfl_sync(grp, base, leader);
+    return base + __popc(grp & ((1u << lane) - 1u));
 }
 
 __global__ void k_bucket_scatter(SolverBuffers sb) {
@@ -277,7 +289,7 @@ __global__ void k_bucket_scatter(SolverBuffers sb) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nCand) return;
     int b = sb.bucket[k];
-    sb.bucketList[sb.bucketStart[b] + atomicAdd(&sb.bucketFill[b], 1)] = k;
+    sb.bucketList[sb.bucketStart[b] + group_take(&sb.bucketFill[b], b)] = k;
 }
 
 // Blocks take parts largest first from a shared counter (ctr[counter], cleared before the
@@ -523,10 +535,10 @@ __global__ void k_slots(DevWorld w, DevPairs P, SolverBuffers sb, DevRows R) {
         int* fill = sb.lcFill + b * (MAX_LOCAL + 1);
         const int* st = sb.lcStart + b * (MAX_LOCAL + 1);
         if (c < 0) c = sb.nLocal[b];
-        slot = st[c] + atomicAdd(&fill[c], 1);
+        slot = st[c] + group_take(&fill[c], b * (MAX_LOCAL + 1) + c);
     } else {
         if (c < 0) c = *sb.nColours;
-        slot = sb.colourStart[c] + atomicAdd(&sb.colourFill[c], 1);
+        slot = sb.colourStart[c] + group_take(&sb.colourFill[c], -1 - c);
     }
     int p = sb.cand[k];
     R.slot_pair[slot] = p;
