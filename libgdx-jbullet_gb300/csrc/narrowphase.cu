@@ -36,9 +36,10 @@ JBD void manifold_refresh(Mf& m, const DevWorld& w, int mb0, int mb1) {
 // Pairs grouped by algorithm before the pass, so that the threads of a warp run the same code:
 // bucket 0 = nothing to do (both bodies inactive, or two planes), 1 convex-plane, 2 sphere-
 // sphere, then GJK pairs by shape kinds: 3 box-box, 4 with a sphere, 5 with a capsule, 6 with a
-// hull.  perm lists buckets 1..6 in order; the pass covers nPairs - count[0] entries.
-constexpr int NB_BUCKETS = 7;
-
+// hull, each split by whether the pair's manifold held points after the last step (7-10: the
+// same kinds, touching) - separated pairs mostly leave GJK after a few iterations, touching
+// ones converge on the contact, so a warp of either kind runs similar iteration counts.  perm
+// lists buckets 1..10 in order; the pass covers nPairs - count[0] entries.
 JBD int narrow_bucket(const DevWorld& w, const DevPairs& P, int p) {
     uint64_t key = P.keys[p];
     int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
@@ -48,10 +49,11 @@ JBD int narrow_bucket(const DevWorld& w, const DevPairs& P, int p) {
     if (t0 == SHAPE_PLANE && t1 == SHAPE_PLANE) return 0;
     if (t0 == SHAPE_PLANE || t1 == SHAPE_PLANE) return 1;
     if (t0 == SHAPE_SPHERE && t1 == SHAPE_SPHERE) return 2;
-    if (t0 == SHAPE_HULL || t1 == SHAPE_HULL) return 6;
-    if (t0 == SHAPE_CAPSULE || t1 == SHAPE_CAPSULE) return 5;
-    if (t0 == SHAPE_SPHERE || t1 == SHAPE_SPHERE) return 4;
-    return 3;
+    const int touching = P.has[p] && P.n[p] > 0 ? 4 : 0;
+    if (t0 == SHAPE_HULL || t1 == SHAPE_HULL) return 6 + touching;
+    if (t0 == SHAPE_CAPSULE || t1 == SHAPE_CAPSULE) return 5 + touching;
+    if (t0 == SHAPE_SPHERE || t1 == SHAPE_SPHERE) return 4 + touching;
+    return 3 + touching;
 }
 
 // Stable grouping: per block and bucket counts, laid out bucket-major with bucket 0 last, then

@@ -4,6 +4,8 @@
 
 namespace jbg {
 
+constexpr int NB_BUCKETS = 11;   // narrowphase algorithm buckets (pairs grouped by them)
+
 // EPA queue (the polytopes live in shared memory, one warp and one polytope per block).
 struct NarrowBuffers {
     void* queue = nullptr;        // EpaRec per queued pair (pair capacity)
@@ -13,7 +15,7 @@ struct NarrowBuffers {
     int* ovfCount = nullptr;
     unsigned char* pairBucket = nullptr;   // algorithm bucket per pair (pair capacity)
     int* perm = nullptr;          // pairs grouped by bucket (pair capacity)
-    int* blockOff = nullptr;      // per block and bucket counts, scanned in place (7 x pair blocks)
+    int* blockOff = nullptr;      // per block and bucket counts, scanned in place (NB_BUCKETS x pair blocks)
     bool group = true;            // group pairs by algorithm (worth it with two or more shape kinds)
     void* scanScratch = nullptr;  // scan scratch for blockOff
 };

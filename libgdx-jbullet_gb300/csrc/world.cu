@@ -167,7 +167,7 @@ int alloc_pair_work(jbgpu_world* w, int cap) {
     dfree(w->nb.ovfQueue); dfree(w->nb.pairBucket); dfree(w->nb.perm); dfree(w->nb.blockOff);
     CK(dalloc(&w->nb.ovfQueue, cap)); CK(dalloc(&w->nb.pairBucket, cap)); CK(dalloc(&w->nb.perm, cap));
     {
-        int nbk = 7 * ((cap + 255) / 256) + 1;
+        int nbk = NB_BUCKETS * ((cap + 255) / 256) + 1;
         CK(dalloc(&w->nb.blockOff, nbk));
         if (w->nb.scanScratch) cudaFree(w->nb.scanScratch);
         CK(cudaMalloc(&w->nb.scanScratch, scan_scratch_bytes(nbk)));
