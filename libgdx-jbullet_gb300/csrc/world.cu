@@ -300,7 +300,9 @@ int sync_planes(jbgpu_world* w) {
             kinds |= 1u << (w->shapes[w->hShape[i]].type & 31);
         }
     }
-    w->nb.group = __builtin_popcount(kinds) >= 2;
+    // grouping pays with two or more shape kinds, or with GJK pairs (split by contact state),
+    // once there are enough pairs to cover its two extra launches
+    w->nb.group = (__builtin_popcount(kinds) >= 2 || (kinds & ~(1u << SHAPE_SPHERE)) != 0) && nf >= 4096;
     std::vector<int> list, start(nw + 1, 0);
     for (int k = 0; k < nw; k++) { start[k] = (int)list.size(); list.insert(list.end(), per[k].begin(), per[k].end()); }
     start[nw] = (int)list.size();
