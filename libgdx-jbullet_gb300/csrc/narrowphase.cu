@@ -191,7 +191,7 @@ __global__ void k_narrow(DevWorld w, DevPairs P, int n, const int* perm, const i
 }
 
 // One queued pair, by the 32 lanes of a warp (see epa.cuh); lane 0 updates the manifold.  With
-// ovfQueue (the small-slot tier) a query that outgrows its slot leaves no result and is queued
+// ovfQueue (a reduced-capacity tier) a query that outgrows its slot leaves no result and is queued
 // for the tier with the full capacities: EPA is deterministic, so its result does not depend on
 // which tier finishes it.
 __device__ void epa_query(const DevWorld& w, DevPairs& P, const EpaRec* queue, int qi, const EpaSlot& sl, int lane,
@@ -262,44 +262,69 @@ constexpr size_t EPA_SMEM_BYTES = (size_t)EPA_FACE_CAP * (4 * sizeof(float4) + s
                                   (size_t)EPA_MKV_CAP * 2 * sizeof(float4) + (size_t)EPA_SEEN_CAP * sizeof(float4) +
                                   (size_t)EPA_STACK_CAP * sizeof(int2);
 
-// Small-slot tier: EPA_SMALL_WARPS warps per block, each with a polytope of reduced
-// capacities in shared memory; queries that outgrow them go to the overflow queue.
-constexpr int EPA_SMALL_WARPS = 4;
-constexpr int EPA_S_FACES = 192, EPA_S_MKV = 96, EPA_S_SEEN = 64, EPA_S_STACK = 384;
-constexpr size_t EPA_SMALL_SLOT_BYTES = (size_t)EPA_S_FACES * (4 * sizeof(float4) + sizeof(float)) +
-                                        (size_t)EPA_S_MKV * 2 * sizeof(float4) + (size_t)EPA_S_SEEN * sizeof(float4) +
-                                        (size_t)EPA_S_STACK * sizeof(int2);
-constexpr size_t EPA_SMALL_SMEM_BYTES = EPA_SMALL_WARPS * EPA_SMALL_SLOT_BYTES;
+// Reduced-capacity tiers: WARPS warps per block, each with a polytope of the given
+// capacities in shared memory, taking the queue (list == null) or the previous tier's overflow
+// list; queries that outgrow the slot go to this tier's overflow list.  Tier 1 (96 faces, 8
+// warps a block) finishes most queries at twice the warps per SM of tier 2 (192 faces, 4 warps).
+template <int FACES, int MKV, int SEEN, int STACK>
+struct EpaTier {
+    static constexpr size_t SLOT_BYTES = (size_t)FACES * (4 * sizeof(float4) + sizeof(float)) +
+                                         (size_t)MKV * 2 * sizeof(float4) + (size_t)SEEN * sizeof(float4) +
+                                         (size_t)STACK * sizeof(int2);
+};
+constexpr int EPA_T1_WARPS = 6, EPA_T2_WARPS = 4;
+constexpr int EPA_T1_SKIP_STEPS = 8;
+using EpaT1 = EpaTier<128, 64, 48, 256>;
+using EpaT2 = EpaTier<192, 96, 64, 384>;
+constexpr size_t EPA_T1_SMEM_BYTES = EPA_T1_WARPS * EpaT1::SLOT_BYTES;
+constexpr size_t EPA_T2_SMEM_BYTES = EPA_T2_WARPS * EpaT2::SLOT_BYTES;
 
-__global__ void __launch_bounds__(32 * EPA_SMALL_WARPS) k_narrow_epa_small(DevWorld w, DevPairs P, const EpaRec* queue,
-                                                                            const int* queueCount, int* ovfQueue,
-                                                                            int* ovfCount) {
+// Tier 1 runs only for a queue longer than tier 2's warps (else its extra warps buy nothing and
+// its overflow would be solved twice on the critical path) and while mode (device) is 0; k > 0
+// skips it for k more steps, set after a step in which it left more than a third of its queue
+// to tier 2.  When tier 1 is skipped, tier 2 takes the queue.
+template <int WARPS, int FACES, int MKV, int SEEN, int STACK>
+__global__ void __launch_bounds__(32 * WARPS) k_narrow_epa_tier(DevWorld w, DevPairs P, const EpaRec* queue,
+                                                                const int* list, const int* count, int* ovfQueue,
+                                                                int* ovfCount, const int* mode, const int* queueCount,
+                                                                int tier2Warps) {
     extern __shared__ float4 epaSmem[];
-    const int n = *queueCount;
+    const bool skipped = *mode != 0 || *queueCount <= tier2Warps;   // tier 1 is skipped this step
+    if (!list && skipped) return;           // this is tier 1
+    if (list && skipped) { list = nullptr; count = queueCount; }   // tier 2 takes the queue
+    const int n = *count;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     EpaSlot sl;
-    sl.fN = (float4*)((unsigned char*)epaSmem + warp * EPA_SMALL_SLOT_BYTES);
-    sl.fV = (int4*)(sl.fN + EPA_S_FACES);
-    sl.fF = sl.fV + EPA_S_FACES;
-    sl.fE = sl.fF + EPA_S_FACES;
-    sl.mW = (float4*)(sl.fE + EPA_S_FACES);
-    sl.mR = sl.mW + EPA_S_MKV;
-    sl.seen = sl.mR + EPA_S_MKV;
-    sl.stack = (int2*)(sl.seen + EPA_S_SEEN);
-    sl.fD = (float*)(sl.stack + EPA_S_STACK);
-    sl.faceCap = EPA_S_FACES;
-    sl.mkvCap = EPA_S_MKV;
-    sl.seenCap = EPA_S_SEEN;
-    sl.stackCap = EPA_S_STACK;
-    const int gw = blockIdx.x * EPA_SMALL_WARPS + warp, nw = gridDim.x * EPA_SMALL_WARPS;
-    for (int qi = gw; qi < n; qi += nw) epa_query(w, P, queue, qi, sl, lane, ovfQueue, ovfCount);
+    sl.fN = (float4*)((unsigned char*)epaSmem + warp * EpaTier<FACES, MKV, SEEN, STACK>::SLOT_BYTES);
+    sl.fV = (int4*)(sl.fN + FACES);
+    sl.fF = sl.fV + FACES;
+    sl.fE = sl.fF + FACES;
+    sl.mW = (float4*)(sl.fE + FACES);
+    sl.mR = sl.mW + MKV;
+    sl.seen = sl.mR + MKV;
+    sl.stack = (int2*)(sl.seen + SEEN);
+    sl.fD = (float*)(sl.stack + STACK);
+    sl.faceCap = FACES;
+    sl.mkvCap = MKV;
+    sl.seenCap = SEEN;
+    sl.stackCap = STACK;
+    const int gw = blockIdx.x * WARPS + warp, nw = gridDim.x * WARPS;
+    for (int j = gw; j < n; j += nw) epa_query(w, P, queue, list ? list[j] : j, sl, lane, ovfQueue, ovfCount);
 }
+#define EPA_T1_KERNEL k_narrow_epa_tier<EPA_T1_WARPS, 128, 64, 48, 256>
+#define EPA_T2_KERNEL k_narrow_epa_tier<EPA_T2_WARPS, 192, 96, 64, 384>
 
-// Full-capacity tier over the queries the small tier could not finish.
+
+// Full-capacity tier over the queries the 192-face tier could not finish.
+// c: the tier counters (c[0] counts list); block 0 also sets the tier mode of the next step.
 __global__ void __launch_bounds__(32) k_narrow_epa_smem(DevWorld w, DevPairs P, const EpaRec* queue, const int* list,
-                                                       const int* listCount) {
+                                                       int* c, const int* queueCount, int tier2Warps) {
     extern __shared__ float4 epaSmem[];
-    int n = *listCount;
+    int n = c[0];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const int q = *queueCount, m = c[2];
+        c[2] = m > 0 ? m - 1 : ((q > tier2Warps && 3 * c[1] > q) ? EPA_T1_SKIP_STEPS : 0);
+    }
     EpaSlot sl;
     sl.fN = epaSmem;
     sl.fV = (int4*)(sl.fN + EPA_FACE_CAP);
@@ -343,11 +368,17 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
     }
     if (prof) { prof->mark(PH_NARROW, 1, s); prof->mark(PH_EPA, 0, s); }
     if (nPairs > 0) {
-        cudaMemsetAsync(nb.ovfCount, 0, sizeof(int), s);
-        k_narrow_epa_small<<<nb.slots, 32 * EPA_SMALL_WARPS, EPA_SMALL_SMEM_BYTES, s>>>(
-            w, P, (const EpaRec*)nb.queue, nb.queueCount, nb.ovfQueue, nb.ovfCount);
+        cudaMemsetAsync(nb.ovfCount, 0, sizeof(int) * 2, s);
+        EPA_T1_KERNEL<<<nb.slots, 32 * EPA_T1_WARPS, EPA_T1_SMEM_BYTES, s>>>(
+            w, P, (const EpaRec*)nb.queue, nullptr, nb.queueCount, nb.ovfQueue2, nb.ovfCount + 1, nb.ovfCount + 2,
+            nb.queueCount, nb.slots * EPA_T2_WARPS);
         note_launch();
-        k_narrow_epa_smem<<<nb.slots, 32, EPA_SMEM_BYTES, s>>>(w, P, (const EpaRec*)nb.queue, nb.ovfQueue, nb.ovfCount);
+        EPA_T2_KERNEL<<<nb.slots, 32 * EPA_T2_WARPS, EPA_T2_SMEM_BYTES, s>>>(
+            w, P, (const EpaRec*)nb.queue, nb.ovfQueue2, nb.ovfCount + 1, nb.ovfQueue, nb.ovfCount, nb.ovfCount + 2,
+            nb.queueCount, nb.slots * EPA_T2_WARPS);
+        note_launch();
+        k_narrow_epa_smem<<<nb.slots, 32, EPA_SMEM_BYTES, s>>>(w, P, (const EpaRec*)nb.queue, nb.ovfQueue, nb.ovfCount,
+                                                                nb.queueCount, nb.slots * EPA_T2_WARPS);
         note_launch();
     }
     if (prof) prof->mark(PH_EPA, 1, s);
@@ -358,8 +389,10 @@ size_t epa_queue_record_bytes() { return sizeof(EpaRec); }
 int narrowphase_configure() {
     return (cudaFuncSetAttribute(k_narrow_epa_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EPA_SMEM_BYTES) ==
                 cudaSuccess &&
-            cudaFuncSetAttribute(k_narrow_epa_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)EPA_SMALL_SMEM_BYTES) == cudaSuccess) ? 0 : 1;
+            cudaFuncSetAttribute(EPA_T1_KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EPA_T1_SMEM_BYTES) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(EPA_T2_KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EPA_T2_SMEM_BYTES) ==
+                cudaSuccess) ? 0 : 1;
 }
 
 // ---- EPA pass on scratch compiled into the library ----------------------------------------

@@ -11,8 +11,9 @@ struct NarrowBuffers {
     void* queue = nullptr;        // EpaRec per queued pair (pair capacity)
     int* queueCount = nullptr;
     int slots = 0;                // EPA blocks, striding over the queue
-    int* ovfQueue = nullptr;      // queries the small-slot tier left to the full-capacity tier
-    int* ovfCount = nullptr;
+    int* ovfQueue = nullptr;      // queries the 192-face tier left to the full-capacity tier
+    int* ovfCount = nullptr;      // 3 ints: that list's count, ovfQueue2's count, the tier mode
+    int* ovfQueue2 = nullptr;     // queries the 96-face tier left to the 192-face tier
     unsigned char* pairBucket = nullptr;   // algorithm bucket per pair (pair capacity)
     int* perm = nullptr;          // pairs grouped by bucket (pair capacity)
     int* blockOff = nullptr;      // per block and bucket counts, scanned in place (NB_BUCKETS x pair blocks)

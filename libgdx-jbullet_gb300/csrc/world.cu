@@ -164,8 +164,9 @@ int alloc_pair_work(jbgpu_world* w, int cap) {
     CK(cudaMalloc(&S.scanScratch, scan_scratch_bytes(cap)));
     if (w->nb.queue) cudaFree(w->nb.queue);
     CK(cudaMalloc(&w->nb.queue, epa_queue_record_bytes() * (size_t)std::max(cap, 1)));
-    dfree(w->nb.ovfQueue); dfree(w->nb.pairBucket); dfree(w->nb.perm); dfree(w->nb.blockOff);
-    CK(dalloc(&w->nb.ovfQueue, cap)); CK(dalloc(&w->nb.pairBucket, cap)); CK(dalloc(&w->nb.perm, cap));
+    dfree(w->nb.ovfQueue); dfree(w->nb.ovfQueue2); dfree(w->nb.pairBucket); dfree(w->nb.perm); dfree(w->nb.blockOff);
+    CK(dalloc(&w->nb.ovfQueue, cap)); CK(dalloc(&w->nb.ovfQueue2, cap)); CK(dalloc(&w->nb.pairBucket, cap));
+    CK(dalloc(&w->nb.perm, cap));
     {
         int nbk = NB_BUCKETS * ((cap + 255) / 256) + 1;
         CK(dalloc(&w->nb.blockOff, nbk));
@@ -674,7 +675,8 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
              N.slots = w->sms * 2;
              if (narrowphase_configure()) return fail(JBGPU_ERR_CUDA, "EPA shared-memory size");
              CK(dalloc(&N.queueCount, 1));
-             CK(dalloc(&N.ovfCount, 1));
+             CK(dalloc(&N.ovfCount, 3));
+             CK(cudaMemset(N.ovfCount, 0, sizeof(int) * 3));
 
              return grow_bodies(w, std::max(1, c.initial_body_capacity));
          }()) != JBGPU_OK) {
@@ -714,7 +716,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.cursor); dfree(B.total); dfree(B.partners);
     NarrowBuffers& N = w->nb;
     if (N.queue) cudaFree(N.queue);
-    dfree(N.queueCount); dfree(N.ovfQueue); dfree(N.ovfCount); dfree(N.pairBucket); dfree(N.perm); dfree(N.blockOff);
+    dfree(N.queueCount); dfree(N.ovfQueue); dfree(N.ovfQueue2); dfree(N.ovfCount); dfree(N.pairBucket); dfree(N.perm); dfree(N.blockOff);
     if (N.scanScratch) cudaFree(N.scanScratch);
     SolverBuffers& V = w->sb;
     dfree(V.parent); dfree(V.keepAwake); dfree(V.inactive); dfree(V.flag); dfree(V.candIdx); dfree(V.cand); dfree(V.colourOf);
