@@ -142,9 +142,10 @@ __global__ void k_refit(DevWorld w, const int* sortedBody, int nf, Bvh t) {
         const int side = t.left[node] == child ? 0 : 2;
         __stcg(&t.node[4 * node + side], make_float4(mn.x, mn.y, mn.z, __int_as_float(child)));
         __stcg(&t.node[4 * node + side + 1], make_float4(mx.x, mx.y, mx.z, __int_as_float(last)));
-        __threadfence();
-        if (atomicAdd(&t.visit[node], 1) == 0) return;
-        __threadfence();
+        // release: this child's record; acquire: the sibling's (the second arrival goes on)
+        int prev;
+        asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(prev) : "l"(t.visit + node) : "memory");
+        if (prev == 0) return;
         const float4 l0 = __ldcg(&t.node[4 * node]), l1 = __ldcg(&t.node[4 * node + 1]);
         const float4 r0 = __ldcg(&t.node[4 * node + 2]), r1 = __ldcg(&t.node[4 * node + 3]);
         mn = make_float4(fminf(l0.x, r0.x), fminf(l0.y, r0.y), fminf(l0.z, r0.z), 0.0f);
