@@ -19,7 +19,7 @@ struct Bvh {           // Karras radix tree over nf sorted leaves; internal node
     float4* node;
 };
 
-constexpr int TRAV_CACHE = 16;         // pairs a counting traversal keeps for the filling one
+constexpr int TRAV_CACHE = 32;         // pairs a counting traversal keeps for the filling one
 
 struct BroadphaseBuffers {
     int nFinite = 0, nPlanes = 0, nWorlds = 1, worldBits = 0;
