@@ -14,6 +14,8 @@
 //   carried over.
 // Static planes (infinite aabb, StaticPlaneShape.java:124-128) stay out of the tree; each
 // finite body tests the planes of its world directly.
+#include <utility>
+
 #include "broadphase.cuh"
 #include "prims.cuh"
 
@@ -271,12 +273,18 @@ __global__ void k_segment_sort(int n, const int* off, const int* cnt, int* partn
     }
 }
 
-// Carry manifolds of persisting pairs (binary search in last step's sorted keys).
-__global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int nOld) {
+// Carry manifolds of persisting pairs (binary search in last step's sorted keys: within the
+// owner's segment when last step's per-owner offsets are at hand, else over all of them).
+__global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int nOld, const int* offPrev) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nNew) return;
     uint64_t key = nw.keys[p];
     int lo = 0, hi = nOld - 1, found = -1;
+    if (offPrev) {
+        const int o = (int)(key >> 32);
+        lo = offPrev[o];
+        hi = min(offPrev[o + 1], nOld) - 1;
+    }
     while (lo <= hi) {
         int mid = (lo + hi) >> 1;
         uint64_t k = old.keys[mid];
@@ -370,8 +378,14 @@ void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw,
     k_segment_sort<<<gridn(n, 128), 128, 0, s>>>(n, bb.off, bb.cursor, bb.partners, nw.keys, capacity); note_launch();
 }
 
-void broadphase_persist(const DevWorld& w, DevPairs& nw, const DevPairs& old, int nNew, int nOld, cudaStream_t s) {
-    if (nNew > 0) { k_persist<<<gridn(nNew, 256), 256, 0, s>>>(w, nw, old, nNew, nOld); note_launch(); }
+void broadphase_persist(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, const DevPairs& old, int nNew, int nOld,
+                        cudaStream_t s) {
+    if (nNew > 0) {
+        k_persist<<<gridn(nNew, 256), 256, 0, s>>>(w, nw, old, nNew, nOld, bb.offPrevValid ? bb.offPrev : nullptr);
+        note_launch();
+    }
+    std::swap(bb.off, bb.offPrev);   // this step's offsets index the pair array the next step persists from
+    bb.offPrevValid = true;
 }
 
 }  // namespace jbg

@@ -41,6 +41,8 @@ struct BroadphaseBuffers {
     int* planeStart = nullptr;           // nWorlds + 1 offsets into planeList
     int* cnt = nullptr;                  // pairs per owner (n + 1)
     int* off = nullptr;                  // exclusive scan of cnt (n + 1); off[n] = total
+    int* offPrev = nullptr;              // last step's off: the old pairs of owner o are [offPrev[o], offPrev[o + 1])
+    bool offPrevValid = false;           // offPrev matches the previous pair array
     int* cursor = nullptr;               // fill cursors (n + 1)
     int* total = nullptr;                // device total pair count
     int* partners = nullptr;             // CSR partner lists (pair capacity)
@@ -50,6 +52,7 @@ struct BroadphaseBuffers {
 
 void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s);
 void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, int capacity, cudaStream_t s);
-void broadphase_persist(const DevWorld& w, DevPairs& nw, const DevPairs& old, int nNew, int nOld, cudaStream_t s);
+void broadphase_persist(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, const DevPairs& old, int nNew, int nOld,
+                        cudaStream_t s);
 
 }  // namespace jbg

@@ -195,13 +195,14 @@ int grow_bodies(jbgpu_world* w, int need) {
     BroadphaseBuffers& B = w->bb;
     dfree(B.mkeys); dfree(B.mkeys_alt); dfree(B.sortedBody); dfree(B.vals_alt);
     dfree(B.bvh.left); dfree(B.bvh.right); dfree(B.bvh.lo); dfree(B.bvh.hi); dfree(B.bvh.parent); dfree(B.bvh.leafParent);
-    dfree(B.bvh.visit); dfree(B.bvh.node); dfree(B.cnt); dfree(B.off); dfree(B.cursor);
+    dfree(B.bvh.visit); dfree(B.bvh.node); dfree(B.cnt); dfree(B.off); dfree(B.offPrev); dfree(B.cursor);
+    B.offPrevValid = false;
     dfree(B.tcount); dfree(B.tcache);
     CK(dalloc(&B.mkeys, nc)); CK(dalloc(&B.mkeys_alt, nc)); CK(dalloc(&B.sortedBody, nc)); CK(dalloc(&B.vals_alt, nc));
     CK(dalloc(&B.bvh.left, nc)); CK(dalloc(&B.bvh.right, nc)); CK(dalloc(&B.bvh.lo, nc)); CK(dalloc(&B.bvh.hi, nc));
     CK(dalloc(&B.bvh.parent, nc)); CK(dalloc(&B.bvh.leafParent, nc)); CK(dalloc(&B.bvh.visit, nc));
     CK(dalloc(&B.bvh.node, 4 * (size_t)nc)); CK(dalloc(&B.tcount, nc)); CK(dalloc(&B.tcache, (size_t)TRAV_CACHE * nc));
-    CK(dalloc(&B.cnt, nc + 1)); CK(dalloc(&B.off, nc + 1)); CK(dalloc(&B.cursor, nc + 1));
+    CK(dalloc(&B.cnt, nc + 1)); CK(dalloc(&B.off, nc + 1)); CK(dalloc(&B.offPrev, nc + 1)); CK(dalloc(&B.cursor, nc + 1));
     if (B.sortScratch) cudaFree(B.sortScratch);
     CK(cudaMalloc(&B.sortScratch, sort_scratch_bytes(nc)));
     if (B.scanScratch) cudaFree(B.scanScratch);
@@ -361,7 +362,7 @@ int stage_pairs(jbgpu_world* w) {
     if (rc) return rc;
     w->prof.mark(PH_PAIR_FILL, 0, s);
     broadphase_run_fill(d, w->bb, w->pairs[nxt], w->capRows, s);
-    broadphase_persist(d, w->pairs[nxt], w->pairs[w->cur], total, w->nPairs, s);
+    broadphase_persist(d, w->bb, w->pairs[nxt], w->pairs[w->cur], total, w->nPairs, s);
     w->prof.mark(PH_PAIR_FILL, 1, s);
     w->cur = nxt;
     w->nPairs = total;
@@ -713,7 +714,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     if (B.scanScratch) cudaFree(B.scanScratch);
     dfree(B.bvh.left); dfree(B.bvh.right); dfree(B.bvh.lo); dfree(B.bvh.hi); dfree(B.bvh.parent); dfree(B.bvh.leafParent);
     dfree(B.bvh.visit); dfree(B.bvh.node); dfree(B.tcount); dfree(B.tcache); dfree(B.wstart); dfree(B.wend); dfree(B.wroot);
-    dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.cursor); dfree(B.total); dfree(B.partners);
+    dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.offPrev); dfree(B.cursor); dfree(B.total); dfree(B.partners);
     NarrowBuffers& N = w->nb;
     if (N.queue) cudaFree(N.queue);
     dfree(N.queueCount); dfree(N.ovfQueue); dfree(N.ovfQueue2); dfree(N.ovfCount); dfree(N.pairBucket); dfree(N.perm); dfree(N.blockOff);
@@ -822,6 +823,7 @@ int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, 
     }
     int rc = grow_bodies(w, w->nBodies + n);
     if (rc) return rc;
+    w->bb.offPrevValid = false;   // last step's per-owner offsets cover the old bodies only
     rc = sync_shapes(w);
     if (rc) return rc;
     std::vector<float4> xr0(n), xr1(n), xr2(n), lv(n), av(n), iloc(n), grav(n), zero(n, make_float4(0, 0, 0, 0));
@@ -1236,6 +1238,7 @@ int jbgpu_world_set_manifolds(jbgpu_world* w, const jbgpu_manifolds* m) {
     }
     CK(cudaStreamSynchronize(s));
     w->nPairs = np;
+    w->bb.offPrevValid = false;   // the per-owner offsets of the pair array are unknown
     return JBGPU_OK;
 }
 
