@@ -338,6 +338,10 @@ int jbgpu_world_set_profiling(jbgpu_world* world, int32_t max_steps);   /* 0 tur
 int jbgpu_world_phase_times(jbgpu_world* world, double* ms, int32_t n_phases, int32_t* steps);
 /* The step counters of each profiled step (pairs, contacts, solver rows, ...). */
 int jbgpu_world_profile_counters(jbgpu_world* world, jbgpu_counters* per_step, int32_t capacity, int32_t* steps);
+/* Device timer on the world's stream (no counterpart in the reference; measurement): mark 0
+ * records the start event; mark 1 records the end event, waits for it and writes the device
+ * milliseconds between the two into *ms. */
+int jbgpu_world_timer(jbgpu_world* world, int32_t mark, double* ms);
 
 #ifdef __cplusplus
 }

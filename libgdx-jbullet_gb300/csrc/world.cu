@@ -79,6 +79,7 @@ struct jbgpu_world {
     cudaStream_t stream = nullptr;
     cudaStream_t aux = nullptr;       // second stream: island unions beside the narrowphase
     cudaEvent_t evFork = nullptr, evJoin = nullptr;
+    cudaEvent_t evT0 = nullptr, evT1 = nullptr;   // jbgpu_world_timer
     float localTime = 1.0f / 60.0f;
     long long steps = 0;
     // shapes
@@ -641,7 +642,8 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
     if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&w->aux, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&w->evFork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&w->evJoin, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&w->evJoin, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreate(&w->evT0) != cudaSuccess || cudaEventCreate(&w->evT1) != cudaSuccess) {
         jbgpu_world_destroy(w);
         return fail(JBGPU_ERR_CUDA, "stream");
     }
@@ -738,6 +740,8 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(w->sampleT);
     if (w->evFork) cudaEventDestroy(w->evFork);
     if (w->evJoin) cudaEventDestroy(w->evJoin);
+    if (w->evT0) cudaEventDestroy(w->evT0);
+    if (w->evT1) cudaEventDestroy(w->evT1);
     if (w->aux) cudaStreamDestroy(w->aux);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
@@ -1016,6 +1020,21 @@ int jbgpu_world_get_samples(jbgpu_world* w, float* x, float* t, int32_t capacity
     }
     *n = cnt;
     if (cnt > capacity && x && t) return fail(JBGPU_ERR_CAPACITY, "sample buffer too small");
+    return JBGPU_OK;
+}
+
+int jbgpu_world_timer(jbgpu_world* w, int32_t mark, double* ms) {
+    if (!w || (mark != 0 && mark != 1) || (mark == 1 && !ms)) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
+    CK(cudaSetDevice(w->device));
+    if (mark == 0) {
+        CK(cudaEventRecord(w->evT0, w->stream));
+        return JBGPU_OK;
+    }
+    CK(cudaEventRecord(w->evT1, w->stream));
+    CK(cudaEventSynchronize(w->evT1));
+    float t = 0.0f;
+    CK(cudaEventElapsedTime(&t, w->evT0, w->evT1));
+    *ms = t;
     return JBGPU_OK;
 }
 

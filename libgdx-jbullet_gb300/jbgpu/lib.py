@@ -55,6 +55,7 @@ def lib():
             "jbgpu_world_apply_forces": ([C.c_void_p, _abi.f32p, _abi.f32p], C.c_int),
             "jbgpu_world_get_transforms": ([C.c_void_p, _abi.f32p], C.c_int),
             "jbgpu_world_set_profiling": ([C.c_void_p, C.c_int32], C.c_int),
+            "jbgpu_world_timer": ([C.c_void_p, C.c_int32, C.POINTER(C.c_double)], C.c_int),
             "jbgpu_world_phase_times": ([C.c_void_p, P(C.c_double), C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_profile_counters": ([C.c_void_p, P(_abi.Counters), C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_narrowphase_static": ([C.c_void_p, C.c_int32], C.c_int),
@@ -86,7 +87,7 @@ EXPORTED = [
     "jbgpu_world_synchronize", "jbgpu_world_get_state", "jbgpu_world_set_state", "jbgpu_world_get_pairs",
     "jbgpu_world_get_manifolds", "jbgpu_world_set_manifolds", "jbgpu_world_get_solver_order", "jbgpu_world_counters",
     "jbgpu_world_apply_forces", "jbgpu_world_get_transforms", "jbgpu_world_set_profiling", "jbgpu_world_phase_times",
-    "jbgpu_world_profile_counters",
+    "jbgpu_world_profile_counters", "jbgpu_world_timer",
 ]
 
 
@@ -286,6 +287,16 @@ class GpuWorld:
 
     def set_profiling(self, max_steps):
         check(lib().jbgpu_world_set_profiling(self.h, max_steps))
+
+    def timer_start(self):
+        """Records the device timer's start event on the world's stream."""
+        check(lib().jbgpu_world_timer(self.h, 0, None))
+
+    def timer_stop(self):
+        """Device milliseconds since timer_start (records the end event and waits for it)."""
+        ms = C.c_double(0.0)
+        check(lib().jbgpu_world_timer(self.h, 1, C.byref(ms)))
+        return ms.value
 
     def phase_times(self):
         """({phase: total device ms}, profiled steps, whole-window device ms)."""
