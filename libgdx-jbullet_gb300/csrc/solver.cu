@@ -736,6 +736,9 @@ JBD float ld_ro_w(const float4* p) {
 // f_nrm, f_rp1, f_rp2, f_angA, f_angB.  Two pools alternate between consecutive colours; when
 // a pool is full the points are read from global memory.
 constexpr int POOL_F4 = 12;
+// entry size of a phase: a normal-phase entry holds 5 float4, so a pool holds 12/5 as many
+JBD int pool_stride(int kind) { return kind == PH_NORMAL ? 5 : POOL_F4; }
+JBD int pool_entries(int cap, int kind) { return kind == PH_NORMAL ? cap * POOL_F4 / 5 : cap; }
 
 struct PointPool {
     float4* e = nullptr;    // this colour's pool (POOL_F4 float4 per entry)
@@ -768,9 +771,10 @@ JBD float4* pool_copy(const PointPool& pp, const DevRows& R, int kind, int z, in
     const int npt = __popc(z & 15), pt0 = z >> 4;
     if (pp.cap == 0 || npt <= j0 || kind == PH_WARM) return nullptr;
     const int base = atomicAdd(pp.top, npt - j0);
-    if (base + npt - j0 > pp.cap) return nullptr;
-    float4* e = pp.e + (size_t)base * POOL_F4;
-    for (int j = j0; j < npt; j++, e += POOL_F4) {
+    if (base + npt - j0 > pool_entries(pp.cap, kind)) return nullptr;
+    const int es = pool_stride(kind);
+    float4* e = pp.e + (size_t)base * es;
+    for (int j = j0; j < npt; j++, e += es) {
         const int ni = pt0 + j;
         if (kind == PH_NORMAL) {
             cp_async16(e + 0, R.n_nrm + ni); cp_async16(e + 1, R.n_rp1 + ni); cp_async16(e + 2, R.n_rp2 + ni);
@@ -785,7 +789,7 @@ JBD float4* pool_copy(const PointPool& pp, const DevRows& R, int kind, int z, in
             }
         }
     }
-    return pp.e + (size_t)base * POOL_F4;
+    return pp.e + (size_t)base * es;
 }
 JBD PoolSlot pool_take(const PointPool& pp, const DevRows& R, int kind, int z) {
     PoolSlot ps;
@@ -804,7 +808,7 @@ JBD void solve_manifold(const DevWorld& w, const DevRows& R, int s, int z, int k
         const float4* pe = nullptr;     // this point's pool entry
         if (ps.e && ni - pt0 >= ps.j0) {
             if (!ps.waited) { cp_async_wait(); ps.waited = true; }
-            pe = ps.e + (size_t)(ni - pt0 - ps.j0) * POOL_F4;
+            pe = ps.e + (size_t)(ni - pt0 - ps.j0) * pool_stride(kind);
         }
         if (kind == PH_WARM) {
             float4 nn = R.n_nrm[ni];
