@@ -110,7 +110,7 @@ __global__ void k_narrow_scatter(int nPairs, const unsigned char* bucket, const 
 JBD int narrow_active(const int* blockOff, int nBlocks) { return blockOff[(NB_BUCKETS - 1) * nBlocks]; }
 
 // With perm: n = the grouping's pair blocks and entry i is pair perm[i]; without: n = pairs.
-__global__ void k_narrow(DevWorld w, DevPairs P, int n, const int* perm, const int* blockOff, EpaRec* queue,
+__global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n, const int* perm, const int* blockOff, EpaRec* queue,
                          int* queueCount) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (perm ? narrow_active(blockOff, n) : n)) return;
