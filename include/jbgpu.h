@@ -307,6 +307,23 @@ int jbgpu_world_set_sample_logging(jbgpu_world* world, int32_t on);
  * islands that reached the residual are samples. */
 int jbgpu_world_get_samples(jbgpu_world* world, float* x, float* t, int32_t capacity, int32_t* n);
 
+/* Point-to-point (ball-socket) joint: DiscreteDynamicsWorld.addConstraint(new
+ * Point2PointConstraint(rbA, rbB, pivotInA, pivotInB), false)
+ * (dynamics/constraintsolver/Point2PointConstraint.java:37-171, DiscreteDynamicsWorld.java:515-521).
+ * body_b = -1 is TypedConstraint's fixed body (static, at the origin; the reference's
+ * one-body constructor passes pivotInB = rbA's transform applied to pivotInA).  Joints join
+ * islands (DiscreteDynamicsWorld.java:649-677) and are solved in every iteration before the
+ * contact rows (SequentialImpulseConstraintSolver.java:823-842), in the order of their colours
+ * (first fit in index order over their dynamic bodies).  Linked bodies still collide
+ * (disableCollisionsBetweenLinkedBodies = false).  *id receives the joint's index. */
+int jbgpu_world_add_point2point(jbgpu_world* world, int32_t body_a, int32_t body_b, const float pivot_a[3],
+                                const float pivot_b[3], int32_t* id);
+/* Point2PointConstraint.ConstraintSetting (tau 0.3, damping 1, impulse clamp 0 by default). */
+int jbgpu_world_set_joint_setting(jbgpu_world* world, int32_t id, float tau, float damping, float impulse_clamp);
+/* TypedConstraint.getAppliedImpulse of every joint after the last solve; with out NULL only *n
+ * is set; n > capacity is JBGPU_ERR_CAPACITY with *n set. */
+int jbgpu_world_get_joint_impulses(jbgpu_world* world, float* out, int32_t capacity, int32_t* n);
+
 int jbgpu_world_get_state(jbgpu_world* world, jbgpu_state* state);
 int jbgpu_world_set_state(jbgpu_world* world, const jbgpu_state* state);
 int jbgpu_world_get_pairs(jbgpu_world* world, uint64_t* keys, int32_t capacity, int32_t* n_pairs);

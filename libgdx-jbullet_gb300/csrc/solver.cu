@@ -43,6 +43,18 @@ __device__ __forceinline__ int uf_find(int* parent, int x) {
     return x;
 }
 
+// Hooks the larger of the two roots under the smaller (bounded; a timeout sets ST_TIMEOUT).
+__device__ __forceinline__ void uf_unite(int* parent, int a, int b, int* ctr) {
+    for (int it = 0; it < 1 << 20; it++) {
+        a = uf_find(parent, a);
+        b = uf_find(parent, b);
+        if (a == b) return;
+        if (a > b) { int t = a; a = b; b = t; }
+        if (atomicCAS(&parent[b], b, a) == b) return;
+    }
+    atomicOr(&ctr[C_STATUS], ST_TIMEOUT);
+}
+
 __global__ void k_uf_init(int n, int* parent) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) parent[i] = i;
@@ -67,14 +79,18 @@ __global__ void k_uf_union(DevWorld w, DevPairs P, int nPairs, int* parent, int 
     if ((rank < 2 ? 0 : rank - 1) != round) return;
     if (!merges_islands(w.flags[a]) || !merges_islands(w.flags[b])) return;
     if (round > 0 && __ldcg(&parent[a]) == __ldcg(&parent[b])) return;
-    for (int it = 0; it < 1 << 20; it++) {
-        a = uf_find(parent, a);
-        b = uf_find(parent, b);
-        if (a == b) return;
-        if (a > b) { int t = a; a = b; b = t; }
-        if (atomicCAS(&parent[b], b, a) == b) return;
-    }
-    atomicOr(&w.ctr[C_STATUS], ST_TIMEOUT);
+    uf_unite(parent, a, b, w.ctr);
+}
+
+// Joints between two dynamic bodies, at least one of them active, join their islands
+// (DiscreteDynamicsWorld.calculateSimulationIslands, java:649-677).
+__global__ void k_joint_union(DevWorld w, SolverBuffers sb) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= sb.J.n) return;
+    const int a = sb.J.a[j], b = sb.J.b[j];
+    if (b < 0 || is_static_or_kin(w.flags[a]) || is_static_or_kin(w.flags[b])) return;
+    if (!is_active_state(w.act[a]) && !is_active_state(w.act[b])) return;
+    uf_unite(sb.parent, a, b, w.ctr);
 }
 
 // Every body pointed at its root (between the union rounds).
@@ -162,6 +178,7 @@ void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, Sol
             k_uf_union<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.parent, r); note_launch();
         }
     }
+    if (sb.J.n > 0) { k_joint_union<<<gridn(sb.J.n, 128), 128, 0, s>>>(w, sb); note_launch(); }
     k_islands<<<gridn(n, 256), 256, 0, s>>>(w, sb.parent, sb.keepAwake, sb.inactive); note_launch();
     k_island_awake<<<gridn(n, 256), 256, 0, s>>>(w, sb.keepAwake); note_launch();
 }
@@ -914,6 +931,104 @@ JBD void gstore(const DevWorld& w, int b, V l, V a) {
     __stcg(&w.angvel[b], f4(a, 0.0f));
 }
 
+// ---- point-to-point joints ----------------------------------------------------------------
+// TypedConstraint's fixed body: identity transform, no mass, no inertia, at rest.
+JBD Xf joint_xf(const DevWorld& w, int b) {
+    if (b >= 0) return load_xf(w, b);
+    Xf t;
+    t.b.r[0] = mk(1.0f, 0.0f, 0.0f);
+    t.b.r[1] = mk(0.0f, 1.0f, 0.0f);
+    t.b.r[2] = mk(0.0f, 0.0f, 1.0f);
+    t.o = mk(0.0f, 0.0f, 0.0f);
+    return t;
+}
+
+// Point2PointConstraint.buildJacobian (java:72-101) of the joints whose island is processed:
+// the pivot offsets, the positional error per axis and 1/Adiag per axis (JacobianEntry.init,
+// JacobianEntry.java:63-78; the port's `bJ.set(rel_pos2).crs(bJ)` crosses rel_pos2 with
+// itself, so the B-side angular Jacobian is the zero vector, kept as the reference computes it).
+// The solve's per-iteration recomputation of these (java:103-140) gives the same floats.
+__global__ void k_joint_setup(DevWorld w, SolverBuffers sb) {
+    const DevJoints& J = sb.J;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= J.n) return;
+    const int a = J.a[j], b = J.b[j];
+    const int ta = w.island[a], tb = b >= 0 ? w.island[b] : -1;
+    const int isl = ta >= 0 ? ta : tb;
+    const int on = isl >= 0 && !sb.inactive[isl];
+    J.act[j] = on;
+    if (!on) return;
+    J.imp[j] = 0.0f;
+    const Xf xa = joint_xf(w, a), xb = joint_xf(w, b);
+    const float4 la = w.iloc[a], lb = b >= 0 ? w.iloc[b] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const V iA = mk(la.x, la.y, la.z), iB = mk(lb.x, lb.y, lb.z);
+    const V pA = xf_apply(xa, mk4(J.pivA[j])), pB = xf_apply(xb, mk4(J.pivB[j]));
+    const V r1 = sub(pA, xa.o), r2 = sub(pB, xb.o);
+    const M w2A = transpose(xa.b), w2B = transpose(xb.b);
+    float inv[3], depth[3];
+    V n = mk(0.0f, 0.0f, 0.0f);
+    for (int i = 0; i < 3; i++) {
+        set_coord(n, i, 1.0f);
+        const V aJ = mulMv(crs(r1, n), w2A);
+        const V bJ = mulMv(crs(r2, r2), w2B);
+        const V m0 = mulc(iA, aJ), m1 = mulc(iB, bJ);
+        const float adiag = __fadd_rn(__fadd_rn(__fadd_rn(la.w, dot(m0, aJ)), lb.w), dot(m1, bJ));
+        inv[i] = jdiv(1.0f, adiag);
+        depth[i] = -dot(sub(pA, pB), n);
+        set_coord(n, i, 0.0f);
+    }
+    J.r1[j] = f4(r1, inv[0]);
+    J.r2[j] = f4(r2, inv[1]);
+    J.dep[j] = make_float4(depth[0], depth[1], depth[2], inv[2]);
+}
+
+// RigidBody.applyImpulse (dynamics/RigidBody.java:401-417) on velocities held in registers.
+JBD void body_impulse(V& lin, V& ang, float im, const M& iw, V impulse, V relPos) {
+    if (im == 0.0f) return;
+    lin = add(lin, scl(impulse, im));
+    ang = add(ang, mulMv(crs(relPos, impulse), iw));
+}
+
+// Point2PointConstraint.solveConstraint (java:103-171) of joint j on the bodies' velocities in
+// global memory: per axis, impulse = depth tau / dt / Adiag - damping relVel / Adiag, clamped,
+// applied to both bodies.
+JBD void joint_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
+    const int a = J.a[j], b = J.b[j];
+    const float4 q1 = J.r1[j], q2 = J.r2[j], dp = J.dep[j], st = J.set[j];
+    const V r1 = mk(q1.x, q1.y, q1.z), r2 = mk(q2.x, q2.y, q2.z);
+    V vA, wA, vB = mk(0.0f, 0.0f, 0.0f), wB = mk(0.0f, 0.0f, 0.0f);
+    gload(w, a, vA, wA);
+    if (b >= 0) gload(w, b, vB, wB);
+    const float imA = w.iloc[a].w, imB = b >= 0 ? w.iloc[b].w : 0.0f;
+    const M IA = load_iw(w, a);
+    M IB;
+    IB.r[0] = IB.r[1] = IB.r[2] = mk(0.0f, 0.0f, 0.0f);
+    if (b >= 0) IB = load_iw(w, b);
+    float acc = __ldcg(J.imp + j);
+    V n = mk(0.0f, 0.0f, 0.0f);
+    for (int i = 0; i < 3; i++) {
+        set_coord(n, i, 1.0f);
+        const float inv = i == 0 ? q1.w : (i == 1 ? q2.w : dp.w);
+        const float depth = i == 0 ? dp.x : (i == 1 ? dp.y : dp.z);
+        const V vel = sub(add(crs(wA, r1), vA), add(crs(wB, r2), vB));   // getVelocityInLocalPoint
+        const float relVel = dot(n, vel);
+        float impulse = __fsub_rn(__fmul_rn(jdiv(__fmul_rn(depth, st.x), dt), inv), __fmul_rn(__fmul_rn(st.y, relVel), inv));
+        if (st.z > 0.0f) {
+            if (impulse < -st.z) impulse = -st.z;
+            if (impulse > st.z) impulse = st.z;
+        }
+        acc = __fadd_rn(acc, impulse);
+        const V iv = scl(n, impulse);
+        body_impulse(vA, wA, imA, IA, iv, r1);
+        body_impulse(vB, wB, imB, IB, scl(iv, -1.0f), r2);
+        set_coord(n, i, 0.0f);
+    }
+    if (imA != 0.0f) gstore(w, a, vA, wA);
+    if (b >= 0 && imB != 0.0f) gstore(w, b, vB, wB);
+    __stcg(J.imp + j, acc);
+}
+
+
 // write-back (java:901-912): appliedImpulse; appliedImpulseLateral1 ends as friction row 2's
 JBD void writeback_slot(const DevPairs& P, const DevRows& R, int s) {
     int p = R.slot_pair[s];
@@ -1106,7 +1221,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
     ResCtl rc;
     rc.on = byRes;
     int step = 0;           // colour steps this block has run (the pool alternates with it)
-    if (nCut == 0 && !byRes) {
+    if (nCut == 0 && !byRes && sb.J.n == 0) {
         __shared__ int shPart;
         int itMax = 0;
         for (int part = next_part(w, sb, C_PART_NEXT1, &shPart); part >= 0; part = next_part(w, sb, C_PART_NEXT1, &shPart)) {
@@ -1140,13 +1255,27 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
         if (threadIdx.x == 0 && itMax > 0) atomicMax(&w.ctr[C_PGS_ITERS], itMax);
         return;
     }
-    if (nSlots == 0) return;
+    if (nSlots == 0 && sb.J.n == 0) return;
+    const bool contacts = nSlots > 0;   // else only joints (the colouring did not run this step)
     if (tid == 0) for (int k = 0; k < 3; k++) w.ctr[C_RES0 + k] = 0;
     Staged st;
     int it = -1;          // -1: the warm-start phase
     for (;;) {
         for (int sub = 0; sub < (it < 0 ? 1 : 2); sub++) {
             const int kind = it < 0 ? PH_WARM : (sub == 0 ? PH_NORMAL : PH_FRICTION);
+            if (kind == PH_NORMAL && sb.J.n > 0) {
+                // the joints of processed islands, before the iteration's contact rows
+                // (SequentialImpulseConstraintSolver.java:823-842), colour by colour
+                for (int c = 0; c < sb.J.nCol; c++) {
+                    const int j0 = sb.J.colStart[c], j1 = sb.J.colStart[c + 1];
+                    for (int q = j0 + spread; q < j1; q += nth) {
+                        const int j = sb.J.order[q];
+                        if (sb.J.act[j]) joint_solve(w, sb.J, j, dt);
+                    }
+                    grid_barrier(w.ctr, nb, barK);
+                }
+            }
+            if (!contacts) continue;
             for (int part = blockIdx.x; part < sb.nParts; part += gridDim.x) {
                 const PartView v = part_view(sb, part);
                 const bool psm = smem && v.np <= sb.smemCap;
@@ -1211,7 +1340,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
         }
         ++it;
         if (it >= maxIt) break;
-        if (byRes && it > 0) {
+        if (byRes && it > 0 && contacts) {
             // island residuals of this iteration; ctr[C_RES0 + it % 3] counts islands still
             // above the tolerance, the next slot is cleared (last read two iterations ago)
             const int flag = C_RES0 + it % 3;
@@ -1223,7 +1352,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
         }
     }
     if (tid == 0 && it > 0) atomicMax(&w.ctr[C_PGS_ITERS], it);
-    if (byRes) {          // per-island statistics: islConv holds the iteration an island converged at
+    if (byRes && contacts) {   // per-island statistics: islConv holds the iteration an island converged at
         const int nChunks = *sb.nIslChunks;
         for (int ch = tid; ch < nChunks; ch += nth) {
             const int2 cd = sb.islChunk[ch];
@@ -1484,11 +1613,22 @@ void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, 
     if (nPairs <= 0 || sb.nFinite <= 0 || sb.nParts <= 0) {
         cudaMemsetAsync(sb.nColours, 0, sizeof(int), s);
         cudaMemsetAsync(sb.nCand, 0, sizeof(int), s);
-        if (prof) {
-            prof->mark(PH_COLOUR, 1, s);
-            prof->mark(PH_SETUP, 0, s); prof->mark(PH_SETUP, 1, s);
-            prof->mark(PH_PGS, 0, s); prof->mark(PH_PGS, 1, s);
+        if (prof) { prof->mark(PH_COLOUR, 1, s); prof->mark(PH_SETUP, 0, s); }
+        const bool joints = sb.J.n > 0 && sb.nFinite > 0 && sb.nParts > 0;
+        if (joints) { k_joint_setup<<<gridn(sb.J.n, 128), 128, 0, s>>>(w, sb); note_launch(); }
+        if (prof) { prof->mark(PH_SETUP, 1, s); prof->mark(PH_PGS, 0, s); }
+        if (joints) {   // no contact manifold: the joints alone
+            cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
+            cudaMemsetAsync(w.ctr + C_PGS_ITERS, 0, sizeof(int), s);
+            DevWorld wc = w;
+            DevPairs pc = P;
+            DevRows rc = R;
+            SolverBuffers sc = sb;
+            float dtc = dt;
+            void* args[] = {&wc, &pc, &rc, &sc, &dtc};
+            cudaLaunchCooperativeKernel((void*)k_pgs, sb.gridPgs, sb.threads, args, pgs_smem(sb), s); note_launch();
         }
+        if (prof) prof->mark(PH_PGS, 1, s);
         return;
     }
     const int parts = sb.nParts;
@@ -1541,6 +1681,7 @@ void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, 
         k_mlp_warmstart<<<tiles, MLP_THREADS, mlp_smem_bytes(), s>>>(w, P, R, *learn.mlp);
         note_launch();
     }
+    if (sb.J.n > 0) { k_joint_setup<<<gridn(sb.J.n, 128), 128, 0, s>>>(w, sb); note_launch(); }
     if (prof) { prof->mark(PH_SETUP, 1, s); prof->mark(PH_PGS, 0, s); }
     cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
     {

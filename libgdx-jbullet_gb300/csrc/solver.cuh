@@ -15,6 +15,24 @@ constexpr int PART_MAX_BODIES = 2048; // bodies of one part (velocities staged i
 // (the broadphase's sorted leaf order: Morton code with the batch world in the high bits).
 // World parts: every world holds at most PART_MAX_BODIES finite bodies, and each world is one
 // part.  Range parts otherwise: nParts equal ranges of the order.
+// Point-to-point joints (jbgpu_world_add_point2point), uploaded by the host when they change.
+struct DevJoints {
+    int n = 0;                    // joints
+    int nCol = 0;                 // colours: first fit in index order over the joints' dynamic bodies
+    int* a = nullptr;             // body A of each joint
+    int* b = nullptr;             // body B, -1 for the fixed body
+    float4* pivA = nullptr;       // pivotInA, pivotInB (xyz)
+    float4* pivB = nullptr;
+    float4* set = nullptr;        // tau, damping, impulse clamp
+    int* order = nullptr;         // joints by (colour, index)
+    int* colStart = nullptr;      // nCol + 1 offsets into order
+    float4* r1 = nullptr;         // per step: pivot A - centre of A, 1/Adiag of axis 0 in .w
+    float4* r2 = nullptr;         // pivot B - centre of B, 1/Adiag of axis 1 in .w
+    float4* dep = nullptr;        // depth per axis, 1/Adiag of axis 2 in .w
+    float* imp = nullptr;         // appliedImpulse
+    int* act = nullptr;           // solved this step (its island is processed)
+};
+
 struct SolverBuffers {
     int* parent = nullptr;        // union-find (bodies)
     int* keepAwake = nullptr;     // per island root
@@ -74,6 +92,7 @@ struct SolverBuffers {
     int gridColour = 0;           // co-resident blocks of the cooperative kernels
     int gridPgs = 0;
     int threads = SOLVER_THREADS;
+    DevJoints J;                  // point-to-point joints
 };
 
 // (Re)plans the parts for nFinite ordered bodies.  worldCounts: finite bodies per batch world;

@@ -93,6 +93,11 @@ struct jbgpu_world {
     int nWorlds = 1;
     bool planesDirty = true;
     std::vector<int> worldFinite;   // finite (non-plane) bodies per batch world
+    // point-to-point joints (host copy; uploaded to sb.J when they change)
+    std::vector<int> jA, jB;
+    std::vector<float4> jPivA, jPivB, jSet;
+    bool jointsDirty = false;
+    int capJoints = 0;
     bool orderValid = false;        // the broadphase leaf order covers every body added
     bool solverDirty = true;        // solver parts must be planned again
     int solverOrderFinite = -1;     // nFinite the parts were planned for
@@ -451,11 +456,68 @@ int run_stage(jbgpu_world* w, int stage, float dt) {
     return JBGPU_OK;
 }
 
+// Joints to the device: arrays grown to the joint count, the colouring (first fit in index
+// order: a joint takes the lowest colour no earlier joint on one of its dynamic bodies holds;
+// static and kinematic bodies take no impulse, so they do not order joints) and the solve order
+// by (colour, index).
+int sync_joints(jbgpu_world* w) {
+    if (!w->jointsDirty) return JBGPU_OK;
+    DevJoints& J = w->sb.J;
+    const int n = (int)w->jA.size();
+    if (n > w->capJoints) {
+        dfree(J.a); dfree(J.b); dfree(J.pivA); dfree(J.pivB); dfree(J.set); dfree(J.order); dfree(J.colStart);
+        dfree(J.r1); dfree(J.r2); dfree(J.dep); dfree(J.imp); dfree(J.act);
+        const int c = std::max(n, 2 * w->capJoints);
+        CK(dalloc(&J.a, c)); CK(dalloc(&J.b, c)); CK(dalloc(&J.pivA, c)); CK(dalloc(&J.pivB, c)); CK(dalloc(&J.set, c));
+        CK(dalloc(&J.order, c)); CK(dalloc(&J.colStart, c + 1)); CK(dalloc(&J.r1, c)); CK(dalloc(&J.r2, c));
+        CK(dalloc(&J.dep, c)); CK(dalloc(&J.imp, c)); CK(dalloc(&J.act, c));
+        CK(cudaMemset(J.imp, 0, sizeof(float) * c));
+        w->capJoints = c;
+    }
+    auto dynBody = [&](int b) { return b >= 0 && !(w->hFlags[b] & (CF_STATIC | CF_KINEMATIC)); };
+    std::vector<std::vector<int>> used(w->nBodies);
+    std::vector<std::pair<int, int>> ck(n);
+    int nCol = 0;
+    for (int k = 0; k < n; k++) {
+        int c = 0;
+        for (;; c++) {
+            bool clash = false;
+            for (int b : {w->jA[k], w->jB[k]})
+                if (dynBody(b))
+                    for (int u : used[b]) clash = clash || u == c;
+            if (!clash) break;
+        }
+        for (int b : {w->jA[k], w->jB[k]})
+            if (dynBody(b)) used[b].push_back(c);
+        ck[k] = {c, k};
+        nCol = std::max(nCol, c + 1);
+    }
+    std::sort(ck.begin(), ck.end());
+    std::vector<int> order(n), colStart(nCol + 1, 0);
+    for (int k = 0; k < n; k++) { order[k] = ck[k].second; colStart[ck[k].first + 1]++; }
+    for (int c = 0; c < nCol; c++) colStart[c + 1] += colStart[c];
+    cudaStream_t s = w->stream;
+    CK(cudaMemcpyAsync(J.a, w->jA.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.b, w->jB.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.pivA, w->jPivA.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.pivB, w->jPivB.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.set, w->jSet.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.colStart, colStart.data(), sizeof(int) * (nCol + 1), cudaMemcpyHostToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    J.n = n;
+    J.nCol = nCol;
+    w->jointsDirty = false;
+    return JBGPU_OK;
+}
+
 int prepare(jbgpu_world* w) {
     CK(cudaSetDevice(w->device));
     int rc = sync_shapes(w);
     if (rc) return rc;
-    return sync_planes(w);
+    rc = sync_planes(w);
+    if (rc) return rc;
+    return sync_joints(w);
 }
 
 // Narrowphase and islands of one step: the island unions run on the second stream while the
@@ -726,6 +788,11 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(V.bucket); dfree(V.bucketList); dfree(V.claim); dfree(V.taken); dfree(V.posOf); dfree(V.candLocal);
     dfree(V.md); dfree(V.ml); dfree(V.slotIsl); dfree(V.islList); dfree(V.islCount); dfree(V.islFill); dfree(V.islStart);
     dfree(V.segFlag); dfree(V.segIdx); dfree(V.islChunk); dfree(V.islConv); dfree(V.islAcc); dfree(V.islDone);
+    {
+        DevJoints& J = V.J;
+        dfree(J.a); dfree(J.b); dfree(J.pivA); dfree(J.pivB); dfree(J.set); dfree(J.order); dfree(J.colStart);
+        dfree(J.r1); dfree(J.r2); dfree(J.dep); dfree(J.imp); dfree(J.act);
+    }
     dfree(V.nIslChunks);
     if (V.islScratch) cudaFree(V.islScratch);
     dfree(V.colourCount); dfree(V.colourFill); dfree(V.colourStart);
@@ -1020,6 +1087,43 @@ int jbgpu_world_get_samples(jbgpu_world* w, float* x, float* t, int32_t capacity
     }
     *n = cnt;
     if (cnt > capacity && x && t) return fail(JBGPU_ERR_CAPACITY, "sample buffer too small");
+    return JBGPU_OK;
+}
+
+int jbgpu_world_add_point2point(jbgpu_world* w, int32_t a, int32_t b, const float pa[3], const float pb[3], int32_t* id) {
+    if (!w || !pa || !pb) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (a < 0 || a >= w->nBodies || b < -1 || b >= w->nBodies || a == b)
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint bodies");
+    w->jA.push_back(a);
+    w->jB.push_back(b);
+    w->jPivA.push_back(make_float4(pa[0], pa[1], pa[2], 0.0f));
+    w->jPivB.push_back(make_float4(pb[0], pb[1], pb[2], 0.0f));
+    w->jSet.push_back(make_float4(0.3f, 1.0f, 0.0f, 0.0f));   // ConstraintSetting defaults
+    w->jointsDirty = true;
+    if (id) *id = (int32_t)w->jA.size() - 1;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_joint_setting(jbgpu_world* w, int32_t id, float tau, float damping, float clamp) {
+    if (!w || id < 0 || id >= (int)w->jA.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
+    w->jSet[id] = make_float4(tau, damping, clamp, 0.0f);
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_get_joint_impulses(jbgpu_world* w, float* out, int32_t cap, int32_t* n) {
+    if (!w || !n) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null argument");
+    const int nj = (int)w->jA.size();
+    *n = nj;
+    if (!out || nj == 0) return JBGPU_OK;
+    if (nj > cap) return fail(JBGPU_ERR_CAPACITY, "caller buffer too small");
+    CK(cudaSetDevice(w->device));
+    if (w->sb.J.n < nj) {   // joints added since the last step: not solved yet
+        std::fill(out, out + nj, 0.0f);
+        if (w->sb.J.n == 0) return JBGPU_OK;
+    }
+    CK(cudaMemcpyAsync(out, w->sb.J.imp, sizeof(float) * w->sb.J.n, cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
     return JBGPU_OK;
 }
 

@@ -56,6 +56,10 @@ def lib():
             "jbgpu_world_get_transforms": ([C.c_void_p, _abi.f32p], C.c_int),
             "jbgpu_world_set_profiling": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_timer": ([C.c_void_p, C.c_int32, C.POINTER(C.c_double)], C.c_int),
+            "jbgpu_world_add_point2point": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p,
+                                             C.POINTER(C.c_int32)], C.c_int),
+            "jbgpu_world_set_joint_setting": ([C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_float], C.c_int),
+            "jbgpu_world_get_joint_impulses": ([C.c_void_p, _abi.f32p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
             "jbgpu_world_phase_times": ([C.c_void_p, P(C.c_double), C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_profile_counters": ([C.c_void_p, P(_abi.Counters), C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_narrowphase_static": ([C.c_void_p, C.c_int32], C.c_int),
@@ -87,7 +91,8 @@ EXPORTED = [
     "jbgpu_world_synchronize", "jbgpu_world_get_state", "jbgpu_world_set_state", "jbgpu_world_get_pairs",
     "jbgpu_world_get_manifolds", "jbgpu_world_set_manifolds", "jbgpu_world_get_solver_order", "jbgpu_world_counters",
     "jbgpu_world_apply_forces", "jbgpu_world_get_transforms", "jbgpu_world_set_profiling", "jbgpu_world_phase_times",
-    "jbgpu_world_profile_counters", "jbgpu_world_timer",
+    "jbgpu_world_profile_counters", "jbgpu_world_timer", "jbgpu_world_add_point2point", "jbgpu_world_set_joint_setting",
+    "jbgpu_world_get_joint_impulses",
 ]
 
 
@@ -176,6 +181,7 @@ class GpuWorld:
         self.h = h
         if scene is not None:
             self.add_scene(scene)
+            self.add_scene_joints(scene)
 
     def close(self):
         if getattr(self, "h", None):
@@ -193,6 +199,31 @@ class GpuWorld:
         check(lib().jbgpu_world_add_shapes(self.h, descs, len(descs), None))
         b, ptr = scene.body_descs_ptr()
         check(lib().jbgpu_world_add_bodies(self.h, ptr, len(b), None))
+
+    def add_point2point(self, a, b, pivot_a, pivot_b):
+        """Point-to-point joint between bodies a and b (b = -1: the fixed body); returns its id."""
+        pa = np.ascontiguousarray(pivot_a, np.float32)
+        pb = np.ascontiguousarray(pivot_b, np.float32)
+        jid = C.c_int32()
+        check(lib().jbgpu_world_add_point2point(self.h, a, b, pa.ctypes.data_as(_abi.f32p), pb.ctypes.data_as(_abi.f32p),
+                                                C.byref(jid)))
+        return jid.value
+
+    def set_joint_setting(self, jid, tau=0.3, damping=1.0, impulse_clamp=0.0):
+        check(lib().jbgpu_world_set_joint_setting(self.h, jid, tau, damping, impulse_clamp))
+
+    def joint_impulses(self):
+        n = C.c_int32()
+        check(lib().jbgpu_world_get_joint_impulses(self.h, None, 0, C.byref(n)))
+        out = np.zeros(max(n.value, 1), np.float32)
+        check(lib().jbgpu_world_get_joint_impulses(self.h, out.ctypes.data_as(_abi.f32p), n.value, C.byref(n)))
+        return out[:n.value].copy()
+
+    def add_scene_joints(self, scene):
+        for j in scene.meta.get("joints", []):
+            jid = self.add_point2point(j["a"], j["b"], j["pivot_a"], j["pivot_b"])
+            if "setting" in j:
+                self.set_joint_setting(jid, *j["setting"])
 
     @property
     def n_bodies(self):

@@ -311,6 +311,61 @@ def box_stack(levels=4, seed=0, steps=120):
                  shapes, bodies, meta={"seed": seed})
 
 
+def jointed_chains(chains=6, links=8, loose=24, seed=0, spacing=2.5, top=10.0, steps=240, worlds=1):
+    """Chains of boxes (half-extents 0.15 x 0.45 x 0.15, 1 m long) joined end to end by point-to-
+    point joints, the top link pinned to a fixed point, each chain started with a sideways
+    velocity so that the chains swing into each other and into loose boxes that fall on them
+    and on the plane.  meta["joints"]: {a, b, pivot_a, pivot_b} per joint (b = -1: fixed body).
+    With worlds > 1 the scene is repeated in that many batch worlds (own plane each)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE), {"type": _abi.SHAPE_BOX, "params": (0.15, 0.45, 0.15, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.3, 0.3, 0.3, 0.0), "points": None}]
+    side = int(np.ceil(np.sqrt(chains)))
+    all_bodies, joints, wid = [], [], []
+    base = 0
+    for wi in range(worlds):
+        plane = _plane_body(0)
+        lb = _bodies(chains * links)
+        lb["shape"] = 1
+        lb["mass"] = 1.0
+        lb["local_inertia"] = box_inertia(1.0, (0.15, 0.45, 0.15))
+        pos = np.zeros((chains * links, 3), F)
+        for c in range(chains):
+            x0, z0 = (c % side - (side - 1) / 2.0) * spacing, (c // side - (side - 1) / 2.0) * spacing
+            v = rng.normal(0.0, 2.0, 2)
+            for i in range(links):
+                k = c * links + i
+                pos[k] = (x0, top - 0.5 - 1.0 * i, z0)
+                lb["linear_velocity"][k] = (v[0] * (i + 1) / links, 0.0, v[1] * (i + 1) / links)
+        lb["transform"][:, 9:] = pos
+        fb = _bodies(loose)
+        fb["shape"] = 2
+        fb["mass"] = 2.0
+        fb["local_inertia"] = box_inertia(2.0, (0.3, 0.3, 0.3))
+        half = side * spacing / 2.0
+        fpos = np.stack([rng.uniform(-half, half, loose), rng.uniform(top + 1.0, top + 6.0, loose),
+                         rng.uniform(-half, half, loose)], 1)
+        _set_transforms(fb, random_rotations(rng, loose), fpos)
+        bodies = np.concatenate([plane, lb, fb])
+        first = base + 1
+        for c in range(chains):
+            x0, y0, z0 = pos[c * links]
+            joints.append({"a": first + c * links, "b": -1, "pivot_a": (0.0, 0.5, 0.0),
+                           "pivot_b": (float(x0), float(y0 + 0.5), float(z0))})
+            for i in range(links - 1):
+                joints.append({"a": first + c * links + i, "b": first + c * links + i + 1,
+                               "pivot_a": (0.0, -0.5, 0.0), "pivot_b": (0.0, 0.5, 0.0)})
+        all_bodies.append(bodies)
+        wid.append(np.full(len(bodies), wi, np.int32))
+        base += len(bodies)
+    bodies = np.concatenate(all_bodies)
+    bodies["world"] = np.concatenate(wid)
+    kw = {"world_of_body": np.concatenate(wid)} if worlds > 1 else {}
+    return Scene("jointed_chains_%dx%d_w%d" % (chains, links, worlds), 1.0 / 60.0, steps,
+                 {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10}, shapes, bodies,
+                 meta={"seed": seed, "joints": joints}, **kw)
+
+
 def small_mixed(n=60, seed=0, region=(6.0, 8.0, 6.0), steps=200, with_hulls=True):
     """A small dense mix of every shape type for stage-by-stage parity checks."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -391,4 +446,5 @@ SCENES = {
     "box_stack": box_stack,
     "small_mixed": small_mixed,
     "learned_warmstart": learned_warmstart,
+    "jointed_chains": jointed_chains,
 }

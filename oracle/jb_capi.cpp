@@ -98,6 +98,28 @@ void orc_stage(void* h, int stage, float dt) {
     }
 }
 
+int orc_add_point2point(void* h, int a, int b, const float* pivA, const float* pivB) {
+    World* w = (World*)h;
+    Joint j;
+    j.a = a;
+    j.b = b;
+    j.pivotA = v3(pivA[0], pivA[1], pivA[2]);
+    j.pivotB = v3(pivB[0], pivB[1], pivB[2]);
+    w->joints.push_back(j);
+    return (int)w->joints.size() - 1;
+}
+void orc_set_joint_setting(void* h, int id, float tau, float damping, float clamp) {
+    Joint& j = ((World*)h)->joints[id];
+    j.tau = tau;
+    j.damping = damping;
+    j.impulseClamp = clamp;
+}
+int orc_get_joint_impulses(void* h, float* out, int cap) {
+    const World* w = (const World*)h;
+    const int n = (int)w->joints.size();
+    for (int k = 0; k < n && k < cap; k++) out[k] = w->joints[k].appliedImpulse;
+    return n;
+}
 void orc_set_order_mode(void* h, int mode) { ((World*)h)->orderMode = mode; }
 void orc_set_explicit_order(void* h, const int* order, int n) { ((World*)h)->explicitOrder.assign(order, order + n); }
 void orc_set_brute_force(void* h, int on) { ((World*)h)->bruteForcePairs = on != 0; }

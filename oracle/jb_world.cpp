@@ -265,6 +265,7 @@ template <class T, class C> static void quick_sort(std::vector<T>& a, int lo, in
 }  // namespace
 
 static std::vector<int> g_islandManifolds;    // islandmanifold of the last ISLANDS stage (pair indices)
+static std::vector<int> g_jointIsland;   // per joint: its processed island, -1 when not solved this step
 
 // calculateSimulationIslands + SimulationIslandManager.buildIslands
 // (dynamics/DiscreteDynamicsWorld.java:649-677; collision/dispatch/SimulationIslandManager.java:57-240)
@@ -278,6 +279,15 @@ void stage_islands(World& w) {
         int a = (int)(w.pairKeys[k] >> 32), b = (int)(w.pairKeys[k] & 0xffffffffu);
         int lo = a < b ? a : b, hi = a < b ? b : a;
         if (w.bodies[lo].mergesIslands() && w.bodies[hi].mergesIslands()) uf.unite(w.bodies[lo].islandTag, w.bodies[hi].islandTag);
+    }
+    // calculateSimulationIslands (DiscreteDynamicsWorld.java:649-677): joints between two
+    // dynamic bodies, at least one active, join their islands
+    for (const Joint& j : w.joints) {
+        if (j.b < 0) continue;
+        const Body& A = w.bodies[j.a];
+        const Body& B = w.bodies[j.b];
+        if (!A.isStaticOrKinematic() && !B.isStaticOrKinematic() && (A.isActive() || B.isActive()))
+            uf.unite(A.islandTag, B.islandTag);
     }
     for (int i = 0; i < n; i++) {   // storeIslandActivationState
         Body& b = w.bodies[i];
@@ -322,6 +332,39 @@ void stage_islands(World& w) {
         int isl = w.bodies[m.body0].islandTag >= 0 ? w.bodies[m.body0].islandTag : w.bodies[m.body1].islandTag;
         if (!inactive[isl]) w.solveList.push_back(k);
     }
+    // joints of processed islands (DiscreteDynamicsWorld.getConstraintIslandId, java:549-557)
+    g_jointIsland.assign(w.joints.size(), -1);
+    for (size_t k = 0; k < w.joints.size(); k++) {
+        const Joint& j = w.joints[k];
+        const int ta = w.bodies[j.a].islandTag, tb = j.b >= 0 ? w.bodies[j.b].islandTag : -1;
+        const int isl = ta >= 0 ? ta : tb;
+        if (isl >= 0 && !inactive[isl]) g_jointIsland[k] = isl;
+    }
+}
+
+std::vector<int> joint_colour_order(const World& w) {
+    const size_t n = w.joints.size();
+    std::vector<std::vector<int>> used(w.bodies.size());
+    std::vector<std::pair<int, int>> ck(n);
+    auto dynBody = [&](int b) { return b >= 0 && !w.bodies[b].isStaticOrKinematic(); };
+    for (size_t k = 0; k < n; k++) {
+        const Joint& j = w.joints[k];
+        int c = 0;
+        for (;; c++) {
+            bool clash = false;
+            for (int b : {j.a, j.b})
+                if (dynBody(b))
+                    for (int u : used[b]) clash = clash || u == c;
+            if (!clash) break;
+        }
+        for (int b : {j.a, j.b})
+            if (dynBody(b)) used[b].push_back(c);
+        ck[k] = {c, (int)k};
+    }
+    std::sort(ck.begin(), ck.end());
+    std::vector<int> order(n);
+    for (size_t k = 0; k < n; k++) order[k] = ck[k].second;
+    return order;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -350,7 +393,77 @@ struct Row {          // dynamics/constraintsolver/SolverConstraint.java:34-58
 };
 }  // namespace
 
-static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
+// TypedConstraint's fixed body (TypedConstraint.java:44-49): static, identity transform.
+static Body fixed_body() {
+    Body b;
+    b.xf = xf_identity();
+    b.invInertiaWorld = m3_identity();
+    for (int r = 0; r < 3; r++) for (int c = 0; c < 3; c++) b.invInertiaWorld.m[r][c] = 0.0f;
+    b.flags = CF_STATIC_OBJECT;
+    return b;
+}
+
+// RigidBody.applyImpulse (dynamics/RigidBody.java:401-417): applyCentralImpulse, then the
+// torque impulse rel_pos x impulse through the world inverse inertia.
+static void apply_impulse(Body& b, V3 impulse, V3 relPos) {
+    if (b.invMass == 0.0f) return;
+    V3 si = v3(impulse.x * b.linearFactor.x, impulse.y * b.linearFactor.y, impulse.z * b.linearFactor.z);
+    b.linvel = add(b.linvel, scl(si, b.invMass));
+    V3 t = crs(relPos, v3(impulse.x * b.linearFactor.x, impulse.y * b.linearFactor.y, impulse.z * b.linearFactor.z));
+    t.x *= b.angularFactor.x;
+    t.y *= b.angularFactor.y;
+    t.z *= b.angularFactor.z;
+    b.angvel = add(b.angvel, mulMv(t, b.invInertiaWorld));
+}
+
+// Point2PointConstraint.buildJacobian (java:72-101) with JacobianEntry.init (JacobianEntry.java:
+// 63-78).  The port's `bJ.set(rel_pos2).crs(bJ)` crosses rel_pos2 with itself, so the B-side
+// angular Jacobian is the zero vector: kept, as the reference computes it.
+static void joint_build(Joint& j, const Body& A, const Body& B) {
+    j.appliedImpulse = 0.0f;
+    V3 normal = v3(0, 0, 0);
+    for (int i = 0; i < 3; i++) {
+        set_coord(normal, i, 1.0f);
+        M3 w2A = transpose(A.xf.b), w2B = transpose(B.xf.b);
+        V3 r1 = sub(xf_apply(A.xf, j.pivotA), A.xf.o);
+        V3 r2 = sub(xf_apply(B.xf, j.pivotB), B.xf.o);
+        V3 aJ = mulMv(crs(r1, normal), w2A);
+        V3 bJ = mulMv(crs(r2, r2), w2B);
+        V3 m0 = v3(A.invInertiaLocal.x * aJ.x, A.invInertiaLocal.y * aJ.y, A.invInertiaLocal.z * aJ.z);
+        V3 m1 = v3(B.invInertiaLocal.x * bJ.x, B.invInertiaLocal.y * bJ.y, B.invInertiaLocal.z * bJ.z);
+        j.adiag[i] = A.invMass + dot(m0, aJ) + B.invMass + dot(m1, bJ);
+        set_coord(normal, i, 0.0f);
+    }
+}
+
+// Point2PointConstraint.solveConstraint (java:103-171): per axis, the positional error and the
+// relative velocity at the pivots give an impulse applied to both bodies.
+static void joint_solve(Joint& j, Body& A, Body& B, float timeStep) {
+    V3 pA = xf_apply(A.xf, j.pivotA), pB = xf_apply(B.xf, j.pivotB);
+    V3 normal = v3(0, 0, 0);
+    for (int i = 0; i < 3; i++) {
+        set_coord(normal, i, 1.0f);
+        float jacDiagABInv = 1.0f / j.adiag[i];
+        V3 r1 = sub(pA, A.xf.o), r2 = sub(pB, B.xf.o);
+        V3 vel1 = add(crs(A.angvel, r1), A.linvel);   // RigidBody.getVelocityInLocalPoint
+        V3 vel2 = add(crs(B.angvel, r2), B.linvel);
+        V3 vel = sub(vel1, vel2);
+        float relVel = dot(normal, vel);
+        float depth = -dot(sub(pA, pB), normal);
+        float impulse = depth * j.tau / timeStep * jacDiagABInv - j.damping * relVel * jacDiagABInv;
+        if (j.impulseClamp > 0.0f) {
+            if (impulse < -j.impulseClamp) impulse = -j.impulseClamp;
+            if (impulse > j.impulseClamp) impulse = j.impulseClamp;
+        }
+        j.appliedImpulse += impulse;
+        V3 iv = scl(normal, impulse);
+        apply_impulse(A, iv, sub(pA, A.xf.o));
+        apply_impulse(B, scl(iv, -1.0f), sub(pB, B.xf.o));
+        set_coord(normal, i, 0.0f);
+    }
+}
+
+static void solve_group(World& w, const std::vector<int>& manifolds, const std::vector<int>& joints, float dt) {
     const Config& cfg = w.cfg;
     std::vector<SolverBody> sb;
     std::vector<Row> rows, frows;
@@ -479,6 +592,9 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
         }
     }
     w.counters.solverRows += (int)rows.size();
+    Body fixedB = fixed_body();
+    auto jointBody = [&](int b) -> Body& { return b >= 0 ? w.bodies[b] : fixedB; };
+    for (int jk : joints) joint_build(w.joints[jk], jointBody(w.joints[jk].a), jointBody(w.joints[jk].b));
     // solveGroupCacheFriendlyIterations (java:788-890), split impulse off.  With a residual
     // tolerance the iterations of an island (the group a reference solveGroup call receives)
     // stop once max|delta lambda| / max(max|lambda|, 1e-6) over its rows is within it (the
@@ -507,13 +623,31 @@ static void solve_group(World& w, const std::vector<int>& manifolds, float dt) {
         if (l > lmax[wi]) lmax[wi] = l;
     };
     int itersUsed = 0;
-    for (int it = 0; it < maxIt && !rows.empty(); it++) {
-        if (byResidual) {
+    for (int it = 0; it < maxIt && (!rows.empty() || !joints.empty()); it++) {
+        if (byResidual && !rows.empty()) {
             bool any = false;
             for (int k = 0; k < nIsl; k++) { dmax[k] = 0.0f; lmax[k] = 0.0f; any = any || !converged[k]; }
             if (!any) break;
         }
         itersUsed = it + 1;
+        // joints first (java:823-842): the solver bodies' velocities are written to the rigid
+        // bodies around each joint's solve
+        for (int jk : joints) {
+            Joint& J = w.joints[jk];
+            Body& A = jointBody(J.a);
+            Body& B = jointBody(J.b);
+            for (Body* b : {&A, &B})
+                if (b->islandTag >= 0 && b->companionId >= 0 && sb[b->companionId].invMass != 0.0f) {
+                    b->linvel = sb[b->companionId].linvel;
+                    b->angvel = sb[b->companionId].angvel;
+                }
+            joint_solve(J, A, B, dt);
+            for (Body* b : {&A, &B})
+                if (b->islandTag >= 0 && b->companionId >= 0 && sb[b->companionId].invMass != 0.0f) {
+                    sb[b->companionId].linvel = b->linvel;
+                    sb[b->companionId].angvel = b->angvel;
+                }
+        }
         for (size_t r = 0; r < rows.size(); r++) {   // resolveSingleCollisionCombinedCacheFriendly (java:234-284)
             Row& c = rows[r];
             if (byResidual && converged[rowIsl[r]]) continue;
@@ -651,6 +785,11 @@ void stage_solve(World& w, float dt) {
     w.counters.solverIterations = 0;
     w.lastOrder.clear();
     w.lastColour.clear();
+    // joints solved this step, in colour order (islands share no dynamic body, so one order
+    // over all of them is equivalent to per-island orders)
+    std::vector<int> jointOrder;
+    for (int k : joint_colour_order(w)) if (g_jointIsland[k] >= 0) jointOrder.push_back(k);
+    w.lastJointOrder = jointOrder;
     if (w.orderMode == ORDER_REFERENCE) {
         std::vector<int> im = g_islandManifolds;
         if (im.size() > 1)
@@ -663,11 +802,26 @@ void stage_solve(World& w, float dt) {
             size_t e = s + 1;
             while (e < im.size() && island_of(w, im[e]) == isl) e++;
             if (!inactive[isl]) {
-                std::vector<int> grp(im.begin() + s, im.begin() + e);
-                solve_group(w, grp, dt);
+                std::vector<int> grp(im.begin() + s, im.begin() + e), gj;
+                for (int k : jointOrder) if (g_jointIsland[k] == isl) gj.push_back(k);
+                solve_group(w, grp, gj, dt);
                 for (int k : grp) if (has_rows(w, k)) w.lastOrder.push_back(k);
             }
             s = e;
+        }
+        // islands with joints and no manifold
+        std::vector<uint8_t> withMf(w.bodies.size(), 0);
+        for (int k : im) withMf[island_of(w, k)] = 1;
+        std::vector<int> rest;
+        for (int k : jointOrder) if (!withMf[g_jointIsland[k]]) rest.push_back(k);
+        std::vector<int> isls;
+        for (int k : rest) isls.push_back(g_jointIsland[k]);
+        std::sort(isls.begin(), isls.end());
+        isls.erase(std::unique(isls.begin(), isls.end()), isls.end());
+        for (int isl : isls) {
+            std::vector<int> gj;
+            for (int k : rest) if (g_jointIsland[k] == isl) gj.push_back(k);
+            solve_group(w, std::vector<int>(), gj, dt);
         }
         w.counters.colours = 0;
     } else {
@@ -683,7 +837,7 @@ void stage_solve(World& w, float dt) {
         } else {
             order = colour_order(w, cand, w.lastColour);
         }
-        solve_group(w, order, dt);
+        solve_group(w, order, jointOrder, dt);
         w.lastOrder = order;
     }
     w.counters.solverManifolds = (int)w.lastOrder.size();

@@ -84,6 +84,17 @@ struct Body {            // dynamics/RigidBody.java + collision/dispatch/Collisi
     void setActivationState(int s) { if (activation != DISABLE_DEACTIVATION && activation != DISABLE_SIMULATION) activation = s; }
 };
 
+// Point2PointConstraint (dynamics/constraintsolver/Point2PointConstraint.java:37-70) with its
+// ConstraintSetting (java:202-206).  b = -1 stands for TypedConstraint's fixed body: static, at
+// the origin with the identity basis, zero mass and inertia (TypedConstraint.java:44-49).
+struct Joint {
+    int a = -1, b = -1;
+    V3 pivotA{0, 0, 0}, pivotB{0, 0, 0};   // pivotInA, pivotInB
+    float tau = 0.3f, damping = 1.0f, impulseClamp = 0.0f;
+    float appliedImpulse = 0.0f;           // TypedConstraint.appliedImpulse after the last solve
+    float adiag[3] = {0, 0, 0};            // JacobianEntry.Adiag per axis, from buildJacobian
+};
+
 struct Config {
     V3 gravity{0, -10, 0};
     float contactBreakingThreshold = 0.02f;
@@ -129,11 +140,16 @@ struct World {
     std::vector<int> lastOrder;           // pair indices in the order the last solve used
     std::vector<int> lastColour;          // colour per entry of lastOrder (ORDER_COLOUR)
     bool bruteForcePairs = false;         // SimpleBroadphase-style O(n^2) pair search
+    std::vector<Joint> joints;            // DiscreteDynamicsWorld.constraints, in insertion order
+    std::vector<int> lastJointOrder;      // joints in the order the last solve used
     Counters counters;
     double phaseSeconds[10] = {0};        // CProfile-like per-phase timers
 };
 
 uint64_t pair_key(const World& w, int a, int b);
+// Joint colours: first fit in index order over the joints' dynamic bodies (neither static nor
+// kinematic); the solve order is (colour, index), the GPU's order.
+std::vector<int> joint_colour_order(const World& w);
 void stage_apply_gravity(World& w);
 void stage_predict(World& w, float dt);
 void stage_aabbs(World& w);

@@ -50,6 +50,9 @@ def lib():
         L.orc_shape_local_inertia.argtypes = [C.POINTER(_abi.ShapeDesc), C.c_float, _abi.f32p]
         L.orc_gjk.argtypes = [C.POINTER(_abi.ShapeDesc), _abi.f32p, C.POINTER(_abi.ShapeDesc), _abi.f32p, C.c_float, _abi.f32p]
         L.orc_integrate_transform.argtypes = [_abi.f32p, _abi.f32p, _abi.f32p, C.c_float, _abi.f32p]
+        L.orc_add_point2point.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
+        L.orc_set_joint_setting.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float]
+        L.orc_get_joint_impulses.argtypes = [C.c_void_p, _abi.f32p, C.c_int]
         _lib = L
     return _lib
 
@@ -66,6 +69,7 @@ class OracleWorld:
         self.set_order_mode(order_mode)
         if scene is not None:
             self.add_scene(scene)
+            self.add_scene_joints(scene)
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -78,6 +82,27 @@ class OracleWorld:
             lib().orc_add_shape(self.h, C.byref(descs[i]))
         b, ptr = scene.body_descs_ptr()
         lib().orc_add_bodies(self.h, ptr, len(b))
+
+    def add_point2point(self, a, b, pivot_a, pivot_b):
+        """Point2PointConstraint between bodies a and b (b = -1: the fixed body); returns its id."""
+        pa = np.ascontiguousarray(pivot_a, np.float32)
+        pb = np.ascontiguousarray(pivot_b, np.float32)
+        return lib().orc_add_point2point(self.h, a, b, _fp(pa), _fp(pb))
+
+    def set_joint_setting(self, jid, tau=0.3, damping=1.0, impulse_clamp=0.0):
+        lib().orc_set_joint_setting(self.h, jid, tau, damping, impulse_clamp)
+
+    def joint_impulses(self):
+        n = lib().orc_get_joint_impulses(self.h, None, 0)
+        out = np.zeros(max(n, 1), np.float32)
+        lib().orc_get_joint_impulses(self.h, _fp(out), n)
+        return out[:n].copy()
+
+    def add_scene_joints(self, scene):
+        for j in scene.meta.get("joints", []):
+            jid = self.add_point2point(j["a"], j["b"], j["pivot_a"], j["pivot_b"])
+            if "setting" in j:
+                self.set_joint_setting(jid, *j["setting"])
 
     @property
     def n_bodies(self):
