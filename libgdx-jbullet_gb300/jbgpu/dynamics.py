@@ -174,6 +174,54 @@ class ContactSolverInfo:
         self.solverMode = _abi.SOLVER_CACHE_FRIENDLY | _abi.SOLVER_USE_WARMSTARTING
 
 
+class ConstraintSetting:
+    """Point2PointConstraint.ConstraintSetting (Point2PointConstraint.java:202-206)."""
+
+    def __init__(self):
+        self.tau = 0.3
+        self.damping = 1.0
+        self.impulseClamp = 0.0
+
+
+class Point2PointConstraint:
+    """dynamics/constraintsolver/Point2PointConstraint.java:37-70: Point2PointConstraint(rbA, rbB,
+    pivotInA, pivotInB), or Point2PointConstraint(rbA, pivotInA) joining rbA to the fixed body at
+    pivotInA taken to world space by rbA's current transform."""
+
+    def __init__(self, rbA, *args):
+        self.rbA = rbA
+        if len(args) == 1:
+            self.rbB = None
+            self.pivotInA = np.asarray(args[0], np.float32)
+            t = rbA.getCenterOfMassTransform()
+            self.pivotInB = (t.basis @ self.pivotInA + t.origin).astype(np.float32)
+        else:
+            self.rbB, pa, pb = args
+            self.pivotInA = np.asarray(pa, np.float32)
+            self.pivotInB = np.asarray(pb, np.float32)
+        self.setting = ConstraintSetting()
+        self._world = None
+        self._id = None
+
+    def getRigidBodyA(self):
+        return self.rbA
+
+    def getRigidBodyB(self):
+        return self.rbB
+
+    def getPivotInA(self):
+        return self.pivotInA.copy()
+
+    def getPivotInB(self):
+        return self.pivotInB.copy()
+
+    def getAppliedImpulse(self):
+        """TypedConstraint.getAppliedImpulse: the impulse of the last solve."""
+        if self._world is None or self._world._g is None:
+            return 0.0
+        return float(self._world._g.joint_impulses()[self._id])
+
+
 class DiscreteDynamicsWorld:
     def __init__(self, dispatcher=None, pairCache=None, constraintSolver=None, collisionConfiguration=None, device=0):
         self._gravity = (0.0, -10.0, 0.0)
@@ -184,6 +232,8 @@ class DiscreteDynamicsWorld:
         self._g = None
         self._forces = None
         self._uploaded = 0
+        self._constraints = []
+        self._sent = 0
 
     # -- configuration (before the first step) --
     def setGravity(self, g):
@@ -211,6 +261,20 @@ class DiscreteDynamicsWorld:
     def getNumCollisionObjects(self):
         return len(self._bodies)
 
+    def addConstraint(self, constraint, disableCollisionsBetweenLinkedBodies=False):
+        """DiscreteDynamicsWorld.addConstraint (java:515-521).  Linked bodies keep colliding:
+        disableCollisionsBetweenLinkedBodies = True is not supported."""
+        if disableCollisionsBetweenLinkedBodies:
+            raise NotImplementedError("disableCollisionsBetweenLinkedBodies is not supported by the GPU world")
+        constraint._world = self
+        self._constraints.append(constraint)
+
+    def getNumConstraints(self):
+        return len(self._constraints)
+
+    def getConstraint(self, i):
+        return self._constraints[i]
+
     # -- stepping --
     def _ensure(self):
         if self._g is None:
@@ -225,6 +289,12 @@ class DiscreteDynamicsWorld:
             self._g = GpuWorld(config=cfg)
         if self._uploaded != len(self._bodies):
             self._upload()
+        for c in self._constraints[self._sent:]:
+            b = -1 if c.rbB is None else c.rbB._index
+            c._id = self._g.add_point2point(c.rbA._index, b, c.pivotInA, c.pivotInB)
+            st = c.setting
+            self._g.set_joint_setting(c._id, st.tau, st.damping, st.impulseClamp)
+        self._sent = len(self._constraints)
         return self._g
 
     def _upload(self):

@@ -92,3 +92,47 @@ def test_gpu_joint_api_errors(gpu_lib):
         g.set_joint_setting(7, 0.3, 1.0, 0.0)
     assert len(g.joint_impulses()) == 2
     g.close()
+
+
+@pytest.mark.gpu
+def test_mirror_pendulum_reads_like_the_reference(gpu_lib, oracle_lib):
+    """The reference's usage through the Python mirror: a plane, a box pinned by
+    Point2PointConstraint(rbA, pivotInA) and a second box hanging from it by
+    Point2PointConstraint(rbA, rbB, pivotInA, pivotInB); stepSimulation for two seconds.  The
+    same world built directly on the oracle ends bit-identical, the pivots stay together and
+    the joints report their applied impulses."""
+    from jbgpu import dynamics as D
+    world = D.DiscreteDynamicsWorld()
+    world.setGravity((0.0, -9.81, 0.0))
+    ground = D.RigidBody(D.RigidBodyConstructionInfo(0.0, None, D.StaticPlaneShape((0.0, 1.0, 0.0), 0.0)))
+    world.addRigidBody(ground)
+    shape = D.BoxShape((0.15, 0.45, 0.15))
+    links = []
+    for i in range(2):
+        info = D.RigidBodyConstructionInfo(1.0, None, shape, shape.calculateLocalInertia(1.0))
+        info.startWorldTransform = D.Transform(origin=(0.0, 5.5 - 1.0 * i, 0.0))
+        body = D.RigidBody(info)
+        world.addRigidBody(body)
+        links.append(body)
+    links[0].setLinearVelocity((1.5, 0.0, 0.0))
+    world.addConstraint(D.Point2PointConstraint(links[0], (0.0, 0.5, 0.0)))
+    world.addConstraint(D.Point2PointConstraint(links[0], links[1], (0.0, -0.5, 0.0), (0.0, 0.5, 0.0)))
+    for _ in range(120):
+        world.stepSimulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    g = world._g
+    joints = [{"a": 1, "b": -1, "pivot_a": (0.0, 0.5, 0.0), "pivot_b": tuple(world.getConstraint(0).getPivotInB())},
+              {"a": 1, "b": 2, "pivot_a": (0.0, -0.5, 0.0), "pivot_b": (0.0, 0.5, 0.0)}]
+    assert _pivot_gaps(g.get_state(), joints).max() < 0.02
+    assert world.getConstraint(1).getAppliedImpulse() != 0.0
+    # the same world on the oracle
+    sc = scenes.jointed_chains(chains=1, links=2, loose=0, seed=0)
+    sc.bodies["transform"][1, 9:] = (0.0, 5.5, 0.0)
+    sc.bodies["transform"][2, 9:] = (0.0, 4.5, 0.0)
+    sc.bodies["linear_velocity"][:] = 0.0
+    sc.bodies["linear_velocity"][1] = (1.5, 0.0, 0.0)
+    sc.meta["joints"] = joints
+    o = pyoracle.OracleWorld(sc, config=_abi.default_config(**dict(sc.config, gravity=(0.0, -9.81, 0.0))))
+    for _ in range(120):
+        o.step_simulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    assert not H.compare_state(o.get_state(), g.get_state())
+    world.close()
