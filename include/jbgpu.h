@@ -318,8 +318,27 @@ int jbgpu_world_get_samples(jbgpu_world* world, float* x, float* t, int32_t capa
  * (disableCollisionsBetweenLinkedBodies = false).  *id receives the joint's index. */
 int jbgpu_world_add_point2point(jbgpu_world* world, int32_t body_a, int32_t body_b, const float pivot_a[3],
                                 const float pivot_b[3], int32_t* id);
-/* Point2PointConstraint.ConstraintSetting (tau 0.3, damping 1, impulse clamp 0 by default). */
+/* Point2PointConstraint.ConstraintSetting (tau 0.3, damping 1, impulse clamp 0 by default);
+ * JBGPU_ERR_INVALID_ARGUMENT for a hinge. */
 int jbgpu_world_set_joint_setting(jbgpu_world* world, int32_t id, float tau, float damping, float impulse_clamp);
+/* Hinge joint: DiscreteDynamicsWorld.addConstraint(new HingeConstraint(...), false)
+ * (dynamics/constraintsolver/HingeConstraint.java:44-533).  frame_a, frame_b: the constraint
+ * frames as the constructed HingeConstraint holds them (getAFrame / getBFrame: basis row-major,
+ * 9 floats, then the origin; z is the hinge axis, B's axis column already negated by the
+ * constructor), in the bodies' centre-of-mass spaces; body_b = -1 is the fixed body.  Starts
+ * free (no limit), without motor, not angular-only.  Islands, colouring and solve order as for
+ * point-to-point joints; getAppliedImpulse sums the three linear rows' impulses. */
+int jbgpu_world_add_hinge(jbgpu_world* world, int32_t body_a, int32_t body_b, const float frame_a[12],
+                          const float frame_b[12], int32_t* id);
+/* HingeConstraint.setLimit(low, high, softness, biasFactor, relaxationFactor) (java:565-577);
+ * the reference's two-argument form passes 0.9, 0.3, 1.0. */
+int jbgpu_world_set_hinge_limit(jbgpu_world* world, int32_t id, float low, float high, float softness,
+                                float bias_factor, float relaxation_factor);
+/* HingeConstraint.enableAngularMotor(enable, targetVelocity, maxMotorImpulse) (java:559-563). */
+int jbgpu_world_enable_hinge_motor(jbgpu_world* world, int32_t id, int32_t enable, float target_velocity,
+                                   float max_motor_impulse);
+/* HingeConstraint.setAngularOnly (java:555-557): no linear rows, the axes alone are held. */
+int jbgpu_world_set_hinge_angular_only(jbgpu_world* world, int32_t id, int32_t angular_only);
 /* TypedConstraint.getAppliedImpulse of every joint after the last solve; with out NULL only *n
  * is set; n > capacity is JBGPU_ERR_CAPACITY with *n set. */
 int jbgpu_world_get_joint_impulses(jbgpu_world* world, float* out, int32_t capacity, int32_t* n);

@@ -948,6 +948,88 @@ JBD Xf joint_xf(const DevWorld& w, int b) {
 // JacobianEntry.java:63-78; the port's `bJ.set(rel_pos2).crs(bJ)` crosses rel_pos2 with
 // itself, so the B-side angular Jacobian is the zero vector, kept as the reference computes it).
 // The solve's per-iteration recomputation of these (java:103-140) gives the same floats.
+// ScalarUtil.atan2Fast (linearmath/ScalarUtil.java:43-57)
+constexpr float SIMD_PI_F = 6.283185307179586232f * 0.5f;   // BulletGlobals.SIMD_PI
+JBD float atan2_fast(float y, float x) {
+    const float c1 = __fdiv_rn(SIMD_PI_F, 4.0f), c2 = __fmul_rn(3.0f, c1);
+    const float ay = fabsf(y);
+    float angle;
+    if (x >= 0.0f) angle = __fsub_rn(c1, __fmul_rn(c1, jdiv(__fsub_rn(x, ay), __fadd_rn(x, ay))));
+    else angle = __fsub_rn(c2, __fmul_rn(c1, jdiv(__fadd_rn(x, ay), __fsub_rn(ay, x))));
+    return y < 0.0f ? -angle : angle;
+}
+JBD V frame_col(const float4* rows, int c) {
+    return mk(c == 0 ? rows[0].x : (c == 1 ? rows[0].y : rows[0].z), c == 0 ? rows[1].x : (c == 1 ? rows[1].y : rows[1].z),
+              c == 0 ? rows[2].x : (c == 1 ? rows[2].y : rows[2].z));
+}
+// RigidBody.computeAngularImpulseDenominator (dynamics/RigidBody.java:534-541)
+JBD float ang_denom(const M& iw, V axis) { return dot(axis, mulMTv(axis, iw)); }
+JBD M joint_iw(const DevWorld& w, int b) {
+    M r;
+    r.r[0] = r.r[1] = r.r[2] = mk(0.0f, 0.0f, 0.0f);
+    if (b >= 0) r = load_iw(w, b);
+    return r;
+}
+
+// HingeConstraint.buildJacobian (HingeConstraint.java:240-340): three linear rows along the
+// pivots' separation and its plane space (JacobianEntry.init as for the point-to-point joint),
+// the limit state from the hinge angle (getHingeAngle, java:535-555), kHinge about A's hinge
+// axis, and both world hinge axes (the solve's per-iteration recomputation gives the same
+// floats).  The angular JacobianEntries the reference also builds are never read by its solve.
+JBD void hinge_setup(const DevWorld& w, const DevJoints& J, int j, int a, int b) {
+    const int kind = J.kind[j];
+    const float4* F = J.frame + 6 * j;
+    const Xf xa = joint_xf(w, a), xb = joint_xf(w, b);
+    const float4 la = w.iloc[a], lb = b >= 0 ? w.iloc[b] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const V iA = mk(la.x, la.y, la.z), iB = mk(lb.x, lb.y, lb.z);
+    const M IA = joint_iw(w, a), IB = joint_iw(w, b);
+    const V pA = xf_apply(xa, mk4(J.pivA[j])), pB = xf_apply(xb, mk4(J.pivB[j]));
+    const V r1 = sub(pA, xa.o), r2 = sub(pB, xb.o);
+    V n[3];
+    float inv[3] = {0.0f, 0.0f, 0.0f}, depth[3] = {0.0f, 0.0f, 0.0f};
+    n[0] = n[1] = n[2] = mk(0.0f, 0.0f, 0.0f);
+    if (!(kind & JK_ANGULAR_ONLY)) {
+        const V rel = sub(pB, pA);
+        n[0] = len2(rel) > FLT_EPS ? nor(rel) : mk(1.0f, 0.0f, 0.0f);
+        plane_space1(n[0], n[1], n[2]);
+        const M w2A = transpose(xa.b), w2B = transpose(xb.b);
+        for (int i = 0; i < 3; i++) {
+            const V aJ = mulMv(crs(r1, n[i]), w2A);
+            const V bJ = mulMv(crs(r2, r2), w2B);
+            const V m0 = mulc(iA, aJ), m1 = mulc(iB, bJ);
+            const float adiag = __fadd_rn(__fadd_rn(__fadd_rn(la.w, dot(m0, aJ)), lb.w), dot(m1, bJ));
+            inv[i] = jdiv(1.0f, adiag);
+            depth[i] = -dot(sub(pA, pB), n[i]);
+        }
+    }
+    const V ref0 = mulMv(frame_col(F, 0), xa.b), ref1 = mulMv(frame_col(F, 1), xa.b);
+    const V swing = mulMv(frame_col(F + 3, 1), xb.b);
+    const float angle = atan2_fast(dot(swing, ref0), dot(swing, ref1));
+    const float4 st = J.set[j];   // lower, upper, softness, bias
+    float correction = 0.0f, sign = 0.0f;
+    if (st.x < st.y) {
+        if (angle <= __fmul_rn(st.x, st.z)) {
+            correction = __fsub_rn(st.x, angle);
+            sign = 1.0f;
+        } else if (angle >= __fmul_rn(st.y, st.z)) {
+            correction = __fsub_rn(st.y, angle);
+            sign = -1.0f;
+        }
+    }
+    const V axisA = mulMv(frame_col(F, 2), xa.b), axisB = mulMv(frame_col(F + 3, 2), xb.b);
+    const float kHinge = jdiv(1.0f, __fadd_rn(ang_denom(IA, axisA), ang_denom(IB, axisA)));
+    J.r1[j] = f4(r1, 0.0f);
+    J.r2[j] = f4(r2, 0.0f);
+    J.dep[j] = make_float4(depth[0], depth[1], depth[2], 0.0f);
+    float4* H = J.hs + HINGE_STEP_F4 * j;
+    H[0] = f4(n[0], inv[0]);
+    H[1] = f4(n[1], inv[1]);
+    H[2] = f4(n[2], inv[2]);
+    H[3] = f4(axisA, kHinge);
+    H[4] = f4(axisB, correction);
+    H[5] = make_float4(sign, 0.0f, 0.0f, 0.0f);
+}
+
 __global__ void k_joint_setup(DevWorld w, SolverBuffers sb) {
     const DevJoints& J = sb.J;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -959,6 +1041,10 @@ __global__ void k_joint_setup(DevWorld w, SolverBuffers sb) {
     J.act[j] = on;
     if (!on) return;
     J.imp[j] = 0.0f;
+    if ((J.kind[j] & JK_TYPE) == JOINT_HINGE) {
+        hinge_setup(w, J, j, a, b);
+        return;
+    }
     const Xf xa = joint_xf(w, a), xb = joint_xf(w, b);
     const float4 la = w.iloc[a], lb = b >= 0 ? w.iloc[b] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const V iA = mk(la.x, la.y, la.z), iB = mk(lb.x, lb.y, lb.z);
@@ -1026,6 +1112,92 @@ JBD void joint_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
     if (imA != 0.0f) gstore(w, a, vA, wA);
     if (b >= 0 && imB != 0.0f) gstore(w, b, vB, wB);
     __stcg(J.imp + j, acc);
+}
+
+// RigidBody.applyTorqueImpulse (dynamics/RigidBody.java:405-411).  A body without mass has a
+// zero inverse inertia: the reference adds a zero vector, here it is skipped.
+JBD void torque_impulse(V& ang, float im, const M& iw, V t) {
+    if (im == 0.0f) return;
+    ang = add(ang, mulMv(t, iw));
+}
+
+// HingeConstraint.solveConstraint (HingeConstraint.java:342-533) of joint j on the bodies'
+// velocities in global memory: the linear rows (tau 0.3, the pivots' relative velocity taken once
+// before the three rows), then the angular part on the angular velocities as they stand after
+// them: the relative angular velocity orthogonal to the hinge axes and the axes' misalignment
+// removed by torque impulses, the limit with its clamped accumulated impulse, the motor clipped
+// per solve.
+JBD void hinge_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
+    const int a = J.a[j], b = J.b[j], kind = J.kind[j];
+    V vA, wA, vB = mk(0.0f, 0.0f, 0.0f), wB = mk(0.0f, 0.0f, 0.0f);
+    gload(w, a, vA, wA);
+    if (b >= 0) gload(w, b, vB, wB);
+    const float imA = w.iloc[a].w, imB = b >= 0 ? w.iloc[b].w : 0.0f;
+    const M IA = load_iw(w, a), IB = joint_iw(w, b);
+    const float4* H = J.hs + HINGE_STEP_F4 * j;
+    float acc = __ldcg(J.imp + j);
+    if (!(kind & JK_ANGULAR_ONLY)) {
+        const float4 q1 = J.r1[j], q2 = J.r2[j], dp = J.dep[j];
+        const V r1 = mk(q1.x, q1.y, q1.z), r2 = mk(q2.x, q2.y, q2.z);
+        const V vel = sub(add(crs(wA, r1), vA), add(crs(wB, r2), vB));
+        for (int i = 0; i < 3; i++) {
+            const float4 h = H[i];
+            const V n = mk(h.x, h.y, h.z);
+            const float depth = i == 0 ? dp.x : (i == 1 ? dp.y : dp.z);
+            const float relVel = dot(n, vel);
+            const float impulse = __fsub_rn(__fmul_rn(jdiv(__fmul_rn(depth, 0.3f), dt), h.w), __fmul_rn(relVel, h.w));
+            acc = __fadd_rn(acc, impulse);
+            const V iv = scl(n, impulse);
+            body_impulse(vA, wA, imA, IA, iv, r1);
+            body_impulse(vB, wB, imB, IB, scl(iv, -1.0f), r2);
+        }
+    }
+    const float4 ha = H[3], hb = H[4], hl = __ldcg(H + 5);
+    const V axisA = mk(ha.x, ha.y, ha.z), axisB = mk(hb.x, hb.y, hb.z);
+    const float kHinge = ha.w;
+    const float4 st = J.set[j], s2 = J.set2[j];   // (lower, upper, softness, bias), (relaxation, target, max impulse)
+    const V angVelA = wA, angVelB = wB;
+    const V aroundA = scl(axisA, dot(axisA, angVelA)), aroundB = scl(axisB, dot(axisB, angVelB));
+    V vro = sub(sub(angVelA, aroundA), sub(angVelB, aroundB));
+    if (len(vro) > 0.00001f) {
+        const V n = nor(vro);
+        const float denom = __fadd_rn(ang_denom(IA, n), ang_denom(IB, n));
+        vro = scl(vro, __fmul_rn(jdiv(1.0f, denom), s2.x));
+    }
+    V err = scl(scl(crs(axisA, axisB), -1.0f), jdiv(1.0f, dt));
+    if (len(err) > 0.00001f) {
+        const V n2 = nor(err);
+        const float denom2 = __fadd_rn(ang_denom(IA, n2), ang_denom(IB, n2));
+        err = scl(err, __fmul_rn(jdiv(1.0f, denom2), 1.0f));
+    }
+    torque_impulse(wA, imA, IA, add(scl(vro, -1.0f), err));
+    torque_impulse(wB, imB, IB, sub(vro, err));
+    float accLimit = hl.y;
+    if (hl.x != 0.0f) {   // solveLimit
+        const float amplitude = __fmul_rn(__fadd_rn(__fmul_rn(dot(sub(angVelB, angVelA), axisA), s2.x),
+                                                    __fmul_rn(__fmul_rn(hb.w, jdiv(1.0f, dt)), st.w)), hl.x);
+        float impulseMag = __fmul_rn(amplitude, kHinge);
+        const float temp = accLimit;
+        accLimit = jmax(__fadd_rn(accLimit, impulseMag), 0.0f);
+        impulseMag = __fsub_rn(accLimit, temp);
+        const V imp = scl(axisA, __fmul_rn(impulseMag, hl.x));
+        torque_impulse(wA, imA, IA, imp);
+        torque_impulse(wB, imB, IB, scl(imp, -1.0f));
+    }
+    if (kind & JK_MOTOR) {
+        const V zero = mk(0.0f, 0.0f, 0.0f);
+        const float projRelVel = dot(sub(aroundA, aroundB), axisA);
+        const float unclipped = __fmul_rn(kHinge, __fsub_rn(s2.y, projRelVel));
+        float clipped = unclipped > s2.z ? s2.z : unclipped;
+        clipped = clipped < -s2.z ? -s2.z : clipped;
+        const V motorImp = scl(axisA, clipped);
+        torque_impulse(wA, imA, IA, add(motorImp, zero));
+        torque_impulse(wB, imB, IB, sub(scl(motorImp, -1.0f), zero));
+    }
+    if (imA != 0.0f) gstore(w, a, vA, wA);
+    if (b >= 0 && imB != 0.0f) gstore(w, b, vB, wB);
+    __stcg(J.imp + j, acc);
+    __stcg(&J.hs[HINGE_STEP_F4 * j + 5].y, accLimit);
 }
 
 
@@ -1270,7 +1442,9 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                     const int j0 = sb.J.colStart[c], j1 = sb.J.colStart[c + 1];
                     for (int q = j0 + spread; q < j1; q += nth) {
                         const int j = sb.J.order[q];
-                        if (sb.J.act[j]) joint_solve(w, sb.J, j, dt);
+                        if (!sb.J.act[j]) continue;
+                        if ((sb.J.kind[j] & JK_TYPE) == JOINT_HINGE) hinge_solve(w, sb.J, j, dt);
+                        else joint_solve(w, sb.J, j, dt);
                     }
                     grid_barrier(w.ctr, nb, barK);
                 }

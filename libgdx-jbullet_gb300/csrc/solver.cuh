@@ -15,15 +15,28 @@ constexpr int PART_MAX_BODIES = 2048; // bodies of one part (velocities staged i
 // (the broadphase's sorted leaf order: Morton code with the batch world in the high bits).
 // World parts: every world holds at most PART_MAX_BODIES finite bodies, and each world is one
 // part.  Range parts otherwise: nParts equal ranges of the order.
-// Point-to-point joints (jbgpu_world_add_point2point), uploaded by the host when they change.
+// Joints (jbgpu_world_add_point2point, jbgpu_world_add_hinge), uploaded by the host when they
+// change.
+constexpr int JOINT_P2P = 0;
+constexpr int JOINT_HINGE = 1;
+constexpr int JK_TYPE = 0xff;         // kind: type in the low byte, hinge switches above it
+constexpr int JK_ANGULAR_ONLY = 1 << 8;
+constexpr int JK_MOTOR = 1 << 9;
+constexpr int HINGE_STEP_F4 = 6;      // float4s of a hinge's per-step state
 struct DevJoints {
     int n = 0;                    // joints
     int nCol = 0;                 // colours: first fit in index order over the joints' dynamic bodies
+    int* kind = nullptr;          // JOINT_P2P / JOINT_HINGE | JK_ANGULAR_ONLY | JK_MOTOR
     int* a = nullptr;             // body A of each joint
     int* b = nullptr;             // body B, -1 for the fixed body
-    float4* pivA = nullptr;       // pivotInA, pivotInB (xyz)
+    float4* pivA = nullptr;       // pivotInA, pivotInB (xyz); a hinge's frame origins
     float4* pivB = nullptr;
-    float4* set = nullptr;        // tau, damping, impulse clamp
+    float4* set = nullptr;        // p2p: tau, damping, impulse clamp; hinge: lower, upper limit, softness, bias
+    float4* set2 = nullptr;       // hinge: relaxation factor, motor target velocity, max motor impulse
+    float4* frame = nullptr;      // hinge: rbAFrame basis rows (3), then rbBFrame basis rows (3)
+    float4* hs = nullptr;         // hinge per step (HINGE_STEP_F4 each): axis n_i with 1/Adiag_i (3),
+                                  // world hinge axis of A with kHinge, of B with the limit correction,
+                                  // (limit sign, accumulated limit impulse, 0, 0)
     int* order = nullptr;         // joints by (colour, index)
     int* colStart = nullptr;      // nCol + 1 offsets into order
     float4* r1 = nullptr;         // per step: pivot A - centre of A, 1/Adiag of axis 0 in .w

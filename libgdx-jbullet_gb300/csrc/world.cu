@@ -94,8 +94,8 @@ struct jbgpu_world {
     bool planesDirty = true;
     std::vector<int> worldFinite;   // finite (non-plane) bodies per batch world
     // point-to-point joints (host copy; uploaded to sb.J when they change)
-    std::vector<int> jA, jB;
-    std::vector<float4> jPivA, jPivB, jSet;
+    std::vector<int> jKind, jA, jB;
+    std::vector<float4> jPivA, jPivB, jSet, jSet2, jFrame;   // jFrame: 6 per joint
     bool jointsDirty = false;
     int capJoints = 0;
     bool orderValid = false;        // the broadphase leaf order covers every body added
@@ -467,8 +467,10 @@ int sync_joints(jbgpu_world* w) {
     if (n > w->capJoints) {
         dfree(J.a); dfree(J.b); dfree(J.pivA); dfree(J.pivB); dfree(J.set); dfree(J.order); dfree(J.colStart);
         dfree(J.r1); dfree(J.r2); dfree(J.dep); dfree(J.imp); dfree(J.act);
+        dfree(J.kind); dfree(J.set2); dfree(J.frame); dfree(J.hs);
         const int c = std::max(n, 2 * w->capJoints);
         CK(dalloc(&J.a, c)); CK(dalloc(&J.b, c)); CK(dalloc(&J.pivA, c)); CK(dalloc(&J.pivB, c)); CK(dalloc(&J.set, c));
+        CK(dalloc(&J.kind, c)); CK(dalloc(&J.set2, c)); CK(dalloc(&J.frame, 6 * c)); CK(dalloc(&J.hs, HINGE_STEP_F4 * c));
         CK(dalloc(&J.order, c)); CK(dalloc(&J.colStart, c + 1)); CK(dalloc(&J.r1, c)); CK(dalloc(&J.r2, c));
         CK(dalloc(&J.dep, c)); CK(dalloc(&J.imp, c)); CK(dalloc(&J.act, c));
         CK(cudaMemset(J.imp, 0, sizeof(float) * c));
@@ -502,6 +504,9 @@ int sync_joints(jbgpu_world* w) {
     CK(cudaMemcpyAsync(J.pivA, w->jPivA.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(J.pivB, w->jPivB.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(J.set, w->jSet.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.kind, w->jKind.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.set2, w->jSet2.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.frame, w->jFrame.data(), sizeof(float4) * 6 * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(J.order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(J.colStart, colStart.data(), sizeof(int) * (nCol + 1), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
@@ -792,6 +797,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
         DevJoints& J = V.J;
         dfree(J.a); dfree(J.b); dfree(J.pivA); dfree(J.pivB); dfree(J.set); dfree(J.order); dfree(J.colStart);
         dfree(J.r1); dfree(J.r2); dfree(J.dep); dfree(J.imp); dfree(J.act);
+        dfree(J.kind); dfree(J.set2); dfree(J.frame); dfree(J.hs);
     }
     dfree(V.nIslChunks);
     if (V.islScratch) cudaFree(V.islScratch);
@@ -1094,11 +1100,14 @@ int jbgpu_world_add_point2point(jbgpu_world* w, int32_t a, int32_t b, const floa
     if (!w || !pa || !pb) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null argument");
     if (a < 0 || a >= w->nBodies || b < -1 || b >= w->nBodies || a == b)
         return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint bodies");
+    w->jKind.push_back(JOINT_P2P);
     w->jA.push_back(a);
     w->jB.push_back(b);
     w->jPivA.push_back(make_float4(pa[0], pa[1], pa[2], 0.0f));
     w->jPivB.push_back(make_float4(pb[0], pb[1], pb[2], 0.0f));
     w->jSet.push_back(make_float4(0.3f, 1.0f, 0.0f, 0.0f));   // ConstraintSetting defaults
+    w->jSet2.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (int r = 0; r < 6; r++) w->jFrame.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     w->jointsDirty = true;
     if (id) *id = (int32_t)w->jA.size() - 1;
     return JBGPU_OK;
@@ -1106,7 +1115,60 @@ int jbgpu_world_add_point2point(jbgpu_world* w, int32_t a, int32_t b, const floa
 
 int jbgpu_world_set_joint_setting(jbgpu_world* w, int32_t id, float tau, float damping, float clamp) {
     if (!w || id < 0 || id >= (int)w->jA.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
+    if (w->jKind[id] != JOINT_P2P) return fail(JBGPU_ERR_INVALID_ARGUMENT, "not a point-to-point joint");
     w->jSet[id] = make_float4(tau, damping, clamp, 0.0f);
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_add_hinge(jbgpu_world* w, int32_t a, int32_t b, const float fa[12], const float fb[12], int32_t* id) {
+    if (!w || !fa || !fb) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (a < 0 || a >= w->nBodies || b < -1 || b >= w->nBodies || a == b)
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint bodies");
+    w->jKind.push_back(JOINT_HINGE);
+    w->jA.push_back(a);
+    w->jB.push_back(b);
+    w->jPivA.push_back(make_float4(fa[9], fa[10], fa[11], 0.0f));
+    w->jPivB.push_back(make_float4(fb[9], fb[10], fb[11], 0.0f));
+    w->jSet.push_back(make_float4(1e30f, -1e30f, 0.9f, 0.3f));   // free: lower > upper; softness, bias
+    w->jSet2.push_back(make_float4(1.0f, 0.0f, 0.0f, 0.0f));     // relaxation, motor target, max motor impulse
+    for (const float* f : {fa, fb})
+        for (int r = 0; r < 3; r++) w->jFrame.push_back(make_float4(f[r * 3], f[r * 3 + 1], f[r * 3 + 2], 0.0f));
+    w->jointsDirty = true;
+    if (id) *id = (int32_t)w->jA.size() - 1;
+    return JBGPU_OK;
+}
+
+static int hinge_id(jbgpu_world* w, int32_t id) {
+    if (!w || id < 0 || id >= (int)w->jA.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
+    if ((w->jKind[id] & JK_TYPE) != JOINT_HINGE) return fail(JBGPU_ERR_INVALID_ARGUMENT, "not a hinge");
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_hinge_limit(jbgpu_world* w, int32_t id, float low, float high, float softness, float bias,
+                                float relaxation) {
+    int rc = hinge_id(w, id);
+    if (rc) return rc;
+    w->jSet[id] = make_float4(low, high, softness, bias);
+    w->jSet2[id].x = relaxation;
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_enable_hinge_motor(jbgpu_world* w, int32_t id, int32_t enable, float target, float maxImpulse) {
+    int rc = hinge_id(w, id);
+    if (rc) return rc;
+    w->jKind[id] = enable ? (w->jKind[id] | JK_MOTOR) : (w->jKind[id] & ~JK_MOTOR);
+    w->jSet2[id].y = target;
+    w->jSet2[id].z = maxImpulse;
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_hinge_angular_only(jbgpu_world* w, int32_t id, int32_t on) {
+    int rc = hinge_id(w, id);
+    if (rc) return rc;
+    w->jKind[id] = on ? (w->jKind[id] | JK_ANGULAR_ONLY) : (w->jKind[id] & ~JK_ANGULAR_ONLY);
     w->jointsDirty = true;
     return JBGPU_OK;
 }

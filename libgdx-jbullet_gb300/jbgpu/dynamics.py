@@ -222,6 +222,114 @@ class Point2PointConstraint:
         return float(self._world._g.joint_impulses()[self._id])
 
 
+class HingeConstraint:
+    """dynamics/constraintsolver/HingeConstraint.java:44-620, with its four constructors:
+    HingeConstraint(rbA, rbB, pivotInA, pivotInB, axisInA, axisInB), HingeConstraint(rbA,
+    pivotInA, axisInA), HingeConstraint(rbA, rbB, rbAFrame, rbBFrame) and HingeConstraint(rbA,
+    rbAFrame) (frames as Transform).  The frames are computed as the reference's constructors
+    compute them (jbgpu.frames) from the bodies' transforms at construction."""
+
+    def __init__(self, rbA, *args):
+        from . import frames
+        self.rbA = rbA
+        ta = rbA.getCenterOfMassTransform()
+        if len(args) == 5:
+            self.rbB, pa, pb, axa, axb = args
+            fa, fb = frames.hinge_frames_two_bodies(ta.basis, pa, pb, axa, axb)
+        elif len(args) == 2 and not isinstance(args[0], Transform):
+            self.rbB = None
+            fa, fb = frames.hinge_frames_one_body(ta.as12(), args[0], args[1])
+        elif len(args) == 3:
+            self.rbB = args[0]
+            fa, fb = frames.hinge_frames_from_frames(ta.as12(), args[1].as12(), args[2].as12())
+        elif len(args) == 1:
+            self.rbB = None
+            fa, fb = frames.hinge_frames_from_frames(ta.as12(), args[0].as12())
+        else:
+            raise TypeError("HingeConstraint(rbA, rbB, pivotInA, pivotInB, axisInA, axisInB), (rbA, pivotInA, axisInA), "
+                            "(rbA, rbB, rbAFrame, rbBFrame) or (rbA, rbAFrame)")
+        self.frameA, self.frameB = Transform.from12(fa), Transform.from12(fb)
+        self.lowerLimit, self.upperLimit = 1e30, -1e30
+        self.limitSoftness, self.biasFactor, self.relaxationFactor = 0.9, 0.3, 1.0
+        self.angularOnly = False
+        self.enableMotor, self.motorTargetVelocity, self.maxMotorImpulse = False, 0.0, 0.0
+        self._world = None
+        self._id = None
+
+    def _push(self):
+        g = self._world._g if self._world is not None else None
+        if g is None or self._id is None:
+            return
+        g.set_hinge_limit(self._id, self.lowerLimit, self.upperLimit, self.limitSoftness, self.biasFactor,
+                          self.relaxationFactor)
+        g.enable_hinge_motor(self._id, self.enableMotor, self.motorTargetVelocity, self.maxMotorImpulse)
+        g.set_hinge_angular_only(self._id, self.angularOnly)
+
+    def setLimit(self, low, high, softness=0.9, biasFactor=0.3, relaxationFactor=1.0):
+        self.lowerLimit, self.upperLimit = float(low), float(high)
+        self.limitSoftness, self.biasFactor, self.relaxationFactor = float(softness), float(biasFactor), float(relaxationFactor)
+        self._push()
+
+    def enableAngularMotor(self, enableMotor, targetVelocity, maxMotorImpulse):
+        self.enableMotor = bool(enableMotor)
+        self.motorTargetVelocity, self.maxMotorImpulse = float(targetVelocity), float(maxMotorImpulse)
+        self._push()
+
+    def setAngularOnly(self, angularOnly):
+        self.angularOnly = bool(angularOnly)
+        self._push()
+
+    def getRigidBodyA(self):
+        return self.rbA
+
+    def getRigidBodyB(self):
+        return self.rbB
+
+    def getAFrame(self):
+        return Transform(self.frameA.basis.copy(), self.frameA.origin.copy())
+
+    def getBFrame(self):
+        return Transform(self.frameB.basis.copy(), self.frameB.origin.copy())
+
+    def getLowerLimit(self):
+        return self.lowerLimit
+
+    def getUpperLimit(self):
+        return self.upperLimit
+
+    def getAngularOnly(self):
+        return self.angularOnly
+
+    def getEnableAngularMotor(self):
+        return self.enableMotor
+
+    def getMaxMotorImpulse(self):
+        return self.maxMotorImpulse
+
+    def getHingeAngle(self):
+        """HingeConstraint.getHingeAngle (java:535-555) from the bodies' current transforms,
+        with ScalarUtil.atan2Fast, in binary32."""
+        from . import frames
+        F = np.float32
+        ta = self.rbA.getCenterOfMassTransform()
+        tb = self.rbB.getCenterOfMassTransform() if self.rbB is not None else Transform()
+        ref0 = frames._mulMv(ta.basis, frames._col(self.frameA.basis, 0))
+        ref1 = frames._mulMv(ta.basis, frames._col(self.frameA.basis, 1))
+        swing = frames._mulMv(tb.basis, frames._col(self.frameB.basis, 1))
+        y, x = frames._dot(swing, ref0), frames._dot(swing, ref1)
+        c1 = F(F(6.283185307179586232) * F(0.5)) / F(4.0)
+        c2 = F(3.0) * c1
+        ay = abs(y)
+        angle = c1 - c1 * ((x - ay) / (x + ay)) if x >= 0 else c2 - c1 * ((x + ay) / (ay - x))
+        return float(-angle if y < 0 else angle)
+
+    def getAppliedImpulse(self):
+        """TypedConstraint.getAppliedImpulse: the sum of the linear rows' impulses of the last solve."""
+        if self._world is None or self._world._g is None:
+            return 0.0
+        return float(self._world._g.joint_impulses()[self._id])
+
+
 class DiscreteDynamicsWorld:
     def __init__(self, dispatcher=None, pairCache=None, constraintSolver=None, collisionConfiguration=None, device=0):
         self._gravity = (0.0, -10.0, 0.0)
@@ -291,6 +399,10 @@ class DiscreteDynamicsWorld:
             self._upload()
         for c in self._constraints[self._sent:]:
             b = -1 if c.rbB is None else c.rbB._index
+            if isinstance(c, HingeConstraint):
+                c._id = self._g.add_hinge(c.rbA._index, b, c.frameA.as12(), c.frameB.as12())
+                c._push()
+                continue
             c._id = self._g.add_point2point(c.rbA._index, b, c.pivotInA, c.pivotInB)
             st = c.setting
             self._g.set_joint_setting(c._id, st.tau, st.damping, st.impulseClamp)

@@ -60,6 +60,11 @@ def lib():
                                              C.POINTER(C.c_int32)], C.c_int),
             "jbgpu_world_set_joint_setting": ([C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_float], C.c_int),
             "jbgpu_world_get_joint_impulses": ([C.c_void_p, _abi.f32p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+            "jbgpu_world_add_hinge": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.POINTER(C.c_int32)],
+                                      C.c_int),
+            "jbgpu_world_set_hinge_limit": ([C.c_void_p, C.c_int32] + [C.c_float] * 5, C.c_int),
+            "jbgpu_world_enable_hinge_motor": ([C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float], C.c_int),
+            "jbgpu_world_set_hinge_angular_only": ([C.c_void_p, C.c_int32, C.c_int32], C.c_int),
             "jbgpu_world_phase_times": ([C.c_void_p, P(C.c_double), C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_profile_counters": ([C.c_void_p, P(_abi.Counters), C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_narrowphase_static": ([C.c_void_p, C.c_int32], C.c_int),
@@ -92,7 +97,8 @@ EXPORTED = [
     "jbgpu_world_get_manifolds", "jbgpu_world_set_manifolds", "jbgpu_world_get_solver_order", "jbgpu_world_counters",
     "jbgpu_world_apply_forces", "jbgpu_world_get_transforms", "jbgpu_world_set_profiling", "jbgpu_world_phase_times",
     "jbgpu_world_profile_counters", "jbgpu_world_timer", "jbgpu_world_add_point2point", "jbgpu_world_set_joint_setting",
-    "jbgpu_world_get_joint_impulses",
+    "jbgpu_world_get_joint_impulses", "jbgpu_world_add_hinge", "jbgpu_world_set_hinge_limit",
+    "jbgpu_world_enable_hinge_motor", "jbgpu_world_set_hinge_angular_only",
 ]
 
 
@@ -219,8 +225,36 @@ class GpuWorld:
         check(lib().jbgpu_world_get_joint_impulses(self.h, out.ctypes.data_as(_abi.f32p), n.value, C.byref(n)))
         return out[:n.value].copy()
 
+    def add_hinge(self, a, b, frame_a, frame_b):
+        """Hinge between bodies a and b (b = -1: the fixed body) with the constraint frames as
+        HingeConstraint holds them (12 floats each: basis row-major, origin); returns its id."""
+        fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
+        fb = np.ascontiguousarray(frame_b, np.float32).reshape(12)
+        jid = C.c_int32()
+        check(lib().jbgpu_world_add_hinge(self.h, a, b, fa.ctypes.data_as(_abi.f32p), fb.ctypes.data_as(_abi.f32p),
+                                          C.byref(jid)))
+        return jid.value
+
+    def set_hinge_limit(self, jid, low, high, softness=0.9, bias_factor=0.3, relaxation_factor=1.0):
+        check(lib().jbgpu_world_set_hinge_limit(self.h, jid, low, high, softness, bias_factor, relaxation_factor))
+
+    def enable_hinge_motor(self, jid, enable, target_velocity, max_motor_impulse):
+        check(lib().jbgpu_world_enable_hinge_motor(self.h, jid, 1 if enable else 0, target_velocity, max_motor_impulse))
+
+    def set_hinge_angular_only(self, jid, on):
+        check(lib().jbgpu_world_set_hinge_angular_only(self.h, jid, 1 if on else 0))
+
     def add_scene_joints(self, scene):
         for j in scene.meta.get("joints", []):
+            if j.get("type") == "hinge":
+                jid = self.add_hinge(j["a"], j["b"], j["frame_a"], j["frame_b"])
+                if "limit" in j:
+                    self.set_hinge_limit(jid, *j["limit"])
+                if "motor" in j:
+                    self.enable_hinge_motor(jid, *j["motor"])
+                if j.get("angular_only"):
+                    self.set_hinge_angular_only(jid, True)
+                continue
             jid = self.add_point2point(j["a"], j["b"], j["pivot_a"], j["pivot_b"])
             if "setting" in j:
                 self.set_joint_setting(jid, *j["setting"])

@@ -366,6 +366,92 @@ def jointed_chains(chains=6, links=8, loose=24, seed=0, spacing=2.5, top=10.0, s
                  meta={"seed": seed, "joints": joints}, **kw)
 
 
+def hinged_chains(chains=6, links=6, loose=16, seed=0, spacing=2.5, top=10.0, steps=240, worlds=1):
+    """Chains of boxes (half-extents 0.15 x 0.45 x 0.15) joined end to end by hinges, the top
+    link hinged to the fixed body (by pivot and axis for c even, by frame for c odd); chain c
+    swings about z (c even) or x (c odd), the inner hinges of chains with c % 3 == 1 carry limits
+    of +-0.6 rad, chains with c % 3 == 2 drive their top hinge with a motor.  Per world also a door (a 0.5 x 1.0 x 0.05 box) hinged to the fixed body by frame with
+    a motor, and two loose boxes held to the same orientation by an angular-only hinge.  Frames
+    come from the reference's constructors (jbgpu.frames).  meta["joints"]: type "hinge",
+    a, b, frame_a, frame_b, optional limit / motor / angular_only."""
+    from .frames import hinge_frames_two_bodies, hinge_frames_one_body, hinge_frames_from_frames
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE), {"type": _abi.SHAPE_BOX, "params": (0.15, 0.45, 0.15, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.3, 0.3, 0.3, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.5, 1.0, 0.05, 0.0), "points": None}]
+    side = int(np.ceil(np.sqrt(chains)))
+    all_bodies, joints, wid = [], [], []
+    base = 0
+    eye = np.eye(3, dtype=F)
+    for wi in range(worlds):
+        plane = _plane_body(0)
+        lb = _bodies(chains * links)
+        lb["shape"] = 1
+        lb["mass"] = 1.0
+        lb["local_inertia"] = box_inertia(1.0, (0.15, 0.45, 0.15))
+        pos = np.zeros((chains * links, 3), F)
+        for c in range(chains):
+            x0, z0 = (c % side - (side - 1) / 2.0) * spacing, (c // side - (side - 1) / 2.0) * spacing
+            v = rng.normal(0.0, 2.0)
+            for i in range(links):
+                k = c * links + i
+                pos[k] = (x0, top - 0.5 - 1.0 * i, z0)
+                lin = (0.0, 0.0, v * (i + 1) / links) if c % 2 else (v * (i + 1) / links, 0.0, 0.0)
+                lb["linear_velocity"][k] = lin
+        lb["transform"][:, 9:] = pos
+        door = _bodies(1)
+        door["shape"] = 3
+        door["mass"] = 2.0
+        door["local_inertia"] = box_inertia(2.0, (0.5, 1.0, 0.05))
+        half = side * spacing / 2.0
+        door["transform"][0, 9:] = (half + 2.0, 1.5, 0.0)
+        fb = _bodies(loose)
+        fb["shape"] = 2
+        fb["mass"] = 2.0
+        fb["local_inertia"] = box_inertia(2.0, (0.3, 0.3, 0.3))
+        fpos = np.stack([rng.uniform(-half, half, loose), rng.uniform(top + 1.0, top + 6.0, loose),
+                         rng.uniform(-half, half, loose)], 1)
+        _set_transforms(fb, random_rotations(rng, loose), fpos)
+        bodies = np.concatenate([plane, lb, door, fb])
+        first = base + 1
+        for c in range(chains):
+            axis = (1.0, 0.0, 0.0) if c % 2 else (0.0, 0.0, 1.0)
+            a0 = first + c * links
+            if c % 2:   # by frame: z along x (the pivot/axis form degenerates for an axis along x)
+                top_frame = np.concatenate([np.array([[0, 0, 1], [0, 1, 0], [-1, 0, 0]], F).reshape(9), [0.0, 0.5, 0.0]])
+                fa, fb_ = hinge_frames_from_frames(lb["transform"][c * links], top_frame)
+            else:
+                fa, fb_ = hinge_frames_one_body(lb["transform"][c * links], (0.0, 0.5, 0.0), axis)
+            j = {"type": "hinge", "a": a0, "b": -1, "frame_a": fa, "frame_b": fb_}
+            if c % 3 == 2:
+                j["motor"] = (True, 1.5, 0.05)
+            joints.append(j)
+            for i in range(links - 1):
+                fa, fb_ = hinge_frames_two_bodies(eye, (0.0, -0.5, 0.0), (0.0, 0.5, 0.0), axis, axis)
+                j = {"type": "hinge", "a": a0 + i, "b": a0 + i + 1, "frame_a": fa, "frame_b": fb_}
+                if c % 3 == 1:
+                    j["limit"] = (-0.6, 0.6, 0.9, 0.3, 1.0)
+                joints.append(j)
+        di = first + chains * links
+        door_frame = np.concatenate([np.array([[1, 0, 0], [0, 0, 1], [0, -1, 0]], F).reshape(9), [-0.5, 0.0, 0.0]])
+        fa, fb_ = hinge_frames_from_frames(door["transform"][0], door_frame)
+        joints.append({"type": "hinge", "a": di, "b": -1, "frame_a": fa, "frame_b": fb_, "motor": (True, -2.0, 5.0)})
+        if loose >= 2:
+            fa, fb_ = hinge_frames_two_bodies(fb["transform"][0, :9], (0.0, 0.0, 0.0), (0.0, 0.0, 0.0),
+                                              (0.0, 1.0, 0.0), (0.0, 1.0, 0.0))
+            joints.append({"type": "hinge", "a": di + 1, "b": di + 2, "frame_a": fa, "frame_b": fb_,
+                           "angular_only": True})
+        all_bodies.append(bodies)
+        wid.append(np.full(len(bodies), wi, np.int32))
+        base += len(bodies)
+    bodies = np.concatenate(all_bodies)
+    bodies["world"] = np.concatenate(wid)
+    kw = {"world_of_body": np.concatenate(wid)} if worlds > 1 else {}
+    return Scene("hinged_chains_%dx%d_w%d" % (chains, links, worlds), 1.0 / 60.0, steps,
+                 {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10}, shapes, bodies,
+                 meta={"seed": seed, "joints": joints}, **kw)
+
+
 def small_mixed(n=60, seed=0, region=(6.0, 8.0, 6.0), steps=200, with_hulls=True):
     """A small dense mix of every shape type for stage-by-stage parity checks."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -447,4 +533,5 @@ SCENES = {
     "small_mixed": small_mixed,
     "learned_warmstart": learned_warmstart,
     "jointed_chains": jointed_chains,
+    "hinged_chains": hinged_chains,
 }

@@ -114,6 +114,38 @@ void orc_set_joint_setting(void* h, int id, float tau, float damping, float clam
     j.damping = damping;
     j.impulseClamp = clamp;
 }
+// frames: basis row-major (9 floats) then origin (3), as HingeConstraint holds rbAFrame/rbBFrame
+int orc_add_hinge(void* h, int a, int b, const float* frameA, const float* frameB) {
+    World* w = (World*)h;
+    Joint j;
+    j.type = JOINT_HINGE;
+    j.a = a;
+    j.b = b;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            j.frameA.m[r][c] = frameA[r * 3 + c];
+            j.frameB.m[r][c] = frameB[r * 3 + c];
+        }
+    j.pivotA = v3(frameA[9], frameA[10], frameA[11]);
+    j.pivotB = v3(frameB[9], frameB[10], frameB[11]);
+    w->joints.push_back(j);
+    return (int)w->joints.size() - 1;
+}
+void orc_set_hinge_limit(void* h, int id, float low, float high, float softness, float bias, float relaxation) {
+    Joint& j = ((World*)h)->joints[id];
+    j.lowerLimit = low;
+    j.upperLimit = high;
+    j.limitSoftness = softness;
+    j.biasFactor = bias;
+    j.relaxationFactor = relaxation;
+}
+void orc_enable_hinge_motor(void* h, int id, int enable, float target, float maxImpulse) {
+    Joint& j = ((World*)h)->joints[id];
+    j.enableMotor = enable != 0;
+    j.motorTarget = target;
+    j.maxMotorImpulse = maxImpulse;
+}
+void orc_set_hinge_angular_only(void* h, int id, int on) { ((World*)h)->joints[id].angularOnly = on != 0; }
 int orc_get_joint_impulses(void* h, float* out, int cap) {
     const World* w = (const World*)h;
     const int n = (int)w->joints.size();

@@ -463,6 +463,145 @@ static void joint_solve(Joint& j, Body& A, Body& B, float timeStep) {
     }
 }
 
+// ScalarUtil.atan2Fast (linearmath/ScalarUtil.java:43-57): a first-order approximation.
+static float atan2_fast(float y, float x) {
+    const float c1 = SIMD_PI / 4.0f, c2 = 3.0f * c1;
+    const float ay = std::fabs(y);
+    float angle;
+    if (x >= 0.0f) {
+        float r = (x - ay) / (x + ay);
+        angle = c1 - c1 * r;
+    } else {
+        float r = (x + ay) / (ay - x);
+        angle = c2 - c1 * r;
+    }
+    return y < 0.0f ? -angle : angle;
+}
+
+static V3 col(const M3& m, int c) { return v3(m.m[0][c], m.m[1][c], m.m[2][c]); }
+
+// RigidBody.computeAngularImpulseDenominator (dynamics/RigidBody.java:534-541)
+static float ang_denom(const Body& b, V3 axis) { return dot(axis, mulMTv(axis, b.invInertiaWorld)); }
+
+// RigidBody.applyTorqueImpulse (dynamics/RigidBody.java:405-411): no mass check; a static
+// body's zero inverse inertia leaves its angular velocity as it is.
+static void apply_torque(Body& b, V3 t) { b.angvel = add(b.angvel, mulMv(t, b.invInertiaWorld)); }
+
+// HingeConstraint.getHingeAngle (HingeConstraint.java:535-555)
+static float hinge_angle(const Joint& j, const Body& A, const Body& B) {
+    V3 ref0 = mulMv(col(j.frameA, 0), A.xf.b);
+    V3 ref1 = mulMv(col(j.frameA, 1), A.xf.b);
+    V3 swing = mulMv(col(j.frameB, 1), B.xf.b);
+    return atan2_fast(dot(swing, ref0), dot(swing, ref1));
+}
+
+// HingeConstraint.buildJacobian (HingeConstraint.java:240-340): three linear rows along the
+// pivots' separation and its plane space (JacobianEntry.init, with the port's zero B-side
+// angular Jacobian), the limit state from the hinge angle and kHinge = 1 / (J W J') about
+// the hinge axis.  The angular JacobianEntries it also builds are never read by the solve.
+static void hinge_build(Joint& j, const Body& A, const Body& B) {
+    j.appliedImpulse = 0.0f;
+    if (!j.angularOnly) {
+        V3 pA = xf_apply(A.xf, j.pivotA), pB = xf_apply(B.xf, j.pivotB);
+        V3 relPos = sub(pB, pA);
+        if (len2(relPos) > FLT_EPS) j.normal[0] = nor(relPos);
+        else j.normal[0] = v3(1.0f, 0.0f, 0.0f);
+        plane_space1(j.normal[0], j.normal[1], j.normal[2]);
+        for (int i = 0; i < 3; i++) {
+            M3 w2A = transpose(A.xf.b), w2B = transpose(B.xf.b);
+            V3 r1 = sub(pA, A.xf.o), r2 = sub(pB, B.xf.o);
+            V3 aJ = mulMv(crs(r1, j.normal[i]), w2A);
+            V3 bJ = mulMv(crs(r2, r2), w2B);
+            V3 m0 = mulc(A.invInertiaLocal, aJ), m1 = mulc(B.invInertiaLocal, bJ);
+            j.adiag[i] = A.invMass + dot(m0, aJ) + B.invMass + dot(m1, bJ);
+        }
+    }
+    float angle = hinge_angle(j, A, B);
+    j.correction = 0.0f;
+    j.limitSign = 0.0f;
+    j.solveLimit = false;
+    j.accLimitImpulse = 0.0f;
+    if (j.lowerLimit < j.upperLimit) {
+        if (angle <= j.lowerLimit * j.limitSoftness) {
+            j.correction = j.lowerLimit - angle;
+            j.limitSign = 1.0f;
+            j.solveLimit = true;
+        } else if (angle >= j.upperLimit * j.limitSoftness) {
+            j.correction = j.upperLimit - angle;
+            j.limitSign = -1.0f;
+            j.solveLimit = true;
+        }
+    }
+    V3 axisA = mulMv(col(j.frameA, 2), A.xf.b);
+    j.kHinge = 1.0f / (ang_denom(A, axisA) + ang_denom(B, axisA));
+}
+
+// HingeConstraint.solveConstraint (HingeConstraint.java:342-533): the linear rows (tau 0.3,
+// the pivots' relative velocity taken once before the three rows), then the angular part on
+// the angular velocities as they stand after it: the relative angular velocity orthogonal to
+// the hinge axes and the axes' misalignment removed by torque impulses, the limit with its
+// clamped accumulated impulse, the motor clipped per solve.
+static void hinge_solve(Joint& j, Body& A, Body& B, float timeStep) {
+    V3 pA = xf_apply(A.xf, j.pivotA), pB = xf_apply(B.xf, j.pivotB);
+    const float tau = 0.3f;
+    if (!j.angularOnly) {
+        V3 r1 = sub(pA, A.xf.o), r2 = sub(pB, B.xf.o);
+        V3 vel = sub(add(crs(A.angvel, r1), A.linvel), add(crs(B.angvel, r2), B.linvel));
+        for (int i = 0; i < 3; i++) {
+            V3 n = j.normal[i];
+            float jacDiagABInv = 1.0f / j.adiag[i];
+            float relVel = dot(n, vel);
+            float depth = -dot(sub(pA, pB), n);
+            float impulse = depth * tau / timeStep * jacDiagABInv - relVel * jacDiagABInv;
+            j.appliedImpulse += impulse;
+            V3 iv = scl(n, impulse);
+            apply_impulse(A, iv, sub(pA, A.xf.o));
+            apply_impulse(B, scl(iv, -1.0f), sub(pB, B.xf.o));
+        }
+    }
+    V3 axisA = mulMv(col(j.frameA, 2), A.xf.b);
+    V3 axisB = mulMv(col(j.frameB, 2), B.xf.b);
+    V3 angVelA = A.angvel, angVelB = B.angvel;
+    V3 aroundA = scl(axisA, dot(axisA, angVelA));
+    V3 aroundB = scl(axisB, dot(axisB, angVelB));
+    V3 velrelOrthog = sub(sub(angVelA, aroundA), sub(angVelB, aroundB));
+    const float relaxation = 1.0f;
+    if (len(velrelOrthog) > 0.00001f) {
+        V3 n = nor(velrelOrthog);
+        float denom = ang_denom(A, n) + ang_denom(B, n);
+        velrelOrthog = scl(velrelOrthog, (1.0f / denom) * j.relaxationFactor);
+    }
+    V3 angularError = scl(scl(crs(axisA, axisB), -1.0f), 1.0f / timeStep);
+    if (len(angularError) > 0.00001f) {
+        V3 n2 = nor(angularError);
+        float denom2 = ang_denom(A, n2) + ang_denom(B, n2);
+        angularError = scl(angularError, (1.0f / denom2) * relaxation);
+    }
+    apply_torque(A, add(scl(velrelOrthog, -1.0f), angularError));
+    apply_torque(B, sub(velrelOrthog, angularError));
+    if (j.solveLimit) {
+        float amplitude = (dot(sub(angVelB, angVelA), axisA) * j.relaxationFactor + j.correction * (1.0f / timeStep) * j.biasFactor) * j.limitSign;
+        float impulseMag = amplitude * j.kHinge;
+        float temp = j.accLimitImpulse;
+        j.accLimitImpulse = jmax(j.accLimitImpulse + impulseMag, 0.0f);
+        impulseMag = j.accLimitImpulse - temp;
+        V3 imp = scl(axisA, impulseMag * j.limitSign);
+        apply_torque(A, imp);
+        apply_torque(B, scl(imp, -1.0f));
+    }
+    if (j.enableMotor) {
+        const V3 angularLimit = v3(0.0f, 0.0f, 0.0f);
+        float projRelVel = dot(sub(aroundA, aroundB), axisA);
+        float motorRelVel = j.motorTarget - projRelVel;
+        float unclipped = j.kHinge * motorRelVel;
+        float clipped = unclipped > j.maxMotorImpulse ? j.maxMotorImpulse : unclipped;
+        clipped = clipped < -j.maxMotorImpulse ? -j.maxMotorImpulse : clipped;
+        V3 motorImp = scl(axisA, clipped);
+        apply_torque(A, add(motorImp, angularLimit));
+        apply_torque(B, sub(scl(motorImp, -1.0f), angularLimit));
+    }
+}
+
 static void solve_group(World& w, const std::vector<int>& manifolds, const std::vector<int>& joints, float dt) {
     const Config& cfg = w.cfg;
     std::vector<SolverBody> sb;
@@ -594,7 +733,11 @@ static void solve_group(World& w, const std::vector<int>& manifolds, const std::
     w.counters.solverRows += (int)rows.size();
     Body fixedB = fixed_body();
     auto jointBody = [&](int b) -> Body& { return b >= 0 ? w.bodies[b] : fixedB; };
-    for (int jk : joints) joint_build(w.joints[jk], jointBody(w.joints[jk].a), jointBody(w.joints[jk].b));
+    for (int jk : joints) {
+        Joint& J = w.joints[jk];
+        if (J.type == JOINT_HINGE) hinge_build(J, jointBody(J.a), jointBody(J.b));
+        else joint_build(J, jointBody(J.a), jointBody(J.b));
+    }
     // solveGroupCacheFriendlyIterations (java:788-890), split impulse off.  With a residual
     // tolerance the iterations of an island (the group a reference solveGroup call receives)
     // stop once max|delta lambda| / max(max|lambda|, 1e-6) over its rows is within it (the
@@ -641,7 +784,8 @@ static void solve_group(World& w, const std::vector<int>& manifolds, const std::
                     b->linvel = sb[b->companionId].linvel;
                     b->angvel = sb[b->companionId].angvel;
                 }
-            joint_solve(J, A, B, dt);
+            if (J.type == JOINT_HINGE) hinge_solve(J, A, B, dt);
+            else joint_solve(J, A, B, dt);
             for (Body* b : {&A, &B})
                 if (b->islandTag >= 0 && b->companionId >= 0 && sb[b->companionId].invMass != 0.0f) {
                     sb[b->companionId].linvel = b->linvel;

@@ -87,12 +87,26 @@ struct Body {            // dynamics/RigidBody.java + collision/dispatch/Collisi
 // Point2PointConstraint (dynamics/constraintsolver/Point2PointConstraint.java:37-70) with its
 // ConstraintSetting (java:202-206).  b = -1 stands for TypedConstraint's fixed body: static, at
 // the origin with the identity basis, zero mass and inertia (TypedConstraint.java:44-49).
+// HingeConstraint (dynamics/constraintsolver/HingeConstraint.java:44-620) holds the two
+// constraint frames as its constructors leave them (rbAFrame, rbBFrame: z is the hinge axis,
+// B's axis column already flipped), its limit (free: lower 1e30 > upper -1e30), motor and
+// angularOnly switch.
+enum JointType { JOINT_P2P = 0, JOINT_HINGE = 1 };
 struct Joint {
+    int type = JOINT_P2P;
     int a = -1, b = -1;
-    V3 pivotA{0, 0, 0}, pivotB{0, 0, 0};   // pivotInA, pivotInB
+    V3 pivotA{0, 0, 0}, pivotB{0, 0, 0};   // pivotInA, pivotInB (hinge: the frames' origins)
     float tau = 0.3f, damping = 1.0f, impulseClamp = 0.0f;
     float appliedImpulse = 0.0f;           // TypedConstraint.appliedImpulse after the last solve
     float adiag[3] = {0, 0, 0};            // JacobianEntry.Adiag per axis, from buildJacobian
+    // hinge
+    M3 frameA = m3_identity(), frameB = m3_identity();   // rbAFrame.basis, rbBFrame.basis
+    bool angularOnly = false, enableMotor = false;
+    float motorTarget = 0.0f, maxMotorImpulse = 0.0f;
+    float lowerLimit = 1e30f, upperLimit = -1e30f, limitSoftness = 0.9f, biasFactor = 0.3f, relaxationFactor = 1.0f;
+    V3 normal[3];                          // buildJacobian: the linear rows' axes
+    float kHinge = 0.0f, correction = 0.0f, limitSign = 0.0f, accLimitImpulse = 0.0f;
+    bool solveLimit = false;
 };
 
 struct Config {

@@ -53,6 +53,10 @@ def lib():
         L.orc_add_point2point.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
         L.orc_set_joint_setting.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float]
         L.orc_get_joint_impulses.argtypes = [C.c_void_p, _abi.f32p, C.c_int]
+        L.orc_add_hinge.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
+        L.orc_set_hinge_limit.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 5
+        L.orc_enable_hinge_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float]
+        L.orc_set_hinge_angular_only.argtypes = [C.c_void_p, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -98,8 +102,33 @@ class OracleWorld:
         lib().orc_get_joint_impulses(self.h, _fp(out), n)
         return out[:n].copy()
 
+    def add_hinge(self, a, b, frame_a, frame_b):
+        """HingeConstraint between bodies a and b (b = -1: the fixed body) with the constraint
+        frames as the reference holds them (12 floats each: basis row-major, origin)."""
+        fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
+        fb = np.ascontiguousarray(frame_b, np.float32).reshape(12)
+        return lib().orc_add_hinge(self.h, a, b, _fp(fa), _fp(fb))
+
+    def set_hinge_limit(self, jid, low, high, softness=0.9, bias_factor=0.3, relaxation_factor=1.0):
+        lib().orc_set_hinge_limit(self.h, jid, low, high, softness, bias_factor, relaxation_factor)
+
+    def enable_hinge_motor(self, jid, enable, target_velocity, max_motor_impulse):
+        lib().orc_enable_hinge_motor(self.h, jid, 1 if enable else 0, target_velocity, max_motor_impulse)
+
+    def set_hinge_angular_only(self, jid, on):
+        lib().orc_set_hinge_angular_only(self.h, jid, 1 if on else 0)
+
     def add_scene_joints(self, scene):
         for j in scene.meta.get("joints", []):
+            if j.get("type") == "hinge":
+                jid = self.add_hinge(j["a"], j["b"], j["frame_a"], j["frame_b"])
+                if "limit" in j:
+                    self.set_hinge_limit(jid, *j["limit"])
+                if "motor" in j:
+                    self.enable_hinge_motor(jid, *j["motor"])
+                if j.get("angular_only"):
+                    self.set_hinge_angular_only(jid, True)
+                continue
             jid = self.add_point2point(j["a"], j["b"], j["pivot_a"], j["pivot_b"])
             if "setting" in j:
                 self.set_joint_setting(jid, *j["setting"])

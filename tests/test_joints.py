@@ -136,3 +136,161 @@ def test_mirror_pendulum_reads_like_the_reference(gpu_lib, oracle_lib):
         o.step_simulation(1.0 / 60.0, 1, 1.0 / 60.0)
     assert not H.compare_state(o.get_state(), g.get_state())
     world.close()
+
+
+# ---- hinges (dynamics/constraintsolver/HingeConstraint.java) ------------------------------
+def _hinge_state(state, joints):
+    """Per hinge: pivot gap, 1 - |cos| between the two world hinge axes, the relative angle
+    about the hinge (exact atan2 of the reference's getHingeAngle projections)."""
+    xf = state["transform"]
+    out = []
+    for j in joints:
+        a, b = j["a"], j["b"]
+        fa, fb = np.asarray(j["frame_a"], np.float64), np.asarray(j["frame_b"], np.float64)
+        Ra = xf[a, :9].reshape(3, 3).astype(np.float64)
+        Rb = xf[b, :9].reshape(3, 3).astype(np.float64) if b >= 0 else np.eye(3)
+        ob = xf[b, 9:] if b >= 0 else np.zeros(3)
+        A, B = fa[:9].reshape(3, 3), fb[:9].reshape(3, 3)
+        gap = 0.0 if j.get("angular_only") else np.linalg.norm(Ra @ fa[9:] + xf[a, 9:] - Rb @ fb[9:] - ob)
+        mis = 1.0 - abs((Ra @ A[:, 2]) @ (Rb @ B[:, 2]))
+        sw = Rb @ B[:, 1]
+        out.append((gap, mis, np.arctan2(sw @ (Ra @ A[:, 0]), sw @ (Ra @ A[:, 1]))))
+    return np.asarray(out)
+
+
+def test_hinge_frames_follow_the_constructors():
+    from jbgpu import frames
+    eye = np.eye(3, dtype=np.float32)
+    fa, fb = frames.hinge_frames_two_bodies(eye, (0, -0.5, 0), (0, 0.5, 0), (0, 0, 1), (0, 0, 1))
+    assert np.array_equal(fa[:9].reshape(3, 3), eye) and np.array_equal(fa[9:], [0, -0.5, 0])
+    assert np.array_equal(fb[:9].reshape(3, 3), np.diag([1, 1, -1]).astype(np.float32))
+    # axis along A's x: the reference picks -z and y for the other two columns
+    fa, fb = frames.hinge_frames_two_bodies(eye, (0, 0, 0), (0, 0, 0), (1, 0, 0), (1, 0, 0))
+    assert np.array_equal(fa[:9].reshape(3, 3), np.array([[0, 0, 1], [0, 1, 0], [-1, 0, 0]], np.float32))
+    # one body: B's frame sits at the pivot's world position; the rest angle is pi
+    t = np.concatenate([eye.reshape(9), [1.0, 2.0, 3.0]]).astype(np.float32)
+    fa, fb = frames.hinge_frames_one_body(t, (0, 0.5, 0), (0, 0, 1))
+    assert np.array_equal(fb[9:], [1.0, 2.5, 3.0])
+    A, B = fa[:9].reshape(3, 3), fb[:9].reshape(3, 3)
+    assert abs(abs(np.arctan2(B[:, 1] @ A[:, 0], B[:, 1] @ A[:, 1])) - np.pi) < 1e-6
+    # by frame: B's z column negated
+    fa, fb = frames.hinge_frames_from_frames(t, np.concatenate([eye.reshape(9), [0, 0, 0]]))
+    assert np.array_equal(fb[:9].reshape(3, 3), np.diag([1, 1, -1]).astype(np.float32))
+    for f in (fa, fb):
+        m = f[:9].reshape(3, 3)
+        assert np.allclose(m @ m.T, np.eye(3), atol=1e-6)
+
+
+def test_oracle_hinges_hold(oracle_lib):
+    """Hinged chains keep their pivots and axes together while they swing; the limited inner
+    hinges stay near +-0.6 rad; the door's motor brings it to its target speed."""
+    sc = scenes.hinged_chains(chains=6, links=5, loose=8, seed=1)
+    J = sc.meta["joints"]
+    o = pyoracle.OracleWorld(sc)
+    a0 = _hinge_state(o.get_state(), J)[:, 2]
+    steady = [k for k, j in enumerate(J) if "motor" not in j and not j.get("angular_only")]
+    limited = [k for k, j in enumerate(J) if "limit" in j]
+    worst = np.zeros(3)
+    for s in range(240):
+        o.step(sc.dt)
+        h = _hinge_state(o.get_state(), J)
+        if s >= 20:
+            worst = np.maximum(worst, [h[steady, 0].max(), h[steady, 1].max(), np.abs(h[limited, 2] - a0[limited]).max()])
+    assert o.counters()["status_flags"] == 0
+    assert worst[0] < 0.2 and worst[1] < 0.02, worst
+    assert worst[2] < 0.75, worst
+    door = 1 + 6 * 5
+    assert abs(o.get_state()["angular_velocity"][door, 1] + 2.0) < 1e-3
+    assert np.any(o.joint_impulses() != 0.0)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["world_part", "range_parts", "batched"])
+def test_gpu_hinges_bit_exact(gpu_lib, oracle_lib, case):
+    if case == "batched":
+        sc = scenes.hinged_chains(chains=3, links=4, loose=6, seed=6, worlds=3)
+    else:
+        sc = scenes.hinged_chains(chains=6, links=5, loose=16, seed=7)
+    cfg = dict(sc.config)
+    if case == "range_parts":
+        cfg["solver_parts"] = 5
+    g = GpuWorld(sc, config=_abi.default_config(**cfg))
+    o = pyoracle.OracleWorld(sc)
+    for s in range(200):
+        g.step(sc.dt)
+        if case == "range_parts":
+            o.set_explicit_order(g.solver_order())
+        o.step(sc.dt)
+        assert o.counters()["status_flags"] == 0, s
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+            assert not bs and not bm, (s, bs, bm)
+            assert np.array_equal(o.joint_impulses().view(np.uint32), g.joint_impulses().view(np.uint32)), s
+    assert g.counters()["status_flags"] == 0
+    g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_hinge_api_errors(gpu_lib):
+    sc = scenes.hinged_chains(chains=1, links=2, loose=0, seed=8)
+    g = GpuWorld(sc)
+    from jbgpu.lib import JbgpuError
+    p2p = g.add_point2point(1, 2, (0, 0, 0), (0, 0, 0))
+    with pytest.raises(JbgpuError):
+        g.set_joint_setting(0, 0.3, 1.0, 0.0)                   # a hinge has no ConstraintSetting
+    with pytest.raises(JbgpuError):
+        g.set_hinge_limit(p2p, -1.0, 1.0)                       # not a hinge
+    with pytest.raises(JbgpuError):
+        g.add_hinge(1, 1, np.zeros(12), np.zeros(12))          # a body hinged to itself
+    g.close()
+
+
+@pytest.mark.gpu
+def test_mirror_hinged_door(gpu_lib, oracle_lib):
+    """HingeConstraint through the mirror: a door hinged to the fixed body about its vertical
+    edge, driven by enableAngularMotor, and a limited hinge to a second panel; the GPU world
+    matches the same world built on the oracle bit for bit, the door turns at the motor's speed
+    and the limited panel stays within its limit."""
+    from jbgpu import dynamics as D
+    world = D.DiscreteDynamicsWorld()
+    world.setGravity((0.0, -9.81, 0.0))
+    world.addRigidBody(D.RigidBody(D.RigidBodyConstructionInfo(0.0, None, D.StaticPlaneShape((0.0, 1.0, 0.0), 0.0))))
+    shape = D.BoxShape((0.5, 1.0, 0.05))
+    panels = []
+    for i in range(2):
+        info = D.RigidBodyConstructionInfo(2.0, None, shape, shape.calculateLocalInertia(2.0))
+        info.startWorldTransform = D.Transform(origin=(1.1 * i, 1.5, 0.0))
+        panels.append(D.RigidBody(info))
+        world.addRigidBody(panels[-1])
+    door = D.HingeConstraint(panels[0], (-0.5, 0.0, 0.0), (0.0, 1.0, 0.0))
+    door.enableAngularMotor(True, -1.0, 5.0)
+    flap = D.HingeConstraint(panels[0], panels[1], (0.55, 0.0, 0.0), (-0.55, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 1.0, 0.0))
+    flap.setLimit(-0.3, 0.3)
+    world.addConstraint(door)
+    world.addConstraint(flap)
+    for _ in range(90):
+        world.stepSimulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    g = world._g
+    assert abs(panels[0].getAngularVelocity()[1] + 1.0) < 0.05
+    assert abs(flap.getHingeAngle()) < 0.45
+    joints = [{"type": "hinge", "a": 1, "b": -1, "frame_a": door.frameA.as12(), "frame_b": door.frameB.as12(),
+               "motor": (True, -1.0, 5.0)},
+              {"type": "hinge", "a": 1, "b": 2, "frame_a": flap.frameA.as12(), "frame_b": flap.frameB.as12(),
+               "limit": (-0.3, 0.3, 0.9, 0.3, 1.0)}]
+    shapes = [dict(scenes.PLANE), {"type": _abi.SHAPE_BOX, "params": (0.5, 1.0, 0.05, 0.0), "points": None}]
+    bodies = np.zeros(3, scenes.BODY_DTYPE)
+    for k in range(3):
+        bodies[k] = scenes._bodies(1)[0]
+    bodies["shape"] = (0, 1, 1)
+    bodies["mass"] = (0.0, 2.0, 2.0)
+    bodies["local_inertia"][1:] = scenes.box_inertia(2.0, (0.5, 1.0, 0.05))
+    bodies["transform"][1, 9:] = (0.0, 1.5, 0.0)
+    bodies["transform"][2, 9:] = (1.1, 1.5, 0.0)
+    sc = scenes.Scene("door", 1.0 / 60.0, 90, {"gravity": (0.0, -9.81, 0.0)}, shapes, bodies, meta={"joints": joints})
+    o = pyoracle.OracleWorld(sc)
+    for _ in range(90):
+        o.step_simulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    assert not H.compare_state(o.get_state(), g.get_state())
+    assert np.array_equal(o.joint_impulses().view(np.uint32), g.joint_impulses().view(np.uint32))
+    world.close()
