@@ -211,7 +211,18 @@ typedef struct jbgpu_counters {
     int32_t solver_islands;   /* residual mode: islands with solver rows in the last solve */
     int32_t solver_islands_converged;  /* ... of which reached the residual */
     int32_t solver_island_iterations;  /* ... sum over them of the iterations they took */
+    int32_t ray_replays;      /* rays of the last jbgpu_world_ray_test replayed in body order */
 } jbgpu_counters;
+
+/* One ray of a batch: CollisionWorld.ClosestRayResultCallback after the ray
+ * (collision/dispatch/CollisionWorld.java:697-729). */
+typedef struct jbgpu_ray_hit {
+    int32_t body;       /* collisionObject hit (body index), -1 when nothing was hit (hasHit() false) */
+    float   fraction;   /* closestHitFraction: 1 when nothing was hit */
+    float   normal[3];  /* hitNormalWorld: unit for convex shapes; for a static plane the triangle
+                           normal rotated to world space, not normalised, as the reference leaves it */
+    float   point[3];   /* hitPointWorld: from + fraction (to - from); 0 when nothing was hit */
+} jbgpu_ray_hit;
 
 /* ---- library -------------------------------------------------------------------- */
 const char* jbgpu_version(void);
@@ -257,6 +268,22 @@ int jbgpu_world_narrowphase_static(jbgpu_world* world, int32_t epa_slots);
 
 /* Wait for the world's stream. */
 int jbgpu_world_synchronize(jbgpu_world* world);
+
+/* CollisionWorld.rayTest(rayFromWorld, rayToWorld, new ClosestRayResultCallback(from, to)) for n
+ * rays at once (collision/dispatch/CollisionWorld.java:553-591, rayTestSingle 260-331):
+ * from and to hold n points (3 floats each); ray_world (NULL: every ray in world 0) the batch
+ * world each ray is cast in; filter_group / filter_mask are the callback's
+ * collisionFilterGroup / collisionFilterMask (the reference's defaults: 1 and -1).  Rays see the
+ * bodies' transforms after the last step.  hits receives one record per ray.  device_buffers
+ * != 0: from, to, ray_world and hits are device pointers and the call returns once the work is
+ * queued on the world's stream (jbgpu_world_synchronize waits for it); else host pointers, and
+ * the call returns with the hits written. */
+int jbgpu_world_ray_test(jbgpu_world* world, const float* from, const float* to, const int32_t* ray_world, int32_t n,
+                         int32_t filter_group, int32_t filter_mask, int32_t device_buffers, jbgpu_ray_hit* hits);
+/* Verification switch, no counterpart in the reference: all != 0 sends every ray of later
+ * jbgpu_world_ray_test calls through the in-order replay of the reference's object loop (the
+ * path rays take when the tree walk cannot decide them); results are the same either way. */
+int jbgpu_world_set_ray_replay(jbgpu_world* world, int32_t all);
 
 /* The iteration fields of the world's ContactSolverInfo, changed between steps as a caller of
  * the reference changes getSolverInfo().numIterations (dynamics/constraintsolver/

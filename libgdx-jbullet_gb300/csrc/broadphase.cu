@@ -317,6 +317,43 @@ static inline int gridn(int n, int b) { return (n + b - 1) / b; }
 // The tree over the Morton order is rebuilt every rebuildInterval steps and only refitted to the
 // new AABBs in between: a refitted tree bounds every body exactly, so the traversal finds the
 // same pair set whatever the tree's shape; only its cost depends on how stale the order is.
+// The tree over the finite bodies' current w.amin/w.amax: Morton keys of the box centres (the
+// batch world in the high bits), radix sort, world leaf ranges, Karras topology.  Boxes are
+// written by a refit.
+void broadphase_build_tree(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s) {
+    const int n = w.nBodies, nf = bb.nFinite;
+    bb.built = true;
+    bb.sinceBuild = 0;
+    cudaMemsetAsync(bb.bounds, 0, sizeof(unsigned) * 6, s);
+    cudaMemsetAsync(bb.bounds, 0xff, sizeof(unsigned) * 3, s);
+    k_bounds<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds); note_launch();
+    k_morton<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds, bb.mkeys, bb.sortedBody); note_launch();
+    radix_sort_pairs(bb.mkeys, bb.sortedBody, bb.mkeys_alt, bb.vals_alt, n, 32 + bb.worldBits, bb.sortScratch, s);
+    if (nf > 0) {
+        cudaMemsetAsync(bb.wstart, 0xff, sizeof(int) * bb.nWorlds, s);
+        cudaMemsetAsync(bb.wend, 0xff, sizeof(int) * bb.nWorlds, s);
+        cudaMemsetAsync(bb.wroot, 0xff, sizeof(int) * bb.nWorlds, s);
+        k_world_ranges<<<gridn(nf, 256), 256, 0, s>>>(bb.mkeys, nf, bb.wstart, bb.wend, bb.wroot); note_launch();
+        if (nf > 1) {
+            cudaMemsetAsync(bb.bvh.parent, 0xff, sizeof(int) * (nf - 1), s);
+            cudaMemsetAsync(bb.bvh.leafParent, 0xff, sizeof(int) * nf, s);   // single-leaf worlds keep -1
+            k_karras<<<gridn(nf - 1, 256), 256, 0, s>>>(bb.mkeys, nf, bb.bvh, bb.wstart, bb.wend, bb.wroot); note_launch();
+        }
+    }
+}
+
+// Refit of the current tree topology over the boxes in wq.amin / wq.amax into another node
+// record array (the broadphase's own records are left as they are).
+void broadphase_refit_into(const DevWorld& wq, const BroadphaseBuffers& bb, float4* node, int* visit, cudaStream_t s) {
+    const int nf = bb.nFinite;
+    if (nf < 2) return;
+    Bvh t = bb.bvh;
+    t.node = node;
+    t.visit = visit;
+    cudaMemsetAsync(visit, 0, sizeof(int) * (nf - 1), s);
+    k_refit<<<gridn(nf, 256), 256, 0, s>>>(wq, bb.sortedBody, nf, t); note_launch();
+}
+
 void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s) {
     int n = w.nBodies;
     if (bb.built && bb.sinceBuild + 1 < bb.rebuildInterval) {
@@ -335,25 +372,12 @@ void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t
         exclusive_scan(bb.cnt, bb.off, bb.total, n + 1, bb.scanScratch, s);
         return;
     }
-    bb.built = true;
-    bb.sinceBuild = 0;
-    cudaMemsetAsync(bb.bounds, 0, sizeof(unsigned) * 6, s);
-    cudaMemsetAsync(bb.bounds, 0xff, sizeof(unsigned) * 3, s);
-    k_bounds<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds); note_launch();
-    k_morton<<<gridn(n, 256), 256, 0, s>>>(w, bb.bounds, bb.mkeys, bb.sortedBody); note_launch();
-    radix_sort_pairs(bb.mkeys, bb.sortedBody, bb.mkeys_alt, bb.vals_alt, n, 32 + bb.worldBits, bb.sortScratch, s);
+    broadphase_build_tree(w, bb, s);
     int nf = bb.nFinite;
     cudaMemsetAsync(bb.cnt, 0, sizeof(int) * (n + 1), s);
     if (nf > 0) {
-        cudaMemsetAsync(bb.wstart, 0xff, sizeof(int) * bb.nWorlds, s);
-        cudaMemsetAsync(bb.wend, 0xff, sizeof(int) * bb.nWorlds, s);
-        cudaMemsetAsync(bb.wroot, 0xff, sizeof(int) * bb.nWorlds, s);
-        k_world_ranges<<<gridn(nf, 256), 256, 0, s>>>(bb.mkeys, nf, bb.wstart, bb.wend, bb.wroot); note_launch();
         if (nf > 1) {
             cudaMemsetAsync(bb.bvh.visit, 0, sizeof(int) * (nf - 1), s);
-            cudaMemsetAsync(bb.bvh.parent, 0xff, sizeof(int) * (nf - 1), s);
-            cudaMemsetAsync(bb.bvh.leafParent, 0xff, sizeof(int) * nf, s);   // single-leaf worlds keep -1
-            k_karras<<<gridn(nf - 1, 256), 256, 0, s>>>(bb.mkeys, nf, bb.bvh, bb.wstart, bb.wend, bb.wroot); note_launch();
             k_refit<<<gridn(nf, 256), 256, 0, s>>>(w, bb.sortedBody, nf, bb.bvh); note_launch();
             k_traverse<false><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, bb.cnt, nullptr,
                                                               nullptr, nullptr, 0, bb.tcount, bb.tcache); note_launch();

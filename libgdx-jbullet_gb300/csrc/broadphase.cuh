@@ -50,6 +50,8 @@ struct BroadphaseBuffers {
     int* tcache = nullptr;               // per sorted leaf: the first TRAV_CACHE partners' sorted leaves
 };
 
+void broadphase_build_tree(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s);
+void broadphase_refit_into(const DevWorld& wq, const BroadphaseBuffers& bb, float4* node, int* visit, cudaStream_t s);
 void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s);
 void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, int capacity, cudaStream_t s);
 void broadphase_persist(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, const DevPairs& old, int nNew, int nOld,

@@ -1,0 +1,475 @@
+// Scene queries: CollisionWorld.rayTest with a ClosestRayResultCallback for batches of rays
+// (collision/dispatch/CollisionWorld.java:553-591, rayTestSingle 260-331,
+// ClosestRayResultCallback 697-729).
+//
+// The reference walks every collision object in insertion order: the object's aabb against the
+// ray (AabbUtil2.rayAabb, accepting entries up to the closest hit so far), then a
+// SubsimplexConvexCast of a point along the ray (convex shapes) or the two triangles a
+// StaticPlaneShape spans around the ray (TriangleRaycastCallback); a hit is taken when its
+// fraction is below the closest so far.  Here one thread per ray walks the broadphase tree
+// (refit over the shapes' current aabbs) and evaluates every object whose aabb the ray enters
+// before its end.  An object's cast does not depend on the hits before it, so the walk keeps
+// the few smallest hits ordered by (fraction, body, triangle).  The smallest, j, is the
+// reference's answer unless an object before j in body order hit below j's aabb entry (then the
+// order-dependent aabb test may have skipped j): such rays, rare, are replayed in body order by
+// a block each.
+#include "../../include/jbgpu.h"
+#include "gjk.cuh"
+#include "prims.cuh"
+#include "query.cuh"
+#include "shapes.cuh"
+
+namespace jbg {
+using namespace jbd;
+
+constexpr int RAY_KEEP = 4;       // smallest hits kept per ray
+constexpr int RAY_STACK = 64;
+constexpr int RAY_THREADS = 128;
+constexpr int SLOW_THREADS = 256;
+
+static inline int gridn(int n, int b) { return (n + b - 1) / b; }
+
+__global__ void k_query_aabb(DevWorld w, float4* qmin, float4* qmax) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    V mn, mx;
+    shape_aabb(w.sh, w.shape[i], load_xf(w, i), mn, mx);
+    qmin[i] = f4(mn, 0.0f);
+    qmax[i] = f4(mx, 0.0f);
+}
+
+// AabbUtil2.outcode (linearmath/AabbUtil2.java:40-43)
+JBD int outcode(V p, V h) {
+    return (p.x < -h.x ? 0x01 : 0x0) | (p.x > h.x ? 0x08 : 0x0) | (p.y < -h.y ? 0x02 : 0x0) | (p.y > h.y ? 0x10 : 0x0) |
+           (p.z < -h.z ? 0x4 : 0x0) | (p.z > h.z ? 0x20 : 0x0);
+}
+
+// AabbUtil2.rayAabb (linearmath/AabbUtil2.java:45-104) split in two: the entry fraction and the
+// exit bound of the box's planes (Math.min from +infinity).  The reference's test with param p
+// passes iff the outcodes allow it and enter <= min(p, exit).
+JBD bool ray_aabb_parts(V from, V to, V mn, V mx, float& enter, float& exit) {
+    const V he = scl(sub(mx, mn), 0.5f);
+    const V c = scl(add(mx, mn), 0.5f);
+    const V source = sub(from, c), target = sub(to, c);
+    const int so = outcode(source, he), tc = outcode(target, he);
+    if ((so & tc) != 0) return false;
+    enter = 0.0f;
+    exit = __int_as_float(0x7f800000);
+    const V r = sub(target, source);
+    float normSign = 1.0f;
+    int bit = 1;
+    for (int j = 0; j < 2; j++) {
+        for (int i = 0; i != 3; ++i) {
+            if ((so & bit) != 0) {
+                const float lambda = jdiv(__fsub_rn(-coord(source, i), __fmul_rn(coord(he, i), normSign)), coord(r, i));
+                if (enter <= lambda) enter = lambda;
+            } else if ((tc & bit) != 0) {
+                const float lambda = jdiv(__fsub_rn(-coord(source, i), __fmul_rn(coord(he, i), normSign)), coord(r, i));
+                exit = jmin(exit, lambda);
+            }
+            bit <<= 1;
+        }
+        normSign = -1.0f;
+    }
+    return true;
+}
+
+// VectorUtil.setInterpolate3 (linearmath/VectorUtil.java:137-144)
+JBD V interp3(V a, V b, float rt) {
+    const float s = __fsub_rn(1.0f, rt);
+    return mk(__fadd_rn(__fmul_rn(s, a.x), __fmul_rn(rt, b.x)), __fadd_rn(__fmul_rn(s, a.y), __fmul_rn(rt, b.y)),
+              __fadd_rn(__fmul_rn(s, a.z), __fmul_rn(rt, b.z)));
+}
+
+JBD M identity3() {
+    M m;
+    m.r[0] = mk(1.0f, 0.0f, 0.0f);
+    m.r[1] = mk(0.0f, 1.0f, 0.0f);
+    m.r[2] = mk(0.0f, 0.0f, 1.0f);
+    return m;
+}
+
+// SubsimplexConvexCast.calcTimeOfImpact (collision/narrowphase/SubsimplexConvexCast.java:62-191)
+// as rayTestSingle runs it: A is a sphere of radius 0 (its support is its centre) moving from the
+// ray's start to its end with the identity basis, B the object's convex shape at rest.
+JBD bool subsimplex_ray(const ShapeRef& sb, const Xf& tB, V from, V to, float& fraction, V& normal) {
+    Simplex s;
+    sx_reset(s);
+    const V zero = mk(0.0f, 0.0f, 0.0f);
+    Xf iA;
+    iA.b = identity3();
+    iA.o = from;
+    const V linVelA = sub(to, from), linVelB = sub(tB.o, tB.o);
+    float lambda = 0.0f;
+    Xf iB = tB;
+    const V r = sub(linVelA, linVelB);
+    V supA = xf_apply(iA, zero);
+    V supB = xf_apply(tB, support_with_margin(sb, mulMTv(r, tB.b)));
+    V v = sub(supA, supB);
+    int maxIter = 32;
+    V n = zero;
+    float dist2 = len2(v);
+    while ((dist2 > 0.0001f) && (maxIter--) != 0) {
+        supA = xf_apply(iA, zero);
+        supB = xf_apply(iB, support_with_margin(sb, mulMTv(v, iB.b)));
+        V w = sub(supA, supB);
+        const float VdotW = dot(v, w);
+        if (lambda > 1.0f) return false;
+        if (VdotW > 0.0f) {
+            const float VdotR = dot(v, r);
+            if (VdotR >= -__fmul_rn(FLT_EPS, FLT_EPS)) return false;
+            lambda = __fsub_rn(lambda, jdiv(VdotW, VdotR));
+            iA.o = interp3(from, to, lambda);
+            iB.o = interp3(tB.o, tB.o, lambda);
+            w = sub(supA, supB);
+            n = v;
+        }
+        s.lastW = w;                                 // addVertex
+        s.needsUpdate = true;
+        s.W[s.nv] = w; s.P[s.nv] = supA; s.Q[s.nv] = supB;
+        s.nv++;
+        const bool ok = sx_update(s);                // closest(v)
+        v = s.cV;
+        dist2 = ok ? len2(v) : 0.0f;
+    }
+    fraction = lambda;
+    normal = len2(n) >= __fmul_rn(FLT_EPS, FLT_EPS) ? nor(n) : zero;
+    return !(dot(normal, r) >= -0.0f);   // no time of impact when moving away (allowedPenetration 0)
+}
+
+// TriangleRaycastCallback.processTriangle (collision/narrowphase/TriangleRaycastCallback.java:
+// 47-117) up to the report: the hit fraction and the local normal of a hit below `below`.
+JBD bool ray_triangle(V t0, V t1, V t2, V from, V to, float below, float& distance, V& normal) {
+    const V tn = crs(sub(t1, t0), sub(t2, t0));
+    const float dist = dot(t0, tn);
+    const float da = __fsub_rn(dot(tn, from), dist), db = __fsub_rn(dot(tn, to), dist);
+    if (__fmul_rn(da, db) >= 0.0f) return false;
+    distance = jdiv(da, __fsub_rn(da, db));
+    if (!(distance < below)) return false;
+    const float tol = __fmul_rn(len2(tn), -0.0001f);
+    const V p = interp3(from, to, distance);
+    const V v0p = sub(t0, p), v1p = sub(t1, p);
+    if (!(dot(crs(v0p, v1p), tn) >= tol)) return false;
+    const V v2p = sub(t2, p);
+    if (!(dot(crs(v1p, v2p), tn) >= tol)) return false;
+    if (!(dot(crs(v2p, v0p), tn) >= tol)) return false;
+    normal = da > 0.0f ? tn : scl(tn, -1.0f);
+    return true;
+}
+
+// One object's part of rayTest with every hit below 1 (the bound of any closest fraction):
+// rayTestSingle's convex branch (the normal rotated by the ray's identity basis and
+// normalised) or its concave branch for a StaticPlaneShape, whose processAllTriangles
+// (collision/shapes/StaticPlaneShape.java:60-120) spans two triangles around the ray's local
+// aabb, taking half of the aabb's minimum corner as the half extent as the port does
+// (halfExtents.set(aabbMax).set(aabbMin)).  Plane normals are the triangle normal times the
+// object's basis (ClosestRayResultCallback with normalInWorldSpace false), not unit length.
+struct ObjHits {
+    int n;
+    float f[2];
+    V nrm[2];
+};
+JBD void ray_object(const DevWorld& w, int b, V from, V to, ObjHits& h) {
+    h.n = 0;
+    const int shape = w.shape[b];
+    const Xf t = load_xf(w, b);
+    if (w.sh.type[shape] != SHAPE_PLANE) {
+        float f;
+        V n;
+        if (subsimplex_ray(shape_ref(w.sh, shape), t, from, to, f, n) && len2(n) > 0.0001f && f < 1.0f) {
+            h.f[0] = f;
+            h.nrm[0] = nor(mulMv(n, identity3()));
+            h.n = 1;
+        }
+        return;
+    }
+    const float4 pl = w.sh.plane[shape];
+    const V pn = mk(pl.x, pl.y, pl.z);
+    const Xf inv = xf_inverse(t);
+    const V lf = xf_apply(inv, from), lt = xf_apply(inv, to);
+    const V mn = mk(jmin(lf.x, lt.x), jmin(lf.y, lt.y), jmin(lf.z, lt.z));
+    const V mx = mk(jmax(lf.x, lt.x), jmax(lf.y, lt.y), jmax(lf.z, lt.z));
+    const float radius = len(scl(mn, 0.5f));
+    const V center = scl(add(mx, mn), 0.5f);
+    V d0, d1;
+    plane_space1(pn, d0, d1);
+    const V pc = sub(center, scl(pn, __fsub_rn(dot(pn, center), pl.w)));
+    const V a = scl(d0, radius), c = scl(d1, radius);
+    const V amc = sub(a, c);
+    float below = 1.0f;
+    float dist;
+    V nl;
+    if (ray_triangle(add(add(pc, a), c), add(pc, amc), sub(pc, amc), lf, lt, below, dist, nl)) {
+        h.f[h.n] = dist;
+        h.nrm[h.n] = mulMv(nl, t.b);
+        h.n++;
+        below = dist;
+    }
+    if (ray_triangle(sub(pc, amc), sub(pc, add(a, c)), add(add(pc, a), c), lf, lt, below, dist, nl)) {
+        h.f[h.n] = dist;
+        h.nrm[h.n] = mulMv(nl, t.b);
+        h.n++;
+    }
+}
+
+JBD bool passes_filter(const DevWorld& w, int b, int group, int mask) {   // RayResultCallback.needsCollision
+    return ((w.group[b] & mask) & 0xFFFF) != 0 && ((group & w.mask[b]) & 0xFFFF) != 0;
+}
+
+struct Hit {
+    float f;
+    int body, sub;
+    float enter;
+    V n;
+};
+JBD bool hit_before(float f, int body, int sub, const Hit& h) {
+    return f < h.f || (f == h.f && (body < h.body || (body == h.body && sub < h.sub)));
+}
+
+// Conservative slab test for the tree's inner boxes (inflated, so that no box the exact test
+// accepts is culled).
+JBD bool slab(V o, V d, float4 mn, float4 mx) {
+    float tn = -1e-3f, tf = 1.001f;
+    const float lo[3] = {mn.x, mn.y, mn.z}, hi[3] = {mx.x, mx.y, mx.z};
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    for (int k = 0; k < 3; k++) {
+        const float e = 1e-4f * (1.0f + fmaxf(fabsf(lo[k]), fabsf(hi[k])));
+        const float a = lo[k] - e, b = hi[k] + e;
+        if (dd[k] == 0.0f) {
+            if (oo[k] < a || oo[k] > b) return false;
+            continue;
+        }
+        const float inv = 1.0f / dd[k];
+        float t0 = (a - oo[k]) * inv, t1 = (b - oo[k]) * inv;
+        if (t0 > t1) { const float x = t0; t0 = t1; t1 = x; }
+        tn = fmaxf(tn, t0);
+        tf = fminf(tf, t1);
+        if (tn > tf) return false;
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(RAY_THREADS) k_rays(DevWorld w, DevWorld wq, const int* sortedBody, Bvh tree,
+                                                     const int* wroot, const int* planeList, const int* planeStart,
+                                                     const float* from, const float* to, const int* rayWorld, int n,
+                                                     int group, int mask, jbgpu_ray_hit* out, int* slow, int* slowCount,
+                                                     int replayAll) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    if (replayAll) {
+        slow[atomicAdd(slowCount, 1)] = r;
+        return;
+    }
+    const V f = mk(from[3 * r], from[3 * r + 1], from[3 * r + 2]);
+    const V t = mk(to[3 * r], to[3 * r + 1], to[3 * r + 2]);
+    const int wi = rayWorld ? rayWorld[r] : 0;
+    Hit keep[RAY_KEEP];
+    int nk = 0;
+    float dropMin = __int_as_float(0x7f800000);
+    auto consider = [&](int b) {
+        if (!passes_filter(w, b, group, mask)) return;
+        float enter, exit;
+        if (!ray_aabb_parts(f, t, mk4(wq.amin[b]), mk4(wq.amax[b]), enter, exit)) return;
+        if (!(enter <= jmin(1.0f, exit))) return;
+        ObjHits h;
+        ray_object(w, b, f, t, h);
+        for (int k = 0; k < h.n; k++) {
+            int pos = nk;
+            while (pos > 0 && hit_before(h.f[k], b, k, keep[pos - 1])) pos--;
+            if (pos >= RAY_KEEP) { dropMin = fminf(dropMin, h.f[k]); continue; }
+            if (nk == RAY_KEEP) dropMin = fminf(dropMin, keep[RAY_KEEP - 1].f);
+            for (int q = (nk < RAY_KEEP ? nk : RAY_KEEP - 1); q > pos; q--) keep[q] = keep[q - 1];
+            keep[pos].f = h.f[k];
+            keep[pos].body = b;
+            keep[pos].sub = k;
+            keep[pos].enter = enter;
+            keep[pos].n = h.nrm[k];
+            if (nk < RAY_KEEP) nk++;
+        }
+    };
+    const int root = wroot[wi];
+    if (root != -1) {
+        if (root & LEAF_FLAG) {
+            consider(sortedBody[root & ~LEAF_FLAG]);
+        } else {
+            const V d = sub(t, f);
+            int stack[RAY_STACK];
+            int sp = 0;
+            stack[sp++] = root;
+            while (sp > 0) {
+                const float4* nd = tree.node + 4 * stack[--sp];
+                const float4 rec[4] = {nd[0], nd[1], nd[2], nd[3]};
+                for (int c = 0; c < 2; c++) {
+                    if (!slab(f, d, rec[2 * c], rec[2 * c + 1])) continue;
+                    const int x = __float_as_int(rec[2 * c].w);
+                    if (x & LEAF_FLAG) consider(sortedBody[x & ~LEAF_FLAG]);
+                    else if (sp < RAY_STACK) stack[sp++] = x;
+                    else atomicOr(&w.ctr[C_STATUS], ST_CAPACITY);
+                }
+            }
+        }
+    }
+    for (int q = planeStart[wi]; q < planeStart[wi + 1]; q++) consider(planeList[q]);
+    jbgpu_ray_hit o;
+    o.body = -1;
+    o.fraction = 1.0f;
+    o.normal[0] = o.normal[1] = o.normal[2] = 0.0f;
+    o.point[0] = o.point[1] = o.point[2] = 0.0f;
+    if (nk > 0) {
+        const Hit& j = keep[0];
+        bool decided = !(dropMin < j.enter);
+        for (int q = 1; q < nk; q++)
+            if (keep[q].body < j.body && keep[q].f < j.enter) decided = false;
+        if (!decided) {
+            slow[atomicAdd(slowCount, 1)] = r;
+            return;
+        }
+        o.body = j.body;
+        o.fraction = j.f;
+        o.normal[0] = j.n.x; o.normal[1] = j.n.y; o.normal[2] = j.n.z;
+        const V p = interp3(f, t, j.f);
+        o.point[0] = p.x; o.point[1] = p.y; o.point[2] = p.z;
+    }
+    out[r] = o;
+}
+
+// The reference's loop for the undecided rays, a block per ray: every body of the ray's world in
+// index order, a chunk of SLOW_THREADS at a time evaluated in parallel (the aabb parts and the
+// object's hits do not depend on the closest fraction), then replayed by one thread with the
+// closest fraction and the break at zero.
+__global__ void __launch_bounds__(SLOW_THREADS) k_rays_slow(DevWorld w, DevWorld wq, const float* from, const float* to,
+                                                          const int* rayWorld, int group, int mask, jbgpu_ray_hit* out,
+                                                          const int* slow, const int* slowCount) {
+    __shared__ int sOk[SLOW_THREADS];
+    __shared__ float sEnter[SLOW_THREADS], sExit[SLOW_THREADS];
+    __shared__ ObjHits sHits[SLOW_THREADS];
+    __shared__ int sStop;
+    const int count = *slowCount;
+    for (int q = blockIdx.x; q < count; q += gridDim.x) {
+        const int r = slow[q];
+        const V f = mk(from[3 * r], from[3 * r + 1], from[3 * r + 2]);
+        const V t = mk(to[3 * r], to[3 * r + 1], to[3 * r + 2]);
+        const int wi = rayWorld ? rayWorld[r] : 0;
+        float closest = 1.0f;
+        int body = -1;
+        V normal = mk(0.0f, 0.0f, 0.0f);
+        if (threadIdx.x == 0) sStop = 0;
+        __syncthreads();
+        for (int base = 0; base < w.nBodies; base += SLOW_THREADS) {
+            const int b = base + threadIdx.x;
+            int ok = 0;
+            if (b < w.nBodies && w.world[b] == wi && passes_filter(w, b, group, mask)) {
+                float enter, exit;
+                if (ray_aabb_parts(f, t, mk4(wq.amin[b]), mk4(wq.amax[b]), enter, exit) && enter <= jmin(1.0f, exit)) {
+                    ok = 1;
+                    sEnter[threadIdx.x] = enter;
+                    sExit[threadIdx.x] = exit;
+                    ray_object(w, b, f, t, sHits[threadIdx.x]);
+                }
+            }
+            sOk[threadIdx.x] = ok;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (int k = 0; k < SLOW_THREADS && base + k < w.nBodies; k++) {
+                    if (closest == 0.0f) { sStop = 1; break; }
+                    if (!sOk[k] || !(sEnter[k] <= jmin(closest, sExit[k]))) continue;
+                    const ObjHits& h = sHits[k];
+                    for (int m = 0; m < h.n; m++)
+                        if (h.f[m] < closest) {
+                            closest = h.f[m];
+                            body = base + k;
+                            normal = h.nrm[m];
+                        }
+                }
+            }
+            __syncthreads();
+            if (sStop) break;
+        }
+        if (threadIdx.x == 0) {
+            jbgpu_ray_hit o;
+            o.body = body;
+            o.fraction = closest;
+            o.normal[0] = normal.x; o.normal[1] = normal.y; o.normal[2] = normal.z;
+            const V p = body >= 0 ? interp3(f, t, closest) : mk(0.0f, 0.0f, 0.0f);
+            o.point[0] = p.x; o.point[1] = p.y; o.point[2] = p.z;
+            out[r] = o;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+static int grow(T*& p, int& cap, int need) {
+    if (need <= cap) return JBGPU_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    const int c = need > 2 * cap ? need : 2 * cap;
+    if (cudaMalloc((void**)&p, sizeof(T) * (size_t)c) != cudaSuccess) { cap = 0; return JBGPU_ERR_CUDA; }
+    cap = c;
+    return JBGPU_OK;
+}
+
+int query_prepare(const DevWorld& w, BroadphaseBuffers& bb, QueryBuffers& qb, cudaStream_t s) {
+    if (w.nBodies > qb.capBodies) {
+        if (qb.qmin) cudaFree(qb.qmin);
+        if (qb.qmax) cudaFree(qb.qmax);
+        qb.qmin = qb.qmax = nullptr;
+        qb.capBodies = 0;
+        const int c = w.nBodies > 2 * qb.capBodies ? w.nBodies : 2 * qb.capBodies;
+        if (cudaMalloc((void**)&qb.qmin, sizeof(float4) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.qmax, sizeof(float4) * (size_t)c) != cudaSuccess)
+            return JBGPU_ERR_CUDA;
+        qb.capBodies = c;
+    }
+    if (w.nBodies == 0) return JBGPU_OK;
+    k_query_aabb<<<gridn(w.nBodies, 256), 256, 0, s>>>(w, qb.qmin, qb.qmax); note_launch();
+    DevWorld wq = w;
+    wq.amin = qb.qmin;
+    wq.amax = qb.qmax;
+    if (!bb.built) broadphase_build_tree(wq, bb, s);
+    const int nodes = bb.nFinite > 1 ? bb.nFinite - 1 : 1;
+    if (nodes > qb.capNodes) {
+        if (qb.node) cudaFree(qb.node);
+        if (qb.visit) cudaFree(qb.visit);
+        qb.node = nullptr;
+        qb.visit = nullptr;
+        const int c = nodes > 2 * qb.capNodes ? nodes : 2 * qb.capNodes;
+        qb.capNodes = 0;
+        if (cudaMalloc((void**)&qb.node, sizeof(float4) * 4 * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.visit, sizeof(int) * (size_t)c) != cudaSuccess)
+            return JBGPU_ERR_CUDA;
+        qb.capNodes = c;
+    }
+    broadphase_refit_into(wq, bb, qb.node, qb.visit, s);
+    return cudaGetLastError() == cudaSuccess ? JBGPU_OK : JBGPU_ERR_CUDA;
+}
+
+int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb, const float* from, const float* to,
+               const int* rayWorld, int n, int group, int mask, jbgpu_ray_hit* hits, int sms, cudaStream_t s) {
+    if (n <= 0) return JBGPU_OK;
+    int rc = grow(qb.slow, qb.capSlow, n);
+    if (rc) return rc;
+    if (!qb.slowCount && cudaMalloc((void**)&qb.slowCount, sizeof(int)) != cudaSuccess) return JBGPU_ERR_CUDA;
+    cudaMemsetAsync(qb.slowCount, 0, sizeof(int), s);
+    DevWorld wq = w;
+    wq.amin = qb.qmin;
+    wq.amax = qb.qmax;
+    Bvh tree = bb.bvh;
+    tree.node = qb.node;
+    k_rays<<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList, bb.planeStart,
+                                                          from, to, rayWorld, n, group, mask, hits, qb.slow, qb.slowCount,
+                                                          qb.replayAll);
+    note_launch();
+    k_rays_slow<<<sms, SLOW_THREADS, 0, s>>>(w, wq, from, to, rayWorld, group, mask, hits, qb.slow, qb.slowCount);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? JBGPU_OK : JBGPU_ERR_CUDA;
+}
+
+void query_free(QueryBuffers& qb) {
+    void* ps[] = {qb.qmin, qb.qmax, qb.node, qb.visit, qb.slow, qb.slowCount, qb.from, qb.to, qb.rayWorld, qb.hits};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    qb = QueryBuffers();
+}
+
+}  // namespace jbg

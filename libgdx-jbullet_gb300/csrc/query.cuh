@@ -1,0 +1,36 @@
+// Scene queries: CollisionWorld.rayTest with a ClosestRayResultCallback for batches of rays
+// (collision/dispatch/CollisionWorld.java:553-591, rayTestSingle 260-331).
+#pragma once
+#include "../../include/jbgpu.h"
+#include "broadphase.cuh"
+
+namespace jbg {
+
+struct QueryBuffers {
+    float4* qmin = nullptr;       // per body: CollisionShape.getAabb at the current transform
+    float4* qmax = nullptr;
+    int capBodies = 0;
+    float4* node = nullptr;       // the broadphase tree's topology refit over qmin / qmax
+    int* visit = nullptr;
+    int capNodes = 0;
+    int* slow = nullptr;          // rays the closest-hit shortcut cannot decide (replayed in body order)
+    int* slowCount = nullptr;
+    int capSlow = 0;
+    int replayAll = 0;            // verification: every ray takes the in-order replay
+    float* from = nullptr;        // staging for host buffers
+    float* to = nullptr;
+    int* rayWorld = nullptr;
+    jbgpu_ray_hit* hits = nullptr;
+    int capIo = 0;
+};
+
+// Query boxes for every body and the refit tree over them; builds the broadphase tree first
+// when the body set changed since its last build.
+int query_prepare(const DevWorld& w, BroadphaseBuffers& bb, QueryBuffers& qb, cudaStream_t s);
+// n rays (device buffers) against the prepared boxes; grows the replay list to n.  sms: blocks
+// of the replay kernel.
+int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb, const float* from, const float* to,
+               const int* rayWorld, int n, int group, int mask, jbgpu_ray_hit* hits, int sms, cudaStream_t s);
+void query_free(QueryBuffers& qb);
+
+}  // namespace jbg

@@ -19,6 +19,7 @@
 #include "mlp.cuh"
 #include "narrowphase.cuh"
 #include "prims.cuh"
+#include "query.cuh"
 #include "solver.cuh"
 
 using namespace jbg;
@@ -112,6 +113,7 @@ struct jbgpu_world {
     BroadphaseBuffers bb;
     NarrowBuffers nb;
     SolverBuffers sb;
+    QueryBuffers qb;                  // ray queries
     int* hostPinned = nullptr;
     Prof prof;
     int* profHist = nullptr;      // per profiled step: device counters + solver manifolds
@@ -762,6 +764,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     cudaSetDevice(w->device);
     if (w->stream) cudaStreamSynchronize(w->stream);
     if (w->aux) cudaStreamSynchronize(w->aux);
+    query_free(w->qb);
     DevWorld& d = w->dw;
     dfree(d.xr0); dfree(d.xr1); dfree(d.xr2); dfree(d.linvel); dfree(d.angvel); dfree(d.iw0); dfree(d.iw1); dfree(d.iw2);
     dfree(d.iloc); dfree(d.force); dfree(d.torque); dfree(d.gravity); dfree(d.amin); dfree(d.amax); dfree(d.act);
@@ -1204,6 +1207,70 @@ int jbgpu_world_timer(jbgpu_world* w, int32_t mark, double* ms) {
     return JBGPU_OK;
 }
 
+int jbgpu_world_ray_test(jbgpu_world* w, const float* from, const float* to, const int32_t* rayWorld, int32_t n,
+                         int32_t group, int32_t mask, int32_t deviceBuffers, jbgpu_ray_hit* hits) {
+    if (!w || n < 0 || (n > 0 && (!from || !to || !hits))) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad ray arguments");
+    if (n == 0) return JBGPU_OK;
+    CK(cudaSetDevice(w->device));
+    int rc = prepare(w);
+    if (rc) return rc;
+    cudaStream_t s = w->stream;
+    if (!deviceBuffers && rayWorld)
+        for (int i = 0; i < n; i++)
+            if (rayWorld[i] < 0 || rayWorld[i] >= w->nWorlds) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad ray world");
+    if (w->nBodies == 0) {
+        jbgpu_ray_hit miss;
+        std::memset(&miss, 0, sizeof(miss));
+        miss.body = -1;
+        miss.fraction = 1.0f;
+        if (deviceBuffers) {
+            std::vector<jbgpu_ray_hit> m(n, miss);
+            CK(cudaMemcpyAsync(hits, m.data(), sizeof(jbgpu_ray_hit) * n, cudaMemcpyHostToDevice, s));
+            CK(cudaStreamSynchronize(s));
+        } else {
+            std::fill(hits, hits + n, miss);
+        }
+        return JBGPU_OK;
+    }
+    DevWorld d = dev_view(w);
+    QueryBuffers& Q = w->qb;
+    rc = query_prepare(d, w->bb, Q, s);
+    if (rc) return fail(rc, "ray query preparation failed");
+    const float* df = from;
+    const float* dt = to;
+    const int* dw = rayWorld;
+    jbgpu_ray_hit* dh = hits;
+    if (!deviceBuffers) {
+        if (n > Q.capIo) {
+            dfree(Q.from); dfree(Q.to); dfree(Q.rayWorld); dfree(Q.hits);
+            const int c = std::max(n, 2 * Q.capIo);
+            Q.capIo = 0;
+            CK(dalloc(&Q.from, 3 * (size_t)c)); CK(dalloc(&Q.to, 3 * (size_t)c)); CK(dalloc(&Q.rayWorld, c)); CK(dalloc(&Q.hits, c));
+            Q.capIo = c;
+        }
+        CK(cudaMemcpyAsync(Q.from, from, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(Q.to, to, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
+        if (rayWorld) CK(cudaMemcpyAsync(Q.rayWorld, rayWorld, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+        df = Q.from;
+        dt = Q.to;
+        dw = rayWorld ? Q.rayWorld : nullptr;
+        dh = Q.hits;
+    }
+    rc = query_rays(d, w->bb, Q, df, dt, dw, n, group, mask, dh, w->sms, s);
+    if (rc) return fail(rc, "ray query failed");
+    if (!deviceBuffers) {
+        CK(cudaMemcpyAsync(hits, Q.hits, sizeof(jbgpu_ray_hit) * n, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+    }
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_ray_replay(jbgpu_world* w, int32_t all) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    w->qb.replayAll = all != 0;
+    return JBGPU_OK;
+}
+
 int jbgpu_world_synchronize(jbgpu_world* w) {
     if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
     CK(cudaStreamSynchronize(w->stream));
@@ -1476,6 +1543,9 @@ int jbgpu_world_counters(jbgpu_world* w, jbgpu_counters* c) {
     c->solver_islands = h[C_ISL_N];
     c->solver_islands_converged = h[C_ISL_CONV];
     c->solver_island_iterations = h[C_ISL_ITERS];
+    if (w->qb.slowCount) {
+        CK(cudaMemcpy(&c->ray_replays, w->qb.slowCount, sizeof(int), cudaMemcpyDeviceToHost));
+    }
     return JBGPU_OK;
 }
 

@@ -157,6 +157,19 @@ class Manifolds(C.Structure):
     ]
 
 
+class RayHit(C.Structure):
+    _fields_ = [
+        ("body", C.c_int32),
+        ("fraction", C.c_float),
+        ("normal", C.c_float * 3),
+        ("point", C.c_float * 3),
+    ]
+
+
+RAY_HIT_DTYPE = np.dtype([("body", np.int32), ("fraction", np.float32), ("normal", np.float32, 3),
+                          ("point", np.float32, 3)])
+
+
 class Counters(C.Structure):
     _fields_ = [
         ("steps", C.c_int64),
@@ -177,6 +190,7 @@ class Counters(C.Structure):
         ("solver_islands", C.c_int32),
         ("solver_islands_converged", C.c_int32),
         ("solver_island_iterations", C.c_int32),
+        ("ray_replays", C.c_int32),
     ]
 
     def as_dict(self):

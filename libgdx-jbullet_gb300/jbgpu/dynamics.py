@@ -330,6 +330,23 @@ class HingeConstraint:
         return float(self._world._g.joint_impulses()[self._id])
 
 
+class ClosestRayResultCallback:
+    """CollisionWorld.ClosestRayResultCallback (collision/dispatch/CollisionWorld.java:697-729)."""
+
+    def __init__(self, rayFromWorld, rayToWorld):
+        self.rayFromWorld = np.asarray(rayFromWorld, np.float32).reshape(3).copy()
+        self.rayToWorld = np.asarray(rayToWorld, np.float32).reshape(3).copy()
+        self.closestHitFraction = 1.0
+        self.collisionObject = None
+        self.collisionFilterGroup = 1      # CollisionFilterGroups.DEFAULT_FILTER
+        self.collisionFilterMask = -1      # CollisionFilterGroups.ALL_FILTER
+        self.hitNormalWorld = np.zeros(3, np.float32)
+        self.hitPointWorld = np.zeros(3, np.float32)
+
+    def hasHit(self):
+        return self.collisionObject is not None
+
+
 class DiscreteDynamicsWorld:
     def __init__(self, dispatcher=None, pairCache=None, constraintSolver=None, collisionConfiguration=None, device=0):
         self._gravity = (0.0, -10.0, 0.0)
@@ -467,6 +484,19 @@ class DiscreteDynamicsWorld:
         n = g.step_simulation(timeStep, maxSubSteps, fixedTimeStep)
         self._cache = None
         return n
+
+    # -- queries --
+    def rayTest(self, rayFromWorld, rayToWorld, resultCallback):
+        """CollisionWorld.rayTest (collision/dispatch/CollisionWorld.java:553-591) with a
+        ClosestRayResultCallback, on the GPU world's bodies as the last step left them."""
+        cb = resultCallback
+        h = self._ensure().ray_test([rayFromWorld], [rayToWorld], group=cb.collisionFilterGroup,
+                                    mask=cb.collisionFilterMask)[0]
+        if h["body"] >= 0:
+            cb.closestHitFraction = float(h["fraction"])
+            cb.collisionObject = self._bodies[int(h["body"])]
+            cb.hitNormalWorld = h["normal"].copy()
+            cb.hitPointWorld = h["point"].copy()
 
     # -- state access --
     _cache = None

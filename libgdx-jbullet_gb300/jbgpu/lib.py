@@ -60,6 +60,9 @@ def lib():
                                              C.POINTER(C.c_int32)], C.c_int),
             "jbgpu_world_set_joint_setting": ([C.c_void_p, C.c_int32, C.c_float, C.c_float, C.c_float], C.c_int),
             "jbgpu_world_get_joint_impulses": ([C.c_void_p, _abi.f32p, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
+            "jbgpu_world_ray_test": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                      C.c_int32, C.c_void_p], C.c_int),
+            "jbgpu_world_set_ray_replay": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_add_hinge": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.POINTER(C.c_int32)],
                                       C.c_int),
             "jbgpu_world_set_hinge_limit": ([C.c_void_p, C.c_int32] + [C.c_float] * 5, C.c_int),
@@ -98,7 +101,8 @@ EXPORTED = [
     "jbgpu_world_apply_forces", "jbgpu_world_get_transforms", "jbgpu_world_set_profiling", "jbgpu_world_phase_times",
     "jbgpu_world_profile_counters", "jbgpu_world_timer", "jbgpu_world_add_point2point", "jbgpu_world_set_joint_setting",
     "jbgpu_world_get_joint_impulses", "jbgpu_world_add_hinge", "jbgpu_world_set_hinge_limit",
-    "jbgpu_world_enable_hinge_motor", "jbgpu_world_set_hinge_angular_only",
+    "jbgpu_world_enable_hinge_motor", "jbgpu_world_set_hinge_angular_only", "jbgpu_world_ray_test",
+    "jbgpu_world_set_ray_replay",
 ]
 
 
@@ -243,6 +247,29 @@ class GpuWorld:
 
     def set_hinge_angular_only(self, jid, on):
         check(lib().jbgpu_world_set_hinge_angular_only(self.h, jid, 1 if on else 0))
+
+    def ray_test(self, ray_from, ray_to, world=None, group=1, mask=-1):
+        """CollisionWorld.rayTest with a ClosestRayResultCallback per ray: ray_from / ray_to (n, 3),
+        world (n,) batch world per ray or None.  Returns a RAY_HIT_DTYPE array (body -1: no hit)."""
+        f = np.ascontiguousarray(ray_from, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(ray_to, np.float32).reshape(-1, 3)
+        n = len(f)
+        if len(t) != n:
+            raise ValueError("ray_from and ray_to differ in length")
+        out = np.zeros(n, _abi.RAY_HIT_DTYPE)
+        wp = None
+        if world is not None:
+            wa = np.ascontiguousarray(world, np.int32).reshape(n)
+            wp = wa.ctypes.data
+        check(lib().jbgpu_world_ray_test(self.h, f.ctypes.data, t.ctypes.data, wp, n, group, mask, 0, out.ctypes.data))
+        return out
+
+    def ray_test_device(self, from_ptr, to_ptr, n, hits_ptr, world_ptr=None, group=1, mask=-1):
+        """rayTest on device buffers (raw pointers); queued on the world's stream."""
+        check(lib().jbgpu_world_ray_test(self.h, from_ptr, to_ptr, world_ptr, n, group, mask, 1, hits_ptr))
+
+    def set_ray_replay(self, all_rays):
+        check(lib().jbgpu_world_set_ray_replay(self.h, 1 if all_rays else 0))
 
     def add_scene_joints(self, scene):
         for j in scene.meta.get("joints", []):

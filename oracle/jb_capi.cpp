@@ -146,6 +146,19 @@ void orc_enable_hinge_motor(void* h, int id, int enable, float target, float max
     j.maxMotorImpulse = maxImpulse;
 }
 void orc_set_hinge_angular_only(void* h, int id, int on) { ((World*)h)->joints[id].angularOnly = on != 0; }
+// CollisionWorld.rayTest with a ClosestRayResultCallback per ray; out: jbgpu_ray_hit records.
+void orc_ray_test(void* h, const float* from, const float* to, const int* world, int n, int group, int mask,
+                  jbgpu_ray_hit* out) {
+    const World& w = *(const World*)h;
+    for (int i = 0; i < n; i++) {
+        RayResult r = ray_test(w, v3(from[3 * i], from[3 * i + 1], from[3 * i + 2]), v3(to[3 * i], to[3 * i + 1], to[3 * i + 2]),
+                               group, mask, world ? world[i] : 0);
+        out[i].body = r.body;
+        out[i].fraction = r.fraction;
+        out[i].normal[0] = r.normal.x; out[i].normal[1] = r.normal.y; out[i].normal[2] = r.normal.z;
+        out[i].point[0] = r.point.x; out[i].point[1] = r.point.y; out[i].point[2] = r.point.z;
+    }
+}
 int orc_get_joint_impulses(void* h, float* out, int cap) {
     const World* w = (const World*)h;
     const int n = (int)w->joints.size();

@@ -931,4 +931,190 @@ void process_pair(World& w, int pi) {
     }
 }
 
+
+// ----------------------------------------------------------------------------------------
+// CollisionWorld.rayTest with a ClosestRayResultCallback (collision/dispatch/CollisionWorld.java:
+// 553-591 and rayTestSingle 260-331, ClosestRayResultCallback 697-729)
+// ----------------------------------------------------------------------------------------
+// AabbUtil2.outcode (linearmath/AabbUtil2.java:40-43)
+static int outcode(V3 p, V3 h) {
+    return (p.x < -h.x ? 0x01 : 0x0) | (p.x > h.x ? 0x08 : 0x0) | (p.y < -h.y ? 0x02 : 0x0) | (p.y > h.y ? 0x10 : 0x0) |
+           (p.z < -h.z ? 0x4 : 0x0) | (p.z > h.z ? 0x20 : 0x0);
+}
+
+// AabbUtil2.rayAabb (linearmath/AabbUtil2.java:45-104): param in = the largest fraction
+// accepted, out = the entry fraction.
+static bool ray_aabb(V3 from, V3 to, V3 mn, V3 mx, float& param) {
+    V3 he = scl(sub(mx, mn), 0.5f);
+    V3 c = scl(add(mx, mn), 0.5f);
+    V3 source = sub(from, c), target = sub(to, c);
+    int so = outcode(source, he), to_ = outcode(target, he);
+    if ((so & to_) != 0) return false;
+    float enter = 0.0f, exit = param;
+    V3 r = sub(target, source);
+    float normSign = 1.0f;
+    int bit = 1;
+    for (int j = 0; j < 2; j++) {
+        for (int i = 0; i != 3; ++i) {
+            if ((so & bit) != 0) {
+                float lambda = (-coord(source, i) - coord(he, i) * normSign) / coord(r, i);
+                if (enter <= lambda) enter = lambda;
+            } else if ((to_ & bit) != 0) {
+                float lambda = (-coord(source, i) - coord(he, i) * normSign) / coord(r, i);
+                exit = jmin(exit, lambda);
+            }
+            bit <<= 1;
+        }
+        normSign = -1.0f;
+    }
+    if (enter <= exit) { param = enter; return true; }
+    return false;
+}
+
+// VectorUtil.setInterpolate3 (linearmath/VectorUtil.java:137-144)
+static V3 interp3(V3 a, V3 b, float rt) {
+    float s = 1.0f - rt;
+    return v3(s * a.x + rt * b.x, s * a.y + rt * b.y, s * a.z + rt * b.z);
+}
+
+// SubsimplexConvexCast.calcTimeOfImpact (collision/narrowphase/SubsimplexConvexCast.java:62-191)
+// for rayTestSingle's cast: A is a sphere of radius 0 (support: its centre) moving from the ray's
+// start to its end with the identity basis, B the object's convex shape at rest.
+static bool subsimplex_ray(const Shape& sb, const Xf& tB, V3 from, V3 to, float& fraction, V3& normal) {
+    VoronoiSimplex s;
+    s.reset();
+    const V3 zero = v3(0.0f, 0.0f, 0.0f);
+    Xf fromA = xf_identity(), toA = xf_identity();
+    fromA.o = from;
+    toA.o = to;
+    V3 linVelA = sub(toA.o, fromA.o), linVelB = sub(tB.o, tB.o);
+    float lambda = 0.0f;
+    Xf iA = fromA, iB = tB;
+    V3 r = sub(linVelA, linVelB);
+    V3 supA = xf_apply(fromA, zero);
+    V3 supB = xf_apply(tB, support_with_margin(sb, mulMTv(r, tB.b)));
+    V3 v = sub(supA, supB);
+    int maxIter = 32;
+    V3 n = zero;
+    float dist2 = len2(v);
+    const float epsilon = 0.0001f;
+    while ((dist2 > epsilon) && (maxIter--) != 0) {
+        supA = xf_apply(iA, zero);
+        supB = xf_apply(iB, support_with_margin(sb, mulMTv(v, iB.b)));
+        V3 w = sub(supA, supB);
+        float VdotW = dot(v, w);
+        if (lambda > 1.0f) return false;
+        if (VdotW > 0.0f) {
+            float VdotR = dot(v, r);
+            if (VdotR >= -(FLT_EPS * FLT_EPS)) return false;
+            lambda = lambda - VdotW / VdotR;
+            iA.o = interp3(fromA.o, toA.o, lambda);
+            iB.o = interp3(tB.o, tB.o, lambda);
+            w = sub(supA, supB);
+            n = v;
+        }
+        s.addVertex(w, supA, supB);
+        if (s.closest(v)) dist2 = len2(v);
+        else dist2 = 0.0f;
+    }
+    fraction = lambda;
+    normal = len2(n) >= FLT_EPS * FLT_EPS ? nor(n) : zero;
+    if (dot(normal, r) >= -0.0f) return false;   // -allowedPenetration (0)
+    return true;
+}
+
+namespace {
+struct RayCallback {          // ClosestRayResultCallback
+    float closest = 1.0f;
+    int body = -1;
+    V3 normal{0, 0, 0};
+};
+}  // namespace
+
+// TriangleRaycastCallback.processTriangle (collision/narrowphase/TriangleRaycastCallback.java:
+// 47-117) with BridgeTriangleRaycastCallback.reportHit (CollisionWorld.java:820-829).
+static void ray_triangle(const V3 tri[3], V3 from, V3 to, float& hitFraction, int body, const Xf& objXf, RayCallback& cb) {
+    V3 v10 = sub(tri[1], tri[0]), v20 = sub(tri[2], tri[0]);
+    V3 tn = crs(v10, v20);
+    float dist = dot(tri[0], tn);
+    float dist_a = dot(tn, from) - dist;
+    float dist_b = dot(tn, to) - dist;
+    if (dist_a * dist_b >= 0.0f) return;
+    float proj = dist_a - dist_b;
+    float distance = dist_a / proj;
+    if (!(distance < hitFraction)) return;
+    float tol = len2(tn) * -0.0001f;
+    V3 point = interp3(from, to, distance);
+    V3 v0p = sub(tri[0], point), v1p = sub(tri[1], point);
+    if (!(dot(crs(v0p, v1p), tn) >= tol)) return;
+    V3 v2p = sub(tri[2], point);
+    if (!(dot(crs(v1p, v2p), tn) >= tol)) return;
+    if (!(dot(crs(v2p, v0p), tn) >= tol)) return;
+    V3 nl = dist_a > 0.0f ? tn : scl(tn, -1.0f);
+    cb.closest = distance;                        // ClosestRayResultCallback.addSingleResult
+    cb.body = body;
+    cb.normal = mulMv(nl, objXf.b);               // normal not in world space: times the basis
+    hitFraction = distance;
+}
+
+// rayTestSingle's concave branch for a StaticPlaneShape: the ray in the object's space and
+// StaticPlaneShape.processAllTriangles (collision/shapes/StaticPlaneShape.java:60-120), which
+// spans two triangles around the ray's local aabb; the port takes half of the aabb's minimum
+// corner as the half extent (halfExtents.set(aabbMax).set(aabbMin)).
+static void ray_plane(const Shape& sh, const Xf& t, int body, V3 fromW, V3 toW, RayCallback& cb) {
+    Xf inv = xf_inverse(t);
+    V3 from = xf_apply(inv, fromW), to = xf_apply(inv, toW);
+    float hitFraction = cb.closest;
+    V3 mn = v3(jmin(from.x, to.x), jmin(from.y, to.y), jmin(from.z, to.z));
+    V3 mx = v3(jmax(from.x, to.x), jmax(from.y, to.y), jmax(from.z, to.z));
+    V3 half = scl(mn, 0.5f);
+    float radius = len(half);
+    V3 center = scl(add(mx, mn), 0.5f);
+    V3 t0, t1;
+    plane_space1(sh.planeNormal, t0, t1);
+    V3 pc = sub(center, scl(sh.planeNormal, dot(sh.planeNormal, center) - sh.planeConstant));
+    V3 a = scl(t0, radius), b = scl(t1, radius);
+    V3 tri[3];
+    tri[0] = add(add(pc, a), b);
+    tri[1] = add(pc, sub(a, b));
+    tri[2] = sub(pc, sub(a, b));
+    ray_triangle(tri, from, to, hitFraction, body, t, cb);
+    tri[0] = sub(pc, sub(a, b));
+    tri[1] = sub(pc, add(a, b));
+    tri[2] = add(add(pc, a), b);
+    ray_triangle(tri, from, to, hitFraction, body, t, cb);
+}
+
+RayResult ray_test(const World& w, V3 from, V3 to, int group, int mask, int world) {
+    RayCallback cb;
+    for (size_t i = 0; i < w.bodies.size(); i++) {
+        if (cb.closest == 0.0f) break;
+        const Body& b = w.bodies[i];
+        if (b.world != world) continue;
+        if (((b.group & mask) & 0xFFFF) == 0 || ((group & b.mask) & 0xFFFF) == 0) continue;   // needsCollision
+        const Shape& sh = w.shapes[b.shape];
+        V3 mn, mx;
+        shape_aabb(sh, b.xf, mn, mx);
+        float param = cb.closest;
+        if (!ray_aabb(from, to, mn, mx, param)) continue;
+        if (sh.isConvex()) {
+            float f;
+            V3 n;
+            if (subsimplex_ray(sh, b.xf, from, to, f, n) && len2(n) > 0.0001f && f < cb.closest) {
+                cb.closest = f;
+                cb.body = (int)i;
+                cb.normal = nor(mulMv(n, m3_identity()));   // rotated by the ray's (identity) basis
+            }
+        } else {
+            ray_plane(sh, b.xf, (int)i, from, to, cb);
+        }
+    }
+    RayResult r;
+    r.body = cb.body;
+    r.fraction = cb.closest;
+    r.normal = cb.normal;
+    r.point = cb.body >= 0 ? interp3(from, to, cb.closest) : v3(0.0f, 0.0f, 0.0f);
+    return r;
+}
+
 }  // namespace jb

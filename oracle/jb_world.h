@@ -167,6 +167,10 @@ std::vector<int> joint_colour_order(const World& w);
 void stage_apply_gravity(World& w);
 void stage_predict(World& w, float dt);
 void stage_aabbs(World& w);
+// CollisionWorld.rayTest(from, to, ClosestRayResultCallback) over the bodies of one batch world,
+// with the callback's collisionFilterGroup / collisionFilterMask.
+struct RayResult { int body = -1; float fraction = 1.0f; V3 normal{0, 0, 0}, point{0, 0, 0}; };
+RayResult ray_test(const World& w, V3 from, V3 to, int group, int mask, int world);
 void stage_pairs(World& w);
 void stage_narrowphase(World& w);
 void stage_islands(World& w);

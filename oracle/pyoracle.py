@@ -53,6 +53,7 @@ def lib():
         L.orc_add_point2point.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
         L.orc_set_joint_setting.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float]
         L.orc_get_joint_impulses.argtypes = [C.c_void_p, _abi.f32p, C.c_int]
+        L.orc_ray_test.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
         L.orc_add_hinge.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
         L.orc_set_hinge_limit.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 5
         L.orc_enable_hinge_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float]
@@ -101,6 +102,16 @@ class OracleWorld:
         out = np.zeros(max(n, 1), np.float32)
         lib().orc_get_joint_impulses(self.h, _fp(out), n)
         return out[:n].copy()
+
+    def ray_test(self, ray_from, ray_to, world=None, group=1, mask=-1):
+        """CollisionWorld.rayTest with a ClosestRayResultCallback per ray (RAY_HIT_DTYPE records)."""
+        f = np.ascontiguousarray(ray_from, np.float32).reshape(-1, 3)
+        t = np.ascontiguousarray(ray_to, np.float32).reshape(-1, 3)
+        out = np.zeros(len(f), _abi.RAY_HIT_DTYPE)
+        wa = None if world is None else np.ascontiguousarray(world, np.int32).reshape(len(f))
+        lib().orc_ray_test(self.h, f.ctypes.data, t.ctypes.data, None if wa is None else wa.ctypes.data, len(f), group,
+                           mask, out.ctypes.data)
+        return out
 
     def add_hinge(self, a, b, frame_a, frame_b):
         """HingeConstraint between bodies a and b (b = -1: the fixed body) with the constraint

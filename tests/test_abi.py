@@ -35,15 +35,17 @@ def test_library_exports_every_declared_symbol(gpu_lib):
 def test_struct_sizes_match_header(tmp_path):
     # sizes as the C compiler lays the header's structs out, against the ctypes mirror
     src = tmp_path / "sz.c"
-    src.write_text('#include <stdio.h>\n#include "jbgpu.h"\nint main(void){printf("%zu %zu %zu %zu %zu %zu\\n",'
+    src.write_text('#include <stdio.h>\n#include "jbgpu.h"\nint main(void){printf("%zu %zu %zu %zu %zu %zu %zu\\n",'
                    'sizeof(jbgpu_config),sizeof(jbgpu_shape_desc),sizeof(jbgpu_body_desc),sizeof(jbgpu_state),'
-                   'sizeof(jbgpu_manifolds),sizeof(jbgpu_counters));return 0;}\n')
+                   'sizeof(jbgpu_manifolds),sizeof(jbgpu_counters),sizeof(jbgpu_ray_hit));return 0;}\n')
     exe = tmp_path / "sz"
     import subprocess
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
     sizes = [int(x) for x in subprocess.check_output([str(exe)]).split()]
-    mirror = [C.sizeof(t) for t in (_abi.Config, _abi.ShapeDesc, _abi.BodyDesc, _abi.State, _abi.Manifolds, _abi.Counters)]
+    mirror = [C.sizeof(t) for t in (_abi.Config, _abi.ShapeDesc, _abi.BodyDesc, _abi.State, _abi.Manifolds, _abi.Counters,
+                                    _abi.RayHit)]
     assert sizes == mirror
+    assert C.sizeof(_abi.RayHit) == _abi.RAY_HIT_DTYPE.itemsize
     assert C.sizeof(_abi.BodyDesc) == scenes.BODY_DTYPE.itemsize
 
 
