@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--rebuild-interval", type=int, default=None, help="jbgpu_config.broadphase_rebuild_interval")
     p.add_argument("--ref-seconds", type=float, default=120.0, help="time budget of the reference arm's timed steps")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start comparison")
+    p.add_argument("--no-rays", action="store_true", help="skip the rayTest batch measurement")
+    p.add_argument("--rays", type=int, default=1 << 20, help="rays per rayTest batch")
     return p.parse_args()
 
 
@@ -225,6 +227,59 @@ def run_cpu_baseline(scene, world_cls, snap_steps, window):
                           window, sorted(set(snap_steps)), scene.name, total_t)}
 
 
+def measure_rays(w, scene, nrays, seed, local):
+    """CollisionWorld.rayTest batches on the world as the timed steps left it: nrays rays per
+    batch from device buffers (half straight down from above the bodies, half between random
+    points of their bounding region), CUDA events on the world's stream around 5 batches after 2
+    untimed ones; a 1,024-ray sample compared with the oracle bit for bit and timed on 1 core."""
+    import torch
+    from jbgpu import _abi
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    st = w.get_state()
+    pos = st["transform"][:, 9:]
+    fin = np.all(np.abs(pos) < 1e6, axis=1)
+    lo, hi = pos[fin].min(0), pos[fin].max(0)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = rng.uniform(lo, hi, (nrays, 3)).astype(np.float32)
+    b = rng.uniform(lo, hi, (nrays, 3)).astype(np.float32)
+    h = nrays // 2
+    a[:h, 1] = hi[1] + 5.0
+    b[:h] = a[:h]
+    b[:h, 1] = lo[1] - 2.0
+    dev = "cuda:%d" % local
+    df, dt = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+    dh = torch.empty(nrays * _abi.RAY_HIT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    for _ in range(2):
+        w.ray_test_device(df.data_ptr(), dt.data_ptr(), nrays, dh.data_ptr())
+    w.synchronize()
+    reps = 5
+    w.timer_start()
+    for _ in range(reps):
+        w.ray_test_device(df.data_ptr(), dt.data_ptr(), nrays, dh.data_ptr())
+    ms = w.timer_stop() / reps
+    replays = w.counters()["ray_replays"]
+    hits = dh.cpu().numpy().view(_abi.RAY_HIT_DTYPE)
+    t0 = time.perf_counter()
+    hh = w.ray_test(a, b)
+    host_ms = (time.perf_counter() - t0) * 1e3
+    o = pyoracle.OracleWorld(scene)
+    o.set_state({"transform": st["transform"]})
+    k = 1024
+    t0 = time.perf_counter()
+    ho = o.ray_test(a[:k], b[:k])
+    cpu_s = time.perf_counter() - t0
+    same = bool(np.array_equal(ho.view(np.uint8), hits[:k].view(np.uint8)) and
+                np.array_equal(hh.view(np.uint8), hits.view(np.uint8)))
+    return {"rays_per_batch": nrays, "ms_per_batch": ms, "rays_per_s": nrays / (ms * 1e-3),
+            "hit_fraction": float(np.mean(hits["body"] >= 0)), "replayed_rays": int(replays),
+            "host_buffers_ms_per_batch": host_ms,
+            "cpu_oracle_rays_per_s": k / cpu_s, "cpu_sample": "%d rays of the batch, oracle (the reference's object "
+                                                                 "loop restated), 1 thread" % k,
+            "bit_exact_vs_oracle_sample": same,
+            "clock": "CUDA events on the world's stream around 5 batches of device buffers"}
+
+
 def run_ours(args, dist):
     from jbgpu import _abi, _build, lib
     from jbgpu.lib import GpuWorld
@@ -265,6 +320,9 @@ def run_ours(args, dist):
     dist.barrier()
     clocks = clk.stop()
     final = w.counters()
+    rays = None
+    if dist.rank == 0 and not args.no_rays:
+        rays = measure_rays(w, sc, args.rays, args.seed + 20, dist.local)
     w.close()
     wall = t1 - t0
     elapsed = dist.max(device_ms * 1e-3)
@@ -363,6 +421,7 @@ def run_ours(args, dist):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "learned_warmstart": learned,
+        "ray_test": rays,
         "clocks": clocks,
         "status_flags": final["status_flags"],
         "autotune": tuned,
