@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--ref-seconds", type=float, default=120.0, help="time budget of the reference arm's timed steps")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start comparison")
     p.add_argument("--no-rays", action="store_true", help="skip the rayTest batch measurement")
+    p.add_argument("--graph", type=int, default=1, help="1: replay the step as CUDA graphs (jbgpu_world_set_graph), 0: launches")
     p.add_argument("--rays", type=int, default=1 << 20, help="rays per rayTest batch")
     return p.parse_args()
 
@@ -303,6 +304,8 @@ def run_ours(args, dist):
     K, W = args.steps, args.warmup
     # ---- device-timed run: CUDA events on the world's stream around K steps ----------------
     w = GpuWorld(sc, config=cfg)
+    if args.graph:
+        w.set_graph(True)
     for _ in range(W):
         w.step(sc.dt)
     clk = ClockSampler(dist.local)
@@ -320,6 +323,10 @@ def run_ours(args, dist):
     dist.barrier()
     clocks = clk.stop()
     final = w.counters()
+    graph_info = None
+    if args.graph:
+        ng, gerr = w.graph_status()
+        graph_info = {"graphs_held": ng, "capture_error": gerr or None}
     rays = None
     if dist.rank == 0 and not args.no_rays:
         rays = measure_rays(w, sc, args.rays, args.seed + 20, dist.local)
@@ -366,6 +373,8 @@ def run_ours(args, dist):
     e2e = None
     if not args.no_e2e:
         w = GpuWorld(sc, config=cfg)
+        if args.graph:
+            w.set_graph(True)
         force = pinned((n, 3))
         xout = pinned((n, 12))
         for _ in range(W):
@@ -422,6 +431,7 @@ def run_ours(args, dist):
         "cpu_baseline": cpu,
         "learned_warmstart": learned,
         "ray_test": rays,
+        "step_graphs": graph_info,
         "clocks": clocks,
         "status_flags": final["status_flags"],
         "autotune": tuned,

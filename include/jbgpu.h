@@ -280,6 +280,17 @@ int jbgpu_world_synchronize(jbgpu_world* world);
  * the call returns with the hits written. */
 int jbgpu_world_ray_test(jbgpu_world* world, const float* from, const float* to, const int32_t* ray_world, int32_t n,
                          int32_t filter_group, int32_t filter_mask, int32_t device_buffers, jbgpu_ray_hit* hits);
+/* CUDA graphs for the step (no counterpart in the reference).  on != 0: every internal step
+ * replays two captured graphs (the launches before the pair-count readback and those after it)
+ * instead of launching its kernels one by one; results are bit-identical to the launch path.
+ * A graph is captured the first time a buffer arrangement occurs and is dropped whenever
+ * buffers or settings change.  Profiling, the learned warm start and sample logging use the
+ * launch path.  If a capture fails the world goes back to launches and
+ * jbgpu_world_graph_status reports why. */
+int jbgpu_world_set_graph(jbgpu_world* world, int32_t on);
+/* Graphs held (*graphs) and the capture failure that turned graphs off ("" when none; the
+ * string lives until the next jbgpu_world_set_graph). */
+int jbgpu_world_graph_status(jbgpu_world* world, int32_t* graphs, const char** error);
 /* Verification switch, no counterpart in the reference: all != 0 sends every ray of later
  * jbgpu_world_ray_test calls through the in-order replay of the reference's object loop (the
  * path rays take when the tree walk cannot decide them); results are the same either way. */

@@ -275,8 +275,11 @@ __global__ void k_segment_sort(int n, const int* off, const int* cnt, int* partn
 
 // Carry manifolds of persisting pairs (binary search in last step's sorted keys: within the
 // owner's segment when last step's per-owner offsets are at hand, else over all of them).
-__global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int nOld, const int* offPrev) {
+__global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int nOld, const int* offPrev, const int* newCnt,
+                          const int* oldCnt) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (newCnt) nNew = min(nNew, *newCnt);
+    if (oldCnt) nOld = min(nOld, *oldCnt);
     if (p >= nNew) return;
     uint64_t key = nw.keys[p];
     int lo = 0, hi = nOld - 1, found = -1;
@@ -403,9 +406,10 @@ void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw,
 }
 
 void broadphase_persist(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, const DevPairs& old, int nNew, int nOld,
-                        cudaStream_t s) {
+                        cudaStream_t s, const int* newCnt, const int* oldCnt) {
     if (nNew > 0) {
-        k_persist<<<gridn(nNew, 256), 256, 0, s>>>(w, nw, old, nNew, nOld, bb.offPrevValid ? bb.offPrev : nullptr);
+        k_persist<<<gridn(nNew, 256), 256, 0, s>>>(w, nw, old, nNew, nOld, bb.offPrevValid ? bb.offPrev : nullptr, newCnt,
+                                                    oldCnt);
         note_launch();
     }
     std::swap(bb.off, bb.offPrev);   // this step's offsets index the pair array the next step persists from

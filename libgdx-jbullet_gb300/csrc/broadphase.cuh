@@ -54,7 +54,8 @@ void broadphase_build_tree(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_
 void broadphase_refit_into(const DevWorld& wq, const BroadphaseBuffers& bb, float4* node, int* visit, cudaStream_t s);
 void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t s);
 void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, int capacity, cudaStream_t s);
+// newCnt / oldCnt (nullable): the pair counts on the device, nNew / nOld then being upper bounds.
 void broadphase_persist(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, const DevPairs& old, int nNew, int nOld,
-                        cudaStream_t s);
+                        cudaStream_t s, const int* newCnt = nullptr, const int* oldCnt = nullptr);
 
 }  // namespace jbg

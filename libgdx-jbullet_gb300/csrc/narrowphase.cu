@@ -73,11 +73,11 @@ JBD void block_bucket_counts(int v, int (*shc)[NB_THREADS / 32]) {
     }
     __syncthreads();
 }
-__global__ void k_narrow_count(DevWorld w, DevPairs P, int nPairs, unsigned char* bucket, int* blockCnt) {
+__global__ void k_narrow_count(DevWorld w, DevPairs P, int nPairs, const int* cntp, unsigned char* bucket, int* blockCnt) {
     __shared__ int shc[NB_BUCKETS][NB_THREADS / 32];
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     int v = -1;
-    if (p < nPairs) {
+    if (p < (cntp ? min(nPairs, *cntp) : nPairs)) {
         v = narrow_bucket(w, P, p);
         bucket[p] = (unsigned char)v;
     }
@@ -89,10 +89,10 @@ __global__ void k_narrow_count(DevWorld w, DevPairs P, int nPairs, unsigned char
     }
 }
 
-__global__ void k_narrow_scatter(int nPairs, const unsigned char* bucket, const int* blockOff, int* perm) {
+__global__ void k_narrow_scatter(int nPairs, const int* cntp, const unsigned char* bucket, const int* blockOff, int* perm) {
     __shared__ int shc[NB_BUCKETS][NB_THREADS / 32];
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    int v = p < nPairs ? bucket[p] : -1;
+    int v = p < (cntp ? min(nPairs, *cntp) : nPairs) ? bucket[p] : -1;
     block_bucket_counts(v, shc);
     if (v < 0) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -111,9 +111,9 @@ JBD int narrow_active(const int* blockOff, int nBlocks) { return blockOff[(NB_BU
 
 // With perm: n = the grouping's pair blocks and entry i is pair perm[i]; without: n = pairs.
 __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n, const int* perm, const int* blockOff, EpaRec* queue,
-                         int* queueCount) {
+                         int* queueCount, const int* cntp) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (perm ? narrow_active(blockOff, n) : n)) return;
+    if (i >= (perm ? narrow_active(blockOff, n) : (cntp ? min(n, *cntp) : n))) return;
     int p = perm ? perm[i] : i;
     uint64_t key = P.keys[p];
     int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
@@ -345,25 +345,26 @@ __global__ void __launch_bounds__(32) k_narrow_epa_smem(DevWorld w, DevPairs P, 
 static int gridn_nb(int nPairs) { return (nPairs + NB_THREADS - 1) / NB_THREADS; }
 
 // Groups the pairs by bucket into nb.perm (blockOff: scanned per-block bucket counts).
-static void narrow_group(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s) {
+static void narrow_group(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
+                         const int* cntp = nullptr) {
     const int blocks = gridn_nb(nPairs);
-    k_narrow_count<<<blocks, NB_THREADS, 0, s>>>(w, P, nPairs, nb.pairBucket, nb.blockOff); note_launch();
+    k_narrow_count<<<blocks, NB_THREADS, 0, s>>>(w, P, nPairs, cntp, nb.pairBucket, nb.blockOff); note_launch();
     exclusive_scan(nb.blockOff, nb.blockOff, nullptr, NB_BUCKETS * blocks, nb.scanScratch, s);
-    k_narrow_scatter<<<blocks, NB_THREADS, 0, s>>>(nPairs, nb.pairBucket, nb.blockOff, nb.perm); note_launch();
+    k_narrow_scatter<<<blocks, NB_THREADS, 0, s>>>(nPairs, cntp, nb.pairBucket, nb.blockOff, nb.perm); note_launch();
 }
 
 void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
-                        const Prof* prof) {
+                        const Prof* prof, const int* cntp) {
     if (prof) prof->mark(PH_NARROW, 0, s);
     cudaMemsetAsync(nb.queueCount, 0, sizeof(int), s);
     if (nPairs > 0) {
         if (nb.group) {
-            narrow_group(w, P, nPairs, nb, s);
+            narrow_group(w, P, nPairs, nb, s, cntp);
             k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, gridn_nb(nPairs), nb.perm, nb.blockOff,
-                                                           (EpaRec*)nb.queue, nb.queueCount); note_launch();
+                                                           (EpaRec*)nb.queue, nb.queueCount, nullptr); note_launch();
         } else {
             k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, nullptr, nullptr, (EpaRec*)nb.queue,
-                                                           nb.queueCount); note_launch();
+                                                           nb.queueCount, cntp); note_launch();
         }
     }
     if (prof) { prof->mark(PH_NARROW, 1, s); prof->mark(PH_EPA, 0, s); }
@@ -449,7 +450,7 @@ void narrowphase_launch_static(const DevWorld& w, DevPairs& P, int nPairs, Narro
     if (nPairs <= 0) return;
     narrow_group(w, P, nPairs, nb, s);
     k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, gridn_nb(nPairs), nb.perm, nb.blockOff, (EpaRec*)nb.queue,
-                                                   nb.queueCount); note_launch();
+                                                   nb.queueCount, nullptr); note_launch();
     unsigned char* b = (unsigned char*)base;
     EpaArena ar;
     ar.fN = (float4*)(b + OFF_FN);

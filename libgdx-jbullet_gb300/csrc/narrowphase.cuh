@@ -23,8 +23,9 @@ struct NarrowBuffers {
 
 size_t epa_queue_record_bytes();
 int narrowphase_configure();      // once per world: the EPA kernel's shared-memory size
+// cntp (nullable): the pair count on the device; nPairs is then an upper bound (graph replays).
 void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
-                        const Prof* prof = nullptr);
+                        const Prof* prof = nullptr, const int* cntp = nullptr);
 
 // Narrowphase whose EPA pass uses scratch compiled into the library (no allocation).
 constexpr int STATIC_EPA_SLOTS = JBGPU_STATIC_EPA_SLOTS_MAX;   // EPA warps that can run at once on it

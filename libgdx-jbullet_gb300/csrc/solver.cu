@@ -69,9 +69,9 @@ __global__ void k_uf_init(int n, int* parent) {
 // partition is the same as one pass over all pairs.
 constexpr int UF_ROUNDS = 4;
 
-__global__ void k_uf_union(DevWorld w, DevPairs P, int nPairs, int* parent, int round) {
+__global__ void k_uf_union(DevWorld w, DevPairs P, int nPairs, const int* cntp, int* parent, int round) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= nPairs) return;
+    if (p >= (cntp ? min(nPairs, *cntp) : nPairs)) return;
     uint64_t key = P.keys[p];
     int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
     int rank = 0;               // pairs of the same owner before p, up to 4
@@ -131,9 +131,10 @@ __global__ void k_island_sleep(DevWorld w, const int* keepAwake, int* inactive) 
 }
 
 // Candidate manifolds: in islandmanifold, island processed, at least one point with distance <= 0.
-__global__ void k_select(DevWorld w, DevPairs P, int nPairs, const int* inactive, int* flag) {
+__global__ void k_select(DevWorld w, DevPairs P, int nPairs, const int* cntp, const int* inactive, int* flag) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nPairs) return;
+    if (cntp && p >= *cntp) { flag[p] = 0; return; }   // past the device pair count: not a candidate
     int f = 0;
     if (P.has[p]) {
         int b0 = P.b0[p], b1 = P.b1[p];
@@ -159,23 +160,26 @@ __global__ void k_compact(int nPairs, const int* flag, const int* idx, int* cand
 }
 
 // Manifold counts (has, points) for the counters.
-__global__ void k_count_manifolds(DevPairs P, int nPairs, int* ctr) {
+__global__ void k_count_manifolds(DevPairs P, int nPairs, const int* cntp, int* ctr) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     int m = 0, c = 0;
-    if (p < nPairs && P.has[p]) { m = 1; c = P.n[p]; }
+    if (p < (cntp ? min(nPairs, *cntp) : nPairs) && P.has[p]) { m = 1; c = P.n[p]; }
     for (int o = 16; o > 0; o >>= 1) { m += __shfl_down_sync(0xffffffffu, m, o); c += __shfl_down_sync(0xffffffffu, c, o); }
     if ((threadIdx.x & 31) == 0 && (m || c)) { atomicAdd(&ctr[C_MANIFOLDS], m); atomicAdd(&ctr[C_CONTACTS], c); }
 }
 
 // Unions and the awake test read only pairs, flags and activation states, none of which the
-// narrowphase writes, so a step runs them beside the narrowphase on a second stream.
-void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s) {
+// narrowphase writes, so a step runs them beside the narrowphase on a second stream.  cntp
+// (nullable): the pair count on the device, nPairs then being only an upper bound (graph
+// replays, whose launches cannot know the count).
+void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s,
+                           const int* cntp) {
     int n = w.nBodies;
     k_uf_init<<<gridn(n, 256), 256, 0, s>>>(n, sb.parent); note_launch();
     if (nPairs > 0) {
         for (int r = 0; r < UF_ROUNDS; r++) {
             if (r > 0) { k_uf_compress<<<gridn(n, 256), 256, 0, s>>>(n, sb.parent); note_launch(); }
-            k_uf_union<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.parent, r); note_launch();
+            k_uf_union<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, cntp, sb.parent, r); note_launch();
         }
     }
     if (sb.J.n > 0) { k_joint_union<<<gridn(sb.J.n, 128), 128, 0, s>>>(w, sb); note_launch(); }
@@ -185,22 +189,23 @@ void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, Sol
 
 // Sleep decisions (they change activation states, which the narrowphase reads) and the
 // manifold selection (it reads the narrowphase's points): after the narrowphase.
-void islands_launch_select(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s) {
+void islands_launch_select(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s,
+                           const int* cntp) {
     int n = w.nBodies;
     k_island_sleep<<<gridn(n, 256), 256, 0, s>>>(w, sb.keepAwake, sb.inactive); note_launch();
     if (nPairs > 0) {
-        k_select<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, sb.inactive, sb.flag); note_launch();
+        k_select<<<gridn(nPairs, 256), 256, 0, s>>>(w, P, nPairs, cntp, sb.inactive, sb.flag); note_launch();
         exclusive_scan(sb.flag, sb.candIdx, sb.nCand, nPairs, sb.scanScratch, s);
         k_compact<<<gridn(nPairs, 256), 256, 0, s>>>(nPairs, sb.flag, sb.candIdx, sb.cand); note_launch();
-        k_count_manifolds<<<gridn(nPairs, 256), 256, 0, s>>>(P, nPairs, w.ctr); note_launch();
+        k_count_manifolds<<<gridn(nPairs, 256), 256, 0, s>>>(P, nPairs, cntp, w.ctr); note_launch();
     } else {
         cudaMemsetAsync(sb.nCand, 0, sizeof(int), s);
     }
 }
 
 void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s) {
-    islands_launch_unions(w, P, nPairs, sb, s);
-    islands_launch_select(w, P, nPairs, sb, s);
+    islands_launch_unions(w, P, nPairs, sb, s, nullptr);
+    islands_launch_select(w, P, nPairs, sb, s, nullptr);
 }
 
 // ---- grid barrier (bounded wait) -----------------------------------------------------------

@@ -114,8 +114,10 @@ struct SolverBuffers {
 int solver_configure(SolverBuffers& sb, int nFinite, const std::vector<int>& worldCounts, int sms, int rangeParts,
                      int threads, int smemBodies);
 void islands_launch(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
-void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
-void islands_launch_select(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s);
+void islands_launch_unions(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s,
+                           const int* cntp);
+void islands_launch_select(const DevWorld& w, const DevPairs& P, int nPairs, SolverBuffers& sb, cudaStream_t s,
+                           const int* cntp);
 void solve_launch(const DevWorld& w, DevPairs& P, int nPairs, DevRows& rows, SolverBuffers& sb, float dt, cudaStream_t s,
                   const Prof* prof = nullptr);
 void solver_free(SolverBuffers& sb);

@@ -126,9 +126,21 @@ struct jbgpu_world {
     float* sampleX = nullptr;     // capRows * 4 * 24
     float* sampleT = nullptr;     // capRows * 4 * 3
     int sampleCap = 0;            // rows the sample buffers hold
+    // CUDA graphs of the step (jbgpu_world_set_graph): the launches before the pair count
+    // readback and those after it, each captured once per buffer arrangement and replayed
+    bool graphOn = false;
+    std::string graphError;       // set when a capture failed: the world went back to launches
+    struct StepGraph {
+        uint64_t key[8];
+        cudaGraphExec_t exec;
+        long long launches;       // kernels in the graph
+    };
+    std::vector<StepGraph> graphs;
 };
 
 namespace {
+
+void graphs_clear(jbgpu_world* w);   // the step graphs bake pointers and arguments: see single_step_graph
 
 int num_sms_of(int dev) {
     int s = 0;
@@ -151,6 +163,7 @@ void free_pairs(DevPairs& P) {
 
 // Work buffers whose size follows the pair capacity.
 int alloc_pair_work(jbgpu_world* w, int cap) {
+    graphs_clear(w);
     DevRows& R = w->rows;
     dfree(R.n_nrm); dfree(R.n_rp1); dfree(R.n_rp2); dfree(R.n_angA); dfree(R.n_angB);
     dfree(R.f_nrm); dfree(R.f_rp1); dfree(R.f_rp2); dfree(R.f_angA); dfree(R.f_angB);
@@ -189,6 +202,7 @@ int alloc_pair_work(jbgpu_world* w, int cap) {
 
 int grow_bodies(jbgpu_world* w, int need) {
     if (need <= w->capBodies) return JBGPU_OK;
+    graphs_clear(w);
     int oldc = w->capBodies;
     int nc = std::max(need, std::max(2 * oldc, w->cfg.initial_body_capacity > 0 ? w->cfg.initial_body_capacity : 1024));
     cudaStream_t s = w->stream;
@@ -234,6 +248,7 @@ int ensure_pair_capacity(jbgpu_world* w, int buf, int need) {
     if (need <= w->capPairs[buf] && need <= w->capRows) return JBGPU_OK;
     int nc = std::max(need + need / 2 + 64, 2 * w->capPairs[buf]);
     if (need > w->capPairs[buf]) {
+        graphs_clear(w);
         free_pairs(w->pairs[buf]);
         int rc = alloc_pairs(w->pairs[buf], nc);
         if (rc) return rc;
@@ -355,6 +370,7 @@ int check_status(jbgpu_world* w) {
 }
 
 // ---- stages --------------------------------------------------------------------------------
+int stage_pairs_fill(jbgpu_world* w, int total);
 int stage_pairs(jbgpu_world* w) {
     DevWorld d = dev_view(w);
     cudaStream_t s = w->stream;
@@ -364,7 +380,13 @@ int stage_pairs(jbgpu_world* w) {
     w->prof.mark(PH_PAIR_COUNT, 1, s);
     CK(cudaMemcpyAsync(w->hostPinned, w->bb.total, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    int total = *w->hostPinned;
+    return stage_pairs_fill(w, *w->hostPinned);
+}
+
+// The pair stage after the count: buffers for `total` pairs, fill, persistence.
+int stage_pairs_fill(jbgpu_world* w, int total) {
+    DevWorld d = dev_view(w);
+    cudaStream_t s = w->stream;
     int nxt = w->cur ^ 1;
     int rc = ensure_pair_capacity(w, nxt, total);
     if (rc) return rc;
@@ -384,6 +406,7 @@ int prepare_solver(jbgpu_world* w) {
     SolverBuffers& S = w->sb;
     const int nf = w->bb.nFinite;
     if (w->solverDirty) {
+        graphs_clear(w);
         int rc = solver_configure(S, nf, w->worldFinite, w->sms, w->cfg.solver_parts,
                                   w->cfg.solver_threads ? w->cfg.solver_threads : SOLVER_THREADS, w->cfg.solver_smem_bodies);
         if (rc) return fail(rc, "solver part tables");
@@ -520,6 +543,7 @@ int sync_joints(jbgpu_world* w) {
 
 int prepare(jbgpu_world* w) {
     CK(cudaSetDevice(w->device));
+    if (w->shapesDirty || w->planesDirty || w->jointsDirty || w->solverDirty) graphs_clear(w);
     int rc = sync_shapes(w);
     if (rc) return rc;
     rc = sync_planes(w);
@@ -527,27 +551,183 @@ int prepare(jbgpu_world* w) {
     return sync_joints(w);
 }
 
+void graphs_clear(jbgpu_world* w) {
+    for (auto& g : w->graphs) cudaGraphExecDestroy(g.exec);
+    w->graphs.clear();
+}
+
 // Narrowphase and islands of one step: the island unions run on the second stream while the
 // narrowphase runs on the world's stream; sleep decisions and manifold selection follow both.
-int narrow_and_islands(jbgpu_world* w) {
+// cntp (nullable): the pair count on the device, w->nPairs then being an upper bound.
+int narrow_and_islands(jbgpu_world* w, const int* cntp = nullptr) {
     cudaStream_t s = w->stream, a = w->aux;
     DevWorld d = dev_view(w);
     CK(cudaEventRecord(w->evFork, s));
     CK(cudaStreamWaitEvent(a, w->evFork, 0));
     CK(cudaMemsetAsync(w->dw.ctr + C_ISLANDS, 0, sizeof(int) * 4, a));
-    islands_launch_unions(d, w->pairs[w->cur], w->nPairs, w->sb, a);
+    islands_launch_unions(d, w->pairs[w->cur], w->nPairs, w->sb, a, cntp);
     CK(cudaEventRecord(w->evJoin, a));
     CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
-    narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s, &w->prof);
+    narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s, &w->prof, cntp);
     CK(cudaStreamWaitEvent(s, w->evJoin, 0));
     w->prof.mark(PH_ISLANDS, 0, s);
-    islands_launch_select(d, w->pairs[w->cur], w->nPairs, w->sb, s);
+    islands_launch_select(d, w->pairs[w->cur], w->nPairs, w->sb, s, cntp);
     w->prof.mark(PH_ISLANDS, 1, s);
     CK(cudaGetLastError());
     return JBGPU_OK;
 }
 
+// ---- the step as two CUDA graphs ------------------------------------------------------------
+// Graph A holds the launches up to the pair count (predict, aabbs, the broadphase count with the
+// tree rebuild or refit) and copies the count to pinned host memory; the host reads it (the one
+// synchronisation of a step, as in the launch path), grows the pair buffers if needed, and
+// replays graph B: pair fill and persistence, narrowphase with the islands on the second stream,
+// the solver, integration and activation.  B's kernels read the pair count from the device
+// (w.ctr[C_PAIRS], the broadphase total) and are sized by the pair capacity.  Launches bake
+// their pointers and host-side arguments, so each graph is kept per arrangement of the
+// alternating buffers (pair arrays, per-owner offsets), the tree path (rebuild or refit) and dt;
+// anything else that changes a buffer or an argument clears them all (graphs_clear).  The host
+// state the launch functions change while a graph is captured (tree age, offset swap) is
+// changed by hand when the graph is replayed.
+namespace {
+constexpr int GRAPH_FALLBACK = -1000;   // a capture failed: the step goes on with launches
+
+template <class F>
+int capture_or_replay(jbgpu_world* w, const uint64_t key[8], F&& body, bool& captured) {
+    captured = false;
+    for (auto& g : w->graphs)
+        if (std::equal(g.key, g.key + 8, key)) {
+            CK(cudaGraphLaunch(g.exec, w->stream));
+            g_launches.fetch_add(g.launches, std::memory_order_relaxed);
+            return JBGPU_OK;
+        }
+    cudaStream_t s = w->stream;
+    const long long l0 = g_launches.load();
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        w->graphError = "stream capture could not begin";
+        cudaGetLastError();
+        return GRAPH_FALLBACK;
+    }
+    int rc = body();
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    const long long n = g_launches.load() - l0;
+    g_launches.fetch_sub(n, std::memory_order_relaxed);
+    cudaGraphExec_t exec = nullptr;
+    if (rc == JBGPU_OK && e == cudaSuccess && graph) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (rc != JBGPU_OK || e != cudaSuccess || !exec) {
+        w->graphError = std::string("graph capture failed: ") + (rc != JBGPU_OK ? g_err : cudaGetErrorString(e));
+        cudaGetLastError();
+        return GRAPH_FALLBACK;
+    }
+    jbgpu_world::StepGraph g;
+    std::copy(key, key + 8, g.key);
+    g.exec = exec;
+    g.launches = n;
+    w->graphs.push_back(g);
+    captured = true;
+    CK(cudaGraphLaunch(exec, s));
+    g_launches.fetch_add(n, std::memory_order_relaxed);
+    return JBGPU_OK;
+}
+
+uint64_t fbits64(float f) { uint32_t u; std::memcpy(&u, &f, 4); return u; }
+
+int single_step_graph(jbgpu_world* w, float dt) {
+    cudaStream_t s = w->stream;
+    BroadphaseBuffers& B = w->bb;
+    const bool rebuild = !(B.built && B.sinceBuild + 1 < B.rebuildInterval);
+    const bool builtBefore = B.built;
+    const int ageBefore = B.sinceBuild;
+    const uint64_t ka[8] = {1, (uint64_t)rebuild, (uint64_t)(uintptr_t)B.off, (uint64_t)(uintptr_t)B.offPrev,
+                            fbits64(dt), 0, 0, 0};
+    bool captured = false;
+    int rc = capture_or_replay(w, ka, [&]() -> int {
+        DevWorld d = dev_view(w);
+        launch_predict(d, dt, s);
+        launch_aabb(d, s);
+        broadphase_run_count(d, B, s);
+        CK(cudaMemcpyAsync(w->hostPinned + 1, B.total, sizeof(int), cudaMemcpyDeviceToHost, s));
+        return JBGPU_OK;
+    }, captured);
+    if (rc == GRAPH_FALLBACK) {            // nothing ran: undo the capture's host side
+        B.built = builtBefore;
+        B.sinceBuild = ageBefore;
+        return GRAPH_FALLBACK;
+    }
+    if (rc) return rc;
+    if (!captured) {                       // what broadphase_run_count does on the host
+        if (rebuild) { B.built = true; B.sinceBuild = 0; }
+        else B.sinceBuild++;
+    }
+    w->orderValid = true;
+    CK(cudaStreamSynchronize(s));
+    const int total = w->hostPinned[1];
+    const int nxt = w->cur ^ 1;
+    const int capBefore = w->capRows;
+    void* keysBefore = w->pairs[nxt].keys;
+    if ((rc = ensure_pair_capacity(w, nxt, total))) return rc;
+    if (w->capRows != capBefore || w->pairs[nxt].keys != keysBefore) graphs_clear(w);
+    if ((rc = prepare_solver(w))) return rc;
+    const int old = w->cur;
+    int* const offBefore = B.off;
+    int* const offPrevBefore = B.offPrev;
+    const bool offValidBefore = B.offPrevValid;
+    const int nPairsBefore = w->nPairs;
+    const uint64_t kb[8] = {2, (uint64_t)(uintptr_t)w->pairs[old].keys, (uint64_t)(uintptr_t)w->pairs[nxt].keys,
+                            (uint64_t)(uintptr_t)B.off, (uint64_t)(uintptr_t)B.offPrev, (uint64_t)B.offPrevValid,
+                            (uint64_t)w->capRows, fbits64(dt)};
+    const int bound = w->capRows;
+    int* cnt = w->dw.ctr + C_PAIRS;
+    w->cur = nxt;
+    w->nPairs = bound;                     // launches are sized by the capacity ...
+    rc = capture_or_replay(w, kb, [&]() -> int {
+        DevWorld d = dev_view(w);
+        broadphase_run_fill(d, B, w->pairs[nxt], bound, s);
+        broadphase_persist(d, B, w->pairs[nxt], w->pairs[old], bound, w->capPairs[old], s, B.total, cnt);
+        CK(cudaMemcpyAsync(cnt, B.total, sizeof(int), cudaMemcpyDeviceToDevice, s));
+        int r = narrow_and_islands(w, cnt);   // ... and read the count from the device
+        if (r) return r;
+        static const int rest[] = {JBGPU_STAGE_SOLVE, JBGPU_STAGE_INTEGRATE, JBGPU_STAGE_ACTIVATION};
+        for (int st : rest)
+            if ((r = run_stage(w, st, dt))) return r;
+        return JBGPU_OK;
+    }, captured);
+    if (rc == GRAPH_FALLBACK) {            // the count ran; the rest with launches
+        B.off = offBefore;
+        B.offPrev = offPrevBefore;
+        B.offPrevValid = offValidBefore;
+        w->cur = old;
+        w->nPairs = nPairsBefore;
+        static const int rest[] = {JBGPU_STAGE_NARROWPHASE, JBGPU_STAGE_SOLVE, JBGPU_STAGE_INTEGRATE,
+                                   JBGPU_STAGE_ACTIVATION};
+        if ((rc = stage_pairs_fill(w, total))) return rc;
+        for (int st : rest)
+            if ((rc = st == JBGPU_STAGE_NARROWPHASE ? narrow_and_islands(w) : run_stage(w, st, dt))) return rc;
+        w->steps++;
+        return JBGPU_OK;
+    }
+    w->nPairs = total;
+    if (rc) return rc;
+    if (!captured) {                       // broadphase_persist's host side
+        std::swap(B.off, B.offPrev);
+        B.offPrevValid = true;
+    }
+    w->steps++;
+    return JBGPU_OK;
+}
+
+bool graph_usable(const jbgpu_world* w) {
+    return w->graphOn && w->graphError.empty() && !w->prof.active() && !w->mlp && !w->logSamples && w->nBodies > 0;
+}
+}  // namespace
+
 int single_step(jbgpu_world* w, float dt) {
+    if (graph_usable(w)) {
+        int rc = single_step_graph(w, dt);
+        if (rc != GRAPH_FALLBACK) return rc;   // else the capture failed before anything ran
+    }
     static const int order[] = {JBGPU_STAGE_PREDICT, JBGPU_STAGE_AABB, JBGPU_STAGE_PAIRS, JBGPU_STAGE_NARROWPHASE,
                                 JBGPU_STAGE_SOLVE, JBGPU_STAGE_INTEGRATE, JBGPU_STAGE_ACTIVATION};
     for (int st : order) {
@@ -764,6 +944,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     cudaSetDevice(w->device);
     if (w->stream) cudaStreamSynchronize(w->stream);
     if (w->aux) cudaStreamSynchronize(w->aux);
+    graphs_clear(w);
     query_free(w->qb);
     DevWorld& d = w->dw;
     dfree(d.xr0); dfree(d.xr1); dfree(d.xr2); dfree(d.linvel); dfree(d.angvel); dfree(d.iw0); dfree(d.iw1); dfree(d.iw2);
@@ -1046,6 +1227,7 @@ int jbgpu_world_set_solver_iterations(jbgpu_world* w, int32_t num_iterations, fl
     w->cfg.num_iterations = num_iterations;
     w->cfg.solver_residual = residual;
     w->cfg.solver_max_iterations = max_iterations;
+    graphs_clear(w);
     w->dw.numIter = num_iterations;
     w->dw.resTol = residual;
     w->dw.maxIter = max_iterations > 0 ? max_iterations : 200;
@@ -1265,6 +1447,23 @@ int jbgpu_world_ray_test(jbgpu_world* w, const float* from, const float* to, con
     return JBGPU_OK;
 }
 
+int jbgpu_world_set_graph(jbgpu_world* w, int32_t on) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    CK(cudaSetDevice(w->device));
+    CK(cudaStreamSynchronize(w->stream));
+    graphs_clear(w);
+    w->graphOn = on != 0;
+    w->graphError.clear();
+    return JBGPU_OK;
+}
+
+int jbgpu_world_graph_status(jbgpu_world* w, int32_t* graphs, const char** error) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (graphs) *graphs = (int32_t)w->graphs.size();
+    if (error) *error = w->graphError.c_str();
+    return JBGPU_OK;
+}
+
 int jbgpu_world_set_ray_replay(jbgpu_world* w, int32_t all) {
     if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
     w->qb.replayAll = all != 0;
@@ -1443,6 +1642,7 @@ int jbgpu_world_get_manifolds(jbgpu_world* w, jbgpu_manifolds* m) {
 int jbgpu_world_set_manifolds(jbgpu_world* w, const jbgpu_manifolds* m) {
     if (!w || !m || m->n_pairs < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
     CK(cudaSetDevice(w->device));
+    graphs_clear(w);
     int rc = prepare(w);
     if (rc) return rc;
     int np = m->n_pairs;

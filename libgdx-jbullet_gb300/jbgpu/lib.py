@@ -63,6 +63,8 @@ def lib():
             "jbgpu_world_ray_test": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.c_void_p], C.c_int),
             "jbgpu_world_set_ray_replay": ([C.c_void_p, C.c_int32], C.c_int),
+            "jbgpu_world_set_graph": ([C.c_void_p, C.c_int32], C.c_int),
+            "jbgpu_world_graph_status": ([C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_char_p)], C.c_int),
             "jbgpu_world_add_hinge": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.POINTER(C.c_int32)],
                                       C.c_int),
             "jbgpu_world_set_hinge_limit": ([C.c_void_p, C.c_int32] + [C.c_float] * 5, C.c_int),
@@ -102,7 +104,7 @@ EXPORTED = [
     "jbgpu_world_profile_counters", "jbgpu_world_timer", "jbgpu_world_add_point2point", "jbgpu_world_set_joint_setting",
     "jbgpu_world_get_joint_impulses", "jbgpu_world_add_hinge", "jbgpu_world_set_hinge_limit",
     "jbgpu_world_enable_hinge_motor", "jbgpu_world_set_hinge_angular_only", "jbgpu_world_ray_test",
-    "jbgpu_world_set_ray_replay",
+    "jbgpu_world_set_ray_replay", "jbgpu_world_set_graph", "jbgpu_world_graph_status",
 ]
 
 
@@ -267,6 +269,16 @@ class GpuWorld:
     def ray_test_device(self, from_ptr, to_ptr, n, hits_ptr, world_ptr=None, group=1, mask=-1):
         """rayTest on device buffers (raw pointers); queued on the world's stream."""
         check(lib().jbgpu_world_ray_test(self.h, from_ptr, to_ptr, world_ptr, n, group, mask, 1, hits_ptr))
+
+    def set_graph(self, on):
+        """Replay the step as CUDA graphs (bit-identical to launching its kernels)."""
+        check(lib().jbgpu_world_set_graph(self.h, 1 if on else 0))
+
+    def graph_status(self):
+        n = C.c_int32()
+        e = C.c_char_p()
+        check(lib().jbgpu_world_graph_status(self.h, C.byref(n), C.byref(e)))
+        return n.value, (e.value or b"").decode()
 
     def set_ray_replay(self, all_rays):
         check(lib().jbgpu_world_set_ray_replay(self.h, 1 if all_rays else 0))
