@@ -134,7 +134,11 @@ typedef struct jbgpu_config {
     int32_t broadphase_rebuild_interval;/* rebuild the broadphase tree every this many steps and
                                            refit it in between (0 or 1: every step; default 4).  The
                                            pair set is the same either way.  A tuning knob. */
-    int32_t reserved[2];
+    int32_t step_graphs;                /* 1 (default): internal steps replay captured CUDA graphs
+                                           (jbgpu_world_set_graph); 0: their kernels are launched one
+                                           by one.  Bit-identical results.  No counterpart in the
+                                           reference. */
+    int32_t reserved[1];
 } jbgpu_config;
 
 typedef struct jbgpu_shape_desc {

@@ -803,6 +803,7 @@ void jbgpu_config_default(jbgpu_config* c) {
     c->initial_body_capacity = 1024;
     c->pairs_per_body = 16;
     c->broadphase_rebuild_interval = 4;
+    c->step_graphs = 1;
 }
 
 int jbgpu_shape_local_inertia(const jbgpu_shape_desc* d, float mass, float out[3]) {
@@ -903,6 +904,7 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
     d.disableDeact = c.disable_deactivation;
     d.numIter = c.num_iterations;
     w->bb.rebuildInterval = std::max(1, c.broadphase_rebuild_interval);
+    w->graphOn = c.step_graphs != 0;
     d.resTol = c.solver_residual > 0.0f ? c.solver_residual : 0.0f;
     d.maxIter = c.solver_max_iterations > 0 ? c.solver_max_iterations : 200;
     d.erp = c.erp;

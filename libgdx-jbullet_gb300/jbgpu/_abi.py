@@ -73,7 +73,8 @@ class Config(C.Structure):
         ("solver_max_iterations", C.c_int32),
         ("solver_smem_bodies", C.c_int32),
         ("broadphase_rebuild_interval", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("step_graphs", C.c_int32),
+        ("reserved", C.c_int32 * 1),
     ]
 
 
@@ -93,6 +94,7 @@ def default_config(**overrides):
     c.initial_body_capacity = 1024
     c.pairs_per_body = 16
     c.broadphase_rebuild_interval = 4
+    c.step_graphs = 1
     for k, v in overrides.items():
         if k == "gravity":
             c.gravity[:] = tuple(v)

@@ -1,6 +1,6 @@
-"""The step replayed as CUDA graphs (jbgpu_world_set_graph) against the same step launched kernel
-by kernel: body state, manifolds and joint impulses bit-identical after every checked step, on
-a falling mix of every shape (the pair count grows, so the pair buffers grow and the graphs are
+"""The step replayed as CUDA graphs (jbgpu_world_set_graph; the default, jbgpu_config.step_graphs)
+against the same step launched kernel by kernel: body state, manifolds and joint impulses
+bit-identical after every checked step, on a falling mix of every shape (the pair count grows, so the pair buffers grow and the graphs are
 captured again), on batch worlds with joints, across a change of the iteration count, and with
 the graphs actually in use (held, no capture failure)."""
 import numpy as np
@@ -15,6 +15,7 @@ import harness as H
 def _pair(sc, **cfg):
     c = _abi.default_config(**dict(sc.config, **cfg))
     eager = GpuWorld(sc, config=c)
+    eager.set_graph(False)
     graph = GpuWorld(sc, config=c)
     graph.set_graph(True)
     return eager, graph
