@@ -7,12 +7,14 @@
 // SubsimplexConvexCast of a point along the ray (convex shapes) or the two triangles a
 // StaticPlaneShape spans around the ray (TriangleRaycastCallback); a hit is taken when its
 // fraction is below the closest so far.  Here one thread per ray walks the broadphase tree
-// (refit over the shapes' current aabbs) and evaluates every object whose aabb the ray enters
-// before its end.  An object's cast does not depend on the hits before it, so the walk keeps
-// the few smallest hits ordered by (fraction, body, triangle).  The smallest, j, is the
-// reference's answer unless an object before j in body order hit below j's aabb entry (then the
-// order-dependent aabb test may have skipped j): such rays, rare, are replayed in body order by
-// a block each.
+// (refit over the shapes' current aabbs) twice - counting, then writing - to list every object
+// whose aabb the ray enters before its end; then one thread per listed (ray, object) runs the
+// object's cast, so that the warps run one code path (a thread per ray walking and casting by
+// turns kept under two threads of a warp active).  An object's cast does not depend on the hits
+// before it, so the ray's answer is its smallest hit by (fraction, body, triangle), j - found by
+// a 64-bit atomicMin - unless an object before j in body order hit below j's aabb entry (then the
+// order-dependent aabb test may have skipped j): such rays, rare, are replayed in body order by a
+// block each.
 #include "../../include/jbgpu.h"
 #include "gjk.cuh"
 #include "prims.cuh"
@@ -22,7 +24,6 @@
 namespace jbg {
 using namespace jbd;
 
-constexpr int RAY_KEEP = 4;       // smallest hits kept per ray
 constexpr int RAY_STACK = 64;
 constexpr int RAY_THREADS = 128;
 constexpr int SLOW_THREADS = 256;
@@ -216,16 +217,6 @@ JBD bool passes_filter(const DevWorld& w, int b, int group, int mask) {   // Ray
     return ((w.group[b] & mask) & 0xFFFF) != 0 && ((group & w.mask[b]) & 0xFFFF) != 0;
 }
 
-struct Hit {
-    float f;
-    int body, sub;
-    float enter;
-    V n;
-};
-JBD bool hit_before(float f, int body, int sub, const Hit& h) {
-    return f < h.f || (f == h.f && (body < h.body || (body == h.body && sub < h.sub)));
-}
-
 // Conservative slab test for the tree's inner boxes (inflated, so that no box the exact test
 // accepts is culled).
 JBD bool slab(V o, V d, float4 mn, float4 mx) {
@@ -249,43 +240,42 @@ JBD bool slab(V o, V d, float4 mn, float4 mx) {
     return true;
 }
 
-__global__ void __launch_bounds__(RAY_THREADS) k_rays(DevWorld w, DevWorld wq, const int* sortedBody, Bvh tree,
-                                                     const int* wroot, const int* planeList, const int* planeStart,
-                                                     const float* from, const float* to, const int* rayWorld, int n,
-                                                     int group, int mask, jbgpu_ray_hit* out, int* slow, int* slowCount,
-                                                     int replayAll) {
+// A ray's candidate: a body whose aabb the ray enters before its end (rayAabb with the bound 1,
+// which every closest fraction respects) and which passes the callback's filter.
+struct RayCand {
+    int ray, body;
+    float enter;
+    int pad;
+};
+
+// Tree walk of one ray per thread: COUNT counts the candidates, else they are written at the
+// ray's offset (the same walk, so the same candidates in the same order).
+template <bool COUNT>
+__global__ void __launch_bounds__(RAY_THREADS) k_ray_walk(DevWorld w, DevWorld wq, const int* sortedBody, Bvh tree,
+                                                         const int* wroot, const int* planeList, const int* planeStart,
+                                                         const float* from, const float* to, const int* rayWorld, int n,
+                                                         int group, int mask, int* cnt, const int* off, RayCand* cand) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
-    if (replayAll) {
-        slow[atomicAdd(slowCount, 1)] = r;
-        return;
-    }
     const V f = mk(from[3 * r], from[3 * r + 1], from[3 * r + 2]);
     const V t = mk(to[3 * r], to[3 * r + 1], to[3 * r + 2]);
     const int wi = rayWorld ? rayWorld[r] : 0;
-    Hit keep[RAY_KEEP];
-    int nk = 0;
-    float dropMin = __int_as_float(0x7f800000);
+    const int base = COUNT ? 0 : off[r];
+    int c = 0;
     auto consider = [&](int b) {
         if (!passes_filter(w, b, group, mask)) return;
         float enter, exit;
         if (!ray_aabb_parts(f, t, mk4(wq.amin[b]), mk4(wq.amax[b]), enter, exit)) return;
         if (!(enter <= jmin(1.0f, exit))) return;
-        ObjHits h;
-        ray_object(w, b, f, t, h);
-        for (int k = 0; k < h.n; k++) {
-            int pos = nk;
-            while (pos > 0 && hit_before(h.f[k], b, k, keep[pos - 1])) pos--;
-            if (pos >= RAY_KEEP) { dropMin = fminf(dropMin, h.f[k]); continue; }
-            if (nk == RAY_KEEP) dropMin = fminf(dropMin, keep[RAY_KEEP - 1].f);
-            for (int q = (nk < RAY_KEEP ? nk : RAY_KEEP - 1); q > pos; q--) keep[q] = keep[q - 1];
-            keep[pos].f = h.f[k];
-            keep[pos].body = b;
-            keep[pos].sub = k;
-            keep[pos].enter = enter;
-            keep[pos].n = h.nrm[k];
-            if (nk < RAY_KEEP) nk++;
+        if (!COUNT) {
+            RayCand rc;
+            rc.ray = r;
+            rc.body = b;
+            rc.enter = enter;
+            rc.pad = 0;
+            cand[base + c] = rc;
         }
+        c++;
     };
     const int root = wroot[wi];
     if (root != -1) {
@@ -299,9 +289,9 @@ __global__ void __launch_bounds__(RAY_THREADS) k_rays(DevWorld w, DevWorld wq, c
             while (sp > 0) {
                 const float4* nd = tree.node + 4 * stack[--sp];
                 const float4 rec[4] = {nd[0], nd[1], nd[2], nd[3]};
-                for (int c = 0; c < 2; c++) {
-                    if (!slab(f, d, rec[2 * c], rec[2 * c + 1])) continue;
-                    const int x = __float_as_int(rec[2 * c].w);
+                for (int k = 0; k < 2; k++) {
+                    if (!slab(f, d, rec[2 * k], rec[2 * k + 1])) continue;
+                    const int x = __float_as_int(rec[2 * k].w);
                     if (x & LEAF_FLAG) consider(sortedBody[x & ~LEAF_FLAG]);
                     else if (sp < RAY_STACK) stack[sp++] = x;
                     else atomicOr(&w.ctr[C_STATUS], ST_CAPACITY);
@@ -310,26 +300,82 @@ __global__ void __launch_bounds__(RAY_THREADS) k_rays(DevWorld w, DevWorld wq, c
         }
     }
     for (int q = planeStart[wi]; q < planeStart[wi + 1]; q++) consider(planeList[q]);
+    if (COUNT) cnt[r] = c;
+}
+
+JBD unsigned long long hit_key(float f, int body, int sub) {    // (fraction, body, triangle) order
+    return ((unsigned long long)__float_as_uint(f) << 32) | ((unsigned long long)body << 1) | (unsigned)sub;
+}
+
+// One candidate per thread: the object's hits (ray_object), kept per candidate (.w = fraction,
+// -1 for none), and the ray's smallest hit key by a 64-bit atomicMin (fractions are >= 0, so
+// their bits order as the values do).
+__global__ void __launch_bounds__(RAY_THREADS) k_ray_cast(DevWorld w, const RayCand* cand, int total, const float* from,
+                                                         const float* to, float4* hitA, float4* hitB,
+                                                         unsigned long long* key) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const RayCand c = cand[i];
+    const V f = mk(from[3 * c.ray], from[3 * c.ray + 1], from[3 * c.ray + 2]);
+    const V t = mk(to[3 * c.ray], to[3 * c.ray + 1], to[3 * c.ray + 2]);
+    ObjHits h;
+    ray_object(w, c.body, f, t, h);
+    hitA[i] = h.n > 0 ? f4(h.nrm[0], h.f[0]) : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    hitB[i] = h.n > 1 ? f4(h.nrm[1], h.f[1]) : make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+    for (int k = 0; k < h.n; k++) atomicMin(key + c.ray, hit_key(h.f[k], c.body, k));
+}
+
+// The candidate holding a ray's smallest hit j writes the ray's record and j's aabb entry.
+__global__ void k_ray_pick(const RayCand* cand, int total, const float4* hitA, const float4* hitB,
+                           const unsigned long long* key, const float* from, const float* to, float* enterJ,
+                           jbgpu_ray_hit* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const RayCand c = cand[i];
+    const unsigned long long k = key[c.ray];
+    if (k == ~0ull || (int)((k >> 1) & 0x7fffffffu) != c.body) return;
+    const float4 h = (k & 1) ? hitB[i] : hitA[i];
+    enterJ[c.ray] = c.enter;
+    jbgpu_ray_hit o;
+    o.body = c.body;
+    o.fraction = h.w;
+    o.normal[0] = h.x; o.normal[1] = h.y; o.normal[2] = h.z;
+    const V p = interp3(mk(from[3 * c.ray], from[3 * c.ray + 1], from[3 * c.ray + 2]),
+                        mk(to[3 * c.ray], to[3 * c.ray + 1], to[3 * c.ray + 2]), h.w);
+    o.point[0] = p.x; o.point[1] = p.y; o.point[2] = p.z;
+    out[c.ray] = o;
+}
+
+// j is the reference's answer unless an object before it in body order hit below j's aabb
+// entry (the reference's aabb test, bounded by the closest hit so far, could then skip j).
+__global__ void k_ray_check(const RayCand* cand, int total, const float4* hitA, const float4* hitB,
+                            const unsigned long long* key, const float* enterJ, int* undecided) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const RayCand c = cand[i];
+    const unsigned long long k = key[c.ray];
+    if (k == ~0ull || c.body >= (int)((k >> 1) & 0x7fffffffu)) return;
+    const float e = enterJ[c.ray];
+    const float a = hitA[i].w, b = hitB[i].w;
+    if ((a >= 0.0f && a < e) || (b >= 0.0f && b < e)) undecided[c.ray] = 1;
+}
+
+// Rays without a hit get the callback's untouched record; undecided rays (and every ray when
+// the replay is forced) go to the in-order replay.
+__global__ void k_ray_finish(int n, const unsigned long long* key, const int* undecided, int replayAll,
+                             jbgpu_ray_hit* out, int* slow, int* slowCount) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    if (replayAll || undecided[r]) {
+        slow[atomicAdd(slowCount, 1)] = r;
+        return;
+    }
+    if (key[r] != ~0ull) return;
     jbgpu_ray_hit o;
     o.body = -1;
     o.fraction = 1.0f;
     o.normal[0] = o.normal[1] = o.normal[2] = 0.0f;
     o.point[0] = o.point[1] = o.point[2] = 0.0f;
-    if (nk > 0) {
-        const Hit& j = keep[0];
-        bool decided = !(dropMin < j.enter);
-        for (int q = 1; q < nk; q++)
-            if (keep[q].body < j.body && keep[q].f < j.enter) decided = false;
-        if (!decided) {
-            slow[atomicAdd(slowCount, 1)] = r;
-            return;
-        }
-        o.body = j.body;
-        o.fraction = j.f;
-        o.normal[0] = j.n.x; o.normal[1] = j.n.y; o.normal[2] = j.n.z;
-        const V p = interp3(f, t, j.f);
-        o.point[0] = p.x; o.point[1] = p.y; o.point[2] = p.z;
-    }
     out[r] = o;
 }
 
@@ -398,17 +444,6 @@ __global__ void __launch_bounds__(SLOW_THREADS) k_rays_slow(DevWorld w, DevWorld
     }
 }
 
-template <typename T>
-static int grow(T*& p, int& cap, int need) {
-    if (need <= cap) return JBGPU_OK;
-    if (p) cudaFree(p);
-    p = nullptr;
-    const int c = need > 2 * cap ? need : 2 * cap;
-    if (cudaMalloc((void**)&p, sizeof(T) * (size_t)c) != cudaSuccess) { cap = 0; return JBGPU_ERR_CUDA; }
-    cap = c;
-    return JBGPU_OK;
-}
-
 int query_prepare(const DevWorld& w, BroadphaseBuffers& bb, QueryBuffers& qb, cudaStream_t s) {
     if (w.nBodies > qb.capBodies) {
         if (qb.qmin) cudaFree(qb.qmin);
@@ -447,18 +482,77 @@ int query_prepare(const DevWorld& w, BroadphaseBuffers& bb, QueryBuffers& qb, cu
 int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb, const float* from, const float* to,
                const int* rayWorld, int n, int group, int mask, jbgpu_ray_hit* hits, int sms, cudaStream_t s) {
     if (n <= 0) return JBGPU_OK;
-    int rc = grow(qb.slow, qb.capSlow, n);
-    if (rc) return rc;
-    if (!qb.slowCount && cudaMalloc((void**)&qb.slowCount, sizeof(int)) != cudaSuccess) return JBGPU_ERR_CUDA;
+    int rc;
+    if (n > qb.capRays) {   // per-ray buffers
+        void* old[] = {qb.slow, qb.rayCnt, qb.rayOff, qb.key, qb.enterJ, qb.undecided, qb.scanScratch};
+        for (void* p : old)
+            if (p) cudaFree(p);
+        qb.slow = qb.rayCnt = qb.rayOff = qb.undecided = nullptr;
+        qb.key = nullptr;
+        qb.enterJ = nullptr;
+        qb.scanScratch = nullptr;
+        qb.capRays = 0;
+        const int c = n > 2 * qb.capRays ? n : 2 * qb.capRays;
+        if (cudaMalloc((void**)&qb.slow, sizeof(int) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.rayCnt, sizeof(int) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.rayOff, sizeof(int) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.key, sizeof(unsigned long long) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.enterJ, sizeof(float) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.undecided, sizeof(int) * (size_t)c) != cudaSuccess ||
+            cudaMalloc(&qb.scanScratch, scan_scratch_bytes(c)) != cudaSuccess)
+            return JBGPU_ERR_CUDA;
+        qb.capRays = c;
+    }
+    if (!qb.slowCount && (cudaMalloc((void**)&qb.slowCount, sizeof(int)) != cudaSuccess ||
+                          cudaMalloc((void**)&qb.candTotal, sizeof(int)) != cudaSuccess))
+        return JBGPU_ERR_CUDA;
     cudaMemsetAsync(qb.slowCount, 0, sizeof(int), s);
+    cudaMemsetAsync(qb.key, 0xff, sizeof(unsigned long long) * n, s);
+    cudaMemsetAsync(qb.undecided, 0, sizeof(int) * n, s);
     DevWorld wq = w;
     wq.amin = qb.qmin;
     wq.amax = qb.qmax;
     Bvh tree = bb.bvh;
     tree.node = qb.node;
-    k_rays<<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList, bb.planeStart,
-                                                          from, to, rayWorld, n, group, mask, hits, qb.slow, qb.slowCount,
-                                                          qb.replayAll);
+    if (!qb.replayAll) {
+        k_ray_walk<true><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList,
+                                                                        bb.planeStart, from, to, rayWorld, n, group, mask,
+                                                                        qb.rayCnt, nullptr, nullptr);
+        note_launch();
+        exclusive_scan(qb.rayCnt, qb.rayOff, qb.candTotal, n, qb.scanScratch, s);
+        int total = 0;
+        if (cudaMemcpyAsync(&total, qb.candTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return JBGPU_ERR_CUDA;
+        if (total > qb.capCand) {
+            void* old[] = {qb.cand, qb.hitA, qb.hitB};
+            for (void* p : old)
+                if (p) cudaFree(p);
+            qb.cand = nullptr;
+            qb.hitA = qb.hitB = nullptr;
+            const int c = total > 2 * qb.capCand ? total : 2 * qb.capCand;
+            qb.capCand = 0;
+            if (cudaMalloc((void**)&qb.cand, sizeof(RayCand) * (size_t)c) != cudaSuccess ||
+                cudaMalloc((void**)&qb.hitA, sizeof(float4) * (size_t)c) != cudaSuccess ||
+                cudaMalloc((void**)&qb.hitB, sizeof(float4) * (size_t)c) != cudaSuccess)
+                return JBGPU_ERR_CUDA;
+            qb.capCand = c;
+        }
+        if (total > 0) {
+            RayCand* cand = (RayCand*)qb.cand;
+            k_ray_walk<false><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(w, wq, bb.sortedBody, tree, bb.wroot,
+                                                                             bb.planeList, bb.planeStart, from, to, rayWorld,
+                                                                             n, group, mask, nullptr, qb.rayOff, cand);
+            note_launch();
+            k_ray_cast<<<gridn(total, RAY_THREADS), RAY_THREADS, 0, s>>>(w, cand, total, from, to, qb.hitA, qb.hitB, qb.key);
+            note_launch();
+            k_ray_pick<<<gridn(total, 256), 256, 0, s>>>(cand, total, qb.hitA, qb.hitB, qb.key, from, to, qb.enterJ, hits);
+            note_launch();
+            k_ray_check<<<gridn(total, 256), 256, 0, s>>>(cand, total, qb.hitA, qb.hitB, qb.key, qb.enterJ, qb.undecided);
+            note_launch();
+        }
+    }
+    k_ray_finish<<<gridn(n, 256), 256, 0, s>>>(n, qb.key, qb.undecided, qb.replayAll, hits, qb.slow, qb.slowCount);
     note_launch();
     k_rays_slow<<<sms, SLOW_THREADS, 0, s>>>(w, wq, from, to, rayWorld, group, mask, hits, qb.slow, qb.slowCount);
     note_launch();
@@ -466,7 +560,9 @@ int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb,
 }
 
 void query_free(QueryBuffers& qb) {
-    void* ps[] = {qb.qmin, qb.qmax, qb.node, qb.visit, qb.slow, qb.slowCount, qb.from, qb.to, qb.rayWorld, qb.hits};
+    void* ps[] = {qb.qmin, qb.qmax, qb.node, qb.visit, qb.slow, qb.slowCount, qb.from, qb.to, qb.rayWorld, qb.hits,
+                  qb.rayCnt, qb.rayOff, qb.candTotal, qb.key, qb.enterJ, qb.undecided, qb.scanScratch, qb.cand, qb.hitA,
+                  qb.hitB};
     for (void* p : ps)
         if (p) cudaFree(p);
     qb = QueryBuffers();

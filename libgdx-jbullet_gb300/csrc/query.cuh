@@ -15,7 +15,18 @@ struct QueryBuffers {
     int capNodes = 0;
     int* slow = nullptr;          // rays the closest-hit shortcut cannot decide (replayed in body order)
     int* slowCount = nullptr;
-    int capSlow = 0;
+    int* rayCnt = nullptr;        // per ray: candidates, their offsets, the smallest hit key,
+    int* rayOff = nullptr;        // the aabb entry of that hit's object, undecided flag
+    unsigned long long* key = nullptr;
+    float* enterJ = nullptr;
+    int* undecided = nullptr;
+    void* scanScratch = nullptr;
+    int* candTotal = nullptr;
+    int capRays = 0;
+    void* cand = nullptr;         // (ray, body, aabb entry) candidates and their hits
+    float4* hitA = nullptr;
+    float4* hitB = nullptr;
+    int capCand = 0;
     int replayAll = 0;            // verification: every ray takes the in-order replay
     float* from = nullptr;        // staging for host buffers
     float* to = nullptr;
