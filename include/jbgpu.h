@@ -381,6 +381,24 @@ int jbgpu_world_enable_hinge_motor(jbgpu_world* world, int32_t id, int32_t enabl
                                    float max_motor_impulse);
 /* HingeConstraint.setAngularOnly (java:555-557): no linear rows, the axes alone are held. */
 int jbgpu_world_set_hinge_angular_only(jbgpu_world* world, int32_t id, int32_t angular_only);
+/* Generic 6-dof joint: addConstraint(new Generic6DofConstraint(rbA, rbB, frameInA, frameInB,
+ * useLinearReferenceFrameA), false) (dynamics/constraintsolver/Generic6DofConstraint.java:88-490).
+ * Frames as 12 floats (basis row-major, origin) in the bodies' centre-of-mass spaces; body_b = -1
+ * is the fixed body.  Defaults as the reference: the three linear axes locked (limits 0, 0),
+ * softness 0.7, damping 1, restitution 0.5; the angular axes free (limits -FLT_MAX, FLT_MAX), motors
+ * off with maxMotorForce 0.1, maxLimitForce 300, damping 1, limitSoftness 0.5, ERP 0.5, bounce 0. */
+int jbgpu_world_add_generic6dof(jbgpu_world* world, int32_t body_a, int32_t body_b, const float frame_a[12],
+                                const float frame_b[12], int32_t use_linear_reference_frame_a, int32_t* id);
+/* Generic6DofConstraint.setLimit(axis, lo, hi) (java:436-446): axes 0-2 linear, 3-5 angular; lo > hi
+ * frees an axis, lo == hi locks it. */
+int jbgpu_world_set_6dof_limit(jbgpu_world* world, int32_t id, int32_t axis, float lo, float hi);
+/* TranslationalLimitMotor.limitSoftness / damping / restitution (TranslationalLimitMotor.java:43-45). */
+int jbgpu_world_set_6dof_linear_motor(jbgpu_world* world, int32_t id, float softness, float damping, float restitution);
+/* RotationalLimitMotor fields of angular axis 0-2 (RotationalLimitMotor.java:44-53): enableMotor,
+ * targetVelocity, maxMotorForce, maxLimitForce, damping, limitSoftness, ERP, bounce. */
+int jbgpu_world_set_6dof_angular_motor(jbgpu_world* world, int32_t id, int32_t axis, int32_t enable,
+                                       float target_velocity, float max_motor_force, float max_limit_force,
+                                       float damping, float limit_softness, float erp, float bounce);
 /* TypedConstraint.getAppliedImpulse of every joint after the last solve; with out NULL only *n
  * is set; n > capacity is JBGPU_ERR_CAPACITY with *n set. */
 int jbgpu_world_get_joint_impulses(jbgpu_world* world, float* out, int32_t capacity, int32_t* n);

@@ -1026,13 +1026,116 @@ JBD void hinge_setup(const DevWorld& w, const DevJoints& J, int j, int a, int b)
     J.r1[j] = f4(r1, 0.0f);
     J.r2[j] = f4(r2, 0.0f);
     J.dep[j] = make_float4(depth[0], depth[1], depth[2], 0.0f);
-    float4* H = J.hs + HINGE_STEP_F4 * j;
+    float4* H = J.hs + JOINT_STEP_F4 * j;
     H[0] = f4(n[0], inv[0]);
     H[1] = f4(n[1], inv[1]);
     H[2] = f4(n[2], inv[2]);
     H[3] = f4(axisA, kHinge);
     H[4] = f4(axisB, correction);
     H[5] = make_float4(sign, 0.0f, 0.0f, 0.0f);
+}
+
+// MatrixUtil.invert (linearmath/MatrixUtil.java:362-395)
+JBD M m3_invert(const M& m) {
+    auto el = [&](int r, int c) { return coord(m.r[r], c); };
+    auto cofac = [&](int r1, int c1, int r2, int c2) {
+        return __fsub_rn(__fmul_rn(el(r1, c1), el(r2, c2)), __fmul_rn(el(r1, c2), el(r2, c1)));
+    };
+    const float co_x = cofac(1, 1, 2, 2), co_y = cofac(1, 2, 2, 0), co_z = cofac(1, 0, 2, 1);
+    const float det = __fadd_rn(__fadd_rn(__fmul_rn(el(0, 0), co_x), __fmul_rn(el(0, 1), co_y)), __fmul_rn(el(0, 2), co_z));
+    const float s = jdiv(1.0f, det);
+    M r;
+    r.r[0] = mk(__fmul_rn(co_x, s), __fmul_rn(cofac(0, 2, 2, 1), s), __fmul_rn(cofac(0, 1, 1, 2), s));
+    r.r[1] = mk(__fmul_rn(co_y, s), __fmul_rn(cofac(0, 0, 2, 2), s), __fmul_rn(cofac(0, 2, 1, 0), s));
+    r.r[2] = mk(__fmul_rn(co_z, s), __fmul_rn(cofac(0, 1, 2, 0), s), __fmul_rn(cofac(0, 0, 1, 1), s));
+    return r;
+}
+
+// Generic6DofConstraint.matrixToEulerXYZ (Generic6DofConstraint.java:125-159): element `index` is
+// row index % 3, column index / 3; atan2 and asin in double precision, rounded to float.
+JBD V euler_xyz(const M& m) {
+    auto e = [&](int index) { return coord(m.r[index % 3], index / 3); };
+    constexpr float HALF_PI = 6.283185307179586232f * 0.25f;   // BulletGlobals.SIMD_HALF_PI
+    if (e(2) < 1.0f) {
+        if (e(2) > -1.0f)
+            return mk((float)atan2((double)-e(5), (double)e(8)), (float)asin((double)e(2)),
+                      (float)atan2((double)-e(1), (double)e(0)));
+        return mk(-(float)atan2((double)e(3), (double)e(4)), -HALF_PI, 0.0f);
+    }
+    return mk((float)atan2((double)e(3), (double)e(4)), HALF_PI, 0.0f);
+}
+
+// Generic6DofConstraint.buildJacobian (java:275-323): calculateTransforms and calculateAngleInfo
+// (relative Euler angles, the three constraint axes), calcAnchorPos, the linear rows of the
+// limited axes (JacobianEntry.init with the port's zero B-side angular part), the limit state of
+// each angular axis (RotationalLimitMotor.testLimitValue) and the rows of the axes whose motor or
+// limit applies; accumulated impulses cleared.
+JBD void d6_setup(const DevWorld& w, const DevJoints& J, int j, int a, int b) {
+    const float4* F = J.frame + 6 * j;
+    const float4* S = J.d6set + D6_SET_F4 * j;
+    const Xf xa = joint_xf(w, a), xb = joint_xf(w, b);
+    const float4 la = w.iloc[a], lb = b >= 0 ? w.iloc[b] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const V iA = mk(la.x, la.y, la.z), iB = mk(lb.x, lb.y, lb.z);
+    Xf fa, fb;
+    fa.b.r[0] = mk4(F[0]); fa.b.r[1] = mk4(F[1]); fa.b.r[2] = mk4(F[2]); fa.o = mk4(J.pivA[j]);
+    fb.b.r[0] = mk4(F[3]); fb.b.r[1] = mk4(F[4]); fb.b.r[2] = mk4(F[5]); fb.o = mk4(J.pivB[j]);
+    const Xf ca = xf_mul(xa, fa), cb = xf_mul(xb, fb);
+    const V diff = euler_xyz(mulMM(m3_invert(ca.b), cb.b));
+    V ax[3];
+    {
+        const V c0 = mk(cb.b.r[0].x, cb.b.r[1].x, cb.b.r[2].x), c2 = mk(ca.b.r[0].z, ca.b.r[1].z, ca.b.r[2].z);
+        ax[1] = crs(c2, c0);
+        ax[0] = crs(ax[1], c2);
+        ax[2] = crs(c0, ax[1]);
+    }
+    const float imA = la.w, imB = lb.w;
+    const float weight = imB == 0.0f ? 1.0f : jdiv(imA, __fadd_rn(imA, imB));
+    const V anchor = add(scl(ca.o, weight), scl(cb.o, __fsub_rn(1.0f, weight)));
+    const V r1 = sub(anchor, xa.o), r2 = sub(anchor, xb.o);
+    const M w2A = transpose(xa.b), w2B = transpose(xb.b);
+    const bool useA = S[0].w != 0.0f;
+    const V lower = mk4(S[0]), upper = mk4(S[1]);
+    float4* H = J.hs + JOINT_STEP_F4 * j;
+    for (int i = 0; i < 3; i++) {
+        float inv = 0.0f;
+        const V n = useA ? mk(coord(ca.b.r[0], i), coord(ca.b.r[1], i), coord(ca.b.r[2], i))
+                         : mk(coord(cb.b.r[0], i), coord(cb.b.r[1], i), coord(cb.b.r[2], i));
+        if (coord(upper, i) >= coord(lower, i)) {
+            const V aJ = mulMv(crs(r1, n), w2A);
+            const V bJ = mulMv(crs(r2, r2), w2B);
+            const V m0 = mulc(iA, aJ), m1 = mulc(iB, bJ);
+            inv = jdiv(1.0f, __fadd_rn(__fadd_rn(__fadd_rn(la.w, dot(m0, aJ)), lb.w), dot(m1, bJ)));
+        }
+        H[3 + i] = f4(n, inv);
+    }
+    float lim[3], err[3];
+    for (int i = 0; i < 3; i++) {
+        const float4 s0 = S[3 + 3 * i], s2 = S[5 + 3 * i];
+        const float v = coord(diff, i);
+        lim[i] = 0.0f;
+        err[i] = 0.0f;
+        if (!(s0.x > s0.y)) {                                     // testLimitValue
+            if (v < s0.x) { lim[i] = 1.0f; err[i] = __fsub_rn(v, s0.x); }
+            else if (v > s0.y) { lim[i] = 2.0f; err[i] = __fsub_rn(v, s0.y); }
+        }
+        float inv = 0.0f;
+        if (lim[i] != 0.0f || s2.y != 0.0f) {                     // needApplyTorques
+            const V aJ = mulMv(ax[i], w2A);
+            const V bJ = mulMv(scl(ax[i], -1.0f), w2B);
+            const V m0 = mulc(iA, aJ), m1 = mulc(iB, bJ);
+            inv = jdiv(1.0f, __fadd_rn(dot(m0, aJ), dot(m1, bJ)));
+        }
+        H[6 + i] = f4(ax[i], inv);
+    }
+    H[0] = f4(ca.o, 0.0f);
+    H[1] = f4(cb.o, 0.0f);
+    H[2] = f4(anchor, 0.0f);
+    H[9] = make_float4(lim[0], err[0], lim[1], err[1]);
+    H[10] = make_float4(lim[2], err[2], 0.0f, 0.0f);
+    H[11] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    H[12] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    J.r1[j] = f4(r1, 0.0f);
+    J.r2[j] = f4(r2, 0.0f);
 }
 
 __global__ void k_joint_setup(DevWorld w, SolverBuffers sb) {
@@ -1048,6 +1151,10 @@ __global__ void k_joint_setup(DevWorld w, SolverBuffers sb) {
     J.imp[j] = 0.0f;
     if ((J.kind[j] & JK_TYPE) == JOINT_HINGE) {
         hinge_setup(w, J, j, a, b);
+        return;
+    }
+    if ((J.kind[j] & JK_TYPE) == JOINT_6DOF) {
+        d6_setup(w, J, j, a, b);
         return;
     }
     const Xf xa = joint_xf(w, a), xb = joint_xf(w, b);
@@ -1139,7 +1246,7 @@ JBD void hinge_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
     if (b >= 0) gload(w, b, vB, wB);
     const float imA = w.iloc[a].w, imB = b >= 0 ? w.iloc[b].w : 0.0f;
     const M IA = load_iw(w, a), IB = joint_iw(w, b);
-    const float4* H = J.hs + HINGE_STEP_F4 * j;
+    const float4* H = J.hs + JOINT_STEP_F4 * j;
     float acc = __ldcg(J.imp + j);
     if (!(kind & JK_ANGULAR_ONLY)) {
         const float4 q1 = J.r1[j], q2 = J.r2[j], dp = J.dep[j];
@@ -1202,9 +1309,89 @@ JBD void hinge_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
     if (imA != 0.0f) gstore(w, a, vA, wA);
     if (b >= 0 && imB != 0.0f) gstore(w, b, vB, wB);
     __stcg(J.imp + j, acc);
-    __stcg(&J.hs[HINGE_STEP_F4 * j + 5].y, accLimit);
+    __stcg(&J.hs[JOINT_STEP_F4 * j + 5].y, accLimit);
 }
 
+
+// Generic6DofConstraint.solveConstraint (java:325-365): TranslationalLimitMotor.solveLinearAxis
+// (TranslationalLimitMotor.java:70-150) per limited linear axis, on the velocities as the earlier
+// axes left them, then RotationalLimitMotor.solveAngularLimits (RotationalLimitMotor.java:135-203)
+// per angular axis whose limit or motor applies.
+JBD void d6_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
+    const int a = J.a[j], b = J.b[j];
+    V vA, wA, vB = mk(0.0f, 0.0f, 0.0f), wB = mk(0.0f, 0.0f, 0.0f);
+    gload(w, a, vA, wA);
+    if (b >= 0) gload(w, b, vB, wB);
+    const float imA = w.iloc[a].w, imB = b >= 0 ? w.iloc[b].w : 0.0f;
+    const M IA = load_iw(w, a), IB = joint_iw(w, b);
+    const float4* S = J.d6set + D6_SET_F4 * j;
+    float4* H = J.hs + JOINT_STEP_F4 * j;
+    const V pA = mk4(H[0]), pB = mk4(H[1]);
+    const float4 q1 = J.r1[j], q2 = J.r2[j];
+    const V r1 = mk(q1.x, q1.y, q1.z), r2 = mk(q2.x, q2.y, q2.z);
+    const V lower = mk4(S[0]), upper = mk4(S[1]);
+    const float softness = S[1].w, damping = S[2].x, restitution = S[2].y;
+    float4 accL = __ldcg(H + 11), accA = __ldcg(H + 12);
+    for (int i = 0; i < 3; i++) {
+        if (!(coord(upper, i) >= coord(lower, i))) continue;
+        const float4 h = H[3 + i];
+        const V axis = mk(h.x, h.y, h.z);
+        const V vel = sub(add(crs(wA, r1), vA), add(crs(wB, r2), vB));
+        const float relVel = dot(axis, vel);
+        float depth = -dot(sub(pA, pB), axis);
+        float lo = -1e30f, hi = 1e30f;
+        const float minLimit = coord(lower, i), maxLimit = coord(upper, i);
+        if (minLimit < maxLimit) {
+            if (depth > maxLimit) { depth = __fsub_rn(depth, maxLimit); lo = 0.0f; }
+            else if (depth < minLimit) { depth = __fsub_rn(depth, minLimit); hi = 0.0f; }
+            else continue;
+        }
+        float ni = __fmul_rn(__fmul_rn(softness, __fsub_rn(jdiv(__fmul_rn(restitution, depth), dt), __fmul_rn(damping, relVel))),
+                             h.w);
+        const float old = i == 0 ? accL.x : (i == 1 ? accL.y : accL.z);
+        const float sum = __fadd_rn(old, ni);
+        const float acc = sum > hi ? 0.0f : (sum < lo ? 0.0f : sum);
+        if (i == 0) accL.x = acc; else if (i == 1) accL.y = acc; else accL.z = acc;
+        ni = __fsub_rn(acc, old);
+        const V iv = scl(axis, ni);
+        body_impulse(vA, wA, imA, IA, iv, r1);
+        body_impulse(vB, wB, imB, IB, scl(iv, -1.0f), r2);
+    }
+    const float4 l01 = H[9], l2 = H[10];
+    for (int i = 0; i < 3; i++) {
+        const float4 s0 = S[3 + 3 * i], s1 = S[4 + 3 * i], s2 = S[5 + 3 * i];
+        const float lim = i == 0 ? l01.x : (i == 1 ? l01.z : l2.x);
+        const float err = i == 0 ? l01.y : (i == 1 ? l01.w : l2.y);
+        if (lim == 0.0f && s2.y == 0.0f) continue;                // needApplyTorques
+        const float4 h = H[6 + i];
+        const V axis = mk(h.x, h.y, h.z);
+        float target = s0.z, maxForce = s0.w;
+        if (lim != 0.0f) {
+            target = jdiv(__fmul_rn(-s1.w, err), dt);
+            maxForce = s1.x;
+        }
+        maxForce = __fmul_rn(maxForce, dt);
+        const float relVel = dot(axis, sub(wA, wB));
+        const float mrv = __fmul_rn(s1.z, __fsub_rn(target, __fmul_rn(s1.y, relVel)));
+        if (mrv < FLT_EPS && mrv > -FLT_EPS) continue;
+        const float unclipped = __fmul_rn(__fmul_rn(__fadd_rn(1.0f, s2.x), mrv), h.w);
+        float clipped;
+        if (unclipped > 0.0f) clipped = unclipped > maxForce ? maxForce : unclipped;
+        else clipped = unclipped < -maxForce ? -maxForce : unclipped;
+        const float old = i == 0 ? accA.x : (i == 1 ? accA.y : accA.z);
+        const float sum = __fadd_rn(old, clipped);
+        const float acc = sum > 1e30f ? 0.0f : (sum < -1e30f ? 0.0f : sum);
+        if (i == 0) accA.x = acc; else if (i == 1) accA.y = acc; else accA.z = acc;
+        clipped = __fsub_rn(acc, old);
+        const V mi = scl(axis, clipped);
+        torque_impulse(wA, imA, IA, mi);
+        torque_impulse(wB, imB, IB, scl(mi, -1.0f));
+    }
+    if (imA != 0.0f) gstore(w, a, vA, wA);
+    if (b >= 0 && imB != 0.0f) gstore(w, b, vB, wB);
+    __stcg(H + 11, accL);
+    __stcg(H + 12, accA);
+}
 
 // write-back (java:901-912): appliedImpulse; appliedImpulseLateral1 ends as friction row 2's
 JBD void writeback_slot(const DevPairs& P, const DevRows& R, int s) {
@@ -1448,7 +1635,9 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                     for (int q = j0 + spread; q < j1; q += nth) {
                         const int j = sb.J.order[q];
                         if (!sb.J.act[j]) continue;
-                        if ((sb.J.kind[j] & JK_TYPE) == JOINT_HINGE) hinge_solve(w, sb.J, j, dt);
+                        const int jt = sb.J.kind[j] & JK_TYPE;
+                        if (jt == JOINT_HINGE) hinge_solve(w, sb.J, j, dt);
+                        else if (jt == JOINT_6DOF) d6_solve(w, sb.J, j, dt);
                         else joint_solve(w, sb.J, j, dt);
                     }
                     grid_barrier(w.ctr, nb, barK);

@@ -19,10 +19,12 @@ constexpr int PART_MAX_BODIES = 2048; // bodies of one part (velocities staged i
 // change.
 constexpr int JOINT_P2P = 0;
 constexpr int JOINT_HINGE = 1;
+constexpr int JOINT_6DOF = 2;
 constexpr int JK_TYPE = 0xff;         // kind: type in the low byte, hinge switches above it
 constexpr int JK_ANGULAR_ONLY = 1 << 8;
 constexpr int JK_MOTOR = 1 << 9;
-constexpr int HINGE_STEP_F4 = 6;      // float4s of a hinge's per-step state
+constexpr int JOINT_STEP_F4 = 13;     // float4s of a hinge's or 6-dof joint's per-step state
+constexpr int D6_SET_F4 = 12;         // float4s of a 6-dof joint's settings
 struct DevJoints {
     int n = 0;                    // joints
     int nCol = 0;                 // colours: first fit in index order over the joints' dynamic bodies
@@ -34,9 +36,16 @@ struct DevJoints {
     float4* set = nullptr;        // p2p: tau, damping, impulse clamp; hinge: lower, upper limit, softness, bias
     float4* set2 = nullptr;       // hinge: relaxation factor, motor target velocity, max motor impulse
     float4* frame = nullptr;      // hinge: rbAFrame basis rows (3), then rbBFrame basis rows (3)
-    float4* hs = nullptr;         // hinge per step (HINGE_STEP_F4 each): axis n_i with 1/Adiag_i (3),
+    float4* hs = nullptr;         // per step (JOINT_STEP_F4 each).  Hinge: axis n_i with 1/Adiag_i (3),
                                   // world hinge axis of A with kHinge, of B with the limit correction,
-                                  // (limit sign, accumulated limit impulse, 0, 0)
+                                  // (limit sign, accumulated limit impulse, 0, 0).  6-dof: the two
+                                  // calculated frame origins, the anchor, linear axes with 1/Adiag
+                                  // (3), angular axes with 1/Adiag (3), (limit state, limit error)
+                                  // per angular axis (2), accumulated linear and angular impulses
+    float4* d6set = nullptr;      // 6-dof settings (D6_SET_F4 each): linear lower xyz | use frame A,
+                                  // upper xyz | softness, (damping, restitution), then per angular axis
+                                  // (lo, hi, target velocity, max motor force), (max limit force,
+                                  // damping, softness, ERP), (bounce, motor enabled)
     int* order = nullptr;         // joints by (colour, index)
     int* colStart = nullptr;      // nCol + 1 offsets into order
     float4* r1 = nullptr;         // per step: pivot A - centre of A, 1/Adiag of axis 0 in .w

@@ -97,6 +97,7 @@ struct jbgpu_world {
     // point-to-point joints (host copy; uploaded to sb.J when they change)
     std::vector<int> jKind, jA, jB;
     std::vector<float4> jPivA, jPivB, jSet, jSet2, jFrame;   // jFrame: 6 per joint
+    std::vector<float4> jD6;                                  // D6_SET_F4 per joint
     bool jointsDirty = false;
     int capJoints = 0;
     bool orderValid = false;        // the broadphase leaf order covers every body added
@@ -492,10 +493,11 @@ int sync_joints(jbgpu_world* w) {
     if (n > w->capJoints) {
         dfree(J.a); dfree(J.b); dfree(J.pivA); dfree(J.pivB); dfree(J.set); dfree(J.order); dfree(J.colStart);
         dfree(J.r1); dfree(J.r2); dfree(J.dep); dfree(J.imp); dfree(J.act);
-        dfree(J.kind); dfree(J.set2); dfree(J.frame); dfree(J.hs);
+        dfree(J.kind); dfree(J.set2); dfree(J.frame); dfree(J.hs); dfree(J.d6set);
         const int c = std::max(n, 2 * w->capJoints);
         CK(dalloc(&J.a, c)); CK(dalloc(&J.b, c)); CK(dalloc(&J.pivA, c)); CK(dalloc(&J.pivB, c)); CK(dalloc(&J.set, c));
-        CK(dalloc(&J.kind, c)); CK(dalloc(&J.set2, c)); CK(dalloc(&J.frame, 6 * c)); CK(dalloc(&J.hs, HINGE_STEP_F4 * c));
+        CK(dalloc(&J.kind, c)); CK(dalloc(&J.set2, c)); CK(dalloc(&J.frame, 6 * c)); CK(dalloc(&J.hs, JOINT_STEP_F4 * c));
+        CK(dalloc(&J.d6set, D6_SET_F4 * (size_t)c));
         CK(dalloc(&J.order, c)); CK(dalloc(&J.colStart, c + 1)); CK(dalloc(&J.r1, c)); CK(dalloc(&J.r2, c));
         CK(dalloc(&J.dep, c)); CK(dalloc(&J.imp, c)); CK(dalloc(&J.act, c));
         CK(cudaMemset(J.imp, 0, sizeof(float) * c));
@@ -532,6 +534,7 @@ int sync_joints(jbgpu_world* w) {
     CK(cudaMemcpyAsync(J.kind, w->jKind.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(J.set2, w->jSet2.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(J.frame, w->jFrame.data(), sizeof(float4) * 6 * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(J.d6set, w->jD6.data(), sizeof(float4) * D6_SET_F4 * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(J.order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(J.colStart, colStart.data(), sizeof(int) * (nCol + 1), cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
@@ -983,7 +986,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
         DevJoints& J = V.J;
         dfree(J.a); dfree(J.b); dfree(J.pivA); dfree(J.pivB); dfree(J.set); dfree(J.order); dfree(J.colStart);
         dfree(J.r1); dfree(J.r2); dfree(J.dep); dfree(J.imp); dfree(J.act);
-        dfree(J.kind); dfree(J.set2); dfree(J.frame); dfree(J.hs);
+        dfree(J.kind); dfree(J.set2); dfree(J.frame); dfree(J.hs); dfree(J.d6set);
     }
     dfree(V.nIslChunks);
     if (V.islScratch) cudaFree(V.islScratch);
@@ -1295,6 +1298,7 @@ int jbgpu_world_add_point2point(jbgpu_world* w, int32_t a, int32_t b, const floa
     w->jSet.push_back(make_float4(0.3f, 1.0f, 0.0f, 0.0f));   // ConstraintSetting defaults
     w->jSet2.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     for (int r = 0; r < 6; r++) w->jFrame.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (int r = 0; r < D6_SET_F4; r++) w->jD6.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     w->jointsDirty = true;
     if (id) *id = (int32_t)w->jA.size() - 1;
     return JBGPU_OK;
@@ -1321,8 +1325,80 @@ int jbgpu_world_add_hinge(jbgpu_world* w, int32_t a, int32_t b, const float fa[1
     w->jSet2.push_back(make_float4(1.0f, 0.0f, 0.0f, 0.0f));     // relaxation, motor target, max motor impulse
     for (const float* f : {fa, fb})
         for (int r = 0; r < 3; r++) w->jFrame.push_back(make_float4(f[r * 3], f[r * 3 + 1], f[r * 3 + 2], 0.0f));
+    for (int r = 0; r < D6_SET_F4; r++) w->jD6.push_back(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     w->jointsDirty = true;
     if (id) *id = (int32_t)w->jA.size() - 1;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_add_generic6dof(jbgpu_world* w, int32_t a, int32_t b, const float fa[12], const float fb[12],
+                                int32_t useLinearReferenceFrameA, int32_t* id) {
+    int32_t k = -1;
+    int rc = jbgpu_world_add_hinge(w, a, b, fa, fb, &k);
+    if (rc) return rc;
+    w->jKind[k] = JOINT_6DOF;
+    w->jSet[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    w->jSet2[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4* d = &w->jD6[(size_t)k * D6_SET_F4];
+    d[0] = make_float4(0.0f, 0.0f, 0.0f, useLinearReferenceFrameA ? 1.0f : 0.0f);   // TranslationalLimitMotor:
+    d[1] = make_float4(0.0f, 0.0f, 0.0f, 0.7f);                                      // limits 0 (locked), softness,
+    d[2] = make_float4(1.0f, 0.5f, 0.0f, 0.0f);                                      // damping, restitution
+    for (int i = 0; i < 3; i++) {                                                     // RotationalLimitMotor defaults
+        d[3 + 3 * i] = make_float4(-3.40282347e+38f, 3.40282347e+38f, 0.0f, 0.1f);
+        d[4 + 3 * i] = make_float4(300.0f, 1.0f, 0.5f, 0.5f);
+        d[5 + 3 * i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    if (id) *id = k;
+    return JBGPU_OK;
+}
+
+static int d6_id(jbgpu_world* w, int32_t id) {
+    if (!w || id < 0 || id >= (int)w->jA.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
+    if ((w->jKind[id] & JK_TYPE) != JOINT_6DOF) return fail(JBGPU_ERR_INVALID_ARGUMENT, "not a generic 6-dof joint");
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_6dof_limit(jbgpu_world* w, int32_t id, int32_t axis, float lo, float hi) {
+    int rc = d6_id(w, id);
+    if (rc) return rc;
+    if (axis < 0 || axis > 5) return fail(JBGPU_ERR_INVALID_ARGUMENT, "axis 0..5");
+    float4* d = &w->jD6[(size_t)id * D6_SET_F4];
+    if (axis < 3) {
+        float* lo3 = &d[0].x;
+        float* hi3 = &d[1].x;
+        lo3[axis] = lo;
+        hi3[axis] = hi;
+    } else {
+        d[3 + 3 * (axis - 3)].x = lo;
+        d[3 + 3 * (axis - 3)].y = hi;
+    }
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_6dof_linear_motor(jbgpu_world* w, int32_t id, float softness, float damping, float restitution) {
+    int rc = d6_id(w, id);
+    if (rc) return rc;
+    float4* d = &w->jD6[(size_t)id * D6_SET_F4];
+    d[1].w = softness;
+    d[2].x = damping;
+    d[2].y = restitution;
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_6dof_angular_motor(jbgpu_world* w, int32_t id, int32_t axis, int32_t enable, float targetVelocity,
+                                       float maxMotorForce, float maxLimitForce, float damping, float softness, float erp,
+                                       float bounce) {
+    int rc = d6_id(w, id);
+    if (rc) return rc;
+    if (axis < 0 || axis > 2) return fail(JBGPU_ERR_INVALID_ARGUMENT, "angular axis 0..2");
+    float4* d = &w->jD6[(size_t)id * D6_SET_F4 + 3 + 3 * axis];
+    d[0].z = targetVelocity;
+    d[0].w = maxMotorForce;
+    d[1] = make_float4(maxLimitForce, damping, softness, erp);
+    d[2] = make_float4(bounce, enable ? 1.0f : 0.0f, 0.0f, 0.0f);
+    w->jointsDirty = true;
     return JBGPU_OK;
 }
 

@@ -330,6 +330,106 @@ class HingeConstraint:
         return float(self._world._g.joint_impulses()[self._id])
 
 
+class RotationalLimitMotor:
+    """dynamics/constraintsolver/RotationalLimitMotor.java:44-70 (settings; defaults as there)."""
+
+    def __init__(self):
+        self.loLimit, self.hiLimit = -3.40282347e+38, 3.40282347e+38
+        self.targetVelocity, self.maxMotorForce, self.maxLimitForce = 0.0, 0.1, 300.0
+        self.damping, self.limitSoftness, self.ERP, self.bounce = 1.0, 0.5, 0.5, 0.0
+        self.enableMotor = False
+
+
+class TranslationalLimitMotor:
+    """dynamics/constraintsolver/TranslationalLimitMotor.java:38-56 (settings; defaults as there)."""
+
+    def __init__(self):
+        self.lowerLimit = np.zeros(3, np.float32)
+        self.upperLimit = np.zeros(3, np.float32)
+        self.limitSoftness, self.damping, self.restitution = 0.7, 1.0, 0.5
+
+
+class Generic6DofConstraint:
+    """dynamics/constraintsolver/Generic6DofConstraint.java:88-490: Generic6DofConstraint(rbA, rbB,
+    frameInA, frameInB, useLinearReferenceFrameA) with its limit motors; settings changed after
+    the constraint entered the world are sent before the next step."""
+
+    def __init__(self, rbA, rbB, frameInA, frameInB, useLinearReferenceFrameA):
+        self.rbA, self.rbB = rbA, rbB
+        self.frameInA = Transform(frameInA.basis.copy(), frameInA.origin.copy())
+        self.frameInB = Transform(frameInB.basis.copy(), frameInB.origin.copy())
+        self.useLinearReferenceFrameA = bool(useLinearReferenceFrameA)
+        self.linearLimits = TranslationalLimitMotor()
+        self.angularLimits = [RotationalLimitMotor() for _ in range(3)]
+        self._world = None
+        self._id = None
+        self._sent = None
+
+    def setLimit(self, axis, lo, hi):
+        if axis < 3:
+            self.linearLimits.lowerLimit[axis], self.linearLimits.upperLimit[axis] = lo, hi
+        else:
+            self.angularLimits[axis - 3].loLimit, self.angularLimits[axis - 3].hiLimit = float(lo), float(hi)
+
+    def setLinearLowerLimit(self, v):
+        self.linearLimits.lowerLimit[:] = v
+
+    def setLinearUpperLimit(self, v):
+        self.linearLimits.upperLimit[:] = v
+
+    def setAngularLowerLimit(self, v):
+        for i in range(3):
+            self.angularLimits[i].loLimit = float(v[i])
+
+    def setAngularUpperLimit(self, v):
+        for i in range(3):
+            self.angularLimits[i].hiLimit = float(v[i])
+
+    def getRotationalLimitMotor(self, index):
+        return self.angularLimits[index]
+
+    def getTranslationalLimitMotor(self):
+        return self.linearLimits
+
+    def getRigidBodyA(self):
+        return self.rbA
+
+    def getRigidBodyB(self):
+        return self.rbB
+
+    def getFrameOffsetA(self):
+        return Transform(self.frameInA.basis.copy(), self.frameInA.origin.copy())
+
+    def getFrameOffsetB(self):
+        return Transform(self.frameInB.basis.copy(), self.frameInB.origin.copy())
+
+    def _settings(self):
+        L = self.linearLimits
+        return (tuple(L.lowerLimit.tolist()), tuple(L.upperLimit.tolist()), L.limitSoftness, L.damping, L.restitution,
+                tuple((m.loLimit, m.hiLimit, m.enableMotor, m.targetVelocity, m.maxMotorForce, m.maxLimitForce, m.damping,
+                       m.limitSoftness, m.ERP, m.bounce) for m in self.angularLimits))
+
+    def _push(self):
+        g = self._world._g if self._world is not None else None
+        if g is None or self._id is None:
+            return
+        st = self._settings()
+        if st == self._sent:
+            return
+        L = self.linearLimits
+        for i in range(3):
+            g.set_6dof_limit(self._id, i, float(L.lowerLimit[i]), float(L.upperLimit[i]))
+        g.set_6dof_linear_motor(self._id, L.limitSoftness, L.damping, L.restitution)
+        for i, m in enumerate(self.angularLimits):
+            g.set_6dof_limit(self._id, 3 + i, m.loLimit, m.hiLimit)
+            g.set_6dof_angular_motor(self._id, i, m.enableMotor, m.targetVelocity, m.maxMotorForce, m.maxLimitForce,
+                                     m.damping, m.limitSoftness, m.ERP, m.bounce)
+        self._sent = st
+
+    def getAppliedImpulse(self):
+        return 0.0    # the reference's 6-dof joint leaves TypedConstraint.appliedImpulse at 0
+
+
 class ClosestRayResultCallback:
     """CollisionWorld.ClosestRayResultCallback (collision/dispatch/CollisionWorld.java:697-729)."""
 
@@ -420,6 +520,11 @@ class DiscreteDynamicsWorld:
                 c._id = self._g.add_hinge(c.rbA._index, b, c.frameA.as12(), c.frameB.as12())
                 c._push()
                 continue
+            if isinstance(c, Generic6DofConstraint):
+                c._id = self._g.add_generic6dof(c.rbA._index, b, c.frameInA.as12(), c.frameInB.as12(),
+                                                c.useLinearReferenceFrameA)
+                c._push()
+                continue
             c._id = self._g.add_point2point(c.rbA._index, b, c.pivotInA, c.pivotInB)
             st = c.setting
             self._g.set_joint_setting(c._id, st.tau, st.damping, st.impulseClamp)
@@ -478,6 +583,9 @@ class DiscreteDynamicsWorld:
 
     def stepSimulation(self, timeStep, maxSubSteps=1, fixedTimeStep=1.0 / 60.0):
         g = self._ensure()
+        for c in self._constraints:
+            if isinstance(c, Generic6DofConstraint):
+                c._push()
         if self._forces is not None:
             g.apply_forces(self._forces)
             self._forces = None

@@ -65,6 +65,12 @@ def lib():
             "jbgpu_world_set_ray_replay": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_set_graph": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_graph_status": ([C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_char_p)], C.c_int),
+            "jbgpu_world_add_generic6dof": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.c_int32,
+                                            C.POINTER(C.c_int32)], C.c_int),
+            "jbgpu_world_set_6dof_limit": ([C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float], C.c_int),
+            "jbgpu_world_set_6dof_linear_motor": ([C.c_void_p, C.c_int32] + [C.c_float] * 3, C.c_int),
+            "jbgpu_world_set_6dof_angular_motor": ([C.c_void_p, C.c_int32, C.c_int32, C.c_int32] + [C.c_float] * 7,
+                                                   C.c_int),
             "jbgpu_world_add_hinge": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.POINTER(C.c_int32)],
                                       C.c_int),
             "jbgpu_world_set_hinge_limit": ([C.c_void_p, C.c_int32] + [C.c_float] * 5, C.c_int),
@@ -104,7 +110,8 @@ EXPORTED = [
     "jbgpu_world_profile_counters", "jbgpu_world_timer", "jbgpu_world_add_point2point", "jbgpu_world_set_joint_setting",
     "jbgpu_world_get_joint_impulses", "jbgpu_world_add_hinge", "jbgpu_world_set_hinge_limit",
     "jbgpu_world_enable_hinge_motor", "jbgpu_world_set_hinge_angular_only", "jbgpu_world_ray_test",
-    "jbgpu_world_set_ray_replay", "jbgpu_world_set_graph", "jbgpu_world_graph_status",
+    "jbgpu_world_set_ray_replay", "jbgpu_world_set_graph", "jbgpu_world_graph_status", "jbgpu_world_add_generic6dof",
+    "jbgpu_world_set_6dof_limit", "jbgpu_world_set_6dof_linear_motor", "jbgpu_world_set_6dof_angular_motor",
 ]
 
 
@@ -283,8 +290,37 @@ class GpuWorld:
     def set_ray_replay(self, all_rays):
         check(lib().jbgpu_world_set_ray_replay(self.h, 1 if all_rays else 0))
 
+    def add_generic6dof(self, a, b, frame_a, frame_b, use_linear_reference_frame_a=True):
+        """Generic 6-dof joint with frames as 12 floats each (basis row-major, origin); returns its id."""
+        fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
+        fb = np.ascontiguousarray(frame_b, np.float32).reshape(12)
+        jid = C.c_int32()
+        check(lib().jbgpu_world_add_generic6dof(self.h, a, b, fa.ctypes.data_as(_abi.f32p), fb.ctypes.data_as(_abi.f32p),
+                                                1 if use_linear_reference_frame_a else 0, C.byref(jid)))
+        return jid.value
+
+    def set_6dof_limit(self, jid, axis, lo, hi):
+        check(lib().jbgpu_world_set_6dof_limit(self.h, jid, axis, lo, hi))
+
+    def set_6dof_linear_motor(self, jid, softness, damping, restitution):
+        check(lib().jbgpu_world_set_6dof_linear_motor(self.h, jid, softness, damping, restitution))
+
+    def set_6dof_angular_motor(self, jid, axis, enable, target_velocity, max_motor_force, max_limit_force=300.0,
+                               damping=1.0, softness=0.5, erp=0.5, bounce=0.0):
+        check(lib().jbgpu_world_set_6dof_angular_motor(self.h, jid, axis, 1 if enable else 0, target_velocity,
+                                                       max_motor_force, max_limit_force, damping, softness, erp, bounce))
+
     def add_scene_joints(self, scene):
         for j in scene.meta.get("joints", []):
+            if j.get("type") == "6dof":
+                jid = self.add_generic6dof(j["a"], j["b"], j["frame_a"], j["frame_b"], j.get("use_a", True))
+                for axis, lo, hi in j.get("limits", []):
+                    self.set_6dof_limit(jid, axis, lo, hi)
+                if "linear_motor" in j:
+                    self.set_6dof_linear_motor(jid, *j["linear_motor"])
+                for m in j.get("angular_motors", []):
+                    self.set_6dof_angular_motor(jid, *m)
+                continue
             if j.get("type") == "hinge":
                 jid = self.add_hinge(j["a"], j["b"], j["frame_a"], j["frame_b"])
                 if "limit" in j:

@@ -452,6 +452,82 @@ def hinged_chains(chains=6, links=6, loose=16, seed=0, spacing=2.5, top=10.0, st
                  meta={"seed": seed, "joints": joints}, **kw)
 
 
+def sixdof_chains(chains=4, links=5, loose=8, seed=0, spacing=2.5, top=10.0, steps=240, worlds=1):
+    """Chains of boxes (half-extents 0.15 x 0.45 x 0.15) joined end to end by generic 6-dof joints,
+    the top link jointed to a static anchor box.  Per chain c: c % 4 == 0 angular limits of
+    +-0.4 rad on all three axes; 1 rotation about x only (the other two angular axes locked);
+    2 a linear axis free within +-0.3, softer linear rows, a motor on angular axis 0 and limits on
+    the others; 3 frames of B as the linear reference, limits with bounce and a motor on axis 2.
+    Loose boxes fall on them.  meta["joints"]: type "6dof", a, b, frame_a, frame_b, use_a, limits
+    [(axis, lo, hi)], optional linear_motor, angular_motors."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE), {"type": _abi.SHAPE_BOX, "params": (0.15, 0.45, 0.15, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.3, 0.3, 0.3, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.2, 0.2, 0.2, 0.0), "points": None}]
+    side = int(np.ceil(np.sqrt(chains)))
+    ident = np.eye(3, dtype=F).reshape(9)
+
+    def frame(origin):
+        return np.concatenate([ident, np.asarray(origin, F)]).astype(F)
+    all_bodies, joints, wid = [], [], []
+    base = 0
+    for wi in range(worlds):
+        plane = _plane_body(0)
+        anchors = _bodies(chains)
+        anchors["shape"] = 3
+        lb = _bodies(chains * links)
+        lb["shape"] = 1
+        lb["mass"] = 1.0
+        lb["local_inertia"] = box_inertia(1.0, (0.15, 0.45, 0.15))
+        for c in range(chains):
+            x0, z0 = (c % side - (side - 1) / 2.0) * spacing, (c // side - (side - 1) / 2.0) * spacing
+            anchors["transform"][c, 9:] = (x0, top + 0.2, z0)
+            v = rng.normal(0.0, 1.5, 2)
+            for i in range(links):
+                k = c * links + i
+                lb["transform"][k, 9:] = (x0, top - 0.5 - 1.0 * i, z0)
+                lb["linear_velocity"][k] = (v[0] * (i + 1) / links, 0.0, v[1] * (i + 1) / links)
+        half = side * spacing / 2.0
+        fb = _bodies(loose)
+        fb["shape"] = 2
+        fb["mass"] = 2.0
+        fb["local_inertia"] = box_inertia(2.0, (0.3, 0.3, 0.3))
+        fpos = np.stack([rng.uniform(-half, half, loose), rng.uniform(top + 1.0, top + 6.0, loose),
+                         rng.uniform(-half, half, loose)], 1)
+        _set_transforms(fb, random_rotations(rng, loose), fpos)
+        bodies = np.concatenate([plane, anchors, lb, fb])
+        first_anchor, first_link = base + 1, base + 1 + chains
+        for c in range(chains):
+            kind = c % 4
+            cfg = {"type": "6dof", "use_a": kind != 3, "limits": []}
+            if kind == 0:
+                cfg["limits"] = [(3, -0.4, 0.4), (4, -0.4, 0.4), (5, -0.4, 0.4)]
+            elif kind == 1:
+                cfg["limits"] = [(3, 1.0, -1.0), (4, 0.0, 0.0), (5, 0.0, 0.0)]
+            elif kind == 2:
+                cfg["limits"] = [(0, -0.3, 0.3), (4, -0.2, 0.2), (5, -0.2, 0.2)]
+                cfg["linear_motor"] = (0.8, 1.0, 0.3)
+                cfg["angular_motors"] = [(0, True, 0.5, 0.2)]
+            else:
+                cfg["limits"] = [(3, -0.3, 0.3), (4, -0.3, 0.3), (5, -0.3, 0.3)]
+                cfg["angular_motors"] = [(2, True, -0.5, 1.0, 300.0, 1.0, 0.5, 0.3, 0.2)]
+            a0 = first_link + c * links
+            joints.append(dict(cfg, a=a0, b=first_anchor + c, frame_a=frame((0.0, 0.5, 0.0)),
+                               frame_b=frame((0.0, -0.2, 0.0))))
+            for i in range(links - 1):
+                joints.append(dict(cfg, a=a0 + i, b=a0 + i + 1, frame_a=frame((0.0, -0.5, 0.0)),
+                                   frame_b=frame((0.0, 0.5, 0.0))))
+        all_bodies.append(bodies)
+        wid.append(np.full(len(bodies), wi, np.int32))
+        base += len(bodies)
+    bodies = np.concatenate(all_bodies)
+    bodies["world"] = np.concatenate(wid)
+    kw = {"world_of_body": np.concatenate(wid)} if worlds > 1 else {}
+    return Scene("sixdof_chains_%dx%d_w%d" % (chains, links, worlds), 1.0 / 60.0, steps,
+                 {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10}, shapes, bodies,
+                 meta={"seed": seed, "joints": joints}, **kw)
+
+
 def small_mixed(n=60, seed=0, region=(6.0, 8.0, 6.0), steps=200, with_hulls=True):
     """A small dense mix of every shape type for stage-by-stage parity checks."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -534,4 +610,5 @@ SCENES = {
     "learned_warmstart": learned_warmstart,
     "jointed_chains": jointed_chains,
     "hinged_chains": hinged_chains,
+    "sixdof_chains": sixdof_chains,
 }

@@ -159,6 +159,36 @@ void orc_ray_test(void* h, const float* from, const float* to, const int* world,
         out[i].point[0] = r.point.x; out[i].point[1] = r.point.y; out[i].point[2] = r.point.z;
     }
 }
+int orc_add_generic6dof(void* h, int a, int b, const float* frameA, const float* frameB, int useA) {
+    int id = orc_add_hinge(h, a, b, frameA, frameB);
+    Joint& j = ((World*)h)->joints[id];
+    j.type = JOINT_6DOF;
+    j.useLinearReferenceFrameA = useA != 0;
+    return id;
+}
+void orc_set_6dof_limit(void* h, int id, int axis, float lo, float hi) {   // Generic6DofConstraint.setLimit
+    Joint& j = ((World*)h)->joints[id];
+    if (axis < 3) { set_coord(j.linLower, axis, lo); set_coord(j.linUpper, axis, hi); }
+    else { j.rot[axis - 3].loLimit = lo; j.rot[axis - 3].hiLimit = hi; }
+}
+void orc_set_6dof_linear_motor(void* h, int id, float softness, float damping, float restitution) {
+    Joint& j = ((World*)h)->joints[id];
+    j.linSoftness = softness;
+    j.linDamping = damping;
+    j.linRestitution = restitution;
+}
+void orc_set_6dof_angular_motor(void* h, int id, int axis, int enable, float targetVelocity, float maxMotorForce,
+                                float maxLimitForce, float damping, float softness, float erp, float bounce) {
+    RotMotor& m = ((World*)h)->joints[id].rot[axis];
+    m.enableMotor = enable != 0;
+    m.targetVelocity = targetVelocity;
+    m.maxMotorForce = maxMotorForce;
+    m.maxLimitForce = maxLimitForce;
+    m.damping = damping;
+    m.limitSoftness = softness;
+    m.ERP = erp;
+    m.bounce = bounce;
+}
 int orc_get_joint_impulses(void* h, float* out, int cap) {
     const World* w = (const World*)h;
     const int n = (int)w->joints.size();

@@ -602,6 +602,156 @@ static void hinge_solve(Joint& j, Body& A, Body& B, float timeStep) {
     }
 }
 
+// MatrixUtil.invert (linearmath/MatrixUtil.java:362-395): cofactors over the determinant.
+static M3 m3_invert(const M3& m) {
+    auto cofac = [&](int r1, int c1, int r2, int c2) { return m.m[r1][c1] * m.m[r2][c2] - m.m[r1][c2] * m.m[r2][c1]; };
+    float co_x = cofac(1, 1, 2, 2), co_y = cofac(1, 2, 2, 0), co_z = cofac(1, 0, 2, 1);
+    float det = m.m[0][0] * co_x + m.m[0][1] * co_y + m.m[0][2] * co_z;
+    float s = 1.0f / det;
+    M3 r;
+    r.m[0][0] = co_x * s;
+    r.m[0][1] = cofac(0, 2, 2, 1) * s;
+    r.m[0][2] = cofac(0, 1, 1, 2) * s;
+    r.m[1][0] = co_y * s;
+    r.m[1][1] = cofac(0, 0, 2, 2) * s;
+    r.m[1][2] = cofac(0, 2, 1, 0) * s;
+    r.m[2][0] = co_z * s;
+    r.m[2][1] = cofac(0, 1, 2, 0) * s;
+    r.m[2][2] = cofac(0, 0, 1, 1) * s;
+    return r;
+}
+
+// Generic6DofConstraint.matrixToEulerXYZ (Generic6DofConstraint.java:125-159): element `index`
+// is row index % 3, column index / 3; atan2 / asin in double, rounded to float.
+static V3 matrix_to_euler_xyz(const M3& m) {
+    auto e = [&](int index) { return m.m[index % 3][index / 3]; };
+    V3 xyz;
+    if (e(2) < 1.0f) {
+        if (e(2) > -1.0f) {
+            xyz.x = (float)std::atan2((double)-e(5), (double)e(8));
+            xyz.y = (float)std::asin((double)e(2));
+            xyz.z = (float)std::atan2((double)-e(1), (double)e(0));
+        } else {
+            xyz.x = -(float)std::atan2((double)e(3), (double)e(4));
+            xyz.y = -SIMD_HALF_PI;
+            xyz.z = 0.0f;
+        }
+    } else {
+        xyz.x = (float)std::atan2((double)e(3), (double)e(4));
+        xyz.y = SIMD_HALF_PI;
+        xyz.z = 0.0f;
+    }
+    return xyz;
+}
+
+// RotationalLimitMotor.testLimitValue (RotationalLimitMotor.java:110-130)
+static void rot_test_limit(RotMotor& m, float v) {
+    if (m.loLimit > m.hiLimit) { m.currentLimit = 0; return; }
+    if (v < m.loLimit) { m.currentLimit = 1; m.currentLimitError = v - m.loLimit; return; }
+    if (v > m.hiLimit) { m.currentLimit = 2; m.currentLimitError = v - m.hiLimit; return; }
+    m.currentLimit = 0;
+}
+static bool rot_need_torques(const RotMotor& m) { return !(m.currentLimit == 0 && !m.enableMotor); }
+
+// Generic6DofConstraint.buildJacobian (java:275-323): accumulators cleared, calculateTransforms
+// and calculateAngleInfo (relative Euler angles, the three constraint axes), calcAnchorPos, the
+// linear rows of the limited axes (JacobianEntry.init with the port's zero B-side angular part)
+// and the angular rows of the axes whose motor or limit applies.
+static void d6_build(Joint& j, const Body& A, const Body& B) {
+    j.linAcc = v3(0.0f, 0.0f, 0.0f);
+    for (int i = 0; i < 3; i++) j.rot[i].accumulatedImpulse = 0.0f;
+    Xf fA, fB;
+    fA.b = j.frameA; fA.o = j.pivotA;
+    fB.b = j.frameB; fB.o = j.pivotB;
+    j.calcA = xf_mul(A.xf, fA);
+    j.calcB = xf_mul(B.xf, fB);
+    M3 rel = mulMM(m3_invert(j.calcA.b), j.calcB.b);
+    j.angleDiff = matrix_to_euler_xyz(rel);
+    V3 axis0 = col(j.calcB.b, 0), axis2 = col(j.calcA.b, 2);
+    j.calcAxis[1] = crs(axis2, axis0);
+    j.calcAxis[0] = crs(j.calcAxis[1], axis2);
+    j.calcAxis[2] = crs(axis0, j.calcAxis[1]);
+    float imA = A.invMass, imB = B.invMass;
+    float weight = imB == 0.0f ? 1.0f : imA / (imA + imB);
+    j.anchor = add(scl(j.calcA.o, weight), scl(j.calcB.o, 1.0f - weight));
+    M3 w2A = transpose(A.xf.b), w2B = transpose(B.xf.b);
+    for (int i = 0; i < 3; i++) {
+        if (!(coord(j.linUpper, i) >= coord(j.linLower, i))) continue;
+        V3 n = col(j.useLinearReferenceFrameA ? j.calcA.b : j.calcB.b, i);
+        V3 r1 = sub(j.anchor, A.xf.o), r2 = sub(j.anchor, B.xf.o);
+        V3 aJ = mulMv(crs(r1, n), w2A);
+        V3 bJ = mulMv(crs(r2, r2), w2B);
+        V3 m0 = mulc(A.invInertiaLocal, aJ), m1 = mulc(B.invInertiaLocal, bJ);
+        j.adiag[i] = A.invMass + dot(m0, aJ) + B.invMass + dot(m1, bJ);
+    }
+    for (int i = 0; i < 3; i++) {
+        rot_test_limit(j.rot[i], coord(j.angleDiff, i));
+        if (!rot_need_torques(j.rot[i])) continue;
+        V3 aJ = mulMv(j.calcAxis[i], w2A);
+        V3 bJ = mulMv(scl(j.calcAxis[i], -1.0f), w2B);
+        V3 m0 = mulc(A.invInertiaLocal, aJ), m1 = mulc(B.invInertiaLocal, bJ);
+        j.adiagAng[i] = dot(m0, aJ) + dot(m1, bJ);
+    }
+}
+
+// Generic6DofConstraint.solveConstraint (java:325-365) with
+// TranslationalLimitMotor.solveLinearAxis (TranslationalLimitMotor.java:70-150) and
+// RotationalLimitMotor.solveAngularLimits (RotationalLimitMotor.java:135-203).
+static void d6_solve(Joint& j, Body& A, Body& B, float timeStep) {
+    const V3 pointInA = j.calcA.o, pointInB = j.calcB.o;
+    for (int i = 0; i < 3; i++) {
+        if (!(coord(j.linUpper, i) >= coord(j.linLower, i))) continue;
+        float jacDiagABInv = 1.0f / j.adiag[i];
+        V3 axis = col(j.useLinearReferenceFrameA ? j.calcA.b : j.calcB.b, i);
+        V3 r1 = sub(j.anchor, A.xf.o), r2 = sub(j.anchor, B.xf.o);
+        V3 vel = sub(add(crs(A.angvel, r1), A.linvel), add(crs(B.angvel, r2), B.linvel));
+        float relVel = dot(axis, vel);
+        float depth = -dot(sub(pointInA, pointInB), axis);
+        float lo = -1e30f, hi = 1e30f;
+        float minLimit = coord(j.linLower, i), maxLimit = coord(j.linUpper, i);
+        if (minLimit < maxLimit) {
+            if (depth > maxLimit) { depth -= maxLimit; lo = 0.0f; }
+            else if (depth < minLimit) { depth -= minLimit; hi = 0.0f; }
+            else continue;
+        }
+        float normalImpulse = j.linSoftness * (j.linRestitution * depth / timeStep - j.linDamping * relVel) * jacDiagABInv;
+        float old = coord(j.linAcc, i);
+        float sum = old + normalImpulse;
+        set_coord(j.linAcc, i, sum > hi ? 0.0f : (sum < lo ? 0.0f : sum));
+        normalImpulse = coord(j.linAcc, i) - old;
+        V3 iv = scl(axis, normalImpulse);
+        apply_impulse(A, iv, r1);
+        apply_impulse(B, scl(iv, -1.0f), r2);
+    }
+    for (int i = 0; i < 3; i++) {
+        RotMotor& m = j.rot[i];
+        if (!rot_need_torques(m)) continue;
+        V3 axis = j.calcAxis[i];
+        float jacDiagABInv = 1.0f / j.adiagAng[i];
+        float targetVelocity = m.targetVelocity, maxMotorForce = m.maxMotorForce;
+        if (m.currentLimit != 0) {
+            targetVelocity = -m.ERP * m.currentLimitError / timeStep;
+            maxMotorForce = m.maxLimitForce;
+        }
+        maxMotorForce *= timeStep;
+        float relVel = dot(axis, sub(A.angvel, B.angvel));
+        float motorRelVel = m.limitSoftness * (targetVelocity - m.damping * relVel);
+        if (motorRelVel < FLT_EPS && motorRelVel > -FLT_EPS) continue;
+        float unclipped = (1.0f + m.bounce) * motorRelVel * jacDiagABInv;
+        float clipped;
+        if (unclipped > 0.0f) clipped = unclipped > maxMotorForce ? maxMotorForce : unclipped;
+        else clipped = unclipped < -maxMotorForce ? -maxMotorForce : unclipped;
+        const float lo = -1e30f, hi = 1e30f;
+        float old = m.accumulatedImpulse;
+        float sum = old + clipped;
+        m.accumulatedImpulse = sum > hi ? 0.0f : (sum < lo ? 0.0f : sum);
+        clipped = m.accumulatedImpulse - old;
+        V3 motorImp = scl(axis, clipped);
+        apply_torque(A, motorImp);
+        apply_torque(B, scl(motorImp, -1.0f));
+    }
+}
+
 static void solve_group(World& w, const std::vector<int>& manifolds, const std::vector<int>& joints, float dt) {
     const Config& cfg = w.cfg;
     std::vector<SolverBody> sb;
@@ -736,6 +886,7 @@ static void solve_group(World& w, const std::vector<int>& manifolds, const std::
     for (int jk : joints) {
         Joint& J = w.joints[jk];
         if (J.type == JOINT_HINGE) hinge_build(J, jointBody(J.a), jointBody(J.b));
+        else if (J.type == JOINT_6DOF) d6_build(J, jointBody(J.a), jointBody(J.b));
         else joint_build(J, jointBody(J.a), jointBody(J.b));
     }
     // solveGroupCacheFriendlyIterations (java:788-890), split impulse off.  With a residual
@@ -785,6 +936,7 @@ static void solve_group(World& w, const std::vector<int>& manifolds, const std::
                     b->angvel = sb[b->companionId].angvel;
                 }
             if (J.type == JOINT_HINGE) hinge_solve(J, A, B, dt);
+            else if (J.type == JOINT_6DOF) d6_solve(J, A, B, dt);
             else joint_solve(J, A, B, dt);
             for (Body* b : {&A, &B})
                 if (b->islandTag >= 0 && b->companionId >= 0 && sb[b->companionId].invMass != 0.0f) {

@@ -91,7 +91,17 @@ struct Body {            // dynamics/RigidBody.java + collision/dispatch/Collisi
 // constraint frames as its constructors leave them (rbAFrame, rbBFrame: z is the hinge axis,
 // B's axis column already flipped), its limit (free: lower 1e30 > upper -1e30), motor and
 // angularOnly switch.
-enum JointType { JOINT_P2P = 0, JOINT_HINGE = 1 };
+// Generic6DofConstraint (dynamics/constraintsolver/Generic6DofConstraint.java:88-490) with its
+// TranslationalLimitMotor (TranslationalLimitMotor.java) and three RotationalLimitMotors
+// (RotationalLimitMotor.java): frames in frameA / frameB with origins in pivotA / pivotB.
+enum JointType { JOINT_P2P = 0, JOINT_HINGE = 1, JOINT_6DOF = 2 };
+struct RotMotor {     // RotationalLimitMotor defaults
+    float loLimit = -SIMD_INFINITY, hiLimit = SIMD_INFINITY, targetVelocity = 0.0f, maxMotorForce = 0.1f;
+    float maxLimitForce = 300.0f, damping = 1.0f, limitSoftness = 0.5f, ERP = 0.5f, bounce = 0.0f;
+    bool enableMotor = false;
+    int currentLimit = 0;
+    float currentLimitError = 0.0f, accumulatedImpulse = 0.0f;
+};
 struct Joint {
     int type = JOINT_P2P;
     int a = -1, b = -1;
@@ -107,6 +117,14 @@ struct Joint {
     V3 normal[3];                          // buildJacobian: the linear rows' axes
     float kHinge = 0.0f, correction = 0.0f, limitSign = 0.0f, accLimitImpulse = 0.0f;
     bool solveLimit = false;
+    // generic 6-dof
+    bool useLinearReferenceFrameA = true;
+    V3 linLower{0, 0, 0}, linUpper{0, 0, 0}, linAcc{0, 0, 0};
+    float linSoftness = 0.7f, linDamping = 1.0f, linRestitution = 0.5f;
+    RotMotor rot[3];
+    Xf calcA, calcB;                       // calculateTransforms
+    V3 angleDiff{0, 0, 0}, calcAxis[3], anchor{0, 0, 0};
+    float adiagAng[3] = {0, 0, 0};
 };
 
 struct Config {

@@ -54,6 +54,10 @@ def lib():
         L.orc_set_joint_setting.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float]
         L.orc_get_joint_impulses.argtypes = [C.c_void_p, _abi.f32p, C.c_int]
         L.orc_ray_test.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]
+        L.orc_add_generic6dof.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p, C.c_int]
+        L.orc_set_6dof_limit.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float]
+        L.orc_set_6dof_linear_motor.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 3
+        L.orc_set_6dof_angular_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_float] * 7
         L.orc_add_hinge.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
         L.orc_set_hinge_limit.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 5
         L.orc_enable_hinge_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float]
@@ -129,8 +133,33 @@ class OracleWorld:
     def set_hinge_angular_only(self, jid, on):
         lib().orc_set_hinge_angular_only(self.h, jid, 1 if on else 0)
 
+    def add_generic6dof(self, a, b, frame_a, frame_b, use_linear_reference_frame_a=True):
+        fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
+        fb = np.ascontiguousarray(frame_b, np.float32).reshape(12)
+        return lib().orc_add_generic6dof(self.h, a, b, _fp(fa), _fp(fb), 1 if use_linear_reference_frame_a else 0)
+
+    def set_6dof_limit(self, jid, axis, lo, hi):
+        lib().orc_set_6dof_limit(self.h, jid, axis, lo, hi)
+
+    def set_6dof_linear_motor(self, jid, softness, damping, restitution):
+        lib().orc_set_6dof_linear_motor(self.h, jid, softness, damping, restitution)
+
+    def set_6dof_angular_motor(self, jid, axis, enable, target_velocity, max_motor_force, max_limit_force=300.0,
+                               damping=1.0, softness=0.5, erp=0.5, bounce=0.0):
+        lib().orc_set_6dof_angular_motor(self.h, jid, axis, 1 if enable else 0, target_velocity, max_motor_force,
+                                         max_limit_force, damping, softness, erp, bounce)
+
     def add_scene_joints(self, scene):
         for j in scene.meta.get("joints", []):
+            if j.get("type") == "6dof":
+                jid = self.add_generic6dof(j["a"], j["b"], j["frame_a"], j["frame_b"], j.get("use_a", True))
+                for axis, lo, hi in j.get("limits", []):
+                    self.set_6dof_limit(jid, axis, lo, hi)
+                if "linear_motor" in j:
+                    self.set_6dof_linear_motor(jid, *j["linear_motor"])
+                for m in j.get("angular_motors", []):
+                    self.set_6dof_angular_motor(jid, *m)
+                continue
             if j.get("type") == "hinge":
                 jid = self.add_hinge(j["a"], j["b"], j["frame_a"], j["frame_b"])
                 if "limit" in j:

@@ -294,3 +294,117 @@ def test_mirror_hinged_door(gpu_lib, oracle_lib):
     assert not H.compare_state(o.get_state(), g.get_state())
     assert np.array_equal(o.joint_impulses().view(np.uint32), g.joint_impulses().view(np.uint32))
     world.close()
+
+
+# ---- generic 6-dof joints (dynamics/constraintsolver/Generic6DofConstraint.java) ----------
+def _d6_state(state, joints):
+    """Per joint: pivot gap, and |relative Euler angles| (x, y, z) of frame B in frame A."""
+    xf = state["transform"].astype(np.float64)
+    out = []
+    for j in joints:
+        a, b = j["a"], j["b"]
+        fa, fb = np.asarray(j["frame_a"], np.float64), np.asarray(j["frame_b"], np.float64)
+        Ra, Rb = xf[a, :9].reshape(3, 3), xf[b, :9].reshape(3, 3)
+        gap = np.linalg.norm(Ra @ fa[9:] + xf[a, 9:] - Rb @ fb[9:] - xf[b, 9:])
+        R = (Ra @ fa[:9].reshape(3, 3)).T @ (Rb @ fb[:9].reshape(3, 3))
+        e = (np.arctan2(-R[1, 2], R[2, 2]), np.arcsin(np.clip(R[0, 2], -1, 1)), np.arctan2(-R[0, 1], R[0, 0]))
+        out.append((gap,) + tuple(np.abs(e)))
+    return np.asarray(out)
+
+
+def test_oracle_generic6dof_limits_hold(oracle_lib):
+    """Locked linear axes keep the pivots together, a free linear axis moves within its +-0.3
+    range, angular limits of +-0.4 hold, locked angular axes stay put."""
+    sc = scenes.sixdof_chains(chains=4, links=5, loose=8, seed=1)
+    J = sc.meta["joints"]
+    o = pyoracle.OracleWorld(sc)
+    worst = np.zeros((len(J), 4))
+    for _ in range(240):
+        o.step(sc.dt)
+        worst = np.maximum(worst, _d6_state(o.get_state(), J))
+    assert o.counters()["status_flags"] == 0
+    kinds = np.array([(k // 5) % 4 for k in range(len(J))])
+    assert worst[kinds != 2, 0].max() < 0.02 and worst[kinds == 2, 0].max() < 0.36
+    assert worst[kinds == 0, 1:].max() < 0.45                       # +-0.4 limits
+    assert worst[kinds == 1, 2:].max() < 0.03                       # y and z locked
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["world_part", "range_parts", "batched"])
+def test_gpu_generic6dof_bit_exact(gpu_lib, oracle_lib, case):
+    if case == "batched":
+        sc = scenes.sixdof_chains(chains=4, links=3, loose=4, seed=9, worlds=3)
+    else:
+        sc = scenes.sixdof_chains(chains=8, links=4, loose=16, seed=10)
+    cfg = dict(sc.config)
+    if case == "range_parts":
+        cfg["solver_parts"] = 5
+    g = GpuWorld(sc, config=_abi.default_config(**cfg))
+    o = pyoracle.OracleWorld(sc)
+    for s in range(200):
+        g.step(sc.dt)
+        if case == "range_parts":
+            o.set_explicit_order(g.solver_order())
+        o.step(sc.dt)
+        assert o.counters()["status_flags"] == 0, s
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+            assert not bs and not bm, (s, bs, bm)
+    assert g.counters()["status_flags"] == 0
+    g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_generic6dof_api_errors(gpu_lib):
+    sc = scenes.sixdof_chains(chains=1, links=2, loose=0, seed=11)
+    g = GpuWorld(sc)
+    from jbgpu.lib import JbgpuError
+    with pytest.raises(JbgpuError):
+        g.set_6dof_limit(0, 6, 0.0, 1.0)                        # axes 0..5
+    with pytest.raises(JbgpuError):
+        g.set_6dof_angular_motor(0, 3, True, 1.0, 1.0)          # angular axes 0..2
+    with pytest.raises(JbgpuError):
+        g.set_hinge_limit(0, -1.0, 1.0)                          # a 6-dof joint is not a hinge
+    p2p = g.add_point2point(2, -1, (0, 0, 0), (0, 0, 0))
+    with pytest.raises(JbgpuError):
+        g.set_6dof_limit(p2p, 0, 0.0, 1.0)
+    g.close()
+
+
+@pytest.mark.gpu
+def test_mirror_generic6dof(gpu_lib):
+    """Generic6DofConstraint through the mirror: a box hung from a static anchor, linear axes
+    locked, rotation limited to +-0.3 rad about x and locked about y and z, then a motor about x
+    switched on between steps through getRotationalLimitMotor."""
+    from jbgpu import dynamics as D
+    world = D.DiscreteDynamicsWorld()
+    world.setGravity((0.0, -9.81, 0.0))
+    anchor = D.RigidBody(D.RigidBodyConstructionInfo(0.0, None, D.BoxShape((0.2, 0.2, 0.2))))
+    anchor.info.startWorldTransform = D.Transform(origin=(0.0, 5.0, 0.0))
+    world.addRigidBody(anchor)
+    shape = D.BoxShape((0.15, 0.45, 0.15))
+    info = D.RigidBodyConstructionInfo(1.0, None, shape, shape.calculateLocalInertia(1.0))
+    info.startWorldTransform = D.Transform(origin=(0.0, 4.3, 0.0))
+    box = D.RigidBody(info)
+    box.setLinearVelocity((0.0, 0.0, 2.0))
+    world.addRigidBody(box)
+    c = D.Generic6DofConstraint(box, anchor, D.Transform(origin=(0.0, 0.5, 0.0)), D.Transform(origin=(0.0, -0.2, 0.0)), True)
+    c.setAngularLowerLimit((-0.3, 0.0, 0.0))
+    c.setAngularUpperLimit((0.3, 0.0, 0.0))
+    world.addConstraint(c)
+    for _ in range(120):
+        world.stepSimulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    st = world._g.get_state()
+    j = {"a": 1, "b": 0, "frame_a": c.frameInA.as12(), "frame_b": c.frameInB.as12()}
+    gap, ex, ey, ez = _d6_state(st, [j])[0]
+    assert gap < 0.02 and ex < 0.4 and ey < 0.02 and ez < 0.02, (gap, ex, ey, ez)
+    m = c.getRotationalLimitMotor(0)
+    m.enableMotor, m.targetVelocity, m.maxMotorForce = True, 0.5, 5.0
+    c.setAngularLowerLimit((1.0, 0.0, 0.0))        # x free (lo > hi)
+    c.setAngularUpperLimit((-1.0, 0.0, 0.0))
+    for _ in range(60):
+        world.stepSimulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    w = box.getAngularVelocity()
+    assert abs(abs(w[0]) - 0.5) < 0.05, w
+    world.close()
