@@ -400,7 +400,7 @@ def test_mirror_generic6dof(gpu_lib):
     gap, ex, ey, ez = _d6_state(st, [j])[0]
     assert gap < 0.02 and ex < 0.4 and ey < 0.02 and ez < 0.02, (gap, ex, ey, ez)
     m = c.getRotationalLimitMotor(0)
-    m.enableMotor, m.targetVelocity, m.maxMotorForce = True, 0.5, 5.0
+    m.enableMotor, m.targetVelocity, m.maxMotorForce = True, 0.5, 50.0
     c.setAngularLowerLimit((1.0, 0.0, 0.0))        # x free (lo > hi)
     c.setAngularUpperLimit((-1.0, 0.0, 0.0))
     for _ in range(60):
