@@ -381,6 +381,19 @@ int jbgpu_world_enable_hinge_motor(jbgpu_world* world, int32_t id, int32_t enabl
                                    float max_motor_impulse);
 /* HingeConstraint.setAngularOnly (java:555-557): no linear rows, the axes alone are held. */
 int jbgpu_world_set_hinge_angular_only(jbgpu_world* world, int32_t id, int32_t angular_only);
+/* Cone-twist joint: addConstraint(new ConeTwistConstraint(rbA, rbB, rbAFrame, rbBFrame), false)
+ * (dynamics/constraintsolver/ConeTwistConstraint.java:43-412), frames as for the hinge (12 floats
+ * each; x is the twist axis); body_b = -1 is the fixed body (the reference's one-body constructor
+ * passes rbBFrame = rbAFrame unchanged).  Spans start at 1e30 and limitSoftness at 0, as the
+ * reference's constructors leave them. */
+int jbgpu_world_add_cone_twist(jbgpu_world* world, int32_t body_a, int32_t body_b, const float frame_a[12],
+                               const float frame_b[12], int32_t* id);
+/* ConeTwistConstraint.setLimit(swingSpan1, swingSpan2, twistSpan, softness, biasFactor,
+ * relaxationFactor) (java:379-389); the three-argument form passes 0.8, 0.3, 1.0. */
+int jbgpu_world_set_cone_twist_limit(jbgpu_world* world, int32_t id, float swing_span1, float swing_span2,
+                                     float twist_span, float softness, float bias_factor, float relaxation_factor);
+/* ConeTwistConstraint.setAngularOnly (java:371-373). */
+int jbgpu_world_set_cone_twist_angular_only(jbgpu_world* world, int32_t id, int32_t angular_only);
 /* Generic 6-dof joint: addConstraint(new Generic6DofConstraint(rbA, rbB, frameInA, frameInB,
  * useLinearReferenceFrameA), false) (dynamics/constraintsolver/Generic6DofConstraint.java:88-490).
  * Frames as 12 floats (basis row-major, origin) in the bodies' centre-of-mass spaces; body_b = -1

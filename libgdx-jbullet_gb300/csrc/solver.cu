@@ -1138,6 +1138,112 @@ JBD void d6_setup(const DevWorld& w, const DevJoints& J, int j, int a, int b) {
     J.r2[j] = f4(r2, 0.0f);
 }
 
+// ConeTwistConstraint.buildJacobian (ConeTwistConstraint.java:111-265): the hinge's linear rows,
+// the swing angles about A's frame axes 1 and 2 (atan2Fast damped by the "fact" factor) against
+// the elliptic cone of the swing spans, the twist about the frames' x axes through
+// shortestArcQuat / quatRotate (linearmath/QuaternionUtil.java:49-90).  For a swing span below
+// 0.05 the reference reads a stack vector it never set; A's frame axis is used here.
+JBD void cone_setup(const DevWorld& w, const DevJoints& J, int j, int a, int b) {
+    const int kind = J.kind[j];
+    const float4* F = J.frame + 6 * j;
+    const Xf xa = joint_xf(w, a), xb = joint_xf(w, b);
+    const float4 la = w.iloc[a], lb = b >= 0 ? w.iloc[b] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const V iA = mk(la.x, la.y, la.z), iB = mk(lb.x, lb.y, lb.z);
+    const M IA = joint_iw(w, a), IB = joint_iw(w, b);
+    const V pA = xf_apply(xa, mk4(J.pivA[j])), pB = xf_apply(xb, mk4(J.pivB[j]));
+    const V r1 = sub(pA, xa.o), r2 = sub(pB, xb.o);
+    float4* H = J.hs + JOINT_STEP_F4 * j;
+    float depth[3] = {0.0f, 0.0f, 0.0f};
+    if (!(kind & JK_ANGULAR_ONLY)) {
+        V n[3];
+        const V rel = sub(pB, pA);
+        n[0] = len2(rel) > FLT_EPS ? nor(rel) : mk(1.0f, 0.0f, 0.0f);
+        plane_space1(n[0], n[1], n[2]);
+        const M w2A = transpose(xa.b), w2B = transpose(xb.b);
+        for (int i = 0; i < 3; i++) {
+            const V aJ = mulMv(crs(r1, n[i]), w2A);
+            const V bJ = mulMv(crs(r2, r2), w2B);
+            const V m0 = mulc(iA, aJ), m1 = mulc(iB, bJ);
+            const float adiag = __fadd_rn(__fadd_rn(__fadd_rn(la.w, dot(m0, aJ)), lb.w), dot(m1, bJ));
+            H[i] = f4(n[i], jdiv(1.0f, adiag));
+            depth[i] = -dot(sub(pA, pB), n[i]);
+        }
+    }
+    const float4 st = J.set[j], s2 = J.set2[j];   // (swing1, swing2, twist, softness), (bias, relaxation)
+    const V b1Axis1 = mulMv(frame_col(F, 0), xa.b), b2Axis1 = mulMv(frame_col(F + 3, 0), xb.b);
+    const V b1Axis2 = mulMv(frame_col(F, 1), xa.b), b1Axis3 = mulMv(frame_col(F, 2), xa.b);
+    float swing1 = 0.0f, swing2 = 0.0f;
+    const float thresh = 10.0f;
+    if (st.x >= 0.05f) {
+        const float swx = dot(b2Axis1, b1Axis1), swy = dot(b2Axis1, b1Axis2);
+        swing1 = atan2_fast(swy, swx);
+        float fact = __fmul_rn(__fmul_rn(__fadd_rn(__fmul_rn(swy, swy), __fmul_rn(swx, swx)), thresh), thresh);
+        fact = jdiv(fact, __fadd_rn(fact, 1.0f));
+        swing1 = __fmul_rn(swing1, fact);
+    }
+    if (st.y >= 0.05f) {
+        const float swx = dot(b2Axis1, b1Axis1), swy = dot(b2Axis1, b1Axis3);
+        swing2 = atan2_fast(swy, swx);
+        float fact = __fmul_rn(__fmul_rn(__fadd_rn(__fmul_rn(swy, swy), __fmul_rn(swx, swx)), thresh), thresh);
+        fact = jdiv(fact, __fadd_rn(fact, 1.0f));
+        swing2 = __fmul_rn(swing2, fact);
+    }
+    const float r1sq = jdiv(1.0f, __fmul_rn(st.x, st.x)), r2sq = jdiv(1.0f, __fmul_rn(st.y, st.y));
+    const float ellipse = __fadd_rn(__fmul_rn(fabsf(__fmul_rn(swing1, swing1)), r1sq), __fmul_rn(fabsf(__fmul_rn(swing2, swing2)), r2sq));
+    V swingAxis = mk(0.0f, 0.0f, 0.0f), twistAxis = mk(0.0f, 0.0f, 0.0f);
+    float kSwing = 0.0f, kTwist = 0.0f, swingCorr = 0.0f, twistCorr = 0.0f, solveSwing = 0.0f, solveTwist = 0.0f;
+    if (ellipse > 1.0f) {
+        swingCorr = __fsub_rn(ellipse, 1.0f);
+        solveSwing = 1.0f;
+        const V t = add(scl(b1Axis2, dot(b2Axis1, b1Axis2)), scl(b1Axis3, dot(b2Axis1, b1Axis3)));
+        swingAxis = scl(nor(crs(b2Axis1, t)), dot(b2Axis1, b1Axis1) >= 0.0f ? 1.0f : -1.0f);
+        kSwing = jdiv(1.0f, __fadd_rn(ang_denom(IA, swingAxis), ang_denom(IB, swingAxis)));
+    }
+    if (st.z >= 0.0f) {
+        const V b2Axis2 = mulMv(frame_col(F + 3, 1), xb.b);
+        const V c = crs(b2Axis1, b1Axis1);
+        const float d = dot(b2Axis1, b1Axis1);
+        Q q;
+        if ((double)d < -1.0 + (double)FLT_EPS) { q.x = 0.0f; q.y = 1.0f; q.z = 0.0f; q.w = 0.0f; }
+        else {
+            const float sq = jsqrt(__fmul_rn(__fadd_rn(1.0f, d), 2.0f));
+            const float rs = jdiv(1.0f, sq);
+            q.x = __fmul_rn(c.x, rs); q.y = __fmul_rn(c.y, rs); q.z = __fmul_rn(c.z, rs); q.w = __fmul_rn(sq, 0.5f);
+        }
+        const V v = b2Axis2;
+        Q qw;
+        qw.x = __fsub_rn(__fadd_rn(__fmul_rn(q.w, v.x), __fmul_rn(q.y, v.z)), __fmul_rn(q.z, v.y));
+        qw.y = __fsub_rn(__fadd_rn(__fmul_rn(q.w, v.y), __fmul_rn(q.z, v.x)), __fmul_rn(q.x, v.z));
+        qw.z = __fsub_rn(__fadd_rn(__fmul_rn(q.w, v.z), __fmul_rn(q.x, v.y)), __fmul_rn(q.y, v.x));
+        qw.w = __fsub_rn(__fsub_rn(__fmul_rn(-q.x, v.x), __fmul_rn(q.y, v.y)), __fmul_rn(q.z, v.z));
+        Q inv;
+        inv.x = -q.x; inv.y = -q.y; inv.z = -q.z; inv.w = q.w;
+        const Q r = qmul(qw, inv);
+        const V ref = mk(r.x, r.y, r.z);
+        const float twist = atan2_fast(dot(ref, b1Axis3), dot(ref, b1Axis2));
+        const float lff = st.z > 0.05f ? st.w : 0.0f;
+        if (twist <= __fmul_rn(-st.z, lff)) {
+            twistCorr = -__fadd_rn(twist, st.z);
+            solveTwist = 1.0f;
+            twistAxis = scl(nor(scl(add(b2Axis1, b1Axis1), 0.5f)), -1.0f);
+            kTwist = jdiv(1.0f, __fadd_rn(ang_denom(IA, twistAxis), ang_denom(IB, twistAxis)));
+        } else if (twist > __fmul_rn(st.z, lff)) {
+            twistCorr = __fsub_rn(twist, st.z);
+            solveTwist = 1.0f;
+            twistAxis = nor(scl(add(b2Axis1, b1Axis1), 0.5f));
+            kTwist = jdiv(1.0f, __fadd_rn(ang_denom(IA, twistAxis), ang_denom(IB, twistAxis)));
+        }
+    }
+    (void)s2;
+    H[3] = f4(swingAxis, kSwing);
+    H[4] = f4(twistAxis, kTwist);
+    H[5] = make_float4(swingCorr, twistCorr, solveSwing, solveTwist);
+    H[6] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    J.r1[j] = f4(r1, 0.0f);
+    J.r2[j] = f4(r2, 0.0f);
+    J.dep[j] = make_float4(depth[0], depth[1], depth[2], 0.0f);
+}
+
 __global__ void k_joint_setup(DevWorld w, SolverBuffers sb) {
     const DevJoints& J = sb.J;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1155,6 +1261,10 @@ __global__ void k_joint_setup(DevWorld w, SolverBuffers sb) {
     }
     if ((J.kind[j] & JK_TYPE) == JOINT_6DOF) {
         d6_setup(w, J, j, a, b);
+        return;
+    }
+    if ((J.kind[j] & JK_TYPE) == JOINT_CONE) {
+        cone_setup(w, J, j, a, b);
         return;
     }
     const Xf xa = joint_xf(w, a), xb = joint_xf(w, b);
@@ -1391,6 +1501,58 @@ JBD void d6_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
     if (b >= 0 && imB != 0.0f) gstore(w, b, vB, wB);
     __stcg(H + 11, accL);
     __stcg(H + 12, accA);
+}
+
+// ConeTwistConstraint.solveConstraint (ConeTwistConstraint.java:267-368): the hinge's linear rows,
+// then the swing and twist limits with clamped accumulated impulses, both from the angular
+// velocities as the linear rows left them.
+JBD void cone_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
+    const int a = J.a[j], b = J.b[j], kind = J.kind[j];
+    V vA, wA, vB = mk(0.0f, 0.0f, 0.0f), wB = mk(0.0f, 0.0f, 0.0f);
+    gload(w, a, vA, wA);
+    if (b >= 0) gload(w, b, vB, wB);
+    const float imA = w.iloc[a].w, imB = b >= 0 ? w.iloc[b].w : 0.0f;
+    const M IA = load_iw(w, a), IB = joint_iw(w, b);
+    float4* H = J.hs + JOINT_STEP_F4 * j;
+    float acc = __ldcg(J.imp + j);
+    if (!(kind & JK_ANGULAR_ONLY)) {
+        const float4 q1 = J.r1[j], q2 = J.r2[j], dp = J.dep[j];
+        const V r1 = mk(q1.x, q1.y, q1.z), r2 = mk(q2.x, q2.y, q2.z);
+        const V vel = sub(add(crs(wA, r1), vA), add(crs(wB, r2), vB));
+        for (int i = 0; i < 3; i++) {
+            const float4 h = H[i];
+            const V n = mk(h.x, h.y, h.z);
+            const float depth = i == 0 ? dp.x : (i == 1 ? dp.y : dp.z);
+            const float impulse = __fsub_rn(__fmul_rn(jdiv(__fmul_rn(depth, 0.3f), dt), h.w), __fmul_rn(dot(n, vel), h.w));
+            acc = __fadd_rn(acc, impulse);
+            const V iv = scl(n, impulse);
+            body_impulse(vA, wA, imA, IA, iv, r1);
+            body_impulse(vB, wB, imB, IB, scl(iv, -1.0f), r2);
+        }
+    }
+    const float4 s2 = J.set2[j], fl = H[5];
+    float4 lim = __ldcg(H + 6);
+    const V angVelA = wA, angVelB = wB;
+    for (int k = 0; k < 2; k++) {
+        if ((k == 0 ? fl.z : fl.w) == 0.0f) continue;
+        const float4 ax = H[3 + k];
+        const V axis = mk(ax.x, ax.y, ax.z);
+        const float corr = k == 0 ? fl.x : fl.y;
+        const float amplitude = __fadd_rn(__fmul_rn(__fmul_rn(dot(sub(angVelB, angVelA), axis), s2.y), s2.y),
+                                          __fmul_rn(__fmul_rn(corr, jdiv(1.0f, dt)), s2.x));
+        float mag = __fmul_rn(amplitude, ax.w);
+        const float temp = k == 0 ? lim.x : lim.y;
+        const float nacc = jmax(__fadd_rn(temp, mag), 0.0f);
+        if (k == 0) lim.x = nacc; else lim.y = nacc;
+        mag = __fsub_rn(nacc, temp);
+        const V imp = scl(axis, mag);
+        torque_impulse(wA, imA, IA, imp);
+        torque_impulse(wB, imB, IB, scl(imp, -1.0f));
+    }
+    if (imA != 0.0f) gstore(w, a, vA, wA);
+    if (b >= 0 && imB != 0.0f) gstore(w, b, vB, wB);
+    __stcg(J.imp + j, acc);
+    __stcg(H + 6, lim);
 }
 
 // write-back (java:901-912): appliedImpulse; appliedImpulseLateral1 ends as friction row 2's
@@ -1638,6 +1800,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                         const int jt = sb.J.kind[j] & JK_TYPE;
                         if (jt == JOINT_HINGE) hinge_solve(w, sb.J, j, dt);
                         else if (jt == JOINT_6DOF) d6_solve(w, sb.J, j, dt);
+                        else if (jt == JOINT_CONE) cone_solve(w, sb.J, j, dt);
                         else joint_solve(w, sb.J, j, dt);
                     }
                     grid_barrier(w.ctr, nb, barK);

@@ -20,6 +20,7 @@ constexpr int PART_MAX_BODIES = 2048; // bodies of one part (velocities staged i
 constexpr int JOINT_P2P = 0;
 constexpr int JOINT_HINGE = 1;
 constexpr int JOINT_6DOF = 2;
+constexpr int JOINT_CONE = 3;
 constexpr int JK_TYPE = 0xff;         // kind: type in the low byte, hinge switches above it
 constexpr int JK_ANGULAR_ONLY = 1 << 8;
 constexpr int JK_MOTOR = 1 << 9;
@@ -33,8 +34,10 @@ struct DevJoints {
     int* b = nullptr;             // body B, -1 for the fixed body
     float4* pivA = nullptr;       // pivotInA, pivotInB (xyz); a hinge's frame origins
     float4* pivB = nullptr;
-    float4* set = nullptr;        // p2p: tau, damping, impulse clamp; hinge: lower, upper limit, softness, bias
-    float4* set2 = nullptr;       // hinge: relaxation factor, motor target velocity, max motor impulse
+    float4* set = nullptr;        // p2p: tau, damping, impulse clamp; hinge: lower, upper limit, softness, bias;
+                                  // cone twist: swing span 1, swing span 2, twist span, softness
+    float4* set2 = nullptr;       // hinge: relaxation factor, motor target velocity, max motor impulse;
+                                  // cone twist: bias factor, relaxation factor
     float4* frame = nullptr;      // hinge: rbAFrame basis rows (3), then rbBFrame basis rows (3)
     float4* hs = nullptr;         // per step (JOINT_STEP_F4 each).  Hinge: axis n_i with 1/Adiag_i (3),
                                   // world hinge axis of A with kHinge, of B with the limit correction,

@@ -1352,6 +1352,41 @@ int jbgpu_world_add_generic6dof(jbgpu_world* w, int32_t a, int32_t b, const floa
     return JBGPU_OK;
 }
 
+int jbgpu_world_add_cone_twist(jbgpu_world* w, int32_t a, int32_t b, const float fa[12], const float fb[12], int32_t* id) {
+    int32_t k = -1;
+    int rc = jbgpu_world_add_hinge(w, a, b, fa, fb, &k);
+    if (rc) return rc;
+    w->jKind[k] = JOINT_CONE;
+    w->jSet[k] = make_float4(1e30f, 1e30f, 1e30f, 0.0f);   // spans 1e30; limitSoftness left unset (0)
+    w->jSet2[k] = make_float4(0.3f, 1.0f, 0.0f, 0.0f);     // biasFactor, relaxationFactor
+    if (id) *id = k;
+    return JBGPU_OK;
+}
+
+static int cone_id(jbgpu_world* w, int32_t id) {
+    if (!w || id < 0 || id >= (int)w->jA.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
+    if ((w->jKind[id] & JK_TYPE) != JOINT_CONE) return fail(JBGPU_ERR_INVALID_ARGUMENT, "not a cone-twist joint");
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_cone_twist_limit(jbgpu_world* w, int32_t id, float swing1, float swing2, float twist, float softness,
+                                     float bias, float relaxation) {
+    int rc = cone_id(w, id);
+    if (rc) return rc;
+    w->jSet[id] = make_float4(swing1, swing2, twist, softness);
+    w->jSet2[id] = make_float4(bias, relaxation, 0.0f, 0.0f);
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_cone_twist_angular_only(jbgpu_world* w, int32_t id, int32_t on) {
+    int rc = cone_id(w, id);
+    if (rc) return rc;
+    w->jKind[id] = on ? (w->jKind[id] | JK_ANGULAR_ONLY) : (w->jKind[id] & ~JK_ANGULAR_ONLY);
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
 static int d6_id(jbgpu_world* w, int32_t id) {
     if (!w || id < 0 || id >= (int)w->jA.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
     if ((w->jKind[id] & JK_TYPE) != JOINT_6DOF) return fail(JBGPU_ERR_INVALID_ARGUMENT, "not a generic 6-dof joint");

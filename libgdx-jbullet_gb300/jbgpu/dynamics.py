@@ -330,6 +330,60 @@ class HingeConstraint:
         return float(self._world._g.joint_impulses()[self._id])
 
 
+class ConeTwistConstraint:
+    """dynamics/constraintsolver/ConeTwistConstraint.java:43-412: ConeTwistConstraint(rbA, rbB,
+    rbAFrame, rbBFrame) or ConeTwistConstraint(rbA, rbAFrame) (B's frame = A's frame, unchanged, on
+    the fixed body, as the reference's constructor leaves it)."""
+
+    def __init__(self, rbA, *args):
+        self.rbA = rbA
+        if len(args) == 3:
+            self.rbB, fa, fb = args
+        else:
+            self.rbB, fa, fb = None, args[0], args[0]
+        self.frameA = Transform(fa.basis.copy(), fa.origin.copy())
+        self.frameB = Transform(fb.basis.copy(), fb.origin.copy())
+        self.swingSpan1 = self.swingSpan2 = self.twistSpan = 1e30
+        self.limitSoftness, self.biasFactor, self.relaxationFactor = 0.0, 0.3, 1.0
+        self.angularOnly = False
+        self._world = None
+        self._id = None
+
+    def _push(self):
+        g = self._world._g if self._world is not None else None
+        if g is None or self._id is None:
+            return
+        g.set_cone_limit(self._id, self.swingSpan1, self.swingSpan2, self.twistSpan, self.limitSoftness, self.biasFactor,
+                         self.relaxationFactor)
+        g.set_cone_angular_only(self._id, self.angularOnly)
+
+    def setLimit(self, swingSpan1, swingSpan2, twistSpan, softness=0.8, biasFactor=0.3, relaxationFactor=1.0):
+        self.swingSpan1, self.swingSpan2, self.twistSpan = float(swingSpan1), float(swingSpan2), float(twistSpan)
+        self.limitSoftness, self.biasFactor, self.relaxationFactor = float(softness), float(biasFactor), float(relaxationFactor)
+        self._push()
+
+    def setAngularOnly(self, angularOnly):
+        self.angularOnly = bool(angularOnly)
+        self._push()
+
+    def getRigidBodyA(self):
+        return self.rbA
+
+    def getRigidBodyB(self):
+        return self.rbB
+
+    def getAFrame(self):
+        return Transform(self.frameA.basis.copy(), self.frameA.origin.copy())
+
+    def getBFrame(self):
+        return Transform(self.frameB.basis.copy(), self.frameB.origin.copy())
+
+    def getAppliedImpulse(self):
+        if self._world is None or self._world._g is None:
+            return 0.0
+        return float(self._world._g.joint_impulses()[self._id])
+
+
 class RotationalLimitMotor:
     """dynamics/constraintsolver/RotationalLimitMotor.java:44-70 (settings; defaults as there)."""
 
@@ -518,6 +572,10 @@ class DiscreteDynamicsWorld:
             b = -1 if c.rbB is None else c.rbB._index
             if isinstance(c, HingeConstraint):
                 c._id = self._g.add_hinge(c.rbA._index, b, c.frameA.as12(), c.frameB.as12())
+                c._push()
+                continue
+            if isinstance(c, ConeTwistConstraint):
+                c._id = self._g.add_cone_twist(c.rbA._index, b, c.frameA.as12(), c.frameB.as12())
                 c._push()
                 continue
             if isinstance(c, Generic6DofConstraint):

@@ -65,6 +65,10 @@ def lib():
             "jbgpu_world_set_ray_replay": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_set_graph": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_graph_status": ([C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_char_p)], C.c_int),
+            "jbgpu_world_add_cone_twist": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.POINTER(C.c_int32)],
+                                           C.c_int),
+            "jbgpu_world_set_cone_twist_limit": ([C.c_void_p, C.c_int32] + [C.c_float] * 6, C.c_int),
+            "jbgpu_world_set_cone_twist_angular_only": ([C.c_void_p, C.c_int32, C.c_int32], C.c_int),
             "jbgpu_world_add_generic6dof": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.c_int32,
                                             C.POINTER(C.c_int32)], C.c_int),
             "jbgpu_world_set_6dof_limit": ([C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float], C.c_int),
@@ -112,6 +116,7 @@ EXPORTED = [
     "jbgpu_world_enable_hinge_motor", "jbgpu_world_set_hinge_angular_only", "jbgpu_world_ray_test",
     "jbgpu_world_set_ray_replay", "jbgpu_world_set_graph", "jbgpu_world_graph_status", "jbgpu_world_add_generic6dof",
     "jbgpu_world_set_6dof_limit", "jbgpu_world_set_6dof_linear_motor", "jbgpu_world_set_6dof_angular_motor",
+    "jbgpu_world_add_cone_twist", "jbgpu_world_set_cone_twist_limit", "jbgpu_world_set_cone_twist_angular_only",
 ]
 
 
@@ -290,6 +295,22 @@ class GpuWorld:
     def set_ray_replay(self, all_rays):
         check(lib().jbgpu_world_set_ray_replay(self.h, 1 if all_rays else 0))
 
+    def add_cone_twist(self, a, b, frame_a, frame_b):
+        """Cone-twist joint with frames as 12 floats each (basis row-major, origin); returns its id."""
+        fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
+        fb = np.ascontiguousarray(frame_b, np.float32).reshape(12)
+        jid = C.c_int32()
+        check(lib().jbgpu_world_add_cone_twist(self.h, a, b, fa.ctypes.data_as(_abi.f32p), fb.ctypes.data_as(_abi.f32p),
+                                               C.byref(jid)))
+        return jid.value
+
+    def set_cone_limit(self, jid, swing1, swing2, twist, softness=0.8, bias_factor=0.3, relaxation_factor=1.0):
+        check(lib().jbgpu_world_set_cone_twist_limit(self.h, jid, swing1, swing2, twist, softness, bias_factor,
+                                                     relaxation_factor))
+
+    def set_cone_angular_only(self, jid, on):
+        check(lib().jbgpu_world_set_cone_twist_angular_only(self.h, jid, 1 if on else 0))
+
     def add_generic6dof(self, a, b, frame_a, frame_b, use_linear_reference_frame_a=True):
         """Generic 6-dof joint with frames as 12 floats each (basis row-major, origin); returns its id."""
         fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
@@ -312,6 +333,13 @@ class GpuWorld:
 
     def add_scene_joints(self, scene):
         for j in scene.meta.get("joints", []):
+            if j.get("type") == "cone":
+                jid = self.add_cone_twist(j["a"], j["b"], j["frame_a"], j["frame_b"])
+                if "limit" in j:
+                    self.set_cone_limit(jid, *j["limit"])
+                if j.get("angular_only"):
+                    self.set_cone_angular_only(jid, True)
+                continue
             if j.get("type") == "6dof":
                 jid = self.add_generic6dof(j["a"], j["b"], j["frame_a"], j["frame_b"], j.get("use_a", True))
                 for axis, lo, hi in j.get("limits", []):

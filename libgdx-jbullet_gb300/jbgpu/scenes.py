@@ -528,6 +528,83 @@ def sixdof_chains(chains=4, links=5, loose=8, seed=0, spacing=2.5, top=10.0, ste
                  meta={"seed": seed, "joints": joints}, **kw)
 
 
+def cone_chains(chains=6, links=5, loose=8, seed=0, spacing=2.5, top=10.0, steps=240, worlds=1):
+    """Chains of boxes (half-extents 0.15 x 0.45 x 0.15) joined end to end by cone-twist joints
+    whose twist axis (frame x) runs down the chain, the top link jointed to a static anchor box.
+    Chain c: c % 3 == 0 setLimit(0.5, 0.5, 0.3); 1 setLimit(0.3, 0.6, 0) (twist locked, with
+    softness, bias and relaxation given); 2 no limit set (the constructors' spans of 1e30 and
+    softness 0).  Loose boxes fall beside the chains; per world two of them are held to the same
+    orientation by an angular-only cone twist.  meta["joints"]: type "cone", a, b, frame_a, frame_b, optional limit, angular_only."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE), {"type": _abi.SHAPE_BOX, "params": (0.15, 0.45, 0.15, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.3, 0.3, 0.3, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.2, 0.2, 0.2, 0.0), "points": None}]
+    side = int(np.ceil(np.sqrt(chains)))
+    basis = np.array([[0, 1, 0], [-1, 0, 0], [0, 0, 1]], F).reshape(9)   # columns: x down the chain
+
+    def frame(origin):
+        return np.concatenate([basis, np.asarray(origin, F)]).astype(F)
+    all_bodies, joints, wid = [], [], []
+    base = 0
+    for wi in range(worlds):
+        plane = _plane_body(0)
+        anchors = _bodies(chains)
+        anchors["shape"] = 3
+        lb = _bodies(chains * links)
+        lb["shape"] = 1
+        lb["mass"] = 1.0
+        lb["local_inertia"] = box_inertia(1.0, (0.15, 0.45, 0.15))
+        for c in range(chains):
+            x0, z0 = (c % side - (side - 1) / 2.0) * spacing, (c // side - (side - 1) / 2.0) * spacing
+            anchors["transform"][c, 9:] = (x0, top + 0.2, z0)
+            v = rng.normal(0.0, 1.5, 2)
+            w = rng.normal(0.0, 1.0)
+            for i in range(links):
+                k = c * links + i
+                lb["transform"][k, 9:] = (x0, top - 0.5 - 1.0 * i, z0)
+                lb["linear_velocity"][k] = (v[0] * (i + 1) / links, 0.0, v[1] * (i + 1) / links)
+                lb["angular_velocity"][k] = (0.0, w, 0.0)
+        half = side * spacing / 2.0
+        fb = _bodies(loose)
+        fb["shape"] = 2
+        fb["mass"] = 2.0
+        fb["local_inertia"] = box_inertia(2.0, (0.3, 0.3, 0.3))
+        fpos = np.stack([rng.uniform(half + 1.0, half + 4.0, loose), rng.uniform(1.0, 6.0, loose),
+                         rng.uniform(-half, half, loose)], 1)   # beside the chains: impacts of 2 kg boxes
+                                                                 # drive the 0.5-rad cones unstable
+        _set_transforms(fb, random_rotations(rng, loose), fpos)
+        bodies = np.concatenate([plane, anchors, lb, fb])
+        first_anchor, first_link = base + 1, base + 1 + chains
+        for c in range(chains):
+            cfg = {"type": "cone"}
+            if c % 3 == 0:
+                cfg["limit"] = (0.5, 0.5, 0.3, 0.8, 0.3, 1.0)
+            elif c % 3 == 1:
+                cfg["limit"] = (0.3, 0.6, 0.0, 0.9, 0.4, 0.9)
+            a0 = first_link + c * links
+            joints.append(dict(cfg, a=a0, b=first_anchor + c, frame_a=frame((0.0, 0.5, 0.0)),
+                               frame_b=frame((0.0, -0.2, 0.0))))
+            for i in range(links - 1):
+                joints.append(dict(cfg, a=a0 + i, b=a0 + i + 1, frame_a=frame((0.0, -0.5, 0.0)),
+                                   frame_b=frame((0.0, 0.5, 0.0))))
+        if loose >= 2:
+            fl = first_link + chains * links
+            ra, rb = fb["transform"][0, :9].reshape(3, 3), fb["transform"][1, :9].reshape(3, 3)
+            fa_ = np.concatenate([np.eye(3, dtype=F).reshape(9), [0, 0, 0]]).astype(F)
+            fb_ = np.concatenate([(rb.T @ ra).astype(F).reshape(9), [0, 0, 0]]).astype(F)
+            joints.append({"type": "cone", "a": fl, "b": fl + 1, "frame_a": fa_, "frame_b": fb_,
+                           "limit": (0.2, 0.2, 0.2, 0.8, 0.3, 1.0), "angular_only": True})
+        all_bodies.append(bodies)
+        wid.append(np.full(len(bodies), wi, np.int32))
+        base += len(bodies)
+    bodies = np.concatenate(all_bodies)
+    bodies["world"] = np.concatenate(wid)
+    kw = {"world_of_body": np.concatenate(wid)} if worlds > 1 else {}
+    return Scene("cone_chains_%dx%d_w%d" % (chains, links, worlds), 1.0 / 60.0, steps,
+                 {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10}, shapes, bodies,
+                 meta={"seed": seed, "joints": joints}, **kw)
+
+
 def small_mixed(n=60, seed=0, region=(6.0, 8.0, 6.0), steps=200, with_hulls=True):
     """A small dense mix of every shape type for stage-by-stage parity checks."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -611,4 +688,5 @@ SCENES = {
     "jointed_chains": jointed_chains,
     "hinged_chains": hinged_chains,
     "sixdof_chains": sixdof_chains,
+    "cone_chains": cone_chains,
 }

@@ -189,6 +189,24 @@ void orc_set_6dof_angular_motor(void* h, int id, int axis, int enable, float tar
     m.ERP = erp;
     m.bounce = bounce;
 }
+int orc_add_cone_twist(void* h, int a, int b, const float* frameA, const float* frameB) {
+    int id = orc_add_hinge(h, a, b, frameA, frameB);
+    Joint& j = ((World*)h)->joints[id];
+    j.type = JOINT_CONE;
+    j.biasFactor = 0.3f;
+    j.relaxationFactor = 1.0f;
+    return id;
+}
+void orc_set_cone_limit(void* h, int id, float swing1, float swing2, float twist, float softness, float bias,
+                        float relaxation) {
+    Joint& j = ((World*)h)->joints[id];
+    j.swingSpan1 = swing1;
+    j.swingSpan2 = swing2;
+    j.twistSpan = twist;
+    j.coneSoftness = softness;
+    j.biasFactor = bias;
+    j.relaxationFactor = relaxation;
+}
 int orc_get_joint_impulses(void* h, float* out, int cap) {
     const World* w = (const World*)h;
     const int n = (int)w->joints.size();

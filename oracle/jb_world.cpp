@@ -752,6 +752,143 @@ static void d6_solve(Joint& j, Body& A, Body& B, float timeStep) {
     }
 }
 
+// ConeTwistConstraint.buildJacobian (ConeTwistConstraint.java:111-265): the hinge's linear rows,
+// the swing angles about A's frame axes 1 and 2 (atan2Fast damped by the "fact" factor) against
+// the elliptic cone of the two swing spans, the twist about the frames' x axes from
+// shortestArcQuat / quatRotate.  For a swing span below 0.05 the reference reads a stack vector it
+// never set (Stack.allocVector3 does not clear it); here that axis is A's frame axis.
+static void cone_build(Joint& j, const Body& A, const Body& B) {
+    j.appliedImpulse = 0.0f;
+    j.swingCorrection = 0.0f;
+    j.solveTwist = false;
+    j.solveSwing = false;
+    j.accTwist = 0.0f;
+    j.accSwing = 0.0f;
+    if (!j.angularOnly) {
+        V3 pA = xf_apply(A.xf, j.pivotA), pB = xf_apply(B.xf, j.pivotB);
+        V3 relPos = sub(pB, pA);
+        if (len2(relPos) > FLT_EPS) j.normal[0] = nor(relPos);
+        else j.normal[0] = v3(1.0f, 0.0f, 0.0f);
+        plane_space1(j.normal[0], j.normal[1], j.normal[2]);
+        for (int i = 0; i < 3; i++) {
+            M3 w2A = transpose(A.xf.b), w2B = transpose(B.xf.b);
+            V3 r1 = sub(pA, A.xf.o), r2 = sub(pB, B.xf.o);
+            V3 aJ = mulMv(crs(r1, j.normal[i]), w2A);
+            V3 bJ = mulMv(crs(r2, r2), w2B);
+            V3 m0 = mulc(A.invInertiaLocal, aJ), m1 = mulc(B.invInertiaLocal, bJ);
+            j.adiag[i] = A.invMass + dot(m0, aJ) + B.invMass + dot(m1, bJ);
+        }
+    }
+    V3 b1Axis1 = mulMv(col(j.frameA, 0), A.xf.b);
+    V3 b2Axis1 = mulMv(col(j.frameB, 0), B.xf.b);
+    V3 b1Axis2 = mulMv(col(j.frameA, 1), A.xf.b);
+    V3 b1Axis3 = mulMv(col(j.frameA, 2), A.xf.b);
+    float swing1 = 0.0f, swing2 = 0.0f;
+    const float thresh = 10.0f;
+    if (j.swingSpan1 >= 0.05f) {
+        float swx = dot(b2Axis1, b1Axis1), swy = dot(b2Axis1, b1Axis2);
+        swing1 = atan2_fast(swy, swx);
+        float fact = (swy * swy + swx * swx) * thresh * thresh;
+        fact = fact / (fact + 1.0f);
+        swing1 *= fact;
+    }
+    if (j.swingSpan2 >= 0.05f) {
+        float swx = dot(b2Axis1, b1Axis1), swy = dot(b2Axis1, b1Axis3);
+        swing2 = atan2_fast(swy, swx);
+        float fact = (swy * swy + swx * swx) * thresh * thresh;
+        fact = fact / (fact + 1.0f);
+        swing2 *= fact;
+    }
+    float r1sq = 1.0f / (j.swingSpan1 * j.swingSpan1);
+    float r2sq = 1.0f / (j.swingSpan2 * j.swingSpan2);
+    float ellipse = std::fabs(swing1 * swing1) * r1sq + std::fabs(swing2 * swing2) * r2sq;
+    if (ellipse > 1.0f) {
+        j.swingCorrection = ellipse - 1.0f;
+        j.solveSwing = true;
+        V3 t = add(scl(b1Axis2, dot(b2Axis1, b1Axis2)), scl(b1Axis3, dot(b2Axis1, b1Axis3)));
+        j.swingAxis = nor(crs(b2Axis1, t));
+        float sign = dot(b2Axis1, b1Axis1) >= 0.0f ? 1.0f : -1.0f;
+        j.swingAxis = scl(j.swingAxis, sign);
+        j.kSwing = 1.0f / (ang_denom(A, j.swingAxis) + ang_denom(B, j.swingAxis));
+    }
+    if (j.twistSpan >= 0.0f) {
+        V3 b2Axis2 = mulMv(col(j.frameB, 1), B.xf.b);
+        // QuaternionUtil.shortestArcQuat (linearmath/QuaternionUtil.java:49-68), quatRotate (78-90)
+        V3 c = crs(b2Axis1, b1Axis1);
+        float d = dot(b2Axis1, b1Axis1);
+        Quat q;
+        if ((double)d < -1.0 + (double)FLT_EPS) q = quat(0.0f, 1.0f, 0.0f, 0.0f);
+        else {
+            float sq = jsqrt((1.0f + d) * 2.0f);
+            float rs = 1.0f / sq;
+            q = quat(c.x * rs, c.y * rs, c.z * rs, sq * 0.5f);
+        }
+        Quat qw = quat(q.w * b2Axis2.x + q.y * b2Axis2.z - q.z * b2Axis2.y, q.w * b2Axis2.y + q.z * b2Axis2.x - q.x * b2Axis2.z,
+                       q.w * b2Axis2.z + q.x * b2Axis2.y - q.y * b2Axis2.x, -q.x * b2Axis2.x - q.y * b2Axis2.y - q.z * b2Axis2.z);
+        Quat r = qmul(qw, quat(-q.x, -q.y, -q.z, q.w));
+        V3 twistRef = v3(r.x, r.y, r.z);
+        float twist = atan2_fast(dot(twistRef, b1Axis3), dot(twistRef, b1Axis2));
+        float lockedFreeFactor = j.twistSpan > 0.05f ? j.coneSoftness : 0.0f;
+        if (twist <= -j.twistSpan * lockedFreeFactor) {
+            j.twistCorrection = -(twist + j.twistSpan);
+            j.solveTwist = true;
+            j.twistAxis = scl(nor(scl(add(b2Axis1, b1Axis1), 0.5f)), -1.0f);
+            j.kTwist = 1.0f / (ang_denom(A, j.twistAxis) + ang_denom(B, j.twistAxis));
+        } else if (twist > j.twistSpan * lockedFreeFactor) {
+            j.twistCorrection = twist - j.twistSpan;
+            j.solveTwist = true;
+            j.twistAxis = nor(scl(add(b2Axis1, b1Axis1), 0.5f));
+            j.kTwist = 1.0f / (ang_denom(A, j.twistAxis) + ang_denom(B, j.twistAxis));
+        }
+    }
+}
+
+// ConeTwistConstraint.solveConstraint (ConeTwistConstraint.java:267-368): the hinge's linear
+// rows, then the swing and twist limits with clamped accumulated impulses, both on the angular
+// velocities as the linear rows left them.
+static void cone_solve(Joint& j, Body& A, Body& B, float timeStep) {
+    V3 pA = xf_apply(A.xf, j.pivotA), pB = xf_apply(B.xf, j.pivotB);
+    const float tau = 0.3f;
+    if (!j.angularOnly) {
+        V3 r1 = sub(pA, A.xf.o), r2 = sub(pB, B.xf.o);
+        V3 vel = sub(add(crs(A.angvel, r1), A.linvel), add(crs(B.angvel, r2), B.linvel));
+        for (int i = 0; i < 3; i++) {
+            V3 n = j.normal[i];
+            float jacDiagABInv = 1.0f / j.adiag[i];
+            float relVel = dot(n, vel);
+            float depth = -dot(sub(pA, pB), n);
+            float impulse = depth * tau / timeStep * jacDiagABInv - relVel * jacDiagABInv;
+            j.appliedImpulse += impulse;
+            V3 iv = scl(n, impulse);
+            apply_impulse(A, iv, sub(pA, A.xf.o));
+            apply_impulse(B, scl(iv, -1.0f), sub(pB, B.xf.o));
+        }
+    }
+    V3 angVelA = A.angvel, angVelB = B.angvel;
+    if (j.solveSwing) {
+        float amplitude = dot(sub(angVelB, angVelA), j.swingAxis) * j.relaxationFactor * j.relaxationFactor +
+                          j.swingCorrection * (1.0f / timeStep) * j.biasFactor;
+        float impulseMag = amplitude * j.kSwing;
+        float temp = j.accSwing;
+        j.accSwing = jmax(j.accSwing + impulseMag, 0.0f);
+        impulseMag = j.accSwing - temp;
+        V3 imp = scl(j.swingAxis, impulseMag);
+        apply_torque(A, imp);
+        apply_torque(B, scl(imp, -1.0f));
+    }
+    if (j.solveTwist) {
+        float amplitude = dot(sub(angVelB, angVelA), j.twistAxis) * j.relaxationFactor * j.relaxationFactor +
+                          j.twistCorrection * (1.0f / timeStep) * j.biasFactor;
+        float impulseMag = amplitude * j.kTwist;
+        float temp = j.accTwist;
+        j.accTwist = jmax(j.accTwist + impulseMag, 0.0f);
+        impulseMag = j.accTwist - temp;
+        V3 imp = scl(j.twistAxis, impulseMag);
+        apply_torque(A, imp);
+        apply_torque(B, scl(imp, -1.0f));
+    }
+}
+
 static void solve_group(World& w, const std::vector<int>& manifolds, const std::vector<int>& joints, float dt) {
     const Config& cfg = w.cfg;
     std::vector<SolverBody> sb;
@@ -887,6 +1024,7 @@ static void solve_group(World& w, const std::vector<int>& manifolds, const std::
         Joint& J = w.joints[jk];
         if (J.type == JOINT_HINGE) hinge_build(J, jointBody(J.a), jointBody(J.b));
         else if (J.type == JOINT_6DOF) d6_build(J, jointBody(J.a), jointBody(J.b));
+        else if (J.type == JOINT_CONE) cone_build(J, jointBody(J.a), jointBody(J.b));
         else joint_build(J, jointBody(J.a), jointBody(J.b));
     }
     // solveGroupCacheFriendlyIterations (java:788-890), split impulse off.  With a residual
@@ -937,6 +1075,7 @@ static void solve_group(World& w, const std::vector<int>& manifolds, const std::
                 }
             if (J.type == JOINT_HINGE) hinge_solve(J, A, B, dt);
             else if (J.type == JOINT_6DOF) d6_solve(J, A, B, dt);
+            else if (J.type == JOINT_CONE) cone_solve(J, A, B, dt);
             else joint_solve(J, A, B, dt);
             for (Body* b : {&A, &B})
                 if (b->islandTag >= 0 && b->companionId >= 0 && sb[b->companionId].invMass != 0.0f) {

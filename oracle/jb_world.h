@@ -94,7 +94,11 @@ struct Body {            // dynamics/RigidBody.java + collision/dispatch/Collisi
 // Generic6DofConstraint (dynamics/constraintsolver/Generic6DofConstraint.java:88-490) with its
 // TranslationalLimitMotor (TranslationalLimitMotor.java) and three RotationalLimitMotors
 // (RotationalLimitMotor.java): frames in frameA / frameB with origins in pivotA / pivotB.
-enum JointType { JOINT_P2P = 0, JOINT_HINGE = 1, JOINT_6DOF = 2 };
+// ConeTwistConstraint (dynamics/constraintsolver/ConeTwistConstraint.java:43-412): frames in
+// frameA / frameB (origins in pivotA / pivotB), swing spans, twist span, softness, bias and
+// relaxation in the hinge's limit fields (swing1 -> lowerLimit, swing2 -> upperLimit, twist ->
+// twistSpan).
+enum JointType { JOINT_P2P = 0, JOINT_HINGE = 1, JOINT_6DOF = 2, JOINT_CONE = 3 };
 struct RotMotor {     // RotationalLimitMotor defaults
     float loLimit = -SIMD_INFINITY, hiLimit = SIMD_INFINITY, targetVelocity = 0.0f, maxMotorForce = 0.1f;
     float maxLimitForce = 300.0f, damping = 1.0f, limitSoftness = 0.5f, ERP = 0.5f, bounce = 0.0f;
@@ -117,6 +121,12 @@ struct Joint {
     V3 normal[3];                          // buildJacobian: the linear rows' axes
     float kHinge = 0.0f, correction = 0.0f, limitSign = 0.0f, accLimitImpulse = 0.0f;
     bool solveLimit = false;
+    // cone twist (limitSoftness starts at 0: the constructors leave it unset)
+    float swingSpan1 = 1e30f, swingSpan2 = 1e30f, twistSpan = 1e30f, coneSoftness = 0.0f;
+    V3 swingAxis{0, 0, 0}, twistAxis{0, 0, 0};
+    float kSwing = 0.0f, kTwist = 0.0f, swingCorrection = 0.0f, twistCorrection = 0.0f;
+    float accSwing = 0.0f, accTwist = 0.0f;
+    bool solveSwing = false, solveTwist = false;
     // generic 6-dof
     bool useLinearReferenceFrameA = true;
     V3 linLower{0, 0, 0}, linUpper{0, 0, 0}, linAcc{0, 0, 0};

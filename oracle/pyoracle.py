@@ -58,6 +58,8 @@ def lib():
         L.orc_set_6dof_limit.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float]
         L.orc_set_6dof_linear_motor.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 3
         L.orc_set_6dof_angular_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_float] * 7
+        L.orc_add_cone_twist.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
+        L.orc_set_cone_limit.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 6
         L.orc_add_hinge.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
         L.orc_set_hinge_limit.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 5
         L.orc_enable_hinge_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float]
@@ -149,8 +151,23 @@ class OracleWorld:
         lib().orc_set_6dof_angular_motor(self.h, jid, axis, 1 if enable else 0, target_velocity, max_motor_force,
                                          max_limit_force, damping, softness, erp, bounce)
 
+    def add_cone_twist(self, a, b, frame_a, frame_b):
+        fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
+        fb = np.ascontiguousarray(frame_b, np.float32).reshape(12)
+        return lib().orc_add_cone_twist(self.h, a, b, _fp(fa), _fp(fb))
+
+    def set_cone_limit(self, jid, swing1, swing2, twist, softness=0.8, bias_factor=0.3, relaxation_factor=1.0):
+        lib().orc_set_cone_limit(self.h, jid, swing1, swing2, twist, softness, bias_factor, relaxation_factor)
+
     def add_scene_joints(self, scene):
         for j in scene.meta.get("joints", []):
+            if j.get("type") == "cone":
+                jid = self.add_cone_twist(j["a"], j["b"], j["frame_a"], j["frame_b"])
+                if "limit" in j:
+                    self.set_cone_limit(jid, *j["limit"])
+                if j.get("angular_only"):
+                    self.set_hinge_angular_only(jid, True)
+                continue
             if j.get("type") == "6dof":
                 jid = self.add_generic6dof(j["a"], j["b"], j["frame_a"], j["frame_b"], j.get("use_a", True))
                 for axis, lo, hi in j.get("limits", []):

@@ -408,3 +408,53 @@ def test_mirror_generic6dof(gpu_lib):
     w = box.getAngularVelocity()
     assert abs(abs(w[0]) - 0.5) < 0.05, w
     world.close()
+
+
+# ---- cone-twist joints (dynamics/constraintsolver/ConeTwistConstraint.java) -----------------
+def test_oracle_cone_twist_holds(oracle_lib):
+    """Cone-twist chains keep their pivots together and their swing within the cones."""
+    sc = scenes.cone_chains(chains=6, links=5, loose=8, seed=1)
+    J = sc.meta["joints"]
+    o = pyoracle.OracleWorld(sc)
+    worst_gap, worst_swing = 0.0, np.zeros(len(J))
+    for _ in range(240):
+        o.step(sc.dt)
+        xf = o.get_state()["transform"].astype(np.float64)
+        for k, j in enumerate(J):
+            fa, fb = np.asarray(j["frame_a"], np.float64), np.asarray(j["frame_b"], np.float64)
+            Ra, Rb = xf[j["a"], :9].reshape(3, 3), xf[j["b"], :9].reshape(3, 3)
+            if not j.get("angular_only"):
+                worst_gap = max(worst_gap, np.linalg.norm(Ra @ fa[9:] + xf[j["a"], 9:] - Rb @ fb[9:] - xf[j["b"], 9:]))
+            A, B = Ra @ fa[:9].reshape(3, 3), Rb @ fb[:9].reshape(3, 3)
+            worst_swing[k] = max(worst_swing[k], np.arccos(np.clip(A[:, 0] @ B[:, 0], -1, 1)))
+    assert o.counters()["status_flags"] == 0
+    assert worst_gap < 0.02, worst_gap
+    limited = [k for k, j in enumerate(J) if "limit" in j and not j.get("angular_only")]
+    assert worst_swing[limited].max() < 0.7
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["world_part", "range_parts", "batched"])
+def test_gpu_cone_twist_bit_exact(gpu_lib, oracle_lib, case):
+    if case == "batched":
+        sc = scenes.cone_chains(chains=3, links=4, loose=4, seed=12, worlds=3)
+    else:
+        sc = scenes.cone_chains(chains=6, links=5, loose=8, seed=13)
+    cfg = dict(sc.config)
+    if case == "range_parts":
+        cfg["solver_parts"] = 5
+    g = GpuWorld(sc, config=_abi.default_config(**cfg))
+    o = pyoracle.OracleWorld(sc)
+    for s in range(200):
+        g.step(sc.dt)
+        if case == "range_parts":
+            o.set_explicit_order(g.solver_order())
+        o.step(sc.dt)
+        assert o.counters()["status_flags"] == 0, s
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+            assert not bs and not bm, (s, bs, bm)
+            assert np.array_equal(o.joint_impulses().view(np.uint32), g.joint_impulses().view(np.uint32)), s
+    assert g.counters()["status_flags"] == 0
+    g.close()
