@@ -394,6 +394,20 @@ int jbgpu_world_set_cone_twist_limit(jbgpu_world* world, int32_t id, float swing
                                      float twist_span, float softness, float bias_factor, float relaxation_factor);
 /* ConeTwistConstraint.setAngularOnly (java:371-373). */
 int jbgpu_world_set_cone_twist_angular_only(jbgpu_world* world, int32_t id, int32_t angular_only);
+/* Slider joint: addConstraint(new SliderConstraint(rbA, rbB, frameInA, frameInB,
+ * useLinearReferenceFrameA), false) (dynamics/constraintsolver/SliderConstraint.java:130-685); frames
+ * as for the 6-dof joint, x is the sliding axis; body_b = -1 is the fixed body.  Parameters as
+ * SliderConstraint.initParams leaves them (java:139-172). */
+int jbgpu_world_add_slider(jbgpu_world* world, int32_t body_a, int32_t body_b, const float frame_a[12],
+                           const float frame_b[12], int32_t use_linear_reference_frame_a, int32_t* id);
+/* The slider's setters (java:217-439) as one record of JBGPU_SLIDER_PARAMS floats: lower / upper
+ * linear limit, lower / upper angular limit; softness, restitution, damping of the directional
+ * linear, directional angular, linear limit, angular limit, orthogonal linear and orthogonal
+ * angular rows (18); powered linear motor (0/1), its target velocity and max force; powered
+ * angular motor, its target velocity and max force. */
+#define JBGPU_SLIDER_PARAMS 28
+int jbgpu_world_set_slider_params(jbgpu_world* world, int32_t id, const float* params);
+int jbgpu_world_get_slider_params(jbgpu_world* world, int32_t id, float* params);
 /* Generic 6-dof joint: addConstraint(new Generic6DofConstraint(rbA, rbB, frameInA, frameInB,
  * useLinearReferenceFrameA), false) (dynamics/constraintsolver/Generic6DofConstraint.java:88-490).
  * Frames as 12 floats (basis row-major, origin) in the bodies' centre-of-mass spaces; body_b = -1

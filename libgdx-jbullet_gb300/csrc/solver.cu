@@ -1244,6 +1244,68 @@ JBD void cone_setup(const DevWorld& w, const DevJoints& J, int j, int a, int b) 
     J.dep[j] = make_float4(depth[0], depth[1], depth[2], 0.0f);
 }
 
+// SliderConstraint.buildJacobianInt (SliderConstraint.java:465-526) with testLinLimits (714-730)
+// and testAngLimits (732-756).  The bodies' roles swap when useLinearReferenceFrameA is false
+// (buildJacobian, java:175-182): "A" is then the joint's body B with frame B.
+JBD void slider_setup(const DevWorld& w, const DevJoints& J, int j, int a, int b) {
+    const bool useA = J.set[j].x != 0.0f;
+    const int ia = useA ? a : b, ib = useA ? b : a;
+    const float4* F = J.frame + 6 * j + (useA ? 0 : 3);
+    const float4* G = J.frame + 6 * j + (useA ? 3 : 0);
+    const float4* P = J.d6set + D6_SET_F4 * j;   // 28 parameters
+    const Xf xa = joint_xf(w, ia), xb = joint_xf(w, ib);
+    const float4 la = ia >= 0 ? w.iloc[ia] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 lb = ib >= 0 ? w.iloc[ib] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const V iA = mk(la.x, la.y, la.z), iB = mk(lb.x, lb.y, lb.z);
+    const M IA = joint_iw(w, ia), IB = joint_iw(w, ib);
+    Xf fa, fb;
+    fa.b.r[0] = mk4(F[0]); fa.b.r[1] = mk4(F[1]); fa.b.r[2] = mk4(F[2]); fa.o = mk4(useA ? J.pivA[j] : J.pivB[j]);
+    fb.b.r[0] = mk4(G[0]); fb.b.r[1] = mk4(G[1]); fb.b.r[2] = mk4(G[2]); fb.o = mk4(useA ? J.pivB[j] : J.pivA[j]);
+    const Xf ca = xf_mul(xa, fa), cb = xf_mul(xb, fb);
+    auto colv = [](const M& m, int c) { return mk(coord(m.r[0], c), coord(m.r[1], c), coord(m.r[2], c)); };
+    const V axis = colv(ca.b, 0);
+    const V delta = sub(cb.o, ca.o);
+    const float ad = dot(axis, delta);
+    const V proj = mk(__fadd_rn(ca.o.x, __fmul_rn(ad, axis.x)), __fadd_rn(ca.o.y, __fmul_rn(ad, axis.y)),
+                      __fadd_rn(ca.o.z, __fmul_rn(ad, axis.z)));
+    const V relA = sub(proj, xa.o), relB = sub(cb.o, xb.o);
+    const M w2A = transpose(xa.b), w2B = transpose(xb.b);
+    float4* H = J.hs + JOINT_STEP_F4 * j;
+    float depth[3];
+    for (int i = 0; i < 3; i++) {
+        const V n = colv(ca.b, i);
+        const V aJ = mulMv(crs(relA, n), w2A);
+        const V bJ = mulMv(crs(relB, relB), w2B);
+        const V m0 = mulc(iA, aJ), m1 = mulc(iB, bJ);
+        const float adiag = __fadd_rn(__fadd_rn(__fadd_rn(la.w, dot(m0, aJ)), lb.w), dot(m1, bJ));
+        H[i] = f4(n, jdiv(1.0f, adiag));
+        depth[i] = dot(delta, n);
+    }
+    const float lowerLin = P[0].x, upperLin = P[0].y, lowerAng = P[0].z, upperAng = P[0].w;
+    float solveLin = 0.0f;
+    if (lowerLin <= upperLin) {
+        if (depth[0] > upperLin) { depth[0] = __fsub_rn(depth[0], upperLin); solveLin = 1.0f; }
+        else if (depth[0] < lowerLin) { depth[0] = __fsub_rn(depth[0], lowerLin); solveLin = 1.0f; }
+        else depth[0] = 0.0f;
+    } else {
+        depth[0] = 0.0f;
+    }
+    float angDepth = 0.0f, solveAng = 0.0f;
+    if (lowerAng <= upperAng) {
+        const V a0 = colv(ca.b, 1), a1 = colv(ca.b, 2), b0 = colv(cb.b, 1);
+        const float rot = (float)atan2((double)dot(b0, a1), (double)dot(b0, a0));
+        if (rot < lowerAng) { angDepth = __fsub_rn(rot, lowerAng); solveAng = 1.0f; }
+        else if (rot > upperAng) { angDepth = __fsub_rn(rot, upperAng); solveAng = 1.0f; }
+    }
+    const float kAngle = jdiv(1.0f, __fadd_rn(ang_denom(IA, axis), ang_denom(IB, axis)));
+    H[3] = f4(relA, depth[0]);
+    H[4] = f4(relB, depth[1]);
+    H[5] = f4(axis, depth[2]);
+    H[6] = f4(colv(cb.b, 0), kAngle);
+    H[7] = make_float4(solveLin, angDepth, solveAng, 0.0f);
+    H[8] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
 __global__ void k_joint_setup(DevWorld w, SolverBuffers sb) {
     const DevJoints& J = sb.J;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1265,6 +1327,10 @@ __global__ void k_joint_setup(DevWorld w, SolverBuffers sb) {
     }
     if ((J.kind[j] & JK_TYPE) == JOINT_CONE) {
         cone_setup(w, J, j, a, b);
+        return;
+    }
+    if ((J.kind[j] & JK_TYPE) == JOINT_SLIDER) {
+        slider_setup(w, J, j, a, b);
         return;
     }
     const Xf xa = joint_xf(w, a), xb = joint_xf(w, b);
@@ -1555,6 +1621,92 @@ JBD void cone_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
     __stcg(H + 6, lim);
 }
 
+// SliderConstraint.solveConstraintInt (SliderConstraint.java:528-685) on the bodies in the roles
+// the setup gave them.
+JBD void slider_solve(const DevWorld& w, const DevJoints& J, int j, float dt) {
+    const bool useA = J.set[j].x != 0.0f;
+    const int ia = useA ? J.a[j] : J.b[j], ib = useA ? J.b[j] : J.a[j];
+    V vA = mk(0.0f, 0.0f, 0.0f), wA = vA, vB = vA, wB = vA;
+    if (ia >= 0) gload(w, ia, vA, wA);
+    if (ib >= 0) gload(w, ib, vB, wB);
+    const float imA = ia >= 0 ? w.iloc[ia].w : 0.0f, imB = ib >= 0 ? w.iloc[ib].w : 0.0f;
+    const M IA = joint_iw(w, ia), IB = joint_iw(w, ib);
+    const float4* P = J.d6set + D6_SET_F4 * j;
+    float4* H = J.hs + JOINT_STEP_F4 * j;
+    // parameters: [0] limits, then (soft, rest, damp) of dir lin, dir ang, lim lin, lim ang, ortho lin,
+    // ortho ang from float 4, then lin motor (on, target, max), ang motor (on, target, max)
+    const float* p = &P[0].x;
+    auto soft = [&](int k) { return p[4 + 3 * k]; };
+    auto rest = [&](int k) { return p[5 + 3 * k]; };
+    auto damp = [&](int k) { return p[6 + 3 * k]; };
+    const float4 h3 = H[3], h4 = H[4], h5 = H[5], h6 = H[6], h7 = H[7];
+    const V relA = mk(h3.x, h3.y, h3.z), relB = mk(h4.x, h4.y, h4.z);
+    const float depthv[3] = {h3.w, h4.w, h5.w};
+    float4 acc = __ldcg(H + 8);
+    const V vel = sub(add(crs(wA, relA), vA), add(crs(wB, relB), vB));
+    for (int i = 0; i < 3; i++) {
+        const float4 h = H[i];
+        const V n = mk(h.x, h.y, h.z);
+        const float relVel = dot(n, vel);
+        const int k = i != 0 ? 4 : (h7.x != 0.0f ? 2 : 0);
+        float ni = __fmul_rn(__fmul_rn(soft(k), __fsub_rn(jdiv(__fmul_rn(rest(k), depthv[i]), dt), __fmul_rn(damp(k), relVel))),
+                             h.w);
+        V iv = scl(n, ni);
+        body_impulse(vA, wA, imA, IA, iv, relA);
+        body_impulse(vB, wB, imB, IB, scl(iv, -1.0f), relB);
+        if (p[22] != 0.0f && i == 0 && acc.x < p[24]) {
+            ni = __fmul_rn(-__fadd_rn(p[23], relVel), h.w);
+            float newAcc = __fadd_rn(acc.x, fabsf(ni));
+            if (newAcc > p[24]) newAcc = p[24];
+            const float del = __fsub_rn(newAcc, acc.x);
+            ni = ni < 0.0f ? -del : del;
+            acc.x = newAcc;
+            iv = scl(n, ni);
+            body_impulse(vA, wA, imA, IA, iv, relA);
+            body_impulse(vB, wB, imB, IB, scl(iv, -1.0f), relB);
+        }
+    }
+    const V axisA = mk(h5.x, h5.y, h5.z), axisB = mk(h6.x, h6.y, h6.z);
+    const float kAngle = h6.w;
+    const V angVelA = wA, angVelB = wB;
+    const V aroundA = scl(axisA, dot(axisA, angVelA)), aroundB = scl(axisB, dot(axisB, angVelB));
+    V vro = sub(sub(angVelA, aroundA), sub(angVelB, aroundB));
+    if (len(vro) > 0.00001f) {
+        const V n = nor(vro);
+        const float denom = __fadd_rn(ang_denom(IA, n), ang_denom(IB, n));
+        vro = scl(vro, __fmul_rn(__fmul_rn(jdiv(1.0f, denom), damp(5)), soft(5)));
+    }
+    V err = scl(crs(axisA, axisB), jdiv(1.0f, dt));
+    if (len(err) > 0.00001f) {
+        const V n2 = nor(err);
+        const float denom2 = __fadd_rn(ang_denom(IA, n2), ang_denom(IB, n2));
+        err = scl(err, __fmul_rn(__fmul_rn(jdiv(1.0f, denom2), rest(5)), soft(5)));
+    }
+    torque_impulse(wA, imA, IA, add(scl(vro, -1.0f), err));
+    torque_impulse(wB, imB, IB, sub(vro, err));
+    const int k = h7.z != 0.0f ? 3 : 1;
+    float mag = __fadd_rn(__fmul_rn(dot(sub(angVelB, angVelA), axisA), damp(k)), jdiv(__fmul_rn(h7.y, rest(k)), dt));
+    mag = __fmul_rn(mag, __fmul_rn(kAngle, soft(k)));
+    const V imp = scl(axisA, mag);
+    torque_impulse(wA, imA, IA, imp);
+    torque_impulse(wB, imB, IB, scl(imp, -1.0f));
+    if (p[25] != 0.0f && acc.y < p[27]) {
+        const float projRelVel = dot(sub(aroundA, aroundB), axisA);
+        float ai = __fmul_rn(kAngle, __fsub_rn(p[26], projRelVel));
+        float newAcc = __fadd_rn(acc.y, fabsf(ai));
+        if (newAcc > p[27]) newAcc = p[27];
+        const float del = __fsub_rn(newAcc, acc.y);
+        ai = ai < 0.0f ? -del : del;
+        acc.y = newAcc;
+        const V mi = scl(axisA, ai);
+        torque_impulse(wA, imA, IA, mi);
+        torque_impulse(wB, imB, IB, scl(mi, -1.0f));
+    }
+    if (ia >= 0 && imA != 0.0f) gstore(w, ia, vA, wA);
+    if (ib >= 0 && imB != 0.0f) gstore(w, ib, vB, wB);
+    __stcg(H + 8, acc);
+}
+
 // write-back (java:901-912): appliedImpulse; appliedImpulseLateral1 ends as friction row 2's
 JBD void writeback_slot(const DevPairs& P, const DevRows& R, int s) {
     int p = R.slot_pair[s];
@@ -1801,6 +1953,7 @@ __global__ void __launch_bounds__(SOLVER_THREADS, 2) k_pgs(DevWorld w, DevPairs 
                         if (jt == JOINT_HINGE) hinge_solve(w, sb.J, j, dt);
                         else if (jt == JOINT_6DOF) d6_solve(w, sb.J, j, dt);
                         else if (jt == JOINT_CONE) cone_solve(w, sb.J, j, dt);
+                        else if (jt == JOINT_SLIDER) slider_solve(w, sb.J, j, dt);
                         else joint_solve(w, sb.J, j, dt);
                     }
                     grid_barrier(w.ctr, nb, barK);

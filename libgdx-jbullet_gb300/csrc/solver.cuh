@@ -21,6 +21,7 @@ constexpr int JOINT_P2P = 0;
 constexpr int JOINT_HINGE = 1;
 constexpr int JOINT_6DOF = 2;
 constexpr int JOINT_CONE = 3;
+constexpr int JOINT_SLIDER = 4;
 constexpr int JK_TYPE = 0xff;         // kind: type in the low byte, hinge switches above it
 constexpr int JK_ANGULAR_ONLY = 1 << 8;
 constexpr int JK_MOTOR = 1 << 9;
@@ -45,7 +46,8 @@ struct DevJoints {
                                   // calculated frame origins, the anchor, linear axes with 1/Adiag
                                   // (3), angular axes with 1/Adiag (3), (limit state, limit error)
                                   // per angular axis (2), accumulated linear and angular impulses
-    float4* d6set = nullptr;      // 6-dof settings (D6_SET_F4 each): linear lower xyz | use frame A,
+    float4* d6set = nullptr;      // slider: its 28 parameters (jbgpu_world_set_slider_params order);
+                                  // 6-dof settings (D6_SET_F4 each): linear lower xyz | use frame A,
                                   // upper xyz | softness, (damping, restitution), then per angular axis
                                   // (lo, hi, target velocity, max motor force), (max limit force,
                                   // damping, softness, ERP), (bounce, motor enabled)

@@ -1387,6 +1387,43 @@ int jbgpu_world_set_cone_twist_angular_only(jbgpu_world* w, int32_t id, int32_t 
     return JBGPU_OK;
 }
 
+// SliderConstraint.initParams (SliderConstraint.java:139-172) in jbgpu_world_set_slider_params order.
+static const float kSliderDefaults[JBGPU_SLIDER_PARAMS] = {
+    1.0f, -1.0f, 0.0f, 0.0f,            // lower / upper linear limit, lower / upper angular limit
+    1.0f, 0.7f, 0.0f, 1.0f, 0.7f, 0.0f, // softness, restitution, damping: dir lin, dir ang
+    1.0f, 0.7f, 1.0f, 1.0f, 0.7f, 1.0f, // lim lin, lim ang
+    1.0f, 0.7f, 1.0f, 1.0f, 0.7f, 1.0f, // ortho lin, ortho ang
+    0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f  // linear motor (on, target velocity, max force), angular motor
+};
+
+int jbgpu_world_add_slider(jbgpu_world* w, int32_t a, int32_t b, const float fa[12], const float fb[12],
+                           int32_t useLinearReferenceFrameA, int32_t* id) {
+    int32_t k = -1;
+    int rc = jbgpu_world_add_hinge(w, a, b, fa, fb, &k);
+    if (rc) return rc;
+    w->jKind[k] = JOINT_SLIDER;
+    w->jSet[k] = make_float4(useLinearReferenceFrameA ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
+    w->jSet2[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    std::memcpy(&w->jD6[(size_t)k * D6_SET_F4], kSliderDefaults, sizeof(kSliderDefaults));
+    if (id) *id = k;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_slider_params(jbgpu_world* w, int32_t id, const float* params) {
+    if (!w || id < 0 || id >= (int)w->jA.size() || !params) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
+    if ((w->jKind[id] & JK_TYPE) != JOINT_SLIDER) return fail(JBGPU_ERR_INVALID_ARGUMENT, "not a slider");
+    std::memcpy(&w->jD6[(size_t)id * D6_SET_F4], params, sizeof(float) * JBGPU_SLIDER_PARAMS);
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_get_slider_params(jbgpu_world* w, int32_t id, float* params) {
+    if (!w || id < 0 || id >= (int)w->jA.size() || !params) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
+    if ((w->jKind[id] & JK_TYPE) != JOINT_SLIDER) return fail(JBGPU_ERR_INVALID_ARGUMENT, "not a slider");
+    std::memcpy(params, &w->jD6[(size_t)id * D6_SET_F4], sizeof(float) * JBGPU_SLIDER_PARAMS);
+    return JBGPU_OK;
+}
+
 static int d6_id(jbgpu_world* w, int32_t id) {
     if (!w || id < 0 || id >= (int)w->jA.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
     if ((w->jKind[id] & JK_TYPE) != JOINT_6DOF) return fail(JBGPU_ERR_INVALID_ARGUMENT, "not a generic 6-dof joint");

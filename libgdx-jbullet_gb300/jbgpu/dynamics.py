@@ -384,6 +384,56 @@ class ConeTwistConstraint:
         return float(self._world._g.joint_impulses()[self._id])
 
 
+class SliderConstraint:
+    """dynamics/constraintsolver/SliderConstraint.java:130-685: SliderConstraint(rbA, rbB, frameInA,
+    frameInB, useLinearReferenceFrameA) with the reference's setters (limits, the softness /
+    restitution / damping of its six row groups, the two motors); changes are sent before the
+    next step."""
+
+    _names = ["LowerLinLimit", "UpperLinLimit", "LowerAngLimit", "UpperAngLimit"]
+    for _g in ("DirLin", "DirAng", "LimLin", "LimAng", "OrthoLin", "OrthoAng"):
+        _names += ["Softness" + _g, "Restitution" + _g, "Damping" + _g]
+    _names += ["PoweredLinMotor", "TargetLinMotorVelocity", "MaxLinMotorForce", "PoweredAngMotor",
+               "TargetAngMotorVelocity", "MaxAngMotorForce"]
+
+    def __init__(self, rbA, rbB, frameInA, frameInB, useLinearReferenceFrameA):
+        self.rbA, self.rbB = rbA, rbB
+        self.frameInA = Transform(frameInA.basis.copy(), frameInA.origin.copy())
+        self.frameInB = Transform(frameInB.basis.copy(), frameInB.origin.copy())
+        self.useLinearReferenceFrameA = bool(useLinearReferenceFrameA)
+        self.params = np.array([1.0, -1.0, 0.0, 0.0] + [1.0, 0.7, 0.0] * 2 + [1.0, 0.7, 1.0] * 4 + [0.0] * 6, np.float32)
+        self._world = None
+        self._id = None
+        self._sent = None
+
+    def __getattr__(self, name):
+        for prefix in ("set", "get"):
+            if name.startswith(prefix) and name[3:] in SliderConstraint._names:
+                k = SliderConstraint._names.index(name[3:])
+                if prefix == "set":
+                    return lambda v: self.params.__setitem__(k, float(v))
+                return lambda: (bool(self.params[k]) if name[3:].startswith("Powered") else float(self.params[k]))
+        raise AttributeError(name)
+
+    def _push(self):
+        g = self._world._g if self._world is not None else None
+        if g is None or self._id is None:
+            return
+        if self._sent is not None and np.array_equal(self._sent, self.params):
+            return
+        g.set_slider_params(self._id, self.params)
+        self._sent = self.params.copy()
+
+    def getRigidBodyA(self):
+        return self.rbA
+
+    def getRigidBodyB(self):
+        return self.rbB
+
+    def getAppliedImpulse(self):
+        return 0.0    # the reference's slider leaves TypedConstraint.appliedImpulse at 0
+
+
 class RotationalLimitMotor:
     """dynamics/constraintsolver/RotationalLimitMotor.java:44-70 (settings; defaults as there)."""
 
@@ -574,6 +624,11 @@ class DiscreteDynamicsWorld:
                 c._id = self._g.add_hinge(c.rbA._index, b, c.frameA.as12(), c.frameB.as12())
                 c._push()
                 continue
+            if isinstance(c, SliderConstraint):
+                c._id = self._g.add_slider(c.rbA._index, b, c.frameInA.as12(), c.frameInB.as12(),
+                                           c.useLinearReferenceFrameA)
+                c._push()
+                continue
             if isinstance(c, ConeTwistConstraint):
                 c._id = self._g.add_cone_twist(c.rbA._index, b, c.frameA.as12(), c.frameB.as12())
                 c._push()
@@ -642,7 +697,7 @@ class DiscreteDynamicsWorld:
     def stepSimulation(self, timeStep, maxSubSteps=1, fixedTimeStep=1.0 / 60.0):
         g = self._ensure()
         for c in self._constraints:
-            if isinstance(c, Generic6DofConstraint):
+            if isinstance(c, (Generic6DofConstraint, SliderConstraint)):
                 c._push()
         if self._forces is not None:
             g.apply_forces(self._forces)

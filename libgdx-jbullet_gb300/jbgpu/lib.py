@@ -69,6 +69,10 @@ def lib():
                                            C.c_int),
             "jbgpu_world_set_cone_twist_limit": ([C.c_void_p, C.c_int32] + [C.c_float] * 6, C.c_int),
             "jbgpu_world_set_cone_twist_angular_only": ([C.c_void_p, C.c_int32, C.c_int32], C.c_int),
+            "jbgpu_world_add_slider": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.c_int32,
+                                       C.POINTER(C.c_int32)], C.c_int),
+            "jbgpu_world_set_slider_params": ([C.c_void_p, C.c_int32, _abi.f32p], C.c_int),
+            "jbgpu_world_get_slider_params": ([C.c_void_p, C.c_int32, _abi.f32p], C.c_int),
             "jbgpu_world_add_generic6dof": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.c_int32,
                                             C.POINTER(C.c_int32)], C.c_int),
             "jbgpu_world_set_6dof_limit": ([C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_float], C.c_int),
@@ -117,6 +121,7 @@ EXPORTED = [
     "jbgpu_world_set_ray_replay", "jbgpu_world_set_graph", "jbgpu_world_graph_status", "jbgpu_world_add_generic6dof",
     "jbgpu_world_set_6dof_limit", "jbgpu_world_set_6dof_linear_motor", "jbgpu_world_set_6dof_angular_motor",
     "jbgpu_world_add_cone_twist", "jbgpu_world_set_cone_twist_limit", "jbgpu_world_set_cone_twist_angular_only",
+    "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
 ]
 
 
@@ -295,6 +300,24 @@ class GpuWorld:
     def set_ray_replay(self, all_rays):
         check(lib().jbgpu_world_set_ray_replay(self.h, 1 if all_rays else 0))
 
+    def add_slider(self, a, b, frame_a, frame_b, use_linear_reference_frame_a=True):
+        """Slider joint with frames as 12 floats each (basis row-major, origin); returns its id."""
+        fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
+        fb = np.ascontiguousarray(frame_b, np.float32).reshape(12)
+        jid = C.c_int32()
+        check(lib().jbgpu_world_add_slider(self.h, a, b, fa.ctypes.data_as(_abi.f32p), fb.ctypes.data_as(_abi.f32p),
+                                           1 if use_linear_reference_frame_a else 0, C.byref(jid)))
+        return jid.value
+
+    def slider_params(self, jid):
+        p = np.zeros(28, np.float32)
+        check(lib().jbgpu_world_get_slider_params(self.h, jid, p.ctypes.data_as(_abi.f32p)))
+        return p
+
+    def set_slider_params(self, jid, params):
+        p = np.ascontiguousarray(params, np.float32).reshape(28)
+        check(lib().jbgpu_world_set_slider_params(self.h, jid, p.ctypes.data_as(_abi.f32p)))
+
     def add_cone_twist(self, a, b, frame_a, frame_b):
         """Cone-twist joint with frames as 12 floats each (basis row-major, origin); returns its id."""
         fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
@@ -333,6 +356,11 @@ class GpuWorld:
 
     def add_scene_joints(self, scene):
         for j in scene.meta.get("joints", []):
+            if j.get("type") == "slider":
+                jid = self.add_slider(j["a"], j["b"], j["frame_a"], j["frame_b"], j.get("use_a", True))
+                if "params" in j:
+                    self.set_slider_params(jid, j["params"])
+                continue
             if j.get("type") == "cone":
                 jid = self.add_cone_twist(j["a"], j["b"], j["frame_a"], j["frame_b"])
                 if "limit" in j:

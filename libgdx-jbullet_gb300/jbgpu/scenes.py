@@ -605,6 +605,81 @@ def cone_chains(chains=6, links=5, loose=8, seed=0, spacing=2.5, top=10.0, steps
                  meta={"seed": seed, "joints": joints}, **kw)
 
 
+def slider_rigs(rigs=6, loose=8, seed=0, spacing=2.5, steps=240, worlds=1):
+    """Boxes (half 0.3, mass 1) on slider joints to static rails (half 1.2 x 0.05 x 0.05) one
+    metre above them, sliding along the rail's x.  Rig r: r % 3 == 0 linear limits [-1, 1],
+    rotation locked (the defaults' angular limits 0, 0); 1 a powered linear motor and a powered
+    angular motor, linear limits [-1.5, 1.5], rotation about the axis free; 2 a vertical rail,
+    useLinearReferenceFrameA false with the box as body A, default parameters (free along the
+    rail).  Loose boxes fall beside the rigs.  meta["joints"]: type "slider", a, b, frame_a,
+    frame_b, use_a, optional params (28 floats, jbgpu_world_set_slider_params order)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE), {"type": _abi.SHAPE_BOX, "params": (0.3, 0.3, 0.3, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (1.2, 0.05, 0.05, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.05, 1.2, 0.05, 0.0), "points": None}]
+    defaults = [1.0, -1.0, 0.0, 0.0, 1.0, 0.7, 0.0, 1.0, 0.7, 0.0, 1.0, 0.7, 1.0, 1.0, 0.7, 1.0, 1.0, 0.7, 1.0,
+                1.0, 0.7, 1.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0]
+    side = int(np.ceil(np.sqrt(rigs)))
+    ident = np.eye(3, dtype=F).reshape(9)
+    vert = np.array([[0, -1, 0], [1, 0, 0], [0, 0, 1]], F).reshape(9)    # columns: x up
+    all_bodies, joints, wid = [], [], []
+    base = 0
+    for wi in range(worlds):
+        plane = _plane_body(0)
+        rails = _bodies(rigs)
+        boxes = _bodies(rigs)
+        boxes["shape"] = 1
+        boxes["mass"] = 1.0
+        boxes["local_inertia"] = box_inertia(1.0, (0.3, 0.3, 0.3))
+        for r in range(rigs):
+            x0, z0 = (r % side - (side - 1) / 2.0) * spacing, (r // side - (side - 1) / 2.0) * spacing
+            if r % 3 == 2:
+                rails["shape"][r] = 3
+                rails["transform"][r, 9:] = (x0 + 0.5, 3.0, z0)
+                boxes["transform"][r, 9:] = (x0, 3.5, z0)
+                boxes["linear_velocity"][r] = (0.0, rng.normal(0.0, 1.0), 0.0)
+            else:
+                rails["shape"][r] = 2
+                rails["transform"][r, 9:] = (x0, 4.0, z0)
+                boxes["transform"][r, 9:] = (x0, 3.0, z0)
+                boxes["linear_velocity"][r] = (rng.normal(0.0, 2.0), 0.0, 0.0)
+        half = side * spacing / 2.0
+        fb = _bodies(loose)
+        fb["shape"] = 1
+        fb["mass"] = 1.0
+        fb["local_inertia"] = box_inertia(1.0, (0.3, 0.3, 0.3))
+        fpos = np.stack([rng.uniform(half + 1.0, half + 4.0, loose), rng.uniform(1.0, 6.0, loose),
+                         rng.uniform(-half, half, loose)], 1)
+        _set_transforms(fb, random_rotations(rng, loose), fpos)
+        bodies = np.concatenate([plane, rails, boxes, fb])
+        fr, fx = base + 1, base + 1 + rigs
+        for r in range(rigs):
+            if r % 3 == 2:
+                joints.append({"type": "slider", "a": fx + r, "b": fr + r, "use_a": False,
+                               "frame_a": np.concatenate([vert, [0.0, 0.0, 0.0]]).astype(F),
+                               "frame_b": np.concatenate([vert, [-0.5, 0.0, 0.0]]).astype(F)})
+                continue
+            p = list(defaults)
+            if r % 3 == 0:
+                p[0], p[1] = -1.0, 1.0
+            else:
+                p[0], p[1], p[2], p[3] = -1.5, 1.5, 1.0, -1.0
+                p[22], p[23], p[24] = 1.0, 1.0, 5.0
+                p[25], p[26], p[27] = 1.0, 2.0, 3.0
+            joints.append({"type": "slider", "a": fr + r, "b": fx + r, "use_a": True,
+                           "frame_a": np.concatenate([ident, [0.0, -1.0, 0.0]]).astype(F),
+                           "frame_b": np.concatenate([ident, [0.0, 0.0, 0.0]]).astype(F), "params": p})
+        all_bodies.append(bodies)
+        wid.append(np.full(len(bodies), wi, np.int32))
+        base += len(bodies)
+    bodies = np.concatenate(all_bodies)
+    bodies["world"] = np.concatenate(wid)
+    kw = {"world_of_body": np.concatenate(wid)} if worlds > 1 else {}
+    return Scene("slider_rigs_%d_w%d" % (rigs, worlds), 1.0 / 60.0, steps,
+                 {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10}, shapes, bodies,
+                 meta={"seed": seed, "joints": joints}, **kw)
+
+
 def small_mixed(n=60, seed=0, region=(6.0, 8.0, 6.0), steps=200, with_hulls=True):
     """A small dense mix of every shape type for stage-by-stage parity checks."""
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -689,4 +764,5 @@ SCENES = {
     "hinged_chains": hinged_chains,
     "sixdof_chains": sixdof_chains,
     "cone_chains": cone_chains,
+    "slider_rigs": slider_rigs,
 }

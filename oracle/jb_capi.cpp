@@ -207,6 +207,23 @@ void orc_set_cone_limit(void* h, int id, float swing1, float swing2, float twist
     j.biasFactor = bias;
     j.relaxationFactor = relaxation;
 }
+int orc_add_slider(void* h, int a, int b, const float* frameA, const float* frameB, int useA) {
+    int id = orc_add_hinge(h, a, b, frameA, frameB);
+    Joint& j = ((World*)h)->joints[id];
+    j.type = JOINT_SLIDER;
+    j.useLinearReferenceFrameA = useA != 0;
+    return id;
+}
+// p: lowerLin, upperLin, lowerAng, upperAng, then softness / restitution / damping for dir lin, dir
+// ang, lim lin, lim ang, ortho lin, ortho ang (18), then lin motor on, target, max force, ang motor
+// on, target, max force
+void orc_set_slider_params(void* h, int id, const float* p) {
+    SliderParams& P = ((World*)h)->joints[id].slider;
+    P.lowerLin = p[0]; P.upperLin = p[1]; P.lowerAng = p[2]; P.upperAng = p[3];
+    for (int k = 0; k < 6; k++) { P.soft[k] = p[4 + 3 * k]; P.rest[k] = p[5 + 3 * k]; P.damp[k] = p[6 + 3 * k]; }
+    P.linMotor = p[22] != 0.0f; P.linTarget = p[23]; P.linMaxForce = p[24];
+    P.angMotor = p[25] != 0.0f; P.angTarget = p[26]; P.angMaxForce = p[27];
+}
 int orc_get_joint_impulses(void* h, float* out, int cap) {
     const World* w = (const World*)h;
     const int n = (int)w->joints.size();

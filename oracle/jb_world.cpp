@@ -889,6 +889,116 @@ static void cone_solve(Joint& j, Body& A, Body& B, float timeStep) {
     }
 }
 
+// SliderConstraint.buildJacobianInt (SliderConstraint.java:465-526) with testLinLimits (714-730)
+// and testAngLimits (732-756); "A" and "B" are the joint's bodies, swapped when
+// useLinearReferenceFrameA is false (buildJacobian, java:175-182).
+static void slider_build(Joint& j, const Body& A, const Body& B, const M3& frA, V3 oA, const M3& frB, V3 oB) {
+    Xf fA, fB;
+    fA.b = frA; fA.o = oA;
+    fB.b = frB; fB.o = oB;
+    j.calcA = xf_mul(A.xf, fA);
+    j.calcB = xf_mul(B.xf, fB);
+    V3 pivA = j.calcA.o, pivB = j.calcB.o;
+    V3 axis = col(j.calcA.b, 0);
+    V3 delta = sub(pivB, pivA);
+    V3 proj = v3(pivA.x + dot(axis, delta) * axis.x, pivA.y + dot(axis, delta) * axis.y, pivA.z + dot(axis, delta) * axis.z);
+    j.slRelA = sub(proj, A.xf.o);
+    j.slRelB = sub(pivB, B.xf.o);
+    M3 w2A = transpose(A.xf.b), w2B = transpose(B.xf.b);
+    for (int i = 0; i < 3; i++) {
+        V3 n = col(j.calcA.b, i);
+        V3 aJ = mulMv(crs(j.slRelA, n), w2A);
+        V3 bJ = mulMv(crs(j.slRelB, j.slRelB), w2B);
+        V3 m0 = mulc(A.invInertiaLocal, aJ), m1 = mulc(B.invInertiaLocal, bJ);
+        j.slInv[i] = 1.0f / (A.invMass + dot(m0, aJ) + B.invMass + dot(m1, bJ));
+        set_coord(j.slDepth, i, dot(delta, n));
+    }
+    const SliderParams& P = j.slider;
+    j.slSolveLin = false;
+    if (P.lowerLin <= P.upperLin) {
+        if (j.slDepth.x > P.upperLin) { j.slDepth.x -= P.upperLin; j.slSolveLin = true; }
+        else if (j.slDepth.x < P.lowerLin) { j.slDepth.x -= P.lowerLin; j.slSolveLin = true; }
+        else j.slDepth.x = 0.0f;
+    } else {
+        j.slDepth.x = 0.0f;
+    }
+    j.slAngDepth = 0.0f;
+    j.slSolveAng = false;
+    if (P.lowerAng <= P.upperAng) {
+        V3 a0 = col(j.calcA.b, 1), a1 = col(j.calcA.b, 2), b0 = col(j.calcB.b, 1);
+        float rot = (float)std::atan2((double)dot(b0, a1), (double)dot(b0, a0));
+        if (rot < P.lowerAng) { j.slAngDepth = rot - P.lowerAng; j.slSolveAng = true; }
+        else if (rot > P.upperAng) { j.slAngDepth = rot - P.upperAng; j.slSolveAng = true; }
+    }
+    j.slKAngle = 1.0f / (ang_denom(A, axis) + ang_denom(B, axis));
+    j.slAccLin = 0.0f;
+    j.slAccAng = 0.0f;
+}
+
+// SliderConstraint.solveConstraintInt (SliderConstraint.java:528-685).
+static void slider_solve(Joint& j, Body& A, Body& B, float timeStep) {
+    const SliderParams& P = j.slider;
+    V3 vel = sub(add(crs(A.angvel, j.slRelA), A.linvel), add(crs(B.angvel, j.slRelB), B.linvel));
+    for (int i = 0; i < 3; i++) {
+        V3 n = col(j.calcA.b, i);
+        float relVel = dot(n, vel);
+        float depth = coord(j.slDepth, i);
+        int k = i != 0 ? SL_ORTHO_LIN : (j.slSolveLin ? SL_LIM_LIN : SL_DIR_LIN);
+        float normalImpulse = P.soft[k] * (P.rest[k] * depth / timeStep - P.damp[k] * relVel) * j.slInv[i];
+        V3 iv = scl(n, normalImpulse);
+        apply_impulse(A, iv, j.slRelA);
+        apply_impulse(B, scl(iv, -1.0f), j.slRelB);
+        if (P.linMotor && i == 0 && j.slAccLin < P.linMaxForce) {
+            float motorRelVel = P.linTarget + relVel;
+            normalImpulse = -motorRelVel * j.slInv[i];
+            float newAcc = j.slAccLin + std::fabs(normalImpulse);
+            if (newAcc > P.linMaxForce) newAcc = P.linMaxForce;
+            float del = newAcc - j.slAccLin;
+            normalImpulse = normalImpulse < 0.0f ? -del : del;
+            j.slAccLin = newAcc;
+            iv = scl(n, normalImpulse);
+            apply_impulse(A, iv, j.slRelA);
+            apply_impulse(B, scl(iv, -1.0f), j.slRelB);
+        }
+    }
+    V3 axisA = col(j.calcA.b, 0), axisB = col(j.calcB.b, 0);
+    V3 angVelA = A.angvel, angVelB = B.angvel;
+    V3 aroundA = scl(axisA, dot(axisA, angVelA)), aroundB = scl(axisB, dot(axisB, angVelB));
+    V3 velrelOrthog = sub(sub(angVelA, aroundA), sub(angVelB, aroundB));
+    if (len(velrelOrthog) > 0.00001f) {
+        V3 n = nor(velrelOrthog);
+        float denom = ang_denom(A, n) + ang_denom(B, n);
+        velrelOrthog = scl(velrelOrthog, (1.0f / denom) * P.damp[SL_ORTHO_ANG] * P.soft[SL_ORTHO_ANG]);
+    }
+    V3 angularError = scl(crs(axisA, axisB), 1.0f / timeStep);
+    if (len(angularError) > 0.00001f) {
+        V3 n2 = nor(angularError);
+        float denom2 = ang_denom(A, n2) + ang_denom(B, n2);
+        angularError = scl(angularError, (1.0f / denom2) * P.rest[SL_ORTHO_ANG] * P.soft[SL_ORTHO_ANG]);
+    }
+    apply_torque(A, add(scl(velrelOrthog, -1.0f), angularError));
+    apply_torque(B, sub(velrelOrthog, angularError));
+    int k = j.slSolveAng ? SL_LIM_ANG : SL_DIR_ANG;
+    float impulseMag = dot(sub(angVelB, angVelA), axisA) * P.damp[k] + j.slAngDepth * P.rest[k] / timeStep;
+    impulseMag *= j.slKAngle * P.soft[k];
+    V3 imp = scl(axisA, impulseMag);
+    apply_torque(A, imp);
+    apply_torque(B, scl(imp, -1.0f));
+    if (P.angMotor && j.slAccAng < P.angMaxForce) {
+        float projRelVel = dot(sub(aroundA, aroundB), axisA);
+        float motorRelVel = P.angTarget - projRelVel;
+        float angImpulse = j.slKAngle * motorRelVel;
+        float newAcc = j.slAccAng + std::fabs(angImpulse);
+        if (newAcc > P.angMaxForce) newAcc = P.angMaxForce;
+        float del = newAcc - j.slAccAng;
+        angImpulse = angImpulse < 0.0f ? -del : del;
+        j.slAccAng = newAcc;
+        V3 mi = scl(axisA, angImpulse);
+        apply_torque(A, mi);
+        apply_torque(B, scl(mi, -1.0f));
+    }
+}
+
 static void solve_group(World& w, const std::vector<int>& manifolds, const std::vector<int>& joints, float dt) {
     const Config& cfg = w.cfg;
     std::vector<SolverBody> sb;
@@ -1025,6 +1135,10 @@ static void solve_group(World& w, const std::vector<int>& manifolds, const std::
         if (J.type == JOINT_HINGE) hinge_build(J, jointBody(J.a), jointBody(J.b));
         else if (J.type == JOINT_6DOF) d6_build(J, jointBody(J.a), jointBody(J.b));
         else if (J.type == JOINT_CONE) cone_build(J, jointBody(J.a), jointBody(J.b));
+        else if (J.type == JOINT_SLIDER) {
+            if (J.useLinearReferenceFrameA) slider_build(J, jointBody(J.a), jointBody(J.b), J.frameA, J.pivotA, J.frameB, J.pivotB);
+            else slider_build(J, jointBody(J.b), jointBody(J.a), J.frameB, J.pivotB, J.frameA, J.pivotA);
+        }
         else joint_build(J, jointBody(J.a), jointBody(J.b));
     }
     // solveGroupCacheFriendlyIterations (java:788-890), split impulse off.  With a residual
@@ -1076,6 +1190,10 @@ static void solve_group(World& w, const std::vector<int>& manifolds, const std::
             if (J.type == JOINT_HINGE) hinge_solve(J, A, B, dt);
             else if (J.type == JOINT_6DOF) d6_solve(J, A, B, dt);
             else if (J.type == JOINT_CONE) cone_solve(J, A, B, dt);
+            else if (J.type == JOINT_SLIDER) {
+                if (J.useLinearReferenceFrameA) slider_solve(J, A, B, dt);
+                else slider_solve(J, B, A, dt);
+            }
             else joint_solve(J, A, B, dt);
             for (Body* b : {&A, &B})
                 if (b->islandTag >= 0 && b->companionId >= 0 && sb[b->companionId].invMass != 0.0f) {

@@ -98,7 +98,20 @@ struct Body {            // dynamics/RigidBody.java + collision/dispatch/Collisi
 // frameA / frameB (origins in pivotA / pivotB), swing spans, twist span, softness, bias and
 // relaxation in the hinge's limit fields (swing1 -> lowerLimit, swing2 -> upperLimit, twist ->
 // twistSpan).
-enum JointType { JOINT_P2P = 0, JOINT_HINGE = 1, JOINT_6DOF = 2, JOINT_CONE = 3 };
+// SliderConstraint (dynamics/constraintsolver/SliderConstraint.java:44-777): frames as for the
+// 6-dof joint, its parameters in `slider` (SliderParams), with useLinearReferenceFrameA == false
+// swapping the bodies' roles.
+enum JointType { JOINT_P2P = 0, JOINT_HINGE = 1, JOINT_6DOF = 2, JOINT_CONE = 3, JOINT_SLIDER = 4 };
+struct SliderParams {   // SliderConstraint.initParams (java:139-172)
+    float lowerLin = 1.0f, upperLin = -1.0f, lowerAng = 0.0f, upperAng = 0.0f;
+    // softness, restitution, damping of: dir lin, dir ang, lim lin, lim ang, ortho lin, ortho ang
+    float soft[6] = {1, 1, 1, 1, 1, 1};
+    float rest[6] = {0.7f, 0.7f, 0.7f, 0.7f, 0.7f, 0.7f};
+    float damp[6] = {0.0f, 0.0f, 1.0f, 1.0f, 1.0f, 1.0f};
+    bool linMotor = false, angMotor = false;
+    float linTarget = 0.0f, linMaxForce = 0.0f, angTarget = 0.0f, angMaxForce = 0.0f;
+};
+enum { SL_DIR_LIN = 0, SL_DIR_ANG, SL_LIM_LIN, SL_LIM_ANG, SL_ORTHO_LIN, SL_ORTHO_ANG };
 struct RotMotor {     // RotationalLimitMotor defaults
     float loLimit = -SIMD_INFINITY, hiLimit = SIMD_INFINITY, targetVelocity = 0.0f, maxMotorForce = 0.1f;
     float maxLimitForce = 300.0f, damping = 1.0f, limitSoftness = 0.5f, ERP = 0.5f, bounce = 0.0f;
@@ -127,6 +140,11 @@ struct Joint {
     float kSwing = 0.0f, kTwist = 0.0f, swingCorrection = 0.0f, twistCorrection = 0.0f;
     float accSwing = 0.0f, accTwist = 0.0f;
     bool solveSwing = false, solveTwist = false;
+    // slider
+    SliderParams slider;
+    V3 slRelA{0, 0, 0}, slRelB{0, 0, 0}, slDepth{0, 0, 0};
+    float slInv[3] = {0, 0, 0}, slAngDepth = 0.0f, slKAngle = 0.0f, slAccLin = 0.0f, slAccAng = 0.0f;
+    bool slSolveLin = false, slSolveAng = false;
     // generic 6-dof
     bool useLinearReferenceFrameA = true;
     V3 linLower{0, 0, 0}, linUpper{0, 0, 0}, linAcc{0, 0, 0};

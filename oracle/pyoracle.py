@@ -60,6 +60,8 @@ def lib():
         L.orc_set_6dof_angular_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_float] * 7
         L.orc_add_cone_twist.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
         L.orc_set_cone_limit.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 6
+        L.orc_add_slider.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p, C.c_int]
+        L.orc_set_slider_params.argtypes = [C.c_void_p, C.c_int, _abi.f32p]
         L.orc_add_hinge.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
         L.orc_set_hinge_limit.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 5
         L.orc_enable_hinge_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float]
@@ -159,8 +161,22 @@ class OracleWorld:
     def set_cone_limit(self, jid, swing1, swing2, twist, softness=0.8, bias_factor=0.3, relaxation_factor=1.0):
         lib().orc_set_cone_limit(self.h, jid, swing1, swing2, twist, softness, bias_factor, relaxation_factor)
 
+    def add_slider(self, a, b, frame_a, frame_b, use_linear_reference_frame_a=True):
+        fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
+        fb = np.ascontiguousarray(frame_b, np.float32).reshape(12)
+        return lib().orc_add_slider(self.h, a, b, _fp(fa), _fp(fb), 1 if use_linear_reference_frame_a else 0)
+
+    def set_slider_params(self, jid, params):
+        p = np.ascontiguousarray(params, np.float32).reshape(28)
+        lib().orc_set_slider_params(self.h, jid, _fp(p))
+
     def add_scene_joints(self, scene):
         for j in scene.meta.get("joints", []):
+            if j.get("type") == "slider":
+                jid = self.add_slider(j["a"], j["b"], j["frame_a"], j["frame_b"], j.get("use_a", True))
+                if "params" in j:
+                    self.set_slider_params(jid, j["params"])
+                continue
             if j.get("type") == "cone":
                 jid = self.add_cone_twist(j["a"], j["b"], j["frame_a"], j["frame_b"])
                 if "limit" in j:

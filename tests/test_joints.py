@@ -458,3 +458,68 @@ def test_gpu_cone_twist_bit_exact(gpu_lib, oracle_lib, case):
             assert np.array_equal(o.joint_impulses().view(np.uint32), g.joint_impulses().view(np.uint32)), s
     assert g.counters()["status_flags"] == 0
     g.close()
+
+
+# ---- slider joints (dynamics/constraintsolver/SliderConstraint.java) ------------------------
+def test_oracle_slider_rigs(oracle_lib):
+    """Limited sliders stop at their limits, the powered one is driven to its limit and spun
+    about the axis by its angular motor, the vertical free one slides down to the plane; every
+    box stays on its rail's axis."""
+    sc = scenes.slider_rigs(rigs=6, loose=8, seed=1)
+    J = sc.meta["joints"]
+    o = pyoracle.OracleWorld(sc)
+    for _ in range(240):
+        o.step(sc.dt)
+    assert o.counters()["status_flags"] == 0
+    st = o.get_state()
+    xf = st["transform"]
+    for r, j in enumerate(J):
+        box, rail = (j["b"], j["a"]) if j["use_a"] else (j["a"], j["b"])
+        if r % 3 == 2:
+            assert abs(xf[box, 9] - (xf[rail, 9] - 0.5)) < 0.02 and xf[box, 10] < 0.35     # on the plane
+        else:
+            off = xf[box, 9] - xf[rail, 9]
+            assert abs(xf[box, 10] - 3.0) < 0.02 and abs(xf[box, 11] - xf[rail, 11]) < 0.02
+            assert abs(abs(off) - (1.0 if r % 3 == 0 else 1.5)) < 0.03, off
+    assert abs(abs(st["angular_velocity"][J[1]["b"], 0]) - 2.0) < 0.05
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["world_part", "range_parts", "batched"])
+def test_gpu_slider_bit_exact(gpu_lib, oracle_lib, case):
+    if case == "batched":
+        sc = scenes.slider_rigs(rigs=6, loose=4, seed=14, worlds=3)
+    else:
+        sc = scenes.slider_rigs(rigs=9, loose=8, seed=15)
+    cfg = dict(sc.config)
+    if case == "range_parts":
+        cfg["solver_parts"] = 5
+    g = GpuWorld(sc, config=_abi.default_config(**cfg))
+    o = pyoracle.OracleWorld(sc)
+    for s in range(200):
+        g.step(sc.dt)
+        if case == "range_parts":
+            o.set_explicit_order(g.solver_order())
+        o.step(sc.dt)
+        assert o.counters()["status_flags"] == 0, s
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+            assert not bs and not bm, (s, bs, bm)
+    assert g.counters()["status_flags"] == 0
+    g.close()
+
+
+@pytest.mark.gpu
+def test_gpu_slider_params_roundtrip(gpu_lib):
+    sc = scenes.slider_rigs(rigs=1, loose=0, seed=16)
+    g = GpuWorld(sc)
+    p = g.slider_params(0)
+    assert p[0] == -1.0 and p[1] == 1.0 and p[5] == np.float32(0.7)
+    p[24] = 9.0
+    g.set_slider_params(0, p)
+    assert g.slider_params(0)[24] == 9.0
+    from jbgpu.lib import JbgpuError
+    with pytest.raises(JbgpuError):
+        g.set_6dof_limit(0, 0, 0.0, 1.0)                        # a slider is not a 6-dof joint
+    g.close()
