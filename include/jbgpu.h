@@ -284,6 +284,17 @@ int jbgpu_world_synchronize(jbgpu_world* world);
  * the call returns with the hits written. */
 int jbgpu_world_ray_test(jbgpu_world* world, const float* from, const float* to, const int32_t* ray_world, int32_t n,
                          int32_t filter_group, int32_t filter_mask, int32_t device_buffers, jbgpu_ray_hit* hits);
+/* CollisionWorld.convexSweepTest(castShape, convexFromWorld, convexToWorld,
+ * new ClosestConvexResultCallback(...)) for n sweeps of one cast shape
+ * (collision/dispatch/CollisionWorld.java:596-645, objectQuerySingle 391-490): shape is a convex
+ * shape id of the world; from and to hold n transforms of 12 floats (basis rows, then origin);
+ * sweep_world, filter_group, filter_mask, device_buffers and hits as for jbgpu_world_ray_test.
+ * Each hit's fraction is GjkConvexCast's time of impact, normal the normalised hit normal and
+ * point the hit point on the body.  A sweep whose path reaches a static plane gets body -2: the
+ * reference throws there (its concave branch calls a null caster). */
+int jbgpu_world_convex_sweep_test(jbgpu_world* world, int32_t shape, const float* from, const float* to,
+                                  const int32_t* sweep_world, int32_t n, int32_t filter_group, int32_t filter_mask,
+                                  int32_t device_buffers, jbgpu_ray_hit* hits);
 /* CUDA graphs for the step (no counterpart in the reference).  on != 0: every internal step
  * replays two captured graphs (the launches before the pair-count readback and those after it)
  * instead of launching its kernels one by one; results are bit-identical to the launch path.

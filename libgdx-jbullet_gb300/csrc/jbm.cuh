@@ -104,6 +104,22 @@ JBD Xf xf_mul(const Xf& a, const Xf& b) { Xf r; r.o = xf_apply(a, b.o); r.b = mu
 JBD V xf_invXform(const Xf& t, V in) { return mulMv(sub(in, t.o), transpose(t.b)); }
 
 struct Q { float x, y, z, w; };
+// MatrixUtil.invert (linearmath/MatrixUtil.java:362-395)
+JBD M m3_invert(const M& m) {
+    auto el = [&](int r, int c) { return coord(m.r[r], c); };
+    auto cofac = [&](int r1, int c1, int r2, int c2) {
+        return __fsub_rn(__fmul_rn(el(r1, c1), el(r2, c2)), __fmul_rn(el(r1, c2), el(r2, c1)));
+    };
+    const float co_x = cofac(1, 1, 2, 2), co_y = cofac(1, 2, 2, 0), co_z = cofac(1, 0, 2, 1);
+    const float det = __fadd_rn(__fadd_rn(__fmul_rn(el(0, 0), co_x), __fmul_rn(el(0, 1), co_y)), __fmul_rn(el(0, 2), co_z));
+    const float s = jdiv(1.0f, det);
+    M r;
+    r.r[0] = mk(__fmul_rn(co_x, s), __fmul_rn(cofac(0, 2, 2, 1), s), __fmul_rn(cofac(0, 1, 1, 2), s));
+    r.r[1] = mk(__fmul_rn(co_y, s), __fmul_rn(cofac(0, 0, 2, 2), s), __fmul_rn(cofac(0, 2, 1, 0), s));
+    r.r[2] = mk(__fmul_rn(co_z, s), __fmul_rn(cofac(0, 1, 2, 0), s), __fmul_rn(cofac(0, 0, 1, 1), s));
+    return r;
+}
+
 JBD Q qmul(Q a, Q o) {                  // libGDX Quaternion.mul: a * o
     Q r;
     r.x = __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(a.w, o.x), __fmul_rn(a.x, o.w)), __fmul_rn(a.y, o.z)), __fmul_rn(a.z, o.y));

@@ -444,6 +444,201 @@ __global__ void __launch_bounds__(SLOW_THREADS) k_rays_slow(DevWorld w, DevWorld
     }
 }
 
+// ---- convexSweepTest ------------------------------------------------------------------------
+// CollisionWorld.convexSweepTest with a ClosestConvexResultCallback (collision/dispatch/
+// CollisionWorld.java:596-645, objectQuerySingle 391-490).  The reference's object loop tests each
+// object's aabb, grown by the cast shape's temporal aabb, against the path of the origins with
+// the fixed bound 1 and keeps a GjkConvexCast hit when it is below the closest so far: the answer
+// is the smallest hit by (fraction, body), whatever the order.  One thread per (sweep, body).
+
+// TransformUtil.calculateVelocity / calculateDiffAxisAngle (linearmath/TransformUtil.java:105-153)
+// and CollisionShape.calculateTemporalAabb with getAngularMotionDisc (CollisionShape.java:44-121).
+__global__ void k_sweep_prep(DevWorld w, int shape, const float* from, const float* to, int n, float4* cmin,
+                             float4* cmax) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const float* f = from + 12 * q;
+    const float* t = to + 12 * q;
+    M b0, b1;
+    b0.r[0] = mk(f[0], f[1], f[2]); b0.r[1] = mk(f[3], f[4], f[5]); b0.r[2] = mk(f[6], f[7], f[8]);
+    b1.r[0] = mk(t[0], t[1], t[2]); b1.r[1] = mk(t[3], t[4], t[5]); b1.r[2] = mk(t[6], t[7], t[8]);
+    const V linVel = scl(sub(mk(t[9], t[10], t[11]), mk(f[9], f[10], f[11])), jdiv(1.0f, 1.0f));
+    const Q dorn = qnor(q_from_matrix(mulMM(b1, m3_invert(b0))));
+    const float angle = __fmul_rn(2.0f, (float)acos((double)dorn.w));
+    V axis = mk(dorn.x, dorn.y, dorn.z);
+    const float l2 = len2(axis);
+    axis = l2 < __fmul_rn(FLT_EPS, FLT_EPS) ? mk(1.0f, 0.0f, 0.0f) : scl(axis, jdiv(1.0f, jsqrt(l2)));
+    const V angVel = scl(axis, jdiv(angle, 1.0f));
+    Xf R;
+    R.b = m_from_quat(q_from_matrix(b0));
+    R.o = mk(0.0f, 0.0f, 0.0f);
+    V mn, mx;
+    shape_aabb(w.sh, shape, R, mn, mx);
+    const V lin = scl(linVel, 1.0f);
+    if (lin.x > 0.0f) mx.x = __fadd_rn(mx.x, lin.x); else mn.x = __fadd_rn(mn.x, lin.x);
+    if (lin.y > 0.0f) mx.y = __fadd_rn(mx.y, lin.y); else mn.y = __fadd_rn(mn.y, lin.y);
+    if (lin.z > 0.0f) mx.z = __fadd_rn(mx.z, lin.z); else mn.z = __fadd_rn(mn.z, lin.z);
+    Xf I;
+    I.b.r[0] = mk(1.0f, 0.0f, 0.0f); I.b.r[1] = mk(0.0f, 1.0f, 0.0f); I.b.r[2] = mk(0.0f, 0.0f, 1.0f);
+    I.o = mk(0.0f, 0.0f, 0.0f);
+    V bmin, bmax;
+    shape_aabb(w.sh, shape, I, bmin, bmax);
+    const float radius = __fmul_rn(len(sub(bmax, bmin)), 0.5f);
+    const float disc = __fadd_rn(radius, len(scl(add(bmin, bmax), 0.5f)));
+    const float am = __fmul_rn(__fmul_rn(len(angVel), disc), 1.0f);
+    cmin[q] = f4(sub(mn, mk(am, am, am)), 0.0f);
+    cmax[q] = f4(add(mx, mk(am, am, am)), 0.0f);
+}
+
+// GjkConvexCast.calcTimeOfImpact (collision/narrowphase/GjkConvexCast.java:67-185): conservative
+// advancement on GjkPairDetector distances without a penetration solver, through a PointCollector
+// that keeps its closest result across the calls.
+JBD bool gjk_convex_cast(const ShapeRef& sa, const Xf& fromA, V toA, const ShapeRef& sb, const Xf& tB, float& fraction,
+                         V& normal, V& hitPoint) {
+    const V r = sub(sub(toA, fromA.o), sub(tB.o, tB.o));
+    float lambda = 0.0f, lastLambda = 0.0f;
+    int numIter = 0;
+    bool has = false;
+    float cdist = 1e30f;
+    V cn = mk(0.0f, 0.0f, 0.0f), cp = cn;
+    Xf iA = fromA, iB = tB;
+    auto collect = [&]() {
+        const GjkPart g = gjk_part(sa, iA, sb, iB, SIMD_INFINITY);
+        if (g.isValid && g.distance < cdist) {
+            has = true;
+            cn = g.normalInB;
+            cp = add(g.pointOnB, g.offset);
+            cdist = g.distance;
+        }
+    };
+    collect();
+    if (!has) return false;
+    V c = cp, n = cn;
+    float dist = cdist;
+    while (dist > 0.001f) {
+        if (++numIter > 32) return false;
+        lambda = __fsub_rn(lambda, jdiv(dist, dot(r, n)));
+        if (lambda > 1.0f || lambda < 0.0f || lambda <= lastLambda) return false;
+        lastLambda = lambda;
+        iA.o = interp3(fromA.o, toA, lambda);
+        iB.o = interp3(tB.o, tB.o, lambda);
+        collect();
+        if (cdist < 0.0f) { fraction = lastLambda; normal = cn; hitPoint = cp; return true; }
+        c = cp;
+        n = cn;
+        dist = cdist;
+    }
+    if (dot(n, r) >= -0.04f) return false;   // DispatcherInfo.allowedCcdPenetration
+    fraction = lambda;
+    normal = n;
+    hitPoint = c;
+    return true;
+}
+
+JBD Xf xf12(const float* f) {
+    Xf t;
+    t.b.r[0] = mk(f[0], f[1], f[2]);
+    t.b.r[1] = mk(f[3], f[4], f[5]);
+    t.b.r[2] = mk(f[6], f[7], f[8]);
+    t.o = mk(f[9], f[10], f[11]);
+    return t;
+}
+
+// PICK == false: every (sweep, body) whose grown aabb the path enters runs the cast; the sweep's
+// smallest hit key by atomicMin, a static plane on the path flagged.  PICK == true: the body
+// holding the sweep's smallest hit runs its cast again and writes the record.
+template <bool PICK>
+__global__ void k_sweep(DevWorld w, DevWorld wq, int shape, const float* from, const float* to, const int* sweepWorld,
+                        int n, int group, int mask, const float4* cmin, const float4* cmax, unsigned long long* key,
+                        int* planeHit, jbgpu_ray_hit* out) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= w.nBodies) return;
+    const int bs = w.shape[b];
+    for (int q = blockIdx.y; q < n; q += gridDim.y) {
+        if (PICK && (key[q] == ~0ull || (int)((key[q] >> 1) & 0x7fffffffu) != b)) continue;
+        if (w.world[b] != (sweepWorld ? sweepWorld[q] : 0) || !passes_filter(w, b, group, mask)) continue;
+        const Xf fa = xf12(from + 12 * q);
+        const V ta = mk(to[12 * q + 9], to[12 * q + 10], to[12 * q + 11]);
+        const V mn = add(mk4(wq.amin[b]), mk4(cmin[q])), mx = add(mk4(wq.amax[b]), mk4(cmax[q]));
+        float enter, exit;
+        if (!ray_aabb_parts(fa.o, ta, mn, mx, enter, exit) || !(enter <= jmin(1.0f, exit))) continue;
+        if (w.sh.type[bs] == SHAPE_PLANE) {
+            if (!PICK) atomicOr(planeHit + q, 1);
+            continue;
+        }
+        float f;
+        V nrm, p;
+        if (!gjk_convex_cast(shape_ref(w.sh, shape), fa, ta, shape_ref(w.sh, bs), load_xf(w, b), f, nrm, p) ||
+            !(len2(nrm) > 0.0001f) || !(f < 1.0f))   // ClosestConvexResultCallback starts at closestHitFraction 1
+            continue;
+        if (!PICK) {
+            atomicMin(key + q, hit_key(f, b, 0));
+            continue;
+        }
+        jbgpu_ray_hit o;
+        o.body = b;
+        o.fraction = f;
+        const V nn = nor(nrm);
+        o.normal[0] = nn.x; o.normal[1] = nn.y; o.normal[2] = nn.z;
+        o.point[0] = p.x; o.point[1] = p.y; o.point[2] = p.z;
+        out[q] = o;
+    }
+}
+
+__global__ void k_sweep_finish(int n, const unsigned long long* key, const int* planeHit, jbgpu_ray_hit* out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    if (!planeHit[q] && key[q] != ~0ull) return;
+    jbgpu_ray_hit o;
+    o.body = planeHit[q] ? -2 : -1;
+    o.fraction = 1.0f;
+    o.normal[0] = o.normal[1] = o.normal[2] = 0.0f;
+    o.point[0] = o.point[1] = o.point[2] = 0.0f;
+    out[q] = o;
+}
+
+__global__ void k_count_flags(int n, const int* flag, int* count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) atomicAdd(count, 1);
+}
+
+int query_sweeps(const DevWorld& w, QueryBuffers& qb, int shape, const float* from, const float* to, const int* sweepWorld,
+                 int n, int group, int mask, jbgpu_ray_hit* hits, int* planeHits, cudaStream_t s) {
+    if (n <= 0) return JBGPU_OK;
+    if (n > qb.capSweeps) {
+        void* old[] = {qb.sweepMin, qb.sweepMax, qb.sweepKey, qb.sweepPlane};
+        for (void* p : old)
+            if (p) cudaFree(p);
+        qb.sweepMin = qb.sweepMax = nullptr;
+        qb.sweepKey = nullptr;
+        qb.sweepPlane = nullptr;
+        const int c = n > 2 * qb.capSweeps ? n : 2 * qb.capSweeps;
+        qb.capSweeps = 0;
+        if (cudaMalloc((void**)&qb.sweepMin, sizeof(float4) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.sweepMax, sizeof(float4) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.sweepKey, sizeof(unsigned long long) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.sweepPlane, sizeof(int) * (size_t)c) != cudaSuccess)
+            return JBGPU_ERR_CUDA;
+        qb.capSweeps = c;
+    }
+    cudaMemsetAsync(qb.sweepKey, 0xff, sizeof(unsigned long long) * n, s);
+    cudaMemsetAsync(qb.sweepPlane, 0, sizeof(int) * n, s);
+    DevWorld wq = w;
+    wq.amin = qb.qmin;
+    wq.amax = qb.qmax;
+    k_sweep_prep<<<gridn(n, 128), 128, 0, s>>>(w, shape, from, to, n, qb.sweepMin, qb.sweepMax); note_launch();
+    const dim3 grid(gridn(w.nBodies, 128), n < 65535 ? n : 65535);
+    k_sweep<false><<<grid, 128, 0, s>>>(w, wq, shape, from, to, sweepWorld, n, group, mask, qb.sweepMin, qb.sweepMax,
+                                         qb.sweepKey, qb.sweepPlane, hits); note_launch();
+    k_sweep<true><<<grid, 128, 0, s>>>(w, wq, shape, from, to, sweepWorld, n, group, mask, qb.sweepMin, qb.sweepMax,
+                                        qb.sweepKey, qb.sweepPlane, hits); note_launch();
+    k_sweep_finish<<<gridn(n, 128), 128, 0, s>>>(n, qb.sweepKey, qb.sweepPlane, hits); note_launch();
+    if (planeHits) {
+        k_count_flags<<<gridn(n, 256), 256, 0, s>>>(n, qb.sweepPlane, planeHits); note_launch();
+    }
+    return cudaGetLastError() == cudaSuccess ? JBGPU_OK : JBGPU_ERR_CUDA;
+}
+
 int query_prepare(const DevWorld& w, BroadphaseBuffers& bb, QueryBuffers& qb, cudaStream_t s) {
     if (w.nBodies > qb.capBodies) {
         if (qb.qmin) cudaFree(qb.qmin);
@@ -562,7 +757,7 @@ int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb,
 void query_free(QueryBuffers& qb) {
     void* ps[] = {qb.qmin, qb.qmax, qb.node, qb.visit, qb.slow, qb.slowCount, qb.from, qb.to, qb.rayWorld, qb.hits,
                   qb.rayCnt, qb.rayOff, qb.candTotal, qb.key, qb.enterJ, qb.undecided, qb.scanScratch, qb.cand, qb.hitA,
-                  qb.hitB};
+                  qb.hitB, qb.sweepMin, qb.sweepMax, qb.sweepKey, qb.sweepPlane};
     for (void* p : ps)
         if (p) cudaFree(p);
     qb = QueryBuffers();

@@ -1035,22 +1035,6 @@ JBD void hinge_setup(const DevWorld& w, const DevJoints& J, int j, int a, int b)
     H[5] = make_float4(sign, 0.0f, 0.0f, 0.0f);
 }
 
-// MatrixUtil.invert (linearmath/MatrixUtil.java:362-395)
-JBD M m3_invert(const M& m) {
-    auto el = [&](int r, int c) { return coord(m.r[r], c); };
-    auto cofac = [&](int r1, int c1, int r2, int c2) {
-        return __fsub_rn(__fmul_rn(el(r1, c1), el(r2, c2)), __fmul_rn(el(r1, c2), el(r2, c1)));
-    };
-    const float co_x = cofac(1, 1, 2, 2), co_y = cofac(1, 2, 2, 0), co_z = cofac(1, 0, 2, 1);
-    const float det = __fadd_rn(__fadd_rn(__fmul_rn(el(0, 0), co_x), __fmul_rn(el(0, 1), co_y)), __fmul_rn(el(0, 2), co_z));
-    const float s = jdiv(1.0f, det);
-    M r;
-    r.r[0] = mk(__fmul_rn(co_x, s), __fmul_rn(cofac(0, 2, 2, 1), s), __fmul_rn(cofac(0, 1, 1, 2), s));
-    r.r[1] = mk(__fmul_rn(co_y, s), __fmul_rn(cofac(0, 0, 2, 2), s), __fmul_rn(cofac(0, 2, 1, 0), s));
-    r.r[2] = mk(__fmul_rn(co_z, s), __fmul_rn(cofac(0, 1, 2, 0), s), __fmul_rn(cofac(0, 0, 1, 1), s));
-    return r;
-}
-
 // Generic6DofConstraint.matrixToEulerXYZ (Generic6DofConstraint.java:125-159): element `index` is
 // row index % 3, column index / 3; atan2 and asin in double precision, rounded to float.
 JBD V euler_xyz(const M& m) {

@@ -1597,6 +1597,60 @@ int jbgpu_world_ray_test(jbgpu_world* w, const float* from, const float* to, con
     return JBGPU_OK;
 }
 
+int jbgpu_world_convex_sweep_test(jbgpu_world* w, int32_t shape, const float* from, const float* to,
+                                  const int32_t* sweepWorld, int32_t n, int32_t group, int32_t mask, int32_t deviceBuffers,
+                                  jbgpu_ray_hit* hits) {
+    if (!w || n < 0 || (n > 0 && (!from || !to || !hits))) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad sweep arguments");
+    if (shape < 0 || shape >= (int)w->shapes.size() || w->shapes[shape].type == JBGPU_SHAPE_STATIC_PLANE)
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "the cast shape must be a convex shape of the world");
+    if (n == 0) return JBGPU_OK;
+    if (!deviceBuffers && sweepWorld)
+        for (int i = 0; i < n; i++)
+            if (sweepWorld[i] < 0 || sweepWorld[i] >= w->nWorlds) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad sweep world");
+    CK(cudaSetDevice(w->device));
+    int rc = prepare(w);
+    if (rc) return rc;
+    cudaStream_t s = w->stream;
+    if (w->nBodies == 0) {
+        jbgpu_ray_hit miss;
+        std::memset(&miss, 0, sizeof(miss));
+        miss.body = -1;
+        miss.fraction = 1.0f;
+        if (deviceBuffers) {
+            std::vector<jbgpu_ray_hit> m(n, miss);
+            CK(cudaMemcpyAsync(hits, m.data(), sizeof(jbgpu_ray_hit) * n, cudaMemcpyHostToDevice, s));
+            CK(cudaStreamSynchronize(s));
+        } else {
+            std::fill(hits, hits + n, miss);
+        }
+        return JBGPU_OK;
+    }
+    DevWorld d = dev_view(w);
+    QueryBuffers& Q = w->qb;
+    rc = query_prepare(d, w->bb, Q, s);
+    if (rc) return fail(rc, "sweep query preparation failed");
+    if (deviceBuffers) {
+        rc = query_sweeps(d, Q, shape, from, to, sweepWorld, n, group, mask, hits, nullptr, s);
+        return rc ? fail(rc, "sweep query failed") : JBGPU_OK;
+    }
+    float *df = nullptr, *dt = nullptr;
+    int* dw = nullptr;
+    jbgpu_ray_hit* dh = nullptr;
+    cudaError_t e = dalloc(&df, 12 * (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&dt, 12 * (size_t)n);
+    if (e == cudaSuccess && sweepWorld) e = dalloc(&dw, (size_t)n);
+    if (e == cudaSuccess) e = dalloc(&dh, (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(df, from, sizeof(float) * 12 * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dt, to, sizeof(float) * 12 * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && sweepWorld) e = cudaMemcpyAsync(dw, sweepWorld, sizeof(int) * n, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) rc = query_sweeps(d, Q, shape, df, dt, dw, n, group, mask, dh, nullptr, s);
+    if (e == cudaSuccess && !rc) e = cudaMemcpyAsync(hits, dh, sizeof(jbgpu_ray_hit) * n, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    dfree(df); dfree(dt); dfree(dw); dfree(dh);
+    if (e != cudaSuccess) return fail(JBGPU_ERR_CUDA, cudaGetErrorString(e));
+    return rc ? fail(rc, "sweep query failed") : JBGPU_OK;
+}
+
 int jbgpu_world_set_graph(jbgpu_world* w, int32_t on) {
     if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
     CK(cudaSetDevice(w->device));

@@ -551,6 +551,23 @@ class ClosestRayResultCallback:
         return self.collisionObject is not None
 
 
+class ClosestConvexResultCallback:
+    """CollisionWorld.ClosestConvexResultCallback (collision/dispatch/CollisionWorld.java:794-836)."""
+
+    def __init__(self, convexFromWorld, convexToWorld):
+        self.convexFromWorld = np.asarray(convexFromWorld, np.float32).reshape(3).copy()
+        self.convexToWorld = np.asarray(convexToWorld, np.float32).reshape(3).copy()
+        self.closestHitFraction = 1.0
+        self.hitCollisionObject = None
+        self.collisionFilterGroup = 1
+        self.collisionFilterMask = -1
+        self.hitNormalWorld = np.zeros(3, np.float32)
+        self.hitPointWorld = np.zeros(3, np.float32)
+
+    def hasHit(self):
+        return self.hitCollisionObject is not None
+
+
 class DiscreteDynamicsWorld:
     def __init__(self, dispatcher=None, pairCache=None, constraintSolver=None, collisionConfiguration=None, device=0):
         self._gravity = (0.0, -10.0, 0.0)
@@ -716,6 +733,29 @@ class DiscreteDynamicsWorld:
         if h["body"] >= 0:
             cb.closestHitFraction = float(h["fraction"])
             cb.collisionObject = self._bodies[int(h["body"])]
+            cb.hitNormalWorld = h["normal"].copy()
+            cb.hitPointWorld = h["point"].copy()
+
+    def convexSweepTest(self, castShape, convexFromWorld, convexToWorld, resultCallback):
+        """CollisionWorld.convexSweepTest (collision/dispatch/CollisionWorld.java:596-645) with a
+        ClosestConvexResultCallback; from / to are Transforms.  Raises RuntimeError where the
+        reference throws: when the sweep's path reaches a static plane."""
+        g = self._ensure()
+        if castShape._id is None:
+            from .scenes import Scene
+            from . import lib
+            descs = Scene("cast", 0, 0, {}, [castShape.desc()], np.zeros(0)).shape_descs()
+            lib.check(lib.lib().jbgpu_world_add_shapes(g.h, descs, 1, None))
+            castShape._id = len(self._shapes)
+            self._shapes.append(castShape)
+        cb = resultCallback
+        h = g.convex_sweep_test(castShape._id, [convexFromWorld.as12()], [convexToWorld.as12()],
+                                group=cb.collisionFilterGroup, mask=cb.collisionFilterMask)[0]
+        if h["body"] == -2:
+            raise RuntimeError("convexSweepTest reached a static plane (the reference throws there)")
+        if h["body"] >= 0:
+            cb.closestHitFraction = float(h["fraction"])
+            cb.hitCollisionObject = self._bodies[int(h["body"])]
             cb.hitNormalWorld = h["normal"].copy()
             cb.hitPointWorld = h["point"].copy()
 

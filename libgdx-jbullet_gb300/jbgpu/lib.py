@@ -63,6 +63,8 @@ def lib():
             "jbgpu_world_ray_test": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
                                       C.c_int32, C.c_void_p], C.c_int),
             "jbgpu_world_set_ray_replay": ([C.c_void_p, C.c_int32], C.c_int),
+            "jbgpu_world_convex_sweep_test": ([C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32,
+                                               C.c_int32, C.c_int32, C.c_int32, C.c_void_p], C.c_int),
             "jbgpu_world_set_graph": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_graph_status": ([C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_char_p)], C.c_int),
             "jbgpu_world_add_cone_twist": ([C.c_void_p, C.c_int32, C.c_int32, _abi.f32p, _abi.f32p, C.POINTER(C.c_int32)],
@@ -118,7 +120,7 @@ EXPORTED = [
     "jbgpu_world_profile_counters", "jbgpu_world_timer", "jbgpu_world_add_point2point", "jbgpu_world_set_joint_setting",
     "jbgpu_world_get_joint_impulses", "jbgpu_world_add_hinge", "jbgpu_world_set_hinge_limit",
     "jbgpu_world_enable_hinge_motor", "jbgpu_world_set_hinge_angular_only", "jbgpu_world_ray_test",
-    "jbgpu_world_set_ray_replay", "jbgpu_world_set_graph", "jbgpu_world_graph_status", "jbgpu_world_add_generic6dof",
+    "jbgpu_world_set_ray_replay", "jbgpu_world_convex_sweep_test", "jbgpu_world_set_graph", "jbgpu_world_graph_status", "jbgpu_world_add_generic6dof",
     "jbgpu_world_set_6dof_limit", "jbgpu_world_set_6dof_linear_motor", "jbgpu_world_set_6dof_angular_motor",
     "jbgpu_world_add_cone_twist", "jbgpu_world_set_cone_twist_limit", "jbgpu_world_set_cone_twist_angular_only",
     "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
@@ -286,6 +288,29 @@ class GpuWorld:
     def ray_test_device(self, from_ptr, to_ptr, n, hits_ptr, world_ptr=None, group=1, mask=-1):
         """rayTest on device buffers (raw pointers); queued on the world's stream."""
         check(lib().jbgpu_world_ray_test(self.h, from_ptr, to_ptr, world_ptr, n, group, mask, 1, hits_ptr))
+
+    def convex_sweep_test(self, shape, xf_from, xf_to, world=None, group=1, mask=-1):
+        """CollisionWorld.convexSweepTest with a ClosestConvexResultCallback per sweep of the convex
+        shape id `shape`: xf_from / xf_to (n, 12) transforms (basis row-major, origin), world (n,)
+        batch world per sweep or None.  Returns a RAY_HIT_DTYPE array (body -1: no hit; -2: the
+        sweep reached a static plane, where the reference throws)."""
+        f = np.ascontiguousarray(xf_from, np.float32).reshape(-1, 12)
+        t = np.ascontiguousarray(xf_to, np.float32).reshape(-1, 12)
+        n = len(f)
+        if len(t) != n:
+            raise ValueError("xf_from and xf_to differ in length")
+        out = np.zeros(n, _abi.RAY_HIT_DTYPE)
+        wp = None
+        if world is not None:
+            wa = np.ascontiguousarray(world, np.int32).reshape(n)
+            wp = wa.ctypes.data
+        check(lib().jbgpu_world_convex_sweep_test(self.h, shape, f.ctypes.data, t.ctypes.data, wp, n, group, mask, 0,
+                                                  out.ctypes.data))
+        return out
+
+    def convex_sweep_test_device(self, shape, from_ptr, to_ptr, n, hits_ptr, world_ptr=None, group=1, mask=-1):
+        """convexSweepTest on device buffers (raw pointers); queued on the world's stream."""
+        check(lib().jbgpu_world_convex_sweep_test(self.h, shape, from_ptr, to_ptr, world_ptr, n, group, mask, 1, hits_ptr))
 
     def set_graph(self, on):
         """Replay the step as CUDA graphs (bit-identical to launching its kernels)."""

@@ -224,6 +224,33 @@ void orc_set_slider_params(void* h, int id, const float* p) {
     P.linMotor = p[22] != 0.0f; P.linTarget = p[23]; P.linMaxForce = p[24];
     P.angMotor = p[25] != 0.0f; P.angTarget = p[26]; P.angMaxForce = p[27];
 }
+// convexSweepTest with a ClosestConvexResultCallback per sweep of the world's shape `shape`:
+// from / to 12 floats each (basis row-major, origin); returns the number of sweeps that reached
+// a static plane (the reference throws there).
+int orc_convex_sweep(void* h, int shape, const float* from, const float* to, const int* world, int n, int group,
+                     int mask, jbgpu_ray_hit* out) {
+    const World& w = *(const World*)h;
+    int planes = 0;
+    auto xf12 = [](const float* f) {
+        Xf t;
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) t.b.m[r][c] = f[r * 3 + c];
+        t.o = v3(f[9], f[10], f[11]);
+        return t;
+    };
+    for (int i = 0; i < n; i++) {
+        bool plane = false;
+        RayResult r = convex_sweep(w, w.shapes[shape], xf12(from + 12 * i), xf12(to + 12 * i), group, mask,
+                                   world ? world[i] : 0, &plane);
+        planes += plane ? 1 : 0;
+        if (plane) r = RayResult();     // the reference throws: no result, the record marked -2
+        out[i].body = plane ? -2 : r.body;
+        out[i].fraction = r.fraction;
+        out[i].normal[0] = r.normal.x; out[i].normal[1] = r.normal.y; out[i].normal[2] = r.normal.z;
+        out[i].point[0] = r.point.x; out[i].point[1] = r.point.y; out[i].point[2] = r.point.z;
+    }
+    return planes;
+}
 int orc_get_joint_impulses(void* h, float* out, int cap) {
     const World* w = (const World*)h;
     const int n = (int)w->joints.size();

@@ -197,6 +197,25 @@ static inline Xf xf_inverse(Xf t) { t.b = transpose(t.b); t.o = scl(t.o, -1.0f);
 static inline Xf xf_mul(const Xf& a, const Xf& b) { Xf r; r.o = xf_apply(a, b.o); r.b = mulMM(a.b, b.b); return r; }
 static inline V3 xf_invXform(const Xf& t, V3 in) { V3 out = sub(in, t.o); return mulMv(out, transpose(t.b)); }
 
+// MatrixUtil.invert (linearmath/MatrixUtil.java:362-395): cofactors over the determinant.
+static inline M3 m3_invert(const M3& m) {
+    auto cofac = [&](int r1, int c1, int r2, int c2) { return m.m[r1][c1] * m.m[r2][c2] - m.m[r1][c2] * m.m[r2][c1]; };
+    float co_x = cofac(1, 1, 2, 2), co_y = cofac(1, 2, 2, 0), co_z = cofac(1, 0, 2, 1);
+    float det = m.m[0][0] * co_x + m.m[0][1] * co_y + m.m[0][2] * co_z;
+    float s = 1.0f / det;
+    M3 r;
+    r.m[0][0] = co_x * s;
+    r.m[0][1] = cofac(0, 2, 2, 1) * s;
+    r.m[0][2] = cofac(0, 1, 1, 2) * s;
+    r.m[1][0] = co_y * s;
+    r.m[1][1] = cofac(0, 0, 2, 2) * s;
+    r.m[1][2] = cofac(0, 2, 1, 0) * s;
+    r.m[2][0] = co_z * s;
+    r.m[2][1] = cofac(0, 1, 2, 0) * s;
+    r.m[2][2] = cofac(0, 0, 1, 1) * s;
+    return r;
+}
+
 // TransformUtil.planeSpace1 (linearmath/TransformUtil.java:45-61)
 static const float SIMDSQRT12 = 0.7071067811865475244008443621048490f;
 static inline void plane_space1(V3 n, V3& p, V3& q) {

@@ -632,7 +632,7 @@ static bool calc_pen_depth(const Shape& s0, const Xf& t0, const Shape& s1, const
 // ----------------------------------------------------------------------------------------
 // GjkPairDetector.getClosestPoints (collision/narrowphase/GjkPairDetector.java:73-316)
 // ----------------------------------------------------------------------------------------
-GjkOut gjk_closest_points(const Shape& sa, const Xf& tA, const Shape& sb, const Xf& tB, float maxDist2) {
+GjkOut gjk_closest_points(const Shape& sa, const Xf& tA, const Shape& sb, const Xf& tB, float maxDist2, bool withEpa) {
     static const float REL_ERROR2 = 1.0e-6f;
     GjkOut out;
     out.valid = false;
@@ -697,7 +697,7 @@ GjkOut gjk_closest_points(const Shape& sa, const Xf& tA, const Shape& sb, const 
         }
     }
     bool catchDegeneratePenetrationCase = (degenerate != 0 && ((distance + margin) < 0.01f));
-    if (checkPenetration && (!isValid || catchDegeneratePenetrationCase)) {
+    if (withEpa && checkPenetration && (!isValid || catchDegeneratePenetrationCase)) {
         out.usedEpa = 1;
         V3 tA2, tB2;
         if (epa::calc_pen_depth(sa, lA, sb, lB, tA2, tB2)) {
@@ -1115,6 +1115,124 @@ RayResult ray_test(const World& w, V3 from, V3 to, int group, int mask, int worl
     r.normal = cb.normal;
     r.point = cb.body >= 0 ? interp3(from, to, cb.closest) : v3(0.0f, 0.0f, 0.0f);
     return r;
+}
+
+
+// ----------------------------------------------------------------------------------------
+// CollisionWorld.convexSweepTest with a ClosestConvexResultCallback (collision/dispatch/
+// CollisionWorld.java:596-645, objectQuerySingle 391-490, ClosestConvexResultCallback 766-805)
+// ----------------------------------------------------------------------------------------
+// TransformUtil.calculateVelocity / calculateDiffAxisAngle (linearmath/TransformUtil.java:105-153)
+static void calculate_velocity(const Xf& t0, const Xf& t1, float timeStep, V3& linVel, V3& angVel) {
+    linVel = scl(sub(t1.o, t0.o), 1.0f / timeStep);
+    M3 dmat = mulMM(t1.b, m3_invert(t0.b));
+    Quat dorn = qnor(q_from_matrix(dmat));
+    float angle = 2.0f * jacos(dorn.w);                     // QuaternionUtil.getAngle
+    V3 axis = v3(dorn.x, dorn.y, dorn.z);
+    float l2 = len2(axis);
+    if (l2 < FLT_EPS * FLT_EPS) axis = v3(1.0f, 0.0f, 0.0f);
+    else axis = scl(axis, 1.0f / jsqrt(l2));
+    angVel = scl(axis, angle / timeStep);
+}
+
+// CollisionShape.calculateTemporalAabb (collision/shapes/CollisionShape.java:76-121) with
+// getAngularMotionDisc / getBoundingSphere (44-72).
+void temporal_aabb(const Shape& s, const Xf& cur, V3 linvel, V3 angvel, float timeStep, V3& mn, V3& mx) {
+    shape_aabb(s, cur, mn, mx);
+    V3 lin = scl(linvel, timeStep);
+    if (lin.x > 0.0f) mx.x += lin.x; else mn.x += lin.x;
+    if (lin.y > 0.0f) mx.y += lin.y; else mn.y += lin.y;
+    if (lin.z > 0.0f) mx.z += lin.z; else mn.z += lin.z;
+    V3 bmin, bmax;
+    shape_aabb(s, xf_identity(), bmin, bmax);
+    float radius = len(sub(bmax, bmin)) * 0.5f;
+    V3 center = scl(add(bmin, bmax), 0.5f);
+    float disc = radius + len(center);
+    float am = len(angvel) * disc * timeStep;
+    mn = sub(mn, v3(am, am, am));
+    mx = add(mx, v3(am, am, am));
+}
+
+// GjkConvexCast.calcTimeOfImpact (collision/narrowphase/GjkConvexCast.java:67-185): conservative
+// advancement on GjkPairDetector distances (no penetration solver), through a PointCollector
+// that keeps its closest result across the calls.
+static bool gjk_convex_cast(const Shape& sa, const Xf& fromA, const Xf& toA, const Shape& sb, const Xf& tB,
+                            float allowedPenetration, float& fraction, V3& normal, V3& hitPoint) {
+    V3 r = sub(sub(toA.o, fromA.o), sub(tB.o, tB.o));
+    const float radius = 0.001f;
+    float lambda = 0.0f, lastLambda = 0.0f;
+    int numIter = 0;
+    bool has = false;
+    float cdist = 1e30f;
+    V3 cn = v3(0, 0, 0), cp = v3(0, 0, 0);
+    auto collect = [&](const GjkOut& o) {
+        if (o.valid && o.distance < cdist) { has = true; cn = o.normal; cp = o.pointOnB; cdist = o.distance; }
+    };
+    Xf iA = fromA, iB = tB;
+    collect(gjk_closest_points(sa, iA, sb, iB, SIMD_INFINITY, false));
+    if (!has) return false;
+    V3 c = cp, n = cn;
+    float dist = cdist;
+    while (dist > radius) {
+        if (++numIter > 32) return false;
+        float dLambda = dist / dot(r, n);
+        lambda = lambda - dLambda;
+        if (lambda > 1.0f || lambda < 0.0f || lambda <= lastLambda) return false;
+        lastLambda = lambda;
+        iA.o = interp3(fromA.o, toA.o, lambda);
+        iB.o = interp3(tB.o, tB.o, lambda);
+        collect(gjk_closest_points(sa, iA, sb, iB, SIMD_INFINITY, false));
+        if (cdist < 0.0f) { fraction = lastLambda; normal = cn; hitPoint = cp; return true; }
+        c = cp;
+        n = cn;
+        dist = cdist;
+    }
+    if (dot(n, r) >= -allowedPenetration) return false;
+    fraction = lambda;
+    normal = n;
+    hitPoint = c;
+    return true;
+}
+
+// convexSweepTest over the bodies of one batch world.  The cast shape's temporal aabb comes from
+// the sweep's start rotation; every object's aabb is grown by it and tested against the path of
+// the origins with the bound 1 (not the closest hit so far), then GjkConvexCast.  A static plane
+// reached by the sweep makes the reference throw (its plane branch calls a caster that is null):
+// *planeHit is set and the result is that of the objects before it.
+RayResult convex_sweep(const World& w, const Shape& cast, const Xf& from, const Xf& to, int group, int mask, int world,
+                       bool* planeHit) {
+    *planeHit = false;
+    V3 linVel, angVel;
+    calculate_velocity(from, to, 1.0f, linVel, angVel);
+    Xf R = xf_identity();
+    R.b = m3_from_quat(q_from_matrix(from.b));
+    V3 cmin, cmax;
+    temporal_aabb(cast, R, linVel, angVel, 1.0f, cmin, cmax);
+    RayResult res;
+    float closest = 1.0f;
+    for (size_t i = 0; i < w.bodies.size(); i++) {
+        const Body& b = w.bodies[i];
+        if (b.world != world) continue;
+        if (((b.group & mask) & 0xFFFF) == 0 || ((group & b.mask) & 0xFFFF) == 0) continue;
+        const Shape& sh = w.shapes[b.shape];
+        V3 mn, mx;
+        shape_aabb(sh, b.xf, mn, mx);
+        mn = add(mn, cmin);
+        mx = add(mx, cmax);
+        float param = 1.0f;
+        if (!ray_aabb(from.o, to.o, mn, mx, param)) continue;
+        if (!sh.isConvex()) { *planeHit = true; return res; }
+        float f;
+        V3 n, p;
+        if (gjk_convex_cast(cast, from, to, sh, b.xf, 0.04f, f, n, p) && len2(n) > 0.0001f && f < closest) {
+            closest = f;
+            res.body = (int)i;
+            res.fraction = f;
+            res.normal = nor(n);
+            res.point = p;
+        }
+    }
+    return res;
 }
 
 }  // namespace jb

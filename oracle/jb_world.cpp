@@ -602,25 +602,6 @@ static void hinge_solve(Joint& j, Body& A, Body& B, float timeStep) {
     }
 }
 
-// MatrixUtil.invert (linearmath/MatrixUtil.java:362-395): cofactors over the determinant.
-static M3 m3_invert(const M3& m) {
-    auto cofac = [&](int r1, int c1, int r2, int c2) { return m.m[r1][c1] * m.m[r2][c2] - m.m[r1][c2] * m.m[r2][c1]; };
-    float co_x = cofac(1, 1, 2, 2), co_y = cofac(1, 2, 2, 0), co_z = cofac(1, 0, 2, 1);
-    float det = m.m[0][0] * co_x + m.m[0][1] * co_y + m.m[0][2] * co_z;
-    float s = 1.0f / det;
-    M3 r;
-    r.m[0][0] = co_x * s;
-    r.m[0][1] = cofac(0, 2, 2, 1) * s;
-    r.m[0][2] = cofac(0, 1, 1, 2) * s;
-    r.m[1][0] = co_y * s;
-    r.m[1][1] = cofac(0, 0, 2, 2) * s;
-    r.m[1][2] = cofac(0, 2, 1, 0) * s;
-    r.m[2][0] = co_z * s;
-    r.m[2][1] = cofac(0, 1, 2, 0) * s;
-    r.m[2][2] = cofac(0, 0, 1, 1) * s;
-    return r;
-}
-
 // Generic6DofConstraint.matrixToEulerXYZ (Generic6DofConstraint.java:125-159): element `index`
 // is row index % 3, column index / 3; atan2 / asin in double, rounded to float.
 static V3 matrix_to_euler_xyz(const M3& m) {

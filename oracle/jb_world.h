@@ -235,6 +235,8 @@ int add_body(World& w, float mass, int shape, const Xf& xf, V3 localInertia, flo
 void process_pair(World& w, int pairIndex);
 // GJK/EPA closest points between two convex bodies (GjkPairDetector.getClosestPoints), exposed for tests.
 struct GjkOut { bool valid; V3 normal; V3 pointOnB; float distance; int usedEpa; };
-GjkOut gjk_closest_points(const Shape& sa, const Xf& ta, const Shape& sb, const Xf& tb, float maxDist2);
+GjkOut gjk_closest_points(const Shape& sa, const Xf& ta, const Shape& sb, const Xf& tb, float maxDist2, bool withEpa = true);
+RayResult convex_sweep(const World& w, const Shape& cast, const Xf& from, const Xf& to, int group, int mask, int world,
+                       bool* planeHit);
 
 }  // namespace jb

@@ -60,6 +60,8 @@ def lib():
         L.orc_set_6dof_angular_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int] + [C.c_float] * 7
         L.orc_add_cone_twist.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
         L.orc_set_cone_limit.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 6
+        L.orc_convex_sweep.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                       C.c_void_p]
         L.orc_add_slider.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p, C.c_int]
         L.orc_set_slider_params.argtypes = [C.c_void_p, C.c_int, _abi.f32p]
         L.orc_add_hinge.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
@@ -136,6 +138,18 @@ class OracleWorld:
 
     def set_hinge_angular_only(self, jid, on):
         lib().orc_set_hinge_angular_only(self.h, jid, 1 if on else 0)
+
+    def convex_sweep(self, shape, xf_from, xf_to, world=None, group=1, mask=-1):
+        """convexSweepTest with a ClosestConvexResultCallback per sweep of shape `shape` from / to
+        transforms (n, 12).  Records as RAY_HIT_DTYPE; body -2 marks a sweep that reached a static
+        plane (where the reference throws).  Returns (records, number of such sweeps)."""
+        f = np.ascontiguousarray(xf_from, np.float32).reshape(-1, 12)
+        t = np.ascontiguousarray(xf_to, np.float32).reshape(-1, 12)
+        out = np.zeros(len(f), _abi.RAY_HIT_DTYPE)
+        wa = None if world is None else np.ascontiguousarray(world, np.int32).reshape(len(f))
+        planes = lib().orc_convex_sweep(self.h, shape, f.ctypes.data, t.ctypes.data, None if wa is None else wa.ctypes.data,
+                                        len(f), group, mask, out.ctypes.data)
+        return out, planes
 
     def add_generic6dof(self, a, b, frame_a, frame_b, use_linear_reference_frame_a=True):
         fa = np.ascontiguousarray(frame_a, np.float32).reshape(12)
