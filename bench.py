@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--ref-seconds", type=float, default=120.0, help="time budget of the reference arm's timed steps")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start comparison")
     p.add_argument("--no-rays", action="store_true", help="skip the rayTest batch measurement")
+    p.add_argument("--sweeps", type=int, default=4096, help="convexSweepTest sweeps per measured batch (0: skip)")
     p.add_argument("--graph", type=int, default=1, help="1: replay the step as CUDA graphs (jbgpu_world_set_graph), 0: launches")
     p.add_argument("--rays", type=int, default=1 << 20, help="rays per rayTest batch")
     return p.parse_args()
@@ -281,6 +282,69 @@ def measure_rays(w, scene, nrays, seed, local):
             "clock": "CUDA events on the world's stream around 5 batches of device buffers"}
 
 
+def measure_sweeps(w, scene, nsweeps, seed, local):
+    """CollisionWorld.convexSweepTest batches on the world as the timed steps left it: nsweeps
+    sweeps of the scene's first sphere shape (else its first convex shape) per batch from device
+    buffers, each with its own start and end rotation (half straight down from above the bodies,
+    half between random points of their bounding region), filter mask without the static group
+    (the reference throws on a sweep that reaches its static plane); CUDA events on the world's
+    stream around 3 batches after 1 untimed one; a 64-sweep sample compared with the oracle bit for
+    bit and timed on 1 core."""
+    import torch
+    from jbgpu import _abi
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    st = w.get_state()
+    pos = st["transform"][:, 9:]
+    fin = np.all(np.abs(pos) < 1e6, axis=1)
+    lo, hi = pos[fin].min(0), pos[fin].max(0)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    a = rng.uniform(lo, hi, (nsweeps, 3)).astype(np.float32)
+    b = rng.uniform(lo, hi, (nsweeps, 3)).astype(np.float32)
+    h = nsweeps // 2
+    a[:h, 1] = hi[1] + 5.0
+    b[:h] = a[:h]
+    b[:h, 1] = lo[1] - 2.0
+
+    def rot(q):
+        x, y, z, ww = q / np.linalg.norm(q)
+        return np.array([1 - 2 * (y * y + z * z), 2 * (x * y - z * ww), 2 * (x * z + y * ww),
+                         2 * (x * y + z * ww), 1 - 2 * (x * x + z * z), 2 * (y * z - x * ww),
+                         2 * (x * z - y * ww), 2 * (y * z + x * ww), 1 - 2 * (x * x + y * y)], np.float32)
+    fr = np.zeros((nsweeps, 12), np.float32)
+    to = np.zeros((nsweeps, 12), np.float32)
+    for i in range(nsweeps):
+        fr[i, :9], to[i, :9] = rot(rng.normal(size=4)), rot(rng.normal(size=4))
+    fr[:, 9:], to[:, 9:] = a, b
+    kinds = [s["type"] for s in scene.shapes]
+    shape = kinds.index(_abi.SHAPE_SPHERE) if _abi.SHAPE_SPHERE in kinds else \
+        next(i for i, k in enumerate(kinds) if k != _abi.SHAPE_STATIC_PLANE)
+    mask = ~2 & 0xFFFF
+    dev = "cuda:%d" % local
+    df, dt = torch.from_numpy(fr).to(dev), torch.from_numpy(to).to(dev)
+    dh = torch.empty(nsweeps * _abi.RAY_HIT_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    w.convex_sweep_test_device(shape, df.data_ptr(), dt.data_ptr(), nsweeps, dh.data_ptr(), mask=mask)
+    w.synchronize()
+    reps = 3
+    w.timer_start()
+    for _ in range(reps):
+        w.convex_sweep_test_device(shape, df.data_ptr(), dt.data_ptr(), nsweeps, dh.data_ptr(), mask=mask)
+    ms = w.timer_stop() / reps
+    hits = dh.cpu().numpy().view(_abi.RAY_HIT_DTYPE)
+    o = pyoracle.OracleWorld(scene)
+    o.set_state({"transform": st["transform"]})
+    k = 64
+    t0 = time.perf_counter()
+    ho, _ = o.convex_sweep(shape, fr[:k], to[:k], mask=mask)
+    cpu_s = time.perf_counter() - t0
+    return {"sweeps_per_batch": nsweeps, "cast_shape": int(kinds[shape]), "ms_per_batch": ms,
+            "sweeps_per_s": nsweeps / (ms * 1e-3), "hit_fraction": float(np.mean(hits["body"] >= 0)),
+            "cpu_oracle_sweeps_per_s": k / cpu_s,
+            "cpu_sample": "%d sweeps of the batch, oracle (the reference's object loop restated), 1 thread" % k,
+            "bit_exact_vs_oracle_sample": bool(np.array_equal(ho.view(np.uint8), hits[:k].view(np.uint8))),
+            "clock": "CUDA events on the world's stream around 3 batches of device buffers"}
+
+
 def run_ours(args, dist):
     from jbgpu import _abi, _build, lib
     from jbgpu.lib import GpuWorld
@@ -330,6 +394,9 @@ def run_ours(args, dist):
     rays = None
     if dist.rank == 0 and not args.no_rays:
         rays = measure_rays(w, sc, args.rays, args.seed + 20, dist.local)
+    sweeps = None
+    if dist.rank == 0 and args.sweeps > 0:
+        sweeps = measure_sweeps(w, sc, args.sweeps, args.seed + 30, dist.local)
     w.close()
     wall = t1 - t0
     elapsed = dist.max(device_ms * 1e-3)
@@ -431,6 +498,7 @@ def run_ours(args, dist):
         "cpu_baseline": cpu,
         "learned_warmstart": learned,
         "ray_test": rays,
+        "convex_sweep_test": sweeps,
         "step_graphs": graph_info,
         "clocks": clocks,
         "status_flags": final["status_flags"],
