@@ -249,23 +249,29 @@ struct RayCand {
 };
 
 // Tree walk of one ray per thread: COUNT counts the candidates, else they are written at the
-// ray's offset (the same walk, so the same candidates in the same order).
-template <bool COUNT>
+// ray's offset (the same walk, so the same candidates in the same order).  GROW: a convex sweep's
+// path of origins, every box (node and body) grown by the sweep's cast-shape box gmin / gmax.
+template <bool COUNT, bool GROW = false>
 __global__ void __launch_bounds__(RAY_THREADS) k_ray_walk(DevWorld w, DevWorld wq, const int* sortedBody, Bvh tree,
                                                          const int* wroot, const int* planeList, const int* planeStart,
                                                          const float* from, const float* to, const int* rayWorld, int n,
-                                                         int group, int mask, int* cnt, const int* off, RayCand* cand) {
+                                                         int group, int mask, int* cnt, const int* off, RayCand* cand,
+                                                         const float4* gmin = nullptr, const float4* gmax = nullptr) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const V f = mk(from[3 * r], from[3 * r + 1], from[3 * r + 2]);
     const V t = mk(to[3 * r], to[3 * r + 1], to[3 * r + 2]);
     const int wi = rayWorld ? rayWorld[r] : 0;
     const int base = COUNT ? 0 : off[r];
+    const float4 g0 = GROW ? gmin[r] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 g1 = GROW ? gmax[r] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     int c = 0;
     auto consider = [&](int b) {
         if (!passes_filter(w, b, group, mask)) return;
         float enter, exit;
-        if (!ray_aabb_parts(f, t, mk4(wq.amin[b]), mk4(wq.amax[b]), enter, exit)) return;
+        const V bmin = GROW ? add(mk4(wq.amin[b]), mk4(g0)) : mk4(wq.amin[b]);
+        const V bmax = GROW ? add(mk4(wq.amax[b]), mk4(g1)) : mk4(wq.amax[b]);
+        if (!ray_aabb_parts(f, t, bmin, bmax, enter, exit)) return;
         if (!(enter <= jmin(1.0f, exit))) return;
         if (!COUNT) {
             RayCand rc;
@@ -290,7 +296,14 @@ __global__ void __launch_bounds__(RAY_THREADS) k_ray_walk(DevWorld w, DevWorld w
                 const float4* nd = tree.node + 4 * stack[--sp];
                 const float4 rec[4] = {nd[0], nd[1], nd[2], nd[3]};
                 for (int k = 0; k < 2; k++) {
-                    if (!slab(f, d, rec[2 * k], rec[2 * k + 1])) continue;
+                    if (GROW) {
+                        const float4 lo = rec[2 * k], hi = rec[2 * k + 1];
+                        if (!slab(f, d, make_float4(__fadd_rn(lo.x, g0.x), __fadd_rn(lo.y, g0.y), __fadd_rn(lo.z, g0.z), 0.0f),
+                                  make_float4(__fadd_rn(hi.x, g1.x), __fadd_rn(hi.y, g1.y), __fadd_rn(hi.z, g1.z), 0.0f)))
+                            continue;
+                    } else if (!slab(f, d, rec[2 * k], rec[2 * k + 1])) {
+                        continue;
+                    }
                     const int x = __float_as_int(rec[2 * k].w);
                     if (x & LEAF_FLAG) consider(sortedBody[x & ~LEAF_FLAG]);
                     else if (sp < RAY_STACK) stack[sp++] = x;
@@ -449,16 +462,22 @@ __global__ void __launch_bounds__(SLOW_THREADS) k_rays_slow(DevWorld w, DevWorld
 // CollisionWorld.java:596-645, objectQuerySingle 391-490).  The reference's object loop tests each
 // object's aabb, grown by the cast shape's temporal aabb, against the path of the origins with
 // the fixed bound 1 and keeps a GjkConvexCast hit when it is below the closest so far: the answer
-// is the smallest hit by (fraction, body), whatever the order.  One thread per (sweep, body).
+// is the smallest hit by (fraction, body), whatever the order.  The rays' tree walk, with every
+// box grown by the cast shape's box, lists the (sweep, body) candidates; a thread per candidate
+// casts.
 
 // TransformUtil.calculateVelocity / calculateDiffAxisAngle (linearmath/TransformUtil.java:105-153)
 // and CollisionShape.calculateTemporalAabb with getAngularMotionDisc (CollisionShape.java:44-121).
 __global__ void k_sweep_prep(DevWorld w, int shape, const float* from, const float* to, int n, float4* cmin,
-                             float4* cmax) {
+                             float4* cmax, float* ofrom, float* oto) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     const float* f = from + 12 * q;
     const float* t = to + 12 * q;
+    for (int k = 0; k < 3; k++) {   // the path of the origins, walked like a ray
+        ofrom[3 * q + k] = f[9 + k];
+        oto[3 * q + k] = t[9 + k];
+    }
     M b0, b1;
     b0.r[0] = mk(f[0], f[1], f[2]); b0.r[1] = mk(f[3], f[4], f[5]); b0.r[2] = mk(f[6], f[7], f[8]);
     b1.r[0] = mk(t[0], t[1], t[2]); b1.r[1] = mk(t[3], t[4], t[5]); b1.r[2] = mk(t[6], t[7], t[8]);
@@ -544,101 +563,6 @@ JBD Xf xf12(const float* f) {
     return t;
 }
 
-// PICK == false: every (sweep, body) whose grown aabb the path enters runs the cast; the sweep's
-// smallest hit key by atomicMin, a static plane on the path flagged.  PICK == true: the body
-// holding the sweep's smallest hit runs its cast again and writes the record.
-template <bool PICK>
-__global__ void k_sweep(DevWorld w, DevWorld wq, int shape, const float* from, const float* to, const int* sweepWorld,
-                        int n, int group, int mask, const float4* cmin, const float4* cmax, unsigned long long* key,
-                        int* planeHit, jbgpu_ray_hit* out) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= w.nBodies) return;
-    const int bs = w.shape[b];
-    for (int q = blockIdx.y; q < n; q += gridDim.y) {
-        if (PICK && (key[q] == ~0ull || (int)((key[q] >> 1) & 0x7fffffffu) != b)) continue;
-        if (w.world[b] != (sweepWorld ? sweepWorld[q] : 0) || !passes_filter(w, b, group, mask)) continue;
-        const Xf fa = xf12(from + 12 * q);
-        const V ta = mk(to[12 * q + 9], to[12 * q + 10], to[12 * q + 11]);
-        const V mn = add(mk4(wq.amin[b]), mk4(cmin[q])), mx = add(mk4(wq.amax[b]), mk4(cmax[q]));
-        float enter, exit;
-        if (!ray_aabb_parts(fa.o, ta, mn, mx, enter, exit) || !(enter <= jmin(1.0f, exit))) continue;
-        if (w.sh.type[bs] == SHAPE_PLANE) {
-            if (!PICK) atomicOr(planeHit + q, 1);
-            continue;
-        }
-        float f;
-        V nrm, p;
-        if (!gjk_convex_cast(shape_ref(w.sh, shape), fa, ta, shape_ref(w.sh, bs), load_xf(w, b), f, nrm, p) ||
-            !(len2(nrm) > 0.0001f) || !(f < 1.0f))   // ClosestConvexResultCallback starts at closestHitFraction 1
-            continue;
-        if (!PICK) {
-            atomicMin(key + q, hit_key(f, b, 0));
-            continue;
-        }
-        jbgpu_ray_hit o;
-        o.body = b;
-        o.fraction = f;
-        const V nn = nor(nrm);
-        o.normal[0] = nn.x; o.normal[1] = nn.y; o.normal[2] = nn.z;
-        o.point[0] = p.x; o.point[1] = p.y; o.point[2] = p.z;
-        out[q] = o;
-    }
-}
-
-__global__ void k_sweep_finish(int n, const unsigned long long* key, const int* planeHit, jbgpu_ray_hit* out) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= n) return;
-    if (!planeHit[q] && key[q] != ~0ull) return;
-    jbgpu_ray_hit o;
-    o.body = planeHit[q] ? -2 : -1;
-    o.fraction = 1.0f;
-    o.normal[0] = o.normal[1] = o.normal[2] = 0.0f;
-    o.point[0] = o.point[1] = o.point[2] = 0.0f;
-    out[q] = o;
-}
-
-__global__ void k_count_flags(int n, const int* flag, int* count) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n && flag[i]) atomicAdd(count, 1);
-}
-
-int query_sweeps(const DevWorld& w, QueryBuffers& qb, int shape, const float* from, const float* to, const int* sweepWorld,
-                 int n, int group, int mask, jbgpu_ray_hit* hits, int* planeHits, cudaStream_t s) {
-    if (n <= 0) return JBGPU_OK;
-    if (n > qb.capSweeps) {
-        void* old[] = {qb.sweepMin, qb.sweepMax, qb.sweepKey, qb.sweepPlane};
-        for (void* p : old)
-            if (p) cudaFree(p);
-        qb.sweepMin = qb.sweepMax = nullptr;
-        qb.sweepKey = nullptr;
-        qb.sweepPlane = nullptr;
-        const int c = n > 2 * qb.capSweeps ? n : 2 * qb.capSweeps;
-        qb.capSweeps = 0;
-        if (cudaMalloc((void**)&qb.sweepMin, sizeof(float4) * (size_t)c) != cudaSuccess ||
-            cudaMalloc((void**)&qb.sweepMax, sizeof(float4) * (size_t)c) != cudaSuccess ||
-            cudaMalloc((void**)&qb.sweepKey, sizeof(unsigned long long) * (size_t)c) != cudaSuccess ||
-            cudaMalloc((void**)&qb.sweepPlane, sizeof(int) * (size_t)c) != cudaSuccess)
-            return JBGPU_ERR_CUDA;
-        qb.capSweeps = c;
-    }
-    cudaMemsetAsync(qb.sweepKey, 0xff, sizeof(unsigned long long) * n, s);
-    cudaMemsetAsync(qb.sweepPlane, 0, sizeof(int) * n, s);
-    DevWorld wq = w;
-    wq.amin = qb.qmin;
-    wq.amax = qb.qmax;
-    k_sweep_prep<<<gridn(n, 128), 128, 0, s>>>(w, shape, from, to, n, qb.sweepMin, qb.sweepMax); note_launch();
-    const dim3 grid(gridn(w.nBodies, 128), n < 65535 ? n : 65535);
-    k_sweep<false><<<grid, 128, 0, s>>>(w, wq, shape, from, to, sweepWorld, n, group, mask, qb.sweepMin, qb.sweepMax,
-                                         qb.sweepKey, qb.sweepPlane, hits); note_launch();
-    k_sweep<true><<<grid, 128, 0, s>>>(w, wq, shape, from, to, sweepWorld, n, group, mask, qb.sweepMin, qb.sweepMax,
-                                        qb.sweepKey, qb.sweepPlane, hits); note_launch();
-    k_sweep_finish<<<gridn(n, 128), 128, 0, s>>>(n, qb.sweepKey, qb.sweepPlane, hits); note_launch();
-    if (planeHits) {
-        k_count_flags<<<gridn(n, 256), 256, 0, s>>>(n, qb.sweepPlane, planeHits); note_launch();
-    }
-    return cudaGetLastError() == cudaSuccess ? JBGPU_OK : JBGPU_ERR_CUDA;
-}
-
 int query_prepare(const DevWorld& w, BroadphaseBuffers& bb, QueryBuffers& qb, cudaStream_t s) {
     if (w.nBodies > qb.capBodies) {
         if (qb.qmin) cudaFree(qb.qmin);
@@ -674,11 +598,8 @@ int query_prepare(const DevWorld& w, BroadphaseBuffers& bb, QueryBuffers& qb, cu
     return cudaGetLastError() == cudaSuccess ? JBGPU_OK : JBGPU_ERR_CUDA;
 }
 
-int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb, const float* from, const float* to,
-               const int* rayWorld, int n, int group, int mask, jbgpu_ray_hit* hits, int sms, cudaStream_t s) {
-    if (n <= 0) return JBGPU_OK;
-    int rc;
-    if (n > qb.capRays) {   // per-ray buffers
+static bool grow_ray_buffers(QueryBuffers& qb, int n) {
+    if (n > qb.capRays) {   // per-ray (per-sweep) buffers
         void* old[] = {qb.slow, qb.rayCnt, qb.rayOff, qb.key, qb.enterJ, qb.undecided, qb.scanScratch};
         for (void* p : old)
             if (p) cudaFree(p);
@@ -686,8 +607,8 @@ int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb,
         qb.key = nullptr;
         qb.enterJ = nullptr;
         qb.scanScratch = nullptr;
-        qb.capRays = 0;
         const int c = n > 2 * qb.capRays ? n : 2 * qb.capRays;
+        qb.capRays = 0;
         if (cudaMalloc((void**)&qb.slow, sizeof(int) * (size_t)c) != cudaSuccess ||
             cudaMalloc((void**)&qb.rayCnt, sizeof(int) * (size_t)c) != cudaSuccess ||
             cudaMalloc((void**)&qb.rayOff, sizeof(int) * (size_t)c) != cudaSuccess ||
@@ -695,12 +616,38 @@ int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb,
             cudaMalloc((void**)&qb.enterJ, sizeof(float) * (size_t)c) != cudaSuccess ||
             cudaMalloc((void**)&qb.undecided, sizeof(int) * (size_t)c) != cudaSuccess ||
             cudaMalloc(&qb.scanScratch, scan_scratch_bytes(c)) != cudaSuccess)
-            return JBGPU_ERR_CUDA;
+            return false;
         qb.capRays = c;
     }
     if (!qb.slowCount && (cudaMalloc((void**)&qb.slowCount, sizeof(int)) != cudaSuccess ||
                           cudaMalloc((void**)&qb.candTotal, sizeof(int)) != cudaSuccess))
-        return JBGPU_ERR_CUDA;
+        return false;
+    return true;
+}
+
+static bool grow_cand_buffers(QueryBuffers& qb, int total) {
+    if (total > qb.capCand) {
+        void* old[] = {qb.cand, qb.hitA, qb.hitB};
+        for (void* p : old)
+            if (p) cudaFree(p);
+        qb.cand = nullptr;
+        qb.hitA = qb.hitB = nullptr;
+        const int c = total > 2 * qb.capCand ? total : 2 * qb.capCand;
+        qb.capCand = 0;
+        if (cudaMalloc((void**)&qb.cand, sizeof(RayCand) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.hitA, sizeof(float4) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.hitB, sizeof(float4) * (size_t)c) != cudaSuccess)
+            return false;
+        qb.capCand = c;
+    }
+    return true;
+}
+
+int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb, const float* from, const float* to,
+               const int* rayWorld, int n, int group, int mask, jbgpu_ray_hit* hits, int sms, cudaStream_t s) {
+    if (n <= 0) return JBGPU_OK;
+    int rc;
+    if (!grow_ray_buffers(qb, n)) return JBGPU_ERR_CUDA;
     cudaMemsetAsync(qb.slowCount, 0, sizeof(int), s);
     cudaMemsetAsync(qb.key, 0xff, sizeof(unsigned long long) * n, s);
     cudaMemsetAsync(qb.undecided, 0, sizeof(int) * n, s);
@@ -719,20 +666,7 @@ int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb,
         if (cudaMemcpyAsync(&total, qb.candTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
             return JBGPU_ERR_CUDA;
-        if (total > qb.capCand) {
-            void* old[] = {qb.cand, qb.hitA, qb.hitB};
-            for (void* p : old)
-                if (p) cudaFree(p);
-            qb.cand = nullptr;
-            qb.hitA = qb.hitB = nullptr;
-            const int c = total > 2 * qb.capCand ? total : 2 * qb.capCand;
-            qb.capCand = 0;
-            if (cudaMalloc((void**)&qb.cand, sizeof(RayCand) * (size_t)c) != cudaSuccess ||
-                cudaMalloc((void**)&qb.hitA, sizeof(float4) * (size_t)c) != cudaSuccess ||
-                cudaMalloc((void**)&qb.hitB, sizeof(float4) * (size_t)c) != cudaSuccess)
-                return JBGPU_ERR_CUDA;
-            qb.capCand = c;
-        }
+        if (!grow_cand_buffers(qb, total)) return JBGPU_ERR_CUDA;
         if (total > 0) {
             RayCand* cand = (RayCand*)qb.cand;
             k_ray_walk<false><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(w, wq, bb.sortedBody, tree, bb.wroot,
@@ -754,10 +688,182 @@ int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb,
     return cudaGetLastError() == cudaSuccess ? JBGPU_OK : JBGPU_ERR_CUDA;
 }
 
+// Candidates of a batch too small to fill the GPU with one walk per sweep: a thread per
+// (sweep, body) runs the walk's leaf test (filter, grown aabb entered before min(1, exit)).
+// COUNT adds up the candidates, else appends them (order is immaterial: the casts keep the
+// smallest key), at most cap.
+template <bool COUNT>
+__global__ void k_sweep_list(DevWorld w, DevWorld wq, const float* ofrom, const float* oto, const int* sweepWorld, int n,
+                             int group, int mask, const float4* gmin, const float4* gmax, int* counter, RayCand* cand,
+                             int cap) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= w.nBodies) return;
+    const int lane = threadIdx.x & 31;
+    const V amn = mk4(wq.amin[b]), amx = mk4(wq.amax[b]);
+    const int bw = w.world[b];
+    const bool filt = passes_filter(w, b, group, mask);
+    for (int q = blockIdx.y; q < n; q += gridDim.y) {
+        bool pass = false;
+        float enter = 0.0f, exit;
+        if (filt && bw == (sweepWorld ? sweepWorld[q] : 0)) {
+            const V f = mk(ofrom[3 * q], ofrom[3 * q + 1], ofrom[3 * q + 2]);
+            const V t = mk(oto[3 * q], oto[3 * q + 1], oto[3 * q + 2]);
+            pass = ray_aabb_parts(f, t, add(amn, mk4(gmin[q])), add(amx, mk4(gmax[q])), enter, exit) &&
+                   enter <= jmin(1.0f, exit);
+        }
+        const unsigned act = __activemask();
+        const unsigned m = __ballot_sync(act, pass);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(counter, __popc(m));
+        base = __shfl_sync(act, base, leader);
+        if (COUNT || !pass) continue;
+        const int idx = base + __popc(m & ((1u << lane) - 1u));
+        if (idx < cap) {
+            RayCand rc;
+            rc.ray = q;
+            rc.body = b;
+            rc.enter = enter;
+            rc.pad = 0;
+            cand[idx] = rc;
+        }
+    }
+}
+
+// One thread per candidate (sweep, body) of the tree walk: a static plane flags the sweep, any
+// other body runs GjkConvexCast and offers (fraction, body) to the sweep's smallest key.
+__global__ void __launch_bounds__(RAY_THREADS) k_sweep_cast(DevWorld w, const RayCand* cand, int total, int shape,
+                                                           const float* from, const float* to, float4* hitA, float4* hitB,
+                                                           unsigned long long* key, int* planeHit) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const RayCand c = cand[i];
+    const int bs = w.shape[c.body];
+    if (w.sh.type[bs] == SHAPE_PLANE) {
+        atomicOr(planeHit + c.ray, 1);
+        return;
+    }
+    const Xf fa = xf12(from + 12 * c.ray);
+    const V ta = mk(to[12 * c.ray + 9], to[12 * c.ray + 10], to[12 * c.ray + 11]);
+    float f;
+    V nrm, p;
+    if (!gjk_convex_cast(shape_ref(w.sh, shape), fa, ta, shape_ref(w.sh, bs), load_xf(w, c.body), f, nrm, p) ||
+        !(len2(nrm) > 0.0001f) || !(f < 1.0f))   // ClosestConvexResultCallback starts at closestHitFraction 1
+        return;
+    hitA[i] = f4(nrm, f);
+    hitB[i] = f4(p, 0.0f);
+    atomicMin(key + c.ray, hit_key(f, c.body, 0));
+}
+
+// The candidate holding its sweep's smallest key writes the record (one body per key).
+__global__ void k_sweep_pick(const RayCand* cand, int total, const float4* hitA, const float4* hitB,
+                             const unsigned long long* key, jbgpu_ray_hit* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const RayCand c = cand[i];
+    const unsigned long long k = key[c.ray];
+    if (k == ~0ull || (int)((k >> 1) & 0x7fffffffu) != c.body) return;
+    const float4 a = hitA[i], b = hitB[i];
+    jbgpu_ray_hit o;
+    o.body = c.body;
+    o.fraction = a.w;
+    const V nn = nor(mk4(a));
+    o.normal[0] = nn.x; o.normal[1] = nn.y; o.normal[2] = nn.z;
+    o.point[0] = b.x; o.point[1] = b.y; o.point[2] = b.z;
+    out[c.ray] = o;
+}
+
+__global__ void k_sweep_finish(int n, const unsigned long long* key, const int* planeHit, jbgpu_ray_hit* out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    if (!planeHit[q] && key[q] != ~0ull) return;
+    jbgpu_ray_hit o;
+    o.body = planeHit[q] ? -2 : -1;
+    o.fraction = 1.0f;
+    o.normal[0] = o.normal[1] = o.normal[2] = 0.0f;
+    o.point[0] = o.point[1] = o.point[2] = 0.0f;
+    out[q] = o;
+}
+
+int query_sweeps(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb, int shape, const float* from,
+                 const float* to, const int* sweepWorld, int n, int group, int mask, jbgpu_ray_hit* hits, int sms,
+                 cudaStream_t s) {
+    if (n <= 0) return JBGPU_OK;
+    if (!grow_ray_buffers(qb, n)) return JBGPU_ERR_CUDA;
+    if (n > qb.capSweeps) {
+        void* old[] = {qb.sweepMin, qb.sweepMax, qb.sweepPlane, qb.sweepFrom, qb.sweepTo};
+        for (void* p : old)
+            if (p) cudaFree(p);
+        qb.sweepMin = qb.sweepMax = nullptr;
+        qb.sweepPlane = nullptr;
+        qb.sweepFrom = qb.sweepTo = nullptr;
+        const int c = n > 2 * qb.capSweeps ? n : 2 * qb.capSweeps;
+        qb.capSweeps = 0;
+        if (cudaMalloc((void**)&qb.sweepMin, sizeof(float4) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.sweepMax, sizeof(float4) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.sweepPlane, sizeof(int) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.sweepFrom, sizeof(float) * 3 * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&qb.sweepTo, sizeof(float) * 3 * (size_t)c) != cudaSuccess)
+            return JBGPU_ERR_CUDA;
+        qb.capSweeps = c;
+    }
+    cudaMemsetAsync(qb.key, 0xff, sizeof(unsigned long long) * n, s);
+    cudaMemsetAsync(qb.sweepPlane, 0, sizeof(int) * n, s);
+    DevWorld wq = w;
+    wq.amin = qb.qmin;
+    wq.amax = qb.qmax;
+    Bvh tree = bb.bvh;
+    tree.node = qb.node;
+    k_sweep_prep<<<gridn(n, 128), 128, 0, s>>>(w, shape, from, to, n, qb.sweepMin, qb.sweepMax, qb.sweepFrom, qb.sweepTo);
+    note_launch();
+    // a walk per sweep once the batch fills the GPU, else the (sweep, body) grid
+    const bool walk = (long long)n >= 8LL * sms * RAY_THREADS;
+    const dim3 grid(gridn(w.nBodies, 128), n < 65535 ? n : 65535);
+    if (walk) {
+        k_ray_walk<true, true><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(
+            w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList, bb.planeStart, qb.sweepFrom, qb.sweepTo, sweepWorld, n,
+            group, mask, qb.rayCnt, nullptr, nullptr, qb.sweepMin, qb.sweepMax);
+        note_launch();
+        exclusive_scan(qb.rayCnt, qb.rayOff, qb.candTotal, n, qb.scanScratch, s);
+    } else {
+        cudaMemsetAsync(qb.candTotal, 0, sizeof(int), s);
+        k_sweep_list<true><<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, group, mask, qb.sweepMin,
+                                                 qb.sweepMax, qb.candTotal, nullptr, 0);
+        note_launch();
+    }
+    int total = 0;
+    if (cudaMemcpyAsync(&total, qb.candTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return JBGPU_ERR_CUDA;
+    if (!grow_cand_buffers(qb, total)) return JBGPU_ERR_CUDA;
+    if (total > 0) {
+        RayCand* cand = (RayCand*)qb.cand;
+        if (walk) {
+            k_ray_walk<false, true><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(
+                w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList, bb.planeStart, qb.sweepFrom, qb.sweepTo, sweepWorld,
+                n, group, mask, nullptr, qb.rayOff, cand, qb.sweepMin, qb.sweepMax);
+        } else {
+            cudaMemsetAsync(qb.candTotal, 0, sizeof(int), s);
+            k_sweep_list<false><<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, group, mask,
+                                                      qb.sweepMin, qb.sweepMax, qb.candTotal, cand, total);
+        }
+        note_launch();
+        k_sweep_cast<<<gridn(total, RAY_THREADS), RAY_THREADS, 0, s>>>(w, cand, total, shape, from, to, qb.hitA, qb.hitB,
+                                                                     qb.key, qb.sweepPlane);
+        note_launch();
+        k_sweep_pick<<<gridn(total, 256), 256, 0, s>>>(cand, total, qb.hitA, qb.hitB, qb.key, hits);
+        note_launch();
+    }
+    k_sweep_finish<<<gridn(n, 256), 256, 0, s>>>(n, qb.key, qb.sweepPlane, hits);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? JBGPU_OK : JBGPU_ERR_CUDA;
+}
+
 void query_free(QueryBuffers& qb) {
     void* ps[] = {qb.qmin, qb.qmax, qb.node, qb.visit, qb.slow, qb.slowCount, qb.from, qb.to, qb.rayWorld, qb.hits,
                   qb.rayCnt, qb.rayOff, qb.candTotal, qb.key, qb.enterJ, qb.undecided, qb.scanScratch, qb.cand, qb.hitA,
-                  qb.hitB, qb.sweepMin, qb.sweepMax, qb.sweepKey, qb.sweepPlane};
+                  qb.hitB, qb.sweepMin, qb.sweepMax, qb.sweepPlane, qb.sweepFrom, qb.sweepTo};
     for (void* p : ps)
         if (p) cudaFree(p);
     qb = QueryBuffers();

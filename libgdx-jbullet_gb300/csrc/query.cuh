@@ -33,10 +33,11 @@ struct QueryBuffers {
     int* rayWorld = nullptr;
     jbgpu_ray_hit* hits = nullptr;
     int capIo = 0;
-    float4* sweepMin = nullptr;   // per sweep: the cast shape's temporal aabb, smallest hit key,
-    float4* sweepMax = nullptr;   // static plane on the path
-    unsigned long long* sweepKey = nullptr;
+    float4* sweepMin = nullptr;   // per sweep: the cast shape's temporal aabb, static plane on the
+    float4* sweepMax = nullptr;   // path, the path of the origins (3 floats each)
     int* sweepPlane = nullptr;
+    float* sweepFrom = nullptr;
+    float* sweepTo = nullptr;
     int capSweeps = 0;
 };
 
@@ -48,10 +49,11 @@ int query_prepare(const DevWorld& w, BroadphaseBuffers& bb, QueryBuffers& qb, cu
 int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb, const float* from, const float* to,
                const int* rayWorld, int n, int group, int mask, jbgpu_ray_hit* hits, int sms, cudaStream_t s);
 // n convex sweeps of shape `shape` (device buffers: 12-float transforms from / to, optional
-// per-sweep batch world) against the prepared boxes.  A sweep that reaches a static plane gets
-// body -2; *planeHits (device) counts those sweeps when non-null.
-int query_sweeps(const DevWorld& w, QueryBuffers& qb, int shape, const float* from, const float* to, const int* sweepWorld,
-                 int n, int group, int mask, jbgpu_ray_hit* hits, int* planeHits, cudaStream_t s);
+// per-sweep batch world) against the prepared boxes and tree.  A sweep that reaches a static
+// plane gets body -2.
+int query_sweeps(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb, int shape, const float* from,
+                 const float* to, const int* sweepWorld, int n, int group, int mask, jbgpu_ray_hit* hits, int sms,
+                 cudaStream_t s);
 void query_free(QueryBuffers& qb);
 
 }  // namespace jbg

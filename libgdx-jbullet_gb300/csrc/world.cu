@@ -1630,7 +1630,7 @@ int jbgpu_world_convex_sweep_test(jbgpu_world* w, int32_t shape, const float* fr
     rc = query_prepare(d, w->bb, Q, s);
     if (rc) return fail(rc, "sweep query preparation failed");
     if (deviceBuffers) {
-        rc = query_sweeps(d, Q, shape, from, to, sweepWorld, n, group, mask, hits, nullptr, s);
+        rc = query_sweeps(d, w->bb, Q, shape, from, to, sweepWorld, n, group, mask, hits, w->sms, s);
         return rc ? fail(rc, "sweep query failed") : JBGPU_OK;
     }
     float *df = nullptr, *dt = nullptr;
@@ -1643,7 +1643,7 @@ int jbgpu_world_convex_sweep_test(jbgpu_world* w, int32_t shape, const float* fr
     if (e == cudaSuccess) e = cudaMemcpyAsync(df, from, sizeof(float) * 12 * n, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(dt, to, sizeof(float) * 12 * n, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && sweepWorld) e = cudaMemcpyAsync(dw, sweepWorld, sizeof(int) * n, cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) rc = query_sweeps(d, Q, shape, df, dt, dw, n, group, mask, dh, nullptr, s);
+    if (e == cudaSuccess) rc = query_sweeps(d, w->bb, Q, shape, df, dt, dw, n, group, mask, dh, w->sms, s);
     if (e == cudaSuccess && !rc) e = cudaMemcpyAsync(hits, dh, sizeof(jbgpu_ray_hit) * n, cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     dfree(df); dfree(dt); dfree(dw); dfree(dh);

@@ -179,3 +179,25 @@ def test_mirror_convex_sweep_test(gpu_lib):
     with pytest.raises(RuntimeError):
         world.convexSweepTest(cast, D.Transform(origin=(3.0, 5.0, 0.0)), D.Transform(origin=(3.0, -5.0, 0.0)), miss)
     world.close()
+
+
+@pytest.mark.gpu
+def test_gpu_sweeps_tree_walk_batch(gpu_lib, oracle_lib):
+    """A batch large enough (at least 8 x SMs x 128 sweeps) to take the per-sweep tree walk instead
+    of the (sweep, body) grid: the same records as the oracle."""
+    sc = scenes.hinged_chains(chains=3, links=4, loose=6, seed=12, worlds=4)
+    g = GpuWorld(sc)
+    for _ in range(20):
+        g.step(sc.dt)
+    o = pyoracle.OracleWorld(sc)
+    H.copy_world(g, o, manifolds=False)
+    rng = np.random.Generator(np.random.PCG64(14))
+    n = 200_000
+    fr, to = _sweeps(rng, 2000, np.array([-4, 0, -4], F), np.array([4, 11, 4], F))
+    fr, to = np.tile(fr, (n // 2000, 1)), np.tile(to, (n // 2000, 1))
+    world = (np.arange(n) % 4).astype(np.int32)
+    shape = _cast_shapes(sc)[-1]
+    hg = g.convex_sweep_test(shape, fr, to, world=world, mask=NO_PLANE)
+    ho, _ = o.convex_sweep(shape, fr, to, world=world, mask=NO_PLANE)
+    assert _same(ho, hg) and (hg["body"] >= 0).sum() > 2000
+    g.close()
