@@ -690,9 +690,8 @@ int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb,
 
 // Candidates of a batch too small to fill the GPU with one walk per sweep: a thread per
 // (sweep, body) runs the walk's leaf test (filter, grown aabb entered before min(1, exit)).
-// COUNT adds up the candidates, else appends them (order is immaterial: the casts keep the
-// smallest key), at most cap.
-template <bool COUNT>
+// Counts the candidates and appends the first cap of them (order is immaterial: the casts keep
+// the smallest key).
 __global__ void k_sweep_list(DevWorld w, DevWorld wq, const float* ofrom, const float* oto, const int* sweepWorld, int n,
                              int group, int mask, const float4* gmin, const float4* gmax, int* counter, RayCand* cand,
                              int cap) {
@@ -718,7 +717,7 @@ __global__ void k_sweep_list(DevWorld w, DevWorld wq, const float* ofrom, const 
         int base = 0;
         if (lane == leader) base = atomicAdd(counter, __popc(m));
         base = __shfl_sync(act, base, leader);
-        if (COUNT || !pass) continue;
+        if (!pass) continue;
         const int idx = base + __popc(m & ((1u << lane) - 1u));
         if (idx < cap) {
             RayCand rc;
@@ -826,29 +825,32 @@ int query_sweeps(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& q
             group, mask, qb.rayCnt, nullptr, nullptr, qb.sweepMin, qb.sweepMax);
         note_launch();
         exclusive_scan(qb.rayCnt, qb.rayOff, qb.candTotal, n, qb.scanScratch, s);
-    } else {
+    } else {   // appended straight into the candidate buffer; listed again only if it overflowed
         cudaMemsetAsync(qb.candTotal, 0, sizeof(int), s);
-        k_sweep_list<true><<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, group, mask, qb.sweepMin,
-                                                 qb.sweepMax, qb.candTotal, nullptr, 0);
+        k_sweep_list<<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, group, mask, qb.sweepMin,
+                                          qb.sweepMax, qb.candTotal, (RayCand*)qb.cand, qb.capCand);
         note_launch();
     }
     int total = 0;
     if (cudaMemcpyAsync(&total, qb.candTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return JBGPU_ERR_CUDA;
+    const bool listed = !walk && total <= qb.capCand;
     if (!grow_cand_buffers(qb, total)) return JBGPU_ERR_CUDA;
     if (total > 0) {
         RayCand* cand = (RayCand*)qb.cand;
-        if (walk) {
-            k_ray_walk<false, true><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(
-                w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList, bb.planeStart, qb.sweepFrom, qb.sweepTo, sweepWorld,
-                n, group, mask, nullptr, qb.rayOff, cand, qb.sweepMin, qb.sweepMax);
-        } else {
-            cudaMemsetAsync(qb.candTotal, 0, sizeof(int), s);
-            k_sweep_list<false><<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, group, mask,
-                                                      qb.sweepMin, qb.sweepMax, qb.candTotal, cand, total);
+        if (!listed) {
+            if (walk) {
+                k_ray_walk<false, true><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(
+                    w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList, bb.planeStart, qb.sweepFrom, qb.sweepTo, sweepWorld,
+                    n, group, mask, nullptr, qb.rayOff, cand, qb.sweepMin, qb.sweepMax);
+            } else {
+                cudaMemsetAsync(qb.candTotal, 0, sizeof(int), s);
+                k_sweep_list<<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, group, mask,
+                                                  qb.sweepMin, qb.sweepMax, qb.candTotal, cand, total);
+            }
+            note_launch();
         }
-        note_launch();
         k_sweep_cast<<<gridn(total, RAY_THREADS), RAY_THREADS, 0, s>>>(w, cand, total, shape, from, to, qb.hitA, qb.hitB,
                                                                      qb.key, qb.sweepPlane);
         note_launch();
