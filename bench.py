@@ -6,25 +6,35 @@ plane, dt = 1/120, 10 PGS iterations; a "step" is one internal single step of th
 pipeline (gravity, predict, aabbs, pairs, narrowphase, islands, solver, integrate,
 activation) over all bodies.  Metric: body-steps/s.
 
-  value  device-timed throughput: W warm-up steps, then K steps through jbgpu_world_step with
-         the world resident in HBM (per-step working set of bodies, pairs, manifolds and solver
-         rows exceeds the 129 MB L2; no separate flush), timed by CUDA events on the world's
-         stream.  The per-phase breakdown comes from a second run of the same steps with phase
-         event marks (the marks themselves cost time, so they stay out of the timed run).
-  e2e    the same K steps from a fresh world through the reference-facing call
-         jbgpu_world_step_simulation, each step with a host->device upload of per-body forces
-         (RigidBody.applyCentralForce) and a device->host read of all body transforms
-         (MotionState synchronisation), both from pinned host memory.
+Every measurement starts from the same point of the drop: the world is stepped --settle
+steps from rest (untimed; 300 by default, when most bodies have reached the pile), then W
+warm-up steps, then the K timed steps.  The timed window is steps settle+W .. settle+W+K-1.
+
+  value  device-timed throughput: K steps through jbgpu_world_step with the world resident in
+         HBM (per-step working set of bodies, pairs, manifolds and solver rows exceeds the
+         129 MB L2; no separate flush), timed by CUDA events on the world's stream.  The
+         per-phase breakdown comes from a second run of the same steps with phase event marks
+         (the marks themselves cost time, so they stay out of the timed run).
+  e2e    the same K steps through the reference-facing call jbgpu_world_step_simulation (the
+         W warm-up steps also go through it, which primes its time accumulator), each step with
+         a host->device upload of per-body forces (RigidBody.applyCentralForce) and a
+         device->host read of all body transforms (MotionState synchronisation), both from
+         pinned host memory; the steps counted are the executed ones, min(returned, maxSubSteps).
   roofline  the phase with the largest device time (CUDA events on the world's stream),
          algorithmic bytes from the per-step counters / measured phase time vs the measured
-         HBM copy bandwidth.
+         HBM copy bandwidth; traffic = the DRAM bytes of one ncu capture of that kernel,
+         scaled to the window's own algorithmic bytes per launch (profiles/traffic.json).
   cpu_baseline  the CPU restatement of the reference (oracle, one core, the reference's island
-         solver order) timed on windows of the same trajectory: GPU snapshots at steps
-         0, K/2 and K-window, each continued for --cpu-window steps.
+         solver order) continued for --cpu-window steps from GPU snapshots inside the timed
+         window.
 
---impl reference times that CPU restatement alone over the same W + K steps from the start.
-Multi-GPU: one process per GPU (torchrun); each rank steps an independent world (weak scaling,
-no collective on the data path); rank 0 prints the line.
+--impl reference times that CPU restatement on the same window: the GPU steps the world to
+the window's first step (untimed set-up), the oracle takes over its state and manifolds and
+is timed alone for K steps (within a time budget).
+Multi-GPU: one process per GPU (torchrun).  A batched workload (independent worlds) is split
+by world across the ranks (jbgpu.shard: greedy by N_w^2, no collective on the data path); a
+single-world workload runs an independent replica per rank.  Weak scaling; rank 0 prints the
+line.
 """
 import argparse
 import json
@@ -45,11 +55,14 @@ UNIT = "body-steps/s"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=600)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="mixed_100k")
     p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--settle", type=int, default=300, help="untimed steps from rest before the warm-up")
+    p.add_argument("--shard-cost", default="square", choices=["square", "linear"],
+                   help="per-world cost used to split a batched workload across ranks")
     p.add_argument("--cpu-window", type=int, default=10)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -190,6 +203,40 @@ def make_scene(name, seed):
     return scenes.SCENES[name](seed=seed)
 
 
+def rank_scene(args, rank, size):
+    """The scene this rank steps: its share of the worlds of a batched workload (split by
+    jbgpu.shard, no world on two ranks), else an independent replica (seed + rank)."""
+    from jbgpu import shard
+    sc = make_scene(args.workload, args.seed)
+    if size > 1 and sc.world_of_body is not None:
+        mine, parts = shard.shard_scene(sc, rank, size, cost=args.shard_cost)
+        return mine, {"mode": "sharded by world", "worlds": len(parts[rank]), "worlds_total": len(parts),
+                      "cost": args.shard_cost}
+    if size > 1:
+        sc = make_scene(args.workload, args.seed + rank)
+    return sc, {"mode": "replica" if size > 1 else "single", "worlds": 1 if sc.world_of_body is None
+                else int(sc.world_of_body.max()) + 1}
+
+
+def window(args):
+    first = args.settle + args.warmup
+    return first, first + args.steps - 1
+
+
+def bench_config(sc, args, iters):
+    """The config keys both arms print (the reference arm's line carries the same ones)."""
+    first, last = window(args)
+    return {"workload": sc.name, "bodies": sc.n_bodies, "dt": sc.dt, "iterations": iters, "seed": args.seed,
+            "settle_steps": args.settle, "warmup_steps": args.warmup,
+            "timed_steps": "%d..%d of the drop from rest" % (first, last),
+            "l2": "no flush: per-step working set (bodies, two pair/manifold buffers, solver rows) exceeds L2"}
+
+
+def advance(w, sc, n):
+    for _ in range(n):
+        w.step(sc.dt)
+
+
 def pinned(shape):
     try:
         import torch
@@ -200,33 +247,40 @@ def pinned(shape):
     return np.zeros(shape, np.float32)
 
 
-def run_cpu_baseline(scene, world_cls, snap_steps, window):
-    """Oracle (reference island order, 1 core) continued for `window` steps from GPU snapshots."""
+def snapshot_to_oracle(g, o):
+    """Hands a GPU world's state and manifolds to an oracle world (the CPU side then continues
+    from exactly the state the GPU reached)."""
+    st = g.get_state()
+    o.set_state({k: st[k] for k in ("transform", "linear_velocity", "angular_velocity", "inv_inertia_world",
+                                     "total_force", "total_torque", "aabb", "activation_state", "deactivation_time")})
+    o.set_manifolds(g.get_manifolds())
+
+
+def run_cpu_baseline(scene, world_cls, cfg, snap_steps, window_len):
+    """Oracle (reference island order, 1 core) continued for `window_len` steps from GPU
+    snapshots at the given steps of the trajectory from rest."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    from jbgpu import _abi
-    g = world_cls(scene)
-    o = pyoracle.OracleWorld(scene, order_mode=pyoracle.ORDER_REFERENCE)
+    g = world_cls(scene, config=cfg)
+    g.set_graph(True)
     done, total_t, total_steps = 0, 0.0, 0
     for s in sorted(set(snap_steps)):
-        while done < s:
-            g.step(scene.dt)
-            done += 1
-        st = g.get_state()
-        o.set_state({k: st[k] for k in ("transform", "linear_velocity", "angular_velocity", "inv_inertia_world",
-                                         "total_force", "total_torque", "aabb", "activation_state", "deactivation_time")})
-        o.set_manifolds(g.get_manifolds())
+        advance(g, scene, s - done)
+        done = s
+        o = pyoracle.OracleWorld(scene, order_mode=pyoracle.ORDER_REFERENCE)
+        snapshot_to_oracle(g, o)
         t0 = time.perf_counter()
-        for _ in range(window):
+        for _ in range(window_len):
             o.step(scene.dt)
         total_t += time.perf_counter() - t0
-        total_steps += window
+        total_steps += window_len
+        del o
     g.close()
     value = scene.n_bodies * total_steps / total_t
     return {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": "CPU restatement of the reference (oracle, 1 thread, reference island solver order): %d-step windows "
-                      "from GPU snapshots at steps %s of the %s trajectory, %.1f s of CPU work" % (
-                          window, sorted(set(snap_steps)), scene.name, total_t)}
+                      "from GPU snapshots at steps %s of the %s trajectory from rest, %.1f s of CPU work" % (
+                          window_len, sorted(set(snap_steps)), scene.name, total_t)}
 
 
 def measure_rays(w, scene, nrays, seed, local):
@@ -345,11 +399,26 @@ def measure_sweeps(w, scene, nsweeps, seed, local):
             "clock": "CUDA events on the world's stream around 3 batches of device buffers"}
 
 
+def traffic_for_window(dom, window_bytes):
+    """DRAM bytes per launch of the dominant kernel for this window: one ncu capture's
+    dram__bytes_read.sum + dram__bytes_write.sum, scaled by the window's algorithmic bytes per
+    launch over the capture's (profiles/traffic.json)."""
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(tp):
+        return None, None
+    rec = json.load(open(tp)).get(dom)
+    if not isinstance(rec, dict) or not rec.get("algorithmic_bytes"):
+        return None, None
+    scale = window_bytes / rec["algorithmic_bytes"]
+    return rec["dram_bytes"] * scale, {"captured": rec.get("captured"), "capture_dram_bytes": rec["dram_bytes"],
+                                       "capture_algorithmic_bytes": rec["algorithmic_bytes"], "scale": scale}
+
+
 def run_ours(args, dist):
     from jbgpu import _abi, _build, lib
     from jbgpu.lib import GpuWorld
     _build.build()
-    sc = make_scene(args.workload, args.seed + dist.rank)
+    sc, split = rank_scene(args, dist.rank, dist.size)
     cfg = _abi.default_config(**sc.config)
     cfg.device = dist.local
     cfg.solver_parts = args.solver_parts
@@ -365,13 +434,13 @@ def run_ours(args, dist):
             setattr(cfg, k, v)
     iters = cfg.num_iterations
     n = sc.n_bodies
-    K, W = args.steps, args.warmup
+    K, W, S = args.steps, args.warmup, args.settle
+    first, last = window(args)
     # ---- device-timed run: CUDA events on the world's stream around K steps ----------------
     w = GpuWorld(sc, config=cfg)
     if args.graph:
         w.set_graph(True)
-    for _ in range(W):
-        w.step(sc.dt)
+    advance(w, sc, S + W)
     clk = ClockSampler(dist.local)
     clk.start()
     dist.barrier()
@@ -402,11 +471,11 @@ def run_ours(args, dist):
     elapsed = dist.max(device_ms * 1e-3)
     # ---- the same steps again with per-phase event marks (the breakdown and the roofline) ---
     w = GpuWorld(sc, config=cfg)
-    for _ in range(W):
-        w.step(sc.dt)
+    if args.graph:
+        w.set_graph(True)
+    advance(w, sc, S + W)
     w.set_profiling(K)
-    for _ in range(K):
-        w.step(sc.dt)
+    advance(w, sc, K)
     w.synchronize()
     phases, nsteps, window_ms = w.phase_times()
     ctrs = w.profile_counters()
@@ -428,14 +497,13 @@ def run_ours(args, dist):
     if by and by[0] is not None:
         achieved = sum(by) / (phases[dom] * 1e-3) / 1e9
         peak = pk["hbm_gbs"] if pk else 6800.0
-        traffic = None
-        tp = os.path.join(ROOT, "profiles", "traffic.json")
-        if os.path.exists(tp):
-            traffic = json.load(open(tp)).get(dom)
+        per_launch = sum(by) / len(by)
+        traffic, traffic_src = traffic_for_window(dom, per_launch)
         roof = {"bound": "hbm", "kernel_phase": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic,
-                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "fallback 6.8 TB/s",
-                "algorithmic_bytes_per_launch": sum(by) / len(by)}
+                "frac": achieved / peak, "traffic": traffic, "traffic_from": traffic_src,
+                "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "of fallback 6.8 TB/s",
+                "algorithmic_bytes_per_launch": per_launch,
+                "timing": "CUDA events around the phase on the world's stream, profiled run of the same window"}
     # ---- end to end through the reference-facing call with host buffers --------------------
     e2e = None
     if not args.no_e2e:
@@ -444,29 +512,33 @@ def run_ours(args, dist):
             w.set_graph(True)
         force = pinned((n, 3))
         xout = pinned((n, 12))
+        advance(w, sc, S)
         for _ in range(W):
-            w.step(sc.dt)
+            w.apply_forces(force, None)
+            w.step_simulation(sc.dt, 1, sc.dt)
+            w.get_transforms(xout)
         dist.barrier()
         w.synchronize()
         ts = time.perf_counter()
-        sub = 0
+        executed = 0
         for _ in range(K):
             w.apply_forces(force, None)
-            sub += w.step_simulation(sc.dt, 1, sc.dt)
+            executed += min(w.step_simulation(sc.dt, 1, sc.dt), 1)
             w.get_transforms(xout)
         te = time.perf_counter()
         dist.barrier()
         w.close()
         e_el = dist.max(te - ts)
-        e2e = {"value": dist.sum(n * sub) / e_el, "unit": UNIT, "h2d_bytes_per_step": int(force.nbytes),
-               "d2h_bytes_per_step": int(xout.nbytes), "substeps": sub,
-               "clock": "host wall clock around the K calls (each ends with its transforms on the host)"}
-    # ---- CPU baseline (rank 0, N = 1 only) ---------------------------------------------------
+        e2e = {"value": dist.sum(n * executed) / e_el, "unit": UNIT, "h2d_bytes_per_step": int(force.nbytes),
+               "d2h_bytes_per_step": int(xout.nbytes), "substeps": executed,
+               "clock": "host wall clock around the K calls (each ends with its transforms on the host)",
+               "call": "jbgpu_world_step_simulation(dt, maxSubSteps 1, fixedTimeStep dt); substeps = executed steps"}
+    # ---- CPU baseline (rank 0, N = 1 only): windows inside the timed window -----------------
     cpu = None
     if dist.rank == 0 and dist.size == 1 and not args.no_cpu:
-        total = W + K
-        snaps = [0, total // 2, max(0, total - args.cpu_window)]
-        cpu = run_cpu_baseline(sc, GpuWorld, snaps, args.cpu_window)
+        win = min(args.cpu_window, K)
+        snaps = [first, first + (K - win) // 2, first + K - win]
+        cpu = run_cpu_baseline(sc, GpuWorld, cfg, snaps, win)
     # ---- learned warm start vs the reference warm start at residual 1e-4 (rank 0) -----------
     learned = None
     if dist.rank == 0 and not args.no_learned:
@@ -476,17 +548,18 @@ def run_ours(args, dist):
             learned = warmstart.evaluate(m, seed=args.seed + 10, settle=900, steps=10)
             learned["weights"] = "jbgpu/warmstart_weights.npz (trained by python -m jbgpu.warmstart train)"
             m.close()
-    last = ctrs[-1] if ctrs else final
+    last_c = ctrs[-1] if ctrs else final
+    config = bench_config(sc, args, iters)
+    config["parallelism"] = split["mode"] if dist.size > 1 else "one world per GPU"
+    config["split"] = split
+    config["last_step_counters"] = {k: last_c[k] for k in ("pairs", "contacts", "solver_manifolds", "solver_rows",
+                                                           "colours", "cut_colours", "cut_manifolds", "islands",
+                                                           "gjk_calls", "epa_calls")}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.size, "steps": K, "warmup": W,
         "ms_per_step": elapsed * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic: seeded PCG64 scene generator (no dataset exists for this workload)",
-        "config": {"workload": sc.name, "bodies": n, "dt": sc.dt, "iterations": iters, "warmup_steps_from_rest": W,
-                   "timed_steps": "%d..%d of the drop" % (W, W + K - 1), "parallelism": "independent world per GPU",
-                   "l2": "no flush: per-step working set (bodies, two pair/manifold buffers, solver rows) exceeds L2",
-                   "last_step_counters": {k: last[k] for k in ("pairs", "contacts", "solver_manifolds", "solver_rows",
-                                                               "colours", "cut_colours", "cut_manifolds", "islands",
-                                                               "gjk_calls", "epa_calls")}},
+        "config": config,
         "timing": {"value_from": "CUDA events on the world's stream around the K steps (jbgpu_world_timer)",
                    "device_ms": device_ms, "host_wall_ms": wall * 1e3,
                    "phases_from": "a second run of the same steps with per-phase event marks",
@@ -508,18 +581,26 @@ def run_ours(args, dist):
 
 
 def run_reference(args, dist):
-    """The reference's CPU path (restated, 1 thread) on the same workload and steps."""
+    """The reference's CPU path (restated as the oracle, 1 thread) on the same window: the GPU
+    world is stepped from rest to the window's first step (untimed set-up), the oracle takes
+    over its state and manifolds and alone is timed over the K steps (within --ref-seconds)."""
     if dist.rank != 0:
         return None
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     pyoracle.build()
+    from jbgpu import _abi, _build
+    from jbgpu.lib import GpuWorld
+    _build.build()
     sc = make_scene(args.workload, args.seed)
+    cfg = _abi.default_config(**sc.config)
+    first, last = window(args)
+    g = GpuWorld(sc, config=cfg)
+    g.set_graph(True)
+    advance(g, sc, first)
     o = pyoracle.OracleWorld(sc, order_mode=pyoracle.ORDER_REFERENCE)
-    for _ in range(args.warmup):
-        o.step(sc.dt)
-    # the sample: the first steps of the timed window that fit in the time budget (the early,
-    # lighter steps of the drop, so the CPU rate it gives is if anything too high)
+    snapshot_to_oracle(g, o)
+    g.close()
     t0 = time.perf_counter()
     done = 0
     while done < args.steps:
@@ -529,14 +610,18 @@ def run_reference(args, dist):
             break
     el = time.perf_counter() - t0
     value = sc.n_bodies * done / el
-    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.size, "steps": done,
+    config = bench_config(sc, args, cfg.num_iterations)
+    config["parallelism"] = "one world, one host thread"
+    config["split"] = {"mode": "single", "worlds": 1 if sc.world_of_body is None else int(sc.world_of_body.max()) + 1}
+    sample = ("CPU restatement of the reference (oracle; no JVM on this machine), 1 thread, full workload, steps "
+              "%d..%d (%d of the %d asked, %.0f s budget), started from the GPU world's state and manifolds at step %d "
+              "(untimed set-up)" % (first, first + done - 1, done, args.steps, args.ref_seconds, first))
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.size, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el * 1e3 / done, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic: seeded PCG64 scene generator",
-            "config": {"workload": sc.name, "bodies": sc.n_bodies, "dt": sc.dt},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": "CPU restatement of the reference (no JVM on this machine), 1 thread, full "
-                                       "workload, steps %d..%d from rest (of %d asked; %.0f s budget)"
-                                       % (args.warmup, args.warmup + done - 1, args.steps, args.ref_seconds)},
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded PCG64 scene generator (no dataset exists for this workload)",
+            "config": config,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

@@ -279,9 +279,11 @@ int jbgpu_world_synchronize(jbgpu_world* world);
  * world each ray is cast in; filter_group / filter_mask are the callback's
  * collisionFilterGroup / collisionFilterMask (the reference's defaults: 1 and -1).  Rays see the
  * bodies' transforms after the last step.  hits receives one record per ray.  device_buffers
- * != 0: from, to, ray_world and hits are device pointers and the call returns once the work is
- * queued on the world's stream (jbgpu_world_synchronize waits for it); else host pointers, and
- * the call returns with the hits written. */
+ * != 0: from, to, ray_world and hits are device pointers (the call returns when the hits are
+ * written to device memory); else host pointers.  Errors: a ray world outside [0, worlds) is
+ * JBGPU_ERR_INVALID_ARGUMENT (host buffers: checked before any work; device buffers: such a ray
+ * finds nothing and the call reports it); a tree walk deeper than its stack, or a batch with more
+ * (ray, body) candidates than an int counts, is JBGPU_ERR_CAPACITY (split the batch). */
 int jbgpu_world_ray_test(jbgpu_world* world, const float* from, const float* to, const int32_t* ray_world, int32_t n,
                          int32_t filter_group, int32_t filter_mask, int32_t device_buffers, jbgpu_ray_hit* hits);
 /* CollisionWorld.convexSweepTest(castShape, convexFromWorld, convexToWorld,
@@ -291,7 +293,8 @@ int jbgpu_world_ray_test(jbgpu_world* world, const float* from, const float* to,
  * sweep_world, filter_group, filter_mask, device_buffers and hits as for jbgpu_world_ray_test.
  * Each hit's fraction is GjkConvexCast's time of impact, normal the normalised hit normal and
  * point the hit point on the body.  A sweep whose path reaches a static plane gets body -2: the
- * reference throws there (its concave branch calls a null caster). */
+ * reference throws there (its concave branch calls a null caster).  Errors as for
+ * jbgpu_world_ray_test. */
 int jbgpu_world_convex_sweep_test(jbgpu_world* world, int32_t shape, const float* from, const float* to,
                                   const int32_t* sweep_world, int32_t n, int32_t filter_group, int32_t filter_mask,
                                   int32_t device_buffers, jbgpu_ray_hit* hits);

@@ -10,7 +10,7 @@ namespace jbg {
 enum { SHAPE_BOX = 0, SHAPE_HULL = 4, SHAPE_SPHERE = 6, SHAPE_CAPSULE = 8, SHAPE_PLANE = 23 };
 enum { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEACTIVATION = 4, DISABLE_SIMULATION = 5 };
 enum { CF_STATIC = 1, CF_KINEMATIC = 2, CF_NO_CONTACT_RESPONSE = 4, CF_PLANE = 64 };
-enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8 };
+enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8, ST_BAD_WORLD = 16 };
 
 // Counters kept on the device (indices into DevWorld::ctr).
 enum {

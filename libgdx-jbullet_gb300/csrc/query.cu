@@ -19,6 +19,7 @@
 #include "gjk.cuh"
 #include "prims.cuh"
 #include "query.cuh"
+#include <climits>
 #include "shapes.cuh"
 
 namespace jbg {
@@ -255,13 +256,21 @@ template <bool COUNT, bool GROW = false>
 __global__ void __launch_bounds__(RAY_THREADS) k_ray_walk(DevWorld w, DevWorld wq, const int* sortedBody, Bvh tree,
                                                          const int* wroot, const int* planeList, const int* planeStart,
                                                          const float* from, const float* to, const int* rayWorld, int n,
-                                                         int group, int mask, int* cnt, const int* off, RayCand* cand,
-                                                         const float4* gmin = nullptr, const float4* gmax = nullptr) {
+                                                         int nWorlds, int group, int mask, int* cnt, const int* off,
+                                                         RayCand* cand, const float4* gmin = nullptr,
+                                                         const float4* gmax = nullptr) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const V f = mk(from[3 * r], from[3 * r + 1], from[3 * r + 2]);
     const V t = mk(to[3 * r], to[3 * r + 1], to[3 * r + 2]);
     const int wi = rayWorld ? rayWorld[r] : 0;
+    if (wi < 0 || wi >= nWorlds) {   // a world the batch does not have: no candidate, flagged
+        if (COUNT) {
+            cnt[r] = 0;
+            atomicOr(&w.ctr[C_STATUS], ST_BAD_WORLD);
+        }
+        return;
+    }
     const int base = COUNT ? 0 : off[r];
     const float4 g0 = GROW ? gmin[r] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const float4 g1 = GROW ? gmax[r] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -620,7 +629,8 @@ static bool grow_ray_buffers(QueryBuffers& qb, int n) {
         qb.capRays = c;
     }
     if (!qb.slowCount && (cudaMalloc((void**)&qb.slowCount, sizeof(int)) != cudaSuccess ||
-                          cudaMalloc((void**)&qb.candTotal, sizeof(int)) != cudaSuccess))
+                          cudaMalloc((void**)&qb.candTotal, sizeof(int)) != cudaSuccess ||
+                          cudaMalloc((void**)&qb.candTotal64, sizeof(unsigned long long)) != cudaSuccess))
         return false;
     return true;
 }
@@ -643,6 +653,32 @@ static bool grow_cand_buffers(QueryBuffers& qb, int total) {
     return true;
 }
 
+// 64-bit sum of the walk's per-ray candidate counts: the int scan that places the candidates is
+// only used when this total fits in an int.
+__global__ void k_total64(const int* cnt, int n, unsigned long long* total) {
+    unsigned long long v = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v += (unsigned)cnt[i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(total, v);
+}
+
+// The candidate total of a walk (per-ray counts already scanned into qb.candTotal): summed again
+// in 64 bits, so that a batch whose (ray, body) candidates do not fit in an int is refused
+// (JBGPU_ERR_CAPACITY: split the batch) instead of wrapping.
+static int candidate_total(QueryBuffers& qb, int n, cudaStream_t s, int& total) {
+    cudaMemsetAsync(qb.candTotal64, 0, sizeof(unsigned long long), s);
+    const int blocks = gridn(n, 256) < 1024 ? gridn(n, 256) : 1024;
+    k_total64<<<blocks, 256, 0, s>>>(qb.rayCnt, n, qb.candTotal64);
+    note_launch();
+    unsigned long long t64 = 0;
+    if (cudaMemcpyAsync(&total, qb.candTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(&t64, qb.candTotal64, sizeof(t64), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return JBGPU_ERR_CUDA;
+    if (t64 > (unsigned long long)INT_MAX) return JBGPU_ERR_CAPACITY;
+    return JBGPU_OK;
+}
+
 int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb, const float* from, const float* to,
                const int* rayWorld, int n, int group, int mask, jbgpu_ray_hit* hits, int sms, cudaStream_t s) {
     if (n <= 0) return JBGPU_OK;
@@ -658,20 +694,19 @@ int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb,
     tree.node = qb.node;
     if (!qb.replayAll) {
         k_ray_walk<true><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList,
-                                                                        bb.planeStart, from, to, rayWorld, n, group, mask,
-                                                                        qb.rayCnt, nullptr, nullptr);
+                                                                        bb.planeStart, from, to, rayWorld, n, bb.nWorlds,
+                                                                        group, mask, qb.rayCnt, nullptr, nullptr);
         note_launch();
         exclusive_scan(qb.rayCnt, qb.rayOff, qb.candTotal, n, qb.scanScratch, s);
         int total = 0;
-        if (cudaMemcpyAsync(&total, qb.candTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-            cudaStreamSynchronize(s) != cudaSuccess)
-            return JBGPU_ERR_CUDA;
+        if ((rc = candidate_total(qb, n, s, total)) != JBGPU_OK) return rc;
         if (!grow_cand_buffers(qb, total)) return JBGPU_ERR_CUDA;
         if (total > 0) {
             RayCand* cand = (RayCand*)qb.cand;
             k_ray_walk<false><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(w, wq, bb.sortedBody, tree, bb.wroot,
                                                                              bb.planeList, bb.planeStart, from, to, rayWorld,
-                                                                             n, group, mask, nullptr, qb.rayOff, cand);
+                                                                             n, bb.nWorlds, group, mask, nullptr, qb.rayOff,
+                                                                             cand);
             note_launch();
             k_ray_cast<<<gridn(total, RAY_THREADS), RAY_THREADS, 0, s>>>(w, cand, total, from, to, qb.hitA, qb.hitB, qb.key);
             note_launch();
@@ -693,8 +728,8 @@ int query_rays(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& qb,
 // Counts the candidates and appends the first cap of them (order is immaterial: the casts keep
 // the smallest key).
 __global__ void k_sweep_list(DevWorld w, DevWorld wq, const float* ofrom, const float* oto, const int* sweepWorld, int n,
-                             int group, int mask, const float4* gmin, const float4* gmax, int* counter, RayCand* cand,
-                             int cap) {
+                             int nWorlds, int group, int mask, const float4* gmin, const float4* gmax,
+                             unsigned long long* counter, RayCand* cand, int cap) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= w.nBodies) return;
     const int lane = threadIdx.x & 31;
@@ -704,7 +739,9 @@ __global__ void k_sweep_list(DevWorld w, DevWorld wq, const float* ofrom, const 
     for (int q = blockIdx.y; q < n; q += gridDim.y) {
         bool pass = false;
         float enter = 0.0f, exit;
-        if (filt && bw == (sweepWorld ? sweepWorld[q] : 0)) {
+        const int sw = sweepWorld ? sweepWorld[q] : 0;
+        if (b == 0 && (sw < 0 || sw >= nWorlds)) atomicOr(&w.ctr[C_STATUS], ST_BAD_WORLD);
+        if (filt && bw == sw) {
             const V f = mk(ofrom[3 * q], ofrom[3 * q + 1], ofrom[3 * q + 2]);
             const V t = mk(oto[3 * q], oto[3 * q + 1], oto[3 * q + 2]);
             pass = ray_aabb_parts(f, t, add(amn, mk4(gmin[q])), add(amx, mk4(gmax[q])), enter, exit) &&
@@ -714,12 +751,12 @@ __global__ void k_sweep_list(DevWorld w, DevWorld wq, const float* ofrom, const 
         const unsigned m = __ballot_sync(act, pass);
         if (!m) continue;
         const int leader = __ffs(m) - 1;
-        int base = 0;
-        if (lane == leader) base = atomicAdd(counter, __popc(m));
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(m));
         base = __shfl_sync(act, base, leader);
         if (!pass) continue;
-        const int idx = base + __popc(m & ((1u << lane) - 1u));
-        if (idx < cap) {
+        const unsigned long long idx = base + __popc(m & ((1u << lane) - 1u));
+        if (idx < (unsigned long long)cap) {
             RayCand rc;
             rc.ray = q;
             rc.body = b;
@@ -822,19 +859,27 @@ int query_sweeps(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& q
     if (walk) {
         k_ray_walk<true, true><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(
             w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList, bb.planeStart, qb.sweepFrom, qb.sweepTo, sweepWorld, n,
-            group, mask, qb.rayCnt, nullptr, nullptr, qb.sweepMin, qb.sweepMax);
+            bb.nWorlds, group, mask, qb.rayCnt, nullptr, nullptr, qb.sweepMin, qb.sweepMax);
         note_launch();
         exclusive_scan(qb.rayCnt, qb.rayOff, qb.candTotal, n, qb.scanScratch, s);
     } else {   // appended straight into the candidate buffer; listed again only if it overflowed
-        cudaMemsetAsync(qb.candTotal, 0, sizeof(int), s);
-        k_sweep_list<<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, group, mask, qb.sweepMin,
-                                          qb.sweepMax, qb.candTotal, (RayCand*)qb.cand, qb.capCand);
+        cudaMemsetAsync(qb.candTotal64, 0, sizeof(unsigned long long), s);
+        k_sweep_list<<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, bb.nWorlds, group, mask,
+                                          qb.sweepMin, qb.sweepMax, qb.candTotal64, (RayCand*)qb.cand, qb.capCand);
         note_launch();
     }
     int total = 0;
-    if (cudaMemcpyAsync(&total, qb.candTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-        return JBGPU_ERR_CUDA;
+    if (walk) {
+        const int rc = candidate_total(qb, n, s, total);
+        if (rc != JBGPU_OK) return rc;
+    } else {
+        unsigned long long t64 = 0;
+        if (cudaMemcpyAsync(&t64, qb.candTotal64, sizeof(t64), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return JBGPU_ERR_CUDA;
+        if (t64 > (unsigned long long)INT_MAX) return JBGPU_ERR_CAPACITY;
+        total = (int)t64;
+    }
     const bool listed = !walk && total <= qb.capCand;
     if (!grow_cand_buffers(qb, total)) return JBGPU_ERR_CUDA;
     if (total > 0) {
@@ -843,11 +888,11 @@ int query_sweeps(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& q
             if (walk) {
                 k_ray_walk<false, true><<<gridn(n, RAY_THREADS), RAY_THREADS, 0, s>>>(
                     w, wq, bb.sortedBody, tree, bb.wroot, bb.planeList, bb.planeStart, qb.sweepFrom, qb.sweepTo, sweepWorld,
-                    n, group, mask, nullptr, qb.rayOff, cand, qb.sweepMin, qb.sweepMax);
+                    n, bb.nWorlds, group, mask, nullptr, qb.rayOff, cand, qb.sweepMin, qb.sweepMax);
             } else {
-                cudaMemsetAsync(qb.candTotal, 0, sizeof(int), s);
-                k_sweep_list<<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, group, mask,
-                                                  qb.sweepMin, qb.sweepMax, qb.candTotal, cand, total);
+                cudaMemsetAsync(qb.candTotal64, 0, sizeof(unsigned long long), s);
+                k_sweep_list<<<grid, 128, 0, s>>>(w, wq, qb.sweepFrom, qb.sweepTo, sweepWorld, n, bb.nWorlds, group, mask,
+                                                  qb.sweepMin, qb.sweepMax, qb.candTotal64, cand, total);
             }
             note_launch();
         }
@@ -864,7 +909,7 @@ int query_sweeps(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& q
 
 void query_free(QueryBuffers& qb) {
     void* ps[] = {qb.qmin, qb.qmax, qb.node, qb.visit, qb.slow, qb.slowCount, qb.from, qb.to, qb.rayWorld, qb.hits,
-                  qb.rayCnt, qb.rayOff, qb.candTotal, qb.key, qb.enterJ, qb.undecided, qb.scanScratch, qb.cand, qb.hitA,
+                  qb.rayCnt, qb.rayOff, qb.candTotal, qb.candTotal64, qb.key, qb.enterJ, qb.undecided, qb.scanScratch, qb.cand, qb.hitA,
                   qb.hitB, qb.sweepMin, qb.sweepMax, qb.sweepPlane, qb.sweepFrom, qb.sweepTo};
     for (void* p : ps)
         if (p) cudaFree(p);

@@ -22,6 +22,7 @@ struct QueryBuffers {
     int* undecided = nullptr;
     void* scanScratch = nullptr;
     int* candTotal = nullptr;
+    unsigned long long* candTotal64 = nullptr;   // the same total in 64 bits (refuses overflowing batches)
     int capRays = 0;
     void* cand = nullptr;         // (ray, body, aabb entry) candidates and their hits
     float4* hitA = nullptr;

@@ -367,6 +367,7 @@ int check_status(jbgpu_world* w) {
     if (st & ST_TIMEOUT) return fail(JBGPU_ERR_TIMEOUT, "a bounded device wait gave up");
     if (st & ST_EPA_POOL) return fail(JBGPU_ERR_EPA_OVERFLOW, "EPA face pool overflow");
     if (st & ST_CAPACITY) return fail(JBGPU_ERR_CAPACITY, "device capacity exceeded (traversal stack or colours)");
+    if (st & ST_BAD_WORLD) return fail(JBGPU_ERR_INVALID_ARGUMENT, "a ray or sweep names a batch world the world does not have");
     return JBGPU_OK;
 }
 
@@ -1566,6 +1567,7 @@ int jbgpu_world_ray_test(jbgpu_world* w, const float* from, const float* to, con
     }
     DevWorld d = dev_view(w);
     QueryBuffers& Q = w->qb;
+    CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), s));   // traversal-stack and world-id flags of this call
     rc = query_prepare(d, w->bb, Q, s);
     if (rc) return fail(rc, "ray query preparation failed");
     const float* df = from;
@@ -1589,12 +1591,10 @@ int jbgpu_world_ray_test(jbgpu_world* w, const float* from, const float* to, con
         dh = Q.hits;
     }
     rc = query_rays(d, w->bb, Q, df, dt, dw, n, group, mask, dh, w->sms, s);
-    if (rc) return fail(rc, "ray query failed");
-    if (!deviceBuffers) {
-        CK(cudaMemcpyAsync(hits, Q.hits, sizeof(jbgpu_ray_hit) * n, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-    }
-    return JBGPU_OK;
+    if (rc) return fail(rc, rc == JBGPU_ERR_CAPACITY ? "too many (ray, body) candidates in one batch: split the batch"
+                                                     : "ray query failed");
+    if (!deviceBuffers) CK(cudaMemcpyAsync(hits, Q.hits, sizeof(jbgpu_ray_hit) * n, cudaMemcpyDeviceToHost, s));
+    return check_status(w);   // a traversal stack overflow or a bad world id is an error, not a silent miss
 }
 
 int jbgpu_world_convex_sweep_test(jbgpu_world* w, int32_t shape, const float* from, const float* to,
@@ -1627,11 +1627,14 @@ int jbgpu_world_convex_sweep_test(jbgpu_world* w, int32_t shape, const float* fr
     }
     DevWorld d = dev_view(w);
     QueryBuffers& Q = w->qb;
+    CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), s));   // traversal-stack and world-id flags of this call
     rc = query_prepare(d, w->bb, Q, s);
     if (rc) return fail(rc, "sweep query preparation failed");
     if (deviceBuffers) {
         rc = query_sweeps(d, w->bb, Q, shape, from, to, sweepWorld, n, group, mask, hits, w->sms, s);
-        return rc ? fail(rc, "sweep query failed") : JBGPU_OK;
+        if (rc) return fail(rc, rc == JBGPU_ERR_CAPACITY ? "too many (sweep, body) candidates in one batch: split the batch"
+                                                         : "sweep query failed");
+        return check_status(w);
     }
     float *df = nullptr, *dt = nullptr;
     int* dw = nullptr;
@@ -1648,7 +1651,9 @@ int jbgpu_world_convex_sweep_test(jbgpu_world* w, int32_t shape, const float* fr
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     dfree(df); dfree(dt); dfree(dw); dfree(dh);
     if (e != cudaSuccess) return fail(JBGPU_ERR_CUDA, cudaGetErrorString(e));
-    return rc ? fail(rc, "sweep query failed") : JBGPU_OK;
+    if (rc) return fail(rc, rc == JBGPU_ERR_CAPACITY ? "too many (sweep, body) candidates in one batch: split the batch"
+                                                     : "sweep query failed");
+    return check_status(w);
 }
 
 int jbgpu_world_set_graph(jbgpu_world* w, int32_t on) {

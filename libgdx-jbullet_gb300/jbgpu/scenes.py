@@ -266,6 +266,12 @@ def hulls(n=20_000, seed=0, box=60.0, y0=1.0, npts=32, steps=400):
                  shapes, bodies, meta={"seed": seed})
 
 
+def batched_world_counts(n_worlds=4096, seed=0, nmin=16, nmax=2048):
+    """Body counts (plane excluded) of the worlds batched_worlds builds for the same arguments."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return np.exp(rng.uniform(np.log(nmin), np.log(nmax), n_worlds)).astype(int)
+
+
 def batched_worlds(n_worlds=4096, seed=0, nmin=16, nmax=2048, sphere_frac=0.1, steps=300):
     """n_worlds independent worlds with log-uniform[16, 2048] bodies each: 90% unit boxes
     (half-extent 0.5, mass 1) and 10% spheres of radius 0.5, each world with its own plane

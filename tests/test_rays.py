@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from jbgpu import _abi, scenes
-from jbgpu.lib import GpuWorld
+from jbgpu.lib import GpuWorld, JbgpuError
 
 import harness as H
 import pyoracle
@@ -117,6 +117,27 @@ def test_gpu_rays_batched_worlds_and_device_buffers(gpu_lib, oracle_lib):
     g.synchronize()
     hd = dh.cpu().numpy().view(_abi.RAY_HIT_DTYPE)
     assert _same(hg, hd)
+    # a world id outside the batch: rejected before any work from host buffers; from device
+    # buffers the ray finds nothing and the call reports the bad id
+    bad = world.copy()
+    bad[7] = 4
+    with pytest.raises(JbgpuError) as e:
+        g.ray_test(frm, to, world=bad)
+    assert e.value.code == _abi.ERR_INVALID_ARGUMENT
+    dw.copy_(torch.from_numpy(bad))
+    with pytest.raises(JbgpuError) as e:
+        g.ray_test_device(df.data_ptr(), dt.data_ptr(), len(frm), dh.data_ptr(), world_ptr=dw.data_ptr())
+    assert e.value.code == _abi.ERR_INVALID_ARGUMENT
+    g.synchronize()
+    hb = dh.cpu().numpy().view(_abi.RAY_HIT_DTYPE)
+    assert hb["body"][7] == -1
+    keep = np.arange(len(frm)) != 7
+    assert _same(hg[keep], hb[keep])
+    # and the next call with good ids succeeds again (the flag belongs to one call)
+    dw.copy_(torch.from_numpy(world))
+    g.ray_test_device(df.data_ptr(), dt.data_ptr(), len(frm), dh.data_ptr(), world_ptr=dw.data_ptr())
+    g.synchronize()
+    assert _same(hg, dh.cpu().numpy().view(_abi.RAY_HIT_DTYPE))
     g.close()
 
 
