@@ -138,7 +138,12 @@ typedef struct jbgpu_config {
                                            (jbgpu_world_set_graph); 0: their kernels are launched one
                                            by one.  Bit-identical results.  No counterpart in the
                                            reference. */
-    int32_t reserved[1];
+    int32_t solver_residual_scope;      /* with solver_residual > 0: 0 (default) tests the residual of
+                                           each island on its own rows (islands stop independently);
+                                           1 tests it once over all rows of the world (every island
+                                           iterates until max|lambda_k - lambda_k-1| over the world
+                                           / max(max|lambda_k| over the world, 1e-6) <= solver_residual).
+                                           No counterpart in the reference. */
 } jbgpu_config;
 
 typedef struct jbgpu_shape_desc {
@@ -318,6 +323,13 @@ int jbgpu_world_set_ray_replay(jbgpu_world* world, int32_t all);
  * the reference changes getSolverInfo().numIterations (dynamics/constraintsolver/
  * ContactSolverInfo.java:38): num_iterations (> 0), and solver_residual / solver_max_iterations
  * with the meaning of jbgpu_config. */
+/* Residual trace of the last step's solve, no counterpart in the reference (residual mode
+ * only): for iteration k = 0 .. *n - 1, out[2k] = max |lambda_k - lambda_k-1| and out[2k + 1] =
+ * max |lambda_k| over the rows still iterating (islands not yet converged; every row with
+ * solver_residual_scope 1), so out[2k] / max(out[2k + 1], 1e-6) is the residual the stopping
+ * test saw.  At most JBGPU_RESIDUAL_TRACE_MAX iterations are kept; out == NULL returns *n only. */
+#define JBGPU_RESIDUAL_TRACE_MAX 4096
+int jbgpu_world_get_residual_trace(jbgpu_world* world, float* out, int32_t cap, int32_t* n);
 int jbgpu_world_set_solver_iterations(jbgpu_world* world, int32_t num_iterations, float residual,
                                       int32_t max_iterations);
 
@@ -356,11 +368,13 @@ int jbgpu_mlp_train(jbgpu_mlp* mlp, int32_t epochs, int32_t batch, float learnin
  * the outputs map to normal = max(0, b + y0 (b + u)) and friction k = y(1+k) mu (b + u), clamped
  * to the cone.  The MLP must live on the world's device and outlive its use by the world. */
 int jbgpu_world_set_warmstart_mlp(jbgpu_world* world, jbgpu_mlp* mlp);
-/* Record features before and converged impulses after every solve (training data). */
+/* Record features before and impulses after every solve (training data): on 1 keeps, with
+ * solver_residual > 0, only points of islands that reached the residual; on 2 keeps every point
+ * (its impulses after the last iteration run, converged or not); 0 stops. */
 int jbgpu_world_set_sample_logging(jbgpu_world* world, int32_t on);
 /* The last solve's samples: x[n][24], t[n][3] (host buffers); with x or t NULL only *n is set;
- * n > capacity is JBGPU_ERR_CAPACITY with *n set.  With solver_residual > 0 only points of
- * islands that reached the residual are samples. */
+ * n > capacity is JBGPU_ERR_CAPACITY with *n set.  With solver_residual > 0 and logging mode 1
+ * only points of islands that reached the residual are samples. */
 int jbgpu_world_get_samples(jbgpu_world* world, float* x, float* t, int32_t capacity, int32_t* n);
 
 /* Point-to-point (ball-socket) joint: DiscreteDynamicsWorld.addConstraint(new

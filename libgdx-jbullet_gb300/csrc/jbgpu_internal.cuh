@@ -104,6 +104,7 @@ struct DevWorld {
     int numIter;
     float resTol;         // > 0: residual-terminated PGS
     int maxIter;          // iteration cap when resTol > 0
+    int resScope;         // 0: residual per island, 1: one residual over the world's rows
     float erp, warm, slop;
     int solverMode;
 };

@@ -1827,6 +1827,10 @@ JBD void island_residuals(const DevWorld& w, const SolverBuffers& sb, int flag, 
             if (ol > r.l) r.l = ol;
         }
         if (lane != 0) continue;
+        if (it <= JBGPU_RESIDUAL_TRACE_MAX) {   // the trace: maxima over every row still tested
+            atomicMax(&sb.resTrace[2 * (it - 1)], __float_as_uint(r.d));
+            atomicMax(&sb.resTrace[2 * (it - 1) + 1], __float_as_uint(r.l));
+        }
         float dm = r.d, lm = r.l;
         const int nch = (i1 - i0 + ISL_CHUNK - 1) / ISL_CHUNK;
         if (nch > 1) {
@@ -2040,7 +2044,8 @@ __global__ void k_isl_count(DevWorld w, DevRows R, SolverBuffers sb) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nSlots) return;
     int4 d = R.slot_desc[s];
-    int isl = w.island[d.x] >= 0 ? w.island[d.x] : w.island[d.y];
+    // world scope: every slot in one group (index 0), tested against one residual
+    int isl = w.resScope ? 0 : (w.island[d.x] >= 0 ? w.island[d.x] : w.island[d.y]);
     sb.slotIsl[s] = isl;
     atomicAdd(&sb.islCount[isl], 1);
 }
@@ -2101,10 +2106,10 @@ __global__ void k_contact_features(DevWorld w, DevPairs P, DevRows R, const int*
 
 // Targets of points whose island did not reach the residual (residual mode) are NaN: they are
 // not converged impulses, and the sample export leaves them out.
-__global__ void k_contact_targets(DevWorld w, DevRows R, SolverBuffers sb, float* T) {
+__global__ void k_contact_targets(DevWorld w, DevRows R, SolverBuffers sb, float* T, int allPoints) {
     const int nq = *R.nPts;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
-        if (w.resTol > 0.0f && __ldcg(&sb.islConv[sb.slotIsl[R.pt_key[q] >> 2]]) == 0) {
+        if (!allPoints && w.resTol > 0.0f && __ldcg(&sb.islConv[sb.slotIsl[R.pt_key[q] >> 2]]) == 0) {
             T[(size_t)q * 3 + 0] = T[(size_t)q * 3 + 1] = T[(size_t)q * 3 + 2] = __int_as_float(0x7fc00000);
             continue;
         }
@@ -2329,6 +2334,7 @@ void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, 
         cudaMemsetAsync(sb.islConv, 0, sizeof(int) * n, s);
         cudaMemsetAsync(sb.islAcc, 0, sizeof(int) * 2 * n, s);
         cudaMemsetAsync(sb.islDone, 0, sizeof(int) * n, s);
+        cudaMemsetAsync(sb.resTrace, 0, sizeof(unsigned) * 2 * JBGPU_RESIDUAL_TRACE_MAX, s);
         k_isl_count<<<gridn(nPairs, 256), 256, 0, s>>>(w, R, sb); note_launch();
         exclusive_scan(sb.islCount, sb.islStart, nullptr, n + 1, sb.islScratch, s);
         k_isl_scatter<<<gridn(std::max(nPairs, n), 256), 256, 0, s>>>(sb, n); note_launch();
@@ -2363,7 +2369,8 @@ void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& R, 
     }
     if (prof) prof->mark(PH_PGS, 1, s);
     if (learn.sampleT) {
-        k_contact_targets<<<std::min(gridn(nPairs * 4, 256), 4096), 256, 0, s>>>(w, R, sb, learn.sampleT);
+        k_contact_targets<<<std::min(gridn(nPairs * 4, 256), 4096), 256, 0, s>>>(w, R, sb, learn.sampleT,
+                                                                                 learn.allPoints);
         note_launch();
     }
 }

@@ -106,6 +106,7 @@ struct SolverBuffers {
     int* islAcc = nullptr;        // per island root: chunk maxima (float bits), 2 per island
     int* islDone = nullptr;       // per island root: chunks reduced this iteration
     int* nIslChunks = nullptr;    // device scalar
+    unsigned* resTrace = nullptr; // per iteration: max |delta lambda|, max |lambda| (float bits) of the rows tested
     void* islScratch = nullptr;   // scan scratch for nBodies + 1
     const int* order = nullptr;   // body order in use
     int nFinite = 0;
@@ -143,6 +144,7 @@ struct SolverLearn {
     const MlpDev* mlp = nullptr;    // non-null: warm-start impulses predicted by the MLP
     float* sampleX = nullptr;       // non-null: features written (capacity rows * 4 * 24)
     float* sampleT = nullptr;       // non-null: converged impulses written (rows * 4 * 3)
+    int allPoints = 0;              // 1: every point's impulses, also of islands not converged
 };
 int solver_learn_configure();     // once per world: shared-memory size of the warm-start kernel
 void solve_launch_learn(const DevWorld& w, DevPairs& P, int nPairs, DevRows& rows, SolverBuffers& sb, float dt,

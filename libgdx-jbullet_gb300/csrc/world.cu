@@ -124,6 +124,7 @@ struct jbgpu_world {
     jbgpu_mlp* mlp = nullptr;     // not owned
     bool learnReady = false;      // warm-start kernel configured
     bool logSamples = false;
+    bool logAll = false;          // samples of every point, not only of converged islands
     float* sampleX = nullptr;     // capRows * 4 * 24
     float* sampleT = nullptr;     // capRows * 4 * 3
     int sampleCap = 0;            // rows the sample buffers hold
@@ -241,6 +242,7 @@ int grow_bodies(jbgpu_world* w, int need) {
     CK(dalloc(&S.islAcc, 2 * (size_t)nc)); CK(dalloc(&S.islDone, nc));
     if (S.islScratch) cudaFree(S.islScratch);
     CK(cudaMalloc(&S.islScratch, scan_scratch_bytes(nc + 1)));
+    if (!S.resTrace) CK(dalloc(&S.resTrace, 2 * (size_t)JBGPU_RESIDUAL_TRACE_MAX));
     w->capBodies = nc;
     return JBGPU_OK;
 }
@@ -470,6 +472,7 @@ int run_stage(jbgpu_world* w, int stage, float dt) {
             }
             learn.sampleX = w->sampleX;
             learn.sampleT = w->sampleT;
+            learn.allPoints = w->logAll ? 1 : 0;
         }
         solve_launch_learn(d, w->pairs[w->cur], w->nPairs, w->rows, w->sb, dt, s, &P, learn);
         break;
@@ -911,6 +914,7 @@ int jbgpu_world_create(const jbgpu_config* cfg, jbgpu_world** out) {
     w->graphOn = c.step_graphs != 0;
     d.resTol = c.solver_residual > 0.0f ? c.solver_residual : 0.0f;
     d.maxIter = c.solver_max_iterations > 0 ? c.solver_max_iterations : 200;
+    d.resScope = c.solver_residual_scope != 0 ? 1 : 0;
     d.erp = c.erp;
     d.warm = c.warmstarting_factor;
     d.slop = c.linear_slop;
@@ -983,6 +987,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(V.bucket); dfree(V.bucketList); dfree(V.claim); dfree(V.taken); dfree(V.posOf); dfree(V.candLocal);
     dfree(V.md); dfree(V.ml); dfree(V.slotIsl); dfree(V.islList); dfree(V.islCount); dfree(V.islFill); dfree(V.islStart);
     dfree(V.segFlag); dfree(V.segIdx); dfree(V.islChunk); dfree(V.islConv); dfree(V.islAcc); dfree(V.islDone);
+    dfree(V.resTrace);
     {
         DevJoints& J = V.J;
         dfree(J.a); dfree(J.b); dfree(J.pivA); dfree(J.pivB); dfree(J.set); dfree(J.order); dfree(J.colStart);
@@ -1224,6 +1229,23 @@ int jbgpu_world_narrowphase_static(jbgpu_world* w, int32_t epa_slots) {
     return check_status(w);
 }
 
+int jbgpu_world_get_residual_trace(jbgpu_world* w, float* out, int32_t cap, int32_t* n) {
+    if (!w || !n || cap < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
+    CK(cudaSetDevice(w->device));
+    *n = 0;
+    if (!(w->dw.resTol > 0.0f) || !w->sb.resTrace) return JBGPU_OK;
+    int iters = 0;
+    CK(cudaMemcpyAsync(&iters, w->dw.ctr + C_PGS_ITERS, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    iters = std::max(0, std::min(iters, (int)JBGPU_RESIDUAL_TRACE_MAX));
+    *n = iters;
+    if (!out || iters == 0) return JBGPU_OK;
+    if (cap < iters) return fail(JBGPU_ERR_CAPACITY, "caller buffer too small");
+    CK(cudaMemcpyAsync(out, w->sb.resTrace, sizeof(float) * 2 * iters, cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    return JBGPU_OK;
+}
+
 int jbgpu_world_set_solver_iterations(jbgpu_world* w, int32_t num_iterations, float residual, int32_t max_iterations) {
     if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
     if (num_iterations < 0 || max_iterations < 0 || !(residual >= 0.0f))
@@ -1254,7 +1276,9 @@ int jbgpu_world_set_warmstart_mlp(jbgpu_world* w, jbgpu_mlp* mlp) {
 
 int jbgpu_world_set_sample_logging(jbgpu_world* w, int32_t on) {
     if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (on < 0 || on > 2) return fail(JBGPU_ERR_INVALID_ARGUMENT, "sample logging is 0, 1 or 2");
     w->logSamples = on != 0;
+    w->logAll = on == 2;
     return JBGPU_OK;
 }
 

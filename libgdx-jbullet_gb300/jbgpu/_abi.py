@@ -74,7 +74,7 @@ class Config(C.Structure):
         ("solver_smem_bodies", C.c_int32),
         ("broadphase_rebuild_interval", C.c_int32),
         ("step_graphs", C.c_int32),
-        ("reserved", C.c_int32 * 1),
+        ("solver_residual_scope", C.c_int32),
     ]
 
 

@@ -99,6 +99,7 @@ def lib():
             "jbgpu_mlp_train": ([C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_uint64, _abi.f32p], C.c_int),
             "jbgpu_world_set_warmstart_mlp": ([C.c_void_p, C.c_void_p], C.c_int),
             "jbgpu_world_set_solver_iterations": ([C.c_void_p, C.c_int32, C.c_float, C.c_int32], C.c_int),
+            "jbgpu_world_get_residual_trace": ([C.c_void_p, _abi.f32p, C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_set_sample_logging": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_get_samples": ([C.c_void_p, _abi.f32p, _abi.f32p, C.c_int32, _abi.i32p], C.c_int),
         }
@@ -124,6 +125,7 @@ EXPORTED = [
     "jbgpu_world_set_6dof_limit", "jbgpu_world_set_6dof_linear_motor", "jbgpu_world_set_6dof_angular_motor",
     "jbgpu_world_add_cone_twist", "jbgpu_world_set_cone_twist_limit", "jbgpu_world_set_cone_twist_angular_only",
     "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
+    "jbgpu_world_get_residual_trace",
 ]
 
 
@@ -473,12 +475,22 @@ class GpuWorld:
     def set_solver_iterations(self, num_iterations, residual=0.0, max_iterations=0):
         check(lib().jbgpu_world_set_solver_iterations(self.h, num_iterations, residual, max_iterations))
 
+    def residual_trace(self):
+        """(max |delta lambda|, max |lambda|) per iteration of the last step's residual-mode solve."""
+        n = C.c_int32()
+        check(lib().jbgpu_world_get_residual_trace(self.h, None, 0, C.byref(n)))
+        out = np.zeros((max(1, n.value), 2), np.float32)
+        check(lib().jbgpu_world_get_residual_trace(self.h, out.ctypes.data_as(_abi.f32p), len(out), C.byref(n)))
+        return out[:n.value]
+
     def set_warmstart_mlp(self, mlp):
         self._mlp = mlp
         check(lib().jbgpu_world_set_warmstart_mlp(self.h, mlp.h if mlp is not None else None))
 
-    def set_sample_logging(self, on=True):
-        check(lib().jbgpu_world_set_sample_logging(self.h, 1 if on else 0))
+    def set_sample_logging(self, on=True, all_points=False):
+        """Training samples of every solve: converged islands' points (all_points False) or every
+        point's impulses after the last iteration run (all_points True)."""
+        check(lib().jbgpu_world_set_sample_logging(self.h, (2 if all_points else 1) if on else 0))
 
     def get_samples(self):
         n = C.c_int32()

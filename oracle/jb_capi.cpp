@@ -48,6 +48,7 @@ void* orc_create(const jbgpu_config* c) {
         w->cfg.solverMode = c->solver_mode;
         w->cfg.residualTol = c->solver_residual;
         w->cfg.maxIterations = c->solver_max_iterations > 0 ? c->solver_max_iterations : 200;
+        w->cfg.residualScope = c->solver_residual_scope != 0 ? 1 : 0;
     }
     return w;
 }

@@ -1136,6 +1136,7 @@ static void solve_group(World& w, const std::vector<int>& manifolds, const std::
         for (size_t r = 0; r < rows.size(); r++) {
             const Manifold& m = w.pairMf[rows[r].mfPair];
             int tag = w.bodies[m.body0].islandTag >= 0 ? w.bodies[m.body0].islandTag : w.bodies[m.body1].islandTag;
+            if (cfg.residualScope) tag = 0;   // one group: the residual over all rows of the world
             auto it = index.find(tag);
             if (it == index.end()) it = index.emplace(tag, nIsl++).first;
             rowIsl[r] = it->second;

@@ -165,6 +165,7 @@ struct Config {
     int solverMode = SOLVER_CACHE_FRIENDLY | SOLVER_USE_WARMSTARTING;
     float residualTol = 0.0f;         // > 0: iterate to this residual per world (jbgpu_config.solver_residual)
     int maxIterations = 200;
+    int residualScope = 0;            // 1: one residual over the world's rows (jbgpu_config.solver_residual_scope)
 };
 
 struct Counters {

@@ -114,13 +114,15 @@ def test_range_parts_lockstep_bit_exact(gpu_lib, oracle_lib, name, parts):
 
 @pytest.mark.parametrize("name", ["stack", "mixed120", "boxes300"])
 @pytest.mark.parametrize("parts", [0, 3])
-def test_residual_mode_bit_exact(gpu_lib, oracle_lib, name, parts):
+@pytest.mark.parametrize("scope", [0, 1])
+def test_residual_mode_bit_exact(gpu_lib, oracle_lib, name, parts, scope):
     """Residual-terminated PGS (tolerance 1e-4, at most 60 iterations): the GPU stops after the
     same iteration as the oracle fed its order, and state and manifolds stay bit-identical.
     parts 0: one solver part per world (block-local residual); 3: range parts, cut manifolds
-    and a grid-wide residual."""
+    and a grid-wide residual.  scope 0: a residual per island; 1: one residual over the world's
+    rows."""
     sc = SCENES[name]()
-    cfg = dict(sc.config, solver_residual=1e-4, solver_max_iterations=60)
+    cfg = dict(sc.config, solver_residual=1e-4, solver_max_iterations=60, solver_residual_scope=scope)
     o = pyoracle.OracleWorld(sc, config=_abi.default_config(**cfg))
     g = GpuWorld(sc, config=_abi.default_config(**dict(cfg, solver_parts=parts)))
     iters = []
@@ -132,6 +134,14 @@ def test_residual_mode_bit_exact(gpu_lib, oracle_lib, name, parts):
         assert co["status_flags"] == 0 and cg["status_flags"] == 0, s
         assert co["solver_iterations"] == cg["solver_iterations"], (s, co["solver_iterations"], cg["solver_iterations"])
         iters.append(cg["solver_iterations"])
+        tr = g.residual_trace()
+        assert len(tr) == cg["solver_iterations"], s
+        if scope == 1 and len(tr) > 0:        # the trace holds the residual the stopping test saw
+            n, tol = len(tr), np.float32(1e-4)
+            r = tr[:, 0] / np.maximum(tr[:, 1], np.float32(1e-6))
+            assert np.all(r[:n - 1] > tol), (s, r)
+            if n < 60:                        # stopped by the test, not by the cap
+                assert r[n - 1] <= tol, (s, r)
         if s % 10 == 9 or s < 5:
             bs = H.compare_state(o.get_state(), g.get_state())
             bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
