@@ -73,6 +73,7 @@ def parse():
     p.add_argument("--rebuild-interval", type=int, default=None, help="jbgpu_config.broadphase_rebuild_interval")
     p.add_argument("--ref-seconds", type=float, default=120.0, help="time budget of the reference arm's timed steps")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start comparison")
+    p.add_argument("--learned-cap", type=int, default=12000, help="iteration cap of the world-residual comparison")
     p.add_argument("--no-rays", action="store_true", help="skip the rayTest batch measurement")
     p.add_argument("--sweeps", type=int, default=4096, help="convexSweepTest sweeps per measured batch (0: skip)")
     p.add_argument("--graph", type=int, default=1, help="1: replay the step as CUDA graphs (jbgpu_world_set_graph), 0: launches")
@@ -545,7 +546,12 @@ def run_ours(args, dist):
         from jbgpu import warmstart
         if os.path.exists(warmstart.WEIGHTS):
             m = warmstart.load(device=dist.local)
-            learned = warmstart.evaluate(m, seed=args.seed + 10, settle=900, steps=10)
+            # the benchmark's rule: every row of the world to residual 1e-4, with a cap the plain
+            # solve does not reach; the per-island rule at the 200 cap beside it
+            learned = warmstart.evaluate(m, seed=args.seed + 10, settle=900, steps=4, max_iter=args.learned_cap,
+                                         scope=1)
+            learned["per_island"] = warmstart.evaluate(m, seed=args.seed + 10, settle=900, steps=10, max_iter=200,
+                                                       scope=0)
             learned["weights"] = "jbgpu/warmstart_weights.npz (trained by python -m jbgpu.warmstart train)"
             m.close()
     last_c = ctrs[-1] if ctrs else final

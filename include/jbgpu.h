@@ -221,6 +221,8 @@ typedef struct jbgpu_counters {
     int32_t solver_islands_converged;  /* ... of which reached the residual */
     int32_t solver_island_iterations;  /* ... sum over them of the iterations they took */
     int32_t ray_replays;      /* rays of the last jbgpu_world_ray_test replayed in body order */
+    int32_t ccd_clamped;      /* bodies of the last integrateTransforms that ran a CCD sweep
+                                 (BulletStats.gNumClampedCcdMotions for one step) */
 } jbgpu_counters;
 
 /* One ray of a batch: CollisionWorld.ClosestRayResultCallback after the ray
@@ -274,6 +276,19 @@ int jbgpu_world_stage(jbgpu_world* world, int32_t stage, float time_step);
  * reference. */
 #define JBGPU_STATIC_EPA_SLOTS_MAX 32
 int jbgpu_world_narrowphase_static(jbgpu_world* world, int32_t epa_slots);
+
+/* CollisionObject.setCcdMotionThreshold / setCcdSweptSphereRadius for n bodies
+ * (collision/dispatch/CollisionObject.java:278-300; both 0 by default).  integrateTransforms
+ * (dynamics/DiscreteDynamicsWorld.java:679-739) then sweeps a sphere of the swept radius along
+ * the predicted motion of an active dynamic body whose displacement squared exceeds threshold^2,
+ * and moves the body only to the first time of impact above 0.0001 (ClosestNotMeConvexResult-
+ * Callback: not itself, the filters, objects it already touches with contact points - found only
+ * when the body precedes the object, as the reference's pair lookup does - and hits whose
+ * normal opposes the motion).  Bodies are clamped in index order, each sweep seeing the bodies
+ * before it where they ended.  A sweep that reaches a static plane, where the reference throws,
+ * makes the step return JBGPU_ERR_UNSUPPORTED (the body moves unclamped by the plane). */
+int jbgpu_world_set_ccd(jbgpu_world* world, const int32_t* bodies, const float* motion_threshold,
+                        const float* swept_sphere_radius, int32_t n);
 
 /* Wait for the world's stream. */
 int jbgpu_world_synchronize(jbgpu_world* world);

@@ -10,14 +10,14 @@ namespace jbg {
 enum { SHAPE_BOX = 0, SHAPE_HULL = 4, SHAPE_SPHERE = 6, SHAPE_CAPSULE = 8, SHAPE_PLANE = 23 };
 enum { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEACTIVATION = 4, DISABLE_SIMULATION = 5 };
 enum { CF_STATIC = 1, CF_KINEMATIC = 2, CF_NO_CONTACT_RESPONSE = 4, CF_PLANE = 64 };
-enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8, ST_BAD_WORLD = 16 };
+enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8, ST_BAD_WORLD = 16, ST_CCD_PLANE = 32 };
 
 // Counters kept on the device (indices into DevWorld::ctr).
 enum {
     C_PAIRS = 0, C_FILL_OVERFLOW, C_EPA_QUEUE, C_GJK, C_EPA, C_SOLVE_N, C_COLOURS, C_ISLANDS,
     C_MANIFOLDS, C_CONTACTS, C_ROWS, C_STATUS, C_BAR_COUNT, C_BAR_GEN, C_CUT_DONE, C_WIN0, C_WIN1, C_WIN2,
     C_PGS_ITERS, C_CUT_COLOURS, C_CUT_MANIFOLDS, C_RES0, C_RES1, C_RES2, C_ISL_N, C_ISL_CONV, C_ISL_ITERS,
-    C_PART_NEXT0, C_PART_NEXT1, C_NCTR = 32
+    C_PART_NEXT0, C_PART_NEXT1, C_CCD_N, C_CCD_BEST, C_NCTR = 32
 };
 
 struct DevShapes {
@@ -78,6 +78,7 @@ struct DevWorld {
     float4 *linvel, *angvel;
     float4 *iw0, *iw1, *iw2;        // inverse inertia tensor (world) rows
     float4 *iloc;                   // inverse inertia (local) xyz, inverse mass w
+    float *ccdThr, *ccdRad;         // CollisionObject.ccdMotionThreshold / ccdSweptSphereRadius
     float4 *force, *torque, *gravity;
     float4 *amin, *amax;            // broadphase proxy aabb
     int* act;

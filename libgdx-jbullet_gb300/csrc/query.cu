@@ -17,6 +17,7 @@
 // block each.
 #include "../../include/jbgpu.h"
 #include "gjk.cuh"
+#include "gridsync.cuh"
 #include "prims.cuh"
 #include "query.cuh"
 #include <climits>
@@ -475,8 +476,49 @@ __global__ void __launch_bounds__(SLOW_THREADS) k_rays_slow(DevWorld w, DevWorld
 // box grown by the cast shape's box, lists the (sweep, body) candidates; a thread per candidate
 // casts.
 
+JBD Xf xf12(const float* f) {
+    Xf t;
+    t.b.r[0] = mk(f[0], f[1], f[2]);
+    t.b.r[1] = mk(f[3], f[4], f[5]);
+    t.b.r[2] = mk(f[6], f[7], f[8]);
+    t.o = mk(f[9], f[10], f[11]);
+    return t;
+}
+
+// The box a cast shape sweeps from transform f to t, as convexSweepTest forms it:
 // TransformUtil.calculateVelocity / calculateDiffAxisAngle (linearmath/TransformUtil.java:105-153)
-// and CollisionShape.calculateTemporalAabb with getAngularMotionDisc (CollisionShape.java:44-121).
+// and CollisionShape.calculateTemporalAabb with getAngularMotionDisc (CollisionShape.java:44-121),
+// at the start rotation.  aabb(x, mn, mx) is the cast shape's getAabb.
+template <class AabbFn>
+JBD void cast_box(const Xf& f, const Xf& t, AabbFn aabb, V& cmin, V& cmax) {
+    const V linVel = scl(sub(t.o, f.o), jdiv(1.0f, 1.0f));
+    const Q dorn = qnor(q_from_matrix(mulMM(t.b, m3_invert(f.b))));
+    const float angle = __fmul_rn(2.0f, (float)acos((double)dorn.w));
+    V axis = mk(dorn.x, dorn.y, dorn.z);
+    const float l2 = len2(axis);
+    axis = l2 < __fmul_rn(FLT_EPS, FLT_EPS) ? mk(1.0f, 0.0f, 0.0f) : scl(axis, jdiv(1.0f, jsqrt(l2)));
+    const V angVel = scl(axis, jdiv(angle, 1.0f));
+    Xf R;
+    R.b = m_from_quat(q_from_matrix(f.b));
+    R.o = mk(0.0f, 0.0f, 0.0f);
+    V mn, mx;
+    aabb(R, mn, mx);
+    const V lin = scl(linVel, 1.0f);
+    if (lin.x > 0.0f) mx.x = __fadd_rn(mx.x, lin.x); else mn.x = __fadd_rn(mn.x, lin.x);
+    if (lin.y > 0.0f) mx.y = __fadd_rn(mx.y, lin.y); else mn.y = __fadd_rn(mn.y, lin.y);
+    if (lin.z > 0.0f) mx.z = __fadd_rn(mx.z, lin.z); else mn.z = __fadd_rn(mn.z, lin.z);
+    Xf I;
+    I.b.r[0] = mk(1.0f, 0.0f, 0.0f); I.b.r[1] = mk(0.0f, 1.0f, 0.0f); I.b.r[2] = mk(0.0f, 0.0f, 1.0f);
+    I.o = mk(0.0f, 0.0f, 0.0f);
+    V bmin, bmax;
+    aabb(I, bmin, bmax);
+    const float radius = __fmul_rn(len(sub(bmax, bmin)), 0.5f);
+    const float disc = __fadd_rn(radius, len(scl(add(bmin, bmax), 0.5f)));
+    const float am = __fmul_rn(__fmul_rn(len(angVel), disc), 1.0f);
+    cmin = sub(mn, mk(am, am, am));
+    cmax = add(mx, mk(am, am, am));
+}
+
 __global__ void k_sweep_prep(DevWorld w, int shape, const float* from, const float* to, int n, float4* cmin,
                              float4* cmax, float* ofrom, float* oto) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -487,35 +529,10 @@ __global__ void k_sweep_prep(DevWorld w, int shape, const float* from, const flo
         ofrom[3 * q + k] = f[9 + k];
         oto[3 * q + k] = t[9 + k];
     }
-    M b0, b1;
-    b0.r[0] = mk(f[0], f[1], f[2]); b0.r[1] = mk(f[3], f[4], f[5]); b0.r[2] = mk(f[6], f[7], f[8]);
-    b1.r[0] = mk(t[0], t[1], t[2]); b1.r[1] = mk(t[3], t[4], t[5]); b1.r[2] = mk(t[6], t[7], t[8]);
-    const V linVel = scl(sub(mk(t[9], t[10], t[11]), mk(f[9], f[10], f[11])), jdiv(1.0f, 1.0f));
-    const Q dorn = qnor(q_from_matrix(mulMM(b1, m3_invert(b0))));
-    const float angle = __fmul_rn(2.0f, (float)acos((double)dorn.w));
-    V axis = mk(dorn.x, dorn.y, dorn.z);
-    const float l2 = len2(axis);
-    axis = l2 < __fmul_rn(FLT_EPS, FLT_EPS) ? mk(1.0f, 0.0f, 0.0f) : scl(axis, jdiv(1.0f, jsqrt(l2)));
-    const V angVel = scl(axis, jdiv(angle, 1.0f));
-    Xf R;
-    R.b = m_from_quat(q_from_matrix(b0));
-    R.o = mk(0.0f, 0.0f, 0.0f);
     V mn, mx;
-    shape_aabb(w.sh, shape, R, mn, mx);
-    const V lin = scl(linVel, 1.0f);
-    if (lin.x > 0.0f) mx.x = __fadd_rn(mx.x, lin.x); else mn.x = __fadd_rn(mn.x, lin.x);
-    if (lin.y > 0.0f) mx.y = __fadd_rn(mx.y, lin.y); else mn.y = __fadd_rn(mn.y, lin.y);
-    if (lin.z > 0.0f) mx.z = __fadd_rn(mx.z, lin.z); else mn.z = __fadd_rn(mn.z, lin.z);
-    Xf I;
-    I.b.r[0] = mk(1.0f, 0.0f, 0.0f); I.b.r[1] = mk(0.0f, 1.0f, 0.0f); I.b.r[2] = mk(0.0f, 0.0f, 1.0f);
-    I.o = mk(0.0f, 0.0f, 0.0f);
-    V bmin, bmax;
-    shape_aabb(w.sh, shape, I, bmin, bmax);
-    const float radius = __fmul_rn(len(sub(bmax, bmin)), 0.5f);
-    const float disc = __fadd_rn(radius, len(scl(add(bmin, bmax), 0.5f)));
-    const float am = __fmul_rn(__fmul_rn(len(angVel), disc), 1.0f);
-    cmin[q] = f4(sub(mn, mk(am, am, am)), 0.0f);
-    cmax[q] = f4(add(mx, mk(am, am, am)), 0.0f);
+    cast_box(xf12(f), xf12(t), [&](const Xf& x, V& a, V& b) { shape_aabb(w.sh, shape, x, a, b); }, mn, mx);
+    cmin[q] = f4(mn, 0.0f);
+    cmax[q] = f4(mx, 0.0f);
 }
 
 // GjkConvexCast.calcTimeOfImpact (collision/narrowphase/GjkConvexCast.java:67-185): conservative
@@ -561,15 +578,6 @@ JBD bool gjk_convex_cast(const ShapeRef& sa, const Xf& fromA, V toA, const Shape
     normal = n;
     hitPoint = c;
     return true;
-}
-
-JBD Xf xf12(const float* f) {
-    Xf t;
-    t.b.r[0] = mk(f[0], f[1], f[2]);
-    t.b.r[1] = mk(f[3], f[4], f[5]);
-    t.b.r[2] = mk(f[6], f[7], f[8]);
-    t.o = mk(f[9], f[10], f[11]);
-    return t;
 }
 
 int query_prepare(const DevWorld& w, BroadphaseBuffers& bb, QueryBuffers& qb, cudaStream_t s) {
@@ -905,6 +913,228 @@ int query_sweeps(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& q
     k_sweep_finish<<<gridn(n, 256), 256, 0, s>>>(n, qb.key, qb.sweepPlane, hits);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? JBGPU_OK : JBGPU_ERR_CUDA;
+}
+
+// ---- CCD motion clamping ---------------------------------------------------------------------
+// integrateTransforms (dynamics/DiscreteDynamicsWorld.java:679-739) for worlds where some body has
+// a CCD motion threshold.  The reference moves bodies one after the other; a body whose predicted
+// displacement squared exceeds ccdMotionThreshold^2 first sweeps a SphereShape of its
+// ccdSweptSphereRadius along its predicted motion with convexSweepTest (CollisionWorld.java:
+// 596-645), the objects seen where they are at that moment: bodies before it in the world's
+// order already moved, the rest not.  Here every body's predicted transform is computed at once;
+// a body that runs no sweep ends there.  The sweeping bodies are then taken in index order by
+// one cooperative launch: all threads test every object of the world against the sweep (seeing
+// the finished transform of objects before the body and the old one of the rest), the smallest
+// accepted fraction is reduced, and one thread clamps the body before the next one is taken.
+
+// Predicted transforms (RigidBody.predictIntegratedTransform), and which bodies sweep.
+__global__ void k_ccd_predict(DevWorld w, float dt, float4* pred, int* flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) w.ctr[C_CCD_BEST] = (int)__float_as_uint(1.0f);
+    if (i >= w.nBodies) return;
+    Xf t = load_xf(w, i);
+    int f = 0;
+    if (is_active_state(w.act[i]) && !is_static_or_kin(w.flags[i])) {
+        const Xf p = integrate_transform(t, mk4(w.linvel[i]), mk4(w.angvel[i]), dt);
+        const float thr = w.ccdThr[i];
+        const float sq = __fmul_rn(thr, thr);                 // getCcdSquareMotionThreshold
+        const float squareMotion = len2(sub(p.o, t.o));
+        f = sq != 0.0f && sq < squareMotion && w.sh.type[w.shape[i]] != SHAPE_PLANE ? 1 : 0;
+        t = p;
+    }
+    pred[3 * i] = make_float4(t.b.r[0].x, t.b.r[0].y, t.b.r[0].z, t.o.x);
+    pred[3 * i + 1] = make_float4(t.b.r[1].x, t.b.r[1].y, t.b.r[1].z, t.o.y);
+    pred[3 * i + 2] = make_float4(t.b.r[2].x, t.b.r[2].y, t.b.r[2].z, t.o.z);
+    flag[i] = f;
+}
+
+__global__ void k_ccd_list(int n, const int* flag, const int* pos, int* list) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && flag[i]) list[pos[i]] = i;
+}
+
+JBD Xf ld_pred(const float4* pred, int i) {
+    const float4 a = __ldcg(&pred[3 * i]), b = __ldcg(&pred[3 * i + 1]), c = __ldcg(&pred[3 * i + 2]);
+    Xf t;
+    t.b.r[0] = mk(a.x, a.y, a.z);
+    t.b.r[1] = mk(b.x, b.y, b.z);
+    t.b.r[2] = mk(c.x, c.y, c.z);
+    t.o = mk(a.w, b.w, c.w);
+    return t;
+}
+
+// Does the sweeping body `me` skip object j because it already touches it?  The reference asks
+// HashedOverlappingPairCache.findPair (collision/broadphase/HashedOverlappingPairCache.java:
+// 231-265), whose swap of its arguments is broken (233-237): the pair is found only when `me`
+// precedes j (key (me << 32) | j: j is the partner whether it is a body or a plane); found with a
+// manifold that holds contact points, j is skipped (DiscreteDynamicsWorld.java:1180-1195).
+JBD bool ccd_touching(const DevPairs& P, int np, int me, int j) {
+    if (me > j) return false;
+    const uint64_t key = ((uint64_t)(unsigned)me << 32) | (unsigned)j;
+    int lo = 0, hi = np - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const uint64_t k = P.keys[mid];
+        if (k == key) return P.has[mid] && P.n[mid] > 0;
+        if (k < key) lo = mid + 1;
+        else hi = mid - 1;
+    }
+    return false;
+}
+
+// The sweeps, in index order (ClosestNotMeConvexResultCallback, DiscreteDynamicsWorld.java:
+// 1129-1198, over convexSweepTest and objectQuerySingle, CollisionWorld.java:391-490,596-645).
+// An accepted hit: GjkConvexCast found one with |normal|^2 > 0.0001 and the normalised normal
+// opposes the motion; the callback keeps the closest, so the answer is the smallest accepted
+// fraction whatever the object order.  Body moved to its transform after dt * fraction when one
+// was accepted above 0.0001.  Static planes the sweep reaches are flagged (the reference throws).
+__global__ void __launch_bounds__(256) k_ccd_sweep(DevWorld w, DevPairs P, int nPairs, const int* cntp, float4* pred,
+                                                   const int* list, float dt) {
+    __shared__ float sBox[6];
+    __shared__ unsigned sBest;
+    unsigned barK = 0;
+    const int nb = gridDim.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+    const int count = __ldcg(&w.ctr[C_CCD_N]);
+    const int np = cntp ? min(nPairs, __ldcg(cntp)) : nPairs;
+    for (int k = 0; k < count; k++) {
+        const int me = list[k];
+        const Xf from = load_xf(w, me);
+        const Xf to = ld_pred(pred, me);
+        const float r = w.ccdRad[me];
+        if (threadIdx.x == 0) {
+            V mn, mx;
+            cast_box(from, to, [&](const Xf& x, V& a, V& b) {   // SphereShape.getAabb: centre -+ radius
+                a = sub(x.o, mk(r, r, r));
+                b = add(x.o, mk(r, r, r));
+            }, mn, mx);
+            sBox[0] = mn.x; sBox[1] = mn.y; sBox[2] = mn.z;
+            sBox[3] = mx.x; sBox[4] = mx.y; sBox[5] = mx.z;
+            sBest = __float_as_uint(1.0f);
+        }
+        __syncthreads();
+        const V cmin = mk(sBox[0], sBox[1], sBox[2]), cmax = mk(sBox[3], sBox[4], sBox[5]);
+        const V motion = sub(to.o, from.o);
+        const int wi = w.world[me], gm = w.group[me], mm = w.mask[me];
+        const bool resp = (w.flags[me] & CF_NO_CONTACT_RESPONSE) == 0;
+        ShapeRef cast;
+        cast.type = SHAPE_SPHERE;
+        cast.margin = r;
+        cast.dims = mk(r, r, r);
+        cast.up = 1;
+        cast.pts = nullptr;
+        cast.npts = 0;
+        for (int j = tid; j < w.nBodies; j += nth) {
+            if (j == me || w.world[j] != wi) continue;
+            if (((w.group[j] & mm) & 0xFFFF) == 0 || ((gm & w.mask[j]) & 0xFFFF) == 0) continue;
+            if (resp && (w.flags[j] & CF_NO_CONTACT_RESPONSE) == 0 && ccd_touching(P, np, me, j)) continue;
+            const Xf tj = j < me ? ld_pred(pred, j) : load_xf(w, j);
+            V bmn, bmx;
+            shape_aabb(w.sh, w.shape[j], tj, bmn, bmx);
+            float enter, exit;
+            if (!(ray_aabb_parts(from.o, to.o, add(bmn, cmin), add(bmx, cmax), enter, exit) && enter <= jmin(1.0f, exit)))
+                continue;
+            if (w.sh.type[w.shape[j]] == SHAPE_PLANE) {
+                atomicOr(&w.ctr[C_STATUS], ST_CCD_PLANE);
+                continue;
+            }
+            float f;
+            V n, p;
+            if (!gjk_convex_cast(cast, from, to.o, shape_ref(w.sh, w.shape[j]), tj, f, n, p)) continue;
+            if (!(len2(n) > 0.0001f) || !(f < 1.0f)) continue;
+            if (dot(nor(n), motion) >= -0.0f) continue;        // moving away from the contact normal
+            atomicMin(&sBest, __float_as_uint(f));
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && sBest < __float_as_uint(1.0f)) atomicMin((unsigned*)&w.ctr[C_CCD_BEST], sBest);
+        grid_barrier(w.ctr, nb, barK);
+        if (tid == 0) {
+            const float f = __uint_as_float((unsigned)__ldcg(&w.ctr[C_CCD_BEST]));
+            if (f < 1.0f && f > 0.0001f) {
+                const Xf p = integrate_transform(from, mk4(w.linvel[me]), mk4(w.angvel[me]), __fmul_rn(dt, f));
+                pred[3 * me] = make_float4(p.b.r[0].x, p.b.r[0].y, p.b.r[0].z, p.o.x);
+                pred[3 * me + 1] = make_float4(p.b.r[1].x, p.b.r[1].y, p.b.r[1].z, p.o.y);
+                pred[3 * me + 2] = make_float4(p.b.r[2].x, p.b.r[2].y, p.b.r[2].z, p.o.z);
+            }
+            w.ctr[C_CCD_BEST] = (int)__float_as_uint(1.0f);
+        }
+        grid_barrier(w.ctr, nb, barK);
+    }
+}
+
+// RigidBody.proceedToTransform: the final transforms and world inverse inertia of moved bodies.
+__global__ void k_ccd_commit(DevWorld w, const float4* pred) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    if (!is_active_state(w.act[i]) || is_static_or_kin(w.flags[i])) return;
+    const Xf p = ld_pred(pred, i);
+    store_xf(w, i, p);
+    M m1 = scaleM(p.b, mk4(w.iloc[i]));
+    M iw = mulMM(m1, transpose(p.b));
+    w.iw0[i] = f4(iw.r[0], 0.0f);
+    w.iw1[i] = f4(iw.r[1], 0.0f);
+    w.iw2[i] = f4(iw.r[2], 0.0f);
+}
+
+int ccd_reserve(CcdBuffers& cb, int n, int sms) {
+    if (n > cb.cap) {
+        void* old[] = {cb.pred, cb.flag, cb.pos, cb.list, cb.scanScratch};
+        for (void* p : old)
+            if (p) cudaFree(p);
+        cb.pred = nullptr;
+        cb.flag = cb.pos = cb.list = nullptr;
+        cb.scanScratch = nullptr;
+        const int c = n > 2 * cb.cap ? n : 2 * cb.cap;
+        cb.cap = 0;
+        if (cudaMalloc((void**)&cb.pred, sizeof(float4) * 3 * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&cb.flag, sizeof(int) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&cb.pos, sizeof(int) * (size_t)c) != cudaSuccess ||
+            cudaMalloc((void**)&cb.list, sizeof(int) * (size_t)c) != cudaSuccess ||
+            cudaMalloc(&cb.scanScratch, scan_scratch_bytes(c)) != cudaSuccess)
+            return JBGPU_ERR_CUDA;
+        cb.cap = c;
+    }
+    if (!cb.grid) {
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ccd_sweep, 256, 0) != cudaSuccess || per < 1)
+            return JBGPU_ERR_CUDA;
+        cb.grid = sms * (per < 2 ? per : 2);
+    }
+    return JBGPU_OK;
+}
+
+int ccd_integrate(const DevWorld& w, const DevPairs& P, int nPairs, const int* cntp, CcdBuffers& cb, float dt, int sms,
+                  cudaStream_t s) {
+    const int n = w.nBodies;
+    if (n <= 0) return JBGPU_OK;
+    if (n > cb.cap || !cb.grid) {
+        const int rc = ccd_reserve(cb, n, sms);
+        if (rc) return rc;
+    }
+    k_ccd_predict<<<gridn(n, 256), 256, 0, s>>>(w, dt, cb.pred, cb.flag); note_launch();
+    exclusive_scan(cb.flag, cb.pos, w.ctr + C_CCD_N, n, cb.scanScratch, s);
+    k_ccd_list<<<gridn(n, 256), 256, 0, s>>>(n, cb.flag, cb.pos, cb.list); note_launch();
+    cudaMemsetAsync(w.ctr + C_BAR_COUNT, 0, sizeof(int), s);
+    {
+        DevWorld wc = w;
+        DevPairs pc = P;
+        int npc = nPairs;
+        const int* cc = cntp;
+        float4* pr = cb.pred;
+        const int* li = cb.list;
+        float dtc = dt;
+        void* args[] = {&wc, &pc, &npc, &cc, &pr, &li, &dtc};
+        cudaLaunchCooperativeKernel((void*)k_ccd_sweep, cb.grid, 256, args, 0, s); note_launch();
+    }
+    k_ccd_commit<<<gridn(n, 256), 256, 0, s>>>(w, cb.pred); note_launch();
+    return cudaGetLastError() == cudaSuccess ? JBGPU_OK : JBGPU_ERR_CUDA;
+}
+
+void ccd_free(CcdBuffers& cb) {
+    void* ps[] = {cb.pred, cb.flag, cb.pos, cb.list, cb.scanScratch};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    cb = CcdBuffers();
 }
 
 void query_free(QueryBuffers& qb) {

@@ -57,4 +57,24 @@ int query_sweeps(const DevWorld& w, const BroadphaseBuffers& bb, QueryBuffers& q
                  cudaStream_t s);
 void query_free(QueryBuffers& qb);
 
+// CCD motion clamping of integrateTransforms (dynamics/DiscreteDynamicsWorld.java:679-739).
+struct CcdBuffers {
+    float4* pred = nullptr;       // per body: predicted transform, 3 float4 (basis rows, origin in .w)
+    int* flag = nullptr;          // per body: runs a CCD sweep
+    int* pos = nullptr;           // exclusive scan of flag
+    int* list = nullptr;          // CCD bodies in index order
+    void* scanScratch = nullptr;
+    int cap = 0;
+    int grid = 0;                 // co-resident blocks of the cooperative sweep kernel
+};
+// The integrate stage with CCD: predicted transforms, the CCD bodies' sweeps in index order (one
+// cooperative launch, two grid barriers per CCD body), then every moved body's transform and
+// world inverse inertia.  P / nPairs / cntp: the step's pair arrays (cntp nullable: nPairs exact).
+int ccd_integrate(const DevWorld& w, const DevPairs& P, int nPairs, const int* cntp, CcdBuffers& cb, float dt, int sms,
+                  cudaStream_t s);
+// Buffers for n bodies and the sweep kernel's grid, ahead of a captured step (no allocation
+// may happen while a stream is captured).
+int ccd_reserve(CcdBuffers& cb, int n, int sms);
+void ccd_free(CcdBuffers& cb);
+
 }  // namespace jbg

@@ -115,6 +115,10 @@ struct jbgpu_world {
     NarrowBuffers nb;
     SolverBuffers sb;
     QueryBuffers qb;                  // ray queries
+    CcdBuffers cb;                    // CCD motion clamping (jbgpu_world_set_ccd)
+    bool ccdOn = false;               // some body has a CCD motion threshold
+    const int* pairCountDev = nullptr;   // while the step's second graph is captured: the pair count
+                                         // on the device (nPairs then being the capacity)
     int* hostPinned = nullptr;
     Prof prof;
     int* profHist = nullptr;      // per profiled step: device counters + solver manifolds
@@ -213,8 +217,10 @@ int grow_bodies(jbgpu_world* w, int need) {
 #define G(ptr) CK(dgrow(&d.ptr, oldc, nc, keep, s))
     G(xr0); G(xr1); G(xr2); G(linvel); G(angvel); G(iw0); G(iw1); G(iw2); G(iloc); G(force); G(torque); G(gravity);
     G(amin); G(amax); G(act); G(deact); G(flags); G(shape); G(group); G(mask); G(world); G(friction); G(restitution);
-    G(linSleep); G(angSleep); G(linDamp); G(angDamp); G(island);
+    G(linSleep); G(angSleep); G(linDamp); G(angDamp); G(island); G(ccdThr); G(ccdRad);
 #undef G
+    CK(cudaMemsetAsync(d.ccdThr + keep, 0, sizeof(float) * (nc - keep), s));   // CCD off for new bodies
+    CK(cudaMemsetAsync(d.ccdRad + keep, 0, sizeof(float) * (nc - keep), s));
     // per-body work buffers (contents not kept)
     BroadphaseBuffers& B = w->bb;
     dfree(B.mkeys); dfree(B.mkeys_alt); dfree(B.sortedBody); dfree(B.vals_alt);
@@ -307,6 +313,10 @@ int sync_shapes(jbgpu_world* w) {
     }
     if (nh) CK(cudaMemcpyAsync(S.hull_pts, w->hullPts.data(), sizeof(float4) * nh, cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
+    bool hulls = false;   // the narrowphase stages hull vertices in shared memory when there are hulls
+    for (int k = 0; k < ns; k++) hulls = hulls || type[k] == JBGPU_SHAPE_CONVEX_HULL;
+    if (hulls != w->nb.stageHulls) graphs_clear(w);
+    w->nb.stageHulls = hulls;
     w->shapesDirty = false;
     return JBGPU_OK;
 }
@@ -370,6 +380,9 @@ int check_status(jbgpu_world* w) {
     if (st & ST_EPA_POOL) return fail(JBGPU_ERR_EPA_OVERFLOW, "EPA face pool overflow");
     if (st & ST_CAPACITY) return fail(JBGPU_ERR_CAPACITY, "device capacity exceeded (traversal stack or colours)");
     if (st & ST_BAD_WORLD) return fail(JBGPU_ERR_INVALID_ARGUMENT, "a ray or sweep names a batch world the world does not have");
+    if (st & ST_CCD_PLANE)
+        return fail(JBGPU_ERR_UNSUPPORTED, "a CCD sweep reached a static plane, where the reference throws "
+                                           "(CollisionWorld.objectQuerySingle's concave branch)");
     return JBGPU_OK;
 }
 
@@ -477,7 +490,16 @@ int run_stage(jbgpu_world* w, int stage, float dt) {
         solve_launch_learn(d, w->pairs[w->cur], w->nPairs, w->rows, w->sb, dt, s, &P, learn);
         break;
     }
-    case JBGPU_STAGE_INTEGRATE: P.mark(PH_INTEGRATE, 0, s); launch_integrate(d, dt, s); P.mark(PH_INTEGRATE, 1, s); break;
+    case JBGPU_STAGE_INTEGRATE:
+        P.mark(PH_INTEGRATE, 0, s);
+        if (w->ccdOn) {
+            int rc = ccd_integrate(d, w->pairs[w->cur], w->nPairs, w->pairCountDev, w->cb, dt, w->sms, s);
+            if (rc) return fail(rc, "CCD integration failed");
+        } else {
+            launch_integrate(d, dt, s);
+        }
+        P.mark(PH_INTEGRATE, 1, s);
+        break;
     case JBGPU_STAGE_ACTIVATION: P.mark(PH_ACTIVATION, 0, s); launch_activation(d, dt, s); P.mark(PH_ACTIVATION, 1, s); break;
     case JBGPU_STAGE_CLEAR_FORCES: launch_clear_forces(d, s); break;
     default: return fail(JBGPU_ERR_INVALID_ARGUMENT, "unknown stage");
@@ -691,6 +713,8 @@ int single_step_graph(jbgpu_world* w, float dt) {
     w->nPairs = bound;                     // launches are sized by the capacity ...
     rc = capture_or_replay(w, kb, [&]() -> int {
         DevWorld d = dev_view(w);
+        w->pairCountDev = cnt;
+        struct Reset { jbgpu_world* w; ~Reset() { w->pairCountDev = nullptr; } } reset{w};
         broadphase_run_fill(d, B, w->pairs[nxt], bound, s);
         broadphase_persist(d, B, w->pairs[nxt], w->pairs[old], bound, w->capPairs[old], s, B.total, cnt);
         CK(cudaMemcpyAsync(cnt, B.total, sizeof(int), cudaMemcpyDeviceToDevice, s));
@@ -731,6 +755,7 @@ bool graph_usable(const jbgpu_world* w) {
 }  // namespace
 
 int single_step(jbgpu_world* w, float dt) {
+    if (w->ccdOn && ccd_reserve(w->cb, w->nBodies, w->sms)) return fail(JBGPU_ERR_CUDA, "CCD buffers");
     if (graph_usable(w)) {
         int rc = single_step_graph(w, dt);
         if (rc != GRAPH_FALLBACK) return rc;   // else the capture failed before anything ran
@@ -961,6 +986,8 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(d.iloc); dfree(d.force); dfree(d.torque); dfree(d.gravity); dfree(d.amin); dfree(d.amax); dfree(d.act);
     dfree(d.deact); dfree(d.flags); dfree(d.shape); dfree(d.group); dfree(d.mask); dfree(d.world); dfree(d.friction);
     dfree(d.restitution); dfree(d.linSleep); dfree(d.angSleep); dfree(d.linDamp); dfree(d.angDamp); dfree(d.island);
+    dfree(d.ccdThr); dfree(d.ccdRad);
+    ccd_free(w->cb);
     dfree(d.ctr);
     DevShapes& S = d.sh;
     dfree(S.type); dfree(S.margin); dfree(S.dims); dfree(S.laabb_min); dfree(S.laabb_max); dfree(S.plane);
@@ -1227,6 +1254,29 @@ int jbgpu_world_narrowphase_static(jbgpu_world* w, int32_t epa_slots) {
     narrowphase_launch_static(dev_view(w), w->pairs[w->cur], w->nPairs, w->nb, base, epa_slots, s);
     CK(cudaGetLastError());
     return check_status(w);
+}
+
+int jbgpu_world_set_ccd(jbgpu_world* w, const int32_t* bodies, const float* thr, const float* rad, int32_t n) {
+    if (!w || n < 0 || (n > 0 && (!bodies || !thr || !rad))) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad CCD arguments");
+    for (int k = 0; k < n; k++)
+        if (bodies[k] < 0 || bodies[k] >= w->nBodies) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad body index");
+    if (n == 0) return JBGPU_OK;
+    CK(cudaSetDevice(w->device));
+    CK(cudaStreamSynchronize(w->stream));
+    std::vector<float> t(w->nBodies), r(w->nBodies);
+    CK(cudaMemcpy(t.data(), w->dw.ccdThr, sizeof(float) * w->nBodies, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(r.data(), w->dw.ccdRad, sizeof(float) * w->nBodies, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < n; k++) {
+        t[bodies[k]] = thr[k];
+        r[bodies[k]] = rad[k];
+    }
+    CK(cudaMemcpy(w->dw.ccdThr, t.data(), sizeof(float) * w->nBodies, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w->dw.ccdRad, r.data(), sizeof(float) * w->nBodies, cudaMemcpyHostToDevice));
+    bool on = false;
+    for (float v : t) on = on || v != 0.0f;
+    if (on != w->ccdOn) graphs_clear(w);   // the integrate stage's launches change
+    w->ccdOn = on;
+    return JBGPU_OK;
 }
 
 int jbgpu_world_get_residual_trace(jbgpu_world* w, float* out, int32_t cap, int32_t* n) {
@@ -1976,6 +2026,7 @@ int jbgpu_world_counters(jbgpu_world* w, jbgpu_counters* c) {
     c->solver_islands = h[C_ISL_N];
     c->solver_islands_converged = h[C_ISL_CONV];
     c->solver_island_iterations = h[C_ISL_ITERS];
+    c->ccd_clamped = w->ccdOn ? h[C_CCD_N] : 0;
     if (w->qb.slowCount) {
         CK(cudaMemcpy(&c->ray_replays, w->qb.slowCount, sizeof(int), cudaMemcpyDeviceToHost));
     }
@@ -2082,6 +2133,7 @@ int jbgpu_world_profile_counters(jbgpu_world* w, jbgpu_counters* out, int32_t ca
         o.solver_islands = c[C_ISL_N];
         o.solver_islands_converged = c[C_ISL_CONV];
         o.solver_island_iterations = c[C_ISL_ITERS];
+        o.ccd_clamped = c[C_CCD_N];
     }
     return JBGPU_OK;
 }

@@ -193,6 +193,7 @@ class Counters(C.Structure):
         ("solver_islands_converged", C.c_int32),
         ("solver_island_iterations", C.c_int32),
         ("ray_replays", C.c_int32),
+        ("ccd_clamped", C.c_int32),
     ]
 
     def as_dict(self):

@@ -100,6 +100,7 @@ def lib():
             "jbgpu_world_set_warmstart_mlp": ([C.c_void_p, C.c_void_p], C.c_int),
             "jbgpu_world_set_solver_iterations": ([C.c_void_p, C.c_int32, C.c_float, C.c_int32], C.c_int),
             "jbgpu_world_get_residual_trace": ([C.c_void_p, _abi.f32p, C.c_int32, _abi.i32p], C.c_int),
+            "jbgpu_world_set_ccd": ([C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_set_sample_logging": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_get_samples": ([C.c_void_p, _abi.f32p, _abi.f32p, C.c_int32, _abi.i32p], C.c_int),
         }
@@ -125,7 +126,7 @@ EXPORTED = [
     "jbgpu_world_set_6dof_limit", "jbgpu_world_set_6dof_linear_motor", "jbgpu_world_set_6dof_angular_motor",
     "jbgpu_world_add_cone_twist", "jbgpu_world_set_cone_twist_limit", "jbgpu_world_set_cone_twist_angular_only",
     "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
-    "jbgpu_world_get_residual_trace",
+    "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd",
 ]
 
 
@@ -215,6 +216,9 @@ class GpuWorld:
         if scene is not None:
             self.add_scene(scene)
             self.add_scene_joints(scene)
+            ccd = scene.meta.get("ccd")
+            if ccd:
+                self.set_ccd(ccd["bodies"], ccd["threshold"], ccd["radius"])
 
     def close(self):
         if getattr(self, "h", None):
@@ -474,6 +478,16 @@ class GpuWorld:
 
     def set_solver_iterations(self, num_iterations, residual=0.0, max_iterations=0):
         check(lib().jbgpu_world_set_solver_iterations(self.h, num_iterations, residual, max_iterations))
+
+    def set_ccd(self, bodies, motion_threshold, swept_sphere_radius):
+        """CollisionObject.setCcdMotionThreshold / setCcdSweptSphereRadius for the given bodies."""
+        b = np.ascontiguousarray(bodies, np.int32).reshape(-1)
+        t = np.ascontiguousarray(np.broadcast_to(np.float32(motion_threshold) if np.isscalar(motion_threshold)
+                                                 else motion_threshold, b.shape), np.float32)
+        r = np.ascontiguousarray(np.broadcast_to(np.float32(swept_sphere_radius) if np.isscalar(swept_sphere_radius)
+                                                 else swept_sphere_radius, b.shape), np.float32)
+        check(lib().jbgpu_world_set_ccd(self.h, b.ctypes.data_as(_abi.i32p), t.ctypes.data_as(_abi.f32p),
+                                        r.ctypes.data_as(_abi.f32p), len(b)))
 
     def residual_trace(self):
         """(max |delta lambda|, max |lambda|) per iteration of the last step's residual-mode solve."""

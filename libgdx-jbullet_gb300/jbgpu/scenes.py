@@ -758,6 +758,58 @@ def learned_warmstart(n=100_000, seed=0, pyramids=50, levels=15, region=(200.0, 
                  meta={"seed": seed, "pyramid_bodies": pyramids * per})
 
 
+def ccd_shots(shots=24, seed=0, steps=90, plane=False, threshold=0.05, swept_radius=0.08):
+    """Fast projectiles fired at thin walls, for CCD motion clamping (DiscreteDynamicsWorld.
+    integrateTransforms' CCD branch): a static box floor (no static plane, since the reference's
+    CCD sweep throws on one), two thin static walls across the x axis, a few loose dynamic boxes
+    in front of them, and `shots` small spheres and boxes moving at 50-90 m/s along +x (about a
+    metre per 1/60 s step, ten times the walls' thickness), some in pairs on one path.  The shots
+    get the CCD motion threshold and swept-sphere radius in meta["ccd"]; plane=True puts a static
+    plane in the world first (the reference throws when a sweep reaches it)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [{"type": _abi.SHAPE_BOX, "params": (30.0, 0.5, 30.0, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.05, 2.5, 4.0, 0.0), "points": None},
+              {"type": _abi.SHAPE_SPHERE, "params": (0.1, 0.0, 0.0, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.1, 0.1, 0.1, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.4, 0.4, 0.4, 0.0), "points": None}]
+    parts = []
+    if plane:
+        shapes.append(dict(PLANE))
+        parts.append(_plane_body(len(shapes) - 1))
+    fixed = _bodies(3)
+    fixed["shape"] = [0, 1, 1]
+    fixed["transform"][:, 9:] = np.array([[0.0, -0.5, 0.0], [6.0, 2.5, 0.0], [12.0, 2.5, 0.0]], F)
+    parts.append(fixed)
+    loose = _bodies(6)
+    loose["shape"] = 4
+    loose["mass"] = 2.0
+    loose["local_inertia"] = box_inertia(2.0, (0.4, 0.4, 0.4))
+    loose["transform"][:, 9:] = np.stack([np.repeat([5.2, 11.2], 3), np.full(6, 0.41),
+                                          np.tile([-2.0, 0.0, 2.0], 2)], 1).astype(F)
+    parts.append(loose)
+    shots_b = _bodies(shots)
+    kind = rng.integers(0, 2, shots)
+    shots_b["shape"] = np.where(kind == 0, 2, 3)
+    shots_b["mass"] = 0.1
+    shots_b["local_inertia"] = np.where((kind == 0)[:, None], sphere_inertia(0.1, 0.1), box_inertia(0.1, (0.1, 0.1, 0.1)))
+    pos = np.stack([rng.uniform(-1.0, 2.0, shots), rng.uniform(0.4, 4.0, shots), rng.uniform(-3.0, 3.0, shots)], 1)
+    for k in range(1, shots, 4):          # every fourth shot follows another on its path
+        pos[k] = pos[k - 1] - np.array([0.6, 0.0, 0.0])
+    _set_transforms(shots_b, random_rotations(rng, shots), pos)
+    vel = np.stack([rng.uniform(50.0, 90.0, shots), rng.uniform(-2.0, 2.0, shots), rng.uniform(-3.0, 3.0, shots)], 1)
+    for k in range(1, shots, 4):
+        vel[k] = vel[k - 1]
+    shots_b["linear_velocity"] = vel.astype(F)
+    shots_b["angular_velocity"] = rng.uniform(-20.0, 20.0, (shots, 3)).astype(F)
+    parts.append(shots_b)
+    bodies = np.concatenate(parts)
+    first = len(bodies) - shots
+    return Scene("ccd_shots_%d%s" % (shots, "_plane" if plane else ""), 1.0 / 60.0, steps,
+                 {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10}, shapes, bodies,
+                 meta={"seed": seed, "ccd": {"bodies": list(range(first, len(bodies))), "threshold": threshold,
+                                             "radius": swept_radius}, "walls_x": (6.0, 12.0)})
+
+
 SCENES = {
     "boxes_1k": boxes_on_plane,
     "mixed_100k": mixed_100k,
@@ -771,4 +823,5 @@ SCENES = {
     "sixdof_chains": sixdof_chains,
     "cone_chains": cone_chains,
     "slider_rigs": slider_rigs,
+    "ccd_shots": ccd_shots,
 }

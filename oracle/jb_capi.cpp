@@ -9,6 +9,9 @@
 // status_flags bit of orc_counters: an explicit solver order was not a permutation of the
 // manifolds the oracle itself would solve.
 static const int ORC_ORDER_MISMATCH = 1 << 16;
+// status_flags bit: a CCD sweep reached a static plane (the reference throws there); the same
+// bit value as the library's JBGPU status report uses for it.
+static const int ORC_CCD_PLANE = 32;
 
 using namespace jb;
 
@@ -283,6 +286,16 @@ int orc_get_state(void* h, jbgpu_state* s) {
     return 0;
 }
 
+int orc_set_ccd(void* h, const int* bodies, const float* threshold, const float* radius, int n) {
+    World& w = *(World*)h;
+    for (int k = 0; k < n; k++) {
+        if (bodies[k] < 0 || bodies[k] >= (int)w.bodies.size()) return JBGPU_ERR_INVALID_ARGUMENT;
+        w.bodies[bodies[k]].ccdMotionThreshold = threshold[k];
+        w.bodies[bodies[k]].ccdSweptSphereRadius = radius[k];
+    }
+    return JBGPU_OK;
+}
+
 int orc_set_state(void* h, const jbgpu_state* s) {
     World& w = *(World*)h;
     int n = (int)w.bodies.size();
@@ -382,7 +395,8 @@ void orc_counters(void* h, jbgpu_counters* c) {
     c->islands = w.counters.islands;
     c->gjk_calls = w.counters.gjk;
     c->epa_calls = w.counters.epa;
-    c->status_flags = w.counters.orderMismatch ? ORC_ORDER_MISMATCH : 0;
+    c->status_flags = (w.counters.orderMismatch ? ORC_ORDER_MISMATCH : 0) | (w.counters.ccdPlane ? ORC_CCD_PLANE : 0);
+    c->ccd_clamped = w.counters.ccdClamped;
     c->solver_iterations = w.counters.solverIterations;
 }
 

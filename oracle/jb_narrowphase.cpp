@@ -1,6 +1,7 @@
 // ORACLE (test infrastructure only): narrowphase of the reference, restated.
 // Citations relative to src/com/bulletphysics/.
 #include <vector>
+#include <algorithm>
 #include "jb_world.h"
 
 namespace jb {
@@ -1233,6 +1234,64 @@ RayResult convex_sweep(const World& w, const Shape& cast, const Xf& from, const 
         }
     }
     return res;
+}
+
+// The CCD sweep of integrateTransforms (dynamics/DiscreteDynamicsWorld.java:700-729): a sphere of
+// the body's ccdSweptSphereRadius swept by convexSweepTest (CollisionWorld.java:596-645) from the
+// body's transform to its predicted one, with ClosestNotMeConvexResultCallback (java:1129-1198).
+// Objects are seen at their transforms of the moment: the bodies before `me` in the world's order
+// have already been moved by this integrateTransforms.  needsCollision: not `me`, the proxies'
+// filters, and, since every body here has contact response, HashedOverlappingPairCache.findPair
+// (collision/broadphase/HashedOverlappingPairCache.java:231-265) - whose argument swap is broken
+// (233-237), so it finds the pair only when `me` precedes the other object; a pair found with a
+// manifold that holds contact points excludes the object.  addSingleResult drops hits whose
+// normal does not oppose the motion (normal . (to - from) >= 0).  A static plane reached by the
+// sweep makes the reference throw (objectQuerySingle's concave branch, CollisionWorld.java:
+// 470-490): *planeHit is set and the plane is skipped.
+bool ccd_sweep(const World& w, int me, const Xf& to, float& fraction, bool* planeHit) {
+    *planeHit = false;
+    const Body& mb = w.bodies[me];
+    const Xf from = mb.xf;
+    const Shape cast = make_sphere(mb.ccdSweptSphereRadius);
+    V3 linVel, angVel;
+    calculate_velocity(from, to, 1.0f, linVel, angVel);
+    Xf R = xf_identity();
+    R.b = m3_from_quat(q_from_matrix(from.b));
+    V3 cmin, cmax;
+    temporal_aabb(cast, R, linVel, angVel, 1.0f, cmin, cmax);
+    const V3 motion = sub(to.o, from.o);        // the callback's convexToWorld - convexFromWorld
+    float closest = 1.0f;
+    bool hit = false;
+    for (size_t i = 0; i < w.bodies.size(); i++) {
+        const Body& b = w.bodies[i];
+        if ((int)i == me || b.world != mb.world) continue;
+        if (((b.group & mb.mask) & 0xFFFF) == 0 || ((mb.group & b.mask) & 0xFFFF) == 0) continue;
+        if (mb.hasContactResponse() && b.hasContactResponse() && me < (int)i) {
+            const uint64_t key = pair_key(w, me, (int)i);
+            auto it = std::lower_bound(w.pairKeys.begin(), w.pairKeys.end(), key);
+            if (it != w.pairKeys.end() && *it == key) {
+                const size_t k = (size_t)(it - w.pairKeys.begin());
+                if (w.pairHasAlgo[k] && w.pairMf[k].n > 0) continue;
+            }
+        }
+        const Shape& sh = w.shapes[b.shape];
+        V3 mn, mx;
+        shape_aabb(sh, b.xf, mn, mx);
+        mn = add(mn, cmin);
+        mx = add(mx, cmax);
+        float param = 1.0f;
+        if (!ray_aabb(from.o, to.o, mn, mx, param)) continue;
+        if (!sh.isConvex()) { *planeHit = true; continue; }
+        float f;
+        V3 n, p;
+        if (gjk_convex_cast(cast, from, to, sh, b.xf, 0.04f, f, n, p) && len2(n) > 0.0001f && f < closest) {
+            if (dot(nor(n), motion) >= -0.0f) continue;   // moving away from the contact normal
+            closest = f;
+            hit = true;
+        }
+    }
+    fraction = closest;
+    return hit;
 }
 
 }  // namespace jb

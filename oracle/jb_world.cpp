@@ -1378,12 +1378,29 @@ void stage_solve(World& w, float dt) {
     w.counters.solverManifolds = (int)w.lastOrder.size();
 }
 
-// integrateTransforms (dynamics/DiscreteDynamicsWorld.java:679-739), CCD off
+// integrateTransforms (dynamics/DiscreteDynamicsWorld.java:679-739) with the CCD motion clamping
+// of bodies whose predicted displacement squared exceeds ccdMotionThreshold^2 (the reference's
+// getCcdSquareMotionThreshold, CollisionObject.java:290-292): the body moves only to the sweep's
+// first accepted time of impact when that is above 0.0001.  Bodies are moved one after the
+// other, so a later body's sweep sees the earlier ones where they ended.
 void stage_integrate(World& w, float dt) {
     PhaseTimer pt(w, 7);
-    for (Body& b : w.bodies) {
+    w.counters.ccdClamped = 0;
+    w.counters.ccdPlane = 0;
+    for (size_t i = 0; i < w.bodies.size(); i++) {
+        Body& b = w.bodies[i];
         if (b.isActive() && !b.isStaticOrKinematic()) {
             Xf p = integrate_transform(b.xf, b.linvel, b.angvel, dt);
+            const float sq = b.ccdMotionThreshold * b.ccdMotionThreshold;
+            const float squareMotion = len2(sub(p.o, b.xf.o));
+            if (sq != 0.0f && sq < squareMotion && w.shapes[b.shape].isConvex()) {
+                w.counters.ccdClamped++;
+                float f = 1.0f;
+                bool plane = false;
+                if (ccd_sweep(w, (int)i, p, f, &plane) && f > 0.0001f)
+                    p = integrate_transform(b.xf, b.linvel, b.angvel, dt * f);
+                if (plane) w.counters.ccdPlane++;
+            }
             b.xf = p;                  // RigidBody.setCenterOfMassTransform
             update_inertia_tensor(b);
         }

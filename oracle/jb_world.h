@@ -75,6 +75,8 @@ struct Body {            // dynamics/RigidBody.java + collision/dispatch/Collisi
     int group = 1, mask = -1;
     int world = 0;                          // batch world index: bodies of different worlds never pair
     V3 aabbMin{0, 0, 0}, aabbMax{0, 0, 0};  // broadphase proxy aabb
+    float ccdMotionThreshold = 0.0f;        // CollisionObject.ccdMotionThreshold (0: no CCD)
+    float ccdSweptSphereRadius = 0.0f;      // CollisionObject.ccdSweptSphereRadius
     bool isStaticOrKinematic() const { return (flags & (CF_STATIC_OBJECT | CF_KINEMATIC_OBJECT)) != 0; }
     bool isStatic() const { return (flags & CF_STATIC_OBJECT) != 0; }
     bool isKinematic() const { return (flags & CF_KINEMATIC_OBJECT) != 0; }
@@ -174,6 +176,8 @@ struct Counters {
     int gjk = 0, epa = 0;
     int orderMismatch = 0;   // solves whose explicit order was not a permutation of the candidates
     int solverIterations = 0;
+    int ccdClamped = 0;      // CCD sweeps of the last integrateTransforms (BulletStats.gNumClampedCcdMotions)
+    int ccdPlane = 0;        // CCD sweeps that reached a static plane, where the reference throws
 };
 
 // Solver order policy (the reference's F8 hook, SequentialImpulseConstraintSolver.java:769-779):
@@ -239,5 +243,8 @@ struct GjkOut { bool valid; V3 normal; V3 pointOnB; float distance; int usedEpa;
 GjkOut gjk_closest_points(const Shape& sa, const Xf& ta, const Shape& sb, const Xf& tb, float maxDist2, bool withEpa = true);
 RayResult convex_sweep(const World& w, const Shape& cast, const Xf& from, const Xf& to, int group, int mask, int world,
                        bool* planeHit);
+// integrateTransforms' CCD sweep of body `me` from its transform to `to` (a sphere of its swept
+// radius, ClosestNotMeConvexResultCallback): true with the closest accepted fraction.
+bool ccd_sweep(const World& w, int me, const Xf& to, float& fraction, bool* planeHit);
 
 }  // namespace jb

@@ -68,6 +68,7 @@ def lib():
         L.orc_set_hinge_limit.argtypes = [C.c_void_p, C.c_int] + [C.c_float] * 5
         L.orc_enable_hinge_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float]
         L.orc_set_hinge_angular_only.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.orc_set_ccd.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, C.c_int]
         _lib = L
     return _lib
 
@@ -85,6 +86,9 @@ class OracleWorld:
         if scene is not None:
             self.add_scene(scene)
             self.add_scene_joints(scene)
+            ccd = scene.meta.get("ccd")
+            if ccd:
+                self.set_ccd(ccd["bodies"], ccd["threshold"], ccd["radius"])
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -223,6 +227,17 @@ class OracleWorld:
     @property
     def n_bodies(self):
         return lib().orc_num_bodies(self.h)
+
+    def set_ccd(self, bodies, motion_threshold, swept_sphere_radius):
+        """CollisionObject.setCcdMotionThreshold / setCcdSweptSphereRadius for the given bodies."""
+        b = np.ascontiguousarray(bodies, np.int32).reshape(-1)
+        t = np.ascontiguousarray(np.broadcast_to(np.float32(motion_threshold) if np.isscalar(motion_threshold)
+                                                 else motion_threshold, b.shape), np.float32)
+        r = np.ascontiguousarray(np.broadcast_to(np.float32(swept_sphere_radius) if np.isscalar(swept_sphere_radius)
+                                                 else swept_sphere_radius, b.shape), np.float32)
+        rc = lib().orc_set_ccd(self.h, b.ctypes.data_as(_abi.i32p), _fp(t), _fp(r), len(b))
+        if rc != 0:
+            raise ValueError("bad body index")
 
     def set_order_mode(self, mode):
         lib().orc_set_order_mode(self.h, mode)
