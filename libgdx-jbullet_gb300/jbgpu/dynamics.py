@@ -121,6 +121,7 @@ class RigidBody:
         self._angvel = (0.0, 0.0, 0.0)
         self._group = -1
         self._mask = -1
+        self._ccd = (0.0, 0.0)          # ccdMotionThreshold, ccdSweptSphereRadius
 
     # velocities set before the body enters the world are uploaded with it
     def setLinearVelocity(self, v):
@@ -163,6 +164,29 @@ class RigidBody:
 
     def getUid(self):
         return self._index + 1
+
+    # CollisionObject.setCcdMotionThreshold / setCcdSweptSphereRadius (collision/dispatch/
+    # CollisionObject.java:278-300): read by integrateTransforms' CCD motion clamping
+    def setCcdMotionThreshold(self, t):
+        self._ccd = (float(t), self._ccd[1])
+        self._push_ccd()
+
+    def setCcdSweptSphereRadius(self, r):
+        self._ccd = (self._ccd[0], float(r))
+        self._push_ccd()
+
+    def getCcdMotionThreshold(self):
+        return self._ccd[0]
+
+    def getCcdSquareMotionThreshold(self):
+        return float(np.float32(self._ccd[0]) * np.float32(self._ccd[0]))
+
+    def getCcdSweptSphereRadius(self):
+        return self._ccd[1]
+
+    def _push_ccd(self):
+        if self._world is not None and self._world._g is not None and self._index < self._world._uploaded:
+            self._world._g.set_ccd([self._index], self._ccd[0], self._ccd[1])
 
 
 class ContactSolverInfo:
@@ -705,6 +729,9 @@ class DiscreteDynamicsWorld:
         lib.check(lib.lib().jbgpu_world_add_bodies(g.h, ptr, len(b), None))
         self._uploaded = len(self._bodies)
         self._forces = None
+        ccd = [b for b in new if b._ccd != (0.0, 0.0)]
+        if ccd:
+            g.set_ccd([b._index for b in ccd], [b._ccd[0] for b in ccd], [b._ccd[1] for b in ccd])
 
     def _pending_force(self, index, f):
         if self._forces is None:

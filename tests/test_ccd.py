@@ -110,3 +110,52 @@ def test_gpu_ccd_reports_a_static_plane_on_the_path(gpu_lib, oracle_lib):
     with pytest.raises(JbgpuError):
         g.set_ccd([g.n_bodies], 1.0, 0.1)             # no such body
     g.close()
+
+
+@pytest.mark.gpu
+def test_mirror_bullet_stops_at_a_thin_wall(gpu_lib, oracle_lib):
+    """The reference's usage through the Python mirror: a static thin box wall and a small sphere
+    fired at 120 m/s (2 m per 1/60 s step, 20 times the wall's thickness) with
+    setCcdMotionThreshold / setCcdSweptSphereRadius; a second sphere without CCD tunnels through.
+    The oracle fed the same world agrees bit for bit."""
+    from jbgpu import dynamics as D
+    world = D.DiscreteDynamicsWorld()
+    world.setGravity((0.0, 0.0, 0.0))
+    winfo = D.RigidBodyConstructionInfo(0.0, None, D.BoxShape((0.05, 2.0, 2.0)))
+    winfo.startWorldTransform = D.Transform(origin=(5.0, 0.0, 0.0))
+    world.addRigidBody(D.RigidBody(winfo))
+    ball = D.SphereShape(0.1)
+    shots = []
+    for z, ccd in ((-1.0, True), (1.0, False)):
+        info = D.RigidBodyConstructionInfo(0.1, None, ball, ball.calculateLocalInertia(0.1))
+        info.startWorldTransform = D.Transform(origin=(0.0, 0.0, z))
+        b = D.RigidBody(info)
+        b.setLinearVelocity((120.0, 0.0, 0.0))
+        if ccd:
+            b.setCcdMotionThreshold(0.05)
+            b.setCcdSweptSphereRadius(0.08)
+        world.addRigidBody(b)
+        shots.append(b)
+    for _ in range(4):
+        world.stepSimulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    assert shots[0].getCenterOfMassTransform().origin[0] < 5.0     # stopped in front of the wall
+    assert shots[1].getCenterOfMassTransform().origin[0] > 5.1     # tunnelled
+    assert shots[0].getCcdSquareMotionThreshold() == np.float32(0.05) * np.float32(0.05)
+    g = world._g
+    sc = scenes.Scene("bullet", 1.0 / 60.0, 4, {"gravity": (0.0, 0.0, 0.0)},
+                      [{"type": _abi.SHAPE_BOX, "params": (0.05, 2.0, 2.0, 0.0), "points": None},
+                       {"type": _abi.SHAPE_SPHERE, "params": (0.1, 0.0, 0.0, 0.0), "points": None}],
+                      np.concatenate([scenes._bodies(1), scenes._bodies(2)]))
+    sc.bodies["shape"] = [0, 1, 1]
+    sc.bodies["transform"][0, 9:] = (5.0, 0.0, 0.0)
+    sc.bodies["transform"][1, 9:] = (0.0, 0.0, -1.0)
+    sc.bodies["transform"][2, 9:] = (0.0, 0.0, 1.0)
+    sc.bodies["mass"][1:] = 0.1
+    sc.bodies["local_inertia"][1:] = ball.calculateLocalInertia(0.1)
+    sc.bodies["linear_velocity"][1:] = (120.0, 0.0, 0.0)
+    sc.meta["ccd"] = {"bodies": [1], "threshold": 0.05, "radius": 0.08}
+    o = pyoracle.OracleWorld(sc)
+    for _ in range(4):
+        o.step_simulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    assert not H.compare_state(o.get_state(), g.get_state())
+    world.close()
