@@ -109,137 +109,11 @@ __global__ void k_narrow_scatter(int nPairs, const int* cntp, const unsigned cha
 // Entries of the pass: the pairs of buckets 1..6 = the start of bucket 0's row.
 JBD int narrow_active(const int* blockOff, int nBlocks) { return blockOff[(NB_BUCKETS - 1) * nBlocks]; }
 
-// ---- hull vertices in shared memory -----------------------------------------------------------
-// With convex hulls in the world, a block of the pass first gathers the hull shapes of its pairs
-// (a shared-memory hash set, so a hull met by several pairs of the block is staged once) and
-// copies each one's vertices into shared memory with one bulk asynchronous copy (cp.async.bulk,
-// completion counted in bytes on an mbarrier); the support maps of GJK and of the convex-plane
-// test then read them there.  Hulls beyond the block's budget stay in global memory.  The wait is
-// bounded: a copy that does not complete in time sets ST_TIMEOUT and the pairs read global memory.
-constexpr int HULL_STAGE_BYTES = 48 * 1024;
-constexpr int HULL_TABLE = 512;             // hash slots (two hull shapes per pair, 128 pairs)
-constexpr long long HULL_WAIT_LIMIT = 4000000;
-
-struct HullStage {
-    int key[HULL_TABLE];                    // shape id, -1 empty
-    int off[HULL_TABLE];                    // byte offset of its vertices in the stage, -1 not staged
-    int bytes;                              // bytes claimed
-    int staged;                             // bytes copied
-    unsigned long long bar;                 // mbarrier of the copies
-};
-
-JBD unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-JBD int hull_slot(const HullStage& H, int s) {
-    unsigned h = ((unsigned)s * 2654435761u) & (HULL_TABLE - 1);
-    for (int k = 0; k < HULL_TABLE; k++) {
-        const int v = H.key[h];
-        if (v == s) return (int)h;
-        if (v < 0) return -1;
-        h = (h + 1) & (HULL_TABLE - 1);
-    }
-    return -1;
-}
-
-// Stages the hulls hs[0..1] (-1: none) of every thread's pair; returns once the copies landed.
-JBD void stage_hulls(const DevWorld& w, HullStage& H, float4* stage, const int hs[2]) {
-    for (int k = threadIdx.x; k < HULL_TABLE; k += blockDim.x) { H.key[k] = -1; H.off[k] = -1; }
-    if (threadIdx.x == 0) { H.bytes = 0; H.staged = 0; }
-    __syncthreads();
-    for (int q = 0; q < 2; q++) {
-        const int s = hs[q];
-        if (s < 0) continue;
-        unsigned h = ((unsigned)s * 2654435761u) & (HULL_TABLE - 1);
-        for (int k = 0; k < HULL_TABLE; k++) {
-            const int prev = atomicCAS(&H.key[h], -1, s);
-            if (prev == -1 || prev == s) break;
-            h = (h + 1) & (HULL_TABLE - 1);
-        }
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < HULL_TABLE; k += blockDim.x) {
-        const int s = H.key[k];
-        if (s < 0) continue;
-        const int nb = w.sh.hull_cnt[s] * 16;
-        if (nb == 0) continue;
-        const int o = atomicAdd(&H.bytes, nb);
-        if (o + nb <= HULL_STAGE_BYTES) {
-            H.off[k] = o;
-            atomicAdd(&H.staged, nb);
-        }
-    }
-    __syncthreads();
-    const int total = H.staged;
-    if (total == 0) return;
-    const unsigned bar = smem_addr(&H.bar);
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(total) : "memory");
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < HULL_TABLE; k += blockDim.x) {
-        const int s = H.key[k];
-        if (s < 0 || H.off[k] < 0) continue;
-        const float4* src = w.sh.hull_pts + w.sh.hull_off[s];
-        const unsigned dst = smem_addr(stage) + (unsigned)H.off[k];
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(dst), "l"(src), "r"(w.sh.hull_cnt[s] * 16), "r"(bar) : "memory");
-    }
-    auto landed = [&]() {
-        unsigned d;
-        asm volatile("{ .reg .pred p; mbarrier.test_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
-                     : "=r"(d) : "r"(bar) : "memory");
-        return d != 0;
-    };
-    bool done = landed();
-    for (long long k = 0; !done && k < HULL_WAIT_LIMIT; k++) done = landed();
-    if (__syncthreads_or(!done)) {   // gave up: flag it, let the copies finish (bounded), read global memory
-        if (threadIdx.x == 0) atomicOr(&w.ctr[C_STATUS], ST_TIMEOUT);
-        for (long long k = 0; !done && k < HULL_WAIT_LIMIT; k++) done = landed();
-        __syncthreads();
-        for (int k = threadIdx.x; k < HULL_TABLE; k += blockDim.x) H.off[k] = -1;
-        __syncthreads();
-    }
-}
-
-// The shape's parameters, its hull vertices from the block's stage when they are there.
-template <bool STAGE>
-JBD ShapeRef staged_ref(const DevWorld& w, int s, const HullStage* H, const float4* stage) {
-    ShapeRef r = shape_ref(w.sh, s);
-    if (STAGE && r.type == SHAPE_HULL) {
-        const int k = hull_slot(*H, s);
-        if (k >= 0 && H->off[k] >= 0) r.pts = stage + H->off[k] / 16;
-    }
-    return r;
-}
-
 // With perm: n = the grouping's pair blocks and entry i is pair perm[i]; without: n = pairs.
-// STAGE: hull vertices staged in shared memory (HULL_STAGE_BYTES of dynamic shared memory).
-template <bool STAGE>
 __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n, const int* perm, const int* blockOff, EpaRec* queue,
                          int* queueCount, const int* cntp) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool inRange = i < (perm ? narrow_active(blockOff, n) : (cntp ? min(n, *cntp) : n));
-    extern __shared__ float4 hullStage[];
-    HullStage* H = nullptr;
-    if (STAGE) {
-        __shared__ HullStage hst;
-        H = &hst;
-        int hs[2] = {-1, -1};
-        if (inRange) {
-            const int p = perm ? perm[i] : i;
-            const uint64_t key = P.keys[p];
-            const int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
-            if (is_active_state(w.act[a]) || is_active_state(w.act[b])) {
-                if (w.sh.type[w.shape[a]] == SHAPE_HULL) hs[0] = w.shape[a];
-                if (w.sh.type[w.shape[b]] == SHAPE_HULL) hs[1] = w.shape[b];
-            }
-        }
-        stage_hulls(w, hst, hullStage, hs);
-    }
-    if (!inRange) return;
+    if (i >= (perm ? narrow_active(blockOff, n) : (cntp ? min(n, *cntp) : n))) return;
     int p = perm ? perm[i] : i;
     uint64_t key = P.keys[p];
     int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
@@ -271,7 +145,7 @@ __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n
         int ci = (t1 == SHAPE_PLANE) ? col0 : col1;       // convex body (manifold body0)
         int pi = (t1 == SHAPE_PLANE) ? col1 : col0;
         Xf cx = (ci == col0) ? x0 : x1, px = (ci == col0) ? x1 : x0;
-        ShapeRef cs = staged_ref<STAGE>(w, w.shape[ci], H, hullStage);
+        ShapeRef cs = shape_ref(w.sh, w.shape[ci]);
         float4 pl = w.sh.plane[w.shape[pi]];
         V pn = mk(pl.x, pl.y, pl.z);
         Xf planeInConvex = xf_mul(xf_inverse(cx), px);
@@ -288,7 +162,7 @@ __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n
         }
         manifold_refresh(m, w, mb0, mb1);
     } else {
-        ShapeRef sa = staged_ref<STAGE>(w, s0, H, hullStage), sb = staged_ref<STAGE>(w, s1, H, hullStage);
+        ShapeRef sa = shape_ref(w.sh, s0), sb = shape_ref(w.sh, s1);
         float md = __fadd_rn(__fadd_rn(sa.margin, sb.margin), w.cbt);
         md = __fmul_rn(md, md);
         {   // one counter atomic per group of converged lanes
@@ -486,21 +360,11 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
     if (nPairs > 0) {
         if (nb.group) {
             narrow_group(w, P, nPairs, nb, s, cntp);
-            if (nb.stageHulls)
-                k_narrow<true><<<(nPairs + 127) / 128, 128, HULL_STAGE_BYTES, s>>>(
-                    w, P, gridn_nb(nPairs), nb.perm, nb.blockOff, (EpaRec*)nb.queue, nb.queueCount, nullptr);
-            else
-                k_narrow<false><<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, gridn_nb(nPairs), nb.perm, nb.blockOff,
-                                                                     (EpaRec*)nb.queue, nb.queueCount, nullptr);
-            note_launch();
+            k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, gridn_nb(nPairs), nb.perm, nb.blockOff,
+                                                           (EpaRec*)nb.queue, nb.queueCount, nullptr); note_launch();
         } else {
-            if (nb.stageHulls)
-                k_narrow<true><<<(nPairs + 127) / 128, 128, HULL_STAGE_BYTES, s>>>(
-                    w, P, nPairs, nullptr, nullptr, (EpaRec*)nb.queue, nb.queueCount, cntp);
-            else
-                k_narrow<false><<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, nullptr, nullptr, (EpaRec*)nb.queue,
-                                                                     nb.queueCount, cntp);
-            note_launch();
+            k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, nullptr, nullptr, (EpaRec*)nb.queue,
+                                                           nb.queueCount, cntp); note_launch();
         }
     }
     if (prof) { prof->mark(PH_NARROW, 1, s); prof->mark(PH_EPA, 0, s); }
@@ -524,9 +388,7 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
 size_t epa_queue_record_bytes() { return sizeof(EpaRec); }
 
 int narrowphase_configure() {
-    return (cudaFuncSetAttribute(k_narrow<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, HULL_STAGE_BYTES) ==
-                cudaSuccess &&
-            cudaFuncSetAttribute(k_narrow_epa_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EPA_SMEM_BYTES) ==
+    return (cudaFuncSetAttribute(k_narrow_epa_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EPA_SMEM_BYTES) ==
                 cudaSuccess &&
             cudaFuncSetAttribute(EPA_T1_KERNEL, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)EPA_T1_SMEM_BYTES) ==
                 cudaSuccess &&
@@ -587,8 +449,8 @@ void narrowphase_launch_static(const DevWorld& w, DevPairs& P, int nPairs, Narro
     cudaMemsetAsync(nb.queueCount, 0, sizeof(int), s);
     if (nPairs <= 0) return;
     narrow_group(w, P, nPairs, nb, s);
-    k_narrow<false><<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, gridn_nb(nPairs), nb.perm, nb.blockOff, (EpaRec*)nb.queue,
-                                                          nb.queueCount, nullptr); note_launch();
+    k_narrow<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, gridn_nb(nPairs), nb.perm, nb.blockOff, (EpaRec*)nb.queue,
+                                                   nb.queueCount, nullptr); note_launch();
     unsigned char* b = (unsigned char*)base;
     EpaArena ar;
     ar.fN = (float4*)(b + OFF_FN);

@@ -18,8 +18,6 @@ struct NarrowBuffers {
     int* perm = nullptr;          // pairs grouped by bucket (pair capacity)
     int* blockOff = nullptr;      // per block and bucket counts, scanned in place (NB_BUCKETS x pair blocks)
     bool group = true;            // group pairs by algorithm (worth it with two or more shape kinds)
-    bool stageHulls = false;      // the world has convex hulls: a block stages its pairs' hull vertices
-                                  // in shared memory (one bulk copy per hull) before the pass
     void* scanScratch = nullptr;  // scan scratch for blockOff
 };
 

@@ -313,10 +313,6 @@ int sync_shapes(jbgpu_world* w) {
     }
     if (nh) CK(cudaMemcpyAsync(S.hull_pts, w->hullPts.data(), sizeof(float4) * nh, cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
-    bool hulls = false;   // the narrowphase stages hull vertices in shared memory when there are hulls
-    for (int k = 0; k < ns; k++) hulls = hulls || type[k] == JBGPU_SHAPE_CONVEX_HULL;
-    if (hulls != w->nb.stageHulls) graphs_clear(w);
-    w->nb.stageHulls = hulls;
     w->shapesDirty = false;
     return JBGPU_OK;
 }
