@@ -27,6 +27,8 @@ warm-up steps, then the K timed steps.  The timed window is steps settle+W .. se
   cpu_baseline  the CPU restatement of the reference (oracle, one core, the reference's island
          solver order) continued for --cpu-window steps from GPU snapshots inside the timed
          window.
+  other_workloads  the 1,000-box, 20,000-hull and 4,096-world workloads measured beside the
+         headline in the same run (device-timed from a settled point, with their phases).
 
 --impl reference times that CPU restatement on the same window: the GPU steps the world to
 the window's first step (untimed set-up), the oracle takes over its state and manifolds and
@@ -73,6 +75,7 @@ def parse():
     p.add_argument("--rebuild-interval", type=int, default=None, help="jbgpu_config.broadphase_rebuild_interval")
     p.add_argument("--ref-seconds", type=float, default=120.0, help="time budget of the reference arm's timed steps")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-warm-start comparison")
+    p.add_argument("--no-others", action="store_true", help="skip the 1k-box, 20k-hull and 4,096-world workloads")
     p.add_argument("--learned-cap", type=int, default=12000, help="iteration cap of the world-residual comparison")
     p.add_argument("--no-rays", action="store_true", help="skip the rayTest batch measurement")
     p.add_argument("--sweeps", type=int, default=4096, help="convexSweepTest sweeps per measured batch (0: skip)")
@@ -415,6 +418,44 @@ def traffic_for_window(dom, window_bytes):
                                        "capture_algorithmic_bytes": rec["algorithmic_bytes"], "scale": scale}
 
 
+# The other workloads of the step, measured beside the headline in the same run: each stepped
+# from rest to a settled point (untimed), then timed over `steps` steps by CUDA events on the
+# world's stream (CUDA graphs, as the headline); the phases come from a second, event-marked run.
+OTHER_WORKLOADS = [("boxes_1k", 100, 100), ("hulls_20k", 300, 20), ("batched_4096", 200, 20)]
+
+
+def measure_workload(name, settle, steps, seed, local):
+    from jbgpu import _abi
+    from jbgpu.lib import GpuWorld
+    sc = make_scene(name, seed)
+    cfg = _abi.default_config(**sc.config)
+    cfg.device = local
+    w = GpuWorld(sc, config=cfg)
+    w.set_graph(True)
+    advance(w, sc, settle)
+    w.synchronize()
+    w.timer_start()
+    advance(w, sc, steps)
+    ms = w.timer_stop() / steps
+    c = w.counters()
+    w.close()
+    w = GpuWorld(sc, config=cfg)
+    advance(w, sc, settle)
+    w.set_profiling(steps)
+    advance(w, sc, steps)
+    w.synchronize()
+    ph, k, _ = w.phase_times()
+    w.close()
+    worlds = 1 if sc.world_of_body is None else int(sc.world_of_body.max()) + 1
+    return {"workload": sc.name, "bodies": sc.n_bodies, "worlds": worlds, "dt": sc.dt, "iterations": cfg.num_iterations,
+            "timed_steps": "%d..%d from rest" % (settle, settle + steps - 1), "ms_per_step": ms,
+            "body_steps_per_s": sc.n_bodies / (ms * 1e-3),
+            "phases_ms": {a: round(b / k, 4) for a, b in ph.items() if b > 0},
+            "counters": {q: c[q] for q in ("pairs", "contacts", "solver_rows", "colours", "cut_colours", "gjk_calls",
+                                           "epa_calls", "status_flags")},
+            "clock": "CUDA events on the world's stream, CUDA graphs; phases from a second event-marked run"}
+
+
 def run_ours(args, dist):
     from jbgpu import _abi, _build, lib
     from jbgpu.lib import GpuWorld
@@ -468,6 +509,10 @@ def run_ours(args, dist):
     if dist.rank == 0 and args.sweeps > 0:
         sweeps = measure_sweeps(w, sc, args.sweeps, args.seed + 30, dist.local)
     w.close()
+    others = None
+    if dist.rank == 0 and dist.size == 1 and not args.no_others:
+        others = [measure_workload(nm, st, k, args.seed, dist.local) for nm, st, k in OTHER_WORKLOADS
+                  if nm != args.workload]
     wall = t1 - t0
     elapsed = dist.max(device_ms * 1e-3)
     # ---- the same steps again with per-phase event marks (the breakdown and the roofline) ---
@@ -578,6 +623,7 @@ def run_ours(args, dist):
         "learned_warmstart": learned,
         "ray_test": rays,
         "convex_sweep_test": sweeps,
+        "other_workloads": others,
         "step_graphs": graph_info,
         "clocks": clocks,
         "status_flags": final["status_flags"],
