@@ -815,6 +815,7 @@ SCENES = {
     "mixed_100k": mixed_100k,
     "hulls_20k": hulls,
     "batched_4096": batched_worlds,
+    "batched_1024": lambda seed=0: batched_worlds(1024, seed=seed),   # a quarter of it (profiling captures)
     "box_stack": box_stack,
     "small_mixed": small_mixed,
     "learned_warmstart": learned_warmstart,
