@@ -403,7 +403,7 @@ def measure_sweeps(w, scene, nsweeps, seed, local):
             "clock": "CUDA events on the world's stream around 3 batches of device buffers"}
 
 
-def traffic_for_window(dom, window_bytes):
+def traffic_for_window(dom, window_bytes, workload):
     """DRAM bytes per launch of the dominant kernel for this window: one ncu capture's
     dram__bytes_read.sum + dram__bytes_write.sum, scaled by the window's algorithmic bytes per
     launch over the capture's (profiles/traffic.json)."""
@@ -411,7 +411,7 @@ def traffic_for_window(dom, window_bytes):
     if not os.path.exists(tp):
         return None, None
     rec = json.load(open(tp)).get(dom)
-    if not isinstance(rec, dict) or not rec.get("algorithmic_bytes"):
+    if not isinstance(rec, dict) or not rec.get("algorithmic_bytes") or rec.get("workload") != workload:
         return None, None
     scale = window_bytes / rec["algorithmic_bytes"]
     return rec["dram_bytes"] * scale, {"captured": rec.get("captured"), "capture_dram_bytes": rec["dram_bytes"],
@@ -544,7 +544,7 @@ def run_ours(args, dist):
         achieved = sum(by) / (phases[dom] * 1e-3) / 1e9
         peak = pk["hbm_gbs"] if pk else 6800.0
         per_launch = sum(by) / len(by)
-        traffic, traffic_src = traffic_for_window(dom, per_launch)
+        traffic, traffic_src = traffic_for_window(dom, per_launch, sc.name)
         roof = {"bound": "hbm", "kernel_phase": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "traffic_from": traffic_src,
                 "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if pk else "of fallback 6.8 TB/s",
