@@ -60,7 +60,10 @@ extern "C" {
 #define JBGPU_SHAPE_CONVEX_HULL  4
 #define JBGPU_SHAPE_SPHERE       6
 #define JBGPU_SHAPE_CAPSULE      8
+#define JBGPU_SHAPE_TRIANGLE_MESH 16  /* BvhTriangleMeshShape, static or kinematic bodies only */
 #define JBGPU_SHAPE_STATIC_PLANE 23
+#define JBGPU_SHAPE_COMPOUND     25
+#define JBGPU_COMPOUND_MAX_CHILDREN 16
 
 /* ---- activation states (collision/dispatch/CollisionObject.java:43-47) ------------ */
 #define JBGPU_ACTIVE_TAG           1
@@ -98,9 +101,15 @@ extern "C" {
 #define JBGPU_MANIFOLD_POINTS 4
 
 /* Pair keys.  A pair of bodies (a, b) (body index = uid - 1) is stored under the
- * canonical key (owner << 32) | partner, where the owner is the non-plane body
- * when exactly one body is a static plane, else min(a, b).  Keys are unique and
- * pair arrays are always sorted by key.  The reference keeps the same set
+ * canonical key (owner << 32) | (sub << 24) | partner, where the owner is the non-plane
+ * body when exactly one body is a static plane, else min(a, b).  sub numbers the child
+ * combinations of a pair with a compound body, each with its own manifold as
+ * CompoundCollisionAlgorithm keeps one child algorithm per child
+ * (collision/dispatch/CompoundCollisionAlgorithm.java:49-67): sub = i * n1 + j for child i of
+ * body min(a, b) and child j of body max(a, b) (n1 = the latter's child count, 1 when it is
+ * not a compound; i, j = 0 for a body that is not one); sub is 0 for every other pair.  Body
+ * indices stay below 2^24.  Keys are unique and pair arrays are always sorted by key.  The
+ * reference keeps the same set of body pairs
  * (collision/broadphase/HashedOverlappingPairCache.java:291-347) in hash order. */
 
 typedef struct jbgpu_config {
@@ -150,9 +159,23 @@ typedef struct jbgpu_shape_desc {
     int32_t      type;       /* JBGPU_SHAPE_* */
     float        params[4];  /* BOX: half extents xyz (BoxShape(Vector3)); SPHERE: radius;
                                 CAPSULE: radius, height (CapsuleShape(radius, height), up axis y);
-                                STATIC_PLANE: normal xyz, plane constant; CONVEX_HULL: unused */
-    const float* points;     /* CONVEX_HULL: num_points * 3 floats (ConvexHullShape(points)) */
+                                STATIC_PLANE: normal xyz, plane constant; CONVEX_HULL: unused;
+                                TRIANGLE_MESH, COMPOUND: params[0] = collision margin
+                                (setMargin; the reference's default is 0) */
+    const float* points;     /* CONVEX_HULL: num_points * 3 floats (ConvexHullShape(points));
+                                TRIANGLE_MESH: the vertex array, num_points * 3 floats */
     int32_t      num_points;
+    /* TRIANGLE_MESH: BvhTriangleMeshShape(new TriangleIndexVertexArray(num_triangles, indices,
+       12, num_points, points, 12), true) - one part, scaling (1,1,1), the quantized tree
+       (collision/shapes/BvhTriangleMeshShape.java:69-93, OptimizedBvh.java:283-342). */
+    const int32_t* indices;  /* 3 vertex indices per triangle */
+    int32_t      num_triangles;
+    /* COMPOUND: CompoundShape with addChildShape(child_transforms[i], children[i]) in order
+       (collision/shapes/CompoundShape.java:59-91); children are BOX, SPHERE, CAPSULE or
+       CONVEX_HULL, at most JBGPU_COMPOUND_MAX_CHILDREN. */
+    const struct jbgpu_shape_desc* children;
+    const float* child_transforms;   /* 12 floats per child: basis rows (row-major 3x3), origin */
+    int32_t      num_children;
 } jbgpu_shape_desc;
 
 /* RigidBodyConstructionInfo (dynamics/RigidBodyConstructionInfo.java:46-79) plus the
@@ -243,6 +266,14 @@ void        jbgpu_config_default(jbgpu_config* cfg);
 
 /* CollisionShape.calculateLocalInertia for a shape description (host arithmetic). */
 int jbgpu_shape_local_inertia(const jbgpu_shape_desc* shape, float mass, float inertia_out[3]);
+/* The quantized tree of a TRIANGLE_MESH descriptor as the library builds it (OptimizedBvh's
+ * quantizedContiguousNodes in walk order, collision/shapes/OptimizedBvh.java:283-342, and the
+ * shape's local aabb, TriangleMeshShape.localAabbMin/Max): 4 int32 per node - min.x | min.y << 16,
+ * min.z | max.x << 16, max.y | max.z << 16 (quantized, unsigned 16-bit), then the triangle index
+ * of a leaf or -escapeIndex of an internal node.  Host only.  n_nodes > capacity is
+ * JBGPU_ERR_CAPACITY with *n_nodes set; local_aabb (nullable): min xyz, max xyz. */
+int jbgpu_shape_mesh_bvh(const jbgpu_shape_desc* mesh, int32_t* nodes, int32_t capacity, int32_t* n_nodes,
+                         float local_aabb[6]);
 
 /* ---- world ---------------------------------------------------------------------- */
 typedef struct jbgpu_world jbgpu_world;

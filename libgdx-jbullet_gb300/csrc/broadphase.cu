@@ -17,6 +17,7 @@
 #include <utility>
 
 #include "broadphase.cuh"
+#include "dispatch.cuh"
 #include "prims.cuh"
 
 namespace jbg {
@@ -179,11 +180,13 @@ __global__ void k_traverse(DevWorld w, const int* sortedBody, int nf, Bvh t, con
     int bi = sortedBody[s];
     auto emit = [&](int bj) {
         int owner = bi < bj ? bi : bj, partner = bi < bj ? bj : bi;
+        const int subs = w.hasCompound ? pair_subs(w.sh, w.shape[owner], w.shape[partner]) : 1;
         if (!FILL) {
-            atomicAdd(&cnt[owner], 1);
+            atomicAdd(&cnt[owner], subs);
         } else {
-            int pos = off[owner] + atomicAdd(&cursor[owner], 1);
-            if (pos < capacity) partners[pos] = partner;
+            int pos = off[owner] + atomicAdd(&cursor[owner], subs);
+            for (int k = 0; k < subs; k++)
+                if (pos + k < capacity) partners[pos + k] = partner | (k << 24);
         }
     };
     if (FILL) {
@@ -238,38 +241,43 @@ __global__ void k_plane_pairs(DevWorld w, const int* planeList, const int* plane
     for (int k = planeStart[wi]; k < planeStart[wi + 1]; k++) {
         int p = planeList[k];
         if (!ovl(a0, a1, w.amin[p], w.amax[p]) || !filt(w, i, p)) continue;
-        if (!FILL) atomicAdd(&cnt[i], 1);
+        const int subs = w.hasCompound ? pair_subs(w.sh, w.shape[i], w.shape[p]) : 1;
+        if (!FILL) atomicAdd(&cnt[i], subs);
         else {
-            int pos = off[i] + atomicAdd(&cursor[i], 1);
-            if (pos < capacity) partners[pos] = p;
+            int pos = off[i] + atomicAdd(&cursor[i], subs);
+            for (int k = 0; k < subs; k++)
+                if (pos + k < capacity) partners[pos + k] = p | (k << 24);
         }
     }
 }
 
-// Sort each owner's partners ascending and emit the canonical keys.
+// Sort each owner's partner words (sub << 24 | partner, compared unsigned) ascending and emit the
+// canonical keys.
 __global__ void k_segment_sort(int n, const int* off, const int* cnt, int* partners, uint64_t* keys, int capacity) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int o = off[i], c = cnt[i];
     if (o + c > capacity) return;
-    int* p = partners + o;
+    unsigned* p = (unsigned*)partners + o;
     if (c <= 32) {
-        int v[32];
+        unsigned v[32];
         for (int k = 0; k < c; k++) v[k] = p[k];
         for (int k = 1; k < c; k++) {
-            int x = v[k], j = k - 1;
+            unsigned x = v[k];
+            int j = k - 1;
             while (j >= 0 && v[j] > x) { v[j + 1] = v[j]; j--; }
             v[j + 1] = x;
         }
-        for (int k = 0; k < c; k++) keys[o + k] = ((uint64_t)(unsigned)i << 32) | (unsigned)v[k];
+        for (int k = 0; k < c; k++) keys[o + k] = ((uint64_t)(unsigned)i << 32) | v[k];
     } else {
         for (int gap = c / 2; gap > 0; gap /= 2)          // Shell sort for rare crowded owners
             for (int k = gap; k < c; k++) {
-                int x = p[k], j = k;
+                unsigned x = p[k];
+                int j = k;
                 while (j >= gap && p[j - gap] > x) { p[j] = p[j - gap]; j -= gap; }
                 p[j] = x;
             }
-        for (int k = 0; k < c; k++) keys[o + k] = ((uint64_t)(unsigned)i << 32) | (unsigned)p[k];
+        for (int k = 0; k < c; k++) keys[o + k] = ((uint64_t)(unsigned)i << 32) | p[k];
     }
 }
 
@@ -284,7 +292,7 @@ __global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int n
     uint64_t key = nw.keys[p];
     int lo = 0, hi = nOld - 1, found = -1;
     if (offPrev) {
-        const int o = (int)(key >> 32);
+        const int o = key_owner(key);
         lo = offPrev[o];
         hi = min(offPrev[o + 1], nOld) - 1;
     }
@@ -294,7 +302,7 @@ __global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int n
         if (k == key) { found = mid; break; }
         if (k < key) lo = mid + 1; else hi = mid - 1;
     }
-    int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+    int a = key_owner(key), b = key_partner(key);
     if (found >= 0 && old.has[found]) {
         int n = old.n[found];
         nw.has[p] = 1;
@@ -309,9 +317,10 @@ __global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int n
     } else {
         nw.has[p] = 0;
         nw.n[p] = 0;
-        bool bPlane = (w.flags[b] & CF_PLANE) != 0;
-        nw.b0[p] = bPlane ? a : min(a, b);   // manifold (convex, plane) or (lower uid, higher uid)
-        nw.b1[p] = bPlane ? b : max(a, b);
+        int mb0, mb1;
+        manifold_bodies(a, b, w.sh.type[w.shape[min(a, b)]], w.sh.type[w.shape[max(a, b)]], mb0, mb1);
+        nw.b0[p] = mb0;
+        nw.b1[p] = mb1;
     }
 }
 

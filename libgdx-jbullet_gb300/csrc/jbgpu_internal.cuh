@@ -7,10 +7,14 @@
 
 namespace jbg {
 
-enum { SHAPE_BOX = 0, SHAPE_HULL = 4, SHAPE_SPHERE = 6, SHAPE_CAPSULE = 8, SHAPE_PLANE = 23 };
+enum { SHAPE_BOX = 0, SHAPE_TRIANGLE = 1, SHAPE_HULL = 4, SHAPE_SPHERE = 6, SHAPE_CAPSULE = 8, SHAPE_MESH = 16,
+       SHAPE_PLANE = 23, SHAPE_COMPOUND = 25 };
+__host__ __device__ inline bool shape_is_convex(int t) { return t < 15; }      // BroadphaseNativeType.isConvex
+__host__ __device__ inline bool shape_is_concave(int t) { return t > 15 && t < 24; }
 enum { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEACTIVATION = 4, DISABLE_SIMULATION = 5 };
 enum { CF_STATIC = 1, CF_KINEMATIC = 2, CF_NO_CONTACT_RESPONSE = 4, CF_PLANE = 64 };
-enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8, ST_BAD_WORLD = 16, ST_CCD_PLANE = 32 };
+enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8, ST_BAD_WORLD = 16, ST_CCD_PLANE = 32,
+       ST_QUERY_SHAPE = 64 };
 
 // Counters kept on the device (indices into DevWorld::ctr).
 enum {
@@ -30,7 +34,43 @@ struct DevShapes {
     int* hull_off;
     int* hull_cnt;
     float4* hull_pts;
+    // CompoundShape: children child_off[s] .. + child_cnt[s] (0 for other shapes) of the child
+    // table: the child's shape index and transform (basis rows, origin in .w; 3 per child)
+    int* child_off;
+    int* child_cnt;
+    int* child_shape;
+    float4* child_xf;
+    // BvhTriangleMeshShape: quantized nodes mesh_node_off[s] .. + mesh_node_cnt[s] in walk order
+    // (x: min.x | min.y << 16, y: min.z | max.x << 16, z: max.y | max.z << 16, w: triangle index
+    // of a leaf or -escapeIndex), triangles from mesh_tri_off[s] (3 vertices each), and per
+    // shape 3 float4: bvhAabbMin, bvhAabbMax, bvhQuantization
+    int* mesh_node_off;
+    int* mesh_node_cnt;
+    int* mesh_tri_off;
+    float4* mesh_q;
+    int4* mesh_nodes;
+    float4* mesh_tris;
 };
+
+// Pair key fields: (owner << 32) | (sub << 24) | partner (sub: child combination of a pair with
+// a compound body).
+__host__ __device__ inline int key_owner(uint64_t k) { return (int)(k >> 32); }
+__host__ __device__ inline int key_partner(uint64_t k) { return (int)(k & 0xffffffu); }
+__host__ __device__ inline int key_sub(uint64_t k) { return (int)((k >> 24) & 0xffu); }
+constexpr int MAX_BODIES_KEYED = 1 << 24;
+
+// The bodies of the manifold a pair's collision algorithm creates, from the two bodies' shape
+// types (DefaultCollisionConfiguration.getCollisionAlgorithmCreateFunc java:160-215 with the
+// algorithms' constructors): a compound's side first (with two compounds the higher body, whose
+// child the swapped CompoundCollisionAlgorithm puts first), else the convex body before a plane
+// or mesh, else (lower, higher).
+__host__ __device__ inline void manifold_bodies(int a, int b, int typeLo, int typeHi, int& mb0, int& mb1) {
+    const int lo = a < b ? a : b, hi = a < b ? b : a;
+    bool hiFirst = typeHi == SHAPE_COMPOUND ||
+                   (typeLo != SHAPE_COMPOUND && shape_is_convex(typeHi) && !shape_is_convex(typeLo));
+    mb0 = hiFirst ? hi : lo;
+    mb1 = hiFirst ? lo : hi;
+}
 
 // Manifold point, one record spread over eight float4 arrays indexed [pair * 4 + point]:
 //  pA  = localPointA.xyz, distance1        pB  = localPointB.xyz, lifeTime (int bits)
@@ -39,7 +79,7 @@ struct DevShapes {
 //  imp = appliedImpulseLateral1, appliedImpulseLateral2, lateralFrictionInitialized, 0
 //  d1  = lateralFrictionDir1.xyz           d2  = lateralFrictionDir2.xyz
 struct DevPairs {
-    uint64_t* keys;       // sorted canonical keys (owner << 32 | partner)
+    uint64_t* keys;       // sorted canonical keys (owner << 32 | sub << 24 | partner)
     int* has;             // pair owns an algorithm + manifold
     int* n;               // manifold points
     int* b0;              // manifold body0 / body1
@@ -106,6 +146,7 @@ struct DevWorld {
     float resTol;         // > 0: residual-terminated PGS
     int maxIter;          // iteration cap when resTol > 0
     int resScope;         // 0: residual per island, 1: one residual over the world's rows
+    int hasCompound;      // some shape is a compound: pairs expand to child combinations
     float erp, warm, slop;
     int solverMode;
 };

@@ -13,6 +13,7 @@
 #include <mutex>
 
 #include "epa.cuh"
+#include "dispatch.cuh"
 #include "prims.cuh"
 #include "manifold.cuh"
 #include "narrowphase.cuh"
@@ -42,13 +43,14 @@ JBD void manifold_refresh(Mf& m, const DevWorld& w, int mb0, int mb1) {
 // lists buckets 1..10 in order; the pass covers nPairs - count[0] entries.
 JBD int narrow_bucket(const DevWorld& w, const DevPairs& P, int p) {
     uint64_t key = P.keys[p];
-    int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+    int a = key_owner(key), b = key_partner(key);
     int col0 = min(a, b), col1 = max(a, b);
     if (!is_active_state(w.act[col0]) && !is_active_state(w.act[col1])) return 0;
-    int t0 = w.sh.type[w.shape[col0]], t1 = w.sh.type[w.shape[col1]];
-    if (t0 == SHAPE_PLANE && t1 == SHAPE_PLANE) return 0;
-    if (t0 == SHAPE_PLANE || t1 == SHAPE_PLANE) return 1;
-    if (t0 == SHAPE_SPHERE && t1 == SHAPE_SPHERE) return 2;
+    int t0, t1;
+    const int kind = pair_leaf_types(w, key, col0, col1, t0, t1);
+    if (kind == ALG_EMPTY || kind >= ALG_CONVEX_CONCAVE) return 0;   // meshes: the concave pass
+    if (kind == ALG_CONVEX_PLANE || kind == ALG_PLANE_CONVEX) return 1;
+    if (kind == ALG_SPHERE_SPHERE) return 2;
     const int touching = P.has[p] && P.n[p] > 0 ? 4 : 0;
     if (t0 == SHAPE_HULL || t1 == SHAPE_HULL) return 6 + touching;
     if (t0 == SHAPE_CAPSULE || t1 == SHAPE_CAPSULE) return 5 + touching;
@@ -116,44 +118,44 @@ __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n
     if (i >= (perm ? narrow_active(blockOff, n) : (cntp ? min(n, *cntp) : n))) return;
     int p = perm ? perm[i] : i;
     uint64_t key = P.keys[p];
-    int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+    int a = key_owner(key), b = key_partner(key);
     int col0 = min(a, b), col1 = max(a, b);
     if (!is_active_state(w.act[col0]) && !is_active_state(w.act[col1])) return;   // needsCollision
-    int s0 = w.shape[col0], s1 = w.shape[col1];
-    int t0 = w.sh.type[s0], t1 = w.sh.type[s1];
-    if (t0 == SHAPE_PLANE && t1 == SHAPE_PLANE) return;
+    Xf x0 = load_xf(w, col0), x1 = load_xf(w, col1);   // the ManifoldResult's root transforms
+    Leaf f, g;
+    const int kind = pair_leaves(w, key, col0, col1, x0, x1, f, g);
+    if (kind == ALG_EMPTY || kind >= ALG_CONVEX_CONCAVE) return;   // no manifold; meshes: the concave pass
     Mf m;
     if (!P.has[p]) { P.has[p] = 1; m.n = 0; }
     else load_mf(P, p, m);
     int mb0 = P.b0[p], mb1 = P.b1[p];
-    Xf x0 = load_xf(w, col0), x1 = load_xf(w, col1);
     float fr0 = w.friction[col0], fr1 = w.friction[col1], re0 = w.restitution[col0], re1 = w.restitution[col1];
-    if (t0 == SHAPE_SPHERE && t1 == SHAPE_SPHERE) {
-        V diff = sub(x0.o, x1.o);
+    if (kind == ALG_SPHERE_SPHERE) {
+        V diff = sub(f.x.o, g.x.o);
         float l = len(diff);
-        float r0 = w.sh.margin[s0], r1 = w.sh.margin[s1];
+        float r0 = w.sh.margin[f.shape], r1 = w.sh.margin[g.shape];
         float rs = __fadd_rn(r0, r1);
         if (!(l > rs)) {
             float dist = __fsub_rn(l, rs);
             V n = mk(1.0f, 0.0f, 0.0f);
             if (l > FLT_EPS) n = scl(diff, jdiv(1.0f, l));
-            V pos1 = add(x1.o, scl(n, r1));
+            V pos1 = add(g.x.o, scl(n, r1));
             add_contact(m, mb0, col0, x0, x1, fr0, fr1, re0, re1, n, pos1, dist, w.cbt);
         }
         manifold_refresh(m, w, mb0, mb1);
-    } else if (t0 == SHAPE_PLANE || t1 == SHAPE_PLANE) {
-        int ci = (t1 == SHAPE_PLANE) ? col0 : col1;       // convex body (manifold body0)
-        int pi = (t1 == SHAPE_PLANE) ? col1 : col0;
-        Xf cx = (ci == col0) ? x0 : x1, px = (ci == col0) ? x1 : x0;
-        ShapeRef cs = shape_ref(w.sh, w.shape[ci]);
-        float4 pl = w.sh.plane[w.shape[pi]];
-        V pn = mk(pl.x, pl.y, pl.z);
+    } else if (kind == ALG_CONVEX_PLANE || kind == ALG_PLANE_CONVEX) {
+        const Leaf& c = kind == ALG_CONVEX_PLANE ? f : g;   // the convex object
+        const Leaf& pl = kind == ALG_CONVEX_PLANE ? g : f;
+        Xf cx = c.x, px = pl.x;
+        ShapeRef cs = shape_ref(w.sh, c.shape);
+        float4 plq = w.sh.plane[pl.shape];
+        V pn = mk(plq.x, plq.y, plq.z);
         Xf planeInConvex = xf_mul(xf_inverse(cx), px);
         Xf convexInPlane = xf_mul(xf_inverse(px), cx);
         V dir = mulMv(scl(pn, -1.0f), planeInConvex.b);
         V vtx = support_with_margin(cs, dir);
         V vtxInPlane = xf_apply(convexInPlane, vtx);
-        float distance = __fsub_rn(dot(pn, vtxInPlane), pl.w);
+        float distance = __fsub_rn(dot(pn, vtxInPlane), plq.w);
         V proj = sub(vtxInPlane, scl(pn, distance));
         V vtxWorld = xf_apply(px, proj);
         if (distance < w.cbt) {
@@ -162,29 +164,29 @@ __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n
         }
         manifold_refresh(m, w, mb0, mb1);
     } else {
-        ShapeRef sa = shape_ref(w.sh, s0), sb = shape_ref(w.sh, s1);
+        ShapeRef sa = shape_ref(w.sh, f.shape), sb = shape_ref(w.sh, g.shape);
         float md = __fadd_rn(__fadd_rn(sa.margin, sb.margin), w.cbt);
         md = __fmul_rn(md, md);
         {   // one counter atomic per group of converged lanes
             const unsigned am = __activemask();
             if ((threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(&w.ctr[C_GJK], __popc(am));
         }
-        GjkPart g = gjk_part(sa, x0, sb, x1, md);
-        if (g.needEpa) {
+        GjkPart gp = gjk_part(sa, f.x, sb, g.x, md);
+        if (gp.needEpa) {
             int q = atomicAdd(queueCount, 1);
             EpaRec r;
             r.pair = p;
-            r.valid = g.isValid ? 1 : 0;
-            r.distance = g.distance;
+            r.valid = gp.isValid ? 1 : 0;
+            r.distance = gp.distance;
             r.pad = 0.0f;
-            r.pA = f4(g.pointOnA, 0.0f);
-            r.pB = f4(g.pointOnB, 0.0f);
-            r.nB = f4(g.normalInB, 0.0f);
+            r.pA = f4(gp.pointOnA, 0.0f);
+            r.pB = f4(gp.pointOnB, 0.0f);
+            r.nB = f4(gp.normalInB, 0.0f);
             queue[q] = r;
             if (P.n[p] == 0 && m.n == 0) P.n[p] = 0;
             return;   // the EPA pass finishes this pair
         }
-        if (g.isValid) add_contact(m, mb0, col0, x0, x1, fr0, fr1, re0, re1, g.normalInB, add(g.pointOnB, g.offset), g.distance, w.cbt);
+        if (gp.isValid) add_contact(m, mb0, col0, x0, x1, fr0, fr1, re0, re1, gp.normalInB, add(gp.pointOnB, gp.offset), gp.distance, w.cbt);
         manifold_refresh(m, w, mb0, mb1);
     }
     store_mf(P, p, m);
@@ -193,19 +195,36 @@ __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n
 // One queued pair, by the 32 lanes of a warp (see epa.cuh); lane 0 updates the manifold.  With
 // ovfQueue (a reduced-capacity tier) a query that outgrows its slot leaves no result and is queued
 // for the tier with the full capacities: EPA is deterministic, so its result does not depend on
-// which tier finishes it.
+// which tier finishes it.  With cand (the concave pass) a queued entry is a (pair, triangle)
+// candidate: the convex object against the mesh triangle, the result into res.
 __device__ void epa_query(const DevWorld& w, DevPairs& P, const EpaRec* queue, int qi, const EpaSlot& sl, int lane,
-                          int* ovfQueue = nullptr, int* ovfCount = nullptr) {
+                          int* ovfQueue = nullptr, int* ovfCount = nullptr, const int2* cand = nullptr,
+                          float4* res = nullptr) {
     EpaRec r = queue[qi];
-    int p = r.pair;
+    const int p = cand ? cand[r.pair].x : r.pair;
     uint64_t key = P.keys[p];
-    int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+    int a = key_owner(key), b = key_partner(key);
     int col0 = min(a, b), col1 = max(a, b);
     int mb0 = P.b0[p], mb1 = P.b1[p];
     Xf x0 = load_xf(w, col0), x1 = load_xf(w, col1);
-    ShapeRef sa = shape_ref(w.sh, w.shape[col0]), sb = shape_ref(w.sh, w.shape[col1]);
-    V offset = scl(add(x0.o, x1.o), 0.5f);
-    Xf lA = x0, lB = x1;
+    Leaf f, g;
+    const int kind = pair_leaves(w, key, col0, col1, x0, x1, f, g);
+    ShapeRef sa, sb;
+    Xf lA, lB;
+    if (cand) {                               // (convex, triangle of the mesh)
+        const Leaf& c = kind == ALG_CONVEX_CONCAVE ? f : g;
+        const Leaf& t = kind == ALG_CONVEX_CONCAVE ? g : f;
+        sa = shape_ref(w.sh, c.shape);
+        sb = triangle_ref(w.sh, t.shape, cand[r.pair].y);
+        lA = c.x;
+        lB = t.x;
+    } else {
+        sa = shape_ref(w.sh, f.shape);
+        sb = shape_ref(w.sh, g.shape);
+        lA = f.x;
+        lB = g.x;
+    }
+    V offset = scl(add(lA.o, lB.o), 0.5f);
     lA.o = sub(lA.o, offset);
     lB.o = sub(lB.o, offset);
     bool isValid = r.valid != 0;
@@ -235,13 +254,18 @@ __device__ void epa_query(const DevWorld& w, DevPairs& P, const EpaRec* queue, i
     if (lane == 0) {
         atomicAdd(&w.ctr[C_EPA], 1);
         if (ovf) atomicOr(&w.ctr[C_STATUS], ST_EPA_POOL);
-        Mf m;
-        load_mf(P, p, m);
-        if (isValid)
-            add_contact(m, mb0, col0, x0, x1, w.friction[col0], w.friction[col1], w.restitution[col0], w.restitution[col1],
-                        normalInB, add(pointOnB, offset), distance, w.cbt);
-        manifold_refresh(m, w, mb0, mb1);
-        store_mf(P, p, m);
+        if (cand) {
+            res[2 * r.pair] = f4(add(pointOnB, offset), distance);
+            res[2 * r.pair + 1] = f4(normalInB, isValid ? 1.0f : 0.0f);
+        } else {
+            Mf m;
+            load_mf(P, p, m);
+            if (isValid)
+                add_contact(m, mb0, col0, x0, x1, w.friction[col0], w.friction[col1], w.restitution[col0],
+                            w.restitution[col1], normalInB, add(pointOnB, offset), distance, w.cbt);
+            manifold_refresh(m, w, mb0, mb1);
+            store_mf(P, p, m);
+        }
     }
     __syncwarp();
 }
@@ -287,7 +311,7 @@ template <int WARPS, int FACES, int MKV, int SEEN, int STACK>
 __global__ void __launch_bounds__(32 * WARPS) k_narrow_epa_tier(DevWorld w, DevPairs P, const EpaRec* queue,
                                                                 const int* list, const int* count, int* ovfQueue,
                                                                 int* ovfCount, const int* mode, const int* queueCount,
-                                                                int tier2Warps) {
+                                                                int tier2Warps, const int2* cand, float4* res) {
     extern __shared__ float4 epaSmem[];
     const bool skipped = *mode != 0 || *queueCount <= tier2Warps;   // tier 1 is skipped this step
     if (!list && skipped) return;           // this is tier 1
@@ -309,7 +333,7 @@ __global__ void __launch_bounds__(32 * WARPS) k_narrow_epa_tier(DevWorld w, DevP
     sl.seenCap = SEEN;
     sl.stackCap = STACK;
     const int gw = blockIdx.x * WARPS + warp, nw = gridDim.x * WARPS;
-    for (int j = gw; j < n; j += nw) epa_query(w, P, queue, list ? list[j] : j, sl, lane, ovfQueue, ovfCount);
+    for (int j = gw; j < n; j += nw) epa_query(w, P, queue, list ? list[j] : j, sl, lane, ovfQueue, ovfCount, cand, res);
 }
 #define EPA_T1_KERNEL k_narrow_epa_tier<EPA_T1_WARPS, 128, 64, 48, 256>
 #define EPA_T2_KERNEL k_narrow_epa_tier<EPA_T2_WARPS, 192, 96, 64, 384>
@@ -318,7 +342,8 @@ __global__ void __launch_bounds__(32 * WARPS) k_narrow_epa_tier(DevWorld w, DevP
 // Full-capacity tier over the queries the 192-face tier could not finish.
 // c: the tier counters (c[0] counts list); block 0 also sets the tier mode of the next step.
 __global__ void __launch_bounds__(32) k_narrow_epa_smem(DevWorld w, DevPairs P, const EpaRec* queue, const int* list,
-                                                       int* c, const int* queueCount, int tier2Warps) {
+                                                       int* c, const int* queueCount, int tier2Warps,
+                                                       const int2* cand, float4* res) {
     extern __shared__ float4 epaSmem[];
     int n = c[0];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -339,10 +364,28 @@ __global__ void __launch_bounds__(32) k_narrow_epa_smem(DevWorld w, DevPairs P, 
     sl.mkvCap = EPA_MKV_CAP;
     sl.seenCap = EPA_SEEN_CAP;
     sl.stackCap = EPA_STACK_CAP;
-    for (int j = blockIdx.x; j < n; j += gridDim.x) epa_query(w, P, queue, list[j], sl, threadIdx.x);
+    for (int j = blockIdx.x; j < n; j += gridDim.x) epa_query(w, P, queue, list[j], sl, threadIdx.x, nullptr, nullptr, cand, res);
 }
 
 static int gridn_nb(int nPairs) { return (nPairs + NB_THREADS - 1) / NB_THREADS; }
+
+// The three EPA tiers over a queue (queueCount on the device); ovfCount: 3 ints (the two
+// overflow lists' counts and the tier mode the last tier sets for the next step).
+static void epa_tiers(const DevWorld& w, DevPairs& P, void* queue, int* queueCount, int* ovfQueue, int* ovfQueue2,
+                      int* ovfCount, int slots, const int2* cand, float4* res, cudaStream_t s) {
+    cudaMemsetAsync(ovfCount, 0, sizeof(int) * 2, s);
+    EPA_T1_KERNEL<<<slots, 32 * EPA_T1_WARPS, EPA_T1_SMEM_BYTES, s>>>(
+        w, P, (const EpaRec*)queue, nullptr, queueCount, ovfQueue2, ovfCount + 1, ovfCount + 2, queueCount,
+        slots * EPA_T2_WARPS, cand, res);
+    note_launch();
+    EPA_T2_KERNEL<<<slots, 32 * EPA_T2_WARPS, EPA_T2_SMEM_BYTES, s>>>(
+        w, P, (const EpaRec*)queue, ovfQueue2, ovfCount + 1, ovfQueue, ovfCount, ovfCount + 2, queueCount,
+        slots * EPA_T2_WARPS, cand, res);
+    note_launch();
+    k_narrow_epa_smem<<<slots, 32, EPA_SMEM_BYTES, s>>>(w, P, (const EpaRec*)queue, ovfQueue, ovfCount, queueCount,
+                                                        slots * EPA_T2_WARPS, cand, res);
+    note_launch();
+}
 
 // Groups the pairs by bucket into nb.perm (blockOff: scanned per-block bucket counts).
 static void narrow_group(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
@@ -368,21 +411,226 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
         }
     }
     if (prof) { prof->mark(PH_NARROW, 1, s); prof->mark(PH_EPA, 0, s); }
-    if (nPairs > 0) {
-        cudaMemsetAsync(nb.ovfCount, 0, sizeof(int) * 2, s);
-        EPA_T1_KERNEL<<<nb.slots, 32 * EPA_T1_WARPS, EPA_T1_SMEM_BYTES, s>>>(
-            w, P, (const EpaRec*)nb.queue, nullptr, nb.queueCount, nb.ovfQueue2, nb.ovfCount + 1, nb.ovfCount + 2,
-            nb.queueCount, nb.slots * EPA_T2_WARPS);
-        note_launch();
-        EPA_T2_KERNEL<<<nb.slots, 32 * EPA_T2_WARPS, EPA_T2_SMEM_BYTES, s>>>(
-            w, P, (const EpaRec*)nb.queue, nb.ovfQueue2, nb.ovfCount + 1, nb.ovfQueue, nb.ovfCount, nb.ovfCount + 2,
-            nb.queueCount, nb.slots * EPA_T2_WARPS);
-        note_launch();
-        k_narrow_epa_smem<<<nb.slots, 32, EPA_SMEM_BYTES, s>>>(w, P, (const EpaRec*)nb.queue, nb.ovfQueue, nb.ovfCount,
-                                                                nb.queueCount, nb.slots * EPA_T2_WARPS);
-        note_launch();
-    }
+    if (nPairs > 0) epa_tiers(w, P, nb.queue, nb.queueCount, nb.ovfQueue, nb.ovfQueue2, nb.ovfCount, nb.slots, nullptr, nullptr, s);
     if (prof) prof->mark(PH_EPA, 1, s);
+}
+
+// ---- concave pass: convex objects against triangle meshes ---------------------------------
+// ConvexConcaveCollisionAlgorithm.processCollision (collision/dispatch/ConvexConcaveCollision
+// Algorithm.java:65-97) for every pair whose algorithm is convex-concave: the convex object's
+// aabb in the mesh's space widened by the mesh margin (ConvexTriangleCallback.
+// setTimeStepAndCounters, java:82-104) is quantized and the mesh's quantized tree walked
+// (OptimizedBvh.walkStacklessQuantizedTree, java:940-997); each triangle found is collided by
+// ConvexConvexAlgorithm as a TriangleShape with the mesh margin (ConvexTriangleCallback.
+// processTriangle, java:109-166) into the pair's one manifold, then the manifold is refreshed.
+// On the GPU the triangles of all pairs become (pair, triangle) candidates - counted, scanned,
+// listed in walk order - whose GJK (and EPA) runs one thread (one warp) each; the points are then
+// added to each pair's manifold in walk order by one thread per pair, which is what makes the
+// result the reference's: a manifold's point replacement depends on the order points arrive.
+
+// OptimizedBvh.quantizeWithClamp (java:1038-1056)
+JBD void mesh_quantize(V p, V bmin, V bmax, V q, int out[3]) {
+    V c = mk(jmax(p.x, bmin.x), jmax(p.y, bmin.y), jmax(p.z, bmin.z));
+    c = mk(jmin(c.x, bmax.x), jmin(c.y, bmax.y), jmin(c.z, bmax.z));
+    V v = mulc(sub(c, bmin), q);
+    out[0] = (int)__fadd_rn(v.x, 0.5f) & 0xFFFF;
+    out[1] = (int)__fadd_rn(v.y, 0.5f) & 0xFFFF;
+    out[2] = (int)__fadd_rn(v.z, 0.5f) & 0xFFFF;
+}
+
+// The convex object and the mesh of a convex-concave pair; false for any other pair or when
+// neither body is active (needsCollision).
+JBD bool concave_pair(const DevWorld& w, const DevPairs& P, int p, int& col0, int& col1, Xf& x0, Xf& x1, Leaf& c,
+                      Leaf& t) {
+    const uint64_t key = P.keys[p];
+    const int a = key_owner(key), b = key_partner(key);
+    col0 = min(a, b);
+    col1 = max(a, b);
+    if (!is_active_state(w.act[col0]) && !is_active_state(w.act[col1])) return false;
+    int t0, t1;
+    const int k = pair_leaf_types(w, key, col0, col1, t0, t1);
+    if (k != ALG_CONVEX_CONCAVE && k != ALG_CONCAVE_CONVEX) return false;
+    x0 = load_xf(w, col0);
+    x1 = load_xf(w, col1);
+    Leaf f, g;
+    pair_leaves(w, key, col0, col1, x0, x1, f, g);
+    c = k == ALG_CONVEX_CONCAVE ? f : g;
+    t = k == ALG_CONVEX_CONCAVE ? g : f;
+    return true;
+}
+
+// Walks the mesh tree with the pair's query box; counts the triangles found, and lists them
+// (pair, triangle) from out when out is given.
+JBD int mesh_walk(const DevWorld& w, const Leaf& c, const Leaf& t, int p, int2* out) {
+    const DevShapes& sh = w.sh;
+    const Xf convexInTri = xf_mul(xf_inverse(t.x), c.x);
+    V mn, mx;
+    shape_aabb(sh, c.shape, convexInTri, mn, mx);
+    const float mt = sh.margin[t.shape];
+    mx = add(mx, mk(mt, mt, mt));
+    mn = sub(mn, mk(mt, mt, mt));
+    const float4* q = sh.mesh_q + 3 * t.shape;
+    const V bmin = mk4(q[0]), bmax = mk4(q[1]), quant = mk4(q[2]);
+    int qa[3], qb[3];
+    mesh_quantize(mn, bmin, bmax, quant, qa);
+    mesh_quantize(mx, bmin, bmax, quant, qb);
+    const int4* nodes = sh.mesh_nodes + sh.mesh_node_off[t.shape];
+    const int nn = sh.mesh_node_cnt[t.shape];
+    int found = 0;
+    for (int cur = 0; cur < nn;) {
+        const int4 nd = nodes[cur];
+        const int n0 = nd.x & 0xFFFF, n1 = (nd.x >> 16) & 0xFFFF, n2 = nd.y & 0xFFFF;
+        const int m0 = (nd.y >> 16) & 0xFFFF, m1 = nd.z & 0xFFFF, m2 = (nd.z >> 16) & 0xFFFF;
+        const bool ov = !(qa[0] > m0 || qb[0] < n0) && !(qa[2] > m2 || qb[2] < n2) && !(qa[1] > m1 || qb[1] < n1);
+        const bool leaf = nd.w >= 0;
+        if (leaf && ov) {
+            if (out) out[found] = make_int2(p, nd.w & ((1 << 21) - 1));
+            ++found;
+        }
+        cur += (ov || leaf) ? 1 : max(1, -nd.w);
+    }
+    return found;
+}
+
+// Per pair: the ConvexTriangleCallback's manifold on first contact, and the candidate count.
+__global__ void k_mesh_count(DevWorld w, DevPairs P, int nPairs, const int* cntp, int* cnt) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nPairs) return;
+    int col0, col1;
+    Xf x0, x1;
+    Leaf c, t;
+    if (p >= (cntp ? min(nPairs, *cntp) : nPairs) || !concave_pair(w, P, p, col0, col1, x0, x1, c, t)) {
+        cnt[p] = 0;
+        return;
+    }
+    if (!P.has[p]) { P.has[p] = 1; P.n[p] = 0; }
+    cnt[p] = mesh_walk(w, c, t, p, nullptr);
+}
+
+__global__ void k_mesh_fill(DevWorld w, DevPairs P, int nPairs, const int* cntp, const int* off, int2* cand) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (cntp ? min(nPairs, *cntp) : nPairs)) return;
+    int col0, col1;
+    Xf x0, x1;
+    Leaf c, t;
+    if (!concave_pair(w, P, p, col0, col1, x0, x1, c, t)) return;
+    mesh_walk(w, c, t, p, cand + off[p]);
+}
+
+// Per candidate: GjkPairDetector between the convex object and the triangle (ConvexConvex
+// Algorithm.processCollision java:90-139 with the callback's manifold); penetrating candidates
+// go to the EPA queue.  res: 2 float4 per candidate (pointOnB + offset, distance; normal, valid).
+__global__ void __launch_bounds__(128, 4) k_mesh_gjk(DevWorld w, DevPairs P, const int2* cand, int n, float4* res,
+                                                     EpaRec* queue, int* queueCount) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 ct = cand[i];
+    int col0, col1;
+    Xf x0, x1;
+    Leaf c, t;
+    concave_pair(w, P, ct.x, col0, col1, x0, x1, c, t);
+    const ShapeRef sa = shape_ref(w.sh, c.shape), sb = triangle_ref(w.sh, t.shape, ct.y);
+    float md = __fadd_rn(__fadd_rn(sa.margin, sb.margin), w.cbt);
+    md = __fmul_rn(md, md);
+    atomicAdd(&w.ctr[C_GJK], 1);
+    const GjkPart g = gjk_part(sa, c.x, sb, t.x, md);
+    if (g.needEpa) {
+        EpaRec r;
+        r.pair = i;
+        r.valid = g.isValid ? 1 : 0;
+        r.distance = g.distance;
+        r.pad = 0.0f;
+        r.pA = f4(g.pointOnA, 0.0f);
+        r.pB = f4(g.pointOnB, 0.0f);
+        r.nB = f4(g.normalInB, 0.0f);
+        queue[atomicAdd(queueCount, 1)] = r;
+        return;
+    }
+    res[2 * i] = f4(add(g.pointOnB, g.offset), g.distance);
+    res[2 * i + 1] = f4(g.normalInB, g.isValid ? 1.0f : 0.0f);
+}
+
+// Per pair: the candidates' points into the manifold in walk order (ManifoldResult.
+// addContactPoint), then ManifoldResult.refreshContactPoints.
+__global__ void k_mesh_merge(DevWorld w, DevPairs P, int nPairs, const int* cntp, const int* cnt, const int* off,
+                             const float4* res) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (cntp ? min(nPairs, *cntp) : nPairs)) return;
+    int col0, col1;
+    Xf x0, x1;
+    Leaf c, t;
+    if (!concave_pair(w, P, p, col0, col1, x0, x1, c, t)) return;
+    const int mb0 = P.b0[p], mb1 = P.b1[p];
+    Mf m;
+    load_mf(P, p, m);
+    const float fr0 = w.friction[col0], fr1 = w.friction[col1], re0 = w.restitution[col0], re1 = w.restitution[col1];
+    for (int k = off[p], e = off[p] + cnt[p]; k < e; k++) {
+        const float4 a = res[2 * k], b = res[2 * k + 1];
+        if (b.w != 0.0f) add_contact(m, mb0, col0, x0, x1, fr0, fr1, re0, re1, mk4(b), mk4(a), a.w, w.cbt);
+    }
+    manifold_refresh(m, w, mb0, mb1);
+    store_mf(P, p, m);
+}
+
+void concave_free(NarrowBuffers& nb) {
+    cudaFree(nb.meshCnt); cudaFree(nb.meshOff); cudaFree(nb.meshTotal); cudaFree(nb.meshScan);
+    cudaFree(nb.cand); cudaFree(nb.candRes); cudaFree(nb.candQueue); cudaFree(nb.candOvf); cudaFree(nb.candOvf2);
+    cudaFree(nb.candCount);
+    nb.meshCnt = nb.meshOff = nb.meshTotal = nullptr;
+    nb.meshScan = nullptr;
+    nb.cand = nullptr;
+    nb.candRes = nullptr;
+    nb.candQueue = nullptr;
+    nb.candOvf = nb.candOvf2 = nb.candCount = nullptr;
+    nb.capMeshPairs = nb.capCand = 0;
+}
+
+int concave_launch(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, NarrowBuffers& nb, int* hostTotal,
+                   cudaStream_t s) {
+    if (nPairs <= 0) return 0;
+    if (nPairs > nb.capMeshPairs) {
+        cudaFree(nb.meshCnt); cudaFree(nb.meshOff); cudaFree(nb.meshScan);
+        nb.meshCnt = nb.meshOff = nullptr;
+        nb.meshScan = nullptr;
+        const int c = std::max(nPairs, 2 * nb.capMeshPairs);
+        if (cudaMalloc(&nb.meshCnt, sizeof(int) * c) != cudaSuccess || cudaMalloc(&nb.meshOff, sizeof(int) * c) != cudaSuccess ||
+            cudaMalloc(&nb.meshScan, scan_scratch_bytes(c)) != cudaSuccess)
+            return 1;
+        nb.capMeshPairs = c;
+    }
+    if (!nb.meshTotal && cudaMalloc(&nb.meshTotal, sizeof(int)) != cudaSuccess) return 1;
+    if (!nb.candCount && cudaMalloc(&nb.candCount, sizeof(int) * 4) != cudaSuccess) return 1;
+    const int blocks = (nPairs + 127) / 128;
+    k_mesh_count<<<blocks, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshCnt); note_launch();
+    exclusive_scan(nb.meshCnt, nb.meshOff, nb.meshTotal, nPairs, nb.meshScan, s);
+    if (cudaMemcpyAsync(hostTotal, nb.meshTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return 1;
+    const int total = *hostTotal;
+    if (total > nb.capCand) {
+        cudaFree(nb.cand); cudaFree(nb.candRes); cudaFree(nb.candQueue); cudaFree(nb.candOvf); cudaFree(nb.candOvf2);
+        nb.cand = nullptr;
+        nb.candRes = nullptr;
+        nb.candQueue = nullptr;
+        nb.candOvf = nb.candOvf2 = nullptr;
+        const int c = std::max(total, 2 * nb.capCand);
+        if (cudaMalloc(&nb.cand, sizeof(int2) * c) != cudaSuccess || cudaMalloc(&nb.candRes, sizeof(float4) * 2 * c) != cudaSuccess ||
+            cudaMalloc(&nb.candQueue, sizeof(EpaRec) * c) != cudaSuccess || cudaMalloc(&nb.candOvf, sizeof(int) * c) != cudaSuccess ||
+            cudaMalloc(&nb.candOvf2, sizeof(int) * c) != cudaSuccess)
+            return 1;
+        nb.capCand = c;
+    }
+    if (total > 0) {
+        k_mesh_fill<<<blocks, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshOff, nb.cand); note_launch();
+        cudaMemsetAsync(nb.candCount, 0, sizeof(int), s);
+        k_mesh_gjk<<<(total + 127) / 128, 128, 0, s>>>(w, P, nb.cand, total, nb.candRes, (EpaRec*)nb.candQueue,
+                                                        nb.candCount);
+        note_launch();
+        epa_tiers(w, P, nb.candQueue, nb.candCount, nb.candOvf, nb.candOvf2, nb.candCount + 1, nb.slots, nb.cand,
+                  nb.candRes, s);
+    }
+    k_mesh_merge<<<blocks, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshCnt, nb.meshOff, nb.candRes); note_launch();
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
 size_t epa_queue_record_bytes() { return sizeof(EpaRec); }

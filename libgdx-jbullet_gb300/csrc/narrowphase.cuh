@@ -19,6 +19,22 @@ struct NarrowBuffers {
     int* blockOff = nullptr;      // per block and bucket counts, scanned in place (NB_BUCKETS x pair blocks)
     bool group = true;            // group pairs by algorithm (worth it with two or more shape kinds)
     void* scanScratch = nullptr;  // scan scratch for blockOff
+    // concave pass (worlds with triangle meshes): per pair its candidate triangle count and
+    // offset, the (pair, triangle) candidates, their GJK/EPA results (2 float4 each) and the
+    // candidates' own EPA queue with its overflow lists and counters (queue count, two overflow
+    // counts, tier mode)
+    int* meshCnt = nullptr;
+    int* meshOff = nullptr;
+    int* meshTotal = nullptr;
+    void* meshScan = nullptr;
+    int capMeshPairs = 0;
+    int2* cand = nullptr;
+    float4* candRes = nullptr;
+    void* candQueue = nullptr;
+    int* candOvf = nullptr;
+    int* candOvf2 = nullptr;
+    int* candCount = nullptr;
+    int capCand = 0;
 };
 
 size_t epa_queue_record_bytes();
@@ -26,6 +42,13 @@ int narrowphase_configure();      // once per world: the EPA kernel's shared-mem
 // cntp (nullable): the pair count on the device; nPairs is then an upper bound (graph replays).
 void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
                         const Prof* prof = nullptr, const int* cntp = nullptr);
+
+// The concave pass (after narrowphase_launch, in a world with triangle meshes): reads the
+// candidate count back to the host (hostTotal: pinned) and grows its buffers, so it runs
+// outside graph capture.  Returns nonzero when a CUDA call failed.
+int concave_launch(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, NarrowBuffers& nb, int* hostTotal,
+                   cudaStream_t s);
+void concave_free(NarrowBuffers& nb);
 
 // Narrowphase whose EPA pass uses scratch compiled into the library (no allocation).
 constexpr int STATIC_EPA_SLOTS = JBGPU_STATIC_EPA_SLOTS_MAX;   // EPA warps that can run at once on it

@@ -20,6 +20,7 @@
 #include "gridsync.cuh"
 #include "prims.cuh"
 #include "query.cuh"
+#include "dispatch.cuh"
 #include <climits>
 #include "shapes.cuh"
 
@@ -176,6 +177,10 @@ JBD void ray_object(const DevWorld& w, int b, V from, V to, ObjHits& h) {
     h.n = 0;
     const int shape = w.shape[b];
     const Xf t = load_xf(w, b);
+    if (w.sh.type[shape] == SHAPE_COMPOUND || w.sh.type[shape] == SHAPE_MESH) {   // not handled: reported
+        atomicOr(&w.ctr[C_STATUS], ST_QUERY_SHAPE);
+        return;
+    }
     if (w.sh.type[shape] != SHAPE_PLANE) {
         float f;
         V n;
@@ -788,6 +793,10 @@ __global__ void __launch_bounds__(RAY_THREADS) k_sweep_cast(DevWorld w, const Ra
         atomicOr(planeHit + c.ray, 1);
         return;
     }
+    if (w.sh.type[bs] == SHAPE_COMPOUND || w.sh.type[bs] == SHAPE_MESH) {   // not handled: reported
+        atomicOr(&w.ctr[C_STATUS], ST_QUERY_SHAPE);
+        return;
+    }
     const Xf fa = xf12(from + 12 * c.ray);
     const V ta = mk(to[12 * c.ray + 9], to[12 * c.ray + 10], to[12 * c.ray + 11]);
     float f;
@@ -968,16 +977,24 @@ JBD Xf ld_pred(const float4* pred, int i) {
 // 231-265), whose swap of its arguments is broken (233-237): the pair is found only when `me`
 // precedes j (key (me << 32) | j: j is the partner whether it is a body or a plane); found with a
 // manifold that holds contact points, j is skipped (DiscreteDynamicsWorld.java:1180-1195).
-JBD bool ccd_touching(const DevPairs& P, int np, int me, int j) {
+// A pair with a compound body has a manifold per child combination (key_sub); the algorithm's
+// getAllContactManifolds lists them all, and any with points counts.
+JBD bool ccd_touching(const DevWorld& w, const DevPairs& P, int np, int me, int j) {
     if (me > j) return false;
-    const uint64_t key = ((uint64_t)(unsigned)me << 32) | (unsigned)j;
-    int lo = 0, hi = np - 1;
-    while (lo <= hi) {
-        const int mid = (lo + hi) >> 1;
-        const uint64_t k = P.keys[mid];
-        if (k == key) return P.has[mid] && P.n[mid] > 0;
-        if (k < key) lo = mid + 1;
-        else hi = mid - 1;
+    const int subs = w.hasCompound ? pair_subs(w.sh, w.shape[me], w.shape[j]) : 1;
+    for (int sub = 0; sub < subs; sub++) {
+        const uint64_t key = ((uint64_t)(unsigned)me << 32) | ((unsigned)sub << 24) | (unsigned)j;
+        int lo = 0, hi = np - 1;
+        while (lo <= hi) {
+            const int mid = (lo + hi) >> 1;
+            const uint64_t k = P.keys[mid];
+            if (k == key) {
+                if (P.has[mid] && P.n[mid] > 0) return true;
+                break;
+            }
+            if (k < key) lo = mid + 1;
+            else hi = mid - 1;
+        }
     }
     return false;
 }
@@ -1027,7 +1044,7 @@ __global__ void __launch_bounds__(256) k_ccd_sweep(DevWorld w, DevPairs P, int n
         for (int j = tid; j < w.nBodies; j += nth) {
             if (j == me || w.world[j] != wi) continue;
             if (((w.group[j] & mm) & 0xFFFF) == 0 || ((gm & w.mask[j]) & 0xFFFF) == 0) continue;
-            if (resp && (w.flags[j] & CF_NO_CONTACT_RESPONSE) == 0 && ccd_touching(P, np, me, j)) continue;
+            if (resp && (w.flags[j] & CF_NO_CONTACT_RESPONSE) == 0 && ccd_touching(w, P, np, me, j)) continue;
             const Xf tj = j < me ? ld_pred(pred, j) : load_xf(w, j);
             V bmn, bmx;
             shape_aabb(w.sh, w.shape[j], tj, bmn, bmx);
@@ -1036,6 +1053,10 @@ __global__ void __launch_bounds__(256) k_ccd_sweep(DevWorld w, DevPairs P, int n
                 continue;
             if (w.sh.type[w.shape[j]] == SHAPE_PLANE) {
                 atomicOr(&w.ctr[C_STATUS], ST_CCD_PLANE);
+                continue;
+            }
+            if (w.sh.type[w.shape[j]] == SHAPE_COMPOUND || w.sh.type[w.shape[j]] == SHAPE_MESH) {
+                atomicOr(&w.ctr[C_STATUS], ST_QUERY_SHAPE);   // not handled: reported
                 continue;
             }
             float f;

@@ -1,5 +1,6 @@
-// Shape queries on the device: aabb and support maps of the five shapes on the path
-// (collision/shapes/{BoxShape,SphereShape,CapsuleShape,ConvexHullShape,StaticPlaneShape}.java).
+// Shape queries on the device: aabb and support maps of the shapes on the path
+// (collision/shapes/{BoxShape,SphereShape,CapsuleShape,ConvexHullShape,StaticPlaneShape,
+// TriangleShape,CompoundShape,TriangleMeshShape}.java).
 // Local scaling is always (1,1,1) here, so the reference's multiplications by the scaling
 // vector are exact identities and are omitted.
 #pragma once
@@ -38,7 +39,9 @@ JBD void shape_aabb(const DevShapes& sh, int s, const Xf& t, V& mn, V& mx) {
         V e = mk(dot(ab.r[0], he), dot(ab.r[1], he), dot(ab.r[2], he));
         mn = sub(t.o, e);
         mx = add(t.o, e);
-    } else if (type == SHAPE_HULL) {          // PolyhedralConvexShape.getAabb -> transformAabb(min,max,...)
+    } else if (type == SHAPE_HULL || type == SHAPE_COMPOUND) {
+        // PolyhedralConvexShape.getAabb -> transformAabb(min,max,margin,t); CompoundShape.getAabb
+        // (CompoundShape.java:126-171) is the same arithmetic over its children's union
         V lmin = mk4(sh.laabb_min[s]), lmax = mk4(sh.laabb_max[s]);
         V lhe = scl(sub(lmax, lmin), 0.5f);
         lhe = mk(__fadd_rn(lhe.x, m), __fadd_rn(lhe.y, m), __fadd_rn(lhe.z, m));
@@ -46,6 +49,16 @@ JBD void shape_aabb(const DevShapes& sh, int s, const Xf& t, V& mn, V& mx) {
         M ab = absM(t.b);
         V c = xf_apply(t, lc);
         V e = mk(dot(ab.r[0], lhe), dot(ab.r[1], lhe), dot(ab.r[2], lhe));
+        mn = sub(c, e);
+        mx = add(c, e);
+    } else if (type == SHAPE_MESH) {          // TriangleMeshShape.getAabb: the margin widens the extent
+        V lmin = mk4(sh.laabb_min[s]), lmax = mk4(sh.laabb_max[s]);
+        V lhe = scl(sub(lmax, lmin), 0.5f);
+        V lc = scl(add(lmax, lmin), 0.5f);
+        M ab = absM(t.b);
+        V c = xf_apply(t, lc);
+        V e = mk(dot(ab.r[0], lhe), dot(ab.r[1], lhe), dot(ab.r[2], lhe));
+        e = mk(__fadd_rn(e.x, m), __fadd_rn(e.y, m), __fadd_rn(e.z, m));
         mn = sub(c, e);
         mx = add(c, e);
     } else {                                  // StaticPlaneShape.getAabb
@@ -71,6 +84,17 @@ struct ShapeRef {
     const float4* pts;
     int npts;
 };
+// A mesh triangle as the TriangleShape ConvexTriangleCallback collides (margin: the mesh's).
+JBD ShapeRef triangle_ref(const DevShapes& sh, int meshShape, int tri) {
+    ShapeRef r;
+    r.type = SHAPE_TRIANGLE;
+    r.margin = sh.margin[meshShape];
+    r.dims = mk(0.0f, 0.0f, 0.0f);
+    r.up = 1;
+    r.pts = sh.mesh_tris + (size_t)3 * (sh.mesh_tri_off[meshShape] + tri);
+    r.npts = 3;
+    return r;
+}
 JBD ShapeRef shape_ref(const DevShapes& sh, int s) {
     ShapeRef r;
     r.type = sh.type[s];
@@ -103,6 +127,16 @@ JBD V support_without_margin(const ShapeRef& s, V vec) {
             V vtx = sub(add(pos, t1), t2);
             float nd = dot(v, vtx);
             if (nd > maxDot) { maxDot = nd; sup = vtx; }
+        }
+        return sup;
+    }
+    if (s.type == SHAPE_TRIANGLE) {           // TriangleShape.localGetSupportingVertexWithoutMargin with
+        float mv = -1e30f;                    // VectorUtil.maxAxis (no normalisation; vertex 0 where
+        V sup = mk4(s.pts[0]);                // the reference would index -1)
+        for (int i = 0; i < 3; i++) {
+            V vtx = mk4(s.pts[i]);
+            float nd = dot(vec, vtx);
+            if (nd > mv) { mv = nd; sup = vtx; }
         }
         return sup;
     }

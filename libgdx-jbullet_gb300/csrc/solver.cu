@@ -74,9 +74,9 @@ __global__ void k_uf_union(DevWorld w, DevPairs P, int nPairs, const int* cntp, 
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= (cntp ? min(nPairs, *cntp) : nPairs)) return;
     uint64_t key = P.keys[p];
-    int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+    int a = key_owner(key), b = key_partner(key);
     int rank = 0;               // pairs of the same owner before p, up to 4
-    while (rank < UF_ROUNDS && p - rank - 1 >= 0 && (int)(P.keys[p - rank - 1] >> 32) == a) rank++;
+    while (rank < UF_ROUNDS && p - rank - 1 >= 0 && key_owner(P.keys[p - rank - 1]) == a) rank++;
     if ((rank < 2 ? 0 : rank - 1) != round) return;
     if (!merges_islands(w.flags[a]) || !merges_islands(w.flags[b])) return;
     if (round > 0 && __ldcg(&parent[a]) == __ldcg(&parent[b])) return;

@@ -18,6 +18,7 @@
 #include "jbgpu_internal.cuh"
 #include "mlp.cuh"
 #include "narrowphase.cuh"
+#include "meshes.cuh"
 #include "prims.cuh"
 #include "query.cuh"
 #include "solver.cuh"
@@ -49,6 +50,9 @@ struct HostShape {
     float lmin[4], lmax[4];
     float plane[4];
     int hull_off, hull_cnt;
+    int child_off, child_cnt;          // compound: its children in jbgpu_world::childShapes / childXf
+    int node_off, node_cnt, tri_off;   // triangle mesh: its tree nodes and triangles
+    float q[12];                       // triangle mesh: bvhAabbMin, bvhAabbMax, bvhQuantization (xyz_)
 };
 
 template <class T> static cudaError_t dalloc(T** p, size_t n) {
@@ -86,6 +90,11 @@ struct jbgpu_world {
     // shapes
     std::vector<HostShape> shapes;
     std::vector<float4> hullPts;
+    std::vector<HostShape> childShapes;   // compound children, appended after the shapes on the device
+    std::vector<float4> childXf;          // 3 per child: basis rows, origin in .w
+    std::vector<int4> meshNodes;          // quantized tree nodes of every triangle mesh
+    std::vector<float4> meshTris;         // 3 vertices per triangle
+    bool hasMesh = false, hasCompound = false;
     bool shapesDirty = true;
     int capShapes = 0, capHull = 0;
     // bodies
@@ -270,16 +279,22 @@ int ensure_pair_capacity(jbgpu_world* w, int buf, int need) {
     return JBGPU_OK;
 }
 
+// The shape table on the device: the world's shapes by id, then every compound's children
+// (a compound's child table entries point at them), and the pools of hull points, tree nodes
+// and triangles.  Re-uploaded whole when shapes were added.
 int sync_shapes(jbgpu_world* w) {
     if (!w->shapesDirty) return JBGPU_OK;
-    int ns = (int)w->shapes.size();
+    const int nu = (int)w->shapes.size(), nc = (int)w->childShapes.size(), ns = nu + nc;
     DevShapes& S = w->dw.sh;
     if (ns > w->capShapes) {
         dfree(S.type); dfree(S.margin); dfree(S.dims); dfree(S.laabb_min); dfree(S.laabb_max); dfree(S.plane);
-        dfree(S.hull_off); dfree(S.hull_cnt);
+        dfree(S.hull_off); dfree(S.hull_cnt); dfree(S.child_off); dfree(S.child_cnt); dfree(S.mesh_node_off);
+        dfree(S.mesh_node_cnt); dfree(S.mesh_tri_off); dfree(S.mesh_q);
         int c = std::max(ns, 2 * w->capShapes);
         CK(dalloc(&S.type, c)); CK(dalloc(&S.margin, c)); CK(dalloc(&S.dims, c)); CK(dalloc(&S.laabb_min, c));
         CK(dalloc(&S.laabb_max, c)); CK(dalloc(&S.plane, c)); CK(dalloc(&S.hull_off, c)); CK(dalloc(&S.hull_cnt, c));
+        CK(dalloc(&S.child_off, c)); CK(dalloc(&S.child_cnt, c)); CK(dalloc(&S.mesh_node_off, c));
+        CK(dalloc(&S.mesh_node_cnt, c)); CK(dalloc(&S.mesh_tri_off, c)); CK(dalloc(&S.mesh_q, 3 * (size_t)c));
         w->capShapes = c;
     }
     int nh = (int)w->hullPts.size();
@@ -289,17 +304,23 @@ int sync_shapes(jbgpu_world* w) {
         CK(dalloc(&S.hull_pts, c));
         w->capHull = c;
     }
-    std::vector<int> type(ns), off(ns), cnt(ns);
+    dfree(S.child_shape); dfree(S.child_xf); dfree(S.mesh_nodes); dfree(S.mesh_tris);
+    CK(dalloc(&S.child_shape, nc)); CK(dalloc(&S.child_xf, 3 * (size_t)nc));
+    CK(dalloc(&S.mesh_nodes, w->meshNodes.size())); CK(dalloc(&S.mesh_tris, w->meshTris.size()));
+    std::vector<int> type(ns), off(ns), cnt(ns), coff(ns), ccnt(ns), noff(ns), ncnt(ns), toff(ns), cshape(nc);
     std::vector<float> margin(ns);
-    std::vector<float4> dims(ns), lmin(ns), lmax(ns), plane(ns);
+    std::vector<float4> dims(ns), lmin(ns), lmax(ns), plane(ns), q(3 * (size_t)ns);
     for (int i = 0; i < ns; i++) {
-        const HostShape& h = w->shapes[i];
+        const HostShape& h = i < nu ? w->shapes[i] : w->childShapes[i - nu];
         type[i] = h.type; off[i] = h.hull_off; cnt[i] = h.hull_cnt; margin[i] = h.margin;
+        coff[i] = h.child_off; ccnt[i] = h.child_cnt; noff[i] = h.node_off; ncnt[i] = h.node_cnt; toff[i] = h.tri_off;
         dims[i] = make_float4(h.dims[0], h.dims[1], h.dims[2], h.dims[3]);
         lmin[i] = make_float4(h.lmin[0], h.lmin[1], h.lmin[2], 0);
         lmax[i] = make_float4(h.lmax[0], h.lmax[1], h.lmax[2], 0);
         plane[i] = make_float4(h.plane[0], h.plane[1], h.plane[2], h.plane[3]);
+        for (int k = 0; k < 3; k++) q[3 * i + k] = make_float4(h.q[4 * k], h.q[4 * k + 1], h.q[4 * k + 2], 0.0f);
     }
+    for (int c = 0; c < nc; c++) cshape[c] = nu + c;   // child c is shape nu + c
     cudaStream_t s = w->stream;
     if (ns) {
         CK(cudaMemcpyAsync(S.type, type.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
@@ -310,9 +331,24 @@ int sync_shapes(jbgpu_world* w) {
         CK(cudaMemcpyAsync(S.laabb_min, lmin.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(S.laabb_max, lmax.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, s));
         CK(cudaMemcpyAsync(S.plane, plane.data(), sizeof(float4) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.child_off, coff.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.child_cnt, ccnt.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.mesh_node_off, noff.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.mesh_node_cnt, ncnt.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.mesh_tri_off, toff.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.mesh_q, q.data(), sizeof(float4) * 3 * ns, cudaMemcpyHostToDevice, s));
     }
+    if (nc) {
+        CK(cudaMemcpyAsync(S.child_shape, cshape.data(), sizeof(int) * nc, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(S.child_xf, w->childXf.data(), sizeof(float4) * 3 * nc, cudaMemcpyHostToDevice, s));
+    }
+    if (!w->meshNodes.empty())
+        CK(cudaMemcpyAsync(S.mesh_nodes, w->meshNodes.data(), sizeof(int4) * w->meshNodes.size(), cudaMemcpyHostToDevice, s));
+    if (!w->meshTris.empty())
+        CK(cudaMemcpyAsync(S.mesh_tris, w->meshTris.data(), sizeof(float4) * w->meshTris.size(), cudaMemcpyHostToDevice, s));
     if (nh) CK(cudaMemcpyAsync(S.hull_pts, w->hullPts.data(), sizeof(float4) * nh, cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
+    w->dw.hasCompound = w->hasCompound ? 1 : 0;
     w->shapesDirty = false;
     return JBGPU_OK;
 }
@@ -379,6 +415,9 @@ int check_status(jbgpu_world* w) {
     if (st & ST_CCD_PLANE)
         return fail(JBGPU_ERR_UNSUPPORTED, "a CCD sweep reached a static plane, where the reference throws "
                                            "(CollisionWorld.objectQuerySingle's concave branch)");
+    if (st & ST_QUERY_SHAPE)
+        return fail(JBGPU_ERR_UNSUPPORTED, "a ray, sweep or CCD sweep reached a compound or triangle-mesh body, "
+                                           "which these queries do not handle");
     return JBGPU_OK;
 }
 
@@ -453,6 +492,8 @@ int run_stage(jbgpu_world* w, int stage, float dt) {
     case JBGPU_STAGE_NARROWPHASE:
         CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
         narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s, &P);
+        if (w->hasMesh && concave_launch(d, w->pairs[w->cur], w->nPairs, nullptr, w->nb, w->hostPinned + 8, s))
+            return fail(JBGPU_ERR_CUDA, "concave narrowphase pass failed");
         break;
     case JBGPU_STAGE_ISLANDS:
         P.mark(PH_ISLANDS, 0, s);
@@ -594,6 +635,8 @@ int narrow_and_islands(jbgpu_world* w, const int* cntp = nullptr) {
     CK(cudaEventRecord(w->evJoin, a));
     CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
     narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s, &w->prof, cntp);
+    if (w->hasMesh && concave_launch(d, w->pairs[w->cur], w->nPairs, cntp, w->nb, w->hostPinned + 8, s))
+        return fail(JBGPU_ERR_CUDA, "concave narrowphase pass failed");
     CK(cudaStreamWaitEvent(s, w->evJoin, 0));
     w->prof.mark(PH_ISLANDS, 0, s);
     islands_launch_select(d, w->pairs[w->cur], w->nPairs, w->sb, s, cntp);
@@ -745,8 +788,11 @@ int single_step_graph(jbgpu_world* w, float dt) {
     return JBGPU_OK;
 }
 
+// Worlds with triangle meshes step with launches: their concave pass reads its candidate count
+// back in the middle of the narrowphase.
 bool graph_usable(const jbgpu_world* w) {
-    return w->graphOn && w->graphError.empty() && !w->prof.active() && !w->mlp && !w->logSamples && w->nBodies > 0;
+    return w->graphOn && w->graphError.empty() && !w->prof.active() && !w->mlp && !w->logSamples && w->nBodies > 0 &&
+           !w->hasMesh;
 }
 }  // namespace
 
@@ -834,6 +880,123 @@ void jbgpu_config_default(jbgpu_config* c) {
     c->step_graphs = 1;
 }
 
+namespace {
+// java.lang.Math.min / max on floats
+float jmin_h(float a, float b) {
+    if (a != a) return a;
+    if (a == 0.0f && b == 0.0f) return std::signbit(b) ? b : a;
+    return a <= b ? a : b;
+}
+float jmax_h(float a, float b) {
+    if (a != a) return a;
+    if (a == 0.0f && b == 0.0f) return std::signbit(a) ? b : a;
+    return a >= b ? a : b;
+}
+float dot3_h(const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+// A convex shape record from its descriptor (BoxShape, SphereShape, CapsuleShape,
+// ConvexHullShape constructors; hull points appended to pts).
+int convex_record(std::vector<float4>& pts, const jbgpu_shape_desc& d, HostShape& h) {
+    std::memset(&h, 0, sizeof(h));
+    h.type = d.type;
+    h.margin = 0.04f;
+    switch (d.type) {
+    case JBGPU_SHAPE_BOX:       // BoxShape: implicit dims = halfExtents * scaling - margin
+        for (int k = 0; k < 3; k++) { volatile float v = d.params[k] * 1.0f; h.dims[k] = v - 0.04f; }
+        return JBGPU_OK;
+    case JBGPU_SHAPE_SPHERE:    // SphereShape: radius in dims.x, margin == radius
+        h.dims[0] = d.params[0];
+        h.margin = d.params[0];
+        return JBGPU_OK;
+    case JBGPU_SHAPE_CAPSULE:   // CapsuleShape(radius, height), up axis y
+        h.dims[0] = d.params[0]; h.dims[1] = 0.5f * d.params[1]; h.dims[2] = d.params[0]; h.dims[3] = 1.0f;
+        return JBGPU_OK;
+    case JBGPU_SHAPE_CONVEX_HULL: {
+        if (!d.points || d.num_points <= 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "hull without points");
+        h.hull_off = (int)pts.size();
+        h.hull_cnt = d.num_points;
+        for (int k = 0; k < d.num_points; k++)
+            pts.push_back(make_float4(d.points[3 * k], d.points[3 * k + 1], d.points[3 * k + 2], 0.0f));
+        for (int a = 0; a < 3; a++) {   // PolyhedralConvexShape.recalcLocalAabb: strict > argmax
+            float bp = -1e30f, bm = -1e30f, vp = 0.0f, vm = 0.0f;
+            for (int k = 0; k < d.num_points; k++) {
+                float x = d.points[3 * k + a];
+                if (x > bp) { bp = x; vp = x; }
+                if (-x > bm) { bm = -x; vm = x; }
+            }
+            h.lmax[a] = vp + 0.04f;
+            h.lmin[a] = vm - 0.04f;
+        }
+        return JBGPU_OK;
+    }
+    }
+    return fail(JBGPU_ERR_UNSUPPORTED, "a compound child must be a box, sphere, capsule or convex hull");
+}
+
+// getAabb of a convex record at a transform t (12 floats: basis rows, origin), the device's
+// shape_aabb on the host: BoxShape via AabbUtil2.transformAabb, SphereShape, CapsuleShape,
+// PolyhedralConvexShape.
+void convex_record_aabb(const HostShape& h, const float* t, float mn[3], float mx[3]) {
+    float ab[9], c[3], he[3];
+    for (int i = 0; i < 9; i++) ab[i] = std::fabs(t[i]);
+    const float m = h.margin;
+    for (int k = 0; k < 3; k++) c[k] = t[9 + k];
+    if (h.type == JBGPU_SHAPE_SPHERE) {
+        for (int k = 0; k < 3; k++) { mn[k] = c[k] - m; mx[k] = c[k] + m; }
+        return;
+    }
+    if (h.type == JBGPU_SHAPE_BOX) {
+        for (int k = 0; k < 3; k++) he[k] = h.dims[k] + m;
+    } else if (h.type == JBGPU_SHAPE_CAPSULE) {
+        const float r = h.dims[0];
+        he[0] = r; he[1] = r + h.dims[1]; he[2] = r;
+        for (int k = 0; k < 3; k++) he[k] = he[k] + m;
+    } else {   // hull: transformAabb(localMin, localMax, margin, t)
+        float lc[3];
+        for (int k = 0; k < 3; k++) {
+            he[k] = (h.lmax[k] - h.lmin[k]) * 0.5f;
+            he[k] = he[k] + m;
+            lc[k] = (h.lmax[k] + h.lmin[k]) * 0.5f;
+        }
+        for (int k = 0; k < 3; k++) c[k] = dot3_h(lc, t + 3 * k) + t[9 + k];
+    }
+    for (int k = 0; k < 3; k++) {
+        const float e = dot3_h(ab + 3 * k, he);
+        mn[k] = c[k] - e;
+        mx[k] = c[k] + e;
+    }
+}
+
+// CompoundShape local aabb: the union of its children's aabbs at their transforms
+// (CompoundShape.addChildShape, CompoundShape.java:59-91).
+void compound_local_aabb(const std::vector<HostShape>& ch, const float* xf, int n, float lmin[3], float lmax[3]) {
+    for (int k = 0; k < 3; k++) { lmin[k] = 1e30f; lmax[k] = -1e30f; }
+    for (int i = 0; i < n; i++) {
+        float mn[3], mx[3];
+        convex_record_aabb(ch[i], xf + 12 * i, mn, mx);
+        for (int k = 0; k < 3; k++) { lmin[k] = jmin_h(lmin[k], mn[k]); lmax[k] = jmax_h(lmax[k], mx[k]); }
+    }
+}
+}  // namespace
+
+int jbgpu_shape_mesh_bvh(const jbgpu_shape_desc* d, int32_t* nodes, int32_t capacity, int32_t* n, float aabb[6]) {
+    if (!d || !n || d->type != JBGPU_SHAPE_TRIANGLE_MESH || capacity < 0 || (capacity > 0 && !nodes))
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "a TRIANGLE_MESH descriptor, a count pointer and a node buffer");
+    MeshBvh m;
+    if (build_mesh_bvh(d->points, d->num_points, d->indices, d->num_triangles, m))
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "a triangle mesh needs vertices, 1 .. 2^21-1 triangles and indices "
+                                                "within the vertex array");
+    *n = (int)m.nodes.size();
+    if (aabb)
+        for (int k = 0; k < 3; k++) { aabb[k] = m.lmin[k]; aabb[3 + k] = m.lmax[k]; }
+    if (*n > capacity) return fail(JBGPU_ERR_CAPACITY, "node buffer too small");
+    for (int i = 0; i < *n; i++) {
+        nodes[4 * i] = m.nodes[i].x; nodes[4 * i + 1] = m.nodes[i].y;
+        nodes[4 * i + 2] = m.nodes[i].z; nodes[4 * i + 3] = m.nodes[i].w;
+    }
+    return JBGPU_OK;
+}
+
 int jbgpu_shape_local_inertia(const jbgpu_shape_desc* d, float mass, float out[3]) {
     if (!d || !out) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null argument");
     const float margin = 0.04f;
@@ -888,8 +1051,34 @@ int jbgpu_shape_local_inertia(const jbgpu_shape_desc* d, float mass, float out[3
         return JBGPU_OK;
     }
     case JBGPU_SHAPE_STATIC_PLANE:
+    case JBGPU_SHAPE_TRIANGLE_MESH:   // TriangleMeshShape.calculateLocalInertia: zero (static meshes)
         out[0] = out[1] = out[2] = 0.0f;
         return JBGPU_OK;
+    case JBGPU_SHAPE_COMPOUND: {      // CompoundShape.calculateLocalInertia: the box of getAabb(identity)
+        if (!d->children || !d->child_transforms || d->num_children <= 0 || d->num_children > JBGPU_COMPOUND_MAX_CHILDREN)
+            return fail(JBGPU_ERR_INVALID_ARGUMENT, "a compound needs 1 .. JBGPU_COMPOUND_MAX_CHILDREN children");
+        std::vector<float4> pts;   // the children's hull points (unused here)
+        std::vector<HostShape> ch(d->num_children);
+        for (int c = 0; c < d->num_children; c++) {
+            int rc = convex_record(pts, d->children[c], ch[c]);
+            if (rc) return rc;
+        }
+        float lmin[3], lmax[3], he[3];
+        compound_local_aabb(ch, d->child_transforms, d->num_children, lmin, lmax);
+        for (int k = 0; k < 3; k++) {
+            float lhe = (lmax[k] - lmin[k]) * 0.5f;
+            lhe = lhe + d->params[0];
+            const float lc = (lmax[k] + lmin[k]) * 0.5f;
+            const float c = lc * 1.0f + 0.0f;   // the identity transform's centre (libGDX mul: x*1 + y*0 + z*0)
+            const float amin = c - lhe, amax = c + lhe;
+            he[k] = (amax - amin) * 0.5f;
+        }
+        const float lx = 2.0f * he[0], ly = 2.0f * he[1], lz = 2.0f * he[2];
+        out[0] = mass / 12.0f * (ly * ly + lz * lz);
+        out[1] = mass / 12.0f * (lx * lx + lz * lz);
+        out[2] = mass / 12.0f * (lx * lx + ly * ly);
+        return JBGPU_OK;
+    }
     }
     return fail(JBGPU_ERR_INVALID_ARGUMENT, "unknown shape type");
 }
@@ -988,6 +1177,9 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     DevShapes& S = d.sh;
     dfree(S.type); dfree(S.margin); dfree(S.dims); dfree(S.laabb_min); dfree(S.laabb_max); dfree(S.plane);
     dfree(S.hull_off); dfree(S.hull_cnt); dfree(S.hull_pts);
+    dfree(S.child_off); dfree(S.child_cnt); dfree(S.child_shape); dfree(S.child_xf); dfree(S.mesh_node_off);
+    dfree(S.mesh_node_cnt); dfree(S.mesh_tri_off); dfree(S.mesh_q); dfree(S.mesh_nodes); dfree(S.mesh_tris);
+    concave_free(w->nb);
     free_pairs(w->pairs[0]);
     free_pairs(w->pairs[1]);
     DevRows& R = w->rows;
@@ -1047,35 +1239,13 @@ int jbgpu_world_add_shapes(jbgpu_world* w, const jbgpu_shape_desc* shapes, int32
         std::memset(&h, 0, sizeof(h));
         h.type = d.type;
         h.margin = 0.04f;
-        h.hull_off = 0;
-        h.hull_cnt = 0;
         switch (d.type) {
-        case JBGPU_SHAPE_BOX:       // BoxShape: implicit dims = halfExtents * scaling - margin
-            for (int k = 0; k < 3; k++) { volatile float v = d.params[k] * 1.0f; h.dims[k] = v - 0.04f; }
-            break;
-        case JBGPU_SHAPE_SPHERE:    // SphereShape: radius in dims.x, margin == radius
-            h.dims[0] = d.params[0];
-            h.margin = d.params[0];
-            break;
-        case JBGPU_SHAPE_CAPSULE:   // CapsuleShape(radius, height), up axis y
-            h.dims[0] = d.params[0]; h.dims[1] = 0.5f * d.params[1]; h.dims[2] = d.params[0]; h.dims[3] = 1.0f;
-            break;
+        case JBGPU_SHAPE_BOX:
+        case JBGPU_SHAPE_SPHERE:
+        case JBGPU_SHAPE_CAPSULE:
         case JBGPU_SHAPE_CONVEX_HULL: {
-            if (!d.points || d.num_points <= 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "hull without points");
-            h.hull_off = (int)w->hullPts.size();
-            h.hull_cnt = d.num_points;
-            for (int k = 0; k < d.num_points; k++)
-                w->hullPts.push_back(make_float4(d.points[3 * k], d.points[3 * k + 1], d.points[3 * k + 2], 0.0f));
-            for (int a = 0; a < 3; a++) {   // PolyhedralConvexShape.recalcLocalAabb: strict > argmax
-                float bp = -1e30f, bm = -1e30f, vp = 0.0f, vm = 0.0f;
-                for (int k = 0; k < d.num_points; k++) {
-                    float x = d.points[3 * k + a];
-                    if (x > bp) { bp = x; vp = x; }
-                    if (-x > bm) { bm = -x; vm = x; }
-                }
-                h.lmax[a] = vp + 0.04f;
-                h.lmin[a] = vm - 0.04f;
-            }
+            int rc = convex_record(w->hullPts, d, h);
+            if (rc) return rc;
             break;
         }
         case JBGPU_SHAPE_STATIC_PLANE: {   // normal.nor() (libGDX: skipped when len2 is 0 or 1)
@@ -1086,6 +1256,46 @@ int jbgpu_world_add_shapes(jbgpu_world* w, const jbgpu_shape_desc* shapes, int32
                 x = x * s; y = y * s; z = z * s;
             }
             h.plane[0] = x; h.plane[1] = y; h.plane[2] = z; h.plane[3] = d.params[3];
+            break;
+        }
+        case JBGPU_SHAPE_TRIANGLE_MESH: {   // BvhTriangleMeshShape(TriangleIndexVertexArray, true), setMargin
+            MeshBvh m;
+            if (build_mesh_bvh(d.points, d.num_points, d.indices, d.num_triangles, m))
+                return fail(JBGPU_ERR_INVALID_ARGUMENT, "a triangle mesh needs vertices, 1 .. 2^21-1 triangles and "
+                                                        "indices within the vertex array");
+            h.margin = d.params[0];
+            h.node_off = (int)w->meshNodes.size();
+            h.node_cnt = (int)m.nodes.size();
+            h.tri_off = (int)(w->meshTris.size() / 3);
+            w->meshNodes.insert(w->meshNodes.end(), m.nodes.begin(), m.nodes.end());
+            w->meshTris.insert(w->meshTris.end(), m.tris.begin(), m.tris.end());
+            for (int k = 0; k < 3; k++) {
+                h.lmin[k] = m.lmin[k]; h.lmax[k] = m.lmax[k];
+                h.q[k] = m.bmin[k]; h.q[4 + k] = m.bmax[k]; h.q[8 + k] = m.quant[k];
+            }
+            w->hasMesh = true;
+            break;
+        }
+        case JBGPU_SHAPE_COMPOUND: {
+            if (!d.children || !d.child_transforms || d.num_children <= 0 || d.num_children > JBGPU_COMPOUND_MAX_CHILDREN)
+                return fail(JBGPU_ERR_INVALID_ARGUMENT, "a compound needs 1 .. JBGPU_COMPOUND_MAX_CHILDREN children");
+            std::vector<HostShape> ch(d.num_children);
+            for (int c = 0; c < d.num_children; c++) {
+                int rc = convex_record(w->hullPts, d.children[c], ch[c]);
+                if (rc) return rc;
+            }
+            compound_local_aabb(ch, d.child_transforms, d.num_children, h.lmin, h.lmax);
+            h.margin = d.params[0];
+            h.child_off = (int)w->childShapes.size();
+            h.child_cnt = d.num_children;
+            for (int c = 0; c < d.num_children; c++) {
+                const float* t = d.child_transforms + 12 * c;
+                w->childShapes.push_back(ch[c]);
+                w->childXf.push_back(make_float4(t[0], t[1], t[2], t[9]));
+                w->childXf.push_back(make_float4(t[3], t[4], t[5], t[10]));
+                w->childXf.push_back(make_float4(t[6], t[7], t[8], t[11]));
+            }
+            w->hasCompound = true;
             break;
         }
         default:
@@ -1109,11 +1319,15 @@ int jbgpu_world_num_bodies(const jbgpu_world* w, int32_t* n) {
 int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, int32_t* uids) {
     if (!w || (!b && n > 0) || n < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
     if (n == 0) return JBGPU_OK;
+    if ((long long)w->nBodies + n > MAX_BODIES_KEYED) return fail(JBGPU_ERR_CAPACITY, "pair keys hold body indices below 2^24");
     CK(cudaSetDevice(w->device));
     for (int i = 0; i < n; i++) {
         if (b[i].shape < 0 || b[i].shape >= (int)w->shapes.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad shape id");
         if (w->shapes[b[i].shape].type == JBGPU_SHAPE_STATIC_PLANE && b[i].mass != 0.0f)
             return fail(JBGPU_ERR_INVALID_ARGUMENT, "a static plane must have mass 0");
+        if (w->shapes[b[i].shape].type == JBGPU_SHAPE_TRIANGLE_MESH && b[i].mass != 0.0f)
+            return fail(JBGPU_ERR_INVALID_ARGUMENT, "a triangle mesh body must have mass 0 (moving concave objects are "
+                                                    "not supported, TriangleMeshShape.calculateLocalInertia)");
         if (b[i].world < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "negative world index");
     }
     int rc = grow_bodies(w, w->nBodies + n);
@@ -1240,6 +1454,8 @@ int jbgpu_world_narrowphase_static(jbgpu_world* w, int32_t epa_slots) {
         return fail(JBGPU_ERR_CAPACITY, "epa_slots exceeds the static EPA scratch (JBGPU_STATIC_EPA_SLOTS_MAX = 32)");
     if (w->shapesDirty || w->planesDirty)
         return fail(JBGPU_ERR_INVALID_ARGUMENT, "shapes or bodies added since the last step or stage: run one first");
+    if (w->hasMesh)
+        return fail(JBGPU_ERR_UNSUPPORTED, "the static-scratch narrowphase does not run the triangle-mesh pass");
     if (w->device >= MAX_STATIC_DEVICES) return fail(JBGPU_ERR_UNSUPPORTED, "device ordinal beyond the static scratch table");
     CK(cudaSetDevice(w->device));
     void* base = nullptr;
@@ -1671,7 +1887,7 @@ int jbgpu_world_convex_sweep_test(jbgpu_world* w, int32_t shape, const float* fr
                                   const int32_t* sweepWorld, int32_t n, int32_t group, int32_t mask, int32_t deviceBuffers,
                                   jbgpu_ray_hit* hits) {
     if (!w || n < 0 || (n > 0 && (!from || !to || !hits))) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad sweep arguments");
-    if (shape < 0 || shape >= (int)w->shapes.size() || w->shapes[shape].type == JBGPU_SHAPE_STATIC_PLANE)
+    if (shape < 0 || shape >= (int)w->shapes.size() || !shape_is_convex(w->shapes[shape].type))
         return fail(JBGPU_ERR_INVALID_ARGUMENT, "the cast shape must be a convex shape of the world");
     if (n == 0) return JBGPU_OK;
     if (!deviceBuffers && sweepWorld)
@@ -1933,12 +2149,14 @@ int jbgpu_world_set_manifolds(jbgpu_world* w, const jbgpu_manifolds* m) {
     for (int k = 0; k < 8; k++) f[k].assign((size_t)np * 4, make_float4(0, 0, 0, 0));
     for (int i = 0; i < np; i++) {
         uint64_t key = m->keys[i];
-        int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+        int a = key_owner(key), b = key_partner(key);
         if (a < 0 || b < 0 || a >= w->nBodies || b >= w->nBodies || a == b) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad pair key");
         if (i > 0 && m->keys[i - 1] >= key) return fail(JBGPU_ERR_INVALID_ARGUMENT, "keys not strictly ascending");
-        bool bPlane = (w->hFlags[b] & CF_PLANE) != 0;
-        b0[i] = bPlane ? a : std::min(a, b);
-        b1[i] = bPlane ? b : std::max(a, b);
+        const HostShape& sl = w->shapes[w->hShape[std::min(a, b)]];
+        const HostShape& sh = w->shapes[w->hShape[std::max(a, b)]];
+        if (key_sub(key) >= std::max(1, sl.child_cnt) * std::max(1, sh.child_cnt))
+            return fail(JBGPU_ERR_INVALID_ARGUMENT, "pair key names a child combination the bodies do not have");
+        manifold_bodies(a, b, sl.type, sh.type, b0[i], b1[i]);
         has[i] = (m->flags[i] & 1) ? 1 : 0;
         cnt[i] = has[i] ? m->num_points[i] : 0;
         if (cnt[i] < 0 || cnt[i] > 4) return fail(JBGPU_ERR_INVALID_ARGUMENT, "num_points out of range");

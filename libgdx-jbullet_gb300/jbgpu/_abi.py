@@ -21,7 +21,10 @@ SHAPE_BOX = 0
 SHAPE_CONVEX_HULL = 4
 SHAPE_SPHERE = 6
 SHAPE_CAPSULE = 8
+SHAPE_TRIANGLE_MESH = 16
 SHAPE_STATIC_PLANE = 23
+SHAPE_COMPOUND = 25
+COMPOUND_MAX_CHILDREN = 16
 
 ACTIVE_TAG = 1
 ISLAND_SLEEPING = 2
@@ -104,12 +107,20 @@ def default_config(**overrides):
 
 
 class ShapeDesc(C.Structure):
-    _fields_ = [
-        ("type", C.c_int32),
-        ("params", C.c_float * 4),
-        ("points", f32p),
-        ("num_points", C.c_int32),
-    ]
+    pass
+
+
+ShapeDesc._fields_ = [
+    ("type", C.c_int32),
+    ("params", C.c_float * 4),
+    ("points", f32p),
+    ("num_points", C.c_int32),
+    ("indices", C.POINTER(C.c_int32)),
+    ("num_triangles", C.c_int32),
+    ("children", C.POINTER(ShapeDesc)),
+    ("child_transforms", f32p),
+    ("num_children", C.c_int32),
+]
 
 
 class BodyDesc(C.Structure):

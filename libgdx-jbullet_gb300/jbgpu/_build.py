@@ -15,7 +15,8 @@ ROOT = os.path.dirname(PKG_DIR)                       # libgdx-jbullet_gb300/
 CSRC = os.path.join(ROOT, "csrc")
 BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(BUILD, "libjbgpu.so")
-SOURCES = ["prims.cu", "bodies.cu", "broadphase.cu", "narrowphase.cu", "solver.cu", "mlp.cu", "query.cu", "world.cu"]
+SOURCES = ["prims.cu", "bodies.cu", "broadphase.cu", "narrowphase.cu", "solver.cu", "mlp.cu", "query.cu", "meshes.cu",
+           "world.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

@@ -35,6 +35,7 @@ def lib():
             "jbgpu_last_error": ([], C.c_char_p),
             "jbgpu_config_default": ([P(_abi.Config)], None),
             "jbgpu_shape_local_inertia": ([P(_abi.ShapeDesc), C.c_float, _abi.f32p], C.c_int),
+            "jbgpu_shape_mesh_bvh": ([P(_abi.ShapeDesc), _abi.i32p, C.c_int32, _abi.i32p, _abi.f32p], C.c_int),
             "jbgpu_world_create": ([P(_abi.Config), P(C.c_void_p)], C.c_int),
             "jbgpu_world_destroy": ([C.c_void_p], C.c_int),
             "jbgpu_world_add_shape": ([C.c_void_p, P(_abi.ShapeDesc), _abi.i32p], C.c_int),
@@ -126,7 +127,7 @@ EXPORTED = [
     "jbgpu_world_set_6dof_limit", "jbgpu_world_set_6dof_linear_motor", "jbgpu_world_set_6dof_angular_motor",
     "jbgpu_world_add_cone_twist", "jbgpu_world_set_cone_twist_limit", "jbgpu_world_set_cone_twist_angular_only",
     "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
-    "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd",
+    "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd", "jbgpu_shape_mesh_bvh",
 ]
 
 
@@ -567,3 +568,19 @@ def shape_local_inertia(shape_dict, mass):
     out = np.zeros(3, np.float32)
     check(lib().jbgpu_shape_local_inertia(C.byref(d[0]), mass, out.ctypes.data_as(_abi.f32p)))
     return out
+
+
+def mesh_bvh(mesh_dict):
+    """The quantized tree the library builds for a triangle-mesh shape dict: (nodes (n, 4) int32 in
+    walk order, local aabb (6,) float32) - see jbgpu_shape_mesh_bvh."""
+    from .scenes import shape_desc_array
+    d = shape_desc_array([mesh_dict])
+    n = C.c_int32()
+    aabb = np.zeros(6, np.float32)
+    rc = lib().jbgpu_shape_mesh_bvh(C.byref(d[0]), None, 0, C.byref(n), aabb.ctypes.data_as(_abi.f32p))
+    if rc not in (_abi.OK, _abi.ERR_CAPACITY):
+        check(rc)
+    nodes = np.zeros((max(n.value, 1), 4), np.int32)
+    check(lib().jbgpu_shape_mesh_bvh(C.byref(d[0]), nodes.ctypes.data_as(_abi.i32p), len(nodes), C.byref(n),
+                                     aabb.ctypes.data_as(_abi.f32p)))
+    return nodes[:n.value], aabb

@@ -34,7 +34,9 @@ class Scene:
     dt: float
     steps: int
     config: dict
-    shapes: list                      # dicts: type, params (4 floats), points (n,3) float32 or None
+    shapes: list                      # dicts: type, params (4 floats), points (n,3) float32 or None;
+                                      # meshes add indices (m,3) int32, compounds children: a list of
+                                      # (shape dict, transform 12 floats)
     bodies: np.ndarray                # BODY_DTYPE records, insertion order (uid = index + 1)
     world_of_body: np.ndarray = None  # batched scenes: world index per body
     meta: dict = field(default_factory=dict)
@@ -45,25 +47,48 @@ class Scene:
 
     def shape_descs(self):
         """ctypes array of ShapeDesc (keeps point buffers alive on the returned object)."""
-        arr = (_abi.ShapeDesc * len(self.shapes))()
-        keep = []
-        for i, s in enumerate(self.shapes):
-            arr[i].type = s["type"]
-            arr[i].params[:] = tuple(float(x) for x in s["params"])
-            if s.get("points") is not None:
-                p = np.ascontiguousarray(s["points"], dtype=np.float32)
-                keep.append(p)
-                arr[i].points = p.ctypes.data_as(_abi.f32p)
-                arr[i].num_points = len(p)
-            else:
-                arr[i].points = None
-                arr[i].num_points = 0
-        arr._keep = keep
-        return arr
+        return shape_desc_array(self.shapes)
 
     def body_descs_ptr(self):
         b = np.ascontiguousarray(self.bodies)
         return b, b.ctypes.data_as(_abi.C.POINTER(_abi.BodyDesc))
+
+
+def _fill_desc(d, s, keep):
+    d.type = s["type"]
+    d.params[:] = tuple(float(x) for x in s["params"])
+    d.points, d.num_points, d.indices, d.num_triangles = None, 0, None, 0
+    d.children, d.child_transforms, d.num_children = None, None, 0
+    if s.get("points") is not None:
+        p = np.ascontiguousarray(s["points"], dtype=np.float32).reshape(-1, 3)
+        keep.append(p)
+        d.points = p.ctypes.data_as(_abi.f32p)
+        d.num_points = len(p)
+    if s.get("indices") is not None:
+        ix = np.ascontiguousarray(s["indices"], dtype=np.int32).reshape(-1, 3)
+        keep.append(ix)
+        d.indices = ix.ctypes.data_as(_abi.C.POINTER(_abi.C.c_int32))
+        d.num_triangles = len(ix)
+    if s.get("children"):
+        ch = (_abi.ShapeDesc * len(s["children"]))()
+        xf = np.ascontiguousarray([np.asarray(t, np.float32).reshape(12) for _, t in s["children"]], np.float32)
+        for k, (c, _) in enumerate(s["children"]):
+            _fill_desc(ch[k], c, keep)
+        keep.extend([ch, xf])
+        d.children = _abi.C.cast(ch, _abi.C.POINTER(_abi.ShapeDesc))
+        d.child_transforms = xf.ctypes.data_as(_abi.f32p)
+        d.num_children = len(s["children"])
+
+
+def shape_desc_array(shapes):
+    """ctypes array of ShapeDesc for a list of shape dicts (the buffers it points into are kept
+    alive on the array)."""
+    arr = (_abi.ShapeDesc * len(shapes))()
+    keep = []
+    for i, s in enumerate(shapes):
+        _fill_desc(arr[i], s, keep)
+    arr._keep = keep
+    return arr
 
 
 # ---- binary32 mass properties (reference operation order) --------------------------------
@@ -810,6 +835,241 @@ def ccd_shots(shots=24, seed=0, steps=90, plane=False, threshold=0.05, swept_rad
                                              "radius": swept_radius}, "walls_x": (6.0, 12.0)})
 
 
+# ---- compound and concave shapes ----------------------------------------------------------
+def _f(x):
+    return F(x)
+
+
+def _row_dot(b, r, v):
+    """dot(row r of the 3x3 `b`, v) in binary32, x*x' + y*y' + z*z' in that order."""
+    return F(F(F(b[r, 0] * v[0]) + F(b[r, 1] * v[1])) + F(b[r, 2] * v[2]))
+
+
+def _xf_apply(b, o, v):
+    """Transform.transform: v.mul(basis) (rows dotted with v) plus the origin, binary32."""
+    return np.array([F(_row_dot(b, r, v) + o[r]) for r in range(3)], F)
+
+
+def convex_aabb(shape, xf12):
+    """CollisionShape.getAabb of a box, sphere, capsule or hull at a transform, binary32 in the
+    reference's operation order (BoxShape.java:146-151 via AabbUtil2.transformAabb,
+    SphereShape.java:56-65, CapsuleShape.java:160-190, PolyhedralConvexShape.java:163-171)."""
+    t = np.asarray(xf12, F)
+    b, o = t[:9].reshape(3, 3), t[9:12]
+    ab = np.abs(b)
+    m = F(0.04)
+    k = shape["type"]
+    if k == _abi.SHAPE_SPHERE:
+        r = F(shape["params"][0])
+        e = np.array([r, r, r], F)
+        return o - e, o + e
+    if k == _abi.SHAPE_BOX:
+        he = np.array(shape["params"][:3], F)
+        dims = he * F(1) - m
+        hem = dims + m
+        c = o
+    elif k == _abi.SHAPE_CAPSULE:
+        r, hh = F(shape["params"][0]), F(F(0.5) * F(shape["params"][1]))
+        hem = np.array([r, F(r + hh), r], F) + m
+        c = o
+    elif k == _abi.SHAPE_CONVEX_HULL:
+        mn, mx = hull_local_aabb(shape["points"], m)
+        hem = (mx - mn) * F(0.5) + m
+        c = _xf_apply(b, o, (mx + mn) * F(0.5))
+    else:
+        raise ValueError("not a convex shape on this path")
+    e = np.array([_row_dot(ab, r, hem) for r in range(3)], F)
+    return c - e, c + e
+
+
+def compound_local_aabb(children):
+    """CompoundShape.addChildShape's running union (CompoundShape.java:59-91)."""
+    mn = np.full(3, 1e30, F)
+    mx = np.full(3, -1e30, F)
+    for shape, xf in children:
+        a, b = convex_aabb(shape, xf)
+        mn, mx = np.minimum(mn, a), np.maximum(mx, b)
+    return mn, mx
+
+
+def compound_inertia(mass, children, margin=0.0):
+    """CompoundShape.calculateLocalInertia: the box inertia of getAabb(identity)
+    (CompoundShape.java:222-243 and 126-171)."""
+    mn, mx = compound_local_aabb(children)
+    lhe = (mx - mn) * F(0.5) + F(margin)
+    lc = (mx + mn) * F(0.5)
+    amin, amax = lc - lhe, lc + lhe
+    he = (amax - amin) * F(0.5)
+    lx, ly, lz = F(2) * he[0], F(2) * he[1], F(2) * he[2]
+    m12 = F(F(mass) / F(12))
+    return np.array([m12 * (ly * ly + lz * lz), m12 * (lx * lx + lz * lz), m12 * (lx * lx + ly * ly)], F)
+
+
+def xf12(basis=None, origin=(0.0, 0.0, 0.0)):
+    b = np.eye(3, dtype=F) if basis is None else np.asarray(basis, F).reshape(3, 3)
+    return np.concatenate([b.reshape(9), np.asarray(origin, F)]).astype(F)
+
+
+def rot_x(a):
+    c, s = np.cos(a), np.sin(a)
+    return np.array([[1, 0, 0], [0, c, -s], [0, s, c]], F)
+
+
+def rot_z(a):
+    c, s = np.cos(a), np.sin(a)
+    return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]], F)
+
+
+def terrain_mesh(nx=24, nz=24, size=24.0, amp=1.2, seed=0, margin=0.0):
+    """A heightfield of nx x nz cells over size x size m (two triangles per cell, alternating
+    diagonals, counter-clockwise seen from above) with smooth random bumps of about amp m on a
+    bowl: the shape dict of a BvhTriangleMeshShape."""
+    rng = np.random.Generator(np.random.PCG64(seed + 7))
+    xs = np.linspace(-size / 2, size / 2, nx + 1)
+    zs = np.linspace(-size / 2, size / 2, nz + 1)
+    X, Z = np.meshgrid(xs, zs, indexing="ij")
+    H = np.zeros_like(X)
+    for _ in range(6):
+        kx, kz, ph = rng.uniform(0.1, 0.5), rng.uniform(0.1, 0.5), rng.uniform(0, 2 * np.pi)
+        H += amp / 3 * np.sin(kx * X + ph) * np.cos(kz * Z - ph)
+    H += rng.uniform(-0.05, 0.05, H.shape)
+    H += 0.4 * (X * X + Z * Z) / size      # a bowl, so that what lands stays on the mesh
+    verts = np.stack([X, H, Z], -1).reshape(-1, 3).astype(F)
+    idx = []
+    for i in range(nx):
+        for j in range(nz):
+            a, b, c, d = i * (nz + 1) + j, (i + 1) * (nz + 1) + j, (i + 1) * (nz + 1) + j + 1, i * (nz + 1) + j + 1
+            if (i + j) % 2 == 0:
+                idx += [(a, d, c), (a, c, b)]
+            else:
+                idx += [(a, d, b), (d, c, b)]
+    return {"type": _abi.SHAPE_TRIANGLE_MESH, "params": (float(margin), 0.0, 0.0, 0.0), "points": verts,
+            "indices": np.asarray(idx, np.int32)}
+
+
+def _convex_kinds(rng, n, hull_pts=12):
+    """n random convex shape dicts (boxes, spheres, capsules, hulls) with their masses (density 1000)."""
+    out = []
+    for i in range(n):
+        k = i % 4
+        if k == 0:
+            h = rng.uniform(0.2, 0.5, 3).astype(F)
+            s = {"type": _abi.SHAPE_BOX, "params": (float(h[0]), float(h[1]), float(h[2]), 0.0), "points": None}
+            m = F(1000.0 * 8.0 * float(h[0]) * float(h[1]) * float(h[2]))
+            inertia = box_inertia(m, h)
+        elif k == 1:
+            r = F(rng.uniform(0.2, 0.5))
+            s = {"type": _abi.SHAPE_SPHERE, "params": (float(r), 0.0, 0.0, 0.0), "points": None}
+            m = F(1000.0 * 4.0 / 3.0 * np.pi * float(r) ** 3)
+            inertia = sphere_inertia(m, r)
+        elif k == 2:
+            r, height = F(0.2), F(rng.uniform(0.4, 1.2))
+            s = {"type": _abi.SHAPE_CAPSULE, "params": (float(r), float(height), 0.0, 0.0), "points": None}
+            m = F(1000.0 * (np.pi * 0.04 * float(height) + 4.0 / 3.0 * np.pi * 0.008))
+            inertia = capsule_inertia(m, r, height)
+        else:
+            ax = rng.uniform(0.25, 0.5, 3)
+            d = rng.standard_normal((hull_pts, 3))
+            d /= np.linalg.norm(d, axis=1, keepdims=True)
+            pts = (d * ax).astype(F)
+            s = {"type": _abi.SHAPE_CONVEX_HULL, "params": (0.0, 0.0, 0.0, 0.0), "points": pts}
+            m = F(1000.0 * 4.0 / 3.0 * np.pi * ax.prod())
+            inertia = hull_inertia(m, pts)
+        out.append((s, m, inertia))
+    return out
+
+
+def _compound_kinds(rng, n):
+    """n random compound shape dicts with masses: dumbbells (two spheres on a capsule), L shapes
+    (two boxes), tables (a top on four legs) and hull pairs, children at rotated transforms."""
+    out = []
+    for i in range(n):
+        k = i % 4
+        if k == 0:
+            r, L = F(rng.uniform(0.2, 0.35)), F(rng.uniform(0.5, 0.9))
+            ch = [({"type": _abi.SHAPE_SPHERE, "params": (float(r), 0.0, 0.0, 0.0), "points": None}, xf12(None, (-L, 0, 0))),
+                  ({"type": _abi.SHAPE_SPHERE, "params": (float(r), 0.0, 0.0, 0.0), "points": None}, xf12(None, (L, 0, 0))),
+                  ({"type": _abi.SHAPE_CAPSULE, "params": (0.1, float(2 * L), 0.0, 0.0), "points": None},
+                   xf12(rot_z(np.pi / 2), (0, 0, 0)))]
+            m = F(1000.0 * (2 * 4.0 / 3.0 * np.pi * float(r) ** 3))
+        elif k == 1:
+            a = rng.uniform(0.3, 0.6)
+            ch = [({"type": _abi.SHAPE_BOX, "params": (float(a), 0.15, 0.15, 0.0), "points": None}, xf12(None, (0, 0, 0))),
+                  ({"type": _abi.SHAPE_BOX, "params": (0.15, float(a), 0.15, 0.0), "points": None},
+                   xf12(rot_x(0.3), (float(a) - 0.15, float(a) - 0.15, 0)))]
+            m = F(1000.0 * 2 * 8 * a * 0.15 * 0.15)
+        elif k == 2:
+            w = rng.uniform(0.5, 0.8)
+            ch = [({"type": _abi.SHAPE_BOX, "params": (float(w), 0.06, float(w), 0.0), "points": None}, xf12(None, (0, 0.4, 0)))]
+            for sx in (-1, 1):
+                for sz in (-1, 1):
+                    ch.append(({"type": _abi.SHAPE_BOX, "params": (0.06, 0.2, 0.06, 0.0), "points": None},
+                               xf12(None, (sx * (w - 0.1), 0.14, sz * (w - 0.1)))))
+            m = F(1000.0 * 8 * w * 0.06 * w)
+        else:
+            chs = []
+            for sgn in (-1, 1):
+                d = rng.standard_normal((10, 3))
+                d /= np.linalg.norm(d, axis=1, keepdims=True)
+                pts = (d * rng.uniform(0.2, 0.4, 3)).astype(F)
+                chs.append(({"type": _abi.SHAPE_CONVEX_HULL, "params": (0.0, 0.0, 0.0, 0.0), "points": pts},
+                            xf12(rot_z(sgn * 0.4), (sgn * 0.3, 0, 0))))
+            ch = chs
+            m = F(1000.0 * 0.2)
+        s = {"type": _abi.SHAPE_COMPOUND, "params": (0.0, 0.0, 0.0, 0.0), "points": None, "children": ch}
+        out.append((s, m, compound_inertia(m, ch)))
+    return out
+
+
+def terrain(n=60, seed=0, cells=16, size=16.0, compounds=0, steps=200, region=(10.0, 6.0, 10.0), y0=4.0):
+    """Convex bodies (boxes, spheres, capsules, hulls; density 1000) and optionally compound bodies
+    dropped on a static triangle-mesh terrain (a BvhTriangleMeshShape heightfield of cells x cells
+    quads over size x size m); no plane; 10 iterations, dt 1/60."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [terrain_mesh(cells, cells, size, seed=seed)]
+    kinds = _convex_kinds(rng, n) + _compound_kinds(rng, compounds)
+    order = rng.permutation(len(kinds))
+    kinds = [kinds[i] for i in order]
+    nb = len(kinds)
+    b = _bodies(nb)
+    for i, (s, m, inertia) in enumerate(kinds):
+        shapes.append(s)
+        b["shape"][i] = i + 1
+        b["mass"][i] = m
+        b["local_inertia"][i] = inertia
+    pos = np.stack([rng.uniform(-region[0] / 2, region[0] / 2, nb), rng.uniform(y0, y0 + region[1], nb),
+                    rng.uniform(-region[2] / 2, region[2] / 2, nb)], 1)
+    _set_transforms(b, random_rotations(rng, nb), pos)
+    ground = _bodies(1)
+    ground["shape"] = 0
+    bodies = np.concatenate([ground, b])
+    return Scene("terrain_%d_c%d" % (n, compounds), 1.0 / 60.0, steps, {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10},
+                 shapes, bodies, meta={"seed": seed})
+
+
+def compounds(n=40, convex=20, seed=0, steps=200, region=(6.0, 10.0, 6.0), y0=1.0):
+    """Compound bodies (dumbbells, L shapes, tables, hull pairs; children at rotated transforms)
+    and convex bodies dropped on a static plane; 10 iterations, dt 1/60."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE)]
+    kinds = _compound_kinds(rng, n) + _convex_kinds(rng, convex)
+    order = rng.permutation(len(kinds))
+    kinds = [kinds[i] for i in order]
+    nb = len(kinds)
+    b = _bodies(nb)
+    for i, (s, m, inertia) in enumerate(kinds):
+        shapes.append(s)
+        b["shape"][i] = i + 1
+        b["mass"][i] = m
+        b["local_inertia"][i] = inertia
+    pos = np.stack([rng.uniform(-region[0] / 2, region[0] / 2, nb), rng.uniform(y0, y0 + region[1], nb),
+                    rng.uniform(-region[2] / 2, region[2] / 2, nb)], 1)
+    _set_transforms(b, random_rotations(rng, nb), pos)
+    bodies = np.concatenate([_plane_body(0), b])
+    return Scene("compounds_%d_%d" % (n, convex), 1.0 / 60.0, steps, {"gravity": (0.0, -9.81, 0.0), "num_iterations": 10},
+                 shapes, bodies, meta={"seed": seed})
+
+
 SCENES = {
     "boxes_1k": boxes_on_plane,
     "mixed_100k": mixed_100k,
@@ -825,4 +1085,6 @@ SCENES = {
     "cone_chains": cone_chains,
     "slider_rigs": slider_rigs,
     "ccd_shots": ccd_shots,
+    "terrain": terrain,
+    "compounds": compounds,
 }

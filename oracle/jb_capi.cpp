@@ -31,6 +31,17 @@ static Shape shape_from_desc(const jbgpu_shape_desc* d) {
     case JBGPU_SHAPE_SPHERE: return make_sphere(d->params[0]);
     case JBGPU_SHAPE_CAPSULE: return make_capsule(d->params[0], d->params[1]);
     case JBGPU_SHAPE_CONVEX_HULL: return make_hull(d->points, d->num_points);
+    case JBGPU_SHAPE_TRIANGLE_MESH:
+        return make_mesh(d->points, d->num_points, d->indices, d->num_triangles, d->params[0]);
+    case JBGPU_SHAPE_COMPOUND: {
+        std::vector<Shape> ch;
+        std::vector<Xf> xf;
+        for (int i = 0; i < d->num_children; i++) {
+            ch.push_back(shape_from_desc(&d->children[i]));
+            xf.push_back(xf_from12(d->child_transforms + 12 * i));
+        }
+        return make_compound(ch, xf, d->params[0]);
+    }
     default: return make_plane(v3(d->params[0], d->params[1], d->params[2]), d->params[3]);
     }
 }
@@ -61,6 +72,35 @@ int orc_add_shape(void* h, const jbgpu_shape_desc* d) {
     World* w = (World*)h;
     w->shapes.push_back(shape_from_desc(d));
     return (int)w->shapes.size() - 1;
+}
+
+// The quantized tree of a TRIANGLE_MESH descriptor in the library's node layout
+// (jbgpu_shape_mesh_bvh); returns the node count.
+int orc_mesh_bvh(const jbgpu_shape_desc* d, int* nodes, int cap, float* aabb) {
+    Shape s = shape_from_desc(d);
+    const QuantizedBvh& t = s.mesh->bvh;
+    for (int i = 0; i < t.curNodeIndex && i < cap; i++) {
+        const uint16_t* q = &t.q[6 * i];
+        nodes[4 * i] = (int)((unsigned)q[0] | ((unsigned)q[1] << 16));
+        nodes[4 * i + 1] = (int)((unsigned)q[2] | ((unsigned)q[3] << 16));
+        nodes[4 * i + 2] = (int)((unsigned)q[4] | ((unsigned)q[5] << 16));
+        nodes[4 * i + 3] = t.escOrTri[i];
+    }
+    if (aabb) {
+        aabb[0] = s.localAabbMin.x; aabb[1] = s.localAabbMin.y; aabb[2] = s.localAabbMin.z;
+        aabb[3] = s.localAabbMax.x; aabb[4] = s.localAabbMax.y; aabb[5] = s.localAabbMax.z;
+    }
+    return t.curNodeIndex;
+}
+
+// OptimizedBvh.reportAabbOverlappingNodex on a TRIANGLE_MESH descriptor: the triangles in report
+// order; returns their count.
+int orc_mesh_query(const jbgpu_shape_desc* d, const float* mn, const float* mx, int* out, int cap) {
+    Shape s = shape_from_desc(d);
+    std::vector<int> tris;
+    mesh_overlapping_triangles(*s.mesh, v3(mn[0], mn[1], mn[2]), v3(mx[0], mx[1], mx[2]), tris);
+    for (size_t i = 0; i < tris.size() && (int)i < cap; i++) out[i] = tris[i];
+    return (int)tris.size();
 }
 
 int orc_shape_local_inertia(const jbgpu_shape_desc* d, float mass, float* out) {
@@ -354,7 +394,8 @@ int orc_get_manifolds(void* h, jbgpu_manifolds* m) {
     return 0;
 }
 
-// Manifold body order is implied by the key: (convex, plane) for plane pairs, (lo, hi) otherwise.
+// Manifold body order is implied by the key (pair_manifold_bodies): convex before plane or mesh,
+// a compound's side first, (lo, hi) otherwise.
 int orc_set_manifolds(void* h, const jbgpu_manifolds* m) {
     World& w = *(World*)h;
     int n = m->n_pairs;
@@ -362,11 +403,11 @@ int orc_set_manifolds(void* h, const jbgpu_manifolds* m) {
     w.pairHasAlgo.assign(n, 0);
     w.pairMf.assign(n, Manifold());
     for (int i = 0; i < n; i++) {
-        int a = (int)(m->keys[i] >> 32), b = (int)(m->keys[i] & 0xffffffffu);
-        bool pb = w.shapes[w.bodies[b].shape].type == STATIC_PLANE;
         Manifold& mf = w.pairMf[i];
-        if (pb) { mf.body0 = a; mf.body1 = b; }
-        else { mf.body0 = a < b ? a : b; mf.body1 = a < b ? b : a; }
+        int mb0 = -1, mb1 = -1;
+        pair_manifold_bodies(w, m->keys[i], mb0, mb1);
+        mf.body0 = mb0;
+        mf.body1 = mb1;
         w.pairHasAlgo[i] = (m->flags[i] & 1) ? 1 : 0;
         mf.n = w.pairHasAlgo[i] ? m->num_points[i] : 0;
         for (int j = 0; j < mf.n; j++) point_from(mf.pts[j], m->points + ((size_t)i * 4 + j) * JBGPU_POINT_FLOATS);

@@ -843,59 +843,90 @@ static void manifold_refresh(World& w, Manifold& m) {   // ManifoldResult.refres
 // ----------------------------------------------------------------------------------------
 // Collision algorithms
 // ----------------------------------------------------------------------------------------
+// A collision object as a collision algorithm sees it: the shape and world transform it holds
+// while the algorithm runs (CompoundCollisionAlgorithm swaps in a child with orgTrans *
+// childTrans, ConvexTriangleCallback a TriangleShape), and its body.
+struct CObj {
+    const Shape* s;
+    Xf xf;
+    int body;
+};
+
 // SphereSphereCollisionAlgorithm.processCollision (java:73-134)
-static void sphere_sphere(World& w, Manifold& m, int col0, int col1) {
-    const Body& b0 = w.bodies[col0];
-    const Body& b1 = w.bodies[col1];
-    V3 diff = sub(b0.xf.o, b1.xf.o);
+static void sphere_sphere(World& w, Manifold& m, int col0, int col1, const CObj& A, const CObj& B) {
+    V3 diff = sub(A.xf.o, B.xf.o);
     float l = len(diff);
-    float r0 = w.shapes[b0.shape].getMargin();
-    float r1 = w.shapes[b1.shape].getMargin();
+    float r0 = A.s->getMargin();
+    float r1 = B.s->getMargin();
     if (l > (r0 + r1)) { manifold_refresh(w, m); return; }
     float dist = l - (r0 + r1);
     V3 n = v3(1, 0, 0);
     if (l > FLT_EPS) n = scl(diff, 1.0f / l);
-    V3 pos1 = add(b1.xf.o, scl(n, r1));
+    V3 pos1 = add(B.xf.o, scl(n, r1));
     manifold_add_contact(w, m, col0, col1, n, pos1, dist);
     manifold_refresh(w, m);
 }
 
 // ConvexPlaneCollisionAlgorithm.processCollision (java:75-136)
-static void convex_plane(World& w, Manifold& m, int col0, int col1, int convexIdx, int planeIdx) {
-    const Body& cb = w.bodies[convexIdx];
-    const Body& pb = w.bodies[planeIdx];
-    const Shape& cs = w.shapes[cb.shape];
-    const Shape& ps = w.shapes[pb.shape];
+static void convex_plane(World& w, Manifold& m, int col0, int col1, const CObj& C, const CObj& P) {
+    const Shape& cs = *C.s;
+    const Shape& ps = *P.s;
     V3 pn = ps.planeNormal;
     float pc = ps.planeConstant;
-    Xf planeInConvex = xf_mul(xf_inverse(cb.xf), pb.xf);
-    Xf convexInPlane = xf_mul(xf_inverse(pb.xf), cb.xf);
+    Xf planeInConvex = xf_mul(xf_inverse(C.xf), P.xf);
+    Xf convexInPlane = xf_mul(xf_inverse(P.xf), C.xf);
     V3 dir = mulMv(scl(pn, -1.0f), planeInConvex.b);
     V3 vtx = support_with_margin(cs, dir);
     V3 vtxInPlane = xf_apply(convexInPlane, vtx);
     float distance = dot(pn, vtxInPlane) - pc;
     V3 proj = sub(vtxInPlane, scl(pn, distance));
-    V3 vtxWorld = xf_apply(pb.xf, proj);
+    V3 vtxWorld = xf_apply(P.xf, proj);
     bool hasCollision = distance < w.cfg.contactBreakingThreshold;
     if (hasCollision) {
-        V3 normalOnB = mulMv(pn, pb.xf.b);
+        V3 normalOnB = mulMv(pn, P.xf.b);
         manifold_add_contact(w, m, col0, col1, normalOnB, vtxWorld, distance);
     }
     if (m.n != 0) manifold_refresh(w, m);
 }
 
-// ConvexConvexAlgorithm.processCollision (java:90-139)
-static void convex_convex(World& w, Manifold& m, int col0, int col1) {
-    const Body& b0 = w.bodies[col0];
-    const Body& b1 = w.bodies[col1];
-    const Shape& s0 = w.shapes[b0.shape];
-    const Shape& s1 = w.shapes[b1.shape];
-    float md = s0.getMargin() + s1.getMargin() + w.cfg.contactBreakingThreshold;
+// GjkPairDetector between A and B as ConvexConvexAlgorithm.processCollision (java:90-139) runs it;
+// adds the point, without the refresh.
+static void convex_convex_point(World& w, Manifold& m, int col0, int col1, const CObj& A, const CObj& B) {
+    float md = A.s->getMargin() + B.s->getMargin() + w.cfg.contactBreakingThreshold;
     md *= md;
     w.counters.gjk++;
-    GjkOut g = gjk_closest_points(s0, b0.xf, s1, b1.xf, md);
+    GjkOut g = gjk_closest_points(*A.s, A.xf, *B.s, B.xf, md);
     if (g.usedEpa) w.counters.epa++;
     if (g.valid) manifold_add_contact(w, m, col0, col1, g.normal, g.pointOnB, g.distance);
+}
+
+// ConvexConvexAlgorithm.processCollision (java:90-139) with its own manifold
+static void convex_convex(World& w, Manifold& m, int col0, int col1, const CObj& A, const CObj& B) {
+    convex_convex_point(w, m, col0, col1, A, B);
+    manifold_refresh(w, m);
+}
+
+// ConvexConcaveCollisionAlgorithm.processCollision (java:65-97): ConvexTriangleCallback's query box
+// (the convex shape's aabb in the mesh's space widened by the mesh margin,
+// ConvexTriangleCallback.setTimeStepAndCounters java:82-104), the mesh's triangles overlapping it
+// in walk order, each collided as a TriangleShape with the mesh margin by ConvexConvexAlgorithm
+// into the shared manifold (ConvexTriangleCallback.processTriangle java:109-166), then one refresh.
+static void convex_concave(World& w, Manifold& m, int col0, int col1, const CObj& C, const CObj& T) {
+    Xf convexInTri = xf_mul(xf_inverse(T.xf), C.xf);
+    V3 mn, mx;
+    shape_aabb(*C.s, convexInTri, mn, mx);
+    float mt = T.s->getMargin();
+    mx = add(mx, v3(mt, mt, mt));
+    mn = sub(mn, v3(mt, mt, mt));
+    std::vector<int> tris;
+    mesh_overlapping_triangles(*T.s->mesh, mn, mx, tris);
+    Shape tm;
+    tm.type = TRIANGLE;
+    tm.collisionMargin = mt;
+    for (int t : tris) {
+        for (int k = 0; k < 3; k++) tm.tri[k] = T.s->mesh->tri[3 * t + k];
+        convex_convex_point(w, m, col0, col1, C, CObj{&tm, T.xf, T.body});
+    }
     manifold_refresh(w, m);
 }
 
@@ -905,30 +936,85 @@ static bool needs_collision(const Body& a, const Body& b) {
     return true;
 }
 
-// DefaultNearCallback.handleCollision (collision/dispatch/DefaultNearCallback.java:39-66) for one pair.
-// col0/col1 are the lower/higher uid (proxy0/proxy1 of the BroadphasePair).
-void process_pair(World& w, int pi) {
-    uint64_t key = w.pairKeys[pi];
-    int a = (int)(key >> 32), b = (int)(key & 0xffffffffu);
+// CompoundShapeChild i of a compound object: orgTrans * childTrans (CompoundCollisionAlgorithm.
+// processCollision java:101-124)
+static CObj compound_child(const CObj& c, int i) {
+    return CObj{&c.s->children[i], xf_mul(c.xf, c.s->childXf[i]), c.body};
+}
+
+// The two leaf objects a pair's algorithm collides, in the algorithm's order.  col0/col1 are the
+// lower/higher uid (proxy0/proxy1 of the BroadphasePair).  A pair with a compound body is one
+// key per child combination: the combination's algorithm is the one CompoundCollisionAlgorithm.
+// init finds for the compound's child against the other object - the compound side first, and
+// with two compounds the higher body's child first (the swapped algorithm that the lower body's
+// child finds against the higher compound).
+static void pair_objects(const World& w, uint64_t key, CObj& f, CObj& g) {
+    int a = key_owner(key), b = key_partner(key), sub = key_sub(key);
     int col0 = a < b ? a : b, col1 = a < b ? b : a;
     const Body& B0 = w.bodies[col0];
     const Body& B1 = w.bodies[col1];
-    if (!needs_collision(B0, B1)) return;
     const Shape& S0 = w.shapes[B0.shape];
     const Shape& S1 = w.shapes[B1.shape];
+    CObj o0{&S0, B0.xf, col0}, o1{&S1, B1.xf, col1};
+    f = o0;
+    g = o1;
+    if (S0.isCompound() || S1.isCompound()) {
+        int n1 = S1.isCompound() ? (int)S1.children.size() : 1;
+        CObj l0 = S0.isCompound() ? compound_child(o0, sub / n1) : o0;
+        CObj l1 = S1.isCompound() ? compound_child(o1, sub % n1) : o1;
+        if (S1.isCompound()) { f = l1; g = l0; }
+        else { f = l0; g = l1; }
+    }
+}
+
+// DefaultCollisionConfiguration.getCollisionAlgorithmCreateFunc (java:160-215) over the leaf shape
+// types: the algorithm kind, and the bodies of the manifold it creates (convex before plane or
+// mesh, else the algorithm's order).  Kind 0: EmptyAlgorithm (two concave shapes), no manifold.
+enum { ALG_EMPTY = 0, ALG_SPHERE_SPHERE, ALG_CONVEX_PLANE, ALG_PLANE_CONVEX, ALG_CONVEX_CONVEX, ALG_CONVEX_CONCAVE,
+       ALG_CONCAVE_CONVEX };
+static int algorithm_kind(const CObj& f, const CObj& g, int& mb0, int& mb1) {
+    const Shape& F = *f.s;
+    const Shape& G = *g.s;
+    int k = ALG_EMPTY;
+    if (F.type == SPHERE && G.type == SPHERE) k = ALG_SPHERE_SPHERE;
+    else if (F.isConvex() && G.type == STATIC_PLANE) k = ALG_CONVEX_PLANE;
+    else if (G.isConvex() && F.type == STATIC_PLANE) k = ALG_PLANE_CONVEX;
+    else if (F.isConvex() && G.isConvex()) k = ALG_CONVEX_CONVEX;
+    else if (F.isConvex() && G.isConcave()) k = ALG_CONVEX_CONCAVE;
+    else if (G.isConvex() && F.isConcave()) k = ALG_CONCAVE_CONVEX;
+    bool swapped = k == ALG_PLANE_CONVEX || k == ALG_CONCAVE_CONVEX;
+    mb0 = swapped ? g.body : f.body;
+    mb1 = swapped ? f.body : g.body;
+    return k;
+}
+
+bool pair_manifold_bodies(const World& w, uint64_t key, int& mb0, int& mb1) {
+    CObj f, g;
+    pair_objects(w, key, f, g);
+    return algorithm_kind(f, g, mb0, mb1) != ALG_EMPTY;
+}
+
+// DefaultNearCallback.handleCollision (collision/dispatch/DefaultNearCallback.java:39-66) for one
+// pair: needsCollision, the algorithm (and its manifold) on first contact, processCollision.
+void process_pair(World& w, int pi) {
+    uint64_t key = w.pairKeys[pi];
+    int a = key_owner(key), b = key_partner(key);
+    int col0 = a < b ? a : b, col1 = a < b ? b : a;
+    if (!needs_collision(w.bodies[col0], w.bodies[col1])) return;
+    CObj f, g;
+    pair_objects(w, key, f, g);
+    int mb0, mb1;
+    int kind = algorithm_kind(f, g, mb0, mb1);
+    if (kind == ALG_EMPTY) return;
     Manifold& m = w.pairMf[pi];
-    if (S0.type == SPHERE && S1.type == SPHERE) {
-        if (!w.pairHasAlgo[pi]) { w.pairHasAlgo[pi] = 1; m = Manifold(); m.body0 = col0; m.body1 = col1; }
-        sphere_sphere(w, m, col0, col1);
-    } else if (S0.isConvex() && S1.type == STATIC_PLANE) {
-        if (!w.pairHasAlgo[pi]) { w.pairHasAlgo[pi] = 1; m = Manifold(); m.body0 = col0; m.body1 = col1; }
-        convex_plane(w, m, col0, col1, col0, col1);
-    } else if (S1.isConvex() && S0.type == STATIC_PLANE) {
-        if (!w.pairHasAlgo[pi]) { w.pairHasAlgo[pi] = 1; m = Manifold(); m.body0 = col1; m.body1 = col0; }
-        convex_plane(w, m, col0, col1, col1, col0);
-    } else if (S0.isConvex() && S1.isConvex()) {
-        if (!w.pairHasAlgo[pi]) { w.pairHasAlgo[pi] = 1; m = Manifold(); m.body0 = col0; m.body1 = col1; }
-        convex_convex(w, m, col0, col1);
+    if (!w.pairHasAlgo[pi]) { w.pairHasAlgo[pi] = 1; m = Manifold(); m.body0 = mb0; m.body1 = mb1; }
+    switch (kind) {
+    case ALG_SPHERE_SPHERE: sphere_sphere(w, m, col0, col1, f, g); break;
+    case ALG_CONVEX_PLANE: convex_plane(w, m, col0, col1, f, g); break;
+    case ALG_PLANE_CONVEX: convex_plane(w, m, col0, col1, g, f); break;
+    case ALG_CONVEX_CONVEX: convex_convex(w, m, col0, col1, f, g); break;
+    case ALG_CONVEX_CONCAVE: convex_concave(w, m, col0, col1, f, g); break;
+    case ALG_CONCAVE_CONVEX: convex_concave(w, m, col0, col1, g, f); break;
     }
 }
 

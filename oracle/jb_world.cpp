@@ -71,6 +71,21 @@ uint64_t pair_key(const World& w, int a, int b) {
     return ((uint64_t)(uint32_t)owner << 32) | (uint32_t)partner;
 }
 
+int pair_subs(const World& w, int a, int b) {
+    const Shape& sa = w.shapes[w.bodies[a].shape];
+    const Shape& sb = w.shapes[w.bodies[b].shape];
+    int na = sa.isCompound() ? (int)sa.children.size() : 1, nb = sb.isCompound() ? (int)sb.children.size() : 1;
+    return na * nb;
+}
+
+// A broadphase pair with its child combinations (one key each; CompoundCollisionAlgorithm keeps
+// one child algorithm, and so one manifold, per combination).
+static void push_pair(const World& w, std::vector<uint64_t>& keys, int a, int b) {
+    uint64_t k = pair_key(w, a, b);
+    int n = pair_subs(w, a, b);
+    for (int s = 0; s < n; s++) keys.push_back(k | ((uint64_t)s << 24));
+}
+
 // ---------------------------------------------------------------------------------------
 // DiscreteDynamicsWorld.applyGravity (dynamics/DiscreteDynamicsWorld.java:239-249)
 void stage_apply_gravity(World& w) {
@@ -178,12 +193,12 @@ void stage_pairs(World& w) {
         for (int i = 0; i < n; i++)
             for (int j = i + 1; j < n; j++)
                 if (!(is_plane(w, i) && is_plane(w, j)) && aabb_overlap(w.bodies[i], w.bodies[j]) && filter_pass(w.bodies[i], w.bodies[j]))
-                    keys.push_back(pair_key(w, i, j));
+                    push_pair(w, keys, i, j);
     } else {
         for (int p : planes)
             for (int j = 0; j < n; j++)
                 if (j != p && !is_plane(w, j) && aabb_overlap(w.bodies[p], w.bodies[j]) && filter_pass(w.bodies[p], w.bodies[j]))
-                    keys.push_back(pair_key(w, p, j));
+                    push_pair(w, keys, p, j);
         if (!finite.empty()) {
             BTree t;
             t.w = &w;
@@ -203,7 +218,7 @@ void stage_pairs(World& w) {
                     if (nd.left < 0) {
                         for (int k = nd.first; k < nd.first + nd.count; k++) {
                             int j = t.idx[k];
-                            if (j > i && aabb_overlap(bi, w.bodies[j]) && filter_pass(bi, w.bodies[j])) keys.push_back(pair_key(w, i, j));
+                            if (j > i && aabb_overlap(bi, w.bodies[j]) && filter_pass(bi, w.bodies[j])) push_pair(w, keys, i, j);
                         }
                     } else {
                         stack.push_back(nd.left);
@@ -276,7 +291,7 @@ void stage_islands(World& w) {
     uf.reset(n);
     for (int i = 0; i < n; i++) { w.bodies[i].islandTag = i; w.bodies[i].companionId = -1; }
     for (size_t k = 0; k < w.pairKeys.size(); k++) {   // findUnions over the pair array
-        int a = (int)(w.pairKeys[k] >> 32), b = (int)(w.pairKeys[k] & 0xffffffffu);
+        int a = key_owner(w.pairKeys[k]), b = key_partner(w.pairKeys[k]);
         int lo = a < b ? a : b, hi = a < b ? b : a;
         if (w.bodies[lo].mergesIslands() && w.bodies[hi].mergesIslands()) uf.unite(w.bodies[lo].islandTag, w.bodies[hi].islandTag);
     }

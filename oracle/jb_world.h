@@ -4,17 +4,37 @@
 // Citations are relative to src/com/bulletphysics/ of the reference.
 #pragma once
 #include <cstdint>
+#include <memory>
 #include <vector>
 #include "jb_math.h"
 
 namespace jb {
 
-enum ShapeType { BOX = 0, CONVEX_HULL = 4, SPHERE = 6, CAPSULE = 8, STATIC_PLANE = 23 };
+// BroadphaseNativeType ordinals (collision/broadphase/BroadphaseNativeType.java:36-72)
+enum ShapeType { BOX = 0, TRIANGLE = 1, CONVEX_HULL = 4, SPHERE = 6, CAPSULE = 8, TRIANGLE_MESH = 16, STATIC_PLANE = 23,
+                 COMPOUND = 25 };
 enum ActState { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEACTIVATION = 4, DISABLE_SIMULATION = 5 };
 enum { CF_STATIC_OBJECT = 1, CF_KINEMATIC_OBJECT = 2, CF_NO_CONTACT_RESPONSE = 4 };
 enum { SOLVER_RANDMIZE_ORDER = 1, SOLVER_USE_WARMSTARTING = 4, SOLVER_CACHE_FRIENDLY = 8 };
 
-// collision/shapes/*.java: one record for the five shape classes on the path.
+// OptimizedBvh with quantized aabb compression (collision/shapes/OptimizedBvh.java), the node
+// array in the order buildTree writes it (depth first, left subtree first).  A node's
+// escOrTri is (partId << 21) | triangleIndex for a leaf, -escapeIndex for an internal node
+// (QuantizedBvhNodes.java).
+struct QuantizedBvh {
+    V3 bvhAabbMin{0, 0, 0}, bvhAabbMax{0, 0, 0}, bvhQuantization{0, 0, 0};
+    std::vector<uint16_t> q;          // 6 per node: quantized min xyz, max xyz
+    std::vector<int> escOrTri;
+    int curNodeIndex = 0;
+};
+// BvhTriangleMeshShape over a TriangleIndexVertexArray of one part, scaling (1,1,1): the
+// triangles' vertices by triangle index, and the quantized tree over them.
+struct MeshData {
+    std::vector<V3> tri;              // 3 per triangle
+    QuantizedBvh bvh;
+};
+
+// collision/shapes/*.java: one record for the shape classes on the path.
 struct Shape {
     int type = BOX;
     float collisionMargin = 0.04f;          // ConvexInternalShape.collisionMargin (BulletGlobals.CONVEX_DISTANCE_MARGIN)
@@ -25,7 +45,13 @@ struct Shape {
     V3 localAabbMin = {1, 1, 1}, localAabbMax = {-1, -1, -1};  // PolyhedralConvexShape local aabb
     V3 planeNormal = {0, 1, 0};             // StaticPlaneShape
     float planeConstant = 0;
-    bool isConvex() const { return type != STATIC_PLANE; }
+    std::shared_ptr<const MeshData> mesh;   // BvhTriangleMeshShape (TriangleMeshShape.localAabbMin/Max above)
+    std::vector<Shape> children;            // CompoundShape children (localAabbMin/Max above)
+    std::vector<Xf> childXf;                // CompoundShapeChild.transform
+    V3 tri[3];                              // TriangleShape.vertices1 (a mesh triangle during a query)
+    bool isConvex() const { return type < 15; }   // BroadphaseNativeType.isConvex
+    bool isConcave() const { return type > 15 && type < 24; }
+    bool isCompound() const { return type == COMPOUND; }
     float getMargin() const;                // SphereShape.getMargin returns the radius
     float capsuleRadius() const { return coord(implicitDims, (upAxis + 2) % 3); }
     float capsuleHalfHeight() const { return coord(implicitDims, upAxis); }
@@ -36,6 +62,12 @@ Shape make_sphere(float radius);
 Shape make_capsule(float radius, float height);
 Shape make_hull(const float* pts, int n);
 Shape make_plane(V3 normal, float constant);
+// BvhTriangleMeshShape(new TriangleIndexVertexArray(...), true) with ConcaveShape.setMargin(margin)
+Shape make_mesh(const float* vertices, int numVertices, const int* indices, int numTriangles, float margin);
+// CompoundShape with addChildShape(transform, child) for each child in order, then setMargin(margin)
+Shape make_compound(const std::vector<Shape>& children, const std::vector<Xf>& xf, float margin);
+// OptimizedBvh.reportAabbOverlappingNodex: triangle indices in the order the walk reports them
+void mesh_overlapping_triangles(const MeshData& m, V3 aabbMin, V3 aabbMax, std::vector<int>& out);
 V3 shape_local_inertia(const Shape& s, float mass);
 void shape_aabb(const Shape& s, const Xf& t, V3& mn, V3& mx);
 V3 support_without_margin(const Shape& s, V3 vec);
@@ -211,7 +243,15 @@ struct World {
     double phaseSeconds[10] = {0};        // CProfile-like per-phase timers
 };
 
+// Pair keys: (owner << 32) | (sub << 24) | partner.  sub numbers the child combinations of a
+// pair with a compound body (0 otherwise): sub = i * n1 + j for child i of the lower-index body
+// and child j of the higher one (n1 = the higher body's child count, 1 when it is not a compound).
 uint64_t pair_key(const World& w, int a, int b);
+int pair_subs(const World& w, int a, int b);   // child combinations of a pair (1 without compounds)
+static inline int key_owner(uint64_t k) { return (int)(k >> 32); }
+static inline int key_partner(uint64_t k) { return (int)(k & 0xffffffu); }
+static inline int key_sub(uint64_t k) { return (int)((k >> 24) & 0xffu); }
+constexpr int MAX_COMPOUND_CHILDREN = 16;
 // Joint colours: first fit in index order over the joints' dynamic bodies (neither static nor
 // kinematic); the solve order is (colour, index), the GPU's order.
 std::vector<int> joint_colour_order(const World& w);
@@ -238,6 +278,8 @@ int add_body(World& w, float mass, int shape, const Xf& xf, V3 localInertia, flo
 
 // narrowphase entry (collision/dispatch/DefaultNearCallback.java:39-66 for one pair)
 void process_pair(World& w, int pairIndex);
+// The bodies of the manifold a pair's algorithm creates (false: EmptyAlgorithm, no manifold).
+bool pair_manifold_bodies(const World& w, uint64_t key, int& mb0, int& mb1);
 // GJK/EPA closest points between two convex bodies (GjkPairDetector.getClosestPoints), exposed for tests.
 struct GjkOut { bool valid; V3 normal; V3 pointOnB; float distance; int usedEpa; };
 GjkOut gjk_closest_points(const Shape& sa, const Xf& ta, const Shape& sb, const Xf& tb, float maxDist2, bool withEpa = true);

@@ -48,6 +48,8 @@ def lib():
         L.orc_counters.argtypes = [C.c_void_p, C.POINTER(_abi.Counters)]
         L.orc_phase_seconds.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         L.orc_shape_local_inertia.argtypes = [C.POINTER(_abi.ShapeDesc), C.c_float, _abi.f32p]
+        L.orc_mesh_bvh.argtypes = [C.POINTER(_abi.ShapeDesc), _abi.i32p, C.c_int, _abi.f32p]
+        L.orc_mesh_query.argtypes = [C.POINTER(_abi.ShapeDesc), _abi.f32p, _abi.f32p, _abi.i32p, C.c_int]
         L.orc_gjk.argtypes = [C.POINTER(_abi.ShapeDesc), _abi.f32p, C.POINTER(_abi.ShapeDesc), _abi.f32p, C.c_float, _abi.f32p]
         L.orc_integrate_transform.argtypes = [_abi.f32p, _abi.f32p, _abi.f32p, C.c_float, _abi.f32p]
         L.orc_add_point2point.argtypes = [C.c_void_p, C.c_int, C.c_int, _abi.f32p, _abi.f32p]
@@ -310,6 +312,29 @@ def shape_local_inertia(shape_dict, mass):
     out = np.zeros(3, np.float32)
     lib().orc_shape_local_inertia(C.byref(d[0]), mass, _fp(out))
     return out
+
+
+def mesh_bvh(mesh_dict):
+    """OptimizedBvh of a triangle-mesh shape dict as the oracle builds it: (nodes (n, 4) int32 in
+    the library's layout, local aabb (6,))."""
+    from jbgpu.scenes import shape_desc_array
+    d = shape_desc_array([mesh_dict])
+    nt = len(mesh_dict["indices"])
+    nodes = np.zeros((2 * nt, 4), np.int32)
+    aabb = np.zeros(6, np.float32)
+    n = lib().orc_mesh_bvh(C.byref(d[0]), nodes.ctypes.data_as(_abi.i32p), len(nodes), _fp(aabb))
+    return nodes[:n].copy(), aabb
+
+
+def mesh_query(mesh_dict, aabb_min, aabb_max):
+    """OptimizedBvh.reportAabbOverlappingNodex: triangle indices in report order."""
+    from jbgpu.scenes import shape_desc_array
+    d = shape_desc_array([mesh_dict])
+    mn = np.ascontiguousarray(aabb_min, np.float32)
+    mx = np.ascontiguousarray(aabb_max, np.float32)
+    out = np.zeros(len(mesh_dict["indices"]), np.int32)
+    n = lib().orc_mesh_query(C.byref(d[0]), _fp(mn), _fp(mx), out.ctypes.data_as(_abi.i32p), len(out))
+    return out[:n].copy()
 
 
 def gjk(shape_a, xf_a, shape_b, xf_b, max_dist2):

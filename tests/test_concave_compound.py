@@ -1,0 +1,303 @@
+"""Compound shapes and triangle meshes (CompoundCollisionAlgorithm, ConvexConcaveCollisionAlgorithm
+over BvhTriangleMeshShape's quantized OptimizedBvh).
+
+CPU: the library's tree equals the oracle's node for node, the oracle's walk reports exactly the
+leaves a brute-force quantized overlap test finds (in node order), compound inertia agrees three
+ways, compound pairs carry one key per child combination, and the oracle's terrain and compound
+scenes stay finite and above the ground.  GPU: stage by stage and closed loop bit-exact against
+the oracle, the range-part solver in lockstep, and queries that reach a compound or a mesh are
+reported as unsupported."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from jbgpu import _abi, lib as jl, scenes
+from jbgpu.lib import GpuWorld
+
+import harness as H
+import pyoracle
+
+F = np.float32
+
+
+def _meshes():
+    rng = np.random.Generator(np.random.PCG64(5))
+    out = [scenes.terrain_mesh(4, 4, 8.0, seed=1), scenes.terrain_mesh(24, 24, 24.0, seed=2),
+           scenes.terrain_mesh(7, 13, 30.0, amp=4.0, seed=3)]
+    # a triangle soup far from the origin, some triangles flat in an axis (MIN_AABB_DIMENSION widening)
+    v = (rng.uniform(-5, 5, (300, 3)) + np.array([1000.0, -200.0, 50.0])).astype(F)
+    v[:60, 1] = F(-200.0)
+    idx = rng.integers(0, 300, (400, 3)).astype(np.int32)
+    idx[:40] = np.stack([np.arange(0, 40), np.arange(1, 41), np.arange(2, 42)], 1)   # flat in y
+    out.append({"type": _abi.SHAPE_TRIANGLE_MESH, "params": (0.0, 0.0, 0.0, 0.0), "points": v, "indices": idx})
+    one = {"type": _abi.SHAPE_TRIANGLE_MESH, "params": (0.02, 0.0, 0.0, 0.0),
+           "points": np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1]], F), "indices": np.array([[0, 2, 1]], np.int32)}
+    out.append(one)
+    return out
+
+
+def _quantizer(mesh):
+    """OptimizedBvh.setQuantizationValues / quantizeWithClamp in binary32 (for the brute force)."""
+    p = np.asarray(mesh["points"], F)[np.asarray(mesh["indices"]).reshape(-1)]
+    bmin, bmax = p.min(0) - F(1), p.max(0) + F(1)
+    q = F(65535.0) / (bmax - bmin)
+
+    def quant(x):
+        c = np.minimum(np.maximum(np.asarray(x, F), bmin), bmax)
+        v = (c - bmin) * q
+        return (np.floor(v + F(0.5)).astype(np.int64) & 0xFFFF)
+    return quant
+
+
+def _unpack(nodes):
+    n = nodes.astype(np.int64) & 0xFFFFFFFF
+    qmin = np.stack([n[:, 0] & 0xFFFF, n[:, 0] >> 16, n[:, 1] & 0xFFFF], 1)
+    qmax = np.stack([n[:, 1] >> 16, n[:, 2] & 0xFFFF, n[:, 2] >> 16], 1)
+    return qmin, qmax, nodes[:, 3]
+
+
+@pytest.mark.parametrize("k", range(5))
+def test_mesh_tree_library_equals_oracle(gpu_lib, oracle_lib, k):
+    mesh = _meshes()[k]
+    ln, la = jl.mesh_bvh(mesh)
+    on, oa = pyoracle.mesh_bvh(mesh)
+    assert ln.shape == on.shape and np.array_equal(ln, on)
+    assert np.array_equal(la.view(np.uint32), oa.view(np.uint32))
+
+
+@pytest.mark.parametrize("k", range(5))
+def test_mesh_tree_structure(oracle_lib, k):
+    mesh = _meshes()[k]
+    nodes, aabb = pyoracle.mesh_bvh(mesh)
+    nt = len(mesh["indices"])
+    assert len(nodes) == 2 * nt - 1
+    w = nodes[:, 3]
+    assert sorted(w[w >= 0].tolist()) == list(range(nt))   # every triangle once, as a leaf
+
+    def size(i):   # subtree size from the escape index, checked against the children's sizes
+        if w[i] >= 0:
+            return 1
+        left = size(i + 1)
+        right = size(i + 1 + left)
+        assert -w[i] == 1 + left + right
+        return -w[i]
+    assert size(0) == len(nodes)
+    p = np.asarray(mesh["points"], F)[np.asarray(mesh["indices"]).reshape(-1)]
+    assert np.array_equal(aabb[:3], p.min(0)) and np.array_equal(aabb[3:], p.max(0))
+
+
+@pytest.mark.parametrize("k", range(5))
+def test_mesh_walk_reports_overlapping_leaves_in_node_order(oracle_lib, k):
+    mesh = _meshes()[k]
+    nodes, _ = pyoracle.mesh_bvh(mesh)
+    qmin, qmax, w = _unpack(nodes)
+    quant = _quantizer(mesh)
+    p = np.asarray(mesh["points"], F)[np.asarray(mesh["indices"]).reshape(-1)]
+    lo, hi = p.min(0), p.max(0)
+    rng = np.random.Generator(np.random.PCG64(k))
+    for _ in range(40):
+        c = rng.uniform(lo - 1, hi + 1).astype(F)
+        e = rng.uniform(0.0, 0.3, 3).astype(F) * (hi - lo + 1)
+        mn, mx = c - e, c + e
+        got = pyoracle.mesh_query(mesh, mn, mx)
+        a, b = quant(mn), quant(mx)
+        ov = np.all((a <= qmax) & (b >= qmin), axis=1)
+        want = w[(w >= 0) & ov]
+        assert np.array_equal(got, want)
+
+
+def test_compound_inertia_three_ways(gpu_lib, oracle_lib):
+    rng = np.random.Generator(np.random.PCG64(3))
+    for s, m, inertia in scenes._compound_kinds(rng, 8):
+        a = jl.shape_local_inertia(s, float(m))
+        b = pyoracle.shape_local_inertia(s, float(m))
+        assert np.array_equal(a.view(np.uint32), inertia.view(np.uint32)), (a, inertia)
+        assert np.array_equal(b.view(np.uint32), inertia.view(np.uint32)), (b, inertia)
+
+
+def test_compound_child_limit(gpu_lib):
+    child = {"type": _abi.SHAPE_SPHERE, "params": (0.1, 0.0, 0.0, 0.0), "points": None}
+    ok = {"type": _abi.SHAPE_COMPOUND, "params": (0.0, 0.0, 0.0, 0.0), "points": None,
+          "children": [(child, scenes.xf12(None, (i, 0, 0))) for i in range(_abi.COMPOUND_MAX_CHILDREN)]}
+    jl.shape_local_inertia(ok, 1.0)
+    bad = dict(ok, children=ok["children"] + [(child, scenes.xf12(None, (20, 0, 0)))])
+    d = scenes.shape_desc_array([bad])
+    out = np.zeros(3, np.float32)
+    assert jl.lib().jbgpu_shape_local_inertia(C.byref(d[0]), 1.0, out.ctypes.data_as(_abi.f32p)) == \
+        _abi.ERR_INVALID_ARGUMENT
+    nested = dict(ok, children=[(ok, scenes.xf12())])
+    d = scenes.shape_desc_array([nested])
+    assert jl.lib().jbgpu_shape_local_inertia(C.byref(d[0]), 1.0, out.ctypes.data_as(_abi.f32p)) == \
+        _abi.ERR_UNSUPPORTED
+
+
+def _subs(sc, a, b):
+    n = [len(sc.shapes[sc.bodies["shape"][x]].get("children") or []) or 1 for x in (a, b)]
+    return n[0] * n[1]
+
+
+def test_compound_pairs_one_key_per_child_combination(oracle_lib):
+    sc = scenes.compounds(12, 6, seed=4)
+    o = pyoracle.OracleWorld(sc)
+    for _ in range(90):
+        o.step(sc.dt)
+    keys = o.get_pairs()
+    assert len(keys) and np.all(np.diff(keys.astype(np.uint64)) > 0)
+    owner, partner, sub = keys >> np.uint64(32), keys & np.uint64(0xFFFFFF), (keys >> np.uint64(24)) & np.uint64(0xFF)
+    per = {}
+    for a, b, s in zip(owner.tolist(), partner.tolist(), sub.tolist()):
+        per.setdefault((a, b), []).append(s)
+    assert any(len(v) > 1 for v in per.values())
+    for (a, b), v in per.items():
+        assert sorted(v) == list(range(_subs(sc, a, b)))
+
+
+@pytest.mark.parametrize("which", ["terrain", "compounds"])
+def test_oracle_f3_scenes_stay_on_the_ground(oracle_lib, which):
+    if which == "terrain":
+        sc = scenes.terrain(40, compounds=8, seed=2)
+        floor = F(sc.shapes[0]["points"][:, 1].min()) - F(0.5)
+    else:
+        sc = scenes.compounds(30, 10, seed=2)
+        floor = F(-0.1)
+    o = pyoracle.OracleWorld(sc)
+    for _ in range(sc.steps):
+        o.step(sc.dt)
+    t = o.get_state()["transform"]
+    assert np.isfinite(t).all()
+    assert (t[1:, 10] > floor).all()
+    c = o.counters()
+    assert c["contacts"] > len(sc.bodies) // 2
+
+
+# ---- GPU -------------------------------------------------------------------------------------
+STAGES = [_abi.STAGE_PREDICT, _abi.STAGE_AABB, _abi.STAGE_PAIRS, _abi.STAGE_NARROWPHASE, _abi.STAGE_ISLANDS,
+          _abi.STAGE_SOLVE, _abi.STAGE_INTEGRATE, _abi.STAGE_ACTIVATION]
+
+SCENES = {
+    "terrain": lambda: scenes.terrain(40, seed=1),
+    "terrain_compounds": lambda: scenes.terrain(30, compounds=12, seed=2),
+    "compounds": lambda: scenes.compounds(30, 10, seed=3),
+    "terrain_margin": lambda: _with_mesh_margin(scenes.terrain(30, compounds=4, seed=5), 0.05),
+}
+
+
+def _with_mesh_margin(sc, m):
+    sc.shapes[0] = dict(sc.shapes[0], params=(m, 0.0, 0.0, 0.0))
+    return sc
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(SCENES))
+@pytest.mark.parametrize("warm", [0, 60, 150])
+def test_f3_stage_by_stage_bit_exact(gpu_lib, oracle_lib, name, warm):
+    sc = SCENES[name]()
+    ref = pyoracle.OracleWorld(sc)
+    for _ in range(warm):
+        ref.step(sc.dt)
+    o = pyoracle.OracleWorld(sc)
+    g = GpuWorld(sc)
+    H.copy_world(ref, o)
+    H.copy_world(ref, g)
+    o.stage(_abi.STAGE_APPLY_GRAVITY, sc.dt)
+    g.stage(_abi.STAGE_APPLY_GRAVITY, sc.dt)
+    for st in STAGES:
+        H.copy_world(o, g)
+        o.stage(st, sc.dt)
+        g.stage(st, sc.dt)
+        bs = H.compare_state(o.get_state(), g.get_state())
+        bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+        assert not bs and not bm, (st, bs, bm)
+        if st == _abi.STAGE_NARROWPHASE:
+            co, cg = o.counters(), g.counters()
+            assert (co["gjk_calls"], co["epa_calls"]) == (cg["gjk_calls"], cg["epa_calls"])
+        if st == _abi.STAGE_SOLVE:
+            assert np.array_equal(o.solver_order(), g.solver_order())
+    g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(SCENES))
+def test_f3_closed_loop_bit_exact(gpu_lib, oracle_lib, name):
+    sc = SCENES[name]()
+    o = pyoracle.OracleWorld(sc)
+    g = GpuWorld(sc)
+    for s in range(sc.steps):
+        o.step(sc.dt)
+        g.step(sc.dt)
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+            assert not bs and not bm, (s, bs, bm)
+    co, cg = o.counters(), g.counters()
+    for k in ("pairs", "manifolds", "contacts", "solver_manifolds", "solver_rows", "gjk_calls", "epa_calls"):
+        assert co[k] == cg[k], (k, co[k], cg[k])
+    assert cg["status_flags"] == 0
+    assert co["contacts"] > 0
+    g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["terrain_compounds", "compounds"])
+def test_f3_range_parts_lockstep_bit_exact(gpu_lib, oracle_lib, name):
+    sc = SCENES[name]()
+    o = pyoracle.OracleWorld(sc)
+    g = GpuWorld(sc, config=_abi.default_config(**dict(sc.config, solver_parts=3)))
+    for s in range(120):
+        g.step(sc.dt)
+        o.set_explicit_order(g.solver_order())
+        o.step(sc.dt)
+        assert o.counters()["status_flags"] == 0, s
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+            assert not bs and not bm, (s, bs, bm)
+    g.close()
+
+
+@pytest.mark.gpu
+def test_f3_batched_worlds_equal_solo(gpu_lib):
+    """Three terrain/compound worlds batched: each world's bodies end where the same world
+    stepped alone leaves them."""
+    parts = [scenes.terrain(12, compounds=4, seed=s) for s in (7, 8, 9)]
+    shapes, bodies, wid = [], [], []
+    for w, sc in enumerate(parts):
+        b = sc.bodies.copy()
+        b["shape"] += len(shapes)
+        b["world"] = w
+        shapes += sc.shapes
+        bodies.append(b)
+        wid.append(np.full(len(b), w, np.int32))
+    batch = scenes.Scene("f3_batch", parts[0].dt, 90, parts[0].config, shapes, np.concatenate(bodies),
+                         world_of_body=np.concatenate(wid))
+    g = GpuWorld(batch)
+    for _ in range(90):
+        g.step(batch.dt)
+    tb = g.get_state()["transform"]
+    g.close()
+    off = 0
+    for sc in parts:
+        s = GpuWorld(sc)
+        for _ in range(90):
+            s.step(sc.dt)
+        ts = s.get_state()["transform"]
+        s.close()
+        assert np.array_equal(tb[off:off + len(ts)].view(np.uint32), ts.view(np.uint32))
+        off += len(ts)
+
+
+@pytest.mark.gpu
+def test_f3_queries_and_bodies_rejected(gpu_lib):
+    sc = scenes.terrain(6, compounds=2, seed=1)
+    g = GpuWorld(sc)
+    g.step(sc.dt)
+    with pytest.raises(jl.JbgpuError) as e:   # a ray straight down through the mesh
+        g.ray_test([[0.0, 20.0, 0.0]], [[0.0, -20.0, 0.0]])
+    assert e.value.code == _abi.ERR_UNSUPPORTED
+    g.close()
+    bad = scenes.terrain(2, seed=1)           # a dynamic triangle-mesh body
+    bad.bodies["mass"][0] = 1.0
+    with pytest.raises(jl.JbgpuError) as e:
+        GpuWorld(bad)
+    assert e.value.code == _abi.ERR_INVALID_ARGUMENT
