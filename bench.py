@@ -421,7 +421,7 @@ def traffic_for_window(dom, window_bytes, workload):
 # The other workloads of the step, measured beside the headline in the same run: each stepped
 # from rest to a settled point (untimed), then timed over `steps` steps by CUDA events on the
 # world's stream (CUDA graphs, as the headline); the phases come from a second, event-marked run.
-OTHER_WORKLOADS = [("boxes_1k", 100, 100), ("hulls_20k", 300, 20), ("batched_4096", 200, 20)]
+OTHER_WORKLOADS = [("boxes_1k", 100, 100), ("hulls_20k", 300, 20), ("batched_4096", 200, 20), ("terrain_20k", 300, 20)]
 
 
 def measure_workload(name, settle, steps, seed, local):

@@ -101,8 +101,8 @@ extern "C" {
 #define JBGPU_MANIFOLD_POINTS 4
 
 /* Pair keys.  A pair of bodies (a, b) (body index = uid - 1) is stored under the
- * canonical key (owner << 32) | (sub << 24) | partner, where the owner is the non-plane
- * body when exactly one body is a static plane, else min(a, b).  sub numbers the child
+ * canonical key (owner << 32) | (sub << 24) | partner, where the owner is the other body when
+ * exactly one body is a static plane or a triangle mesh, else min(a, b).  sub numbers the child
  * combinations of a pair with a compound body, each with its own manifold as
  * CompoundCollisionAlgorithm keeps one child algorithm per child
  * (collision/dispatch/CompoundCollisionAlgorithm.java:49-67): sub = i * n1 + j for child i of
@@ -526,8 +526,9 @@ int jbgpu_world_get_transforms(jbgpu_world* world, float* transforms);
  * reference's CProfileManager table, linearmath/CProfileManager.java:41-100).  Phases:
  * 0 predict, 1 aabb, 2 pair count (bounds, morton, sort, tree, count, scan), 3 pair fill
  * (fill, sort, persist), 4 narrowphase GJK pass, 5 EPA pass, 6 islands, 7 colouring,
- * 8 solver setup, 9 PGS, 10 integrate, 11 activation, 12 gravity + clear forces. */
-#define JBGPU_NUM_PHASES 13
+ * 8 solver setup, 9 PGS, 10 integrate, 11 activation, 12 gravity + clear forces, 13 the
+ * triangle-mesh pass of the narrowphase (worlds with meshes). */
+#define JBGPU_NUM_PHASES 14
 int jbgpu_world_set_profiling(jbgpu_world* world, int32_t max_steps);   /* 0 turns it off */
 /* Sum of each phase's device milliseconds over the profiled steps so far (waits for them).
  * With n_phases > JBGPU_NUM_PHASES, ms[JBGPU_NUM_PHASES] receives the device time of the whole

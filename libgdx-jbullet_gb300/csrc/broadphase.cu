@@ -37,7 +37,7 @@ __global__ void k_bounds(DevWorld w, unsigned* bnd) {
     if (threadIdx.x < 6) s[threadIdx.x] = (threadIdx.x < 3) ? 0xffffffffu : 0u;
     __syncthreads();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < w.nBodies && !(w.flags[i] & CF_PLANE)) {
+    if (i < w.nBodies && !(w.flags[i] & CF_LISTED)) {
         float4 a = w.amin[i], b = w.amax[i];
         float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
         for (int k = 0; k < 3; k++) {
@@ -63,7 +63,7 @@ __global__ void k_morton(DevWorld w, const unsigned* bnd, uint64_t* keys, int* v
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.nBodies) return;
     vals[i] = i;
-    if (w.flags[i] & CF_PLANE) { keys[i] = ~0ull; return; }
+    if (w.flags[i] & CF_LISTED) { keys[i] = ~0ull; return; }
     float lo[3], hi[3];
     for (int k = 0; k < 3; k++) { lo[k] = ord2f(bnd[k]); hi[k] = ord2f(bnd[3 + k]); }
     float4 a = w.amin[i], b = w.amax[i];
@@ -230,12 +230,13 @@ __global__ void k_traverse(DevWorld w, const int* sortedBody, int nf, Bvh t, con
     if (!FILL) tcount[s] = found;
 }
 
-// Pairs of each finite body with the static planes of its world.
+// Pairs of each body in the tree with the listed bodies (static planes, triangle meshes) of its
+// world, owned by the former.
 template <bool FILL>
 __global__ void k_plane_pairs(DevWorld w, const int* planeList, const int* planeStart, int* cnt, const int* off,
                               int* cursor, int* partners, int capacity) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= w.nBodies || (w.flags[i] & CF_PLANE)) return;
+    if (i >= w.nBodies || (w.flags[i] & CF_LISTED)) return;
     int wi = w.world[i];
     float4 a0 = w.amin[i], a1 = w.amax[i];
     for (int k = planeStart[wi]; k < planeStart[wi + 1]; k++) {

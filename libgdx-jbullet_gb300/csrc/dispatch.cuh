@@ -102,4 +102,15 @@ JBD int pair_leaf_types(const DevWorld& w, uint64_t key, int col0, int col1, int
     return algorithm_kind(tf, tg);
 }
 
+// OptimizedBvh.quantizeWithClamp (collision/shapes/OptimizedBvh.java:1038-1056) with a mesh's
+// bvhAabbMin, bvhAabbMax and bvhQuantization.
+JBD void mesh_quantize(V p, V bmin, V bmax, V q, int out[3]) {
+    V c = mk(jmax(p.x, bmin.x), jmax(p.y, bmin.y), jmax(p.z, bmin.z));
+    c = mk(jmin(c.x, bmax.x), jmin(c.y, bmax.y), jmin(c.z, bmax.z));
+    V v = mulc(sub(c, bmin), q);
+    out[0] = (int)__fadd_rn(v.x, 0.5f) & 0xFFFF;
+    out[1] = (int)__fadd_rn(v.y, 0.5f) & 0xFFFF;
+    out[2] = (int)__fadd_rn(v.z, 0.5f) & 0xFFFF;
+}
+
 }  // namespace jbg

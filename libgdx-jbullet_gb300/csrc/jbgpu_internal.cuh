@@ -12,7 +12,10 @@ enum { SHAPE_BOX = 0, SHAPE_TRIANGLE = 1, SHAPE_HULL = 4, SHAPE_SPHERE = 6, SHAP
 __host__ __device__ inline bool shape_is_convex(int t) { return t < 15; }      // BroadphaseNativeType.isConvex
 __host__ __device__ inline bool shape_is_concave(int t) { return t > 15 && t < 24; }
 enum { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEACTIVATION = 4, DISABLE_SIMULATION = 5 };
-enum { CF_STATIC = 1, CF_KINEMATIC = 2, CF_NO_CONTACT_RESPONSE = 4, CF_PLANE = 64 };
+// CF_LISTED: a static plane or triangle mesh - kept out of the broadphase tree and paired through
+// its world's list by every other body of the world (a plane's box is infinite, a terrain's spans
+// the world: either would make one tree leaf own and walk to all pairs).
+enum { CF_STATIC = 1, CF_KINEMATIC = 2, CF_NO_CONTACT_RESPONSE = 4, CF_LISTED = 64 };
 enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8, ST_BAD_WORLD = 16, ST_CCD_PLANE = 32,
        ST_QUERY_SHAPE = 64 };
 
@@ -179,7 +182,7 @@ JBD int set_activation(int cur, int s) { return (cur != DISABLE_DEACTIVATION && 
 
 // ---- per-phase event timing ---------------------------------------------------------------
 enum { PH_PREDICT = 0, PH_AABB, PH_PAIR_COUNT, PH_PAIR_FILL, PH_NARROW, PH_EPA, PH_ISLANDS, PH_COLOUR, PH_SETUP, PH_PGS,
-       PH_INTEGRATE, PH_ACTIVATION, PH_OTHER, NUM_PHASES };
+       PH_INTEGRATE, PH_ACTIVATION, PH_OTHER, PH_CONCAVE, NUM_PHASES };
 
 struct Prof {
     int maxSteps = 0;

@@ -428,16 +428,6 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
 // added to each pair's manifold in walk order by one thread per pair, which is what makes the
 // result the reference's: a manifold's point replacement depends on the order points arrive.
 
-// OptimizedBvh.quantizeWithClamp (java:1038-1056)
-JBD void mesh_quantize(V p, V bmin, V bmax, V q, int out[3]) {
-    V c = mk(jmax(p.x, bmin.x), jmax(p.y, bmin.y), jmax(p.z, bmin.z));
-    c = mk(jmin(c.x, bmax.x), jmin(c.y, bmax.y), jmin(c.z, bmax.z));
-    V v = mulc(sub(c, bmin), q);
-    out[0] = (int)__fadd_rn(v.x, 0.5f) & 0xFFFF;
-    out[1] = (int)__fadd_rn(v.y, 0.5f) & 0xFFFF;
-    out[2] = (int)__fadd_rn(v.z, 0.5f) & 0xFFFF;
-}
-
 // The convex object and the mesh of a convex-concave pair; false for any other pair or when
 // neither body is active (needsCollision).
 JBD bool concave_pair(const DevWorld& w, const DevPairs& P, int p, int& col0, int& col1, Xf& x0, Xf& x1, Leaf& c,

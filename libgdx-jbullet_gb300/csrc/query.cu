@@ -161,6 +161,73 @@ JBD bool ray_triangle(V t0, V t1, V t2, V from, V to, float below, float& distan
     return true;
 }
 
+// rayTestSingle's compound branch (CollisionWorld.java:340-355): the convex branch on every child
+// at the body's transform times the child's, in child order; the first smallest hit below 1 (the
+// one the reference keeps, whatever closest fraction it enters with, whenever that hit wins).
+JBD bool ray_compound(const DevShapes& sh, int s, const Xf& t, V from, V to, float& best, V& nrm) {
+    best = 1.0f;
+    bool hit = false;
+    for (int i = 0, n = sh.child_cnt[s]; i < n; i++) {
+        const int c = sh.child_off[s] + i;
+        float f;
+        V nl;
+        if (subsimplex_ray(shape_ref(sh, sh.child_shape[c]), xf_mul(t, child_xf(sh, c)), from, to, f, nl) &&
+            len2(nl) > 0.0001f && f < best) {
+            best = f;
+            nrm = nor(mulMv(nl, identity3()));
+            hit = true;
+        }
+    }
+    return hit;
+}
+
+// rayTestSingle's BvhTriangleMeshShape branch (CollisionWorld.java:297-311): the ray in the mesh's
+// space walked through the quantized tree as OptimizedBvh.walkStacklessQuantizedTreeAgainstRay
+// does (java:817-938: a node is entered when its quantized box overlaps the ray's quantized box
+// and AabbUtil2.rayAabb with the bound 1 accepts its unquantized box), each leaf entered tested by
+// TriangleRaycastCallback; the first smallest hit below 1, its normal times the mesh's basis.
+JBD bool ray_mesh(const DevShapes& sh, int s, const Xf& t, V from, V to, float& best, V& nrm) {
+    const Xf inv = xf_inverse(t);
+    const V lf = xf_apply(inv, from), lt = xf_apply(inv, to);
+    const V zero = mk(0.0f, 0.0f, 0.0f);
+    const float4* q = sh.mesh_q + 3 * s;
+    const V bmin = mk4(q[0]), bmax = mk4(q[1]), quant = mk4(q[2]);
+    int qa[3], qb[3];
+    mesh_quantize(add(mk(jmin(lf.x, lt.x), jmin(lf.y, lt.y), jmin(lf.z, lt.z)), zero), bmin, bmax, quant, qa);
+    mesh_quantize(add(mk(jmax(lf.x, lt.x), jmax(lf.y, lt.y), jmax(lf.z, lt.z)), zero), bmin, bmax, quant, qb);
+    const int4* nodes = sh.mesh_nodes + sh.mesh_node_off[s];
+    const float4* tris = sh.mesh_tris + (size_t)3 * sh.mesh_tri_off[s];
+    const int nn = sh.mesh_node_cnt[s];
+    best = 1.0f;
+    bool hit = false;
+    for (int cur = 0; cur < nn;) {
+        const int4 nd = nodes[cur];
+        const int n0 = nd.x & 0xFFFF, n1 = (nd.x >> 16) & 0xFFFF, n2 = nd.y & 0xFFFF;
+        const int m0 = (nd.y >> 16) & 0xFFFF, m1 = nd.z & 0xFFFF, m2 = (nd.z >> 16) & 0xFFFF;
+        const bool boxOv = !(qa[0] > m0 || qb[0] < n0) && !(qa[2] > m2 || qb[2] < n2) && !(qa[1] > m1 || qb[1] < n1);
+        const bool leaf = nd.w >= 0;
+        bool rayOv = false;
+        if (boxOv) {
+            const V b0 = add(add(mk(jdiv((float)n0, quant.x), jdiv((float)n1, quant.y), jdiv((float)n2, quant.z)), bmin), zero);
+            const V b1 = add(add(mk(jdiv((float)m0, quant.x), jdiv((float)m1, quant.y), jdiv((float)m2, quant.z)), bmin), zero);
+            float enter, exit;
+            rayOv = ray_aabb_parts(lf, lt, b0, b1, enter, exit) && enter <= jmin(1.0f, exit);
+        }
+        if (leaf && rayOv) {
+            const float4* tv = tris + 3 * (nd.w & ((1 << 21) - 1));
+            float f;
+            V nl;
+            if (ray_triangle(mk4(tv[0]), mk4(tv[1]), mk4(tv[2]), lf, lt, best, f, nl)) {
+                best = f;
+                nrm = mulMv(nl, t.b);
+                hit = true;
+            }
+        }
+        cur += (rayOv || leaf) ? 1 : max(1, -nd.w);
+    }
+    return hit;
+}
+
 // One object's part of rayTest with every hit below 1 (the bound of any closest fraction):
 // rayTestSingle's convex branch (the normal rotated by the ray's identity basis and
 // normalised) or its concave branch for a StaticPlaneShape, whose processAllTriangles
@@ -177,8 +244,15 @@ JBD void ray_object(const DevWorld& w, int b, V from, V to, ObjHits& h) {
     h.n = 0;
     const int shape = w.shape[b];
     const Xf t = load_xf(w, b);
-    if (w.sh.type[shape] == SHAPE_COMPOUND || w.sh.type[shape] == SHAPE_MESH) {   // not handled: reported
-        atomicOr(&w.ctr[C_STATUS], ST_QUERY_SHAPE);
+    if (w.sh.type[shape] == SHAPE_COMPOUND || w.sh.type[shape] == SHAPE_MESH) {
+        float f;
+        V n;
+        if (w.sh.type[shape] == SHAPE_COMPOUND ? ray_compound(w.sh, shape, t, from, to, f, n)
+                                               : ray_mesh(w.sh, shape, t, from, to, f, n)) {
+            h.f[0] = f;
+            h.nrm[0] = n;
+            h.n = 1;
+        }
         return;
     }
     if (w.sh.type[shape] != SHAPE_PLANE) {
@@ -793,20 +867,31 @@ __global__ void __launch_bounds__(RAY_THREADS) k_sweep_cast(DevWorld w, const Ra
         atomicOr(planeHit + c.ray, 1);
         return;
     }
-    if (w.sh.type[bs] == SHAPE_COMPOUND || w.sh.type[bs] == SHAPE_MESH) {   // not handled: reported
+    if (w.sh.type[bs] == SHAPE_MESH) {   // not handled: reported
         atomicOr(&w.ctr[C_STATUS], ST_QUERY_SHAPE);
         return;
     }
     const Xf fa = xf12(from + 12 * c.ray);
     const V ta = mk(to[12 * c.ray + 9], to[12 * c.ray + 10], to[12 * c.ray + 11]);
-    float f;
-    V nrm, p;
-    if (!gjk_convex_cast(shape_ref(w.sh, shape), fa, ta, shape_ref(w.sh, bs), load_xf(w, c.body), f, nrm, p) ||
-        !(len2(nrm) > 0.0001f) || !(f < 1.0f))   // ClosestConvexResultCallback starts at closestHitFraction 1
-        return;
-    hitA[i] = f4(nrm, f);
-    hitB[i] = f4(p, 0.0f);
-    atomicMin(key + c.ray, hit_key(f, c.body, 0));
+    const Xf tb = load_xf(w, c.body);
+    // objectQuerySingle's convex branch, or its compound branch over the children at the body's
+    // transform times the child's (CollisionWorld.java:391-430, 491-510): the first smallest hit
+    const bool compound = w.sh.type[bs] == SHAPE_COMPOUND;
+    const int nc = compound ? w.sh.child_cnt[bs] : 1;
+    float best = 1.0f;   // ClosestConvexResultCallback starts at closestHitFraction 1
+    for (int k = 0; k < nc; k++) {
+        const int cc = compound ? w.sh.child_off[bs] + k : 0;
+        float f;
+        V nrm, p;
+        if (!gjk_convex_cast(shape_ref(w.sh, shape), fa, ta, shape_ref(w.sh, compound ? w.sh.child_shape[cc] : bs),
+                             compound ? xf_mul(tb, child_xf(w.sh, cc)) : tb, f, nrm, p) ||
+            !(len2(nrm) > 0.0001f) || !(f < best))
+            continue;
+        best = f;
+        hitA[i] = f4(nrm, f);
+        hitB[i] = f4(p, 0.0f);
+    }
+    if (best < 1.0f) atomicMin(key + c.ray, hit_key(best, c.body, 0));
 }
 
 // The candidate holding its sweep's smallest key writes the record (one body per key).
@@ -948,7 +1033,8 @@ __global__ void k_ccd_predict(DevWorld w, float dt, float4* pred, int* flag) {
         const float thr = w.ccdThr[i];
         const float sq = __fmul_rn(thr, thr);                 // getCcdSquareMotionThreshold
         const float squareMotion = len2(sub(p.o, t.o));
-        f = sq != 0.0f && sq < squareMotion && w.sh.type[w.shape[i]] != SHAPE_PLANE ? 1 : 0;
+        // only a convex body sweeps (integrateTransforms' isConvex test, DiscreteDynamicsWorld.java:703)
+        f = sq != 0.0f && sq < squareMotion && shape_is_convex(w.sh.type[w.shape[i]]) ? 1 : 0;
         t = p;
     }
     pred[3 * i] = make_float4(t.b.r[0].x, t.b.r[0].y, t.b.r[0].z, t.o.x);
@@ -1055,16 +1141,23 @@ __global__ void __launch_bounds__(256) k_ccd_sweep(DevWorld w, DevPairs P, int n
                 atomicOr(&w.ctr[C_STATUS], ST_CCD_PLANE);
                 continue;
             }
-            if (w.sh.type[w.shape[j]] == SHAPE_COMPOUND || w.sh.type[w.shape[j]] == SHAPE_MESH) {
+            const int sj = w.shape[j];
+            if (w.sh.type[sj] == SHAPE_MESH) {
                 atomicOr(&w.ctr[C_STATUS], ST_QUERY_SHAPE);   // not handled: reported
                 continue;
             }
-            float f;
-            V n, p;
-            if (!gjk_convex_cast(cast, from, to.o, shape_ref(w.sh, w.shape[j]), tj, f, n, p)) continue;
-            if (!(len2(n) > 0.0001f) || !(f < 1.0f)) continue;
-            if (dot(nor(n), motion) >= -0.0f) continue;        // moving away from the contact normal
-            atomicMin(&sBest, __float_as_uint(f));
+            const bool compound = w.sh.type[sj] == SHAPE_COMPOUND;   // the compound branch: every child
+            for (int k = 0, nc = compound ? w.sh.child_cnt[sj] : 1; k < nc; k++) {
+                const int cc = compound ? w.sh.child_off[sj] + k : 0;
+                float f;
+                V n, p;
+                if (!gjk_convex_cast(cast, from, to.o, shape_ref(w.sh, compound ? w.sh.child_shape[cc] : sj),
+                                     compound ? xf_mul(tj, child_xf(w.sh, cc)) : tj, f, n, p))
+                    continue;
+                if (!(len2(n) > 0.0001f) || !(f < 1.0f)) continue;
+                if (dot(nor(n), motion) >= -0.0f) continue;        // moving away from the contact normal
+                atomicMin(&sBest, __float_as_uint(f));
+            }
         }
         __syncthreads();
         if (threadIdx.x == 0 && sBest < __float_as_uint(1.0f)) atomicMin((unsigned*)&w.ctr[C_CCD_BEST], sBest);

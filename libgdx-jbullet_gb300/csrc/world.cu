@@ -363,7 +363,7 @@ int sync_planes(jbgpu_world* w) {
     std::vector<int> finite(nw, 0);
     unsigned kinds = 0;                 // convex shape kinds present
     for (int i = 0; i < w->nBodies; i++) {
-        if (w->hFlags[i] & CF_PLANE) { per[w->hWorld[i]].push_back(i); np++; }
+        if (w->hFlags[i] & CF_LISTED) { per[w->hWorld[i]].push_back(i); np++; }
         else {
             nf++;
             finite[w->hWorld[i]]++;
@@ -471,7 +471,7 @@ int prepare_solver(jbgpu_world* w) {
     std::vector<int> at(w->nWorlds + 1, 0), ord(std::max(nf, 1));
     for (int q = 0; q < w->nWorlds; q++) at[q + 1] = at[q] + w->worldFinite[q];
     for (int i = 0; i < w->nBodies; i++)
-        if (!(w->hFlags[i] & CF_PLANE)) ord[at[w->hWorld[i]]++] = i;
+        if (!(w->hFlags[i] & CF_LISTED)) ord[at[w->hWorld[i]]++] = i;
     dfree(S.orderFallback);
     CK(dalloc(&S.orderFallback, ord.size()));
     CK(cudaMemcpyAsync(S.orderFallback, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice, w->stream));
@@ -492,8 +492,12 @@ int run_stage(jbgpu_world* w, int stage, float dt) {
     case JBGPU_STAGE_NARROWPHASE:
         CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
         narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s, &P);
-        if (w->hasMesh && concave_launch(d, w->pairs[w->cur], w->nPairs, nullptr, w->nb, w->hostPinned + 8, s))
-            return fail(JBGPU_ERR_CUDA, "concave narrowphase pass failed");
+        if (w->hasMesh) {
+            P.mark(PH_CONCAVE, 0, s);
+            if (concave_launch(d, w->pairs[w->cur], w->nPairs, nullptr, w->nb, w->hostPinned + 8, s))
+                return fail(JBGPU_ERR_CUDA, "concave narrowphase pass failed");
+            P.mark(PH_CONCAVE, 1, s);
+        }
         break;
     case JBGPU_STAGE_ISLANDS:
         P.mark(PH_ISLANDS, 0, s);
@@ -635,8 +639,12 @@ int narrow_and_islands(jbgpu_world* w, const int* cntp = nullptr) {
     CK(cudaEventRecord(w->evJoin, a));
     CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
     narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s, &w->prof, cntp);
-    if (w->hasMesh && concave_launch(d, w->pairs[w->cur], w->nPairs, cntp, w->nb, w->hostPinned + 8, s))
-        return fail(JBGPU_ERR_CUDA, "concave narrowphase pass failed");
+    if (w->hasMesh) {
+        w->prof.mark(PH_CONCAVE, 0, s);
+        if (concave_launch(d, w->pairs[w->cur], w->nPairs, cntp, w->nb, w->hostPinned + 8, s))
+            return fail(JBGPU_ERR_CUDA, "concave narrowphase pass failed");
+        w->prof.mark(PH_CONCAVE, 1, s);
+    }
     CK(cudaStreamWaitEvent(s, w->evJoin, 0));
     w->prof.mark(PH_ISLANDS, 0, s);
     islands_launch_select(d, w->pairs[w->cur], w->nPairs, w->sb, s, cntp);
@@ -1349,7 +1357,8 @@ int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, 
         int f = 0;
         float im;
         if (d.mass == 0.0f) { f |= CF_STATIC; im = 0.0f; } else im = 1.0f / d.mass;
-        if (w->shapes[d.shape].type == JBGPU_SHAPE_STATIC_PLANE) f |= CF_PLANE;
+        if (w->shapes[d.shape].type == JBGPU_SHAPE_STATIC_PLANE || w->shapes[d.shape].type == JBGPU_SHAPE_TRIANGLE_MESH)
+            f |= CF_LISTED;
         float il[3];
         for (int k = 0; k < 3; k++) il[k] = d.local_inertia[k] != 0.0f ? 1.0f / d.local_inertia[k] : 0.0f;
         iloc[i] = make_float4(il[0], il[1], il[2], im);

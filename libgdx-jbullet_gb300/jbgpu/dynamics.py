@@ -97,6 +97,90 @@ class StaticPlaneShape(_Shape):
         return {"type": _abi.SHAPE_STATIC_PLANE, "params": self.normal + (self.constant,), "points": None}
 
 
+class TriangleIndexVertexArray:
+    """collision/shapes/TriangleIndexVertexArray.java with one IndexedMesh part: triangle vertex
+    indices (m, 3) and vertices (n, 3); scaling (1, 1, 1)."""
+
+    def __init__(self, triangleIndices, vertices):
+        self.indices = np.ascontiguousarray(triangleIndices, np.int32).reshape(-1, 3)
+        self.vertices = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+
+    def getNumSubParts(self):
+        return 1
+
+
+class BvhTriangleMeshShape(_Shape):
+    """collision/shapes/BvhTriangleMeshShape.java over a TriangleIndexVertexArray, with the
+    quantized OptimizedBvh (useQuantizedAabbCompression = true, the tree the library builds and
+    walks).  For static (mass 0) or kinematic bodies, as in the reference."""
+
+    def __init__(self, meshInterface, useQuantizedAabbCompression=True):
+        super().__init__()
+        if not useQuantizedAabbCompression:
+            raise NotImplementedError("only the quantized tree (useQuantizedAabbCompression=True) is built")
+        self.meshInterface = meshInterface
+        self.margin = 0.0   # ConcaveShape.collisionMargin
+
+    def setMargin(self, margin):
+        if self._id is not None:
+            raise RuntimeError("setMargin after the shape was added to a world")
+        self.margin = float(margin)
+
+    def getMargin(self):
+        return self.margin
+
+    def getMeshInterface(self):
+        return self.meshInterface
+
+    def desc(self):
+        return {"type": _abi.SHAPE_TRIANGLE_MESH, "params": (self.margin, 0.0, 0.0, 0.0),
+                "points": self.meshInterface.vertices, "indices": self.meshInterface.indices}
+
+    def calculateLocalInertia(self, mass):
+        return np.zeros(3, np.float32)   # TriangleMeshShape.calculateLocalInertia: moving meshes unsupported
+
+
+class CompoundShape(_Shape):
+    """collision/shapes/CompoundShape.java: convex children (boxes, spheres, capsules, convex
+    hulls) at local transforms, at most 16 of them; collisionMargin 0."""
+
+    def __init__(self):
+        super().__init__()
+        self.children = []
+        self.margin = 0.0
+
+    def addChildShape(self, localTransform, shape):
+        if self._id is not None:
+            raise RuntimeError("addChildShape after the shape was added to a world")
+        if len(self.children) >= _abi.COMPOUND_MAX_CHILDREN:
+            raise ValueError("a compound holds at most %d children" % _abi.COMPOUND_MAX_CHILDREN)
+        if isinstance(shape, (CompoundShape, BvhTriangleMeshShape, StaticPlaneShape)):
+            raise NotImplementedError("compound children must be convex shapes")
+        self.children.append((Transform(localTransform.basis.copy(), localTransform.origin.copy()), shape))
+
+    def getNumChildShapes(self):
+        return len(self.children)
+
+    def getChildShape(self, i):
+        return self.children[i][1]
+
+    def getChildTransform(self, i):
+        t = self.children[i][0]
+        return Transform(t.basis.copy(), t.origin.copy())
+
+    def setMargin(self, margin):
+        if self._id is not None:
+            raise RuntimeError("setMargin after the shape was added to a world")
+        self.margin = float(margin)
+
+    def getMargin(self):
+        return self.margin
+
+    def desc(self):
+        return {"type": _abi.SHAPE_COMPOUND, "params": (self.margin, 0.0, 0.0, 0.0), "points": None,
+                "children": [(s.desc(), t.as12()) for t, s in self.children]}
+
+
 class RigidBodyConstructionInfo:
     def __init__(self, mass, motionState, collisionShape, localInertia=(0.0, 0.0, 0.0)):
         self.mass = float(mass)

@@ -197,7 +197,7 @@ class Mlp:
         return losses
 
 PHASES = ["predict", "aabb", "pair_count", "pair_fill", "narrow_gjk", "narrow_epa", "islands", "colour", "setup", "pgs",
-          "integrate", "activation", "gravity"]
+          "integrate", "activation", "gravity", "concave"]
 
 
 def check(rc):

@@ -920,7 +920,7 @@ def rot_z(a):
     return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]], F)
 
 
-def terrain_mesh(nx=24, nz=24, size=24.0, amp=1.2, seed=0, margin=0.0):
+def terrain_mesh(nx=24, nz=24, size=24.0, amp=1.2, seed=0, margin=0.0, bowl=0.4):
     """A heightfield of nx x nz cells over size x size m (two triangles per cell, alternating
     diagonals, counter-clockwise seen from above) with smooth random bumps of about amp m on a
     bowl: the shape dict of a BvhTriangleMeshShape."""
@@ -933,7 +933,7 @@ def terrain_mesh(nx=24, nz=24, size=24.0, amp=1.2, seed=0, margin=0.0):
         kx, kz, ph = rng.uniform(0.1, 0.5), rng.uniform(0.1, 0.5), rng.uniform(0, 2 * np.pi)
         H += amp / 3 * np.sin(kx * X + ph) * np.cos(kz * Z - ph)
     H += rng.uniform(-0.05, 0.05, H.shape)
-    H += 0.4 * (X * X + Z * Z) / size      # a bowl, so that what lands stays on the mesh
+    H += bowl * (X * X + Z * Z) / size     # a bowl (edges bowl * size / 2 higher), so that what lands stays on it
     verts = np.stack([X, H, Z], -1).reshape(-1, 3).astype(F)
     idx = []
     for i in range(nx):
@@ -1021,12 +1021,12 @@ def _compound_kinds(rng, n):
     return out
 
 
-def terrain(n=60, seed=0, cells=16, size=16.0, compounds=0, steps=200, region=(10.0, 6.0, 10.0), y0=4.0):
+def terrain(n=60, seed=0, cells=16, size=16.0, compounds=0, steps=200, region=(10.0, 6.0, 10.0), y0=4.0, bowl=0.4):
     """Convex bodies (boxes, spheres, capsules, hulls; density 1000) and optionally compound bodies
     dropped on a static triangle-mesh terrain (a BvhTriangleMeshShape heightfield of cells x cells
     quads over size x size m); no plane; 10 iterations, dt 1/60."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    shapes = [terrain_mesh(cells, cells, size, seed=seed)]
+    shapes = [terrain_mesh(cells, cells, size, seed=seed, bowl=bowl)]
     kinds = _convex_kinds(rng, n) + _compound_kinds(rng, compounds)
     order = rng.permutation(len(kinds))
     kinds = [kinds[i] for i in order]
@@ -1087,4 +1087,8 @@ SCENES = {
     "ccd_shots": ccd_shots,
     "terrain": terrain,
     "compounds": compounds,
+    # 20,000 convex and 2,000 compound bodies dropped on a 128 x 128-cell terrain (32,768
+    # triangles) over 200 x 200 m
+    "terrain_20k": lambda seed=0: terrain(20000, seed=seed, cells=128, size=200.0, compounds=2000, steps=300,
+                                          region=(180.0, 40.0, 180.0), y0=6.0, bowl=0.02),
 }

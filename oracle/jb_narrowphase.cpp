@@ -1172,6 +1172,68 @@ static void ray_plane(const Shape& sh, const Xf& t, int body, V3 fromW, V3 toW, 
     ray_triangle(tri, from, to, hitFraction, body, t, cb);
 }
 
+// rayTestSingle's BvhTriangleMeshShape branch (CollisionWorld.java:297-311): the ray in the mesh's
+// space, BvhTriangleMeshShape.performRaycast -> OptimizedBvh.reportRayOverlappingNodex ->
+// walkStacklessQuantizedTreeAgainstRay (OptimizedBvh.java:817-938, 999-1015): a node is entered
+// when its quantized box overlaps the ray's quantized box and AabbUtil2.rayAabb (bound 1) accepts
+// its unquantized box; each leaf entered is tested by TriangleRaycastCallback.
+static void ray_mesh(const Shape& sh, const Xf& t, int body, V3 fromW, V3 toW, RayCallback& cb) {
+    Xf inv = xf_inverse(t);
+    V3 from = xf_apply(inv, fromW), to = xf_apply(inv, toW);
+    float hitFraction = cb.closest;
+    const QuantizedBvh& q = sh.mesh->bvh;
+    const V3 zero = v3(0, 0, 0);
+    V3 amin = v3(jmin(from.x, to.x), jmin(from.y, to.y), jmin(from.z, to.z));
+    V3 amax = v3(jmax(from.x, to.x), jmax(from.y, to.y), jmax(from.z, to.z));
+    amin = add(amin, zero);
+    amax = add(amax, zero);
+    auto quant = [&](V3 p, int o[3]) {   // quantizeWithClamp
+        V3 c = v3(jmax(p.x, q.bvhAabbMin.x), jmax(p.y, q.bvhAabbMin.y), jmax(p.z, q.bvhAabbMin.z));
+        c = v3(jmin(c.x, q.bvhAabbMax.x), jmin(c.y, q.bvhAabbMax.y), jmin(c.z, q.bvhAabbMax.z));
+        V3 v = mulc(sub(c, q.bvhAabbMin), q.bvhQuantization);
+        o[0] = (int)(v.x + 0.5f) & 0xFFFF;
+        o[1] = (int)(v.y + 0.5f) & 0xFFFF;
+        o[2] = (int)(v.z + 0.5f) & 0xFFFF;
+    };
+    auto unquant = [&](const uint16_t* n) {
+        V3 v = v3((float)n[0] / q.bvhQuantization.x, (float)n[1] / q.bvhQuantization.y, (float)n[2] / q.bvhQuantization.z);
+        return add(v, q.bvhAabbMin);
+    };
+    int qa[3], qb[3];
+    quant(amin, qa);
+    quant(amax, qb);
+    int cur = 0;
+    while (cur < q.curNodeIndex) {
+        const uint16_t* n = &q.q[6 * cur];
+        bool boxOv = !(qa[0] > n[3] || qb[0] < n[0]) && !(qa[2] > n[5] || qb[2] < n[2]) && !(qa[1] > n[4] || qb[1] < n[1]);
+        bool leaf = q.escOrTri[cur] >= 0;
+        bool rayOv = false;
+        if (boxOv) {
+            V3 b0 = add(unquant(n), zero), b1 = add(unquant(n + 3), zero);
+            float param = 1.0f;
+            rayOv = ray_aabb(from, to, b0, b1, param);
+        }
+        if (leaf && rayOv) {
+            int tri = q.escOrTri[cur] & ((1 << 21) - 1);
+            V3 tv[3] = {sh.mesh->tri[3 * tri], sh.mesh->tri[3 * tri + 1], sh.mesh->tri[3 * tri + 2]};
+            ray_triangle(tv, from, to, hitFraction, body, t, cb);
+        }
+        if (rayOv || leaf) cur++;
+        else cur += -q.escOrTri[cur];
+    }
+}
+
+// rayTestSingle's convex branch (CollisionWorld.java:267-293) on one convex shape at t.
+static void ray_convex(const Shape& sh, const Xf& t, int body, V3 from, V3 to, RayCallback& cb) {
+    float f;
+    V3 n;
+    if (subsimplex_ray(sh, t, from, to, f, n) && len2(n) > 0.0001f && f < cb.closest) {
+        cb.closest = f;
+        cb.body = body;
+        cb.normal = nor(mulMv(n, m3_identity()));   // rotated by the ray's (identity) basis
+    }
+}
+
 RayResult ray_test(const World& w, V3 from, V3 to, int group, int mask, int world) {
     RayCallback cb;
     for (size_t i = 0; i < w.bodies.size(); i++) {
@@ -1185,13 +1247,12 @@ RayResult ray_test(const World& w, V3 from, V3 to, int group, int mask, int worl
         float param = cb.closest;
         if (!ray_aabb(from, to, mn, mx, param)) continue;
         if (sh.isConvex()) {
-            float f;
-            V3 n;
-            if (subsimplex_ray(sh, b.xf, from, to, f, n) && len2(n) > 0.0001f && f < cb.closest) {
-                cb.closest = f;
-                cb.body = (int)i;
-                cb.normal = nor(mulMv(n, m3_identity()));   // rotated by the ray's (identity) basis
-            }
+            ray_convex(sh, b.xf, (int)i, from, to, cb);
+        } else if (sh.type == TRIANGLE_MESH) {
+            ray_mesh(sh, b.xf, (int)i, from, to, cb);
+        } else if (sh.isCompound()) {   // rayTestSingle's compound branch (CollisionWorld.java:340-355)
+            for (size_t c = 0; c < sh.children.size(); c++)
+                ray_convex(sh.children[c], xf_mul(b.xf, sh.childXf[c]), (int)i, from, to, cb);
         } else {
             ray_plane(sh, b.xf, (int)i, from, to, cb);
         }
@@ -1308,15 +1369,22 @@ RayResult convex_sweep(const World& w, const Shape& cast, const Xf& from, const 
         mx = add(mx, cmax);
         float param = 1.0f;
         if (!ray_aabb(from.o, to.o, mn, mx, param)) continue;
-        if (!sh.isConvex()) { *planeHit = true; return res; }
-        float f;
-        V3 n, p;
-        if (gjk_convex_cast(cast, from, to, sh, b.xf, 0.04f, f, n, p) && len2(n) > 0.0001f && f < closest) {
-            closest = f;
-            res.body = (int)i;
-            res.fraction = f;
-            res.normal = nor(n);
-            res.point = p;
+        if (!sh.isConvex() && !sh.isCompound()) { *planeHit = true; return res; }
+        // objectQuerySingle's convex branch, or its compound branch over the children at the
+        // body's transform times the child's (CollisionWorld.java:391-430, 491-510)
+        const int nc = sh.isCompound() ? (int)sh.children.size() : 1;
+        for (int c = 0; c < nc; c++) {
+            const Shape& cs = sh.isCompound() ? sh.children[c] : sh;
+            const Xf cx = sh.isCompound() ? xf_mul(b.xf, sh.childXf[c]) : b.xf;
+            float f;
+            V3 n, p;
+            if (gjk_convex_cast(cast, from, to, cs, cx, 0.04f, f, n, p) && len2(n) > 0.0001f && f < closest) {
+                closest = f;
+                res.body = (int)i;
+                res.fraction = f;
+                res.normal = nor(n);
+                res.point = p;
+            }
         }
     }
     return res;
@@ -1353,12 +1421,17 @@ bool ccd_sweep(const World& w, int me, const Xf& to, float& fraction, bool* plan
         if ((int)i == me || b.world != mb.world) continue;
         if (((b.group & mb.mask) & 0xFFFF) == 0 || ((mb.group & b.mask) & 0xFFFF) == 0) continue;
         if (mb.hasContactResponse() && b.hasContactResponse() && me < (int)i) {
-            const uint64_t key = pair_key(w, me, (int)i);
-            auto it = std::lower_bound(w.pairKeys.begin(), w.pairKeys.end(), key);
-            if (it != w.pairKeys.end() && *it == key) {
-                const size_t k = (size_t)(it - w.pairKeys.begin());
-                if (w.pairHasAlgo[k] && w.pairMf[k].n > 0) continue;
+            // the pair's algorithm's manifolds (getAllContactManifolds): one per child combination
+            bool touching = false;
+            for (int sub = 0, ns = pair_subs(w, me, (int)i); sub < ns && !touching; sub++) {
+                const uint64_t key = pair_key(w, me, (int)i) | ((uint64_t)sub << 24);
+                auto it = std::lower_bound(w.pairKeys.begin(), w.pairKeys.end(), key);
+                if (it != w.pairKeys.end() && *it == key) {
+                    const size_t k = (size_t)(it - w.pairKeys.begin());
+                    touching = w.pairHasAlgo[k] && w.pairMf[k].n > 0;
+                }
             }
+            if (touching) continue;
         }
         const Shape& sh = w.shapes[b.shape];
         V3 mn, mx;
@@ -1367,13 +1440,18 @@ bool ccd_sweep(const World& w, int me, const Xf& to, float& fraction, bool* plan
         mx = add(mx, cmax);
         float param = 1.0f;
         if (!ray_aabb(from.o, to.o, mn, mx, param)) continue;
-        if (!sh.isConvex()) { *planeHit = true; continue; }
-        float f;
-        V3 n, p;
-        if (gjk_convex_cast(cast, from, to, sh, b.xf, 0.04f, f, n, p) && len2(n) > 0.0001f && f < closest) {
-            if (dot(nor(n), motion) >= -0.0f) continue;   // moving away from the contact normal
-            closest = f;
-            hit = true;
+        if (!sh.isConvex() && !sh.isCompound()) { *planeHit = true; continue; }
+        const int nc = sh.isCompound() ? (int)sh.children.size() : 1;
+        for (int c = 0; c < nc; c++) {
+            const Shape& cs = sh.isCompound() ? sh.children[c] : sh;
+            const Xf cx = sh.isCompound() ? xf_mul(b.xf, sh.childXf[c]) : b.xf;
+            float f;
+            V3 n, p;
+            if (gjk_convex_cast(cast, from, to, cs, cx, 0.04f, f, n, p) && len2(n) > 0.0001f && f < closest) {
+                if (dot(nor(n), motion) >= -0.0f) continue;   // moving away from the contact normal
+                closest = f;
+                hit = true;
+            }
         }
     }
     fraction = closest;

@@ -60,10 +60,14 @@ int add_body(World& w, float mass, int shape, const Xf& xf, V3 inertia, float li
     return (int)w.bodies.size() - 1;
 }
 
-static bool is_plane(const World& w, int i) { return w.shapes[w.bodies[i].shape].type == STATIC_PLANE; }
+// Static planes and triangle meshes: paired by every other body of the world, which owns the key.
+static bool is_listed(const World& w, int i) {
+    const int t = w.shapes[w.bodies[i].shape].type;
+    return t == STATIC_PLANE || t == TRIANGLE_MESH;
+}
 
 uint64_t pair_key(const World& w, int a, int b) {
-    bool pa = is_plane(w, a), pb = is_plane(w, b);
+    bool pa = is_listed(w, a), pb = is_listed(w, b);
     int owner, partner;
     if (pa && !pb) { owner = b; partner = a; }
     else if (pb && !pa) { owner = a; partner = b; }
@@ -188,16 +192,16 @@ void stage_pairs(World& w) {
     const int n = (int)w.bodies.size();
     std::vector<uint64_t> keys;
     std::vector<int> planes, finite;
-    for (int i = 0; i < n; i++) (is_plane(w, i) ? planes : finite).push_back(i);
+    for (int i = 0; i < n; i++) (is_listed(w, i) ? planes : finite).push_back(i);
     if (w.bruteForcePairs) {   // SimpleBroadphase.calculateOverlappingPairs-style O(n^2) (SimpleBroadphase.java:87-110)
         for (int i = 0; i < n; i++)
             for (int j = i + 1; j < n; j++)
-                if (!(is_plane(w, i) && is_plane(w, j)) && aabb_overlap(w.bodies[i], w.bodies[j]) && filter_pass(w.bodies[i], w.bodies[j]))
+                if (!(is_listed(w, i) && is_listed(w, j)) && aabb_overlap(w.bodies[i], w.bodies[j]) && filter_pass(w.bodies[i], w.bodies[j]))
                     push_pair(w, keys, i, j);
     } else {
         for (int p : planes)
             for (int j = 0; j < n; j++)
-                if (j != p && !is_plane(w, j) && aabb_overlap(w.bodies[p], w.bodies[j]) && filter_pass(w.bodies[p], w.bodies[j]))
+                if (j != p && !is_listed(w, j) && aabb_overlap(w.bodies[p], w.bodies[j]) && filter_pass(w.bodies[p], w.bodies[j]))
                     push_pair(w, keys, p, j);
         if (!finite.empty()) {
             BTree t;

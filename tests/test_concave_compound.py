@@ -288,12 +288,15 @@ def test_f3_batched_worlds_equal_solo(gpu_lib):
 
 
 @pytest.mark.gpu
-def test_f3_queries_and_bodies_rejected(gpu_lib):
+def test_f3_mesh_sweeps_and_dynamic_meshes_rejected(gpu_lib):
     sc = scenes.terrain(6, compounds=2, seed=1)
     g = GpuWorld(sc)
     g.step(sc.dt)
-    with pytest.raises(jl.JbgpuError) as e:   # a ray straight down through the mesh
-        g.ray_test([[0.0, 20.0, 0.0]], [[0.0, -20.0, 0.0]])
+    cast = next(i for i, x in enumerate(sc.shapes) if x["type"] == _abi.SHAPE_SPHERE)
+    fr = scenes.xf12(None, (0.0, 20.0, 0.0))[None]
+    to = scenes.xf12(None, (0.0, -20.0, 0.0))[None]
+    with pytest.raises(jl.JbgpuError) as e:   # a convex sweep reaching the mesh
+        g.convex_sweep_test(cast, fr, to)
     assert e.value.code == _abi.ERR_UNSUPPORTED
     g.close()
     bad = scenes.terrain(2, seed=1)           # a dynamic triangle-mesh body
@@ -301,3 +304,176 @@ def test_f3_queries_and_bodies_rejected(gpu_lib):
     with pytest.raises(jl.JbgpuError) as e:
         GpuWorld(bad)
     assert e.value.code == _abi.ERR_INVALID_ARGUMENT
+
+
+def _same(a, b):
+    return np.array_equal(a.view(np.uint8).reshape(len(a), -1), b.view(np.uint8).reshape(len(b), -1))
+
+
+def _ray_tri(o, d, tri):
+    """Moller-Trumbore in float64: the ray parameter of a hit, or inf."""
+    e1, e2 = tri[1] - tri[0], tri[2] - tri[0]
+    p = np.cross(d, e2)
+    det = e1 @ p
+    if abs(det) < 1e-12:
+        return np.inf
+    t0 = o - tri[0]
+    u = (t0 @ p) / det
+    q = np.cross(t0, e1)
+    v = (d @ q) / det
+    t = (e2 @ q) / det
+    return t if (u >= 0 and v >= 0 and u + v <= 1 and 0 <= t <= 1) else np.inf
+
+
+def test_oracle_rays_hit_the_mesh_and_compound_children(oracle_lib):
+    sc = scenes.terrain(4, compounds=2, seed=3)
+    o = pyoracle.OracleWorld(sc)
+    tm = sc.shapes[0]
+    tris = np.asarray(tm["points"], np.float64)[np.asarray(tm["indices"])]
+    rng = np.random.Generator(np.random.PCG64(2))
+    frm = np.stack([rng.uniform(-7, 7, 64), np.full(64, 30.0), rng.uniform(-7, 7, 64)], 1).astype(F)
+    to = frm.copy()
+    to[:, 1] = -30.0
+    to[:, 0] += rng.uniform(-2, 2, 64).astype(F)
+    h = o.ray_test(frm, to)
+    ground = np.nonzero(h["body"] == 0)[0]
+    assert len(ground) > 40
+    for k in ground:
+        d = to[k].astype(np.float64) - frm[k]
+        want = min(_ray_tri(frm[k].astype(np.float64), d, t) for t in tris)
+        assert abs(h["fraction"][k] - want) < 1e-5
+        assert h["normal"][k][1] > 0
+    # a compound: rays at its body origin hit a child at most 0.01 before the child's surface
+    comp = [i for i in range(1, len(sc.bodies)) if sc.shapes[sc.bodies["shape"][i]]["type"] == _abi.SHAPE_COMPOUND]
+    for i in comp:
+        c = sc.bodies["transform"][i, 9:12]
+        r = o.ray_test((c + np.array([0, 10, 0], F))[None], (c - np.array([0, 10, 0], F))[None])
+        assert r["body"][0] == i
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("steps", [0, 90])
+def test_f3_rays_bit_exact(gpu_lib, oracle_lib, steps):
+    sc = scenes.terrain(40, compounds=16, seed=6)
+    g = GpuWorld(sc)
+    for _ in range(steps):
+        g.step(sc.dt)
+    o = pyoracle.OracleWorld(sc)
+    H.copy_world(g, o, manifolds=False)
+    rng = np.random.Generator(np.random.PCG64(8))
+    n = 4096
+    frm = rng.uniform(-8, 8, (n, 3)).astype(F)
+    frm[:, 1] = rng.uniform(-1, 12, n)
+    to = rng.uniform(-8, 8, (n, 3)).astype(F)
+    to[:, 1] = rng.uniform(-3, 12, n)
+    to[: n // 2, :] = frm[: n // 2]
+    to[: n // 2, 1] = -3.0                     # half straight down
+    hg = g.ray_test(frm, to)
+    ho = o.ray_test(frm, to)
+    assert _same(ho, hg), np.nonzero(ho != hg)[0][:10]
+    kinds = np.array([sc.shapes[x]["type"] for x in sc.bodies["shape"]])
+    hit = hg["body"][hg["body"] >= 0]
+    assert (kinds[hit] == _abi.SHAPE_TRIANGLE_MESH).sum() > 500
+    assert (kinds[hit] == _abi.SHAPE_COMPOUND).sum() > 20
+    g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("steps", [0, 60])
+def test_f3_sweeps_bit_exact_on_compounds(gpu_lib, oracle_lib, steps):
+    sc = scenes.compounds(30, 12, seed=7)
+    g = GpuWorld(sc)
+    for _ in range(steps):
+        g.step(sc.dt)
+    o = pyoracle.OracleWorld(sc)
+    H.copy_world(g, o, manifolds=False)
+    rng = np.random.Generator(np.random.PCG64(4))
+    casts = [i for i, x in enumerate(sc.shapes) if x["type"] in (_abi.SHAPE_BOX, _abi.SHAPE_SPHERE, _abi.SHAPE_CAPSULE,
+                                                                   _abi.SHAPE_CONVEX_HULL)][:4]
+    kinds = np.array([sc.shapes[x]["type"] for x in sc.bodies["shape"]])
+    on_compounds = 0
+    for shape in casts:
+        m = 256
+        a = rng.uniform(-4, 4, (m, 3)).astype(F)
+        a[:, 1] = rng.uniform(0.2, 8, m)
+        b = rng.uniform(-4, 4, (m, 3)).astype(F)
+        b[:, 1] = rng.uniform(0.2, 8, m)
+        R = scenes.random_rotations(rng, m)
+        fr = np.concatenate([R.reshape(m, 9), a], 1).astype(F)
+        to = np.concatenate([R.reshape(m, 9), b], 1).astype(F)
+        hg = g.convex_sweep_test(shape, fr, to, mask=~2)
+        ho, planes = o.convex_sweep(shape, fr, to, mask=~2)
+        assert planes == 0 and _same(ho, hg), (shape, np.nonzero(ho != hg)[0][:10])
+        on_compounds += (kinds[hg["body"][hg["body"] >= 0]] == _abi.SHAPE_COMPOUND).sum()
+    assert on_compounds > 50
+    g.close()
+
+
+@pytest.mark.gpu
+def test_f3_ccd_with_compounds_closed_loop_bit_exact(gpu_lib, oracle_lib):
+    """CCD motion clamping where the swept bodies meet compound bodies (the sweep's compound branch);
+    fast compound bodies move unclamped, as integrateTransforms sweeps convex bodies only
+    (DiscreteDynamicsWorld.java:700-729)."""
+    sc = scenes.compounds(20, 10, seed=9, region=(3.0, 4.0, 3.0), y0=0.5)
+    # a static box for ground (a CCD sweep reaching a static plane is where the reference throws)
+    sc.shapes[0] = {"type": _abi.SHAPE_BOX, "params": (20.0, 0.5, 20.0, 0.0), "points": None}
+    sc.bodies["transform"][0, 9:12] = (0.0, -0.5, 0.0)
+    sc.bodies["linear_velocity"][1::3] = (0.0, -25.0, 0.0)
+    sc.meta["ccd"] = {"bodies": list(range(1, len(sc.bodies))), "threshold": 0.05, "radius": 0.1}
+    o = pyoracle.OracleWorld(sc)
+    g = GpuWorld(sc)
+    clamped = 0
+    for s in range(90):
+        o.step(sc.dt)
+        g.step(sc.dt)
+        clamped += g.counters()["ccd_clamped"]
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            assert not bs, (s, bs)
+    assert not H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+    assert clamped > 0
+    g.close()
+
+
+@pytest.mark.gpu
+def test_mirror_compound_on_mesh_reads_like_the_reference(gpu_lib, oracle_lib):
+    """The reference's usage through the Python mirror: a BvhTriangleMeshShape ground over a
+    TriangleIndexVertexArray, CompoundShape dumbbells built with addChildShape and a box; two
+    seconds of stepSimulation.  The same world given to the oracle ends bit-identical."""
+    from jbgpu import dynamics as D
+    tm = scenes.terrain_mesh(8, 8, 12.0, seed=4)
+    world = D.DiscreteDynamicsWorld()
+    world.setGravity((0.0, -9.81, 0.0))
+    ground_shape = D.BvhTriangleMeshShape(D.TriangleIndexVertexArray(tm["indices"], tm["points"]), True)
+    ground = D.RigidBody(D.RigidBodyConstructionInfo(0.0, None, ground_shape))
+    world.addRigidBody(ground)
+    bell = D.CompoundShape()
+    bell.addChildShape(D.Transform(origin=(-0.6, 0.0, 0.0)), D.SphereShape(0.3))
+    bell.addChildShape(D.Transform(origin=(0.6, 0.0, 0.0)), D.SphereShape(0.3))
+    bell.addChildShape(D.Transform(basis=scenes.rot_z(np.pi / 2)), D.CapsuleShape(0.1, 1.2))
+    box = D.BoxShape((0.4, 0.3, 0.2))
+    specs = [(bell, 2.0, (0.0, 4.0, 0.0)), (bell, 2.0, (0.5, 6.0, 0.3)), (box, 1.0, (-0.8, 5.0, -0.4))]
+    for shape, m, pos in specs:
+        info = D.RigidBodyConstructionInfo(m, None, shape, shape.calculateLocalInertia(m))
+        info.startWorldTransform = D.Transform(basis=scenes.rot_x(0.4), origin=pos)
+        world.addRigidBody(D.RigidBody(info))
+    for _ in range(120):
+        world.stepSimulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    g = world._g
+    # the same world on the oracle
+    b = scenes._bodies(4)
+    b["shape"] = [0, 1, 1, 2]
+    b["mass"] = [0.0, 2.0, 2.0, 1.0]
+    b["local_inertia"][1:3] = bell.calculateLocalInertia(2.0)
+    b["local_inertia"][3] = box.calculateLocalInertia(1.0)
+    for k, (_, _, pos) in enumerate(specs):
+        b["transform"][k + 1] = scenes.xf12(scenes.rot_x(0.4), pos)
+    sc = scenes.Scene("mirror_f3", 1.0 / 60.0, 120, {"gravity": (0.0, -9.81, 0.0)},
+                      [ground_shape.desc(), bell.desc(), box.desc()], b)
+    o = pyoracle.OracleWorld(sc, config=_abi.default_config(gravity=(0.0, -9.81, 0.0)))
+    for _ in range(120):
+        o.step_simulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    assert not H.compare_state(o.get_state(), g.get_state())
+    assert not H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+    assert o.counters()["contacts"] > 0
+    world.close()
