@@ -16,8 +16,7 @@ enum { ACTIVE_TAG = 1, ISLAND_SLEEPING = 2, WANTS_DEACTIVATION = 3, DISABLE_DEAC
 // its world's list by every other body of the world (a plane's box is infinite, a terrain's spans
 // the world: either would make one tree leaf own and walk to all pairs).
 enum { CF_STATIC = 1, CF_KINEMATIC = 2, CF_NO_CONTACT_RESPONSE = 4, CF_LISTED = 64 };
-enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8, ST_BAD_WORLD = 16, ST_CCD_PLANE = 32,
-       ST_QUERY_SHAPE = 64 };
+enum { ST_CAPACITY = 1, ST_EPA_POOL = 2, ST_TIMEOUT = 4, ST_NONFINITE = 8, ST_BAD_WORLD = 16, ST_CCD_PLANE = 32 };
 
 // Counters kept on the device (indices into DevWorld::ctr).
 enum {

@@ -181,25 +181,20 @@ JBD bool ray_compound(const DevShapes& sh, int s, const Xf& t, V from, V to, flo
     return hit;
 }
 
-// rayTestSingle's BvhTriangleMeshShape branch (CollisionWorld.java:297-311): the ray in the mesh's
-// space walked through the quantized tree as OptimizedBvh.walkStacklessQuantizedTreeAgainstRay
-// does (java:817-938: a node is entered when its quantized box overlaps the ray's quantized box
-// and AabbUtil2.rayAabb with the bound 1 accepts its unquantized box), each leaf entered tested by
-// TriangleRaycastCallback; the first smallest hit below 1, its normal times the mesh's basis.
-JBD bool ray_mesh(const DevShapes& sh, int s, const Xf& t, V from, V to, float& best, V& nrm) {
-    const Xf inv = xf_inverse(t);
-    const V lf = xf_apply(inv, from), lt = xf_apply(inv, to);
-    const V zero = mk(0.0f, 0.0f, 0.0f);
+// OptimizedBvh.walkStacklessQuantizedTreeAgainstRay (OptimizedBvh.java:817-938) in mesh shape s:
+// the ray lf -> lt in the mesh's space, widened by a box cast's extents bmin / bmax (zero for a
+// ray); a node is entered when its quantized box overlaps the query's quantized box and
+// AabbUtil2.rayAabb with the bound 1 accepts its unquantized, widened box.  visit(tri) is called
+// for every leaf entered, in walk order.
+template <class Visit>
+JBD void mesh_cast_walk(const DevShapes& sh, int s, V lf, V lt, V bmin, V bmax, Visit visit) {
     const float4* q = sh.mesh_q + 3 * s;
-    const V bmin = mk4(q[0]), bmax = mk4(q[1]), quant = mk4(q[2]);
+    const V qmin = mk4(q[0]), qmax = mk4(q[1]), quant = mk4(q[2]);
     int qa[3], qb[3];
-    mesh_quantize(add(mk(jmin(lf.x, lt.x), jmin(lf.y, lt.y), jmin(lf.z, lt.z)), zero), bmin, bmax, quant, qa);
-    mesh_quantize(add(mk(jmax(lf.x, lt.x), jmax(lf.y, lt.y), jmax(lf.z, lt.z)), zero), bmin, bmax, quant, qb);
+    mesh_quantize(add(mk(jmin(lf.x, lt.x), jmin(lf.y, lt.y), jmin(lf.z, lt.z)), bmin), qmin, qmax, quant, qa);
+    mesh_quantize(add(mk(jmax(lf.x, lt.x), jmax(lf.y, lt.y), jmax(lf.z, lt.z)), bmax), qmin, qmax, quant, qb);
     const int4* nodes = sh.mesh_nodes + sh.mesh_node_off[s];
-    const float4* tris = sh.mesh_tris + (size_t)3 * sh.mesh_tri_off[s];
     const int nn = sh.mesh_node_cnt[s];
-    best = 1.0f;
-    bool hit = false;
     for (int cur = 0; cur < nn;) {
         const int4 nd = nodes[cur];
         const int n0 = nd.x & 0xFFFF, n1 = (nd.x >> 16) & 0xFFFF, n2 = nd.y & 0xFFFF;
@@ -208,24 +203,109 @@ JBD bool ray_mesh(const DevShapes& sh, int s, const Xf& t, V from, V to, float& 
         const bool leaf = nd.w >= 0;
         bool rayOv = false;
         if (boxOv) {
-            const V b0 = add(add(mk(jdiv((float)n0, quant.x), jdiv((float)n1, quant.y), jdiv((float)n2, quant.z)), bmin), zero);
-            const V b1 = add(add(mk(jdiv((float)m0, quant.x), jdiv((float)m1, quant.y), jdiv((float)m2, quant.z)), bmin), zero);
+            const V b0 = add(add(mk(jdiv((float)n0, quant.x), jdiv((float)n1, quant.y), jdiv((float)n2, quant.z)), qmin), bmin);
+            const V b1 = add(add(mk(jdiv((float)m0, quant.x), jdiv((float)m1, quant.y), jdiv((float)m2, quant.z)), qmin), bmax);
             float enter, exit;
             rayOv = ray_aabb_parts(lf, lt, b0, b1, enter, exit) && enter <= jmin(1.0f, exit);
         }
-        if (leaf && rayOv) {
-            const float4* tv = tris + 3 * (nd.w & ((1 << 21) - 1));
-            float f;
-            V nl;
-            if (ray_triangle(mk4(tv[0]), mk4(tv[1]), mk4(tv[2]), lf, lt, best, f, nl)) {
-                best = f;
-                nrm = mulMv(nl, t.b);
-                hit = true;
-            }
-        }
+        if (leaf && rayOv) visit(nd.w & ((1 << 21) - 1));
         cur += (rayOv || leaf) ? 1 : max(1, -nd.w);
     }
+}
+
+// rayTestSingle's BvhTriangleMeshShape branch (CollisionWorld.java:297-311): the ray in the mesh's
+// space through the walk without extents (reportRayOverlappingNodex), TriangleRaycastCallback on
+// each leaf reached; the first smallest hit below 1, its normal times the mesh's basis.
+JBD bool ray_mesh(const DevShapes& sh, int s, const Xf& t, V from, V to, float& best, V& nrm) {
+    const Xf inv = xf_inverse(t);
+    const V lf = xf_apply(inv, from), lt = xf_apply(inv, to);
+    const V zero = mk(0.0f, 0.0f, 0.0f);
+    const float4* tris = sh.mesh_tris + (size_t)3 * sh.mesh_tri_off[s];
+    best = 1.0f;
+    bool hit = false;
+    mesh_cast_walk(sh, s, lf, lt, zero, zero, [&](int tri) {
+        const float4* tv = tris + 3 * tri;
+        float f;
+        V nl;
+        if (ray_triangle(mk4(tv[0]), mk4(tv[1]), mk4(tv[2]), lf, lt, best, f, nl)) {
+            best = f;
+            nrm = mulMv(nl, t.b);
+            hit = true;
+        }
+    });
     return hit;
+}
+
+// SubsimplexConvexCast.calcTimeOfImpact (collision/narrowphase/SubsimplexConvexCast.java:62-191)
+// for A moving from fromA to the origin toA (A's basis kept), B at rest at tB, allowedPenetration
+// 0: the fraction, the unit normal and B's closest point (compute_points).
+JBD bool subsimplex_cast(const ShapeRef& sa, const Xf& fromA, V toA, const ShapeRef& sb, const Xf& tB, float& fraction,
+                         V& normal, V& hitPoint) {
+    Simplex s;
+    sx_reset(s);
+    const V zero = mk(0.0f, 0.0f, 0.0f);
+    Xf iA = fromA, iB = tB;
+    const V r = sub(sub(toA, fromA.o), sub(tB.o, tB.o));
+    V supA = xf_apply(fromA, support_with_margin(sa, mulMTv(scl(r, -1.0f), fromA.b)));
+    V supB = xf_apply(tB, support_with_margin(sb, mulMTv(r, tB.b)));
+    V v = sub(supA, supB);
+    float lambda = 0.0f;
+    int maxIter = 32;
+    V n = zero;
+    float dist2 = len2(v);
+    while ((dist2 > 0.0001f) && (maxIter--) != 0) {
+        supA = xf_apply(iA, support_with_margin(sa, mulMTv(scl(v, -1.0f), iA.b)));
+        supB = xf_apply(iB, support_with_margin(sb, mulMTv(v, iB.b)));
+        V w = sub(supA, supB);
+        const float VdotW = dot(v, w);
+        if (lambda > 1.0f) return false;
+        if (VdotW > 0.0f) {
+            const float VdotR = dot(v, r);
+            if (VdotR >= -__fmul_rn(FLT_EPS, FLT_EPS)) return false;
+            lambda = __fsub_rn(lambda, jdiv(VdotW, VdotR));
+            iA.o = interp3(fromA.o, toA, lambda);
+            iB.o = interp3(tB.o, tB.o, lambda);
+            w = sub(supA, supB);
+            n = v;
+        }
+        s.lastW = w;                                 // addVertex
+        s.needsUpdate = true;
+        s.W[s.nv] = w; s.P[s.nv] = supA; s.Q[s.nv] = supB;
+        s.nv++;
+        const bool ok = sx_update(s);                // closest(v)
+        v = s.cV;
+        dist2 = ok ? len2(v) : 0.0f;
+    }
+    fraction = lambda;
+    normal = len2(n) >= __fmul_rn(FLT_EPS, FLT_EPS) ? nor(n) : zero;
+    if (dot(normal, r) >= -0.0f) return false;
+    sx_update(s);
+    hitPoint = s.cP2;
+    return true;
+}
+
+// objectQuerySingle's BvhTriangleMeshShape branch (CollisionWorld.java:425-455) for one mesh object
+// at tM: the cast's origins in the mesh's space, widened by the cast shape's box (cbmin / cbmax: its
+// aabb at the mesh-space rotation of its end transform), walked through the tree
+// (reportBoxCastOverlappingNodex); each triangle reached is cast against by
+// TriangleConvexcastCallback (SubsimplexConvexCast, |n|^2 > 1e-4) and accept(f, n, p) is offered
+// every hit below 1 whose fraction is <= the last accepted one (BridgeTriangleConvexcastCallback.
+// reportHit), in walk order; n is the cast's unit normal, which processTriangle normalises once
+// more before reporting it (the caller does).
+template <class Accept>
+JBD void sweep_mesh(const DevShapes& sh, int s, const Xf& tM, const ShapeRef& cast, const Xf& from, V to, V cbmin,
+                    V cbmax, Accept accept) {
+    const Xf inv = xf_inverse(tM);
+    const V lf = xf_apply(inv, from.o), lt = xf_apply(inv, to);
+    float closest = 1.0f;
+    mesh_cast_walk(sh, s, lf, lt, cbmin, cbmax, [&](int tri) {
+        const ShapeRef tr = triangle_ref(sh, s, tri);
+        float f;
+        V n, p;
+        if (!subsimplex_cast(cast, from, to, tr, tM, f, n, p)) return;
+        if (!(len2(n) > 0.0001f) || !(f < 1.0f)) return;
+        if (f <= closest && accept(f, n, p)) closest = f;
+    });
 }
 
 // One object's part of rayTest with every hit below 1 (the bound of any closest fraction):
@@ -867,13 +947,25 @@ __global__ void __launch_bounds__(RAY_THREADS) k_sweep_cast(DevWorld w, const Ra
         atomicOr(planeHit + c.ray, 1);
         return;
     }
-    if (w.sh.type[bs] == SHAPE_MESH) {   // not handled: reported
-        atomicOr(&w.ctr[C_STATUS], ST_QUERY_SHAPE);
-        return;
-    }
     const Xf fa = xf12(from + 12 * c.ray);
     const V ta = mk(to[12 * c.ray + 9], to[12 * c.ray + 10], to[12 * c.ray + 11]);
     const Xf tb = load_xf(w, c.body);
+    if (w.sh.type[bs] == SHAPE_MESH) {   // objectQuerySingle's BvhTriangleMeshShape branch
+        Xf rot;
+        rot.b = mulMM(xf_inverse(tb).b, xf12(to + 12 * c.ray).b);   // the end rotation in the mesh's space
+        rot.o = mk(0.0f, 0.0f, 0.0f);
+        V cbmin, cbmax;
+        shape_aabb(w.sh, shape, rot, cbmin, cbmax);
+        float best = 1.0f;
+        sweep_mesh(w.sh, bs, tb, shape_ref(w.sh, shape), fa, ta, cbmin, cbmax, [&](float f, V n, V p) {
+            best = f;                        // ClosestConvexResultCallback.addSingleResult
+            hitA[i] = f4(n, f);              // k_sweep_pick applies processTriangle's normalisation
+            hitB[i] = f4(p, 0.0f);
+            return true;
+        });
+        if (best < 1.0f) atomicMin(key + c.ray, hit_key(best, c.body, 0));
+        return;
+    }
     // objectQuerySingle's convex branch, or its compound branch over the children at the body's
     // transform times the child's (CollisionWorld.java:391-430, 491-510): the first smallest hit
     const bool compound = w.sh.type[bs] == SHAPE_COMPOUND;
@@ -1142,8 +1234,12 @@ __global__ void __launch_bounds__(256) k_ccd_sweep(DevWorld w, DevPairs P, int n
                 continue;
             }
             const int sj = w.shape[j];
-            if (w.sh.type[sj] == SHAPE_MESH) {
-                atomicOr(&w.ctr[C_STATUS], ST_QUERY_SHAPE);   // not handled: reported
+            if (w.sh.type[sj] == SHAPE_MESH) {   // the mesh branch; the sphere's box is -r .. r at any rotation
+                sweep_mesh(w.sh, sj, tj, cast, from, to.o, mk(-r, -r, -r), mk(r, r, r), [&](float f, V n, V) {
+                    if (dot(nor(n), motion) >= -0.0f) return false;   // ClosestNotMeConvexResultCallback rejects
+                    atomicMin(&sBest, __float_as_uint(f));
+                    return true;
+                });
                 continue;
             }
             const bool compound = w.sh.type[sj] == SHAPE_COMPOUND;   // the compound branch: every child

@@ -415,9 +415,6 @@ int check_status(jbgpu_world* w) {
     if (st & ST_CCD_PLANE)
         return fail(JBGPU_ERR_UNSUPPORTED, "a CCD sweep reached a static plane, where the reference throws "
                                            "(CollisionWorld.objectQuerySingle's concave branch)");
-    if (st & ST_QUERY_SHAPE)
-        return fail(JBGPU_ERR_UNSUPPORTED, "a ray, sweep or CCD sweep reached a compound or triangle-mesh body, "
-                                           "which these queries do not handle");
     return JBGPU_OK;
 }
 

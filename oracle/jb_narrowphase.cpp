@@ -1172,21 +1172,17 @@ static void ray_plane(const Shape& sh, const Xf& t, int body, V3 fromW, V3 toW, 
     ray_triangle(tri, from, to, hitFraction, body, t, cb);
 }
 
-// rayTestSingle's BvhTriangleMeshShape branch (CollisionWorld.java:297-311): the ray in the mesh's
-// space, BvhTriangleMeshShape.performRaycast -> OptimizedBvh.reportRayOverlappingNodex ->
-// walkStacklessQuantizedTreeAgainstRay (OptimizedBvh.java:817-938, 999-1015): a node is entered
-// when its quantized box overlaps the ray's quantized box and AabbUtil2.rayAabb (bound 1) accepts
-// its unquantized box; each leaf entered is tested by TriangleRaycastCallback.
-static void ray_mesh(const Shape& sh, const Xf& t, int body, V3 fromW, V3 toW, RayCallback& cb) {
-    Xf inv = xf_inverse(t);
-    V3 from = xf_apply(inv, fromW), to = xf_apply(inv, toW);
-    float hitFraction = cb.closest;
-    const QuantizedBvh& q = sh.mesh->bvh;
-    const V3 zero = v3(0, 0, 0);
+// OptimizedBvh.walkStacklessQuantizedTreeAgainstRay (OptimizedBvh.java:817-938): the leaves a ray
+// (or a box cast: the box's extents aabbMin / aabbMax added to the ray's box and to every node's
+// box) reaches, in walk order.  A node is entered when its quantized box overlaps the query's
+// quantized box and AabbUtil2.rayAabb (bound 1) accepts its unquantized, widened box.
+static void mesh_cast_walk(const MeshData& m, V3 from, V3 to, V3 bmin, V3 bmax, std::vector<int>& out) {
+    out.clear();
+    const QuantizedBvh& q = m.bvh;
     V3 amin = v3(jmin(from.x, to.x), jmin(from.y, to.y), jmin(from.z, to.z));
     V3 amax = v3(jmax(from.x, to.x), jmax(from.y, to.y), jmax(from.z, to.z));
-    amin = add(amin, zero);
-    amax = add(amax, zero);
+    amin = add(amin, bmin);
+    amax = add(amax, bmax);
     auto quant = [&](V3 p, int o[3]) {   // quantizeWithClamp
         V3 c = v3(jmax(p.x, q.bvhAabbMin.x), jmax(p.y, q.bvhAabbMin.y), jmax(p.z, q.bvhAabbMin.z));
         c = v3(jmin(c.x, q.bvhAabbMax.x), jmin(c.y, q.bvhAabbMax.y), jmin(c.z, q.bvhAabbMax.z));
@@ -1209,17 +1205,28 @@ static void ray_mesh(const Shape& sh, const Xf& t, int body, V3 fromW, V3 toW, R
         bool leaf = q.escOrTri[cur] >= 0;
         bool rayOv = false;
         if (boxOv) {
-            V3 b0 = add(unquant(n), zero), b1 = add(unquant(n + 3), zero);
+            V3 b0 = add(unquant(n), bmin), b1 = add(unquant(n + 3), bmax);
             float param = 1.0f;
             rayOv = ray_aabb(from, to, b0, b1, param);
         }
-        if (leaf && rayOv) {
-            int tri = q.escOrTri[cur] & ((1 << 21) - 1);
-            V3 tv[3] = {sh.mesh->tri[3 * tri], sh.mesh->tri[3 * tri + 1], sh.mesh->tri[3 * tri + 2]};
-            ray_triangle(tv, from, to, hitFraction, body, t, cb);
-        }
+        if (leaf && rayOv) out.push_back(q.escOrTri[cur] & ((1 << 21) - 1));
         if (rayOv || leaf) cur++;
         else cur += -q.escOrTri[cur];
+    }
+}
+
+// rayTestSingle's BvhTriangleMeshShape branch (CollisionWorld.java:297-311): the ray in the mesh's
+// space, BvhTriangleMeshShape.performRaycast -> OptimizedBvh.reportRayOverlappingNodex (no box
+// extents, java:999-1015), each leaf reached tested by TriangleRaycastCallback.
+static void ray_mesh(const Shape& sh, const Xf& t, int body, V3 fromW, V3 toW, RayCallback& cb) {
+    Xf inv = xf_inverse(t);
+    V3 from = xf_apply(inv, fromW), to = xf_apply(inv, toW);
+    float hitFraction = cb.closest;
+    std::vector<int> tris;
+    mesh_cast_walk(*sh.mesh, from, to, v3(0, 0, 0), v3(0, 0, 0), tris);
+    for (int tri : tris) {
+        V3 tv[3] = {sh.mesh->tri[3 * tri], sh.mesh->tri[3 * tri + 1], sh.mesh->tri[3 * tri + 2]};
+        ray_triangle(tv, from, to, hitFraction, body, t, cb);
     }
 }
 
@@ -1347,6 +1354,88 @@ static bool gjk_convex_cast(const Shape& sa, const Xf& fromA, const Xf& toA, con
 // the origins with the bound 1 (not the closest hit so far), then GjkConvexCast.  A static plane
 // reached by the sweep makes the reference throw (its plane branch calls a caster that is null):
 // *planeHit is set and the result is that of the objects before it.
+// SubsimplexConvexCast.calcTimeOfImpact (collision/narrowphase/SubsimplexConvexCast.java:62-191)
+// for A moving from fromA to toA (origins interpolated, A's basis kept), B at rest at tB,
+// allowedPenetration 0 (a fresh CastResult): the fraction, the unit normal and B's closest point.
+static bool subsimplex_cast(const Shape& sa, const Xf& fromA, const Xf& toA, const Shape& sb, const Xf& tB,
+                            float& fraction, V3& normal, V3& hitPoint) {
+    VoronoiSimplex s;
+    s.reset();
+    const V3 zero = v3(0.0f, 0.0f, 0.0f);
+    V3 linVelA = sub(toA.o, fromA.o), linVelB = sub(tB.o, tB.o);
+    float lambda = 0.0f;
+    Xf iA = fromA, iB = tB;
+    V3 r = sub(linVelA, linVelB);
+    V3 supA = xf_apply(fromA, support_with_margin(sa, mulMTv(scl(r, -1.0f), fromA.b)));
+    V3 supB = xf_apply(tB, support_with_margin(sb, mulMTv(r, tB.b)));
+    V3 v = sub(supA, supB);
+    int maxIter = 32;
+    V3 n = zero;
+    float dist2 = len2(v);
+    while ((dist2 > 0.0001f) && (maxIter--) != 0) {
+        supA = xf_apply(iA, support_with_margin(sa, mulMTv(scl(v, -1.0f), iA.b)));
+        supB = xf_apply(iB, support_with_margin(sb, mulMTv(v, iB.b)));
+        V3 w = sub(supA, supB);
+        float VdotW = dot(v, w);
+        if (lambda > 1.0f) return false;
+        if (VdotW > 0.0f) {
+            float VdotR = dot(v, r);
+            if (VdotR >= -(FLT_EPS * FLT_EPS)) return false;
+            lambda = lambda - VdotW / VdotR;
+            iA.o = interp3(fromA.o, toA.o, lambda);
+            iB.o = interp3(tB.o, tB.o, lambda);
+            w = sub(supA, supB);
+            n = v;
+        }
+        s.addVertex(w, supA, supB);
+        if (s.closest(v)) dist2 = len2(v);
+        else dist2 = 0.0f;
+    }
+    fraction = lambda;
+    normal = len2(n) >= FLT_EPS * FLT_EPS ? nor(n) : zero;
+    if (dot(normal, r) >= -0.0f) return false;
+    V3 hA, hB;
+    s.compute_points(hA, hB);
+    hitPoint = hB;
+    return true;
+}
+
+// objectQuerySingle's BvhTriangleMeshShape branch (CollisionWorld.java:425-455): the cast's
+// origins in the mesh's space and its shape's aabb at the mesh-space rotation of its end
+// transform widen the ray of BvhTriangleMeshShape.performConvexcast
+// (OptimizedBvh.reportBoxCastOverlappingNodex, java:1017-1036); each triangle reached is cast
+// against by TriangleConvexcastCallback.processTriangle (TriangleConvexcastCallback.java:53-88:
+// SubsimplexConvexCast, the fraction below the callback's hitFraction - which it never lowers -,
+// the normal normalised once more) and reported through BridgeTriangleConvexcastCallback.reportHit
+// (CollisionWorld.java:840-851: accepted when the fraction is <= the result callback's closest).
+// accept(f, n, p) stands for the result callback's addSingleResult and returns its closest.
+template <class Accept>
+static void sweep_mesh(const Shape& cast, const Xf& from, const Xf& to, const Shape& mesh, const Xf& tM, float closest,
+                       Accept accept) {
+    Xf inv = xf_inverse(tM);
+    V3 fromL = xf_apply(inv, from.o), toL = xf_apply(inv, to.o);
+    Xf rot;
+    rot.b = mulMM(inv.b, to.b);   // rotationXform.set(worldToObject.basis * convexToTrans.basis)
+    rot.o = v3(0.0f, 0.0f, 0.0f);
+    V3 bmin, bmax;
+    shape_aabb(cast, rot, bmin, bmax);
+    std::vector<int> tris;
+    mesh_cast_walk(*mesh.mesh, fromL, toL, bmin, bmax, tris);
+    const float hitFraction = closest;
+    Shape tm;
+    tm.type = TRIANGLE;
+    tm.collisionMargin = mesh.getMargin();
+    for (int t : tris) {
+        for (int k = 0; k < 3; k++) tm.tri[k] = mesh.mesh->tri[3 * t + k];
+        float f;
+        V3 n, p;
+        if (!subsimplex_cast(cast, from, to, tm, tM, f, n, p)) continue;
+        if (!(len2(n) > 0.0001f) || !(f < hitFraction)) continue;
+        n = nor(n);
+        if (f <= closest) closest = accept(f, n, p);
+    }
+}
+
 RayResult convex_sweep(const World& w, const Shape& cast, const Xf& from, const Xf& to, int group, int mask, int world,
                        bool* planeHit) {
     *planeHit = false;
@@ -1369,6 +1458,17 @@ RayResult convex_sweep(const World& w, const Shape& cast, const Xf& from, const 
         mx = add(mx, cmax);
         float param = 1.0f;
         if (!ray_aabb(from.o, to.o, mn, mx, param)) continue;
+        if (sh.type == TRIANGLE_MESH) {
+            sweep_mesh(cast, from, to, sh, b.xf, closest, [&](float f, V3 n, V3 p) {
+                closest = f;   // ClosestConvexResultCallback.addSingleResult
+                res.body = (int)i;
+                res.fraction = f;
+                res.normal = n;
+                res.point = p;
+                return closest;
+            });
+            continue;
+        }
         if (!sh.isConvex() && !sh.isCompound()) { *planeHit = true; return res; }
         // objectQuerySingle's convex branch, or its compound branch over the children at the
         // body's transform times the child's (CollisionWorld.java:391-430, 491-510)
@@ -1440,6 +1540,15 @@ bool ccd_sweep(const World& w, int me, const Xf& to, float& fraction, bool* plan
         mx = add(mx, cmax);
         float param = 1.0f;
         if (!ray_aabb(from.o, to.o, mn, mx, param)) continue;
+        if (sh.type == TRIANGLE_MESH) {
+            sweep_mesh(cast, from, to, sh, b.xf, closest, [&](float f, V3 n, V3) {
+                if (dot(n, motion) >= -0.0f) return closest;   // ClosestNotMeConvexResultCallback rejects
+                closest = f;
+                hit = true;
+                return closest;
+            });
+            continue;
+        }
         if (!sh.isConvex() && !sh.isCompound()) { *planeHit = true; continue; }
         const int nc = sh.isCompound() ? (int)sh.children.size() : 1;
         for (int c = 0; c < nc; c++) {

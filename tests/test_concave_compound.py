@@ -288,17 +288,7 @@ def test_f3_batched_worlds_equal_solo(gpu_lib):
 
 
 @pytest.mark.gpu
-def test_f3_mesh_sweeps_and_dynamic_meshes_rejected(gpu_lib):
-    sc = scenes.terrain(6, compounds=2, seed=1)
-    g = GpuWorld(sc)
-    g.step(sc.dt)
-    cast = next(i for i, x in enumerate(sc.shapes) if x["type"] == _abi.SHAPE_SPHERE)
-    fr = scenes.xf12(None, (0.0, 20.0, 0.0))[None]
-    to = scenes.xf12(None, (0.0, -20.0, 0.0))[None]
-    with pytest.raises(jl.JbgpuError) as e:   # a convex sweep reaching the mesh
-        g.convex_sweep_test(cast, fr, to)
-    assert e.value.code == _abi.ERR_UNSUPPORTED
-    g.close()
+def test_f3_dynamic_mesh_rejected(gpu_lib):
     bad = scenes.terrain(2, seed=1)           # a dynamic triangle-mesh body
     bad.bodies["mass"][0] = 1.0
     with pytest.raises(jl.JbgpuError) as e:
@@ -349,6 +339,99 @@ def test_oracle_rays_hit_the_mesh_and_compound_children(oracle_lib):
         c = sc.bodies["transform"][i, 9:12]
         r = o.ray_test((c + np.array([0, 10, 0], F))[None], (c - np.array([0, 10, 0], F))[None])
         assert r["body"][0] == i
+
+
+def _height(tm, x, z):
+    """The terrain surface's height under (x, z) (float64 barycentric over the cell's triangles)."""
+    tris = np.asarray(tm["points"], np.float64)[np.asarray(tm["indices"])]
+    for t in tris:
+        a, b, c = t[0][[0, 2]], t[1][[0, 2]], t[2][[0, 2]]
+        m = np.array([b - a, c - a]).T
+        if abs(np.linalg.det(m)) < 1e-12:
+            continue
+        u, v = np.linalg.solve(m, np.array([x, z]) - a)
+        if u >= -1e-9 and v >= -1e-9 and u + v <= 1 + 1e-9:
+            return t[0][1] + u * (t[1][1] - t[0][1]) + v * (t[2][1] - t[0][1])
+    return None
+
+
+def test_oracle_sweeps_hit_the_mesh(oracle_lib):
+    """A sphere of radius 0.3 swept straight down onto the terrain stops with its centre about 0.3
+    from the reported point, which lies on the mesh."""
+    sc = scenes.terrain(2, seed=3)
+    o = pyoracle.OracleWorld(sc)
+    tm = sc.shapes[0]
+    cast = next(i for i, x in enumerate(sc.shapes) if x["type"] == _abi.SHAPE_SPHERE)
+    r = sc.shapes[cast]["params"][0]
+    rng = np.random.Generator(np.random.PCG64(5))
+    m = 32
+    xz = rng.uniform(-6, 6, (m, 2)).astype(F)
+    fr = np.stack([scenes.xf12(None, (x, 30.0, z)) for x, z in xz])
+    to = np.stack([scenes.xf12(None, (x, -30.0, z)) for x, z in xz])
+    h, planes = o.convex_sweep(cast, fr, to)
+    assert planes == 0
+    ground = np.nonzero(h["body"] == 0)[0]    # the other sweeps meet one of the scene's two bodies
+    assert len(ground) >= m - 4
+    for k in ground:
+        c = fr[k, 9:12] + h["fraction"][k] * (to[k, 9:12] - fr[k, 9:12])
+        p = h["point"][k].astype(np.float64)
+        assert abs(np.linalg.norm(c - p) - r) < 0.02
+        y = _height(tm, p[0], p[2])
+        assert y is not None and abs(y - p[1]) < 1e-3
+        assert h["normal"][k][1] > 0.5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("steps", [0, 90])
+def test_f3_sweeps_bit_exact_on_the_mesh(gpu_lib, oracle_lib, steps):
+    sc = scenes.terrain(40, compounds=16, seed=6)
+    g = GpuWorld(sc)
+    for _ in range(steps):
+        g.step(sc.dt)
+    o = pyoracle.OracleWorld(sc)
+    H.copy_world(g, o, manifolds=False)
+    rng = np.random.Generator(np.random.PCG64(12))
+    casts = [i for i, x in enumerate(sc.shapes) if x["type"] in (_abi.SHAPE_BOX, _abi.SHAPE_SPHERE, _abi.SHAPE_CAPSULE,
+                                                                   _abi.SHAPE_CONVEX_HULL)][:4]
+    kinds = np.array([sc.shapes[x]["type"] for x in sc.bodies["shape"]])
+    on_mesh = 0
+    for shape in casts:
+        m = 256
+        a = rng.uniform(-7, 7, (m, 3)).astype(F)
+        a[:, 1] = rng.uniform(2, 10, m)
+        b = a + rng.uniform(-3, 3, (m, 3)).astype(F)
+        b[:, 1] = rng.uniform(-3, 4, m)
+        Ra, Rb = scenes.random_rotations(rng, m), scenes.random_rotations(rng, m)
+        fr = np.concatenate([Ra.reshape(m, 9), a], 1).astype(F)
+        to = np.concatenate([Rb.reshape(m, 9), b], 1).astype(F)
+        hg = g.convex_sweep_test(shape, fr, to)
+        ho, planes = o.convex_sweep(shape, fr, to)
+        assert planes == 0 and _same(ho, hg), (shape, np.nonzero(ho != hg)[0][:10])
+        on_mesh += (kinds[hg["body"][hg["body"] >= 0]] == _abi.SHAPE_TRIANGLE_MESH).sum()
+    assert on_mesh > 200
+    g.close()
+
+
+@pytest.mark.gpu
+def test_f3_ccd_on_the_mesh_closed_loop_bit_exact(gpu_lib, oracle_lib):
+    """CCD motion clamping of fast convex bodies onto the triangle-mesh terrain (the sweep's mesh
+    branch) and onto compound bodies."""
+    sc = scenes.terrain(30, compounds=6, seed=10)
+    sc.bodies["linear_velocity"][1::2] = (0.0, -40.0, 0.0)
+    sc.meta["ccd"] = {"bodies": list(range(1, len(sc.bodies))), "threshold": 0.05, "radius": 0.1}
+    o = pyoracle.OracleWorld(sc)
+    g = GpuWorld(sc)
+    clamped = 0
+    for s in range(90):
+        o.step(sc.dt)
+        g.step(sc.dt)
+        clamped += g.counters()["ccd_clamped"]
+        if s % 10 == 9 or s < 5:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            assert not bs, (s, bs)
+    assert not H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+    assert clamped > 0 and g.counters()["status_flags"] == 0
+    g.close()
 
 
 @pytest.mark.gpu
