@@ -7,11 +7,18 @@
 namespace jbg {
 using namespace jbd;
 
+// A manifold point as the narrowphase sees it.  The fields it reads or recomputes every step are
+// held here; the ones it only carries along (the lateral impulses, lateralFrictionInitialized and
+// the two friction directions, which the solver writes) stay in memory: src is the slot the point
+// came from in the stored manifold (-1 for a point added this step) and repl marks a point
+// replaced in place (replaceContactPoint keeps its lateral impulses and directions and clears
+// lateralFrictionInitialized), so that store_mf moves or resets them only when needed.
 struct MP {
     V la, lb, wa, wb, n;
-    float dist, fr, rest, ai, l1, l2, latInit;
+    float dist, fr, rest, ai;
     int life;
-    V d1, d2;
+    int src;
+    bool repl;
 };
 struct Mf {
     int n;
@@ -22,30 +29,44 @@ JBD void load_mf(const DevPairs& P, int pair, Mf& m) {
     m.n = P.n[pair];
     for (int j = 0; j < m.n; j++) {
         int k = pair * 4 + j;
-        float4 a = P.pA[k], b = P.pB[k], c = P.wA[k], d = P.wB[k], e = P.nrm[k], f = P.imp[k], g = P.d1[k], h = P.d2[k];
+        float4 a = P.pA[k], b = P.pB[k], c = P.wA[k], d = P.wB[k], e = P.nrm[k];
         MP& q = m.p[j];
         q.la = mk(a.x, a.y, a.z); q.dist = a.w;
         q.lb = mk(b.x, b.y, b.z); q.life = __float_as_int(b.w);
         q.wa = mk(c.x, c.y, c.z); q.fr = c.w;
         q.wb = mk(d.x, d.y, d.z); q.rest = d.w;
         q.n = mk(e.x, e.y, e.z); q.ai = e.w;
-        q.l1 = f.x; q.l2 = f.y; q.latInit = f.z;
-        q.d1 = mk(g.x, g.y, g.z); q.d2 = mk(h.x, h.y, h.z);
+        q.src = j;
+        q.repl = false;
     }
 }
+// Slots are written in increasing order; a moved point's source slot is never below its new slot
+// (removeContactPoint moves the last point down), so a source is read before it is overwritten.
 JBD void store_mf(const DevPairs& P, int pair, const Mf& m) {
     P.n[pair] = m.n;
+    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     for (int j = 0; j < m.n; j++) {
-        int k = pair * 4 + j;
+        const int k = pair * 4 + j;
         const MP& q = m.p[j];
+        const int s = pair * 4 + q.src;
+        if (q.src < 0) {                           // added this step: no impulses, no directions
+            P.imp[k] = zero;
+            P.d1[k] = zero;
+            P.d2[k] = zero;
+        } else if (q.repl) {                       // replaced: impulses and directions kept, not initialised
+            const float4 im = P.imp[s];
+            if (q.src != j) { P.d1[k] = P.d1[s]; P.d2[k] = P.d2[s]; }
+            P.imp[k] = make_float4(im.x, im.y, 0.0f, 0.0f);
+        } else if (q.src != j) {                   // moved down by a removal
+            P.imp[k] = P.imp[s];
+            P.d1[k] = P.d1[s];
+            P.d2[k] = P.d2[s];
+        }
         P.pA[k] = f4(q.la, q.dist);
         P.pB[k] = f4(q.lb, __int_as_float(q.life));
         P.wA[k] = f4(q.wa, q.fr);
         P.wB[k] = f4(q.wb, q.rest);
-        P.nrm[k] = f4(q.n, q.ai);
-        P.imp[k] = make_float4(q.l1, q.l2, q.latInit, 0.0f);
-        P.d1[k] = f4(q.d1, 0.0f);
-        P.d2[k] = f4(q.d2, 0.0f);
+        if (q.src != j || q.repl) P.nrm[k] = f4(q.n, q.ai);
     }
 }
 
@@ -69,17 +90,12 @@ JBD int sort_cached_points(const Mf& m, const MP& pt) {
     return idx;
 }
 
-// PersistentManifold.removeContactPoint (java:259-278)
+// PersistentManifold.removeContactPoint (java:259-278): the last point moves into the hole (the
+// reference also clears the vacated slot's impulses and lifetime; the slot is past the count and
+// is written in full before it is used again).
 JBD void remove_point(Mf& m, int index) {
     int last = m.n - 1;
-    if (index != last) {
-        m.p[index] = m.p[last];
-        m.p[last].ai = 0.0f;
-        m.p[last].latInit = 0.0f;
-        m.p[last].l1 = 0.0f;
-        m.p[last].l2 = 0.0f;
-        m.p[last].life = 0;
-    }
+    if (index != last) m.p[index] = m.p[last];
     m.n--;
 }
 
@@ -118,8 +134,9 @@ JBD void add_contact(Mf& m, int mb0, int col0, const Xf& xf0, const Xf& xf1, flo
     MP np;
     np.la = la; np.lb = lb; np.n = normalOnB; np.dist = depth;
     np.wa = pointA; np.wb = pointInWorld;
-    np.ai = 0.0f; np.l1 = 0.0f; np.l2 = 0.0f; np.latInit = 0.0f; np.life = 0;
-    np.d1 = mk(0.0f, 0.0f, 0.0f); np.d2 = mk(0.0f, 0.0f, 0.0f);
+    np.ai = 0.0f; np.life = 0;
+    np.src = -1;
+    np.repl = false;
     float shortest = __fmul_rn(cbt, cbt);   // PersistentManifold.getCacheEntry (java:214-233)
     int nearest = -1;
     for (int i = 0; i < m.n; i++) {
@@ -134,12 +151,12 @@ JBD void add_contact(Mf& m, int mb0, int col0, const Xf& xf0, const Xf& xf1, flo
     np.rest = __fmul_rn(re0, re1);
     if (nearest >= 0) {                       // replaceContactPoint keeps impulses and lifetime
         MP& o = m.p[nearest];
-        float ai = o.ai, l1 = o.l1, l2 = o.l2;
-        int life = o.life;
-        V d1 = o.d1, d2 = o.d2;
+        const float ai = o.ai;
+        const int life = o.life, src = o.src;
         o = np;
-        o.ai = ai; o.l1 = l1; o.l2 = l2; o.life = life;
-        o.d1 = d1; o.d2 = d2;
+        o.ai = ai; o.life = life;
+        o.src = src;                          // its lateral impulses and directions (store_mf)
+        o.repl = true;
     } else {                                  // addManifoldPoint
         int ins = m.n;
         if (ins == 4) ins = sort_cached_points(m, np);

@@ -125,24 +125,25 @@ __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n
     Leaf f, g;
     const int kind = pair_leaves(w, key, col0, col1, x0, x1, f, g);
     if (kind == ALG_EMPTY || kind >= ALG_CONVEX_CONCAVE) return;   // no manifold; meshes: the concave pass
-    Mf m;
-    if (!P.has[p]) { P.has[p] = 1; m.n = 0; }
-    else load_mf(P, p, m);
-    int mb0 = P.b0[p], mb1 = P.b1[p];
-    float fr0 = w.friction[col0], fr1 = w.friction[col1], re0 = w.restitution[col0], re1 = w.restitution[col1];
+    const bool fresh = !P.has[p];            // the algorithm and its manifold come with the first dispatch
+    if (fresh) P.has[p] = 1;
+    // The collision first, without the manifold (it reads nothing of it), so that GJK's state and
+    // the manifold's 4 points are never live together: at most one point for the manifold.
+    bool hit = false;
+    V nB, pW;
+    float dist = 0.0f;
     if (kind == ALG_SPHERE_SPHERE) {
         V diff = sub(f.x.o, g.x.o);
         float l = len(diff);
         float r0 = w.sh.margin[f.shape], r1 = w.sh.margin[g.shape];
         float rs = __fadd_rn(r0, r1);
         if (!(l > rs)) {
-            float dist = __fsub_rn(l, rs);
-            V n = mk(1.0f, 0.0f, 0.0f);
-            if (l > FLT_EPS) n = scl(diff, jdiv(1.0f, l));
-            V pos1 = add(g.x.o, scl(n, r1));
-            add_contact(m, mb0, col0, x0, x1, fr0, fr1, re0, re1, n, pos1, dist, w.cbt);
+            dist = __fsub_rn(l, rs);
+            nB = mk(1.0f, 0.0f, 0.0f);
+            if (l > FLT_EPS) nB = scl(diff, jdiv(1.0f, l));
+            pW = add(g.x.o, scl(nB, r1));
+            hit = true;
         }
-        manifold_refresh(m, w, mb0, mb1);
     } else if (kind == ALG_CONVEX_PLANE || kind == ALG_PLANE_CONVEX) {
         const Leaf& c = kind == ALG_CONVEX_PLANE ? f : g;   // the convex object
         const Leaf& pl = kind == ALG_CONVEX_PLANE ? g : f;
@@ -157,12 +158,12 @@ __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n
         V vtxInPlane = xf_apply(convexInPlane, vtx);
         float distance = __fsub_rn(dot(pn, vtxInPlane), plq.w);
         V proj = sub(vtxInPlane, scl(pn, distance));
-        V vtxWorld = xf_apply(px, proj);
         if (distance < w.cbt) {
-            V nB = mulMv(pn, px.b);
-            add_contact(m, mb0, col0, x0, x1, fr0, fr1, re0, re1, nB, vtxWorld, distance, w.cbt);
+            pW = xf_apply(px, proj);
+            nB = mulMv(pn, px.b);
+            dist = distance;
+            hit = true;
         }
-        manifold_refresh(m, w, mb0, mb1);
     } else {
         ShapeRef sa = shape_ref(w.sh, f.shape), sb = shape_ref(w.sh, g.shape);
         float md = __fadd_rn(__fadd_rn(sa.margin, sb.margin), w.cbt);
@@ -183,12 +184,25 @@ __global__ void __launch_bounds__(128, 4) k_narrow(DevWorld w, DevPairs P, int n
             r.pB = f4(gp.pointOnB, 0.0f);
             r.nB = f4(gp.normalInB, 0.0f);
             queue[q] = r;
-            if (P.n[p] == 0 && m.n == 0) P.n[p] = 0;
+            if (fresh) P.n[p] = 0;
             return;   // the EPA pass finishes this pair
         }
-        if (gp.isValid) add_contact(m, mb0, col0, x0, x1, fr0, fr1, re0, re1, gp.normalInB, add(gp.pointOnB, gp.offset), gp.distance, w.cbt);
-        manifold_refresh(m, w, mb0, mb1);
+        if (gp.isValid) {
+            nB = gp.normalInB;
+            pW = add(gp.pointOnB, gp.offset);
+            dist = gp.distance;
+            hit = true;
+        }
     }
+    // ManifoldResult.addContactPoint and refreshContactPoints on the pair's manifold
+    Mf m;
+    if (fresh) m.n = 0;
+    else load_mf(P, p, m);
+    const int mb0 = P.b0[p], mb1 = P.b1[p];
+    if (hit)
+        add_contact(m, mb0, col0, x0, x1, w.friction[col0], w.friction[col1], w.restitution[col0], w.restitution[col1],
+                    nB, pW, dist, w.cbt);
+    manifold_refresh(m, w, mb0, mb1);
     store_mf(P, p, m);
 }
 
