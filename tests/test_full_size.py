@@ -6,7 +6,11 @@
   pair sets and manifolds bit-identical.
 * 4,096 batched worlds of 16..2,048 bodies (~1.7 M bodies): 16 sampled worlds, the largest
   among them, equal the same worlds stepped alone on the GPU and by the oracle (every world is
-  one solver part, so the oracle's own colouring is the GPU's), bit for bit."""
+  one solver part, so the oracle's own colouring is the GPU's), bit for bit.
+* The terrain workload (20,000 convex and 2,000 compound bodies on a 32,768-triangle mesh): from
+  the GPU's state after 300 steps, one open-loop pass through the narrowphase (pairs with one key
+  per compound child combination, the mesh pairs' triangle candidates) bit-identical to the
+  oracle's, then one whole step in lockstep (the oracle fed the GPU's solver order)."""
 import numpy as np
 import pytest
 
@@ -70,3 +74,34 @@ def test_batched_4096_sampled_worlds_equal_solo_and_oracle(gpu_lib, oracle_lib):
         assert not H.compare_state(so, ss), wi
         assert not H.compare_manifolds(o.get_manifolds(), solo.get_manifolds()), wi
         solo.close()
+
+
+def test_terrain_20k_settled_narrowphase_and_step_lockstep(gpu_lib, oracle_lib):
+    sc = scenes.SCENES["terrain_20k"]()
+    g = GpuWorld(sc)
+    for _ in range(300):
+        g.step(sc.dt)
+    c = g.counters()
+    assert c["status_flags"] == 0
+    assert c["contacts"] > 40_000 and c["gjk_calls"] > 100_000, c     # settled on the mesh
+    o = pyoracle.OracleWorld(sc)
+    H.copy_world(g, o)
+    g.stage(_abi.STAGE_APPLY_GRAVITY, sc.dt)
+    o.stage(_abi.STAGE_APPLY_GRAVITY, sc.dt)
+    for st in (_abi.STAGE_PREDICT, _abi.STAGE_AABB, _abi.STAGE_PAIRS, _abi.STAGE_NARROWPHASE):
+        g.stage(st, sc.dt)
+        o.stage(st, sc.dt)
+        if st == _abi.STAGE_PAIRS:
+            assert np.array_equal(o.get_pairs(), g.get_pairs())
+    assert not H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+    co, cg = o.counters(), g.counters()
+    assert (co["gjk_calls"], co["epa_calls"]) == (cg["gjk_calls"], cg["epa_calls"])
+    # one whole step more in lockstep: the GPU's solver order fed to the oracle
+    H.copy_world(g, o)
+    g.step(sc.dt)
+    o.set_explicit_order(g.solver_order())
+    o.step(sc.dt)
+    assert o.counters()["status_flags"] == 0
+    assert not H.compare_state(o.get_state(), g.get_state())
+    assert not H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+    g.close()
