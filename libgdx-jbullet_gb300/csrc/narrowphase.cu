@@ -496,28 +496,39 @@ JBD int mesh_walk(const DevWorld& w, const Leaf& c, const Leaf& t, int p, int2* 
     return found;
 }
 
-// Per pair: the ConvexTriangleCallback's manifold on first contact, and the candidate count.
-__global__ void k_mesh_count(DevWorld w, DevPairs P, int nPairs, const int* cntp, int* cnt) {
+// Per pair: the ConvexTriangleCallback's manifold on first contact, the candidate count, and the
+// pair appended to the list of mesh pairs (list[0] counts them; the fill and the merge run over
+// the list, a thread per mesh pair, in whatever order the appends landed - pairs are independent).
+__global__ void k_mesh_count(DevWorld w, DevPairs P, int nPairs, const int* cntp, int* cnt, int* list) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= nPairs) return;
     int col0, col1;
     Xf x0, x1;
     Leaf c, t;
-    if (p >= (cntp ? min(nPairs, *cntp) : nPairs) || !concave_pair(w, P, p, col0, col1, x0, x1, c, t)) {
+    const bool mine = p < (cntp ? min(nPairs, *cntp) : nPairs) && concave_pair(w, P, p, col0, col1, x0, x1, c, t);
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, mine);
+    if (!mine) {
         cnt[p] = 0;
         return;
     }
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(list, __popc(m));
+    base = __shfl_sync(m, base, leader);
+    list[1 + base + __popc(m & ((1u << lane) - 1u))] = p;
     if (!P.has[p]) { P.has[p] = 1; P.n[p] = 0; }
     cnt[p] = mesh_walk(w, c, t, p, nullptr);
 }
 
-__global__ void k_mesh_fill(DevWorld w, DevPairs P, int nPairs, const int* cntp, const int* off, int2* cand) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (cntp ? min(nPairs, *cntp) : nPairs)) return;
+__global__ void k_mesh_fill(DevWorld w, DevPairs P, const int* list, const int* off, int2* cand) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= list[0]) return;
+    const int p = list[1 + i];
     int col0, col1;
     Xf x0, x1;
     Leaf c, t;
-    if (!concave_pair(w, P, p, col0, col1, x0, x1, c, t)) return;
+    concave_pair(w, P, p, col0, col1, x0, x1, c, t);
     mesh_walk(w, c, t, p, cand + off[p]);
 }
 
@@ -556,14 +567,15 @@ __global__ void __launch_bounds__(128, 4) k_mesh_gjk(DevWorld w, DevPairs P, con
 
 // Per pair: the candidates' points into the manifold in walk order (ManifoldResult.
 // addContactPoint), then ManifoldResult.refreshContactPoints.
-__global__ void k_mesh_merge(DevWorld w, DevPairs P, int nPairs, const int* cntp, const int* cnt, const int* off,
+__global__ void k_mesh_merge(DevWorld w, DevPairs P, const int* list, const int* cnt, const int* off,
                              const float4* res) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= (cntp ? min(nPairs, *cntp) : nPairs)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= list[0]) return;
+    const int p = list[1 + i];
     int col0, col1;
     Xf x0, x1;
     Leaf c, t;
-    if (!concave_pair(w, P, p, col0, col1, x0, x1, c, t)) return;
+    concave_pair(w, P, p, col0, col1, x0, x1, c, t);
     const int mb0 = P.b0[p], mb1 = P.b1[p];
     Mf m;
     load_mf(P, p, m);
@@ -577,7 +589,8 @@ __global__ void k_mesh_merge(DevWorld w, DevPairs P, int nPairs, const int* cntp
 }
 
 void concave_free(NarrowBuffers& nb) {
-    cudaFree(nb.meshCnt); cudaFree(nb.meshOff); cudaFree(nb.meshTotal); cudaFree(nb.meshScan);
+    cudaFree(nb.meshCnt); cudaFree(nb.meshOff); cudaFree(nb.meshTotal); cudaFree(nb.meshScan); cudaFree(nb.meshList);
+    nb.meshList = nullptr;
     cudaFree(nb.cand); cudaFree(nb.candRes); cudaFree(nb.candQueue); cudaFree(nb.candOvf); cudaFree(nb.candOvf2);
     cudaFree(nb.candCount);
     nb.meshCnt = nb.meshOff = nb.meshTotal = nullptr;
@@ -593,24 +606,30 @@ int concave_launch(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, 
                    cudaStream_t s) {
     if (nPairs <= 0) return 0;
     if (nPairs > nb.capMeshPairs) {
-        cudaFree(nb.meshCnt); cudaFree(nb.meshOff); cudaFree(nb.meshScan);
-        nb.meshCnt = nb.meshOff = nullptr;
+        cudaFree(nb.meshCnt); cudaFree(nb.meshOff); cudaFree(nb.meshScan); cudaFree(nb.meshList);
+        nb.meshCnt = nb.meshOff = nb.meshList = nullptr;
         nb.meshScan = nullptr;
         const int c = std::max(nPairs, 2 * nb.capMeshPairs);
         if (cudaMalloc(&nb.meshCnt, sizeof(int) * c) != cudaSuccess || cudaMalloc(&nb.meshOff, sizeof(int) * c) != cudaSuccess ||
+            cudaMalloc(&nb.meshList, sizeof(int) * (c + 1)) != cudaSuccess ||
             cudaMalloc(&nb.meshScan, scan_scratch_bytes(c)) != cudaSuccess)
             return 1;
         nb.capMeshPairs = c;
     }
     if (!nb.meshTotal && cudaMalloc(&nb.meshTotal, sizeof(int)) != cudaSuccess) return 1;
-    if (!nb.candCount && cudaMalloc(&nb.candCount, sizeof(int) * 4) != cudaSuccess) return 1;
-    const int blocks = (nPairs + 127) / 128;
-    k_mesh_count<<<blocks, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshCnt); note_launch();
+    if (!nb.candCount) {
+        if (cudaMalloc(&nb.candCount, sizeof(int) * 4) != cudaSuccess) return 1;
+        cudaMemsetAsync(nb.candCount, 0, sizeof(int) * 4, s);
+    }
+    cudaMemsetAsync(nb.meshList, 0, sizeof(int), s);
+    k_mesh_count<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshCnt, nb.meshList); note_launch();
     exclusive_scan(nb.meshCnt, nb.meshOff, nb.meshTotal, nPairs, nb.meshScan, s);
     if (cudaMemcpyAsync(hostTotal, nb.meshTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(hostTotal + 1, nb.meshList, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return 1;
-    const int total = *hostTotal;
+    const int total = hostTotal[0], meshPairs = hostTotal[1];
+    const int blocks = (meshPairs + 127) / 128;
     if (total > nb.capCand) {
         cudaFree(nb.cand); cudaFree(nb.candRes); cudaFree(nb.candQueue); cudaFree(nb.candOvf); cudaFree(nb.candOvf2);
         nb.cand = nullptr;
@@ -625,7 +644,7 @@ int concave_launch(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, 
         nb.capCand = c;
     }
     if (total > 0) {
-        k_mesh_fill<<<blocks, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshOff, nb.cand); note_launch();
+        k_mesh_fill<<<blocks, 128, 0, s>>>(w, P, nb.meshList, nb.meshOff, nb.cand); note_launch();
         cudaMemsetAsync(nb.candCount, 0, sizeof(int), s);
         k_mesh_gjk<<<(total + 127) / 128, 128, 0, s>>>(w, P, nb.cand, total, nb.candRes, (EpaRec*)nb.candQueue,
                                                         nb.candCount);
@@ -633,7 +652,10 @@ int concave_launch(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, 
         epa_tiers(w, P, nb.candQueue, nb.candCount, nb.candOvf, nb.candOvf2, nb.candCount + 1, nb.slots, nb.cand,
                   nb.candRes, s);
     }
-    k_mesh_merge<<<blocks, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshCnt, nb.meshOff, nb.candRes); note_launch();
+    if (meshPairs > 0) {
+        k_mesh_merge<<<blocks, 128, 0, s>>>(w, P, nb.meshList, nb.meshCnt, nb.meshOff, nb.candRes);
+        note_launch();
+    }
     return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 

@@ -25,6 +25,7 @@ struct NarrowBuffers {
     // counts, tier mode)
     int* meshCnt = nullptr;
     int* meshOff = nullptr;
+    int* meshList = nullptr;      // [0]: mesh pairs this step, then their pair indices
     int* meshTotal = nullptr;
     void* meshScan = nullptr;
     int capMeshPairs = 0;
@@ -44,8 +45,8 @@ void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffer
                         const Prof* prof = nullptr, const int* cntp = nullptr);
 
 // The concave pass (after narrowphase_launch, in a world with triangle meshes): reads the
-// candidate count back to the host (hostTotal: pinned) and grows its buffers, so it runs
-// outside graph capture.  Returns nonzero when a CUDA call failed.
+// candidate and mesh-pair counts back to the host (hostTotal: 2 pinned ints) and grows its
+// buffers, so it runs outside graph capture.  Returns nonzero when a CUDA call failed.
 int concave_launch(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, NarrowBuffers& nb, int* hostTotal,
                    cudaStream_t s);
 void concave_free(NarrowBuffers& nb);
