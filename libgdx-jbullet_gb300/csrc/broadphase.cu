@@ -252,14 +252,59 @@ __global__ void k_plane_pairs(DevWorld w, const int* planeList, const int* plane
     }
 }
 
+// Ascending sort of c words in place: in registers up to 32, else a Shell sort in memory.
+JBD void sort_words(unsigned* p, int c) {
+    if (c <= 32) {
+        unsigned v[32];
+        for (int k = 0; k < c; k++) v[k] = p[k];
+        for (int k = 1; k < c; k++) {
+            unsigned x = v[k];
+            int j = k - 1;
+            while (j >= 0 && v[j] > x) { v[j + 1] = v[j]; j--; }
+            v[j + 1] = x;
+        }
+        for (int k = 0; k < c; k++) p[k] = v[k];
+        return;
+    }
+    for (int gap = c / 2; gap > 0; gap /= 2)
+        for (int k = gap; k < c; k++) {
+            unsigned x = p[k];
+            int j = k;
+            while (j >= gap && p[j - gap] > x) { p[j] = p[j - gap]; j -= gap; }
+            p[j] = x;
+        }
+}
+
 // Sort each owner's partner words (sub << 24 | partner, compared unsigned) ascending and emit the
-// canonical keys.
-__global__ void k_segment_sort(int n, const int* off, const int* cnt, int* partners, uint64_t* keys, int capacity) {
+// canonical keys.  With compounds a partner's child combinations are written together, so the
+// owner's distinct partners (the words with sub 0) are sorted alone and the keys generated sub
+// by sub - the same ascending order without sorting every combination.
+__global__ void k_segment_sort(DevWorld w, int n, const int* off, const int* cnt, int* partners, uint64_t* keys,
+                               int capacity) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int o = off[i], c = cnt[i];
     if (o + c > capacity) return;
     unsigned* p = (unsigned*)partners + o;
+    if (w.hasCompound) {
+        int np = 0;
+        for (int k = 0; k < c; k++)
+            if ((p[k] >> 24) == 0) p[np++] = p[k];   // in place: np <= k
+        sort_words(p, np);
+        const uint64_t hi = (uint64_t)(unsigned)i << 32;
+        int at = 0, more = 1;
+        for (unsigned sub = 0; more && at < c; sub++) {
+            more = 0;
+            for (int k = 0; k < np; k++) {
+                const int subs = pair_subs(w.sh, w.shape[i], w.shape[p[k]]);
+                if ((int)sub < subs) {
+                    keys[o + at++] = hi | (sub << 24) | p[k];
+                    more |= (int)sub + 1 < subs;
+                }
+            }
+        }
+        return;
+    }
     if (c <= 32) {
         unsigned v[32];
         for (int k = 0; k < c; k++) v[k] = p[k];
@@ -412,7 +457,7 @@ void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw,
     if (bb.nPlanes > 0)
         k_plane_pairs<true><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, nullptr, bb.off, bb.cursor,
                                                            bb.partners, capacity); note_launch();
-    k_segment_sort<<<gridn(n, 128), 128, 0, s>>>(n, bb.off, bb.cursor, bb.partners, nw.keys, capacity); note_launch();
+    k_segment_sort<<<gridn(n, 128), 128, 0, s>>>(w, n, bb.off, bb.cursor, bb.partners, nw.keys, capacity); note_launch();
 }
 
 void broadphase_persist(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, const DevPairs& old, int nNew, int nOld,
