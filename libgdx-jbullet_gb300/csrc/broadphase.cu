@@ -232,9 +232,11 @@ __global__ void k_traverse(DevWorld w, const int* sortedBody, int nf, Bvh t, con
 
 // Pairs of each body in the tree with the listed bodies (static planes, triangle meshes) of its
 // world, owned by the former.
+// The counting pass also sums, into candBound, the triangle candidates the concave pass will
+// list for the body's mesh pairs (an upper bound: pairs whose bodies are both inactive list none).
 template <bool FILL>
 __global__ void k_plane_pairs(DevWorld w, const int* planeList, const int* planeStart, int* cnt, const int* off,
-                              int* cursor, int* partners, int capacity) {
+                              int* cursor, int* partners, int capacity, int* candBound) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.nBodies || (w.flags[i] & CF_LISTED)) return;
     int wi = w.world[i];
@@ -243,6 +245,10 @@ __global__ void k_plane_pairs(DevWorld w, const int* planeList, const int* plane
         int p = planeList[k];
         if (!ovl(a0, a1, w.amin[p], w.amax[p]) || !filt(w, i, p)) continue;
         const int subs = w.hasCompound ? pair_subs(w.sh, w.shape[i], w.shape[p]) : 1;
+        if (!FILL && candBound) {
+            const int c = mesh_candidates(w, i, p);
+            if (c) atomicAdd(candBound, c);
+        }
         if (!FILL) atomicAdd(&cnt[i], subs);
         else {
             int pos = off[i] + atomicAdd(&cursor[i], subs);
@@ -424,9 +430,10 @@ void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t
             k_traverse<false><<<gridn(nf, 128), 128, 0, s>>>(w, bb.sortedBody, nf, bb.bvh, bb.wroot, bb.cnt, nullptr,
                                                               nullptr, nullptr, 0, bb.tcount, bb.tcache); note_launch();
         }
+        cudaMemsetAsync(bb.candBound, 0, sizeof(int), s);
         if (bb.nPlanes > 0)
             k_plane_pairs<false><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, bb.cnt, nullptr, nullptr,
-                                                                nullptr, 0); note_launch();
+                                                                nullptr, 0, bb.candBound); note_launch();
         exclusive_scan(bb.cnt, bb.off, bb.total, n + 1, bb.scanScratch, s);
         return;
     }
@@ -441,9 +448,10 @@ void broadphase_run_count(const DevWorld& w, BroadphaseBuffers& bb, cudaStream_t
                                                               nullptr, nullptr, 0, bb.tcount, bb.tcache); note_launch();
         }
     }
+    cudaMemsetAsync(bb.candBound, 0, sizeof(int), s);
     if (bb.nPlanes > 0)
         k_plane_pairs<false><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, bb.cnt, nullptr, nullptr,
-                                                            nullptr, 0); note_launch();
+                                                            nullptr, 0, bb.candBound); note_launch();
     exclusive_scan(bb.cnt, bb.off, bb.total, n + 1, bb.scanScratch, s);
 }
 
@@ -456,7 +464,7 @@ void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw,
                                                          bb.cursor, bb.partners, capacity, bb.tcount, bb.tcache); note_launch();
     if (bb.nPlanes > 0)
         k_plane_pairs<true><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, nullptr, bb.off, bb.cursor,
-                                                           bb.partners, capacity); note_launch();
+                                                           bb.partners, capacity, nullptr); note_launch();
     k_segment_sort<<<gridn(n, 128), 128, 0, s>>>(w, n, bb.off, bb.cursor, bb.partners, nw.keys, capacity); note_launch();
 }
 

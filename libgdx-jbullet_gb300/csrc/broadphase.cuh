@@ -45,6 +45,7 @@ struct BroadphaseBuffers {
     bool offPrevValid = false;           // offPrev matches the previous pair array
     int* cursor = nullptr;               // fill cursors (n + 1)
     int* total = nullptr;                // device total pair count
+    int* candBound = nullptr;            // device: the concave pass's candidates, bounded by the count pass
     int* partners = nullptr;             // CSR partner lists (pair capacity)
     int* tcount = nullptr;               // per sorted leaf: pairs its counting traversal found
     int* tcache = nullptr;               // per sorted leaf: the first TRAV_CACHE partners' sorted leaves

@@ -113,4 +113,65 @@ JBD void mesh_quantize(V p, V bmin, V bmax, V q, int out[3]) {
     out[2] = (int)__fadd_rn(v.z, 0.5f) & 0xFFFF;
 }
 
+// ConvexTriangleCallback's query of a convex leaf c against the mesh leaf t: c's box in the mesh's
+// space widened by the mesh margin (setTimeStepAndCounters, ConvexTriangleCallback.java:82-104),
+// quantized, and the mesh's tree walked as OptimizedBvh.walkStacklessQuantizedTree does
+// (OptimizedBvh.java:940-997).  Returns the triangles found; the first `room` of them are written
+// as (p, triangle) in walk order to out when out is given.
+JBD int mesh_walk(const DevWorld& w, const Leaf& c, const Leaf& t, int p, int2* out, int room = 0) {
+    const DevShapes& sh = w.sh;
+    const Xf convexInTri = xf_mul(xf_inverse(t.x), c.x);
+    V mn, mx;
+    shape_aabb(sh, c.shape, convexInTri, mn, mx);
+    const float mt = sh.margin[t.shape];
+    mx = add(mx, mk(mt, mt, mt));
+    mn = sub(mn, mk(mt, mt, mt));
+    const float4* q = sh.mesh_q + 3 * t.shape;
+    const V bmin = mk4(q[0]), bmax = mk4(q[1]), quant = mk4(q[2]);
+    int qa[3], qb[3];
+    mesh_quantize(mn, bmin, bmax, quant, qa);
+    mesh_quantize(mx, bmin, bmax, quant, qb);
+    const int4* nodes = sh.mesh_nodes + sh.mesh_node_off[t.shape];
+    const int nn = sh.mesh_node_cnt[t.shape];
+    int found = 0;
+    for (int cur = 0; cur < nn;) {
+        const int4 nd = nodes[cur];
+        const int n0 = nd.x & 0xFFFF, n1 = (nd.x >> 16) & 0xFFFF, n2 = nd.y & 0xFFFF;
+        const int m0 = (nd.y >> 16) & 0xFFFF, m1 = nd.z & 0xFFFF, m2 = (nd.z >> 16) & 0xFFFF;
+        const bool ov = !(qa[0] > m0 || qb[0] < n0) && !(qa[2] > m2 || qb[2] < n2) && !(qa[1] > m1 || qb[1] < n1);
+        const bool leaf = nd.w >= 0;
+        if (leaf && ov) {
+            if (out && found < room) out[found] = make_int2(p, nd.w & ((1 << 21) - 1));
+            ++found;
+        }
+        cur += (ov || leaf) ? 1 : max(1, -nd.w);
+    }
+    return found;
+}
+
+// The triangle candidates the concave pass will list for body i against the listed mesh body m
+// (every convex leaf of i: its compound children, or itself): the bound the pair count pass
+// sums so that the candidate buffer is sized before the narrowphase.
+JBD int mesh_candidates(const DevWorld& w, int i, int m) {
+    const int si = w.shape[i], sm = w.shape[m];
+    if (w.sh.type[sm] != SHAPE_MESH) return 0;
+    Leaf t;
+    t.shape = sm;
+    t.x = load_xf(w, m);
+    t.body = m;
+    const Xf xi = load_xf(w, i);
+    const int ti = w.sh.type[si];
+    if (ti == SHAPE_COMPOUND) {
+        int n = 0;
+        for (int k = 0; k < w.sh.child_cnt[si]; k++) n += mesh_walk(w, compound_child(w.sh, si, k, xi, i), t, 0, nullptr);
+        return n;
+    }
+    if (!shape_is_convex(ti)) return 0;
+    Leaf c;
+    c.shape = si;
+    c.x = xi;
+    c.body = i;
+    return mesh_walk(w, c, t, 0, nullptr);
+}
+
 }  // namespace jbg

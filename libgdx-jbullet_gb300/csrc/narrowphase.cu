@@ -463,39 +463,6 @@ JBD bool concave_pair(const DevWorld& w, const DevPairs& P, int p, int& col0, in
     return true;
 }
 
-// Walks the mesh tree with the pair's query box; counts the triangles found, and lists them
-// (pair, triangle) from out when out is given.
-JBD int mesh_walk(const DevWorld& w, const Leaf& c, const Leaf& t, int p, int2* out) {
-    const DevShapes& sh = w.sh;
-    const Xf convexInTri = xf_mul(xf_inverse(t.x), c.x);
-    V mn, mx;
-    shape_aabb(sh, c.shape, convexInTri, mn, mx);
-    const float mt = sh.margin[t.shape];
-    mx = add(mx, mk(mt, mt, mt));
-    mn = sub(mn, mk(mt, mt, mt));
-    const float4* q = sh.mesh_q + 3 * t.shape;
-    const V bmin = mk4(q[0]), bmax = mk4(q[1]), quant = mk4(q[2]);
-    int qa[3], qb[3];
-    mesh_quantize(mn, bmin, bmax, quant, qa);
-    mesh_quantize(mx, bmin, bmax, quant, qb);
-    const int4* nodes = sh.mesh_nodes + sh.mesh_node_off[t.shape];
-    const int nn = sh.mesh_node_cnt[t.shape];
-    int found = 0;
-    for (int cur = 0; cur < nn;) {
-        const int4 nd = nodes[cur];
-        const int n0 = nd.x & 0xFFFF, n1 = (nd.x >> 16) & 0xFFFF, n2 = nd.y & 0xFFFF;
-        const int m0 = (nd.y >> 16) & 0xFFFF, m1 = nd.z & 0xFFFF, m2 = (nd.z >> 16) & 0xFFFF;
-        const bool ov = !(qa[0] > m0 || qb[0] < n0) && !(qa[2] > m2 || qb[2] < n2) && !(qa[1] > m1 || qb[1] < n1);
-        const bool leaf = nd.w >= 0;
-        if (leaf && ov) {
-            if (out) out[found] = make_int2(p, nd.w & ((1 << 21) - 1));
-            ++found;
-        }
-        cur += (ov || leaf) ? 1 : max(1, -nd.w);
-    }
-    return found;
-}
-
 // Per pair: the ConvexTriangleCallback's manifold on first contact, the candidate count, and the
 // pair appended to the list of mesh pairs (list[0] counts them; the fill and the merge run over
 // the list, a thread per mesh pair, in whatever order the appends landed - pairs are independent).
@@ -521,7 +488,9 @@ __global__ void k_mesh_count(DevWorld w, DevPairs P, int nPairs, const int* cntp
     cnt[p] = mesh_walk(w, c, t, p, nullptr);
 }
 
-__global__ void k_mesh_fill(DevWorld w, DevPairs P, const int* list, const int* off, int2* cand) {
+// The pair's candidates in walk order at its offset; cap: the candidate buffer's capacity (sized
+// from the count pass's bound; a pair that would run past it flags ST_CAPACITY).
+__global__ void k_mesh_fill(DevWorld w, DevPairs P, const int* list, const int* off, int2* cand, int cap) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= list[0]) return;
     const int p = list[1 + i];
@@ -529,16 +498,17 @@ __global__ void k_mesh_fill(DevWorld w, DevPairs P, const int* list, const int* 
     Xf x0, x1;
     Leaf c, t;
     concave_pair(w, P, p, col0, col1, x0, x1, c, t);
-    mesh_walk(w, c, t, p, cand + off[p]);
+    const int room = cap - off[p];
+    if (mesh_walk(w, c, t, p, cand + off[p], room) > room) atomicOr(&w.ctr[C_STATUS], ST_CAPACITY);
 }
 
 // Per candidate: GjkPairDetector between the convex object and the triangle (ConvexConvex
 // Algorithm.processCollision java:90-139 with the callback's manifold); penetrating candidates
 // go to the EPA queue.  res: 2 float4 per candidate (pointOnB + offset, distance; normal, valid).
-__global__ void __launch_bounds__(128, 4) k_mesh_gjk(DevWorld w, DevPairs P, const int2* cand, int n, float4* res,
-                                                     EpaRec* queue, int* queueCount) {
+__global__ void __launch_bounds__(128, 4) k_mesh_gjk(DevWorld w, DevPairs P, const int2* cand, const int* total, int cap,
+                                                     float4* res, EpaRec* queue, int* queueCount) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    if (i >= min(*total, cap)) return;
     const int2 ct = cand[i];
     int col0, col1;
     Xf x0, x1;
@@ -602,60 +572,92 @@ void concave_free(NarrowBuffers& nb) {
     nb.capMeshPairs = nb.capCand = 0;
 }
 
-int concave_launch(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, NarrowBuffers& nb, int* hostTotal,
-                   cudaStream_t s) {
-    if (nPairs <= 0) return 0;
-    if (nPairs > nb.capMeshPairs) {
+// Buffers of the concave pass for pairCap pairs and candCap candidates (grown, never shrunk).
+// Returns -1 when a CUDA allocation failed, 1 when a buffer moved (captured graphs hold the old
+// pointers), 0 otherwise.
+int concave_reserve(NarrowBuffers& nb, int pairCap, int candCap, cudaStream_t s) {
+    int moved = 0;
+    if (pairCap > nb.capMeshPairs) {
         cudaFree(nb.meshCnt); cudaFree(nb.meshOff); cudaFree(nb.meshScan); cudaFree(nb.meshList);
         nb.meshCnt = nb.meshOff = nb.meshList = nullptr;
         nb.meshScan = nullptr;
-        const int c = std::max(nPairs, 2 * nb.capMeshPairs);
+        const int c = std::max(pairCap, 2 * nb.capMeshPairs);
         if (cudaMalloc(&nb.meshCnt, sizeof(int) * c) != cudaSuccess || cudaMalloc(&nb.meshOff, sizeof(int) * c) != cudaSuccess ||
             cudaMalloc(&nb.meshList, sizeof(int) * (c + 1)) != cudaSuccess ||
             cudaMalloc(&nb.meshScan, scan_scratch_bytes(c)) != cudaSuccess)
-            return 1;
+            return -1;
         nb.capMeshPairs = c;
+        moved = 1;
     }
-    if (!nb.meshTotal && cudaMalloc(&nb.meshTotal, sizeof(int)) != cudaSuccess) return 1;
+    if (!nb.meshTotal) {
+        if (cudaMalloc(&nb.meshTotal, sizeof(int)) != cudaSuccess) return -1;
+        moved = 1;
+    }
     if (!nb.candCount) {
-        if (cudaMalloc(&nb.candCount, sizeof(int) * 4) != cudaSuccess) return 1;
+        if (cudaMalloc(&nb.candCount, sizeof(int) * 4) != cudaSuccess) return -1;
         cudaMemsetAsync(nb.candCount, 0, sizeof(int) * 4, s);
+        moved = 1;
     }
-    cudaMemsetAsync(nb.meshList, 0, sizeof(int), s);
-    k_mesh_count<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshCnt, nb.meshList); note_launch();
-    exclusive_scan(nb.meshCnt, nb.meshOff, nb.meshTotal, nPairs, nb.meshScan, s);
-    if (cudaMemcpyAsync(hostTotal, nb.meshTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaMemcpyAsync(hostTotal + 1, nb.meshList, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-        return 1;
-    const int total = hostTotal[0], meshPairs = hostTotal[1];
-    const int blocks = (meshPairs + 127) / 128;
-    if (total > nb.capCand) {
+    if (candCap > nb.capCand || !nb.cand) {
         cudaFree(nb.cand); cudaFree(nb.candRes); cudaFree(nb.candQueue); cudaFree(nb.candOvf); cudaFree(nb.candOvf2);
         nb.cand = nullptr;
         nb.candRes = nullptr;
         nb.candQueue = nullptr;
         nb.candOvf = nb.candOvf2 = nullptr;
-        const int c = std::max(total, 2 * nb.capCand);
+        const int c = std::max(std::max(candCap, 1), 2 * nb.capCand);
         if (cudaMalloc(&nb.cand, sizeof(int2) * c) != cudaSuccess || cudaMalloc(&nb.candRes, sizeof(float4) * 2 * c) != cudaSuccess ||
             cudaMalloc(&nb.candQueue, sizeof(EpaRec) * c) != cudaSuccess || cudaMalloc(&nb.candOvf, sizeof(int) * c) != cudaSuccess ||
             cudaMalloc(&nb.candOvf2, sizeof(int) * c) != cudaSuccess)
-            return 1;
+            return -1;
         nb.capCand = c;
+        moved = 1;
     }
-    if (total > 0) {
-        k_mesh_fill<<<blocks, 128, 0, s>>>(w, P, nb.meshList, nb.meshOff, nb.cand); note_launch();
+    return moved;
+}
+
+// The pass on reserved buffers with every count on the device: nPairs bounds the pair count (cntp:
+// the device count, or null for exactly nPairs) and the candidate buffer holds the count pass's
+// bound.  Grids are sized by the capacities; kernels read the counts.
+static void concave_passes(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, NarrowBuffers& nb, cudaStream_t s,
+                           bool haveCandidates) {
+    const int blocks = (nPairs + 127) / 128;
+    cudaMemsetAsync(nb.meshList, 0, sizeof(int), s);
+    k_mesh_count<<<blocks, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshCnt, nb.meshList); note_launch();
+    exclusive_scan(nb.meshCnt, nb.meshOff, nb.meshTotal, nPairs, nb.meshScan, s);
+    if (haveCandidates) {
+        k_mesh_fill<<<blocks, 128, 0, s>>>(w, P, nb.meshList, nb.meshOff, nb.cand, nb.capCand); note_launch();
         cudaMemsetAsync(nb.candCount, 0, sizeof(int), s);
-        k_mesh_gjk<<<(total + 127) / 128, 128, 0, s>>>(w, P, nb.cand, total, nb.candRes, (EpaRec*)nb.candQueue,
-                                                        nb.candCount);
+        k_mesh_gjk<<<(nb.capCand + 127) / 128, 128, 0, s>>>(w, P, nb.cand, nb.meshTotal, nb.capCand, nb.candRes,
+                                                            (EpaRec*)nb.candQueue, nb.candCount);
         note_launch();
         epa_tiers(w, P, nb.candQueue, nb.candCount, nb.candOvf, nb.candOvf2, nb.candCount + 1, nb.slots, nb.cand,
                   nb.candRes, s);
     }
-    if (meshPairs > 0) {
-        k_mesh_merge<<<blocks, 128, 0, s>>>(w, P, nb.meshList, nb.meshCnt, nb.meshOff, nb.candRes);
-        note_launch();
-    }
+    k_mesh_merge<<<blocks, 128, 0, s>>>(w, P, nb.meshList, nb.meshCnt, nb.meshOff, nb.candRes); note_launch();
+}
+
+int concave_launch_bounded(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, NarrowBuffers& nb, int candBound,
+                           cudaStream_t s) {
+    (void)candBound;   // the buffers hold it (concave_reserve); the candidate kernels always run, so a
+                       // captured graph replays for any count
+    if (nPairs <= 0) return 0;
+    concave_passes(w, P, nPairs, cntp, nb, s, true);
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+int concave_launch(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, NarrowBuffers& nb, int* hostTotal,
+                   cudaStream_t s) {
+    if (nPairs <= 0) return 0;
+    if (concave_reserve(nb, nPairs, 0, s) < 0) return 1;
+    // the exact candidate count first (the stage path: no bound from a count pass of this step)
+    cudaMemsetAsync(nb.meshList, 0, sizeof(int), s);
+    k_mesh_count<<<(nPairs + 127) / 128, 128, 0, s>>>(w, P, nPairs, cntp, nb.meshCnt, nb.meshList); note_launch();
+    exclusive_scan(nb.meshCnt, nb.meshOff, nb.meshTotal, nPairs, nb.meshScan, s);
+    if (cudaMemcpyAsync(hostTotal, nb.meshTotal, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+        return 1;
+    if (concave_reserve(nb, nPairs, *hostTotal, s) < 0) return 1;
+    concave_passes(w, P, nPairs, cntp, nb, s, *hostTotal > 0);
     return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 

@@ -44,11 +44,17 @@ int narrowphase_configure();      // once per world: the EPA kernel's shared-mem
 void narrowphase_launch(const DevWorld& w, DevPairs& P, int nPairs, NarrowBuffers& nb, cudaStream_t s,
                         const Prof* prof = nullptr, const int* cntp = nullptr);
 
-// The concave pass (after narrowphase_launch, in a world with triangle meshes): reads the
-// candidate and mesh-pair counts back to the host (hostTotal: 2 pinned ints) and grows its
-// buffers, so it runs outside graph capture.  Returns nonzero when a CUDA call failed.
+// The concave pass (after narrowphase_launch, in a world with triangle meshes).
+// concave_launch reads the exact candidate count back to the host (hostTotal: a pinned int) and
+// grows its buffers (the stage path); concave_launch_bounded runs on buffers reserved beforehand
+// for the bound the step's pair count pass computed (candBound), every count read on the device,
+// so that it can be captured in a graph.  Both return nonzero when a CUDA call failed.
+// concave_reserve: -1 allocation failed, 1 a buffer moved, 0 nothing changed.
+int concave_reserve(NarrowBuffers& nb, int pairCap, int candCap, cudaStream_t s);
 int concave_launch(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, NarrowBuffers& nb, int* hostTotal,
                    cudaStream_t s);
+int concave_launch_bounded(const DevWorld& w, DevPairs& P, int nPairs, const int* cntp, NarrowBuffers& nb, int candBound,
+                           cudaStream_t s);
 void concave_free(NarrowBuffers& nb);
 
 // Narrowphase whose EPA pass uses scratch compiled into the library (no allocation).

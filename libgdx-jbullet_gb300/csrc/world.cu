@@ -95,6 +95,7 @@ struct jbgpu_world {
     std::vector<int4> meshNodes;          // quantized tree nodes of every triangle mesh
     std::vector<float4> meshTris;         // 3 vertices per triangle
     bool hasMesh = false, hasCompound = false;
+    int candBound = 0;                    // the concave pass's candidates of this step (count pass bound)
     bool shapesDirty = true;
     int capShapes = 0, capHull = 0;
     // bodies
@@ -377,8 +378,10 @@ int sync_planes(jbgpu_world* w) {
     for (int k = 0; k < nw; k++) { start[k] = (int)list.size(); list.insert(list.end(), per[k].begin(), per[k].end()); }
     start[nw] = (int)list.size();
     dfree(B.planeList); dfree(B.planeStart); dfree(B.wstart); dfree(B.wend); dfree(B.wroot); dfree(B.bounds); dfree(B.total);
+    dfree(B.candBound);
     CK(dalloc(&B.planeList, std::max<size_t>(1, list.size()))); CK(dalloc(&B.planeStart, nw + 1));
     CK(dalloc(&B.wstart, nw)); CK(dalloc(&B.wend, nw)); CK(dalloc(&B.wroot, nw)); CK(dalloc(&B.bounds, 6)); CK(dalloc(&B.total, 1));
+    CK(dalloc(&B.candBound, 1));
     if (!list.empty()) CK(cudaMemcpy(B.planeList, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(B.planeStart, start.data(), sizeof(int) * (nw + 1), cudaMemcpyHostToDevice));
     B.nFinite = nf;
@@ -428,7 +431,9 @@ int stage_pairs(jbgpu_world* w) {
     w->orderValid = true;
     w->prof.mark(PH_PAIR_COUNT, 1, s);
     CK(cudaMemcpyAsync(w->hostPinned, w->bb.total, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(w->hostPinned + 2, w->bb.candBound, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    w->candBound = w->hostPinned[2];
     return stage_pairs_fill(w, *w->hostPinned);
 }
 
@@ -439,6 +444,8 @@ int stage_pairs_fill(jbgpu_world* w, int total) {
     int nxt = w->cur ^ 1;
     int rc = ensure_pair_capacity(w, nxt, total);
     if (rc) return rc;
+    if (w->hasMesh && concave_reserve(w->nb, w->capRows, w->candBound, s) < 0)
+        return fail(JBGPU_ERR_CUDA, "concave pass buffers");
     w->prof.mark(PH_PAIR_FILL, 0, s);
     broadphase_run_fill(d, w->bb, w->pairs[nxt], w->capRows, s);
     broadphase_persist(d, w->bb, w->pairs[nxt], w->pairs[w->cur], total, w->nPairs, s);
@@ -636,9 +643,9 @@ int narrow_and_islands(jbgpu_world* w, const int* cntp = nullptr) {
     CK(cudaEventRecord(w->evJoin, a));
     CK(cudaMemsetAsync(w->dw.ctr + C_GJK, 0, sizeof(int) * 2, s));
     narrowphase_launch(d, w->pairs[w->cur], w->nPairs, w->nb, s, &w->prof, cntp);
-    if (w->hasMesh) {
+    if (w->hasMesh) {   // buffers reserved for the count pass's bound (stage_pairs_fill, single_step_graph)
         w->prof.mark(PH_CONCAVE, 0, s);
-        if (concave_launch(d, w->pairs[w->cur], w->nPairs, cntp, w->nb, w->hostPinned + 8, s))
+        if (concave_launch_bounded(d, w->pairs[w->cur], w->nPairs, cntp, w->nb, w->candBound, s))
             return fail(JBGPU_ERR_CUDA, "concave narrowphase pass failed");
         w->prof.mark(PH_CONCAVE, 1, s);
     }
@@ -722,6 +729,7 @@ int single_step_graph(jbgpu_world* w, float dt) {
         launch_aabb(d, s);
         broadphase_run_count(d, B, s);
         CK(cudaMemcpyAsync(w->hostPinned + 1, B.total, sizeof(int), cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(w->hostPinned + 2, B.candBound, sizeof(int), cudaMemcpyDeviceToHost, s));
         return JBGPU_OK;
     }, captured);
     if (rc == GRAPH_FALLBACK) {            // nothing ran: undo the capture's host side
@@ -737,11 +745,17 @@ int single_step_graph(jbgpu_world* w, float dt) {
     w->orderValid = true;
     CK(cudaStreamSynchronize(s));
     const int total = w->hostPinned[1];
+    w->candBound = w->hostPinned[2];
     const int nxt = w->cur ^ 1;
     const int capBefore = w->capRows;
     void* keysBefore = w->pairs[nxt].keys;
     if ((rc = ensure_pair_capacity(w, nxt, total))) return rc;
     if (w->capRows != capBefore || w->pairs[nxt].keys != keysBefore) graphs_clear(w);
+    if (w->hasMesh) {   // the concave pass's buffers for this step's bound, before graph B is replayed
+        const int moved = concave_reserve(w->nb, w->capRows, w->candBound, s);
+        if (moved < 0) return fail(JBGPU_ERR_CUDA, "concave pass buffers");
+        if (moved) graphs_clear(w);
+    }
     if ((rc = prepare_solver(w))) return rc;
     const int old = w->cur;
     int* const offBefore = B.off;
@@ -793,11 +807,8 @@ int single_step_graph(jbgpu_world* w, float dt) {
     return JBGPU_OK;
 }
 
-// Worlds with triangle meshes step with launches: their concave pass reads its candidate count
-// back in the middle of the narrowphase.
 bool graph_usable(const jbgpu_world* w) {
-    return w->graphOn && w->graphError.empty() && !w->prof.active() && !w->mlp && !w->logSamples && w->nBodies > 0 &&
-           !w->hasMesh;
+    return w->graphOn && w->graphError.empty() && !w->prof.active() && !w->mlp && !w->logSamples && w->nBodies > 0;
 }
 }  // namespace
 
@@ -1198,6 +1209,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(B.bvh.left); dfree(B.bvh.right); dfree(B.bvh.lo); dfree(B.bvh.hi); dfree(B.bvh.parent); dfree(B.bvh.leafParent);
     dfree(B.bvh.visit); dfree(B.bvh.node); dfree(B.tcount); dfree(B.tcache); dfree(B.wstart); dfree(B.wend); dfree(B.wroot);
     dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.offPrev); dfree(B.cursor); dfree(B.total); dfree(B.partners);
+    dfree(B.candBound);
     NarrowBuffers& N = w->nb;
     if (N.queue) cudaFree(N.queue);
     dfree(N.queueCount); dfree(N.ovfQueue); dfree(N.ovfQueue2); dfree(N.ovfCount); dfree(N.pairBucket); dfree(N.perm); dfree(N.blockOff);
