@@ -161,13 +161,18 @@ typedef struct jbgpu_shape_desc {
                                 CAPSULE: radius, height (CapsuleShape(radius, height), up axis y);
                                 STATIC_PLANE: normal xyz, plane constant; CONVEX_HULL: unused;
                                 TRIANGLE_MESH, COMPOUND: params[0] = collision margin
-                                (setMargin; the reference's default is 0) */
+                                (setMargin; the reference's default is 0);
+                                TRIANGLE_MESH: params[1..3] = local scaling
+                                (setLocalScaling before setMargin; all zero: none) */
     const float* points;     /* CONVEX_HULL: num_points * 3 floats (ConvexHullShape(points));
                                 TRIANGLE_MESH: the vertex array, num_points * 3 floats */
     int32_t      num_points;
     /* TRIANGLE_MESH: BvhTriangleMeshShape(new TriangleIndexVertexArray(num_triangles, indices,
-       12, num_points, points, 12), true) - one part, scaling (1,1,1), the quantized tree
-       (collision/shapes/BvhTriangleMeshShape.java:69-93, OptimizedBvh.java:283-342). */
+       12, num_points, points, 12), true) - one part, the quantized tree
+       (collision/shapes/BvhTriangleMeshShape.java:69-93, OptimizedBvh.java:283-342); a scaling
+       given in params[1..3] is applied as setLocalScaling does (BvhTriangleMeshShape.java:195-212:
+       ignored within a squared distance of SIMD_EPSILON from (1,1,1), else every vertex is
+       multiplied by it and the tree rebuilt). */
     const int32_t* indices;  /* 3 vertex indices per triangle */
     int32_t      num_triangles;
     /* COMPOUND: CompoundShape with addChildShape(child_transforms[i], children[i]) in order

@@ -993,13 +993,33 @@ void compound_local_aabb(const std::vector<HostShape>& ch, const float* xf, int 
         for (int k = 0; k < 3; k++) { lmin[k] = jmin_h(lmin[k], mn[k]); lmax[k] = jmax_h(lmax[k], mx[k]); }
     }
 }
+// The vertices of a TRIANGLE_MESH descriptor as the reference reads them: each multiplied by the
+// mesh interface's scaling (VertexData.getTriangle, VertexData.java:50-55), which
+// BvhTriangleMeshShape.setLocalScaling sets - and rebuilds the tree over - only when it differs
+// from the current (1, 1, 1) by a squared length above SIMD_EPSILON
+// (BvhTriangleMeshShape.java:195-212).  params[1..3] all zero: no scaling.
+const float* mesh_vertices(const jbgpu_shape_desc& d, std::vector<float>& buf) {
+    const float sx = d.params[1], sy = d.params[2], sz = d.params[3];
+    if (!d.points || d.num_points <= 0 || (sx == 0.0f && sy == 0.0f && sz == 0.0f)) return d.points;
+    const float dx = 1.0f - sx, dy = 1.0f - sy, dz = 1.0f - sz;
+    const float l2 = dx * dx + dy * dy + dz * dz;
+    if (!(l2 > 1.1920929e-7f)) return d.points;
+    buf.resize((size_t)3 * d.num_points);
+    for (int i = 0; i < d.num_points; i++) {
+        buf[3 * i] = d.points[3 * i] * sx;
+        buf[3 * i + 1] = d.points[3 * i + 1] * sy;
+        buf[3 * i + 2] = d.points[3 * i + 2] * sz;
+    }
+    return buf.data();
+}
 }  // namespace
 
 int jbgpu_shape_mesh_bvh(const jbgpu_shape_desc* d, int32_t* nodes, int32_t capacity, int32_t* n, float aabb[6]) {
     if (!d || !n || d->type != JBGPU_SHAPE_TRIANGLE_MESH || capacity < 0 || (capacity > 0 && !nodes))
         return fail(JBGPU_ERR_INVALID_ARGUMENT, "a TRIANGLE_MESH descriptor, a count pointer and a node buffer");
     MeshBvh m;
-    if (build_mesh_bvh(d->points, d->num_points, d->indices, d->num_triangles, m))
+    std::vector<float> scaled;
+    if (build_mesh_bvh(mesh_vertices(*d, scaled), d->num_points, d->indices, d->num_triangles, m))
         return fail(JBGPU_ERR_INVALID_ARGUMENT, "a triangle mesh needs vertices, 1 .. 2^21-1 triangles and indices "
                                                 "within the vertex array");
     *n = (int)m.nodes.size();
@@ -1275,9 +1295,11 @@ int jbgpu_world_add_shapes(jbgpu_world* w, const jbgpu_shape_desc* shapes, int32
             h.plane[0] = x; h.plane[1] = y; h.plane[2] = z; h.plane[3] = d.params[3];
             break;
         }
-        case JBGPU_SHAPE_TRIANGLE_MESH: {   // BvhTriangleMeshShape(TriangleIndexVertexArray, true), setMargin
+        case JBGPU_SHAPE_TRIANGLE_MESH: {   // BvhTriangleMeshShape(TriangleIndexVertexArray, true),
+                                            // setLocalScaling, setMargin
             MeshBvh m;
-            if (build_mesh_bvh(d.points, d.num_points, d.indices, d.num_triangles, m))
+            std::vector<float> scaled;
+            if (build_mesh_bvh(mesh_vertices(d, scaled), d.num_points, d.indices, d.num_triangles, m))
                 return fail(JBGPU_ERR_INVALID_ARGUMENT, "a triangle mesh needs vertices, 1 .. 2^21-1 triangles and "
                                                         "indices within the vertex array");
             h.margin = d.params[0];

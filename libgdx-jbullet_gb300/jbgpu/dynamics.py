@@ -99,7 +99,7 @@ class StaticPlaneShape(_Shape):
 
 class TriangleIndexVertexArray:
     """collision/shapes/TriangleIndexVertexArray.java with one IndexedMesh part: triangle vertex
-    indices (m, 3) and vertices (n, 3); scaling (1, 1, 1)."""
+    indices (m, 3) and vertices (n, 3); its scaling is set through BvhTriangleMeshShape.setLocalScaling."""
 
     def __init__(self, triangleIndices, vertices):
         self.indices = np.ascontiguousarray(triangleIndices, np.int32).reshape(-1, 3)
@@ -120,11 +120,29 @@ class BvhTriangleMeshShape(_Shape):
             raise NotImplementedError("only the quantized tree (useQuantizedAabbCompression=True) is built")
         self.meshInterface = meshInterface
         self.margin = 0.0   # ConcaveShape.collisionMargin
+        self.scaling = (0.0, 0.0, 0.0)   # (0, 0, 0): setLocalScaling not called
 
     def setMargin(self, margin):
         if self._id is not None:
             raise RuntimeError("setMargin after the shape was added to a world")
         self.margin = float(margin)
+
+    def setLocalScaling(self, scaling):
+        """BvhTriangleMeshShape.setLocalScaling (java:195-212): the tree is rebuilt over the scaled
+        vertices.  Its quantization bounds then include the margin set so far, so only a call
+        before setMargin is supported."""
+        if self._id is not None:
+            raise RuntimeError("setLocalScaling after the shape was added to a world")
+        if self.margin != 0.0:
+            raise NotImplementedError("setLocalScaling after setMargin (the rebuilt tree's bounds would include the margin)")
+        self.scaling = tuple(float(x) for x in scaling)
+
+    def getLocalScaling(self):
+        s = self.scaling
+        d = np.float32(1.0) - np.asarray(s, np.float32)
+        if s == (0.0, 0.0, 0.0) or not (np.float32(d[0] * d[0] + d[1] * d[1]) + np.float32(d[2] * d[2]) > np.float32(1.1920929e-7)):
+            return np.ones(3, np.float32)
+        return np.asarray(s, np.float32)
 
     def getMargin(self):
         return self.margin
@@ -133,7 +151,7 @@ class BvhTriangleMeshShape(_Shape):
         return self.meshInterface
 
     def desc(self):
-        return {"type": _abi.SHAPE_TRIANGLE_MESH, "params": (self.margin, 0.0, 0.0, 0.0),
+        return {"type": _abi.SHAPE_TRIANGLE_MESH, "params": (self.margin,) + self.scaling,
                 "points": self.meshInterface.vertices, "indices": self.meshInterface.indices}
 
     def calculateLocalInertia(self, mass):

@@ -920,10 +920,10 @@ def rot_z(a):
     return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]], F)
 
 
-def terrain_mesh(nx=24, nz=24, size=24.0, amp=1.2, seed=0, margin=0.0, bowl=0.4):
+def terrain_mesh(nx=24, nz=24, size=24.0, amp=1.2, seed=0, margin=0.0, bowl=0.4, scaling=(0.0, 0.0, 0.0)):
     """A heightfield of nx x nz cells over size x size m (two triangles per cell, alternating
     diagonals, counter-clockwise seen from above) with smooth random bumps of about amp m on a
-    bowl: the shape dict of a BvhTriangleMeshShape."""
+    bowl: the shape dict of a BvhTriangleMeshShape (scaling: its setLocalScaling, (0, 0, 0) none)."""
     rng = np.random.Generator(np.random.PCG64(seed + 7))
     xs = np.linspace(-size / 2, size / 2, nx + 1)
     zs = np.linspace(-size / 2, size / 2, nz + 1)
@@ -943,8 +943,8 @@ def terrain_mesh(nx=24, nz=24, size=24.0, amp=1.2, seed=0, margin=0.0, bowl=0.4)
                 idx += [(a, d, c), (a, c, b)]
             else:
                 idx += [(a, d, b), (d, c, b)]
-    return {"type": _abi.SHAPE_TRIANGLE_MESH, "params": (float(margin), 0.0, 0.0, 0.0), "points": verts,
-            "indices": np.asarray(idx, np.int32)}
+    return {"type": _abi.SHAPE_TRIANGLE_MESH, "params": (float(margin),) + tuple(float(x) for x in scaling),
+            "points": verts, "indices": np.asarray(idx, np.int32)}
 
 
 def _convex_kinds(rng, n, hull_pts=12):
@@ -1021,12 +1021,14 @@ def _compound_kinds(rng, n):
     return out
 
 
-def terrain(n=60, seed=0, cells=16, size=16.0, compounds=0, steps=200, region=(10.0, 6.0, 10.0), y0=4.0, bowl=0.4):
+def terrain(n=60, seed=0, cells=16, size=16.0, compounds=0, steps=200, region=(10.0, 6.0, 10.0), y0=4.0, bowl=0.4,
+            mesh_scaling=(0.0, 0.0, 0.0)):
     """Convex bodies (boxes, spheres, capsules, hulls; density 1000) and optionally compound bodies
     dropped on a static triangle-mesh terrain (a BvhTriangleMeshShape heightfield of cells x cells
-    quads over size x size m); no plane; 10 iterations, dt 1/60."""
+    quads over size x size m, with setLocalScaling(mesh_scaling) unless it is (0, 0, 0)); no plane;
+    10 iterations, dt 1/60."""
     rng = np.random.Generator(np.random.PCG64(seed))
-    shapes = [terrain_mesh(cells, cells, size, seed=seed, bowl=bowl)]
+    shapes = [terrain_mesh(cells, cells, size, seed=seed, bowl=bowl, scaling=mesh_scaling)]
     kinds = _convex_kinds(rng, n) + _compound_kinds(rng, compounds)
     order = rng.permutation(len(kinds))
     kinds = [kinds[i] for i in order]

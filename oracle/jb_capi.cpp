@@ -32,7 +32,8 @@ static Shape shape_from_desc(const jbgpu_shape_desc* d) {
     case JBGPU_SHAPE_CAPSULE: return make_capsule(d->params[0], d->params[1]);
     case JBGPU_SHAPE_CONVEX_HULL: return make_hull(d->points, d->num_points);
     case JBGPU_SHAPE_TRIANGLE_MESH:
-        return make_mesh(d->points, d->num_points, d->indices, d->num_triangles, d->params[0]);
+        return make_mesh(d->points, d->num_points, d->indices, d->num_triangles, d->params[0],
+                         v3(d->params[1], d->params[2], d->params[3]));
     case JBGPU_SHAPE_COMPOUND: {
         std::vector<Shape> ch;
         std::vector<Xf> xf;

@@ -377,16 +377,27 @@ struct BvhBuild {
 };
 }  // namespace
 
-Shape make_mesh(const float* vtx, int nv, const int* idx, int nt, float margin) {
+Shape make_mesh(const float* vtx, int nv, const int* idx, int nt, float margin, V3 scaling) {
     Shape s;
     s.type = TRIANGLE_MESH;
     s.collisionMargin = 0.0f;   // ConcaveShape.collisionMargin
+    // BvhTriangleMeshShape.setLocalScaling (java:195-212): the mesh interface's scaling is set,
+    // and the tree rebuilt over the scaled triangles, only when the scaling differs from the
+    // current (1, 1, 1) by a squared length above SIMD_EPSILON; the margin is still 0 then, so the
+    // rebuilt tree's quantization bounds equal the brute-force box of the scaled vertices
+    bool scaled = false;
+    if (!(scaling.x == 0.0f && scaling.y == 0.0f && scaling.z == 0.0f)) {
+        const V3 d = sub(v3(1.0f, 1.0f, 1.0f), scaling);
+        scaled = len2(d) > 1.1920929e-7f;
+    }
     auto md = std::make_shared<MeshData>();
     md->tri.resize((size_t)3 * nt);
-    for (int i = 0; i < nt; i++)   // VertexData.getTriangle with scaling (1,1,1)
+    for (int i = 0; i < nt; i++)   // VertexData.getTriangle (VertexData.java:50-55): vertex times scaling
         for (int k = 0; k < 3; k++) {
             int v = idx[3 * i + k];
-            md->tri[3 * i + k] = v3(vtx[3 * v], vtx[3 * v + 1], vtx[3 * v + 2]);
+            V3 p = v3(vtx[3 * v], vtx[3 * v + 1], vtx[3 * v + 2]);
+            if (scaled) p = v3(p.x * scaling.x, p.y * scaling.y, p.z * scaling.z);
+            md->tri[3 * i + k] = p;
         }
     (void)nv;
     // StridingMeshInterface.calculateAabbBruteForce (StridingMeshInterface.java:70-87)

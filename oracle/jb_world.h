@@ -63,7 +63,9 @@ Shape make_capsule(float radius, float height);
 Shape make_hull(const float* pts, int n);
 Shape make_plane(V3 normal, float constant);
 // BvhTriangleMeshShape(new TriangleIndexVertexArray(...), true) with ConcaveShape.setMargin(margin)
-Shape make_mesh(const float* vertices, int numVertices, const int* indices, int numTriangles, float margin);
+// scaling: BvhTriangleMeshShape.setLocalScaling before setMargin ((0, 0, 0): not called)
+Shape make_mesh(const float* vertices, int numVertices, const int* indices, int numTriangles, float margin,
+                V3 scaling = V3{0.0f, 0.0f, 0.0f});
 // CompoundShape with addChildShape(transform, child) for each child in order, then setMargin(margin)
 Shape make_compound(const std::vector<Shape>& children, const std::vector<Xf>& xf, float margin);
 // OptimizedBvh.reportAabbOverlappingNodex: triangle indices in the order the walk reports them

@@ -34,12 +34,32 @@ def _meshes():
     one = {"type": _abi.SHAPE_TRIANGLE_MESH, "params": (0.02, 0.0, 0.0, 0.0),
            "points": np.array([[0, 0, 0], [1, 0, 0], [0, 0, 1]], F), "indices": np.array([[0, 2, 1]], np.int32)}
     out.append(one)
+    # BvhTriangleMeshShape.setLocalScaling: a scaling that rebuilds the tree, and one within
+    # SIMD_EPSILON (squared) of (1, 1, 1) that the reference ignores
+    out.append(scenes.terrain_mesh(24, 24, 24.0, seed=2, scaling=(1.5, 0.6, 0.8)))
+    out.append(scenes.terrain_mesh(7, 13, 30.0, amp=4.0, seed=3, scaling=(1.0001, 1.0, 0.9999)))
     return out
+
+
+NMESH = 7
+
+
+def _scaled_points(mesh):
+    """The vertices as the reference reads them (VertexData.getTriangle: times the scaling, set by
+    setLocalScaling only when it is more than SIMD_EPSILON (squared) away from (1, 1, 1))."""
+    p = np.asarray(mesh["points"], F)
+    s = np.asarray(mesh["params"][1:4], F)
+    if not s.any():
+        return p
+    d = F(1) - s
+    if not (F(d[0] * d[0] + d[1] * d[1]) + F(d[2] * d[2]) > F(1.1920929e-7)):
+        return p
+    return (p * s).astype(F)
 
 
 def _quantizer(mesh):
     """OptimizedBvh.setQuantizationValues / quantizeWithClamp in binary32 (for the brute force)."""
-    p = np.asarray(mesh["points"], F)[np.asarray(mesh["indices"]).reshape(-1)]
+    p = _scaled_points(mesh)[np.asarray(mesh["indices"]).reshape(-1)]
     bmin, bmax = p.min(0) - F(1), p.max(0) + F(1)
     q = F(65535.0) / (bmax - bmin)
 
@@ -57,7 +77,7 @@ def _unpack(nodes):
     return qmin, qmax, nodes[:, 3]
 
 
-@pytest.mark.parametrize("k", range(5))
+@pytest.mark.parametrize("k", range(NMESH))
 def test_mesh_tree_library_equals_oracle(gpu_lib, oracle_lib, k):
     mesh = _meshes()[k]
     ln, la = jl.mesh_bvh(mesh)
@@ -66,7 +86,7 @@ def test_mesh_tree_library_equals_oracle(gpu_lib, oracle_lib, k):
     assert np.array_equal(la.view(np.uint32), oa.view(np.uint32))
 
 
-@pytest.mark.parametrize("k", range(5))
+@pytest.mark.parametrize("k", range(NMESH))
 def test_mesh_tree_structure(oracle_lib, k):
     mesh = _meshes()[k]
     nodes, aabb = pyoracle.mesh_bvh(mesh)
@@ -83,17 +103,48 @@ def test_mesh_tree_structure(oracle_lib, k):
         assert -w[i] == 1 + left + right
         return -w[i]
     assert size(0) == len(nodes)
-    p = np.asarray(mesh["points"], F)[np.asarray(mesh["indices"]).reshape(-1)]
+    p = _scaled_points(mesh)[np.asarray(mesh["indices"]).reshape(-1)]
     assert np.array_equal(aabb[:3], p.min(0)) and np.array_equal(aabb[3:], p.max(0))
 
 
-@pytest.mark.parametrize("k", range(5))
+def test_mesh_scaling_rebuilds_over_the_scaled_vertices(gpu_lib, oracle_lib):
+    """setLocalScaling's tree is the tree of the scaled vertex array; a scaling within
+    SIMD_EPSILON of (1, 1, 1) leaves the mesh as it was."""
+    meshes = _meshes()
+    scaled, near = meshes[5], meshes[6]
+    plain = dict(scaled, params=(0.0, 0.0, 0.0, 0.0), points=_scaled_points(scaled))
+    assert not np.array_equal(plain["points"], scaled["points"])
+    for fn in (jl.mesh_bvh, pyoracle.mesh_bvh):
+        a, b = fn(scaled), fn(plain)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32))
+        c, d = fn(near), fn(dict(near, params=(0.0, 0.0, 0.0, 0.0)))
+        assert np.array_equal(c[0], d[0]) and np.array_equal(c[1].view(np.uint32), d[1].view(np.uint32))
+
+
+def test_mirror_mesh_scaling_order():
+    """The mirror takes setLocalScaling before setMargin (the reference's rebuilt tree would take
+    the margin into its quantization bounds otherwise) and reports the scaling the reference keeps."""
+    from jbgpu import dynamics as D
+    tm = scenes.terrain_mesh(4, 4, 8.0, seed=1)
+    s = D.BvhTriangleMeshShape(D.TriangleIndexVertexArray(tm["indices"], tm["points"]), True)
+    assert np.array_equal(s.getLocalScaling(), np.ones(3, F))
+    s.setLocalScaling((1.0001, 1.0, 1.0))
+    assert np.array_equal(s.getLocalScaling(), np.ones(3, F))
+    s.setLocalScaling((2.0, 0.5, 1.0))
+    s.setMargin(0.04)
+    assert s.desc()["params"] == (0.04, 2.0, 0.5, 1.0)
+    assert np.array_equal(s.getLocalScaling(), np.array([2.0, 0.5, 1.0], F))
+    with pytest.raises(NotImplementedError):
+        s.setLocalScaling((1.5, 1.5, 1.5))
+
+
+@pytest.mark.parametrize("k", range(NMESH))
 def test_mesh_walk_reports_overlapping_leaves_in_node_order(oracle_lib, k):
     mesh = _meshes()[k]
     nodes, _ = pyoracle.mesh_bvh(mesh)
     qmin, qmax, w = _unpack(nodes)
     quant = _quantizer(mesh)
-    p = np.asarray(mesh["points"], F)[np.asarray(mesh["indices"]).reshape(-1)]
+    p = _scaled_points(mesh)[np.asarray(mesh["indices"]).reshape(-1)]
     lo, hi = p.min(0), p.max(0)
     rng = np.random.Generator(np.random.PCG64(k))
     for _ in range(40):
@@ -180,11 +231,13 @@ SCENES = {
     "terrain_compounds": lambda: scenes.terrain(30, compounds=12, seed=2),
     "compounds": lambda: scenes.compounds(30, 10, seed=3),
     "terrain_margin": lambda: _with_mesh_margin(scenes.terrain(30, compounds=4, seed=5), 0.05),
+    "terrain_scaled": lambda: _with_mesh_margin(scenes.terrain(30, compounds=4, seed=7, mesh_scaling=(1.3, 0.7, 1.1)),
+                                                0.02),
 }
 
 
 def _with_mesh_margin(sc, m):
-    sc.shapes[0] = dict(sc.shapes[0], params=(m, 0.0, 0.0, 0.0))
+    sc.shapes[0] = dict(sc.shapes[0], params=(m,) + tuple(sc.shapes[0]["params"][1:4]))
     return sc
 
 
@@ -521,13 +574,16 @@ def test_f3_ccd_with_compounds_closed_loop_bit_exact(gpu_lib, oracle_lib):
 @pytest.mark.gpu
 def test_mirror_compound_on_mesh_reads_like_the_reference(gpu_lib, oracle_lib):
     """The reference's usage through the Python mirror: a BvhTriangleMeshShape ground over a
-    TriangleIndexVertexArray, CompoundShape dumbbells built with addChildShape and a box; two
-    seconds of stepSimulation.  The same world given to the oracle ends bit-identical."""
+    TriangleIndexVertexArray (setLocalScaling, then setMargin), CompoundShape dumbbells built with
+    addChildShape and a box; two seconds of stepSimulation.  The same world given to the oracle
+    ends bit-identical."""
     from jbgpu import dynamics as D
     tm = scenes.terrain_mesh(8, 8, 12.0, seed=4)
     world = D.DiscreteDynamicsWorld()
     world.setGravity((0.0, -9.81, 0.0))
     ground_shape = D.BvhTriangleMeshShape(D.TriangleIndexVertexArray(tm["indices"], tm["points"]), True)
+    ground_shape.setLocalScaling((1.2, 0.8, 1.1))
+    ground_shape.setMargin(0.01)
     ground = D.RigidBody(D.RigidBodyConstructionInfo(0.0, None, ground_shape))
     world.addRigidBody(ground)
     bell = D.CompoundShape()
