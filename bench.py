@@ -601,16 +601,19 @@ def run_ours(args, dist):
             m.close()
     last_c = ctrs[-1] if ctrs else final
     config = bench_config(sc, args, iters)
-    config["parallelism"] = split["mode"] if dist.size > 1 else "one world per GPU"
+    # the workload only, key for key as the reference arm prints it; how each arm runs it is
+    # in "execution"
+    config["parallelism"] = split["mode"] if dist.size > 1 else "one world"
     config["split"] = split
-    config["last_step_counters"] = {k: last_c[k] for k in ("pairs", "contacts", "solver_manifolds", "solver_rows",
-                                                           "colours", "cut_colours", "cut_manifolds", "islands",
-                                                           "gjk_calls", "epa_calls")}
+    last_step_counters = {k: last_c[k] for k in ("pairs", "contacts", "solver_manifolds", "solver_rows", "colours",
+                                                 "cut_colours", "cut_manifolds", "islands", "gjk_calls", "epa_calls")}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.size, "steps": K, "warmup": W,
         "ms_per_step": elapsed * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic: seeded PCG64 scene generator (no dataset exists for this workload)",
         "config": config,
+        "execution": "one world per GPU" if dist.size == 1 else "worlds split across the GPUs (config.split)",
+        "last_step_counters": last_step_counters,
         "timing": {"value_from": "CUDA events on the world's stream around the K steps (jbgpu_world_timer)",
                    "device_ms": device_ms, "host_wall_ms": wall * 1e3,
                    "phases_from": "a second run of the same steps with per-phase event marks",
@@ -663,7 +666,7 @@ def run_reference(args, dist):
     el = time.perf_counter() - t0
     value = sc.n_bodies * done / el
     config = bench_config(sc, args, cfg.num_iterations)
-    config["parallelism"] = "one world, one host thread"
+    config["parallelism"] = "one world"
     config["split"] = {"mode": "single", "worlds": 1 if sc.world_of_body is None else int(sc.world_of_body.max()) + 1}
     sample = ("CPU restatement of the reference (oracle; no JVM on this machine), 1 thread, full workload, steps "
               "%d..%d (%d of the %d asked, %.0f s budget), started from the GPU world's state and manifolds at step %d "
@@ -673,6 +676,7 @@ def run_reference(args, dist):
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded PCG64 scene generator (no dataset exists for this workload)",
             "config": config,
+            "execution": "one world, one host thread",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
