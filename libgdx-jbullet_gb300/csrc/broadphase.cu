@@ -333,6 +333,84 @@ __global__ void k_segment_sort(DevWorld w, int n, const int* off, const int* cnt
     }
 }
 
+// The same for worlds without compounds, in two passes.  A thread per owner sorts a segment of up
+// to SEG_REG partner words in registers (a bitonic network over 8, padding words 0xffffffff
+// sorting last) and lists the owners of longer segments; then a warp per listed owner sorts up
+// to 32 words across the lanes by a bitonic network, a crowded segment in place by one lane.
+constexpr int SEG_REG = 8;
+__global__ void k_segment_sort_short(int n, const int* off, const int* cnt, const int* partners, uint64_t* keys,
+                                     int capacity, int* longList, int* longCount) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;   // the grid covers whole warps
+    int o = 0, c = 0;
+    if (i < n) {
+        o = off[i];
+        c = cnt[i];
+        if (o + c > capacity) c = 0;
+    }
+    if (c > 0 && c <= SEG_REG) {
+        const unsigned* p = (const unsigned*)partners + o;
+        unsigned r[SEG_REG];
+#pragma unroll
+        for (int k = 0; k < SEG_REG; k++) r[k] = k < c ? p[k] : 0xffffffffu;
+#pragma unroll
+        for (int k = 2; k <= SEG_REG; k <<= 1)
+#pragma unroll
+            for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+                for (int a = 0; a < SEG_REG; a++) {
+                    const int b = a ^ j;
+                    if (b > a) {
+                        const unsigned x = r[a], y = r[b];
+                        if ((x > y) == ((a & k) == 0)) { r[a] = y; r[b] = x; }
+                    }
+                }
+        const uint64_t hi = (uint64_t)(unsigned)i << 32;
+#pragma unroll
+        for (int k = 0; k < SEG_REG; k++)
+            if (k < c) keys[o + k] = hi | r[k];
+    }
+    const bool lng = c > SEG_REG;
+    const unsigned m = __ballot_sync(0xffffffffu, lng);
+    if (m) {
+        const int leader = __ffs(m) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(longCount, __popc(m));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (lng) longList[base + __popc(m & ((1u << lane) - 1u))] = i;
+    }
+}
+__global__ void k_segment_sort_long(const int* off, const int* cnt, int* partners, uint64_t* keys, const int* longList,
+                                    const int* longCount) {
+    const int lane = threadIdx.x & 31;
+    const int nl = *longCount, nw = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int q = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); q < nl; q += nw) {   // uniform per warp
+        const int i = longList[q], o = off[i], c = cnt[i];
+        const uint64_t hi = (uint64_t)(unsigned)i << 32;
+        unsigned* p = (unsigned*)partners + o;
+        if (c <= 32) {
+            unsigned v = lane < c ? p[lane] : 0xffffffffu;
+            for (int k = 2; k <= 32; k <<= 1)
+                for (int j = k >> 1; j > 0; j >>= 1) {
+                    const unsigned u = __shfl_xor_sync(0xffffffffu, v, j);
+                    v = (((lane & j) == 0) == ((lane & k) == 0)) ? min(v, u) : max(v, u);
+                }
+            if (lane < c) keys[o + lane] = hi | v;
+        } else {
+            if (lane == 0)
+                for (int gap = c / 2; gap > 0; gap /= 2)   // Shell sort for rare crowded owners
+                    for (int k = gap; k < c; k++) {
+                        const unsigned x = p[k];
+                        int j = k;
+                        while (j >= gap && p[j - gap] > x) { p[j] = p[j - gap]; j -= gap; }
+                        p[j] = x;
+                    }
+            __syncwarp();
+            for (int k = lane; k < c; k += 32) keys[o + k] = hi | p[k];
+            __syncwarp();
+        }
+    }
+}
+
 // Carry manifolds of persisting pairs (binary search in last step's sorted keys: within the
 // owner's segment when last step's per-owner offsets are at hand, else over all of them).
 __global__ void k_persist(DevWorld w, DevPairs nw, DevPairs old, int nNew, int nOld, const int* offPrev, const int* newCnt,
@@ -465,7 +543,18 @@ void broadphase_run_fill(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw,
     if (bb.nPlanes > 0)
         k_plane_pairs<true><<<gridn(n, 256), 256, 0, s>>>(w, bb.planeList, bb.planeStart, nullptr, bb.off, bb.cursor,
                                                            bb.partners, capacity, nullptr); note_launch();
-    k_segment_sort<<<gridn(n, 128), 128, 0, s>>>(w, n, bb.off, bb.cursor, bb.partners, nw.keys, capacity); note_launch();
+    if (w.hasCompound) {
+        k_segment_sort<<<gridn(n, 128), 128, 0, s>>>(w, n, bb.off, bb.cursor, bb.partners, nw.keys, capacity);
+    } else {
+        // the long segments' owners are listed in tcount, which the filling traversal has read
+        cudaMemsetAsync(bb.segLong, 0, sizeof(int), s);
+        k_segment_sort_short<<<gridn(n, 128), 128, 0, s>>>(n, bb.off, bb.cursor, bb.partners, nw.keys, capacity,
+                                                            bb.tcount, bb.segLong);
+        note_launch();
+        k_segment_sort_long<<<std::min(gridn(n, 4), 1024), 128, 0, s>>>(bb.off, bb.cursor, bb.partners, nw.keys,
+                                                                        bb.tcount, bb.segLong);
+    }
+    note_launch();
 }
 
 void broadphase_persist(const DevWorld& w, BroadphaseBuffers& bb, DevPairs& nw, const DevPairs& old, int nNew, int nOld,

@@ -19,7 +19,7 @@ struct Bvh {           // Karras radix tree over nf sorted leaves; internal node
     float4* node;
 };
 
-constexpr int TRAV_CACHE = 32;         // pairs a counting traversal keeps for the filling one
+constexpr int TRAV_CACHE = 64;         // pairs a counting traversal keeps for the filling one
 
 struct BroadphaseBuffers {
     int nFinite = 0, nPlanes = 0, nWorlds = 1, worldBits = 0;
@@ -45,6 +45,7 @@ struct BroadphaseBuffers {
     bool offPrevValid = false;           // offPrev matches the previous pair array
     int* cursor = nullptr;               // fill cursors (n + 1)
     int* total = nullptr;                // device total pair count
+    int* segLong = nullptr;              // device: owners whose partner segments the warp pass sorts
     int* candBound = nullptr;            // device: the concave pass's candidates, bounded by the count pass
     int* partners = nullptr;             // CSR partner lists (pair capacity)
     int* tcount = nullptr;               // per sorted leaf: pairs its counting traversal found

@@ -378,10 +378,10 @@ int sync_planes(jbgpu_world* w) {
     for (int k = 0; k < nw; k++) { start[k] = (int)list.size(); list.insert(list.end(), per[k].begin(), per[k].end()); }
     start[nw] = (int)list.size();
     dfree(B.planeList); dfree(B.planeStart); dfree(B.wstart); dfree(B.wend); dfree(B.wroot); dfree(B.bounds); dfree(B.total);
-    dfree(B.candBound);
+    dfree(B.candBound); dfree(B.segLong);
     CK(dalloc(&B.planeList, std::max<size_t>(1, list.size()))); CK(dalloc(&B.planeStart, nw + 1));
     CK(dalloc(&B.wstart, nw)); CK(dalloc(&B.wend, nw)); CK(dalloc(&B.wroot, nw)); CK(dalloc(&B.bounds, 6)); CK(dalloc(&B.total, 1));
-    CK(dalloc(&B.candBound, 1));
+    CK(dalloc(&B.candBound, 1)); CK(dalloc(&B.segLong, 1));
     if (!list.empty()) CK(cudaMemcpy(B.planeList, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(B.planeStart, start.data(), sizeof(int) * (nw + 1), cudaMemcpyHostToDevice));
     B.nFinite = nf;
@@ -1229,7 +1229,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     dfree(B.bvh.left); dfree(B.bvh.right); dfree(B.bvh.lo); dfree(B.bvh.hi); dfree(B.bvh.parent); dfree(B.bvh.leafParent);
     dfree(B.bvh.visit); dfree(B.bvh.node); dfree(B.tcount); dfree(B.tcache); dfree(B.wstart); dfree(B.wend); dfree(B.wroot);
     dfree(B.planeList); dfree(B.planeStart); dfree(B.cnt); dfree(B.off); dfree(B.offPrev); dfree(B.cursor); dfree(B.total); dfree(B.partners);
-    dfree(B.candBound);
+    dfree(B.candBound); dfree(B.segLong);
     NarrowBuffers& N = w->nb;
     if (N.queue) cudaFree(N.queue);
     dfree(N.queueCount); dfree(N.ovfQueue); dfree(N.ovfQueue2); dfree(N.ovfCount); dfree(N.pairBucket); dfree(N.perm); dfree(N.blockOff);
