@@ -15,6 +15,9 @@
  *   jbgpu_world_add_shape         BoxShape/SphereShape/CapsuleShape/ConvexHullShape/StaticPlaneShape constructors
  *                                 (collision/shapes/BoxShape.java:46-50, SphereShape.java:38-41,
  *                                 CapsuleShape.java:55-58, ConvexHullShape.java:44-50, StaticPlaneShape.java:45-48)
+ *   jbgpu_world_refit_mesh        BvhTriangleMeshShape.refitTree + CollisionWorld.updateSingleAabb
+ *                                 (collision/shapes/BvhTriangleMeshShape.java:172-178,
+ *                                 collision/dispatch/CollisionWorld.java:195-224)
  *   jbgpu_shape_local_inertia     CollisionShape.calculateLocalInertia (BoxShape.java:153-167,
  *                                 SphereShape.java:72-76, CapsuleShape.java:125-153, PolyhedralConvexShape.java:133-159)
  *   jbgpu_world_add_bodies        new RigidBody(RigidBodyConstructionInfo) + DiscreteDynamicsWorld.addRigidBody
@@ -288,6 +291,17 @@ int jbgpu_world_destroy(jbgpu_world* world);
 int jbgpu_world_add_shape(jbgpu_world* world, const jbgpu_shape_desc* shape, int32_t* shape_id);
 /* n shapes at once; ids_out (may be NULL) receives consecutive ids. */
 int jbgpu_world_add_shapes(jbgpu_world* world, const jbgpu_shape_desc* shapes, int32_t n, int32_t* ids_out);
+/* BvhTriangleMeshShape.refitTree (collision/shapes/BvhTriangleMeshShape.java:172-178) after the
+ * positions of a TRIANGLE_MESH shape's vertices changed: points holds num_points * 3 floats (the
+ * shape's vertex count; its triangle indices and scaling stay).  The tree keeps its topology and
+ * is requantized as OptimizedBvh.refit does (OptimizedBvh.java:344-367,411-470), the local aabb is
+ * recomputed with the shape's margin, and every body with the shape gets
+ * CollisionWorld.updateSingleAabb (CollisionWorld.java:195-224) before the next step. */
+int jbgpu_world_refit_mesh(jbgpu_world* world, int32_t shape, const float* points, int32_t num_points);
+/* The current tree and local aabb of a TRIANGLE_MESH shape of the world (after any refit), in
+ * jbgpu_shape_mesh_bvh's layout.  Host only. */
+int jbgpu_world_mesh_bvh(const jbgpu_world* world, int32_t shape, int32_t* nodes, int32_t capacity, int32_t* n_nodes,
+                         float local_aabb[6]);
 int jbgpu_world_add_bodies(jbgpu_world* world, const jbgpu_body_desc* bodies, int32_t n, int32_t* uids_out);
 int jbgpu_world_num_bodies(const jbgpu_world* world, int32_t* n);
 

@@ -147,6 +147,30 @@ struct Builder {
     }
 };
 
+// TriangleMeshShape.recalcLocalAabb (TriangleMeshShape.java:79-95): per axis the first vertex, in
+// walk order (every leaf), with the largest (smallest) coordinate, taken through the dot with the
+// unit axis as the support callback does, plus (minus) the shape's margin at that time.
+void local_aabb(MeshBvh& m, float margin) {
+    const int nn = (int)m.nodes.size();
+    for (int k = 0; k < 3; k++) {
+        for (int sg = 0; sg < 2; sg++) {
+            float dir[3] = {0.0f, 0.0f, 0.0f};
+            dir[k] = sg == 0 ? 1.0f : -1.0f;
+            float best = -1e30f, sup = 0.0f;
+            for (int i = 0; i < nn; i++) {
+                if (m.nodes[i].w < 0) continue;
+                for (int j = 0; j < 3; j++) {
+                    const float4& p = m.tris[3 * (m.nodes[i].w & ((1 << 21) - 1)) + j];
+                    const float d = dir[0] * p.x + dir[1] * p.y + dir[2] * p.z;
+                    if (d > best) { best = d; sup = k == 0 ? p.x : (k == 1 ? p.y : p.z); }
+                }
+            }
+            if (sg == 0) m.lmax[k] = sup + margin;
+            else m.lmin[k] = sup - margin;
+        }
+    }
+}
+
 }  // namespace
 
 int build_mesh_bvh(const float* v, int nv, const int* idx, int nt, MeshBvh& out) {
@@ -199,27 +223,60 @@ int build_mesh_bvh(const float* v, int nv, const int* idx, int nt, MeshBvh& out)
                                  (int)((unsigned)q[4] | ((unsigned)q[5] << 16)), b.nodeW[i]);
     }
     for (int k = 0; k < 3; k++) { out.bmin[k] = b.bmin[k]; out.bmax[k] = b.bmax[k]; out.quant[k] = b.quant[k]; }
-    // recalcLocalAabb: per axis the first vertex, in walk order (every leaf), with the largest
-    // (smallest) coordinate, taken through the dot with the unit axis as the support callback
-    // does; the shape's margin is 0 when the constructor runs
+    local_aabb(out, 0.0f);   // the shape's margin is 0 when the constructor runs
+    return 0;
+}
+
+// OptimizedBvh.refit (OptimizedBvh.java:344-367): the quantization from the new brute-force box;
+// updateBvhNodes (java:411-470) from the last node to the first: a leaf's box from its triangle
+// (without the build's minimum extent), an internal node's the union of its two children's
+// quantized boxes (the right child follows the left one's subtree); then recalcLocalAabb with
+// the current margin (BvhTriangleMeshShape.refitTree, java:172-178).
+void refit_mesh_bvh(const float* v, const int* idx, int nt, float margin, MeshBvh& m) {
+    for (int i = 0; i < nt; i++)
+        for (int k = 0; k < 3; k++) {
+            const float* p = v + 3 * idx[3 * i + k];
+            m.tris[3 * i + k] = make_float4(p[0], p[1], p[2], 0.0f);
+        }
+    float amin[3] = {1e30f, 1e30f, 1e30f}, amax[3] = {-1e30f, -1e30f, -1e30f};
+    for (const float4& p : m.tris) {
+        const float c[3] = {p.x, p.y, p.z};
+        for (int k = 0; k < 3; k++) { amin[k] = fmin_j(amin[k], c[k]); amax[k] = fmax_j(amax[k], c[k]); }
+    }
+    Builder b;
     for (int k = 0; k < 3; k++) {
-        for (int sg = 0; sg < 2; sg++) {
-            float dir[3] = {0.0f, 0.0f, 0.0f};
-            dir[k] = sg == 0 ? 1.0f : -1.0f;
-            float best = -1e30f, sup = 0.0f;
-            for (int i = 0; i < nn; i++) {
-                if (b.nodeW[i] < 0) continue;
-                for (int j = 0; j < 3; j++) {
-                    const float4& p = out.tris[3 * b.nodeW[i] + j];
-                    const float d = dir[0] * p.x + dir[1] * p.y + dir[2] * p.z;
-                    if (d > best) { best = d; sup = k == 0 ? p.x : (k == 1 ? p.y : p.z); }
-                }
+        b.bmin[k] = amin[k] - 1.0f;
+        b.bmax[k] = amax[k] + 1.0f;
+        b.quant[k] = 65535.0f / (b.bmax[k] - b.bmin[k]);
+        m.bmin[k] = b.bmin[k]; m.bmax[k] = b.bmax[k]; m.quant[k] = b.quant[k];
+    }
+    const int nn = (int)m.nodes.size();
+    std::vector<uint16_t> q((size_t)6 * nn);
+    for (int i = nn - 1; i >= 0; i--) {
+        const int w = m.nodes[i].w;
+        if (w >= 0) {
+            float mn[3] = {1e30f, 1e30f, 1e30f}, mx[3] = {-1e30f, -1e30f, -1e30f};
+            for (int j = 0; j < 3; j++) {
+                const float4& p = m.tris[3 * (w & ((1 << 21) - 1)) + j];
+                const float c[3] = {p.x, p.y, p.z};
+                for (int k = 0; k < 3; k++) { mn[k] = fmin_j(mn[k], c[k]); mx[k] = fmax_j(mx[k], c[k]); }
             }
-            if (sg == 0) out.lmax[k] = sup + 0.0f;
-            else out.lmin[k] = sup - 0.0f;
+            b.quantize(mn, &q[6 * i]);
+            b.quantize(mx, &q[6 * i + 3]);
+        } else {
+            const int l = i + 1, r = m.nodes[l].w >= 0 ? i + 2 : i + 1 - m.nodes[l].w;
+            for (int k = 0; k < 3; k++) {
+                q[6 * i + k] = q[6 * l + k] > q[6 * r + k] ? q[6 * r + k] : q[6 * l + k];
+                q[6 * i + 3 + k] = q[6 * l + 3 + k] < q[6 * r + 3 + k] ? q[6 * r + 3 + k] : q[6 * l + 3 + k];
+            }
         }
     }
-    return 0;
+    for (int i = 0; i < nn; i++) {
+        const uint16_t* p = &q[6 * i];
+        m.nodes[i] = make_int4((int)((unsigned)p[0] | ((unsigned)p[1] << 16)), (int)((unsigned)p[2] | ((unsigned)p[3] << 16)),
+                               (int)((unsigned)p[4] | ((unsigned)p[5] << 16)), m.nodes[i].w);
+    }
+    local_aabb(m, margin);
 }
 
 }  // namespace jbg

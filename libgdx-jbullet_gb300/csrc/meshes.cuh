@@ -18,4 +18,9 @@ struct MeshBvh {
 // Returns nonzero for an empty mesh, an index out of range or more than 2^21 - 1 triangles.
 int build_mesh_bvh(const float* vertices, int numVertices, const int* indices, int numTriangles, MeshBvh& out);
 
+// BvhTriangleMeshShape.refitTree over new vertex positions: m holds the tree built over the same
+// indices; its triangles, quantization, node boxes and local aabb (with the shape's current
+// margin) are updated, its topology kept.
+void refit_mesh_bvh(const float* vertices, const int* indices, int numTriangles, float margin, MeshBvh& m);
+
 }  // namespace jbg

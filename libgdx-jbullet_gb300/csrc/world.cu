@@ -25,6 +25,9 @@
 
 using namespace jbg;
 
+// Kernel: CollisionWorld.updateSingleAabb for every body whose shape is `shape` (after a refit).
+__global__ void k_shape_aabbs(DevWorld w, int shape);
+
 static thread_local std::string g_err;
 static int fail(int code, const std::string& msg) { g_err = msg; return code; }
 namespace jbg {
@@ -42,6 +45,13 @@ void jbg::note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
     } while (0)
 
 namespace {
+
+// A triangle mesh's vertex count, triangle indices and scaling, kept for jbgpu_world_refit_mesh.
+struct MeshSource {
+    int shape = -1, numPoints = 0;
+    std::vector<int> idx;
+    float scaling[3] = {0.0f, 0.0f, 0.0f};
+};
 
 struct HostShape {
     int type;
@@ -92,6 +102,8 @@ struct jbgpu_world {
     std::vector<float4> hullPts;
     std::vector<HostShape> childShapes;   // compound children, appended after the shapes on the device
     std::vector<float4> childXf;          // 3 per child: basis rows, origin in .w
+    std::vector<MeshSource> meshSrc;      // per triangle mesh: what a refit needs
+    std::vector<int> aabbRefresh;         // shapes whose bodies' aabbs the next prepare recomputes
     std::vector<int4> meshNodes;          // quantized tree nodes of every triangle mesh
     std::vector<float4> meshTris;         // 3 vertices per triangle
     bool hasMesh = false, hasCompound = false;
@@ -620,6 +632,14 @@ int prepare(jbgpu_world* w) {
     if (w->shapesDirty || w->planesDirty || w->jointsDirty || w->solverDirty) graphs_clear(w);
     int rc = sync_shapes(w);
     if (rc) return rc;
+    if (!w->aabbRefresh.empty()) {   // refitted meshes: updateSingleAabb of their bodies
+        if (w->nBodies > 0) {
+            DevWorld d = dev_view(w);
+            for (int s : w->aabbRefresh) { k_shape_aabbs<<<(w->nBodies + 255) / 256, 256, 0, w->stream>>>(d, s); note_launch(); }
+            CK(cudaGetLastError());
+        }
+        w->aabbRefresh.clear();
+    }
     rc = sync_planes(w);
     if (rc) return rc;
     return sync_joints(w);
@@ -998,19 +1018,22 @@ void compound_local_aabb(const std::vector<HostShape>& ch, const float* xf, int 
 // BvhTriangleMeshShape.setLocalScaling sets - and rebuilds the tree over - only when it differs
 // from the current (1, 1, 1) by a squared length above SIMD_EPSILON
 // (BvhTriangleMeshShape.java:195-212).  params[1..3] all zero: no scaling.
-const float* mesh_vertices(const jbgpu_shape_desc& d, std::vector<float>& buf) {
-    const float sx = d.params[1], sy = d.params[2], sz = d.params[3];
-    if (!d.points || d.num_points <= 0 || (sx == 0.0f && sy == 0.0f && sz == 0.0f)) return d.points;
+const float* scaled_vertices(const float* points, int n, const float s[3], std::vector<float>& buf) {
+    const float sx = s[0], sy = s[1], sz = s[2];
+    if (!points || n <= 0 || (sx == 0.0f && sy == 0.0f && sz == 0.0f)) return points;
     const float dx = 1.0f - sx, dy = 1.0f - sy, dz = 1.0f - sz;
     const float l2 = dx * dx + dy * dy + dz * dz;
-    if (!(l2 > 1.1920929e-7f)) return d.points;
-    buf.resize((size_t)3 * d.num_points);
-    for (int i = 0; i < d.num_points; i++) {
-        buf[3 * i] = d.points[3 * i] * sx;
-        buf[3 * i + 1] = d.points[3 * i + 1] * sy;
-        buf[3 * i + 2] = d.points[3 * i + 2] * sz;
+    if (!(l2 > 1.1920929e-7f)) return points;
+    buf.resize((size_t)3 * n);
+    for (int i = 0; i < n; i++) {
+        buf[3 * i] = points[3 * i] * sx;
+        buf[3 * i + 1] = points[3 * i + 1] * sy;
+        buf[3 * i + 2] = points[3 * i + 2] * sz;
     }
     return buf.data();
+}
+const float* mesh_vertices(const jbgpu_shape_desc& d, std::vector<float>& buf) {
+    return scaled_vertices(d.points, d.num_points, d.params + 1, buf);
 }
 }  // namespace
 
@@ -1306,6 +1329,12 @@ int jbgpu_world_add_shapes(jbgpu_world* w, const jbgpu_shape_desc* shapes, int32
             h.node_off = (int)w->meshNodes.size();
             h.node_cnt = (int)m.nodes.size();
             h.tri_off = (int)(w->meshTris.size() / 3);
+            MeshSource src;   // what a refit of this mesh needs
+            src.shape = (int)w->shapes.size();
+            src.numPoints = d.num_points;
+            src.idx.assign(d.indices, d.indices + (size_t)3 * d.num_triangles);
+            for (int k = 0; k < 3; k++) src.scaling[k] = d.params[1 + k];
+            w->meshSrc.push_back(std::move(src));
             w->meshNodes.insert(w->meshNodes.end(), m.nodes.begin(), m.nodes.end());
             w->meshTris.insert(w->meshTris.end(), m.tris.begin(), m.tris.end());
             for (int k = 0; k < 3; k++) {
@@ -1348,6 +1377,50 @@ int jbgpu_world_add_shapes(jbgpu_world* w, const jbgpu_shape_desc* shapes, int32
 }
 
 int jbgpu_world_add_shape(jbgpu_world* w, const jbgpu_shape_desc* s, int32_t* id) { return jbgpu_world_add_shapes(w, s, 1, id); }
+
+int jbgpu_world_refit_mesh(jbgpu_world* w, int32_t shape, const float* points, int32_t num_points) {
+    if (!w || !points || shape < 0 || shape >= (int)w->shapes.size() || w->shapes[shape].type != JBGPU_SHAPE_TRIANGLE_MESH)
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "refit_mesh: a triangle-mesh shape id and its vertices");
+    const MeshSource* src = nullptr;
+    for (const MeshSource& m : w->meshSrc)
+        if (m.shape == shape) src = &m;
+    if (!src || num_points != src->numPoints)
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "refit_mesh: the vertex count differs from the shape's");
+    HostShape& h = w->shapes[shape];
+    const int nt = (int)src->idx.size() / 3;
+    std::vector<float> buf;
+    const float* v = scaled_vertices(points, num_points, src->scaling, buf);
+    MeshBvh m;
+    m.nodes.assign(w->meshNodes.begin() + h.node_off, w->meshNodes.begin() + h.node_off + h.node_cnt);
+    m.tris.resize((size_t)3 * nt);
+    refit_mesh_bvh(v, src->idx.data(), nt, h.margin, m);
+    std::copy(m.nodes.begin(), m.nodes.end(), w->meshNodes.begin() + h.node_off);
+    std::copy(m.tris.begin(), m.tris.end(), w->meshTris.begin() + (size_t)3 * h.tri_off);
+    for (int k = 0; k < 3; k++) {
+        h.lmin[k] = m.lmin[k]; h.lmax[k] = m.lmax[k];
+        h.q[k] = m.bmin[k]; h.q[4 + k] = m.bmax[k]; h.q[8 + k] = m.quant[k];
+    }
+    w->shapesDirty = true;
+    w->aabbRefresh.push_back(shape);
+    return JBGPU_OK;
+}
+
+int jbgpu_world_mesh_bvh(const jbgpu_world* w, int32_t shape, int32_t* nodes, int32_t capacity, int32_t* n,
+                         float aabb[6]) {
+    if (!w || !n || shape < 0 || shape >= (int)w->shapes.size() || w->shapes[shape].type != JBGPU_SHAPE_TRIANGLE_MESH ||
+        capacity < 0 || (capacity > 0 && !nodes))
+        return fail(JBGPU_ERR_INVALID_ARGUMENT, "mesh_bvh: a triangle-mesh shape id, a count pointer and a node buffer");
+    const HostShape& h = w->shapes[shape];
+    *n = h.node_cnt;
+    if (aabb)
+        for (int k = 0; k < 3; k++) { aabb[k] = h.lmin[k]; aabb[3 + k] = h.lmax[k]; }
+    if (h.node_cnt > capacity) return fail(JBGPU_ERR_CAPACITY, "node buffer too small");
+    for (int i = 0; i < h.node_cnt; i++) {
+        const int4 q = w->meshNodes[h.node_off + i];
+        nodes[4 * i] = q.x; nodes[4 * i + 1] = q.y; nodes[4 * i + 2] = q.z; nodes[4 * i + 3] = q.w;
+    }
+    return JBGPU_OK;
+}
 
 int jbgpu_world_num_bodies(const jbgpu_world* w, int32_t* n) {
     if (!w || !n) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
@@ -2434,4 +2507,25 @@ __global__ void k_init_bodies(DevWorld w, int first, int count) {
     w.amin[i] = f4(mn, 0.0f);
     w.amax[i] = f4(mx, 0.0f);
     w.island[i] = -1;
+}
+
+// CollisionWorld.updateSingleAabb (CollisionWorld.java:195-224): the shape's aabb at the body's
+// transform widened by the contact breaking threshold; an oversized box of a non-static body
+// disables its simulation.
+__global__ void k_shape_aabbs(DevWorld w, int shape) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies || w.shape[i] != shape) return;
+    using namespace jbd;
+    V mn, mx;
+    shape_aabb(w.sh, shape, load_xf(w, i), mn, mx);
+    const float c = w.cbt;
+    mn = sub(mn, mk(c, c, c));
+    mx = add(mx, mk(c, c, c));
+    const V d = sub(mx, mn);
+    if ((w.flags[i] & CF_STATIC) || (len2(d) < 1e12f)) {
+        w.amin[i] = f4(mn, 0.0f);
+        w.amax[i] = f4(mx, 0.0f);
+    } else {
+        w.act[i] = set_activation(w.act[i], DISABLE_SIMULATION);
+    }
 }

@@ -150,6 +150,15 @@ class BvhTriangleMeshShape(_Shape):
     def getMeshInterface(self):
         return self.meshInterface
 
+    def refitTree(self, aabbMin=None, aabbMax=None):
+        """BvhTriangleMeshShape.refitTree (java:172-178) after meshInterface.vertices were changed
+        in place (same count): the tree is refitted and, as CollisionWorld.updateSingleAabb would
+        be called for them, the aabbs of the bodies using the shape are recomputed.  The shape
+        must have been added to a world (the world's tree is the one refitted)."""
+        if self._id is None or getattr(self, "_world", None) is None or self._world._g is None:
+            raise RuntimeError("refitTree on a shape that is not in a world yet")
+        self._world._g.refit_mesh(self._id, self.meshInterface.vertices)
+
     def desc(self):
         return {"type": _abi.SHAPE_TRIANGLE_MESH, "params": (self.margin,) + self.scaling,
                 "points": self.meshInterface.vertices, "indices": self.meshInterface.indices}
@@ -825,6 +834,7 @@ class DiscreteDynamicsWorld:
             lib.check(lib.lib().jbgpu_world_add_shapes(g.h, descs, len(descs), None))
             for s in shapes:
                 s._id = ids[id(s)]
+                s._world = self
         self._shapes += shapes
         b, ptr = sc.body_descs_ptr()
         from . import lib

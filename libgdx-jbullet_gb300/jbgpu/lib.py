@@ -102,6 +102,8 @@ def lib():
             "jbgpu_world_set_solver_iterations": ([C.c_void_p, C.c_int32, C.c_float, C.c_int32], C.c_int),
             "jbgpu_world_get_residual_trace": ([C.c_void_p, _abi.f32p, C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_set_ccd": ([C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, C.c_int32], C.c_int),
+            "jbgpu_world_refit_mesh": ([C.c_void_p, C.c_int32, _abi.f32p, C.c_int32], C.c_int),
+            "jbgpu_world_mesh_bvh": ([C.c_void_p, C.c_int32, _abi.i32p, C.c_int32, _abi.i32p, _abi.f32p], C.c_int),
             "jbgpu_world_set_sample_logging": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_get_samples": ([C.c_void_p, _abi.f32p, _abi.f32p, C.c_int32, _abi.i32p], C.c_int),
         }
@@ -127,7 +129,8 @@ EXPORTED = [
     "jbgpu_world_set_6dof_limit", "jbgpu_world_set_6dof_linear_motor", "jbgpu_world_set_6dof_angular_motor",
     "jbgpu_world_add_cone_twist", "jbgpu_world_set_cone_twist_limit", "jbgpu_world_set_cone_twist_angular_only",
     "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
-    "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd", "jbgpu_shape_mesh_bvh",
+    "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd", "jbgpu_shape_mesh_bvh", "jbgpu_world_refit_mesh",
+    "jbgpu_world_mesh_bvh",
 ]
 
 
@@ -479,6 +482,24 @@ class GpuWorld:
 
     def set_solver_iterations(self, num_iterations, residual=0.0, max_iterations=0):
         check(lib().jbgpu_world_set_solver_iterations(self.h, num_iterations, residual, max_iterations))
+
+    def refit_mesh(self, shape, points):
+        """New positions of a triangle mesh's vertices: BvhTriangleMeshShape.refitTree and
+        updateSingleAabb of its bodies (jbgpu_world_refit_mesh)."""
+        p = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        check(lib().jbgpu_world_refit_mesh(self.h, int(shape), p.ctypes.data_as(_abi.f32p), len(p)))
+
+    def mesh_bvh(self, shape):
+        """The world's current tree of a triangle-mesh shape: (nodes (n, 4) int32, local aabb (6,))."""
+        n = C.c_int32()
+        aabb = np.zeros(6, np.float32)
+        rc = lib().jbgpu_world_mesh_bvh(self.h, int(shape), None, 0, C.byref(n), aabb.ctypes.data_as(_abi.f32p))
+        if rc not in (0, _abi.ERR_CAPACITY):
+            check(rc)
+        nodes = np.zeros((n.value, 4), np.int32)
+        check(lib().jbgpu_world_mesh_bvh(self.h, int(shape), nodes.ctypes.data_as(_abi.i32p), n.value, C.byref(n),
+                                         aabb.ctypes.data_as(_abi.f32p)))
+        return nodes, aabb
 
     def set_ccd(self, bodies, motion_threshold, swept_sphere_radius):
         """CollisionObject.setCcdMotionThreshold / setCcdSweptSphereRadius for the given bodies."""

@@ -75,6 +75,50 @@ int orc_add_shape(void* h, const jbgpu_shape_desc* d) {
     return (int)w->shapes.size() - 1;
 }
 
+// The world's current tree of a TRIANGLE_MESH shape (after any refit) in the library's node
+// layout; returns the node count, -1 for a shape that is not a triangle mesh.
+int orc_world_mesh_bvh(void* h, int shape, int* nodes, int cap, float* aabb) {
+    World* w = (World*)h;
+    if (shape < 0 || shape >= (int)w->shapes.size() || w->shapes[shape].type != TRIANGLE_MESH) return -1;
+    const Shape& s = w->shapes[shape];
+    const QuantizedBvh& t = s.mesh->bvh;
+    for (int i = 0; i < t.curNodeIndex && i < cap; i++) {
+        const uint16_t* q = &t.q[6 * i];
+        nodes[4 * i] = (int)((unsigned)q[0] | ((unsigned)q[1] << 16));
+        nodes[4 * i + 1] = (int)((unsigned)q[2] | ((unsigned)q[3] << 16));
+        nodes[4 * i + 2] = (int)((unsigned)q[4] | ((unsigned)q[5] << 16));
+        nodes[4 * i + 3] = t.escOrTri[i];
+    }
+    if (aabb) {
+        aabb[0] = s.localAabbMin.x; aabb[1] = s.localAabbMin.y; aabb[2] = s.localAabbMin.z;
+        aabb[3] = s.localAabbMax.x; aabb[4] = s.localAabbMax.y; aabb[5] = s.localAabbMax.z;
+    }
+    return t.curNodeIndex;
+}
+
+// BvhTriangleMeshShape.refitTree over new vertex positions, then CollisionWorld.updateSingleAabb
+// (CollisionWorld.java:195-224) for every body of the shape; -1 for a shape that is not a
+// triangle mesh or another vertex count.
+int orc_refit_mesh(void* h, int shape, const float* points, int n) {
+    World* w = (World*)h;
+    if (shape < 0 || shape >= (int)w->shapes.size() || w->shapes[shape].type != TRIANGLE_MESH || !points ||
+        n != w->shapes[shape].mesh->numVertices)
+        return -1;
+    mesh_refit(w->shapes[shape], points);
+    const float t = w->cfg.contactBreakingThreshold;
+    for (Body& b : w->bodies) {
+        if (b.shape != shape) continue;
+        V3 mn, mx;
+        shape_aabb(w->shapes[shape], b.xf, mn, mx);
+        mn = sub(mn, v3(t, t, t));
+        mx = add(mx, v3(t, t, t));
+        V3 d = sub(mx, mn);
+        if (b.isStatic() || (len2(d) < 1e12f)) { b.aabbMin = mn; b.aabbMax = mx; }
+        else b.setActivationState(DISABLE_SIMULATION);
+    }
+    return 0;
+}
+
 // The quantized tree of a TRIANGLE_MESH descriptor in the library's node layout
 // (jbgpu_shape_mesh_bvh); returns the node count.
 int orc_mesh_bvh(const jbgpu_shape_desc* d, int* nodes, int cap, float* aabb) {

@@ -391,6 +391,10 @@ Shape make_mesh(const float* vtx, int nv, const int* idx, int nt, float margin, 
         scaled = len2(d) > 1.1920929e-7f;
     }
     auto md = std::make_shared<MeshData>();
+    md->idx.assign(idx, idx + (size_t)3 * nt);
+    md->numVertices = nv;
+    md->scaling = scaling;
+    md->scaled = scaled;
     md->tri.resize((size_t)3 * nt);
     for (int i = 0; i < nt; i++)   // VertexData.getTriangle (VertexData.java:50-55): vertex times scaling
         for (int k = 0; k < 3; k++) {
@@ -459,6 +463,77 @@ Shape make_mesh(const float* vtx, int nv, const int* idx, int nt, float margin, 
     }
     s.collisionMargin = margin;   // ConcaveShape.setMargin after construction
     return s;
+}
+
+// BvhTriangleMeshShape.refitTree (BvhTriangleMeshShape.java:172-178) after the mesh interface's
+// vertices were replaced: OptimizedBvh.refit (OptimizedBvh.java:344-367) takes the quantization
+// from the new brute-force box, and updateBvhNodes (java:411-470) requantizes the nodes from the
+// last to the first - a leaf from its triangle's box (without the build's minimum extent), an
+// internal node as the union of its two children's quantized boxes (the right child follows the
+// left one's subtree); recalcLocalAabb then runs with the shape's current margin.
+void mesh_refit(Shape& s, const float* vtx) {
+    MeshData& md = const_cast<MeshData&>(*s.mesh);   // the world's own mesh (make_mesh made it)
+    const int nt = (int)md.tri.size() / 3;
+    for (int i = 0; i < nt; i++)
+        for (int k = 0; k < 3; k++) {
+            int v = md.idx[3 * i + k];
+            V3 p = v3(vtx[3 * v], vtx[3 * v + 1], vtx[3 * v + 2]);
+            if (md.scaled) p = v3(p.x * md.scaling.x, p.y * md.scaling.y, p.z * md.scaling.z);
+            md.tri[3 * i + k] = p;
+        }
+    V3 amin = v3(1e30f, 1e30f, 1e30f), amax = v3(-1e30f, -1e30f, -1e30f);   // calculateAabbBruteForce
+    for (const V3& p : md.tri) {
+        amin = v3(jmin(amin.x, p.x), jmin(amin.y, p.y), jmin(amin.z, p.z));
+        amax = v3(jmax(amax.x, p.x), jmax(amax.y, p.y), jmax(amax.z, p.z));
+    }
+    QuantizedBvh& t = md.bvh;
+    t.bvhAabbMin = sub(amin, v3(1, 1, 1));   // setQuantizationValues, quantizationMargin 1
+    t.bvhAabbMax = add(amax, v3(1, 1, 1));
+    V3 size = sub(t.bvhAabbMax, t.bvhAabbMin);
+    t.bvhQuantization = v3(65535.0f / size.x, 65535.0f / size.y, 65535.0f / size.z);
+    BvhBuild b{t, {}, {}};
+    for (int i = t.curNodeIndex - 1; i >= 0; i--) {
+        if (t.escOrTri[i] >= 0) {
+            const int tri = t.escOrTri[i] & ((1 << 21) - 1);
+            V3 mn = v3(1e30f, 1e30f, 1e30f), mx = v3(-1e30f, -1e30f, -1e30f);
+            for (int k = 0; k < 3; k++) {
+                V3 p = md.tri[3 * tri + k];
+                mn = v3(jmin(mn.x, p.x), jmin(mn.y, p.y), jmin(mn.z, p.z));
+                mx = v3(jmax(mx.x, p.x), jmax(mx.y, p.y), jmax(mx.z, p.z));
+            }
+            b.quantize(mn, &t.q[6 * i]);
+            b.quantize(mx, &t.q[6 * i + 3]);
+        } else {
+            const int l = i + 1;
+            const int r = t.escOrTri[l] >= 0 ? i + 2 : i + 1 - t.escOrTri[l];
+            for (int k = 0; k < 3; k++) {
+                t.q[6 * i + k] = t.q[6 * l + k];
+                if (t.q[6 * i + k] > t.q[6 * r + k]) t.q[6 * i + k] = t.q[6 * r + k];
+                t.q[6 * i + 3 + k] = t.q[6 * l + 3 + k];
+                if (t.q[6 * i + 3 + k] < t.q[6 * r + 3 + k]) t.q[6 * i + 3 + k] = t.q[6 * r + 3 + k];
+            }
+        }
+    }
+    const float m = s.collisionMargin;
+    for (int i = 0; i < 3; i++) {
+        for (int sg = 0; sg < 2; sg++) {
+            float best = -1e30f;
+            V3 sup = v3(0, 0, 0);
+            for (int node = 0; node < t.curNodeIndex; node++) {
+                if (t.escOrTri[node] < 0) continue;
+                int tri = t.escOrTri[node] & ((1 << 21) - 1);
+                for (int k = 0; k < 3; k++) {
+                    V3 p = md.tri[3 * tri + k];
+                    V3 dir = v3(0, 0, 0);
+                    set_coord(dir, i, sg == 0 ? 1.0f : -1.0f);
+                    float d = dot(dir, p);
+                    if (d > best) { best = d; sup = p; }
+                }
+            }
+            if (sg == 0) set_coord(s.localAabbMax, i, coord(sup, i) + m);
+            else set_coord(s.localAabbMin, i, coord(sup, i) - m);
+        }
+    }
 }
 
 // OptimizedBvh.walkStacklessQuantizedTree (java:940-997) with testQuantizedAabbAgainstQuantizedAabb

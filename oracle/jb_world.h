@@ -27,11 +27,16 @@ struct QuantizedBvh {
     std::vector<int> escOrTri;
     int curNodeIndex = 0;
 };
-// BvhTriangleMeshShape over a TriangleIndexVertexArray of one part, scaling (1,1,1): the
-// triangles' vertices by triangle index, and the quantized tree over them.
+// BvhTriangleMeshShape over a TriangleIndexVertexArray of one part: the triangles' vertices by
+// triangle index (times the scaling when setLocalScaling applied one), and the quantized tree
+// over them; the indices and scaling are kept for refitTree.
 struct MeshData {
     std::vector<V3> tri;              // 3 per triangle
     QuantizedBvh bvh;
+    std::vector<int> idx;             // 3 vertex indices per triangle
+    int numVertices = 0;
+    V3 scaling{1, 1, 1};
+    bool scaled = false;
 };
 
 // collision/shapes/*.java: one record for the shape classes on the path.
@@ -66,6 +71,8 @@ Shape make_plane(V3 normal, float constant);
 // scaling: BvhTriangleMeshShape.setLocalScaling before setMargin ((0, 0, 0): not called)
 Shape make_mesh(const float* vertices, int numVertices, const int* indices, int numTriangles, float margin,
                 V3 scaling = V3{0.0f, 0.0f, 0.0f});
+// BvhTriangleMeshShape.refitTree over new positions of the mesh's vertices (same count)
+void mesh_refit(Shape& s, const float* vertices);
 // CompoundShape with addChildShape(transform, child) for each child in order, then setMargin(margin)
 Shape make_compound(const std::vector<Shape>& children, const std::vector<Xf>& xf, float margin);
 // OptimizedBvh.reportAabbOverlappingNodex: triangle indices in the order the walk reports them

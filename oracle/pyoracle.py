@@ -71,6 +71,8 @@ def lib():
         L.orc_enable_hinge_motor.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float]
         L.orc_set_hinge_angular_only.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.orc_set_ccd.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, C.c_int]
+        L.orc_refit_mesh.argtypes = [C.c_void_p, C.c_int, _abi.f32p, C.c_int]
+        L.orc_world_mesh_bvh.argtypes = [C.c_void_p, C.c_int, _abi.i32p, C.c_int, _abi.f32p]
         _lib = L
     return _lib
 
@@ -257,6 +259,23 @@ class OracleWorld:
 
     def step_simulation(self, time_step, max_sub_steps=1, fixed_time_step=1.0 / 60.0):
         return lib().orc_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step)
+
+    def refit_mesh(self, shape, points):
+        """New positions of a triangle mesh's vertices, then BvhTriangleMeshShape.refitTree and
+        updateSingleAabb of its bodies."""
+        p = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        if lib().orc_refit_mesh(self.h, int(shape), _fp(p), len(p)) != 0:
+            raise ValueError("refit_mesh: not a triangle mesh, or another vertex count")
+
+    def mesh_bvh(self, shape):
+        """The world's current tree of a triangle-mesh shape: (nodes (n, 4) int32, local aabb (6,))."""
+        aabb = np.zeros(6, np.float32)
+        n = lib().orc_world_mesh_bvh(self.h, int(shape), None, 0, _fp(aabb))
+        if n < 0:
+            raise ValueError("mesh_bvh: not a triangle mesh")
+        nodes = np.zeros((n, 4), np.int32)
+        lib().orc_world_mesh_bvh(self.h, int(shape), nodes.ctypes.data_as(_abi.i32p), n, _fp(aabb))
+        return nodes, aabb
 
     def stage(self, stage, dt=1.0 / 60.0):
         lib().orc_stage(self.h, stage, dt)

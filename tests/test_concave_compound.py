@@ -138,6 +138,51 @@ def test_mirror_mesh_scaling_order():
         s.setLocalScaling((1.5, 1.5, 1.5))
 
 
+def _deformed(mesh, seed):
+    """The mesh's vertices moved (same count): heights shifted by up to 0.4 m, x and z by up to
+    0.05 m, and one vertex lifted 2 m."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = np.asarray(mesh["points"], F).copy()
+    p[:, 1] += rng.uniform(-0.4, 0.4, len(p)).astype(F)
+    p[:, 0] += rng.uniform(-0.05, 0.05, len(p)).astype(F)
+    p[:, 2] += rng.uniform(-0.05, 0.05, len(p)).astype(F)
+    p[len(p) // 2, 1] += F(2.0)
+    return p
+
+
+def _static_mesh_scene(mesh):
+    b = scenes._bodies(1)
+    b["transform"][0] = scenes.xf12()
+    return scenes.Scene("mesh_only", 1.0 / 60.0, 1, {}, [mesh], b)
+
+
+@pytest.mark.parametrize("k", [1, 2, 5])
+def test_oracle_refit_keeps_topology_and_requantizes(oracle_lib, k):
+    """OptimizedBvh.refit in the oracle: the same nodes, every leaf the quantized box of its moved
+    triangle under the new quantization (no minimum extent), every internal node the union of its
+    two children, the local aabb the moved vertices' box widened by the margin."""
+    mesh = dict(_meshes()[k], params=(0.03,) + tuple(_meshes()[k]["params"][1:4]))
+    o = pyoracle.OracleWorld(_static_mesh_scene(mesh))
+    n0, _ = o.mesh_bvh(0)
+    moved = _deformed(mesh, k)
+    o.refit_mesh(0, moved)
+    n1, aabb = o.mesh_bvh(0)
+    assert np.array_equal(n0[:, 3], n1[:, 3])
+    quant = _quantizer(dict(mesh, points=moved))
+    p = _scaled_points(dict(mesh, points=moved))[np.asarray(mesh["indices"]).reshape(-1, 3)]
+    qmin, qmax, w = _unpack(n1)
+    leaves = np.nonzero(w >= 0)[0]
+    assert np.array_equal(qmin[leaves], quant(p[w[leaves]].min(1))) and np.array_equal(qmax[leaves], quant(p[w[leaves]].max(1)))
+    for i in np.nonzero(w < 0)[0]:
+        l = i + 1
+        r = i + 2 if w[l] >= 0 else i + 1 - w[l]
+        assert np.array_equal(qmin[i], np.minimum(qmin[l], qmin[r])) and np.array_equal(qmax[i], np.maximum(qmax[l], qmax[r]))
+    flat = p.reshape(-1, 3)
+    assert np.array_equal(aabb[:3], flat.min(0) - F(0.03)) and np.array_equal(aabb[3:], flat.max(0) + F(0.03))
+    with pytest.raises(ValueError):
+        o.refit_mesh(0, moved[:-1])
+
+
 @pytest.mark.parametrize("k", range(NMESH))
 def test_mesh_walk_reports_overlapping_leaves_in_node_order(oracle_lib, k):
     mesh = _meshes()[k]
@@ -575,8 +620,8 @@ def test_f3_ccd_with_compounds_closed_loop_bit_exact(gpu_lib, oracle_lib):
 def test_mirror_compound_on_mesh_reads_like_the_reference(gpu_lib, oracle_lib):
     """The reference's usage through the Python mirror: a BvhTriangleMeshShape ground over a
     TriangleIndexVertexArray (setLocalScaling, then setMargin), CompoundShape dumbbells built with
-    addChildShape and a box; two seconds of stepSimulation.  The same world given to the oracle
-    ends bit-identical."""
+    addChildShape and a box; two seconds of stepSimulation with the ground deformed in place and
+    refitTree called after the first.  The same world given to the oracle ends bit-identical."""
     from jbgpu import dynamics as D
     tm = scenes.terrain_mesh(8, 8, 12.0, seed=4)
     world = D.DiscreteDynamicsWorld()
@@ -596,7 +641,16 @@ def test_mirror_compound_on_mesh_reads_like_the_reference(gpu_lib, oracle_lib):
         info = D.RigidBodyConstructionInfo(m, None, shape, shape.calculateLocalInertia(m))
         info.startWorldTransform = D.Transform(basis=scenes.rot_x(0.4), origin=pos)
         world.addRigidBody(D.RigidBody(info))
-    for _ in range(120):
+    for _ in range(60):
+        world.stepSimulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    # the terrain deformed in place, then refitTree (the mesh interface's vertices are the array)
+    verts = ground_shape.getMeshInterface().vertices
+    orig = verts.copy()
+    moved = orig.copy()
+    moved[:, 1] = moved[:, 1] * F(0.9) + F(0.05)   # the ground flattened a little and raised 5 cm
+    verts[:] = moved
+    ground_shape.refitTree(None, None)
+    for _ in range(60):
         world.stepSimulation(1.0 / 60.0, 1, 1.0 / 60.0)
     g = world._g
     # the same world on the oracle
@@ -609,10 +663,47 @@ def test_mirror_compound_on_mesh_reads_like_the_reference(gpu_lib, oracle_lib):
         b["transform"][k + 1] = scenes.xf12(scenes.rot_x(0.4), pos)
     sc = scenes.Scene("mirror_f3", 1.0 / 60.0, 120, {"gravity": (0.0, -9.81, 0.0)},
                       [ground_shape.desc(), bell.desc(), box.desc()], b)
+    sc.shapes[0] = dict(sc.shapes[0], points=orig)   # the vertices it was built over
     o = pyoracle.OracleWorld(sc, config=_abi.default_config(gravity=(0.0, -9.81, 0.0)))
-    for _ in range(120):
+    for _ in range(60):
+        o.step_simulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    o.refit_mesh(0, moved)
+    for _ in range(60):
         o.step_simulation(1.0 / 60.0, 1, 1.0 / 60.0)
     assert not H.compare_state(o.get_state(), g.get_state())
     assert not H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
     assert o.counters()["contacts"] > 0
     world.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scaled", [False, True])
+def test_refit_tree_and_closed_loop_bit_exact(gpu_lib, oracle_lib, scaled):
+    """BvhTriangleMeshShape.refitTree on a terrain under falling and resting bodies, twice: the
+    library's refitted tree equals the oracle's node for node, and the worlds stay bit-identical
+    through the refits (updateSingleAabb of the static mesh body included)."""
+    sc = _with_mesh_margin(scenes.terrain(30, compounds=4, seed=11, mesh_scaling=(1.2, 0.8, 1.1) if scaled else
+                                          (0.0, 0.0, 0.0)), 0.02)
+    o = pyoracle.OracleWorld(sc)
+    g = GpuWorld(sc)
+    mesh = sc.shapes[0]
+    for s in range(sc.steps):
+        if s in (40, 120):
+            moved = _deformed(dict(mesh, points=mesh["points"] if s == 40 else moved), s)
+            o.refit_mesh(0, moved)
+            g.refit_mesh(0, moved)
+            on, oa = o.mesh_bvh(0)
+            gn, ga = g.mesh_bvh(0)
+            assert np.array_equal(on, gn) and np.array_equal(oa.view(np.uint32), ga.view(np.uint32))
+        o.step(sc.dt)
+        g.step(sc.dt)
+        if s % 10 == 9:
+            bs = H.compare_state(o.get_state(), g.get_state())
+            bm = H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+            assert not bs and not bm, (s, bs, bm)
+    assert g.counters()["status_flags"] == 0 and o.counters()["contacts"] > 0
+    with pytest.raises(jl.JbgpuError):
+        g.refit_mesh(0, moved[:-1])
+    with pytest.raises(jl.JbgpuError):
+        g.refit_mesh(1, moved)
+    g.close()
