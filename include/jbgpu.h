@@ -75,6 +75,10 @@ extern "C" {
 #define JBGPU_DISABLE_DEACTIVATION 4
 #define JBGPU_DISABLE_SIMULATION   5
 
+/* ---- collision flags a body may be given (collision/dispatch/CollisionFlags.java:31-36) -- */
+#define JBGPU_CF_KINEMATIC_OBJECT     2   /* moved by the caller; saveKinematicState gives it velocities */
+#define JBGPU_CF_NO_CONTACT_RESPONSE  4   /* contacts are found, never solved (trigger volumes) */
+
 /* ---- SolverMode bits (dynamics/constraintsolver/SolverMode.java:33-36) ------------ */
 #define JBGPU_SOLVER_RANDMIZE_ORDER    1  /* rejected: the GPU order is the colour order */
 #define JBGPU_SOLVER_FRICTION_SEPARATE 2
@@ -92,6 +96,7 @@ extern "C" {
 #define JBGPU_STAGE_INTEGRATE     7 /* integrateTransforms                              */
 #define JBGPU_STAGE_ACTIVATION    8 /* updateActivationState                            */
 #define JBGPU_STAGE_CLEAR_FORCES  9 /* clearForces                                      */
+#define JBGPU_STAGE_SAVE_KINEMATIC 10 /* saveKinematicState(dt): velocities of kinematic bodies */
 
 /* Floats per manifold point in jbgpu_manifolds.points (ManifoldPoint,
  * collision/narrowphase/ManifoldPoint.java:36-62):
@@ -205,6 +210,11 @@ typedef struct jbgpu_body_desc {
     int32_t collision_mask;             /* -1: ALL / ALL^STATIC  (DiscreteDynamicsWorld.java:426-440) */
     int32_t world;                      /* batch world index: bodies of different worlds never collide
                                            (0 for an ordinary single world) */
+    int32_t collision_flags;            /* CollisionObject.setCollisionFlags before addRigidBody:
+                                           JBGPU_CF_KINEMATIC_OBJECT, JBGPU_CF_NO_CONTACT_RESPONSE (0: none;
+                                           STATIC_OBJECT follows from mass 0) */
+    int32_t activation_state;           /* setActivationState before addRigidBody (0: the constructor's
+                                           JBGPU_ACTIVE_TAG) */
 } jbgpu_body_desc;
 
 /* Body state, structure of arrays.  Any pointer may be NULL (field skipped). */

@@ -128,6 +128,33 @@ __global__ void k_clear_forces(DevWorld w) {   // DiscreteDynamicsWorld.clearFor
     w.torque[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
+// DiscreteDynamicsWorld.saveKinematicState (DiscreteDynamicsWorld.java:105-119) ->
+// RigidBody.saveKinematicState (RigidBody.java:190-205): a kinematic body that is not
+// ISLAND_SLEEPING takes the velocities that carry its last saved transform to its current one,
+// which becomes the saved transform.
+__global__ void k_save_kinematic(DevWorld w, float timeStep) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    if (!(w.flags[i] & CF_KINEMATIC) || w.act[i] == ISLAND_SLEEPING || timeStep == 0.0f) return;
+    const Xf cur = load_xf(w, i);
+    Xf prev;
+    const float4 a = w.kx0[i], b = w.kx1[i], c = w.kx2[i];
+    prev.b.r[0] = mk(a.x, a.y, a.z);
+    prev.b.r[1] = mk(b.x, b.y, b.z);
+    prev.b.r[2] = mk(c.x, c.y, c.z);
+    prev.o = mk(a.w, b.w, c.w);
+    V lin, ang;
+    calc_velocity(prev, cur, timeStep, lin, ang);
+    w.linvel[i] = f4(lin, 0.0f);
+    w.angvel[i] = f4(ang, 0.0f);
+    w.kx0[i] = w.xr0[i];
+    w.kx1[i] = w.xr1[i];
+    w.kx2[i] = w.xr2[i];
+}
+
+void launch_save_kinematic(const DevWorld& w, float timeStep, cudaStream_t s) {
+    if (w.nBodies) { k_save_kinematic<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, timeStep); note_launch(); }
+}
 void launch_apply_gravity(const DevWorld& w, cudaStream_t s) {
     if (w.nBodies) { k_apply_gravity<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w); note_launch(); }
 }

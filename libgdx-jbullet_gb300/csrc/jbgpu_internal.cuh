@@ -117,6 +117,7 @@ struct DevWorld {
     int nPairs;           // pairs of the current pair arrays (device copy in ctr[C_PAIRS])
     // body state
     float4 *xr0, *xr1, *xr2;        // basis rows; origin in .w
+    float4 *kx0, *kx1, *kx2;        // interpolationWorldTransform (saveKinematicState), same layout
     float4 *linvel, *angvel;
     float4 *iw0, *iw1, *iw2;        // inverse inertia tensor (world) rows
     float4 *iloc;                   // inverse inertia (local) xyz, inverse mass w
@@ -204,6 +205,7 @@ void launch_aabb(const DevWorld& w, cudaStream_t s);
 void launch_integrate(const DevWorld& w, float dt, cudaStream_t s);
 void launch_activation(const DevWorld& w, float dt, cudaStream_t s);
 void launch_clear_forces(const DevWorld& w, cudaStream_t s);
+void launch_save_kinematic(const DevWorld& w, float timeStep, cudaStream_t s);
 
 int num_sms();
 

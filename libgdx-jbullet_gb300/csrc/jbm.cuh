@@ -242,4 +242,16 @@ JBD Xf integrate_transform(const Xf& cur, V lin, V ang, float dt) {
     return p;
 }
 
+// TransformUtil.calculateVelocity / calculateDiffAxisAngle (linearmath/TransformUtil.java:105-153):
+// the velocities that carry t0 to t1 in timeStep (QuaternionUtil.getAngle: 2 Math.acos(w)).
+JBD void calc_velocity(const Xf& t0, const Xf& t1, float timeStep, V& lin, V& ang) {
+    lin = scl(sub(t1.o, t0.o), jdiv(1.0f, timeStep));
+    const Q dorn = qnor(q_from_matrix(mulMM(t1.b, m3_invert(t0.b))));
+    const float angle = __fmul_rn(2.0f, (float)acos((double)dorn.w));
+    V axis = mk(dorn.x, dorn.y, dorn.z);
+    const float l2 = len2(axis);
+    axis = l2 < __fmul_rn(FLT_EPS, FLT_EPS) ? mk(1.0f, 0.0f, 0.0f) : scl(axis, jdiv(1.0f, jsqrt(l2)));
+    ang = scl(axis, jdiv(angle, timeStep));
+}
+
 }  // namespace jbd

@@ -107,6 +107,7 @@ struct jbgpu_world {
     std::vector<int4> meshNodes;          // quantized tree nodes of every triangle mesh
     std::vector<float4> meshTris;         // 3 vertices per triangle
     bool hasMesh = false, hasCompound = false;
+    bool hasKinematic = false;            // some body is kinematic: saveKinematicState runs
     int candBound = 0;                    // the concave pass's candidates of this step (count pass bound)
     bool shapesDirty = true;
     int capShapes = 0, capHull = 0;
@@ -237,7 +238,8 @@ int grow_bodies(jbgpu_world* w, int need) {
     DevWorld& d = w->dw;
     size_t keep = (size_t)w->nBodies;
 #define G(ptr) CK(dgrow(&d.ptr, oldc, nc, keep, s))
-    G(xr0); G(xr1); G(xr2); G(linvel); G(angvel); G(iw0); G(iw1); G(iw2); G(iloc); G(force); G(torque); G(gravity);
+    G(xr0); G(xr1); G(xr2); G(kx0); G(kx1); G(kx2); G(linvel); G(angvel); G(iw0); G(iw1); G(iw2); G(iloc); G(force);
+    G(torque); G(gravity);
     G(amin); G(amax); G(act); G(deact); G(flags); G(shape); G(group); G(mask); G(world); G(friction); G(restitution);
     G(linSleep); G(angSleep); G(linDamp); G(angDamp); G(island); G(ccdThr); G(ccdRad);
 #undef G
@@ -559,6 +561,7 @@ int run_stage(jbgpu_world* w, int stage, float dt) {
         break;
     case JBGPU_STAGE_ACTIVATION: P.mark(PH_ACTIVATION, 0, s); launch_activation(d, dt, s); P.mark(PH_ACTIVATION, 1, s); break;
     case JBGPU_STAGE_CLEAR_FORCES: launch_clear_forces(d, s); break;
+    case JBGPU_STAGE_SAVE_KINEMATIC: launch_save_kinematic(d, dt, s); break;
     default: return fail(JBGPU_ERR_INVALID_ARGUMENT, "unknown stage");
     }
     CK(cudaGetLastError());
@@ -1226,7 +1229,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     graphs_clear(w);
     query_free(w->qb);
     DevWorld& d = w->dw;
-    dfree(d.xr0); dfree(d.xr1); dfree(d.xr2); dfree(d.linvel); dfree(d.angvel); dfree(d.iw0); dfree(d.iw1); dfree(d.iw2);
+    dfree(d.xr0); dfree(d.xr1); dfree(d.xr2); dfree(d.kx0); dfree(d.kx1); dfree(d.kx2); dfree(d.linvel); dfree(d.angvel); dfree(d.iw0); dfree(d.iw1); dfree(d.iw2);
     dfree(d.iloc); dfree(d.force); dfree(d.torque); dfree(d.gravity); dfree(d.amin); dfree(d.amax); dfree(d.act);
     dfree(d.deact); dfree(d.flags); dfree(d.shape); dfree(d.group); dfree(d.mask); dfree(d.world); dfree(d.friction);
     dfree(d.restitution); dfree(d.linSleep); dfree(d.angSleep); dfree(d.linDamp); dfree(d.angDamp); dfree(d.island);
@@ -1441,6 +1444,10 @@ int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, 
             return fail(JBGPU_ERR_INVALID_ARGUMENT, "a triangle mesh body must have mass 0 (moving concave objects are "
                                                     "not supported, TriangleMeshShape.calculateLocalInertia)");
         if (b[i].world < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "negative world index");
+        if (b[i].collision_flags & ~(1 | JBGPU_CF_KINEMATIC_OBJECT | JBGPU_CF_NO_CONTACT_RESPONSE))
+            return fail(JBGPU_ERR_UNSUPPORTED, "collision flags other than KINEMATIC_OBJECT and NO_CONTACT_RESPONSE");
+        if (b[i].activation_state < 0 || b[i].activation_state > JBGPU_DISABLE_SIMULATION)
+            return fail(JBGPU_ERR_INVALID_ARGUMENT, "activation state outside 0 .. DISABLE_SIMULATION");
     }
     int rc = grow_bodies(w, w->nBodies + n);
     if (rc) return rc;
@@ -1458,7 +1465,9 @@ int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, 
         xr2[i] = make_float4(t[6], t[7], t[8], t[11]);
         lv[i] = make_float4(d.linear_velocity[0], d.linear_velocity[1], d.linear_velocity[2], 0);
         av[i] = make_float4(d.angular_velocity[0], d.angular_velocity[1], d.angular_velocity[2], 0);
-        int f = 0;
+        int f = d.collision_flags & (CF_KINEMATIC | CF_NO_CONTACT_RESPONSE);
+        if (f & CF_KINEMATIC) w->hasKinematic = true;
+        if (d.activation_state != 0) act[i] = d.activation_state;
         float im;
         if (d.mass == 0.0f) { f |= CF_STATIC; im = 0.0f; } else im = 1.0f / d.mass;
         if (w->shapes[d.shape].type == JBGPU_SHAPE_STATIC_PLANE || w->shapes[d.shape].type == JBGPU_SHAPE_TRIANGLE_MESH)
@@ -1492,6 +1501,7 @@ int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, 
     DevWorld& D = w->dw;
 #define UP(dst, src, T) CK(cudaMemcpyAsync(D.dst + o, src.data(), sizeof(T) * n, cudaMemcpyHostToDevice, s))
     UP(xr0, xr0, float4); UP(xr1, xr1, float4); UP(xr2, xr2, float4); UP(linvel, lv, float4); UP(angvel, av, float4);
+    UP(kx0, xr0, float4); UP(kx1, xr1, float4); UP(kx2, xr2, float4);   // interpolationWorldTransform = worldTransform
     UP(iloc, iloc, float4); UP(gravity, grav, float4); UP(force, zero, float4); UP(torque, zero, float4);
     UP(act, act, int); UP(deact, deact, float); UP(flags, flags, int); UP(shape, shape, int); UP(group, group, int);
     UP(mask, mask, int); UP(world, world, int); UP(friction, fr, float); UP(restitution, re, float);
@@ -1511,6 +1521,7 @@ int jbgpu_world_step(jbgpu_world* w, float dt, int32_t substeps) {
     int rc = prepare(w);
     if (rc) return rc;
     CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), w->stream));
+    if (w->hasKinematic && (rc = run_stage(w, JBGPU_STAGE_SAVE_KINEMATIC, dt))) return rc;
     if ((rc = run_stage(w, JBGPU_STAGE_APPLY_GRAVITY, dt))) return rc;
     for (int i = 0; i < substeps; i++)
         if ((rc = single_step(w, dt))) return rc;
@@ -1538,6 +1549,7 @@ int jbgpu_world_step_simulation(jbgpu_world* w, float timeStep, int32_t maxSubSt
     if (rc) return rc;
     CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), w->stream));
     if (num != 0) {
+        if (w->hasKinematic && (rc = run_stage(w, JBGPU_STAGE_SAVE_KINEMATIC, fixedTimeStep))) return rc;
         if ((rc = run_stage(w, JBGPU_STAGE_APPLY_GRAVITY, fixedTimeStep))) return rc;
         int clamped = num > maxSubSteps ? maxSubSteps : num;
         for (int i = 0; i < clamped; i++)

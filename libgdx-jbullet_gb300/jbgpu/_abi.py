@@ -47,6 +47,11 @@ STAGE_SOLVE = 6
 STAGE_INTEGRATE = 7
 STAGE_ACTIVATION = 8
 STAGE_CLEAR_FORCES = 9
+STAGE_SAVE_KINEMATIC = 10
+
+CF_STATIC_OBJECT = 1
+CF_KINEMATIC_OBJECT = 2
+CF_NO_CONTACT_RESPONSE = 4
 
 POINT_FLOATS = 32
 MANIFOLD_POINTS = 4
@@ -140,6 +145,8 @@ class BodyDesc(C.Structure):
         ("collision_group", C.c_int32),
         ("collision_mask", C.c_int32),
         ("world", C.c_int32),
+        ("collision_flags", C.c_int32),
+        ("activation_state", C.c_int32),
     ]
 
 

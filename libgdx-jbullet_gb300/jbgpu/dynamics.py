@@ -233,6 +233,47 @@ class RigidBody:
         self._group = -1
         self._mask = -1
         self._ccd = (0.0, 0.0)          # ccdMotionThreshold, ccdSweptSphereRadius
+        self._flags = 0                 # KINEMATIC_OBJECT / NO_CONTACT_RESPONSE set before addRigidBody
+        self._activation = 0            # setActivationState before addRigidBody (0: ACTIVE_TAG)
+
+    # CollisionObject.setCollisionFlags / getCollisionFlags (collision/dispatch/CollisionObject.java):
+    # KINEMATIC_OBJECT and NO_CONTACT_RESPONSE, set before the body is added; STATIC_OBJECT
+    # follows from mass 0
+    def setCollisionFlags(self, flags):
+        if self._world is not None:
+            raise NotImplementedError("setCollisionFlags after addRigidBody")
+        if flags & ~(_abi.CF_STATIC_OBJECT | _abi.CF_KINEMATIC_OBJECT | _abi.CF_NO_CONTACT_RESPONSE):
+            raise NotImplementedError("collision flags other than KINEMATIC_OBJECT and NO_CONTACT_RESPONSE")
+        self._flags = int(flags) & (_abi.CF_KINEMATIC_OBJECT | _abi.CF_NO_CONTACT_RESPONSE)
+
+    def getCollisionFlags(self):
+        return self._flags | (_abi.CF_STATIC_OBJECT if self.info.mass == 0.0 else 0)
+
+    def isKinematicObject(self):
+        return (self._flags & _abi.CF_KINEMATIC_OBJECT) != 0
+
+    def setActivationState(self, state):
+        """CollisionObject.setActivationState: no change from DISABLE_DEACTIVATION or DISABLE_SIMULATION."""
+        if self._world is None or self._world._g is None:
+            if self._activation not in (DISABLE_DEACTIVATION, DISABLE_SIMULATION):
+                self._activation = int(state)
+            return
+        if self.getActivationState() not in (DISABLE_DEACTIVATION, DISABLE_SIMULATION):
+            self._world._set_field("activation_state", self._index, int(state))
+
+    def forceActivationState(self, state):
+        if self._world is None or self._world._g is None:
+            self._activation = int(state)
+        else:
+            self._world._set_field("activation_state", self._index, int(state))
+
+    def setWorldTransform(self, transform):
+        """CollisionObject.setWorldTransform: for a kinematic body, the pose saveKinematicState
+        turns into velocities at the next stepSimulation."""
+        if self._world is not None and self._world._g is not None:
+            self._world._set_field("transform", self._index, transform.as12())
+        else:
+            self.info.startWorldTransform = transform
 
     # velocities set before the body enters the world are uploaded with it
     def setLinearVelocity(self, v):
@@ -825,6 +866,8 @@ class DiscreteDynamicsWorld:
             recs[k]["linear_velocity"] = b._linvel
             recs[k]["angular_velocity"] = b._angvel
             recs[k]["collision_group"] = b._group
+            recs[k]["collision_flags"] = b._flags
+            recs[k]["activation_state"] = b._activation
             recs[k]["collision_mask"] = b._mask
         sc = Scene("staged", 0, 0, {}, [s.desc() for s in shapes], recs)
         g = self._g
@@ -858,6 +901,18 @@ class DiscreteDynamicsWorld:
         if self._forces is not None:
             g.apply_forces(self._forces)
             self._forces = None
+        # saveKinematicState reads a kinematic body's motion state (RigidBody.java:190-205): its
+        # pose is written to the world first, for the bodies that are not ISLAND_SLEEPING
+        kin = [b for b in self._bodies if b.isKinematicObject() and b.info.motionState is not None and
+               hasattr(b.info.motionState, "getWorldTransform")]
+        if kin:
+            st = self._state()
+            t = st["transform"].copy()
+            for b in kin:
+                if st["activation_state"][b._index] != ISLAND_SLEEPING:
+                    t[b._index] = b.info.motionState.getWorldTransform().as12()
+            g.set_state({"transform": t})
+            self._cache = None
         n = g.step_simulation(timeStep, maxSubSteps, fixedTimeStep)
         self._cache = None
         return n

@@ -24,8 +24,9 @@ BODY_DTYPE = np.dtype([
     ("linear_sleeping_threshold", "<f4"), ("angular_sleeping_threshold", "<f4"),
     ("linear_velocity", "<f4", (3,)), ("angular_velocity", "<f4", (3,)),
     ("collision_group", "<i4"), ("collision_mask", "<i4"), ("world", "<i4"),
+    ("collision_flags", "<i4"), ("activation_state", "<i4"),
 ])
-assert BODY_DTYPE.itemsize == 128
+assert BODY_DTYPE.itemsize == 136
 
 
 @dataclass
@@ -835,6 +836,68 @@ def ccd_shots(shots=24, seed=0, steps=90, plane=False, threshold=0.05, swept_rad
                                              "radius": swept_radius}, "walls_x": (6.0, 12.0)})
 
 
+# ---- kinematic and trigger bodies ------------------------------------------------------------
+def kinematic_platforms(platforms=4, boxes=3, seed=0, steps=240):
+    """Kinematic platforms (mass 0, KINEMATIC_OBJECT, DISABLE_DEACTIVATION) that the caller moves
+    every step (kinematic_pose) along small loops with a slow turn about y, dynamic boxes dropped
+    onto them, a ground plane; a static trigger box (NO_CONTACT_RESPONSE) under a box that falls
+    through it, a trigger sphere (dynamic, NO_CONTACT_RESPONSE) that falls through the ground, and
+    a kinematic box left at rest with the default activation (it falls asleep)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    shapes = [dict(PLANE),
+              {"type": _abi.SHAPE_BOX, "params": (1.5, 0.2, 1.5, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (0.3, 0.3, 0.3, 0.0), "points": None},
+              {"type": _abi.SHAPE_BOX, "params": (1.0, 0.5, 1.0, 0.0), "points": None},
+              {"type": _abi.SHAPE_SPHERE, "params": (0.4, 0.0, 0.0, 0.0), "points": None}]
+    parts = [_plane_body(0)]
+    base = np.array([[6.0 * (k % 2) - 3.0, 2.0 + 0.5 * (k // 2), 6.0 * (k // 2) - 3.0] for k in range(platforms)])
+    kin = _bodies(platforms)
+    kin["shape"] = 1
+    kin["collision_flags"] = _abi.CF_KINEMATIC_OBJECT
+    kin["activation_state"] = _abi.DISABLE_DEACTIVATION
+    kin["transform"][:, [0, 4, 8]] = 1.0
+    kin["transform"][:, 9:] = base.astype(F)
+    parts.append(kin)
+    box = _bodies(platforms * boxes)
+    box["shape"] = 2
+    box["mass"] = 1.0
+    box["local_inertia"] = box_inertia(1.0, (0.3, 0.3, 0.3))
+    pos = np.repeat(base, boxes, 0) + np.stack([rng.uniform(-0.8, 0.8, platforms * boxes),
+                                                np.tile(0.8 + 0.7 * np.arange(boxes), platforms),
+                                                rng.uniform(-0.8, 0.8, platforms * boxes)], 1)
+    _set_transforms(box, random_rotations(rng, platforms * boxes), pos)
+    parts.append(box)
+    extra = _bodies(4)
+    extra["shape"] = [3, 2, 4, 2]
+    extra["mass"] = [0.0, 1.0, 2.0, 0.0]
+    extra["collision_flags"] = [_abi.CF_NO_CONTACT_RESPONSE, 0, _abi.CF_NO_CONTACT_RESPONSE, _abi.CF_KINEMATIC_OBJECT]
+    extra["local_inertia"][1] = box_inertia(1.0, (0.3, 0.3, 0.3))
+    extra["local_inertia"][2] = sphere_inertia(2.0, 0.4)
+    extra["transform"][:, [0, 4, 8]] = 1.0
+    extra["transform"][:, 9:] = np.array([[10.0, 0.5, 0.0], [10.0, 2.5, 0.0], [-10.0, 3.0, 0.0], [0.0, 0.3, 10.0]], F)
+    parts.append(extra)
+    bodies = np.concatenate(parts)
+    return Scene("kinematic_platforms_%d" % platforms, 1.0 / 60.0, steps, {"gravity": (0.0, -9.81, 0.0)}, shapes,
+                 bodies, meta={"seed": seed, "kinematic": {"bodies": list(range(1, 1 + platforms)), "base": base}})
+
+
+def kinematic_pose(scene, step):
+    """The poses of the moving kinematic platforms at `step` (12 binary32 values each): origins
+    on loops of 1.2 m radius at about 1 m/s (faster than the sleeping threshold), turned about y
+    by up to 0.3 rad."""
+    k = scene.meta["kinematic"]
+    t = step * scene.dt
+    out = np.zeros((len(k["bodies"]), 12), F)
+    for j, base in enumerate(k["base"]):
+        ph = 0.7 * j
+        a = 0.3 * np.sin(0.5 * t + ph)
+        c, s = np.cos(a), np.sin(a)
+        out[j, :9] = np.array([c, 0.0, s, 0.0, 1.0, 0.0, -s, 0.0, c], F)
+        out[j, 9:] = (base + np.array([1.2 * np.sin(0.8 * t + ph), 0.2 * np.sin(1.1 * t + ph),
+                                       1.2 * np.cos(0.8 * t + ph) - 1.2])).astype(F)
+    return out
+
+
 # ---- compound and concave shapes ----------------------------------------------------------
 def _f(x):
     return F(x)
@@ -1087,6 +1150,7 @@ SCENES = {
     "cone_chains": cone_chains,
     "slider_rigs": slider_rigs,
     "ccd_shots": ccd_shots,
+    "kinematic_platforms": kinematic_platforms,
     "terrain": terrain,
     "compounds": compounds,
     # 20,000 convex and 2,000 compound bodies dropped on a 128 x 128-cell terrain (32,768

@@ -163,7 +163,7 @@ int orc_add_bodies(void* h, const jbgpu_body_desc* b, int n) {
                  d.linear_damping, d.angular_damping, d.friction, d.restitution, d.linear_sleeping_threshold,
                  d.angular_sleeping_threshold, v3(d.linear_velocity[0], d.linear_velocity[1], d.linear_velocity[2]),
                  v3(d.angular_velocity[0], d.angular_velocity[1], d.angular_velocity[2]), d.collision_group, d.collision_mask,
-                 d.world);
+                 d.world, d.collision_flags, d.activation_state);
     }
     return (int)w->bodies.size();
 }
@@ -184,6 +184,7 @@ void orc_stage(void* h, int stage, float dt) {
     case JBGPU_STAGE_INTEGRATE: stage_integrate(w, dt); break;
     case JBGPU_STAGE_ACTIVATION: stage_activation(w, dt); break;
     case JBGPU_STAGE_CLEAR_FORCES: stage_clear_forces(w); break;
+    case JBGPU_STAGE_SAVE_KINEMATIC: stage_save_kinematic(w, dt); break;
     }
 }
 

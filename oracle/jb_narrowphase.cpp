@@ -1278,7 +1278,7 @@ RayResult ray_test(const World& w, V3 from, V3 to, int group, int mask, int worl
 // CollisionWorld.java:596-645, objectQuerySingle 391-490, ClosestConvexResultCallback 766-805)
 // ----------------------------------------------------------------------------------------
 // TransformUtil.calculateVelocity / calculateDiffAxisAngle (linearmath/TransformUtil.java:105-153)
-static void calculate_velocity(const Xf& t0, const Xf& t1, float timeStep, V3& linVel, V3& angVel) {
+void calculate_velocity(const Xf& t0, const Xf& t1, float timeStep, V3& linVel, V3& angVel) {
     linVel = scl(sub(t1.o, t0.o), 1.0f / timeStep);
     M3 dmat = mulMM(t1.b, m3_invert(t0.b));
     Quat dorn = qnor(q_from_matrix(dmat));

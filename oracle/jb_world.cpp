@@ -31,10 +31,14 @@ static float gen_clamped(float a, float lb, float ub) { return a < lb ? lb : (ub
 // (dynamics/RigidBody.java:121-164,301-312; dynamics/DiscreteDynamicsWorld.java:426-440;
 //  collision/dispatch/CollisionWorld.java:103-121)
 int add_body(World& w, float mass, int shape, const Xf& xf, V3 inertia, float linDamp, float angDamp, float friction,
-             float restitution, float linSleep, float angSleep, V3 linvel, V3 angvel, int group, int mask, int world) {
+             float restitution, float linSleep, float angSleep, V3 linvel, V3 angvel, int group, int mask, int world,
+             int collisionFlags, int activationState) {
     Body b;
     b.world = world;
     b.xf = xf;
+    b.ixf = xf;   // RigidBody.setupRigidBody: interpolationWorldTransform = worldTransform
+    b.flags |= collisionFlags & (CF_KINEMATIC_OBJECT | CF_NO_CONTACT_RESPONSE);
+    if (activationState != 0) b.activation = activationState;
     b.shape = shape;
     b.friction = friction;
     b.restitution = restitution;
@@ -1475,6 +1479,17 @@ void internal_single_step(World& w, float dt) {
 }
 
 // stepSimulation (dynamics/DiscreteDynamicsWorld.java:290-354)
+// DiscreteDynamicsWorld.saveKinematicState (DiscreteDynamicsWorld.java:105-119): every kinematic
+// body that is not ISLAND_SLEEPING takes the velocities that carry its last saved transform to
+// its current one (RigidBody.saveKinematicState, RigidBody.java:190-205).
+void stage_save_kinematic(World& w, float timeStep) {
+    for (Body& b : w.bodies) {
+        if (b.activation == ISLAND_SLEEPING || !b.isKinematic() || timeStep == 0.0f) continue;
+        calculate_velocity(b.ixf, b.xf, timeStep, b.linvel, b.angvel);
+        b.ixf = b.xf;
+    }
+}
+
 int step_simulation(World& w, float timeStep, int maxSubSteps, float fixedTimeStep) {
     int num = 0;
     if (maxSubSteps != 0) {
@@ -1490,6 +1505,7 @@ int step_simulation(World& w, float timeStep, int maxSubSteps, float fixedTimeSt
         else { num = 1; maxSubSteps = 1; }
     }
     if (num != 0) {
+        stage_save_kinematic(w, fixedTimeStep);
         stage_apply_gravity(w);
         int clamped = num > maxSubSteps ? maxSubSteps : num;
         for (int i = 0; i < clamped; i++) internal_single_step(w, fixedTimeStep);
@@ -1499,6 +1515,7 @@ int step_simulation(World& w, float timeStep, int maxSubSteps, float fixedTimeSt
 }
 
 void step_fixed(World& w, float dt, int substeps) {
+    stage_save_kinematic(w, dt);
     stage_apply_gravity(w);
     for (int i = 0; i < substeps; i++) internal_single_step(w, dt);
     stage_clear_forces(w);

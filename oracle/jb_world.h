@@ -99,6 +99,7 @@ struct Manifold {        // collision/narrowphase/PersistentManifold.java
 
 struct Body {            // dynamics/RigidBody.java + collision/dispatch/CollisionObject.java
     Xf xf;
+    Xf ixf;                                 // interpolationWorldTransform (saveKinematicState)
     V3 linvel{0, 0, 0}, angvel{0, 0, 0};
     float invMass = 0;
     V3 invInertiaLocal{0, 0, 0};
@@ -280,10 +281,14 @@ void stage_activation(World& w, float dt);
 void stage_clear_forces(World& w);
 void internal_single_step(World& w, float dt);
 int step_simulation(World& w, float timeStep, int maxSubSteps, float fixedTimeStep);
+void stage_save_kinematic(World& w, float timeStep);
+void calculate_velocity(const Xf& t0, const Xf& t1, float timeStep, V3& linVel, V3& angVel);
 void step_fixed(World& w, float dt, int substeps);
+// collisionFlags: setCollisionFlags (KINEMATIC_OBJECT, NO_CONTACT_RESPONSE) and activationState:
+// setActivationState (0: ACTIVE_TAG), both called before addRigidBody
 int add_body(World& w, float mass, int shape, const Xf& xf, V3 localInertia, float linDamp, float angDamp,
              float friction, float restitution, float linSleep, float angSleep, V3 linvel, V3 angvel, int group, int mask,
-             int world = 0);
+             int world = 0, int collisionFlags = 0, int activationState = 0);
 
 // narrowphase entry (collision/dispatch/DefaultNearCallback.java:39-66 for one pair)
 void process_pair(World& w, int pairIndex);
