@@ -350,6 +350,14 @@ int jbgpu_world_narrowphase_static(jbgpu_world* world, int32_t epa_slots);
 int jbgpu_world_set_ccd(jbgpu_world* world, const int32_t* bodies, const float* motion_threshold,
                         const float* swept_sphere_radius, int32_t n);
 
+/* DiscreteDynamicsWorld.setGravity (dynamics/DiscreteDynamicsWorld.java:403-412): the gravity of
+ * bodies added later, and RigidBody.setGravity for every body already in the world. */
+int jbgpu_world_set_gravity(jbgpu_world* world, const float gravity[3]);
+/* RigidBody.setGravity (dynamics/RigidBody.java:213-217) for n bodies, acceleration 3 floats each:
+ * the body's gravity force becomes acceleration scaled by 1 / inverseMass; a body of inverse mass 0
+ * keeps its own. */
+int jbgpu_world_set_body_gravity(jbgpu_world* world, const int32_t* bodies, const float* acceleration, int32_t n);
+
 /* Wait for the world's stream. */
 int jbgpu_world_synchronize(jbgpu_world* world);
 

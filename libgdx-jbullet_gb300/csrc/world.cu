@@ -1616,6 +1616,42 @@ int jbgpu_world_set_ccd(jbgpu_world* w, const int32_t* bodies, const float* thr,
     return JBGPU_OK;
 }
 
+// RigidBody.setGravity on the host copy of the bodies' inverse masses and gravity forces:
+// gravity = acceleration * (1 / inverseMass) for inverseMass != 0 (binary32, no contraction).
+static int body_gravity(jbgpu_world* w, const int32_t* bodies, const float* acc, int32_t n, bool all) {
+    if (w->nBodies == 0) return JBGPU_OK;
+    CK(cudaSetDevice(w->device));
+    CK(cudaStreamSynchronize(w->stream));
+    std::vector<float4> il(w->nBodies), g(w->nBodies);
+    CK(cudaMemcpy(il.data(), w->dw.iloc, sizeof(float4) * w->nBodies, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(g.data(), w->dw.gravity, sizeof(float4) * w->nBodies, cudaMemcpyDeviceToHost));
+    const int m = all ? w->nBodies : n;
+    for (int k = 0; k < m; k++) {
+        const int i = all ? k : bodies[k];
+        const float* a = all ? acc : acc + 3 * k;
+        const float im = il[i].w;
+        if (im != 0.0f) {
+            const float s = 1.0f / im;
+            g[i] = make_float4(a[0] * s, a[1] * s, a[2] * s, 0.0f);
+        }
+    }
+    CK(cudaMemcpy(w->dw.gravity, g.data(), sizeof(float4) * w->nBodies, cudaMemcpyHostToDevice));
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_gravity(jbgpu_world* w, const float gravity[3]) {
+    if (!w || !gravity) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    for (int k = 0; k < 3; k++) { w->cfg.gravity[k] = gravity[k]; w->dw.gravityAcc[k] = gravity[k]; }
+    return body_gravity(w, nullptr, gravity, 0, true);
+}
+
+int jbgpu_world_set_body_gravity(jbgpu_world* w, const int32_t* bodies, const float* acc, int32_t n) {
+    if (!w || n < 0 || (n > 0 && (!bodies || !acc))) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad gravity arguments");
+    for (int k = 0; k < n; k++)
+        if (bodies[k] < 0 || bodies[k] >= w->nBodies) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad body index");
+    return n == 0 ? JBGPU_OK : body_gravity(w, bodies, acc, n, false);
+}
+
 int jbgpu_world_get_residual_trace(jbgpu_world* w, float* out, int32_t cap, int32_t* n) {
     if (!w || !n || cap < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
     CK(cudaSetDevice(w->device));

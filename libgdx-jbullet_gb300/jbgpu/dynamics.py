@@ -235,6 +235,18 @@ class RigidBody:
         self._ccd = (0.0, 0.0)          # ccdMotionThreshold, ccdSweptSphereRadius
         self._flags = 0                 # KINEMATIC_OBJECT / NO_CONTACT_RESPONSE set before addRigidBody
         self._activation = 0            # setActivationState before addRigidBody (0: ACTIVE_TAG)
+        self._gravity_acc = None        # RigidBody.setGravity staged until the body is on the device
+
+    def setGravity(self, acceleration):
+        """RigidBody.setGravity (RigidBody.java:213-217).  Before addRigidBody it has no lasting
+        effect: addRigidBody sets the world's gravity on a body that is not static or kinematic."""
+        a = tuple(float(x) for x in acceleration)
+        if self._world is None:
+            return
+        if self._world._g is not None and self._index < self._world._uploaded:
+            self._world._g.set_body_gravity([self._index], [a])
+        else:
+            self._gravity_acc = a
 
     # CollisionObject.setCollisionFlags / getCollisionFlags (collision/dispatch/CollisionObject.java):
     # KINEMATIC_OBJECT and NO_CONTACT_RESPONSE, set before the body is added; STATIC_OBJECT
@@ -759,9 +771,12 @@ class DiscreteDynamicsWorld:
 
     # -- configuration (before the first step) --
     def setGravity(self, g):
-        if self._g is not None:
-            raise RuntimeError("setGravity after the first step is not supported by the GPU world")
+        """DiscreteDynamicsWorld.setGravity: the world's gravity and RigidBody.setGravity of every body."""
         self._gravity = tuple(float(x) for x in g)
+        if self._g is not None:
+            self._g.set_gravity(self._gravity)
+        for b in self._bodies:
+            b._gravity_acc = None   # the world's call overrides a body's own setGravity staged before upload
 
     def getGravity(self):
         return self._gravity
@@ -884,6 +899,11 @@ class DiscreteDynamicsWorld:
         lib.check(lib.lib().jbgpu_world_add_bodies(g.h, ptr, len(b), None))
         self._uploaded = len(self._bodies)
         self._forces = None
+        grav = [b for b in new if b._gravity_acc is not None]
+        if grav:   # addRigidBody set the world's gravity; a later setGravity of the body overrides it
+            g.set_body_gravity([b._index for b in grav], [b._gravity_acc for b in grav])
+            for b in grav:
+                b._gravity_acc = None
         ccd = [b for b in new if b._ccd != (0.0, 0.0)]
         if ccd:
             g.set_ccd([b._index for b in ccd], [b._ccd[0] for b in ccd], [b._ccd[1] for b in ccd])

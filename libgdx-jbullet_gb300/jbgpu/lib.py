@@ -103,6 +103,8 @@ def lib():
             "jbgpu_world_get_residual_trace": ([C.c_void_p, _abi.f32p, C.c_int32, _abi.i32p], C.c_int),
             "jbgpu_world_set_ccd": ([C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_refit_mesh": ([C.c_void_p, C.c_int32, _abi.f32p, C.c_int32], C.c_int),
+            "jbgpu_world_set_gravity": ([C.c_void_p, _abi.f32p], C.c_int),
+            "jbgpu_world_set_body_gravity": ([C.c_void_p, _abi.i32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_mesh_bvh": ([C.c_void_p, C.c_int32, _abi.i32p, C.c_int32, _abi.i32p, _abi.f32p], C.c_int),
             "jbgpu_world_set_sample_logging": ([C.c_void_p, C.c_int32], C.c_int),
             "jbgpu_world_get_samples": ([C.c_void_p, _abi.f32p, _abi.f32p, C.c_int32, _abi.i32p], C.c_int),
@@ -130,7 +132,7 @@ EXPORTED = [
     "jbgpu_world_add_cone_twist", "jbgpu_world_set_cone_twist_limit", "jbgpu_world_set_cone_twist_angular_only",
     "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
     "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd", "jbgpu_shape_mesh_bvh", "jbgpu_world_refit_mesh",
-    "jbgpu_world_mesh_bvh",
+    "jbgpu_world_mesh_bvh", "jbgpu_world_set_gravity", "jbgpu_world_set_body_gravity",
 ]
 
 
@@ -482,6 +484,18 @@ class GpuWorld:
 
     def set_solver_iterations(self, num_iterations, residual=0.0, max_iterations=0):
         check(lib().jbgpu_world_set_solver_iterations(self.h, num_iterations, residual, max_iterations))
+
+    def set_gravity(self, g):
+        """DiscreteDynamicsWorld.setGravity (jbgpu_world_set_gravity)."""
+        a = np.ascontiguousarray(g, np.float32).reshape(3)
+        check(lib().jbgpu_world_set_gravity(self.h, a.ctypes.data_as(_abi.f32p)))
+
+    def set_body_gravity(self, bodies, acceleration):
+        """RigidBody.setGravity for the given bodies (one acceleration each, or one for all)."""
+        b = np.ascontiguousarray(bodies, np.int32).reshape(-1)
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(acceleration, np.float32).reshape(-1, 3), (len(b), 3)),
+                                 np.float32)
+        check(lib().jbgpu_world_set_body_gravity(self.h, b.ctypes.data_as(_abi.i32p), a.ctypes.data_as(_abi.f32p), len(b)))
 
     def refit_mesh(self, shape, points):
         """New positions of a triangle mesh's vertices: BvhTriangleMeshShape.refitTree and

@@ -372,6 +372,24 @@ int orc_get_state(void* h, jbgpu_state* s) {
     return 0;
 }
 
+// DiscreteDynamicsWorld.setGravity (DiscreteDynamicsWorld.java:403-412) and RigidBody.setGravity
+// (RigidBody.java:213-217): gravity = acceleration scaled by 1 / inverseMass when that is nonzero.
+static void set_body_gravity(Body& b, V3 acc) {
+    if (b.invMass != 0.0f) b.gravity = scl(acc, 1.0f / b.invMass);
+}
+void orc_set_gravity(void* h, const float* g) {
+    World* w = (World*)h;
+    w->cfg.gravity = v3(g[0], g[1], g[2]);
+    for (Body& b : w->bodies) set_body_gravity(b, w->cfg.gravity);
+}
+int orc_set_body_gravity(void* h, const int* bodies, const float* acc, int n) {
+    World* w = (World*)h;
+    for (int k = 0; k < n; k++)
+        if (bodies[k] < 0 || bodies[k] >= (int)w->bodies.size()) return -1;
+    for (int k = 0; k < n; k++) set_body_gravity(w->bodies[bodies[k]], v3(acc[3 * k], acc[3 * k + 1], acc[3 * k + 2]));
+    return 0;
+}
+
 int orc_set_ccd(void* h, const int* bodies, const float* threshold, const float* radius, int n) {
     World& w = *(World*)h;
     for (int k = 0; k < n; k++) {

@@ -72,6 +72,8 @@ def lib():
         L.orc_set_hinge_angular_only.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.orc_set_ccd.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, C.c_int]
         L.orc_refit_mesh.argtypes = [C.c_void_p, C.c_int, _abi.f32p, C.c_int]
+        L.orc_set_gravity.argtypes = [C.c_void_p, _abi.f32p]
+        L.orc_set_body_gravity.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, C.c_int]
         L.orc_world_mesh_bvh.argtypes = [C.c_void_p, C.c_int, _abi.i32p, C.c_int, _abi.f32p]
         _lib = L
     return _lib
@@ -259,6 +261,19 @@ class OracleWorld:
 
     def step_simulation(self, time_step, max_sub_steps=1, fixed_time_step=1.0 / 60.0):
         return lib().orc_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step)
+
+    def set_gravity(self, g):
+        """DiscreteDynamicsWorld.setGravity."""
+        a = np.ascontiguousarray(g, np.float32).reshape(3)
+        lib().orc_set_gravity(self.h, _fp(a))
+
+    def set_body_gravity(self, bodies, acceleration):
+        """RigidBody.setGravity for the given bodies (one acceleration each, or one for all)."""
+        b = np.ascontiguousarray(bodies, np.int32).reshape(-1)
+        a = np.ascontiguousarray(np.broadcast_to(np.asarray(acceleration, np.float32).reshape(-1, 3), (len(b), 3)),
+                                 np.float32)
+        if lib().orc_set_body_gravity(self.h, b.ctypes.data_as(_abi.i32p), _fp(a), len(b)) != 0:
+            raise ValueError("set_body_gravity: bad body index")
 
     def refit_mesh(self, shape, points):
         """New positions of a triangle mesh's vertices, then BvhTriangleMeshShape.refitTree and
