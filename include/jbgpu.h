@@ -313,6 +313,13 @@ int jbgpu_world_refit_mesh(jbgpu_world* world, int32_t shape, const float* point
 int jbgpu_world_mesh_bvh(const jbgpu_world* world, int32_t shape, int32_t* nodes, int32_t capacity, int32_t* n_nodes,
                          float local_aabb[6]);
 int jbgpu_world_add_bodies(jbgpu_world* world, const jbgpu_body_desc* bodies, int32_t n, int32_t* uids_out);
+/* DiscreteDynamicsWorld.removeRigidBody for n distinct bodies (dynamics/DiscreteDynamicsWorld.java:
+ * 442-445 -> CollisionWorld.removeCollisionObject, collision/dispatch/CollisionWorld.java:157-176):
+ * the pairs and manifolds that involve them go (cleanProxyFromPairs, destroyProxy), and the bodies
+ * after each removed one move down as in the reference's collisionObjects list - a body's index
+ * drops by the number of removed bodies before it.  A body that a joint uses is refused
+ * (JBGPU_ERR_INVALID_ARGUMENT). */
+int jbgpu_world_remove_bodies(jbgpu_world* world, const int32_t* bodies, int32_t n);
 int jbgpu_world_num_bodies(const jbgpu_world* world, int32_t* n);
 
 /* stepSimulation: the reference's fixed-timestep accumulator, applyGravity once per call,

@@ -894,6 +894,47 @@ int ensure_io(jbgpu_world* w) {
 }
 }  // namespace
 
+namespace removal {
+// Body removal: dst[j] = src[from[j]] for every kept body, and the pairs whose bodies both stay,
+// moved to the other pair buffer in their order with the bodies renumbered.
+template <class T>
+__global__ void k_gather(const T* src, T* dst, const int* from, int n) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) dst[j] = src[from[j]];
+}
+__global__ void k_pairs_keep(DevPairs P, int nPairs, const int* newIndex, int* flag) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nPairs) return;
+    const uint64_t k = P.keys[p];
+    flag[p] = newIndex[key_owner(k)] >= 0 && newIndex[key_partner(k)] >= 0;
+}
+__global__ void k_pairs_move(DevPairs S, DevPairs D, int nPairs, const int* flag, const int* pos, const int* newIndex) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nPairs || !flag[p]) return;
+    const int q = pos[p];
+    const uint64_t k = S.keys[p];
+    D.keys[q] = ((uint64_t)(unsigned)newIndex[key_owner(k)] << 32) | ((uint64_t)key_sub(k) << 24) |
+                (uint64_t)(unsigned)newIndex[key_partner(k)];
+    D.has[q] = S.has[p];
+    D.n[q] = S.n[p];
+    D.b0[q] = S.b0[p] >= 0 ? newIndex[S.b0[p]] : S.b0[p];
+    D.b1[q] = S.b1[p] >= 0 ? newIndex[S.b1[p]] : S.b1[p];
+    for (int j = 0; j < 4; j++) {
+        const int s = 4 * p + j, d = 4 * q + j;
+        D.pA[d] = S.pA[s]; D.pB[d] = S.pB[s]; D.wA[d] = S.wA[s]; D.wB[d] = S.wB[s];
+        D.nrm[d] = S.nrm[s]; D.imp[d] = S.imp[s]; D.d1[d] = S.d1[s]; D.d2[d] = S.d2[s];
+    }
+}
+template <class T>
+int gather_array(T* a, const int* from, int n, void* tmp, cudaStream_t s) {
+    if (n == 0) return JBGPU_OK;
+    k_gather<T><<<(n + 255) / 256, 256, 0, s>>>(a, (T*)tmp, from, n);
+    note_launch();
+    CK(cudaMemcpyAsync(a, tmp, sizeof(T) * n, cudaMemcpyDeviceToDevice, s));
+    return JBGPU_OK;
+}
+}  // namespace removal
+
 extern "C" {
 
 const char* jbgpu_version(void) { return "jbgpu 0.1 (sm_103a)"; }
@@ -1513,6 +1554,93 @@ int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, 
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(s));
     w->planesDirty = true;
+    return JBGPU_OK;
+}
+
+
+int jbgpu_world_remove_bodies(jbgpu_world* w, const int32_t* bodies, int32_t n) {
+    if (!w || n < 0 || (n > 0 && !bodies)) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (n == 0) return JBGPU_OK;
+    const int nOld = w->nBodies;
+    std::vector<int> newIndex(nOld, 0);
+    for (int k = 0; k < n; k++) {
+        if (bodies[k] < 0 || bodies[k] >= nOld) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad body index");
+        if (newIndex[bodies[k]] < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "a body listed twice");
+        newIndex[bodies[k]] = -1;
+    }
+    for (size_t j = 0; j < w->jA.size(); j++)
+        if ((w->jA[j] >= 0 && newIndex[w->jA[j]] < 0) || (w->jB[j] >= 0 && newIndex[w->jB[j]] < 0))
+            return fail(JBGPU_ERR_INVALID_ARGUMENT, "a joint uses a body to remove (remove the joint first)");
+    std::vector<int> from;
+    for (int i = 0; i < nOld; i++)
+        if (newIndex[i] >= 0) { newIndex[i] = (int)from.size(); from.push_back(i); }
+    const int nNew = (int)from.size();
+    CK(cudaSetDevice(w->device));
+    cudaStream_t s = w->stream;
+    CK(cudaStreamSynchronize(s));
+    int *dFrom = nullptr, *dNew = nullptr;
+    void* tmp = nullptr;
+    CK(dalloc(&dFrom, std::max(nNew, 1)));
+    CK(dalloc(&dNew, nOld));
+    CK(cudaMalloc(&tmp, sizeof(float4) * std::max(nNew, 1)));
+    CK(cudaMemcpy(dFrom, from.data(), sizeof(int) * nNew, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dNew, newIndex.data(), sizeof(int) * nOld, cudaMemcpyHostToDevice));
+    DevWorld& d = w->dw;
+    int rc = 0;
+    using namespace removal;
+#define GA(ptr) if (!rc) rc = gather_array(d.ptr, dFrom, nNew, tmp, s)
+    GA(xr0); GA(xr1); GA(xr2); GA(kx0); GA(kx1); GA(kx2); GA(linvel); GA(angvel); GA(iw0); GA(iw1); GA(iw2); GA(iloc);
+    GA(force); GA(torque); GA(gravity); GA(amin); GA(amax); GA(act); GA(deact); GA(flags); GA(shape); GA(group);
+    GA(mask); GA(world); GA(friction); GA(restitution); GA(linSleep); GA(angSleep); GA(linDamp); GA(angDamp);
+    GA(ccdThr); GA(ccdRad);
+#undef GA
+    // the pairs of kept bodies, renumbered, into the other pair buffer
+    const int np = w->nPairs;
+    int kept = 0;
+    if (!rc && np > 0) {
+        const int nxt = w->cur ^ 1;
+        rc = ensure_pair_capacity(w, nxt, np);
+        int *flag = nullptr, *pos = nullptr, *tot = nullptr;
+        void* scratch = nullptr;
+        if (!rc && (dalloc(&flag, np) != cudaSuccess || dalloc(&pos, np) != cudaSuccess || dalloc(&tot, 1) != cudaSuccess ||
+                    cudaMalloc(&scratch, scan_scratch_bytes(np)) != cudaSuccess))
+            rc = fail(JBGPU_ERR_CUDA, "pair compaction buffers");
+        if (!rc) {
+            k_pairs_keep<<<(np + 255) / 256, 256, 0, s>>>(w->pairs[w->cur], np, dNew, flag); note_launch();
+            exclusive_scan(flag, pos, tot, np, scratch, s);
+            k_pairs_move<<<(np + 255) / 256, 256, 0, s>>>(w->pairs[w->cur], w->pairs[nxt], np, flag, pos, dNew);
+            note_launch();
+            // the device's pair count (which the replayed step reads as last step's) follows
+            if (cudaMemcpyAsync(w->dw.ctr + C_PAIRS, tot, sizeof(int), cudaMemcpyDeviceToDevice, s) != cudaSuccess ||
+                cudaMemcpyAsync(&kept, tot, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                cudaStreamSynchronize(s) != cudaSuccess)
+                rc = fail(JBGPU_ERR_CUDA, "pair compaction");
+            else
+                w->cur = nxt;
+        }
+        dfree(flag); dfree(pos); dfree(tot);
+        if (scratch) cudaFree(scratch);
+    }
+    if (!rc && cudaStreamSynchronize(s) != cudaSuccess) rc = fail(JBGPU_ERR_CUDA, "body compaction");
+    dfree(dFrom); dfree(dNew);
+    cudaFree(tmp);
+    if (rc) return rc;
+    w->nPairs = kept;
+    auto compact = [&](std::vector<int>& v) {
+        std::vector<int> o(nNew);
+        for (int j = 0; j < nNew; j++) o[j] = v[from[j]];
+        v.swap(o);
+    };
+    compact(w->hShape); compact(w->hWorld); compact(w->hFlags);
+    for (size_t j = 0; j < w->jA.size(); j++) {   // the joints' bodies renumbered
+        if (w->jA[j] >= 0) w->jA[j] = newIndex[w->jA[j]];
+        if (w->jB[j] >= 0) w->jB[j] = newIndex[w->jB[j]];
+    }
+    if (!w->jA.empty()) w->jointsDirty = true;
+    w->nBodies = nNew;
+    w->bb.offPrevValid = false;
+    w->planesDirty = true;   // listed bodies, per-world counts, the tree and the solver parts
+    graphs_clear(w);
     return JBGPU_OK;
 }
 

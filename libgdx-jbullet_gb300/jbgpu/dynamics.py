@@ -795,6 +795,27 @@ class DiscreteDynamicsWorld:
         if self._g is not None:
             self._upload()
 
+    def removeRigidBody(self, body):
+        """DiscreteDynamicsWorld.removeRigidBody: the body leaves the world with its pairs and
+        manifolds; the bodies after it move down (their _index drops by one)."""
+        if body._world is not self:
+            return
+        i = body._index
+        for c in self._constraints:
+            if c.rbA is body or getattr(c, "rbB", None) is body:
+                raise RuntimeError("removeRigidBody of a body a constraint uses (remove the constraint first)")
+        if self._g is not None and i < self._uploaded:
+            self._g.remove_bodies([i])
+            self._uploaded -= 1
+        del self._bodies[i]
+        for b in self._bodies[i:]:
+            b._index -= 1
+        if self._forces is not None:
+            self._forces = np.delete(self._forces, i, 0)
+        self._cache = None
+        body._world = None
+        body._index = None
+
     def getNumCollisionObjects(self):
         return len(self._bodies)
 

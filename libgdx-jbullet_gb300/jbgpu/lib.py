@@ -104,6 +104,7 @@ def lib():
             "jbgpu_world_set_ccd": ([C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_refit_mesh": ([C.c_void_p, C.c_int32, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_set_gravity": ([C.c_void_p, _abi.f32p], C.c_int),
+            "jbgpu_world_remove_bodies": ([C.c_void_p, _abi.i32p, C.c_int32], C.c_int),
             "jbgpu_world_set_body_gravity": ([C.c_void_p, _abi.i32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_mesh_bvh": ([C.c_void_p, C.c_int32, _abi.i32p, C.c_int32, _abi.i32p, _abi.f32p], C.c_int),
             "jbgpu_world_set_sample_logging": ([C.c_void_p, C.c_int32], C.c_int),
@@ -132,7 +133,7 @@ EXPORTED = [
     "jbgpu_world_add_cone_twist", "jbgpu_world_set_cone_twist_limit", "jbgpu_world_set_cone_twist_angular_only",
     "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
     "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd", "jbgpu_shape_mesh_bvh", "jbgpu_world_refit_mesh",
-    "jbgpu_world_mesh_bvh", "jbgpu_world_set_gravity", "jbgpu_world_set_body_gravity",
+    "jbgpu_world_mesh_bvh", "jbgpu_world_set_gravity", "jbgpu_world_set_body_gravity", "jbgpu_world_remove_bodies",
 ]
 
 
@@ -484,6 +485,12 @@ class GpuWorld:
 
     def set_solver_iterations(self, num_iterations, residual=0.0, max_iterations=0):
         check(lib().jbgpu_world_set_solver_iterations(self.h, num_iterations, residual, max_iterations))
+
+    def remove_bodies(self, bodies):
+        """DiscreteDynamicsWorld.removeRigidBody for the given bodies (jbgpu_world_remove_bodies):
+        the bodies after each removed one move down."""
+        b = np.ascontiguousarray(bodies, np.int32).reshape(-1)
+        check(lib().jbgpu_world_remove_bodies(self.h, b.ctypes.data_as(_abi.i32p), len(b)))
 
     def set_gravity(self, g):
         """DiscreteDynamicsWorld.setGravity (jbgpu_world_set_gravity)."""

@@ -372,6 +372,53 @@ int orc_get_state(void* h, jbgpu_state* s) {
     return 0;
 }
 
+// DiscreteDynamicsWorld.removeRigidBody -> CollisionWorld.removeCollisionObject
+// (CollisionWorld.java:157-176): the pairs (with their manifolds) that involve a removed body go,
+// the bodies after it move down in the collision object list and the remaining keys are
+// renumbered; -1 for a bad or repeated index or a body a joint uses.
+int orc_remove_bodies(void* h, const int* bodies, int n) {
+    World* w = (World*)h;
+    const int nOld = (int)w->bodies.size();
+    std::vector<int> newIndex(nOld, 0);
+    for (int k = 0; k < n; k++) {
+        if (bodies[k] < 0 || bodies[k] >= nOld || newIndex[bodies[k]] < 0) return -1;
+        newIndex[bodies[k]] = -1;
+    }
+    for (const Joint& j : w->joints)
+        if ((j.a >= 0 && newIndex[j.a] < 0) || (j.b >= 0 && newIndex[j.b] < 0)) return -1;
+    int m = 0;
+    std::vector<Body> kept;
+    for (int i = 0; i < nOld; i++)
+        if (newIndex[i] >= 0) { newIndex[i] = m++; kept.push_back(w->bodies[i]); }
+    w->bodies.swap(kept);
+    std::vector<uint64_t> keys;
+    std::vector<uint8_t> has;
+    std::vector<Manifold> mf;
+    for (size_t p = 0; p < w->pairKeys.size(); p++) {
+        const uint64_t k = w->pairKeys[p];
+        const int o = newIndex[key_owner(k)], q = newIndex[key_partner(k)];
+        if (o < 0 || q < 0) continue;
+        keys.push_back(((uint64_t)(unsigned)o << 32) | ((uint64_t)key_sub(k) << 24) | (uint64_t)(unsigned)q);
+        has.push_back(w->pairHasAlgo[p]);
+        Manifold f = w->pairMf[p];
+        if (f.body0 >= 0) f.body0 = newIndex[f.body0];
+        if (f.body1 >= 0) f.body1 = newIndex[f.body1];
+        mf.push_back(f);
+    }
+    w->pairKeys.swap(keys);
+    w->pairHasAlgo.swap(has);
+    w->pairMf.swap(mf);
+    for (Joint& j : w->joints) {
+        if (j.a >= 0) j.a = newIndex[j.a];
+        if (j.b >= 0) j.b = newIndex[j.b];
+    }
+    w->solveList.clear();
+    w->lastOrder.clear();
+    w->lastColour.clear();
+    w->explicitOrder.clear();
+    return 0;
+}
+
 // DiscreteDynamicsWorld.setGravity (DiscreteDynamicsWorld.java:403-412) and RigidBody.setGravity
 // (RigidBody.java:213-217): gravity = acceleration scaled by 1 / inverseMass when that is nonzero.
 static void set_body_gravity(Body& b, V3 acc) {

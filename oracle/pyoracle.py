@@ -73,6 +73,7 @@ def lib():
         L.orc_set_ccd.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, C.c_int]
         L.orc_refit_mesh.argtypes = [C.c_void_p, C.c_int, _abi.f32p, C.c_int]
         L.orc_set_gravity.argtypes = [C.c_void_p, _abi.f32p]
+        L.orc_remove_bodies.argtypes = [C.c_void_p, _abi.i32p, C.c_int]
         L.orc_set_body_gravity.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, C.c_int]
         L.orc_world_mesh_bvh.argtypes = [C.c_void_p, C.c_int, _abi.i32p, C.c_int, _abi.f32p]
         _lib = L
@@ -261,6 +262,12 @@ class OracleWorld:
 
     def step_simulation(self, time_step, max_sub_steps=1, fixed_time_step=1.0 / 60.0):
         return lib().orc_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step)
+
+    def remove_bodies(self, bodies):
+        """DiscreteDynamicsWorld.removeRigidBody for the given bodies (later bodies move down)."""
+        b = np.ascontiguousarray(bodies, np.int32).reshape(-1)
+        if lib().orc_remove_bodies(self.h, b.ctypes.data_as(_abi.i32p), len(b)) != 0:
+            raise ValueError("remove_bodies: bad index, repeated index or a body a joint uses")
 
     def set_gravity(self, g):
         """DiscreteDynamicsWorld.setGravity."""
