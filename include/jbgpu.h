@@ -357,6 +357,14 @@ int jbgpu_world_narrowphase_static(jbgpu_world* world, int32_t epa_slots);
 int jbgpu_world_set_ccd(jbgpu_world* world, const int32_t* bodies, const float* motion_threshold,
                         const float* swept_sphere_radius, int32_t n);
 
+/* RigidBody impulses for n distinct bodies (dynamics/RigidBody.java:395-430), 3 floats each:
+ * impulses with rel_pos NULL is applyCentralImpulse (v += impulse * inverseMass), with rel_pos
+ * applyImpulse (for a body of nonzero inverse mass: the central impulse, then applyTorqueImpulse of
+ * rel_pos x impulse); torque_impulses (nullable) then applyTorqueImpulse
+ * (w += invInertiaTensorWorld * torque).  impulses may be NULL when only torque impulses are given. */
+int jbgpu_world_apply_impulses(jbgpu_world* world, const int32_t* bodies, const float* impulses, const float* rel_pos,
+                               const float* torque_impulses, int32_t n);
+
 /* DiscreteDynamicsWorld.setGravity (dynamics/DiscreteDynamicsWorld.java:403-412): the gravity of
  * bodies added later, and RigidBody.setGravity for every body already in the world. */
 int jbgpu_world_set_gravity(jbgpu_world* world, const float gravity[3]);

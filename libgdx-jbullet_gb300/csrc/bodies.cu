@@ -155,6 +155,36 @@ __global__ void k_save_kinematic(DevWorld w, float timeStep) {
 void launch_save_kinematic(const DevWorld& w, float timeStep, cudaStream_t s) {
     if (w.nBodies) { k_save_kinematic<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w, timeStep); note_launch(); }
 }
+// RigidBody.applyCentralImpulse / applyImpulse / applyTorqueImpulse (RigidBody.java:395-430),
+// linear and angular factors 1: a thread per listed body (distinct bodies).
+__global__ void k_apply_impulses(DevWorld w, const int* bodies, const float* imp, const float* rel, const float* tq, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int i = bodies[k];
+    const float im = w.iloc[i].w;
+    const float4 a = w.iw0[i], b = w.iw1[i], c = w.iw2[i];
+    M iw;
+    iw.r[0] = mk(a.x, a.y, a.z);
+    iw.r[1] = mk(b.x, b.y, b.z);
+    iw.r[2] = mk(c.x, c.y, c.z);
+    V lin = mk4(w.linvel[i]), ang = mk4(w.angvel[i]);
+    if (imp) {
+        const V J = mk(imp[3 * k], imp[3 * k + 1], imp[3 * k + 2]);
+        if (!rel || im != 0.0f) lin = add(lin, scl(J, im));                    // applyCentralImpulse
+        if (rel && im != 0.0f) {                                                  // applyImpulse's torque part
+            const V r = mk(rel[3 * k], rel[3 * k + 1], rel[3 * k + 2]);
+            ang = add(ang, mulMv(crs(r, J), iw));
+        }
+    }
+    if (tq) ang = add(ang, mulMv(mk(tq[3 * k], tq[3 * k + 1], tq[3 * k + 2]), iw));   // applyTorqueImpulse
+    w.linvel[i] = f4(lin, 0.0f);
+    w.angvel[i] = f4(ang, 0.0f);
+}
+void launch_apply_impulses(const DevWorld& w, const int* bodies, const float* imp, const float* rel, const float* tq, int n,
+                           cudaStream_t s) {
+    if (n > 0) { k_apply_impulses<<<grid_for(n, 128), 128, 0, s>>>(w, bodies, imp, rel, tq, n); note_launch(); }
+}
+
 void launch_apply_gravity(const DevWorld& w, cudaStream_t s) {
     if (w.nBodies) { k_apply_gravity<<<grid_for(w.nBodies, 256), 256, 0, s>>>(w); note_launch(); }
 }

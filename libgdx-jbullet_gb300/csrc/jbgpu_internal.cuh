@@ -206,6 +206,8 @@ void launch_integrate(const DevWorld& w, float dt, cudaStream_t s);
 void launch_activation(const DevWorld& w, float dt, cudaStream_t s);
 void launch_clear_forces(const DevWorld& w, cudaStream_t s);
 void launch_save_kinematic(const DevWorld& w, float timeStep, cudaStream_t s);
+void launch_apply_impulses(const DevWorld& w, const int* bodies, const float* imp, const float* rel, const float* tq, int n,
+                           cudaStream_t s);
 
 int num_sms();
 

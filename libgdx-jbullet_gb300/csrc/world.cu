@@ -1767,6 +1767,37 @@ static int body_gravity(jbgpu_world* w, const int32_t* bodies, const float* acc,
     return JBGPU_OK;
 }
 
+int jbgpu_world_apply_impulses(jbgpu_world* w, const int32_t* bodies, const float* imp, const float* rel, const float* tq,
+                               int32_t n) {
+    if (!w || n < 0 || (n > 0 && (!bodies || (!imp && !tq)))) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad impulse arguments");
+    if (n == 0) return JBGPU_OK;
+    std::vector<char> seen(w->nBodies, 0);
+    for (int k = 0; k < n; k++) {
+        if (bodies[k] < 0 || bodies[k] >= w->nBodies) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad body index");
+        if (seen[bodies[k]]) return fail(JBGPU_ERR_INVALID_ARGUMENT, "a body listed twice in one call");
+        seen[bodies[k]] = 1;
+    }
+    CK(cudaSetDevice(w->device));
+    cudaStream_t s = w->stream;
+    int* dB = nullptr;
+    float* dF = nullptr;
+    CK(dalloc(&dB, n));
+    CK(dalloc(&dF, (size_t)9 * n));
+    CK(cudaMemcpyAsync(dB, bodies, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    float* dI = imp ? dF : nullptr;
+    float* dR = rel ? dF + 3 * n : nullptr;
+    float* dT = tq ? dF + 6 * n : nullptr;
+    if (imp) CK(cudaMemcpyAsync(dI, imp, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
+    if (rel) CK(cudaMemcpyAsync(dR, rel, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
+    if (tq) CK(cudaMemcpyAsync(dT, tq, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, s));
+    launch_apply_impulses(dev_view(w), dB, dI, dR, dT, n, s);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    dfree(dB);
+    dfree(dF);
+    return JBGPU_OK;
+}
+
 int jbgpu_world_set_gravity(jbgpu_world* w, const float gravity[3]) {
     if (!w || !gravity) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
     for (int k = 0; k < 3; k++) { w->cfg.gravity[k] = gravity[k]; w->dw.gravityAcc[k] = gravity[k]; }

@@ -326,6 +326,23 @@ class RigidBody:
     def applyCentralForce(self, f):
         self._world._pending_force(self._index, f)
 
+    # RigidBody.applyCentralImpulse / applyImpulse / applyTorqueImpulse (RigidBody.java:395-430):
+    # the velocity changes now, on the body's device state (the body must be in a world)
+    def _impulse(self, **kw):
+        if self._world is None:
+            raise RuntimeError("impulses apply to a body added to a DiscreteDynamicsWorld")
+        self._world._ensure().apply_impulses([self._index], **kw)
+        self._world._cache = None
+
+    def applyCentralImpulse(self, impulse):
+        self._impulse(impulses=[impulse])
+
+    def applyImpulse(self, impulse, rel_pos):
+        self._impulse(impulses=[impulse], rel_pos=[rel_pos])
+
+    def applyTorqueImpulse(self, torque):
+        self._impulse(torque_impulses=[torque])
+
     def getUid(self):
         return self._index + 1
 

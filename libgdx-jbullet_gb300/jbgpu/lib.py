@@ -105,6 +105,7 @@ def lib():
             "jbgpu_world_refit_mesh": ([C.c_void_p, C.c_int32, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_set_gravity": ([C.c_void_p, _abi.f32p], C.c_int),
             "jbgpu_world_remove_bodies": ([C.c_void_p, _abi.i32p, C.c_int32], C.c_int),
+            "jbgpu_world_apply_impulses": ([C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_set_body_gravity": ([C.c_void_p, _abi.i32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_mesh_bvh": ([C.c_void_p, C.c_int32, _abi.i32p, C.c_int32, _abi.i32p, _abi.f32p], C.c_int),
             "jbgpu_world_set_sample_logging": ([C.c_void_p, C.c_int32], C.c_int),
@@ -134,6 +135,7 @@ EXPORTED = [
     "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
     "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd", "jbgpu_shape_mesh_bvh", "jbgpu_world_refit_mesh",
     "jbgpu_world_mesh_bvh", "jbgpu_world_set_gravity", "jbgpu_world_set_body_gravity", "jbgpu_world_remove_bodies",
+    "jbgpu_world_apply_impulses",
 ]
 
 
@@ -485,6 +487,16 @@ class GpuWorld:
 
     def set_solver_iterations(self, num_iterations, residual=0.0, max_iterations=0):
         check(lib().jbgpu_world_set_solver_iterations(self.h, num_iterations, residual, max_iterations))
+
+    def apply_impulses(self, bodies, impulses=None, rel_pos=None, torque_impulses=None):
+        """RigidBody.applyCentralImpulse / applyImpulse (rel_pos given) / applyTorqueImpulse for
+        distinct bodies (jbgpu_world_apply_impulses)."""
+        b = np.ascontiguousarray(bodies, np.int32).reshape(-1)
+        arrs = [None if a is None else np.ascontiguousarray(np.broadcast_to(np.asarray(a, np.float32).reshape(-1, 3),
+                                                                            (len(b), 3)), np.float32)
+                for a in (impulses, rel_pos, torque_impulses)]
+        ptr = [None if a is None else a.ctypes.data_as(_abi.f32p) for a in arrs]
+        check(lib().jbgpu_world_apply_impulses(self.h, b.ctypes.data_as(_abi.i32p), ptr[0], ptr[1], ptr[2], len(b)))
 
     def remove_bodies(self, bodies):
         """DiscreteDynamicsWorld.removeRigidBody for the given bodies (jbgpu_world_remove_bodies):

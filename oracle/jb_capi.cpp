@@ -419,6 +419,27 @@ int orc_remove_bodies(void* h, const int* bodies, int n) {
     return 0;
 }
 
+// RigidBody.applyCentralImpulse / applyImpulse / applyTorqueImpulse (RigidBody.java:395-430) with
+// linear and angular factors 1, in list order; -1 for a bad index.
+int orc_apply_impulses(void* h, const int* bodies, const float* imp, const float* rel, const float* tq, int n) {
+    World* w = (World*)h;
+    for (int k = 0; k < n; k++)
+        if (bodies[k] < 0 || bodies[k] >= (int)w->bodies.size()) return -1;
+    for (int k = 0; k < n; k++) {
+        Body& b = w->bodies[bodies[k]];
+        if (imp) {
+            const V3 J = v3(imp[3 * k], imp[3 * k + 1], imp[3 * k + 2]);
+            if (!rel || b.invMass != 0.0f) b.linvel = add(b.linvel, scl(J, b.invMass));
+            if (rel && b.invMass != 0.0f) {
+                const V3 r = v3(rel[3 * k], rel[3 * k + 1], rel[3 * k + 2]);
+                b.angvel = add(b.angvel, mulMv(crs(r, J), b.invInertiaWorld));
+            }
+        }
+        if (tq) b.angvel = add(b.angvel, mulMv(v3(tq[3 * k], tq[3 * k + 1], tq[3 * k + 2]), b.invInertiaWorld));
+    }
+    return 0;
+}
+
 // DiscreteDynamicsWorld.setGravity (DiscreteDynamicsWorld.java:403-412) and RigidBody.setGravity
 // (RigidBody.java:213-217): gravity = acceleration scaled by 1 / inverseMass when that is nonzero.
 static void set_body_gravity(Body& b, V3 acc) {

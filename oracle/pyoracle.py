@@ -74,6 +74,7 @@ def lib():
         L.orc_refit_mesh.argtypes = [C.c_void_p, C.c_int, _abi.f32p, C.c_int]
         L.orc_set_gravity.argtypes = [C.c_void_p, _abi.f32p]
         L.orc_remove_bodies.argtypes = [C.c_void_p, _abi.i32p, C.c_int]
+        L.orc_apply_impulses.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, _abi.f32p, C.c_int]
         L.orc_set_body_gravity.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, C.c_int]
         L.orc_world_mesh_bvh.argtypes = [C.c_void_p, C.c_int, _abi.i32p, C.c_int, _abi.f32p]
         _lib = L
@@ -262,6 +263,16 @@ class OracleWorld:
 
     def step_simulation(self, time_step, max_sub_steps=1, fixed_time_step=1.0 / 60.0):
         return lib().orc_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step)
+
+    def apply_impulses(self, bodies, impulses=None, rel_pos=None, torque_impulses=None):
+        """RigidBody.applyCentralImpulse / applyImpulse (rel_pos given) / applyTorqueImpulse."""
+        b = np.ascontiguousarray(bodies, np.int32).reshape(-1)
+        arrs = [None if a is None else np.ascontiguousarray(np.broadcast_to(np.asarray(a, np.float32).reshape(-1, 3),
+                                                                            (len(b), 3)), np.float32)
+                for a in (impulses, rel_pos, torque_impulses)]
+        ptr = [None if a is None else _fp(a) for a in arrs]
+        if lib().orc_apply_impulses(self.h, b.ctypes.data_as(_abi.i32p), ptr[0], ptr[1], ptr[2], len(b)) != 0:
+            raise ValueError("apply_impulses: bad body index")
 
     def remove_bodies(self, bodies):
         """DiscreteDynamicsWorld.removeRigidBody for the given bodies (later bodies move down)."""
