@@ -365,6 +365,26 @@ int jbgpu_world_set_ccd(jbgpu_world* world, const int32_t* bodies, const float* 
 int jbgpu_world_apply_impulses(jbgpu_world* world, const int32_t* bodies, const float* impulses, const float* rel_pos,
                                const float* torque_impulses, int32_t n);
 
+/* Body properties after the bodies were added, for n distinct bodies, each array nullable (one
+ * value per body): RigidBody.setDamping (dynamics/RigidBody.java:224-227; both values clamped to
+ * [0, 1] by MiscUtil.GEN_clamped), CollisionObject.setFriction / setRestitution
+ * (collision/dispatch/CollisionObject.java:186-196; they enter the combined values of contact
+ * points made from then on, points already in a manifold keep theirs, as in the reference) and
+ * RigidBody.setSleepingThresholds (RigidBody.java:371-374). */
+int jbgpu_world_set_body_properties(jbgpu_world* world, const int32_t* bodies, int32_t n, const float* linear_damping,
+                                    const float* angular_damping, const float* friction, const float* restitution,
+                                    const float* linear_sleeping_threshold, const float* angular_sleeping_threshold);
+
+/* DynamicsWorld.setInternalTickCallback (dynamics/DynamicsWorld.java:141-144), called at the end of
+ * every internalSingleStepSimulation (DiscreteDynamicsWorld.java:393-395): cb(world, time_step, user)
+ * runs on the calling thread after each substep of jbgpu_world_step_simulation and jbgpu_world_step,
+ * with the world's stream synchronised.  It may read state and change it (impulses, forces, gravity,
+ * state, body properties, bodies added or removed): the next substep sees the change.  It may not
+ * step the world (jbgpu_world_step, _step_simulation and _stage return JBGPU_ERR_INVALID_ARGUMENT
+ * inside it).  NULL removes the callback. */
+typedef void (*jbgpu_tick_callback)(jbgpu_world* world, float time_step, void* user);
+int jbgpu_world_set_internal_tick_callback(jbgpu_world* world, jbgpu_tick_callback cb, void* user);
+
 /* DiscreteDynamicsWorld.setGravity (dynamics/DiscreteDynamicsWorld.java:403-412): the gravity of
  * bodies added later, and RigidBody.setGravity for every body already in the world. */
 int jbgpu_world_set_gravity(jbgpu_world* world, const float gravity[3]);
@@ -552,6 +572,10 @@ int jbgpu_world_set_6dof_linear_motor(jbgpu_world* world, int32_t id, float soft
 int jbgpu_world_set_6dof_angular_motor(jbgpu_world* world, int32_t id, int32_t axis, int32_t enable,
                                        float target_velocity, float max_motor_force, float max_limit_force,
                                        float damping, float limit_softness, float erp, float bounce);
+/* DiscreteDynamicsWorld.removeConstraint (dynamics/DiscreteDynamicsWorld.java:524-528): joint id
+ * leaves the world; the joints after it move down (id - 1), as in the reference's constraint list,
+ * and keep their settings and last applied impulses. */
+int jbgpu_world_remove_joint(jbgpu_world* world, int32_t id);
 /* TypedConstraint.getAppliedImpulse of every joint after the last solve; with out NULL only *n
  * is set; n > capacity is JBGPU_ERR_CAPACITY with *n set. */
 int jbgpu_world_get_joint_impulses(jbgpu_world* world, float* out, int32_t capacity, int32_t* n);

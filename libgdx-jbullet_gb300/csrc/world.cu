@@ -97,6 +97,9 @@ struct jbgpu_world {
     cudaEvent_t evT0 = nullptr, evT1 = nullptr;   // jbgpu_world_timer
     float localTime = 1.0f / 60.0f;
     long long steps = 0;
+    jbgpu_tick_callback tickCb = nullptr;   // DynamicsWorld.setInternalTickCallback
+    void* tickUser = nullptr;
+    bool inTick = false;
     // shapes
     std::vector<HostShape> shapes;
     std::vector<float4> hullPts;
@@ -894,6 +897,40 @@ int ensure_io(jbgpu_world* w) {
 }
 }  // namespace
 
+namespace bodyprops {
+// Per-body values written at the listed bodies (the listed bodies are distinct).
+__global__ void k_scatter(float* dst, const int* idx, const float* v, int n) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) dst[idx[k]] = v[k];
+}
+
+// n body indices, each in range and listed once.
+int check_distinct(const jbgpu_world* w, const int32_t* bodies, int n) {
+    std::vector<char> seen(w->nBodies, 0);
+    for (int k = 0; k < n; k++) {
+        if (bodies[k] < 0 || bodies[k] >= w->nBodies) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad body index");
+        if (seen[bodies[k]]) return fail(JBGPU_ERR_INVALID_ARGUMENT, "a body listed twice in one call");
+        seen[bodies[k]] = 1;
+    }
+    return JBGPU_OK;
+}
+
+// The tick callback after a substep: the substep's status is checked first (a later call from
+// the callback resets the status word), the world is brought up to date after it (the callback
+// may have added or removed bodies or joints).
+int after_substep(jbgpu_world* w, float dt) {
+    if (!w->tickCb) return JBGPU_OK;
+    int rc = check_status(w);
+    if (rc) return rc;
+    w->inTick = true;
+    w->tickCb(w, dt, w->tickUser);
+    w->inTick = false;
+    if ((rc = prepare(w))) return rc;
+    CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), w->stream));
+    return JBGPU_OK;
+}
+}  // namespace bodyprops
+
 namespace removal {
 // Body removal: dst[j] = src[from[j]] for every kept body, and the pairs whose bodies both stay,
 // moved to the other pair buffer in their order with the bodies renumbered.
@@ -1646,19 +1683,21 @@ int jbgpu_world_remove_bodies(jbgpu_world* w, const int32_t* bodies, int32_t n) 
 
 int jbgpu_world_step(jbgpu_world* w, float dt, int32_t substeps) {
     if (!w || substeps < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
+    if (w->inTick) return fail(JBGPU_ERR_INVALID_ARGUMENT, "a tick callback cannot step the world");
     int rc = prepare(w);
     if (rc) return rc;
     CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), w->stream));
     if (w->hasKinematic && (rc = run_stage(w, JBGPU_STAGE_SAVE_KINEMATIC, dt))) return rc;
     if ((rc = run_stage(w, JBGPU_STAGE_APPLY_GRAVITY, dt))) return rc;
     for (int i = 0; i < substeps; i++)
-        if ((rc = single_step(w, dt))) return rc;
+        if ((rc = single_step(w, dt)) || (rc = bodyprops::after_substep(w, dt))) return rc;
     if ((rc = run_stage(w, JBGPU_STAGE_CLEAR_FORCES, dt))) return rc;
     return check_status(w);
 }
 
 int jbgpu_world_step_simulation(jbgpu_world* w, float timeStep, int32_t maxSubSteps, float fixedTimeStep, int32_t* numOut) {
     if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (w->inTick) return fail(JBGPU_ERR_INVALID_ARGUMENT, "a tick callback cannot step the world");
     int num = 0;
     if (maxSubSteps != 0) {
         w->localTime += timeStep;
@@ -1681,7 +1720,7 @@ int jbgpu_world_step_simulation(jbgpu_world* w, float timeStep, int32_t maxSubSt
         if ((rc = run_stage(w, JBGPU_STAGE_APPLY_GRAVITY, fixedTimeStep))) return rc;
         int clamped = num > maxSubSteps ? maxSubSteps : num;
         for (int i = 0; i < clamped; i++)
-            if ((rc = single_step(w, fixedTimeStep))) return rc;
+            if ((rc = single_step(w, fixedTimeStep)) || (rc = bodyprops::after_substep(w, fixedTimeStep))) return rc;
     }
     if ((rc = run_stage(w, JBGPU_STAGE_CLEAR_FORCES, fixedTimeStep))) return rc;
     return check_status(w);
@@ -1689,6 +1728,7 @@ int jbgpu_world_step_simulation(jbgpu_world* w, float timeStep, int32_t maxSubSt
 
 int jbgpu_world_stage(jbgpu_world* w, int32_t stage, float dt) {
     if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (w->inTick) return fail(JBGPU_ERR_INVALID_ARGUMENT, "a tick callback cannot step the world");
     int rc = prepare(w);
     if (rc) return rc;
     CK(cudaMemsetAsync(w->dw.ctr + C_STATUS, 0, sizeof(int), w->stream));
@@ -1771,12 +1811,7 @@ int jbgpu_world_apply_impulses(jbgpu_world* w, const int32_t* bodies, const floa
                                int32_t n) {
     if (!w || n < 0 || (n > 0 && (!bodies || (!imp && !tq)))) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad impulse arguments");
     if (n == 0) return JBGPU_OK;
-    std::vector<char> seen(w->nBodies, 0);
-    for (int k = 0; k < n; k++) {
-        if (bodies[k] < 0 || bodies[k] >= w->nBodies) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad body index");
-        if (seen[bodies[k]]) return fail(JBGPU_ERR_INVALID_ARGUMENT, "a body listed twice in one call");
-        seen[bodies[k]] = 1;
-    }
+    if (int rc = bodyprops::check_distinct(w, bodies, n)) return rc;
     CK(cudaSetDevice(w->device));
     cudaStream_t s = w->stream;
     int* dB = nullptr;
@@ -1795,6 +1830,56 @@ int jbgpu_world_apply_impulses(jbgpu_world* w, const int32_t* bodies, const floa
     CK(cudaStreamSynchronize(s));
     dfree(dB);
     dfree(dF);
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_body_properties(jbgpu_world* w, const int32_t* bodies, int32_t n, const float* linear_damping,
+                                    const float* angular_damping, const float* friction, const float* restitution,
+                                    const float* linear_sleeping_threshold, const float* angular_sleeping_threshold) {
+    if (!w || n < 0 || (n > 0 && !bodies)) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad body property arguments");
+    if (n == 0) return JBGPU_OK;
+    if (int rc = bodyprops::check_distinct(w, bodies, n)) return rc;
+    const float* src[6] = {linear_damping, angular_damping, friction, restitution, linear_sleeping_threshold,
+                           angular_sleeping_threshold};
+    float* dst[6] = {w->dw.linDamp, w->dw.angDamp, w->dw.friction, w->dw.restitution, w->dw.linSleep, w->dw.angSleep};
+    std::vector<float> host((size_t)6 * n);
+    int m = 0;
+    for (int q = 0; q < 6; q++) {
+        if (!src[q]) continue;
+        for (int k = 0; k < n; k++) {
+            float x = src[q][k];
+            if (q < 2) x = x < 0.0f ? 0.0f : (1.0f < x ? 1.0f : x);   // RigidBody.setDamping: MiscUtil.GEN_clamped to [0, 1]
+            host[(size_t)m * n + k] = x;
+        }
+        m++;
+    }
+    if (m == 0) return JBGPU_OK;
+    CK(cudaSetDevice(w->device));
+    cudaStream_t s = w->stream;
+    int* dB = nullptr;
+    float* dV = nullptr;
+    CK(dalloc(&dB, n));
+    CK(dalloc(&dV, (size_t)m * n));
+    CK(cudaMemcpyAsync(dB, bodies, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dV, host.data(), sizeof(float) * m * n, cudaMemcpyHostToDevice, s));
+    for (int q = 0, j = 0; q < 6; q++) {
+        if (!src[q]) continue;
+        bodyprops::k_scatter<<<(n + 127) / 128, 128, 0, s>>>(dst[q], dB, dV + (size_t)j * n, n);
+        note_launch();
+        j++;
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    dfree(dB);
+    dfree(dV);
+    return JBGPU_OK;
+}
+
+int jbgpu_world_set_internal_tick_callback(jbgpu_world* w, jbgpu_tick_callback cb, void* user) {
+    if (!w) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (w->inTick) return fail(JBGPU_ERR_INVALID_ARGUMENT, "the tick callback cannot be replaced from inside it");
+    w->tickCb = cb;
+    w->tickUser = cb ? user : nullptr;
     return JBGPU_OK;
 }
 
@@ -2111,6 +2196,28 @@ int jbgpu_world_set_hinge_angular_only(jbgpu_world* w, int32_t id, int32_t on) {
     int rc = hinge_id(w, id);
     if (rc) return rc;
     w->jKind[id] = on ? (w->jKind[id] | JK_ANGULAR_ONLY) : (w->jKind[id] & ~JK_ANGULAR_ONLY);
+    w->jointsDirty = true;
+    return JBGPU_OK;
+}
+
+int jbgpu_world_remove_joint(jbgpu_world* w, int32_t id) {
+    if (!w || id < 0 || id >= (int)w->jA.size()) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad joint id");
+    auto drop = [id](auto& v, size_t per) { v.erase(v.begin() + (size_t)id * per, v.begin() + (size_t)(id + 1) * per); };
+    drop(w->jKind, 1); drop(w->jA, 1); drop(w->jB, 1); drop(w->jPivA, 1); drop(w->jPivB, 1);
+    drop(w->jSet, 1); drop(w->jSet2, 1); drop(w->jFrame, 6); drop(w->jD6, D6_SET_F4);
+    DevJoints& J = w->sb.J;
+    if (id < J.n) {   // the solved joints' applied impulses move down with them
+        CK(cudaSetDevice(w->device));
+        std::vector<float> imp(J.n);
+        CK(cudaMemcpyAsync(imp.data(), J.imp, sizeof(float) * J.n, cudaMemcpyDeviceToHost, w->stream));
+        CK(cudaStreamSynchronize(w->stream));
+        imp.erase(imp.begin() + id);
+        J.n -= 1;
+        if (J.n > 0) {
+            CK(cudaMemcpyAsync(J.imp, imp.data(), sizeof(float) * J.n, cudaMemcpyHostToDevice, w->stream));
+            CK(cudaStreamSynchronize(w->stream));
+        }
+    }
     w->jointsDirty = true;
     return JBGPU_OK;
 }

@@ -53,6 +53,46 @@ CF_STATIC_OBJECT = 1
 CF_KINEMATIC_OBJECT = 2
 CF_NO_CONTACT_RESPONSE = 4
 
+# per-body properties settable after the bodies were added, in the C call's argument order
+BODY_PROPERTIES = ("linear_damping", "angular_damping", "friction", "restitution", "linear_sleeping_threshold",
+                   "angular_sleeping_threshold")
+# DynamicsWorld.setInternalTickCallback: (world handle, time step, user pointer)
+TICK_CALLBACK = C.CFUNCTYPE(None, C.c_void_p, C.c_float, C.c_void_p)
+
+
+def body_property_arrays(bodies, props):
+    """The bodies as int32 and one float32 array per named property (None where not given)."""
+    b = np.ascontiguousarray(bodies, np.int32).reshape(-1)
+    bad = set(props) - set(BODY_PROPERTIES)
+    if bad:
+        raise TypeError(f"unknown body properties {sorted(bad)}")
+    arrs = [None if props.get(k) is None else
+            np.ascontiguousarray(np.broadcast_to(np.asarray(props[k], np.float32).reshape(-1), (len(b),)), np.float32)
+            for k in BODY_PROPERTIES]
+    return b, arrs
+
+
+class TickTrampoline:
+    """A Python tick callback behind the C function pointer: cb(world, time_step).  An exception in
+    it is kept and raised by `reraise` after the stepping call returns (ctypes would swallow it)."""
+
+    def __init__(self, world, cb):
+        self.error = None
+
+        def tramp(_h, dt, _user):
+            if self.error is not None:
+                return
+            try:
+                cb(world, dt)
+            except BaseException as e:   # noqa: BLE001 - kept and raised after the step
+                self.error = e
+        self.fn = TICK_CALLBACK(tramp)
+
+    def reraise(self):
+        if self.error is not None:
+            e, self.error = self.error, None
+            raise e
+
 POINT_FLOATS = 32
 MANIFOLD_POINTS = 4
 

@@ -37,6 +37,50 @@ class Transform:
         return cls(np.asarray(t[:9]).reshape(3, 3), t[9:12])
 
 
+F32 = np.float32
+
+
+def _crs(a, b):
+    """Vector3.crs in binary32: a x b."""
+    a = np.asarray(a, F32).reshape(3)
+    b = np.asarray(b, F32).reshape(3)
+    return np.array([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]], F32)
+
+
+def _clamp01(x):
+    """MiscUtil.GEN_clamped(x, 0, 1) in binary32."""
+    x = F32(x)
+    return F32(0.0) if x < F32(0.0) else (F32(1.0) if F32(1.0) < x else x)
+
+
+def _quat_from_basis(m):
+    """RigidBody.getOrientation: MatrixUtil.getRotation, i.e. libGDX Quaternion.setFromMatrix(true, basis)
+    (rows normalised, then the trace or largest-diagonal branch, the "1 + ..." sums in double);
+    returns (x, y, z, w) as binary32."""
+    m = np.asarray(m, F32).reshape(3, 3)
+    r = [m[i] * (F32(1.0) / F32(np.sqrt(float(m[i, 0] * m[i, 0] + m[i, 1] * m[i, 1] + m[i, 2] * m[i, 2]))))
+         for i in range(3)]
+    (xx, xy, xz), (yx, yy, yz), (zx, zy, zz) = r
+    t = xx + yy + zz
+    half = F32(0.5)
+    if t >= 0:
+        sq = F32(np.sqrt(float(t + F32(1.0))))
+        w = half * sq
+        k = half / sq
+        return np.array([(zy - yz) * k, (xz - zx) * k, (yx - xy) * k, w], F32)
+    if xx > yy and xx > zz:
+        sq = F32(np.sqrt(1.0 + float(xx) - float(yy) - float(zz)))
+        k = half / sq
+        return np.array([sq * half, (yx + xy) * k, (xz + zx) * k, (zy - yz) * k], F32)
+    if yy > zz:
+        sq = F32(np.sqrt(1.0 + float(yy) - float(xx) - float(zz)))
+        k = half / sq
+        return np.array([(yx + xy) * k, sq * half, (zy + yz) * k, (xz - zx) * k], F32)
+    sq = F32(np.sqrt(1.0 + float(zz) - float(xx) - float(yy)))
+    k = half / sq
+    return np.array([(xz + zx) * k, (zy + yz) * k, sq * half, (yx - xy) * k], F32)
+
+
 class _Shape:
     shape_type = None
 
@@ -324,7 +368,162 @@ class RigidBody:
         return 0.0 if self.info.mass == 0.0 else 1.0 / np.float32(self.info.mass)
 
     def applyCentralForce(self, f):
-        self._world._pending_force(self._index, f)
+        self._world._pending_force(self._index, force=f)
+
+    # RigidBody.applyTorque / applyForce / clearForces (RigidBody.java:355-394): the accumulators
+    # totalForce / totalTorque that stepSimulation's substeps integrate and then clear
+    def applyTorque(self, torque):
+        self._world._pending_force(self._index, torque=torque)
+
+    def applyForce(self, force, rel_pos):
+        self.applyCentralForce(force)
+        self.applyTorque(_crs(rel_pos, force))
+
+    def clearForces(self):
+        w = self._world
+        if w is None:
+            return
+        w._flush_forces()
+        if w._g is not None:
+            st = w._state()
+            st["total_force"][self._index] = 0.0
+            st["total_torque"][self._index] = 0.0
+            w._g.set_state({"total_force": st["total_force"], "total_torque": st["total_torque"]})
+            w._cache = None
+
+    def getTotalForce(self):
+        self._world._flush_forces()
+        return self._state("total_force")
+
+    def getTotalTorque(self):
+        self._world._flush_forces()
+        return self._state("total_torque")
+
+    # per-body properties (RigidBody.java:224-227, 371-374; CollisionObject.java:186-196): kept
+    # in the construction info until the body is on the device, written there after
+    def _live(self):
+        return self._world is not None and self._world._g is not None and self._index < self._world._uploaded
+
+    def _set_props(self, **kw):
+        if self._live():
+            self._world._g.set_body_properties([self._index], **kw)
+
+    def setDamping(self, lin_damping, ang_damping):
+        self.info.linearDamping = float(_clamp01(lin_damping))
+        self.info.angularDamping = float(_clamp01(ang_damping))
+        self._set_props(linear_damping=lin_damping, angular_damping=ang_damping)
+
+    def getLinearDamping(self):
+        return float(_clamp01(self.info.linearDamping))
+
+    def getAngularDamping(self):
+        return float(_clamp01(self.info.angularDamping))
+
+    def setFriction(self, friction):
+        self.info.friction = float(friction)
+        self._set_props(friction=friction)
+
+    def getFriction(self):
+        return self.info.friction
+
+    def setRestitution(self, restitution):
+        self.info.restitution = float(restitution)
+        self._set_props(restitution=restitution)
+
+    def getRestitution(self):
+        return self.info.restitution
+
+    def setSleepingThresholds(self, linear, angular):
+        self.info.linearSleepingThreshold = float(linear)
+        self.info.angularSleepingThreshold = float(angular)
+        self._set_props(linear_sleeping_threshold=linear, angular_sleeping_threshold=angular)
+
+    def getLinearSleepingThreshold(self):
+        return self.info.linearSleepingThreshold
+
+    def getAngularSleepingThreshold(self):
+        return self.info.angularSleepingThreshold
+
+    def getLinearFactor(self):
+        return np.ones(3, F32)
+
+    def getAngularFactor(self):
+        return np.ones(3, F32)
+
+    # CollisionObject / RigidBody getters over the body's device state
+    def getCollisionShape(self):
+        return self.info.collisionShape
+
+    def getMotionState(self):
+        return self.info.motionState
+
+    def setMotionState(self, motionState):
+        self.info.motionState = motionState
+
+    def isInWorld(self):
+        return self._world is not None
+
+    _user = None
+
+    def getUserPointer(self):
+        return self._user
+
+    def setUserPointer(self, obj):
+        self._user = obj
+
+    def isStaticObject(self):
+        return (self.getCollisionFlags() & _abi.CF_STATIC_OBJECT) != 0
+
+    def isStaticOrKinematicObject(self):
+        return (self.getCollisionFlags() & (_abi.CF_STATIC_OBJECT | _abi.CF_KINEMATIC_OBJECT)) != 0
+
+    def hasContactResponse(self):
+        return (self.getCollisionFlags() & _abi.CF_NO_CONTACT_RESPONSE) == 0
+
+    def mergesSimulationIslands(self):
+        return (self.getCollisionFlags() & (_abi.CF_STATIC_OBJECT | _abi.CF_KINEMATIC_OBJECT |
+                                            _abi.CF_NO_CONTACT_RESPONSE)) == 0
+
+    def getCenterOfMassPosition(self):
+        return self._state("transform")[9:12].copy()
+
+    def getOrientation(self):
+        return _quat_from_basis(self._state("transform")[:9])
+
+    def getVelocityInLocalPoint(self, rel_pos):
+        """RigidBody.getVelocityInLocalPoint: linearVelocity + angularVelocity x rel_pos."""
+        return (self.getLinearVelocity() + _crs(self.getAngularVelocity(), rel_pos)).astype(F32)
+
+    def getInvInertiaTensorWorld(self):
+        return self._state("inv_inertia_world").reshape(3, 3).copy()
+
+    def getInvInertiaDiagLocal(self):
+        """RigidBody.setMassProps: 1 / localInertia per axis, 0 where it is 0."""
+        li = np.asarray(self.info.localInertia, F32)
+        return np.array([F32(0.0) if x == 0.0 else F32(1.0) / x for x in li], F32)
+
+    def getAabb(self):
+        a = self._state("aabb")
+        return a[:3].copy(), a[3:].copy()
+
+    def getIslandTag(self):
+        return int(self._state("island_tag"))
+
+    def getDeactivationTime(self):
+        return float(self._state("deactivation_time"))
+
+    def setDeactivationTime(self, t):
+        if self._world is None or self._world._g is None:
+            raise RuntimeError("setDeactivationTime applies to a body in a world that has stepped")
+        self._world._set_field("deactivation_time", self._index, float(t))
+
+    def activate(self, forceActivation=False):
+        """CollisionObject.activate: ACTIVE_TAG and deactivationTime 0 unless the body is static or
+        kinematic (and forceActivation is false)."""
+        if forceActivation or not self.isStaticOrKinematicObject():
+            self.setActivationState(ACTIVE_TAG)
+            if self._world is not None and self._world._g is not None:
+                self._world._set_field("deactivation_time", self._index, 0.0)
 
     # RigidBody.applyCentralImpulse / applyImpulse / applyTorqueImpulse (RigidBody.java:395-430):
     # the velocity changes now, on the body's device state (the body must be in a world)
@@ -781,10 +980,12 @@ class DiscreteDynamicsWorld:
         self._bodies = []
         self._shapes = []
         self._g = None
-        self._forces = None
+        self._forces = self._torques = None
         self._uploaded = 0
         self._constraints = []
         self._sent = 0
+        self._tick_cb = None
+        self._world_user_info = None
 
     # -- configuration (before the first step) --
     def setGravity(self, g):
@@ -827,8 +1028,9 @@ class DiscreteDynamicsWorld:
         del self._bodies[i]
         for b in self._bodies[i:]:
             b._index -= 1
-        if self._forces is not None:
+        if self._forces is not None and i < len(self._forces):
             self._forces = np.delete(self._forces, i, 0)
+            self._torques = np.delete(self._torques, i, 0)
         self._cache = None
         body._world = None
         body._index = None
@@ -850,6 +1052,64 @@ class DiscreteDynamicsWorld:
     def getConstraint(self, i):
         return self._constraints[i]
 
+    def removeConstraint(self, constraint):
+        """DiscreteDynamicsWorld.removeConstraint (java:524-528): the constraints after it move down."""
+        if constraint not in self._constraints:
+            return
+        k = self._constraints.index(constraint)
+        if constraint._id is not None:
+            self._g.remove_joint(constraint._id)
+            for c in self._constraints[k + 1:]:
+                if c._id is not None:
+                    c._id -= 1
+            self._sent -= 1
+        del self._constraints[k]
+        constraint._id = None
+        constraint._world = None
+
+    def getCollisionObjectArray(self):
+        return list(self._bodies)
+
+    # DiscreteDynamicsWorld.clearForces / applyGravity (java:226-250): on the device accumulators
+    def clearForces(self):
+        self._forces = self._torques = None
+        self._ensure().stage(_abi.STAGE_CLEAR_FORCES)
+        self._cache = None
+
+    def applyGravity(self):
+        self._flush_forces()
+        self._ensure().stage(_abi.STAGE_APPLY_GRAVITY)
+        self._cache = None
+
+    # DynamicsWorld.setInternalTickCallback (DynamicsWorld.java:141-144): cb.internalTick(world,
+    # timeStep) (or cb(world, timeStep)) after every substep; forces it applies act from the next
+    # substep on, as the reference's accumulators do
+    def setInternalTickCallback(self, cb, worldUserInfo=None):
+        self._tick_cb = cb
+        self._world_user_info = worldUserInfo
+        if self._g is not None:
+            self._install_tick()
+
+    def getWorldUserInfo(self):
+        return self._world_user_info
+
+    def setWorldUserInfo(self, info):
+        self._world_user_info = info
+
+    def _install_tick(self):
+        cb = self._tick_cb
+        if cb is None:
+            self._g.set_internal_tick_callback(None)
+            return
+        fn = cb.internalTick if hasattr(cb, "internalTick") else cb
+
+        def tick(_g, dt):
+            self._cache = None
+            fn(self, dt)
+            self._flush_forces()
+            self._cache = None
+        self._g.set_internal_tick_callback(tick)
+
     # -- stepping --
     def _ensure(self):
         if self._g is None:
@@ -862,6 +1122,8 @@ class DiscreteDynamicsWorld:
             cfg.solver_mode = s.solverMode
             cfg.device = self._device
             self._g = GpuWorld(config=cfg)
+            if self._tick_cb is not None:
+                self._install_tick()
         if self._uploaded != len(self._bodies):
             self._upload()
         for c in self._constraints[self._sent:]:
@@ -936,7 +1198,6 @@ class DiscreteDynamicsWorld:
         from . import lib
         lib.check(lib.lib().jbgpu_world_add_bodies(g.h, ptr, len(b), None))
         self._uploaded = len(self._bodies)
-        self._forces = None
         grav = [b for b in new if b._gravity_acc is not None]
         if grav:   # addRigidBody set the world's gravity; a later setGravity of the body overrides it
             g.set_body_gravity([b._index for b in grav], [b._gravity_acc for b in grav])
@@ -946,19 +1207,41 @@ class DiscreteDynamicsWorld:
         if ccd:
             g.set_ccd([b._index for b in ccd], [b._ccd[0] for b in ccd], [b._ccd[1] for b in ccd])
 
-    def _pending_force(self, index, f):
+    def _pending_force(self, index, force=None, torque=None):
+        """Forces and torques applied since the last flush, summed per body in call order."""
+        n = len(self._bodies)
         if self._forces is None:
-            self._forces = np.zeros((len(self._bodies), 3), np.float32)
-        self._forces[index] += np.asarray(f, np.float32)
+            self._forces = np.zeros((n, 3), F32)
+            self._torques = np.zeros((n, 3), F32)
+        elif len(self._forces) < n:
+            pad = np.zeros((n - len(self._forces), 3), F32)
+            self._forces = np.concatenate([self._forces, pad])
+            self._torques = np.concatenate([self._torques, pad])
+        if force is not None:
+            self._forces[index] += np.asarray(force, F32)
+        if torque is not None:
+            self._torques[index] += np.asarray(torque, F32)
+
+    def _flush_forces(self):
+        """The pending forces and torques added to the device accumulators."""
+        if self._forces is None:
+            return
+        g = self._ensure()
+        n = len(self._bodies)
+        f, t = self._forces, self._torques
+        if len(f) < n:
+            pad = np.zeros((n - len(f), 3), F32)
+            f, t = np.concatenate([f, pad]), np.concatenate([t, pad])
+        self._forces = self._torques = None
+        g.apply_forces(f, t if np.any(t) else None)
+        self._cache = None
 
     def stepSimulation(self, timeStep, maxSubSteps=1, fixedTimeStep=1.0 / 60.0):
         g = self._ensure()
         for c in self._constraints:
             if isinstance(c, (Generic6DofConstraint, SliderConstraint)):
                 c._push()
-        if self._forces is not None:
-            g.apply_forces(self._forces)
-            self._forces = None
+        self._flush_forces()
         # saveKinematicState reads a kinematic body's motion state (RigidBody.java:190-205): its
         # pose is written to the world first, for the bodies that are not ISLAND_SLEEPING
         kin = [b for b in self._bodies if b.isKinematicObject() and b.info.motionState is not None and

@@ -106,6 +106,9 @@ def lib():
             "jbgpu_world_set_gravity": ([C.c_void_p, _abi.f32p], C.c_int),
             "jbgpu_world_remove_bodies": ([C.c_void_p, _abi.i32p, C.c_int32], C.c_int),
             "jbgpu_world_apply_impulses": ([C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, _abi.f32p, C.c_int32], C.c_int),
+            "jbgpu_world_set_body_properties": ([C.c_void_p, _abi.i32p, C.c_int32] + [_abi.f32p] * 6, C.c_int),
+            "jbgpu_world_remove_joint": ([C.c_void_p, C.c_int32], C.c_int),
+            "jbgpu_world_set_internal_tick_callback": ([C.c_void_p, _abi.TICK_CALLBACK, C.c_void_p], C.c_int),
             "jbgpu_world_set_body_gravity": ([C.c_void_p, _abi.i32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_mesh_bvh": ([C.c_void_p, C.c_int32, _abi.i32p, C.c_int32, _abi.i32p, _abi.f32p], C.c_int),
             "jbgpu_world_set_sample_logging": ([C.c_void_p, C.c_int32], C.c_int),
@@ -135,7 +138,8 @@ EXPORTED = [
     "jbgpu_world_add_slider", "jbgpu_world_set_slider_params", "jbgpu_world_get_slider_params",
     "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd", "jbgpu_shape_mesh_bvh", "jbgpu_world_refit_mesh",
     "jbgpu_world_mesh_bvh", "jbgpu_world_set_gravity", "jbgpu_world_set_body_gravity", "jbgpu_world_remove_bodies",
-    "jbgpu_world_apply_impulses",
+    "jbgpu_world_apply_impulses", "jbgpu_world_set_body_properties", "jbgpu_world_set_internal_tick_callback",
+    "jbgpu_world_remove_joint",
 ]
 
 
@@ -216,6 +220,8 @@ def check(rc):
 
 
 class GpuWorld:
+    _tick = None
+
     def __init__(self, scene=None, config=None):
         cfg = config if config is not None else _abi.default_config(**(scene.config if scene else {}))
         self._cfg = cfg
@@ -257,6 +263,10 @@ class GpuWorld:
 
     def set_joint_setting(self, jid, tau=0.3, damping=1.0, impulse_clamp=0.0):
         check(lib().jbgpu_world_set_joint_setting(self.h, jid, tau, damping, impulse_clamp))
+
+    def remove_joint(self, jid):
+        """DiscreteDynamicsWorld.removeConstraint: the joints after it move down one id."""
+        check(lib().jbgpu_world_remove_joint(self.h, jid))
 
     def joint_impulses(self):
         n = C.c_int32()
@@ -437,12 +447,32 @@ class GpuWorld:
         return n.value
 
     def step(self, dt, substeps=1):
-        check(lib().jbgpu_world_step(self.h, dt, substeps))
+        rc = lib().jbgpu_world_step(self.h, dt, substeps)
+        if self._tick:
+            self._tick.reraise()
+        check(rc)
 
     def step_simulation(self, time_step, max_sub_steps=1, fixed_time_step=1.0 / 60.0):
         n = C.c_int32()
-        check(lib().jbgpu_world_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step, C.byref(n)))
+        rc = lib().jbgpu_world_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step, C.byref(n))
+        if self._tick:
+            self._tick.reraise()
+        check(rc)
         return n.value
+
+    def set_internal_tick_callback(self, cb):
+        """DynamicsWorld.setInternalTickCallback: cb(world, time_step) after every substep; None removes it."""
+        t = None if cb is None else _abi.TickTrampoline(self, cb)
+        check(lib().jbgpu_world_set_internal_tick_callback(self.h, _abi.TICK_CALLBACK() if t is None else t.fn, None))
+        self._tick = t
+
+    def set_body_properties(self, bodies, **props):
+        """RigidBody.setDamping / setSleepingThresholds, CollisionObject.setFriction / setRestitution
+        after the bodies were added (jbgpu_world_set_body_properties); keywords are
+        _abi.BODY_PROPERTIES, each a scalar or one value per body."""
+        b, arrs = _abi.body_property_arrays(bodies, props)
+        ptr = [None if a is None else a.ctypes.data_as(_abi.f32p) for a in arrs]
+        check(lib().jbgpu_world_set_body_properties(self.h, b.ctypes.data_as(_abi.i32p), len(b), *ptr))
 
     def stage(self, stage, dt=1.0 / 60.0):
         check(lib().jbgpu_world_stage(self.h, stage, dt))

@@ -440,6 +440,46 @@ int orc_apply_impulses(void* h, const int* bodies, const float* imp, const float
     return 0;
 }
 
+// RigidBody.setDamping (RigidBody.java:224-227, clamped to [0, 1]), CollisionObject.setFriction /
+// setRestitution (CollisionObject.java:186-196), RigidBody.setSleepingThresholds (RigidBody.java:371-374)
+// for distinct bodies; null arrays leave their property unchanged.
+int orc_set_body_properties(void* h, const int* bodies, int n, const float* ld, const float* ad, const float* fr,
+                            const float* re, const float* ls, const float* as) {
+    World* w = (World*)h;
+    std::vector<char> seen(w->bodies.size(), 0);
+    for (int k = 0; k < n; k++) {
+        if (bodies[k] < 0 || bodies[k] >= (int)w->bodies.size() || seen[bodies[k]]) return -1;
+        seen[bodies[k]] = 1;
+    }
+    auto clamp01 = [](float x) { return x < 0.0f ? 0.0f : (1.0f < x ? 1.0f : x); };
+    for (int k = 0; k < n; k++) {
+        Body& b = w->bodies[bodies[k]];
+        if (ld) b.linearDamping = clamp01(ld[k]);
+        if (ad) b.angularDamping = clamp01(ad[k]);
+        if (fr) b.friction = fr[k];
+        if (re) b.restitution = re[k];
+        if (ls) b.linSleep = ls[k];
+        if (as) b.angSleep = as[k];
+    }
+    return 0;
+}
+
+// DiscreteDynamicsWorld.removeConstraint (DiscreteDynamicsWorld.java:524-528): the joints after it move down.
+int orc_remove_joint(void* h, int id) {
+    World* w = (World*)h;
+    if (id < 0 || id >= (int)w->joints.size()) return -1;
+    w->joints.erase(w->joints.begin() + id);
+    return 0;
+}
+
+// DynamicsWorld.setInternalTickCallback (DynamicsWorld.java:141-144): cb(world handle, timeStep, user)
+// after every internal single step.
+void orc_set_tick_callback(void* h, void (*cb)(void*, float, void*), void* user) {
+    World* w = (World*)h;
+    w->tickCb = cb;
+    w->tickUser = user;
+}
+
 // DiscreteDynamicsWorld.setGravity (DiscreteDynamicsWorld.java:403-412) and RigidBody.setGravity
 // (RigidBody.java:213-217): gravity = acceleration scaled by 1 / inverseMass when that is nonzero.
 static void set_body_gravity(Body& b, V3 acc) {

@@ -1476,6 +1476,7 @@ void internal_single_step(World& w, float dt) {
     stage_integrate(w, dt);
     stage_activation(w, dt);
     w.counters.steps++;
+    if (w.tickCb) w.tickCb(&w, dt, w.tickUser);   // java:393-395
 }
 
 // stepSimulation (dynamics/DiscreteDynamicsWorld.java:290-354)

@@ -241,6 +241,8 @@ struct World {
     std::vector<uint8_t> pairHasAlgo;
     std::vector<Manifold> pairMf;
     float localTime = 1.0f / 60.0f;       // DiscreteDynamicsWorld.localTime
+    void (*tickCb)(void* world, float timeStep, void* user) = nullptr;   // DynamicsWorld.internalTickCallback
+    void* tickUser = nullptr;
     int orderMode = ORDER_COLOUR;
     std::vector<int> explicitOrder;
     std::vector<int> solveList;           // pair indices of islandmanifold (after ISLANDS stage)

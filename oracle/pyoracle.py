@@ -75,6 +75,10 @@ def lib():
         L.orc_set_gravity.argtypes = [C.c_void_p, _abi.f32p]
         L.orc_remove_bodies.argtypes = [C.c_void_p, _abi.i32p, C.c_int]
         L.orc_apply_impulses.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, _abi.f32p, C.c_int]
+        L.orc_set_body_properties.argtypes = [C.c_void_p, _abi.i32p, C.c_int] + [_abi.f32p] * 6
+        L.orc_set_tick_callback.argtypes = [C.c_void_p, _abi.TICK_CALLBACK, C.c_void_p]
+        L.orc_set_tick_callback.restype = None
+        L.orc_remove_joint.argtypes = [C.c_void_p, C.c_int]
         L.orc_set_body_gravity.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, C.c_int]
         L.orc_world_mesh_bvh.argtypes = [C.c_void_p, C.c_int, _abi.i32p, C.c_int, _abi.f32p]
         _lib = L
@@ -86,6 +90,8 @@ def _fp(a):
 
 
 class OracleWorld:
+    _tick = None
+
     def __init__(self, scene=None, config=None, order_mode=ORDER_COLOUR):
         cfg = config if config is not None else _abi.default_config(**(scene.config if scene else {}))
         self._cfg = cfg
@@ -118,6 +124,11 @@ class OracleWorld:
 
     def set_joint_setting(self, jid, tau=0.3, damping=1.0, impulse_clamp=0.0):
         lib().orc_set_joint_setting(self.h, jid, tau, damping, impulse_clamp)
+
+    def remove_joint(self, jid):
+        """DiscreteDynamicsWorld.removeConstraint: the joints after it move down one id."""
+        if lib().orc_remove_joint(self.h, jid) != 0:
+            raise ValueError("remove_joint: bad joint id")
 
     def joint_impulses(self):
         n = lib().orc_get_joint_impulses(self.h, None, 0)
@@ -260,9 +271,26 @@ class OracleWorld:
 
     def step(self, dt, substeps=1):
         lib().orc_step(self.h, dt, substeps)
+        if self._tick:
+            self._tick.reraise()
 
     def step_simulation(self, time_step, max_sub_steps=1, fixed_time_step=1.0 / 60.0):
-        return lib().orc_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step)
+        n = lib().orc_step_simulation(self.h, time_step, max_sub_steps, fixed_time_step)
+        if self._tick:
+            self._tick.reraise()
+        return n
+
+    def set_internal_tick_callback(self, cb):
+        """DynamicsWorld.setInternalTickCallback: cb(world, time_step) after every internal single step."""
+        self._tick = None if cb is None else _abi.TickTrampoline(self, cb)
+        lib().orc_set_tick_callback(self.h, _abi.TICK_CALLBACK() if self._tick is None else self._tick.fn, None)
+
+    def set_body_properties(self, bodies, **props):
+        """RigidBody.setDamping / setSleepingThresholds, CollisionObject.setFriction / setRestitution."""
+        b, arrs = _abi.body_property_arrays(bodies, props)
+        ptr = [None if a is None else _fp(a) for a in arrs]
+        if lib().orc_set_body_properties(self.h, b.ctypes.data_as(_abi.i32p), len(b), *ptr) != 0:
+            raise ValueError("set_body_properties: bad or repeated body index")
 
     def apply_impulses(self, bodies, impulses=None, rel_pos=None, torque_impulses=None):
         """RigidBody.applyCentralImpulse / applyImpulse (rel_pos given) / applyTorqueImpulse."""
