@@ -1314,6 +1314,28 @@ class DiscreteDynamicsWorld:
     def getDispatcher(self):
         return _Dispatcher(self)
 
+    # CollisionWorld.updateAabbs / performDiscreteCollisionDetection (collision/dispatch/
+    # CollisionWorld.java:101-155): the collision half of a step without the dynamics, e.g. to
+    # read contacts after moving bodies by hand
+    def updateAabbs(self):
+        self._ensure().stage(_abi.STAGE_AABB)
+        self._cache = None
+
+    def performDiscreteCollisionDetection(self):
+        g = self._ensure()
+        for st in (_abi.STAGE_AABB, _abi.STAGE_PAIRS, _abi.STAGE_NARROWPHASE):
+            g.stage(st)
+        self._cache = None
+
+    def getWorldType(self):
+        return "DISCRETE_DYNAMICS_WORLD"   # DynamicsWorldType
+
+    def getConstraintSolver(self):
+        return self._solver
+
+    def setNumTasks(self, n):
+        """DiscreteDynamicsWorld.setNumTasks is a no-op in the reference too (java:1084-1085)."""
+
     def getPairCache(self):
         return self._ensure().get_pairs()
 

@@ -266,3 +266,49 @@ def test_mirror_getters_without_a_device():
     assert np.array_equal(D._crs((1, 0, 0), (0, 1, 0)), np.array([0, 0, 1], F))
     static = D.RigidBody(D.RigidBodyConstructionInfo(0.0, None, D.StaticPlaneShape((0.0, 1.0, 0.0), 0.0)))
     assert static.isStaticObject() and static.isStaticOrKinematicObject() and not static.mergesSimulationIslands()
+
+
+@pytest.mark.gpu
+def test_mirror_collision_detection_without_a_step(gpu_lib, oracle_lib):
+    """performDiscreteCollisionDetection after a body was moved by hand: the pairs and manifolds
+    equal the oracle's aabb, pair and narrowphase stages on the same state, and no body moved."""
+    from jbgpu import dynamics as D
+    world = D.DiscreteDynamicsWorld()
+    world.setGravity((0.0, -9.81, 0.0))
+    world.addRigidBody(D.RigidBody(D.RigidBodyConstructionInfo(0.0, None, D.StaticPlaneShape((0.0, 1.0, 0.0), 0.0))))
+    box = D.BoxShape((0.5, 0.5, 0.5))
+    bodies = []
+    for k in range(3):
+        info = D.RigidBodyConstructionInfo(1.0, None, box, box.calculateLocalInertia(1.0))
+        info.startWorldTransform = D.Transform(origin=(2.0 * k, 0.6, 0.0))
+        bodies.append(D.RigidBody(info))
+        world.addRigidBody(bodies[-1])
+    for _ in range(10):
+        world.stepSimulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    before = world._g.get_state()["transform"].copy()
+    bodies[2].setWorldTransform(D.Transform(origin=(0.6, 1.5, 0.1)))   # onto body 1
+    world.performDiscreteCollisionDetection()
+    assert world.getDispatcher().getNumManifolds() >= 3
+    g = world._g
+
+    b = scenes._bodies(4)
+    b["shape"] = [0, 1, 1, 1]
+    b["mass"] = [0.0, 1.0, 1.0, 1.0]
+    b["local_inertia"][1:] = box.calculateLocalInertia(1.0)
+    b["transform"][:, [0, 4, 8]] = 1.0
+    b["transform"][1:, 9:] = np.array([[0, 0.6, 0], [2, 0.6, 0], [4, 0.6, 0]], F)
+    sc = scenes.Scene("mirror_collide", 1.0 / 60.0, 10, {"gravity": (0.0, -9.81, 0.0)},
+                      [D.StaticPlaneShape((0.0, 1.0, 0.0), 0.0).desc(), box.desc()], b)
+    o = pyoracle.OracleWorld(sc, config=_abi.default_config(gravity=(0.0, -9.81, 0.0)))
+    for _ in range(10):
+        o.step_simulation(1.0 / 60.0, 1, 1.0 / 60.0)
+    t = o.get_state()["transform"]
+    t[3] = D.Transform(origin=(0.6, 1.5, 0.1)).as12()
+    o.set_state({"transform": t})
+    for st in (_abi.STAGE_AABB, _abi.STAGE_PAIRS, _abi.STAGE_NARROWPHASE):
+        o.stage(st, 1.0 / 60.0)
+    assert not H.compare_state(o.get_state(), g.get_state())
+    assert not H.compare_manifolds(o.get_manifolds(), g.get_manifolds())
+    after = g.get_state()["transform"]
+    assert np.array_equal(np.delete(after, 3, 0), np.delete(before, 3, 0))
+    world.close()
