@@ -375,6 +375,13 @@ int jbgpu_world_set_body_properties(jbgpu_world* world, const int32_t* bodies, i
                                     const float* angular_damping, const float* friction, const float* restitution,
                                     const float* linear_sleeping_threshold, const float* angular_sleeping_threshold);
 
+/* DiscreteDynamicsWorld.synchronizeMotionStates (dynamics/DiscreteDynamicsWorld.java:251-276): per
+ * body 12 floats (basis row-major, origin) of the transform the reference passes to
+ * MotionState.setWorldTransform - the interpolation transform integrated by the interpolation
+ * velocities over localTime * hitFraction (TransformUtil.integrateTransform); for static and
+ * kinematic bodies, which it skips, the world transform. */
+int jbgpu_world_get_interpolated_transforms(jbgpu_world* world, float* out);
+
 /* DynamicsWorld.setInternalTickCallback (dynamics/DynamicsWorld.java:141-144), called at the end of
  * every internalSingleStepSimulation (DiscreteDynamicsWorld.java:393-395): cb(world, time_step, user)
  * runs on the calling thread after each substep of jbgpu_world_step_simulation and jbgpu_world_step,

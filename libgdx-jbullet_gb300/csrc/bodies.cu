@@ -71,10 +71,12 @@ __global__ void k_aabb(DevWorld w) {
 __global__ void k_integrate(DevWorld w, float dt) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.nBodies) return;
+    w.hitf[i] = 1.0f;
     if (!is_active_state(w.act[i]) || is_static_or_kin(w.flags[i])) return;
     Xf t = load_xf(w, i);
     Xf p = integrate_transform(t, mk4(w.linvel[i]), mk4(w.angvel[i]), dt);
     store_xf(w, i, p);
+    store_interpolation(w, i, p);
     M m1 = scaleM(p.b, mk4(w.iloc[i]));
     M iw = mulMM(m1, transpose(p.b));
     w.iw0[i] = f4(iw.r[0], 0.0f);
@@ -147,6 +149,8 @@ __global__ void k_save_kinematic(DevWorld w, float timeStep) {
     calc_velocity(prev, cur, timeStep, lin, ang);
     w.linvel[i] = f4(lin, 0.0f);
     w.angvel[i] = f4(ang, 0.0f);
+    w.ilv[i] = f4(lin, 0.0f);
+    w.iav[i] = f4(ang, 0.0f);
     w.kx0[i] = w.xr0[i];
     w.kx1[i] = w.xr1[i];
     w.kx2[i] = w.xr2[i];

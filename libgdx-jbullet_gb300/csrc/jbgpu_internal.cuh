@@ -117,7 +117,9 @@ struct DevWorld {
     int nPairs;           // pairs of the current pair arrays (device copy in ctr[C_PAIRS])
     // body state
     float4 *xr0, *xr1, *xr2;        // basis rows; origin in .w
-    float4 *kx0, *kx1, *kx2;        // interpolationWorldTransform (saveKinematicState), same layout
+    float4 *kx0, *kx1, *kx2;        // interpolationWorldTransform (saveKinematicState, proceedToTransform), same layout
+    float4 *ilv, *iav;              // interpolationLinearVelocity / interpolationAngularVelocity
+    float* hitf;                    // CollisionObject.hitFraction (1, or 0 after a CCD clamp)
     float4 *linvel, *angvel;
     float4 *iw0, *iw1, *iw2;        // inverse inertia tensor (world) rows
     float4 *iloc;                   // inverse inertia (local) xyz, inverse mass w
@@ -167,6 +169,15 @@ JBD void store_xf(const DevWorld& w, int i, const jbd::Xf& t) {
     w.xr0[i] = make_float4(t.b.r[0].x, t.b.r[0].y, t.b.r[0].z, t.o.x);
     w.xr1[i] = make_float4(t.b.r[1].x, t.b.r[1].y, t.b.r[1].z, t.o.y);
     w.xr2[i] = make_float4(t.b.r[2].x, t.b.r[2].y, t.b.r[2].z, t.o.z);
+}
+// RigidBody.setCenterOfMassTransform of a dynamic body (proceedToTransform): the interpolation
+// transform and velocities follow the new transform and the current velocities.
+JBD void store_interpolation(const DevWorld& w, int i, const jbd::Xf& t) {
+    w.kx0[i] = make_float4(t.b.r[0].x, t.b.r[0].y, t.b.r[0].z, t.o.x);
+    w.kx1[i] = make_float4(t.b.r[1].x, t.b.r[1].y, t.b.r[1].z, t.o.y);
+    w.kx2[i] = make_float4(t.b.r[2].x, t.b.r[2].y, t.b.r[2].z, t.o.z);
+    w.ilv[i] = w.linvel[i];
+    w.iav[i] = w.angvel[i];
 }
 JBD jbd::M load_iw(const DevWorld& w, int i) {
     jbd::M m;

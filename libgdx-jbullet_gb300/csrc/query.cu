@@ -1118,6 +1118,7 @@ __global__ void k_ccd_predict(DevWorld w, float dt, float4* pred, int* flag) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) w.ctr[C_CCD_BEST] = (int)__float_as_uint(1.0f);
     if (i >= w.nBodies) return;
+    w.hitf[i] = 1.0f;
     Xf t = load_xf(w, i);
     int f = 0;
     if (is_active_state(w.act[i]) && !is_static_or_kin(w.flags[i])) {
@@ -1262,6 +1263,7 @@ __global__ void __launch_bounds__(256) k_ccd_sweep(DevWorld w, DevPairs P, int n
             const float f = __uint_as_float((unsigned)__ldcg(&w.ctr[C_CCD_BEST]));
             if (f < 1.0f && f > 0.0001f) {
                 const Xf p = integrate_transform(from, mk4(w.linvel[me]), mk4(w.angvel[me]), __fmul_rn(dt, f));
+                w.hitf[me] = 0.0f;   // integrateTransforms: setHitFraction(0) after the clamp
                 pred[3 * me] = make_float4(p.b.r[0].x, p.b.r[0].y, p.b.r[0].z, p.o.x);
                 pred[3 * me + 1] = make_float4(p.b.r[1].x, p.b.r[1].y, p.b.r[1].z, p.o.y);
                 pred[3 * me + 2] = make_float4(p.b.r[2].x, p.b.r[2].y, p.b.r[2].z, p.o.z);
@@ -1279,6 +1281,7 @@ __global__ void k_ccd_commit(DevWorld w, const float4* pred) {
     if (!is_active_state(w.act[i]) || is_static_or_kin(w.flags[i])) return;
     const Xf p = ld_pred(pred, i);
     store_xf(w, i, p);
+    store_interpolation(w, i, p);
     M m1 = scaleM(p.b, mk4(w.iloc[i]));
     M iw = mulMM(m1, transpose(p.b));
     w.iw0[i] = f4(iw.r[0], 0.0f);

@@ -241,7 +241,7 @@ int grow_bodies(jbgpu_world* w, int need) {
     DevWorld& d = w->dw;
     size_t keep = (size_t)w->nBodies;
 #define G(ptr) CK(dgrow(&d.ptr, oldc, nc, keep, s))
-    G(xr0); G(xr1); G(xr2); G(kx0); G(kx1); G(kx2); G(linvel); G(angvel); G(iw0); G(iw1); G(iw2); G(iloc); G(force);
+    G(xr0); G(xr1); G(xr2); G(kx0); G(kx1); G(kx2); G(ilv); G(iav); G(hitf); G(linvel); G(angvel); G(iw0); G(iw1); G(iw2); G(iloc); G(force);
     G(torque); G(gravity);
     G(amin); G(amax); G(act); G(deact); G(flags); G(shape); G(group); G(mask); G(world); G(friction); G(restitution);
     G(linSleep); G(angSleep); G(linDamp); G(angDamp); G(island); G(ccdThr); G(ccdRad);
@@ -884,6 +884,7 @@ struct BodyInit {
 __global__ void k_init_bodies(DevWorld w, int first, int count);
 __global__ void k_add_forces(DevWorld w, const float* f, const float* t);
 __global__ void k_pack_transforms(DevWorld w, float* out);
+__global__ void k_pack_interpolated(DevWorld w, float t, float* out);
 
 namespace {
 int ensure_io(jbgpu_world* w) {
@@ -1307,7 +1308,7 @@ int jbgpu_world_destroy(jbgpu_world* w) {
     graphs_clear(w);
     query_free(w->qb);
     DevWorld& d = w->dw;
-    dfree(d.xr0); dfree(d.xr1); dfree(d.xr2); dfree(d.kx0); dfree(d.kx1); dfree(d.kx2); dfree(d.linvel); dfree(d.angvel); dfree(d.iw0); dfree(d.iw1); dfree(d.iw2);
+    dfree(d.xr0); dfree(d.xr1); dfree(d.xr2); dfree(d.kx0); dfree(d.kx1); dfree(d.kx2); dfree(d.ilv); dfree(d.iav); dfree(d.hitf); dfree(d.linvel); dfree(d.angvel); dfree(d.iw0); dfree(d.iw1); dfree(d.iw2);
     dfree(d.iloc); dfree(d.force); dfree(d.torque); dfree(d.gravity); dfree(d.amin); dfree(d.amax); dfree(d.act);
     dfree(d.deact); dfree(d.flags); dfree(d.shape); dfree(d.group); dfree(d.mask); dfree(d.world); dfree(d.friction);
     dfree(d.restitution); dfree(d.linSleep); dfree(d.angSleep); dfree(d.linDamp); dfree(d.angDamp); dfree(d.island);
@@ -1580,6 +1581,11 @@ int jbgpu_world_add_bodies(jbgpu_world* w, const jbgpu_body_desc* b, int32_t n, 
 #define UP(dst, src, T) CK(cudaMemcpyAsync(D.dst + o, src.data(), sizeof(T) * n, cudaMemcpyHostToDevice, s))
     UP(xr0, xr0, float4); UP(xr1, xr1, float4); UP(xr2, xr2, float4); UP(linvel, lv, float4); UP(angvel, av, float4);
     UP(kx0, xr0, float4); UP(kx1, xr1, float4); UP(kx2, xr2, float4);   // interpolationWorldTransform = worldTransform
+    UP(ilv, zero, float4); UP(iav, zero, float4);                          // interpolation velocities 0
+    {
+        const std::vector<float> one(n, 1.0f);                              // hitFraction 1
+        UP(hitf, one, float);
+    }
     UP(iloc, iloc, float4); UP(gravity, grav, float4); UP(force, zero, float4); UP(torque, zero, float4);
     UP(act, act, int); UP(deact, deact, float); UP(flags, flags, int); UP(shape, shape, int); UP(group, group, int);
     UP(mask, mask, int); UP(world, world, int); UP(friction, fr, float); UP(restitution, re, float);
@@ -1626,7 +1632,7 @@ int jbgpu_world_remove_bodies(jbgpu_world* w, const int32_t* bodies, int32_t n) 
     int rc = 0;
     using namespace removal;
 #define GA(ptr) if (!rc) rc = gather_array(d.ptr, dFrom, nNew, tmp, s)
-    GA(xr0); GA(xr1); GA(xr2); GA(kx0); GA(kx1); GA(kx2); GA(linvel); GA(angvel); GA(iw0); GA(iw1); GA(iw2); GA(iloc);
+    GA(xr0); GA(xr1); GA(xr2); GA(kx0); GA(kx1); GA(kx2); GA(ilv); GA(iav); GA(hitf); GA(linvel); GA(angvel); GA(iw0); GA(iw1); GA(iw2); GA(iloc);
     GA(force); GA(torque); GA(gravity); GA(amin); GA(amax); GA(act); GA(deact); GA(flags); GA(shape); GA(group);
     GA(mask); GA(world); GA(friction); GA(restitution); GA(linSleep); GA(angSleep); GA(linDamp); GA(angDamp);
     GA(ccdThr); GA(ccdRad);
@@ -2705,6 +2711,20 @@ int jbgpu_world_get_transforms(jbgpu_world* w, float* out) {
     return JBGPU_OK;
 }
 
+int jbgpu_world_get_interpolated_transforms(jbgpu_world* w, float* out) {
+    if (!w || !out) return fail(JBGPU_ERR_INVALID_ARGUMENT, "null");
+    if (w->nBodies == 0) return JBGPU_OK;
+    CK(cudaSetDevice(w->device));
+    int rc = ensure_io(w);
+    if (rc) return rc;
+    cudaStream_t s = w->stream;
+    k_pack_interpolated<<<(w->nBodies + 255) / 256, 256, 0, s>>>(dev_view(w), w->localTime, w->ioStage); note_launch();
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, w->ioStage, sizeof(float) * 12 * (size_t)w->nBodies, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return JBGPU_OK;
+}
+
 int jbgpu_world_set_profiling(jbgpu_world* w, int32_t max_steps) {
     if (!w || max_steps < 0) return fail(JBGPU_ERR_INVALID_ARGUMENT, "bad arguments");
     CK(cudaSetDevice(w->device));
@@ -2801,6 +2821,29 @@ __global__ void k_pack_transforms(DevWorld w, float* out) {
     float* o = out + 12 * (size_t)i;
     o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = b.x; o[4] = b.y; o[5] = b.z;
     o[6] = c.x; o[7] = c.y; o[8] = c.z; o[9] = a.w; o[10] = b.w; o[11] = c.w;
+}
+
+// synchronizeMotionStates (DiscreteDynamicsWorld.java:251-276): a dynamic body's interpolation
+// transform integrated by its interpolation velocities over localTime * hitFraction; static and
+// kinematic bodies, which the reference leaves out, get their world transform.
+__global__ void k_pack_interpolated(DevWorld w, float t, float* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nBodies) return;
+    jbd::Xf x;
+    if (is_static_or_kin(w.flags[i])) {
+        x = load_xf(w, i);
+    } else {
+        const float4 a = w.kx0[i], b = w.kx1[i], c = w.kx2[i];
+        jbd::Xf k;
+        k.b.r[0] = jbd::mk(a.x, a.y, a.z);
+        k.b.r[1] = jbd::mk(b.x, b.y, b.z);
+        k.b.r[2] = jbd::mk(c.x, c.y, c.z);
+        k.o = jbd::mk(a.w, b.w, c.w);
+        x = jbd::integrate_transform(k, jbd::mk4(w.ilv[i]), jbd::mk4(w.iav[i]), __fmul_rn(t, w.hitf[i]));
+    }
+    float* o = out + 12 * (size_t)i;
+    o[0] = x.b.r[0].x; o[1] = x.b.r[0].y; o[2] = x.b.r[0].z; o[3] = x.b.r[1].x; o[4] = x.b.r[1].y; o[5] = x.b.r[1].z;
+    o[6] = x.b.r[2].x; o[7] = x.b.r[2].y; o[8] = x.b.r[2].z; o[9] = x.o.x; o[10] = x.o.y; o[11] = x.o.z;
 }
 
 // updateInertiaTensor and the creation-time proxy aabb for new bodies.

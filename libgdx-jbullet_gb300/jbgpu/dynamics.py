@@ -1256,7 +1256,20 @@ class DiscreteDynamicsWorld:
             self._cache = None
         n = g.step_simulation(timeStep, maxSubSteps, fixedTimeStep)
         self._cache = None
+        self._synchronize_motion_states(g)
         return n
+
+    def _synchronize_motion_states(self, g):
+        """synchronizeMotionStates (java:251-276): MotionState.setWorldTransform of every dynamic
+        body that has one, with the interpolated transform (once per stepSimulation call: the
+        reference's calls after each substep hand over the same values for the last one)."""
+        dyn = [b for b in self._bodies if b.info.motionState is not None and not b.isStaticOrKinematicObject()
+               and hasattr(b.info.motionState, "setWorldTransform")]
+        if not dyn:
+            return
+        xf = g.get_interpolated_transforms()
+        for b in dyn:
+            b.info.motionState.setWorldTransform(Transform.from12(xf[b._index]))
 
     # -- queries --
     def rayTest(self, rayFromWorld, rayToWorld, resultCallback):

@@ -108,6 +108,7 @@ def lib():
             "jbgpu_world_apply_impulses": ([C.c_void_p, _abi.i32p, _abi.f32p, _abi.f32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_set_body_properties": ([C.c_void_p, _abi.i32p, C.c_int32] + [_abi.f32p] * 6, C.c_int),
             "jbgpu_world_remove_joint": ([C.c_void_p, C.c_int32], C.c_int),
+            "jbgpu_world_get_interpolated_transforms": ([C.c_void_p, _abi.f32p], C.c_int),
             "jbgpu_world_set_internal_tick_callback": ([C.c_void_p, _abi.TICK_CALLBACK, C.c_void_p], C.c_int),
             "jbgpu_world_set_body_gravity": ([C.c_void_p, _abi.i32p, _abi.f32p, C.c_int32], C.c_int),
             "jbgpu_world_mesh_bvh": ([C.c_void_p, C.c_int32, _abi.i32p, C.c_int32, _abi.i32p, _abi.f32p], C.c_int),
@@ -139,7 +140,7 @@ EXPORTED = [
     "jbgpu_world_get_residual_trace", "jbgpu_world_set_ccd", "jbgpu_shape_mesh_bvh", "jbgpu_world_refit_mesh",
     "jbgpu_world_mesh_bvh", "jbgpu_world_set_gravity", "jbgpu_world_set_body_gravity", "jbgpu_world_remove_bodies",
     "jbgpu_world_apply_impulses", "jbgpu_world_set_body_properties", "jbgpu_world_set_internal_tick_callback",
-    "jbgpu_world_remove_joint",
+    "jbgpu_world_remove_joint", "jbgpu_world_get_interpolated_transforms",
 ]
 
 
@@ -263,6 +264,12 @@ class GpuWorld:
 
     def set_joint_setting(self, jid, tau=0.3, damping=1.0, impulse_clamp=0.0):
         check(lib().jbgpu_world_set_joint_setting(self.h, jid, tau, damping, impulse_clamp))
+
+    def get_interpolated_transforms(self):
+        """synchronizeMotionStates' transforms (jbgpu_world_get_interpolated_transforms), (n, 12)."""
+        out = np.zeros((max(self.n_bodies, 1), 12), np.float32)
+        check(lib().jbgpu_world_get_interpolated_transforms(self.h, out.ctypes.data_as(_abi.f32p)))
+        return out[:self.n_bodies]
 
     def remove_joint(self, jid):
         """DiscreteDynamicsWorld.removeConstraint: the joints after it move down one id."""

@@ -464,6 +464,18 @@ int orc_set_body_properties(void* h, const int* bodies, int n, const float* ld, 
     return 0;
 }
 
+// DiscreteDynamicsWorld.synchronizeMotionStates (DiscreteDynamicsWorld.java:251-276): the transform
+// handed to each dynamic body's MotionState; static and kinematic bodies get their world transform.
+void orc_get_interpolated_transforms(void* h, float* out) {
+    World* w = (World*)h;
+    for (size_t i = 0; i < w->bodies.size(); i++) {
+        const Body& b = w->bodies[i];
+        const Xf x = b.isStaticOrKinematic() ? b.xf
+                                             : integrate_transform(b.ixf, b.ilv, b.iav, w->localTime * b.hitFraction);
+        xf_to12(x, out + 12 * i);
+    }
+}
+
 // DiscreteDynamicsWorld.removeConstraint (DiscreteDynamicsWorld.java:524-528): the joints after it move down.
 int orc_remove_joint(void* h, int id) {
     World* w = (World*)h;

@@ -1412,6 +1412,7 @@ void stage_integrate(World& w, float dt) {
     w.counters.ccdPlane = 0;
     for (size_t i = 0; i < w.bodies.size(); i++) {
         Body& b = w.bodies[i];
+        b.hitFraction = 1.0f;          // java:692
         if (b.isActive() && !b.isStaticOrKinematic()) {
             Xf p = integrate_transform(b.xf, b.linvel, b.angvel, dt);
             const float sq = b.ccdMotionThreshold * b.ccdMotionThreshold;
@@ -1420,11 +1421,16 @@ void stage_integrate(World& w, float dt) {
                 w.counters.ccdClamped++;
                 float f = 1.0f;
                 bool plane = false;
-                if (ccd_sweep(w, (int)i, p, f, &plane) && f > 0.0001f)
+                if (ccd_sweep(w, (int)i, p, f, &plane) && f > 0.0001f) {
                     p = integrate_transform(b.xf, b.linvel, b.angvel, dt * f);
+                    b.hitFraction = 0.0f;   // java:717
+                }
                 if (plane) w.counters.ccdPlane++;
             }
             b.xf = p;                  // RigidBody.setCenterOfMassTransform
+            b.ixf = p;
+            b.ilv = b.linvel;
+            b.iav = b.angvel;
             update_inertia_tensor(b);
         }
     }
@@ -1487,6 +1493,8 @@ void stage_save_kinematic(World& w, float timeStep) {
     for (Body& b : w.bodies) {
         if (b.activation == ISLAND_SLEEPING || !b.isKinematic() || timeStep == 0.0f) continue;
         calculate_velocity(b.ixf, b.xf, timeStep, b.linvel, b.angvel);
+        b.ilv = b.linvel;   // RigidBody.java:200-202
+        b.iav = b.angvel;
         b.ixf = b.xf;
     }
 }

@@ -99,7 +99,9 @@ struct Manifold {        // collision/narrowphase/PersistentManifold.java
 
 struct Body {            // dynamics/RigidBody.java + collision/dispatch/CollisionObject.java
     Xf xf;
-    Xf ixf;                                 // interpolationWorldTransform (saveKinematicState)
+    Xf ixf;                                 // interpolationWorldTransform (saveKinematicState, proceedToTransform)
+    V3 ilv{0, 0, 0}, iav{0, 0, 0};          // interpolationLinearVelocity / interpolationAngularVelocity
+    float hitFraction = 1.0f;               // CollisionObject.hitFraction
     V3 linvel{0, 0, 0}, angvel{0, 0, 0};
     float invMass = 0;
     V3 invInertiaLocal{0, 0, 0};

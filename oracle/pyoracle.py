@@ -79,6 +79,8 @@ def lib():
         L.orc_set_tick_callback.argtypes = [C.c_void_p, _abi.TICK_CALLBACK, C.c_void_p]
         L.orc_set_tick_callback.restype = None
         L.orc_remove_joint.argtypes = [C.c_void_p, C.c_int]
+        L.orc_get_interpolated_transforms.argtypes = [C.c_void_p, _abi.f32p]
+        L.orc_get_interpolated_transforms.restype = None
         L.orc_set_body_gravity.argtypes = [C.c_void_p, _abi.i32p, _abi.f32p, C.c_int]
         L.orc_world_mesh_bvh.argtypes = [C.c_void_p, C.c_int, _abi.i32p, C.c_int, _abi.f32p]
         _lib = L
@@ -124,6 +126,13 @@ class OracleWorld:
 
     def set_joint_setting(self, jid, tau=0.3, damping=1.0, impulse_clamp=0.0):
         lib().orc_set_joint_setting(self.h, jid, tau, damping, impulse_clamp)
+
+    def get_interpolated_transforms(self):
+        """synchronizeMotionStates' transforms, (n, 12)."""
+        n = len(self.get_state()["transform"])
+        out = np.zeros((max(n, 1), 12), np.float32)
+        lib().orc_get_interpolated_transforms(self.h, _fp(out))
+        return out[:n]
 
     def remove_joint(self, jid):
         """DiscreteDynamicsWorld.removeConstraint: the joints after it move down one id."""

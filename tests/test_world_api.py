@@ -312,3 +312,74 @@ def test_mirror_collision_detection_without_a_step(gpu_lib, oracle_lib):
     after = g.get_state()["transform"]
     assert np.array_equal(np.delete(after, 3, 0), np.delete(before, 3, 0))
     world.close()
+
+
+def _interp(o, g, where):
+    a, b = o.get_interpolated_transforms(), g.get_interpolated_transforms()
+    assert a.shape == b.shape and np.array_equal(a.view(np.uint32), b.view(np.uint32)), where
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("make", ["mixed", "ccd"])
+def test_interpolated_transforms_bit_exact(gpu_lib, oracle_lib, make):
+    """synchronizeMotionStates' transforms with a residual localTime (time steps that are not
+    multiples of the fixed step), sleeping bodies and, in the CCD scene, clamped bodies
+    (hitFraction 0)."""
+    sc = scenes.small_mixed(60, seed=13) if make == "mixed" else scenes.ccd_shots(seed=4)
+    o = pyoracle.OracleWorld(sc)
+    g = GpuWorld(sc)
+    _interp(o, g, "start")
+    for s in range(120):
+        ts = (1.0 / 60.0) * (0.37, 1.0, 1.61, 2.9)[s % 4]
+        assert o.step_simulation(ts, 2, 1.0 / 60.0) == g.step_simulation(ts, 2, 1.0 / 60.0)
+        if s % 3 == 0:
+            _interp(o, g, s)
+            assert not H.compare_state(o.get_state(), g.get_state()), s
+    g.close()
+
+
+@pytest.mark.gpu
+def test_mirror_motion_states_read_like_the_reference(gpu_lib, oracle_lib):
+    """A dynamic body with a MotionState gets setWorldTransform after every stepSimulation call,
+    with the oracle's interpolated transform; a static body's motion state is left alone."""
+    from jbgpu import dynamics as D
+
+    class Motion:
+        def __init__(self):
+            self.calls = 0
+            self.t = None
+
+        def setWorldTransform(self, t):
+            self.calls += 1
+            self.t = t.as12()
+
+    world = D.DiscreteDynamicsWorld()
+    world.setGravity((0.0, -9.81, 0.0))
+    ground_motion = Motion()
+    world.addRigidBody(D.RigidBody(D.RigidBodyConstructionInfo(0.0, ground_motion,
+                                                               D.StaticPlaneShape((0.0, 1.0, 0.0), 0.0))))
+    sph = D.SphereShape(0.5)
+    motion = Motion()
+    info = D.RigidBodyConstructionInfo(1.0, motion, sph, sph.calculateLocalInertia(1.0))
+    info.startWorldTransform = D.Transform(origin=(0.0, 3.0, 0.0))
+    ball = D.RigidBody(info)
+    world.addRigidBody(ball)
+    ball.setAngularVelocity((0.0, 2.0, 1.0))
+    b = scenes._bodies(2)
+    b["shape"] = [0, 1]
+    b["mass"] = [0.0, 1.0]
+    b["local_inertia"][1] = sph.calculateLocalInertia(1.0)
+    b["transform"][:, [0, 4, 8]] = 1.0
+    b["transform"][1, 9:] = (0.0, 3.0, 0.0)
+    b["angular_velocity"][1] = (0.0, 2.0, 1.0)
+    sc = scenes.Scene("mirror_motion", 1.0 / 60.0, 40, {"gravity": (0.0, -9.81, 0.0)},
+                      [D.StaticPlaneShape((0.0, 1.0, 0.0), 0.0).desc(), sph.desc()], b)
+    o = pyoracle.OracleWorld(sc, config=_abi.default_config(gravity=(0.0, -9.81, 0.0)))
+    for s in range(40):
+        ts = (1.0 / 60.0) * (0.5 if s % 2 else 1.3)
+        world.stepSimulation(ts, 2, 1.0 / 60.0)
+        o.step_simulation(ts, 2, 1.0 / 60.0)
+        want = o.get_interpolated_transforms()[1]
+        assert np.array_equal(motion.t.view(np.uint32), want.view(np.uint32)), s
+    assert motion.calls == 40 and ground_motion.calls == 0
+    world.close()
