@@ -383,3 +383,34 @@ def test_mirror_motion_states_read_like_the_reference(gpu_lib, oracle_lib):
         assert np.array_equal(motion.t.view(np.uint32), want.view(np.uint32)), s
     assert motion.calls == 40 and ground_motion.calls == 0
     world.close()
+
+
+@pytest.mark.gpu
+def test_tick_callback_removes_bodies_between_substeps(gpu_lib, oracle_lib):
+    """Bodies removed from inside the tick callback are gone from the next substep on, in the
+    same stepSimulation call; the worlds stay bit-identical."""
+    sc = scenes.small_mixed(60, seed=14)
+    o = pyoracle.OracleWorld(sc)
+    g = GpuWorld(sc)
+    removals = {4: [10, 20], 9: [3], 15: [len(sc.bodies) - 5]}
+
+    def make():
+        count = [0]
+
+        def cb(w, dt):
+            k = count[0]
+            count[0] += 1
+            if k in removals:
+                w.remove_bodies(removals[k])
+        return cb, count
+    cbo, co = make()
+    cbg, cg = make()
+    o.set_internal_tick_callback(cbo)
+    g.set_internal_tick_callback(cbg)
+    for s in range(40):
+        ts = (1.0 / 60.0) * (2.5 if s % 2 else 1.0)      # one or two substeps per call
+        assert o.step_simulation(ts, 3, 1.0 / 60.0) == g.step_simulation(ts, 3, 1.0 / 60.0)
+        _assert_same(o, g, s)
+    assert co[0] == cg[0] > 16
+    assert len(g.get_state()["transform"]) == len(sc.bodies) - 4
+    g.close()
